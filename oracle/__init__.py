@@ -1,0 +1,183 @@
+"""ctypes bridge to the CPU oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY.  The oracle is a CPU FP64 restatement of Xyce's
+transient Newton hot path (see oracle/oracle.h for the reference functions
+it follows).  Only tests/, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU
+baseline load it, and only as the checker; the product library never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+KSPARSE_PATH = os.path.join(HERE, "_ref", "libksparse.so")
+REFERENCE_KSPARSE = "/root/reference/src/LinearAlgebraServicesPKG/ksparse"
+
+_lib = None
+
+
+def build(with_reference: bool | None = None) -> None:
+    """Compile the oracle; also compile ksparse from the reference's own
+    sources when the reference tree is present."""
+    subprocess.check_call(["make", "-s", "-C", HERE, "all"])
+    if with_reference is None:
+        with_reference = os.path.isdir(REFERENCE_KSPARSE)
+    if with_reference:
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={REFERENCE_KSPARSE}"])
+
+
+class TranParams(C.Structure):
+    _fields_ = [("tstart", C.c_double), ("tstop", C.c_double), ("hmax", C.c_double),
+                ("hmin", C.c_double), ("reltol", C.c_double), ("abstol", C.c_double),
+                ("nl_reltol", C.c_double), ("nl_abstol", C.c_double),
+                ("nl_deltaxtol", C.c_double), ("nl_rhstol", C.c_double),
+                ("nl_smallupdatetol", C.c_double), ("nl_maxstep", C.c_int),
+                ("max_steps", C.c_int), ("max_order", C.c_int)]
+
+
+class TranStats(C.Structure):
+    _fields_ = [("accepted", C.c_int), ("rejected", C.c_int), ("newton_iters", C.c_int),
+                ("newton_fail", C.c_int), ("lte_fail", C.c_int), ("dcop_iters", C.c_int),
+                ("status", C.c_int), ("t_final", C.c_double), ("time_load", C.c_double),
+                ("time_solve", C.c_double), ("time_total", C.c_double)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build(with_reference=False)
+        L = C.CDLL(LIB_PATH)
+        P = C.c_void_p
+        ip = np.ctypeslib.ndpointer(np.int32, flags="C")
+        dp = np.ctypeslib.ndpointer(np.float64, flags="C")
+        L.orc_create.restype = P
+        L.orc_create.argtypes = [C.c_int, C.c_int, ip]
+        L.orc_destroy.argtypes = [P]
+        L.orc_add_resistors.argtypes = [P, C.c_int, ip, ip, dp]
+        L.orc_add_capacitors.argtypes = [P, C.c_int, ip, ip, dp]
+        L.orc_add_vsources.argtypes = [P, C.c_int, ip, ip, ip, ip, ip, dp]
+        L.orc_add_isources.argtypes = [P, C.c_int, ip, ip, ip, ip, dp]
+        L.orc_add_diodes.argtypes = [P, C.c_int, ip, ip, ip, dp]
+        L.orc_add_mosfet1.argtypes = [P, C.c_int, ip, ip, ip, ip, dp]
+        L.orc_finalize.argtypes = [P]
+        L.orc_sizes.argtypes = [P] + [C.POINTER(C.c_int)] * 4
+        L.orc_pattern.argtypes = [P, ip, ip]
+        L.orc_load.argtypes = [P, C.c_double, dp, dp, dp, dp, C.c_int, C.c_int] + [dp] * 9
+        L.orc_lu_solve.argtypes = [P, dp, dp, dp]
+        L.orc_transient.argtypes = [P, C.POINTER(TranParams), C.c_int, ip, C.c_int, dp, dp,
+                                    C.POINTER(C.c_int), C.POINTER(TranStats)]
+        L.orc_dcop.argtypes = [P, dp, C.POINTER(C.c_int)]
+        _lib = L
+    return _lib
+
+
+class Oracle:
+    """One circuit (or batch of circuits) loaded into the CPU oracle."""
+
+    def __init__(self, netlist):
+        L = lib()
+        a = netlist.arrays()
+        self.netlist = netlist
+        self.h = L.orc_create(a["n"], len(a["offsets"]) - 1, a["offsets"])
+        p, m, v = a["res"]
+        L.orc_add_resistors(self.h, len(p), p, m, v)
+        p, m, v = a["cap"]
+        L.orc_add_capacitors(self.h, len(p), p, m, v)
+        p, m, b, k, o, d = a["vsrc"]
+        L.orc_add_vsources(self.h, len(p), p, m, b, k, o, d)
+        p, m, k, o, d = a["isrc"]
+        L.orc_add_isources(self.h, len(p), p, m, k, o, d)
+        p, m, r, prm = a["diode"]
+        L.orc_add_diodes(self.h, len(p), p, m, r, prm)
+        dd, g, s, b, prm = a["mos1"]
+        rc = L.orc_add_mosfet1(self.h, len(dd), dd, g, s, b, prm)
+        if rc != 0:
+            raise ValueError("oracle: MOSFET series resistance is not restated")
+        L.orc_finalize(self.h)
+        n, nnz, nsta, nsto = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        L.orc_sizes(self.h, C.byref(n), C.byref(nnz), C.byref(nsta), C.byref(nsto))
+        self.n, self.nnz, self.nsta, self.nsto = n.value, nnz.value, nsta.value, nsto.value
+        self.row_ptr = np.zeros(self.n + 1, np.int32)
+        self.col_idx = np.zeros(self.nnz, np.int32)
+        L.orc_pattern(self.h, self.row_ptr, self.col_idx)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_destroy(self.h)
+            self.h = None
+
+    def load(self, x, time=0.0, sta_curr=None, sto_curr=None, sto_prev=None, newton_iter=0,
+             dcop=False, init_jct=False):
+        """One device load; returns dict of F, Q, B, dFdxdVp, dQdxdVp, dFdx, dQdx
+        (CSR values on self.row_ptr/self.col_idx), sta_next, sto_next."""
+        n, nnz = self.n, self.nnz
+        z = lambda k: np.zeros(max(1, k))
+        sta_curr = z(self.nsta) if sta_curr is None else np.ascontiguousarray(sta_curr, np.float64)
+        sto_curr = z(self.nsto) if sto_curr is None else np.ascontiguousarray(sto_curr, np.float64)
+        sto_prev = z(self.nsto) if sto_prev is None else np.ascontiguousarray(sto_prev, np.float64)
+        out = {k: np.zeros(n) for k in ("F", "Q", "B", "dFdxdVp", "dQdxdVp")}
+        out["dFdx"] = np.zeros(nnz)
+        out["dQdx"] = np.zeros(nnz)
+        out["sta_next"] = z(self.nsta)
+        out["sto_next"] = z(self.nsto)
+        flags = (1 if dcop else 0) | (2 if init_jct else 0)
+        lib().orc_load(self.h, float(time), np.ascontiguousarray(x, np.float64), sta_curr,
+                       sto_curr, sto_prev, int(newton_iter), flags, out["sta_next"],
+                       out["sto_next"], out["F"], out["Q"], out["B"], out["dFdxdVp"],
+                       out["dQdxdVp"], out["dFdx"], out["dQdx"])
+        return out
+
+    def lu_solve(self, vals, b):
+        x = np.zeros(self.n)
+        rc = lib().orc_lu_solve(self.h, np.ascontiguousarray(vals, np.float64),
+                                np.ascontiguousarray(b, np.float64), x)
+        if rc != 0:
+            raise np.linalg.LinAlgError("oracle LU: singular")
+        return x
+
+    def dcop(self):
+        x = np.zeros(self.n)
+        it = C.c_int()
+        st = lib().orc_dcop(self.h, x, C.byref(it))
+        return st, x, it.value
+
+    def transient(self, tran=None, probes=None, cap=2_000_000):
+        tran = tran or self.netlist.tran
+        probes = np.asarray(probes if probes is not None else [], np.int32)
+        tp = TranParams(tran.tstart, tran.tstop, tran.hmax, tran.hmin, tran.reltol,
+                        tran.abstol, tran.nl_reltol, tran.nl_abstol, tran.nl_deltaxtol,
+                        tran.nl_rhstol, tran.nl_smallupdatetol, tran.nl_maxstep,
+                        tran.max_steps, tran.max_order)
+        times = np.zeros(cap)
+        vals = np.zeros(cap * max(1, len(probes)))
+        nout = C.c_int()
+        st = TranStats()
+        lib().orc_transient(self.h, C.byref(tp), len(probes), probes, cap, times, vals,
+                            C.byref(nout), C.byref(st))
+        k = nout.value
+        return (times[:k].copy(), vals[: k * len(probes)].reshape(k, len(probes)).copy(),
+                {f: getattr(st, f) for f, _ in TranStats._fields_})
+
+
+def ksparse_solve(row_ptr, col_idx, vals, b):
+    """Solve with Kundert Sparse compiled from the reference sources
+    (oracle/_ref/libksparse.so); raises FileNotFoundError when not built."""
+    if not os.path.exists(KSPARSE_PATH):
+        raise FileNotFoundError(KSPARSE_PATH)
+    L = C.CDLL(KSPARSE_PATH)
+    ip = np.ctypeslib.ndpointer(np.int32, flags="C")
+    dp = np.ctypeslib.ndpointer(np.float64, flags="C")
+    L.ks_solve.argtypes = [C.c_int, ip, ip, dp, dp, dp]
+    n = len(row_ptr) - 1
+    x = np.zeros(n)
+    rc = L.ks_solve(n, np.ascontiguousarray(row_ptr, np.int32), np.ascontiguousarray(col_idx, np.int32),
+                    np.ascontiguousarray(vals, np.float64), np.ascontiguousarray(b, np.float64), x)
+    if rc != 0:
+        raise np.linalg.LinAlgError(f"ksparse status {rc}")
+    return x

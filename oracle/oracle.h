@@ -1,0 +1,97 @@
+/*
+ * oracle.h — CPU FP64 restatement of Xyce's transient Newton hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU
+ * implementation in xyce_gb300/: only tests/, __graft_entry__.smoke() and
+ * bench.py's cpu_baseline / reference arm may load it.  The product never
+ * links, imports or calls it.
+ *
+ * What it restates (file:line within the Xyce source tree):
+ *   - SourceData SIN/PULSE/PWL       src/DeviceModelPKG/Core/N_DEV_SourceData.C:475,1168,1770
+ *   - pnjlim/fetlim/limvds/qmeyer    src/DeviceModelPKG/Core/N_DEV_DeviceSupport.C:161-745
+ *   - Resistor/Capacitor/Vsrc/ISRC   src/DeviceModelPKG/OpenModels/N_DEV_{Resistor,Capacitor,Vsrc,ISRC}.C
+ *   - Diode level 1                  src/DeviceModelPKG/OpenModels/N_DEV_Diode.C:1072-1950,2040-2237
+ *   - MOSFET level 1                 src/DeviceModelPKG/OpenModels/N_DEV_MOSFET1.C:2689-3730,4241-4876
+ *   - OneStep (BE/trapezoid)         src/TimeIntegrationPKG/N_TIA_OneStep.C:135-500,1390-1640,1684-2240
+ *   - DataStore error weights/WRMS   src/TimeIntegrationPKG/N_TIA_DataStore.C:1304-1550,1737
+ *   - StepErrorControl accept test   src/TimeIntegrationPKG/N_TIA_StepErrorControl.C:458-575
+ *   - DampedNewton                   src/NonlinearSolverPKG/N_NLS_DampedNewton.C:297-520,1147-1396
+ *   - Sparse LU: Gilbert-Peierls left-looking LU with threshold partial
+ *     pivoting (the algorithm of KLU, which Xyce calls through Amesos in
+ *     src/LinearAlgebraServicesPKG/N_LAS_AmesosSolver.C:309-396).  It is
+ *     cross-checked against Kundert Sparse 1.3 compiled from the reference's
+ *     own sources (src/LinearAlgebraServicesPKG/ksparse) by oracle/Makefile.
+ *
+ * Parity pinning: the Xyce regression waveforms are not in the reference
+ * tree and Xyce cannot be built here (Trilinos absent), so the device
+ * models are pinned by finite-difference Jacobian checks (the reference's
+ * TESTJAC idea, src/DeviceModelPKG/Core/N_DEV_NumericalJacobian.C:154) and
+ * by analytic circuits; the linear solve is pinned by ksparse.
+ */
+#ifndef XG_ORACLE_H
+#define XG_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_ctx orc_ctx;
+
+/* Waveform kinds shared with the GPU library's C-ABI. */
+enum { ORC_WAVE_DC = 0, ORC_WAVE_SIN = 1, ORC_WAVE_PULSE = 2, ORC_WAVE_PWL = 3 };
+
+orc_ctx *orc_create(int n_unknowns, int n_circuits, const int *circuit_offsets);
+void orc_destroy(orc_ctx *c);
+int orc_add_resistors(orc_ctx *c, int n, const int *pos, const int *neg, const double *r);
+int orc_add_capacitors(orc_ctx *c, int n, const int *pos, const int *neg, const double *cap);
+int orc_add_vsources(orc_ctx *c, int n, const int *pos, const int *neg, const int *branch,
+                     const int *kind, const int *off, const double *data);
+int orc_add_isources(orc_ctx *c, int n, const int *pos, const int *neg,
+                     const int *kind, const int *off, const double *data);
+int orc_add_diodes(orc_ctx *c, int n, const int *pos, const int *neg, const int *pri,
+                   const double *params);
+int orc_add_mosfet1(orc_ctx *c, int n, const int *d, const int *g, const int *s, const int *b,
+                    const double *params);
+int orc_finalize(orc_ctx *c);
+
+int orc_sizes(orc_ctx *c, int *n_unknowns, int *nnz, int *n_state, int *n_store);
+int orc_pattern(orc_ctx *c, int *row_ptr, int *col_idx);
+
+/* One device load (updateState + loadDAEVectors + loadDAEMatrices) at
+ * x_next, with the reference's zeroed-output precondition done here.
+ * flags: bit0 dcop, bit1 initJct, newton_iter selects limiter history. */
+int orc_load(orc_ctx *c, double time, const double *x_next, const double *sta_curr,
+             const double *sto_curr, const double *sto_next_in, int newton_iter, int flags,
+             double *sta_next, double *sto_next, double *F, double *Q, double *B,
+             double *dFdxdVp, double *dQdxdVp, double *dFdx, double *dQdx);
+
+/* Sparse LU solve of A x = b on the context's pattern (for solver checks). */
+int orc_lu_solve(orc_ctx *c, const double *vals, const double *b, double *x);
+
+typedef struct orc_tran_params {
+  double tstart, tstop, hmax, hmin;
+  double reltol, abstol;            /* TIMEINT RELTOL/ABSTOL */
+  double nl_reltol, nl_abstol, nl_deltaxtol, nl_rhstol, nl_smallupdatetol;
+  int nl_maxstep;
+  int max_steps;                    /* safety cap on accepted steps, 0 = none */
+  int max_order;                    /* 1 = BE only, 2 = trapezoid */
+} orc_tran_params;
+
+typedef struct orc_tran_stats {
+  int accepted, rejected, newton_iters, newton_fail, lte_fail, dcop_iters, status;
+  double t_final;
+  double time_load, time_solve, time_total;
+} orc_tran_stats;
+
+/* Transient run from a DC operating point.  Output: times[] and
+ * values[n_probe x cap] at each accepted point (row-major by point). */
+int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, const int *probes,
+                  int cap, double *times, double *values, int *n_out, orc_tran_stats *st);
+
+/* Operating point only (x out, length n_unknowns). */
+int orc_dcop(orc_ctx *c, double *x, int *iters);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

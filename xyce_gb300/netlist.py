@@ -1,0 +1,326 @@
+"""Circuit descriptions and seeded synthetic generators.
+
+A :class:`Netlist` is the flat, array-of-devices description that the C-ABI
+(``include/xyce_gb300.h``) uploads: unknown indices are 0-based MNA
+unknowns, ground is ``-1``.  Several independent circuits may be packed
+into one netlist (the batched Monte-Carlo form); ``offsets`` gives the
+contiguous unknown range of each circuit.
+
+Device parameter rows follow the layouts declared in the C header
+(``XG_DIODE_*`` and ``XG_MOS1_*``), which mirror the instance/model
+parameters of Xyce's Diode (src/DeviceModelPKG/OpenModels/N_DEV_Diode.C:100-345)
+and MOSFET level 1 (src/DeviceModelPKG/OpenModels/N_DEV_MOSFET1.C:61-331).
+
+The generators build the synthetic workloads with numpy ``default_rng``
+seeds: the diode-RC ladder, CMOS ring oscillators, the power-grid mesh and
+the batch of uneven Monte-Carlo rings.  No public benchmark netlists are
+involved.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+WAVE_DC, WAVE_SIN, WAVE_PULSE, WAVE_PWL = 0, 1, 2, 3
+
+# Diode parameter row (N_DEV_Diode.C addPar defaults).
+DIODE_FIELDS = ["IS", "N", "RS", "CJO", "VJ", "M", "FC", "TT", "BV", "IBV", "NBV",
+                "IKF", "ISR", "NR", "EG", "XTI", "AREA", "BVGIVEN"]
+DIODE_DEFAULTS = dict(IS=1e-14, N=1.0, RS=0.0, CJO=0.0, VJ=1.0, M=0.5, FC=0.5, TT=0.0,
+                      BV=1e99, IBV=1e-3, NBV=None, IKF=0.0, ISR=0.0, NR=2.0, EG=1.11,
+                      XTI=3.0, AREA=1.0, BVGIVEN=0.0)
+
+# MOSFET level-1 parameter row (model + instance; N_DEV_MOSFET1.C addPar defaults).
+MOS1_FIELDS = ["TYPE", "VTO", "KP", "GAMMA", "PHI", "LAMBDA", "RD", "RS", "CBD", "CBS",
+               "IS", "PB", "CGSO", "CGDO", "CGBO", "CJ", "MJ", "CJSW", "MJSW", "JS",
+               "TOX", "LD", "FC", "W", "L", "AD", "AS", "PD", "PS", "M"]
+MOS1_DEFAULTS = dict(TYPE=1.0, VTO=0.0, KP=2e-5, GAMMA=0.0, PHI=0.6, LAMBDA=0.0, RD=0.0,
+                     RS=0.0, CBD=0.0, CBS=0.0, IS=1e-14, PB=0.8, CGSO=0.0, CGDO=0.0,
+                     CGBO=0.0, CJ=0.0, MJ=0.5, CJSW=0.0, MJSW=0.5, JS=0.0, TOX=0.0, LD=0.0,
+                     FC=0.5, W=1e-4, L=1e-4, AD=0.0, AS=0.0, PD=0.0, PS=0.0, M=1.0)
+
+
+def diode_row(**kw) -> np.ndarray:
+    p = dict(DIODE_DEFAULTS)
+    p.update(kw)
+    if p["NBV"] is None:
+        p["NBV"] = p["N"]
+    if "BV" in kw:
+        p["BVGIVEN"] = 1.0
+    return np.array([p[f] for f in DIODE_FIELDS], dtype=np.float64)
+
+
+def mos1_row(**kw) -> np.ndarray:
+    p = dict(MOS1_DEFAULTS)
+    p.update(kw)
+    return np.array([p[f] for f in MOS1_FIELDS], dtype=np.float64)
+
+
+@dataclass
+class Tran:
+    """Transient options: .TRAN and .OPTIONS TIMEINT / NONLIN-TRAN values.
+
+    Defaults follow TIAParams (src/TimeIntegrationPKG/N_TIA_TIAParams.C:95-115)
+    and the NONLIN-TRAN table (src/NonlinearSolverPKG/N_NLS_Manager.C:1056-1066).
+    """
+    tstop: float
+    hmax: float = 0.0
+    tstart: float = 0.0
+    hmin: float = 0.0
+    reltol: float = 1e-3
+    abstol: float = 1e-6
+    nl_reltol: float = 1e-2
+    nl_abstol: float = 1e-6
+    nl_deltaxtol: float = 0.33
+    nl_rhstol: float = 1e-2
+    nl_smallupdatetol: float = 1e-6
+    nl_maxstep: int = 20
+    max_order: int = 2
+    max_steps: int = 0
+
+
+@dataclass
+class Netlist:
+    n: int = 0
+    offsets: list = field(default_factory=lambda: [0])
+    res: list = field(default_factory=list)      # (p, n, R)
+    cap: list = field(default_factory=list)      # (p, n, C)
+    vsrc: list = field(default_factory=list)     # (p, n, branch, kind, data)
+    isrc: list = field(default_factory=list)     # (p, n, kind, data)
+    diode: list = field(default_factory=list)    # (p, n, pri, row)
+    mos1: list = field(default_factory=list)     # (d, g, s, b, row)
+    names: dict = field(default_factory=dict)
+    tran: Tran | None = None
+    label: str = ""
+
+    # ---- construction ---------------------------------------------------
+    def node(self, name: str | None = None) -> int:
+        i = self.n
+        self.n += 1
+        if name is not None:
+            self.names[name] = i
+        return i
+
+    def end_circuit(self):
+        """Close the current circuit: unknowns allocated so far belong to it."""
+        if self.offsets[-1] != self.n:
+            self.offsets.append(self.n)
+
+    def R(self, a, b, r):
+        self.res.append((a, b, float(r)))
+
+    def C(self, a, b, c):
+        self.cap.append((a, b, float(c)))
+
+    def V(self, a, b, kind, data, name=None):
+        br = self.node(name)
+        self.vsrc.append((a, b, br, kind, [float(x) for x in data]))
+        return br
+
+    def I(self, a, b, kind, data):
+        self.isrc.append((a, b, kind, [float(x) for x in data]))
+
+    def D(self, a, b, **params):
+        row = diode_row(**params)
+        pri = a
+        if row[DIODE_FIELDS.index("RS")] != 0.0:
+            pri = self.node()
+        self.diode.append((a, b, pri, row))
+
+    def M1(self, d, g, s, b, **params):
+        self.mos1.append((d, g, s, b, mos1_row(**params)))
+
+    # ---- flat arrays (C-ABI order) ------------------------------------
+    def arrays(self) -> dict:
+        self.end_circuit()
+        i32 = lambda x: np.ascontiguousarray(np.asarray(x, dtype=np.int32))
+        f64 = lambda x: np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+
+        def waves(lst, k_kind, k_data):
+            kinds = [w[k_kind] for w in lst]
+            off = [0]
+            data = []
+            for w in lst:
+                data.extend(w[k_data])
+                off.append(len(data))
+            return i32(kinds), i32(off), f64(data if data else [0.0])
+
+        out = dict(n=self.n, offsets=i32(self.offsets))
+        out["res"] = (i32([r[0] for r in self.res]), i32([r[1] for r in self.res]),
+                      f64([r[2] for r in self.res]))
+        out["cap"] = (i32([c[0] for c in self.cap]), i32([c[1] for c in self.cap]),
+                      f64([c[2] for c in self.cap]))
+        vk, vo, vd = waves(self.vsrc, 3, 4)
+        out["vsrc"] = (i32([v[0] for v in self.vsrc]), i32([v[1] for v in self.vsrc]),
+                       i32([v[2] for v in self.vsrc]), vk, vo, vd)
+        ik, io, idat = waves(self.isrc, 2, 3)
+        out["isrc"] = (i32([v[0] for v in self.isrc]), i32([v[1] for v in self.isrc]), ik, io, idat)
+        out["diode"] = (i32([d[0] for d in self.diode]), i32([d[1] for d in self.diode]),
+                        i32([d[2] for d in self.diode]),
+                        f64(np.array([d[3] for d in self.diode]).reshape(-1, len(DIODE_FIELDS))))
+        out["mos1"] = (i32([m[0] for m in self.mos1]), i32([m[1] for m in self.mos1]),
+                       i32([m[2] for m in self.mos1]), i32([m[3] for m in self.mos1]),
+                       f64(np.array([m[4] for m in self.mos1]).reshape(-1, len(MOS1_FIELDS))))
+        return out
+
+    @property
+    def n_circuits(self) -> int:
+        self.end_circuit()
+        return len(self.offsets) - 1
+
+    def device_count(self) -> int:
+        return len(self.res) + len(self.cap) + len(self.vsrc) + len(self.isrc) + \
+            len(self.diode) + len(self.mos1)
+
+
+# ---------------------------------------------------------------------------
+# Small known-answer circuits.
+
+def test_netlist1() -> Netlist:
+    """V1 1 0 5; R1 1 0 1; .TRAN 0 1 — V(1) = 5 exactly."""
+    nl = Netlist(label="testnetlist1")
+    n1 = nl.node("1")
+    nl.V(n1, -1, WAVE_DC, [5.0], name="V1#branch")
+    nl.R(n1, -1, 1.0)
+    nl.tran = Tran(tstop=1.0)
+    return nl
+
+
+def test_netlist2() -> Netlist:
+    """V1 1 0 SIN(0 1 1); R1 1 2 50; R2 2 0 100; C1 1 0 1e-6; .TRAN 0 1.
+
+    V(1) = sin(2 pi t) and V(2) = V(1) * 100/150 exactly.
+    """
+    nl = Netlist(label="testnetlist2")
+    n1, n2 = nl.node("1"), nl.node("2")
+    nl.V(n1, -1, WAVE_SIN, [0.0, 1.0, 1.0, 0.0, 0.0, 0.0], name="V1#branch")
+    nl.R(n1, n2, 50.0)
+    nl.R(n2, -1, 100.0)
+    nl.C(n1, -1, 1e-6)
+    nl.tran = Tran(tstop=1.0)
+    return nl
+
+
+def rc_step(r=1e3, c=1e-9, v=1.0, tstop=5e-6) -> Netlist:
+    """PULSE-driven RC low-pass: V(out) = v (1 - exp(-t/RC)) after the edge."""
+    nl = Netlist(label="rc_step")
+    a, o = nl.node("in"), nl.node("out")
+    nl.V(a, -1, WAVE_PULSE, [0.0, v, 0.0, 1e-12, 1e-12, 1.0, 0.0])
+    nl.R(a, o, r)
+    nl.C(o, -1, c)
+    nl.tran = Tran(tstop=tstop, hmax=tstop / 200)
+    return nl
+
+
+# ---------------------------------------------------------------------------
+# Synthetic workloads.
+
+def diode_ladder(n_nodes=1000, seed=1) -> Netlist:
+    """Diode-RC ladder: chain of n_nodes, R_i ~ U[500,2000] ohm, C_i ~ U[0.1,1] pF,
+    a level-1 diode (IS=1e-14, N=1, RS=10) from every node to ground, node 1
+    driven by SIN(1 1 1MEG); .TRAN 0 5u, max step 10 n, RELTOL 1e-3 ABSTOL 1e-12."""
+    rng = np.random.default_rng(seed)
+    nl = Netlist(label=f"diode_ladder_{n_nodes}")
+    nodes = [nl.node(f"n{i + 1}") for i in range(n_nodes)]
+    rv = rng.uniform(500.0, 2000.0, n_nodes - 1)
+    cv = rng.uniform(0.1e-12, 1e-12, n_nodes)
+    nl.V(nodes[0], -1, WAVE_SIN, [1.0, 1.0, 1e6, 0.0, 0.0, 0.0], name="V1#branch")
+    for i in range(n_nodes - 1):
+        nl.R(nodes[i], nodes[i + 1], rv[i])
+    for i in range(n_nodes):
+        nl.C(nodes[i], -1, cv[i])
+        nl.D(nodes[i], -1, IS=1e-14, N=1.0, RS=10.0)
+    nl.tran = Tran(tstop=5e-6, hmax=10e-9, reltol=1e-3, abstol=1e-12)
+    return nl
+
+
+NMOS_CARD = dict(TYPE=1.0, VTO=0.5, KP=120e-6, W=2e-6, L=0.18e-6)
+PMOS_CARD = dict(TYPE=-1.0, VTO=-0.5, KP=40e-6, W=4e-6, L=0.18e-6)
+
+
+def _ring(nl: Netlist, stages: int, vdd=1.8, cload=5e-15, nmos=None, pmos=None,
+          kick=100e-6, prefix="") -> None:
+    nmos = nmos or NMOS_CARD
+    pmos = pmos or PMOS_CARD
+    outs = [nl.node(f"{prefix}n{i + 1}") for i in range(stages)]
+    vdd_n = nl.node(f"{prefix}vdd")
+    nl.V(vdd_n, -1, WAVE_DC, [vdd], name=f"{prefix}VDD#branch")
+    for i in range(stages):
+        inp = outs[i - 1]
+        out = outs[i]
+        cl = cload[i] if hasattr(cload, "__len__") else cload
+        nc = nmos[i] if isinstance(nmos, list) else nmos
+        pc = pmos[i] if isinstance(pmos, list) else pmos
+        nl.M1(out, inp, -1, -1, **nc)
+        nl.M1(out, inp, vdd_n, vdd_n, **pc)
+        nl.C(out, -1, cl)
+    # 1 ns current kick into the first node (PWL source from ground to n1)
+    nl.I(-1, outs[0], WAVE_PWL, [0.0, 0.0, 10e-12, kick, 990e-12, kick, 1e-9, 0.0])
+
+
+def ring_oscillator(stages=101) -> Netlist:
+    """CMOS ring oscillator of MOSFET level-1 inverters: VDD=1.8 V, NMOS VTO=0.5
+    KP=120u, PMOS VTO=-0.5 KP=40u, W/L=2u/0.18u (PMOS W=4u), 5 fF per stage, a
+    1 ns PWL kick on node 1; .TRAN 0 20n, max step 5 p."""
+    assert stages % 2 == 1
+    nl = Netlist(label=f"ring_{stages}")
+    _ring(nl, stages)
+    nl.tran = Tran(tstop=20e-9, hmax=5e-12)
+    return nl
+
+
+def power_grid(k=500, n_sinks=2000, seed=3) -> Netlist:
+    """k x k resistive mesh, R ~ U[0.05,0.2] ohm, decaps ~ U[1,10] fF, n_sinks
+    seed-placed PWL current sinks ramping to U[0,5] mA over 100 ps windows,
+    four corner pads tied to 1.0 V through 0.01 ohm; .TRAN 0 2n step 1 p."""
+    rng = np.random.default_rng(seed)
+    nl = Netlist(label=f"power_grid_{k}")
+    base = nl.n
+    nl.n += k * k
+    idx = lambda r, c: base + r * k + c
+    rh = rng.uniform(0.05, 0.2, (k, k - 1))
+    rvv = rng.uniform(0.05, 0.2, (k - 1, k))
+    for r in range(k):
+        for c in range(k - 1):
+            nl.R(idx(r, c), idx(r, c + 1), rh[r, c])
+    for r in range(k - 1):
+        for c in range(k):
+            nl.R(idx(r, c), idx(r + 1, c), rvv[r, c])
+    cv = rng.uniform(1e-15, 10e-15, k * k)
+    for i in range(k * k):
+        nl.C(base + i, -1, cv[i])
+    for (r, c) in [(0, 0), (0, k - 1), (k - 1, 0), (k - 1, k - 1)]:
+        pad = nl.node()
+        nl.V(pad, -1, WAVE_DC, [1.0])
+        nl.R(pad, idx(r, c), 0.01)
+    where = rng.choice(k * k, size=min(n_sinks, k * k), replace=False)
+    amp = rng.uniform(0.0, 5e-3, len(where))
+    start = rng.uniform(0.0, 1.8e-9, len(where))
+    for i, node in enumerate(where):
+        t0 = start[i]
+        nl.I(base + int(node), -1, WAVE_PWL, [t0, 0.0, t0 + 100e-12, amp[i]])
+    nl.names["center"] = idx(k // 2, k // 2)
+    nl.tran = Tran(tstop=2e-9, hmax=1e-12)
+    return nl
+
+
+def monte_carlo_rings(count=4096, min_stages=11, max_stages=301, seed=4) -> Netlist:
+    """Batch of independent ring oscillators with uneven sizes: odd stage
+    counts uniform in [min_stages, max_stages], per-instance VTO ~ N(+-0.5,
+    0.03), KP ~ N(nominal, 5%), load C ~ U[3,7] fF; .TRAN 0 10n."""
+    rng = np.random.default_rng(seed)
+    nl = Netlist(label=f"mc_rings_{count}")
+    odd = np.arange(min_stages, max_stages + 1, 2)
+    sizes = rng.choice(odd, size=count)
+    for ci, st in enumerate(sizes):
+        st = int(st)
+        nm = [dict(NMOS_CARD, VTO=rng.normal(0.5, 0.03), KP=rng.normal(120e-6, 0.05 * 120e-6))
+              for _ in range(st)]
+        pm = [dict(PMOS_CARD, VTO=rng.normal(-0.5, 0.03), KP=rng.normal(40e-6, 0.05 * 40e-6))
+              for _ in range(st)]
+        cl = rng.uniform(3e-15, 7e-15, st)
+        _ring(nl, st, cload=cl, nmos=nm, pmos=pm, prefix=f"c{ci}.")
+        nl.end_circuit()
+    nl.tran = Tran(tstop=10e-9, hmax=5e-12)
+    return nl
