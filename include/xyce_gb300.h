@@ -1,0 +1,199 @@
+/*
+ * xyce_gb300.h — C-ABI of the GB300 transient Newton hot path.
+ *
+ * One library, libxyce_gb300.so, built for sm_103a.  It replaces, behind
+ * plain pointers and sizes, the path Xyce runs on every Newton iteration:
+ *
+ *   Device::DeviceMgr::updateState / loadDAEVectors / loadDAEMatrices
+ *     src/DeviceModelPKG/Core/N_DEV_DeviceMgr.C:3857, 4156, 3980
+ *     (called by Loader::CktLoader, src/LoaderServicesPKG/N_LOA_CktLoader.C:913, 615, 458,
+ *      abstract interface src/LoaderServicesPKG/N_LOA_Loader.h:97-365)
+ *   the KLU numeric refactorization and solve
+ *     src/LinearAlgebraServicesPKG/N_LAS_AmesosSolver.C:216-440
+ *   Nonlinear::DampedNewton::solve / converged_
+ *     src/NonlinearSolverPKG/N_NLS_DampedNewton.C:362-520, 1191-1396
+ *   TimeIntg::OneStep predictor / residual / Jacobian / step control
+ *     src/TimeIntegrationPKG/N_TIA_OneStep.C:135-500, 1584-2240
+ *
+ * Conventions
+ *   - Unknowns are 0-based MNA indices; ground is -1.
+ *   - Every vector or matrix-value pointer passed to the loader, solve and
+ *     update entry points is a DEVICE pointer (cudaMalloc'd by the caller,
+ *     on the context's device).  Setup entry points take HOST arrays.
+ *   - Matrix values are in the CSR pattern returned by xg_get_pattern.
+ *   - All entry points return an int status: XG_OK (0) or a negative code.
+ *   - Calls are ordered on the context's CUDA stream; functions that return
+ *     numeric results to the host synchronize that stream.
+ *   - No entry point falls back to the CPU: without a usable GB300 (sm_103a)
+ *     device, xg_create fails with XG_ERR_CUDA.
+ */
+#ifndef XYCE_GB300_H
+#define XYCE_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define XG_OK               0
+#define XG_ERR_ARG         -1   /* bad argument or size */
+#define XG_ERR_CUDA        -2   /* CUDA runtime failure / no sm_103a device */
+#define XG_ERR_STATE       -3   /* call out of order (e.g. load before finalize) */
+#define XG_ERR_UNSUPPORTED -4   /* device feature not implemented */
+#define XG_ERR_NAN         -6   /* DampedNewton nanFail */
+#define XG_ERR_SINGULAR    -9   /* DampedNewton linearSolverFailed: pivot breakdown */
+#define XG_ERR_TIMEOUT    -10   /* a bounded device-side wait ran out */
+
+/* ---- loadType (Xyce Loader: ALL / LINEAR / NONLINEAR) ------------------ */
+#define XG_LOAD_ALL        0
+#define XG_LOAD_LINEAR     1
+#define XG_LOAD_NONLINEAR  2
+
+/* ---- solver-state flags for xg_update_state ---------------------------- */
+#define XG_FLAG_DCOP       1    /* SolverState::dcopFlag (operating point) */
+#define XG_FLAG_INITJCT    2    /* SolverState::initJctFlag_ (first DC iteration) */
+
+/* ---- source waveform kinds (N_DEV_SourceData.C) ------------------------ */
+#define XG_WAVE_DC    0   /* data: V                                        */
+#define XG_WAVE_SIN   1   /* data: V0 VA FREQ TD THETA PHASE                */
+#define XG_WAVE_PULSE 2   /* data: V1 V2 TD TR TF PW PER                    */
+#define XG_WAVE_PWL   3   /* data: t0 v0 t1 v1 ...                          */
+
+/* ---- diode parameter row (Diode model/instance params, N_DEV_Diode.C:100-345) */
+enum {
+  XG_DIODE_IS, XG_DIODE_N, XG_DIODE_RS, XG_DIODE_CJO, XG_DIODE_VJ, XG_DIODE_M,
+  XG_DIODE_FC, XG_DIODE_TT, XG_DIODE_BV, XG_DIODE_IBV, XG_DIODE_NBV, XG_DIODE_IKF,
+  XG_DIODE_ISR, XG_DIODE_NR, XG_DIODE_EG, XG_DIODE_XTI, XG_DIODE_AREA,
+  XG_DIODE_BVGIVEN, XG_DIODE_NPARAM
+};
+
+/* ---- MOSFET level-1 parameter row (N_DEV_MOSFET1.C:61-331) -------------- */
+enum {
+  XG_MOS1_TYPE, XG_MOS1_VTO, XG_MOS1_KP, XG_MOS1_GAMMA, XG_MOS1_PHI, XG_MOS1_LAMBDA,
+  XG_MOS1_RD, XG_MOS1_RS, XG_MOS1_CBD, XG_MOS1_CBS, XG_MOS1_IS, XG_MOS1_PB,
+  XG_MOS1_CGSO, XG_MOS1_CGDO, XG_MOS1_CGBO, XG_MOS1_CJ, XG_MOS1_MJ, XG_MOS1_CJSW,
+  XG_MOS1_MJSW, XG_MOS1_JS, XG_MOS1_TOX, XG_MOS1_LD, XG_MOS1_FC, XG_MOS1_W, XG_MOS1_L,
+  XG_MOS1_AD, XG_MOS1_AS, XG_MOS1_PD, XG_MOS1_PS, XG_MOS1_M, XG_MOS1_NPARAM
+};
+
+typedef struct xg_ctx xg_ctx;
+
+/* ---- context ------------------------------------------------------------ */
+/* Replaces Simulator::doAllocations_ for this path (N_CIR_Xyce.C:515-566):
+ * binds the calling thread to `device` and creates the context's stream. */
+int xg_create(xg_ctx **out, int device);
+int xg_destroy(xg_ctx *ctx);
+/* Last error message of the context (never NULL). */
+const char *xg_error_string(const xg_ctx *ctx);
+/* cudaStream_t of the context, as void*. */
+void *xg_get_stream(xg_ctx *ctx);
+int xg_synchronize(xg_ctx *ctx);
+
+/* ---- topology upload (host arrays) ---------------------------------------
+ * Replaces Topology::registerLIDswithDevs + Builder::generateGraphs
+ * (N_CIR_Xyce.C:657-696, N_LAS_Builder.C:384-418).  n_circuits independent
+ * circuits occupy contiguous unknown ranges [offsets[c], offsets[c+1]). */
+int xg_set_unknowns(xg_ctx *ctx, int n_unknowns, int n_circuits, const int *offsets);
+/* Resistor::Instance (N_DEV_Resistor.C), value in ohms. */
+int xg_add_resistors(xg_ctx *ctx, int n, const int *pos, const int *neg, const double *r);
+/* Capacitor::Instance (N_DEV_Capacitor.C), value in farads. */
+int xg_add_capacitors(xg_ctx *ctx, int n, const int *pos, const int *neg, const double *c);
+/* Vsrc::Instance (N_DEV_Vsrc.C): branch = unknown of the branch current.
+ * Waveform k is kind[k] with data[off[k] .. off[k+1]). */
+int xg_add_vsources(xg_ctx *ctx, int n, const int *pos, const int *neg, const int *branch,
+                    const int *kind, const int *off, const double *data);
+/* ISRC::Instance (N_DEV_ISRC.C). */
+int xg_add_isources(xg_ctx *ctx, int n, const int *pos, const int *neg,
+                    const int *kind, const int *off, const double *data);
+/* Diode::Instance level 1 (N_DEV_Diode.C); pri = internal node (== pos when RS = 0);
+ * params is n x XG_DIODE_NPARAM row-major. */
+int xg_add_diodes(xg_ctx *ctx, int n, const int *pos, const int *neg, const int *pri,
+                  const double *params);
+/* MOSFET1::Instance (N_DEV_MOSFET1.C); params n x XG_MOS1_NPARAM row-major.
+ * Series drain/source resistance (RD, RS, RSH) is XG_ERR_UNSUPPORTED. */
+int xg_add_mosfet1(xg_ctx *ctx, int n, const int *d, const int *g, const int *s,
+                   const int *b, const double *params);
+/* Builds the CSR pattern, the stamp map, device-resident SoA instance
+ * arrays and the symbolic structures (DeviceMgr::initializeAll + setupPointers,
+ * N_CIR_Xyce.C:698-717, N_DEV_Diode.C:778-800). */
+int xg_finalize(xg_ctx *ctx);
+
+int xg_get_sizes(xg_ctx *ctx, int *n_unknowns, int *nnz, int *n_state, int *n_store);
+/* Host copies of the CSR pattern: row_ptr[n+1], col_idx[nnz]. */
+int xg_get_pattern(xg_ctx *ctx, int *row_ptr, int *col_idx);
+
+/* ---- loader (DEVICE pointers) --------------------------------------------- */
+/* DeviceMgr::updateSources (N_DEV_DeviceMgr.C:4900): source values at `time`. */
+int xg_update_sources(xg_ctx *ctx, double time);
+/* DeviceMgr::updateState (N_DEV_DeviceMgr.C:3857-3936): evaluates every
+ * nonlinear device at next_sol, writes next_sta / next_sto, and keeps the
+ * per-instance stamp values for the two load calls that follow.
+ * History selection follows the reference: newton_iter == 0 reads curr_sto,
+ * later iterations read next_sto as left by the previous call. */
+int xg_update_state(xg_ctx *ctx, const double *next_sol, const double *curr_sta,
+                    const double *curr_sto, double *next_sta, double *next_sto,
+                    int newton_iter, int flags);
+/* DeviceMgr::loadDAEVectors (N_DEV_DeviceMgr.C:4156-4284): ADDS the device
+ * contributions into Q, F, B, dFdxdVp, dQdxdVp (length n).  As in the
+ * reference, the caller zeroes them first (N_LOA_NonlinearEquationLoader.C:385-390). */
+int xg_load_dae_vectors(xg_ctx *ctx, const double *next_sol, double *Q, double *F,
+                        double *B, double *dFdxdVp, double *dQdxdVp, int load_type);
+/* DeviceMgr::loadDAEMatrices (N_DEV_DeviceMgr.C:3980-4115): ADDS into the
+ * dQdx and dFdx CSR value arrays (length nnz); caller zeroes first
+ * (N_LOA_NonlinearEquationLoader.C:525-526). */
+int xg_load_dae_matrices(xg_ctx *ctx, double *dQdx, double *dFdx, int load_type);
+
+/* ---- sparse direct solve on the frozen pattern ----------------------------
+ * AmesosSolver::doSolve with KLU (N_LAS_AmesosSolver.C:216-440): symbolic
+ * analysis once (row matching from the values, fill-reducing order,
+ * level schedule), numeric refactorization with frozen pivots on every call.
+ * xg_lu_factor returns XG_ERR_SINGULAR when a pivot breaks down; calling
+ * xg_lu_analyze again with the current values re-pivots. */
+int xg_lu_analyze(xg_ctx *ctx, const double *vals);
+int xg_lu_factor(xg_ctx *ctx, const double *vals);
+int xg_lu_solve(xg_ctx *ctx, const double *rhs, double *x);
+/* Statistics of the current analysis: nnz(L+U), factor/solve level counts. */
+int xg_lu_info(xg_ctx *ctx, long long *nnz_lu, int *factor_levels, int *lsolve_levels,
+               int *usolve_levels);
+
+/* ---- Newton + time integration driver --------------------------------------
+ * Transient::doRun (N_ANP_Transient.C:739-772, 1184-1410, 3262-3325): DC
+ * operating point, then OneStep (backward Euler start, trapezoid) with
+ * DampedNewton on every step, all device-resident.  Each circuit of a batch
+ * runs its own step-size control. */
+typedef struct xg_tran_params {
+  double tstart, tstop, hmax, hmin;
+  double reltol, abstol;                       /* .OPTIONS TIMEINT */
+  double nl_reltol, nl_abstol, nl_deltaxtol, nl_rhstol, nl_smallupdatetol;
+  int nl_maxstep;                              /* .OPTIONS NONLIN-TRAN */
+  int max_steps;                               /* stop after this many accepted steps (0 = none) */
+  int max_order;                               /* 1 = backward Euler, 2 = trapezoid */
+} xg_tran_params;
+
+typedef struct xg_tran_stats {
+  long long accepted, rejected, newton_iters, newton_fail, lte_fail, dcop_iters;
+  long long ticks, device_evals;               /* Newton iterations launched; instance evaluations */
+  int status;                                  /* 0 ok, else first failing circuit's code */
+  int n_analyze;                               /* symbolic (re)analyses performed */
+  double t_final_min, t_final_max;
+  double seconds;                              /* wall time of the run */
+} xg_tran_stats;
+
+/* Runs the transient.  probes: global unknown indices to record; every
+ * circuit records, at each accepted point, its time and the values of the
+ * probes inside it (in the order given), up to cap points per circuit.
+ * Host outputs: counts[n_circuits], times[n_circuits*cap],
+ * values[n_circuits*cap*pmax] where pmax = the largest number of probes in one circuit.
+ * Any output pointer may be NULL when cap == 0. */
+int xg_transient(xg_ctx *ctx, const xg_tran_params *p, int n_probe, const int *probes,
+                 int cap, int *counts, double *times, double *values, xg_tran_stats *stats);
+/* Operating point only; x_host receives the n solution values. */
+int xg_dcop(xg_ctx *ctx, double *x_host, int *iters);
+
+/* Version of the library (major*10000 + minor*100 + patch). */
+int xg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XYCE_GB300_H */

@@ -1,0 +1,245 @@
+"""xyce_gb300 — GB300-native transient Newton hot path of the Xyce circuit simulator.
+
+The compute path is libxyce_gb300.so (hand-written sm_103a CUDA + C++ host,
+C-ABI declared in include/xyce_gb300.h).  This module is a thin ctypes
+binding to that library; it never computes anything itself and has no CPU
+fallback: without the library or without a GB300 device every call raises.
+
+Python mirror of the reference interfaces:
+  * :class:`Circuit.update_state` / :meth:`Circuit.load_dae_vectors` /
+    :meth:`Circuit.load_dae_matrices` follow Device::DeviceMgr's
+    updateState / loadDAEVectors / loadDAEMatrices
+    (src/DeviceModelPKG/Core/N_DEV_DeviceMgr.C:3857, 4156, 3980) and take
+    torch CUDA tensors as the Linear::Vector / Linear::Matrix storage;
+  * :meth:`Circuit.lu_analyze` / :meth:`lu_factor` / :meth:`lu_solve` follow
+    AmesosSolver::doSolve (src/LinearAlgebraServicesPKG/N_LAS_AmesosSolver.C:216-440);
+  * :meth:`Circuit.transient` runs Transient::doRun (src/AnalysisPKG/N_ANP_Transient.C:739)
+    with DampedNewton and OneStep entirely on the device.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import netlist  # noqa: F401  (re-export)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libxyce_gb300.so")
+
+XG_OK = 0
+XG_ERR = {-1: "ARG", -2: "CUDA", -3: "STATE", -4: "UNSUPPORTED", -6: "NAN", -9: "SINGULAR",
+          -10: "TIMEOUT"}
+LOAD_ALL, LOAD_LINEAR, LOAD_NONLINEAR = 0, 1, 2
+FLAG_DCOP, FLAG_INITJCT = 1, 2
+
+# Every symbol declared in include/xyce_gb300.h.
+EXPORTED = [
+    "xg_create", "xg_destroy", "xg_error_string", "xg_get_stream", "xg_synchronize",
+    "xg_set_unknowns", "xg_add_resistors", "xg_add_capacitors", "xg_add_vsources",
+    "xg_add_isources", "xg_add_diodes", "xg_add_mosfet1", "xg_finalize", "xg_get_sizes",
+    "xg_get_pattern", "xg_update_sources", "xg_update_state", "xg_load_dae_vectors",
+    "xg_load_dae_matrices", "xg_lu_analyze", "xg_lu_factor", "xg_lu_solve", "xg_lu_info",
+    "xg_transient", "xg_dcop", "xg_version",
+]
+
+
+class XgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"xyce_gb300 error {code} ({XG_ERR.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class TranParams(C.Structure):
+    _fields_ = [("tstart", C.c_double), ("tstop", C.c_double), ("hmax", C.c_double),
+                ("hmin", C.c_double), ("reltol", C.c_double), ("abstol", C.c_double),
+                ("nl_reltol", C.c_double), ("nl_abstol", C.c_double),
+                ("nl_deltaxtol", C.c_double), ("nl_rhstol", C.c_double),
+                ("nl_smallupdatetol", C.c_double), ("nl_maxstep", C.c_int),
+                ("max_steps", C.c_int), ("max_order", C.c_int)]
+
+
+class TranStats(C.Structure):
+    _fields_ = [("accepted", C.c_longlong), ("rejected", C.c_longlong),
+                ("newton_iters", C.c_longlong), ("newton_fail", C.c_longlong),
+                ("lte_fail", C.c_longlong), ("dcop_iters", C.c_longlong),
+                ("ticks", C.c_longlong), ("device_evals", C.c_longlong), ("status", C.c_int),
+                ("n_analyze", C.c_int), ("t_final_min", C.c_double),
+                ("t_final_max", C.c_double), ("seconds", C.c_double)]
+
+
+_lib = None
+
+
+def build(**kw) -> str:
+    from .build import build as _b
+    return _b(**kw)
+
+
+def lib() -> C.CDLL:
+    """Load libxyce_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: run __graft_entry__.build()")
+    L = C.CDLL(LIB_PATH)
+    P, I, D = C.c_void_p, C.c_int, C.c_double
+    ip = np.ctypeslib.ndpointer(np.int32, flags="C")
+    dp = np.ctypeslib.ndpointer(np.float64, flags="C")
+    L.xg_create.argtypes = [C.POINTER(P), I]
+    L.xg_destroy.argtypes = [P]
+    L.xg_error_string.argtypes = [P]
+    L.xg_error_string.restype = C.c_char_p
+    L.xg_get_stream.argtypes = [P]
+    L.xg_get_stream.restype = P
+    L.xg_synchronize.argtypes = [P]
+    L.xg_set_unknowns.argtypes = [P, I, I, ip]
+    L.xg_add_resistors.argtypes = [P, I, ip, ip, dp]
+    L.xg_add_capacitors.argtypes = [P, I, ip, ip, dp]
+    L.xg_add_vsources.argtypes = [P, I, ip, ip, ip, ip, ip, dp]
+    L.xg_add_isources.argtypes = [P, I, ip, ip, ip, ip, dp]
+    L.xg_add_diodes.argtypes = [P, I, ip, ip, ip, dp]
+    L.xg_add_mosfet1.argtypes = [P, I, ip, ip, ip, ip, dp]
+    L.xg_finalize.argtypes = [P]
+    L.xg_get_sizes.argtypes = [P] + [C.POINTER(I)] * 4
+    L.xg_get_pattern.argtypes = [P, ip, ip]
+    L.xg_update_sources.argtypes = [P, D]
+    L.xg_update_state.argtypes = [P, P, P, P, P, P, I, I]
+    L.xg_load_dae_vectors.argtypes = [P, P, P, P, P, P, P, I]
+    L.xg_load_dae_matrices.argtypes = [P, P, P, I]
+    L.xg_lu_analyze.argtypes = [P, P]
+    L.xg_lu_factor.argtypes = [P, P]
+    L.xg_lu_solve.argtypes = [P, P, P]
+    L.xg_lu_info.argtypes = [P, C.POINTER(C.c_longlong), C.POINTER(I), C.POINTER(I), C.POINTER(I)]
+    L.xg_transient.argtypes = [P, C.POINTER(TranParams), I, ip, I, ip, dp, dp, C.POINTER(TranStats)]
+    L.xg_dcop.argtypes = [P, dp, C.POINTER(I)]
+    L.xg_version.argtypes = []
+    _lib = L
+    return L
+
+
+def _ptr(t):
+    """Device pointer of a torch CUDA tensor (float64, contiguous)."""
+    if t is None:
+        return None
+    if not t.is_cuda or not t.is_contiguous():
+        raise ValueError("expected a contiguous CUDA tensor")
+    return C.c_void_p(t.data_ptr())
+
+
+class Circuit:
+    """A netlist (or batch of circuits) resident on one GB300."""
+
+    def __init__(self, nl, device: int = 0):
+        L = lib()
+        self.netlist = nl
+        self.h = C.c_void_p()
+        rc = L.xg_create(C.byref(self.h), device)
+        if rc != XG_OK:
+            raise XgError(rc, "xg_create: no usable sm_103a (GB300) device")
+        a = nl.arrays()
+        self._check(L.xg_set_unknowns(self.h, a["n"], len(a["offsets"]) - 1, a["offsets"]))
+        p, m, v = a["res"]
+        self._check(L.xg_add_resistors(self.h, len(p), p, m, v))
+        p, m, v = a["cap"]
+        self._check(L.xg_add_capacitors(self.h, len(p), p, m, v))
+        p, m, b, k, o, d = a["vsrc"]
+        self._check(L.xg_add_vsources(self.h, len(p), p, m, b, k, o, d))
+        p, m, k, o, d = a["isrc"]
+        self._check(L.xg_add_isources(self.h, len(p), p, m, k, o, d))
+        p, m, r, prm = a["diode"]
+        self._check(L.xg_add_diodes(self.h, len(p), p, m, r, prm))
+        dd, g, s, b, prm = a["mos1"]
+        self._check(L.xg_add_mosfet1(self.h, len(dd), dd, g, s, b, prm))
+        self._check(L.xg_finalize(self.h))
+        n, nnz, nsta, nsto = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        self._check(L.xg_get_sizes(self.h, C.byref(n), C.byref(nnz), C.byref(nsta), C.byref(nsto)))
+        self.n, self.nnz, self.nsta, self.nsto = n.value, nnz.value, nsta.value, nsto.value
+        self.row_ptr = np.zeros(self.n + 1, np.int32)
+        self.col_idx = np.zeros(self.nnz, np.int32)
+        self._check(L.xg_get_pattern(self.h, self.row_ptr, self.col_idx))
+        self.n_circuits = len(a["offsets"]) - 1
+
+    def _check(self, rc):
+        if rc != XG_OK:
+            raise XgError(rc, lib().xg_error_string(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().xg_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- loader (DeviceMgr mirror) -------------------------------------
+    def update_sources(self, time: float):
+        self._check(lib().xg_update_sources(self.h, float(time)))
+
+    def update_state(self, next_sol, curr_sta, curr_sto, next_sta, next_sto, newton_iter=0, flags=0):
+        self._check(lib().xg_update_state(self.h, _ptr(next_sol), _ptr(curr_sta), _ptr(curr_sto),
+                                          _ptr(next_sta), _ptr(next_sto), int(newton_iter), int(flags)))
+
+    def load_dae_vectors(self, next_sol, Q, F, B, dFdxdVp, dQdxdVp, load_type=LOAD_ALL):
+        self._check(lib().xg_load_dae_vectors(self.h, _ptr(next_sol), _ptr(Q), _ptr(F), _ptr(B),
+                                              _ptr(dFdxdVp), _ptr(dQdxdVp), int(load_type)))
+
+    def load_dae_matrices(self, dQdx, dFdx, load_type=LOAD_ALL):
+        self._check(lib().xg_load_dae_matrices(self.h, _ptr(dQdx), _ptr(dFdx), int(load_type)))
+
+    def synchronize(self):
+        self._check(lib().xg_synchronize(self.h))
+
+    # ---- linear solve (AmesosSolver mirror) ----------------------------
+    def lu_analyze(self, vals):
+        self._check(lib().xg_lu_analyze(self.h, _ptr(vals)))
+
+    def lu_factor(self, vals):
+        self._check(lib().xg_lu_factor(self.h, _ptr(vals)))
+
+    def lu_solve(self, rhs, x):
+        self._check(lib().xg_lu_solve(self.h, _ptr(rhs), _ptr(x)))
+
+    def lu_info(self):
+        nnz = C.c_longlong()
+        f, l, u = C.c_int(), C.c_int(), C.c_int()
+        self._check(lib().xg_lu_info(self.h, C.byref(nnz), C.byref(f), C.byref(l), C.byref(u)))
+        return dict(nnz_lu=nnz.value, factor_levels=f.value, lsolve_levels=l.value,
+                    usolve_levels=u.value)
+
+    # ---- analyses -------------------------------------------------------
+    def dcop(self):
+        x = np.zeros(self.n)
+        it = C.c_int()
+        self._check(lib().xg_dcop(self.h, x, C.byref(it)))
+        return x, it.value
+
+    def transient(self, tran=None, probes=(), cap=0):
+        """Run the transient; returns (counts, times, values, stats) where
+        times is [n_circuits, cap] and values [n_circuits, cap, pmax]."""
+        tran = tran or self.netlist.tran
+        probes = np.asarray(probes, np.int32)
+        tp = TranParams(tran.tstart, tran.tstop, tran.hmax, tran.hmin, tran.reltol, tran.abstol,
+                        tran.nl_reltol, tran.nl_abstol, tran.nl_deltaxtol, tran.nl_rhstol,
+                        tran.nl_smallupdatetol, tran.nl_maxstep, tran.max_steps, tran.max_order)
+        nc = self.n_circuits
+        offs = np.asarray(self.netlist.offsets)
+        per = np.bincount(np.searchsorted(offs, probes, side="right") - 1, minlength=nc) \
+            if len(probes) else np.zeros(nc, int)
+        pmax = max(1, int(per.max()) if len(per) else 1)
+        counts = np.zeros(nc, np.int32)
+        times = np.zeros(max(1, nc * cap))
+        values = np.zeros(max(1, nc * cap * pmax))
+        st = TranStats()
+        self._check(lib().xg_transient(self.h, C.byref(tp), len(probes), probes, int(cap), counts,
+                                       times, values, C.byref(st)))
+        stats = {f: getattr(st, f) for f, _ in TranStats._fields_}
+        if cap:
+            times = times[: nc * cap].reshape(nc, cap)
+            values = values[: nc * cap * pmax].reshape(nc, cap, pmax)
+        return counts, times, values, stats

@@ -1,0 +1,947 @@
+// xg_api.cpp — the C-ABI of libxyce_gb300.so: context, topology upload,
+// stamp-map construction, loader entry points, LU entry points and the
+// device-resident transient driver.
+#include <algorithm>
+#include <chrono>
+#include <cstddef>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "xg_internal.h"
+#include "xg_params.h"
+
+using namespace xg;
+
+struct Wave {
+  int kind;
+  std::vector<double> d;
+};
+
+struct xg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err = "";
+  int n = 0, ncirc = 0;
+  std::vector<int> offsets;
+  bool unknowns_set = false, finalized = false;
+  // host copies of the devices
+  std::vector<int> r_p, r_n, c_p, c_n, v_p, v_n, v_b, i_p, i_n;
+  std::vector<double> r_v, c_v;
+  std::vector<Wave> v_w, i_w;
+  std::vector<int> d_p, d_n, d_r;
+  std::vector<double> d_par;
+  std::vector<int> m_d, m_g, m_s, m_b;
+  std::vector<double> m_par;
+  // finalized structure
+  std::vector<int> rp, ci, circ_of_row;
+  std::vector<long long> inst_of_circ;  // nonlinear device instances per circuit
+  int nnz = 0, nm = 0, nd = 0, nv = 0, ni = 0;
+  int nsto = 0, nsta = 0, sto_base_m = 0;
+  int sF_m = 0, sF_d = 0, sQ_m = 0, sQ_d = 0, sL_m = 0, sL_d = 0, sM_m = 0, sM_d = 0;
+  int n_pairs = 0, n_rowblocks = 0;
+  DevArrays d;
+  LUDev L;
+  bool lu_ready = false;
+  int n_analyze = 0;
+  std::vector<void *> allocs;      // device allocations owned by the context
+  std::vector<void *> lu_allocs;   // allocations of the current LU analysis
+  int *status_host = nullptr;      // mapped [finished, breakdown]
+  int *status_dev = nullptr;
+  int *breakdown_dev = nullptr;
+};
+
+namespace {
+
+int fail(xg_ctx *c, int code, const std::string &msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                      \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess)                                                            \
+      return fail(ctx, XG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+int dev_alloc(xg_ctx *ctx, T **p, size_t count, std::vector<void *> &owner) {
+  *p = nullptr;
+  size_t bytes = std::max<size_t>(1, count) * sizeof(T);
+  cudaError_t e = cudaMalloc((void **)p, bytes);
+  if (e != cudaSuccess) return fail(ctx, XG_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  owner.push_back(*p);
+  e = cudaMemsetAsync(*p, 0, bytes, ctx->stream);
+  if (e != cudaSuccess) return fail(ctx, XG_ERR_CUDA, std::string("cudaMemset: ") + cudaGetErrorString(e));
+  return XG_OK;
+}
+
+template <class T>
+int dev_upload(xg_ctx *ctx, T **p, const std::vector<T> &v, std::vector<void *> &owner) {
+  int rc = dev_alloc(ctx, p, v.size(), owner);
+  if (rc) return rc;
+  if (!v.empty()) {
+    cudaError_t e = cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, XG_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+  }
+  return XG_OK;
+}
+
+void free_list(std::vector<void *> &v) {
+  for (void *p : v) cudaFree(p);
+  v.clear();
+}
+
+bool valid_node(const xg_ctx *c, int i) { return i >= -1 && i < c->n; }
+
+// First circuit among the given nodes (ground ignored).
+int circuit_of_nodes(const xg_ctx *c, std::initializer_list<int> nodes) {
+  for (int v : nodes)
+    if (v >= 0) return c->circ_of_row[v];
+  return -1;
+}
+
+}  // namespace
+
+extern "C" {
+
+int xg_version(void) { return 100; }
+
+int xg_create(xg_ctx **out, int device) {
+  if (!out) return XG_ERR_ARG;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= device || device < 0) return XG_ERR_CUDA;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return XG_ERR_CUDA;
+  if (!(prop.major == 10 && prop.minor == 3)) {
+    // the kernels are built for sm_103a only; there is no other path
+    return XG_ERR_CUDA;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) return XG_ERR_CUDA;
+  xg_ctx *c = new xg_ctx;
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return XG_ERR_CUDA;
+  }
+  if (cudaHostAlloc((void **)&c->status_host, 4 * sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostGetDevicePointer((void **)&c->status_dev, c->status_host, 0) != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return XG_ERR_CUDA;
+  }
+  memset(c->status_host, 0, 4 * sizeof(int));
+  *out = c;
+  return XG_OK;
+}
+
+int xg_destroy(xg_ctx *ctx) {
+  if (!ctx) return XG_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  free_list(ctx->lu_allocs);
+  free_list(ctx->allocs);
+  if (ctx->status_host) cudaFreeHost(ctx->status_host);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return XG_OK;
+}
+
+const char *xg_error_string(const xg_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+void *xg_get_stream(xg_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int xg_synchronize(xg_ctx *ctx) {
+  if (!ctx) return XG_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return XG_OK;
+}
+
+int xg_set_unknowns(xg_ctx *ctx, int n, int ncirc, const int *offsets) {
+  if (!ctx || n <= 0 || ncirc <= 0 || !offsets) return fail(ctx, XG_ERR_ARG, "xg_set_unknowns: bad arguments");
+  if (ctx->finalized) return fail(ctx, XG_ERR_STATE, "xg_set_unknowns after finalize");
+  if (offsets[0] != 0 || offsets[ncirc] != n) return fail(ctx, XG_ERR_ARG, "offsets must span [0, n]");
+  for (int c = 0; c < ncirc; ++c)
+    if (offsets[c + 1] <= offsets[c]) return fail(ctx, XG_ERR_ARG, "empty or decreasing circuit range");
+  ctx->n = n;
+  ctx->ncirc = ncirc;
+  ctx->offsets.assign(offsets, offsets + ncirc + 1);
+  ctx->circ_of_row.assign(n, 0);
+  for (int c = 0; c < ncirc; ++c)
+    for (int i = offsets[c]; i < offsets[c + 1]; ++i) ctx->circ_of_row[i] = c;
+  ctx->unknowns_set = true;
+  return XG_OK;
+}
+
+#define SETUP_CHECK()                                                                  \
+  if (!ctx) return XG_ERR_ARG;                                                         \
+  if (!ctx->unknowns_set) return fail(ctx, XG_ERR_STATE, "call xg_set_unknowns first"); \
+  if (ctx->finalized) return fail(ctx, XG_ERR_STATE, "topology is already finalized"); \
+  if (n < 0) return fail(ctx, XG_ERR_ARG, "negative count");
+
+int xg_add_resistors(xg_ctx *ctx, int n, const int *pos, const int *neg, const double *r) {
+  SETUP_CHECK();
+  for (int k = 0; k < n; ++k) {
+    if (!valid_node(ctx, pos[k]) || !valid_node(ctx, neg[k])) return fail(ctx, XG_ERR_ARG, "resistor node out of range");
+    if (!(r[k] != 0.0) || !std::isfinite(r[k])) return fail(ctx, XG_ERR_ARG, "resistor value must be finite and nonzero");
+    ctx->r_p.push_back(pos[k]); ctx->r_n.push_back(neg[k]); ctx->r_v.push_back(r[k]);
+  }
+  return XG_OK;
+}
+
+int xg_add_capacitors(xg_ctx *ctx, int n, const int *pos, const int *neg, const double *cv) {
+  SETUP_CHECK();
+  for (int k = 0; k < n; ++k) {
+    if (!valid_node(ctx, pos[k]) || !valid_node(ctx, neg[k])) return fail(ctx, XG_ERR_ARG, "capacitor node out of range");
+    if (!std::isfinite(cv[k])) return fail(ctx, XG_ERR_ARG, "capacitor value must be finite");
+    ctx->c_p.push_back(pos[k]); ctx->c_n.push_back(neg[k]); ctx->c_v.push_back(cv[k]);
+  }
+  return XG_OK;
+}
+
+static int check_wave(xg_ctx *ctx, int kind, int len) {
+  static const int need[4] = {1, 6, 7, 2};
+  if (kind < 0 || kind > 3) return fail(ctx, XG_ERR_ARG, "unknown waveform kind");
+  if (len < need[kind]) return fail(ctx, XG_ERR_ARG, "waveform has too few values");
+  if (kind == XG_WAVE_PWL && (len % 2) != 0) return fail(ctx, XG_ERR_ARG, "PWL needs time/value pairs");
+  return XG_OK;
+}
+
+int xg_add_vsources(xg_ctx *ctx, int n, const int *pos, const int *neg, const int *branch, const int *kind,
+                    const int *off, const double *data) {
+  SETUP_CHECK();
+  for (int k = 0; k < n; ++k) {
+    if (!valid_node(ctx, pos[k]) || !valid_node(ctx, neg[k]) || branch[k] < 0 || branch[k] >= ctx->n)
+      return fail(ctx, XG_ERR_ARG, "voltage source node out of range");
+    int rc = check_wave(ctx, kind[k], off[k + 1] - off[k]);
+    if (rc) return rc;
+    ctx->v_p.push_back(pos[k]); ctx->v_n.push_back(neg[k]); ctx->v_b.push_back(branch[k]);
+    ctx->v_w.push_back({kind[k], std::vector<double>(data + off[k], data + off[k + 1])});
+  }
+  return XG_OK;
+}
+
+int xg_add_isources(xg_ctx *ctx, int n, const int *pos, const int *neg, const int *kind, const int *off,
+                    const double *data) {
+  SETUP_CHECK();
+  for (int k = 0; k < n; ++k) {
+    if (!valid_node(ctx, pos[k]) || !valid_node(ctx, neg[k])) return fail(ctx, XG_ERR_ARG, "current source node out of range");
+    int rc = check_wave(ctx, kind[k], off[k + 1] - off[k]);
+    if (rc) return rc;
+    ctx->i_p.push_back(pos[k]); ctx->i_n.push_back(neg[k]);
+    ctx->i_w.push_back({kind[k], std::vector<double>(data + off[k], data + off[k + 1])});
+  }
+  return XG_OK;
+}
+
+int xg_add_diodes(xg_ctx *ctx, int n, const int *pos, const int *neg, const int *pri, const double *params) {
+  SETUP_CHECK();
+  for (int k = 0; k < n; ++k) {
+    if (!valid_node(ctx, pos[k]) || !valid_node(ctx, neg[k]) || !valid_node(ctx, pri[k]))
+      return fail(ctx, XG_ERR_ARG, "diode node out of range");
+    const double *p = params + (size_t)k * XG_DIODE_NPARAM;
+    if ((p[XG_DIODE_RS] == 0.0) != (pri[k] == pos[k]))
+      return fail(ctx, XG_ERR_ARG, "diode internal node must equal pos exactly when RS = 0");
+    ctx->d_p.push_back(pos[k]); ctx->d_n.push_back(neg[k]); ctx->d_r.push_back(pri[k]);
+    ctx->d_par.insert(ctx->d_par.end(), p, p + XG_DIODE_NPARAM);
+  }
+  return XG_OK;
+}
+
+int xg_add_mosfet1(xg_ctx *ctx, int n, const int *dd, const int *g, const int *s, const int *b,
+                   const double *params) {
+  SETUP_CHECK();
+  for (int k = 0; k < n; ++k) {
+    if (!valid_node(ctx, dd[k]) || !valid_node(ctx, g[k]) || !valid_node(ctx, s[k]) || !valid_node(ctx, b[k]))
+      return fail(ctx, XG_ERR_ARG, "MOSFET node out of range");
+    const double *p = params + (size_t)k * XG_MOS1_NPARAM;
+    if (p[XG_MOS1_RD] != 0.0 || p[XG_MOS1_RS] != 0.0)
+      return fail(ctx, XG_ERR_UNSUPPORTED, "MOSFET level 1 with series drain/source resistance");
+    if (p[XG_MOS1_TYPE] != 1.0 && p[XG_MOS1_TYPE] != -1.0) return fail(ctx, XG_ERR_ARG, "MOSFET TYPE must be +1 or -1");
+    ctx->m_d.push_back(dd[k]); ctx->m_g.push_back(g[k]); ctx->m_s.push_back(s[k]); ctx->m_b.push_back(b[k]);
+    ctx->m_par.insert(ctx->m_par.end(), p, p + XG_MOS1_NPARAM);
+  }
+  return XG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// finalize: pattern, stamp map, SoA tables, device buffers.
+int xg_finalize(xg_ctx *ctx) {
+  if (!ctx) return XG_ERR_ARG;
+  if (!ctx->unknowns_set) return fail(ctx, XG_ERR_STATE, "call xg_set_unknowns first");
+  if (ctx->finalized) return fail(ctx, XG_ERR_STATE, "already finalized");
+  CK(cudaSetDevice(ctx->device));
+  const int n = ctx->n;
+  ctx->nm = (int)ctx->m_d.size();
+  ctx->nd = (int)ctx->d_p.size();
+  ctx->nv = (int)ctx->v_p.size();
+  ctx->ni = (int)ctx->i_p.size();
+  const int nm = ctx->nm, nd = ctx->nd, nv = ctx->nv, ni = ctx->ni;
+  // device circuits must not straddle circuits
+  auto same_circuit = [&](std::initializer_list<int> nodes) {
+    int c = -2;
+    for (int v : nodes) {
+      if (v < 0) continue;
+      int cc = ctx->circ_of_row[v];
+      if (c == -2) c = cc;
+      else if (c != cc) return false;
+    }
+    return true;
+  };
+  for (int k = 0; k < nm; ++k)
+    if (!same_circuit({ctx->m_d[k], ctx->m_g[k], ctx->m_s[k], ctx->m_b[k]})) return fail(ctx, XG_ERR_ARG, "MOSFET spans two circuits");
+  for (int k = 0; k < nd; ++k)
+    if (!same_circuit({ctx->d_p[k], ctx->d_n[k], ctx->d_r[k]})) return fail(ctx, XG_ERR_ARG, "diode spans two circuits");
+  // matrix stamp positions (row, col) with their slot ids; -1 for ground rows/cols
+  std::vector<std::vector<int>> rows(n);
+  auto addp = [&](int r, int c) { if (r >= 0 && c >= 0) rows[r].push_back(c); };
+  for (size_t k = 0; k < ctx->r_p.size(); ++k) {
+    int p = ctx->r_p[k], m = ctx->r_n[k];
+    addp(p, p); addp(p, m); addp(m, p); addp(m, m);
+  }
+  for (size_t k = 0; k < ctx->c_p.size(); ++k) {
+    int p = ctx->c_p[k], m = ctx->c_n[k];
+    addp(p, p); addp(p, m); addp(m, p); addp(m, m);
+  }
+  for (int k = 0; k < nv; ++k) {
+    int p = ctx->v_p[k], m = ctx->v_n[k], b = ctx->v_b[k];
+    addp(p, b); addp(m, b); addp(b, p); addp(b, m);
+  }
+  const int dpair[7][2] = {{0, 0}, {0, 2}, {1, 1}, {1, 2}, {2, 0}, {2, 1}, {2, 2}};
+  for (int k = 0; k < nd; ++k) {
+    int nn[3] = {ctx->d_p[k], ctx->d_n[k], ctx->d_r[k]};
+    for (auto &pr : dpair) addp(nn[pr[0]], nn[pr[1]]);
+  }
+  for (int k = 0; k < nm; ++k) {
+    int nn[4] = {ctx->m_d[k], ctx->m_g[k], ctx->m_s[k], ctx->m_b[k]};
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b) addp(nn[a], nn[b]);
+  }
+  for (int i = 0; i < n; ++i) rows[i].push_back(i);
+  ctx->rp.assign(n + 1, 0);
+  ctx->ci.clear();
+  for (int i = 0; i < n; ++i) {
+    auto &r = rows[i];
+    std::sort(r.begin(), r.end());
+    r.erase(std::unique(r.begin(), r.end()), r.end());
+    ctx->ci.insert(ctx->ci.end(), r.begin(), r.end());
+    ctx->rp[i + 1] = (int)ctx->ci.size();
+    std::vector<int>().swap(r);
+  }
+  const int nnz = ctx->nnz = (int)ctx->ci.size();
+  auto find = [&](int r, int c) -> int {
+    if (r < 0 || c < 0) return -1;
+    auto b = ctx->ci.begin() + ctx->rp[r], e = ctx->ci.begin() + ctx->rp[r + 1];
+    auto it = std::lower_bound(b, e, c);
+    return (int)(it - ctx->ci.begin());
+  };
+  std::vector<int> erow(nnz);
+  for (int i = 0; i < n; ++i)
+    for (int e = ctx->rp[i]; e < ctx->rp[i + 1]; ++e) erow[e] = i;
+  // linear part: constant G (R, V incidence) and C values per CSR entry
+  std::vector<double> Glin(nnz, 0.0), Clin(nnz, 0.0);
+  auto addv = [&](std::vector<double> &v, int r, int c, double x) { int e = find(r, c); if (e >= 0) v[e] += x; };
+  for (size_t k = 0; k < ctx->r_p.size(); ++k) {
+    int p = ctx->r_p[k], m = ctx->r_n[k];
+    double G = 1.0 / ctx->r_v[k];
+    addv(Glin, p, p, G); addv(Glin, p, m, -G); addv(Glin, m, p, -G); addv(Glin, m, m, G);
+  }
+  for (size_t k = 0; k < ctx->c_p.size(); ++k) {
+    int p = ctx->c_p[k], m = ctx->c_n[k];
+    double C = ctx->c_v[k];
+    addv(Clin, p, p, C); addv(Clin, p, m, -C); addv(Clin, m, p, -C); addv(Clin, m, m, C);
+  }
+  for (int k = 0; k < nv; ++k) {
+    int p = ctx->v_p[k], m = ctx->v_n[k], b = ctx->v_b[k];
+    addv(Glin, p, b, 1.0); addv(Glin, m, b, -1.0); addv(Glin, b, p, 1.0); addv(Glin, b, m, -1.0);
+  }
+  // slot layout: MOSFETs first, then diodes, plane-major within a type
+  ctx->sF_m = 0; ctx->sF_d = kMosF * nm;
+  ctx->sQ_m = 0; ctx->sQ_d = kMosQ * nm;
+  ctx->sL_m = 0; ctx->sL_d = kMosL * nm;
+  ctx->sM_m = 0; ctx->sM_d = kMosM * nm;
+  const int nF = kMosF * nm + kDioF * nd, nQ = kMosQ * nm + kDioQ * nd, nL = kMosL * nm + kDioL * nd;
+  const int nMs = kMosM * nm + kDioM * nd, nB = nv + 2 * ni;
+  // contribution lists (row -> slots, CSR entry -> slots)
+  std::vector<std::vector<int>> lF(n), lQ(n), lL(n), lB(n), lM(nnz);
+  auto pushv = [&](std::vector<std::vector<int>> &l, int r, int slot) { if (r >= 0) l[r].push_back(slot); };
+  for (int k = 0; k < nm; ++k) {
+    int D = ctx->m_d[k], G = ctx->m_g[k], S = ctx->m_s[k], B = ctx->m_b[k];
+    pushv(lF, D, ctx->sF_m + 0 * nm + k); pushv(lF, S, ctx->sF_m + 1 * nm + k); pushv(lF, B, ctx->sF_m + 2 * nm + k);
+    int qn[4] = {G, B, D, S};
+    for (int j = 0; j < 4; ++j) { pushv(lQ, qn[j], ctx->sQ_m + j * nm + k); pushv(lL, qn[j], ctx->sL_m + j * nm + k); }
+    int nn[4] = {D, G, S, B};
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b) {
+        int e = find(nn[a], nn[b]);
+        if (e >= 0) lM[e].push_back(ctx->sM_m + (4 * a + b) * nm + k);
+      }
+  }
+  for (int k = 0; k < nd; ++k) {
+    int P = ctx->d_p[k], N = ctx->d_n[k], R = ctx->d_r[k];
+    int fn[3] = {P, N, R};
+    for (int j = 0; j < 3; ++j) pushv(lF, fn[j], ctx->sF_d + j * nd + k);
+    int qn[2] = {N, R};
+    for (int j = 0; j < 2; ++j) { pushv(lQ, qn[j], ctx->sQ_d + j * nd + k); pushv(lL, qn[j], ctx->sL_d + j * nd + k); }
+    int nn[3] = {P, N, R};
+    for (int s = 0; s < 7; ++s) {
+      int e = find(nn[dpair[s][0]], nn[dpair[s][1]]);
+      if (e >= 0) lM[e].push_back(ctx->sM_d + s * nd + k);
+    }
+  }
+  for (int k = 0; k < nv; ++k) pushv(lB, ctx->v_b[k], k);
+  for (int k = 0; k < ni; ++k) { pushv(lB, ctx->i_p[k], nv + 2 * k); pushv(lB, ctx->i_n[k], nv + 2 * k + 1); }
+  auto flatten = [&](std::vector<std::vector<int>> &l, std::vector<int> &ptr, std::vector<int> &idx) {
+    ptr.assign(l.size() + 1, 0);
+    for (size_t i = 0; i < l.size(); ++i) ptr[i + 1] = ptr[i] + (int)l[i].size();
+    idx.clear();
+    idx.reserve(ptr.back());
+    for (auto &v : l) { idx.insert(idx.end(), v.begin(), v.end()); std::vector<int>().swap(v); }
+  };
+  std::vector<int> pF, iF, pQ, iQ, pL, iL, pB, iB, pM, iM;
+  flatten(lF, pF, iF); flatten(lQ, pQ, iQ); flatten(lL, pL, iL); flatten(lB, pB, iB); flatten(lM, pM, iM);
+  // sources (V first, then I)
+  std::vector<int> skind, soff(1, 0), scirc;
+  std::vector<double> sdata;
+  for (int k = 0; k < nv; ++k) {
+    skind.push_back(ctx->v_w[k].kind);
+    sdata.insert(sdata.end(), ctx->v_w[k].d.begin(), ctx->v_w[k].d.end());
+    soff.push_back((int)sdata.size());
+    scirc.push_back(ctx->circ_of_row[ctx->v_b[k]]);
+  }
+  for (int k = 0; k < ni; ++k) {
+    skind.push_back(ctx->i_w[k].kind);
+    sdata.insert(sdata.end(), ctx->i_w[k].d.begin(), ctx->i_w[k].d.end());
+    soff.push_back((int)sdata.size());
+    int c = circuit_of_nodes(ctx, {ctx->i_p[k], ctx->i_n[k]});
+    scirc.push_back(c < 0 ? 0 : c);
+  }
+  // MOSFET SoA with effective-model dedup
+  std::vector<int> m1node(4 * (size_t)nm), m1model(nm), m1circ(nm);
+  std::vector<double> m1beta(nm), m1vbi(nm);
+  std::vector<Mos1Model> models;
+  std::map<std::vector<double>, int> model_index;
+  for (int k = 0; k < nm; ++k) {
+    Mos1Instance mi = mos1_instance(&ctx->m_par[(size_t)k * XG_MOS1_NPARAM]);
+    if (!mi.valid) return fail(ctx, XG_ERR_ARG, "MOSFET effective channel length or width is not positive");
+    const double *mp = reinterpret_cast<const double *>(&mi.model);
+    std::vector<double> key(mp, mp + offsetof(Mos1Model, has_gate_caps) / sizeof(double));
+    auto it = model_index.find(key);
+    int id;
+    if (it == model_index.end()) {
+      id = (int)models.size();
+      model_index.emplace(key, id);
+      models.push_back(mi.model);
+    } else {
+      id = it->second;
+    }
+    m1model[k] = id;
+    m1beta[k] = mi.beta;
+    m1vbi[k] = mi.tVbi;
+    m1node[k] = ctx->m_d[k]; m1node[nm + k] = ctx->m_g[k];
+    m1node[2 * (size_t)nm + k] = ctx->m_s[k]; m1node[3 * (size_t)nm + k] = ctx->m_b[k];
+    int c = circuit_of_nodes(ctx, {ctx->m_d[k], ctx->m_g[k], ctx->m_s[k], ctx->m_b[k]});
+    m1circ[k] = c < 0 ? 0 : c;
+  }
+  std::vector<int> dnode(3 * (size_t)nd), dmodel(nd), dcirc(nd);
+  std::vector<DiodeModel> dmodels;
+  std::map<std::vector<double>, int> dindex;
+  for (int k = 0; k < nd; ++k) {
+    std::vector<double> key(&ctx->d_par[(size_t)k * XG_DIODE_NPARAM], &ctx->d_par[(size_t)(k + 1) * XG_DIODE_NPARAM]);
+    auto it = dindex.find(key);
+    int id;
+    if (it == dindex.end()) {
+      id = (int)dmodels.size();
+      dindex.emplace(key, id);
+      dmodels.push_back(diode_model(key.data()));
+    } else {
+      id = it->second;
+    }
+    dmodel[k] = id;
+    dnode[k] = ctx->d_p[k]; dnode[nd + k] = ctx->d_n[k]; dnode[2 * (size_t)nd + k] = ctx->d_r[k];
+    int c = circuit_of_nodes(ctx, {ctx->d_p[k], ctx->d_n[k], ctx->d_r[k]});
+    dcirc[k] = c < 0 ? 0 : c;
+  }
+  ctx->inst_of_circ.assign(ctx->ncirc, 0);
+  for (int k = 0; k < nm; ++k) ctx->inst_of_circ[m1circ[k]]++;
+  for (int k = 0; k < nd; ++k) ctx->inst_of_circ[dcirc[k]]++;
+  // row blocks x circuits partial slots
+  const int nblocks = (n + kRowBlock - 1) / kRowBlock;
+  std::vector<int> pair_base(nblocks + 1), blk_cfirst(nblocks), pair_cstart(ctx->ncirc + 1, 0);
+  int pairs = 0;
+  std::vector<int> pair_circ;
+  for (int b = 0; b < nblocks; ++b) {
+    int r0 = b * kRowBlock, r1 = std::min(n, r0 + kRowBlock);
+    int c0 = ctx->circ_of_row[r0], c1 = ctx->circ_of_row[r1 - 1];
+    blk_cfirst[b] = c0;
+    pair_base[b] = pairs;
+    for (int c = c0; c <= c1; ++c) pair_circ.push_back(c);
+    pairs += c1 - c0 + 1;
+  }
+  pair_base[nblocks] = pairs;
+  // pairs are ordered by block then circuit, hence by circuit too
+  for (int p = 0; p < pairs; ++p) pair_cstart[pair_circ[p] + 1]++;
+  for (int c = 0; c < ctx->ncirc; ++c) pair_cstart[c + 1] += pair_cstart[c];
+  ctx->n_pairs = pairs;
+  ctx->n_rowblocks = nblocks;
+  // state layout (SoA): store = diode [vd qd cd] then MOSFET [vbd vbs vgs vds von gm]; state = MOSFET 8 planes
+  ctx->sto_base_m = 3 * nd;
+  ctx->nsto = 3 * nd + 6 * nm;
+  ctx->nsta = 8 * nm;
+  // upload
+  DevArrays &d = ctx->d;
+  auto &A = ctx->allocs;
+  int rc = 0;
+#define UP(ptr, vec) if ((rc = dev_upload(ctx, &ptr, vec, A))) return rc
+#define AL(ptr, cnt) if ((rc = dev_alloc(ctx, &ptr, cnt, A))) return rc
+  UP(d.circ_of_row, ctx->circ_of_row);
+  UP(d.offsets, ctx->offsets);
+  AL(d.cs, ctx->ncirc);
+  AL(d.tp, 1);
+  UP(d.rp, ctx->rp); UP(d.ci, ctx->ci); UP(d.erow, erow);
+  UP(d.Glin, Glin); UP(d.Clin, Clin);
+  UP(d.vF_ptr, pF); UP(d.vF_idx, iF); UP(d.vQ_ptr, pQ); UP(d.vQ_idx, iQ);
+  UP(d.vL_ptr, pL); UP(d.vL_idx, iL); UP(d.vB_ptr, pB); UP(d.vB_idx, iB);
+  UP(d.m_ptr, pM); UP(d.m_idx, iM);
+  AL(d.sF, nF); AL(d.sQ, nQ); AL(d.sL, nL); AL(d.sL2, nL); AL(d.sB, nB); AL(d.sM, nMs); AL(d.sM2, nMs);
+  UP(d.src_kind, skind); UP(d.src_off, soff); UP(d.src_circ, scirc); UP(d.src_data, sdata);
+  UP(d.m1_node, m1node); UP(d.m1_model, m1model); UP(d.m1_circ, m1circ);
+  UP(d.m1_beta, m1beta); UP(d.m1_vbi, m1vbi); UP(d.m1_models, models);
+  UP(d.d_node, dnode); UP(d.d_model, dmodel); UP(d.d_circ, dcirc); UP(d.d_models, dmodels);
+  AL(d.sta_curr, ctx->nsta); AL(d.sta_next, ctx->nsta); AL(d.sto_curr, ctx->nsto); AL(d.sto_next, ctx->nsto);
+  for (double **v : {&d.x, &d.xcurr, &d.xn0, &d.dx, &d.rhs, &d.Qv, &d.FmB, &d.Fv, &d.Bv, &d.qh0, &d.qh1,
+                     &d.qh2, &d.xh1, &d.xh2, &d.Qc, &d.FmBc, &d.solwt})
+    AL(*v, n);
+  AL(d.J, nnz);
+  UP(d.pair_base, pair_base); UP(d.blk_cfirst, blk_cfirst); UP(d.pair_cstart, pair_cstart);
+  AL(d.pmax, pairs); AL(d.psum, pairs);
+  AL(d.probe_idx, n);
+  AL(ctx->breakdown_dev, 1);
+  d.status = ctx->status_dev;
+#undef UP
+#undef AL
+  CK(cudaMemsetAsync(d.probe_idx, 0xff, sizeof(int) * n, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->finalized = true;
+  return XG_OK;
+}
+
+int xg_get_sizes(xg_ctx *ctx, int *n, int *nnz, int *nsta, int *nsto) {
+  if (!ctx) return XG_ERR_ARG;
+  if (!ctx->finalized) return fail(ctx, XG_ERR_STATE, "not finalized");
+  if (n) *n = ctx->n;
+  if (nnz) *nnz = ctx->nnz;
+  if (nsta) *nsta = ctx->nsta;
+  if (nsto) *nsto = ctx->nsto;
+  return XG_OK;
+}
+
+int xg_get_pattern(xg_ctx *ctx, int *row_ptr, int *col_idx) {
+  if (!ctx || !row_ptr || !col_idx) return XG_ERR_ARG;
+  if (!ctx->finalized) return fail(ctx, XG_ERR_STATE, "not finalized");
+  std::copy(ctx->rp.begin(), ctx->rp.end(), row_ptr);
+  std::copy(ctx->ci.begin(), ctx->ci.end(), col_idx);
+  return XG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Loader entry points.
+int xg_update_sources(xg_ctx *ctx, double time) {
+  if (!ctx) return XG_ERR_ARG;
+  if (!ctx->finalized) return fail(ctx, XG_ERR_STATE, "not finalized");
+  launch_sources_k(ctx->stream, ctx->d, ctx->nv, ctx->nv + ctx->ni, 1, time);
+  CK(cudaGetLastError());
+  return XG_OK;
+}
+
+int xg_update_state(xg_ctx *ctx, const double *next_sol, const double *curr_sta, const double *curr_sto,
+                    double *next_sta, double *next_sto, int newton_iter, int flags) {
+  if (!ctx || !next_sol) return XG_ERR_ARG;
+  if (!ctx->finalized) return fail(ctx, XG_ERR_STATE, "not finalized");
+  if ((ctx->nsta > 0 && (!curr_sta || !next_sta)) || (ctx->nsto > 0 && (!curr_sto || !next_sto)))
+    return fail(ctx, XG_ERR_ARG, "state/store vectors are required");
+  DevArrays d = ctx->d;
+  d.x = const_cast<double *>(next_sol);
+  d.sta_curr = const_cast<double *>(curr_sta);
+  d.sta_next = next_sta;
+  d.sto_curr = const_cast<double *>(curr_sto);
+  d.sto_next = next_sto;
+  launch_mos1_k(ctx->stream, d, ctx->nm, ctx->sto_base_m, 0, 0, newton_iter, flags, ctx->sF_m, ctx->sQ_m,
+                ctx->sL_m, ctx->sM_m);
+  launch_diode_k(ctx->stream, d, ctx->nd, 0, 0, newton_iter, flags, ctx->sF_d, ctx->sQ_d, ctx->sL_d, ctx->sM_d);
+  CK(cudaGetLastError());
+  return XG_OK;
+}
+
+int xg_load_dae_vectors(xg_ctx *ctx, const double *next_sol, double *Q, double *F, double *B, double *dFdxdVp,
+                        double *dQdxdVp, int load_type) {
+  if (!ctx || !next_sol || !Q || !F || !B || !dFdxdVp || !dQdxdVp) return XG_ERR_ARG;
+  if (!ctx->finalized) return fail(ctx, XG_ERR_STATE, "not finalized");
+  if (load_type < 0 || load_type > 2) return fail(ctx, XG_ERR_ARG, "bad load type");
+  launch_load_vectors_k(ctx->stream, ctx->d, ctx->n, next_sol, Q, F, B, dFdxdVp, dQdxdVp, load_type);
+  CK(cudaGetLastError());
+  return XG_OK;
+}
+
+int xg_load_dae_matrices(xg_ctx *ctx, double *dQdx, double *dFdx, int load_type) {
+  if (!ctx || !dQdx || !dFdx) return XG_ERR_ARG;
+  if (!ctx->finalized) return fail(ctx, XG_ERR_STATE, "not finalized");
+  if (load_type < 0 || load_type > 2) return fail(ctx, XG_ERR_ARG, "bad load type");
+  launch_load_matrices_k(ctx->stream, ctx->d, ctx->nnz, dQdx, dFdx, load_type);
+  CK(cudaGetLastError());
+  return XG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// LU entry points.
+static int lu_upload(xg_ctx *ctx, const LUHost &H) {
+  CK(cudaStreamSynchronize(ctx->stream));
+  free_list(ctx->lu_allocs);
+  LUDev &L = ctx->L;
+  L = LUDev();
+  L.n = H.n;
+  L.nnz = (long long)H.ri.size();
+  auto &A = ctx->lu_allocs;
+  int rc = 0;
+#define UP(ptr, vec) if ((rc = dev_upload(ctx, &ptr, vec, A))) return rc
+  UP(L.row_of_step, H.row_of_step); UP(L.col_of_step, H.col_of_step);
+  std::vector<int> cstep(H.n);
+  for (int p = 0; p < H.n; ++p) cstep[p] = ctx->circ_of_row[H.col_of_step[p]];
+  UP(L.circ_of_step, cstep);
+  UP(L.cp, H.cp); UP(L.ri, H.ri); UP(L.diag, H.diag); UP(L.src, H.src);
+  UP(L.f_lvl_ptr, H.f_lvl_ptr); UP(L.f_cols, H.f_cols);
+  UP(L.l_lvl_ptr, H.l_lvl_ptr); UP(L.l_rows, H.l_rows); UP(L.l_ptr, H.l_ptr); UP(L.l_pos, H.l_pos); UP(L.l_col, H.l_col);
+  UP(L.u_lvl_ptr, H.u_lvl_ptr); UP(L.u_rows, H.u_rows); UP(L.u_ptr, H.u_ptr); UP(L.u_pos, H.u_pos); UP(L.u_col, H.u_col);
+  UP(L.exempt, H.exempt);
+#undef UP
+  if ((rc = dev_alloc(ctx, &L.lu, (size_t)L.nnz, A))) return rc;
+  if ((rc = dev_alloc(ctx, &L.y, (size_t)H.n, A))) return rc;
+  L.breakdown = ctx->breakdown_dev;
+  L.h_f_lvl = H.f_lvl_ptr;
+  L.h_l_lvl = H.l_lvl_ptr;
+  L.h_u_lvl = H.u_lvl_ptr;
+  CK(cudaMemsetAsync(ctx->breakdown_dev, 0, sizeof(int), ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->lu_ready = true;
+  ctx->n_analyze++;
+  return XG_OK;
+}
+
+static int lu_analyze_from_device(xg_ctx *ctx, const double *vals_dev) {
+  std::vector<double> v(ctx->nnz);
+  CK(cudaMemcpyAsync(v.data(), vals_dev, sizeof(double) * ctx->nnz, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  LUHost H;
+  std::string err;
+  int rc = lu_analyze_host(ctx->n, ctx->rp, ctx->ci, v, H, err);
+  if (rc) return fail(ctx, rc, "LU analysis: " + err);
+  return lu_upload(ctx, H);
+}
+
+int xg_lu_analyze(xg_ctx *ctx, const double *vals) {
+  if (!ctx || !vals) return XG_ERR_ARG;
+  if (!ctx->finalized) return fail(ctx, XG_ERR_STATE, "not finalized");
+  return lu_analyze_from_device(ctx, vals);
+}
+
+int xg_lu_factor(xg_ctx *ctx, const double *vals) {
+  if (!ctx || !vals) return XG_ERR_ARG;
+  if (!ctx->lu_ready) return fail(ctx, XG_ERR_STATE, "call xg_lu_analyze first");
+  CK(cudaMemsetAsync(ctx->breakdown_dev, 0, sizeof(int), ctx->stream));
+  launch_lu_factor_k(ctx->stream, ctx->L, vals, ctx->d.cs, 0, 1e-3);
+  CK(cudaGetLastError());
+  int bd = 0;
+  CK(cudaMemcpyAsync(&bd, ctx->breakdown_dev, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (bd) {
+    char buf[96];
+    snprintf(buf, sizeof buf, "pivot breakdown at step %d: re-run xg_lu_analyze", bd - 1);
+    return fail(ctx, XG_ERR_SINGULAR, buf);
+  }
+  return XG_OK;
+}
+
+int xg_lu_solve(xg_ctx *ctx, const double *rhs, double *x) {
+  if (!ctx || !rhs || !x) return XG_ERR_ARG;
+  if (!ctx->lu_ready) return fail(ctx, XG_ERR_STATE, "call xg_lu_analyze first");
+  launch_lu_solve_k(ctx->stream, ctx->L, rhs, x, ctx->d.cs, 0);
+  CK(cudaGetLastError());
+  return XG_OK;
+}
+
+int xg_lu_info(xg_ctx *ctx, long long *nnz_lu, int *fl, int *ll, int *ul) {
+  if (!ctx) return XG_ERR_ARG;
+  if (!ctx->lu_ready) return fail(ctx, XG_ERR_STATE, "no LU analysis");
+  if (nnz_lu) *nnz_lu = ctx->L.nnz;
+  if (fl) *fl = (int)ctx->L.h_f_lvl.size() - 1;
+  if (ll) *ll = (int)ctx->L.h_l_lvl.size() - 1;
+  if (ul) *ul = (int)ctx->L.h_u_lvl.size() - 1;
+  return XG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Device-resident transient driver.
+namespace {
+
+struct Run {
+  xg_ctx *ctx;
+  int cap, pmax;
+  double *bps = nullptr;
+  int *bp_ptr = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  double pivot_tol = 1e-3;
+  std::vector<void *> allocs;
+  ~Run() {
+    if (exec) cudaGraphExecDestroy(exec);
+    free_list(allocs);
+  }
+};
+
+void launch_front(Run &R) {
+  xg_ctx *c = R.ctx;
+  DevArrays &d = c->d;
+  launch_sources_k(c->stream, d, c->nv, c->nv + c->ni, 0, 0.0);
+  launch_mos1_k(c->stream, d, c->nm, c->sto_base_m, 1, 1, 0, 0, c->sF_m, c->sQ_m, c->sL_m, c->sM_m);
+  launch_diode_k(c->stream, d, c->nd, 1, 1, 0, 0, c->sF_d, c->sQ_d, c->sL_d, c->sM_d);
+  launch_assemble_k(c->stream, d, c->n, c->nnz);
+  launch_newton_ctl_k(c->stream, d, c->ncirc);
+}
+
+void launch_back(Run &R) {
+  xg_ctx *c = R.ctx;
+  DevArrays &d = c->d;
+  launch_lu_factor_k(c->stream, c->L, d.J, d.cs, 1, R.pivot_tol);
+  launch_lu_solve_k(c->stream, c->L, d.rhs, d.dx, d.cs, 1);
+  launch_update_k(c->stream, d, c->n);
+  launch_step_ctl_k(c->stream, d, c->ncirc, R.bps, R.bp_ptr, R.cap);
+  launch_history_k(c->stream, d, c->n, R.cap, R.pmax);
+  launch_state_commit_k(c->stream, d, c->nm, c->nd, c->sto_base_m);
+}
+
+int capture(Run &R) {
+  xg_ctx *ctx = R.ctx;
+  if (R.exec) { cudaGraphExecDestroy(R.exec); R.exec = nullptr; }
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  launch_front(R);
+  launch_back(R);
+  launch_count_done_k(ctx->stream, ctx->d, ctx->ncirc, ctx->breakdown_dev, ctx->status_dev);
+  CK(cudaStreamEndCapture(ctx->stream, &g));
+  cudaError_t e = cudaGraphInstantiate(&R.exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(ctx, XG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  return XG_OK;
+}
+
+// Source breakpoints of one circuit (PulseData/PWLinData::getBreakPoints,
+// N_DEV_SourceData.C:1442, 2044) plus tstop.
+void breakpoints(const Wave &w, double tstop, std::vector<double> &bp) {
+  const auto &d = w.d;
+  if (w.kind == XG_WAVE_PWL) {
+    for (size_t i = 0; i + 1 < d.size(); i += 2)
+      if (d[i] > 0 && d[i] < tstop) bp.push_back(d[i]);
+  } else if (w.kind == XG_WAVE_PULSE) {
+    double base = d[2];
+    for (int k = 0; k < 100000 && base < tstop; ++k) {
+      double cand[4] = {base, base + d[3], base + d[3] + d[5], base + d[3] + d[5] + d[4]};
+      for (double x : cand)
+        if (x > 0 && x < tstop) bp.push_back(x);
+      if (d[6] <= 0) break;
+      base += d[6];
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" int xg_transient(xg_ctx *ctx, const xg_tran_params *p, int n_probe, const int *probes, int cap,
+                            int *counts, double *times, double *values, xg_tran_stats *stats) {
+  if (!ctx || !p) return XG_ERR_ARG;
+  if (!ctx->finalized) return fail(ctx, XG_ERR_STATE, "not finalized");
+  if (!(p->tstop > p->tstart)) return fail(ctx, XG_ERR_ARG, "tstop must exceed tstart");
+  if (cap < 0 || n_probe < 0) return fail(ctx, XG_ERR_ARG, "negative cap or probe count");
+  if (cap > 0 && (!counts || !times || (n_probe > 0 && !values))) return fail(ctx, XG_ERR_ARG, "output buffers required");
+  CK(cudaSetDevice(ctx->device));
+  auto t0 = std::chrono::steady_clock::now();
+  const int n = ctx->n, ncirc = ctx->ncirc;
+  DevArrays &d = ctx->d;
+  Run R;
+  R.ctx = ctx;
+  R.cap = cap;
+  // probes grouped by circuit
+  std::vector<int> probe_idx(n, -1), pcount(ncirc, 0);
+  for (int k = 0; k < n_probe; ++k) {
+    if (probes[k] < 0 || probes[k] >= n) return fail(ctx, XG_ERR_ARG, "probe out of range");
+    int c = ctx->circ_of_row[probes[k]];
+    probe_idx[probes[k]] = pcount[c]++;
+  }
+  R.pmax = 1;
+  for (int c = 0; c < ncirc; ++c) R.pmax = std::max(R.pmax, pcount[c]);
+  CK(cudaMemcpyAsync(d.probe_idx, probe_idx.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+  int rc = 0;
+  if ((rc = dev_alloc(ctx, &d.out_t, (size_t)ncirc * std::max(cap, 1), R.allocs))) return rc;
+  if ((rc = dev_alloc(ctx, &d.out_v, (size_t)ncirc * std::max(cap, 1) * R.pmax, R.allocs))) return rc;
+  // breakpoints per circuit
+  std::vector<std::vector<double>> cb(ncirc);
+  for (int k = 0; k < ctx->nv; ++k) breakpoints(ctx->v_w[k], p->tstop, cb[ctx->circ_of_row[ctx->v_b[k]]]);
+  for (int k = 0; k < ctx->ni; ++k) {
+    int c = circuit_of_nodes(ctx, {ctx->i_p[k], ctx->i_n[k]});
+    breakpoints(ctx->i_w[k], p->tstop, cb[c < 0 ? 0 : c]);
+  }
+  std::vector<double> bps;
+  std::vector<int> bp_ptr(1, 0);
+  for (int c = 0; c < ncirc; ++c) {
+    auto &v = cb[c];
+    v.push_back(p->tstop);
+    std::sort(v.begin(), v.end());
+    bps.insert(bps.end(), v.begin(), v.end());
+    bp_ptr.push_back((int)bps.size());
+  }
+  if ((rc = dev_upload(ctx, &R.bps, bps, R.allocs))) return rc;
+  if ((rc = dev_upload(ctx, &R.bp_ptr, bp_ptr, R.allocs))) return rc;
+  // parameters
+  TranParams tp{};
+  tp.tstart = p->tstart; tp.tstop = p->tstop;
+  tp.hmax = p->hmax > 0 ? p->hmax : 0.1 * (p->tstop - p->tstart);
+  tp.hmin = p->hmin;
+  tp.reltol = p->reltol; tp.abstol = p->abstol;
+  tp.nl_reltol = p->nl_reltol; tp.nl_abstol = p->nl_abstol; tp.nl_deltaxtol = p->nl_deltaxtol;
+  tp.nl_rhstol = p->nl_rhstol; tp.nl_smallupdatetol = p->nl_smallupdatetol; tp.nl_maxstep = p->nl_maxstep;
+  tp.max_steps = p->max_steps; tp.max_order = p->max_order > 0 ? p->max_order : 2;
+  tp.bptol = 1e-15 * (p->tstop - p->tstart);
+  tp.dc_reltol = 1e-3; tp.dc_abstol = 1e-12; tp.dc_deltaxtol = 1.0; tp.dc_rhstol = 1e-6; tp.dc_maxstep = 200;
+  tp.dc_only = (p->max_steps < 0) ? 1 : 0;
+  CK(cudaMemcpyAsync(d.tp, &tp, sizeof tp, cudaMemcpyHostToDevice, ctx->stream));
+  // circuit states: operating point first
+  std::vector<CircState> cs(ncirc);
+  for (auto &s : cs) {
+    memset(&s, 0, sizeof s);
+    s.phase = PH_DC;
+    s.tn = p->tstart;
+    s.t = p->tstart;
+    s.qscale = 0.0; s.fscale = 1.0; s.hscale = 0.0;
+    s.init_jct = 1;
+    s.order = 1;
+  }
+  CK(cudaMemcpyAsync(d.cs, cs.data(), sizeof(CircState) * ncirc, cudaMemcpyHostToDevice, ctx->stream));
+  for (double *v : {d.x, d.xcurr, d.xn0, d.dx, d.rhs, d.Qv, d.FmB, d.qh0, d.qh1, d.qh2, d.xh1, d.xh2, d.Qc, d.FmBc, d.solwt})
+    CK(cudaMemsetAsync(v, 0, sizeof(double) * n, ctx->stream));
+  for (double *v : {d.sta_curr, d.sta_next})
+    CK(cudaMemsetAsync(v, 0, sizeof(double) * std::max(1, ctx->nsta), ctx->stream));
+  for (double *v : {d.sto_curr, d.sto_next})
+    CK(cudaMemsetAsync(v, 0, sizeof(double) * std::max(1, ctx->nsto), ctx->stream));
+  CK(cudaMemsetAsync(ctx->breakdown_dev, 0, sizeof(int), ctx->stream));
+  ctx->status_host[0] = ctx->status_host[1] = 0;
+  // first tick: evaluate and assemble, then analyze the Jacobian, then finish the tick
+  long long ticks = 1;
+  launch_front(R);
+  CK(cudaGetLastError());
+  if ((rc = lu_analyze_from_device(ctx, d.J))) return rc;
+  if ((rc = capture(R))) return rc;
+  launch_back(R);
+  launch_count_done_k(ctx->stream, d, ncirc, ctx->breakdown_dev, ctx->status_dev);
+  CK(cudaGetLastError());
+  int batch = 4;
+  const long long max_ticks = 200000000LL;
+  int consecutive_reanalysis = 0;
+  while (true) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    volatile int *st = ctx->status_host;
+    const int finished = st[0], breakdown = st[1];
+    if (breakdown) {
+      // frozen pivots failed: re-pivot from the parked Jacobian and resume
+      consecutive_reanalysis++;
+      if (consecutive_reanalysis > 4) return fail(ctx, XG_ERR_SINGULAR, "LU keeps breaking down after re-pivoting");
+      if ((rc = lu_analyze_from_device(ctx, d.J))) return rc;
+      R.pivot_tol = (consecutive_reanalysis >= 2) ? 0.0 : 1e-3;
+      if ((rc = capture(R))) return rc;
+      launch_unstall_k(ctx->stream, d, ncirc);
+      launch_back(R);
+      launch_count_done_k(ctx->stream, d, ncirc, ctx->breakdown_dev, ctx->status_dev);
+      CK(cudaGetLastError());
+      continue;
+    }
+    if (consecutive_reanalysis && R.pivot_tol == 0.0) {
+      R.pivot_tol = 1e-3;
+      if ((rc = capture(R))) return rc;
+    }
+    consecutive_reanalysis = 0;
+    if (finished >= ncirc) break;
+    if (ticks > max_ticks) return fail(ctx, XG_ERR_TIMEOUT, "transient exceeded the tick limit");
+    for (int k = 0; k < batch; ++k) CK(cudaGraphLaunch(R.exec, ctx->stream));
+    ticks += batch;
+    if (batch < 64) batch *= 2;
+  }
+  // results
+  std::vector<CircState> out(ncirc);
+  CK(cudaMemcpyAsync(out.data(), d.cs, sizeof(CircState) * ncirc, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (cap > 0) {
+    std::vector<double> ot((size_t)ncirc * cap), ov((size_t)ncirc * cap * R.pmax);
+    CK(cudaMemcpy(ot.data(), d.out_t, sizeof(double) * ot.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ov.data(), d.out_v, sizeof(double) * ov.size(), cudaMemcpyDeviceToHost));
+    for (int c = 0; c < ncirc; ++c) counts[c] = std::min(out[c].n_out, cap);
+    memcpy(times, ot.data(), sizeof(double) * ot.size());
+    if (n_probe > 0) memcpy(values, ov.data(), sizeof(double) * ov.size());
+  }
+  int status = 0;
+  if (stats) {
+    memset(stats, 0, sizeof *stats);
+    stats->t_final_min = 1e300;
+    stats->t_final_max = -1e300;
+    for (auto &s : out) {
+      stats->accepted += s.accepted;
+      stats->rejected += s.rejected;
+      stats->newton_iters += s.newton_iters;
+      stats->newton_fail += s.newton_fail;
+      stats->lte_fail += s.lte_fail;
+      stats->dcop_iters += s.dcop_iters;
+      stats->t_final_min = std::min(stats->t_final_min, s.t);
+      stats->t_final_max = std::max(stats->t_final_max, s.t);
+    }
+    stats->ticks = ticks;
+    stats->device_evals = 0;
+    stats->n_analyze = ctx->n_analyze;
+  }
+  for (auto &s : out)
+    if (s.phase == PH_FAILED) { status = s.newton_status ? s.newton_status : -1; break; }
+  if (stats) {
+    stats->status = status;
+    // instance evaluations: every Newton solve is followed by one device pass,
+    // and every step attempt / operating-point solve starts with one
+    long long evals = 0;
+    for (int c = 0; c < ncirc; ++c) {
+      const CircState &s = out[c];
+      const long long passes = s.newton_iters + s.accepted + s.rejected + s.dcop_iters + 1;
+      evals += (long long)ctx->inst_of_circ[c] * passes;
+    }
+    stats->device_evals = evals;
+    stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  d.out_t = nullptr;
+  d.out_v = nullptr;
+  if (status) return fail(ctx, status, "a circuit failed to converge");
+  return XG_OK;
+}
+
+extern "C" int xg_dcop(xg_ctx *ctx, double *x_host, int *iters) {
+  if (!ctx || !x_host) return XG_ERR_ARG;
+  xg_tran_params p{};
+  p.tstart = 0.0; p.tstop = 1.0; p.hmax = 0.1;
+  p.reltol = 1e-3; p.abstol = 1e-6;
+  p.nl_reltol = 1e-2; p.nl_abstol = 1e-6; p.nl_deltaxtol = 0.33; p.nl_rhstol = 1e-2; p.nl_smallupdatetol = 1e-6;
+  p.nl_maxstep = 20; p.max_steps = -1; p.max_order = 2;
+  xg_tran_stats st;
+  int rc = xg_transient(ctx, &p, 0, nullptr, 0, nullptr, nullptr, nullptr, &st);
+  if (iters) *iters = (int)st.dcop_iters;
+  if (rc) return rc;
+  CK(cudaMemcpy(x_host, ctx->d.xcurr, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost));
+  return XG_OK;
+}

@@ -1,0 +1,180 @@
+// xg_internal.h — shared host/device declarations of the GB300 hot path.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/xyce_gb300.h"
+
+namespace xg {
+
+constexpr int kRowBlock = 256;       // rows per block of the row kernels (fixed: partial slots)
+constexpr int kMaxPwlScan = 1 << 20; // bound on PWL point scans
+
+// Circuit phases of the device-resident state machine.
+enum Phase : int { PH_DC = 0, PH_TRAN = 1, PH_DONE = 2, PH_FAILED = 3, PH_STALL = 4 };
+
+// Per-circuit integrator / Newton state, one struct per circuit in HBM.
+// Field names follow StepErrorControl / OneStep / DampedNewton members.
+struct CircState {
+  // time integration (StepErrorControl, OneStep)
+  double t;            // currentTime (last accepted)
+  double h;            // currentTimeStep
+  double tn;           // time of the step being attempted
+  double stopTime;     // next breakpoint or tstop
+  double lastTimeStep, tsum, saved, estOverTol;
+  double psi[3], beta[3], ck;
+  double qscale, fscale, hscale;   // residual/Jacobian coefficients of this attempt
+  double errwt;        // reltol*max|x_curr| + abstol (NEWLTE = 1)
+  double xmax_curr;    // max |x_curr|
+  double gshunt;       // operating-point gmin stepping shunt
+  // Newton (DampedNewton)
+  double normRHS, normRHS_init, normRHS_old, maxNormRHS, wtNormDX, tmpConvRate;
+  double wrms_sum;
+  int phase, iter, order, numberOfSteps, nef, stepNumber;
+  int beginning, lastOk, count, newton_status;
+  int need_solve;      // this tick factors/solves/updates
+  int step_end;        // 1 = Newton finished this tick (converged or failed)
+  int accept;          // 1 accepted / 0 rejected (valid when step_end)
+  int start_step;      // 1 = next tick begins a new step attempt (predictor applied)
+  int init_jct, init_hist, dc_stage, limited, bp_index, singular, stall_prev;
+  // counters
+  long long accepted, rejected, newton_iters, newton_fail, lte_fail, dcop_iters;
+  int n_out;
+};
+
+struct TranParams {
+  double tstart, tstop, hmax, hmin, reltol, abstol;
+  double nl_reltol, nl_abstol, nl_deltaxtol, nl_rhstol, nl_smallupdatetol;
+  int nl_maxstep, max_steps, max_order;
+  double bptol;
+  // operating-point options (N_NLS_Manager.C:1030-1052)
+  double dc_reltol, dc_abstol, dc_deltaxtol, dc_rhstol;
+  int dc_maxstep;
+  int dc_only;  // stop every circuit once its operating point converges
+};
+
+// MOSFET level-1 model-level (effective model) parameters after temperature
+// and geometry processing (N_DEV_MOSFET1.C:383-470, 3487-3730, 3939-4020).
+struct Mos1Model {
+  double dtype, gamma, tPhi, lambda, vt, DrainSatCur, SourceSatCur, sourceVcrit, drainVcrit;
+  double OxideCap, Cgso, Cgdo, Cgbo, Cbd, Cbdsw, Cbs, Cbssw, tDepCap, tBulkPot, MJ, MJSW;
+  double f2d, f3d, f4d, f2s, f3s, f4s, M, gammaSqrtPhi;
+  int has_gate_caps, has_junc_caps;
+};
+
+// Diode model-level parameters after temperature processing (N_DEV_Diode.C:2040-2237).
+struct DiodeModel {
+  double Isat, IsatR, Vte, VteR, VteBRK, Gspr, tVcrit, tIKF, tJctPot, tJctCap, tDepCap;
+  double tF1, F2, F3, M, TT, tBrkdwnV;
+  int bvGiven;
+};
+
+// Slot counts per instance.
+constexpr int kMosF = 3, kMosQ = 4, kMosL = 4, kMosM = 16;
+constexpr int kDioF = 3, kDioQ = 2, kDioL = 2, kDioM = 7;
+
+// Device-resident arrays (all cudaMalloc'd, owned by the context).
+struct DevArrays {
+  // circuits
+  int *circ_of_row = nullptr;
+  int *offsets = nullptr;
+  CircState *cs = nullptr;
+  TranParams *tp = nullptr;
+  // linear part (CSR order) and pattern
+  int *rp = nullptr, *ci = nullptr, *erow = nullptr, *diag = nullptr;
+  double *Glin = nullptr, *Clin = nullptr;
+  // contribution lists: per row for vector slots, per CSR entry for matrix slots
+  int *vF_ptr = nullptr, *vF_idx = nullptr;
+  int *vQ_ptr = nullptr, *vQ_idx = nullptr;
+  int *vL_ptr = nullptr, *vL_idx = nullptr;
+  int *vB_ptr = nullptr, *vB_idx = nullptr;
+  int *m_ptr = nullptr, *m_idx = nullptr;
+  // slot value buffers
+  double *sF = nullptr, *sQ = nullptr, *sL = nullptr, *sL2 = nullptr, *sB = nullptr;
+  double *sM = nullptr, *sM2 = nullptr;   // combined J slots / (dF, dQ) in separate mode
+  // sources
+  int *src_kind = nullptr, *src_off = nullptr, *src_circ = nullptr;
+  double *src_data = nullptr;
+  // MOSFET-1 SoA
+  int *m1_node = nullptr;   // 4*n: D,G,S,B planes
+  int *m1_model = nullptr, *m1_circ = nullptr;
+  double *m1_beta = nullptr, *m1_vbi = nullptr;
+  Mos1Model *m1_models = nullptr;
+  // diode SoA
+  int *d_node = nullptr;    // 3*n: P,N,R planes
+  int *d_model = nullptr, *d_circ = nullptr;
+  DiodeModel *d_models = nullptr;
+  // state / store (curr = accepted, next = iterate)
+  double *sta_curr = nullptr, *sta_next = nullptr, *sto_curr = nullptr, *sto_next = nullptr;
+  // vectors (length n)
+  double *x = nullptr, *xcurr = nullptr, *xn0 = nullptr, *dx = nullptr, *rhs = nullptr;
+  double *Qv = nullptr, *FmB = nullptr, *Fv = nullptr, *Bv = nullptr;
+  double *qh0 = nullptr, *qh1 = nullptr, *qh2 = nullptr, *xh1 = nullptr, *xh2 = nullptr;
+  double *Qc = nullptr, *FmBc = nullptr, *solwt = nullptr;
+  double *J = nullptr;      // Jacobian values (CSR order)
+  // per-(block,circuit) partial reduction slots
+  int *pair_base = nullptr, *blk_cfirst = nullptr, *pair_cstart = nullptr;
+  double *pmax = nullptr, *psum = nullptr;
+  // recording
+  int *probe_idx = nullptr, *probe_ptr = nullptr;
+  double *out_t = nullptr, *out_v = nullptr;
+  int *status = nullptr;      // mapped host memory: [0] finished circuits, [1] LU breakdown
+};
+
+// LU structures (device) produced by the host analysis.
+struct LUDev {
+  int n = 0;
+  long long nnz = 0;
+  int *row_of_step = nullptr, *col_of_step = nullptr, *circ_of_step = nullptr;
+  int *cp = nullptr, *ri = nullptr, *diag = nullptr, *src = nullptr;
+  double *lu = nullptr, *y = nullptr;
+  int *f_lvl_ptr = nullptr, *f_cols = nullptr;
+  int *l_lvl_ptr = nullptr, *l_rows = nullptr, *l_ptr = nullptr, *l_pos = nullptr, *l_col = nullptr;
+  int *u_lvl_ptr = nullptr, *u_rows = nullptr, *u_ptr = nullptr, *u_pos = nullptr, *u_col = nullptr;
+  char *exempt = nullptr;    // per step: skip the threshold test
+  int *breakdown = nullptr;  // device flag: first failing step + 1
+  std::vector<int> h_f_lvl, h_l_lvl, h_u_lvl;  // host copies of the level pointers
+};
+
+// Host-side analysis result.
+struct LUHost {
+  int n = 0;
+  std::vector<int> row_of_step, col_of_step, cp, ri, diag, src;
+  std::vector<int> f_lvl_ptr, f_cols, l_lvl_ptr, l_rows, l_ptr, l_pos, l_col;
+  std::vector<int> u_lvl_ptr, u_rows, u_ptr, u_pos, u_col;
+  std::vector<char> exempt;  // columns exempt from the pivot threshold test
+};
+
+// Analysis entry (xg_symbolic.cpp): CSR pattern + values -> LUHost.
+int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &ci,
+                    const std::vector<double> &vals, LUHost &out, std::string &err);
+
+// Kernel launchers (xg_kernels.cu, xg_lu.cu).
+void launch_sources_k(cudaStream_t st, const DevArrays &d, int n_v, int n_src, int use_explicit, double t);
+void launch_mos1_k(cudaStream_t st, const DevArrays &d, int nm, int sto_base, int combined, int masked,
+                   int it, int flags, int sF, int sQ, int sL, int sM);
+void launch_diode_k(cudaStream_t st, const DevArrays &d, int nd, int combined, int masked, int it,
+                    int flags, int sF, int sQ, int sL, int sM);
+void launch_assemble_k(cudaStream_t st, const DevArrays &d, int n, int nnz);
+void launch_load_vectors_k(cudaStream_t st, const DevArrays &d, int n, const double *x, double *Q,
+                           double *F, double *B, double *dFv, double *dQv, int lt);
+void launch_load_matrices_k(cudaStream_t st, const DevArrays &d, int nnz, double *dQdx, double *dFdx,
+                            int lt);
+void launch_newton_ctl_k(cudaStream_t st, const DevArrays &d, int ncirc);
+void launch_update_k(cudaStream_t st, const DevArrays &d, int n);
+void launch_step_ctl_k(cudaStream_t st, const DevArrays &d, int ncirc, const double *bps,
+                       const int *bp_ptr, int cap);
+void launch_history_k(cudaStream_t st, const DevArrays &d, int n, int cap, int pmax);
+void launch_state_commit_k(cudaStream_t st, const DevArrays &d, int nm, int nd, int sto_base_m);
+void launch_count_done_k(cudaStream_t st, const DevArrays &d, int ncirc, const int *breakdown,
+                         int *status_out);
+void launch_unstall_k(cudaStream_t st, const DevArrays &d, int ncirc);
+void launch_lu_factor_k(cudaStream_t st, const LUDev &L, const double *vals, CircState *cs, int masked,
+                        double pivot_tol);
+void launch_lu_solve_k(cudaStream_t st, const LUDev &L, const double *b, double *x, const CircState *cs,
+                       int masked);
+
+}  // namespace xg

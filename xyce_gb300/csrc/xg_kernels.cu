@@ -1,0 +1,1035 @@
+// xg_kernels.cu — sm_103a kernels of the transient Newton hot path.
+//
+// Data flow of one Newton iteration ("tick"), every circuit of a batch at once:
+//   k_sources        source values at each circuit's attempt time      (SourceData::updateSource)
+//   k_mos1, k_diode  device evaluation, one thread per instance, SoA;   (Master::updateState +
+//                    writes store/state and per-instance stamp slots     loadDAEVectors/Matrices)
+//   k_assemble_rows  gather-sum of the vector slots per row (atomic-free), linear part as a
+//                    CSR SpMV, residual of the integration method, per-circuit partial norms
+//                                                                       (OneStep::obtainResidual)
+//   k_assemble_J     gather-sum of the matrix slots per CSR entry       (OneStep::obtainJacobian)
+//   k_newton_ctl     per-circuit DampedNewton::converged_ decision
+//   LU factor/solve  level-scheduled, frozen pivots (xg_lu.cu)
+//   k_update         x += dx, weighted update norm, LTE sums
+//   k_step_ctl       per-circuit accept/reject and next step (StepErrorControl, OneStep)
+//   k_history        OneStep::updateHistory, initialize, obtainPredictor
+//   k_state_commit   accepted store/state become current
+#include <cuda_runtime.h>
+
+#include "xg_internal.h"
+#include "xg_models.cuh"
+
+namespace xg {
+
+__device__ __forceinline__ bool circ_active(const CircState &s) {
+  return s.phase == PH_DC || s.phase == PH_TRAN;
+}
+
+// ---------------------------------------------------------------------------
+// Sources: SinData/PulseData/PWLinData::updateSource (N_DEV_SourceData.C:475,1168,1770)
+__device__ double wave_value_d(int kind, const double *d, int nd, double t) {
+  switch (kind) {
+    case XG_WAVE_DC: return d[0];
+    case XG_WAVE_SIN: {
+      double time = t - d[3];
+      if (time <= 0) return d[0] + d[1] * sin(2.0 * M_PI * (d[5] / 360));
+      return d[0] + d[1] * sin(2.0 * M_PI * (d[2] * time + d[5] / 360)) * exp(-(time * d[4]));
+    }
+    case XG_WAVE_PULSE: {
+      double V1 = d[0], V2 = d[1], TR = d[3], TF = d[4], PW = d[5], PER = d[6];
+      double time = t - d[2];
+      if (time > PER && PER != 0.0) time -= PER * floor(time / PER);
+      if (time <= 0 || time > TR + PW + TF) return V1;
+      if (time > TR && time < TR + PW) return V2;
+      if (time > 0 && time <= TR) return (TR != 0.0) ? V1 + (V2 - V1) * time / TR : V1;
+      if (time >= TR + PW && time <= TR + PW + TF)
+        return (TF != 0.0) ? V2 + (V1 - V2) * (time - (TR + PW)) / TF : V2;
+      return V2;
+    }
+    case XG_WAVE_PWL: {
+      int npts = nd / 2;
+      if (t < 0) return 0.0;
+      double t1, t2, v1, v2;
+      if (t <= d[2 * (npts - 1)]) {
+        int loc = npts - 1;
+        for (int i = 0; i < npts && i < kMaxPwlScan; ++i)
+          if (t < d[2 * i]) { loc = i; break; }
+        if (loc == 0) { t1 = 0.0; v1 = 0.0; }
+        else { t1 = d[2 * (loc - 1)]; v1 = d[2 * (loc - 1) + 1]; }
+        t2 = d[2 * loc]; v2 = d[2 * loc + 1];
+      } else {
+        t1 = 0.0; t2 = 1.0; v1 = v2 = d[2 * (npts - 1) + 1];
+      }
+      if (t1 == t2) return v2;
+      double length = t2 - t1;
+      return (t2 - t) * v1 / length + (-t1 + t) * v2 / length;
+    }
+  }
+  return 0.0;
+}
+
+// One thread per source; V sources own one B slot, I sources two (pos, neg).
+__global__ void k_sources(DevArrays d, int n_v, int n_src, int use_explicit, double t_explicit) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_src) return;
+  double t;
+  if (use_explicit) {
+    t = t_explicit;
+  } else {
+    const CircState &s = d.cs[d.src_circ[k]];
+    if (!circ_active(s)) return;
+    t = s.tn;
+  }
+  int o0 = d.src_off[k], o1 = d.src_off[k + 1];
+  double v = wave_value_d(d.src_kind[k], d.src_data + o0, o1 - o0, t);
+  if (k < n_v) {
+    d.sB[k] = v;
+  } else {
+    int j = n_v + 2 * (k - n_v);
+    d.sB[j] = -v;
+    d.sB[j + 1] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// MOSFET level 1, drain/source primes merged (RD = RS = 0).
+// Store planes (x nm): vbd vbs vgs vds von gm; state planes: capgs capgd capgb qgs qgd qgb qbd qbs.
+// Slots: F[D,S,B]  Q[G,B,D,S]  L[G,B,D,S]  M[4x4 over D,G,S,B].
+__global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base, int combined,
+                                              int masked, int it_arg, int flags_arg,
+                                              int slotF, int slotQ, int slotL, int slotM) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nm) return;
+  int c = __ldg(d.m1_circ + i);
+  int iter = it_arg;
+  bool dcop = flags_arg & XG_FLAG_DCOP, initJct = flags_arg & XG_FLAG_INITJCT;
+  double qs = 1.0, fs = 1.0;
+  if (masked) {
+    const CircState &s = d.cs[c];
+    if (!circ_active(s)) return;
+    iter = s.iter;
+    dcop = s.phase == PH_DC;
+    initJct = dcop && s.init_jct && iter == 0;
+    qs = s.qscale; fs = s.fscale;
+  }
+  const Mos1Model m = d.m1_models[__ldg(d.m1_model + i)];
+  const int nD = __ldg(d.m1_node + i), nG = __ldg(d.m1_node + nm + i);
+  const int nS = __ldg(d.m1_node + 2 * nm + i), nB = __ldg(d.m1_node + 3 * nm + i);
+  const double *x = d.x;
+  double Vd = nD >= 0 ? x[nD] : 0.0, Vg = nG >= 0 ? x[nG] : 0.0;
+  double Vs = nS >= 0 ? x[nS] : 0.0, Vb = nB >= 0 ? x[nB] : 0.0;
+  const double dt = m.dtype;
+  const double Beta = __ldg(d.m1_beta + i), tVbi = __ldg(d.m1_vbi + i);
+  const double tVto = tVbi + dt * m.gammaSqrtPhi;
+  double *sto_n = d.sto_next + sto_base;
+  const double *sto_c = d.sto_curr + sto_base;
+
+  double vbs = dt * (Vb - Vs), vgs = dt * (Vg - Vs), vds = dt * (Vd - Vs);
+  double vbd = vbs - vds, vgd = vgs - vds;
+  const double vgs_o = vgs, vds_o = vds, vbs_o = vbs, vbd_o = vbd, vgd_o = vgd;
+  if (initJct) {
+    vbs = -1; vgs = dt * tVto; vds = 0; vbd = vbs - vds; vgd = vgs - vds;
+  }
+  double vbs_old, vbd_old, vgs_old, vds_old, Von;
+  if (iter == 0 && dcop) {
+    vbs_old = vbs; vbd_old = vbd; vgs_old = vgs; vds_old = vds; Von = 0.0;
+  } else {
+    const double *h = (iter == 0) ? sto_c : sto_n;
+    vbd_old = h[i]; vbs_old = h[nm + i]; vgs_old = h[2 * nm + i]; vds_old = h[3 * nm + i];
+    Von = dt * h[4 * nm + i];
+  }
+  double vgd_old = vgs_old - vds_old;
+  int Check = 1;
+  if (vds_old >= 0) {
+    vgs = fetlim_d(vgs, vgs_old, Von);
+    vds = vgs - vgd;
+    vds = limvds_d(vds, vds_old);
+    vgd = vgs - vds;
+  } else {
+    vgd = fetlim_d(vgd, vgd_old, Von);
+    vds = vgs - vgd;
+    vds = -limvds_d(-vds, -vds_old);
+    vgs = vgd + vds;
+  }
+  if (vds >= 0.0) {
+    vbs = pnjlim_d(vbs, vbs_old, m.vt, m.sourceVcrit, Check);
+    vbd = vbs - vds;
+  } else {
+    vbd = pnjlim_d(vbd, vbd_old, m.vt, m.drainVcrit, Check);
+    vbs = vbd + vds;
+  }
+  vbd = vbs - vds;
+  vgd = vgs - vds;
+  const double Vgb = vgs - vbs;
+  const bool origFlag = !(vgs_o != vgs || vds_o != vds || vbs_o != vbs || vbd_o != vbd || vgd_o != vgd);
+  double gbs, cbs, gbd, cbd;
+  if (vbs <= 0) {
+    gbs = m.SourceSatCur / m.vt + kGmin;
+    cbs = gbs * vbs;
+  } else {
+    double e = exp(fmin(kMaxExpArg, vbs / m.vt));
+    gbs = m.SourceSatCur * e / m.vt + kGmin;
+    cbs = m.SourceSatCur * (e - 1) + kGmin * vbs;
+  }
+  if (vbd <= 0) {
+    gbd = m.DrainSatCur / m.vt + kGmin;
+    cbd = gbd * vbd;
+  } else {
+    double e = exp(fmin(kMaxExpArg, vbd / m.vt));
+    gbd = m.DrainSatCur * e / m.vt + kGmin;
+    cbd = m.DrainSatCur * (e - 1) + kGmin * vbd;
+  }
+  const int mode = (vds >= 0) ? 1 : -1;
+  double cdrain, gm, gds, gmbs, Vdsat;
+  {
+    double vbx = (mode == 1) ? vbs : vbd;
+    double sarg;
+    if (vbx <= 0) {
+      sarg = sqrt(m.tPhi - vbx);
+    } else {
+      sarg = sqrt(m.tPhi);
+      sarg = sarg - vbx / (sarg + sarg);
+      sarg = fmax(0.0, sarg);
+    }
+    Von = (tVbi * dt) + m.gamma * sarg;
+    double vgst = ((mode == 1) ? vgs : vgd) - Von;
+    Vdsat = fmax(vgst, 0.0);
+    double arg = (sarg <= 0) ? 0 : m.gamma / (sarg + sarg);
+    if (vgst <= 0) {
+      cdrain = 0; gm = 0; gds = 0; gmbs = 0;
+    } else {
+      double vdsm = vds * mode;
+      double betap = Beta * (1 + m.lambda * vdsm);
+      if (vgst <= vdsm) {
+        cdrain = betap * vgst * vgst * .5;
+        gm = betap * vgst;
+        gds = m.lambda * Beta * vgst * vgst * .5;
+      } else {
+        cdrain = betap * vdsm * (vgst - .5 * vdsm);
+        gm = betap * vdsm;
+        gds = betap * (vgst - vdsm) + m.lambda * Beta * vdsm * (vgst - .5 * vdsm);
+      }
+      gmbs = gm * arg;
+    }
+  }
+  double qbs = 0, capbs = 0, qbd = 0, capbd = 0;
+  if (m.has_junc_caps) {
+    mos1_junction(m, vbs, m.Cbs, m.Cbssw, m.f2s, m.f3s, m.f4s, qbs, capbs);
+    mos1_junction(m, vbd, m.Cbd, m.Cbdsw, m.f2d, m.f3d, m.f4d, qbd, capbd);
+  }
+  double capgs = 0, capgd = 0, capgb = 0, Capgs = 0, Capgd = 0, Capgb = 0, qgs = 0, qgd = 0, qgb = 0;
+  double *sta_n = d.sta_next;
+  const double *sta_c = d.sta_curr;
+  if (m.has_gate_caps) {
+    if (mode > 0) qmeyer_d(vgs, vgd, Von, Vdsat, capgs, capgd, capgb, m.tPhi, m.OxideCap);
+    else qmeyer_d(vgd, vgs, Von, Vdsat, capgd, capgs, capgb, m.tPhi, m.OxideCap);
+    if (dcop) {
+      Capgs = 2.0 * capgs + m.Cgso; Capgd = 2.0 * capgd + m.Cgdo; Capgb = 2.0 * capgb + m.Cgbo;
+    } else {
+      Capgs = capgs + sta_c[i] + m.Cgso;
+      Capgd = capgd + sta_c[nm + i] + m.Cgdo;
+      Capgb = capgb + sta_c[2 * nm + i] + m.Cgbo;
+    }
+    Capgs = fabs(Capgs); Capgd = fabs(Capgd); Capgb = fabs(Capgb);
+    if (dcop) {
+      qgs = Capgs * vgs; qgd = Capgd * vgd; qgb = Capgb * Vgb;
+    } else {
+      double vgs1 = sto_c[2 * nm + i], vbs1 = sto_c[nm + i], vds1 = sto_c[3 * nm + i];
+      qgs = sta_c[3 * nm + i] + Capgs * (vgs - vgs1);
+      qgd = sta_c[4 * nm + i] + Capgd * (vgd - (vgs1 - vds1));
+      qgb = sta_c[5 * nm + i] + Capgb * ((vgs - vbs) - (vgs1 - vbs1));
+    }
+  }
+  double Gm, Gmbs, nrmsum, revsum, cdreq;
+  if (mode >= 0) {
+    Gm = gm; Gmbs = gmbs; nrmsum = Gm + Gmbs; revsum = 0; cdreq = dt * cdrain;
+  } else {
+    Gm = -gm; Gmbs = -gmbs; nrmsum = 0; revsum = -(Gm + Gmbs); cdreq = -dt * cdrain;
+  }
+  // store / state (Master::updateState, N_DEV_MOSFET1.C:4241-4333)
+  sto_n[i] = vbd; sto_n[nm + i] = vbs; sto_n[2 * nm + i] = vgs; sto_n[3 * nm + i] = vds;
+  sto_n[4 * nm + i] = dt * Von; sto_n[5 * nm + i] = Gm;
+  sta_n[i] = capgs; sta_n[nm + i] = capgd; sta_n[2 * nm + i] = capgb;
+  sta_n[3 * nm + i] = qgs; sta_n[4 * nm + i] = qgd; sta_n[5 * nm + i] = qgb;
+  sta_n[6 * nm + i] = qbd; sta_n[7 * nm + i] = qbs;
+  if (!origFlag && masked && dcop) {
+    // "some device limited" flag for the operating-point device-convergence test
+    atomicOr(&d.cs[c].limited, 1);
+  }
+  const double M = m.M;
+  // loadDAEVectors (N_DEV_MOSFET1.C:4343-4576), old Meyer
+  const double ceqbs = dt * cbs, ceqbd = dt * cbd;
+  double *sF = d.sF + slotF, *sQ = d.sQ + slotQ;
+  sF[i] = (-(ceqbd - cdreq)) * M;                 // D
+  sF[nm + i] = (-(ceqbs + cdreq)) * M;            // S
+  sF[2 * nm + i] = (ceqbs + ceqbd) * M;           // B
+  const double Qbs = dt * qbs, Qbd = dt * qbd, Qgb = dt * qgb, Qgs = dt * qgs, Qgd = dt * qgd;
+  sQ[i] = (Qgs + Qgd + Qgb) * M;                  // G
+  sQ[nm + i] = (Qbs + Qbd - Qgb) * M;             // B
+  sQ[2 * nm + i] = -(Qbd + Qgd) * M;              // D
+  sQ[3 * nm + i] = -(Qbs + Qgs) * M;              // S
+  double lf[4] = {0, 0, 0, 0}, lq[4] = {0, 0, 0, 0};
+  if (!origFlag) {
+    double dvbd = vbd - vbd_o, dvbs = vbs - vbs_o, dvds = vds - vds_o, dvgs = vgs - vgs_o,
+           dvgd = vgd - vgd_o;
+    double sw = Gm * ((mode > 0) ? dvgs : dvgd) + Gmbs * ((mode > 0) ? dvbs : dvbd);
+    lf[1] = dt * ((gbd - kGmin) * dvbd + (gbs - kGmin) * dvbs) * M;
+    lf[2] = dt * (-(gbd - kGmin) * dvbd + gds * dvds + sw) * M;
+    lf[3] = dt * (-(gbs - kGmin) * dvbs - gds * dvds - sw) * M;
+    lq[0] = dt * (Capgd * dvgd + Capgs * dvgs + Capgb * (dvgs - dvbs)) * M;
+    lq[1] = dt * (-Capgb * (dvgs - dvbs) + Capgb * dvbd + capbs * dvbs) * M;
+    lq[2] = dt * (-Capgd * dvgd - capbd * dvbd) * M;
+    lq[3] = dt * (-Capgs * dvgs - capbs * dvbs) * M;
+  }
+  double *sL = d.sL + slotL;
+  if (combined) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) sL[k * nm + i] = fs * lf[k] + qs * lq[k];
+  } else {
+    double *sL2 = d.sL2 + slotL;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { sL[k * nm + i] = lf[k]; sL2[k * nm + i] = lq[k]; }
+  }
+  // loadDAEMatrices (N_DEV_MOSFET1.C:4587-4876), nodes (0=D,1=G,2=S,3=B)
+  double f[16], q[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) { f[k] = 0.0; q[k] = 0.0; }
+  f[15] = gbs + gbd; f[12] = -gbd; f[14] = -gbs;
+  f[1] = Gm; f[3] = -gbd + Gmbs; f[0] = gds + gbd + revsum; f[2] = -gds - nrmsum;
+  f[9] = -Gm; f[11] = -(gbs + Gmbs); f[8] = -(gds + revsum); f[10] = gds + gbs + nrmsum;
+  q[5] = Capgd + Capgs + Capgb; q[7] = -Capgb; q[4] = -Capgd; q[6] = -Capgs;
+  q[13] = -Capgb; q[15] = capbs + capbd + Capgb; q[12] = -capbd; q[14] = -capbs;
+  q[1] = -Capgd; q[3] = -capbd; q[0] = capbd + Capgd;
+  q[9] = -Capgs; q[11] = -capbs; q[10] = capbs + Capgs;
+  double *sM = d.sM + slotM;
+  if (combined) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) sM[k * nm + i] = (fs * f[k] + qs * q[k]) * M;
+  } else {
+    double *sM2 = d.sM2 + slotM;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) { sM[k * nm + i] = f[k] * M; sM2[k * nm + i] = q[k] * M; }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Diode level 1 (no sidewall).  Store planes: vd qd cd.
+// Slots: F[P,N,R]  Q[N,R]  L[N,R]  M[(P,P)(P,R)(N,N)(N,R)(R,P)(R,N)(R,R)].
+__global__ void __launch_bounds__(128) k_diode(DevArrays d, int nd, int combined, int masked,
+                                               int it_arg, int flags_arg, int slotF, int slotQ,
+                                               int slotL, int slotM) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nd) return;
+  int c = __ldg(d.d_circ + i);
+  int iter = it_arg;
+  bool dcop = flags_arg & XG_FLAG_DCOP, initJct = flags_arg & XG_FLAG_INITJCT;
+  double qs = 1.0, fs = 1.0;
+  if (masked) {
+    const CircState &s = d.cs[c];
+    if (!circ_active(s)) return;
+    iter = s.iter;
+    dcop = s.phase == PH_DC;
+    initJct = dcop && s.init_jct && iter == 0;
+    qs = s.qscale; fs = s.fscale;
+  }
+  const DiodeModel t = d.d_models[__ldg(d.d_model + i)];
+  const int nP = __ldg(d.d_node + i), nN = __ldg(d.d_node + nd + i), nR = __ldg(d.d_node + 2 * nd + i);
+  const double *x = d.x;
+  const double VP = nP >= 0 ? x[nP] : 0.0, VN = nN >= 0 ? x[nN] : 0.0, VR = nR >= 0 ? x[nR] : 0.0;
+  double Vd = VR - VN;
+  const double Vd_orig = Vd;
+  double Vd_old;
+  if (iter == 0) {
+    if (initJct) Vd = t.tVcrit;
+    Vd_old = dcop ? Vd : d.sto_curr[i];
+  } else {
+    Vd_old = d.sto_next[i];
+  }
+  int ichk = 0;
+  if (t.bvGiven && Vd < fmin(0.0, -t.tBrkdwnV + 10.0 * t.VteBRK)) {
+    double Vdtmp = -(t.tBrkdwnV + Vd);
+    Vdtmp = pnjlim_d(Vdtmp, -(Vd_old + t.tBrkdwnV), t.VteBRK, t.tVcrit, ichk);
+    Vd = -(Vdtmp + t.tBrkdwnV);
+  } else {
+    Vd = pnjlim_d(Vd, Vd_old, t.Vte, t.tVcrit, ichk);
+  }
+  double Id, Gd;
+  if (Vd >= -3.0 * t.Vte) {
+    double evd = exp(fmin(kMaxExpArg, Vd / t.Vte));
+    double Inorm = t.Isat * (evd - 1.0) + kGmin * Vd;
+    double Gd1 = t.Isat * evd / t.Vte + kGmin;
+    evd = exp(fmin(kMaxExpArg, Vd / t.VteR));
+    double Irec = t.IsatR * (evd - 1.0);
+    double Gd2 = t.IsatR * evd / t.VteR;
+    double Khi = 1, DKhi = 0;
+    if (t.tIKF > 0) {
+      Khi = sqrt(t.tIKF / (t.tIKF + Inorm));
+      DKhi = -0.5 * Khi * Gd1 / (t.tIKF + Inorm);
+    }
+    double Kgen = 0, DKgen = 0;
+    if (Irec != 0) {
+      double a = 1 - Vd / t.tJctPot;
+      Kgen = sqrt(pow(a * a + 0.005, t.M));
+      DKgen = -t.M * a * Kgen / (t.tJctPot * (a * a + 0.005));
+    }
+    Id = Inorm * Khi + Irec * Kgen;
+    Gd = Gd1 * Khi + Inorm * DKhi + Gd2 * Kgen + Irec * DKgen;
+  } else if (!t.tBrkdwnV || Vd >= -t.tBrkdwnV) {
+    double arg = 3.0 * t.Vte / (Vd * kE);
+    arg = arg * arg * arg;
+    Id = -t.Isat * (1.0 + arg) + kGmin * Vd;
+    Gd = t.Isat * 3.0 * arg / Vd + kGmin;
+  } else {
+    double evrev = exp(fmin(kMaxExpArg, -(t.tBrkdwnV + Vd) / t.VteBRK));
+    Id = -t.Isat * evrev + kGmin * Vd;
+    Gd = t.Isat * evrev / t.VteBRK + kGmin;
+  }
+  double Qd = 0, Cd = 0;
+  if (t.tJctCap != 0.0) {
+    double Czero = t.tJctCap;
+    if (Vd < t.tDepCap) {
+      double arg = 1.0 - Vd / t.tJctPot;
+      double sarg = exp(fmin(kMaxExpArg, -t.M * log(arg)));
+      Qd = t.TT * Id + t.tJctPot * Czero * (1.0 - arg * sarg) / (1.0 - t.M);
+      Cd = t.TT * Gd + Czero * sarg;
+    } else {
+      double Czof2 = Czero / t.F2;
+      double MotJctPot = t.M / t.tJctPot;
+      Qd = t.TT * Id + Czero * t.tF1 +
+           Czof2 * (t.F3 * (Vd - t.tDepCap) + 0.5 * MotJctPot * (Vd * Vd - t.tDepCap * t.tDepCap));
+      Cd = t.TT * Gd + Czof2 * (t.F3 + MotJctPot * Vd);
+    }
+  }
+  d.sto_next[i] = Vd; d.sto_next[nd + i] = Qd; d.sto_next[2 * nd + i] = Cd;
+  if (Vd != Vd_orig && masked && dcop) atomicOr(&d.cs[c].limited, 1);
+  const double Ir = t.Gspr * (VP - VR);
+  double *sF = d.sF + slotF, *sQ = d.sQ + slotQ;
+  sF[i] = Ir; sF[nd + i] = -Id; sF[2 * nd + i] = Id - Ir;
+  sQ[i] = -Qd; sQ[nd + i] = Qd;
+  const double dv = Vd - Vd_orig;
+  const double Gj = -Gd * dv, Cj = -Cd * dv;
+  double *sL = d.sL + slotL;
+  if (combined) {
+    sL[i] = fs * Gj + qs * Cj; sL[nd + i] = -(fs * Gj + qs * Cj);
+  } else {
+    double *sL2 = d.sL2 + slotL;
+    sL[i] = Gj; sL[nd + i] = -Gj; sL2[i] = Cj; sL2[nd + i] = -Cj;
+  }
+  const double G = t.Gspr;
+  double f[7] = {G, -G, Gd, -Gd, -G, -Gd, G + Gd};
+  double q[7] = {0, 0, Cd, -Cd, 0, -Cd, Cd};
+  double *sM = d.sM + slotM;
+  if (combined) {
+#pragma unroll
+    for (int k = 0; k < 7; ++k) sM[k * nd + i] = fs * f[k] + qs * q[k];
+  } else {
+    double *sM2 = d.sM2 + slotM;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) { sM[k * nd + i] = f[k]; sM2[k * nd + i] = q[k]; }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic per-(block, circuit) partial reductions.  A row block covers
+// rows [b*kRowBlock, (b+1)*kRowBlock); pair_base[b] is the first partial slot
+// of the block, blk_cfirst[b] its first circuit.
+__device__ void block_partials(const DevArrays &d, int n, double vmax, double vsum, int r) {
+  __shared__ double smax[kRowBlock], ssum[kRowBlock];
+  smax[threadIdx.x] = vmax;
+  ssum[threadIdx.x] = vsum;
+  __syncthreads();
+  const int b = blockIdx.x;
+  const int r0 = b * kRowBlock, r1 = min(n, r0 + kRowBlock);
+  const int cfirst = d.blk_cfirst[b];
+  const int nseg = d.circ_of_row[r1 - 1] - cfirst + 1;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int seg = warp; seg < nseg; seg += kRowBlock / 32) {
+    const int cc = cfirst + seg;
+    const int lo = max(d.offsets[cc], r0) - r0, hi = min(d.offsets[cc + 1], r1) - r0;
+    double m = 0.0, s = 0.0;
+    for (int k = lo + lane; k < hi; k += 32) {
+      m = fmax(m, smax[k]);
+      s += ssum[k];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+      s += __shfl_xor_sync(0xffffffffu, s, o);
+    }
+    if (lane == 0) {
+      d.pmax[d.pair_base[b] + seg] = m;
+      d.psum[d.pair_base[b] + seg] = s;
+    }
+  }
+  (void)r;
+}
+
+// Residual per row: RHS = -(qscale (Q - Q_hist0) + fscale (F - B) + hscale Q_hist2 + gshunt x)
+//                        + limiter terms     (OneStep::obtainResidual, N_TIA_OneStep.C:219-290)
+__global__ void __launch_bounds__(kRowBlock) k_assemble_rows(DevArrays d, int n) {
+  const int r = blockIdx.x * kRowBlock + threadIdx.x;
+  double vmax = 0.0, vsum = 0.0;
+  if (r < n) {
+    const int c = d.circ_of_row[r];
+    const CircState &s = d.cs[c];
+    if (circ_active(s)) {
+      double Fl = 0.0, Ql = 0.0;
+      for (int e = d.rp[r]; e < d.rp[r + 1]; ++e) {
+        const double xv = d.x[d.ci[e]];
+        Fl += d.Glin[e] * xv;
+        Ql += d.Clin[e] * xv;
+      }
+      double F = Fl, Q = Ql, B = 0.0, L = 0.0;
+      for (int k = d.vF_ptr[r]; k < d.vF_ptr[r + 1]; ++k) F += d.sF[d.vF_idx[k]];
+      for (int k = d.vQ_ptr[r]; k < d.vQ_ptr[r + 1]; ++k) Q += d.sQ[d.vQ_idx[k]];
+      for (int k = d.vB_ptr[r]; k < d.vB_ptr[r + 1]; ++k) B += d.sB[d.vB_idx[k]];
+      for (int k = d.vL_ptr[r]; k < d.vL_ptr[r + 1]; ++k) L += d.sL[d.vL_idx[k]];
+      double res = s.fscale * (F - B);
+      if (s.qscale != 0.0) res += s.qscale * (Q - d.qh0[r]);
+      if (s.hscale != 0.0) res += s.hscale * d.qh2[r];
+      if (s.gshunt != 0.0) res += s.gshunt * d.x[r];
+      const double rhs = -res + L;
+      d.rhs[r] = rhs;
+      d.Qv[r] = Q;
+      d.FmB[r] = F - B;
+      vmax = fabs(rhs);
+      vsum = rhs * rhs;
+      if (!(vsum == vsum) || isinf(vsum)) vmax = vsum = __longlong_as_double(0x7ff8000000000000ULL);
+    }
+  }
+  block_partials(d, n, vmax, vsum, r);
+}
+
+// Jacobian per CSR entry: J = qscale dQdx + fscale dFdx (+ gshunt on the diagonal)
+// (OneStep::obtainJacobian, N_TIA_OneStep.C:469-500; EpetraMatrix::linearCombo)
+__global__ void k_assemble_J(DevArrays d, int nnz) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nnz) return;
+  const int r = d.erow[e];
+  const CircState &s = d.cs[d.circ_of_row[r]];
+  if (!circ_active(s)) return;
+  double v = s.qscale * d.Clin[e] + s.fscale * d.Glin[e];
+  for (int k = d.m_ptr[e]; k < d.m_ptr[e + 1]; ++k) v += d.sM[d.m_idx[k]];
+  if (s.gshunt != 0.0 && d.ci[e] == r) v += s.gshunt;
+  d.J[e] = v;
+}
+
+// Loader-API assembly: ADD device contributions into caller vectors (loadDAEVectors).
+__global__ void k_load_vectors(DevArrays d, int n, const double *x, double *Q, double *F, double *B,
+                               double *dFv, double *dQv, int load_type) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  if (load_type != XG_LOAD_NONLINEAR) {
+    double Fl = 0.0, Ql = 0.0;
+    for (int e = d.rp[r]; e < d.rp[r + 1]; ++e) {
+      const double xv = x[d.ci[e]];
+      Fl += d.Glin[e] * xv;
+      Ql += d.Clin[e] * xv;
+    }
+    double Bs = 0.0;
+    for (int k = d.vB_ptr[r]; k < d.vB_ptr[r + 1]; ++k) Bs += d.sB[d.vB_idx[k]];
+    F[r] += Fl; Q[r] += Ql; B[r] += Bs;
+  }
+  if (load_type != XG_LOAD_LINEAR) {
+    double Fs = 0.0, Qs = 0.0, Lf = 0.0, Lq = 0.0;
+    for (int k = d.vF_ptr[r]; k < d.vF_ptr[r + 1]; ++k) Fs += d.sF[d.vF_idx[k]];
+    for (int k = d.vQ_ptr[r]; k < d.vQ_ptr[r + 1]; ++k) Qs += d.sQ[d.vQ_idx[k]];
+    for (int k = d.vL_ptr[r]; k < d.vL_ptr[r + 1]; ++k) { Lf += d.sL[d.vL_idx[k]]; Lq += d.sL2[d.vL_idx[k]]; }
+    F[r] += Fs; Q[r] += Qs; dFv[r] += Lf; dQv[r] += Lq;
+  }
+}
+
+// Loader-API assembly: ADD into caller dQdx / dFdx CSR values (loadDAEMatrices).
+__global__ void k_load_matrices(DevArrays d, int nnz, double *dQdx, double *dFdx, int load_type) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nnz) return;
+  double f = 0.0, q = 0.0;
+  if (load_type != XG_LOAD_NONLINEAR) { f += d.Glin[e]; q += d.Clin[e]; }
+  if (load_type != XG_LOAD_LINEAR)
+    for (int k = d.m_ptr[e]; k < d.m_ptr[e + 1]; ++k) { f += d.sM[d.m_idx[k]]; q += d.sM2[d.m_idx[k]]; }
+  dFdx[e] += f;
+  dQdx[e] += q;
+}
+
+// ---------------------------------------------------------------------------
+// Per-circuit Newton decision: DampedNewton::converged_ (N_NLS_DampedNewton.C:1191-1396).
+// One warp per circuit reduces the row partials of its residual.
+__global__ void k_newton_ctl(DevArrays d, int ncirc) {
+  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (c >= ncirc) return;
+  CircState &s = d.cs[c];
+  if (s.phase == PH_STALL) return;  // parked until the host re-pivots; flags kept
+  if (!circ_active(s)) {
+    if (lane == 0) { s.need_solve = 0; s.step_end = 0; s.accept = 0; s.start_step = 0; }
+    return;
+  }
+  double m = 0.0, sum = 0.0;
+  bool bad = false;
+  for (int k = d.pair_cstart[c] + lane; k < d.pair_cstart[c + 1]; k += 32) {
+    double a = d.pmax[k], b = d.psum[k];
+    if (!(a == a) || !(b == b)) bad = true;
+    m = fmax(m, a);
+    sum += b;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  }
+  bad = __any_sync(0xffffffffu, bad);
+  if (lane != 0) return;
+  const TranParams &p = *d.tp;
+  const bool tran = s.phase == PH_TRAN;
+  const double normRHS = bad ? __longlong_as_double(0x7ff8000000000000ULL) : sqrt(sum);
+  const bool nan = !(normRHS == normRHS) || isinf(normRHS);
+  s.accept = 0; s.start_step = 0; s.step_end = 0; s.need_solve = 0;
+  const int limited = s.limited;
+  s.limited = 0;
+  int status = 0;
+  if (s.iter == 0) {
+    s.normRHS = normRHS;
+    s.normRHS_init = normRHS;
+    s.normRHS_old = normRHS;
+    s.count = 0;
+    s.tmpConvRate = 1.0;
+    if (nan) status = -6;
+  } else {
+    const double eps = 2.220446049250313e-16;
+    const double convRateMax = 0.5 * 1.7976931348623157e308;
+    const int maxstep = tran ? p.nl_maxstep : p.dc_maxstep;
+    const int nlStep = s.iter;
+    s.normRHS = normRHS;
+    s.maxNormRHS = m;
+    if (nan) {
+      status = -6;
+    } else if (!tran && limited) {
+      status = (nlStep < maxstep) ? 0 : -1;
+    } else if (normRHS < eps) {
+      status = 1;
+    } else {
+      const double rel = normRHS / s.normRHS_init;
+      const double rate = normRHS / s.normRHS_old;
+      s.normRHS_old = normRHS;
+      const double rhstol = tran ? p.nl_rhstol : p.dc_rhstol;
+      const double dxtol = tran ? p.nl_deltaxtol : p.dc_deltaxtol;
+      if (m <= rhstol && s.wtNormDX <= dxtol) status = 2;
+      else if (nlStep >= maxstep && tran && rel <= 0.9 && rate <= 1.0) status = -3;
+      else if (s.wtNormDX <= p.nl_smallupdatetol) status = 4;
+      else if (nlStep >= maxstep) status = -1;
+      else if (rate > convRateMax) status = -2;
+      else {
+        if (tran && fabs(rate - 1.0) <= 1.0e-3) {
+          if (s.count == 0 || rate < s.tmpConvRate) s.tmpConvRate = rate;
+          s.count++;
+        } else {
+          s.count = 0;
+        }
+        if (tran && s.count == 5) { s.count = 0; status = -3; }
+      }
+    }
+  }
+  s.newton_status = status;
+  if (status != 0) {
+    s.step_end = 1;
+  } else {
+    s.need_solve = 1;
+    s.singular = 0;
+  }
+}
+
+// x += dx with the update norm; at the end of a Newton solve, the LTE sum
+// (DataStore::stepLinearCombo + WRMS_errorNorm, N_TIA_DataStore.C:1495,1737)
+// and max|x| for the next error weights.
+__global__ void __launch_bounds__(kRowBlock) k_update(DevArrays d, int n) {
+  const int r = blockIdx.x * kRowBlock + threadIdx.x;
+  double vmax = 0.0, vsum = 0.0;
+  if (r < n) {
+    const int c = d.circ_of_row[r];
+    const CircState &s = d.cs[c];
+    if (circ_active(s)) {
+      if (s.need_solve) {
+        if (!s.singular) {
+          const double dxr = d.dx[r];
+          const double xnew = d.x[r] + dxr;
+          d.x[r] = xnew;
+          double w = d.solwt[r];
+          if (s.phase == PH_DC) {
+            const TranParams &p = *d.tp;
+            w = p.dc_reltol * fmax(fabs(xnew), fabs(d.xcurr[r])) + p.dc_abstol;
+            d.solwt[r] = w;
+          }
+          vmax = fabs(dxr) / w;
+          if (!(dxr == dxr) || isinf(dxr)) vsum = 1.0;  // NaN / Inf marker
+        }
+      } else if (s.step_end) {
+        const double xr = d.x[r];
+        vmax = fabs(xr);
+        if (s.phase == PH_TRAN && s.newton_status > 0) {
+          const double e = (xr - d.xn0[r]) / s.errwt;
+          vsum = e * e;
+        }
+      }
+    }
+  }
+  block_partials(d, n, vmax, vsum, r);
+}
+
+// Next step of one circuit: OneStep::initialize (N_TIA_OneStep.C:1684-1800),
+// updateCoeffs (:1584-1640) and the error weights of DataStore::setErrorWtVector.
+__device__ void start_next_step(CircState &s, const TranParams &p, int &init_hist) {
+  init_hist = 0;
+  if (s.beginning && s.lastOk) {
+    const double time_to_stop = s.stopTime - s.t;
+    double hn = (s.t == p.tstart) ? 0.005 * time_to_stop : 0.1 * fmin(s.saved, time_to_stop);
+    if (hn > p.hmax) hn = p.hmax;
+    s.h = (s.t != p.tstart) ? fmin(s.h, hn) : hn;
+    s.h = fmin(fmax(s.h, p.hmin), p.hmax);
+    s.tsum = 2.0 * s.h;
+    s.lastTimeStep = s.h;
+    s.numberOfSteps = 0;
+    s.order = 1;
+    s.psi[0] = s.h;
+    init_hist = 1;
+  }
+  const double h = s.h;
+  if (s.order == 2) s.psi[2] = s.psi[1];
+  s.psi[1] = s.psi[0];
+  s.psi[0] = h;
+  if (s.order == 2) {
+    s.beta[1] = h / s.psi[1] + (h / s.psi[1]) * (h / s.psi[1]) / 2;
+    s.beta[2] = -1.0 * h * h / s.psi[1] / s.psi[2] / 2;
+    s.ck = (h / s.tsum) / 3.0;
+  } else {
+    s.beta[1] = h / s.psi[1];
+    s.ck = h / s.tsum;
+  }
+  s.errwt = p.reltol * s.xmax_curr + p.abstol;
+  double tn = s.t + h;
+  if (fabs(tn - s.stopTime) <= p.bptol) tn = s.stopTime;
+  s.tn = tn;
+  s.qscale = 1.0 / h;
+  s.fscale = (s.order == 2) ? 0.5 : 1.0;
+  s.hscale = (s.order == 2) ? 0.5 : 0.0;
+  s.iter = 0;
+  s.start_step = 1;
+}
+
+__device__ double next_bp(const double *bps, int lo, int hi, double t, double bptol, int &idx) {
+  int k = idx;
+  if (k < lo) k = lo;
+  while (k < hi && !(bps[k] > t + bptol)) ++k;
+  idx = k;
+  return (k < hi) ? bps[k] : bps[hi - 1];
+}
+
+// Per-circuit step decision (StepErrorControl::evaluateStepError, OneStep::completeStep /
+// rejectStep, Transient::processSuccessfulStep) and the operating-point stages.
+__global__ void k_step_ctl(DevArrays d, int ncirc, const double *bps, const int *bp_ptr, int cap) {
+  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (c >= ncirc) return;
+  CircState &s = d.cs[c];
+  if (!circ_active(s)) return;
+  double m = 0.0, sum = 0.0;
+  for (int k = d.pair_cstart[c] + lane; k < d.pair_cstart[c + 1]; k += 32) {
+    m = fmax(m, d.pmax[k]);
+    sum += d.psum[k];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  }
+  if (lane != 0) return;
+  const TranParams &p = *d.tp;
+  if (s.need_solve) {
+    if (s.singular) {
+      // frozen pivot failed the threshold test: park this Newton iteration
+      // (J and RHS stay intact) until the host re-pivots and resumes it
+      s.stall_prev = s.phase;
+      s.phase = PH_STALL;
+      return;
+    } else if (sum != 0.0) {
+      s.newton_status = -6;   // NaN or Inf in the Newton update
+    } else {
+      s.wtNormDX = m;
+      s.iter++;
+      return;
+    }
+    s.iter++;
+    s.need_solve = 0;
+    s.step_end = 1;
+  }
+  if (!s.step_end) return;
+  const int n_c = d.offsets[c + 1] - d.offsets[c];
+  const int status = s.newton_status;
+  const int b0 = bp_ptr[c], b1 = bp_ptr[c + 1];
+  s.accept = 0;
+  if (s.phase == PH_DC) {
+    s.dcop_iters += s.iter;
+    if (status > 0) {
+      if (s.gshunt > 0.0) {
+        s.gshunt = (s.gshunt / 10.0 >= 1e-12 * 0.999) ? s.gshunt / 10.0 : 0.0;
+        s.iter = 0;
+        s.init_jct = 0;
+        return;
+      }
+      // operating point done: the DC solution is the accepted state at tstart
+      s.accept = 2;  // "DC accepted" event for k_history / k_state_commit
+      s.xmax_curr = m;
+      s.phase = p.dc_only ? PH_DONE : PH_TRAN;
+      s.t = p.tstart;
+      s.beginning = 1;
+      s.lastOk = 1;
+      s.stepNumber = 0;
+      s.estOverTol = 0.0;
+      s.saved = p.hmax;
+      s.nef = 0;
+      s.order = 1;
+      s.bp_index = b0;
+      s.stopTime = next_bp(bps, b0, b1, s.t, p.bptol, s.bp_index);
+      s.init_jct = 0;
+      s.gshunt = 0.0;
+      if (s.n_out < cap) { d.out_t[(size_t)c * cap + s.n_out] = s.t; }
+      s.n_out++;
+      if (p.dc_only) return;
+    } else {
+      if (s.dc_stage == 0) {
+        s.dc_stage = 1;
+        s.gshunt = 1e-2;
+        s.init_jct = 1;
+        s.iter = 0;
+        s.accept = 3;  // restart from x = 0
+        return;
+      }
+      s.phase = PH_FAILED;
+      s.newton_status = status;
+      return;
+    }
+  } else {
+    // transient step end
+    s.newton_iters += s.iter;
+    bool ok = status > 0;
+    if (!ok) s.newton_fail++;
+    if (ok) {
+      const bool test = (s.t == p.tstart) ? (s.stepNumber >= 1 && !s.beginning) : (s.stepNumber >= 1);
+      if (test) {
+        s.estOverTol = s.ck * sqrt(sum / n_c);
+        if (!(s.estOverTol <= 1.0)) { ok = false; s.lte_fail++; }
+      }
+    }
+    if (ok) {
+      s.numberOfSteps++;
+      s.nef = 0;
+      s.t = s.tn;
+      s.lastTimeStep = s.h;
+      double rr = pow(0.5 / (s.estOverTol + 0.0001), 1.0 / (s.order + 1.0));
+      if (s.numberOfSteps >= 2 && p.max_order == 2 && s.order == 1) {
+        s.order = 2;
+        rr = pow(0.5 / (s.estOverTol + 0.0001), 1.0 / 3.0);
+        if (rr <= 1.05) s.order = 1;
+      }
+      double hnew = s.h;
+      if (rr >= 2.0) hnew = 2.0 * s.h;
+      else if (rr <= 1) hnew = fmax(0.25, fmin(0.9, rr)) * s.h;
+      hnew = fmin(fmax(hnew, p.hmin), p.hmax);
+      const bool hit_bp = fabs(s.t - s.stopTime) <= p.bptol && fabs(s.t - p.tstop) > p.bptol;
+      if (hit_bp) {
+        s.saved = hnew;
+        s.beginning = 1;
+        s.stopTime = next_bp(bps, b0, b1, s.t, p.bptol, s.bp_index);
+      } else {
+        s.beginning = 0;
+        if (s.t + hnew > s.stopTime) { s.saved = hnew; hnew = s.stopTime - s.t; }
+        s.h = hnew;
+        s.tsum = s.h + s.lastTimeStep;
+      }
+      s.stepNumber++;
+      s.accepted++;
+      s.lastOk = 1;
+      s.accept = 1;
+      s.xmax_curr = m;
+      if (s.n_out < cap) { d.out_t[(size_t)c * cap + s.n_out] = s.t; }
+      s.n_out++;
+      if (s.t >= p.tstop - p.bptol || (p.max_steps > 0 && s.accepted >= p.max_steps)) {
+        s.phase = PH_DONE;
+        return;
+      }
+    } else {
+      s.rejected++;
+      s.lastOk = 0;
+      s.nef++;
+      for (int i = 1; i <= s.order; ++i) s.psi[i - 1] = s.psi[i];
+      if (s.nef >= 15) { s.phase = PH_FAILED; s.newton_status = -1; return; }
+      double hnew;
+      if (status <= 0) {
+        hnew = s.h / 8; s.order = 1;
+      } else if (s.nef == 1) {
+        s.order = 1;
+        double rr = pow(0.5 / (s.estOverTol + 0.0001), 1.0 / (s.order + 1.0));
+        rr = fmax(0.25, fmin(0.9, rr));
+        hnew = rr * s.h;
+      } else {
+        hnew = 0.25 * s.h; s.order = 1;
+      }
+      hnew = fmin(fmax(hnew, p.hmin), p.hmax);
+      if (s.t + hnew > s.stopTime) hnew = s.stopTime - s.t;
+      s.h = hnew;
+      s.tsum = s.h + s.lastTimeStep;
+      if (!(s.h > 0.0)) { s.phase = PH_FAILED; s.newton_status = -2; return; }
+    }
+  }
+  int init_hist = 0;
+  start_next_step(s, p, init_hist);
+  s.init_hist = init_hist;
+}
+
+// OneStep::updateHistory (N_TIA_OneStep.C:1390-1440), OneStep::initialize history
+// (:1800-1830) and obtainPredictor (:135-175), per row.
+__global__ void k_history(DevArrays d, int n, int cap, int pmax) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int c = d.circ_of_row[r];
+  const CircState &s = d.cs[c];
+  if (s.accept == 3) { d.x[r] = 0.0; return; }
+  if (!s.step_end && !s.start_step) return;
+  const bool accepted_tran = s.accept == 1;
+  const bool accepted_dc = s.accept == 2;
+  if (accepted_tran) {
+    if (s.order == 2) { d.xh2[r] = d.xh1[r]; d.qh2[r] = d.FmB[r]; }
+    d.xh1[r] = d.x[r] - d.xcurr[r];
+    d.qh1[r] = d.Qv[r] - d.qh0[r];
+  }
+  if (accepted_tran || accepted_dc) {
+    const double xr = d.x[r];
+    d.xcurr[r] = xr;
+    d.qh0[r] = d.Qv[r];
+    d.Qc[r] = d.Qv[r];
+    d.FmBc[r] = d.FmB[r];
+    const int pj = d.probe_idx[r];
+    if (pj >= 0 && s.n_out - 1 < cap) d.out_v[((size_t)c * cap + (s.n_out - 1)) * pmax + pj] = xr;
+  }
+  if (s.start_step && s.phase == PH_TRAN) {
+    const TranParams &p = *d.tp;
+    if (s.init_hist) {  // OneStep::initialize history
+      d.xh1[r] = 0.0;
+      d.qh1[r] = -d.FmBc[r] * s.h;
+      d.qh0[r] = d.Qc[r];
+    }
+    const double xc = d.xcurr[r];
+    double xn = xc + s.beta[1] * d.xh1[r];
+    if (s.order == 2) xn += s.beta[2] * d.xh2[r];
+    d.xn0[r] = xn;
+    d.x[r] = xn;
+    d.solwt[r] = p.nl_reltol * fmax(fabs(xn), fabs(xc)) + p.nl_abstol;
+  }
+}
+
+// Accepted store/state become current (curr <- next) for accepted circuits.
+__global__ void k_state_commit(DevArrays d, int nm, int nd, int sto_base_m) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nm) {
+    const CircState &s = d.cs[d.m1_circ[i]];
+    if (s.accept == 1 || s.accept == 2) {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) d.sto_curr[sto_base_m + k * nm + i] = d.sto_next[sto_base_m + k * nm + i];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) d.sta_curr[k * nm + i] = d.sta_next[k * nm + i];
+    }
+  } else if (i < nm + nd) {
+    const int j = i - nm;
+    const CircState &s = d.cs[d.d_circ[j]];
+    if (s.accept == 1 || s.accept == 2) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) d.sto_curr[k * nd + j] = d.sto_next[k * nd + j];
+    }
+  }
+}
+
+// Number of finished circuits (done or failed) and the LU breakdown flag,
+// into mapped host memory read by the driver between tick batches.
+__global__ void k_count_done(DevArrays d, int ncirc, const int *breakdown, int *status_out) {
+  __shared__ int cnt;
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  int local = 0;
+  for (int c = threadIdx.x; c < ncirc; c += blockDim.x) {
+    int ph = d.cs[c].phase;
+    local += (ph == PH_DONE || ph == PH_FAILED) ? 1 : 0;
+  }
+  atomicAdd(&cnt, local);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    status_out[0] = cnt;
+    status_out[1] = *breakdown;
+  }
+}
+
+// Circuits parked by an LU breakdown resume their phase after the host re-pivots.
+__global__ void k_unstall(DevArrays d, int ncirc) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncirc) return;
+  CircState &s = d.cs[c];
+  if (s.phase == PH_STALL) {
+    s.phase = s.stall_prev;
+    s.singular = 0;
+  } else {
+    // the other circuits already finished this tick: clear its events so the
+    // resumed factor/solve/update/step/history launches leave them untouched
+    s.need_solve = 0; s.step_end = 0; s.accept = 0; s.start_step = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers.
+static inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
+
+void launch_sources_k(cudaStream_t st, const DevArrays &d, int n_v, int n_src, int use_explicit,
+                      double t) {
+  if (n_src > 0) k_sources<<<nblk(n_src, 128), 128, 0, st>>>(d, n_v, n_src, use_explicit, t);
+}
+void launch_mos1_k(cudaStream_t st, const DevArrays &d, int nm, int sto_base, int combined, int masked,
+                   int it, int flags, int sF, int sQ, int sL, int sM) {
+  if (nm > 0)
+    k_mos1<<<nblk(nm, 128), 128, 0, st>>>(d, nm, sto_base, combined, masked, it, flags, sF, sQ, sL, sM);
+}
+void launch_diode_k(cudaStream_t st, const DevArrays &d, int nd, int combined, int masked, int it,
+                    int flags, int sF, int sQ, int sL, int sM) {
+  if (nd > 0)
+    k_diode<<<nblk(nd, 128), 128, 0, st>>>(d, nd, combined, masked, it, flags, sF, sQ, sL, sM);
+}
+void launch_assemble_k(cudaStream_t st, const DevArrays &d, int n, int nnz) {
+  k_assemble_rows<<<nblk(n, kRowBlock), kRowBlock, 0, st>>>(d, n);
+  k_assemble_J<<<nblk(nnz, 256), 256, 0, st>>>(d, nnz);
+}
+void launch_load_vectors_k(cudaStream_t st, const DevArrays &d, int n, const double *x, double *Q,
+                           double *F, double *B, double *dFv, double *dQv, int lt) {
+  k_load_vectors<<<nblk(n, 256), 256, 0, st>>>(d, n, x, Q, F, B, dFv, dQv, lt);
+}
+void launch_load_matrices_k(cudaStream_t st, const DevArrays &d, int nnz, double *dQdx, double *dFdx,
+                            int lt) {
+  k_load_matrices<<<nblk(nnz, 256), 256, 0, st>>>(d, nnz, dQdx, dFdx, lt);
+}
+void launch_newton_ctl_k(cudaStream_t st, const DevArrays &d, int ncirc) {
+  k_newton_ctl<<<nblk(ncirc, 4), 128, 0, st>>>(d, ncirc);
+}
+void launch_update_k(cudaStream_t st, const DevArrays &d, int n) {
+  k_update<<<nblk(n, kRowBlock), kRowBlock, 0, st>>>(d, n);
+}
+void launch_step_ctl_k(cudaStream_t st, const DevArrays &d, int ncirc, const double *bps,
+                       const int *bp_ptr, int cap) {
+  k_step_ctl<<<nblk(ncirc, 4), 128, 0, st>>>(d, ncirc, bps, bp_ptr, cap);
+}
+void launch_history_k(cudaStream_t st, const DevArrays &d, int n, int cap, int pmax) {
+  k_history<<<nblk(n, 256), 256, 0, st>>>(d, n, cap, pmax);
+}
+void launch_state_commit_k(cudaStream_t st, const DevArrays &d, int nm, int nd, int sto_base_m) {
+  if (nm + nd > 0) k_state_commit<<<nblk(nm + nd, 256), 256, 0, st>>>(d, nm, nd, sto_base_m);
+}
+void launch_count_done_k(cudaStream_t st, const DevArrays &d, int ncirc, const int *breakdown,
+                         int *status_out) {
+  k_count_done<<<1, 256, 0, st>>>(d, ncirc, breakdown, status_out);
+}
+void launch_unstall_k(cudaStream_t st, const DevArrays &d, int ncirc) {
+  k_unstall<<<nblk(ncirc, 128), 128, 0, st>>>(d, ncirc);
+}
+
+}  // namespace xg

@@ -1,0 +1,447 @@
+// xg_symbolic.cpp — host analysis for the frozen-pattern GPU LU.
+//
+// Replaces the symbolic part of the KLU path Xyce takes through Amesos
+// (src/LinearAlgebraServicesPKG/N_LAS_AmesosSolver.C:309-335: symbolic
+// factorization once per pattern) with an analysis designed for a
+// level-scheduled GPU refactorization:
+//   1. row matching from the current values (a nonzero, large diagonal;
+//      voltage-source branch rows swap with their node rows),
+//   2. peeling of row singletons to the front and column singletons to the
+//      back (the 1x1 blocks a block-triangular form would find: ideal
+//      voltage sources to ground and their branch currents),
+//   3. nested dissection of the remaining core (BFS level-set bisection,
+//      each connected component — e.g. each circuit of a batch — apart),
+//   4. Gilbert-Peierls symbolic factorization of the permuted matrix, and
+//   5. level schedules for the left-looking factorization and for the
+//      row-oriented L and U solves.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <functional>
+#include <numeric>
+#include <deque>
+#include <queue>
+
+#include "xg_internal.h"
+
+namespace xg {
+namespace {
+
+struct Csc {
+  std::vector<int> cp, ri, src;  // src = CSR index of the entry
+};
+
+Csc to_csc(int n, const std::vector<int> &rp, const std::vector<int> &ci) {
+  Csc c;
+  c.cp.assign(n + 1, 0);
+  for (int e = 0; e < (int)ci.size(); ++e) c.cp[ci[e] + 1]++;
+  for (int j = 0; j < n; ++j) c.cp[j + 1] += c.cp[j];
+  c.ri.resize(ci.size());
+  c.src.resize(ci.size());
+  std::vector<int> nxt(c.cp.begin(), c.cp.end() - 1);
+  for (int i = 0; i < n; ++i)
+    for (int e = rp[i]; e < rp[i + 1]; ++e) {
+      int q = nxt[ci[e]]++;
+      c.ri[q] = i;
+      c.src[q] = e;
+    }
+  return c;
+}
+
+// Maximum transversal preferring large entries: diagonal when it passes the
+// 1e-3 threshold of its column, then greedy by magnitude, then augmenting
+// paths (MC21-style depth-first search) for what is left.
+bool match_rows(int n, const Csc &A, const std::vector<double> &vals, std::vector<int> &row_of_col,
+                std::string &err) {
+  std::vector<int> col_of_row(n, -1);
+  row_of_col.assign(n, -1);
+  std::vector<double> colmax(n, 0.0);
+  for (int j = 0; j < n; ++j)
+    for (int q = A.cp[j]; q < A.cp[j + 1]; ++q) colmax[j] = std::max(colmax[j], std::fabs(vals[A.src[q]]));
+  for (int j = 0; j < n; ++j)
+    for (int q = A.cp[j]; q < A.cp[j + 1]; ++q)
+      if (A.ri[q] == j) {
+        double a = std::fabs(vals[A.src[q]]);
+        if (a > 0 && a >= 1e-3 * colmax[j]) { row_of_col[j] = j; col_of_row[j] = j; }
+      }
+  for (int j = 0; j < n; ++j) {
+    if (row_of_col[j] >= 0) continue;
+    int best = -1;
+    double bv = 0.0;
+    for (int q = A.cp[j]; q < A.cp[j + 1]; ++q) {
+      int i = A.ri[q];
+      double a = std::fabs(vals[A.src[q]]);
+      if (col_of_row[i] < 0 && a > bv) { bv = a; best = i; }
+    }
+    if (best >= 0) { row_of_col[j] = best; col_of_row[best] = j; }
+  }
+  // Augmenting paths for the unmatched columns (MC21: depth-first search with
+  // a look-ahead for a free row at every visited column).  A first pass uses
+  // only numerically nonzero entries; structural zeros are a last resort.
+  std::vector<int> visited(n, -1), cols, pos, via;
+  std::vector<char> looked;
+  int stamp = 0;
+  for (int j0 = 0; j0 < n; ++j0) {
+    if (row_of_col[j0] >= 0) continue;
+    int found = -1;
+    for (int pass = 0; pass < 2 && found < 0; ++pass) {
+      const bool allow_zero = pass == 1;
+      ++stamp;
+      cols.assign(1, j0);
+      pos.assign(1, A.cp[j0]);
+      looked.assign(1, 0);
+      via.clear();
+      while (!cols.empty()) {
+        const int L = (int)cols.size() - 1;
+        const int j = cols[L];
+        if (!looked[L]) {
+          looked[L] = 1;
+          for (int q = A.cp[j]; q < A.cp[j + 1]; ++q) {
+            const int i = A.ri[q];
+            if (col_of_row[i] < 0 && (allow_zero || vals[A.src[q]] != 0.0)) { found = i; break; }
+          }
+          if (found >= 0) break;
+        }
+        if (pos[L] >= A.cp[j + 1]) {
+          cols.pop_back();
+          pos.pop_back();
+          looked.pop_back();
+          if (!via.empty() && via.size() >= cols.size()) via.pop_back();
+          continue;
+        }
+        const int q = pos[L]++;
+        const int i = A.ri[q];
+        if (visited[i] == stamp || col_of_row[i] < 0) continue;
+        if (!allow_zero && vals[A.src[q]] == 0.0) continue;
+        visited[i] = stamp;
+        via.push_back(i);
+        cols.push_back(col_of_row[i]);
+        pos.push_back(A.cp[col_of_row[i]]);
+        looked.push_back(0);
+      }
+    }
+    if (found < 0) {
+      char buf[128];
+      snprintf(buf, sizeof buf, "structurally singular matrix: column %d has no matching row", j0);
+      err = buf;
+      return false;
+    }
+    const int L = (int)cols.size() - 1;
+    row_of_col[cols[L]] = found;
+    col_of_row[found] = cols[L];
+    for (int k = L - 1; k >= 0; --k) {
+      row_of_col[cols[k]] = via[k];
+      col_of_row[via[k]] = cols[k];
+    }
+  }
+  return true;
+}
+
+// Nested dissection by BFS level-set bisection on the graph adj restricted to
+// the nodes with part[v] == id.  Appends an elimination order to out.
+struct ND {
+  const std::vector<std::vector<int>> &adj;
+  std::vector<int> part, dist;
+  int next_id = 1;
+  std::vector<int> &out;
+  static constexpr int kLeaf = 8;
+  ND(const std::vector<std::vector<int>> &a, std::vector<int> &o) : adj(a), out(o) {
+    part.assign(a.size(), 0);
+    dist.assign(a.size(), -1);
+  }
+
+  // BFS inside subset `id` from `src`; returns visit order and fills levels.
+  void bfs(int src, int id, std::vector<int> &order, std::vector<int> &lvl_ptr) {
+    order.clear();
+    lvl_ptr.assign(1, 0);
+    order.push_back(src);
+    dist[src] = 0;
+    size_t head = 0;
+    int cur = 0;
+    while (head < order.size()) {
+      int v = order[head++];
+      if (dist[v] != cur) { lvl_ptr.push_back((int)head - 1); cur = dist[v]; }
+      for (int w : adj[v])
+        if (part[w] == id && dist[w] < 0) { dist[w] = dist[v] + 1; order.push_back(w); }
+    }
+    lvl_ptr.push_back((int)order.size());
+    for (int v : order) dist[v] = -1;
+  }
+
+  void run(std::vector<int> nodes, int id) {
+    if ((int)nodes.size() <= kLeaf) {
+      for (int v : nodes) { out.push_back(v); part[v] = -1; }
+      return;
+    }
+    std::vector<int> order, lvl;
+    bfs(nodes[0], id, order, lvl);
+    if (order.size() < nodes.size()) {
+      // disconnected: split off each component
+      std::vector<std::vector<int>> comps;
+      for (int v : nodes) {
+        if (part[v] != id) continue;
+        std::vector<int> o, l;
+        bfs(v, id, o, l);
+        int cid = next_id++;
+        for (int w : o) part[w] = cid;
+        comps.push_back(o);
+      }
+      for (auto &cmp : comps) run(cmp, part[cmp[0]]);
+      return;
+    }
+    // pseudo-peripheral node: two sweeps
+    int start = order.back();
+    for (int sweep = 0; sweep < 2; ++sweep) {
+      bfs(start, id, order, lvl);
+      int lo = lvl[lvl.size() - 2];
+      int best = order[lo];
+      for (int k = lo; k < (int)order.size(); ++k)
+        if (adj[order[k]].size() < adj[best].size()) best = order[k];
+      start = best;
+    }
+    bfs(start, id, order, lvl);
+    int nl = (int)lvl.size() - 1;
+    if (nl < 3) {
+      for (int v : nodes) { out.push_back(v); part[v] = -1; }
+      return;
+    }
+    int half = (int)order.size() / 2, m = 1;
+    for (int k = 1; k < nl - 1; ++k) {
+      m = k;
+      if (lvl[k + 1] >= half) break;
+    }
+    int ida = next_id++, idb = next_id++;
+    std::vector<int> A(order.begin(), order.begin() + lvl[m]);
+    std::vector<int> S(order.begin() + lvl[m], order.begin() + lvl[m + 1]);
+    std::vector<int> B(order.begin() + lvl[m + 1], order.end());
+    for (int v : A) part[v] = ida;
+    for (int v : B) part[v] = idb;
+    for (int v : S) part[v] = -1;
+    run(A, ida);
+    run(B, idb);
+    for (int v : S) out.push_back(v);
+  }
+};
+
+}  // namespace
+
+int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &ci,
+                    const std::vector<double> &vals, LUHost &out, std::string &err) {
+  out = LUHost();
+  out.n = n;
+  Csc A = to_csc(n, rp, ci);
+  std::vector<int> row_of_col;
+  if (!match_rows(n, A, vals, row_of_col, err)) return XG_ERR_SINGULAR;
+  std::vector<int> inv(n);  // A row -> M index
+  for (int j = 0; j < n; ++j) inv[row_of_col[j]] = j;
+  // M = rows permuted: M row j = A row row_of_col[j].  Build M's row and column lists.
+  std::vector<std::vector<int>> mrow(n), mcol(n);
+  for (int j = 0; j < n; ++j)
+    for (int q = A.cp[j]; q < A.cp[j + 1]; ++q) {
+      int r = inv[A.ri[q]];
+      mrow[r].push_back(j);
+      mcol[j].push_back(r);
+    }
+  // singleton peeling
+  std::vector<int> rowcnt(n), colcnt(n);
+  std::vector<char> removed(n, 0);
+  for (int j = 0; j < n; ++j) { rowcnt[j] = (int)mrow[j].size(); colcnt[j] = (int)mcol[j].size(); }
+  std::vector<int> front, back;
+  std::deque<std::pair<int, int>> q;
+  for (int j = 0; j < n; ++j) {
+    if (rowcnt[j] == 1) q.push_back({j, 0});
+    if (colcnt[j] == 1) q.push_back({j, 1});
+  }
+  auto remove = [&](int j) {
+    removed[j] = 1;
+    for (int r : mcol[j])
+      if (r != j && !removed[r] && --rowcnt[r] == 1) q.push_back({r, 0});
+    for (int c : mrow[j])
+      if (c != j && !removed[c] && --colcnt[c] == 1) q.push_back({c, 1});
+  };
+  while (!q.empty()) {
+    auto [j, kind] = q.front();
+    q.pop_front();
+    if (removed[j]) continue;
+    if (kind == 0 && rowcnt[j] == 1) { front.push_back(j); remove(j); }
+    else if (kind == 1 && colcnt[j] == 1) { back.push_back(j); remove(j); }
+  }
+  // core graph (symmetrized, without the diagonal)
+  std::vector<std::vector<int>> adj(n);
+  for (int j = 0; j < n; ++j) {
+    if (removed[j]) continue;
+    for (int c : mrow[j])
+      if (c != j && !removed[c]) { adj[j].push_back(c); adj[c].push_back(j); }
+  }
+  std::vector<int> core;
+  for (int j = 0; j < n; ++j)
+    if (!removed[j]) {
+      auto &a = adj[j];
+      std::sort(a.begin(), a.end());
+      a.erase(std::unique(a.begin(), a.end()), a.end());
+      core.push_back(j);
+    }
+  std::vector<int> order;
+  order.reserve(n);
+  for (int j : front) order.push_back(j);
+  if (!core.empty()) {
+    ND nd(adj, order);
+    for (int j = 0; j < n; ++j) nd.part[j] = removed[j] ? -1 : 0;
+    nd.run(core, 0);
+  }
+  for (auto it = back.rbegin(); it != back.rend(); ++it) order.push_back(*it);
+  if ((int)order.size() != n) {
+    err = "ordering lost unknowns";
+    return XG_ERR_STATE;
+  }
+  std::vector<int> qinv(n);
+  for (int p = 0; p < n; ++p) qinv[order[p]] = p;
+  out.row_of_step.resize(n);
+  out.col_of_step.resize(n);
+  for (int p = 0; p < n; ++p) {
+    out.col_of_step[p] = order[p];
+    out.row_of_step[p] = row_of_col[order[p]];
+  }
+  // A' = Q^T M Q columns in step indices
+  std::vector<std::vector<int>> acol(n);
+  for (int p = 0; p < n; ++p) {
+    int j = order[p];
+    for (int q2 = A.cp[j]; q2 < A.cp[j + 1]; ++q2) acol[p].push_back(qinv[inv[A.ri[q2]]]);
+  }
+  // Gilbert-Peierls symbolic: pattern of column p = reach of A'(:,p) through L.
+  std::vector<std::vector<int>> Lcol(n);  // rows > k of each finished column
+  out.cp.assign(n + 1, 0);
+  out.diag.assign(n, -1);
+  std::vector<int> mark(n, -1), stk, pos;
+  std::vector<int> colrows;
+  for (int p = 0; p < n; ++p) {
+    colrows.clear();
+    for (int r0 : acol[p]) {
+      if (mark[r0] == p) continue;
+      stk.assign(1, r0);
+      mark[r0] = p;
+      while (!stk.empty()) {
+        int r = stk.back();
+        stk.pop_back();
+        colrows.push_back(r);
+        if (r < p)
+          for (int i : Lcol[r])
+            if (mark[i] != p) { mark[i] = p; stk.push_back(i); }
+      }
+    }
+    std::sort(colrows.begin(), colrows.end());
+    if (!std::binary_search(colrows.begin(), colrows.end(), p)) {
+      err = "missing structural diagonal after matching";
+      return XG_ERR_SINGULAR;
+    }
+    for (int r : colrows)
+      if (r > p) Lcol[p].push_back(r);
+    out.ri.insert(out.ri.end(), colrows.begin(), colrows.end());
+    out.cp[p + 1] = (int)out.ri.size();
+    out.diag[p] = out.cp[p] + (int)(std::lower_bound(colrows.begin(), colrows.end(), p) - colrows.begin());
+    if ((long long)out.ri.size() > 1900000000LL) {
+      err = "LU fill exceeds the int32 index range";
+      return XG_ERR_UNSUPPORTED;
+    }
+  }
+  const long long nnz = (long long)out.ri.size();
+  // value sources
+  out.src.assign(nnz, -1);
+  for (int p = 0; p < n; ++p) {
+    int j = order[p];
+    for (int q2 = A.cp[j]; q2 < A.cp[j + 1]; ++q2) {
+      int r = qinv[inv[A.ri[q2]]];
+      auto b = out.ri.begin() + out.cp[p], e = out.ri.begin() + out.cp[p + 1];
+      auto it = std::lower_bound(b, e, r);
+      out.src[it - out.ri.begin()] = A.src[q2];
+    }
+  }
+  // factor levels: column p after every k with U(k,p) != 0
+  std::vector<int> flev(n, 0);
+  int fmaxl = 0;
+  for (int p = 0; p < n; ++p) {
+    int l = 0;
+    for (int t = out.cp[p]; t < out.diag[p]; ++t) l = std::max(l, flev[out.ri[t]] + 1);
+    flev[p] = l;
+    fmaxl = std::max(fmaxl, l);
+  }
+  // row structures for the solves
+  std::vector<int> lcnt(n, 0), ucnt(n, 0);
+  for (int p = 0; p < n; ++p) {
+    for (int t = out.cp[p]; t < out.diag[p]; ++t) ucnt[out.ri[t]]++;      // U(k,p): row k
+    for (int t = out.diag[p] + 1; t < out.cp[p + 1]; ++t) lcnt[out.ri[t]]++;  // L(i,p): row i
+  }
+  out.l_ptr.assign(n + 1, 0);
+  out.u_ptr.assign(n + 1, 0);
+  for (int i = 0; i < n; ++i) { out.l_ptr[i + 1] = out.l_ptr[i] + lcnt[i]; out.u_ptr[i + 1] = out.u_ptr[i] + ucnt[i]; }
+  out.l_pos.resize(out.l_ptr[n]); out.l_col.resize(out.l_ptr[n]);
+  out.u_pos.resize(out.u_ptr[n]); out.u_col.resize(out.u_ptr[n]);
+  std::vector<int> lf(out.l_ptr.begin(), out.l_ptr.end() - 1), uf(out.u_ptr.begin(), out.u_ptr.end() - 1);
+  for (int p = 0; p < n; ++p) {
+    for (int t = out.cp[p]; t < out.diag[p]; ++t) {
+      int k = out.ri[t];
+      out.u_pos[uf[k]] = t; out.u_col[uf[k]++] = p;
+    }
+    for (int t = out.diag[p] + 1; t < out.cp[p + 1]; ++t) {
+      int i = out.ri[t];
+      out.l_pos[lf[i]] = t; out.l_col[lf[i]++] = p;
+    }
+  }
+  std::vector<int> llev(n, 0), ulev(n, 0);
+  int lmax = 0, umax = 0;
+  for (int i = 0; i < n; ++i) {
+    int l = 0;
+    for (int t = out.l_ptr[i]; t < out.l_ptr[i + 1]; ++t) l = std::max(l, llev[out.l_col[t]] + 1);
+    llev[i] = l;
+    lmax = std::max(lmax, l);
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    int l = 0;
+    for (int t = out.u_ptr[k]; t < out.u_ptr[k + 1]; ++t) l = std::max(l, ulev[out.u_col[t]] + 1);
+    ulev[k] = l;
+    umax = std::max(umax, l);
+  }
+  auto buckets = [&](const std::vector<int> &lev, int maxl, std::vector<int> &ptr, std::vector<int> &items) {
+    ptr.assign(maxl + 2, 0);
+    for (int v : lev) ptr[v + 1]++;
+    for (int l = 0; l <= maxl; ++l) ptr[l + 1] += ptr[l];
+    items.resize(lev.size());
+    std::vector<int> f(ptr.begin(), ptr.end() - 1);
+    for (int v = 0; v < (int)lev.size(); ++v) items[f[lev[v]]++] = v;
+  };
+  // Host trial factorization with the analysis values: a column whose
+  // frozen pivot fails the threshold test even right after re-pivoting is
+  // exempt from that test on the device (re-pivoting cannot improve it; a
+  // typical case is a structurally present but zero U row).
+  out.exempt.assign(n, 0);
+  {
+    std::vector<double> lu(nnz);
+    for (int p = 0; p < n; ++p) {
+      const int p0 = out.cp[p], p1 = out.cp[p + 1], pd = out.diag[p];
+      for (int t = p0; t < p1; ++t) lu[t] = out.src[t] >= 0 ? vals[out.src[t]] : 0.0;
+      for (int t = p0; t < pd; ++t) {
+        const int k = out.ri[t];
+        const double ukj = lu[t];
+        if (ukj == 0.0) continue;
+        for (int q2 = out.diag[k] + 1; q2 < out.cp[k + 1]; ++q2) {
+          auto it = std::lower_bound(out.ri.begin() + t + 1, out.ri.begin() + p1, out.ri[q2]);
+          lu[it - out.ri.begin()] -= lu[q2] * ukj;
+        }
+      }
+      const double d = lu[pd];
+      double amax = 0.0;
+      for (int t = pd; t < p1; ++t) amax = std::max(amax, std::fabs(lu[t]));
+      if (!(std::fabs(d) >= 1e-3 * amax)) out.exempt[p] = 1;
+      if (d != 0.0)
+        for (int t = pd + 1; t < p1; ++t) lu[t] /= d;
+    }
+  }
+  if (n > 0) {
+    buckets(flev, fmaxl, out.f_lvl_ptr, out.f_cols);
+    buckets(llev, lmax, out.l_lvl_ptr, out.l_rows);
+    buckets(ulev, umax, out.u_lvl_ptr, out.u_rows);
+  }
+  return XG_OK;
+}
+
+}  // namespace xg
