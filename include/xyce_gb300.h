@@ -187,6 +187,16 @@ typedef struct xg_tran_stats {
  * Any output pointer may be NULL when cap == 0. */
 int xg_transient(xg_ctx *ctx, const xg_tran_params *p, int n_probe, const int *probes,
                  int cap, int *counts, double *times, double *values, xg_tran_stats *stats);
+/* The same run in stages, for callers that stream results or time windows:
+ * xg_tran_start computes the operating point and the first analysis;
+ * xg_tran_advance runs until every circuit has accepted n_steps more steps
+ * (n_steps <= 0: to tstop); xg_tran_results copies outputs and statistics so
+ * far; xg_tran_end releases the run.  xg_transient = start + advance + results + end. */
+int xg_tran_start(xg_ctx *ctx, const xg_tran_params *p, int n_probe, const int *probes, int cap);
+int xg_tran_advance(xg_ctx *ctx, int n_steps);
+int xg_tran_results(xg_ctx *ctx, int *counts, double *times, double *values, xg_tran_stats *stats);
+int xg_tran_end(xg_ctx *ctx);
+
 /* Operating point only; x_host receives the n solution values. */
 int xg_dcop(xg_ctx *ctx, double *x_host, int *iters);
 

@@ -73,6 +73,7 @@ def lib():
         L.orc_transient.argtypes = [P, C.POINTER(TranParams), C.c_int, ip, C.c_int, dp, dp,
                                     C.POINTER(C.c_int), C.POINTER(TranStats)]
         L.orc_dcop.argtypes = [P, dp, C.POINTER(C.c_int)]
+        L.orc_set_wall_log.argtypes = [P, C.c_void_p, C.c_int]
         _lib = L
     return _lib
 
@@ -147,8 +148,14 @@ class Oracle:
         st = lib().orc_dcop(self.h, x, C.byref(it))
         return st, x, it.value
 
-    def transient(self, tran=None, probes=None, cap=2_000_000):
+    def transient(self, tran=None, probes=None, cap=2_000_000, wall_log=None):
+        """Transient run; wall_log (float64 array) receives the wall-clock
+        seconds at each accepted step when given."""
         tran = tran or self.netlist.tran
+        if wall_log is not None:
+            lib().orc_set_wall_log(self.h, wall_log.ctypes.data, len(wall_log))
+        else:
+            lib().orc_set_wall_log(self.h, None, 0)
         probes = np.asarray(probes if probes is not None else [], np.int32)
         tp = TranParams(tran.tstart, tran.tstop, tran.hmax, tran.hmin, tran.reltol,
                         tran.abstol, tran.nl_reltol, tran.nl_abstol, tran.nl_deltaxtol,

@@ -19,7 +19,9 @@ int ks_solve(int n, const int *row_ptr, const int *col_idx, const double *vals,
   double *rhs = (double *)malloc(sizeof(double) * (n + 1));
   double *sol = (double *)malloc(sizeof(double) * (n + 1));
   for (int i = 0; i < n; ++i) rhs[i + 1] = b[i];
-  int st = spOrderAndFactor(m, NULL, 1.0e-3, 0.0, 1, 1);
+  /* RelThreshold 1e-3, AbsThreshold 1e-13, DiagPivoting: the defaults of
+   * Epetra_CrsKundertSparse.h:130-132 */
+  int st = spOrderAndFactor(m, NULL, 1.0e-3, 1.0e-13, 1, 1);
   if (st == 0) {
     spSolve(m, rhs, sol, NULL, NULL);
     for (int i = 0; i < n; ++i) x[i] = sol[i + 1];

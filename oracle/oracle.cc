@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <map>
 #include <vector>
 
@@ -92,8 +93,13 @@ void wave_breakpoints(const Wave &w, double tstop, std::vector<double> &bp) {
 
 // ---------------------------------------------------------------------------
 // Sparse LU: Gilbert-Peierls left-looking factorization with threshold
-// partial pivoting (tol 1e-3, diagonal preferred) — KLU's algorithm as
-// called by N_LAS_AmesosSolver.C:309-396 with re-pivoting on every factor.
+// partial pivoting, diagonal preferred — KLU's algorithm as called by
+// N_LAS_AmesosSolver.C:309-396 with re-pivoting on every factor.  The
+// diagonal-preference threshold is 0.1, not KLU's default 0.001: at 0.001 the
+// operating-point Jacobian of a ring oscillator (weak diagonals, a cyclic
+// chain of transconductances) grows by ~100 per eliminated stage and the
+// solve loses every digit.
+static const double kPivotTol = 0.1;
 struct SparseLU {
   int n = 0;
   std::vector<int> Lp, Li, Up, Ui;   // L by columns (unit diag implicit), U by columns (diag last)
@@ -160,7 +166,7 @@ struct SparseLU {
         }
       }
       if (ipiv < 0 || amax <= 0.0 || !std::isfinite(amax)) return -1;
-      if (pinv[k] < 0 && flag[k] == k && std::fabs(x[k]) >= 1e-3 * amax) ipiv = k;
+      if (pinv[k] < 0 && flag[k] == k && std::fabs(x[k]) >= kPivotTol * amax) ipiv = k;
       double piv = x[ipiv];
       for (int t = top; t < n; ++t) {
         int r = topo[t];
@@ -218,6 +224,8 @@ struct orc_ctx {
   SparseLU lu;
   int nsta = 0, nsto = 0;
   int last_limited = 0;  // devices whose junction voltages were limited in the last load
+  double *wall_log = nullptr;  // optional: wall-clock seconds at each accepted step
+  int wall_cap = 0;
   bool finalized = false;
   // state layout: store diode [vd,qd,cd] then mos1 [vbd,vbs,vgs,vds,von,gm];
   // state mos1 [capgs,capgd,capgb,qgs,qgd,qgb,qbd,qbs]  (field-major, SoA)
@@ -888,6 +896,7 @@ extern "C" int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, 
       w.xcurr = w.x; w.sta_curr = w.sta_next; w.sto_curr = w.sto_next;
       Fc = w.F; Qc = w.Q; Bc = w.B;
       record(t, w.xcurr);
+      if (c->wall_log && st->accepted <= c->wall_cap) c->wall_log[st->accepted - 1] = now() - tstart_wall;
     } else {
       // OneStep::rejectStep (:1946-2105) and restoreHistory (:1540)
       st->rejected++;
@@ -918,4 +927,12 @@ extern "C" int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, 
   st->time_total = now() - tstart_wall;
   *n_out = nout;
   return st->status;
+}
+
+// Benchmark support: wall-clock time (seconds since the start of the
+// transient call) at every accepted step, into buf[0 .. cap).
+extern "C" int orc_set_wall_log(orc_ctx *c, double *buf, int cap) {
+  c->wall_log = buf;
+  c->wall_cap = cap;
+  return 0;
 }

@@ -91,6 +91,9 @@ int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, const int *
 /* Operating point only (x out, length n_unknowns). */
 int orc_dcop(orc_ctx *c, double *x, int *iters);
 
+/* Benchmark support: record wall-clock seconds at each accepted step. */
+int orc_set_wall_log(orc_ctx *c, double *buf, int cap);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,155 @@
+"""CPU tests of the oracle (the checker of the GPU path).
+
+Pins, in the absence of the reference's own regression waveforms (they live in
+the separate Xyce_Regression repository, not in the reference tree):
+  * known answers of the reference's unit-test netlists
+    (test/CircuitPKG/TestNetlist1.cir: V(1) = 5; TestNetlist2.cir: V(1) = sin(2 pi t),
+    V(2) = V(1)*100/150),
+  * an analytic RC step response,
+  * finite-difference Jacobians of every device load (the reference's TESTJAC
+    check, src/DeviceModelPKG/Core/N_DEV_NumericalJacobian.C:154),
+  * the sparse LU against Kundert Sparse compiled from the reference's sources
+    (golden fixture tests/golden/ksparse_solves.npz) and against scipy.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spl
+
+from xyce_gb300 import netlist as N
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ksparse_solves.npz")
+
+
+def test_testnetlist1_dc_value(oracle_mod):
+    nl = N.test_netlist1()
+    t, v, st = oracle_mod.Oracle(nl).transient(probes=[nl.names["1"]])
+    assert st["status"] == 0 and st["t_final"] == pytest.approx(1.0)
+    np.testing.assert_array_equal(v[:, 0], 5.0)
+
+
+def test_testnetlist2_analytic(oracle_mod):
+    nl = N.test_netlist2()
+    t, v, st = oracle_mod.Oracle(nl).transient(probes=[nl.names["1"], nl.names["2"]])
+    assert st["status"] == 0
+    np.testing.assert_allclose(v[:, 0], np.sin(2 * np.pi * t), atol=1e-12)
+    np.testing.assert_allclose(v[:, 1], np.sin(2 * np.pi * t) * 100 / 150, atol=1e-12)
+
+
+def test_rc_step_within_reltol(oracle_mod):
+    nl = N.rc_step(r=1e3, c=1e-9, v=1.0, tstop=5e-6)
+    t, v, st = oracle_mod.Oracle(nl).transient(probes=[nl.names["out"]])
+    ref = 1.0 - np.exp(-np.maximum(t - 1e-12, 0.0) / 1e-6)
+    # TIMEINT RELTOL 1e-3 on a 1 V signal: the LTE control keeps the error near it
+    assert np.max(np.abs(v[:, 0] - ref)) < 1e-3
+
+
+def _fd_check(oracle_mod, nl, rng, dcop):
+    o = oracle_mod.Oracle(nl)
+    _, x0, _ = o.dcop()
+    x = x0 + 0.05 * rng.standard_normal(o.n)
+    z = np.zeros(max(1, o.nsta))
+    base = o.load(x, dcop=dcop, sta_curr=z, sto_curr=np.zeros(max(1, o.nsto)), newton_iter=0)
+    # history equal to the point itself: no limiting, and the back-averaged
+    # Meyer charge has its capacitance as exact derivative
+    sta_c, sto_c = base["sta_next"], base["sto_next"]
+    ref = o.load(x, dcop=dcop, sta_curr=sta_c, sto_curr=sto_c, sto_prev=sto_c, newton_iter=1)
+    J = {k: sp.csr_matrix((ref[k], o.col_idx, o.row_ptr), shape=(o.n, o.n)).toarray()
+         for k in ("dFdx", "dQdx")}
+    for j in range(o.n):
+        h = 1e-7 * (1.0 + abs(x[j]))
+        xp, xm = x.copy(), x.copy()
+        xp[j] += h
+        xm[j] -= h
+        lp = o.load(xp, dcop=dcop, sta_curr=sta_c, sto_curr=sto_c, sto_prev=sto_c, newton_iter=1)
+        lm = o.load(xm, dcop=dcop, sta_curr=sta_c, sto_curr=sto_c, sto_prev=sto_c, newton_iter=1)
+        for vec, mat in (("F", "dFdx"), ("Q", "dQdx")):
+            fd = (lp[vec] - lm[vec]) / (2 * h)
+            an = J[mat][:, j]
+            scale = np.max(np.abs(J[mat])) + 1e-300
+            np.testing.assert_allclose(fd, an, rtol=1e-4, atol=1e-5 * scale,
+                                       err_msg=f"{nl.label} {mat}[:, {j}]")
+
+
+@pytest.mark.parametrize("maker", [lambda: N.diode_ladder(8, seed=3),
+                                   lambda: N.ring_oscillator(5),
+                                   lambda: N.ring_oscillator(5, caps=True)])
+def test_finite_difference_jacobian(oracle_mod, maker):
+    rng = np.random.default_rng(7)
+    _fd_check(oracle_mod, maker(), rng, dcop=False)
+
+
+def test_lu_matches_ksparse_golden(oracle_mod):
+    """The oracle's LU reproduces the reference solver's own solutions."""
+    sys.path.insert(0, os.path.dirname(__file__))
+    from golden.make_golden import circuits
+    g = np.load(GOLDEN)
+    specs = {name: nl for name, nl, _ in circuits()}
+    for name in g["names"]:
+        rp, ci, vals, b, xk = (g[f"{name}.{k}"] for k in ("row_ptr", "col_idx", "vals", "b", "x_ksparse"))
+        o = oracle_mod.Oracle(specs[str(name)])
+        np.testing.assert_array_equal(o.row_ptr, rp)
+        np.testing.assert_array_equal(o.col_idx, ci)
+        x = o.lu_solve(vals, b)
+        np.testing.assert_allclose(x, xk, rtol=1e-9, atol=1e-12 * np.max(np.abs(xk)), err_msg=str(name))
+
+
+def test_oracle_lu_matches_scipy_and_ksparse(oracle_mod):
+    rng = np.random.default_rng(5)
+    for nl, h in [(N.ring_oscillator(31), 1e-12), (N.diode_ladder(40, seed=2), 1e-9),
+                  (N.ring_oscillator(21, caps=True), 1e-12), (N.power_grid(10, 10), 1e-12)]:
+        o = oracle_mod.Oracle(nl)
+        _, x0, _ = o.dcop()
+        ld = o.load(x0 + 0.01 * rng.standard_normal(o.n))
+        for vals in (ld["dFdx"] + ld["dQdx"] / h, ld["dFdx"]):
+            b = rng.standard_normal(o.n)
+            A = sp.csr_matrix((vals, o.col_idx, o.row_ptr), shape=(o.n, o.n))
+            x = o.lu_solve(vals, b)
+            assert np.linalg.norm(A @ x - b) <= 1e-10 * np.linalg.norm(b)
+        if os.path.exists(oracle_mod.KSPARSE_PATH):
+            vals = ld["dFdx"] + ld["dQdx"] / h
+            b = rng.standard_normal(o.n)
+            xk = oracle_mod.ksparse_solve(o.row_ptr, o.col_idx, vals, b)
+            np.testing.assert_allclose(o.lu_solve(vals, b), xk, rtol=1e-8,
+                                       atol=1e-12 * np.max(np.abs(xk)))
+
+
+def test_ring_dc_operating_point_symmetric(oracle_mod):
+    """An odd ring has one DC solution: every stage at the inverter's switching
+    point, where the NMOS and PMOS saturation currents are equal."""
+    nl = N.ring_oscillator(11)
+    st, x, it = oracle_mod.Oracle(nl).dcop()
+    assert st > 0
+    v = x[[nl.names[f"n{i + 1}"] for i in range(11)]]
+    bn = 120e-6 * 2 / 0.18
+    bp = 40e-6 * 4 / 0.18
+    vm = (1.3 * np.sqrt(bp) + 0.5 * np.sqrt(bn)) / (np.sqrt(bn) + np.sqrt(bp))
+    np.testing.assert_allclose(v, vm, atol=1e-6)
+
+
+def test_ring_oscillates(oracle_mod):
+    nl = N.ring_oscillator(21)
+    nl.tran.tstop = 5e-9
+    t, v, st = oracle_mod.Oracle(nl).transient(probes=[nl.names["n5"]])
+    assert st["status"] == 0
+    assert v[:, 0].max() > 1.7 and v[:, 0].min() < 0.1
+
+
+def test_diode_iv_point(oracle_mod):
+    """Diode from a 1 V source through 1 kohm: Id = IS (exp(Vd/Vt) - 1), KVL."""
+    nl = N.Netlist(label="diode_iv")
+    a, k = nl.node("a"), nl.node("k")
+    nl.V(a, -1, N.WAVE_DC, [1.0])
+    nl.R(a, k, 1e3)
+    nl.D(k, -1, IS=1e-14, N=1.0)
+    st, x, it = oracle_mod.Oracle(nl).dcop()
+    vd = x[k]
+    vt = 1.3806226e-23 * 300.15 / 1.6021918e-19
+    i_r = (1.0 - vd) / 1e3
+    i_d = 1e-14 * np.expm1(vd / vt) + 1e-12 * vd
+    # the operating-point Newton stops at RHSTOL = 1e-6 A (N_NLS_Manager.C:1033)
+    assert abs(i_r - i_d) < 1e-6
+    assert 0.55 < vd < 0.75

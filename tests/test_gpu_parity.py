@@ -1,0 +1,224 @@
+"""GPU parity tests: the CUDA path through the C-ABI against the CPU oracle.
+
+Tolerances (written here, used below):
+  * device stamps (F, Q, B, limiter vectors, dFdx, dQdx, state, store):
+    |gpu - ref| <= 1e-12 * max(|gpu|, |ref|) + STAMP_FLOOR, where the floor
+    absorbs cancellation on values that are zero in exact arithmetic
+    (e.g. Isat*(exp(vd/vt)-1) near vd = 0, the sum of a node's stamps);
+  * linear solves: relative error 1e-9 against Kundert Sparse compiled from
+    the reference (golden fixture) and against scipy;
+  * waveforms: at the oracle's accepted time points (GPU waveform linearly
+    interpolated), |dv| <= 1e-6 * max|v| + 1e-9 (reltol 1e-6 of the target
+    forms), and the accepted/rejected step counts agree.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spl
+
+from xyce_gb300 import netlist as N
+
+pytestmark = pytest.mark.gpu
+
+STAMP_RTOL = 1e-12
+STAMP_FLOOR = 1e-20
+WAVE_RTOL, WAVE_ATOL = 1e-6, 1e-9
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ksparse_solves.npz")
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _t(torch, a):
+    return torch.as_tensor(np.ascontiguousarray(a, np.float64), device="cuda:0")
+
+
+def _assert_stamps(name, g, r, floor=STAMP_FLOOR):
+    tol = STAMP_RTOL * np.maximum(np.abs(g), np.abs(r)) + floor
+    bad = np.abs(g - r) > tol
+    assert not bad.any(), f"{name}: {np.count_nonzero(bad)} entries, worst {np.max(np.abs(g - r)[bad])}"
+
+
+def _loader_case(xg, oracle_mod, torch, nl, seed, newton_iter, dcop, init_jct, consistent_caps):
+    c = xg.Circuit(nl)
+    o = oracle_mod.Oracle(nl)
+    assert (c.n, c.nnz, c.nsta, c.nsto) == (o.n, o.nnz, o.nsta, o.nsto)
+    np.testing.assert_array_equal(c.row_ptr, o.row_ptr)
+    np.testing.assert_array_equal(c.col_idx, o.col_idx)
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-0.4, 2.0, o.n)
+    sta_c = rng.standard_normal(max(1, o.nsta)) * 1e-15
+    if not consistent_caps:
+        sta_c[:] = 0.0  # models without gate capacitance only ever hold zero gate states
+    sto_c = rng.uniform(-1.0, 1.9, max(1, o.nsto))
+    sto_p = rng.uniform(-1.0, 1.9, max(1, o.nsto))
+    t = 0.7e-9
+    ref = o.load(x, time=t, sta_curr=sta_c, sto_curr=sto_c, sto_prev=sto_p,
+                 newton_iter=newton_iter, dcop=dcop, init_jct=init_jct)
+    xs, stac, stoc = _t(torch, x), _t(torch, sta_c), _t(torch, sto_c)
+    stan, ston = torch.zeros_like(stac), _t(torch, sto_p)
+    c.update_sources(t)
+    flags = (xg.FLAG_DCOP if dcop else 0) | (xg.FLAG_INITJCT if init_jct else 0)
+    c.update_state(xs, stac, stoc, stan, ston, newton_iter=newton_iter, flags=flags)
+    z = lambda k: torch.zeros(k, dtype=torch.float64, device="cuda:0")
+    Q, F, B, dF, dQ = (z(c.n) for _ in range(5))
+    c.load_dae_vectors(xs, Q, F, B, dF, dQ)
+    dQdx, dFdx = z(c.nnz), z(c.nnz)
+    c.load_dae_matrices(dQdx, dFdx)
+    torch.cuda.synchronize()
+    got = dict(F=F, Q=Q, B=B, dFdxdVp=dF, dQdxdVp=dQ, dFdx=dFdx, dQdx=dQdx, sta_next=stan, sto_next=ston)
+    for k, v in got.items():
+        _assert_stamps(f"{nl.label}:{k}", v.cpu().numpy(), ref[k])
+    # loadType: LINEAR + NONLINEAR == ALL
+    Q1, F1, B1, dF1, dQ1 = (z(c.n) for _ in range(5))
+    c.load_dae_vectors(xs, Q1, F1, B1, dF1, dQ1, xg.LOAD_LINEAR)
+    c.load_dae_vectors(xs, Q1, F1, B1, dF1, dQ1, xg.LOAD_NONLINEAR)
+    a1, b1 = z(c.nnz), z(c.nnz)
+    c.load_dae_matrices(a1, b1, xg.LOAD_LINEAR)
+    c.load_dae_matrices(a1, b1, xg.LOAD_NONLINEAR)
+    torch.cuda.synchronize()
+    for x1, x0 in ((F1, F), (Q1, Q), (B1, B), (a1, dQdx), (b1, dFdx)):
+        np.testing.assert_allclose(x1.cpu().numpy(), x0.cpu().numpy(), rtol=1e-14, atol=1e-30)
+    c.close()
+
+
+@pytest.mark.parametrize("maker,caps", [
+    (lambda: N.diode_ladder(30, seed=3), False),
+    (lambda: N.ring_oscillator(11), False),
+    (lambda: N.ring_oscillator(11, caps=True), True),
+    (lambda: N.monte_carlo_rings(3, 11, 21, seed=2), False),
+    (lambda: N.power_grid(6, 5, seed=1), False),
+])
+@pytest.mark.parametrize("mode", ["tran0", "tran2", "dcop_init"])
+def test_device_stamps_match_oracle(xg, oracle_mod, torch_cuda, maker, caps, mode):
+    it, dcop, init = {"tran0": (0, False, False), "tran2": (2, False, False),
+                      "dcop_init": (0, True, True)}[mode]
+    _loader_case(xg, oracle_mod, torch_cuda, maker(), 11, it, dcop, init, caps)
+
+
+def test_lu_matches_ksparse_golden(xg, torch_cuda):
+    sys.path.insert(0, os.path.dirname(__file__))
+    from golden.make_golden import circuits
+    g = np.load(GOLDEN)
+    specs = {name: nl for name, nl, _ in circuits()}
+    for name in g["names"]:
+        vals, b, xk = (g[f"{name}.{k}"] for k in ("vals", "b", "x_ksparse"))
+        c = xg.Circuit(specs[str(name)])
+        np.testing.assert_array_equal(c.row_ptr, g[f"{name}.row_ptr"])
+        v, bb = _t(torch_cuda, vals), _t(torch_cuda, b)
+        x = torch_cuda.zeros_like(bb)
+        c.lu_analyze(v)
+        c.lu_factor(v)
+        c.lu_solve(bb, x)
+        torch_cuda.cuda.synchronize()
+        np.testing.assert_allclose(x.cpu().numpy(), xk, rtol=1e-9, atol=1e-12 * np.max(np.abs(xk)),
+                                   err_msg=str(name))
+        c.close()
+
+
+def test_lu_refactor_same_pattern_new_values(xg, oracle_mod, torch_cuda):
+    """Frozen pivots: analyze once, refactor with new values, solve."""
+    nl = N.ring_oscillator(101)
+    c = xg.Circuit(nl)
+    o = oracle_mod.Oracle(nl)
+    rng = np.random.default_rng(3)
+    _, x0, _ = o.dcop()
+    first = None
+    for k in range(4):
+        ld = o.load(x0 + 0.05 * rng.standard_normal(o.n))
+        vals = ld["dFdx"] + ld["dQdx"] / (1e-12 * (k + 1))
+        b = rng.standard_normal(o.n)
+        v, bb = _t(torch_cuda, vals), _t(torch_cuda, b)
+        if first is None:
+            c.lu_analyze(v)
+            first = True
+        c.lu_factor(v)
+        x = torch_cuda.zeros_like(bb)
+        c.lu_solve(bb, x)
+        torch_cuda.cuda.synchronize()
+        A = sp.csr_matrix((vals, o.col_idx, o.row_ptr), shape=(o.n, o.n))
+        xr = spl.spsolve(A.tocsc(), b)
+        np.testing.assert_allclose(x.cpu().numpy(), xr, rtol=1e-9, atol=1e-12 * np.max(np.abs(xr)))
+    c.close()
+
+
+def _compare_waveforms(t_ref, v_ref, t_gpu, v_gpu):
+    g = np.stack([np.interp(t_ref, t_gpu, v_gpu[:, j]) for j in range(v_gpu.shape[1])], axis=1)
+    err = np.max(np.abs(g - v_ref))
+    return err, WAVE_RTOL * np.max(np.abs(v_ref)) + WAVE_ATOL
+
+
+@pytest.mark.parametrize("name,maker,probes", [
+    ("testnetlist1", N.test_netlist1, ["1"]),
+    ("testnetlist2", N.test_netlist2, ["1", "2"]),
+    ("rc_step", N.rc_step, ["in", "out"]),
+    ("diode_ladder_50", lambda: N.diode_ladder(50, seed=5), ["n1", "n25", "n50"]),
+    ("ring_101", lambda: N.ring_oscillator(101), ["n1", "n50", "n101"]),
+    ("ring_21_caps", lambda: N.ring_oscillator(21, caps=True), ["n1", "n11"]),
+])
+def test_transient_matches_oracle(xg, oracle_mod, torch_cuda, name, maker, probes):
+    nl = maker()
+    pr = [nl.names[p] for p in probes]
+    counts, t, v, st = xg.Circuit(nl).transient(probes=pr, cap=400000)
+    to, vo, so = oracle_mod.Oracle(nl).transient(probes=pr)
+    assert st["status"] == 0 and so["status"] == 0
+    k = int(counts[0])
+    assert st["accepted"] == so["accepted"] and st["rejected"] == so["rejected"]
+    assert k == len(to)
+    err, tol = _compare_waveforms(to, vo, t[0, :k], v[0, :k])
+    assert err <= tol, (err, tol)
+
+
+def test_testnetlists_analytic_on_gpu(xg, torch_cuda):
+    nl = N.test_netlist1()
+    counts, t, v, st = xg.Circuit(nl).transient(probes=[nl.names["1"]], cap=1000)
+    np.testing.assert_array_equal(v[0, :counts[0], 0], 5.0)
+    nl = N.test_netlist2()
+    counts, t, v, st = xg.Circuit(nl).transient(probes=[nl.names["1"], nl.names["2"]], cap=1000)
+    k = counts[0]
+    np.testing.assert_allclose(v[0, :k, 0], np.sin(2 * np.pi * t[0, :k]), atol=1e-12)
+    np.testing.assert_allclose(v[0, :k, 1], np.sin(2 * np.pi * t[0, :k]) * 2 / 3, atol=1e-12)
+
+
+def test_batched_circuits_match_independent_runs(xg, oracle_mod, torch_cuda):
+    """Uneven Monte-Carlo rings in one batch: every circuit keeps its own step
+    control and matches the oracle run on that circuit alone."""
+    rng_count, lo, hi = 6, 11, 41
+    batch = N.monte_carlo_rings(rng_count, lo, hi, seed=21)
+    batch.tran.tstop = 3e-9
+    probes = [batch.names[f"c{i}.n1"] for i in range(rng_count)]
+    counts, t, v, st = xg.Circuit(batch).transient(probes=probes, cap=100000)
+    assert st["status"] == 0
+    for i in range(rng_count):
+        single = N.Netlist(label=f"single{i}")
+        # rebuild circuit i alone with the same devices
+        off0, off1 = batch.offsets[i], batch.offsets[i + 1]
+        remap = lambda u: -1 if u < 0 else u - off0
+        single.n = off1 - off0
+        single.names = {"n1": batch.names[f"c{i}.n1"] - off0}
+        for (a, b, val) in batch.cap:
+            if off0 <= max(a, b) < off1:
+                single.C(remap(a), remap(b), val)
+        for (a, b, br, kind, data) in batch.vsrc:
+            if off0 <= br < off1:
+                single.vsrc.append((remap(a), remap(b), remap(br), kind, data))
+        for (a, b, kind, data) in batch.isrc:
+            if off0 <= max(a, b) < off1:
+                single.isrc.append((remap(a), remap(b), kind, data))
+        for (d, g, s, bb, row) in batch.mos1:
+            if off0 <= d < off1:
+                single.mos1.append((remap(d), remap(g), remap(s), remap(bb), row))
+        single.tran = batch.tran
+        to, vo, so = oracle_mod.Oracle(single).transient(probes=[single.names["n1"]])
+        k = int(counts[i])
+        assert k == len(to), (i, k, len(to))
+        err, tol = _compare_waveforms(to, vo, t[i, :k], v[i, :k, :1])
+        assert err <= tol, (i, err, tol)

@@ -41,7 +41,8 @@ EXPORTED = [
     "xg_add_isources", "xg_add_diodes", "xg_add_mosfet1", "xg_finalize", "xg_get_sizes",
     "xg_get_pattern", "xg_update_sources", "xg_update_state", "xg_load_dae_vectors",
     "xg_load_dae_matrices", "xg_lu_analyze", "xg_lu_factor", "xg_lu_solve", "xg_lu_info",
-    "xg_transient", "xg_dcop", "xg_version",
+    "xg_transient", "xg_tran_start", "xg_tran_advance", "xg_tran_results", "xg_tran_end",
+    "xg_dcop", "xg_version",
 ]
 
 
@@ -114,6 +115,10 @@ def lib() -> C.CDLL:
     L.xg_lu_solve.argtypes = [P, P, P]
     L.xg_lu_info.argtypes = [P, C.POINTER(C.c_longlong), C.POINTER(I), C.POINTER(I), C.POINTER(I)]
     L.xg_transient.argtypes = [P, C.POINTER(TranParams), I, ip, I, ip, dp, dp, C.POINTER(TranStats)]
+    L.xg_tran_start.argtypes = [P, C.POINTER(TranParams), I, ip, I]
+    L.xg_tran_advance.argtypes = [P, I]
+    L.xg_tran_results.argtypes = [P, ip, dp, dp, C.POINTER(TranStats)]
+    L.xg_tran_end.argtypes = [P]
     L.xg_dcop.argtypes = [P, dp, C.POINTER(I)]
     L.xg_version.argtypes = []
     _lib = L
@@ -218,6 +223,44 @@ class Circuit:
         it = C.c_int()
         self._check(lib().xg_dcop(self.h, x, C.byref(it)))
         return x, it.value
+
+    def _tran_params(self, tran):
+        return TranParams(tran.tstart, tran.tstop, tran.hmax, tran.hmin, tran.reltol, tran.abstol,
+                          tran.nl_reltol, tran.nl_abstol, tran.nl_deltaxtol, tran.nl_rhstol,
+                          tran.nl_smallupdatetol, tran.nl_maxstep, tran.max_steps, tran.max_order)
+
+    def tran_start(self, tran=None, probes=(), cap=0):
+        """Operating point + first analysis; keeps the run resident for tran_advance."""
+        tran = tran or self.netlist.tran
+        probes = np.asarray(probes, np.int32)
+        self._run = (len(probes), cap, probes)
+        self._check(lib().xg_tran_start(self.h, C.byref(self._tran_params(tran)), len(probes),
+                                        probes, int(cap)))
+
+    def tran_advance(self, n_steps: int):
+        self._check(lib().xg_tran_advance(self.h, int(n_steps)))
+
+    def tran_results(self):
+        """(counts, times, values, stats) of the run so far."""
+        n_probe, cap, probes = self._run
+        nc = self.n_circuits
+        offs = np.asarray(self.netlist.offsets)
+        per = np.bincount(np.searchsorted(offs, probes, side="right") - 1, minlength=nc) \
+            if n_probe else np.zeros(nc, int)
+        pmax = max(1, int(per.max()) if len(per) else 1)
+        counts = np.zeros(nc, np.int32)
+        times = np.zeros(max(1, nc * cap))
+        values = np.zeros(max(1, nc * cap * pmax))
+        st = TranStats()
+        self._check(lib().xg_tran_results(self.h, counts, times, values, C.byref(st)))
+        stats = {f: getattr(st, f) for f, _ in TranStats._fields_}
+        if cap:
+            times = times[: nc * cap].reshape(nc, cap)
+            values = values[: nc * cap * pmax].reshape(nc, cap, pmax)
+        return counts, times, values, stats
+
+    def tran_end(self):
+        self._check(lib().xg_tran_end(self.h))
 
     def transient(self, tran=None, probes=(), cap=0):
         """Run the transient; returns (counts, times, values, stats) where

@@ -21,7 +21,10 @@ struct Wave {
   std::vector<double> d;
 };
 
+struct TranRun;
+
 struct xg_ctx {
+  TranRun *run = nullptr;          // transient in progress (xg_tran_start .. xg_tran_end)
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string err = "";
@@ -53,6 +56,8 @@ struct xg_ctx {
   int *status_dev = nullptr;
   int *breakdown_dev = nullptr;
 };
+
+void xg_free_run(xg_ctx *ctx);
 
 namespace {
 
@@ -125,7 +130,8 @@ int xg_create(xg_ctx **out, int device) {
   if (cudaSetDevice(device) != cudaSuccess) return XG_ERR_CUDA;
   xg_ctx *c = new xg_ctx;
   c->device = device;
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  // a blocking stream: ordered with work the caller issued on the legacy default stream
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamDefault) != cudaSuccess) {
     delete c;
     return XG_ERR_CUDA;
   }
@@ -144,6 +150,7 @@ int xg_destroy(xg_ctx *ctx) {
   if (!ctx) return XG_ERR_ARG;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  if (ctx->run) xg_free_run(ctx);
   free_list(ctx->lu_allocs);
   free_list(ctx->allocs);
   if (ctx->status_host) cudaFreeHost(ctx->status_host);
@@ -653,7 +660,7 @@ int xg_lu_factor(xg_ctx *ctx, const double *vals) {
   if (!ctx || !vals) return XG_ERR_ARG;
   if (!ctx->lu_ready) return fail(ctx, XG_ERR_STATE, "call xg_lu_analyze first");
   CK(cudaMemsetAsync(ctx->breakdown_dev, 0, sizeof(int), ctx->stream));
-  launch_lu_factor_k(ctx->stream, ctx->L, vals, ctx->d.cs, 0, 1e-3);
+  launch_lu_factor_k(ctx->stream, ctx->L, vals, ctx->d.cs, 0, kRuntimePivotTol);
   CK(cudaGetLastError());
   int bd = 0;
   CK(cudaMemcpyAsync(&bd, ctx->breakdown_dev, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -688,23 +695,33 @@ int xg_lu_info(xg_ctx *ctx, long long *nnz_lu, int *fl, int *ll, int *ul) {
 
 // ---------------------------------------------------------------------------
 // Device-resident transient driver.
-namespace {
-
-struct Run {
-  xg_ctx *ctx;
-  int cap, pmax;
+struct TranRun {
+  xg_ctx *ctx = nullptr;
+  int cap = 0, pmax = 1;
   double *bps = nullptr;
   int *bp_ptr = nullptr;
   cudaGraphExec_t exec = nullptr;
-  double pivot_tol = 1e-3;
+  double pivot_tol = kRuntimePivotTol;
   std::vector<void *> allocs;
-  ~Run() {
+  std::vector<int> pcount;
+  long long ticks = 0;
+  int batch = 4;
+  std::chrono::steady_clock::time_point t0;
+  ~TranRun() {
     if (exec) cudaGraphExecDestroy(exec);
     free_list(allocs);
+    if (ctx) { ctx->d.out_t = nullptr; ctx->d.out_v = nullptr; }
   }
 };
 
-void launch_front(Run &R) {
+void xg_free_run(xg_ctx *ctx) {
+  delete ctx->run;
+  ctx->run = nullptr;
+}
+
+namespace {
+
+void launch_front(TranRun &R) {
   xg_ctx *c = R.ctx;
   DevArrays &d = c->d;
   launch_sources_k(c->stream, d, c->nv, c->nv + c->ni, 0, 0.0);
@@ -714,7 +731,7 @@ void launch_front(Run &R) {
   launch_newton_ctl_k(c->stream, d, c->ncirc);
 }
 
-void launch_back(Run &R) {
+void launch_back(TranRun &R) {
   xg_ctx *c = R.ctx;
   DevArrays &d = c->d;
   launch_lu_factor_k(c->stream, c->L, d.J, d.cs, 1, R.pivot_tol);
@@ -725,7 +742,7 @@ void launch_back(Run &R) {
   launch_state_commit_k(c->stream, d, c->nm, c->nd, c->sto_base_m);
 }
 
-int capture(Run &R) {
+int capture(TranRun &R) {
   xg_ctx *ctx = R.ctx;
   if (R.exec) { cudaGraphExecDestroy(R.exec); R.exec = nullptr; }
   cudaGraph_t g;
@@ -759,36 +776,73 @@ void breakpoints(const Wave &w, double tstop, std::vector<double> &bp) {
   }
 }
 
+// Runs tick batches until every circuit is done, failed or paused; re-pivots
+// on LU breakdown.  One host synchronization per batch of ticks.
+int run_until_idle(TranRun &R) {
+  xg_ctx *ctx = R.ctx;
+  DevArrays &d = ctx->d;
+  const long long max_ticks = 400000000LL;
+  int consecutive = 0;
+  int rc = 0;
+  while (true) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    volatile int *st = ctx->status_host;
+    const int finished = st[0], breakdown = st[1];
+    if (breakdown) {
+      // frozen pivots failed: re-pivot from the parked Jacobian and resume it
+      consecutive++;
+      if (consecutive > 4) return fail(ctx, XG_ERR_SINGULAR, "LU keeps breaking down after re-pivoting");
+      if ((rc = lu_analyze_from_device(ctx, d.J))) return rc;
+      R.pivot_tol = (consecutive >= 2) ? 0.0 : kRuntimePivotTol;
+      if ((rc = capture(R))) return rc;
+      launch_unstall_k(ctx->stream, d, ctx->ncirc);
+      launch_back(R);
+      launch_count_done_k(ctx->stream, d, ctx->ncirc, ctx->breakdown_dev, ctx->status_dev);
+      CK(cudaGetLastError());
+      continue;
+    }
+    if (consecutive && R.pivot_tol == 0.0) {
+      R.pivot_tol = kRuntimePivotTol;
+      if ((rc = capture(R))) return rc;
+    }
+    consecutive = 0;
+    if (finished >= ctx->ncirc) return XG_OK;
+    if (R.ticks > max_ticks) return fail(ctx, XG_ERR_TIMEOUT, "transient exceeded the tick limit");
+    for (int k = 0; k < R.batch; ++k) CK(cudaGraphLaunch(R.exec, ctx->stream));
+    R.ticks += R.batch;
+    if (R.batch < 64) R.batch *= 2;
+  }
+}
+
 }  // namespace
 
-extern "C" int xg_transient(xg_ctx *ctx, const xg_tran_params *p, int n_probe, const int *probes, int cap,
-                            int *counts, double *times, double *values, xg_tran_stats *stats) {
+extern "C" int xg_tran_start(xg_ctx *ctx, const xg_tran_params *p, int n_probe, const int *probes, int cap) {
   if (!ctx || !p) return XG_ERR_ARG;
   if (!ctx->finalized) return fail(ctx, XG_ERR_STATE, "not finalized");
   if (!(p->tstop > p->tstart)) return fail(ctx, XG_ERR_ARG, "tstop must exceed tstart");
   if (cap < 0 || n_probe < 0) return fail(ctx, XG_ERR_ARG, "negative cap or probe count");
-  if (cap > 0 && (!counts || !times || (n_probe > 0 && !values))) return fail(ctx, XG_ERR_ARG, "output buffers required");
   CK(cudaSetDevice(ctx->device));
-  auto t0 = std::chrono::steady_clock::now();
-  const int n = ctx->n, ncirc = ctx->ncirc;
-  DevArrays &d = ctx->d;
-  Run R;
+  if (ctx->run) xg_free_run(ctx);
+  ctx->run = new TranRun;
+  TranRun &R = *ctx->run;
+  R.t0 = std::chrono::steady_clock::now();
   R.ctx = ctx;
   R.cap = cap;
-  // probes grouped by circuit
-  std::vector<int> probe_idx(n, -1), pcount(ncirc, 0);
+  const int n = ctx->n, ncirc = ctx->ncirc;
+  DevArrays &d = ctx->d;
+  std::vector<int> probe_idx(n, -1);
+  R.pcount.assign(ncirc, 0);
   for (int k = 0; k < n_probe; ++k) {
     if (probes[k] < 0 || probes[k] >= n) return fail(ctx, XG_ERR_ARG, "probe out of range");
     int c = ctx->circ_of_row[probes[k]];
-    probe_idx[probes[k]] = pcount[c]++;
+    probe_idx[probes[k]] = R.pcount[c]++;
   }
   R.pmax = 1;
-  for (int c = 0; c < ncirc; ++c) R.pmax = std::max(R.pmax, pcount[c]);
+  for (int c = 0; c < ncirc; ++c) R.pmax = std::max(R.pmax, R.pcount[c]);
   CK(cudaMemcpyAsync(d.probe_idx, probe_idx.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
   int rc = 0;
   if ((rc = dev_alloc(ctx, &d.out_t, (size_t)ncirc * std::max(cap, 1), R.allocs))) return rc;
   if ((rc = dev_alloc(ctx, &d.out_v, (size_t)ncirc * std::max(cap, 1) * R.pmax, R.allocs))) return rc;
-  // breakpoints per circuit
   std::vector<std::vector<double>> cb(ncirc);
   for (int k = 0; k < ctx->nv; ++k) breakpoints(ctx->v_w[k], p->tstop, cb[ctx->circ_of_row[ctx->v_b[k]]]);
   for (int k = 0; k < ctx->ni; ++k) {
@@ -806,7 +860,6 @@ extern "C" int xg_transient(xg_ctx *ctx, const xg_tran_params *p, int n_probe, c
   }
   if ((rc = dev_upload(ctx, &R.bps, bps, R.allocs))) return rc;
   if ((rc = dev_upload(ctx, &R.bp_ptr, bp_ptr, R.allocs))) return rc;
-  // parameters
   TranParams tp{};
   tp.tstart = p->tstart; tp.tstop = p->tstop;
   tp.hmax = p->hmax > 0 ? p->hmax : 0.1 * (p->tstop - p->tstart);
@@ -819,7 +872,6 @@ extern "C" int xg_transient(xg_ctx *ctx, const xg_tran_params *p, int n_probe, c
   tp.dc_reltol = 1e-3; tp.dc_abstol = 1e-12; tp.dc_deltaxtol = 1.0; tp.dc_rhstol = 1e-6; tp.dc_maxstep = 200;
   tp.dc_only = (p->max_steps < 0) ? 1 : 0;
   CK(cudaMemcpyAsync(d.tp, &tp, sizeof tp, cudaMemcpyHostToDevice, ctx->stream));
-  // circuit states: operating point first
   std::vector<CircState> cs(ncirc);
   for (auto &s : cs) {
     memset(&s, 0, sizeof s);
@@ -829,6 +881,7 @@ extern "C" int xg_transient(xg_ctx *ctx, const xg_tran_params *p, int n_probe, c
     s.qscale = 0.0; s.fscale = 1.0; s.hscale = 0.0;
     s.init_jct = 1;
     s.order = 1;
+    s.stop_at = 0;  // pause once the operating point is done
   }
   CK(cudaMemcpyAsync(d.cs, cs.data(), sizeof(CircState) * ncirc, cudaMemcpyHostToDevice, ctx->stream));
   for (double *v : {d.x, d.xcurr, d.xn0, d.dx, d.rhs, d.Qv, d.FmB, d.qh0, d.qh1, d.qh2, d.xh1, d.xh2, d.Qc, d.FmBc, d.solwt})
@@ -839,8 +892,8 @@ extern "C" int xg_transient(xg_ctx *ctx, const xg_tran_params *p, int n_probe, c
     CK(cudaMemsetAsync(v, 0, sizeof(double) * std::max(1, ctx->nsto), ctx->stream));
   CK(cudaMemsetAsync(ctx->breakdown_dev, 0, sizeof(int), ctx->stream));
   ctx->status_host[0] = ctx->status_host[1] = 0;
-  // first tick: evaluate and assemble, then analyze the Jacobian, then finish the tick
-  long long ticks = 1;
+  // first tick: evaluate and assemble, analyze that Jacobian, finish the tick
+  R.ticks = 1;
   launch_front(R);
   CK(cudaGetLastError());
   if ((rc = lu_analyze_from_device(ctx, d.J))) return rc;
@@ -848,55 +901,45 @@ extern "C" int xg_transient(xg_ctx *ctx, const xg_tran_params *p, int n_probe, c
   launch_back(R);
   launch_count_done_k(ctx->stream, d, ncirc, ctx->breakdown_dev, ctx->status_dev);
   CK(cudaGetLastError());
-  int batch = 4;
-  const long long max_ticks = 200000000LL;
-  int consecutive_reanalysis = 0;
-  while (true) {
-    CK(cudaStreamSynchronize(ctx->stream));
-    volatile int *st = ctx->status_host;
-    const int finished = st[0], breakdown = st[1];
-    if (breakdown) {
-      // frozen pivots failed: re-pivot from the parked Jacobian and resume
-      consecutive_reanalysis++;
-      if (consecutive_reanalysis > 4) return fail(ctx, XG_ERR_SINGULAR, "LU keeps breaking down after re-pivoting");
-      if ((rc = lu_analyze_from_device(ctx, d.J))) return rc;
-      R.pivot_tol = (consecutive_reanalysis >= 2) ? 0.0 : 1e-3;
-      if ((rc = capture(R))) return rc;
-      launch_unstall_k(ctx->stream, d, ncirc);
-      launch_back(R);
-      launch_count_done_k(ctx->stream, d, ncirc, ctx->breakdown_dev, ctx->status_dev);
-      CK(cudaGetLastError());
-      continue;
-    }
-    if (consecutive_reanalysis && R.pivot_tol == 0.0) {
-      R.pivot_tol = 1e-3;
-      if ((rc = capture(R))) return rc;
-    }
-    consecutive_reanalysis = 0;
-    if (finished >= ncirc) break;
-    if (ticks > max_ticks) return fail(ctx, XG_ERR_TIMEOUT, "transient exceeded the tick limit");
-    for (int k = 0; k < batch; ++k) CK(cudaGraphLaunch(R.exec, ctx->stream));
-    ticks += batch;
-    if (batch < 64) batch *= 2;
-  }
-  // results
+  return run_until_idle(R);
+}
+
+extern "C" int xg_tran_advance(xg_ctx *ctx, int n_steps) {
+  if (!ctx) return XG_ERR_ARG;
+  if (!ctx->run) return fail(ctx, XG_ERR_STATE, "call xg_tran_start first");
+  TranRun &R = *ctx->run;
+  launch_set_target_k(ctx->stream, ctx->d, ctx->ncirc, n_steps);
+  launch_count_done_k(ctx->stream, ctx->d, ctx->ncirc, ctx->breakdown_dev, ctx->status_dev);
+  CK(cudaGetLastError());
+  R.batch = 4;
+  return run_until_idle(R);
+}
+
+extern "C" int xg_tran_results(xg_ctx *ctx, int *counts, double *times, double *values, xg_tran_stats *stats) {
+  if (!ctx) return XG_ERR_ARG;
+  if (!ctx->run) return fail(ctx, XG_ERR_STATE, "call xg_tran_start first");
+  TranRun &R = *ctx->run;
+  const int ncirc = ctx->ncirc;
+  DevArrays &d = ctx->d;
   std::vector<CircState> out(ncirc);
   CK(cudaMemcpyAsync(out.data(), d.cs, sizeof(CircState) * ncirc, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  if (cap > 0) {
-    std::vector<double> ot((size_t)ncirc * cap), ov((size_t)ncirc * cap * R.pmax);
-    CK(cudaMemcpy(ot.data(), d.out_t, sizeof(double) * ot.size(), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(ov.data(), d.out_v, sizeof(double) * ov.size(), cudaMemcpyDeviceToHost));
+  const int cap = R.cap;
+  if (cap > 0 && counts && times) {
     for (int c = 0; c < ncirc; ++c) counts[c] = std::min(out[c].n_out, cap);
-    memcpy(times, ot.data(), sizeof(double) * ot.size());
-    if (n_probe > 0) memcpy(values, ov.data(), sizeof(double) * ov.size());
+    CK(cudaMemcpy(times, d.out_t, sizeof(double) * (size_t)ncirc * cap, cudaMemcpyDeviceToHost));
+    if (values) CK(cudaMemcpy(values, d.out_v, sizeof(double) * (size_t)ncirc * cap * R.pmax, cudaMemcpyDeviceToHost));
   }
   int status = 0;
+  for (auto &s : out)
+    if (s.phase == PH_FAILED) { status = s.newton_status ? s.newton_status : -1; break; }
   if (stats) {
     memset(stats, 0, sizeof *stats);
     stats->t_final_min = 1e300;
     stats->t_final_max = -1e300;
-    for (auto &s : out) {
+    long long evals = 0;
+    for (int c = 0; c < ncirc; ++c) {
+      const CircState &s = out[c];
       stats->accepted += s.accepted;
       stats->rejected += s.rejected;
       stats->newton_iters += s.newton_iters;
@@ -905,30 +948,42 @@ extern "C" int xg_transient(xg_ctx *ctx, const xg_tran_params *p, int n_probe, c
       stats->dcop_iters += s.dcop_iters;
       stats->t_final_min = std::min(stats->t_final_min, s.t);
       stats->t_final_max = std::max(stats->t_final_max, s.t);
-    }
-    stats->ticks = ticks;
-    stats->device_evals = 0;
-    stats->n_analyze = ctx->n_analyze;
-  }
-  for (auto &s : out)
-    if (s.phase == PH_FAILED) { status = s.newton_status ? s.newton_status : -1; break; }
-  if (stats) {
-    stats->status = status;
-    // instance evaluations: every Newton solve is followed by one device pass,
-    // and every step attempt / operating-point solve starts with one
-    long long evals = 0;
-    for (int c = 0; c < ncirc; ++c) {
-      const CircState &s = out[c];
+      // instance evaluations: one device pass per Newton solve, plus the
+      // first pass of every step attempt and of the operating point
       const long long passes = s.newton_iters + s.accepted + s.rejected + s.dcop_iters + 1;
       evals += (long long)ctx->inst_of_circ[c] * passes;
     }
+    stats->ticks = R.ticks;
     stats->device_evals = evals;
-    stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    stats->n_analyze = ctx->n_analyze;
+    stats->status = status;
+    stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - R.t0).count();
   }
-  d.out_t = nullptr;
-  d.out_v = nullptr;
   if (status) return fail(ctx, status, "a circuit failed to converge");
   return XG_OK;
+}
+
+extern "C" int xg_tran_end(xg_ctx *ctx) {
+  if (!ctx) return XG_ERR_ARG;
+  if (ctx->run) {
+    cudaStreamSynchronize(ctx->stream);
+    xg_free_run(ctx);
+  }
+  return XG_OK;
+}
+
+extern "C" int xg_transient(xg_ctx *ctx, const xg_tran_params *p, int n_probe, const int *probes, int cap,
+                            int *counts, double *times, double *values, xg_tran_stats *stats) {
+  if (!ctx || !p) return XG_ERR_ARG;
+  if (cap > 0 && (!counts || !times || (n_probe > 0 && !values))) return fail(ctx, XG_ERR_ARG, "output buffers required");
+  int rc = xg_tran_start(ctx, p, n_probe, probes, cap);
+  if (rc == XG_OK && p->max_steps >= 0) rc = xg_tran_advance(ctx, p->max_steps > 0 ? p->max_steps : 0);
+  int rr = XG_OK;
+  if (ctx->run) rr = xg_tran_results(ctx, counts, times, values, stats);
+  std::string keep = ctx->err;
+  xg_tran_end(ctx);
+  ctx->err = keep;
+  return rc ? rc : rr;
 }
 
 extern "C" int xg_dcop(xg_ctx *ctx, double *x_host, int *iters) {

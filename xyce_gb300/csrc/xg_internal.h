@@ -12,9 +12,12 @@ namespace xg {
 
 constexpr int kRowBlock = 256;       // rows per block of the row kernels (fixed: partial slots)
 constexpr int kMaxPwlScan = 1 << 20; // bound on PWL point scans
+// Frozen-pivot acceptance on the device: a pivot below this fraction of its
+// updated column triggers re-pivoting by the host.
+constexpr double kRuntimePivotTol = 1e-2;
 
 // Circuit phases of the device-resident state machine.
-enum Phase : int { PH_DC = 0, PH_TRAN = 1, PH_DONE = 2, PH_FAILED = 3, PH_STALL = 4 };
+enum Phase : int { PH_DC = 0, PH_TRAN = 1, PH_DONE = 2, PH_FAILED = 3, PH_STALL = 4, PH_PAUSED = 5 };
 
 // Per-circuit integrator / Newton state, one struct per circuit in HBM.
 // Field names follow StepErrorControl / OneStep / DampedNewton members.
@@ -42,6 +45,7 @@ struct CircState {
   int init_jct, init_hist, dc_stage, limited, bp_index, singular, stall_prev;
   // counters
   long long accepted, rejected, newton_iters, newton_fail, lte_fail, dcop_iters;
+  long long stop_at;   // pause once this many steps are accepted
   int n_out;
 };
 
@@ -172,6 +176,7 @@ void launch_state_commit_k(cudaStream_t st, const DevArrays &d, int nm, int nd, 
 void launch_count_done_k(cudaStream_t st, const DevArrays &d, int ncirc, const int *breakdown,
                          int *status_out);
 void launch_unstall_k(cudaStream_t st, const DevArrays &d, int ncirc);
+void launch_set_target_k(cudaStream_t st, const DevArrays &d, int ncirc, int n_steps);
 void launch_lu_factor_k(cudaStream_t st, const LUDev &L, const double *vals, CircState *cs, int masked,
                         double pivot_tol);
 void launch_lu_solve_k(cudaStream_t st, const LUDev &L, const double *b, double *x, const CircState *cs,

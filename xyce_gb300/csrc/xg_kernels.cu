@@ -880,6 +880,7 @@ __global__ void k_step_ctl(DevArrays d, int ncirc, const double *bps, const int 
   int init_hist = 0;
   start_next_step(s, p, init_hist);
   s.init_hist = init_hist;
+  if (s.accepted >= s.stop_at) s.phase = PH_PAUSED;  // the predictor is applied, then the circuit waits
 }
 
 // OneStep::updateHistory (N_TIA_OneStep.C:1390-1440), OneStep::initialize history
@@ -907,7 +908,7 @@ __global__ void k_history(DevArrays d, int n, int cap, int pmax) {
     const int pj = d.probe_idx[r];
     if (pj >= 0 && s.n_out - 1 < cap) d.out_v[((size_t)c * cap + (s.n_out - 1)) * pmax + pj] = xr;
   }
-  if (s.start_step && s.phase == PH_TRAN) {
+  if (s.start_step && (s.phase == PH_TRAN || s.phase == PH_PAUSED)) {
     const TranParams &p = *d.tp;
     if (s.init_hist) {  // OneStep::initialize history
       d.xh1[r] = 0.0;
@@ -953,7 +954,7 @@ __global__ void k_count_done(DevArrays d, int ncirc, const int *breakdown, int *
   int local = 0;
   for (int c = threadIdx.x; c < ncirc; c += blockDim.x) {
     int ph = d.cs[c].phase;
-    local += (ph == PH_DONE || ph == PH_FAILED) ? 1 : 0;
+    local += (ph == PH_DONE || ph == PH_FAILED || ph == PH_PAUSED) ? 1 : 0;
   }
   atomicAdd(&cnt, local);
   __syncthreads();
@@ -1028,6 +1029,19 @@ void launch_count_done_k(cudaStream_t st, const DevArrays &d, int ncirc, const i
                          int *status_out) {
   k_count_done<<<1, 256, 0, st>>>(d, ncirc, breakdown, status_out);
 }
+// Next advance: pause again after n_steps more accepted steps (unbounded if <= 0).
+__global__ void k_set_target(DevArrays d, int ncirc, int n_steps) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncirc) return;
+  CircState &s = d.cs[c];
+  s.stop_at = (n_steps > 0) ? s.accepted + n_steps : 0x7fffffffffffffffLL;
+  if (s.phase == PH_PAUSED) s.phase = PH_TRAN;
+}
+
+void launch_set_target_k(cudaStream_t st, const DevArrays &d, int ncirc, int n_steps) {
+  k_set_target<<<nblk(ncirc, 128), 128, 0, st>>>(d, ncirc, n_steps);
+}
+
 void launch_unstall_k(cudaStream_t st, const DevArrays &d, int ncirc) {
   k_unstall<<<nblk(ncirc, 128), 128, 0, st>>>(d, ncirc);
 }

@@ -5,9 +5,9 @@
 // Pivots are frozen by the host analysis (xg_symbolic.cpp); every column of
 // a level is independent, one warp per column, left-looking:
 //   load column j of A'  ->  for each U(k,j), k ascending: col_j -= L(:,k) * U(k,j)
-//   ->  threshold test of the diagonal against the updated column (KLU's
-//       partial-pivoting tolerance 1e-3); failing columns raise a breakdown
-//       flag so the host re-pivots  ->  L(:,j) /= U(j,j).
+//   ->  threshold test of the diagonal against the updated column
+//       (kRuntimePivotTol); failing columns raise a breakdown flag so the
+//       host re-pivots  ->  L(:,j) /= U(j,j).
 // The triangular solves are row-oriented (gather, no atomics), 8 lanes per row.
 #include <cuda_runtime.h>
 

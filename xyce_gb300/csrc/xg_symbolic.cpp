@@ -27,6 +27,11 @@
 namespace xg {
 namespace {
 
+// Diagonal preference of the row matching.  Weak diagonals (e.g. 1% of the
+// column, as in the operating point of a ring oscillator, where gds << gm)
+// are not kept: a static pivot that small compounds growth along a cycle.
+constexpr double kDiagPref = 0.1;
+
 struct Csc {
   std::vector<int> cp, ri, src;  // src = CSR index of the entry
 };
@@ -48,8 +53,8 @@ Csc to_csc(int n, const std::vector<int> &rp, const std::vector<int> &ci) {
   return c;
 }
 
-// Maximum transversal preferring large entries: diagonal when it passes the
-// 1e-3 threshold of its column, then greedy by magnitude, then augmenting
+// Maximum transversal preferring large entries: diagonal when it is at least
+// kDiagPref of its column's largest entry, then greedy by magnitude, then augmenting
 // paths (MC21-style depth-first search) for what is left.
 bool match_rows(int n, const Csc &A, const std::vector<double> &vals, std::vector<int> &row_of_col,
                 std::string &err) {
@@ -62,7 +67,7 @@ bool match_rows(int n, const Csc &A, const std::vector<double> &vals, std::vecto
     for (int q = A.cp[j]; q < A.cp[j + 1]; ++q)
       if (A.ri[q] == j) {
         double a = std::fabs(vals[A.src[q]]);
-        if (a > 0 && a >= 1e-3 * colmax[j]) { row_of_col[j] = j; col_of_row[j] = j; }
+        if (a > 0 && a >= kDiagPref * colmax[j]) { row_of_col[j] = j; col_of_row[j] = j; }
       }
   for (int j = 0; j < n; ++j) {
     if (row_of_col[j] >= 0) continue;
@@ -431,7 +436,7 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
       const double d = lu[pd];
       double amax = 0.0;
       for (int t = pd; t < p1; ++t) amax = std::max(amax, std::fabs(lu[t]));
-      if (!(std::fabs(d) >= 1e-3 * amax)) out.exempt[p] = 1;
+      if (!(std::fabs(d) >= kRuntimePivotTol * amax)) out.exempt[p] = 1;
       if (d != 0.0)
         for (int t = pd + 1; t < p1; ++t) lu[t] /= d;
     }

@@ -259,13 +259,22 @@ def _ring(nl: Netlist, stages: int, vdd=1.8, cload=5e-15, nmos=None, pmos=None,
     nl.I(-1, outs[0], WAVE_PWL, [0.0, 0.0, 10e-12, kick, 990e-12, kick, 1e-9, 0.0])
 
 
-def ring_oscillator(stages=101) -> Netlist:
+def ring_oscillator(stages=101, caps=False) -> Netlist:
     """CMOS ring oscillator of MOSFET level-1 inverters: VDD=1.8 V, NMOS VTO=0.5
     KP=120u, PMOS VTO=-0.5 KP=40u, W/L=2u/0.18u (PMOS W=4u), 5 fF per stage, a
-    1 ns PWL kick on node 1; .TRAN 0 20n, max step 5 p."""
+    1 ns PWL kick on node 1; .TRAN 0 20n, max step 5 p.
+
+    caps=True adds gate oxide (TOX), overlap and bulk-junction capacitances so
+    that the Meyer and junction-charge paths of the model are exercised."""
     assert stages % 2 == 1
-    nl = Netlist(label=f"ring_{stages}")
-    _ring(nl, stages)
+    nl = Netlist(label=f"ring_{stages}" + ("_caps" if caps else ""))
+    if caps:
+        extra = dict(TOX=4e-9, CGSO=2e-10, CGDO=2e-10, CGBO=1e-10, CJ=1e-3, CJSW=2e-10,
+                     MJ=0.45, MJSW=0.33, AD=1e-12, AS=1e-12, PD=4e-6, PS=4e-6, GAMMA=0.4,
+                     LAMBDA=0.05, PHI=0.7)
+        _ring(nl, stages, nmos=dict(NMOS_CARD, **extra), pmos=dict(PMOS_CARD, **extra))
+    else:
+        _ring(nl, stages)
     nl.tran = Tran(tstop=20e-9, hmax=5e-12)
     return nl
 
