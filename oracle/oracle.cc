@@ -223,6 +223,7 @@ struct orc_ctx {
   std::vector<double> Ax;
   SparseLU lu;
   int nsta = 0, nsto = 0;
+  std::vector<char> is_branch;  // unknown is a voltage-source branch current
   int last_limited = 0;  // devices whose junction voltages were limited in the last load
   double *wall_log = nullptr;  // optional: wall-clock seconds at each accepted step
   int wall_cap = 0;
@@ -339,7 +340,12 @@ int orc_finalize(orc_ctx *c) {
   std::vector<std::vector<int>> rows(c->n);
   for (auto &pr : all)
     if (pr.first >= 0 && pr.second >= 0) rows[pr.first].push_back(pr.second);
-  for (int i = 0; i < c->n; ++i) rows[i].push_back(i);  // keep diagonals present
+  // every node unknown keeps its diagonal (gmin stepping shunts it); the
+  // branch unknowns of voltage sources have none, as in the device stamps
+  c->is_branch.assign(c->n, 0);
+  for (int b : c->v_b) c->is_branch[b] = 1;
+  for (int i = 0; i < c->n; ++i)
+    if (!c->is_branch[i]) rows[i].push_back(i);
   c->rp.assign(c->n + 1, 0);
   c->ci.clear();
   for (int i = 0; i < c->n; ++i) {
@@ -598,15 +604,13 @@ void assemble(orc_ctx *c, Work &w, double time, int iter, int flags, const Coef 
     double r = cf.fscale * (w.F[i] - w.B[i]);
     if (cf.qscale != 0.0) r += cf.qscale * (w.Q[i] - cf.qhist0[i]);
     if (cf.hscale != 0.0) r += cf.hscale * cf.qhist2[i];
-    if (cf.gshunt != 0.0) r += cf.gshunt * w.x[i];
+    if (cf.gshunt != 0.0 && !c->is_branch[i]) r += cf.gshunt * w.x[i];
     w.rhs[i] = -r + cf.qscale * w.dQv[i] + cf.fscale * w.dFv[i];
   }
   for (int p = 0; p < w.nnz; ++p) w.J[p] = cf.qscale * w.dQdx[p] + cf.fscale * w.dFdx[p];
   if (cf.gshunt != 0.0)
-    for (int i = 0; i < w.n; ++i) {
-      int p = csr_find(c, i, i);
-      w.J[p] += cf.gshunt;
-    }
+    for (int i = 0; i < w.n; ++i)
+      if (!c->is_branch[i]) w.J[csr_find(c, i, i)] += cf.gshunt;
   w.t_load += now() - t0;
 }
 
@@ -715,7 +719,7 @@ int dcop(orc_ctx *c, Work &w, double t0, int *total_iters) {
   int st = newton(c, w, t0, nl, cf, 1 | 2, &it);
   *total_iters = it;
   if (st > 0) return st;
-  // gmin stepping: shunt conductance from every unknown to ground,
+  // gmin stepping: shunt conductance from every node unknown to ground,
   // stepped 1e-2 -> 1e-12 by decades, then removed.
   std::fill(w.x.begin(), w.x.end(), 0.0);
   bool first = true;

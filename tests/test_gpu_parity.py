@@ -74,7 +74,11 @@ def _loader_case(xg, oracle_mod, torch, nl, seed, newton_iter, dcop, init_jct, c
     dQdx, dFdx = z(c.nnz), z(c.nnz)
     c.load_dae_matrices(dQdx, dFdx)
     torch.cuda.synchronize()
-    got = dict(F=F, Q=Q, B=B, dFdxdVp=dF, dQdxdVp=dQ, dFdx=dFdx, dQdx=dQdx, sta_next=stan, sto_next=ston)
+    got = dict(F=F, Q=Q, B=B, dFdxdVp=dF, dQdxdVp=dQ, dFdx=dFdx, dQdx=dQdx)
+    if o.nsta:
+        got["sta_next"] = stan
+    if o.nsto:
+        got["sto_next"] = ston
     for k, v in got.items():
         _assert_stamps(f"{nl.label}:{k}", v.cpu().numpy(), ref[k])
     # loadType: LINEAR + NONLINEAR == ALL
@@ -190,10 +194,17 @@ def test_testnetlists_analytic_on_gpu(xg, torch_cuda):
 
 def test_batched_circuits_match_independent_runs(xg, oracle_mod, torch_cuda):
     """Uneven Monte-Carlo rings in one batch: every circuit keeps its own step
-    control and matches the oracle run on that circuit alone."""
+    control; its waveform is bit-for-bit the one of the same circuit run alone
+    on the GPU, and matches the oracle run on that circuit alone.
+
+    Tight tolerances (TIMEINT and Newton reltol 1e-6) are used: at the default
+    Newton RELTOL of 1e-2 two correct runs whose round-off differs may accept
+    different step sequences and drift apart in oscillation phase."""
     rng_count, lo, hi = 6, 11, 41
     batch = N.monte_carlo_rings(rng_count, lo, hi, seed=21)
-    batch.tran.tstop = 3e-9
+    batch.tran.tstop = 2e-9
+    batch.tran.reltol, batch.tran.abstol = 1e-6, 1e-9
+    batch.tran.nl_reltol, batch.tran.nl_abstol = 1e-6, 1e-9
     probes = [batch.names[f"c{i}.n1"] for i in range(rng_count)]
     counts, t, v, st = xg.Circuit(batch).transient(probes=probes, cap=100000)
     assert st["status"] == 0
@@ -217,8 +228,15 @@ def test_batched_circuits_match_independent_runs(xg, oracle_mod, torch_cuda):
             if off0 <= d < off1:
                 single.mos1.append((remap(d), remap(g), remap(s), remap(bb), row))
         single.tran = batch.tran
-        to, vo, so = oracle_mod.Oracle(single).transient(probes=[single.names["n1"]])
         k = int(counts[i])
-        assert k == len(to), (i, k, len(to))
-        err, tol = _compare_waveforms(to, vo, t[i, :k], v[i, :k, :1])
+        # the same circuit alone on the GPU
+        c1, t1, v1, s1 = xg.Circuit(single).transient(probes=[single.names["n1"]], cap=100000)
+        k1 = int(c1[0])
+        assert k == k1, (i, k, k1)
+        np.testing.assert_array_equal(t[i, :k], t1[0, :k1])
+        np.testing.assert_allclose(v[i, :k, 0], v1[0, :k1, 0], rtol=0, atol=1e-12)
+        to, vo, so = oracle_mod.Oracle(single).transient(probes=[single.names["n1"]])
+        assert abs(k - len(to)) <= 0.02 * len(to), (i, k, len(to))
+        err, _ = _compare_waveforms(to, vo, t[i, :k], v[i, :k, :1])
+        tol = 1e-3 * np.max(np.abs(vo))
         assert err <= tol, (i, err, tol)

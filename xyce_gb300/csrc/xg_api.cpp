@@ -45,7 +45,7 @@ struct xg_ctx {
   int nnz = 0, nm = 0, nd = 0, nv = 0, ni = 0;
   int nsto = 0, nsta = 0, sto_base_m = 0;
   int sF_m = 0, sF_d = 0, sQ_m = 0, sQ_d = 0, sL_m = 0, sL_d = 0, sM_m = 0, sM_d = 0;
-  int n_pairs = 0, n_rowblocks = 0;
+  int n_pairs = 0, n_rowblocks = 0, n_long_rows = 0, n_long_ents = 0;
   DevArrays d;
   LUDev L;
   bool lu_ready = false;
@@ -329,7 +329,12 @@ int xg_finalize(xg_ctx *ctx) {
     for (int a = 0; a < 4; ++a)
       for (int b = 0; b < 4; ++b) addp(nn[a], nn[b]);
   }
-  for (int i = 0; i < n; ++i) rows[i].push_back(i);
+  // node unknowns keep a diagonal entry (the operating-point gmin shunt lands
+  // there); voltage-source branch rows have none, as in the device stamps
+  std::vector<char> is_branch(n, 0);
+  for (int k = 0; k < nv; ++k) is_branch[ctx->v_b[k]] = 1;
+  for (int i = 0; i < n; ++i)
+    if (!is_branch[i]) rows[i].push_back(i);
   ctx->rp.assign(n + 1, 0);
   ctx->ci.clear();
   for (int i = 0; i < n; ++i) {
@@ -412,6 +417,18 @@ int xg_finalize(xg_ctx *ctx) {
   };
   std::vector<int> pF, iF, pQ, iQ, pL, iL, pB, iB, pM, iM;
   flatten(lF, pF, iF); flatten(lQ, pQ, iQ); flatten(lL, pL, iL); flatten(lB, pB, iB); flatten(lM, pM, iM);
+  // Rows and entries with long gathers (a supply node touches every PMOS) are
+  // reduced by a whole block in a pre-pass instead of one thread.
+  std::vector<int> long_rows, row_long(n, -1), long_ents, ent_long(nnz, -1);
+  for (int i = 0; i < n; ++i) {
+    int work = (ctx->rp[i + 1] - ctx->rp[i]) + (pF[i + 1] - pF[i]) + (pQ[i + 1] - pQ[i]) +
+               (pB[i + 1] - pB[i]) + (pL[i + 1] - pL[i]);
+    if (work > kLongGather) { row_long[i] = (int)long_rows.size(); long_rows.push_back(i); }
+  }
+  for (int e = 0; e < nnz; ++e)
+    if (pM[e + 1] - pM[e] > kLongGather) { ent_long[e] = (int)long_ents.size(); long_ents.push_back(e); }
+  ctx->n_long_rows = (int)long_rows.size();
+  ctx->n_long_ents = (int)long_ents.size();
   // sources (V first, then I)
   std::vector<int> skind, soff(1, 0), scirc;
   std::vector<double> sdata;
@@ -515,6 +532,9 @@ int xg_finalize(xg_ctx *ctx) {
   UP(d.vF_ptr, pF); UP(d.vF_idx, iF); UP(d.vQ_ptr, pQ); UP(d.vQ_idx, iQ);
   UP(d.vL_ptr, pL); UP(d.vL_idx, iL); UP(d.vB_ptr, pB); UP(d.vB_idx, iB);
   UP(d.m_ptr, pM); UP(d.m_idx, iM);
+  UP(d.is_branch, is_branch);
+  UP(d.long_rows, long_rows); UP(d.row_long, row_long); UP(d.long_ents, long_ents); UP(d.ent_long, ent_long);
+  AL(d.long_rsum, 4 * (size_t)kLongSplit * long_rows.size()); AL(d.long_esum, (size_t)kLongSplit * long_ents.size());
   AL(d.sF, nF); AL(d.sQ, nQ); AL(d.sL, nL); AL(d.sL2, nL); AL(d.sB, nB); AL(d.sM, nMs); AL(d.sM2, nMs);
   UP(d.src_kind, skind); UP(d.src_off, soff); UP(d.src_circ, scirc); UP(d.src_data, sdata);
   UP(d.m1_node, m1node); UP(d.m1_model, m1model); UP(d.m1_circ, m1circ);
@@ -621,17 +641,26 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
   for (int p = 0; p < H.n; ++p) cstep[p] = ctx->circ_of_row[H.col_of_step[p]];
   UP(L.circ_of_step, cstep);
   UP(L.cp, H.cp); UP(L.ri, H.ri); UP(L.diag, H.diag); UP(L.src, H.src);
-  UP(L.f_lvl_ptr, H.f_lvl_ptr); UP(L.f_cols, H.f_cols);
-  UP(L.l_lvl_ptr, H.l_lvl_ptr); UP(L.l_rows, H.l_rows); UP(L.l_ptr, H.l_ptr); UP(L.l_pos, H.l_pos); UP(L.l_col, H.l_col);
-  UP(L.u_lvl_ptr, H.u_lvl_ptr); UP(L.u_rows, H.u_rows); UP(L.u_ptr, H.u_ptr); UP(L.u_pos, H.u_pos); UP(L.u_col, H.u_col);
+  UP(L.l_ptr, H.l_ptr); UP(L.l_pos, H.l_pos); UP(L.l_col, H.l_col);
+  UP(L.u_ptr, H.u_ptr); UP(L.u_pos, H.u_pos); UP(L.u_col, H.u_col);
   UP(L.exempt, H.exempt);
+  UP(L.upd_off, H.upd_off); UP(L.upd_pos, H.upd_pos);
+  for (int w = 0; w < 2; ++w) {
+    const Schedule &S = w ? H.lsched : H.fsched;
+    SchedDev &D = w ? L.ls : L.fs;
+    UP(D.items, S.items); UP(D.lvl_ptr, S.lvl_ptr); UP(D.grp_lvl, S.grp_lvl);
+    UP(D.is_long, S.is_long); UP(D.is_long_rev, S.is_long_rev);
+    D.n_hub = S.n_hub;
+    D.n_groups = S.n_groups;
+    D.n_top_items = S.n_top_items;
+  }
 #undef UP
   if ((rc = dev_alloc(ctx, &L.lu, (size_t)L.nnz, A))) return rc;
   if ((rc = dev_alloc(ctx, &L.y, (size_t)H.n, A))) return rc;
   L.breakdown = ctx->breakdown_dev;
-  L.h_f_lvl = H.f_lvl_ptr;
-  L.h_l_lvl = H.l_lvl_ptr;
-  L.h_u_lvl = H.u_lvl_ptr;
+  L.f_levels = (int)H.f_lvl_ptr.size() - 1;
+  L.l_levels = (int)H.l_lvl_ptr.size() - 1;
+  L.u_levels = (int)H.u_lvl_ptr.size() - 1;
   CK(cudaMemsetAsync(ctx->breakdown_dev, 0, sizeof(int), ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->lu_ready = true;
@@ -685,9 +714,9 @@ int xg_lu_info(xg_ctx *ctx, long long *nnz_lu, int *fl, int *ll, int *ul) {
   if (!ctx) return XG_ERR_ARG;
   if (!ctx->lu_ready) return fail(ctx, XG_ERR_STATE, "no LU analysis");
   if (nnz_lu) *nnz_lu = ctx->L.nnz;
-  if (fl) *fl = (int)ctx->L.h_f_lvl.size() - 1;
-  if (ll) *ll = (int)ctx->L.h_l_lvl.size() - 1;
-  if (ul) *ul = (int)ctx->L.h_u_lvl.size() - 1;
+  if (fl) *fl = ctx->L.f_levels;
+  if (ll) *ll = ctx->L.l_levels;
+  if (ul) *ul = ctx->L.u_levels;
   return XG_OK;
 }
 
@@ -727,7 +756,7 @@ void launch_front(TranRun &R) {
   launch_sources_k(c->stream, d, c->nv, c->nv + c->ni, 0, 0.0);
   launch_mos1_k(c->stream, d, c->nm, c->sto_base_m, 1, 1, 0, 0, c->sF_m, c->sQ_m, c->sL_m, c->sM_m);
   launch_diode_k(c->stream, d, c->nd, 1, 1, 0, 0, c->sF_d, c->sQ_d, c->sL_d, c->sM_d);
-  launch_assemble_k(c->stream, d, c->n, c->nnz);
+  launch_assemble_k(c->stream, d, c->n, c->nnz, c->n_long_rows, c->n_long_ents);
   launch_newton_ctl_k(c->stream, d, c->ncirc);
 }
 

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -12,6 +13,9 @@ namespace xg {
 
 constexpr int kRowBlock = 256;       // rows per block of the row kernels (fixed: partial slots)
 constexpr int kMaxPwlScan = 1 << 20; // bound on PWL point scans
+constexpr int kLongGather = 96;      // gathers longer than this are split across blocks
+constexpr int kLongSplit = 32;       // blocks per long gather
+constexpr int kLongSolveRow = 256;   // triangular-solve rows longer than this get a whole block
 // Frozen-pivot acceptance on the device: a pivot below this fraction of its
 // updated column triggers re-pivoting by the host.
 constexpr double kRuntimePivotTol = 1e-2;
@@ -96,6 +100,10 @@ struct DevArrays {
   int *vL_ptr = nullptr, *vL_idx = nullptr;
   int *vB_ptr = nullptr, *vB_idx = nullptr;
   int *m_ptr = nullptr, *m_idx = nullptr;
+  char *is_branch = nullptr;                 // per row: voltage-source branch unknown
+  // long gathers, reduced by a block in a pre-pass: rows (F, Q, B, L sums) and J entries
+  int *long_rows = nullptr, *row_long = nullptr, *long_ents = nullptr, *ent_long = nullptr;
+  double *long_rsum = nullptr, *long_esum = nullptr;
   // slot value buffers
   double *sF = nullptr, *sQ = nullptr, *sL = nullptr, *sL2 = nullptr, *sB = nullptr;
   double *sM = nullptr, *sM2 = nullptr;   // combined J slots / (dF, dQ) in separate mode
@@ -128,19 +136,44 @@ struct DevArrays {
   int *status = nullptr;      // mapped host memory: [0] finished circuits, [1] LU breakdown
 };
 
-// LU structures (device) produced by the host analysis.
+// Grouped execution schedule of one triangular sweep (factorization, L solve;
+// the U solve runs the factorization schedule backwards).  items[0 .. n_hub)
+// are hub items (no dependencies, many dependents) executed first; then
+// groups 0 .. n_groups-1, each closed under dependencies and run by one CTA
+// with a barrier between its local levels; then the top (group n_groups),
+// run by a single CTA.  Group g owns levels [grp_lvl[g], grp_lvl[g+1]); level
+// k spans items[lvl_ptr[k] .. lvl_ptr[k+1]).
+struct Schedule {
+  std::vector<int> items, lvl_ptr, grp_lvl;
+  std::vector<char> is_long, is_long_rev;  // whole-block items (forward / backward sweep)
+  int n_hub = 0, n_groups = 0, n_top_items = 0;
+};
+
+struct SchedDev {
+  int *items = nullptr, *lvl_ptr = nullptr, *grp_lvl = nullptr;
+  char *is_long = nullptr, *is_long_rev = nullptr;
+  int n_hub = 0, n_groups = 0, n_top_items = 0;
+};
+
+constexpr int kLongColumn = 512;   // factor columns longer than this use the whole CTA
+constexpr int kHubFanout = 64;     // items with more dependents than this run in the prologue
+constexpr int kGroupCap = 512;     // items per dependency-closed group
+
+// LU structures (device) produced by the host analysis.  Plain data: it is
+// passed to kernels by value.
 struct LUDev {
   int n = 0;
   long long nnz = 0;
   int *row_of_step = nullptr, *col_of_step = nullptr, *circ_of_step = nullptr;
   int *cp = nullptr, *ri = nullptr, *diag = nullptr, *src = nullptr;
   double *lu = nullptr, *y = nullptr;
-  int *f_lvl_ptr = nullptr, *f_cols = nullptr;
-  int *l_lvl_ptr = nullptr, *l_rows = nullptr, *l_ptr = nullptr, *l_pos = nullptr, *l_col = nullptr;
-  int *u_lvl_ptr = nullptr, *u_rows = nullptr, *u_ptr = nullptr, *u_pos = nullptr, *u_col = nullptr;
+  int *l_ptr = nullptr, *l_pos = nullptr, *l_col = nullptr;   // L by rows (solves)
+  int *u_ptr = nullptr, *u_pos = nullptr, *u_col = nullptr;   // U by rows (solves)
   char *exempt = nullptr;    // per step: skip the threshold test
   int *breakdown = nullptr;  // device flag: first failing step + 1
-  std::vector<int> h_f_lvl, h_l_lvl, h_u_lvl;  // host copies of the level pointers
+  int *upd_off = nullptr, *upd_pos = nullptr;  // per U entry: target positions of its update
+  SchedDev fs, ls;           // factor (and, backwards, U solve) / L-solve schedules
+  int f_levels = 0, l_levels = 0, u_levels = 0;  // plain level counts (statistics)
 };
 
 // Host-side analysis result.
@@ -150,7 +183,14 @@ struct LUHost {
   std::vector<int> f_lvl_ptr, f_cols, l_lvl_ptr, l_rows, l_ptr, l_pos, l_col;
   std::vector<int> u_lvl_ptr, u_rows, u_ptr, u_pos, u_col;
   std::vector<char> exempt;  // columns exempt from the pivot threshold test
+  std::vector<int> l_long, u_long;  // per solve level: long rows at the end of the level
+  Schedule fsched, lsched;
+  std::vector<int> upd_off, upd_pos;  // scatter positions of each U entry's update
 };
+
+Schedule build_schedule(int n, const std::function<void(int, std::vector<int> &)> &deps_of,
+                        const std::function<bool(int)> &is_long,
+                        const std::function<bool(int)> &is_long_rev);
 
 // Analysis entry (xg_symbolic.cpp): CSR pattern + values -> LUHost.
 int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &ci,
@@ -162,7 +202,8 @@ void launch_mos1_k(cudaStream_t st, const DevArrays &d, int nm, int sto_base, in
                    int it, int flags, int sF, int sQ, int sL, int sM);
 void launch_diode_k(cudaStream_t st, const DevArrays &d, int nd, int combined, int masked, int it,
                     int flags, int sF, int sQ, int sL, int sM);
-void launch_assemble_k(cudaStream_t st, const DevArrays &d, int n, int nnz);
+void launch_assemble_k(cudaStream_t st, const DevArrays &d, int n, int nnz, int n_long_rows,
+                       int n_long_ents);
 void launch_load_vectors_k(cudaStream_t st, const DevArrays &d, int n, const double *x, double *Q,
                            double *F, double *B, double *dFv, double *dQv, int lt);
 void launch_load_matrices_k(cudaStream_t st, const DevArrays &d, int nnz, double *dQdx, double *dFdx,

@@ -463,6 +463,62 @@ __device__ void block_partials(const DevArrays &d, int n, double vmax, double vs
   (void)r;
 }
 
+// Block-wide sum of one double (blockDim.x a multiple of 32, <= 1024).
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double wsum[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x < 32) {
+    t = (threadIdx.x < (blockDim.x >> 5)) ? wsum[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  }
+  return t;  // valid in thread 0
+}
+
+// Long rows (e.g. a supply node touching every PMOS): kLongSplit blocks per
+// row gather F, Q, B, L partial sums, grid-strided over the row's lists.
+__global__ void __launch_bounds__(256) k_long_rows(DevArrays d) {
+  const int lr = blockIdx.x / kLongSplit, part = blockIdx.x % kLongSplit;
+  const int r = d.long_rows[lr];
+  const CircState &s = d.cs[d.circ_of_row[r]];
+  if (!circ_active(s)) return;
+  const int start = part * blockDim.x + threadIdx.x, stride = kLongSplit * blockDim.x;
+  double F = 0.0, Q = 0.0, B = 0.0, L = 0.0;
+  for (int e = d.rp[r] + start; e < d.rp[r + 1]; e += stride) {
+    const double xv = d.x[d.ci[e]];
+    F += d.Glin[e] * xv;
+    Q += d.Clin[e] * xv;
+  }
+  for (int k = d.vF_ptr[r] + start; k < d.vF_ptr[r + 1]; k += stride) F += d.sF[d.vF_idx[k]];
+  for (int k = d.vQ_ptr[r] + start; k < d.vQ_ptr[r + 1]; k += stride) Q += d.sQ[d.vQ_idx[k]];
+  for (int k = d.vB_ptr[r] + start; k < d.vB_ptr[r + 1]; k += stride) B += d.sB[d.vB_idx[k]];
+  for (int k = d.vL_ptr[r] + start; k < d.vL_ptr[r + 1]; k += stride) L += d.sL[d.vL_idx[k]];
+  F = block_sum(F);
+  Q = block_sum(Q);
+  B = block_sum(B);
+  L = block_sum(L);
+  if (threadIdx.x == 0) {
+    double *o = d.long_rsum + 4 * ((size_t)lr * kLongSplit + part);
+    o[0] = F; o[1] = Q; o[2] = B; o[3] = L;
+  }
+}
+
+// Long Jacobian entries (e.g. a supply node's diagonal): kLongSplit blocks each.
+__global__ void __launch_bounds__(256) k_long_entries(DevArrays d) {
+  const int le = blockIdx.x / kLongSplit, part = blockIdx.x % kLongSplit;
+  const int e = d.long_ents[le];
+  const CircState &s = d.cs[d.circ_of_row[d.erow[e]]];
+  if (!circ_active(s)) return;
+  const int start = part * blockDim.x + threadIdx.x, stride = kLongSplit * blockDim.x;
+  double v = 0.0;
+  for (int k = d.m_ptr[e] + start; k < d.m_ptr[e + 1]; k += stride) v += d.sM[d.m_idx[k]];
+  v = block_sum(v);
+  if (threadIdx.x == 0) d.long_esum[(size_t)le * kLongSplit + part] = v;
+}
+
 // Residual per row: RHS = -(qscale (Q - Q_hist0) + fscale (F - B) + hscale Q_hist2 + gshunt x)
 //                        + limiter terms     (OneStep::obtainResidual, N_TIA_OneStep.C:219-290)
 __global__ void __launch_bounds__(kRowBlock) k_assemble_rows(DevArrays d, int n) {
@@ -472,21 +528,30 @@ __global__ void __launch_bounds__(kRowBlock) k_assemble_rows(DevArrays d, int n)
     const int c = d.circ_of_row[r];
     const CircState &s = d.cs[c];
     if (circ_active(s)) {
-      double Fl = 0.0, Ql = 0.0;
-      for (int e = d.rp[r]; e < d.rp[r + 1]; ++e) {
-        const double xv = d.x[d.ci[e]];
-        Fl += d.Glin[e] * xv;
-        Ql += d.Clin[e] * xv;
+      double F, Q, B, L;
+      const int lr = d.row_long[r];
+      if (lr >= 0) {
+        F = 0.0; Q = 0.0; B = 0.0; L = 0.0;
+        const double *o = d.long_rsum + 4 * (size_t)lr * kLongSplit;
+        for (int k = 0; k < kLongSplit; ++k) {
+          F += o[4 * k]; Q += o[4 * k + 1]; B += o[4 * k + 2]; L += o[4 * k + 3];
+        }
+      } else {
+        F = 0.0; Q = 0.0; B = 0.0; L = 0.0;
+        for (int e = d.rp[r]; e < d.rp[r + 1]; ++e) {
+          const double xv = d.x[d.ci[e]];
+          F += d.Glin[e] * xv;
+          Q += d.Clin[e] * xv;
+        }
+        for (int k = d.vF_ptr[r]; k < d.vF_ptr[r + 1]; ++k) F += d.sF[d.vF_idx[k]];
+        for (int k = d.vQ_ptr[r]; k < d.vQ_ptr[r + 1]; ++k) Q += d.sQ[d.vQ_idx[k]];
+        for (int k = d.vB_ptr[r]; k < d.vB_ptr[r + 1]; ++k) B += d.sB[d.vB_idx[k]];
+        for (int k = d.vL_ptr[r]; k < d.vL_ptr[r + 1]; ++k) L += d.sL[d.vL_idx[k]];
       }
-      double F = Fl, Q = Ql, B = 0.0, L = 0.0;
-      for (int k = d.vF_ptr[r]; k < d.vF_ptr[r + 1]; ++k) F += d.sF[d.vF_idx[k]];
-      for (int k = d.vQ_ptr[r]; k < d.vQ_ptr[r + 1]; ++k) Q += d.sQ[d.vQ_idx[k]];
-      for (int k = d.vB_ptr[r]; k < d.vB_ptr[r + 1]; ++k) B += d.sB[d.vB_idx[k]];
-      for (int k = d.vL_ptr[r]; k < d.vL_ptr[r + 1]; ++k) L += d.sL[d.vL_idx[k]];
       double res = s.fscale * (F - B);
       if (s.qscale != 0.0) res += s.qscale * (Q - d.qh0[r]);
       if (s.hscale != 0.0) res += s.hscale * d.qh2[r];
-      if (s.gshunt != 0.0) res += s.gshunt * d.x[r];
+      if (s.gshunt != 0.0 && !d.is_branch[r]) res += s.gshunt * d.x[r];
       const double rhs = -res + L;
       d.rhs[r] = rhs;
       d.Qv[r] = Q;
@@ -508,8 +573,14 @@ __global__ void k_assemble_J(DevArrays d, int nnz) {
   const CircState &s = d.cs[d.circ_of_row[r]];
   if (!circ_active(s)) return;
   double v = s.qscale * d.Clin[e] + s.fscale * d.Glin[e];
-  for (int k = d.m_ptr[e]; k < d.m_ptr[e + 1]; ++k) v += d.sM[d.m_idx[k]];
-  if (s.gshunt != 0.0 && d.ci[e] == r) v += s.gshunt;
+  const int le = d.ent_long[e];
+  if (le >= 0) {
+    const double *o = d.long_esum + (size_t)le * kLongSplit;
+    for (int k = 0; k < kLongSplit; ++k) v += o[k];
+  } else {
+    for (int k = d.m_ptr[e]; k < d.m_ptr[e + 1]; ++k) v += d.sM[d.m_idx[k]];
+  }
+  if (s.gshunt != 0.0 && d.ci[e] == r) v += s.gshunt;  // branch rows have no diagonal entry
   d.J[e] = v;
 }
 
@@ -997,7 +1068,10 @@ void launch_diode_k(cudaStream_t st, const DevArrays &d, int nd, int combined, i
   if (nd > 0)
     k_diode<<<nblk(nd, 128), 128, 0, st>>>(d, nd, combined, masked, it, flags, sF, sQ, sL, sM);
 }
-void launch_assemble_k(cudaStream_t st, const DevArrays &d, int n, int nnz) {
+void launch_assemble_k(cudaStream_t st, const DevArrays &d, int n, int nnz, int n_long_rows,
+                       int n_long_ents) {
+  if (n_long_rows > 0) k_long_rows<<<n_long_rows * kLongSplit, 256, 0, st>>>(d);
+  if (n_long_ents > 0) k_long_entries<<<n_long_ents * kLongSplit, 256, 0, st>>>(d);
   k_assemble_rows<<<nblk(n, kRowBlock), kRowBlock, 0, st>>>(d, n);
   k_assemble_J<<<nblk(nnz, 256), 256, 0, st>>>(d, nnz);
 }

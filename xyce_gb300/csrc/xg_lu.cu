@@ -1,71 +1,107 @@
-// xg_lu.cu — level-scheduled sparse LU refactorization and solves (sm_103a).
+// xg_lu.cu — sparse LU refactorization and triangular solves on the frozen
+// pattern (sm_103a).
 //
 // Replaces the KLU numeric factorization + solve that Xyce runs on every
 // Newton iteration (src/LinearAlgebraServicesPKG/N_LAS_AmesosSolver.C:358-396).
-// Pivots are frozen by the host analysis (xg_symbolic.cpp); every column of
-// a level is independent, one warp per column, left-looking:
-//   load column j of A'  ->  for each U(k,j), k ascending: col_j -= L(:,k) * U(k,j)
-//   ->  threshold test of the diagonal against the updated column
-//       (kRuntimePivotTol); failing columns raise a breakdown flag so the
-//       host re-pivots  ->  L(:,j) /= U(j,j).
-// The triangular solves are row-oriented (gather, no atomics), 8 lanes per row.
+// Pivots are frozen by the host analysis (xg_symbolic.cpp).  Each sweep runs
+// on a grouped schedule:
+//   hubs   — items without dependencies that many others need (e.g. a supply
+//            node's column), one CTA each;
+//   groups — dependency-closed sets of columns/rows, one CTA each, a CTA
+//            barrier between local levels (e.g. one ring of a Monte-Carlo
+//            batch is one group: its whole factorization stays in one CTA);
+//   top    — what remains (the upper separators of the nested dissection),
+//            one 1024-thread CTA.
+// Factorization is left-looking per column: load A'(:,j); for each U(k,j), k
+// ascending: col_j -= L(:,k) U(k,j); threshold test of the diagonal against
+// the updated column (kRuntimePivotTol; failures raise a breakdown flag and
+// the host re-pivots); L(:,j) /= U(j,j).  Short columns use a warp, long ones
+// the whole CTA.  The solves are row-oriented gathers (no atomics): 8 lanes
+// per row, the whole CTA for long rows.  The U solve runs the factorization
+// schedule backwards (its dependency graph is the factor graph reversed).
 #include <cuda_runtime.h>
 
 #include "xg_internal.h"
 
 namespace xg {
 
-__device__ __forceinline__ int find_row(const int *ri, int lo, int hi, int key) {
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (ri[mid] < key) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
+constexpr int kGroupThreads = 512;  // threads of a group CTA (the top uses 1024)
+
+__device__ __forceinline__ bool item_active(const LUDev &L, const CircState *cs, int masked, int j) {
+  if (!masked) return true;
+  const CircState &s = cs[L.circ_of_step[j]];
+  return s.need_solve && !s.singular && (s.phase == PH_DC || s.phase == PH_TRAN);
 }
 
-__global__ void k_lu_factor_level(LUDev L, const double *__restrict__ vals, const int *cols, int count,
-                                  CircState *cs, int masked, double pivot_tol) {
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (w >= count) return;
-  const int j = cols[w];
-  if (masked) {
-    const CircState &s = cs[L.circ_of_step[j]];
-    if (!s.need_solve || (s.phase != PH_DC && s.phase != PH_TRAN)) return;
-  }
+template <bool BLOCK>
+__device__ __forceinline__ void team_sync() {
+  if (BLOCK) __syncthreads();
+  else __syncwarp();
+}
+
+// max over the team (warp or whole CTA); every thread gets the result
+template <bool BLOCK>
+__device__ __forceinline__ double team_max(double v, double *sm) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if (!BLOCK) return v;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double r = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, sm[w]);
+  return r;
+}
+
+template <bool BLOCK>
+__device__ __forceinline__ double team_sum(double v, double *sm) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (!BLOCK) return v;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double r = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += sm[w];
+  return r;
+}
+
+template <bool BLOCK>
+__device__ void factor_column(const LUDev &L, const double *__restrict__ vals, int j, CircState *cs,
+                              int masked, double pivot_tol, double *sm) {
+  const int lane = BLOCK ? (int)threadIdx.x : (int)(threadIdx.x & 31);
+  const int nl = BLOCK ? (int)blockDim.x : 32;
   const int p0 = L.cp[j], p1 = L.cp[j + 1], pd = L.diag[j];
   double *lu = L.lu;
-  for (int p = p0 + lane; p < p1; p += 32) {
+  for (int p = p0 + lane; p < p1; p += nl) {
     const int s = L.src[p];
     lu[p] = (s >= 0) ? vals[s] : 0.0;
   }
-  __syncwarp();
-  bool lost = false;
+  team_sync<BLOCK>();
+  double lost = 0.0;
   for (int p = p0; p < pd; ++p) {
     const int k = L.ri[p];
     const double ukj = lu[p];
     if (ukj != 0.0) {
-      const int q1 = L.cp[k + 1];
-      for (int q = L.diag[k] + 1 + lane; q < q1; q += 32) {
-        const int i = L.ri[q];
-        const int pos = find_row(L.ri, p + 1, p1, i);
-        if (pos < p1 && L.ri[pos] == i) lu[pos] -= lu[q] * ukj;
-        else lost = true;
+      // positions of L(:,k)'s rows in column j come from the analysis
+      const int q0 = L.diag[k] + 1, q1 = L.cp[k + 1];
+      const int *tgt = L.upd_pos + L.upd_off[p];
+      for (int q = q0 + lane; q < q1; q += nl) {
+        const int pos = tgt[q - q0];
+        if (pos > p && pos < p1) lu[pos] -= lu[q] * ukj;
+        else lost = 1.0;
       }
     }
-    __syncwarp();
+    team_sync<BLOCK>();
   }
   const double d = lu[pd];
   double amax = 0.0;
-  for (int p = pd + lane; p < p1; p += 32) amax = fmax(amax, fabs(lu[p]));
-  for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-  lost = __any_sync(0xffffffffu, lost);
+  for (int p = pd + lane; p < p1; p += nl) amax = fmax(amax, fabs(lu[p]));
+  amax = team_max<BLOCK>(amax, sm);
+  lost = team_max<BLOCK>(lost, sm);
   // The threshold only matters when row j of U has entries right of the
   // diagonal: otherwise the multipliers never reach the Schur complement
   // (e.g. the branch row of a grounded voltage source).
   const bool urow = L.u_ptr[j + 1] > L.u_ptr[j] && !L.exempt[j];
-  const bool bad = lost || (urow && !(fabs(d) >= pivot_tol * amax)) || !(fabs(d) > 0.0) || isinf(d);
+  const bool bad = lost != 0.0 || (urow && !(fabs(d) >= pivot_tol * amax)) || !(fabs(d) > 0.0) || isinf(d);
   if (bad) {
     if (lane == 0) {
       atomicCAS(L.breakdown, 0, j + 1);
@@ -74,77 +110,184 @@ __global__ void k_lu_factor_level(LUDev L, const double *__restrict__ vals, cons
     return;
   }
   const double inv = 1.0 / d;
-  for (int p = pd + 1 + lane; p < p1; p += 32) lu[p] *= inv;
+  for (int p = pd + 1 + lane; p < p1; p += nl) lu[p] *= inv;
 }
 
-// y[i] = b[row_of_step[i]] - sum_k L(i,k) y[k]
-__global__ void k_lu_lsolve_level(LUDev L, const double *__restrict__ b, const int *rows, int count,
-                                  const CircState *cs, int masked) {
-  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
-  const int sub = threadIdx.x & 7;
-  if (g >= count) return;
-  const int i = rows[g];
-  if (masked) {
-    const CircState &s = cs[L.circ_of_step[i]];
-    if (!s.need_solve || s.singular || (s.phase != PH_DC && s.phase != PH_TRAN)) return;
-  }
+// y[i] = b[row_of_step[i]] - sum_k L(i,k) y[k]          (LOWER)
+// y[i] = (y[i] - sum_j U(i,j) y[j]) / U(i,i); x[col_of_step[i]] = y[i]   (upper)
+// Team: 8 lanes (width 8) or the whole CTA (BLOCK).
+template <bool LOWER, bool BLOCK>
+__device__ void solve_row(const LUDev &L, const double *__restrict__ b, double *__restrict__ x, int i,
+                          int sub, double *sm) {
+  const int *ptr = LOWER ? L.l_ptr : L.u_ptr;
+  const int *pos = LOWER ? L.l_pos : L.u_pos;
+  const int *col = LOWER ? L.l_col : L.u_col;
+  const int nl = BLOCK ? (int)blockDim.x : 8;
   double sum = 0.0;
-  for (int t = L.l_ptr[i] + sub; t < L.l_ptr[i + 1]; t += 8) sum += L.lu[L.l_pos[t]] * L.y[L.l_col[t]];
-  for (int o = 4; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, 8);
-  if (sub == 0) L.y[i] = b[L.row_of_step[i]] - sum;
-}
-
-// z[k] = (y[k] - sum_j U(k,j) z[j]) / U(k,k);  x[col_of_step[k]] = z[k]
-__global__ void k_lu_usolve_level(LUDev L, double *__restrict__ x, const int *rows, int count,
-                                  const CircState *cs, int masked) {
-  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
-  const int sub = threadIdx.x & 7;
-  if (g >= count) return;
-  const int k = rows[g];
-  if (masked) {
-    const CircState &s = cs[L.circ_of_step[k]];
-    if (!s.need_solve || s.singular || (s.phase != PH_DC && s.phase != PH_TRAN)) return;
+  for (int t = ptr[i] + sub; t < ptr[i + 1]; t += nl) sum += L.lu[pos[t]] * L.y[col[t]];
+  if (BLOCK) {
+    sum = team_sum<true>(sum, sm);
+  } else {
+    for (int o = 4; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, 8);
   }
-  double sum = 0.0;
-  for (int t = L.u_ptr[k] + sub; t < L.u_ptr[k + 1]; t += 8) sum += L.lu[L.u_pos[t]] * L.y[L.u_col[t]];
-  for (int o = 4; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, 8);
   if (sub == 0) {
-    const double z = (L.y[k] - sum) / L.lu[L.diag[k]];
-    L.y[k] = z;
-    x[L.col_of_step[k]] = z;
+    if (LOWER) {
+      L.y[i] = b[L.row_of_step[i]] - sum;
+    } else {
+      const double z = (L.y[i] - sum) / L.lu[L.diag[i]];
+      L.y[i] = z;
+      x[L.col_of_step[i]] = z;
+    }
   }
 }
 
+// ---- factorization ----------------------------------------------------------
+__global__ void __launch_bounds__(256) k_factor_hubs(LUDev L, const double *__restrict__ vals, CircState *cs,
+                                                     int masked, double pivot_tol) {
+  __shared__ double sm[32];
+  const int j = L.fs.items[blockIdx.x];
+  if (!item_active(L, cs, masked, j)) return;
+  factor_column<true>(L, vals, j, cs, masked, pivot_tol, sm);
+}
+
+__global__ void __launch_bounds__(1024) k_factor_groups(LUDev L, const double *__restrict__ vals, CircState *cs,
+                                                        int masked, double pivot_tol, int top) {
+  __shared__ double sm[32];
+  const SchedDev &S = L.fs;
+  const int g = top ? S.n_groups : (int)blockIdx.x;
+  const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int lv = S.grp_lvl[g]; lv < S.grp_lvl[g + 1]; ++lv) {
+    const int b = S.lvl_ptr[lv], e = S.lvl_ptr[lv + 1];
+    bool any_long = false;
+    for (int t = b + warp; t < e; t += nwarps) {
+      const int j = S.items[t];
+      if (S.is_long[j]) { any_long = true; continue; }
+      if (item_active(L, cs, masked, j)) factor_column<false>(L, vals, j, cs, masked, pivot_tol, sm);
+    }
+    if (__syncthreads_or(any_long)) {
+      for (int t = b; t < e; ++t) {
+        const int j = S.items[t];
+        if (!S.is_long[j] || !item_active(L, cs, masked, j)) continue;
+        factor_column<true>(L, vals, j, cs, masked, pivot_tol, sm);
+        __syncthreads();
+      }
+    }
+  }
+}
+
+// ---- L solve (L schedule, forward) ------------------------------------------
+__global__ void k_lsolve_hubs(LUDev L, const double *__restrict__ b, const CircState *cs, int masked) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= L.ls.n_hub) return;
+  const int i = L.ls.items[t];
+  if (!item_active(L, cs, masked, i)) return;
+  L.y[i] = b[L.row_of_step[i]];  // hubs have no L entries
+}
+
+__global__ void __launch_bounds__(1024) k_lsolve_groups(LUDev L, const double *__restrict__ b,
+                                                        const CircState *cs, int masked, int top) {
+  __shared__ double sm[32];
+  const SchedDev &S = L.ls;
+  const int g = top ? S.n_groups : (int)blockIdx.x;
+  const int team = threadIdx.x >> 3, nteams = blockDim.x >> 3, sub = threadIdx.x & 7;
+  for (int lv = S.grp_lvl[g]; lv < S.grp_lvl[g + 1]; ++lv) {
+    const int bb = S.lvl_ptr[lv], e = S.lvl_ptr[lv + 1];
+    bool any_long = false;
+    // teams of 8 lanes stride over the level; the loop bound is warp-uniform
+    for (int t0 = bb; t0 < e; t0 += nteams) {
+      const int t = t0 + team;
+      bool act = false;
+      int i = 0;
+      if (t < e) {
+        i = S.items[t];
+        if (S.is_long[i]) any_long = true;
+        else act = item_active(L, cs, masked, i);
+      }
+      if (__any_sync(0xffffffffu, act)) {
+        double sum = 0.0;
+        if (act)
+          for (int q = L.l_ptr[i] + sub; q < L.l_ptr[i + 1]; q += 8) sum += L.lu[L.l_pos[q]] * L.y[L.l_col[q]];
+        for (int o = 4; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, 8);
+        if (act && sub == 0) L.y[i] = b[L.row_of_step[i]] - sum;
+      }
+    }
+    if (__syncthreads_or(any_long)) {
+      for (int t = bb; t < e; ++t) {
+        const int i = S.items[t];
+        if (!S.is_long[i] || !item_active(L, cs, masked, i)) continue;
+        solve_row<true, true>(L, b, nullptr, i, threadIdx.x, sm);
+        __syncthreads();
+      }
+    }
+  }
+}
+
+// ---- U solve (factor schedule, backward) ------------------------------------
+__global__ void __launch_bounds__(1024) k_usolve_groups(LUDev L, double *__restrict__ x, const CircState *cs,
+                                                        int masked, int top) {
+  __shared__ double sm[32];
+  const SchedDev &S = L.fs;
+  const int g = top ? S.n_groups : (int)blockIdx.x;
+  const int team = threadIdx.x >> 3, nteams = blockDim.x >> 3, sub = threadIdx.x & 7;
+  for (int lv = S.grp_lvl[g + 1] - 1; lv >= S.grp_lvl[g]; --lv) {
+    const int bb = S.lvl_ptr[lv], e = S.lvl_ptr[lv + 1];
+    bool any_long = false;
+    for (int t0 = bb; t0 < e; t0 += nteams) {
+      const int t = t0 + team;
+      bool act = false;
+      int k = 0;
+      if (t < e) {
+        k = S.items[t];
+        if (S.is_long_rev[k]) any_long = true;
+        else act = item_active(L, cs, masked, k);
+      }
+      if (__any_sync(0xffffffffu, act)) {
+        double sum = 0.0;
+        if (act)
+          for (int q = L.u_ptr[k] + sub; q < L.u_ptr[k + 1]; q += 8) sum += L.lu[L.u_pos[q]] * L.y[L.u_col[q]];
+        for (int o = 4; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, 8);
+        if (act && sub == 0) {
+          const double z = (L.y[k] - sum) / L.lu[L.diag[k]];
+          L.y[k] = z;
+          x[L.col_of_step[k]] = z;
+        }
+      }
+    }
+    if (__syncthreads_or(any_long)) {
+      for (int t = bb; t < e; ++t) {
+        const int k = S.items[t];
+        if (!S.is_long_rev[k] || !item_active(L, cs, masked, k)) continue;
+        solve_row<false, true>(L, nullptr, x, k, threadIdx.x, sm);
+        __syncthreads();
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_usolve_hubs(LUDev L, double *__restrict__ x, const CircState *cs,
+                                                     int masked) {
+  __shared__ double sm[32];
+  const int k = L.fs.items[blockIdx.x];
+  if (!item_active(L, cs, masked, k)) return;
+  solve_row<false, true>(L, nullptr, x, k, threadIdx.x, sm);
+}
+
+// ---- launchers --------------------------------------------------------------
 void launch_lu_factor_k(cudaStream_t st, const LUDev &L, const double *vals, CircState *cs, int masked,
                         double pivot_tol) {
-  const int nl = (int)L.h_f_lvl.size() - 1;
-  for (int l = 0; l < nl; ++l) {
-    const int cnt = L.h_f_lvl[l + 1] - L.h_f_lvl[l];
-    if (cnt <= 0) continue;
-    const int threads = 128;
-    const int blocks = (cnt * 32 + threads - 1) / threads;
-    k_lu_factor_level<<<blocks, threads, 0, st>>>(L, vals, L.f_cols + L.h_f_lvl[l], cnt, cs, masked,
-                                                  pivot_tol);
-  }
+  if (L.fs.n_hub > 0) k_factor_hubs<<<L.fs.n_hub, 256, 0, st>>>(L, vals, cs, masked, pivot_tol);
+  if (L.fs.n_groups > 0) k_factor_groups<<<L.fs.n_groups, kGroupThreads, 0, st>>>(L, vals, cs, masked, pivot_tol, 0);
+  if (L.fs.n_top_items > 0) k_factor_groups<<<1, 1024, 0, st>>>(L, vals, cs, masked, pivot_tol, 1);
 }
 
 void launch_lu_solve_k(cudaStream_t st, const LUDev &L, const double *b, double *x, const CircState *cs,
                        int masked) {
-  const int threads = 128;
-  const int nl = (int)L.h_l_lvl.size() - 1;
-  for (int l = 0; l < nl; ++l) {
-    const int cnt = L.h_l_lvl[l + 1] - L.h_l_lvl[l];
-    if (cnt <= 0) continue;
-    k_lu_lsolve_level<<<(cnt * 8 + threads - 1) / threads, threads, 0, st>>>(L, b, L.l_rows + L.h_l_lvl[l],
-                                                                             cnt, cs, masked);
-  }
-  const int nu = (int)L.h_u_lvl.size() - 1;
-  for (int l = 0; l < nu; ++l) {
-    const int cnt = L.h_u_lvl[l + 1] - L.h_u_lvl[l];
-    if (cnt <= 0) continue;
-    k_lu_usolve_level<<<(cnt * 8 + threads - 1) / threads, threads, 0, st>>>(L, x, L.u_rows + L.h_u_lvl[l],
-                                                                             cnt, cs, masked);
-  }
+  if (L.ls.n_hub > 0) k_lsolve_hubs<<<(L.ls.n_hub + 255) / 256, 256, 0, st>>>(L, b, cs, masked);
+  if (L.ls.n_groups > 0) k_lsolve_groups<<<L.ls.n_groups, kGroupThreads, 0, st>>>(L, b, cs, masked, 0);
+  if (L.ls.n_top_items > 0) k_lsolve_groups<<<1, 1024, 0, st>>>(L, b, cs, masked, 1);
+  if (L.fs.n_top_items > 0) k_usolve_groups<<<1, 1024, 0, st>>>(L, x, cs, masked, 1);
+  if (L.fs.n_groups > 0) k_usolve_groups<<<L.fs.n_groups, kGroupThreads, 0, st>>>(L, x, cs, masked, 0);
+  if (L.fs.n_hub > 0) k_usolve_hubs<<<L.fs.n_hub, 256, 0, st>>>(L, x, cs, masked);
 }
 
 }  // namespace xg

@@ -441,12 +441,184 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
         for (int t = pd + 1; t < p1; ++t) lu[t] /= d;
     }
   }
+  // within each solve level, long rows go last: they get a whole block each
+  auto split_long = [&](const std::vector<int> &ptr, std::vector<int> &items, const std::vector<int> &rptr,
+                        std::vector<int> &nlong) {
+    nlong.assign(ptr.size() > 0 ? ptr.size() - 1 : 0, 0);
+    for (size_t l = 0; l + 1 < ptr.size(); ++l) {
+      auto b = items.begin() + ptr[l], e = items.begin() + ptr[l + 1];
+      auto mid = std::stable_partition(b, e, [&](int r) { return rptr[r + 1] - rptr[r] <= kLongSolveRow; });
+      nlong[l] = (int)(e - mid);
+    }
+  };
   if (n > 0) {
     buckets(flev, fmaxl, out.f_lvl_ptr, out.f_cols);
     buckets(llev, lmax, out.l_lvl_ptr, out.l_rows);
     buckets(ulev, umax, out.u_lvl_ptr, out.u_rows);
+    split_long(out.l_lvl_ptr, out.l_rows, out.l_ptr, out.l_long);
+    split_long(out.u_lvl_ptr, out.u_rows, out.u_ptr, out.u_long);
   }
+  // Update maps: for U entry p = (k, j), upd_off[p] .. upd_off[p+1] lists the
+  // positions in column j of the rows of L(:,k), so the device factorization
+  // scatters without searching.
+  out.upd_off.assign(nnz + 1, 0);
+  {
+    long long total = 0;
+    for (int j = 0; j < n; ++j)
+      for (int t = out.cp[j]; t < out.diag[j]; ++t) {
+        const int k = out.ri[t];
+        total += out.cp[k + 1] - out.diag[k] - 1;
+      }
+    if (total > 1900000000LL) {
+      err = "LU update map exceeds the int32 index range";
+      return XG_ERR_UNSUPPORTED;
+    }
+    out.upd_pos.resize(total);
+    long long w = 0;
+    for (int j = 0; j < n; ++j) {
+      const int p1 = out.cp[j + 1];
+      for (int t = out.cp[j]; t < out.cp[j + 1]; ++t) {
+        out.upd_off[t] = (int)w;
+        if (t >= out.diag[j]) continue;
+        const int k = out.ri[t];
+        int pos = t + 1;
+        for (int q2 = out.diag[k] + 1; q2 < out.cp[k + 1]; ++q2) {
+          const int i = out.ri[q2];
+          while (pos < p1 && out.ri[pos] < i) ++pos;  // both lists ascend
+          if (pos >= p1 || out.ri[pos] != i) {
+            err = "symbolic factorization lost a fill entry";
+            return XG_ERR_STATE;
+          }
+          out.upd_pos[w++] = pos;
+        }
+      }
+    }
+    out.upd_off[nnz] = (int)w;
+  }
+  // Grouped schedules: factorization (deps = U-part rows of each column) and
+  // L solve (deps = L-row columns); the U solve runs the factor schedule backwards.
+  out.fsched = build_schedule(
+      n, [&](int j, std::vector<int> &d) { for (int t = out.cp[j]; t < out.diag[j]; ++t) d.push_back(out.ri[t]); },
+      [&](int j) { return (out.cp[j + 1] - out.diag[j] - 1) > kLongColumn || (out.diag[j] - out.cp[j]) > kLongColumn; },
+      [&](int j) { return (out.u_ptr[j + 1] - out.u_ptr[j]) > kLongSolveRow; });
+  out.lsched = build_schedule(
+      n, [&](int i, std::vector<int> &d) { for (int t = out.l_ptr[i]; t < out.l_ptr[i + 1]; ++t) d.push_back(out.l_col[t]); },
+      [&](int i) { return (out.l_ptr[i + 1] - out.l_ptr[i]) > kLongSolveRow; }, nullptr);
   return XG_OK;
+}
+
+// Dependency-closed groups for one CTA each, a prologue of "hub" items (no
+// dependencies, many dependents) and a single-CTA top for the rest.
+Schedule build_schedule(int n, const std::function<void(int, std::vector<int> &)> &deps_of,
+                        const std::function<bool(int)> &is_long,
+                        const std::function<bool(int)> &is_long_rev) {
+  Schedule S;
+  if (n == 0) {
+    S.grp_lvl.assign(2, 0);
+    S.lvl_ptr.assign(1, 0);
+    return S;
+  }
+  std::vector<int> dptr(n + 1, 0), didx;
+  std::vector<int> tmp;
+  for (int j = 0; j < n; ++j) {
+    tmp.clear();
+    deps_of(j, tmp);
+    didx.insert(didx.end(), tmp.begin(), tmp.end());
+    dptr[j + 1] = (int)didx.size();
+  }
+  std::vector<int> outdeg(n, 0);
+  for (int k : didx) outdeg[k]++;
+  std::vector<char> hub(n, 0), top(n, 0);
+  for (int j = 0; j < n; ++j)
+    if (dptr[j + 1] == dptr[j] && outdeg[j] > kHubFanout) hub[j] = 1;
+  std::vector<int> parent(n), gsize(n, 1);
+  std::iota(parent.begin(), parent.end(), 0);
+  std::function<int(int)> find = [&](int v) {
+    while (parent[v] != v) { parent[v] = parent[parent[v]]; v = parent[v]; }
+    return v;
+  };
+  std::vector<int> roots;
+  for (int j = 0; j < n; ++j) {
+    if (hub[j]) continue;
+    roots.clear();
+    bool to_top = false;
+    for (int t = dptr[j]; t < dptr[j + 1]; ++t) {
+      const int k = didx[t];
+      if (hub[k]) continue;
+      if (top[k]) { to_top = true; break; }
+      roots.push_back(find(k));
+    }
+    if (!to_top) {
+      std::sort(roots.begin(), roots.end());
+      roots.erase(std::unique(roots.begin(), roots.end()), roots.end());
+      long long total = 1;
+      for (int r : roots) total += gsize[r];
+      if (total > kGroupCap) to_top = true;
+      else
+        for (int r : roots) { parent[r] = j; gsize[j] += gsize[r]; }
+    }
+    if (to_top) top[j] = 1;
+  }
+  // levels: group-local for grouped items, top-local for the top
+  std::vector<int> lev(n, 0);
+  for (int j = 0; j < n; ++j) {
+    if (hub[j]) continue;
+    int l = 0;
+    for (int t = dptr[j]; t < dptr[j + 1]; ++t) {
+      const int k = didx[t];
+      if (hub[k]) continue;
+      if (top[j] && !top[k]) continue;  // groups finish before the top starts
+      l = std::max(l, lev[k] + 1);
+    }
+    lev[j] = l;
+  }
+  // group ids in order of first appearance; the top is the last group
+  std::vector<int> gid(n, -1);
+  int ng = 0;
+  for (int j = 0; j < n; ++j) {
+    if (hub[j] || top[j]) continue;
+    const int r = find(j);
+    if (gid[r] < 0) gid[r] = ng++;
+    gid[j] = gid[r];
+  }
+  for (int j = 0; j < n; ++j)
+    if (top[j]) gid[j] = ng;
+  S.n_groups = ng;
+  std::vector<int> order;
+  for (int j = 0; j < n; ++j)
+    if (hub[j]) S.items.push_back(j);
+  S.n_hub = (int)S.items.size();
+  for (int j = 0; j < n; ++j)
+    if (!hub[j]) order.push_back(j);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    if (gid[a] != gid[b]) return gid[a] < gid[b];
+    return lev[a] < lev[b];
+  });
+  S.lvl_ptr.push_back(S.n_hub);
+  S.grp_lvl.assign(ng + 2, 0);
+  int cur_g = -1, cur_l = -1;
+  int nlv = 0;
+  for (size_t q = 0; q < order.size(); ++q) {
+    const int j = order[q];
+    if (gid[j] != cur_g || lev[j] != cur_l) {
+      if (q > 0) { S.lvl_ptr.push_back(S.n_hub + (int)q); nlv++; }
+      while (cur_g < gid[j]) { cur_g++; S.grp_lvl[cur_g] = nlv; }
+      cur_l = lev[j];
+    }
+    S.items.push_back(j);
+  }
+  if (!order.empty()) { S.lvl_ptr.push_back(S.n_hub + (int)order.size()); nlv++; }
+  while (cur_g < ng + 1) { cur_g++; S.grp_lvl[cur_g] = nlv; }
+  // long items are processed by the whole block, the others by warps
+  S.is_long.assign(n, 0);
+  S.is_long_rev.assign(n, 0);
+  for (int j = 0; j < n; ++j) {
+    S.is_long[j] = is_long(j) ? 1 : 0;
+    if (is_long_rev) S.is_long_rev[j] = is_long_rev(j) ? 1 : 0;
+  }
+  S.n_top_items = 0;
+  for (int j = 0; j < n; ++j) S.n_top_items += top[j];
+  return S;
 }
 
 }  // namespace xg
