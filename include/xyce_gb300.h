@@ -152,6 +152,20 @@ int xg_load_dae_matrices(xg_ctx *ctx, double *dQdx, double *dFdx, int load_type)
 int xg_lu_analyze(xg_ctx *ctx, const double *vals);
 int xg_lu_factor(xg_ctx *ctx, const double *vals);
 int xg_lu_solve(xg_ctx *ctx, const double *rhs, double *x);
+/* Allocation-free variant of xg_lu_solve.  No counterpart in the reference:
+ * Xyce's solvers allocate their own workspace.  It is for callers that must
+ * not call cudaMalloc (device memory fully owned by another allocator, or a
+ * loop that must not block on the CUDA allocator): the solve's scratch vector
+ * is a static device array of XG_NOALLOC_MAX_N doubles (2 MiB, held by every
+ * GPU that loads the library until exit) instead of allocated memory.  Same
+ * inputs and outputs as xg_lu_solve (device pointers; the factorization comes
+ * from xg_lu_factor on ctx).  Returns XG_ERR_ARG when the system has more than
+ * XG_NOALLOC_MAX_N unknowns.  The first call on a device looks the scratch
+ * address up; make it before any stream capture.  Every call shares the one
+ * scratch array: calls that overlap on the GPU race. */
+#define XG_NOALLOC_MAX_N 262144
+int xg_lu_solve_noalloc(xg_ctx *ctx, const double *rhs, double *x);
+
 /* Statistics of the current analysis: nnz(L+U), factor/solve level counts. */
 int xg_lu_info(xg_ctx *ctx, long long *nnz_lu, int *factor_levels, int *lsolve_levels,
                int *usolve_levels);

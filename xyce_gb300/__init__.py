@@ -40,7 +40,8 @@ EXPORTED = [
     "xg_set_unknowns", "xg_add_resistors", "xg_add_capacitors", "xg_add_vsources",
     "xg_add_isources", "xg_add_diodes", "xg_add_mosfet1", "xg_finalize", "xg_get_sizes",
     "xg_get_pattern", "xg_update_sources", "xg_update_state", "xg_load_dae_vectors",
-    "xg_load_dae_matrices", "xg_lu_analyze", "xg_lu_factor", "xg_lu_solve", "xg_lu_info",
+    "xg_load_dae_matrices", "xg_lu_analyze", "xg_lu_factor", "xg_lu_solve",
+    "xg_lu_solve_noalloc", "xg_lu_info",
     "xg_transient", "xg_tran_start", "xg_tran_advance", "xg_tran_results", "xg_tran_end",
     "xg_dcop", "xg_version",
 ]
@@ -113,6 +114,7 @@ def lib() -> C.CDLL:
     L.xg_lu_analyze.argtypes = [P, P]
     L.xg_lu_factor.argtypes = [P, P]
     L.xg_lu_solve.argtypes = [P, P, P]
+    L.xg_lu_solve_noalloc.argtypes = [P, P, P]
     L.xg_lu_info.argtypes = [P, C.POINTER(C.c_longlong), C.POINTER(I), C.POINTER(I), C.POINTER(I)]
     L.xg_transient.argtypes = [P, C.POINTER(TranParams), I, ip, I, ip, dp, dp, C.POINTER(TranStats)]
     L.xg_tran_start.argtypes = [P, C.POINTER(TranParams), I, ip, I]
@@ -209,6 +211,10 @@ class Circuit:
 
     def lu_solve(self, rhs, x):
         self._check(lib().xg_lu_solve(self.h, _ptr(rhs), _ptr(x)))
+
+    def lu_solve_noalloc(self, rhs, x):
+        """xg_lu_solve without allocated scratch (see include/xyce_gb300.h)."""
+        self._check(lib().xg_lu_solve_noalloc(self.h, _ptr(rhs), _ptr(x)))
 
     def lu_info(self):
         nnz = C.c_longlong()

@@ -710,6 +710,33 @@ int xg_lu_solve(xg_ctx *ctx, const double *rhs, double *x) {
   return XG_OK;
 }
 
+// Allocation-free variant of xg_lu_solve: the solve's scratch vector lives in
+// a static device array (see xg_lu.cu) instead of memory from cudaMalloc.
+// For callers that must not call the CUDA allocator — code whose device memory
+// is entirely owned by another allocator, or a loop that must not block on
+// cudaMalloc/cudaFree.  The first call on a device looks up the scratch
+// address (cudaGetSymbolAddress); make that first call before any stream
+// capture.  All calls share the one scratch array: calls that overlap on the
+// GPU (other streams, other host threads) race and must be serialized.
+int xg_lu_solve_noalloc(xg_ctx *ctx, const double *rhs, double *x) {
+  if (!ctx || !rhs || !x) return XG_ERR_ARG;
+  if (ctx->n > kNoAllocMaxN) {
+    char buf[160];
+    snprintf(buf, sizeof buf, "xg_lu_solve_noalloc: %d unknowns exceed the scratch limit of %d", ctx->n,
+             kNoAllocMaxN);
+    return fail(ctx, XG_ERR_ARG, buf);
+  }
+  if (!ctx->lu_ready) return fail(ctx, XG_ERR_STATE, "call xg_lu_analyze first");
+  CK(cudaSetDevice(ctx->device));
+  double *scratch = nullptr;
+  std::string err;
+  int rc = noalloc_scratch(ctx->device, &scratch, err);
+  if (rc) return fail(ctx, rc, err);
+  launch_lu_solve_noalloc_k(ctx->stream, ctx->L, scratch, rhs, x, ctx->d.cs);
+  CK(cudaGetLastError());
+  return XG_OK;
+}
+
 int xg_lu_info(xg_ctx *ctx, long long *nnz_lu, int *fl, int *ll, int *ul) {
   if (!ctx) return XG_ERR_ARG;
   if (!ctx->lu_ready) return fail(ctx, XG_ERR_STATE, "no LU analysis");

@@ -155,6 +155,11 @@ struct SchedDev {
   int n_hub = 0, n_groups = 0, n_top_items = 0;
 };
 
+// Allocation-free solve (xg_lu_solve_noalloc): largest system it accepts and
+// the number of devices whose scratch address is cached.
+constexpr int kNoAllocMaxN = XG_NOALLOC_MAX_N;
+constexpr int kNoAllocMaxDevices = 64;
+
 constexpr int kLongColumn = 512;   // factor columns longer than this use the whole CTA
 constexpr int kHubFanout = 64;     // items with more dependents than this run in the prologue
 constexpr int kGroupCap = 512;     // items per dependency-closed group
@@ -222,5 +227,8 @@ void launch_lu_factor_k(cudaStream_t st, const LUDev &L, const double *vals, Cir
                         double pivot_tol);
 void launch_lu_solve_k(cudaStream_t st, const LUDev &L, const double *b, double *x, const CircState *cs,
                        int masked);
+int noalloc_scratch(int device, double **out, std::string &err);
+void launch_lu_solve_noalloc_k(cudaStream_t st, LUDev L, double *scratch, const double *b, double *x,
+                               const CircState *cs);
 
 }  // namespace xg

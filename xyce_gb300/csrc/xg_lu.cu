@@ -21,11 +21,17 @@
 // schedule backwards (its dependency graph is the factor graph reversed).
 #include <cuda_runtime.h>
 
+#include <mutex>
+#include <string>
+
 #include "xg_internal.h"
 
 namespace xg {
 
 constexpr int kGroupThreads = 512;  // threads of a group CTA (the top uses 1024)
+
+void launch_lu_solve_k(cudaStream_t st, const LUDev &L, const double *b, double *x, const CircState *cs,
+                       int masked);
 
 __device__ __forceinline__ bool item_active(const LUDev &L, const CircState *cs, int masked, int j) {
   if (!masked) return true;
@@ -270,6 +276,47 @@ __global__ void __launch_bounds__(256) k_usolve_hubs(LUDev L, double *__restrict
   const int k = L.fs.items[blockIdx.x];
   if (!item_active(L, cs, masked, k)) return;
   solve_row<false, true>(L, nullptr, x, k, threadIdx.x, sm);
+}
+
+// ---- allocation-free solve --------------------------------------------------
+// Scratch of xg_lu_solve_noalloc: the intermediate vector y of L y = P b, in a
+// file-scope device array that every GPU loading the library holds until the
+// process exits (kNoAllocMaxN doubles = 2 MiB).  All calls share it.
+static __device__ __align__(256) double g_noalloc_y[kNoAllocMaxN];
+
+namespace {
+std::mutex g_noalloc_mu;
+double *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+}  // namespace
+
+// Device address of the scratch on `device` (which must be current); looked
+// up once per device with cudaGetSymbolAddress — a host-side reference to
+// g_noalloc_y is not a device address.
+int noalloc_scratch(int device, double **out, std::string &err) {
+  if (device < 0 || device >= kNoAllocMaxDevices) {
+    err = "device ordinal out of range for the allocation-free scratch";
+    return XG_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_y);
+    if (e != cudaSuccess || !p) {
+      err = std::string("cudaGetSymbolAddress(g_noalloc_y): ") + cudaGetErrorString(e);
+      return XG_ERR_CUDA;
+    }
+    g_noalloc_ptr[device] = static_cast<double *>(p);
+  }
+  *out = g_noalloc_ptr[device];
+  return XG_OK;
+}
+
+// The triangular solves of launch_lu_solve_k with the static scratch in place
+// of the analysis' y vector (unmasked: every row is solved).
+void launch_lu_solve_noalloc_k(cudaStream_t st, LUDev L, double *scratch, const double *b, double *x,
+                               const CircState *cs) {
+  L.y = scratch;
+  launch_lu_solve_k(st, L, b, x, cs, 0);
 }
 
 // ---- launchers --------------------------------------------------------------
