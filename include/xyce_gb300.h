@@ -166,6 +166,19 @@ int xg_lu_solve(xg_ctx *ctx, const double *rhs, double *x);
 #define XG_NOALLOC_MAX_N 262144
 int xg_lu_solve_noalloc(xg_ctx *ctx, const double *rhs, double *x);
 
+/* Precision of the factors used by xg_lu_factor / xg_lu_solve and by the
+ * transient driver.  XG_PREC_FP64 (default): FP64 factors, one solve.
+ * XG_PREC_FP32_IR: FP32 factors, then n_refine steps of FP64 iterative
+ * refinement per solve (r = b - A x with the FP64 values last passed to
+ * xg_lu_factor, x += (LU)^-1 r) — the precedent is Xyce's IRSolver
+ * (src/LinearAlgebraServicesPKG/N_LAS_IRSolver.C:428-560), which refines
+ * with a stale factorization.  Those values must stay unchanged until the
+ * solves that use them are done.  Takes effect at the next xg_lu_analyze (or
+ * transient); not allowed while a transient is in progress. */
+#define XG_PREC_FP64     0
+#define XG_PREC_FP32_IR  1
+int xg_lu_set_precision(xg_ctx *ctx, int precision, int n_refine);
+
 /* Statistics of the current analysis: nnz(L+U), factor/solve level counts. */
 int xg_lu_info(xg_ctx *ctx, long long *nnz_lu, int *factor_levels, int *lsolve_levels,
                int *usolve_levels);

@@ -6,6 +6,7 @@
 // Xyce tree).
 #include "oracle.h"
 #include "devices.h"
+#include "bsim4.h"
 
 #include <algorithm>
 #include <chrono>
@@ -215,9 +216,11 @@ struct orc_ctx {
   std::vector<int> i_p, i_n; std::vector<Wave> i_w;
   std::vector<int> d_p, d_n, d_pri; std::vector<DiodeT> d_t;
   std::vector<int> m_d, m_g, m_s, m_b; std::vector<Mos1T> m_t;
+  std::vector<int> b_d, b_g, b_s, b_b; std::vector<b4::Inst> b_t;
+  std::vector<double> b_von;  // BSIM4 instance member von (last evaluation's Vth)
   // pattern (CSR) and per-device stamp positions
   std::vector<int> rp, ci;
-  std::vector<int> pos_r, pos_c, pos_v, pos_d, pos_m;
+  std::vector<int> pos_r, pos_c, pos_v, pos_d, pos_m, pos_b;
   // CSC view for the LU
   std::vector<int> Ap, Ai, csr2csc;
   std::vector<double> Ax;
@@ -228,8 +231,9 @@ struct orc_ctx {
   double *wall_log = nullptr;  // optional: wall-clock seconds at each accepted step
   int wall_cap = 0;
   bool finalized = false;
-  // state layout: store diode [vd,qd,cd] then mos1 [vbd,vbs,vgs,vds,von,gm];
-  // state mos1 [capgs,capgd,capgb,qgs,qgd,qgb,qbd,qbs]  (field-major, SoA)
+  // state layout: store diode [vd,qd,cd] then mos1 [vbd,vbs,vgs,vds,von,gm]
+  // then bsim4 [vbd,vbs,vgs,vds,von]; state mos1 [capgs,capgd,capgb,qgs,qgd,
+  // qgb,qbd,qbs] then bsim4 [qg,qd,qb]  (field-major, SoA)
 };
 
 namespace {
@@ -266,6 +270,12 @@ void stamp_pairs(orc_ctx *c, std::vector<std::pair<int, int>> &all) {
   }
   for (size_t k = 0; k < c->m_d.size(); ++k) {
     int nd[4] = {c->m_d[k], c->m_g[k], c->m_s[k], c->m_b[k]};
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b) all.push_back({nd[a], nd[b]});
+  }
+  // BSIM4 without internal nodes: full 4x4 over (D,G,S,B)
+  for (size_t k = 0; k < c->b_d.size(); ++k) {
+    int nd[4] = {c->b_d[k], c->b_g[k], c->b_s[k], c->b_b[k]};
     for (int a = 0; a < 4; ++a)
       for (int b = 0; b < 4; ++b) all.push_back({nd[a], nd[b]});
   }
@@ -332,6 +342,19 @@ int orc_add_mosfet1(orc_ctx *c, int n, const int *d, const int *g, const int *s,
   return 0;
 }
 
+int orc_add_bsim4(orc_ctx *c, int n, const int *d, const int *g, const int *s, const int *b,
+                  const double *params) {
+  for (int k = 0; k < n; ++k) {
+    b4::Inst I;
+    std::string why;
+    if (b4::setup(params + (size_t)k * b4::P_COUNT, I, &why) != 0) return -4;
+    c->b_d.push_back(d[k]); c->b_g.push_back(g[k]); c->b_s.push_back(s[k]); c->b_b.push_back(b[k]);
+    c->b_t.push_back(I);
+    c->b_von.push_back(0.0);  // Instance constructor: von(0.0), N_DEV_MOSFET_B4.C:4995
+  }
+  return 0;
+}
+
 // Builder::generateGraphs + setupPointers restated: the CSR pattern is the
 // union of every device's jacobianStamp; each stamp caches its position.
 int orc_finalize(orc_ctx *c) {
@@ -364,6 +387,7 @@ int orc_finalize(orc_ctx *c) {
   fill(c->pos_v, o, 4 * c->v_p.size()); o += 4 * c->v_p.size();
   fill(c->pos_d, o, 7 * c->d_p.size()); o += 7 * c->d_p.size();
   fill(c->pos_m, o, 16 * c->m_d.size()); o += 16 * c->m_d.size();
+  fill(c->pos_b, o, 16 * c->b_d.size()); o += 16 * c->b_d.size();
   // CSC structure of the same pattern
   int nnz = (int)c->ci.size();
   c->Ap.assign(c->n + 1, 0);
@@ -377,8 +401,8 @@ int orc_finalize(orc_ctx *c) {
       c->Ai[q] = i; c->csr2csc[p] = q;
     }
   c->Ax.resize(nnz);
-  c->nsto = 3 * (int)c->d_p.size() + 6 * (int)c->m_d.size();
-  c->nsta = 8 * (int)c->m_d.size();
+  c->nsto = 3 * (int)c->d_p.size() + 6 * (int)c->m_d.size() + 5 * (int)c->b_d.size();
+  c->nsta = 8 * (int)c->m_d.size() + 3 * (int)c->b_d.size();
   c->finalized = true;
   return 0;
 }
@@ -545,6 +569,115 @@ int orc_load(orc_ctx *c, double time, const double *x, const double *sta_curr, c
     addm(dQdx, J(2, 3), -gcbs * M);
     addm(dQdx, J(2, 2), (gcbs + gcgs) * M);
   }
+
+  // BSIM4: Master::updateState / loadDAEVectors / loadDAEMatrices
+  // (N_DEV_MOSFET_B4.C:10540-11687), limiting per updateIntermediateVars4p82_
+  // (N_DEV_MOSFET_B4p82.C:3016-3240)
+  const int nb = (int)c->b_d.size();
+  const int sob = 3 * nd + 6 * nm, stb = 8 * nm;
+  for (int k = 0; k < nb; ++k) {
+    const b4::Inst &I = c->b_t[k];
+    const int D = c->b_d[k], G = c->b_g[k], S = c->b_s[k], Bn = c->b_b[k];
+    const double dt = I.dtype, M = I.M;
+    double vgs = dt * (X(G) - X(S)), vds = dt * (X(D) - X(S)), vbs = dt * (X(Bn) - X(S));
+    double vbd = vbs - vds, vgd = vgs - vds;
+    const double vgs_o = vgs, vds_o = vds, vbs_o = vbs;
+    int origFlag = 1;
+    if (initJct) {
+      vds = 0.1; vgs = dt * I.vth0 + 0.1; vbs = 0.0;
+      vbd = vbs - vds; vgd = vgs - vds;
+      origFlag = 0;
+    }
+    double vbd_old, vbs_old, vgs_old, vds_old;
+    if (newton_iter == 0 && dcop) {
+      vbd_old = vbd; vbs_old = vbs; vgs_old = vgs; vds_old = vds;
+    } else {
+      const double *h = (newton_iter == 0) ? sto_curr : sto_next_in;
+      vbd_old = h[sob + k]; vbs_old = h[sob + nb + k]; vgs_old = h[sob + 2 * nb + k]; vds_old = h[sob + 3 * nb + k];
+    }
+    const double von_prev = sto_next_in[sob + 4 * nb + k];  // instance member von: last evaluation
+    const double vgd_old = vgs_old - vds_old;
+    if (!initJct) {
+      int Check = 0;
+      if (vds_old >= 0.0) {
+        vgs = fetlim(vgs, vgs_old, von_prev);
+        vds = vgs - vgd;
+        vds = limvds(vds, vds_old);
+        vgd = vgs - vds;
+      } else {
+        vgd = fetlim(vgd, vgd_old, von_prev);
+        vds = vgs - vgd;
+        vds = -limvds(-vds, -vds_old);
+        vgs = vgd + vds;
+      }
+      if (vds >= 0.0) {
+        vbs = pnjlim(vbs, vbs_old, b4::kVt0, I.vcrit, &Check);
+        vbd = vbs - vds;
+      } else {
+        vbd = pnjlim(vbd, vbd_old, b4::kVt0, I.vcrit, &Check);
+        vbs = vbd + vds;
+      }
+    }
+    vbd = vbs - vds;
+    const double eps = 2.220446049250313e-16;
+    if (std::fabs(vbs_o - vbs) > eps || std::fabs(vgs_o - vgs) > eps || std::fabs(vds_o - vds) > eps) origFlag = 0;
+    if (!origFlag) c->last_limited++;
+    // values, then complex-step partials along vgs, vds, vbs
+    b4::Out<double> o;
+    b4::core(I, vgs, vds, vbs, o, -1);
+    double dF[3][3], dq[3][3];  // [output D/S/B or G/D/B][vgs, vds, vbs]
+    const double hcs = 1e-30;
+    for (int dir = 0; dir < 3; ++dir) {
+      using Cx = std::complex<double>;
+      Cx a(vgs, dir == 0 ? hcs : 0.0), bb(vds, dir == 1 ? hcs : 0.0), cc(vbs, dir == 2 ? hcs : 0.0);
+      b4::Out<Cx> oc;
+      b4::core(I, a, bb, cc, oc, dir);
+      dF[0][dir] = oc.Fd.imag() / hcs; dF[1][dir] = oc.Fs.imag() / hcs; dF[2][dir] = oc.Fb.imag() / hcs;
+      dq[0][dir] = oc.qg.imag() / hcs; dq[1][dir] = oc.qd.imag() / hcs; dq[2][dir] = oc.qb.imag() / hcs;
+    }
+    sto_next[sob + k] = vbd; sto_next[sob + nb + k] = vbs;
+    sto_next[sob + 2 * nb + k] = vgs; sto_next[sob + 3 * nb + k] = vds;
+    sto_next[sob + 4 * nb + k] = o.von;
+    c->b_von[k] = o.von;
+    sta_next[stb + k] = o.qg; sta_next[stb + nb + k] = o.qd; sta_next[stb + 2 * nb + k] = o.qb;
+    addv(F, D, o.Fd * M); addv(F, S, o.Fs * M); addv(F, Bn, o.Fb * M);
+    addv(Q, G, dt * o.qg * M); addv(Q, D, dt * o.qd * M); addv(Q, Bn, dt * o.qb * M);
+    addv(Q, S, -dt * (o.qg + o.qd + o.qb) * M);
+    if (!origFlag) {
+      const double dv[3] = {vgs - vgs_o, vds - vds_o, vbs - vbs_o};
+      double lf[3] = {0, 0, 0}, lq[3] = {0, 0, 0};
+      for (int a = 0; a < 3; ++a)
+        for (int j = 0; j < 3; ++j) { lf[a] += dF[a][j] * dv[j]; lq[a] += dq[a][j] * dv[j]; }
+      addv(dFdxdVp, D, lf[0] * M); addv(dFdxdVp, S, lf[1] * M); addv(dFdxdVp, Bn, lf[2] * M);
+      // the gate-charge limiter terms carry no dtype (N_DEV_MOSFET_B4.C:7215-7232)
+      addv(dQdxdVp, G, lq[0] * M); addv(dQdxdVp, D, lq[1] * M); addv(dQdxdVp, Bn, lq[2] * M);
+      addv(dQdxdVp, S, -(lq[0] + lq[1] + lq[2]) * M);
+    }
+    // node columns: G <- vgs, D <- vds, B <- vbs, S <- -(sum); rows D,G,S,B = 0,1,2,3
+    const int *ps = &c->pos_b[16 * k];
+    auto Jp = [&](int a, int b) { return ps[4 * a + b]; };
+    const int rowF[3] = {0, 2, 3};   // D, S, B
+    const int rowQ[3] = {1, 0, 3};   // G, D, B
+    const int colv[3] = {1, 0, 3};   // vgs -> G, vds -> D, vbs -> B
+    for (int a = 0; a < 3; ++a) {
+      double sf = 0.0, sq = 0.0;
+      for (int j = 0; j < 3; ++j) {
+        addm(dFdx, Jp(rowF[a], colv[j]), dt * dF[a][j] * M);
+        addm(dQdx, Jp(rowQ[a], colv[j]), dq[a][j] * M);
+        sf += dF[a][j]; sq += dq[a][j];
+      }
+      addm(dFdx, Jp(rowF[a], 2), -dt * sf * M);
+      addm(dQdx, Jp(rowQ[a], 2), -sq * M);
+    }
+    // source row of Q: -(qg + qd + qb)
+    double ss = 0.0;
+    for (int j = 0; j < 3; ++j) {
+      const double v = -(dq[0][j] + dq[1][j] + dq[2][j]);
+      addm(dQdx, Jp(2, colv[j]), v * M);
+      ss += v;
+    }
+    addm(dQdx, Jp(2, 2), -ss * M);
+  }
   return 0;
 }
 
@@ -596,6 +729,13 @@ bool device_limited(orc_ctx *c, Work &) { return c->last_limited > 0; }
 
 void assemble(orc_ctx *c, Work &w, double time, int iter, int flags, const Coef &cf) {
   double t0 = now();
+  // BSIM4 limiting reads von of the instance's last evaluation (an instance
+  // member in the reference); orc_load takes it from the von plane of its
+  // store input
+  {
+    const int nb = (int)c->b_d.size(), sob = 3 * (int)c->d_p.size() + 6 * (int)c->m_d.size();
+    for (int k = 0; k < nb; ++k) w.sto_prev[sob + 4 * nb + k] = c->b_von[k];
+  }
   orc_load(c, time, w.x.data(), w.sta_curr.data(), w.sto_curr.data(), w.sto_prev.data(), iter, flags,
            w.sta_next.data(), w.sto_next.data(), w.F.data(), w.Q.data(), w.B.data(), w.dFv.data(),
            w.dQv.data(), w.dFdx.data(), w.dQdx.data());

@@ -52,6 +52,10 @@ int orc_add_diodes(orc_ctx *c, int n, const int *pos, const int *neg, const int 
                    const double *params);
 int orc_add_mosfet1(orc_ctx *c, int n, const int *d, const int *g, const int *s, const int *b,
                     const double *params);
+/* BSIM 4.8.2 (level 54), restated scope in bsim4.h; params n x b4::P_COUNT
+ * (NaN = not given).  Returns -4 for a card outside that scope. */
+int orc_add_bsim4(orc_ctx *c, int n, const int *d, const int *g, const int *s, const int *b,
+                  const double *params);
 int orc_finalize(orc_ctx *c);
 
 int orc_sizes(orc_ctx *c, int *n_unknowns, int *nnz, int *n_state, int *n_store);

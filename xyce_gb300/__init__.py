@@ -32,6 +32,7 @@ XG_OK = 0
 XG_ERR = {-1: "ARG", -2: "CUDA", -3: "STATE", -4: "UNSUPPORTED", -6: "NAN", -9: "SINGULAR",
           -10: "TIMEOUT"}
 LOAD_ALL, LOAD_LINEAR, LOAD_NONLINEAR = 0, 1, 2
+PREC_FP64, PREC_FP32_IR = 0, 1
 FLAG_DCOP, FLAG_INITJCT = 1, 2
 
 # Every symbol declared in include/xyce_gb300.h.
@@ -41,7 +42,7 @@ EXPORTED = [
     "xg_add_isources", "xg_add_diodes", "xg_add_mosfet1", "xg_finalize", "xg_get_sizes",
     "xg_get_pattern", "xg_update_sources", "xg_update_state", "xg_load_dae_vectors",
     "xg_load_dae_matrices", "xg_lu_analyze", "xg_lu_factor", "xg_lu_solve",
-    "xg_lu_solve_noalloc", "xg_lu_info",
+    "xg_lu_solve_noalloc", "xg_lu_set_precision", "xg_lu_info",
     "xg_transient", "xg_tran_start", "xg_tran_advance", "xg_tran_results", "xg_tran_end",
     "xg_dcop", "xg_version",
 ]
@@ -115,6 +116,7 @@ def lib() -> C.CDLL:
     L.xg_lu_factor.argtypes = [P, P]
     L.xg_lu_solve.argtypes = [P, P, P]
     L.xg_lu_solve_noalloc.argtypes = [P, P, P]
+    L.xg_lu_set_precision.argtypes = [P, I, I]
     L.xg_lu_info.argtypes = [P, C.POINTER(C.c_longlong), C.POINTER(I), C.POINTER(I), C.POINTER(I)]
     L.xg_transient.argtypes = [P, C.POINTER(TranParams), I, ip, I, ip, dp, dp, C.POINTER(TranStats)]
     L.xg_tran_start.argtypes = [P, C.POINTER(TranParams), I, ip, I]
@@ -215,6 +217,10 @@ class Circuit:
     def lu_solve_noalloc(self, rhs, x):
         """xg_lu_solve without allocated scratch (see include/xyce_gb300.h)."""
         self._check(lib().xg_lu_solve_noalloc(self.h, _ptr(rhs), _ptr(x)))
+
+    def lu_set_precision(self, precision: int, n_refine: int = 2):
+        """PREC_FP64, or PREC_FP32_IR: FP32 factors + n_refine FP64 refinement steps."""
+        self._check(lib().xg_lu_set_precision(self.h, int(precision), int(n_refine)))
 
     def lu_info(self):
         nnz = C.c_longlong()

@@ -50,6 +50,7 @@ struct xg_ctx {
   LUDev L;
   bool lu_ready = false;
   int n_analyze = 0;
+  int lu_prec = XG_PREC_FP64, lu_refine = 2;  // xg_lu_set_precision
   std::vector<void *> allocs;      // device allocations owned by the context
   std::vector<void *> lu_allocs;   // allocations of the current LU analysis
   int *status_host = nullptr;      // mapped [finished, breakdown]
@@ -657,6 +658,16 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
 #undef UP
   if ((rc = dev_alloc(ctx, &L.lu, (size_t)L.nnz, A))) return rc;
   if ((rc = dev_alloc(ctx, &L.y, (size_t)H.n, A))) return rc;
+  if (ctx->lu_prec == XG_PREC_FP32_IR) {
+    if ((rc = dev_alloc(ctx, &L.lu32, (size_t)L.nnz, A))) return rc;
+    if ((rc = dev_alloc(ctx, &L.ir_r, (size_t)H.n, A))) return rc;
+    L.mixed = 1;
+    L.n_refine = ctx->lu_refine;
+    L.a_rp = ctx->d.rp;
+    L.a_ci = ctx->d.ci;
+    L.a_circ = ctx->d.circ_of_row;
+    L.a_vals = ctx->d.J;  // the transient's Jacobian; xg_lu_factor points it at its values
+  }
   L.breakdown = ctx->breakdown_dev;
   L.f_levels = (int)H.f_lvl_ptr.size() - 1;
   L.l_levels = (int)H.l_lvl_ptr.size() - 1;
@@ -689,6 +700,7 @@ int xg_lu_factor(xg_ctx *ctx, const double *vals) {
   if (!ctx || !vals) return XG_ERR_ARG;
   if (!ctx->lu_ready) return fail(ctx, XG_ERR_STATE, "call xg_lu_analyze first");
   CK(cudaMemsetAsync(ctx->breakdown_dev, 0, sizeof(int), ctx->stream));
+  if (ctx->L.mixed) ctx->L.a_vals = vals;
   launch_lu_factor_k(ctx->stream, ctx->L, vals, ctx->d.cs, 0, kRuntimePivotTol);
   CK(cudaGetLastError());
   int bd = 0;
@@ -734,6 +746,18 @@ int xg_lu_solve_noalloc(xg_ctx *ctx, const double *rhs, double *x) {
   if (rc) return fail(ctx, rc, err);
   launch_lu_solve_noalloc_k(ctx->stream, ctx->L, scratch, rhs, x, ctx->d.cs);
   CK(cudaGetLastError());
+  return XG_OK;
+}
+
+int xg_lu_set_precision(xg_ctx *ctx, int precision, int n_refine) {
+  if (!ctx) return XG_ERR_ARG;
+  if (precision != XG_PREC_FP64 && precision != XG_PREC_FP32_IR)
+    return fail(ctx, XG_ERR_ARG, "precision must be XG_PREC_FP64 or XG_PREC_FP32_IR");
+  if (n_refine < 0 || n_refine > 16) return fail(ctx, XG_ERR_ARG, "n_refine must be in [0, 16]");
+  if (ctx->run) return fail(ctx, XG_ERR_STATE, "precision cannot change during a transient");
+  ctx->lu_prec = precision;
+  ctx->lu_refine = n_refine;
+  ctx->lu_ready = false;  // the next xg_lu_analyze (or transient) builds factors of this precision
   return XG_OK;
 }
 

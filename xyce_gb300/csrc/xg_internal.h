@@ -179,6 +179,14 @@ struct LUDev {
   int *upd_off = nullptr, *upd_pos = nullptr;  // per U entry: target positions of its update
   SchedDev fs, ls;           // factor (and, backwards, U solve) / L-solve schedules
   int f_levels = 0, l_levels = 0, u_levels = 0;  // plain level counts (statistics)
+  // Mixed precision (FP32 factors, FP64 iterative refinement): lu32 holds the
+  // factors; each solve is refined n_refine times against the FP64 matrix
+  // a_vals (CSR a_rp/a_ci in unknown order, the values last factored).
+  int mixed = 0, n_refine = 0;
+  float *lu32 = nullptr;
+  double *ir_r = nullptr;
+  const int *a_rp = nullptr, *a_ci = nullptr, *a_circ = nullptr;
+  const double *a_vals = nullptr;
 };
 
 // Host-side analysis result.

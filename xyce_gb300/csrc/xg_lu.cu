@@ -70,23 +70,28 @@ __device__ __forceinline__ double team_sum(double v, double *sm) {
   return r;
 }
 
-template <bool BLOCK>
+// Factor values of precision T: L.lu (FP64) or L.lu32 (FP32, refined solves).
+template <typename T> __device__ __forceinline__ T *lu_of(const LUDev &L);
+template <> __device__ __forceinline__ double *lu_of<double>(const LUDev &L) { return L.lu; }
+template <> __device__ __forceinline__ float *lu_of<float>(const LUDev &L) { return L.lu32; }
+
+template <bool BLOCK, typename T>
 __device__ void factor_column(const LUDev &L, const double *__restrict__ vals, int j, CircState *cs,
                               int masked, double pivot_tol, double *sm) {
   const int lane = BLOCK ? (int)threadIdx.x : (int)(threadIdx.x & 31);
   const int nl = BLOCK ? (int)blockDim.x : 32;
   const int p0 = L.cp[j], p1 = L.cp[j + 1], pd = L.diag[j];
-  double *lu = L.lu;
+  T *lu = lu_of<T>(L);
   for (int p = p0 + lane; p < p1; p += nl) {
     const int s = L.src[p];
-    lu[p] = (s >= 0) ? vals[s] : 0.0;
+    lu[p] = (s >= 0) ? (T)vals[s] : (T)0;
   }
   team_sync<BLOCK>();
   double lost = 0.0;
   for (int p = p0; p < pd; ++p) {
     const int k = L.ri[p];
-    const double ukj = lu[p];
-    if (ukj != 0.0) {
+    const T ukj = lu[p];
+    if (ukj != (T)0) {
       // positions of L(:,k)'s rows in column j come from the analysis
       const int q0 = L.diag[k] + 1, q1 = L.cp[k + 1];
       const int *tgt = L.upd_pos + L.upd_off[p];
@@ -98,9 +103,9 @@ __device__ void factor_column(const LUDev &L, const double *__restrict__ vals, i
     }
     team_sync<BLOCK>();
   }
-  const double d = lu[pd];
+  const double d = (double)lu[pd];
   double amax = 0.0;
-  for (int p = pd + lane; p < p1; p += nl) amax = fmax(amax, fabs(lu[p]));
+  for (int p = pd + lane; p < p1; p += nl) amax = fmax(amax, fabs((double)lu[p]));
   amax = team_max<BLOCK>(amax, sm);
   lost = team_max<BLOCK>(lost, sm);
   // The threshold only matters when row j of U has entries right of the
@@ -115,22 +120,25 @@ __device__ void factor_column(const LUDev &L, const double *__restrict__ vals, i
     }
     return;
   }
-  const double inv = 1.0 / d;
+  const T inv = (T)1 / lu[pd];
   for (int p = pd + 1 + lane; p < p1; p += nl) lu[p] *= inv;
 }
 
 // y[i] = b[row_of_step[i]] - sum_k L(i,k) y[k]          (LOWER)
-// y[i] = (y[i] - sum_j U(i,j) y[j]) / U(i,i); x[col_of_step[i]] = y[i]   (upper)
-// Team: 8 lanes (width 8) or the whole CTA (BLOCK).
-template <bool LOWER, bool BLOCK>
+// y[i] = (y[i] - sum_j U(i,j) y[j]) / U(i,i); x[col_of_step[i]] = y[i]   (upper;
+//   ACC: x[col_of_step[i]] += y[i], the correction step of a refined solve)
+// Team: 8 lanes (width 8) or the whole CTA (BLOCK).  Factors of precision T,
+// accumulation in FP64.
+template <bool LOWER, bool BLOCK, typename T, bool ACC>
 __device__ void solve_row(const LUDev &L, const double *__restrict__ b, double *__restrict__ x, int i,
                           int sub, double *sm) {
   const int *ptr = LOWER ? L.l_ptr : L.u_ptr;
   const int *pos = LOWER ? L.l_pos : L.u_pos;
   const int *col = LOWER ? L.l_col : L.u_col;
+  const T *lu = lu_of<T>(L);
   const int nl = BLOCK ? (int)blockDim.x : 8;
   double sum = 0.0;
-  for (int t = ptr[i] + sub; t < ptr[i + 1]; t += nl) sum += L.lu[pos[t]] * L.y[col[t]];
+  for (int t = ptr[i] + sub; t < ptr[i + 1]; t += nl) sum += (double)lu[pos[t]] * L.y[col[t]];
   if (BLOCK) {
     sum = team_sum<true>(sum, sm);
   } else {
@@ -140,22 +148,25 @@ __device__ void solve_row(const LUDev &L, const double *__restrict__ b, double *
     if (LOWER) {
       L.y[i] = b[L.row_of_step[i]] - sum;
     } else {
-      const double z = (L.y[i] - sum) / L.lu[L.diag[i]];
+      const double z = (L.y[i] - sum) / (double)lu[L.diag[i]];
       L.y[i] = z;
-      x[L.col_of_step[i]] = z;
+      if (ACC) x[L.col_of_step[i]] += z;
+      else x[L.col_of_step[i]] = z;
     }
   }
 }
 
 // ---- factorization ----------------------------------------------------------
+template <typename T>
 __global__ void __launch_bounds__(256) k_factor_hubs(LUDev L, const double *__restrict__ vals, CircState *cs,
                                                      int masked, double pivot_tol) {
   __shared__ double sm[32];
   const int j = L.fs.items[blockIdx.x];
   if (!item_active(L, cs, masked, j)) return;
-  factor_column<true>(L, vals, j, cs, masked, pivot_tol, sm);
+  factor_column<true, T>(L, vals, j, cs, masked, pivot_tol, sm);
 }
 
+template <typename T>
 __global__ void __launch_bounds__(1024) k_factor_groups(LUDev L, const double *__restrict__ vals, CircState *cs,
                                                         int masked, double pivot_tol, int top) {
   __shared__ double sm[32];
@@ -168,13 +179,13 @@ __global__ void __launch_bounds__(1024) k_factor_groups(LUDev L, const double *_
     for (int t = b + warp; t < e; t += nwarps) {
       const int j = S.items[t];
       if (S.is_long[j]) { any_long = true; continue; }
-      if (item_active(L, cs, masked, j)) factor_column<false>(L, vals, j, cs, masked, pivot_tol, sm);
+      if (item_active(L, cs, masked, j)) factor_column<false, T>(L, vals, j, cs, masked, pivot_tol, sm);
     }
     if (__syncthreads_or(any_long)) {
       for (int t = b; t < e; ++t) {
         const int j = S.items[t];
         if (!S.is_long[j] || !item_active(L, cs, masked, j)) continue;
-        factor_column<true>(L, vals, j, cs, masked, pivot_tol, sm);
+        factor_column<true, T>(L, vals, j, cs, masked, pivot_tol, sm);
         __syncthreads();
       }
     }
@@ -190,10 +201,12 @@ __global__ void k_lsolve_hubs(LUDev L, const double *__restrict__ b, const CircS
   L.y[i] = b[L.row_of_step[i]];  // hubs have no L entries
 }
 
+template <typename T>
 __global__ void __launch_bounds__(1024) k_lsolve_groups(LUDev L, const double *__restrict__ b,
                                                         const CircState *cs, int masked, int top) {
   __shared__ double sm[32];
   const SchedDev &S = L.ls;
+  const T *lu = lu_of<T>(L);
   const int g = top ? S.n_groups : (int)blockIdx.x;
   const int team = threadIdx.x >> 3, nteams = blockDim.x >> 3, sub = threadIdx.x & 7;
   for (int lv = S.grp_lvl[g]; lv < S.grp_lvl[g + 1]; ++lv) {
@@ -212,7 +225,8 @@ __global__ void __launch_bounds__(1024) k_lsolve_groups(LUDev L, const double *_
       if (__any_sync(0xffffffffu, act)) {
         double sum = 0.0;
         if (act)
-          for (int q = L.l_ptr[i] + sub; q < L.l_ptr[i + 1]; q += 8) sum += L.lu[L.l_pos[q]] * L.y[L.l_col[q]];
+          for (int q = L.l_ptr[i] + sub; q < L.l_ptr[i + 1]; q += 8)
+            sum += (double)lu[L.l_pos[q]] * L.y[L.l_col[q]];
         for (int o = 4; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, 8);
         if (act && sub == 0) L.y[i] = b[L.row_of_step[i]] - sum;
       }
@@ -221,7 +235,7 @@ __global__ void __launch_bounds__(1024) k_lsolve_groups(LUDev L, const double *_
       for (int t = bb; t < e; ++t) {
         const int i = S.items[t];
         if (!S.is_long[i] || !item_active(L, cs, masked, i)) continue;
-        solve_row<true, true>(L, b, nullptr, i, threadIdx.x, sm);
+        solve_row<true, true, T, false>(L, b, nullptr, i, threadIdx.x, sm);
         __syncthreads();
       }
     }
@@ -229,10 +243,12 @@ __global__ void __launch_bounds__(1024) k_lsolve_groups(LUDev L, const double *_
 }
 
 // ---- U solve (factor schedule, backward) ------------------------------------
+template <typename T, bool ACC>
 __global__ void __launch_bounds__(1024) k_usolve_groups(LUDev L, double *__restrict__ x, const CircState *cs,
                                                         int masked, int top) {
   __shared__ double sm[32];
   const SchedDev &S = L.fs;
+  const T *lu = lu_of<T>(L);
   const int g = top ? S.n_groups : (int)blockIdx.x;
   const int team = threadIdx.x >> 3, nteams = blockDim.x >> 3, sub = threadIdx.x & 7;
   for (int lv = S.grp_lvl[g + 1] - 1; lv >= S.grp_lvl[g]; --lv) {
@@ -250,12 +266,14 @@ __global__ void __launch_bounds__(1024) k_usolve_groups(LUDev L, double *__restr
       if (__any_sync(0xffffffffu, act)) {
         double sum = 0.0;
         if (act)
-          for (int q = L.u_ptr[k] + sub; q < L.u_ptr[k + 1]; q += 8) sum += L.lu[L.u_pos[q]] * L.y[L.u_col[q]];
+          for (int q = L.u_ptr[k] + sub; q < L.u_ptr[k + 1]; q += 8)
+            sum += (double)lu[L.u_pos[q]] * L.y[L.u_col[q]];
         for (int o = 4; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, 8);
         if (act && sub == 0) {
-          const double z = (L.y[k] - sum) / L.lu[L.diag[k]];
+          const double z = (L.y[k] - sum) / (double)lu[L.diag[k]];
           L.y[k] = z;
-          x[L.col_of_step[k]] = z;
+          if (ACC) x[L.col_of_step[k]] += z;
+          else x[L.col_of_step[k]] = z;
         }
       }
     }
@@ -263,19 +281,42 @@ __global__ void __launch_bounds__(1024) k_usolve_groups(LUDev L, double *__restr
       for (int t = bb; t < e; ++t) {
         const int k = S.items[t];
         if (!S.is_long_rev[k] || !item_active(L, cs, masked, k)) continue;
-        solve_row<false, true>(L, nullptr, x, k, threadIdx.x, sm);
+        solve_row<false, true, T, ACC>(L, nullptr, x, k, threadIdx.x, sm);
         __syncthreads();
       }
     }
   }
 }
 
+template <typename T, bool ACC>
 __global__ void __launch_bounds__(256) k_usolve_hubs(LUDev L, double *__restrict__ x, const CircState *cs,
                                                      int masked) {
   __shared__ double sm[32];
   const int k = L.fs.items[blockIdx.x];
   if (!item_active(L, cs, masked, k)) return;
-  solve_row<false, true>(L, nullptr, x, k, threadIdx.x, sm);
+  solve_row<false, true, T, ACC>(L, nullptr, x, k, threadIdx.x, sm);
+}
+
+// ---- FP64 residual of a refined solve ---------------------------------------
+// r = b - A x over the rows of active circuits, A in the context's CSR order
+// (IRSolver's residual step, src/LinearAlgebraServicesPKG/N_LAS_IRSolver.C:482-540).
+// One 8-lane team per row.
+__global__ void __launch_bounds__(256) k_ir_residual(LUDev L, const double *__restrict__ b,
+                                                     const double *__restrict__ x, const CircState *cs,
+                                                     int masked) {
+  const int row = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 3);
+  const int sub = threadIdx.x & 7;
+  const bool in = row < L.n;
+  bool act = in;
+  if (in && masked) {
+    const CircState &s = cs[L.a_circ[row]];
+    act = s.need_solve && !s.singular && (s.phase == PH_DC || s.phase == PH_TRAN);
+  }
+  double sum = 0.0;
+  if (act)
+    for (int e = L.a_rp[row] + sub; e < L.a_rp[row + 1]; e += 8) sum += L.a_vals[e] * x[L.a_ci[e]];
+  for (int o = 4; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, 8);
+  if (act && sub == 0) L.ir_r[row] = b[row] - sum;
 }
 
 // ---- allocation-free solve --------------------------------------------------
@@ -320,21 +361,48 @@ void launch_lu_solve_noalloc_k(cudaStream_t st, LUDev L, double *scratch, const 
 }
 
 // ---- launchers --------------------------------------------------------------
-void launch_lu_factor_k(cudaStream_t st, const LUDev &L, const double *vals, CircState *cs, int masked,
-                        double pivot_tol) {
-  if (L.fs.n_hub > 0) k_factor_hubs<<<L.fs.n_hub, 256, 0, st>>>(L, vals, cs, masked, pivot_tol);
-  if (L.fs.n_groups > 0) k_factor_groups<<<L.fs.n_groups, kGroupThreads, 0, st>>>(L, vals, cs, masked, pivot_tol, 0);
-  if (L.fs.n_top_items > 0) k_factor_groups<<<1, 1024, 0, st>>>(L, vals, cs, masked, pivot_tol, 1);
+template <typename T>
+static void factor_sweeps(cudaStream_t st, const LUDev &L, const double *vals, CircState *cs, int masked,
+                          double pivot_tol) {
+  if (L.fs.n_hub > 0) k_factor_hubs<T><<<L.fs.n_hub, 256, 0, st>>>(L, vals, cs, masked, pivot_tol);
+  if (L.fs.n_groups > 0)
+    k_factor_groups<T><<<L.fs.n_groups, kGroupThreads, 0, st>>>(L, vals, cs, masked, pivot_tol, 0);
+  if (L.fs.n_top_items > 0) k_factor_groups<T><<<1, 1024, 0, st>>>(L, vals, cs, masked, pivot_tol, 1);
 }
 
+// FP64 factors, or FP32 factors when the analysis selected the refined solve.
+void launch_lu_factor_k(cudaStream_t st, const LUDev &L, const double *vals, CircState *cs, int masked,
+                        double pivot_tol) {
+  if (L.mixed) factor_sweeps<float>(st, L, vals, cs, masked, pivot_tol);
+  else factor_sweeps<double>(st, L, vals, cs, masked, pivot_tol);
+}
+
+// One forward + backward sweep: x = (LU)^-1 b, or x += (LU)^-1 b (ACC).
+template <typename T, bool ACC>
+static void solve_sweeps(cudaStream_t st, const LUDev &L, const double *b, double *x, const CircState *cs,
+                         int masked) {
+  if (L.ls.n_hub > 0) k_lsolve_hubs<<<(L.ls.n_hub + 255) / 256, 256, 0, st>>>(L, b, cs, masked);
+  if (L.ls.n_groups > 0) k_lsolve_groups<T><<<L.ls.n_groups, kGroupThreads, 0, st>>>(L, b, cs, masked, 0);
+  if (L.ls.n_top_items > 0) k_lsolve_groups<T><<<1, 1024, 0, st>>>(L, b, cs, masked, 1);
+  if (L.fs.n_top_items > 0) k_usolve_groups<T, ACC><<<1, 1024, 0, st>>>(L, x, cs, masked, 1);
+  if (L.fs.n_groups > 0) k_usolve_groups<T, ACC><<<L.fs.n_groups, kGroupThreads, 0, st>>>(L, x, cs, masked, 0);
+  if (L.fs.n_hub > 0) k_usolve_hubs<T, ACC><<<L.fs.n_hub, 256, 0, st>>>(L, x, cs, masked);
+}
+
+// FP64: one solve.  FP32 factors: one solve, then n_refine steps of
+// r = b - A x (FP64), x += (LU)^-1 r.
 void launch_lu_solve_k(cudaStream_t st, const LUDev &L, const double *b, double *x, const CircState *cs,
                        int masked) {
-  if (L.ls.n_hub > 0) k_lsolve_hubs<<<(L.ls.n_hub + 255) / 256, 256, 0, st>>>(L, b, cs, masked);
-  if (L.ls.n_groups > 0) k_lsolve_groups<<<L.ls.n_groups, kGroupThreads, 0, st>>>(L, b, cs, masked, 0);
-  if (L.ls.n_top_items > 0) k_lsolve_groups<<<1, 1024, 0, st>>>(L, b, cs, masked, 1);
-  if (L.fs.n_top_items > 0) k_usolve_groups<<<1, 1024, 0, st>>>(L, x, cs, masked, 1);
-  if (L.fs.n_groups > 0) k_usolve_groups<<<L.fs.n_groups, kGroupThreads, 0, st>>>(L, x, cs, masked, 0);
-  if (L.fs.n_hub > 0) k_usolve_hubs<<<L.fs.n_hub, 256, 0, st>>>(L, x, cs, masked);
+  if (!L.mixed) {
+    solve_sweeps<double, false>(st, L, b, x, cs, masked);
+    return;
+  }
+  solve_sweeps<float, false>(st, L, b, x, cs, masked);
+  const unsigned blocks = (unsigned)(((size_t)L.n * 8 + 255) / 256);
+  for (int k = 0; k < L.n_refine; ++k) {
+    k_ir_residual<<<blocks, 256, 0, st>>>(L, b, x, cs, masked);
+    solve_sweeps<float, true>(st, L, L.ir_r, x, cs, masked);
+  }
 }
 
 }  // namespace xg

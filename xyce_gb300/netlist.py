@@ -169,6 +169,11 @@ class Netlist:
         self.end_circuit()
         return len(self.offsets) - 1
 
+    def circuit_of(self, u: int) -> int:
+        """Index of the circuit that owns unknown u."""
+        self.end_circuit()
+        return int(np.searchsorted(self.offsets, u, side="right") - 1)
+
     def device_count(self) -> int:
         return len(self.res) + len(self.cap) + len(self.vsrc) + len(self.isrc) + \
             len(self.diode) + len(self.mos1)
@@ -333,3 +338,23 @@ def monte_carlo_rings(count=4096, min_stages=11, max_stages=301, seed=4) -> Netl
         nl.end_circuit()
     nl.tran = Tran(tstop=10e-9, hmax=5e-12)
     return nl
+
+
+def extract_circuit(nl: Netlist, ci: int) -> Netlist:
+    """Circuit ci of a batch as a netlist of its own (unknowns renumbered from
+    0, ground kept at -1), with the batch's transient options."""
+    nl.end_circuit()
+    off0, off1 = nl.offsets[ci], nl.offsets[ci + 1]
+    inside = lambda *us: any(off0 <= u < off1 for u in us)
+    rm = lambda u: -1 if u < 0 else u - off0
+    out = Netlist(label=f"{nl.label}.c{ci}")
+    out.n = off1 - off0
+    out.names = {k: v - off0 for k, v in nl.names.items() if off0 <= v < off1}
+    out.res = [(rm(a), rm(b), r) for (a, b, r) in nl.res if inside(a, b)]
+    out.cap = [(rm(a), rm(b), c) for (a, b, c) in nl.cap if inside(a, b)]
+    out.vsrc = [(rm(a), rm(b), rm(br), k, d) for (a, b, br, k, d) in nl.vsrc if inside(br)]
+    out.isrc = [(rm(a), rm(b), k, d) for (a, b, k, d) in nl.isrc if inside(a, b)]
+    out.diode = [(rm(a), rm(b), rm(r), row) for (a, b, r, row) in nl.diode if inside(a, b, r)]
+    out.mos1 = [(rm(d), rm(g), rm(s), rm(b), row) for (d, g, s, b, row) in nl.mos1 if inside(d, g, s, b)]
+    out.tran = nl.tran
+    return out
