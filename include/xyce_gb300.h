@@ -76,6 +76,38 @@ enum {
   XG_MOS1_AD, XG_MOS1_AS, XG_MOS1_PD, XG_MOS1_PS, XG_MOS1_M, XG_MOS1_NPARAM
 };
 
+/* ---- BSIM4 (Xyce level 54, BSIM 4.8.2) parameter row --------------------
+ * Instance (L W AS AD PS PD M) and model parameters, N_DEV_MOSFET_B4.C:337-4840.
+ * A NaN entry means "not given": the library derives it as the reference
+ * does (Model::processParams4p82_, N_DEV_MOSFET_B4p82.C:7769-8136).
+ * Restated scope: the default model selection (capMod 2, mobMod 0, dioMod 1,
+ * every other *MOD 0), no binning, no stress, NF 1, RSH 0 (no internal
+ * nodes), device temperature TNOM = 27 C. */
+enum {
+  XG_B4_TYPE, XG_B4_L, XG_B4_W, XG_B4_AS, XG_B4_AD, XG_B4_PS, XG_B4_PD, XG_B4_M, XG_B4_TOXE,
+  XG_B4_TOXP, XG_B4_TOXM, XG_B4_DTOX, XG_B4_EPSROX, XG_B4_VTH0, XG_B4_VFB, XG_B4_K1, XG_B4_K2,
+  XG_B4_K3, XG_B4_K3B, XG_B4_W0, XG_B4_LPE0, XG_B4_LPEB, XG_B4_DVT0, XG_B4_DVT1, XG_B4_DVT2,
+  XG_B4_DVT0W, XG_B4_DVT1W, XG_B4_DVT2W, XG_B4_DSUB, XG_B4_DROUT, XG_B4_NDEP, XG_B4_NSUB,
+  XG_B4_NSD, XG_B4_NGATE, XG_B4_PHIN, XG_B4_XJ, XG_B4_XT, XG_B4_VBM, XG_B4_VBX, XG_B4_GAMMA1,
+  XG_B4_GAMMA2, XG_B4_CDSC, XG_B4_CDSCB, XG_B4_CDSCD, XG_B4_CIT, XG_B4_NFACTOR, XG_B4_ETA0,
+  XG_B4_ETAB, XG_B4_VOFF, XG_B4_VOFFL, XG_B4_MINV, XG_B4_DVTP0, XG_B4_DVTP1, XG_B4_U0,
+  XG_B4_UA, XG_B4_UB, XG_B4_UC, XG_B4_UD, XG_B4_UP, XG_B4_LP, XG_B4_VSAT, XG_B4_A0, XG_B4_AGS,
+  XG_B4_A1, XG_B4_A2, XG_B4_B0, XG_B4_B1, XG_B4_KETA, XG_B4_DWG, XG_B4_DWB, XG_B4_RDSW,
+  XG_B4_RDSWMIN, XG_B4_PRWG, XG_B4_PRWB, XG_B4_WR, XG_B4_PCLM, XG_B4_PDIBLC1, XG_B4_PDIBLC2,
+  XG_B4_PDIBLCB, XG_B4_PVAG, XG_B4_DELTA, XG_B4_FPROUT, XG_B4_PDITS, XG_B4_PDITSD,
+  XG_B4_PDITSL, XG_B4_PSCBE1, XG_B4_PSCBE2, XG_B4_ALPHA0, XG_B4_ALPHA1, XG_B4_BETA0,
+  XG_B4_AGIDL, XG_B4_BGIDL, XG_B4_CGIDL, XG_B4_EGIDL, XG_B4_AGISL, XG_B4_BGISL, XG_B4_CGISL,
+  XG_B4_EGISL, XG_B4_CGSO, XG_B4_CGDO, XG_B4_CGBO, XG_B4_CGSL, XG_B4_CGDL, XG_B4_CKAPPAS,
+  XG_B4_CKAPPAD, XG_B4_CF, XG_B4_CLC, XG_B4_CLE, XG_B4_DLC, XG_B4_DWC, XG_B4_DWJ, XG_B4_LINT,
+  XG_B4_WINT, XG_B4_XL, XG_B4_XW, XG_B4_NOFF, XG_B4_VOFFCV, XG_B4_ACDE, XG_B4_MOIN, XG_B4_ADOS,
+  XG_B4_BDOS, XG_B4_XPART, XG_B4_MINVCV, XG_B4_VOFFCVL, XG_B4_CJS, XG_B4_CJD, XG_B4_CJSWS,
+  XG_B4_CJSWD, XG_B4_CJSWGS, XG_B4_CJSWGD, XG_B4_MJS, XG_B4_MJD, XG_B4_MJSWS, XG_B4_MJSWD,
+  XG_B4_MJSWGS, XG_B4_MJSWGD, XG_B4_PBS, XG_B4_PBD, XG_B4_PBSWS, XG_B4_PBSWD, XG_B4_PBSWGS,
+  XG_B4_PBSWGD, XG_B4_JSS, XG_B4_JSD, XG_B4_JSWS, XG_B4_JSWD, XG_B4_JSWGS, XG_B4_JSWGD,
+  XG_B4_NJS, XG_B4_NJD, XG_B4_IJTHSFWD, XG_B4_IJTHDFWD, XG_B4_DMCG, XG_B4_DMCI, XG_B4_DMDG,
+  XG_B4_DMCGT, XG_B4_NPARAM
+};
+
 typedef struct xg_ctx xg_ctx;
 
 /* ---- context ------------------------------------------------------------ */
@@ -113,6 +145,10 @@ int xg_add_diodes(xg_ctx *ctx, int n, const int *pos, const int *neg, const int 
  * Series drain/source resistance (RD, RS, RSH) is XG_ERR_UNSUPPORTED. */
 int xg_add_mosfet1(xg_ctx *ctx, int n, const int *d, const int *g, const int *s,
                    const int *b, const double *params);
+/* MOSFET_B4::Instance (N_DEV_MOSFET_B4.C); params n x XG_B4_NPARAM row-major.
+ * A card outside the restated scope is XG_ERR_UNSUPPORTED. */
+int xg_add_bsim4(xg_ctx *ctx, int n, const int *d, const int *g, const int *s,
+                 const int *b, const double *params);
 /* Builds the CSR pattern, the stamp map, device-resident SoA instance
  * arrays and the symbolic structures (DeviceMgr::initializeAll + setupPointers,
  * N_CIR_Xyce.C:698-717, N_DEV_Diode.C:778-800). */

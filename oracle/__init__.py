@@ -65,6 +65,7 @@ def lib():
         L.orc_add_isources.argtypes = [P, C.c_int, ip, ip, ip, ip, dp]
         L.orc_add_diodes.argtypes = [P, C.c_int, ip, ip, ip, dp]
         L.orc_add_mosfet1.argtypes = [P, C.c_int, ip, ip, ip, ip, dp]
+        L.orc_add_bsim4.argtypes = [P, C.c_int, ip, ip, ip, ip, dp]
         L.orc_finalize.argtypes = [P]
         L.orc_sizes.argtypes = [P] + [C.POINTER(C.c_int)] * 4
         L.orc_pattern.argtypes = [P, ip, ip]
@@ -100,6 +101,11 @@ class Oracle:
         rc = L.orc_add_mosfet1(self.h, len(dd), dd, g, s, b, prm)
         if rc != 0:
             raise ValueError("oracle: MOSFET series resistance is not restated")
+        dd, g, s, b, prm = a["bsim4"]
+        if len(dd):
+            rc = L.orc_add_bsim4(self.h, len(dd), dd, g, s, b, np.ascontiguousarray(prm))
+            if rc != 0:
+                raise ValueError("oracle: BSIM4 card outside the restated scope")
         L.orc_finalize(self.h)
         n, nnz, nsta, nsto = C.c_int(), C.c_int(), C.c_int(), C.c_int()
         L.orc_sizes(self.h, C.byref(n), C.byref(nnz), C.byref(nsta), C.byref(nsto))

@@ -42,3 +42,15 @@ def test_create_fails_loudly_without_gpu(xg):
     assert xg.lib().xg_create(C.byref(h), 0) == -2  # XG_ERR_CUDA: no CPU fallback
     with pytest.raises(xg.XgError):
         xg.Circuit(__import__("xyce_gb300.netlist", fromlist=["x"]).test_netlist1())
+
+
+def test_bsim4_row_layout_matches_header_and_oracle():
+    """XG_B4_* (C header), the oracle's row and netlist.B4_FIELDS agree."""
+    from xyce_gb300 import netlist as N
+    hdr = open(HEADER).read()
+    body = hdr[hdr.index("XG_B4_TYPE"):hdr.index("XG_B4_NPARAM")]
+    names = re.findall(r"XG_B4_(\w+)", body)
+    assert names == N.B4_FIELDS
+    orc = open(os.path.join(os.path.dirname(HEADER), "..", "oracle", "bsim4.h")).read()
+    body = orc[orc.index("#define ORC_B4_PARAMS"):orc.index("#define ORC_B4_ENUM")]
+    assert re.findall(r"X\((\w+)\)", body) == N.B4_FIELDS

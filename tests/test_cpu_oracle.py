@@ -76,7 +76,9 @@ def _fd_check(oracle_mod, nl, rng, dcop):
 
 @pytest.mark.parametrize("maker", [lambda: N.diode_ladder(8, seed=3),
                                    lambda: N.ring_oscillator(5),
-                                   lambda: N.ring_oscillator(5, caps=True)])
+                                   lambda: N.ring_oscillator(5, caps=True),
+                                   lambda: N.bsim4_inverter_chain(2),
+                                   lambda: N.bsim4_logic_dag(60, 4, seed=2, tstop=0.3e-9)])
 def test_finite_difference_jacobian(oracle_mod, maker):
     rng = np.random.default_rng(7)
     _fd_check(oracle_mod, maker(), rng, dcop=False)
@@ -153,3 +155,40 @@ def test_diode_iv_point(oracle_mod):
     # the operating-point Newton stops at RHSTOL = 1e-6 A (N_NLS_Manager.C:1033)
     assert abs(i_r - i_d) < 1e-6
     assert 0.55 < vd < 0.75
+
+
+def test_bsim4_iv_known_behaviour(oracle_mod):
+    """BSIM4 (level 54) drain current of the 45 nm-like cards: off current
+    far below on current, monotone in Vgs, sign set by TYPE, zero at Vds = 0."""
+    for typ in (1.0, -1.0):
+        nl = N.Netlist(label="b4_iv")
+        d, g = nl.node("d"), nl.node("g")
+        nl.V(d, -1, N.WAVE_DC, [typ])
+        nl.V(g, -1, N.WAVE_DC, [typ])
+        nl.M4(d, g, -1, -1, **(N.B4_NMOS if typ > 0 else N.B4_PMOS))
+        nl.tran = N.Tran(tstop=1e-9)
+        o = oracle_mod.Oracle(nl)
+        z = np.zeros(o.nsto)
+        ids = []
+        for vg in np.linspace(0.0, 1.0, 11):
+            x = np.zeros(o.n)
+            x[d], x[g] = typ * 1.0, typ * vg
+            ids.append(typ * o.load(x, newton_iter=1, sto_curr=z, sto_prev=z)["F"][d])
+        ids = np.array(ids)
+        assert np.all(np.diff(ids) > 0), ids
+        assert ids[0] < 1e-9 and ids[-1] > 5e-5 and ids[-1] / ids[0] > 1e5, ids
+        x = np.zeros(o.n)
+        x[g] = typ * 1.0
+        assert abs(o.load(x, newton_iter=1, sto_curr=z, sto_prev=z)["F"][d]) < 1e-15
+
+
+def test_bsim4_chain_switches(oracle_mod):
+    """Three BSIM4 inverters follow their PULSE input with alternating polarity."""
+    nl = N.bsim4_inverter_chain(3)
+    pr = [nl.names[k] for k in ("in", "n1", "n2", "n3")]
+    t, v, st = oracle_mod.Oracle(nl).transient(probes=pr)
+    assert st["status"] == 0
+    k = np.searchsorted(t, 0.3e-9)  # input high since ~70 ps
+    assert v[k, 0] > 0.99 and v[k, 1] < 0.05 and v[k, 2] > 0.95 and v[k, 3] < 0.05
+    k = np.searchsorted(t, 0.65e-9)  # input low again since ~390 ps
+    assert v[k, 0] < 0.01 and v[k, 1] > 0.95 and v[k, 3] > 0.95

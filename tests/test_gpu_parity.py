@@ -100,6 +100,8 @@ def _loader_case(xg, oracle_mod, torch, nl, seed, newton_iter, dcop, init_jct, c
     (lambda: N.ring_oscillator(11, caps=True), True),
     (lambda: N.monte_carlo_rings(3, 11, 21, seed=2), False),
     (lambda: N.power_grid(6, 5, seed=1), False),
+    (lambda: N.bsim4_inverter_chain(3), True),
+    (lambda: N.bsim4_logic_dag(120, 6, seed=3, tstop=0.5e-9), True),
 ])
 @pytest.mark.parametrize("mode", ["tran0", "tran2", "dcop_init"])
 def test_device_stamps_match_oracle(xg, oracle_mod, torch_cuda, maker, caps, mode):
@@ -167,6 +169,8 @@ def _compare_waveforms(t_ref, v_ref, t_gpu, v_gpu):
     ("diode_ladder_50", lambda: N.diode_ladder(50, seed=5), ["n1", "n25", "n50"]),
     ("ring_101", lambda: N.ring_oscillator(101), ["n1", "n50", "n101"]),
     ("ring_21_caps", lambda: N.ring_oscillator(21, caps=True), ["n1", "n11"]),
+    ("b4_chain_3", lambda: N.bsim4_inverter_chain(3), ["in", "n1", "n3"]),
+    ("b4_dag_300", lambda: N.bsim4_logic_dag(300, 8, seed=4, tstop=1e-9), ["g10", "g40", "g70"]),
 ])
 def test_transient_matches_oracle(xg, oracle_mod, torch_cuda, name, maker, probes):
     nl = maker()

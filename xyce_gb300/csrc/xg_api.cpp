@@ -39,12 +39,15 @@ struct xg_ctx {
   std::vector<double> d_par;
   std::vector<int> m_d, m_g, m_s, m_b;
   std::vector<double> m_par;
+  std::vector<int> b_d, b_g, b_s, b_b;
+  std::vector<double> b_par;
   // finalized structure
   std::vector<int> rp, ci, circ_of_row;
   std::vector<long long> inst_of_circ;  // nonlinear device instances per circuit
-  int nnz = 0, nm = 0, nd = 0, nv = 0, ni = 0;
-  int nsto = 0, nsta = 0, sto_base_m = 0;
+  int nnz = 0, nm = 0, nd = 0, nv = 0, ni = 0, nb = 0;
+  int nsto = 0, nsta = 0, sto_base_m = 0, sto_base_b = 0, sta_base_b = 0;
   int sF_m = 0, sF_d = 0, sQ_m = 0, sQ_d = 0, sL_m = 0, sL_d = 0, sM_m = 0, sM_d = 0;
+  int sF_b = 0, sQ_b = 0, sL_b = 0, sM_b = 0;
   int n_pairs = 0, n_rowblocks = 0, n_long_rows = 0, n_long_ents = 0;
   DevArrays d;
   LUDev L;
@@ -277,6 +280,23 @@ int xg_add_mosfet1(xg_ctx *ctx, int n, const int *dd, const int *g, const int *s
   return XG_OK;
 }
 
+int xg_add_bsim4(xg_ctx *ctx, int n, const int *dd, const int *g, const int *s, const int *b,
+                 const double *params) {
+  SETUP_CHECK();
+  for (int k = 0; k < n; ++k) {
+    if (!valid_node(ctx, dd[k]) || !valid_node(ctx, g[k]) || !valid_node(ctx, s[k]) || !valid_node(ctx, b[k]))
+      return fail(ctx, XG_ERR_ARG, "BSIM4 node out of range");
+    const double *p = params + (size_t)k * XG_B4_NPARAM;
+    b4::B4Model probe;
+    std::string why;
+    int rc = b4::setup(p, probe, &why);
+    if (rc) return fail(ctx, rc, "BSIM4: " + why);
+    ctx->b_d.push_back(dd[k]); ctx->b_g.push_back(g[k]); ctx->b_s.push_back(s[k]); ctx->b_b.push_back(b[k]);
+    ctx->b_par.insert(ctx->b_par.end(), p, p + XG_B4_NPARAM);
+  }
+  return XG_OK;
+}
+
 // ---------------------------------------------------------------------------
 // finalize: pattern, stamp map, SoA tables, device buffers.
 int xg_finalize(xg_ctx *ctx) {
@@ -286,10 +306,11 @@ int xg_finalize(xg_ctx *ctx) {
   CK(cudaSetDevice(ctx->device));
   const int n = ctx->n;
   ctx->nm = (int)ctx->m_d.size();
+  ctx->nb = (int)ctx->b_d.size();
   ctx->nd = (int)ctx->d_p.size();
   ctx->nv = (int)ctx->v_p.size();
   ctx->ni = (int)ctx->i_p.size();
-  const int nm = ctx->nm, nd = ctx->nd, nv = ctx->nv, ni = ctx->ni;
+  const int nm = ctx->nm, nd = ctx->nd, nv = ctx->nv, ni = ctx->ni, nb = ctx->nb;
   // device circuits must not straddle circuits
   auto same_circuit = [&](std::initializer_list<int> nodes) {
     int c = -2;
@@ -305,6 +326,8 @@ int xg_finalize(xg_ctx *ctx) {
     if (!same_circuit({ctx->m_d[k], ctx->m_g[k], ctx->m_s[k], ctx->m_b[k]})) return fail(ctx, XG_ERR_ARG, "MOSFET spans two circuits");
   for (int k = 0; k < nd; ++k)
     if (!same_circuit({ctx->d_p[k], ctx->d_n[k], ctx->d_r[k]})) return fail(ctx, XG_ERR_ARG, "diode spans two circuits");
+  for (int k = 0; k < nb; ++k)
+    if (!same_circuit({ctx->b_d[k], ctx->b_g[k], ctx->b_s[k], ctx->b_b[k]})) return fail(ctx, XG_ERR_ARG, "BSIM4 spans two circuits");
   // matrix stamp positions (row, col) with their slot ids; -1 for ground rows/cols
   std::vector<std::vector<int>> rows(n);
   auto addp = [&](int r, int c) { if (r >= 0 && c >= 0) rows[r].push_back(c); };
@@ -327,6 +350,11 @@ int xg_finalize(xg_ctx *ctx) {
   }
   for (int k = 0; k < nm; ++k) {
     int nn[4] = {ctx->m_d[k], ctx->m_g[k], ctx->m_s[k], ctx->m_b[k]};
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b) addp(nn[a], nn[b]);
+  }
+  for (int k = 0; k < nb; ++k) {
+    int nn[4] = {ctx->b_d[k], ctx->b_g[k], ctx->b_s[k], ctx->b_b[k]};
     for (int a = 0; a < 4; ++a)
       for (int b = 0; b < 4; ++b) addp(nn[a], nn[b]);
   }
@@ -373,13 +401,15 @@ int xg_finalize(xg_ctx *ctx) {
     int p = ctx->v_p[k], m = ctx->v_n[k], b = ctx->v_b[k];
     addv(Glin, p, b, 1.0); addv(Glin, m, b, -1.0); addv(Glin, b, p, 1.0); addv(Glin, b, m, -1.0);
   }
-  // slot layout: MOSFETs first, then diodes, plane-major within a type
-  ctx->sF_m = 0; ctx->sF_d = kMosF * nm;
-  ctx->sQ_m = 0; ctx->sQ_d = kMosQ * nm;
-  ctx->sL_m = 0; ctx->sL_d = kMosL * nm;
-  ctx->sM_m = 0; ctx->sM_d = kMosM * nm;
-  const int nF = kMosF * nm + kDioF * nd, nQ = kMosQ * nm + kDioQ * nd, nL = kMosL * nm + kDioL * nd;
-  const int nMs = kMosM * nm + kDioM * nd, nB = nv + 2 * ni;
+  // slot layout: MOSFET level 1, then BSIM4 (same slot counts), then
+  // diodes, plane-major within a type
+  const int nmb = nm + nb;
+  ctx->sF_m = 0; ctx->sF_b = kMosF * nm; ctx->sF_d = kMosF * nmb;
+  ctx->sQ_m = 0; ctx->sQ_b = kMosQ * nm; ctx->sQ_d = kMosQ * nmb;
+  ctx->sL_m = 0; ctx->sL_b = kMosL * nm; ctx->sL_d = kMosL * nmb;
+  ctx->sM_m = 0; ctx->sM_b = kMosM * nm; ctx->sM_d = kMosM * nmb;
+  const int nF = kMosF * nmb + kDioF * nd, nQ = kMosQ * nmb + kDioQ * nd, nL = kMosL * nmb + kDioL * nd;
+  const int nMs = kMosM * nmb + kDioM * nd, nB = nv + 2 * ni;
   // contribution lists (row -> slots, CSR entry -> slots)
   std::vector<std::vector<int>> lF(n), lQ(n), lL(n), lB(n), lM(nnz);
   auto pushv = [&](std::vector<std::vector<int>> &l, int r, int slot) { if (r >= 0) l[r].push_back(slot); };
@@ -393,6 +423,18 @@ int xg_finalize(xg_ctx *ctx) {
       for (int b = 0; b < 4; ++b) {
         int e = find(nn[a], nn[b]);
         if (e >= 0) lM[e].push_back(ctx->sM_m + (4 * a + b) * nm + k);
+      }
+  }
+  for (int k = 0; k < nb; ++k) {
+    int D = ctx->b_d[k], G = ctx->b_g[k], S = ctx->b_s[k], B = ctx->b_b[k];
+    pushv(lF, D, ctx->sF_b + 0 * nb + k); pushv(lF, S, ctx->sF_b + 1 * nb + k); pushv(lF, B, ctx->sF_b + 2 * nb + k);
+    int qn[4] = {G, B, D, S};
+    for (int j = 0; j < 4; ++j) { pushv(lQ, qn[j], ctx->sQ_b + j * nb + k); pushv(lL, qn[j], ctx->sL_b + j * nb + k); }
+    int nn[4] = {D, G, S, B};
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b) {
+        int e = find(nn[a], nn[b]);
+        if (e >= 0) lM[e].push_back(ctx->sM_b + (4 * a + b) * nb + k);
       }
   }
   for (int k = 0; k < nd; ++k) {
@@ -492,8 +534,37 @@ int xg_finalize(xg_ctx *ctx) {
     int c = circuit_of_nodes(ctx, {ctx->d_p[k], ctx->d_n[k], ctx->d_r[k]});
     dcirc[k] = c < 0 ? 0 : c;
   }
+  // BSIM4 SoA with a table of evaluated cards (one per distinct row)
+  std::vector<int> b4node(4 * (size_t)nb), b4model(nb), b4circ(nb);
+  std::vector<b4::B4Model> b4models;
+  std::map<std::vector<double>, int> b4index;
+  for (int k = 0; k < nb; ++k) {
+    const double *row = &ctx->b_par[(size_t)k * XG_B4_NPARAM];
+    std::vector<double> key(row, row + XG_B4_NPARAM);
+    for (double &v : key)
+      if (std::isnan(v)) v = -1.2345e-300;  // NaN never compares equal: give "not given" one key
+    auto it = b4index.find(key);
+    int id;
+    if (it == b4index.end()) {
+      b4::B4Model m;
+      std::string why;
+      int rc = b4::setup(row, m, &why);
+      if (rc) return fail(ctx, rc, "BSIM4: " + why);
+      id = (int)b4models.size();
+      b4index.emplace(key, id);
+      b4models.push_back(m);
+    } else {
+      id = it->second;
+    }
+    b4model[k] = id;
+    b4node[k] = ctx->b_d[k]; b4node[nb + k] = ctx->b_g[k];
+    b4node[2 * (size_t)nb + k] = ctx->b_s[k]; b4node[3 * (size_t)nb + k] = ctx->b_b[k];
+    int c = circuit_of_nodes(ctx, {ctx->b_d[k], ctx->b_g[k], ctx->b_s[k], ctx->b_b[k]});
+    b4circ[k] = c < 0 ? 0 : c;
+  }
   ctx->inst_of_circ.assign(ctx->ncirc, 0);
   for (int k = 0; k < nm; ++k) ctx->inst_of_circ[m1circ[k]]++;
+  for (int k = 0; k < nb; ++k) ctx->inst_of_circ[b4circ[k]]++;
   for (int k = 0; k < nd; ++k) ctx->inst_of_circ[dcirc[k]]++;
   // row blocks x circuits partial slots
   const int nblocks = (n + kRowBlock - 1) / kRowBlock;
@@ -516,8 +587,10 @@ int xg_finalize(xg_ctx *ctx) {
   ctx->n_rowblocks = nblocks;
   // state layout (SoA): store = diode [vd qd cd] then MOSFET [vbd vbs vgs vds von gm]; state = MOSFET 8 planes
   ctx->sto_base_m = 3 * nd;
-  ctx->nsto = 3 * nd + 6 * nm;
-  ctx->nsta = 8 * nm;
+  ctx->sto_base_b = 3 * nd + 6 * nm;   // BSIM4 store [vbd vbs vgs vds von]
+  ctx->sta_base_b = 8 * nm;            // BSIM4 state [qg qd qb]
+  ctx->nsto = 3 * nd + 6 * nm + 5 * nb;
+  ctx->nsta = 8 * nm + 3 * nb;
   // upload
   DevArrays &d = ctx->d;
   auto &A = ctx->allocs;
@@ -541,6 +614,7 @@ int xg_finalize(xg_ctx *ctx) {
   UP(d.m1_node, m1node); UP(d.m1_model, m1model); UP(d.m1_circ, m1circ);
   UP(d.m1_beta, m1beta); UP(d.m1_vbi, m1vbi); UP(d.m1_models, models);
   UP(d.d_node, dnode); UP(d.d_model, dmodel); UP(d.d_circ, dcirc); UP(d.d_models, dmodels);
+  UP(d.b4_node, b4node); UP(d.b4_model, b4model); UP(d.b4_circ, b4circ); UP(d.b4_models, b4models);
   AL(d.sta_curr, ctx->nsta); AL(d.sta_next, ctx->nsta); AL(d.sto_curr, ctx->nsto); AL(d.sto_next, ctx->nsto);
   for (double **v : {&d.x, &d.xcurr, &d.xn0, &d.dx, &d.rhs, &d.Qv, &d.FmB, &d.Fv, &d.Bv, &d.qh0, &d.qh1,
                      &d.qh2, &d.xh1, &d.xh2, &d.Qc, &d.FmBc, &d.solwt})
@@ -599,6 +673,8 @@ int xg_update_state(xg_ctx *ctx, const double *next_sol, const double *curr_sta,
   d.sta_next = next_sta;
   d.sto_curr = const_cast<double *>(curr_sto);
   d.sto_next = next_sto;
+  launch_bsim4_k(ctx->stream, d, ctx->nb, ctx->sto_base_b, ctx->sta_base_b, 0, 0, newton_iter, flags, ctx->sF_b,
+                 ctx->sQ_b, ctx->sL_b, ctx->sM_b);
   launch_mos1_k(ctx->stream, d, ctx->nm, ctx->sto_base_m, 0, 0, newton_iter, flags, ctx->sF_m, ctx->sQ_m,
                 ctx->sL_m, ctx->sM_m);
   launch_diode_k(ctx->stream, d, ctx->nd, 0, 0, newton_iter, flags, ctx->sF_d, ctx->sQ_d, ctx->sL_d, ctx->sM_d);
@@ -806,6 +882,8 @@ void launch_front(TranRun &R) {
   DevArrays &d = c->d;
   launch_sources_k(c->stream, d, c->nv, c->nv + c->ni, 0, 0.0);
   launch_mos1_k(c->stream, d, c->nm, c->sto_base_m, 1, 1, 0, 0, c->sF_m, c->sQ_m, c->sL_m, c->sM_m);
+  launch_bsim4_k(c->stream, d, c->nb, c->sto_base_b, c->sta_base_b, 1, 1, 0, 0, c->sF_b, c->sQ_b, c->sL_b,
+                 c->sM_b);
   launch_diode_k(c->stream, d, c->nd, 1, 1, 0, 0, c->sF_d, c->sQ_d, c->sL_d, c->sM_d);
   launch_assemble_k(c->stream, d, c->n, c->nnz, c->n_long_rows, c->n_long_ents);
   launch_newton_ctl_k(c->stream, d, c->ncirc);
@@ -819,7 +897,7 @@ void launch_back(TranRun &R) {
   launch_update_k(c->stream, d, c->n);
   launch_step_ctl_k(c->stream, d, c->ncirc, R.bps, R.bp_ptr, R.cap);
   launch_history_k(c->stream, d, c->n, R.cap, R.pmax);
-  launch_state_commit_k(c->stream, d, c->nm, c->nd, c->sto_base_m);
+  launch_state_commit_k(c->stream, d, c->nm, c->nd, c->sto_base_m, c->nb, c->sto_base_b, c->sta_base_b);
 }
 
 int capture(TranRun &R) {

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../../include/xyce_gb300.h"
+#include "xg_bsim4.h"
 
 namespace xg {
 
@@ -115,6 +116,10 @@ struct DevArrays {
   int *m1_model = nullptr, *m1_circ = nullptr;
   double *m1_beta = nullptr, *m1_vbi = nullptr;
   Mos1Model *m1_models = nullptr;
+  // BSIM4 SoA
+  int *b4_node = nullptr;   // 4*n: D,G,S,B planes
+  int *b4_model = nullptr, *b4_circ = nullptr;
+  b4::B4Model *b4_models = nullptr;
   // diode SoA
   int *d_node = nullptr;    // 3*n: P,N,R planes
   int *d_model = nullptr, *d_circ = nullptr;
@@ -213,6 +218,8 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
 void launch_sources_k(cudaStream_t st, const DevArrays &d, int n_v, int n_src, int use_explicit, double t);
 void launch_mos1_k(cudaStream_t st, const DevArrays &d, int nm, int sto_base, int combined, int masked,
                    int it, int flags, int sF, int sQ, int sL, int sM);
+void launch_bsim4_k(cudaStream_t st, const DevArrays &d, int nb, int sto_base, int sta_base, int combined,
+                    int masked, int it, int flags, int sF, int sQ, int sL, int sM);
 void launch_diode_k(cudaStream_t st, const DevArrays &d, int nd, int combined, int masked, int it,
                     int flags, int sF, int sQ, int sL, int sM);
 void launch_assemble_k(cudaStream_t st, const DevArrays &d, int n, int nnz, int n_long_rows,
@@ -226,7 +233,8 @@ void launch_update_k(cudaStream_t st, const DevArrays &d, int n);
 void launch_step_ctl_k(cudaStream_t st, const DevArrays &d, int ncirc, const double *bps,
                        const int *bp_ptr, int cap);
 void launch_history_k(cudaStream_t st, const DevArrays &d, int n, int cap, int pmax);
-void launch_state_commit_k(cudaStream_t st, const DevArrays &d, int nm, int nd, int sto_base_m);
+void launch_state_commit_k(cudaStream_t st, const DevArrays &d, int nm, int nd, int sto_base_m, int nb,
+                           int sto_base_b, int sta_base_b);
 void launch_count_done_k(cudaStream_t st, const DevArrays &d, int ncirc, const int *breakdown,
                          int *status_out);
 void launch_unstall_k(cudaStream_t st, const DevArrays &d, int ncirc);

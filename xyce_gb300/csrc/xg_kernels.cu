@@ -996,8 +996,20 @@ __global__ void k_history(DevArrays d, int n, int cap, int pmax) {
 }
 
 // Accepted store/state become current (curr <- next) for accepted circuits.
-__global__ void k_state_commit(DevArrays d, int nm, int nd, int sto_base_m) {
+__global__ void k_state_commit(DevArrays d, int nm, int nd, int sto_base_m, int nb, int sto_base_b,
+                               int sta_base_b) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nm + nd && i < nm + nd + nb) {
+    const int j = i - nm - nd;
+    const CircState &s = d.cs[d.b4_circ[j]];
+    if (s.accept == 1 || s.accept == 2) {
+#pragma unroll
+      for (int k = 0; k < 5; ++k) d.sto_curr[sto_base_b + k * nb + j] = d.sto_next[sto_base_b + k * nb + j];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) d.sta_curr[sta_base_b + k * nb + j] = d.sta_next[sta_base_b + k * nb + j];
+    }
+    return;
+  }
   if (i < nm) {
     const CircState &s = d.cs[d.m1_circ[i]];
     if (s.accept == 1 || s.accept == 2) {
@@ -1096,8 +1108,10 @@ void launch_step_ctl_k(cudaStream_t st, const DevArrays &d, int ncirc, const dou
 void launch_history_k(cudaStream_t st, const DevArrays &d, int n, int cap, int pmax) {
   k_history<<<nblk(n, 256), 256, 0, st>>>(d, n, cap, pmax);
 }
-void launch_state_commit_k(cudaStream_t st, const DevArrays &d, int nm, int nd, int sto_base_m) {
-  if (nm + nd > 0) k_state_commit<<<nblk(nm + nd, 256), 256, 0, st>>>(d, nm, nd, sto_base_m);
+void launch_state_commit_k(cudaStream_t st, const DevArrays &d, int nm, int nd, int sto_base_m, int nb,
+                           int sto_base_b, int sta_base_b) {
+  if (nm + nd + nb > 0)
+    k_state_commit<<<nblk(nm + nd + nb, 256), 256, 0, st>>>(d, nm, nd, sto_base_m, nb, sto_base_b, sta_base_b);
 }
 void launch_count_done_k(cudaStream_t st, const DevArrays &d, int ncirc, const int *breakdown,
                          int *status_out) {

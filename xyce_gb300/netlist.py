@@ -41,6 +41,31 @@ MOS1_DEFAULTS = dict(TYPE=1.0, VTO=0.0, KP=2e-5, GAMMA=0.0, PHI=0.6, LAMBDA=0.0,
                      FC=0.5, W=1e-4, L=1e-4, AD=0.0, AS=0.0, PD=0.0, PS=0.0, M=1.0)
 
 
+# BSIM4 (level 54) parameter row: instance + model parameters in the order of
+# XG_B4_* (include/xyce_gb300.h).  NaN = not given: the model derives it as the
+# reference does (Model::processParams4p82_, N_DEV_MOSFET_B4p82.C:7769-8136).
+B4_FIELDS = (
+    "TYPE L W AS AD PS PD M TOXE TOXP TOXM DTOX EPSROX VTH0 VFB K1 K2 K3 K3B W0 "
+    "LPE0 LPEB DVT0 DVT1 DVT2 DVT0W DVT1W DVT2W DSUB DROUT NDEP NSUB NSD NGATE PHIN XJ XT "
+    "VBM VBX GAMMA1 GAMMA2 CDSC CDSCB CDSCD CIT NFACTOR ETA0 ETAB VOFF VOFFL MINV DVTP0 DVTP1 "
+    "U0 UA UB UC UD UP LP VSAT A0 AGS A1 A2 B0 B1 KETA DWG DWB RDSW RDSWMIN PRWG PRWB WR PCLM "
+    "PDIBLC1 PDIBLC2 PDIBLCB PVAG DELTA FPROUT PDITS PDITSD PDITSL PSCBE1 PSCBE2 ALPHA0 "
+    "ALPHA1 BETA0 AGIDL BGIDL CGIDL EGIDL AGISL BGISL CGISL EGISL CGSO CGDO CGBO CGSL CGDL "
+    "CKAPPAS CKAPPAD CF CLC CLE DLC DWC DWJ LINT WINT XL XW NOFF VOFFCV ACDE MOIN ADOS BDOS "
+    "XPART MINVCV VOFFCVL CJS CJD CJSWS CJSWD CJSWGS CJSWGD MJS MJD MJSWS MJSWD MJSWGS MJSWGD "
+    "PBS PBD PBSWS PBSWD PBSWGS PBSWGD JSS JSD JSWS JSWD JSWGS JSWGD NJS NJD IJTHSFWD IJTHDFWD "
+    "DMCG DMCI DMDG DMCGT").split()
+
+
+def b4_row(**kw) -> np.ndarray:
+    """BSIM4 row: every parameter not named is 'not given' (NaN)."""
+    row = np.full(len(B4_FIELDS), np.nan)
+    row[B4_FIELDS.index("M")] = 1.0
+    for k, v in kw.items():
+        row[B4_FIELDS.index(k)] = float(v)
+    return row
+
+
 def diode_row(**kw) -> np.ndarray:
     p = dict(DIODE_DEFAULTS)
     p.update(kw)
@@ -90,6 +115,7 @@ class Netlist:
     isrc: list = field(default_factory=list)     # (p, n, kind, data)
     diode: list = field(default_factory=list)    # (p, n, pri, row)
     mos1: list = field(default_factory=list)     # (d, g, s, b, row)
+    bsim4: list = field(default_factory=list)    # (d, g, s, b, row)
     names: dict = field(default_factory=dict)
     tran: Tran | None = None
     label: str = ""
@@ -131,6 +157,10 @@ class Netlist:
     def M1(self, d, g, s, b, **params):
         self.mos1.append((d, g, s, b, mos1_row(**params)))
 
+    def M4(self, d, g, s, b, **params):
+        """BSIM4 (level 54) instance; parameters not named are not given."""
+        self.bsim4.append((d, g, s, b, b4_row(**params)))
+
     # ---- flat arrays (C-ABI order) ------------------------------------
     def arrays(self) -> dict:
         self.end_circuit()
@@ -162,6 +192,9 @@ class Netlist:
         out["mos1"] = (i32([m[0] for m in self.mos1]), i32([m[1] for m in self.mos1]),
                        i32([m[2] for m in self.mos1]), i32([m[3] for m in self.mos1]),
                        f64(np.array([m[4] for m in self.mos1]).reshape(-1, len(MOS1_FIELDS))))
+        out["bsim4"] = (i32([m[0] for m in self.bsim4]), i32([m[1] for m in self.bsim4]),
+                        i32([m[2] for m in self.bsim4]), i32([m[3] for m in self.bsim4]),
+                        f64(np.array([m[4] for m in self.bsim4]).reshape(-1, len(B4_FIELDS))))
         return out
 
     @property
@@ -176,7 +209,7 @@ class Netlist:
 
     def device_count(self) -> int:
         return len(self.res) + len(self.cap) + len(self.vsrc) + len(self.isrc) + \
-            len(self.diode) + len(self.mos1)
+            len(self.diode) + len(self.mos1) + len(self.bsim4)
 
 
 # ---------------------------------------------------------------------------
@@ -356,5 +389,91 @@ def extract_circuit(nl: Netlist, ci: int) -> Netlist:
     out.isrc = [(rm(a), rm(b), k, d) for (a, b, k, d) in nl.isrc if inside(a, b)]
     out.diode = [(rm(a), rm(b), rm(r), row) for (a, b, r, row) in nl.diode if inside(a, b, r)]
     out.mos1 = [(rm(d), rm(g), rm(s), rm(b), row) for (d, g, s, b, row) in nl.mos1 if inside(d, g, s, b)]
+    out.bsim4 = [(rm(d), rm(g), rm(s), rm(b), row) for (d, g, s, b, row) in nl.bsim4 if inside(d, g, s, b)]
     out.tran = nl.tran
     return out
+
+
+# 45 nm-like BSIM4 cards: TOXE 1.8 nm, VTH0 +-0.4 V, L 45 nm; every other
+# parameter keeps the BSIM4 default.
+B4_NMOS = dict(TYPE=1.0, L=45e-9, W=90e-9, TOXE=1.8e-9, VTH0=0.4)
+B4_PMOS = dict(TYPE=-1.0, L=45e-9, W=180e-9, TOXE=1.8e-9, VTH0=-0.4)
+
+
+def _bit_stream_pwl(bits, period=1e-9, edge=20e-12, vdd=1.0):
+    """PWL points of a bit stream: one bit per period, edges of `edge` s."""
+    pts = [0.0, vdd * bits[0]]
+    for k in range(1, len(bits)):
+        if bits[k] != bits[k - 1]:
+            t0 = k * period
+            pts += [t0, vdd * bits[k - 1], t0 + edge, vdd * bits[k]]
+    return pts
+
+
+def bsim4_inverter_chain(stages=3, vdd=1.0, cload=2e-15) -> Netlist:
+    """Small BSIM4 inverter chain driven by a PULSE: the FD-Jacobian and
+    parity case of the level-54 path."""
+    nl = Netlist(label=f"b4_chain_{stages}")
+    vdd_n = nl.node("vdd")
+    nl.V(vdd_n, -1, WAVE_DC, [vdd], name="VDD#branch")
+    inp = nl.node("in")
+    nl.V(inp, -1, WAVE_PULSE, [0.0, vdd, 50e-12, 20e-12, 20e-12, 300e-12, 700e-12], name="VIN#branch")
+    prev = inp
+    for i in range(stages):
+        out = nl.node(f"n{i + 1}")
+        nl.M4(out, prev, -1, -1, **B4_NMOS)
+        nl.M4(out, prev, vdd_n, vdd_n, **B4_PMOS)
+        nl.C(out, -1, cload)
+        prev = out
+    nl.tran = Tran(tstop=1e-9, hmax=5e-12)
+    return nl
+
+
+def bsim4_logic_dag(n_transistors=50000, n_inputs=64, seed=5, vdd=1.0, wire_c=2e-15,
+                    tstop=5e-9) -> Netlist:
+    """Random CMOS logic DAG of INV / NAND2 / NOR2 gates with BSIM4 (level 54)
+    transistors: each gate draws its inputs from the primary inputs and the
+    outputs of earlier gates (seeded fan-in), every gate output carries a
+    wire load; the primary inputs are random PWL bit streams at 1 GHz with
+    20 ps edges; .TRAN 0 5n."""
+    rng = np.random.default_rng(seed)
+    nl = Netlist(label=f"b4_dag_{n_transistors}")
+    vdd_n = nl.node("vdd")
+    nl.V(vdd_n, -1, WAVE_DC, [vdd], name="VDD#branch")
+    nbits = int(np.ceil(tstop / 1e-9)) + 1
+    sources = []
+    for k in range(n_inputs):
+        pi = nl.node(f"pi{k}")
+        nl.V(pi, -1, WAVE_PWL, _bit_stream_pwl(rng.integers(0, 2, nbits), vdd=vdd))
+        sources.append(pi)
+    n_t = 0
+    g = 0
+    while n_t < n_transistors:
+        kind = rng.choice(3, p=[0.34, 0.33, 0.33])  # 0 INV, 1 NAND2, 2 NOR2
+        # fan-in from a window of recent signals keeps logic depth moderate
+        lo = max(0, len(sources) - 64)
+        a, b = (sources[int(i)] for i in rng.integers(lo, len(sources), 2))
+        out = nl.node(f"g{g}")
+        if kind == 0:
+            nl.M4(out, a, -1, -1, **B4_NMOS)
+            nl.M4(out, a, vdd_n, vdd_n, **B4_PMOS)
+            n_t += 2
+        elif kind == 1:  # NAND2: series NMOS, parallel PMOS
+            mid = nl.node()
+            nl.M4(out, a, mid, -1, **B4_NMOS)
+            nl.M4(mid, b, -1, -1, **B4_NMOS)
+            nl.M4(out, a, vdd_n, vdd_n, **B4_PMOS)
+            nl.M4(out, b, vdd_n, vdd_n, **B4_PMOS)
+            n_t += 4
+        else:  # NOR2: parallel NMOS, series PMOS
+            mid = nl.node()
+            nl.M4(out, a, -1, -1, **B4_NMOS)
+            nl.M4(out, b, -1, -1, **B4_NMOS)
+            nl.M4(mid, a, vdd_n, vdd_n, **B4_PMOS)
+            nl.M4(out, b, mid, vdd_n, **B4_PMOS)
+            n_t += 4
+        nl.C(out, -1, wire_c)
+        sources.append(out)
+        g += 1
+    nl.tran = Tran(tstop=tstop, hmax=5e-12)
+    return nl
