@@ -260,6 +260,47 @@ int xg_tran_advance(xg_ctx *ctx, int n_steps);
 int xg_tran_results(xg_ctx *ctx, int *counts, double *times, double *values, xg_tran_stats *stats);
 int xg_tran_end(xg_ctx *ctx);
 
+/* Predictor values of the recorded points (same layout as xg_tran_results'
+ * values): at each accepted transient point, the Newton initial guess that
+ * step started from — the training target of the learned predictor is the
+ * accepted solution minus this guess. */
+int xg_tran_predictors(xg_ctx *ctx, double *pred_values);
+/* Steps and Newton iterations taken with the learned and with the
+ * polynomial predictor in the current run (learned predictor mode). */
+int xg_tran_predictor_stats(xg_ctx *ctx, long long *learned_steps, long long *learned_iters,
+                            long long *poly_steps, long long *poly_iters);
+
+/* ---- learned predictor ------------------------------------------------------
+ * No counterpart in the reference: a per-node MLP (5 -> 64 -> 64 -> 1, tanh,
+ * BF16 weights on the tensor cores, FP32 accumulation) corrects the
+ * polynomial predictor of WorkingIntegrationMethod::obtainPredictor
+ * (src/TimeIntegrationPKG/N_TIA_WorkingIntegrationMethod.C:176) at the start
+ * of each step attempt.  Features of node unknown r: x_n - x_{n-1},
+ * x_{n-1} - x_{n-2}, x_{n-2} - x_{n-3}, x_n, log(h_{n+1} / h_n), standardized
+ * as (f - shift) * scale; output corr = out_shift + out_scale * MLP.
+ * Newton to the unchanged tolerances still decides every step; a circuit
+ * whose learned step needs more Newton iterations than its polynomial steps
+ * falls back to the polynomial predictor for 16 steps.
+ * theta: XG_MLP_NPARAM floats, W1[5][64] | b1[64] | W2[64][64] (in x out) |
+ * b2[64] | w3[64] | b3.  norm: in_shift[5], in_scale[5], out_shift, out_scale. */
+#define XG_MLP_NPARAM 4609
+#define XG_MLP_NNORM  12
+#define XG_PRED_POLY     0
+#define XG_PRED_LEARNED  1
+int xg_set_predictor(xg_ctx *ctx, int mode);
+int xg_mlp_set(xg_ctx *ctx, const float *theta, const float *norm);
+int xg_mlp_get(xg_ctx *ctx, float *theta, float *norm);
+/* Training on the GPU (own forward / backward kernels, Adam): X is n x 5
+ * standardized features and Y n standardized targets, DEVICE pointers;
+ * loss_hist (host, iters) receives 0.5 mean squared error per iteration. */
+int xg_mlp_train(xg_ctx *ctx, const float *X, const float *Y, int n, int iters, float lr,
+                 float *loss_hist);
+/* Loss and gradient of the current weights on (X, Y) (host outputs). */
+int xg_mlp_grad(xg_ctx *ctx, const float *X, const float *Y, int n, float *grad_host,
+                float *loss_host);
+/* out[r] = MLP(X[r]) in standardized units (DEVICE pointers). */
+int xg_mlp_forward(xg_ctx *ctx, const float *X, int n, float *out);
+
 /* Operating point only; x_host receives the n solution values. */
 int xg_dcop(xg_ctx *ctx, double *x_host, int *iters);
 

@@ -33,6 +33,8 @@ XG_ERR = {-1: "ARG", -2: "CUDA", -3: "STATE", -4: "UNSUPPORTED", -6: "NAN", -9: 
           -10: "TIMEOUT"}
 LOAD_ALL, LOAD_LINEAR, LOAD_NONLINEAR = 0, 1, 2
 PREC_FP64, PREC_FP32_IR = 0, 1
+PRED_POLY, PRED_LEARNED = 0, 1
+MLP_NPARAM, MLP_NNORM = 4609, 12
 FLAG_DCOP, FLAG_INITJCT = 1, 2
 
 # Every symbol declared in include/xyce_gb300.h.
@@ -44,6 +46,8 @@ EXPORTED = [
     "xg_load_dae_matrices", "xg_lu_analyze", "xg_lu_factor", "xg_lu_solve",
     "xg_lu_solve_noalloc", "xg_lu_set_precision", "xg_lu_info",
     "xg_transient", "xg_tran_start", "xg_tran_advance", "xg_tran_results", "xg_tran_end",
+    "xg_tran_predictors", "xg_tran_predictor_stats", "xg_set_predictor", "xg_mlp_set", "xg_mlp_get",
+    "xg_mlp_train", "xg_mlp_grad", "xg_mlp_forward",
     "xg_dcop", "xg_version",
 ]
 
@@ -125,6 +129,16 @@ def lib() -> C.CDLL:
     L.xg_tran_results.argtypes = [P, ip, dp, dp, C.POINTER(TranStats)]
     L.xg_tran_end.argtypes = [P]
     L.xg_dcop.argtypes = [P, dp, C.POINTER(I)]
+    fp = np.ctypeslib.ndpointer(np.float32, flags="C")
+    LL = C.POINTER(C.c_longlong)
+    L.xg_tran_predictors.argtypes = [P, dp]
+    L.xg_tran_predictor_stats.argtypes = [P, LL, LL, LL, LL]
+    L.xg_set_predictor.argtypes = [P, I]
+    L.xg_mlp_set.argtypes = [P, fp, fp]
+    L.xg_mlp_get.argtypes = [P, fp, fp]
+    L.xg_mlp_train.argtypes = [P, P, P, I, I, C.c_float, fp]
+    L.xg_mlp_grad.argtypes = [P, P, P, I, fp, fp]
+    L.xg_mlp_forward.argtypes = [P, P, I, P]
     L.xg_version.argtypes = []
     _lib = L
     return L
@@ -277,6 +291,52 @@ class Circuit:
 
     def tran_end(self):
         self._check(lib().xg_tran_end(self.h))
+
+    def tran_predictors(self):
+        """Newton initial guesses of the recorded points, [n_circuits, cap, pmax]."""
+        n_probe, cap, probes = self._run
+        nc = self.n_circuits
+        offs = np.asarray(self.netlist.offsets)
+        per = np.bincount(np.searchsorted(offs, probes, side="right") - 1, minlength=nc) \
+            if n_probe else np.zeros(nc, int)
+        pmax = max(1, int(per.max()) if len(per) else 1)
+        out = np.zeros(max(1, nc * cap * pmax))
+        self._check(lib().xg_tran_predictors(self.h, out))
+        return out[: nc * cap * pmax].reshape(nc, cap, pmax)
+
+    def predictor_stats(self):
+        v = [C.c_longlong() for _ in range(4)]
+        self._check(lib().xg_tran_predictor_stats(self.h, *[C.byref(x) for x in v]))
+        return dict(learned_steps=v[0].value, learned_iters=v[1].value, poly_steps=v[2].value,
+                    poly_iters=v[3].value)
+
+    # ---- learned predictor ------------------------------------------------
+    def set_predictor(self, mode: int):
+        self._check(lib().xg_set_predictor(self.h, int(mode)))
+
+    def mlp_set(self, theta, norm):
+        self._check(lib().xg_mlp_set(self.h, np.ascontiguousarray(theta, np.float32),
+                                     np.ascontiguousarray(norm, np.float32)))
+
+    def mlp_get(self):
+        theta, norm = np.zeros(MLP_NPARAM, np.float32), np.zeros(MLP_NNORM, np.float32)
+        self._check(lib().xg_mlp_get(self.h, theta, norm))
+        return theta, norm
+
+    def mlp_train(self, X, Y, iters: int, lr: float):
+        """X (n x 5), Y (n): float32 CUDA tensors; returns the loss history."""
+        hist = np.zeros(max(1, iters), np.float32)
+        self._check(lib().xg_mlp_train(self.h, _ptr(X), _ptr(Y), int(Y.shape[0]), int(iters),
+                                       float(lr), hist))
+        return hist[:iters]
+
+    def mlp_grad(self, X, Y):
+        g, l = np.zeros(MLP_NPARAM, np.float32), np.zeros(1, np.float32)
+        self._check(lib().xg_mlp_grad(self.h, _ptr(X), _ptr(Y), int(Y.shape[0]), g, l))
+        return float(l[0]), g
+
+    def mlp_forward(self, X, out):
+        self._check(lib().xg_mlp_forward(self.h, _ptr(X), int(X.shape[0]), _ptr(out)))
 
     def transient(self, tran=None, probes=(), cap=0):
         """Run the transient; returns (counts, times, values, stats) where

@@ -15,7 +15,7 @@ CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU = ["xg_kernels.cu", "xg_lu.cu", "xg_bsim4.cu"]
+CU = ["xg_kernels.cu", "xg_lu.cu", "xg_bsim4.cu", "xg_mlp.cu"]
 CPP = ["xg_api.cpp", "xg_symbolic.cpp", "xg_params.cpp", "xg_bsim4_params.cpp"]
 
 

@@ -54,6 +54,10 @@ struct xg_ctx {
   bool lu_ready = false;
   int n_analyze = 0;
   int lu_prec = XG_PREC_FP64, lu_refine = 2;  // xg_lu_set_precision
+  int predictor = XG_PRED_POLY;                // xg_set_predictor
+  bool mlp_ready = false;                      // weights set (xg_mlp_set) or trained
+  float *mlp_m1 = nullptr, *mlp_m2 = nullptr, *mlp_grad = nullptr, *mlp_loss = nullptr;
+  int mlp_adam_t = 0;
   std::vector<void *> allocs;      // device allocations owned by the context
   std::vector<void *> lu_allocs;   // allocations of the current LU analysis
   int *status_host = nullptr;      // mapped [finished, breakdown]
@@ -620,6 +624,11 @@ int xg_finalize(xg_ctx *ctx) {
                      &d.qh2, &d.xh1, &d.xh2, &d.Qc, &d.FmBc, &d.solwt})
     AL(*v, n);
   AL(d.J, nnz);
+  AL(d.mlh1, n); AL(d.mlh2, n); AL(d.mlh3, n);
+  AL(d.mlp.theta, kMlpParams); AL(d.mlp.norm, kMlpNorm);
+  AL(d.mlp.w1t, kMlpHid * kMlpInPad); AL(d.mlp.w2t, kMlpHid * kMlpHid); AL(d.mlp.w2, kMlpHid * kMlpHid);
+  AL(ctx->mlp_m1, kMlpParams); AL(ctx->mlp_m2, kMlpParams); AL(ctx->mlp_grad, kMlpParams);
+  AL(ctx->mlp_loss, 1);
   UP(d.pair_base, pair_base); UP(d.blk_cfirst, blk_cfirst); UP(d.pair_cstart, pair_cstart);
   AL(d.pmax, pairs); AL(d.psum, pairs);
   AL(d.probe_idx, n);
@@ -866,7 +875,7 @@ struct TranRun {
   ~TranRun() {
     if (exec) cudaGraphExecDestroy(exec);
     free_list(allocs);
-    if (ctx) { ctx->d.out_t = nullptr; ctx->d.out_v = nullptr; }
+    if (ctx) { ctx->d.out_t = nullptr; ctx->d.out_v = nullptr; ctx->d.out_p = nullptr; }
   }
 };
 
@@ -897,6 +906,7 @@ void launch_back(TranRun &R) {
   launch_update_k(c->stream, d, c->n);
   launch_step_ctl_k(c->stream, d, c->ncirc, R.bps, R.bp_ptr, R.cap);
   launch_history_k(c->stream, d, c->n, R.cap, R.pmax);
+  if (c->predictor == XG_PRED_LEARNED) launch_ml_predict_k(c->stream, d, c->n, c->ncirc, 1);
   launch_state_commit_k(c->stream, d, c->nm, c->nd, c->sto_base_m, c->nb, c->sto_base_b, c->sta_base_b);
 }
 
@@ -1001,6 +1011,9 @@ extern "C" int xg_tran_start(xg_ctx *ctx, const xg_tran_params *p, int n_probe, 
   int rc = 0;
   if ((rc = dev_alloc(ctx, &d.out_t, (size_t)ncirc * std::max(cap, 1), R.allocs))) return rc;
   if ((rc = dev_alloc(ctx, &d.out_v, (size_t)ncirc * std::max(cap, 1) * R.pmax, R.allocs))) return rc;
+  if ((rc = dev_alloc(ctx, &d.out_p, (size_t)ncirc * std::max(cap, 1) * R.pmax, R.allocs))) return rc;
+  if (ctx->predictor == XG_PRED_LEARNED && !ctx->mlp_ready)
+    return fail(ctx, XG_ERR_STATE, "learned predictor selected but no weights: call xg_mlp_set or xg_mlp_train");
   std::vector<std::vector<double>> cb(ncirc);
   for (int k = 0; k < ctx->nv; ++k) breakpoints(ctx->v_w[k], p->tstop, cb[ctx->circ_of_row[ctx->v_b[k]]]);
   for (int k = 0; k < ctx->ni; ++k) {
@@ -1042,7 +1055,8 @@ extern "C" int xg_tran_start(xg_ctx *ctx, const xg_tran_params *p, int n_probe, 
     s.stop_at = 0;  // pause once the operating point is done
   }
   CK(cudaMemcpyAsync(d.cs, cs.data(), sizeof(CircState) * ncirc, cudaMemcpyHostToDevice, ctx->stream));
-  for (double *v : {d.x, d.xcurr, d.xn0, d.dx, d.rhs, d.Qv, d.FmB, d.qh0, d.qh1, d.qh2, d.xh1, d.xh2, d.Qc, d.FmBc, d.solwt})
+  for (double *v : {d.x, d.xcurr, d.xn0, d.dx, d.rhs, d.Qv, d.FmB, d.qh0, d.qh1, d.qh2, d.xh1, d.xh2, d.Qc, d.FmBc, d.solwt,
+                    d.mlh1, d.mlh2, d.mlh3})
     CK(cudaMemsetAsync(v, 0, sizeof(double) * n, ctx->stream));
   for (double *v : {d.sta_curr, d.sta_next})
     CK(cudaMemsetAsync(v, 0, sizeof(double) * std::max(1, ctx->nsta), ctx->stream));
@@ -1121,6 +1135,33 @@ extern "C" int xg_tran_results(xg_ctx *ctx, int *counts, double *times, double *
   return XG_OK;
 }
 
+extern "C" int xg_tran_predictors(xg_ctx *ctx, double *pred_values) {
+  if (!ctx || !pred_values) return XG_ERR_ARG;
+  if (!ctx->run) return fail(ctx, XG_ERR_STATE, "call xg_tran_start first");
+  TranRun &R = *ctx->run;
+  if (R.cap <= 0) return fail(ctx, XG_ERR_STATE, "nothing recorded (cap = 0)");
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(pred_values, ctx->d.out_p, sizeof(double) * (size_t)ctx->ncirc * R.cap * R.pmax,
+                cudaMemcpyDeviceToHost));
+  return XG_OK;
+}
+
+extern "C" int xg_tran_predictor_stats(xg_ctx *ctx, long long *learned_steps, long long *learned_iters,
+                                       long long *poly_steps, long long *poly_iters) {
+  if (!ctx) return XG_ERR_ARG;
+  if (!ctx->run) return fail(ctx, XG_ERR_STATE, "call xg_tran_start first");
+  std::vector<CircState> out(ctx->ncirc);
+  CK(cudaMemcpyAsync(out.data(), ctx->d.cs, sizeof(CircState) * ctx->ncirc, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  long long a = 0, b = 0, c = 0, e = 0;
+  for (auto &s : out) { a += s.ml_steps; b += s.ml_iters; c += s.plain_steps; e += s.plain_iters; }
+  if (learned_steps) *learned_steps = a;
+  if (learned_iters) *learned_iters = b;
+  if (poly_steps) *poly_steps = c;
+  if (poly_iters) *poly_iters = e;
+  return XG_OK;
+}
+
 extern "C" int xg_tran_end(xg_ctx *ctx) {
   if (!ctx) return XG_ERR_ARG;
   if (ctx->run) {
@@ -1156,5 +1197,91 @@ extern "C" int xg_dcop(xg_ctx *ctx, double *x_host, int *iters) {
   if (iters) *iters = (int)st.dcop_iters;
   if (rc) return rc;
   CK(cudaMemcpy(x_host, ctx->d.xcurr, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost));
+  return XG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Learned predictor (xg_mlp.cu).
+extern "C" int xg_set_predictor(xg_ctx *ctx, int mode) {
+  if (!ctx) return XG_ERR_ARG;
+  if (mode != XG_PRED_POLY && mode != XG_PRED_LEARNED) return fail(ctx, XG_ERR_ARG, "unknown predictor mode");
+  if (ctx->run) return fail(ctx, XG_ERR_STATE, "predictor cannot change during a transient");
+  ctx->predictor = mode;
+  return XG_OK;
+}
+
+extern "C" int xg_mlp_set(xg_ctx *ctx, const float *theta, const float *norm) {
+  if (!ctx || !theta || !norm) return XG_ERR_ARG;
+  if (!ctx->finalized) return fail(ctx, XG_ERR_STATE, "not finalized");
+  CK(cudaMemcpyAsync(ctx->d.mlp.theta, theta, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d.mlp.norm, norm, sizeof(float) * kMlpNorm, cudaMemcpyHostToDevice, ctx->stream));
+  launch_mlp_refresh_k(ctx->stream, ctx->d.mlp);
+  CK(cudaGetLastError());
+  CK(cudaMemsetAsync(ctx->mlp_m1, 0, sizeof(float) * kMlpParams, ctx->stream));
+  CK(cudaMemsetAsync(ctx->mlp_m2, 0, sizeof(float) * kMlpParams, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->mlp_adam_t = 0;
+  ctx->mlp_ready = true;
+  return XG_OK;
+}
+
+extern "C" int xg_mlp_get(xg_ctx *ctx, float *theta, float *norm) {
+  if (!ctx) return XG_ERR_ARG;
+  if (!ctx->finalized) return fail(ctx, XG_ERR_STATE, "not finalized");
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (theta) CK(cudaMemcpy(theta, ctx->d.mlp.theta, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost));
+  if (norm) CK(cudaMemcpy(norm, ctx->d.mlp.norm, sizeof(float) * kMlpNorm, cudaMemcpyDeviceToHost));
+  return XG_OK;
+}
+
+static int sm_count(xg_ctx *ctx) {
+  int v = 0;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess || v <= 0) v = 132;
+  return v;
+}
+
+extern "C" int xg_mlp_grad(xg_ctx *ctx, const float *X, const float *Y, int n, float *grad_host, float *loss_host) {
+  if (!ctx || !X || !Y || n <= 0) return XG_ERR_ARG;
+  if (!ctx->mlp_ready) return fail(ctx, XG_ERR_STATE, "call xg_mlp_set first");
+  CK(cudaMemsetAsync(ctx->mlp_grad, 0, sizeof(float) * kMlpParams, ctx->stream));
+  CK(cudaMemsetAsync(ctx->mlp_loss, 0, sizeof(float), ctx->stream));
+  int rc = launch_mlp_grad_k(ctx->stream, ctx->d.mlp, X, Y, n, ctx->mlp_grad, ctx->mlp_loss, sm_count(ctx));
+  if (rc) return fail(ctx, rc, "MLP gradient kernel launch");
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (grad_host) CK(cudaMemcpy(grad_host, ctx->mlp_grad, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost));
+  if (loss_host) CK(cudaMemcpy(loss_host, ctx->mlp_loss, sizeof(float), cudaMemcpyDeviceToHost));
+  return XG_OK;
+}
+
+extern "C" int xg_mlp_train(xg_ctx *ctx, const float *X, const float *Y, int n, int iters, float lr,
+                            float *loss_hist) {
+  if (!ctx || !X || !Y || n <= 0 || iters < 0) return XG_ERR_ARG;
+  if (!ctx->mlp_ready) return fail(ctx, XG_ERR_STATE, "call xg_mlp_set first (initial weights)");
+  const int sms = sm_count(ctx);
+  std::vector<float> hist(iters > 0 ? iters : 1);
+  for (int it = 0; it < iters; ++it) {
+    CK(cudaMemsetAsync(ctx->mlp_grad, 0, sizeof(float) * kMlpParams, ctx->stream));
+    CK(cudaMemsetAsync(ctx->mlp_loss, 0, sizeof(float), ctx->stream));
+    int rc = launch_mlp_grad_k(ctx->stream, ctx->d.mlp, X, Y, n, ctx->mlp_grad, ctx->mlp_loss, sms);
+    if (rc) return fail(ctx, rc, "MLP gradient kernel launch");
+    ctx->mlp_adam_t++;
+    const float b1c = 1.0f - std::pow(0.9f, (float)ctx->mlp_adam_t);
+    const float b2c = 1.0f - std::pow(0.999f, (float)ctx->mlp_adam_t);
+    launch_mlp_adam_k(ctx->stream, ctx->d.mlp, ctx->mlp_grad, ctx->mlp_m1, ctx->mlp_m2, lr, b1c, b2c);
+    launch_mlp_refresh_k(ctx->stream, ctx->d.mlp);
+    CK(cudaMemcpyAsync(&hist[it], ctx->mlp_loss, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (loss_hist) std::copy(hist.begin(), hist.begin() + iters, loss_hist);
+  return XG_OK;
+}
+
+extern "C" int xg_mlp_forward(xg_ctx *ctx, const float *X, int n, float *out) {
+  if (!ctx || !X || !out || n <= 0) return XG_ERR_ARG;
+  if (!ctx->mlp_ready) return fail(ctx, XG_ERR_STATE, "call xg_mlp_set first");
+  launch_mlp_forward_k(ctx->stream, ctx->d.mlp, X, n, out);
+  CK(cudaGetLastError());
   return XG_OK;
 }

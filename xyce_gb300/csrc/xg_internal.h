@@ -48,6 +48,10 @@ struct CircState {
   int accept;          // 1 accepted / 0 rejected (valid when step_end)
   int start_step;      // 1 = next tick begins a new step attempt (predictor applied)
   int init_jct, init_hist, dc_stage, limited, bp_index, singular, stall_prev;
+  // learned predictor (xg_mlp.cu): gate state and per-predictor statistics
+  int ml_use, ml_pending, ml_backoff, last_iters, ml_steps, plain_steps;
+  double plain_ema;
+  long long ml_iters, plain_iters;
   // counters
   long long accepted, rejected, newton_iters, newton_fail, lte_fail, dcop_iters;
   long long stop_at;   // pause once this many steps are accepted
@@ -79,6 +83,19 @@ struct DiodeModel {
   double Isat, IsatR, Vte, VteR, VteBRK, Gspr, tVcrit, tIKF, tJctPot, tJctCap, tDepCap;
   double tF1, F2, F3, M, TT, tBrkdwnV;
   int bvGiven;
+};
+
+// Learned predictor MLP 5 -> 64 -> 64 -> 1 (xg_mlp.cu).  Master parameter
+// vector (FP32): W1[5][64] | b1[64] | W2[64][64] (in x out) | b2 | w3 | b3.
+constexpr int kMlpIn = 5, kMlpInPad = 16, kMlpHid = 64;
+constexpr int kMlpOffW1 = 0, kMlpOffB1 = kMlpIn * kMlpHid, kMlpOffW2 = kMlpOffB1 + kMlpHid;
+constexpr int kMlpOffB2 = kMlpOffW2 + kMlpHid * kMlpHid, kMlpOffW3 = kMlpOffB2 + kMlpHid;
+constexpr int kMlpOffB3 = kMlpOffW3 + kMlpHid, kMlpParams = kMlpOffB3 + 1;
+constexpr int kMlpNorm = 2 * kMlpIn + 2;  // in_shift[5], in_scale[5], out_shift, out_scale
+constexpr int kMlBackoff = 16;            // polynomial-predictor steps after a worse learned step
+struct MlpDev {
+  float *theta = nullptr, *norm = nullptr;
+  unsigned short *w1t = nullptr, *w2t = nullptr, *w2 = nullptr;  // BF16 operand copies
 };
 
 // Slot counts per instance.
@@ -132,6 +149,10 @@ struct DevArrays {
   double *qh0 = nullptr, *qh1 = nullptr, *qh2 = nullptr, *xh1 = nullptr, *xh2 = nullptr;
   double *Qc = nullptr, *FmBc = nullptr, *solwt = nullptr;
   double *J = nullptr;      // Jacobian values (CSR order)
+  // learned predictor: network and the differences of the last four accepted solutions
+  MlpDev mlp;
+  double *mlh1 = nullptr, *mlh2 = nullptr, *mlh3 = nullptr;
+  double *out_p = nullptr;  // recorded predictor values (training targets)
   // per-(block,circuit) partial reduction slots
   int *pair_base = nullptr, *blk_cfirst = nullptr, *pair_cstart = nullptr;
   double *pmax = nullptr, *psum = nullptr;
@@ -244,6 +265,13 @@ void launch_lu_factor_k(cudaStream_t st, const LUDev &L, const double *vals, Cir
 void launch_lu_solve_k(cudaStream_t st, const LUDev &L, const double *b, double *x, const CircState *cs,
                        int masked);
 int noalloc_scratch(int device, double **out, std::string &err);
+void launch_ml_predict_k(cudaStream_t st, const DevArrays &d, int n, int ncirc, int enabled);
+void launch_mlp_refresh_k(cudaStream_t st, const MlpDev &P);
+int launch_mlp_grad_k(cudaStream_t st, const MlpDev &P, const float *X, const float *Y, int N, float *grad,
+                      float *loss, int sm_count);
+void launch_mlp_adam_k(cudaStream_t st, const MlpDev &P, const float *grad, float *m1, float *m2, float lr,
+                       float b1c, float b2c);
+void launch_mlp_forward_k(cudaStream_t st, const MlpDev &P, const float *X, int N, float *out);
 void launch_lu_solve_noalloc_k(cudaStream_t st, LUDev L, double *scratch, const double *b, double *x,
                                const CircState *cs);
 

@@ -878,6 +878,7 @@ __global__ void k_step_ctl(DevArrays d, int ncirc, const double *bps, const int 
   } else {
     // transient step end
     s.newton_iters += s.iter;
+    s.last_iters = s.iter;
     bool ok = status > 0;
     if (!ok) s.newton_fail++;
     if (ok) {
@@ -969,6 +970,10 @@ __global__ void k_history(DevArrays d, int n, int cap, int pmax) {
     if (s.order == 2) { d.xh2[r] = d.xh1[r]; d.qh2[r] = d.FmB[r]; }
     d.xh1[r] = d.x[r] - d.xcurr[r];
     d.qh1[r] = d.Qv[r] - d.qh0[r];
+    // the learned predictor's history: differences of the last four solutions
+    d.mlh3[r] = d.mlh2[r];
+    d.mlh2[r] = d.mlh1[r];
+    d.mlh1[r] = d.x[r] - d.xcurr[r];
   }
   if (accepted_tran || accepted_dc) {
     const double xr = d.x[r];
@@ -977,7 +982,11 @@ __global__ void k_history(DevArrays d, int n, int cap, int pmax) {
     d.Qc[r] = d.Qv[r];
     d.FmBc[r] = d.FmB[r];
     const int pj = d.probe_idx[r];
-    if (pj >= 0 && s.n_out - 1 < cap) d.out_v[((size_t)c * cap + (s.n_out - 1)) * pmax + pj] = xr;
+    if (pj >= 0 && s.n_out - 1 < cap) {
+      const size_t o = ((size_t)c * cap + (s.n_out - 1)) * pmax + pj;
+      d.out_v[o] = xr;
+      d.out_p[o] = accepted_tran ? d.xn0[r] : xr;  // the predictor of the accepted step
+    }
   }
   if (s.start_step && (s.phase == PH_TRAN || s.phase == PH_PAUSED)) {
     const TranParams &p = *d.tp;
