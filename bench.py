@@ -1,27 +1,38 @@
 """Benchmark of the transient Newton hot path on GB300.
 
-Workload (default): the CMOS ring oscillator of 10,001 MOSFET level-1
-inverter stages (20,002 transistors, 10,003 unknowns), VDD 1.8 V, 5 fF loads,
-a 1 ns PWL kick, .TRAN 0 20n with 5 ps maximum step, FP64 throughout.
+Workloads (--workload):
+  mc    (default) batched Monte-Carlo form: 4,096 MOSFET level-1 ring
+        oscillators in one netlist, odd stage counts uniform in [11, 301]
+        (~1.28 M transistors, ~0.64 M unknowns), per-instance VTO ~ N(+-0.5, 0.03),
+        KP ~ N(nominal, 5 %), load C ~ U[3, 7] fF; .TRAN 0 10n; every ring keeps
+        its own step control; FP64 device evaluation, residual and LU.
+  ring  plain GPU path: one ring oscillator of 10,001 MOSFET level-1 inverter
+        stages (20,002 transistors), .TRAN 0 20n with 5 ps maximum step.
 
-A bench step is one window of WINDOW accepted transient time steps of that
-circuit, advanced through the device-resident Newton/OneStep loop
-(xg_tran_advance).  value = accepted transient steps per second over the
-timed windows (L2 flushed between windows with a 256 MiB write), summed over
-ranks for --gpus N (independent replicas: the circuit is one coupled system).
+A bench step is one window in which every circuit accepts WINDOW more
+transient steps, advanced by the device-resident Newton/OneStep loop
+(xg_tran_advance).  value = accepted transient steps per second summed over
+all circuits of the timed windows (inputs > L2: the device state of the mc
+workload is ~2 GB, and L2 is flushed with a 256 MiB write before every
+window), summed over ranks for --gpus N (independent replicas).
 
 e2e = the same metric through the full C-ABI call a user makes with host
-buffers: context creation, netlist upload, operating point, analysis, the
-transient windows and the copy of the probe waveforms back to the host.
+buffers (xg_transient): context creation, netlist upload, operating point,
+analysis, the transient windows and the copy of the probe waveforms back.
+
+The FP32-LU + FP64 iterative-refinement form is timed on the same workload
+in the same run (key "forms").
 
 --impl reference times the CPU FP64 restatement of the reference's
-algorithms (oracle/, single thread: the reference path is serial) on the same
-workload, metric and windows.
+algorithms (oracle/) on the same metric: for mc, a sample of the same rings
+run one per process on every host core; for ring, the whole circuit on one
+thread (the reference path is serial).
 """
 from __future__ import annotations
 
 import argparse
 import json
+import multiprocessing as mp
 import os
 import statistics
 import subprocess
@@ -31,10 +42,12 @@ import time
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
-METRIC = "transient steps/s (device evals/s alongside), plain GPU path, FP64"
+METRIC = "transient steps/s (device evals/s alongside), FP64"
 UNIT = "steps/s"
-WINDOW = 200          # accepted time steps per bench step
-CPU_SAMPLE_STEPS = 1500
+WORKLOADS = {
+    "mc": dict(window=50, cpu_steps=300, cpu_rings=64),
+    "ring": dict(window=200, cpu_steps=1500, cpu_rings=0),
+}
 
 
 def _peaks():
@@ -81,11 +94,19 @@ def _clock_summary(path, device_index):
     return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons)}
 
 
-def _workload(stages):
+def _workload(name):
     from xyce_gb300 import netlist as N
-    nl = N.ring_oscillator(stages)
-    probes = [nl.names["n1"], nl.names[f"n{stages // 2}"]]
-    return nl, probes
+    if name == "mc":
+        nl = N.monte_carlo_rings(4096)
+        probes = [nl.names[f"c{i}.n1"] for i in (0, 1, 2, 3)]
+        desc = dict(workload="monte_carlo_rings_4096", circuits=4096, mosfets=len(nl.mos1),
+                    stages="odd U[11,301]", tran="0 10n, hmax 5p")
+    else:
+        nl = N.ring_oscillator(10001)
+        probes = [nl.names["n1"], nl.names["n5000"]]
+        desc = dict(workload="ring_oscillator_10001_stages", circuits=1, mosfets=len(nl.mos1),
+                    tran="0 20n, hmax 5p")
+    return nl, probes, desc
 
 
 def _dist():
@@ -95,56 +116,113 @@ def _dist():
     return world, rank, local
 
 
+# ---- CPU: the oracle (CPU FP64 restatement of the reference algorithms) ----
+_BATCH = None
+
+
+def _cpu_init():
+    global _BATCH
+    sys.path.insert(0, HERE)
+    from xyce_gb300 import netlist as N
+    _BATCH = N.monte_carlo_rings(4096)
+
+
+def _cpu_ring_task(args):
+    """One Monte-Carlo ring, run alone by the oracle for its first n accepted steps."""
+    idx, n_steps = args
+    import oracle
+    from xyce_gb300 import netlist as N
+    nl = N.extract_circuit(_BATCH, idx)
+    nl.tran.max_steps = n_steps
+    t0 = time.perf_counter()
+    _, _, st = oracle.Oracle(nl).transient(nl.tran, probes=[0], cap=8)
+    return st["accepted"], time.perf_counter() - t0
+
+
+def cpu_mc(n_rings, n_steps, cores):
+    """Aggregate steps/s of the oracle on a sample of the batch's rings, one
+    ring per process on `cores` processes (spawned: no state shared with a
+    CUDA context)."""
+    import oracle
+    if not os.path.exists(oracle.LIB_PATH):
+        oracle.build(with_reference=False)
+    tasks = [(int(i), n_steps) for i in range(0, 4096, max(1, 4096 // n_rings))][:n_rings]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores, initializer=_cpu_init) as pool:
+        pool.map(abs, range(cores))  # workers up and the batch built before the clock starts
+        t0 = time.perf_counter()
+        res = pool.map(_cpu_ring_task, tasks, chunksize=1)
+        wall = time.perf_counter() - t0
+    steps = sum(r[0] for r in res)
+    return steps / wall, steps, wall
+
+
+def cpu_ring(n_steps):
+    import oracle
+    if not os.path.exists(oracle.LIB_PATH):
+        oracle.build(with_reference=False)
+    nl, probes, _ = _workload("ring")
+    nl.tran.max_steps = n_steps
+    t0 = time.perf_counter()
+    _, _, st = oracle.Oracle(nl).transient(nl.tran, probes=probes, cap=8)
+    dt = time.perf_counter() - t0
+    return st["accepted"] / dt, st["accepted"], dt
+
+
+def cpu_baseline(args):
+    w = WORKLOADS[args.workload]
+    if args.workload == "mc":
+        cores = os.cpu_count() or 1
+        v, steps, wall = cpu_mc(w["cpu_rings"], w["cpu_steps"], cores)
+        return {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                "sample": f"{w['cpu_rings']} rings of the same batch, first {w['cpu_steps']} accepted "
+                          f"steps of each from its operating point ({steps} steps, {wall:.1f} s wall), "
+                          f"CPU FP64 restatement (oracle/), one ring per process on {cores} processes"}
+    v, steps, dt = cpu_ring(w["cpu_steps"])
+    return {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"first {steps} accepted steps of the same circuit from its operating point "
+                      f"({dt:.1f} s), CPU FP64 restatement (oracle/), one thread"}
+
+
 def run_reference(args):
-    """CPU restatement of the reference path, single thread, same windows."""
+    """The reference algorithms on the CPU (the oracle port), same metric."""
     world, rank, _ = _dist()
     if rank != 0:
         return
-    import oracle
-    if not os.path.exists(oracle.LIB_PATH):
-        oracle.build(with_reference=False)
-    import numpy as np
-    nl, probes = _workload(args.stages)
-    o = oracle.Oracle(nl)
-    # one run of (warmup + steps) windows; the wall clock at every accepted
-    # step gives each window's time
-    tran = nl.tran
-    total = args.warmup + args.steps
-    tran.max_steps = total * WINDOW
-    wall = np.zeros(total * WINDOW)
-    _, _, st = o.transient(tran, probes=probes, cap=8, wall_log=wall)
-    done = st["accepted"]
-    first = args.warmup * WINDOW
-    secs = wall[done - 1] - wall[first - 1]
-    steps = done - first
-    value = steps / secs
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic",
-            "config": {"workload": f"ring_oscillator_{args.stages}_stages", "window_steps": WINDOW,
-                       "mosfets": 2 * args.stages},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
-                             "sample": f"{args.steps} windows of {WINDOW} accepted steps after "
-                                       f"{args.warmup} warm-up windows, CPU FP64 restatement of "
-                                       "the reference algorithms (oracle/), one thread"},
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    _, _, desc = _workload(args.workload)
+    cb = cpu_baseline(args)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": desc,
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline(stages, n_steps):
-    import oracle
-    if not os.path.exists(oracle.LIB_PATH):
-        oracle.build(with_reference=False)
-    nl, probes = _workload(stages)
-    o = oracle.Oracle(nl)
-    nl.tran.max_steps = n_steps
-    t0 = time.perf_counter()
-    _, _, st = o.transient(nl.tran, probes=probes, cap=8)
-    dt = time.perf_counter() - t0
-    return {"value": st["accepted"] / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"first {st['accepted']} accepted steps of the same circuit from its "
-                      f"operating point ({dt:.1f} s), CPU FP64 restatement (oracle/), one thread"}
+# ---- GPU ----------------------------------------------------------------
+def _timed_windows(xg, nl, probes, dev, args, window, prec, flush, stream_of):
+    import torch
+    circ = xg.Circuit(nl, device=dev)
+    circ.lu_set_precision(prec, 2)
+    circ.tran_start(probes=probes, cap=16)
+    stream = stream_of(circ)
+    for _ in range(args.warmup):
+        circ.tran_advance(window)
+    st0 = circ.tran_results()[3]
+    torch.cuda.synchronize()
+    ms = 0.0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        circ.tran_advance(window)
+        e1.record(stream)
+        e1.synchronize()
+        ms += e0.elapsed_time(e1)
+    torch.cuda.synchronize()
+    st1 = circ.tran_results()[3]
+    return circ, ms, st0, st1
 
 
 def run_ours(args):
@@ -161,42 +239,25 @@ def run_ours(args):
     if not os.path.exists(xg.LIB_PATH):
         xg.build()
     hbm_peak, peak_kind = _peaks()
-    nl, probes = _workload(args.stages)
-
-    # ---- device-resident windows -----------------------------------------
-    circ = xg.Circuit(nl, device=dev)
-    circ.tran_start(probes=probes, cap=16)
-    stream = torch.cuda.ExternalStream(xg.lib().xg_get_stream(circ.h))
+    w = WORKLOADS[args.workload]
+    window = w["window"]
+    nl, probes, desc = _workload(args.workload)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
-    for _ in range(args.warmup):
-        circ.tran_advance(WINDOW)
-    st0 = circ.tran_results()[3]
-    info = circ.lu_info()
+    stream_of = lambda c: torch.cuda.ExternalStream(xg.lib().xg_get_stream(c.h))
+
     clk_path = os.path.join(HERE, "gpurun_out", f"clocks_rank{rank}.csv") \
         if os.path.isdir(os.path.join(HERE, "gpurun_out")) else f"/tmp/xg_clocks_{os.getpid()}.csv"
     sampler = _clock_sampler(clk_path)
     if world > 1:
         torch.distributed.barrier()
-    torch.cuda.synchronize()
-    ms_total = 0.0
-    for _ in range(args.steps):
-        flush.fill_(1.0)
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        circ.tran_advance(WINDOW)
-        e1.record(stream)
-        e1.synchronize()
-        ms_total += e0.elapsed_time(e1)
-    torch.cuda.synchronize()
+    circ, ms_total, st0, st1 = _timed_windows(xg, nl, probes, dev, args, window, xg.PREC_FP64, flush, stream_of)
     if sampler:
         sampler.terminate()
         sampler.wait()
-    st1 = circ.tran_results()[3]
     steps_done = st1["accepted"] - st0["accepted"]
     ticks = st1["ticks"] - st0["ticks"]
     evals = st1["device_evals"] - st0["device_evals"]
+    info = circ.lu_info()
     local_vals = torch.tensor([ms_total, float(steps_done), float(evals)], dtype=torch.float64,
                               device=f"cuda:{dev}")
     if world > 1:
@@ -208,7 +269,10 @@ def run_ours(args):
     else:
         ms_max, steps_all, evals_all = ms_total, float(steps_done), float(evals)
     value = steps_all / (ms_max / 1e3)
-    kernels_per_tick = 11 + info["factor_levels"] + info["lsolve_levels"] + info["usolve_levels"]
+    # kernels per tick: sources, MOSFET, assembly (+2 long-gather pre-passes when
+    # present), Newton control, factor (hub/groups/top), L/U solves, update,
+    # step control, history, state commit, completion count
+    kernels_per_tick = 12 + 3 + 6
     gpu_launches = int(ticks * kernels_per_tick)
     circ.tran_end()
 
@@ -216,54 +280,74 @@ def run_ours(args):
     roof = None
     if rank == 0:
         n = circ.n
+        stream = stream_of(circ)
         z = lambda k: torch.zeros(max(1, k), dtype=torch.float64, device=f"cuda:{dev}")
         x = torch.full((n,), 0.9, dtype=torch.float64, device=f"cuda:{dev}")
         stac, stan, stoc, ston = z(circ.nsta), z(circ.nsta), z(circ.nsto), z(circ.nsto)
         for _ in range(5):
             circ.update_state(x, stac, stoc, stan, ston, newton_iter=1)
-        reps = 200
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        e0.record(stream)
+        reps = 50
+        us_all = 0.0
         for _ in range(reps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
             circ.update_state(x, stac, stoc, stan, ston, newton_iter=1)
-        e1.record(stream)
-        e1.synchronize()
-        us = e0.elapsed_time(e1) * 1e3 / reps
-        nm = 2 * args.stages
+            e1.record(stream)
+            e1.synchronize()
+            us_all += e0.elapsed_time(e1) * 1e3
+        us = us_all / reps
+        nm = len(nl.mos1)
         # per instance: reads 4 node indices, model index, circuit index (24 B),
         # beta + vbi (16 B), 4 node voltages (32 B), 5 history stores (40 B);
         # writes 6 stores + 8 states (112 B) and 47 stamp slots (376 B): 600 B
         bytes_per_inst = 24 + 16 + 32 + 40 + 112 + 376
         achieved = bytes_per_inst * nm / (us * 1e-6) / 1e9
         traffic = None
-        prof = os.path.join(HERE, "profiles", "k_mos1_ring10001.traffic.json")
+        prof = os.path.join(HERE, "profiles", f"k_mos1_{args.workload}.traffic.json")
         if os.path.exists(prof):
             try:
                 traffic = json.load(open(prof)).get("dram_bytes_per_launch")
             except Exception:
                 traffic = None
-        roof = {"kernel": "k_mos1 (MOSFET-1 evaluation + stamp, separate dF/dQ slots)",
+        roof = {"kernel": "k_mos1 (MOSFET-1 evaluation + stamp, separate dF/dQ slots, one launch over "
+                          f"{nm} instances, L2 flushed before each launch)",
                 "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
                 "algorithmic_bytes_per_launch": bytes_per_inst * nm, "launch_us": us}
     circ.close()
 
+    # ---- the FP32-LU + FP64-refinement form, same workload ------------------
+    forms = None
+    if rank == 0 and args.forms:
+        c2, ms2, s0, s1 = _timed_windows(xg, nl, probes, dev, args, window, xg.PREC_FP32_IR, flush, stream_of)
+        forms = {"fp64": value,
+                 "fp32_lu_fp64_ir": (s1["accepted"] - s0["accepted"]) / (ms2 / 1e3),
+                 "fp32_lu_fp64_ir_newton_iters_per_step":
+                     (s1["newton_iters"] - s0["newton_iters"]) / max(1, s1["accepted"] - s0["accepted"])}
+        c2.tran_end()
+        c2.close()
+
     # ---- end to end through the C-ABI with host buffers --------------------
     e2e = None
     if rank == 0:
         tr = nl.tran
-        tr.max_steps = (args.warmup + args.steps) * WINDOW
+        per_circuit = (args.warmup + args.steps) * window
+        tr.max_steps = per_circuit
         a = nl.arrays()
         h2d = sum(v.nbytes for k, v in a.items() if hasattr(v, "nbytes"))
-        h2d += sum(x.nbytes for k in ("res", "cap", "vsrc", "isrc", "diode", "mos1") for x in a[k])
+        h2d += sum(x.nbytes for k in ("res", "cap", "vsrc", "isrc", "diode", "mos1", "bsim4") for x in a[k])
+        cap = per_circuit + 8
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        c2 = xg.Circuit(nl, device=dev)
-        counts, tt, vv, st = c2.transient(tr, probes=probes, cap=tr.max_steps + 8)
+        c3 = xg.Circuit(nl, device=dev)
+        counts, tt, vv, st = c3.transient(tr, probes=probes, cap=cap)
         dt = time.perf_counter() - t0
-        c2.close()
-        d2h = int(counts[0]) * (8 + 8 * len(probes))
+        c3.close()
+        cap = per_circuit + 8
+        # xg_tran_results copies the time and probe buffers of every circuit
+        d2h = nl.n_circuits * cap * 8 * 2 + nl.n_circuits * 4
         nsteps = args.warmup + args.steps
         e2e = {"value": st["accepted"] / dt, "unit": UNIT,
                "h2d_bytes_per_step": h2d / nsteps, "d2h_bytes_per_step": d2h / nsteps,
@@ -271,20 +355,21 @@ def run_ours(args):
         tr.max_steps = 0
 
     if rank == 0:
-        cpu = cpu_baseline(args.stages, args.cpu_steps) if args.cpu_steps > 0 else None
+        cpu = cpu_baseline(args) if args.cpu else None
         clocks = _clock_summary(clk_path, dev)
+        config = dict(desc)
+        config.update({"unknowns": n, "window_steps_per_circuit": window,
+                       "l2": "flushed between windows (256 MiB write); device state > L2",
+                       "parallelism": f"replicas x{world}"})
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": f"ring_oscillator_{args.stages}_stages",
-                           "mosfets": 2 * args.stages, "unknowns": n,
-                           "window_steps": WINDOW, "tran": "0 20n, hmax 5p",
-                           "l2": "flushed between windows (256 MiB write)",
-                           "parallelism": f"replicas x{world}"},
+                "config": config,
                 "device_evals_per_s": evals_all / (ms_max / 1e3),
                 "newton_iters_per_step": (st1["newton_iters"] - st0["newton_iters"]) / max(1, steps_done),
                 "ticks": ticks, "gpu_launches": gpu_launches,
-                "lu": info, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
+                "lu": info, "roofline": roof, "forms": forms, "cpu_baseline": cpu, "e2e": e2e,
+                "clocks": clocks}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -296,8 +381,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--stages", type=int, default=10001)
-    ap.add_argument("--cpu-steps", type=int, default=CPU_SAMPLE_STEPS)
+    ap.add_argument("--workload", default="mc", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", dest="cpu", action="store_false", help="skip the CPU baseline")
+    ap.add_argument("--no-forms", dest="forms", action="store_false", help="skip the FP32-IR form")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

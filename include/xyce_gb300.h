@@ -275,9 +275,12 @@ int xg_tran_predictor_stats(xg_ctx *ctx, long long *learned_steps, long long *le
  * BF16 weights on the tensor cores, FP32 accumulation) corrects the
  * polynomial predictor of WorkingIntegrationMethod::obtainPredictor
  * (src/TimeIntegrationPKG/N_TIA_WorkingIntegrationMethod.C:176) at the start
- * of each step attempt.  Features of node unknown r: x_n - x_{n-1},
- * x_{n-1} - x_{n-2}, x_{n-2} - x_{n-3}, x_n, log(h_{n+1} / h_n), standardized
- * as (f - shift) * scale; output corr = out_shift + out_scale * MLP.
+ * of each step attempt.  With d1 = x_n - x_{n-1}, d2 = x_{n-1} - x_{n-2},
+ * d3 = x_{n-2} - x_{n-3} and s = |d1| + |d2| + |d3| + 1e-9 V, the features of
+ * node unknown r are d1/s, d2/s, d3/s, x_n, log(h_{n+1} / h_n), standardized
+ * as (f - shift) * scale, and Newton starts from the polynomial guess plus
+ * s * (out_shift + out_scale * MLP).  The polynomial guess stays the
+ * predictor of the error estimate and step control.
  * Newton to the unchanged tolerances still decides every step; a circuit
  * whose learned step needs more Newton iterations than its polynomial steps
  * falls back to the polynomial predictor for 16 steps.

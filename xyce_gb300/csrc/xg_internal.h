@@ -93,6 +93,7 @@ constexpr int kMlpOffB2 = kMlpOffW2 + kMlpHid * kMlpHid, kMlpOffW3 = kMlpOffB2 +
 constexpr int kMlpOffB3 = kMlpOffW3 + kMlpHid, kMlpParams = kMlpOffB3 + 1;
 constexpr int kMlpNorm = 2 * kMlpIn + 2;  // in_shift[5], in_scale[5], out_shift, out_scale
 constexpr int kMlBackoff = 16;            // polynomial-predictor steps after a worse learned step
+constexpr double kMlpScaleFloor = 1e-9;   // V: motion scale floor of the learned correction
 struct MlpDev {
   float *theta = nullptr, *norm = nullptr;
   unsigned short *w1t = nullptr, *w2t = nullptr, *w2 = nullptr;  // BF16 operand copies

@@ -140,10 +140,15 @@ __device__ __forceinline__ void mlp_forward_warp(const MlpSmem &S, const float (
 
 // ---- inference inside the transient tick ------------------------------------
 // After k_history has written the polynomial predictor xn0 of every step
-// attempt, rows of circuits whose learned predictor is on get
-// xn0 += out_shift + out_scale * MLP(features); features of row r:
-//   (x_n - x_{n-1}, x_{n-1} - x_{n-2}, x_{n-2} - x_{n-3}, x_n, log(h_{n+1} / h_n)),
-// standardized by in_shift / in_scale.  Branch currents keep the polynomial guess.
+// attempt, rows of circuits whose learned predictor is on start Newton from
+//   x = xn0 + s * (out_shift + out_scale * MLP(features)),
+// where s = |d1| + |d2| + |d3| + kMlpScaleFloor (d1 = x_n - x_{n-1},
+// d2 = x_{n-1} - x_{n-2}, d3 = x_{n-2} - x_{n-3}) is the node's recent motion
+// and the features are (d1 / s, d2 / s, d3 / s, x_n, log(h_{n+1} / h_n)),
+// standardized by in_shift / in_scale: a node at rest keeps its polynomial
+// guess.  xn0 itself stays the polynomial predictor, so the predictor-
+// corrector error estimate (OneStep, N_TIA_OneStep.C:1584-1640) and the step
+// control are those of the reference.  Branch currents keep the polynomial guess.
 __global__ void __launch_bounds__(128) k_ml_predict(DevArrays d, int n) {
   __shared__ MlpSmem S;
   mlp_load_smem(d.mlp, S);
@@ -153,6 +158,7 @@ __global__ void __launch_bounds__(128) k_ml_predict(DevArrays d, int n) {
   const int rows[2] = {warp_row0 + g, warp_row0 + g + 8};
   bool use[2];
   float f[2][kMlpIn];
+  double scale[2] = {0.0, 0.0};
   for (int q = 0; q < 2; ++q) {
     const int r = rows[q];
     use[q] = false;
@@ -161,7 +167,10 @@ __global__ void __launch_bounds__(128) k_ml_predict(DevArrays d, int n) {
       const CircState &s = d.cs[d.circ_of_row[r]];
       if (s.start_step && s.phase == PH_TRAN && s.ml_use && s.lastTimeStep > 0.0) {
         use[q] = true;
-        const double raw[kMlpIn] = {d.mlh1[r], d.mlh2[r], d.mlh3[r], d.xcurr[r], log(s.h / s.lastTimeStep)};
+        const double d1 = d.mlh1[r], d2 = d.mlh2[r], d3 = d.mlh3[r];
+        const double sc = fabs(d1) + fabs(d2) + fabs(d3) + kMlpScaleFloor;
+        scale[q] = sc;
+        const double raw[kMlpIn] = {d1 / sc, d2 / sc, d3 / sc, d.xcurr[r], log(s.h / s.lastTimeStep)};
         for (int k = 0; k < kMlpIn; ++k) f[q][k] = (float)((raw[k] - S.in_shift[k]) * S.in_scale[k]);
       }
     }
@@ -170,15 +179,11 @@ __global__ void __launch_bounds__(128) k_ml_predict(DevArrays d, int n) {
   float h1[8][4], h2[8][4], y[2];
   mlp_forward_warp(S, f[0], f[1], h1, h2, y);
   if (t != 0) return;
-  const TranParams &p = *d.tp;
   for (int q = 0; q < 2; ++q) {
     if (!use[q]) continue;
     const int r = rows[q];
-    const double corr = (double)S.out_shift + (double)S.out_scale * (double)y[q];
-    const double xn = d.xn0[r] + corr;
-    d.xn0[r] = xn;
-    d.x[r] = xn;
-    d.solwt[r] = p.nl_reltol * fmax(fabs(xn), fabs(d.xcurr[r])) + p.nl_abstol;
+    const double corr = scale[q] * ((double)S.out_shift + (double)S.out_scale * (double)y[q]);
+    d.x[r] = d.xn0[r] + corr;
   }
 }
 

@@ -6,9 +6,13 @@ plain (polynomial-predictor) runs recorded on the GPU and trains the network
 there with the library's own forward/backward kernels.
 
 Training set (one row per node unknown and accepted step n+1 with four
-accepted solutions before it, as the device applies the network):
-  features  x_n - x_{n-1}, x_{n-1} - x_{n-2}, x_{n-2} - x_{n-3}, x_n, log(h_{n+1} / h_n)
-  target    x_{n+1} - (polynomial predictor of step n+1)
+accepted solutions before it, as the device applies the network), with the
+node's recent motion s = |d1| + |d2| + |d3| + 1e-9 V (d1 = x_n - x_{n-1},
+d2 = x_{n-1} - x_{n-2}, d3 = x_{n-2} - x_{n-3}):
+  features  d1 / s, d2 / s, d3 / s, x_n, log(h_{n+1} / h_n)
+  target    (x_{n+1} - polynomial predictor of step n+1) / s
+The device starts Newton from the polynomial predictor plus s times the
+network's output, so a node at rest keeps the polynomial guess.
 The recorded sequence of a circuit starts with its operating point (index 0)
 followed by the accepted transient points, so step index m >= 5 qualifies.
 """
@@ -19,6 +23,7 @@ import numpy as np
 from . import MLP_NNORM, MLP_NPARAM, PRED_LEARNED, PRED_POLY, Circuit
 
 N_IN, N_HID = 5, 64
+SCALE_FLOOR = 1e-9  # V, as kMlpScaleFloor in the library
 
 
 def node_unknowns(nl) -> np.ndarray:
@@ -57,14 +62,14 @@ def dataset(counts, t, v, p, pcount):
             h1, h0 = tt[m] - tt[m - 1], tt[m - 1] - tt[m - 2]
             if h1 <= 0 or h0 <= 0:
                 continue
+            d1, d2, d3 = vv[m - 1] - vv[m - 2], vv[m - 2] - vv[m - 3], vv[m - 3] - vv[m - 4]
+            sc = np.abs(d1) + np.abs(d2) + np.abs(d3) + SCALE_FLOOR
             f = np.empty((q, N_IN))
-            f[:, 0] = vv[m - 1] - vv[m - 2]
-            f[:, 1] = vv[m - 2] - vv[m - 3]
-            f[:, 2] = vv[m - 3] - vv[m - 4]
+            f[:, 0], f[:, 1], f[:, 2] = d1 / sc, d2 / sc, d3 / sc
             f[:, 3] = vv[m - 1]
             f[:, 4] = np.log(h1 / h0)
             xs.append(f)
-            ys.append(vv[m] - pp[m])
+            ys.append((vv[m] - pp[m]) / sc)
     return np.concatenate(xs), np.concatenate(ys)
 
 
