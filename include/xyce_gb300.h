@@ -279,7 +279,8 @@ int xg_tran_predictor_stats(xg_ctx *ctx, long long *learned_steps, long long *le
  * d3 = x_{n-2} - x_{n-3} and s = |d1| + |d2| + |d3| + 1e-9 V, the features of
  * node unknown r are d1/s, d2/s, d3/s, x_n, log(h_{n+1} / h_n), standardized
  * as (f - shift) * scale, and Newton starts from the polynomial guess plus
- * s * (out_shift + out_scale * MLP).  The polynomial guess stays the
+ * s * (out_shift + out_scale * MLP); nodes with s < 1e-5 V keep the
+ * polynomial guess.  The polynomial guess stays the
  * predictor of the error estimate and step control.
  * Newton to the unchanged tolerances still decides every step; a circuit
  * whose learned step needs more Newton iterations than its polynomial steps

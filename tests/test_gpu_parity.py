@@ -156,6 +156,33 @@ def test_lu_refactor_same_pattern_new_values(xg, oracle_mod, torch_cuda):
     c.close()
 
 
+@pytest.mark.parametrize("maker", [lambda: N.power_grid(40, 50, seed=2),
+                                   lambda: N.bsim4_logic_dag(3000, 16, seed=9, tstop=1e-9)])
+def test_lu_large_top_matches_scipy(xg, oracle_mod, torch_cuda, maker):
+    """Systems whose nested-dissection top is large (a 40 x 40 grid, a BSIM4
+    logic DAG): the top is factored by the pull + right-looking kernels."""
+    nl = maker()
+    c = xg.Circuit(nl)
+    o = oracle_mod.Oracle(nl)
+    rng = np.random.default_rng(5)
+    x = rng.uniform(0.0, 1.0, o.n)
+    ld = o.load(x, newton_iter=1, sto_curr=np.zeros(max(1, o.nsto)), sto_prev=np.zeros(max(1, o.nsto)))
+    vals = ld["dFdx"] + ld["dQdx"] / 1e-12
+    A = sp.csr_matrix((vals, o.col_idx, o.row_ptr), shape=(o.n, o.n))
+    for k in range(2):
+        b = rng.standard_normal(o.n)
+        v, bb = _t(torch_cuda, vals), _t(torch_cuda, b)
+        if k == 0:
+            c.lu_analyze(v)
+        c.lu_factor(v)
+        xs = torch_cuda.zeros_like(bb)
+        c.lu_solve(bb, xs)
+        torch_cuda.cuda.synchronize()
+        xr = spl.spsolve(A.tocsc(), b)
+        np.testing.assert_allclose(xs.cpu().numpy(), xr, rtol=1e-9, atol=1e-12 * np.max(np.abs(xr)))
+    c.close()
+
+
 def _compare_waveforms(t_ref, v_ref, t_gpu, v_gpu):
     g = np.stack([np.interp(t_ref, t_gpu, v_gpu[:, j]) for j in range(v_gpu.shape[1])], axis=1)
     err = np.max(np.abs(g - v_ref))

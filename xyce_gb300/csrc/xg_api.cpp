@@ -49,6 +49,7 @@ struct xg_ctx {
   int sF_m = 0, sF_d = 0, sQ_m = 0, sQ_d = 0, sL_m = 0, sL_d = 0, sM_m = 0, sM_d = 0;
   int sF_b = 0, sQ_b = 0, sL_b = 0, sM_b = 0;
   int n_pairs = 0, n_rowblocks = 0, n_long_rows = 0, n_long_ents = 0;
+  int n_long_row_blocks = 0, n_long_ent_blocks = 0;
   DevArrays d;
   LUDev L;
   bool lu_ready = false;
@@ -476,6 +477,24 @@ int xg_finalize(xg_ctx *ctx) {
     if (pM[e + 1] - pM[e] > kLongGather) { ent_long[e] = (int)long_ents.size(); long_ents.push_back(e); }
   ctx->n_long_rows = (int)long_rows.size();
   ctx->n_long_ents = (int)long_ents.size();
+  // blocks of the long gathers: ceil(items / kLongPart) each
+  std::vector<int> lrow_ptr(1, 0), lrow_blk, lent_ptr(1, 0), lent_blk;
+  for (int l = 0; l < (int)long_rows.size(); ++l) {
+    const int i = long_rows[l];
+    const int work = (ctx->rp[i + 1] - ctx->rp[i]) + (pF[i + 1] - pF[i]) + (pQ[i + 1] - pQ[i]) +
+                     (pB[i + 1] - pB[i]) + (pL[i + 1] - pL[i]);
+    const int parts = std::max(1, (work + kLongPart - 1) / kLongPart);
+    for (int b = 0; b < parts; ++b) lrow_blk.push_back(l);
+    lrow_ptr.push_back(lrow_ptr.back() + parts);
+  }
+  for (int l = 0; l < (int)long_ents.size(); ++l) {
+    const int e = long_ents[l];
+    const int parts = std::max(1, (pM[e + 1] - pM[e] + kLongPart - 1) / kLongPart);
+    for (int b = 0; b < parts; ++b) lent_blk.push_back(l);
+    lent_ptr.push_back(lent_ptr.back() + parts);
+  }
+  ctx->n_long_row_blocks = lrow_ptr.back();
+  ctx->n_long_ent_blocks = lent_ptr.back();
   // sources (V first, then I)
   std::vector<int> skind, soff(1, 0), scirc;
   std::vector<double> sdata;
@@ -612,7 +631,8 @@ int xg_finalize(xg_ctx *ctx) {
   UP(d.m_ptr, pM); UP(d.m_idx, iM);
   UP(d.is_branch, is_branch);
   UP(d.long_rows, long_rows); UP(d.row_long, row_long); UP(d.long_ents, long_ents); UP(d.ent_long, ent_long);
-  AL(d.long_rsum, 4 * (size_t)kLongSplit * long_rows.size()); AL(d.long_esum, (size_t)kLongSplit * long_ents.size());
+  UP(d.lrow_ptr, lrow_ptr); UP(d.lrow_blk, lrow_blk); UP(d.lent_ptr, lent_ptr); UP(d.lent_blk, lent_blk);
+  AL(d.long_rsum, 4 * (size_t)ctx->n_long_row_blocks); AL(d.long_esum, (size_t)ctx->n_long_ent_blocks);
   AL(d.sF, nF); AL(d.sQ, nQ); AL(d.sL, nL); AL(d.sL2, nL); AL(d.sB, nB); AL(d.sM, nMs); AL(d.sM2, nMs);
   UP(d.src_kind, skind); UP(d.src_off, soff); UP(d.src_circ, scirc); UP(d.src_data, sdata);
   UP(d.m1_node, m1node); UP(d.m1_model, m1model); UP(d.m1_circ, m1circ);
@@ -754,6 +774,7 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
     L.a_vals = ctx->d.J;  // the transient's Jacobian; xg_lu_factor points it at its values
   }
   L.breakdown = ctx->breakdown_dev;
+  L.top_start = H.top_start;
   L.f_levels = (int)H.f_lvl_ptr.size() - 1;
   L.l_levels = (int)H.l_lvl_ptr.size() - 1;
   L.u_levels = (int)H.u_lvl_ptr.size() - 1;
@@ -894,7 +915,7 @@ void launch_front(TranRun &R) {
   launch_bsim4_k(c->stream, d, c->nb, c->sto_base_b, c->sta_base_b, 1, 1, 0, 0, c->sF_b, c->sQ_b, c->sL_b,
                  c->sM_b);
   launch_diode_k(c->stream, d, c->nd, 1, 1, 0, 0, c->sF_d, c->sQ_d, c->sL_d, c->sM_d);
-  launch_assemble_k(c->stream, d, c->n, c->nnz, c->n_long_rows, c->n_long_ents);
+  launch_assemble_k(c->stream, d, c->n, c->nnz, c->n_long_row_blocks, c->n_long_ent_blocks);
   launch_newton_ctl_k(c->stream, d, c->ncirc);
 }
 

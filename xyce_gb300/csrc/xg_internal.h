@@ -15,7 +15,7 @@ namespace xg {
 constexpr int kRowBlock = 256;       // rows per block of the row kernels (fixed: partial slots)
 constexpr int kMaxPwlScan = 1 << 20; // bound on PWL point scans
 constexpr int kLongGather = 96;      // gathers longer than this are split across blocks
-constexpr int kLongSplit = 32;       // blocks per long gather
+constexpr int kLongPart = 2048;      // gathered items per block of a long gather
 constexpr int kLongSolveRow = 256;   // triangular-solve rows longer than this get a whole block
 // Frozen-pivot acceptance on the device: a pivot below this fraction of its
 // updated column triggers re-pivoting by the host.
@@ -94,6 +94,7 @@ constexpr int kMlpOffB3 = kMlpOffW3 + kMlpHid, kMlpParams = kMlpOffB3 + 1;
 constexpr int kMlpNorm = 2 * kMlpIn + 2;  // in_shift[5], in_scale[5], out_shift, out_scale
 constexpr int kMlBackoff = 16;            // polynomial-predictor steps after a worse learned step
 constexpr double kMlpScaleFloor = 1e-9;   // V: motion scale floor of the learned correction
+constexpr double kMlpActive = 1e-5;       // V: nodes moving less keep the polynomial guess
 struct MlpDev {
   float *theta = nullptr, *norm = nullptr;
   unsigned short *w1t = nullptr, *w2t = nullptr, *w2 = nullptr;  // BF16 operand copies
@@ -121,7 +122,11 @@ struct DevArrays {
   int *m_ptr = nullptr, *m_idx = nullptr;
   char *is_branch = nullptr;                 // per row: voltage-source branch unknown
   // long gathers, reduced by a block in a pre-pass: rows (F, Q, B, L sums) and J entries
+  // (a long gather of w items is split over ceil(w / kLongPart) blocks; block b
+  // handles part b - ptr[l] of gather l = *_blk[b]; the parts of gather l are
+  // blocks ptr[l] .. ptr[l+1])
   int *long_rows = nullptr, *row_long = nullptr, *long_ents = nullptr, *ent_long = nullptr;
+  int *lrow_ptr = nullptr, *lrow_blk = nullptr, *lent_ptr = nullptr, *lent_blk = nullptr;
   double *long_rsum = nullptr, *long_esum = nullptr;
   // slot value buffers
   double *sF = nullptr, *sQ = nullptr, *sL = nullptr, *sL2 = nullptr, *sB = nullptr;
@@ -190,6 +195,7 @@ constexpr int kNoAllocMaxDevices = 64;
 constexpr int kLongColumn = 512;   // factor columns longer than this use the whole CTA
 constexpr int kHubFanout = 64;     // items with more dependents than this run in the prologue
 constexpr int kGroupCap = 512;     // items per dependency-closed group
+constexpr int kTopRightLooking = 64;  // tops at least this large factor right-looking
 
 // LU structures (device) produced by the host analysis.  Plain data: it is
 // passed to kernels by value.
@@ -210,6 +216,10 @@ struct LUDev {
   // factors; each solve is refined n_refine times against the FP64 matrix
   // a_vals (CSR a_rp/a_ci in unknown order, the values last factored).
   int mixed = 0, n_refine = 0;
+  // factor schedule's top as a contiguous suffix of steps [top_start, n):
+  // factored by a multi-CTA pull of the sub-tree updates, then one
+  // right-looking CTA (top_start < 0: the top runs left-looking like a group)
+  int top_start = -1;
   float *lu32 = nullptr;
   double *ir_r = nullptr;
   const int *a_rp = nullptr, *a_ci = nullptr, *a_circ = nullptr;
@@ -219,6 +229,7 @@ struct LUDev {
 // Host-side analysis result.
 struct LUHost {
   int n = 0;
+  int top_start = -1;  // first step of the factor schedule's top when the top is a suffix, else -1
   std::vector<int> row_of_step, col_of_step, cp, ri, diag, src;
   std::vector<int> f_lvl_ptr, f_cols, l_lvl_ptr, l_rows, l_ptr, l_pos, l_col;
   std::vector<int> u_lvl_ptr, u_rows, u_ptr, u_pos, u_col;
@@ -244,8 +255,8 @@ void launch_bsim4_k(cudaStream_t st, const DevArrays &d, int nb, int sto_base, i
                     int masked, int it, int flags, int sF, int sQ, int sL, int sM);
 void launch_diode_k(cudaStream_t st, const DevArrays &d, int nd, int combined, int masked, int it,
                     int flags, int sF, int sQ, int sL, int sM);
-void launch_assemble_k(cudaStream_t st, const DevArrays &d, int n, int nnz, int n_long_rows,
-                       int n_long_ents);
+void launch_assemble_k(cudaStream_t st, const DevArrays &d, int n, int nnz, int n_long_row_blocks,
+                       int n_long_ent_blocks);
 void launch_load_vectors_k(cudaStream_t st, const DevArrays &d, int n, const double *x, double *Q,
                            double *F, double *B, double *dFv, double *dQv, int lt);
 void launch_load_matrices_k(cudaStream_t st, const DevArrays &d, int nnz, double *dQdx, double *dFdx,

@@ -478,14 +478,15 @@ __device__ __forceinline__ double block_sum(double v) {
   return t;  // valid in thread 0
 }
 
-// Long rows (e.g. a supply node touching every PMOS): kLongSplit blocks per
-// row gather F, Q, B, L partial sums, grid-strided over the row's lists.
+// Long rows (e.g. a supply node touching every PMOS): ceil(items / kLongPart)
+// blocks per row gather F, Q, B, L partial sums, strided over the row's lists.
 __global__ void __launch_bounds__(256) k_long_rows(DevArrays d) {
-  const int lr = blockIdx.x / kLongSplit, part = blockIdx.x % kLongSplit;
+  const int lr = d.lrow_blk[blockIdx.x], part = blockIdx.x - d.lrow_ptr[lr];
+  const int nparts = d.lrow_ptr[lr + 1] - d.lrow_ptr[lr];
   const int r = d.long_rows[lr];
   const CircState &s = d.cs[d.circ_of_row[r]];
   if (!circ_active(s)) return;
-  const int start = part * blockDim.x + threadIdx.x, stride = kLongSplit * blockDim.x;
+  const int start = part * blockDim.x + threadIdx.x, stride = nparts * blockDim.x;
   double F = 0.0, Q = 0.0, B = 0.0, L = 0.0;
   for (int e = d.rp[r] + start; e < d.rp[r + 1]; e += stride) {
     const double xv = d.x[d.ci[e]];
@@ -501,22 +502,23 @@ __global__ void __launch_bounds__(256) k_long_rows(DevArrays d) {
   B = block_sum(B);
   L = block_sum(L);
   if (threadIdx.x == 0) {
-    double *o = d.long_rsum + 4 * ((size_t)lr * kLongSplit + part);
+    double *o = d.long_rsum + 4 * (size_t)blockIdx.x;
     o[0] = F; o[1] = Q; o[2] = B; o[3] = L;
   }
 }
 
-// Long Jacobian entries (e.g. a supply node's diagonal): kLongSplit blocks each.
+// Long Jacobian entries (e.g. a supply node's diagonal): ceil(items / kLongPart) blocks each.
 __global__ void __launch_bounds__(256) k_long_entries(DevArrays d) {
-  const int le = blockIdx.x / kLongSplit, part = blockIdx.x % kLongSplit;
+  const int le = d.lent_blk[blockIdx.x], part = blockIdx.x - d.lent_ptr[le];
+  const int nparts = d.lent_ptr[le + 1] - d.lent_ptr[le];
   const int e = d.long_ents[le];
   const CircState &s = d.cs[d.circ_of_row[d.erow[e]]];
   if (!circ_active(s)) return;
-  const int start = part * blockDim.x + threadIdx.x, stride = kLongSplit * blockDim.x;
+  const int start = part * blockDim.x + threadIdx.x, stride = nparts * blockDim.x;
   double v = 0.0;
   for (int k = d.m_ptr[e] + start; k < d.m_ptr[e + 1]; k += stride) v += d.sM[d.m_idx[k]];
   v = block_sum(v);
-  if (threadIdx.x == 0) d.long_esum[(size_t)le * kLongSplit + part] = v;
+  if (threadIdx.x == 0) d.long_esum[blockIdx.x] = v;
 }
 
 // Residual per row: RHS = -(qscale (Q - Q_hist0) + fscale (F - B) + hscale Q_hist2 + gshunt x)
@@ -532,8 +534,8 @@ __global__ void __launch_bounds__(kRowBlock) k_assemble_rows(DevArrays d, int n)
       const int lr = d.row_long[r];
       if (lr >= 0) {
         F = 0.0; Q = 0.0; B = 0.0; L = 0.0;
-        const double *o = d.long_rsum + 4 * (size_t)lr * kLongSplit;
-        for (int k = 0; k < kLongSplit; ++k) {
+        const double *o = d.long_rsum + 4 * (size_t)d.lrow_ptr[lr];
+        for (int k = 0; k < d.lrow_ptr[lr + 1] - d.lrow_ptr[lr]; ++k) {
           F += o[4 * k]; Q += o[4 * k + 1]; B += o[4 * k + 2]; L += o[4 * k + 3];
         }
       } else {
@@ -575,8 +577,8 @@ __global__ void k_assemble_J(DevArrays d, int nnz) {
   double v = s.qscale * d.Clin[e] + s.fscale * d.Glin[e];
   const int le = d.ent_long[e];
   if (le >= 0) {
-    const double *o = d.long_esum + (size_t)le * kLongSplit;
-    for (int k = 0; k < kLongSplit; ++k) v += o[k];
+    const double *o = d.long_esum + (size_t)d.lent_ptr[le];
+    for (int k = 0; k < d.lent_ptr[le + 1] - d.lent_ptr[le]; ++k) v += o[k];
   } else {
     for (int k = d.m_ptr[e]; k < d.m_ptr[e + 1]; ++k) v += d.sM[d.m_idx[k]];
   }
@@ -1089,10 +1091,10 @@ void launch_diode_k(cudaStream_t st, const DevArrays &d, int nd, int combined, i
   if (nd > 0)
     k_diode<<<nblk(nd, 128), 128, 0, st>>>(d, nd, combined, masked, it, flags, sF, sQ, sL, sM);
 }
-void launch_assemble_k(cudaStream_t st, const DevArrays &d, int n, int nnz, int n_long_rows,
-                       int n_long_ents) {
-  if (n_long_rows > 0) k_long_rows<<<n_long_rows * kLongSplit, 256, 0, st>>>(d);
-  if (n_long_ents > 0) k_long_entries<<<n_long_ents * kLongSplit, 256, 0, st>>>(d);
+void launch_assemble_k(cudaStream_t st, const DevArrays &d, int n, int nnz, int n_long_row_blocks,
+                       int n_long_ent_blocks) {
+  if (n_long_row_blocks > 0) k_long_rows<<<n_long_row_blocks, 256, 0, st>>>(d);
+  if (n_long_ent_blocks > 0) k_long_entries<<<n_long_ent_blocks, 256, 0, st>>>(d);
   k_assemble_rows<<<nblk(n, kRowBlock), kRowBlock, 0, st>>>(d, n);
   k_assemble_J<<<nblk(nnz, 256), 256, 0, st>>>(d, nnz);
 }

@@ -192,6 +192,101 @@ __global__ void __launch_bounds__(1024) k_factor_groups(LUDev L, const double *_
   }
 }
 
+// ---- top of the factorization: pull, then right-looking -------------------
+// When the factor schedule's top is the step suffix [top_start, n) (the upper
+// separators of the nested dissection), its columns first pull, in parallel
+// (one warp each), the updates of every column before the top — all factored
+// by then — and then one CTA factors the top right-looking: pivot test and
+// scaling of column k, then the rank-1 update of every column j with
+// U(k, j) != 0 (a warp per U entry, lanes over L(:, k)).  One barrier pair per
+// top column replaces the per-(column, row) barriers of the left-looking walk.
+template <typename T>
+__global__ void __launch_bounds__(256) k_top_pull(LUDev L, const double *__restrict__ vals, CircState *cs,
+                                                   int masked) {
+  const int lane = threadIdx.x & 31;
+  const int j = L.top_start + (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  if (j >= L.n) return;  // warp-uniform
+  if (!item_active(L, cs, masked, j)) return;
+  T *lu = lu_of<T>(L);
+  const int p0 = L.cp[j], p1 = L.cp[j + 1], pd = L.diag[j];
+  for (int p = p0 + lane; p < p1; p += 32) {
+    const int s = L.src[p];
+    lu[p] = (s >= 0) ? (T)vals[s] : (T)0;
+  }
+  __syncwarp();
+  bool lost = false;
+  for (int p = p0; p < pd; ++p) {
+    const int k = L.ri[p];
+    if (k >= L.top_start) break;  // the top's own updates come right-looking
+    const T ukj = lu[p];
+    if (ukj != (T)0) {
+      const int q0 = L.diag[k] + 1, q1 = L.cp[k + 1];
+      const int *tgt = L.upd_pos + L.upd_off[p];
+      for (int q = q0 + lane; q < q1; q += 32) {
+        const int pos = tgt[q - q0];
+        if (pos > p && pos < p1) lu[pos] -= lu[q] * ukj;
+        else lost = true;
+      }
+    }
+    __syncwarp();
+  }
+  if (__any_sync(0xffffffffu, lost) && lane == 0) {
+    atomicCAS(L.breakdown, 0, j + 1);
+    if (masked) cs[L.circ_of_step[j]].singular = 1;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_top_rl(LUDev L, CircState *cs, int masked, double pivot_tol) {
+  __shared__ double sm[32];
+  T *lu = lu_of<T>(L);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (int k = L.top_start; k < L.n; ++k) {
+    if (!item_active(L, cs, masked, k)) continue;  // uniform: every thread reads the same flags
+    const int pd = L.diag[k], p1 = L.cp[k + 1];
+    double amax = 0.0;
+    for (int p = pd + threadIdx.x; p < p1; p += blockDim.x) amax = fmax(amax, fabs((double)lu[p]));
+    amax = team_max<true>(amax, sm);
+    const double d = (double)lu[pd];
+    const bool urow = L.u_ptr[k + 1] > L.u_ptr[k] && !L.exempt[k];
+    const bool bad = (urow && !(fabs(d) >= pivot_tol * amax)) || !(fabs(d) > 0.0) || isinf(d);
+    if (bad) {
+      if (threadIdx.x == 0) {
+        atomicCAS(L.breakdown, 0, k + 1);
+        if (masked) cs[L.circ_of_step[k]].singular = 1;
+      }
+      if (!masked) return;  // uniform
+      __syncthreads();      // the circuit's later columns see it singular and are skipped
+      continue;
+    }
+    const T inv = (T)1 / lu[pd];
+    for (int p = pd + 1 + threadIdx.x; p < p1; p += blockDim.x) lu[p] *= inv;
+    __syncthreads();
+    const int q0 = pd + 1, nl = p1 - q0;
+    if (nl > 0) {
+      for (int e = L.u_ptr[k] + warp; e < L.u_ptr[k + 1]; e += nwarps) {
+        const int p = L.u_pos[e];  // U(k, j) in column j
+        const int j = L.u_col[e];
+        const T ukj = lu[p];
+        if (ukj == (T)0) continue;
+        const int *tgt = L.upd_pos + L.upd_off[p];
+        const int cend = L.cp[j + 1];
+        bool lost = false;
+        for (int q = lane; q < nl; q += 32) {
+          const int pos = tgt[q];
+          if (pos > p && pos < cend) lu[pos] -= lu[q0 + q] * ukj;
+          else lost = true;
+        }
+        if (__any_sync(0xffffffffu, lost) && lane == 0) {
+          atomicCAS(L.breakdown, 0, j + 1);
+          if (masked) cs[L.circ_of_step[j]].singular = 1;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // ---- L solve (L schedule, forward) ------------------------------------------
 __global__ void k_lsolve_hubs(LUDev L, const double *__restrict__ b, const CircState *cs, int masked) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -367,7 +462,15 @@ static void factor_sweeps(cudaStream_t st, const LUDev &L, const double *vals, C
   if (L.fs.n_hub > 0) k_factor_hubs<T><<<L.fs.n_hub, 256, 0, st>>>(L, vals, cs, masked, pivot_tol);
   if (L.fs.n_groups > 0)
     k_factor_groups<T><<<L.fs.n_groups, kGroupThreads, 0, st>>>(L, vals, cs, masked, pivot_tol, 0);
-  if (L.fs.n_top_items > 0) k_factor_groups<T><<<1, 1024, 0, st>>>(L, vals, cs, masked, pivot_tol, 1);
+  if (L.fs.n_top_items > 0) {
+    if (L.top_start >= 0) {
+      const long long threads = (long long)(L.n - L.top_start) * 32;
+      k_top_pull<T><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(L, vals, cs, masked);
+      k_top_rl<T><<<1, 1024, 0, st>>>(L, cs, masked, pivot_tol);
+    } else {
+      k_factor_groups<T><<<1, 1024, 0, st>>>(L, vals, cs, masked, pivot_tol, 1);
+    }
+  }
 }
 
 // FP64 factors, or FP32 factors when the analysis selected the refined solve.

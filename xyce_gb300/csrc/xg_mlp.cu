@@ -146,7 +146,7 @@ __device__ __forceinline__ void mlp_forward_warp(const MlpSmem &S, const float (
 // d2 = x_{n-1} - x_{n-2}, d3 = x_{n-2} - x_{n-3}) is the node's recent motion
 // and the features are (d1 / s, d2 / s, d3 / s, x_n, log(h_{n+1} / h_n)),
 // standardized by in_shift / in_scale: a node at rest keeps its polynomial
-// guess.  xn0 itself stays the polynomial predictor, so the predictor-
+// guess (rows with s < kMlpActive are not corrected).  xn0 itself stays the polynomial predictor, so the predictor-
 // corrector error estimate (OneStep, N_TIA_OneStep.C:1584-1640) and the step
 // control are those of the reference.  Branch currents keep the polynomial guess.
 __global__ void __launch_bounds__(128) k_ml_predict(DevArrays d, int n) {
@@ -166,9 +166,10 @@ __global__ void __launch_bounds__(128) k_ml_predict(DevArrays d, int n) {
     if (r < n && !d.is_branch[r]) {
       const CircState &s = d.cs[d.circ_of_row[r]];
       if (s.start_step && s.phase == PH_TRAN && s.ml_use && s.lastTimeStep > 0.0) {
-        use[q] = true;
         const double d1 = d.mlh1[r], d2 = d.mlh2[r], d3 = d.mlh3[r];
         const double sc = fabs(d1) + fabs(d2) + fabs(d3) + kMlpScaleFloor;
+        if (sc < kMlpActive) continue;  // a node at rest keeps the polynomial guess
+        use[q] = true;
         scale[q] = sc;
         const double raw[kMlpIn] = {d1 / sc, d2 / sc, d3 / sc, d.xcurr[r], log(s.h / s.lastTimeStep)};
         for (int k = 0; k < kMlpIn; ++k) f[q][k] = (float)((raw[k] - S.in_shift[k]) * S.in_scale[k]);

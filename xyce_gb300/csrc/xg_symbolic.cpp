@@ -504,6 +504,20 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
   out.lsched = build_schedule(
       n, [&](int i, std::vector<int> &d) { for (int t = out.l_ptr[i]; t < out.l_ptr[i + 1]; ++t) d.push_back(out.l_col[t]); },
       [&](int i) { return (out.l_ptr[i + 1] - out.l_ptr[i]) > kLongSolveRow; }, nullptr);
+  // Is the factor schedule's top the suffix [n - n_top, n) of the steps?  (Nested
+  // dissection numbers the upper separators last, so it normally is.)
+  {
+    const Schedule &S = out.fsched;
+    const int nt = S.n_top_items;
+    out.top_start = -1;
+    if (nt >= kTopRightLooking) {
+      const int first = S.lvl_ptr[S.grp_lvl[S.n_groups]];
+      bool suffix = ((int)S.items.size() - first) == nt;
+      for (int q = first; suffix && q < (int)S.items.size(); ++q)
+        if (S.items[q] < n - nt) suffix = false;
+      if (suffix) out.top_start = n - nt;
+    }
+  }
   return XG_OK;
 }
 

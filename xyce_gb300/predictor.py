@@ -12,7 +12,8 @@ d2 = x_{n-1} - x_{n-2}, d3 = x_{n-2} - x_{n-3}):
   features  d1 / s, d2 / s, d3 / s, x_n, log(h_{n+1} / h_n)
   target    (x_{n+1} - polynomial predictor of step n+1) / s
 The device starts Newton from the polynomial predictor plus s times the
-network's output, so a node at rest keeps the polynomial guess.
+network's output; nodes with s < 1e-5 V keep the polynomial guess and are
+left out of the training set.
 The recorded sequence of a circuit starts with its operating point (index 0)
 followed by the accepted transient points, so step index m >= 5 qualifies.
 """
@@ -24,6 +25,7 @@ from . import MLP_NNORM, MLP_NPARAM, PRED_LEARNED, PRED_POLY, Circuit
 
 N_IN, N_HID = 5, 64
 SCALE_FLOOR = 1e-9  # V, as kMlpScaleFloor in the library
+ACTIVE = 1e-5       # V, as kMlpActive: nodes moving less are not corrected
 
 
 def node_unknowns(nl) -> np.ndarray:
@@ -64,12 +66,15 @@ def dataset(counts, t, v, p, pcount):
                 continue
             d1, d2, d3 = vv[m - 1] - vv[m - 2], vv[m - 2] - vv[m - 3], vv[m - 3] - vv[m - 4]
             sc = np.abs(d1) + np.abs(d2) + np.abs(d3) + SCALE_FLOOR
-            f = np.empty((q, N_IN))
-            f[:, 0], f[:, 1], f[:, 2] = d1 / sc, d2 / sc, d3 / sc
-            f[:, 3] = vv[m - 1]
+            act = sc >= ACTIVE
+            if not act.any():
+                continue
+            f = np.empty((int(act.sum()), N_IN))
+            f[:, 0], f[:, 1], f[:, 2] = d1[act] / sc[act], d2[act] / sc[act], d3[act] / sc[act]
+            f[:, 3] = vv[m - 1][act]
             f[:, 4] = np.log(h1 / h0)
             xs.append(f)
-            ys.append((vv[m] - pp[m]) / sc)
+            ys.append((vv[m][act] - pp[m][act]) / sc[act])
     return np.concatenate(xs), np.concatenate(ys)
 
 
