@@ -774,7 +774,13 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
     L.a_vals = ctx->d.J;  // the transient's Jacobian; xg_lu_factor points it at its values
   }
   L.breakdown = ctx->breakdown_dev;
-  L.top_start = H.top_start;
+  L.n_top_rl = (int)H.top_items.size();
+  if (L.n_top_rl > 0) {
+    if ((rc = dev_upload(ctx, &L.top_items, H.top_items, A))) return rc;
+    std::vector<char> is_top(H.n, 0);
+    for (int j : H.top_items) is_top[j] = 1;
+    if ((rc = dev_upload(ctx, &L.is_top, is_top, A))) return rc;
+  }
   L.f_levels = (int)H.f_lvl_ptr.size() - 1;
   L.l_levels = (int)H.l_lvl_ptr.size() - 1;
   L.u_levels = (int)H.u_lvl_ptr.size() - 1;

@@ -216,10 +216,12 @@ struct LUDev {
   // factors; each solve is refined n_refine times against the FP64 matrix
   // a_vals (CSR a_rp/a_ci in unknown order, the values last factored).
   int mixed = 0, n_refine = 0;
-  // factor schedule's top as a contiguous suffix of steps [top_start, n):
-  // factored by a multi-CTA pull of the sub-tree updates, then one
-  // right-looking CTA (top_start < 0: the top runs left-looking like a group)
-  int top_start = -1;
+  // factor schedule's top (n_top_rl steps, ascending, every L row of a top
+  // column a top step): a multi-CTA pull of the sub-tree updates, then one
+  // right-looking CTA; n_top_rl == 0: the top runs left-looking like a group
+  int n_top_rl = 0;
+  int *top_items = nullptr;
+  char *is_top = nullptr;
   float *lu32 = nullptr;
   double *ir_r = nullptr;
   const int *a_rp = nullptr, *a_ci = nullptr, *a_circ = nullptr;
@@ -229,7 +231,9 @@ struct LUDev {
 // Host-side analysis result.
 struct LUHost {
   int n = 0;
-  int top_start = -1;  // first step of the factor schedule's top when the top is a suffix, else -1
+  // steps of the factor schedule's top in ascending order when the top can be
+  // factored right-looking (every L row of a top column is a top step), else empty
+  std::vector<int> top_items;
   std::vector<int> row_of_step, col_of_step, cp, ri, diag, src;
   std::vector<int> f_lvl_ptr, f_cols, l_lvl_ptr, l_rows, l_ptr, l_pos, l_col;
   std::vector<int> u_lvl_ptr, u_rows, u_ptr, u_pos, u_col;

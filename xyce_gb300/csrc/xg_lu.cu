@@ -193,19 +193,21 @@ __global__ void __launch_bounds__(1024) k_factor_groups(LUDev L, const double *_
 }
 
 // ---- top of the factorization: pull, then right-looking -------------------
-// When the factor schedule's top is the step suffix [top_start, n) (the upper
-// separators of the nested dissection), its columns first pull, in parallel
-// (one warp each), the updates of every column before the top — all factored
-// by then — and then one CTA factors the top right-looking: pivot test and
-// scaling of column k, then the rank-1 update of every column j with
-// U(k, j) != 0 (a warp per U entry, lanes over L(:, k)).  One barrier pair per
-// top column replaces the per-(column, row) barriers of the left-looking walk.
+// When every L row of a top column is itself a top step (the analysis checks
+// it; the top holds the upper separators of the nested dissection), the top
+// columns first pull, in parallel (one warp each), the updates of every
+// sub-tree column — all factored by then — and then one CTA factors the top
+// right-looking in step order: pivot test and scaling of column k, then the
+// rank-1 update of every column j with U(k, j) != 0 (a warp per U entry,
+// lanes over L(:, k)).  One barrier pair per top column replaces the
+// per-(column, row) barriers of the left-looking walk.
 template <typename T>
 __global__ void __launch_bounds__(256) k_top_pull(LUDev L, const double *__restrict__ vals, CircState *cs,
                                                    int masked) {
   const int lane = threadIdx.x & 31;
-  const int j = L.top_start + (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-  if (j >= L.n) return;  // warp-uniform
+  const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  if (w >= L.n_top_rl) return;  // warp-uniform
+  const int j = L.top_items[w];
   if (!item_active(L, cs, masked, j)) return;
   T *lu = lu_of<T>(L);
   const int p0 = L.cp[j], p1 = L.cp[j + 1], pd = L.diag[j];
@@ -217,7 +219,7 @@ __global__ void __launch_bounds__(256) k_top_pull(LUDev L, const double *__restr
   bool lost = false;
   for (int p = p0; p < pd; ++p) {
     const int k = L.ri[p];
-    if (k >= L.top_start) break;  // the top's own updates come right-looking
+    if (L.is_top[k]) continue;  // the top's own updates come right-looking
     const T ukj = lu[p];
     if (ukj != (T)0) {
       const int q0 = L.diag[k] + 1, q1 = L.cp[k + 1];
@@ -241,7 +243,8 @@ __global__ void __launch_bounds__(1024) k_top_rl(LUDev L, CircState *cs, int mas
   __shared__ double sm[32];
   T *lu = lu_of<T>(L);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-  for (int k = L.top_start; k < L.n; ++k) {
+  for (int t = 0; t < L.n_top_rl; ++t) {
+    const int k = L.top_items[t];
     if (!item_active(L, cs, masked, k)) continue;  // uniform: every thread reads the same flags
     const int pd = L.diag[k], p1 = L.cp[k + 1];
     double amax = 0.0;
@@ -463,8 +466,8 @@ static void factor_sweeps(cudaStream_t st, const LUDev &L, const double *vals, C
   if (L.fs.n_groups > 0)
     k_factor_groups<T><<<L.fs.n_groups, kGroupThreads, 0, st>>>(L, vals, cs, masked, pivot_tol, 0);
   if (L.fs.n_top_items > 0) {
-    if (L.top_start >= 0) {
-      const long long threads = (long long)(L.n - L.top_start) * 32;
+    if (L.n_top_rl > 0) {
+      const long long threads = (long long)L.n_top_rl * 32;
       k_top_pull<T><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(L, vals, cs, masked);
       k_top_rl<T><<<1, 1024, 0, st>>>(L, cs, masked, pivot_tol);
     } else {

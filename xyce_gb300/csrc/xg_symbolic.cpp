@@ -504,18 +504,35 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
   out.lsched = build_schedule(
       n, [&](int i, std::vector<int> &d) { for (int t = out.l_ptr[i]; t < out.l_ptr[i + 1]; ++t) d.push_back(out.l_col[t]); },
       [&](int i) { return (out.l_ptr[i + 1] - out.l_ptr[i]) > kLongSolveRow; }, nullptr);
-  // Is the factor schedule's top the suffix [n - n_top, n) of the steps?  (Nested
-  // dissection numbers the upper separators last, so it normally is.)
+  // Can the factor schedule's top run right-looking?  The sub-tree (non-top)
+  // rows k of a top column j are pulled first, in step order; that is exact
+  // when no top column m < k updates such a row, i.e. when every non-top L
+  // row r of a top column has no U entry in a top column.  (Typical non-top
+  // L rows of the top: the branch unknowns of voltage sources peeled to the
+  // end of the order, whose U rows are empty.)
   {
     const Schedule &S = out.fsched;
-    const int nt = S.n_top_items;
-    out.top_start = -1;
-    if (nt >= kTopRightLooking) {
+    out.top_items.clear();
+    if (S.n_top_items >= kTopRightLooking) {
       const int first = S.lvl_ptr[S.grp_lvl[S.n_groups]];
-      bool suffix = ((int)S.items.size() - first) == nt;
-      for (int q = first; suffix && q < (int)S.items.size(); ++q)
-        if (S.items[q] < n - nt) suffix = false;
-      if (suffix) out.top_start = n - nt;
+      std::vector<char> is_top(n, 0);
+      for (int q = first; q < (int)S.items.size(); ++q) is_top[S.items[q]] = 1;
+      bool ok = true;
+      std::vector<char> checked(n, 0);
+      for (int m = 0; m < n && ok; ++m) {
+        if (!is_top[m]) continue;
+        for (int p = out.diag[m] + 1; p < out.cp[m + 1] && ok; ++p) {
+          const int r = out.ri[p];
+          if (is_top[r] || checked[r]) continue;
+          checked[r] = 1;
+          for (int t = out.u_ptr[r]; t < out.u_ptr[r + 1]; ++t)
+            if (is_top[out.u_col[t]]) { ok = false; break; }
+        }
+      }
+      if (ok) {
+        for (int m = 0; m < n; ++m)
+          if (is_top[m]) out.top_items.push_back(m);
+      }
     }
   }
   return XG_OK;
