@@ -56,6 +56,7 @@ struct xg_ctx {
   int n_analyze = 0;
   int lu_prec = XG_PREC_FP64, lu_refine = 2;  // xg_lu_set_precision
   int predictor = XG_PRED_POLY;                // xg_set_predictor
+  std::vector<int> h_tlv_item_ptr, h_tlv_grp_ptr;  // host copies for the per-level top launches
   bool mlp_ready = false;                      // weights set (xg_mlp_set) or trained
   float *mlp_m1 = nullptr, *mlp_m2 = nullptr, *mlp_grad = nullptr, *mlp_loss = nullptr;
   int mlp_adam_t = 0;
@@ -780,6 +781,16 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
     std::vector<char> is_top(H.n, 0);
     for (int j : H.top_items) is_top[j] = 1;
     if ((rc = dev_upload(ctx, &L.is_top, is_top, A))) return rc;
+    for (auto pr : {std::make_pair(&L.tlv_items, &H.tlv_items), std::make_pair(&L.tlv_item_ptr, &H.tlv_item_ptr),
+                    std::make_pair(&L.tlv_grp_ptr, &H.tlv_grp_ptr), std::make_pair(&L.tgrp_col, &H.tgrp_col),
+                    std::make_pair(&L.tgrp_ptr, &H.tgrp_ptr), std::make_pair(&L.tgrp_pos, &H.tgrp_pos),
+                    std::make_pair(&L.tgrp_k, &H.tgrp_k)})
+      if ((rc = dev_upload(ctx, pr.first, *pr.second, A))) return rc;
+    ctx->h_tlv_item_ptr = H.tlv_item_ptr;
+    ctx->h_tlv_grp_ptr = H.tlv_grp_ptr;
+    L.n_top_lv = (int)H.tlv_item_ptr.size() - 1;
+    L.h_tlv_item_ptr = ctx->h_tlv_item_ptr.data();
+    L.h_tlv_grp_ptr = ctx->h_tlv_grp_ptr.data();
   }
   L.f_levels = (int)H.f_lvl_ptr.size() - 1;
   L.l_levels = (int)H.l_lvl_ptr.size() - 1;

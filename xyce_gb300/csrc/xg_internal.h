@@ -222,6 +222,12 @@ struct LUDev {
   int n_top_rl = 0;
   int *top_items = nullptr;
   char *is_top = nullptr;
+  // level-synchronous right-looking top (all SMs; see LUHost::tlv_*): device
+  // arrays, and host copies of the level pointers for the per-level launches
+  int n_top_lv = 0;
+  int *tlv_items = nullptr, *tlv_item_ptr = nullptr, *tlv_grp_ptr = nullptr;
+  int *tgrp_col = nullptr, *tgrp_ptr = nullptr, *tgrp_pos = nullptr, *tgrp_k = nullptr;
+  const int *h_tlv_item_ptr = nullptr, *h_tlv_grp_ptr = nullptr;
   float *lu32 = nullptr;
   double *ir_r = nullptr;
   const int *a_rp = nullptr, *a_ci = nullptr, *a_circ = nullptr;
@@ -234,6 +240,12 @@ struct LUHost {
   // steps of the factor schedule's top in ascending order when the top can be
   // factored right-looking (every L row of a top column is a top step), else empty
   std::vector<int> top_items;
+  // levels of the right-looking top: level l pivots tlv_items[tlv_item_ptr[l] ..
+  // tlv_item_ptr[l+1]) (independent columns), then updates the target-column
+  // groups tlv_grp_ptr[l] .. tlv_grp_ptr[l+1]; group g is column tgrp_col[g]
+  // receiving the U entries (positions) tgrp_pos[tgrp_ptr[g] .. tgrp_ptr[g+1])
+  // of pivots tgrp_k[...] of that level
+  std::vector<int> tlv_items, tlv_item_ptr, tlv_grp_ptr, tgrp_col, tgrp_ptr, tgrp_pos, tgrp_k;
   std::vector<int> row_of_step, col_of_step, cp, ri, diag, src;
   std::vector<int> f_lvl_ptr, f_cols, l_lvl_ptr, l_rows, l_ptr, l_pos, l_col;
   std::vector<int> u_lvl_ptr, u_rows, u_ptr, u_pos, u_col;

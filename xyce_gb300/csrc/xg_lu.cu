@@ -290,6 +290,67 @@ __global__ void __launch_bounds__(1024) k_top_rl(LUDev L, CircState *cs, int mas
   }
 }
 
+// Level-synchronous right-looking top on all SMs.  Level l: (1) every pivot
+// column of the level (independent of each other) is tested and scaled, a
+// warp each; (2) every target column j that receives updates from pivots of
+// the level is updated by one warp, which applies its pivots' rank-1 terms
+// one after the other (deterministic, no atomics), lanes over L(:, k).
+template <typename T>
+__global__ void __launch_bounds__(256) k_toplv_pivot(LUDev L, int lv, CircState *cs, int masked, double pivot_tol) {
+  const int lane = threadIdx.x & 31;
+  const int t = L.tlv_item_ptr[lv] + (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  if (t >= L.tlv_item_ptr[lv + 1]) return;  // warp-uniform
+  const int k = L.tlv_items[t];
+  if (!item_active(L, cs, masked, k)) return;
+  T *lu = lu_of<T>(L);
+  const int pd = L.diag[k], p1 = L.cp[k + 1];
+  double amax = 0.0;
+  for (int p = pd + lane; p < p1; p += 32) amax = fmax(amax, fabs((double)lu[p]));
+  for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+  const double d = (double)lu[pd];
+  const bool urow = L.u_ptr[k + 1] > L.u_ptr[k] && !L.exempt[k];
+  const bool bad = (urow && !(fabs(d) >= pivot_tol * amax)) || !(fabs(d) > 0.0) || isinf(d);
+  if (bad) {
+    if (lane == 0) {
+      atomicCAS(L.breakdown, 0, k + 1);
+      if (masked) cs[L.circ_of_step[k]].singular = 1;
+    }
+    return;
+  }
+  const T inv = (T)1 / lu[pd];
+  for (int p = pd + 1 + lane; p < p1; p += 32) lu[p] *= inv;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_toplv_update(LUDev L, int lv, CircState *cs, int masked) {
+  const int lane = threadIdx.x & 31;
+  const int g = L.tlv_grp_ptr[lv] + (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  if (g >= L.tlv_grp_ptr[lv + 1]) return;  // warp-uniform
+  T *lu = lu_of<T>(L);
+  const int j = L.tgrp_col[g], cend = L.cp[j + 1];
+  bool lost = false;
+  for (int e = L.tgrp_ptr[g]; e < L.tgrp_ptr[g + 1]; ++e) {
+    const int k = L.tgrp_k[e];
+    if (!item_active(L, cs, masked, k)) continue;  // warp-uniform
+    const int p = L.tgrp_pos[e];  // U(k, j)
+    const T ukj = lu[p];
+    if (ukj != (T)0) {
+      const int q0 = L.diag[k] + 1, nl = L.cp[k + 1] - q0;
+      const int *tgt = L.upd_pos + L.upd_off[p];
+      for (int q = lane; q < nl; q += 32) {
+        const int pos = tgt[q];
+        if (pos > p && pos < cend) lu[pos] -= lu[q0 + q] * ukj;
+        else lost = true;
+      }
+    }
+    __syncwarp();
+  }
+  if (__any_sync(0xffffffffu, lost) && lane == 0) {
+    atomicCAS(L.breakdown, 0, j + 1);
+    if (masked) cs[L.circ_of_step[j]].singular = 1;
+  }
+}
+
 // ---- L solve (L schedule, forward) ------------------------------------------
 __global__ void k_lsolve_hubs(LUDev L, const double *__restrict__ b, const CircState *cs, int masked) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -469,7 +530,16 @@ static void factor_sweeps(cudaStream_t st, const LUDev &L, const double *vals, C
     if (L.n_top_rl > 0) {
       const long long threads = (long long)L.n_top_rl * 32;
       k_top_pull<T><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(L, vals, cs, masked);
-      k_top_rl<T><<<1, 1024, 0, st>>>(L, cs, masked, pivot_tol);
+      if (L.n_top_lv > 0 && L.h_tlv_item_ptr) {
+        for (int lv = 0; lv < L.n_top_lv; ++lv) {
+          const int ni = L.h_tlv_item_ptr[lv + 1] - L.h_tlv_item_ptr[lv];
+          const int ng = L.h_tlv_grp_ptr[lv + 1] - L.h_tlv_grp_ptr[lv];
+          if (ni > 0) k_toplv_pivot<T><<<(ni + 7) / 8, 256, 0, st>>>(L, lv, cs, masked, pivot_tol);
+          if (ng > 0) k_toplv_update<T><<<(ng + 7) / 8, 256, 0, st>>>(L, lv, cs, masked);
+        }
+      } else {
+        k_top_rl<T><<<1, 1024, 0, st>>>(L, cs, masked, pivot_tol);
+      }
     } else {
       k_factor_groups<T><<<1, 1024, 0, st>>>(L, vals, cs, masked, pivot_tol, 1);
     }

@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstdio>
 #include <functional>
+#include <map>
 #include <numeric>
 #include <deque>
 #include <queue>
@@ -532,6 +533,44 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
       if (ok) {
         for (int m = 0; m < n; ++m)
           if (is_top[m]) out.top_items.push_back(m);
+        // right-looking levels: column k pivots after every top k' with
+        // U(k', k) != 0 (its updates) and every top k' with L(k, k') != 0 (an
+        // update of k' writes row k, which k reads as U(k, j))
+        std::vector<int> lev(n, 0);
+        int nlev = 0;
+        for (int k : out.top_items) {
+          int l = 0;
+          for (int p = out.cp[k]; p < out.diag[k]; ++p)
+            if (is_top[out.ri[p]]) l = std::max(l, lev[out.ri[p]] + 1);
+          for (int t = out.l_ptr[k]; t < out.l_ptr[k + 1]; ++t)
+            if (is_top[out.l_col[t]]) l = std::max(l, lev[out.l_col[t]] + 1);
+          lev[k] = l;
+          nlev = std::max(nlev, l + 1);
+        }
+        std::vector<std::vector<int>> at(nlev);
+        for (int k : out.top_items) at[lev[k]].push_back(k);
+        out.tlv_items.clear();
+        out.tlv_item_ptr.assign(1, 0);
+        out.tlv_grp_ptr.assign(1, 0);
+        out.tgrp_col.clear();
+        out.tgrp_ptr.assign(1, 0);
+        out.tgrp_pos.clear();
+        out.tgrp_k.clear();
+        std::map<int, std::vector<std::pair<int, int>>> by_col;  // j -> (k, position of U(k, j))
+        for (int l = 0; l < nlev; ++l) {
+          by_col.clear();
+          for (int k : at[l]) {
+            out.tlv_items.push_back(k);
+            for (int t = out.u_ptr[k]; t < out.u_ptr[k + 1]; ++t) by_col[out.u_col[t]].push_back({k, out.u_pos[t]});
+          }
+          out.tlv_item_ptr.push_back((int)out.tlv_items.size());
+          for (auto &kv : by_col) {
+            out.tgrp_col.push_back(kv.first);
+            for (auto &e : kv.second) { out.tgrp_k.push_back(e.first); out.tgrp_pos.push_back(e.second); }
+            out.tgrp_ptr.push_back((int)out.tgrp_pos.size());
+          }
+          out.tlv_grp_ptr.push_back((int)out.tgrp_col.size());
+        }
       }
     }
   }
