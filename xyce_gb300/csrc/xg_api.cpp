@@ -57,6 +57,7 @@ struct xg_ctx {
   int lu_prec = XG_PREC_FP64, lu_refine = 2;  // xg_lu_set_precision
   int predictor = XG_PRED_POLY;                // xg_set_predictor
   std::vector<int> h_tlv_item_ptr, h_tlv_grp_ptr;  // host copies for the per-level top launches
+  std::vector<int> h_ls_lvl_ptr, h_fs_lvl_ptr;
   bool mlp_ready = false;                      // weights set (xg_mlp_set) or trained
   float *mlp_m1 = nullptr, *mlp_m2 = nullptr, *mlp_grad = nullptr, *mlp_loss = nullptr;
   int mlp_adam_t = 0;
@@ -791,6 +792,16 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
     L.n_top_lv = (int)H.tlv_item_ptr.size() - 1;
     L.h_tlv_item_ptr = ctx->h_tlv_item_ptr.data();
     L.h_tlv_grp_ptr = ctx->h_tlv_grp_ptr.data();
+  }
+  if (H.fsched.n_top_items >= kTopRightLooking) {
+    ctx->h_ls_lvl_ptr = H.lsched.lvl_ptr;
+    ctx->h_fs_lvl_ptr = H.fsched.lvl_ptr;
+    L.h_ls_lvl_ptr = ctx->h_ls_lvl_ptr.data();
+    L.h_fs_lvl_ptr = ctx->h_fs_lvl_ptr.data();
+    L.ls_top_lo = H.lsched.grp_lvl[H.lsched.n_groups];
+    L.ls_top_hi = H.lsched.grp_lvl[H.lsched.n_groups + 1];
+    L.fs_top_lo = H.fsched.grp_lvl[H.fsched.n_groups];
+    L.fs_top_hi = H.fsched.grp_lvl[H.fsched.n_groups + 1];
   }
   L.f_levels = (int)H.f_lvl_ptr.size() - 1;
   L.l_levels = (int)H.l_lvl_ptr.size() - 1;

@@ -228,6 +228,11 @@ struct LUDev {
   int *tlv_items = nullptr, *tlv_item_ptr = nullptr, *tlv_grp_ptr = nullptr;
   int *tgrp_col = nullptr, *tgrp_ptr = nullptr, *tgrp_pos = nullptr, *tgrp_k = nullptr;
   const int *h_tlv_item_ptr = nullptr, *h_tlv_grp_ptr = nullptr;
+  // the tops of the solves one level per launch on all SMs (when the top is
+  // large): host copies of the L- and factor-schedule level pointers and the
+  // tops' level ranges [lo, hi)
+  const int *h_ls_lvl_ptr = nullptr, *h_fs_lvl_ptr = nullptr;
+  int ls_top_lo = 0, ls_top_hi = 0, fs_top_lo = 0, fs_top_hi = 0;
   float *lu32 = nullptr;
   double *ir_r = nullptr;
   const int *a_rp = nullptr, *a_ci = nullptr, *a_circ = nullptr;

@@ -456,6 +456,44 @@ __global__ void __launch_bounds__(256) k_usolve_hubs(LUDev L, double *__restrict
   solve_row<false, true, T, ACC>(L, nullptr, x, k, threadIdx.x, sm);
 }
 
+// ---- the tops of the solves, one level per launch on all SMs --------------
+// (large tops: the upper separators give hundreds of levels that one CTA
+// would walk alone).  A warp per row; the level's rows are independent.
+template <typename T>
+__global__ void __launch_bounds__(256) k_lsolve_level(LUDev L, int lv, const double *__restrict__ b,
+                                                      const CircState *cs, int masked) {
+  const int lane = threadIdx.x & 31;
+  const int t = L.ls.lvl_ptr[lv] + (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  if (t >= L.ls.lvl_ptr[lv + 1]) return;  // warp-uniform
+  const int i = L.ls.items[t];
+  if (!item_active(L, cs, masked, i)) return;
+  const T *lu = lu_of<T>(L);
+  double sum = 0.0;
+  for (int q = L.l_ptr[i] + lane; q < L.l_ptr[i + 1]; q += 32) sum += (double)lu[L.l_pos[q]] * L.y[L.l_col[q]];
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (lane == 0) L.y[i] = b[L.row_of_step[i]] - sum;
+}
+
+template <typename T, bool ACC>
+__global__ void __launch_bounds__(256) k_usolve_level(LUDev L, int lv, double *__restrict__ x, const CircState *cs,
+                                                      int masked) {
+  const int lane = threadIdx.x & 31;
+  const int t = L.fs.lvl_ptr[lv] + (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  if (t >= L.fs.lvl_ptr[lv + 1]) return;  // warp-uniform
+  const int k = L.fs.items[t];
+  if (!item_active(L, cs, masked, k)) return;
+  const T *lu = lu_of<T>(L);
+  double sum = 0.0;
+  for (int q = L.u_ptr[k] + lane; q < L.u_ptr[k + 1]; q += 32) sum += (double)lu[L.u_pos[q]] * L.y[L.u_col[q]];
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (lane == 0) {
+    const double z = (L.y[k] - sum) / (double)lu[L.diag[k]];
+    L.y[k] = z;
+    if (ACC) x[L.col_of_step[k]] += z;
+    else x[L.col_of_step[k]] = z;
+  }
+}
+
 // ---- FP64 residual of a refined solve ---------------------------------------
 // r = b - A x over the rows of active circuits, A in the context's CSR order
 // (IRSolver's residual step, src/LinearAlgebraServicesPKG/N_LAS_IRSolver.C:482-540).
@@ -559,8 +597,26 @@ static void solve_sweeps(cudaStream_t st, const LUDev &L, const double *b, doubl
                          int masked) {
   if (L.ls.n_hub > 0) k_lsolve_hubs<<<(L.ls.n_hub + 255) / 256, 256, 0, st>>>(L, b, cs, masked);
   if (L.ls.n_groups > 0) k_lsolve_groups<T><<<L.ls.n_groups, kGroupThreads, 0, st>>>(L, b, cs, masked, 0);
-  if (L.ls.n_top_items > 0) k_lsolve_groups<T><<<1, 1024, 0, st>>>(L, b, cs, masked, 1);
-  if (L.fs.n_top_items > 0) k_usolve_groups<T, ACC><<<1, 1024, 0, st>>>(L, x, cs, masked, 1);
+  if (L.ls.n_top_items > 0) {
+    if (L.h_ls_lvl_ptr) {
+      for (int lv = L.ls_top_lo; lv < L.ls_top_hi; ++lv) {
+        const int nr = L.h_ls_lvl_ptr[lv + 1] - L.h_ls_lvl_ptr[lv];
+        if (nr > 0) k_lsolve_level<T><<<(nr + 7) / 8, 256, 0, st>>>(L, lv, b, cs, masked);
+      }
+    } else {
+      k_lsolve_groups<T><<<1, 1024, 0, st>>>(L, b, cs, masked, 1);
+    }
+  }
+  if (L.fs.n_top_items > 0) {
+    if (L.h_fs_lvl_ptr) {
+      for (int lv = L.fs_top_hi - 1; lv >= L.fs_top_lo; --lv) {
+        const int nr = L.h_fs_lvl_ptr[lv + 1] - L.h_fs_lvl_ptr[lv];
+        if (nr > 0) k_usolve_level<T, ACC><<<(nr + 7) / 8, 256, 0, st>>>(L, lv, x, cs, masked);
+      }
+    } else {
+      k_usolve_groups<T, ACC><<<1, 1024, 0, st>>>(L, x, cs, masked, 1);
+    }
+  }
   if (L.fs.n_groups > 0) k_usolve_groups<T, ACC><<<L.fs.n_groups, kGroupThreads, 0, st>>>(L, x, cs, masked, 0);
   if (L.fs.n_hub > 0) k_usolve_hubs<T, ACC><<<L.fs.n_hub, 256, 0, st>>>(L, x, cs, masked);
 }
