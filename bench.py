@@ -94,12 +94,12 @@ def _clock_summary(path, device_index):
     return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons)}
 
 
-def _workload(name):
+def _workload(name, rings=4096):
     from xyce_gb300 import netlist as N
     if name == "mc":
-        nl = N.monte_carlo_rings(4096)
+        nl = N.monte_carlo_rings(rings)
         probes = [nl.names[f"c{i}.n1"] for i in (0, 1, 2, 3)]
-        desc = dict(workload="monte_carlo_rings_4096", circuits=4096, mosfets=len(nl.mos1),
+        desc = dict(workload=f"monte_carlo_rings_{rings}", circuits=rings, mosfets=len(nl.mos1),
                     stages="odd U[11,301]", tran="0 10n, hmax 5p")
     else:
         nl = N.ring_oscillator(10001)
@@ -189,7 +189,7 @@ def run_reference(args):
     world, rank, _ = _dist()
     if rank != 0:
         return
-    _, _, desc = _workload(args.workload)
+    _, _, desc = _workload(args.workload, args.rings)
     cb = cpu_baseline(args)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
@@ -225,6 +225,53 @@ def _timed_windows(xg, nl, probes, dev, args, window, prec, flush, stream_of):
     return circ, ms, st0, st1
 
 
+def _roofline(xg, circ, nl, dev, flush, stream_of, hbm_peak, peak_kind, args):
+    """k_mos1 in loader mode (xg_update_state, separate dF/dQ slots), one
+    launch over every MOSFET of the workload, L2 flushed before each launch."""
+    import torch
+    n = circ.n
+    stream = stream_of(circ)
+    z = lambda k: torch.zeros(max(1, k), dtype=torch.float64, device=f"cuda:{dev}")
+    x = torch.full((n,), 0.9, dtype=torch.float64, device=f"cuda:{dev}")
+    stac, stan, stoc, ston = z(circ.nsta), z(circ.nsta), z(circ.nsto), z(circ.nsto)
+    for _ in range(5):
+        circ.update_state(x, stac, stoc, stan, ston, newton_iter=1)
+    reps = 50
+    us_all = 0.0
+    for _ in range(reps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        circ.update_state(x, stac, stoc, stan, ston, newton_iter=1)
+        e1.record(stream)
+        e1.synchronize()
+        us_all += e0.elapsed_time(e1) * 1e3
+    us = us_all / reps
+    nm = len(nl.mos1)
+    # per instance: reads 4 node indices, model index, circuit index (24 B),
+    # beta + vbi (16 B), 4 node voltages (32 B), 5 history stores (40 B);
+    # writes 6 stores + 8 states (112 B) and 47 stamp slots (376 B): 600 B
+    bytes_per_inst = 24 + 16 + 32 + 40 + 112 + 376
+    achieved = bytes_per_inst * nm / (us * 1e-6) / 1e9
+    traffic = None
+    prof = os.path.join(HERE, "profiles", f"k_mos1_{args.workload}.traffic.json")
+    if args.workload == "mc" and args.rings != 4096:
+        prof = ""
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+    return {"kernel": "k_mos1 (MOSFET-1 evaluation + stamp, separate dF/dQ slots, one launch over "
+                      f"{nm} instances, L2 flushed before each launch)",
+            "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
+            "algorithmic_bytes_per_launch": bytes_per_inst * nm, "launch_us": us,
+            "fp64_pipe_note": "ncu: FP64 pipe 83.6 % busy in this kernel (profiles/k_mos1_mc1024_full.md); "
+                              "the FP64 pipe, not HBM, bounds it on GB300"}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -241,10 +288,15 @@ def run_ours(args):
     hbm_peak, peak_kind = _peaks()
     w = WORKLOADS[args.workload]
     window = w["window"]
-    nl, probes, desc = _workload(args.workload)
+    nl, probes, desc = _workload(args.workload, args.rings)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
     stream_of = lambda c: torch.cuda.ExternalStream(xg.lib().xg_get_stream(c.h))
 
+    if args.roofline_only:
+        circ = xg.Circuit(nl, device=dev)
+        print(json.dumps(_roofline(xg, circ, nl, dev, flush, stream_of, hbm_peak, peak_kind, args)), flush=True)
+        circ.close()
+        return
     clk_path = os.path.join(HERE, "gpurun_out", f"clocks_rank{rank}.csv") \
         if os.path.isdir(os.path.join(HERE, "gpurun_out")) else f"/tmp/xg_clocks_{os.getpid()}.csv"
     sampler = _clock_sampler(clk_path)
@@ -277,45 +329,8 @@ def run_ours(args):
     circ.tran_end()
 
     # ---- roofline of the device-evaluation kernel (MOSFET eval + stamp) ----
-    roof = None
-    if rank == 0:
-        n = circ.n
-        stream = stream_of(circ)
-        z = lambda k: torch.zeros(max(1, k), dtype=torch.float64, device=f"cuda:{dev}")
-        x = torch.full((n,), 0.9, dtype=torch.float64, device=f"cuda:{dev}")
-        stac, stan, stoc, ston = z(circ.nsta), z(circ.nsta), z(circ.nsto), z(circ.nsto)
-        for _ in range(5):
-            circ.update_state(x, stac, stoc, stan, ston, newton_iter=1)
-        reps = 50
-        us_all = 0.0
-        for _ in range(reps):
-            flush.fill_(1.0)
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            circ.update_state(x, stac, stoc, stan, ston, newton_iter=1)
-            e1.record(stream)
-            e1.synchronize()
-            us_all += e0.elapsed_time(e1) * 1e3
-        us = us_all / reps
-        nm = len(nl.mos1)
-        # per instance: reads 4 node indices, model index, circuit index (24 B),
-        # beta + vbi (16 B), 4 node voltages (32 B), 5 history stores (40 B);
-        # writes 6 stores + 8 states (112 B) and 47 stamp slots (376 B): 600 B
-        bytes_per_inst = 24 + 16 + 32 + 40 + 112 + 376
-        achieved = bytes_per_inst * nm / (us * 1e-6) / 1e9
-        traffic = None
-        prof = os.path.join(HERE, "profiles", f"k_mos1_{args.workload}.traffic.json")
-        if os.path.exists(prof):
-            try:
-                traffic = json.load(open(prof)).get("dram_bytes_per_launch")
-            except Exception:
-                traffic = None
-        roof = {"kernel": "k_mos1 (MOSFET-1 evaluation + stamp, separate dF/dQ slots, one launch over "
-                          f"{nm} instances, L2 flushed before each launch)",
-                "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
-                "algorithmic_bytes_per_launch": bytes_per_inst * nm, "launch_us": us}
+    n_unknowns = circ.n
+    roof = _roofline(xg, circ, nl, dev, flush, stream_of, hbm_peak, peak_kind, args) if rank == 0 else None
     circ.close()
 
     # ---- the FP32-LU + FP64-refinement form, same workload ------------------
@@ -358,7 +373,7 @@ def run_ours(args):
         cpu = cpu_baseline(args) if args.cpu else None
         clocks = _clock_summary(clk_path, dev)
         config = dict(desc)
-        config.update({"unknowns": n, "window_steps_per_circuit": window,
+        config.update({"unknowns": n_unknowns, "window_steps_per_circuit": window,
                        "l2": "flushed between windows (256 MiB write); device state > L2",
                        "parallelism": f"replicas x{world}"})
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -382,7 +397,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="mc", choices=sorted(WORKLOADS))
+    ap.add_argument("--rings", type=int, default=4096,
+                    help="rings of the mc workload (a smaller batch is the profiling case)")
     ap.add_argument("--no-cpu", dest="cpu", action="store_false", help="skip the CPU baseline")
+    ap.add_argument("--roofline-only", action="store_true",
+                    help="only the k_mos1 roofline launches (the profiling case of that kernel)")
     ap.add_argument("--no-forms", dest="forms", action="store_false", help="skip the FP32-IR form")
     args = ap.parse_args()
     if args.warmup < 3:

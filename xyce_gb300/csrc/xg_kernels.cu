@@ -301,14 +301,31 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
   q[13] = -Capgb; q[15] = capbs + capbd + Capgb; q[12] = -capbd; q[14] = -capbs;
   q[1] = -Capgd; q[3] = -capbd; q[0] = capbd + Capgd;
   q[9] = -Capgs; q[11] = -capbs; q[10] = capbs + Capgs;
+  // structural zeros of the two 4x4 blocks (the gate conducts no current;
+  // no capacitance couples D-S) are stored without FP64 arithmetic, and the
+  // multiplier is applied only when it is not 1: the FP64 pipe bounds this
+  // kernel on GB300
+  constexpr bool kFnz[16] = {1, 1, 1, 1, 0, 0, 0, 0, 1, 1, 1, 1, 1, 0, 1, 1};
+  constexpr bool kQnz[16] = {1, 1, 0, 1, 1, 1, 1, 1, 0, 1, 1, 1, 1, 1, 1, 1};
+  const bool unitM = (M == 1.0);
   double *sM = d.sM + slotM;
   if (combined) {
 #pragma unroll
-    for (int k = 0; k < 16; ++k) sM[k * nm + i] = (fs * f[k] + qs * q[k]) * M;
+    for (int k = 0; k < 16; ++k) {
+      double v;
+      if (kFnz[k] && kQnz[k]) v = fs * f[k] + qs * q[k];
+      else if (kFnz[k]) v = fs * f[k];
+      else if (kQnz[k]) v = qs * q[k];
+      else v = 0.0;
+      sM[k * nm + i] = unitM ? v : v * M;
+    }
   } else {
     double *sM2 = d.sM2 + slotM;
 #pragma unroll
-    for (int k = 0; k < 16; ++k) { sM[k * nm + i] = f[k] * M; sM2[k * nm + i] = q[k] * M; }
+    for (int k = 0; k < 16; ++k) {
+      sM[k * nm + i] = kFnz[k] ? (unitM ? f[k] : f[k] * M) : 0.0;
+      sM2[k * nm + i] = kQnz[k] ? (unitM ? q[k] : q[k] * M) : 0.0;
+    }
   }
 }
 
