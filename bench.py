@@ -21,7 +21,8 @@ buffers (xg_transient): context creation, netlist upload, operating point,
 analysis, the transient windows and the copy of the probe waveforms back.
 
 The FP32-LU + FP64 iterative-refinement form is timed on the same workload
-in the same run (key "forms").
+in the same run (key "forms"), and so is, for mc, the plain unbatched path: a
+sample of the rings run one at a time, each in its own context.
 
 --impl reference times the CPU FP64 restatement of the reference's
 algorithms (oracle/) on the same metric: for mc, a sample of the same rings
@@ -225,6 +226,40 @@ def _timed_windows(xg, nl, probes, dev, args, window, prec, flush, stream_of):
     return circ, ms, st0, st1
 
 
+def _one_at_a_time(xg, nl, dev, window, stream_of, batched, sample=8, timed=4):
+    """The plain (unbatched) GPU path on the same rings: a sample of `sample`
+    rings spread over the batch, each alone in its own context, `timed`
+    windows of `window` steps after 3 warm-up windows; steps/s = all accepted
+    steps / all device time, i.e. the rate of running the batch one ring at a
+    time."""
+    import torch
+    from xyce_gb300 import netlist as N
+    steps, ms = 0, 0.0
+    picks = [int(i * nl.n_circuits / sample) for i in range(sample)]
+    for ci in picks:
+        sub = N.extract_circuit(nl, ci)
+        c = xg.Circuit(sub, device=dev)
+        c.tran_start(probes=[0], cap=16)
+        stream = stream_of(c)
+        for _ in range(3):
+            c.tran_advance(window)
+        a0 = c.tran_results()[3]["accepted"]
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(timed):
+            c.tran_advance(window)
+        e1.record(stream)
+        e1.synchronize()
+        ms += e0.elapsed_time(e1)
+        steps += c.tran_results()[3]["accepted"] - a0
+        c.tran_end()
+        c.close()
+    rate = steps / (ms / 1e3)
+    return {"one_ring_at_a_time": rate, "one_ring_at_a_time_sample": f"{sample} rings x {timed * window} steps",
+            "batched_over_one_ring_at_a_time": batched / rate}
+
+
 def _roofline(xg, circ, nl, dev, flush, stream_of, hbm_peak, peak_kind, args):
     """k_mos1 in loader mode (xg_update_state, separate dF/dQ slots), one
     launch over every MOSFET of the workload, L2 flushed before each launch."""
@@ -343,6 +378,8 @@ def run_ours(args):
                      (s1["newton_iters"] - s0["newton_iters"]) / max(1, s1["accepted"] - s0["accepted"])}
         c2.tran_end()
         c2.close()
+        if args.workload == "mc":
+            forms.update(_one_at_a_time(xg, nl, dev, window, stream_of, value))
 
     # ---- end to end through the C-ABI with host buffers --------------------
     e2e = None

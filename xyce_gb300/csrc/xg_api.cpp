@@ -758,6 +758,7 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
     SchedDev &D = w ? L.ls : L.fs;
     UP(D.items, S.items); UP(D.lvl_ptr, S.lvl_ptr); UP(D.grp_lvl, S.grp_lvl);
     UP(D.is_long, S.is_long); UP(D.is_long_rev, S.is_long_rev);
+    UP(D.is_thread, S.is_thread); UP(D.is_thread_rev, S.is_thread_rev);
     D.n_hub = S.n_hub;
     D.n_groups = S.n_groups;
     D.n_top_items = S.n_top_items;
@@ -792,6 +793,18 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
     L.n_top_lv = (int)H.tlv_item_ptr.size() - 1;
     L.h_tlv_item_ptr = ctx->h_tlv_item_ptr.data();
     L.h_tlv_grp_ptr = ctx->h_tlv_grp_ptr.data();
+  }
+  if (!H.grp_snz.empty()) {
+    for (int w = 0; w < 2; ++w) {
+      const int cap = kGroupSmemBytes / (w ? (int)sizeof(float) : (int)sizeof(double));
+      for (int z : H.grp_snz)
+        if (z <= cap) L.grp_fit[w] = std::max(L.grp_fit[w], z);
+    }
+    if (L.grp_fit[0] > 0 || L.grp_fit[1] > 0) {
+      if ((rc = lu_prepare_k())) return rc;
+      if ((rc = dev_upload(ctx, &L.grp_soff, H.grp_soff, A))) return rc;
+      if ((rc = dev_upload(ctx, &L.grp_snz, H.grp_snz, A))) return rc;
+    }
   }
   if (H.fsched.n_top_items >= kTopRightLooking) {
     ctx->h_ls_lvl_ptr = H.lsched.lvl_ptr;

@@ -178,12 +178,14 @@ struct DevArrays {
 struct Schedule {
   std::vector<int> items, lvl_ptr, grp_lvl;
   std::vector<char> is_long, is_long_rev;  // whole-block items (forward / backward sweep)
+  std::vector<char> is_thread, is_thread_rev;  // single-thread items (forward / backward sweep)
   int n_hub = 0, n_groups = 0, n_top_items = 0;
 };
 
 struct SchedDev {
   int *items = nullptr, *lvl_ptr = nullptr, *grp_lvl = nullptr;
   char *is_long = nullptr, *is_long_rev = nullptr;
+  char *is_thread = nullptr, *is_thread_rev = nullptr;
   int n_hub = 0, n_groups = 0, n_top_items = 0;
 };
 
@@ -196,6 +198,14 @@ constexpr int kLongColumn = 512;   // factor columns longer than this use the wh
 constexpr int kHubFanout = 64;     // items with more dependents than this run in the prologue
 constexpr int kGroupCap = 512;     // items per dependency-closed group
 constexpr int kTopRightLooking = 64;  // tops at least this large factor right-looking
+constexpr int kGroupSmemBytes = 96 * 1024;  // largest group buffer staged in shared memory
+// Short items of the grouped sweeps run on one thread each: a warp-wide FP64
+// instruction takes the same FP64-pipe time with one active lane as with 32,
+// and GB300's FP64 pipe is narrow, so a warp spent on a 3-entry column wastes
+// most of it.
+constexpr int kThreadColumn = 32;  // factor columns with at most this many entries ...
+constexpr int kThreadWork = 96;    // ... and at most this many update products
+constexpr int kThreadRow = 16;     // solve rows with at most this many entries
 
 // LU structures (device) produced by the host analysis.  Plain data: it is
 // passed to kernels by value.
@@ -232,6 +242,10 @@ struct LUDev {
   // large): host copies of the L- and factor-schedule level pointers and the
   // tops' level ranges [lo, hi)
   const int *h_ls_lvl_ptr = nullptr, *h_fs_lvl_ptr = nullptr;
+  // factor groups staged in shared memory (see LUHost::grp_soff); grp_fit[0|1]
+  // = entries of the largest group within kGroupSmemBytes as double | float
+  int *grp_soff = nullptr, *grp_snz = nullptr;
+  int grp_fit[2] = {0, 0};
   int ls_top_lo = 0, ls_top_hi = 0, fs_top_lo = 0, fs_top_hi = 0;
   float *lu32 = nullptr;
   double *ir_r = nullptr;
@@ -251,6 +265,10 @@ struct LUHost {
   // receiving the U entries (positions) tgrp_pos[tgrp_ptr[g] .. tgrp_ptr[g+1])
   // of pivots tgrp_k[...] of that level
   std::vector<int> tlv_items, tlv_item_ptr, tlv_grp_ptr, tgrp_col, tgrp_ptr, tgrp_pos, tgrp_k;
+  // shared-memory staging of the factor groups: column j of a group sits at
+  // grp_soff[j] .. grp_soff[j] + nnz(col j) of its group's buffer (-1: not in a
+  // group); grp_snz[g] = entries of group g
+  std::vector<int> grp_soff, grp_snz;
   std::vector<int> row_of_step, col_of_step, cp, ri, diag, src;
   std::vector<int> f_lvl_ptr, f_cols, l_lvl_ptr, l_rows, l_ptr, l_pos, l_col;
   std::vector<int> u_lvl_ptr, u_rows, u_ptr, u_pos, u_col;
@@ -293,6 +311,7 @@ void launch_count_done_k(cudaStream_t st, const DevArrays &d, int ncirc, const i
                          int *status_out);
 void launch_unstall_k(cudaStream_t st, const DevArrays &d, int ncirc);
 void launch_set_target_k(cudaStream_t st, const DevArrays &d, int ncirc, int n_steps);
+int lu_prepare_k();  // shared-memory opt-in of the staged group factorization
 void launch_lu_factor_k(cudaStream_t st, const LUDev &L, const double *vals, CircState *cs, int masked,
                         double pivot_tol);
 void launch_lu_solve_k(cudaStream_t st, const LUDev &L, const double *b, double *x, const CircState *cs,

@@ -58,6 +58,49 @@ __device__ __forceinline__ double team_max(double v, double *sm) {
   return r;
 }
 
+// Zero tests and magnitude maxima of the factorization run on the integer
+// pipe: GB300's FP64 pipe is narrow and a warp-wide FP64 instruction costs
+// the same with one active lane as with 32.
+__device__ __forceinline__ bool nz(double v) { return (__double_as_longlong(v) << 1) != 0; }
+__device__ __forceinline__ bool nz(float v) { return (__float_as_uint(v) << 1) != 0u; }
+// |v| as an integer key ordered like |v|; NaN maps to 0 (ignored, as by fmax)
+__device__ __forceinline__ unsigned long long mag_key(double v) {
+  const unsigned long long a = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
+  return a > 0x7ff0000000000000ULL ? 0ULL : a;
+}
+__device__ __forceinline__ unsigned long long mag_key(float v) {
+  const unsigned a = __float_as_uint(v) & 0x7fffffffu;
+  return a > 0x7f800000u ? 0ULL : (unsigned long long)a;
+}
+template <typename T> __device__ __forceinline__ double key_value(unsigned long long k);
+template <> __device__ __forceinline__ double key_value<double>(unsigned long long k) {
+  return __longlong_as_double((long long)k);
+}
+template <> __device__ __forceinline__ double key_value<float>(unsigned long long k) {
+  return (double)__uint_as_float((unsigned)k);
+}
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) {
+  return a > b ? a : b;
+}
+// max of keys over the team (warp or whole CTA); every thread gets the result
+template <bool BLOCK>
+__device__ __forceinline__ unsigned long long team_max_key(unsigned long long v, double *sm) {
+  for (int o = 16; o > 0; o >>= 1) v = umax64(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if (!BLOCK) return v;
+  unsigned long long *su = reinterpret_cast<unsigned long long *>(sm);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) su[threadIdx.x >> 5] = v;
+  __syncthreads();
+  unsigned long long r = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = umax64(r, su[w]);
+  return r;
+}
+template <bool BLOCK>
+__device__ __forceinline__ bool team_any(bool v) {
+  if (BLOCK) return __syncthreads_or(v) != 0;
+  return __any_sync(0xffffffffu, v) != 0;
+}
+
 template <bool BLOCK>
 __device__ __forceinline__ double team_sum(double v, double *sm) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -75,6 +118,23 @@ template <typename T> __device__ __forceinline__ T *lu_of(const LUDev &L);
 template <> __device__ __forceinline__ double *lu_of<double>(const LUDev &L) { return L.lu; }
 template <> __device__ __forceinline__ float *lu_of<float>(const LUDev &L) { return L.lu32; }
 
+// Pivot test and scaling of column j once its updates are in: d = U(j,j),
+// amax = the largest |L(:,j)| entry (as a key), lost = an update that missed
+// the pattern.  Returns false on breakdown (flag raised by `leader`).
+__device__ __forceinline__ bool pivot_ok(const LUDev &L, int j, CircState *cs, int masked, double pivot_tol,
+                                         double d, double amax, bool lost, bool leader) {
+  // The threshold only matters when row j of U has entries right of the
+  // diagonal: otherwise the multipliers never reach the Schur complement
+  // (e.g. the branch row of a grounded voltage source).
+  const bool urow = L.u_ptr[j + 1] > L.u_ptr[j] && !L.exempt[j];
+  const bool bad = lost || (urow && !(fabs(d) >= pivot_tol * amax)) || !(fabs(d) > 0.0) || isinf(d);
+  if (bad && leader) {
+    atomicCAS(L.breakdown, 0, j + 1);
+    if (masked) cs[L.circ_of_step[j]].singular = 1;
+  }
+  return !bad;
+}
+
 template <bool BLOCK, typename T>
 __device__ void factor_column(const LUDev &L, const double *__restrict__ vals, int j, CircState *cs,
                               int masked, double pivot_tol, double *sm) {
@@ -87,41 +147,64 @@ __device__ void factor_column(const LUDev &L, const double *__restrict__ vals, i
     lu[p] = (s >= 0) ? (T)vals[s] : (T)0;
   }
   team_sync<BLOCK>();
-  double lost = 0.0;
+  bool lost = false;
   for (int p = p0; p < pd; ++p) {
     const int k = L.ri[p];
     const T ukj = lu[p];
-    if (ukj != (T)0) {
+    if (nz(ukj)) {
       // positions of L(:,k)'s rows in column j come from the analysis
       const int q0 = L.diag[k] + 1, q1 = L.cp[k + 1];
       const int *tgt = L.upd_pos + L.upd_off[p];
       for (int q = q0 + lane; q < q1; q += nl) {
         const int pos = tgt[q - q0];
         if (pos > p && pos < p1) lu[pos] -= lu[q] * ukj;
-        else lost = 1.0;
+        else lost = true;
       }
     }
     team_sync<BLOCK>();
   }
-  const double d = (double)lu[pd];
-  double amax = 0.0;
-  for (int p = pd + lane; p < p1; p += nl) amax = fmax(amax, fabs((double)lu[p]));
-  amax = team_max<BLOCK>(amax, sm);
-  lost = team_max<BLOCK>(lost, sm);
-  // The threshold only matters when row j of U has entries right of the
-  // diagonal: otherwise the multipliers never reach the Schur complement
-  // (e.g. the branch row of a grounded voltage source).
-  const bool urow = L.u_ptr[j + 1] > L.u_ptr[j] && !L.exempt[j];
-  const bool bad = lost != 0.0 || (urow && !(fabs(d) >= pivot_tol * amax)) || !(fabs(d) > 0.0) || isinf(d);
-  if (bad) {
-    if (lane == 0) {
-      atomicCAS(L.breakdown, 0, j + 1);
-      if (masked) cs[L.circ_of_step[j]].singular = 1;
-    }
-    return;
-  }
+  unsigned long long ak = 0;
+  for (int p = pd + lane; p < p1; p += nl) ak = umax64(ak, mag_key(lu[p]));
+  ak = team_max_key<BLOCK>(ak, sm);
+  lost = team_any<BLOCK>(lost);
+  if (!pivot_ok(L, j, cs, masked, pivot_tol, (double)lu[pd], key_value<T>(ak), lost, lane == 0)) return;
   const T inv = (T)1 / lu[pd];
   for (int p = pd + 1 + lane; p < p1; p += nl) lu[p] *= inv;
+}
+
+// A short column on one thread.  S: the group's shared-memory buffer (column
+// k at S[grp_soff[k]]), or nullptr to factor in place in global memory.
+template <typename T>
+__device__ void factor_column_t(const LUDev &L, const double *__restrict__ vals, int j, CircState *cs,
+                                int masked, double pivot_tol, T *S) {
+  const int p0 = L.cp[j], p1 = L.cp[j + 1], pd = L.diag[j];
+  T *glu = lu_of<T>(L);
+  T *cj = S ? S + L.grp_soff[j] : glu + p0;  // cj[p - p0]
+  if (!S)
+    for (int p = p0; p < p1; ++p) {
+      const int s = L.src[p];
+      cj[p - p0] = (s >= 0) ? (T)vals[s] : (T)0;
+    }
+  bool lost = false;
+  for (int p = p0; p < pd; ++p) {
+    const T ukj = cj[p - p0];
+    if (!nz(ukj)) continue;
+    const int k = L.ri[p];
+    const int q0 = L.diag[k] + 1, q1 = L.cp[k + 1];
+    const int sk = S ? L.grp_soff[k] : -1;
+    const int *tgt = L.upd_pos + L.upd_off[p];
+    for (int q = q0; q < q1; ++q) {
+      const int pos = tgt[q - q0];
+      const T lqk = (sk >= 0) ? S[sk + (q - L.cp[k])] : glu[q];
+      if (pos > p && pos < p1) cj[pos - p0] -= lqk * ukj;
+      else lost = true;
+    }
+  }
+  unsigned long long ak = 0;
+  for (int p = pd; p < p1; ++p) ak = umax64(ak, mag_key(cj[p - p0]));
+  if (!pivot_ok(L, j, cs, masked, pivot_tol, (double)cj[pd - p0], key_value<T>(ak), lost, true)) return;
+  const T inv = (T)1 / cj[pd - p0];
+  for (int p = pd + 1; p < p1; ++p) cj[p - p0] *= inv;
 }
 
 // y[i] = b[row_of_step[i]] - sum_k L(i,k) y[k]          (LOWER)
@@ -167,18 +250,22 @@ __global__ void __launch_bounds__(256) k_factor_hubs(LUDev L, const double *__re
 }
 
 template <typename T>
-__global__ void __launch_bounds__(1024) k_factor_groups(LUDev L, const double *__restrict__ vals, CircState *cs,
-                                                        int masked, double pivot_tol, int top) {
-  __shared__ double sm[32];
+__device__ void factor_group(const LUDev &L, const double *__restrict__ vals, CircState *cs, int masked,
+                             double pivot_tol, double *sm, int g) {
   const SchedDev &S = L.fs;
-  const int g = top ? S.n_groups : (int)blockIdx.x;
   const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   for (int lv = S.grp_lvl[g]; lv < S.grp_lvl[g + 1]; ++lv) {
     const int b = S.lvl_ptr[lv], e = S.lvl_ptr[lv + 1];
     bool any_long = false;
+    for (int t = b + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
+      const int j = S.items[t];
+      if (S.is_thread[j] && item_active(L, cs, masked, j))
+        factor_column_t<T>(L, vals, j, cs, masked, pivot_tol, nullptr);
+    }
     for (int t = b + warp; t < e; t += nwarps) {
       const int j = S.items[t];
       if (S.is_long[j]) { any_long = true; continue; }
+      if (S.is_thread[j]) continue;
       if (item_active(L, cs, masked, j)) factor_column<false, T>(L, vals, j, cs, masked, pivot_tol, sm);
     }
     if (__syncthreads_or(any_long)) {
@@ -190,6 +277,13 @@ __global__ void __launch_bounds__(1024) k_factor_groups(LUDev L, const double *_
       }
     }
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_factor_groups(LUDev L, const double *__restrict__ vals, CircState *cs,
+                                                        int masked, double pivot_tol, int top) {
+  __shared__ double sm[32];
+  factor_group<T>(L, vals, cs, masked, pivot_tol, sm, top ? L.fs.n_groups : (int)blockIdx.x);
 }
 
 // ---- top of the factorization: pull, then right-looking -------------------
@@ -351,6 +445,103 @@ __global__ void __launch_bounds__(256) k_toplv_update(LUDev L, int lv, CircState
   }
 }
 
+// ---- factor groups staged in shared memory --------------------------------
+// A group's columns are loaded from A once, factored left-looking in shared
+// memory (the dependent chain of each update step reads U(k, j) and scatters
+// into column j at shared-memory latency), and written back once.  L columns
+// of hubs (outside every group) are read from global memory.
+template <bool BLOCK, typename T>
+__device__ void factor_column_s(const LUDev &L, int j, CircState *cs, int masked, double pivot_tol, double *sm,
+                                T *S) {
+  const int lane = BLOCK ? (int)threadIdx.x : (int)(threadIdx.x & 31);
+  const int nl = BLOCK ? (int)blockDim.x : 32;
+  const int p0 = L.cp[j], p1 = L.cp[j + 1], pd = L.diag[j];
+  T *cj = S + L.grp_soff[j];  // cj[p - p0]
+  const T *glu = lu_of<T>(L);
+  bool lost = false;
+  for (int p = p0; p < pd; ++p) {
+    const int k = L.ri[p];
+    const T ukj = cj[p - p0];
+    if (nz(ukj)) {
+      const int q0 = L.diag[k] + 1, q1 = L.cp[k + 1];
+      const int sk = L.grp_soff[k];
+      const int *tgt = L.upd_pos + L.upd_off[p];
+      for (int q = q0 + lane; q < q1; q += nl) {
+        const int pos = tgt[q - q0];
+        const T lqk = (sk >= 0) ? S[sk + (q - L.cp[k])] : glu[q];
+        if (pos > p && pos < p1) cj[pos - p0] -= lqk * ukj;
+        else lost = true;
+      }
+    }
+    team_sync<BLOCK>();
+  }
+  unsigned long long ak = 0;
+  for (int p = pd + lane; p < p1; p += nl) ak = umax64(ak, mag_key(cj[p - p0]));
+  ak = team_max_key<BLOCK>(ak, sm);
+  lost = team_any<BLOCK>(lost);
+  if (!pivot_ok(L, j, cs, masked, pivot_tol, (double)cj[pd - p0], key_value<T>(ak), lost, lane == 0)) return;
+  const T inv = (T)1 / cj[pd - p0];
+  for (int p = pd + 1 + lane; p < p1; p += nl) cj[p - p0] *= inv;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, const double *__restrict__ vals,
+                                                                    CircState *cs, int masked, double pivot_tol,
+                                                                    int cap) {
+  extern __shared__ __align__(16) unsigned char smraw_lu[];
+  T *S = reinterpret_cast<T *>(smraw_lu);
+  __shared__ double sm[32];
+  const SchedDev &SD = L.fs;
+  const int g = blockIdx.x;
+  if (L.grp_snz[g] > cap) {  // too large for the buffer: factor in place in global memory
+    factor_group<T>(L, vals, cs, masked, pivot_tol, sm, g);
+    return;
+  }
+  const int it0 = SD.lvl_ptr[SD.grp_lvl[g]], it1 = SD.lvl_ptr[SD.grp_lvl[g + 1]];
+  if (it0 >= it1) return;
+  // a group belongs to one circuit: activity is uniform over the CTA
+  if (!item_active(L, cs, masked, SD.items[it0])) return;
+  // load the group's columns from A (warp per column)
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (int t = it0 + warp; t < it1; t += nwarps) {
+    const int j = SD.items[t], p0 = L.cp[j], p1 = L.cp[j + 1], o = L.grp_soff[j];
+    for (int p = p0 + lane; p < p1; p += 32) {
+      const int s = L.src[p];
+      S[o + (p - p0)] = (s >= 0) ? (T)vals[s] : (T)0;
+    }
+  }
+  __syncthreads();
+  for (int lv = SD.grp_lvl[g]; lv < SD.grp_lvl[g + 1]; ++lv) {
+    const int b = SD.lvl_ptr[lv], e = SD.lvl_ptr[lv + 1];
+    bool any_long = false;
+    for (int t = b + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
+      const int j = SD.items[t];
+      if (SD.is_thread[j]) factor_column_t<T>(L, vals, j, cs, masked, pivot_tol, S);
+    }
+    for (int t = b + warp; t < e; t += nwarps) {
+      const int j = SD.items[t];
+      if (SD.is_long[j]) { any_long = true; continue; }
+      if (SD.is_thread[j]) continue;
+      factor_column_s<false, T>(L, j, cs, masked, pivot_tol, sm, S);
+    }
+    if (__syncthreads_or(any_long)) {
+      for (int t = b; t < e; ++t) {
+        const int j = SD.items[t];
+        if (!SD.is_long[j]) continue;
+        factor_column_s<true, T>(L, j, cs, masked, pivot_tol, sm, S);
+        __syncthreads();
+      }
+    }
+  }
+  __syncthreads();
+  // write the factored columns back (the solves and the top read them)
+  T *lu = lu_of<T>(L);
+  for (int t = it0 + warp; t < it1; t += nwarps) {
+    const int j = SD.items[t], p0 = L.cp[j], p1 = L.cp[j + 1], o = L.grp_soff[j];
+    for (int p = p0 + lane; p < p1; p += 32) lu[p] = S[o + (p - p0)];
+  }
+}
+
 // ---- L solve (L schedule, forward) ------------------------------------------
 __global__ void k_lsolve_hubs(LUDev L, const double *__restrict__ b, const CircState *cs, int masked) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -371,7 +562,16 @@ __global__ void __launch_bounds__(1024) k_lsolve_groups(LUDev L, const double *_
   for (int lv = S.grp_lvl[g]; lv < S.grp_lvl[g + 1]; ++lv) {
     const int bb = S.lvl_ptr[lv], e = S.lvl_ptr[lv + 1];
     bool any_long = false;
-    // teams of 8 lanes stride over the level; the loop bound is warp-uniform
+    // short rows: a thread each
+    for (int t = bb + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
+      const int i = S.items[t];
+      if (!S.is_thread[i] || !item_active(L, cs, masked, i)) continue;
+      double sum = 0.0;
+      for (int q = L.l_ptr[i]; q < L.l_ptr[i + 1]; ++q) sum += (double)lu[L.l_pos[q]] * L.y[L.l_col[q]];
+      L.y[i] = b[L.row_of_step[i]] - sum;
+    }
+    // the others: teams of 8 lanes stride over the level; the loop bound is
+    // warp-uniform
     for (int t0 = bb; t0 < e; t0 += nteams) {
       const int t = t0 + team;
       bool act = false;
@@ -379,7 +579,7 @@ __global__ void __launch_bounds__(1024) k_lsolve_groups(LUDev L, const double *_
       if (t < e) {
         i = S.items[t];
         if (S.is_long[i]) any_long = true;
-        else act = item_active(L, cs, masked, i);
+        else act = !S.is_thread[i] && item_active(L, cs, masked, i);
       }
       if (__any_sync(0xffffffffu, act)) {
         double sum = 0.0;
@@ -413,6 +613,16 @@ __global__ void __launch_bounds__(1024) k_usolve_groups(LUDev L, double *__restr
   for (int lv = S.grp_lvl[g + 1] - 1; lv >= S.grp_lvl[g]; --lv) {
     const int bb = S.lvl_ptr[lv], e = S.lvl_ptr[lv + 1];
     bool any_long = false;
+    for (int t = bb + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
+      const int k = S.items[t];
+      if (!S.is_thread_rev[k] || !item_active(L, cs, masked, k)) continue;
+      double sum = 0.0;
+      for (int q = L.u_ptr[k]; q < L.u_ptr[k + 1]; ++q) sum += (double)lu[L.u_pos[q]] * L.y[L.u_col[q]];
+      const double z = (L.y[k] - sum) / (double)lu[L.diag[k]];
+      L.y[k] = z;
+      if (ACC) x[L.col_of_step[k]] += z;
+      else x[L.col_of_step[k]] = z;
+    }
     for (int t0 = bb; t0 < e; t0 += nteams) {
       const int t = t0 + team;
       bool act = false;
@@ -420,7 +630,7 @@ __global__ void __launch_bounds__(1024) k_usolve_groups(LUDev L, double *__restr
       if (t < e) {
         k = S.items[t];
         if (S.is_long_rev[k]) any_long = true;
-        else act = item_active(L, cs, masked, k);
+        else act = !S.is_thread_rev[k] && item_active(L, cs, masked, k);
       }
       if (__any_sync(0xffffffffu, act)) {
         double sum = 0.0;
@@ -562,8 +772,16 @@ template <typename T>
 static void factor_sweeps(cudaStream_t st, const LUDev &L, const double *vals, CircState *cs, int masked,
                           double pivot_tol) {
   if (L.fs.n_hub > 0) k_factor_hubs<T><<<L.fs.n_hub, 256, 0, st>>>(L, vals, cs, masked, pivot_tol);
-  if (L.fs.n_groups > 0)
-    k_factor_groups<T><<<L.fs.n_groups, kGroupThreads, 0, st>>>(L, vals, cs, masked, pivot_tol, 0);
+  if (L.fs.n_groups > 0) {
+    // groups of up to kGroupSmemBytes factor in shared memory; the buffer is
+    // sized for the largest of them, larger groups factor in global memory
+    const int fit = L.grp_fit[sizeof(T) == 4 ? 1 : 0];
+    if (L.grp_snz && fit > 0)
+      k_factor_groups_s<T><<<L.fs.n_groups, kGroupThreads, (size_t)fit * sizeof(T), st>>>(L, vals, cs, masked,
+                                                                                          pivot_tol, fit);
+    else
+      k_factor_groups<T><<<L.fs.n_groups, kGroupThreads, 0, st>>>(L, vals, cs, masked, pivot_tol, 0);
+  }
   if (L.fs.n_top_items > 0) {
     if (L.n_top_rl > 0) {
       const long long threads = (long long)L.n_top_rl * 32;
@@ -585,6 +803,15 @@ static void factor_sweeps(cudaStream_t st, const LUDev &L, const double *vals, C
 }
 
 // FP64 factors, or FP32 factors when the analysis selected the refined solve.
+int lu_prepare_k() {
+  if (cudaFuncSetAttribute(k_factor_groups_s<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kGroupSmemBytes) != cudaSuccess ||
+      cudaFuncSetAttribute(k_factor_groups_s<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kGroupSmemBytes) != cudaSuccess)
+    return XG_ERR_CUDA;
+  return XG_OK;
+}
+
 void launch_lu_factor_k(cudaStream_t st, const LUDev &L, const double *vals, CircState *cs, int masked,
                         double pivot_tol) {
   if (L.mixed) factor_sweeps<float>(st, L, vals, cs, masked, pivot_tol);

@@ -505,6 +505,38 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
   out.lsched = build_schedule(
       n, [&](int i, std::vector<int> &d) { for (int t = out.l_ptr[i]; t < out.l_ptr[i + 1]; ++t) d.push_back(out.l_col[t]); },
       [&](int i) { return (out.l_ptr[i + 1] - out.l_ptr[i]) > kLongSolveRow; }, nullptr);
+  // Single-thread items: short factor columns (entries and update products),
+  // short U rows (backward sweep of the factor schedule), short L rows.
+  out.fsched.is_thread.assign(n, 0);
+  out.fsched.is_thread_rev.assign(n, 0);
+  out.lsched.is_thread.assign(n, 0);
+  out.lsched.is_thread_rev.assign(n, 0);
+  for (int j = 0; j < n; ++j) {
+    long long work = 0;
+    for (int t = out.cp[j]; t < out.diag[j]; ++t) {
+      const int k = out.ri[t];
+      work += out.cp[k + 1] - out.diag[k] - 1;
+    }
+    if (!out.fsched.is_long[j] && out.cp[j + 1] - out.cp[j] <= kThreadColumn && work <= kThreadWork)
+      out.fsched.is_thread[j] = 1;
+    if (!out.fsched.is_long_rev[j] && out.u_ptr[j + 1] - out.u_ptr[j] <= kThreadRow) out.fsched.is_thread_rev[j] = 1;
+    if (!out.lsched.is_long[j] && out.l_ptr[j + 1] - out.l_ptr[j] <= kThreadRow) out.lsched.is_thread[j] = 1;
+  }
+  // Shared-memory buffers of the factor groups (not the hubs, not the top).
+  {
+    const Schedule &S = out.fsched;
+    out.grp_soff.assign(n, -1);
+    out.grp_snz.assign(S.n_groups, 0);
+    for (int g = 0; g < S.n_groups; ++g) {
+      int off = 0;
+      for (int q = S.lvl_ptr[S.grp_lvl[g]]; q < S.lvl_ptr[S.grp_lvl[g + 1]]; ++q) {
+        const int j = S.items[q];
+        out.grp_soff[j] = off;
+        off += out.cp[j + 1] - out.cp[j];
+      }
+      out.grp_snz[g] = off;
+    }
+  }
   // Can the factor schedule's top run right-looking?  The sub-tree (non-top)
   // rows k of a top column j are pulled first, in step order; that is exact
   // when no top column m < k updates such a row, i.e. when every non-top L
