@@ -1,0 +1,166 @@
+"""SPICE-subset reader, .prn / .mt0 writers and measures (CPU only)."""
+import os
+
+import numpy as np
+import pytest
+
+from xyce_gb300 import netlist as N
+from xyce_gb300 import spice as S
+
+REF_TESTS = "/root/reference/test/CircuitPKG"  # read only when present (this container)
+
+
+@pytest.mark.parametrize("tok,val", [
+    ("5", 5.0), ("1MEG", 1e6), ("1meg", 1e6), ("1m", 1e-3), ("1M", 1e-3), ("10pF", 10e-12),
+    ("2.5u", 2.5e-6), ("1e-3", 1e-3), ("3k", 3e3), ("1F", 1e-15), ("4n", 4e-9), ("2mil", 50.8e-6),
+    ("-0.5", -0.5), (".5", 0.5), ("1.8V", 1.8), ("1T", 1e12), ("2G", 2e9),
+])
+def test_numbers(tok, val):
+    assert S.number(tok) == pytest.approx(val, rel=1e-15)
+
+
+def test_not_a_number():
+    with pytest.raises(ValueError):
+        S.number("abc")
+
+
+RC = """RC low-pass driven by a pulse
+* comment line
+V1 in 0 PULSE(0 1 1n)   ; TR, TF, PW, PER from .TRAN
+R1 in out 1k
+C1 out 0 1n
+.TRAN 10p 5u 0 25n
+.OPTIONS TIMEINT RELTOL=1e-4 ABSTOL=1e-9
+.PRINT TRAN V(out) V(in,out) I(V1)
+.MEASURE TRAN vmax MAX V(out)
+.MEASURE TRAN vavg AVG V(out) FROM=1u TO=4u
+.END
+"""
+
+
+def test_rc_deck():
+    d = S.parse(RC)
+    nl = d.netlist
+    assert d.title == "RC low-pass driven by a pulse"
+    a = nl.arrays()
+    assert nl.n == 3  # in, out, V1 branch
+    np.testing.assert_array_equal(a["res"][2], [1e3])
+    np.testing.assert_array_equal(a["cap"][2], [1e-9])
+    kinds, offs, data = a["vsrc"][3], a["vsrc"][4], a["vsrc"][5]
+    assert kinds[0] == N.WAVE_PULSE
+    # PULSE(V1 V2 TD) + TR = TF = TSTEP, PW = PER = TSTOP
+    np.testing.assert_array_equal(data[offs[0]:offs[1]], [0, 1, 1e-9, 10e-12, 10e-12, 5e-6, 5e-6])
+    assert nl.tran.tstop == 5e-6 and nl.tran.hmax == 25e-9
+    assert nl.tran.reltol == 1e-4 and nl.tran.abstol == 1e-9
+    assert d.prints == ["V(OUT)", "V(IN,OUT)", "I(V1)"]
+    assert [(m.name, m.func, m.var, m.frm, m.to) for m in d.measures] == [
+        ("VMAX", "MAX", "V(OUT)", None, None), ("VAVG", "AVG", "V(OUT)", 1e-6, 4e-6)]
+    assert d.branches["V1"] == nl.names["V1#branch"]
+
+
+def test_sin_defaults_and_continuation():
+    d = S.parse("t\nV1 a 0 SIN(0.5 2\n+ )\nR1 a 0 1\n.TRAN 1n 2u\n.END\n")
+    a = d.netlist.arrays()
+    offs, data = a["vsrc"][4], a["vsrc"][5]
+    # FREQ = 1/TSTOP, TD = THETA = PHASE = 0
+    np.testing.assert_array_equal(data[offs[0]:offs[1]], [0.5, 2.0, 1 / 2e-6, 0, 0, 0])
+
+
+INV_RING = """three-stage ring from an inverter subcircuit
+.SUBCKT INV in out vdd
+MN out in 0 0 nch W=2u L=0.18u
+MP out in vdd vdd pch W=4u L=0.18u
+C1 out 0 5f
+.ENDS
+.MODEL nch NMOS (VTO=0.5 KP=120u)
+.MODEL pch PMOS (LEVEL=1 VTO=-0.5 KP=40u)
+VDD vdd 0 1.8
+X1 n1 n2 vdd INV
+X2 n2 n3 vdd INV
+X3 n3 n1 vdd INV
+I1 0 n1 PWL(0 0 10p 100u 990p 100u 1n 0)
+.TRAN 1p 2n 0 5p
+.PRINT TRAN V(n1)
+.END
+"""
+
+
+def test_subcircuit_flattening():
+    d = S.parse(INV_RING)
+    nl = d.netlist
+    assert len(nl.mos1) == 6 and len(nl.cap) == 3
+    assert {"N1", "N2", "N3", "VDD"} <= set(nl.names)
+    rows = np.array([m[4] for m in nl.mos1])
+    t = N.MOS1_FIELDS.index
+    np.testing.assert_array_equal(rows[:, t("TYPE")], [1, -1] * 3)
+    np.testing.assert_array_equal(rows[:, t("KP")], [120e-6, 40e-6] * 3)
+    np.testing.assert_array_equal(rows[:, t("W")], [2e-6, 4e-6] * 3)
+    # X1's NMOS: drain n2, gate n1, source/bulk ground
+    d0, g0, s0, b0 = nl.mos1[0][:4]
+    assert (d0, g0, s0, b0) == (nl.names["N2"], nl.names["N1"], -1, -1)
+    # PMOS bulk/source on the shared supply node
+    assert nl.mos1[1][2] == nl.names["VDD"] == nl.mos1[1][3]
+
+
+@pytest.mark.parametrize("bad,msg", [
+    ("t\nL1 a 0 1n\n.TRAN 1n 1u\n.END\n", "not supported"),
+    ("t\nM1 d g 0 0 m1\n.MODEL m1 NMOS (LEVEL=3)\n.TRAN 1n 1u\n.END\n", "level 3"),
+    ("t\nM1 d g 0 0 m1\n.MODEL m1 NMOS (UO=600)\n.TRAN 1n 1u\n.END\n", "UO"),
+    ("t\nR1 a 0 1\n.END\n", ".TRAN"),
+    ("t\nR1 a 0 1\n.AC DEC 10 1 1k\n.TRAN 1n 1u\n.END\n", ".AC"),
+])
+def test_unsupported_input_raises(bad, msg):
+    with pytest.raises(ValueError, match=msg):
+        S.parse(bad)
+
+
+def test_measures():
+    t = np.array([0.0, 1.0, 2.0, 4.0])
+    v = np.array([0.0, 2.0, -1.0, 3.0])
+    assert S.measure("MAX", t, v) == 3.0
+    assert S.measure("MIN", t, v) == -1.0
+    assert S.measure("PP", t, v) == 4.0
+    integ = 0.5 * 1 * 2 + 0.5 * 1 * 1 + 0.5 * 2 * 2
+    assert S.measure("INTEG", t, v) == pytest.approx(integ)
+    assert S.measure("AVG", t, v) == pytest.approx(integ / 4)
+    rms = np.sqrt((0.5 * 1 * 4 + 0.5 * 1 * 5 + 0.5 * 2 * 10) / 4)
+    assert S.measure("RMS", t, v) == pytest.approx(rms)
+    assert S.measure("MAX", t, v, frm=0.5, to=2.5) == 2.0
+
+
+def test_prn_layout_and_round_trip(tmp_path):
+    d = S.parse(RC)
+    t = np.array([0.0, 1e-9, 2.5e-9])
+    res = S.Result(t, {"V(OUT)": np.array([0.0, 0.25, -1e-20]), "V(IN,OUT)": np.array([1.0, 0.75, 0.5]),
+                       "I(V1)": np.array([-1e-3, -7.5e-4, -5e-4])},
+                   {"VMAX": 0.25, "VAVG": float("nan")}, {})
+    p = tmp_path / "rc.cir.prn"
+    S.write_prn(str(p), d, res)
+    lines = p.read_text().splitlines()
+    # header: Index, then 17-wide centred names separated by one space
+    assert lines[0] == "Index" + " " + "      TIME       " + " " + "     V(OUT)      " + " " + \
+        "    V(IN,OUT)    " + " " + "      I(V1)      "
+    assert lines[1] == "0    " + " " + "  0.000000000e+00" + " " + "  0.000000000e+00" + " " + \
+        "  1.000000000e+00" + " " + " -1.000000000e-03"
+    assert lines[-1] == "End of Xyce(TM) Simulation"
+    names, vals = S.read_prn(str(p))
+    assert names == ["Index", "TIME", "V(OUT)", "V(IN,OUT)", "I(V1)"]
+    np.testing.assert_array_equal(vals[:, 1], t)
+    np.testing.assert_array_equal(vals[:, 2], res.columns["V(OUT)"])
+    m = tmp_path / "rc.cir.mt0"
+    S.write_mt0(str(m), d, res)
+    assert m.read_text().splitlines() == ["VMAX = 2.500000e-01", "VAVG = FAILED"]
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_TESTS), reason="reference test netlists not present")
+@pytest.mark.parametrize("fname,maker", [("TestNetlist1.cir", N.test_netlist1),
+                                         ("TestNetlist2.cir", N.test_netlist2)])
+def test_reference_test_netlists_parse_to_the_known_answer_circuits(fname, maker):
+    d = S.read(os.path.join(REF_TESTS, fname))
+    got, want = d.netlist.arrays(), maker().arrays()
+    assert d.netlist.n == maker().n
+    for k in ("res", "cap", "vsrc", "isrc"):
+        for g, w in zip(got[k], want[k]):
+            np.testing.assert_array_equal(g, w)
+    assert d.netlist.tran.tstop == 1.0
+    assert [m.name for m in d.measures][:2] == ["MAXV1", "MINV1"]

@@ -794,6 +794,9 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
     L.h_tlv_item_ptr = ctx->h_tlv_item_ptr.data();
     L.h_tlv_grp_ptr = ctx->h_tlv_grp_ptr.data();
   }
+  L.fs_threads = H.fs_threads;
+  L.ls_threads = H.ls_threads;
+  L.us_threads = H.us_threads;
   if (!H.grp_snz.empty()) {
     for (int w = 0; w < 2; ++w) {
       const int cap = kGroupSmemBytes / (w ? (int)sizeof(float) : (int)sizeof(double));

@@ -75,6 +75,7 @@ struct Mos1Model {
   double dtype, gamma, tPhi, lambda, vt, DrainSatCur, SourceSatCur, sourceVcrit, drainVcrit;
   double OxideCap, Cgso, Cgdo, Cgbo, Cbd, Cbdsw, Cbs, Cbssw, tDepCap, tBulkPot, MJ, MJSW;
   double f2d, f3d, f4d, f2s, f3s, f4s, M, gammaSqrtPhi;
+  double gsatD, gsatS;  // DrainSatCur / vt, SourceSatCur / vt (reverse-bias conductances)
   int has_gate_caps, has_junc_caps;
 };
 
@@ -205,7 +206,7 @@ constexpr int kGroupSmemBytes = 96 * 1024;  // largest group buffer staged in sh
 // most of it.
 constexpr int kThreadColumn = 32;  // factor columns with at most this many entries ...
 constexpr int kThreadWork = 96;    // ... and at most this many update products
-constexpr int kThreadRow = 16;     // solve rows with at most this many entries
+constexpr int kThreadRow = 4;      // solve rows with at most this many entries
 
 // LU structures (device) produced by the host analysis.  Plain data: it is
 // passed to kernels by value.
@@ -246,6 +247,7 @@ struct LUDev {
   // = entries of the largest group within kGroupSmemBytes as double | float
   int *grp_soff = nullptr, *grp_snz = nullptr;
   int grp_fit[2] = {0, 0};
+  int fs_threads = 512, ls_threads = 512, us_threads = 512;  // CTA sizes of the group sweeps
   int ls_top_lo = 0, ls_top_hi = 0, fs_top_lo = 0, fs_top_hi = 0;
   float *lu32 = nullptr;
   double *ir_r = nullptr;
@@ -269,6 +271,8 @@ struct LUHost {
   // grp_soff[j] .. grp_soff[j] + nnz(col j) of its group's buffer (-1: not in a
   // group); grp_snz[g] = entries of group g
   std::vector<int> grp_soff, grp_snz;
+  // CTA sizes of the group sweeps (factor, L solve, U solve)
+  int fs_threads = 512, ls_threads = 512, us_threads = 512;
   std::vector<int> row_of_step, col_of_step, cp, ri, diag, src;
   std::vector<int> f_lvl_ptr, f_cols, l_lvl_ptr, l_rows, l_ptr, l_pos, l_col;
   std::vector<int> u_lvl_ptr, u_rows, u_ptr, u_pos, u_col;

@@ -119,16 +119,20 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
   double Vd = nD >= 0 ? x[nD] : 0.0, Vg = nG >= 0 ? x[nG] : 0.0;
   double Vs = nS >= 0 ? x[nS] : 0.0, Vb = nB >= 0 ? x[nB] : 0.0;
   const double dt = m.dtype;
+  // dt is +1 or -1: products with it are sign flips, done on the integer pipe
+  // (exactly the IEEE product) — the FP64 pipe bounds this kernel on GB300
+  const long long tsgn = (dt < 0.0) ? (long long)0x8000000000000000ULL : 0LL;
+  auto T = [tsgn](double v) { return __longlong_as_double(__double_as_longlong(v) ^ tsgn); };
   const double Beta = __ldg(d.m1_beta + i), tVbi = __ldg(d.m1_vbi + i);
-  const double tVto = tVbi + dt * m.gammaSqrtPhi;
+  const double tVto = tVbi + T(m.gammaSqrtPhi);
   double *sto_n = d.sto_next + sto_base;
   const double *sto_c = d.sto_curr + sto_base;
 
-  double vbs = dt * (Vb - Vs), vgs = dt * (Vg - Vs), vds = dt * (Vd - Vs);
+  double vbs = T(Vb - Vs), vgs = T(Vg - Vs), vds = T(Vd - Vs);
   double vbd = vbs - vds, vgd = vgs - vds;
   const double vgs_o = vgs, vds_o = vds, vbs_o = vbs, vbd_o = vbd, vgd_o = vgd;
   if (initJct) {
-    vbs = -1; vgs = dt * tVto; vds = 0; vbd = vbs - vds; vgd = vgs - vds;
+    vbs = -1; vgs = T(tVto); vds = 0; vbd = vbs - vds; vgd = vgs - vds;
   }
   double vbs_old, vbd_old, vgs_old, vds_old, Von;
   if (iter == 0 && dcop) {
@@ -136,7 +140,7 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
   } else {
     const double *h = (iter == 0) ? sto_c : sto_n;
     vbd_old = h[i]; vbs_old = h[nm + i]; vgs_old = h[2 * nm + i]; vds_old = h[3 * nm + i];
-    Von = dt * h[4 * nm + i];
+    Von = T(h[4 * nm + i]);
   }
   double vgd_old = vgs_old - vds_old;
   int Check = 1;
@@ -164,7 +168,7 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
   const bool origFlag = !(vgs_o != vgs || vds_o != vds || vbs_o != vbs || vbd_o != vbd || vgd_o != vgd);
   double gbs, cbs, gbd, cbd;
   if (vbs <= 0) {
-    gbs = m.SourceSatCur / m.vt + kGmin;
+    gbs = m.gsatS + kGmin;
     cbs = gbs * vbs;
   } else {
     double e = exp(fmin(kMaxExpArg, vbs / m.vt));
@@ -172,7 +176,7 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
     cbs = m.SourceSatCur * (e - 1) + kGmin * vbs;
   }
   if (vbd <= 0) {
-    gbd = m.DrainSatCur / m.vt + kGmin;
+    gbd = m.gsatD + kGmin;
     cbd = gbd * vbd;
   } else {
     double e = exp(fmin(kMaxExpArg, vbd / m.vt));
@@ -191,7 +195,7 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
       sarg = sarg - vbx / (sarg + sarg);
       sarg = fmax(0.0, sarg);
     }
-    Von = (tVbi * dt) + m.gamma * sarg;
+    Von = T(tVbi) + m.gamma * sarg;
     double vgst = ((mode == 1) ? vgs : vgd) - Von;
     Vdsat = fmax(vgst, 0.0);
     double arg = (sarg <= 0) ? 0 : m.gamma / (sarg + sarg);
@@ -242,13 +246,13 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
   }
   double Gm, Gmbs, nrmsum, revsum, cdreq;
   if (mode >= 0) {
-    Gm = gm; Gmbs = gmbs; nrmsum = Gm + Gmbs; revsum = 0; cdreq = dt * cdrain;
+    Gm = gm; Gmbs = gmbs; nrmsum = Gm + Gmbs; revsum = 0; cdreq = T(cdrain);
   } else {
-    Gm = -gm; Gmbs = -gmbs; nrmsum = 0; revsum = -(Gm + Gmbs); cdreq = -dt * cdrain;
+    Gm = -gm; Gmbs = -gmbs; nrmsum = 0; revsum = -(Gm + Gmbs); cdreq = -T(cdrain);
   }
   // store / state (Master::updateState, N_DEV_MOSFET1.C:4241-4333)
   sto_n[i] = vbd; sto_n[nm + i] = vbs; sto_n[2 * nm + i] = vgs; sto_n[3 * nm + i] = vds;
-  sto_n[4 * nm + i] = dt * Von; sto_n[5 * nm + i] = Gm;
+  sto_n[4 * nm + i] = T(Von); sto_n[5 * nm + i] = Gm;
   sta_n[i] = capgs; sta_n[nm + i] = capgd; sta_n[2 * nm + i] = capgb;
   sta_n[3 * nm + i] = qgs; sta_n[4 * nm + i] = qgd; sta_n[5 * nm + i] = qgb;
   sta_n[6 * nm + i] = qbd; sta_n[7 * nm + i] = qbs;
@@ -257,30 +261,38 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
     atomicOr(&d.cs[c].limited, 1);
   }
   const double M = m.M;
+  const bool unitM = (M == 1.0);
   // loadDAEVectors (N_DEV_MOSFET1.C:4343-4576), old Meyer
-  const double ceqbs = dt * cbs, ceqbd = dt * cbd;
-  double *sF = d.sF + slotF, *sQ = d.sQ + slotQ;
-  sF[i] = (-(ceqbd - cdreq)) * M;                 // D
-  sF[nm + i] = (-(ceqbs + cdreq)) * M;            // S
-  sF[2 * nm + i] = (ceqbs + ceqbd) * M;           // B
-  const double Qbs = dt * qbs, Qbd = dt * qbd, Qgb = dt * qgb, Qgs = dt * qgs, Qgd = dt * qgd;
-  sQ[i] = (Qgs + Qgd + Qgb) * M;                  // G
-  sQ[nm + i] = (Qbs + Qbd - Qgb) * M;             // B
-  sQ[2 * nm + i] = -(Qbd + Qgd) * M;              // D
-  sQ[3 * nm + i] = -(Qbs + Qgs) * M;              // S
+  const double ceqbs = T(cbs), ceqbd = T(cbd);
+  const double Qbs = T(qbs), Qbd = T(qbd), Qgb = T(qgb), Qgs = T(qgs), Qgd = T(qgd);
+  double fv[3] = {-(ceqbd - cdreq), -(ceqbs + cdreq), ceqbs + ceqbd};  // D S B
+  double qv[4] = {Qgs + Qgd + Qgb, Qbs + Qbd - Qgb, -(Qbd + Qgd), -(Qbs + Qgs)};  // G B D S
   double lf[4] = {0, 0, 0, 0}, lq[4] = {0, 0, 0, 0};
   if (!origFlag) {
     double dvbd = vbd - vbd_o, dvbs = vbs - vbs_o, dvds = vds - vds_o, dvgs = vgs - vgs_o,
            dvgd = vgd - vgd_o;
     double sw = Gm * ((mode > 0) ? dvgs : dvgd) + Gmbs * ((mode > 0) ? dvbs : dvbd);
-    lf[1] = dt * ((gbd - kGmin) * dvbd + (gbs - kGmin) * dvbs) * M;
-    lf[2] = dt * (-(gbd - kGmin) * dvbd + gds * dvds + sw) * M;
-    lf[3] = dt * (-(gbs - kGmin) * dvbs - gds * dvds - sw) * M;
-    lq[0] = dt * (Capgd * dvgd + Capgs * dvgs + Capgb * (dvgs - dvbs)) * M;
-    lq[1] = dt * (-Capgb * (dvgs - dvbs) + Capgb * dvbd + capbs * dvbs) * M;
-    lq[2] = dt * (-Capgd * dvgd - capbd * dvbd) * M;
-    lq[3] = dt * (-Capgs * dvgs - capbs * dvbs) * M;
+    lf[1] = T((gbd - kGmin) * dvbd + (gbs - kGmin) * dvbs);
+    lf[2] = T(-(gbd - kGmin) * dvbd + gds * dvds + sw);
+    lf[3] = T(-(gbs - kGmin) * dvbs - gds * dvds - sw);
+    lq[0] = T(Capgd * dvgd + Capgs * dvgs + Capgb * (dvgs - dvbs));
+    lq[1] = T(-Capgb * (dvgs - dvbs) + Capgb * dvbd + capbs * dvbs);
+    lq[2] = T(-Capgd * dvgd - capbd * dvbd);
+    lq[3] = T(-Capgs * dvgs - capbs * dvbs);
   }
+  // the multiplier is applied only when it is not 1 (a branch, not a select,
+  // so that the FP64 products are skipped)
+  if (!unitM) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) fv[k] *= M;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { qv[k] *= M; lf[k] *= M; lq[k] *= M; }
+  }
+  double *sF = d.sF + slotF, *sQ = d.sQ + slotQ;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) sF[k * nm + i] = fv[k];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) sQ[k * nm + i] = qv[k];
   double *sL = d.sL + slotL;
   if (combined) {
 #pragma unroll
@@ -302,12 +314,16 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
   q[1] = -Capgd; q[3] = -capbd; q[0] = capbd + Capgd;
   q[9] = -Capgs; q[11] = -capbs; q[10] = capbs + Capgs;
   // structural zeros of the two 4x4 blocks (the gate conducts no current;
-  // no capacitance couples D-S) are stored without FP64 arithmetic, and the
-  // multiplier is applied only when it is not 1: the FP64 pipe bounds this
-  // kernel on GB300
+  // no capacitance couples D-S) are stored without FP64 arithmetic
   constexpr bool kFnz[16] = {1, 1, 1, 1, 0, 0, 0, 0, 1, 1, 1, 1, 1, 0, 1, 1};
   constexpr bool kQnz[16] = {1, 1, 0, 1, 1, 1, 1, 1, 0, 1, 1, 1, 1, 1, 1, 1};
-  const bool unitM = (M == 1.0);
+  if (!unitM) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      if (kFnz[k]) f[k] *= M;
+      if (kQnz[k]) q[k] *= M;
+    }
+  }
   double *sM = d.sM + slotM;
   if (combined) {
 #pragma unroll
@@ -317,14 +333,14 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
       else if (kFnz[k]) v = fs * f[k];
       else if (kQnz[k]) v = qs * q[k];
       else v = 0.0;
-      sM[k * nm + i] = unitM ? v : v * M;
+      sM[k * nm + i] = v;
     }
   } else {
     double *sM2 = d.sM2 + slotM;
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
-      sM[k * nm + i] = kFnz[k] ? (unitM ? f[k] : f[k] * M) : 0.0;
-      sM2[k * nm + i] = kQnz[k] ? (unitM ? q[k] : q[k] * M) : 0.0;
+      sM[k * nm + i] = kFnz[k] ? f[k] : 0.0;
+      sM2[k * nm + i] = kQnz[k] ? q[k] : 0.0;
     }
   }
 }

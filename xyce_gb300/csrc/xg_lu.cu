@@ -28,7 +28,7 @@
 
 namespace xg {
 
-constexpr int kGroupThreads = 512;  // threads of a group CTA (the top uses 1024)
+constexpr int kGroupThreads = 512;  // largest group CTA (the analysis picks 64..512)
 
 void launch_lu_solve_k(cudaStream_t st, const LUDev &L, const double *b, double *x, const CircState *cs,
                        int masked);
@@ -551,8 +551,29 @@ __global__ void k_lsolve_hubs(LUDev L, const double *__restrict__ b, const CircS
   L.y[i] = b[L.row_of_step[i]];  // hubs have no L entries
 }
 
+// Dot product of a short row (at most kThreadRow entries) on one thread:
+// all indices are loaded, then all values, then summed in entry order, so a
+// row costs two load latencies whatever its length.
 template <typename T>
-__global__ void __launch_bounds__(1024) k_lsolve_groups(LUDev L, const double *__restrict__ b,
+__device__ __forceinline__ double row_dot_t(const T *__restrict__ lu, const int *__restrict__ pos,
+                                            const int *__restrict__ col, const double *y, int q0, int n) {
+  int ps[kThreadRow], cl[kThreadRow];
+#pragma unroll
+  for (int u = 0; u < kThreadRow; ++u)
+    if (u < n) { ps[u] = pos[q0 + u]; cl[u] = col[q0 + u]; }
+  double a[kThreadRow], b[kThreadRow];
+#pragma unroll
+  for (int u = 0; u < kThreadRow; ++u)
+    if (u < n) { a[u] = (double)lu[ps[u]]; b[u] = y[cl[u]]; }
+  double sum = 0.0;
+#pragma unroll
+  for (int u = 0; u < kThreadRow; ++u)
+    if (u < n) sum += a[u] * b[u];
+  return sum;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kGroupThreads) k_lsolve_groups(LUDev L, const double *__restrict__ b,
                                                         const CircState *cs, int masked, int top) {
   __shared__ double sm[32];
   const SchedDev &S = L.ls;
@@ -566,8 +587,8 @@ __global__ void __launch_bounds__(1024) k_lsolve_groups(LUDev L, const double *_
     for (int t = bb + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
       const int i = S.items[t];
       if (!S.is_thread[i] || !item_active(L, cs, masked, i)) continue;
-      double sum = 0.0;
-      for (int q = L.l_ptr[i]; q < L.l_ptr[i + 1]; ++q) sum += (double)lu[L.l_pos[q]] * L.y[L.l_col[q]];
+      const int q0 = L.l_ptr[i];
+      const double sum = row_dot_t<T>(lu, L.l_pos, L.l_col, L.y, q0, L.l_ptr[i + 1] - q0);
       L.y[i] = b[L.row_of_step[i]] - sum;
     }
     // the others: teams of 8 lanes stride over the level; the loop bound is
@@ -603,7 +624,7 @@ __global__ void __launch_bounds__(1024) k_lsolve_groups(LUDev L, const double *_
 
 // ---- U solve (factor schedule, backward) ------------------------------------
 template <typename T, bool ACC>
-__global__ void __launch_bounds__(1024) k_usolve_groups(LUDev L, double *__restrict__ x, const CircState *cs,
+__global__ void __launch_bounds__(kGroupThreads) k_usolve_groups(LUDev L, double *__restrict__ x, const CircState *cs,
                                                         int masked, int top) {
   __shared__ double sm[32];
   const SchedDev &S = L.fs;
@@ -616,8 +637,8 @@ __global__ void __launch_bounds__(1024) k_usolve_groups(LUDev L, double *__restr
     for (int t = bb + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
       const int k = S.items[t];
       if (!S.is_thread_rev[k] || !item_active(L, cs, masked, k)) continue;
-      double sum = 0.0;
-      for (int q = L.u_ptr[k]; q < L.u_ptr[k + 1]; ++q) sum += (double)lu[L.u_pos[q]] * L.y[L.u_col[q]];
+      const int q0 = L.u_ptr[k];
+      const double sum = row_dot_t<T>(lu, L.u_pos, L.u_col, L.y, q0, L.u_ptr[k + 1] - q0);
       const double z = (L.y[k] - sum) / (double)lu[L.diag[k]];
       L.y[k] = z;
       if (ACC) x[L.col_of_step[k]] += z;
@@ -777,10 +798,10 @@ static void factor_sweeps(cudaStream_t st, const LUDev &L, const double *vals, C
     // sized for the largest of them, larger groups factor in global memory
     const int fit = L.grp_fit[sizeof(T) == 4 ? 1 : 0];
     if (L.grp_snz && fit > 0)
-      k_factor_groups_s<T><<<L.fs.n_groups, kGroupThreads, (size_t)fit * sizeof(T), st>>>(L, vals, cs, masked,
+      k_factor_groups_s<T><<<L.fs.n_groups, L.fs_threads, (size_t)fit * sizeof(T), st>>>(L, vals, cs, masked,
                                                                                           pivot_tol, fit);
     else
-      k_factor_groups<T><<<L.fs.n_groups, kGroupThreads, 0, st>>>(L, vals, cs, masked, pivot_tol, 0);
+      k_factor_groups<T><<<L.fs.n_groups, L.fs_threads, 0, st>>>(L, vals, cs, masked, pivot_tol, 0);
   }
   if (L.fs.n_top_items > 0) {
     if (L.n_top_rl > 0) {
@@ -823,7 +844,7 @@ template <typename T, bool ACC>
 static void solve_sweeps(cudaStream_t st, const LUDev &L, const double *b, double *x, const CircState *cs,
                          int masked) {
   if (L.ls.n_hub > 0) k_lsolve_hubs<<<(L.ls.n_hub + 255) / 256, 256, 0, st>>>(L, b, cs, masked);
-  if (L.ls.n_groups > 0) k_lsolve_groups<T><<<L.ls.n_groups, kGroupThreads, 0, st>>>(L, b, cs, masked, 0);
+  if (L.ls.n_groups > 0) k_lsolve_groups<T><<<L.ls.n_groups, L.ls_threads, 0, st>>>(L, b, cs, masked, 0);
   if (L.ls.n_top_items > 0) {
     if (L.h_ls_lvl_ptr) {
       for (int lv = L.ls_top_lo; lv < L.ls_top_hi; ++lv) {
@@ -831,7 +852,7 @@ static void solve_sweeps(cudaStream_t st, const LUDev &L, const double *b, doubl
         if (nr > 0) k_lsolve_level<T><<<(nr + 7) / 8, 256, 0, st>>>(L, lv, b, cs, masked);
       }
     } else {
-      k_lsolve_groups<T><<<1, 1024, 0, st>>>(L, b, cs, masked, 1);
+      k_lsolve_groups<T><<<1, kGroupThreads, 0, st>>>(L, b, cs, masked, 1);
     }
   }
   if (L.fs.n_top_items > 0) {
@@ -841,10 +862,11 @@ static void solve_sweeps(cudaStream_t st, const LUDev &L, const double *b, doubl
         if (nr > 0) k_usolve_level<T, ACC><<<(nr + 7) / 8, 256, 0, st>>>(L, lv, x, cs, masked);
       }
     } else {
-      k_usolve_groups<T, ACC><<<1, 1024, 0, st>>>(L, x, cs, masked, 1);
+      k_usolve_groups<T, ACC><<<1, kGroupThreads, 0, st>>>(L, x, cs, masked, 1);
     }
   }
-  if (L.fs.n_groups > 0) k_usolve_groups<T, ACC><<<L.fs.n_groups, kGroupThreads, 0, st>>>(L, x, cs, masked, 0);
+  if (L.fs.n_groups > 0)
+    k_usolve_groups<T, ACC><<<L.fs.n_groups, L.us_threads, 0, st>>>(L, x, cs, masked, 0);
   if (L.fs.n_hub > 0) k_usolve_hubs<T, ACC><<<L.fs.n_hub, 256, 0, st>>>(L, x, cs, masked);
 }
 

@@ -153,6 +153,8 @@ Mos1Instance mos1_instance(const double *p) {
   m.gammaSqrtPhi = gamma * std::sqrt(tPhi);
   m.lambda = p[XG_MOS1_LAMBDA];
   m.vt = vt;
+  m.gsatD = m.DrainSatCur / vt;
+  m.gsatS = m.SourceSatCur / vt;
   m.OxideCap = oxideCapFactor * Leff * W;
   m.Cgso = p[XG_MOS1_CGSO] * W;
   m.Cgdo = p[XG_MOS1_CGDO] * W;

@@ -522,6 +522,29 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
     if (!out.fsched.is_long_rev[j] && out.u_ptr[j + 1] - out.u_ptr[j] <= kThreadRow) out.fsched.is_thread_rev[j] = 1;
     if (!out.lsched.is_long[j] && out.l_ptr[j + 1] - out.l_ptr[j] <= kThreadRow) out.lsched.is_thread[j] = 1;
   }
+  // CTA size of each group sweep.  The groups are latency-bound chains of
+  // levels; a smaller CTA lets more groups share an SM.  Level l of group g
+  // needs need(l) threads (a thread per single-thread item, `team` per other
+  // item); a CTA of B threads walks it in ceil(need / B) passes and 2048 / B
+  // CTAs fit on an SM, so B minimizes sum_g sum_l ceil(need / B) * B.
+  auto cta_size = [&](const Schedule &S, const std::vector<char> &thr, int team) {
+    long long best_cost = -1;
+    int best = 512;
+    for (int B = 64; B <= 512; B *= 2) {
+      long long cost = 0;
+      for (int g = 0; g < S.n_groups; ++g)
+        for (int lv = S.grp_lvl[g]; lv < S.grp_lvl[g + 1]; ++lv) {
+          long long need = 0;
+          for (int t = S.lvl_ptr[lv]; t < S.lvl_ptr[lv + 1]; ++t) need += thr[S.items[t]] ? 1 : team;
+          cost += (need + B - 1) / B * B;
+        }
+      if (best_cost < 0 || cost < best_cost) { best_cost = cost; best = B; }
+    }
+    return best;
+  };
+  out.fs_threads = cta_size(out.fsched, out.fsched.is_thread, 32);
+  out.ls_threads = cta_size(out.lsched, out.lsched.is_thread, 8);
+  out.us_threads = cta_size(out.fsched, out.fsched.is_thread_rev, 8);
   // Shared-memory buffers of the factor groups (not the hubs, not the top).
   {
     const Schedule &S = out.fsched;

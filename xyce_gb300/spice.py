@@ -1,0 +1,664 @@
+"""SPICE-subset netlist reader and ``.prn`` / ``.mt0`` writers for the GPU
+transient path.
+
+Lets a netlist written for the reference drive the device-resident
+transient (``Circuit.transient``) and produce the reference's tabular
+output.  The subset is what the path simulates:
+
+* elements ``R``, ``C``, ``V`` and ``I`` (DC, ``SIN``, ``PULSE``, ``PWL``),
+  ``D`` (diode level 1), ``M`` (MOSFET level 1; level 54/14 = BSIM4 4.8.2),
+  ``X`` (subcircuit instances, flattened);
+* ``.MODEL``, ``.SUBCKT``/``.ENDS``, ``.TRAN``, ``.OPTIONS TIMEINT``
+  (RELTOL, ABSTOL), ``.PRINT TRAN``, ``.MEASURE TRAN`` (MAX, MIN, PP, AVG,
+  RMS, INTEG with FROM/TO), ``.END``; ``*`` and ``;`` comments, ``+``
+  continuation lines, engineering suffixes (T G MEG K M MIL U N P F);
+* print variables ``V(n)``, ``V(a,b)``, ``I(Vname)``, ``TIME``, ``TEMP``
+  and ``<R|C name>:R|C`` (the element value).
+
+Anything outside the subset (another element letter, a model level, an
+unknown model parameter, an expression) raises ``ValueError`` rather than
+simulating something else.
+
+Reference behaviour restated:
+* source defaults — SIN: FREQ = 1/TSTOP, TD = THETA = PHASE = 0; PULSE:
+  TD = 0, TR = TF = TSTEP, PW = PER = TSTOP
+  (SinData/PulseData::initializeSource, src/DeviceModelPKG/Core/N_DEV_SourceData.C:342-355,1142-1157);
+* ``.prn`` table — an Index column (fixed, width 5, left-justified, header
+  "Index"), then TIME and the print variables, each scientific with 9
+  digits, width 17, right-justified under a centred header, columns
+  separated by one space, footer "End of Xyce(TM) Simulation"
+  (src/IOInterfacePKG/N_IO_OutputterLocal.C:201-250,402-423,452-470;
+  column defaults src/IOInterfacePKG/N_IO_Outputter.h:91-100,192-193;
+  footer src/IOInterfacePKG/N_IO_OutputterTimePrn.C:150-160);
+* measures — evaluated at every accepted time point inside [FROM, TO]:
+  MAX/MIN the extreme value (src/IOInterfacePKG/Output/N_IO_MeasureExtrema.C:109-165),
+  AVG the trapezoid integral over the window divided by its length
+  (src/IOInterfacePKG/Output/N_IO_MeasureAverage.C:96-130), ``.mt0`` lines
+  ``NAME = value`` in scientific with 6 digits
+  (src/IOInterfacePKG/Output/N_IO_MeasureMax.C:141-161).
+"""
+from __future__ import annotations
+
+import math
+import os
+from decimal import Decimal
+import re
+import sys
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import netlist as N
+
+# decimal exponents of the engineering suffixes (MIL = 25.4e-6 separately)
+_SUFFIX = {"t": 12, "g": 9, "meg": 6, "k": 3, "m": -3, "u": -6, "n": -9, "p": -12, "f": -15}
+_NUM = re.compile(r"^([+-]?(?:\d+\.?\d*|\.\d+)(?:[eE][+-]?\d+)?)(meg|mil|[tgkmunpf])?[a-z]*$", re.I)
+
+
+def number(tok: str) -> float:
+    """SPICE number with an optional engineering suffix and unit letters."""
+    m = _NUM.match(tok.strip())
+    if not m:
+        raise ValueError(f"not a number: {tok!r}")
+    suf = (m.group(2) or "").lower()
+    if suf == "mil":
+        return float(Decimal(m.group(1)) * Decimal("25.4e-6"))
+    # decimal arithmetic: "5u" is the double nearest 5e-6
+    return float(Decimal(m.group(1)).scaleb(_SUFFIX.get(suf, 0)))
+
+
+def _is_number(tok: str) -> bool:
+    return bool(_NUM.match(tok))
+
+
+def _tokens(line: str) -> list[str]:
+    line = re.sub(r"([(),=])", r" \1 ", line)
+    return [t for t in line.split() if t != ","]
+
+
+def _logical_lines(text: str) -> tuple[str, list[str]]:
+    raw = text.splitlines()
+    title = raw[0].strip() if raw else ""
+    out: list[str] = []
+    for ln in raw[1:]:
+        s = ln.split(";", 1)[0]
+        s = re.split(r"\s\$\s", s, maxsplit=1)[0].rstrip()
+        st = s.strip()
+        if not st or st.startswith("*"):
+            continue
+        if st.startswith("+"):
+            if not out:
+                raise ValueError("continuation line without a line to continue")
+            out[-1] += " " + st[1:]
+        else:
+            out.append(st)
+    return title, out
+
+
+def _params(toks: list[str]) -> tuple[list[str], dict[str, str]]:
+    """Split a token list into positional tokens and NAME=value pairs."""
+    pos, kv = [], {}
+    i = 0
+    while i < len(toks):
+        if i + 1 < len(toks) and toks[i + 1] == "=":
+            if i + 2 >= len(toks):
+                raise ValueError(f"missing value after {toks[i]}=")
+            kv[toks[i].upper()] = toks[i + 2]
+            i += 3
+        elif toks[i] in ("(", ")"):
+            i += 1
+        else:
+            pos.append(toks[i])
+            i += 1
+    return pos, kv
+
+
+@dataclass
+class Model:
+    name: str
+    kind: str                 # D, NMOS, PMOS
+    level: int
+    params: dict[str, float]
+
+
+@dataclass
+class Measure:
+    name: str
+    func: str
+    var: str
+    frm: float | None = None
+    to: float | None = None
+
+
+@dataclass
+class Deck:
+    """A parsed netlist: the flat :class:`Netlist` plus output requests."""
+    netlist: N.Netlist
+    title: str = ""
+    prints: list[str] = field(default_factory=list)
+    measures: list[Measure] = field(default_factory=list)
+    tstep: float = 0.0
+    element_values: dict[str, float] = field(default_factory=dict)
+    branches: dict[str, int] = field(default_factory=dict)
+
+
+_DIODE_ALIASES = {"CJ0": "CJO", "CJ": "CJO", "PB": "VJ", "MJ": "M"}
+_MOS1_MODEL = {"VTO", "KP", "GAMMA", "PHI", "LAMBDA", "RD", "RS", "CBD", "CBS", "IS", "PB", "CGSO",
+               "CGDO", "CGBO", "CJ", "MJ", "CJSW", "MJSW", "JS", "TOX", "LD", "FC"}
+_MOS1_INST = {"W", "L", "AD", "AS", "PD", "PS", "M"}
+_B4_INST = {"L", "W", "AS", "AD", "PS", "PD", "M"}
+_IGNORED_MODEL = {"LEVEL", "VERSION", "TNOM"}
+
+
+class _Builder:
+    def __init__(self, title: str):
+        self.nl = N.Netlist(label=title)
+        self.deck = Deck(netlist=self.nl, title=title)
+        self.models: dict[str, Model] = {}
+        self.subckts: dict[str, tuple[list[str], list[str]]] = {}
+        self.tran = None
+
+    # ---- nodes ----------------------------------------------------------
+    def node(self, name: str) -> int:
+        u = name.upper()
+        if u in ("0", "GND", "GND!"):
+            return -1
+        if u not in self.nl.names:
+            self.nl.node(u)
+        return self.nl.names[u]
+
+    # ---- waveforms --------------------------------------------------------
+    def _wave(self, name: str, toks: list[str]):
+        """(kind, data) of a V/I source specification; the defaults that
+        depend on .TRAN are filled in later (kind, data, given flags)."""
+        pos, _ = _params(toks)
+        up = [t.upper() for t in pos]
+        dc = None
+        i = 0
+        tran = None
+        while i < len(up):
+            t = up[i]
+            if t == "DC":
+                dc = number(pos[i + 1])
+                i += 2
+            elif t == "AC":  # small-signal magnitude and phase: no transient effect
+                i += 1
+                while i < len(up) and _is_number(pos[i]):
+                    i += 1
+            elif t in ("SIN", "PULSE", "PWL"):
+                j = i + 1
+                vals = []
+                while j < len(pos) and _is_number(pos[j]):
+                    vals.append(number(pos[j]))
+                    j += 1
+                tran = (t, vals)
+                i = j
+            elif _is_number(pos[i]):
+                dc = number(pos[i])
+                i += 1
+            else:
+                raise ValueError(f"{name}: unsupported source specification {pos[i]!r}")
+        if tran is None:
+            return ("DC", [dc if dc is not None else 0.0])
+        return tran
+
+    # ---- elements ---------------------------------------------------------
+    def element(self, toks: list[str], prefix: str, nodemap: dict[str, str]):
+        name = (prefix + toks[0]).upper()
+        letter = toks[0][0].upper()
+        pos, kv = _params(toks[1:])
+
+        def nd(t):
+            t = t.upper()
+            if t in nodemap:
+                return self.node(nodemap[t])
+            if t in ("0", "GND", "GND!"):
+                return -1
+            return self.node(prefix + t)
+
+        if letter in "RC":
+            if len(pos) < 3:
+                raise ValueError(f"{name}: needs two nodes and a value")
+            a, b, v = nd(pos[0]), nd(pos[1]), number(pos[2])
+            (self.nl.R if letter == "R" else self.nl.C)(a, b, v)
+            self.deck.element_values[name] = v
+        elif letter in "VI":
+            if len(pos) < 2:
+                raise ValueError(f"{name}: needs two nodes")
+            a, b = nd(pos[0]), nd(pos[1])
+            wave = self._wave(name, toks[3:])
+            self._pending_sources.append((letter, name, a, b, wave))
+        elif letter == "D":
+            if len(pos) < 3:
+                raise ValueError(f"{name}: needs two nodes and a model")
+            m = self._model(pos[2], "D")
+            p = dict(m.params)
+            area = kv.get("AREA") or (pos[3] if len(pos) > 3 else None)
+            if area is not None:
+                p["AREA"] = number(area)
+            self.nl.D(nd(pos[0]), nd(pos[1]), **p)
+        elif letter == "M":
+            if len(pos) < 5:
+                raise ValueError(f"{name}: needs four nodes and a model")
+            m = self._model(pos[4], "M")
+            d, g, s, b = (nd(t) for t in pos[:4])
+            inst = {k: number(v) for k, v in kv.items()}
+            if m.level == 1:
+                bad = set(inst) - _MOS1_INST
+                if bad:
+                    raise ValueError(f"{name}: unsupported MOSFET instance parameter(s) {sorted(bad)}")
+                p = dict(m.params)
+                p.update(inst)
+                p["TYPE"] = 1.0 if m.kind == "NMOS" else -1.0
+                self.nl.M1(d, g, s, b, **p)
+            else:
+                bad = set(inst) - _B4_INST
+                if bad:
+                    raise ValueError(f"{name}: unsupported BSIM4 instance parameter(s) {sorted(bad)}")
+                p = dict(m.params)
+                p.update(inst)
+                p["TYPE"] = 1.0 if m.kind == "NMOS" else -1.0
+                self.nl.M4(d, g, s, b, **p)
+        elif letter == "X":
+            if not pos:
+                raise ValueError(f"{name}: needs a subcircuit name")
+            sub = pos[-1].upper()
+            if sub not in self.subckts:
+                raise ValueError(f"{name}: unknown subcircuit {pos[-1]}")
+            pins, body = self.subckts[sub]
+            conns = pos[:-1]
+            if len(conns) != len(pins):
+                raise ValueError(f"{name}: {len(conns)} nodes for {len(pins)} pins of {sub}")
+            inner = prefix + toks[0].upper() + ":"
+            mapping = {}
+            for pin, c in zip(pins, conns):
+                cu = c.upper()
+                mapping[pin] = nodemap.get(cu, cu if cu in ("0", "GND", "GND!") else prefix + cu)
+            for ln in body:
+                self.element(_tokens(ln), inner, mapping)
+        else:
+            raise ValueError(f"{name}: element type {letter!r} is not supported")
+
+    def _model(self, mname: str, letter: str) -> Model:
+        m = self.models.get(mname.upper())
+        if m is None:
+            raise ValueError(f"unknown model {mname}")
+        if letter == "D" and m.kind != "D":
+            raise ValueError(f"model {mname} is not a diode model")
+        if letter == "M" and m.kind not in ("NMOS", "PMOS"):
+            raise ValueError(f"model {mname} is not a MOSFET model")
+        return m
+
+    def model(self, toks: list[str]):
+        pos, kv = _params(toks[1:])
+        if len(pos) < 2:
+            raise ValueError(".MODEL needs a name and a type")
+        name, kind = pos[0].upper(), pos[1].upper()
+        level = int(number(kv.get("LEVEL", "1")))
+        params = {}
+        for k, v in kv.items():
+            if k in _IGNORED_MODEL:
+                if k == "TNOM" and abs(number(v) - 27.0) > 1e-12:
+                    raise ValueError(f"model {name}: TNOM other than 27 is not supported")
+                continue
+            params[k] = number(v)
+        if kind == "D":
+            out = {}
+            for k, v in params.items():
+                k = _DIODE_ALIASES.get(k, k)
+                if k not in N.DIODE_FIELDS or k == "BVGIVEN":
+                    raise ValueError(f"model {name}: unsupported diode parameter {k}")
+                out[k] = v
+            params = out
+        elif kind in ("NMOS", "PMOS"):
+            if level == 1:
+                bad = set(params) - _MOS1_MODEL
+                if bad:
+                    raise ValueError(f"model {name}: unsupported level-1 parameter(s) {sorted(bad)}")
+            elif level in (14, 54):
+                bad = set(params) - set(N.B4_FIELDS)
+                if bad:
+                    raise ValueError(f"model {name}: unsupported BSIM4 parameter(s) {sorted(bad)}")
+            else:
+                raise ValueError(f"model {name}: MOSFET level {level} is not supported")
+        else:
+            raise ValueError(f"model {name}: type {kind} is not supported")
+        self.models[name] = Model(name, kind, level, params)
+
+    # ---- sources need .TRAN for their defaults ----------------------------
+    def finish_sources(self, tstep: float, tstop: float):
+        for letter, name, a, b, (kind, vals) in self._pending_sources:
+            if kind == "DC":
+                k, data = N.WAVE_DC, vals
+            elif kind == "SIN":
+                if len(vals) < 2:
+                    raise ValueError(f"{name}: SIN needs at least VO and VA")
+                d = list(vals) + [None] * (6 - len(vals))
+                data = [d[0], d[1], d[2] if d[2] is not None else 1.0 / tstop,
+                        d[3] or 0.0, d[4] or 0.0, d[5] or 0.0]
+                k = N.WAVE_SIN
+            elif kind == "PULSE":
+                if len(vals) < 2:
+                    raise ValueError(f"{name}: PULSE needs at least V1 and V2")
+                d = list(vals) + [None] * (7 - len(vals))
+                data = [d[0], d[1], d[2] or 0.0,
+                        d[3] if d[3] is not None else tstep, d[4] if d[4] is not None else tstep,
+                        d[5] if d[5] is not None else tstop, d[6] if d[6] is not None else tstop]
+                k = N.WAVE_PULSE
+            else:
+                if len(vals) < 2 or len(vals) % 2:
+                    raise ValueError(f"{name}: PWL needs time/value pairs")
+                k, data = N.WAVE_PWL, vals
+            if letter == "V":
+                br = self.nl.V(a, b, k, data, name=f"{name}#branch")
+                self.deck.branches[name] = br
+            else:
+                self.nl.I(a, b, k, data)
+
+
+def parse(text: str) -> Deck:
+    """Parse a netlist (the first line is the title, as in SPICE)."""
+    title, lines = _logical_lines(text)
+    B = _Builder(title)
+    B._pending_sources = []
+    # pass 1: subcircuit bodies and models
+    body_lines = []
+    cur = None
+    for ln in lines:
+        toks = _tokens(ln)
+        head = toks[0].upper()
+        if head == ".SUBCKT":
+            if cur is not None:
+                raise ValueError("nested .SUBCKT definitions are not supported")
+            pos, kv = _params(toks[1:])
+            if kv:
+                raise ValueError(".SUBCKT parameters are not supported")
+            cur = (pos[0].upper(), [p.upper() for p in pos[1:]], [])
+        elif head == ".ENDS":
+            if cur is None:
+                raise ValueError(".ENDS without .SUBCKT")
+            B.subckts[cur[0]] = (cur[1], cur[2])
+            cur = None
+        elif cur is not None:
+            if head == ".MODEL":
+                B.model(toks)
+            elif head.startswith("."):
+                raise ValueError(f"{head} inside a subcircuit is not supported")
+            else:
+                cur[2].append(ln)
+        elif head == ".MODEL":
+            B.model(toks)
+        else:
+            body_lines.append((ln, toks))
+    if cur is not None:
+        raise ValueError(".SUBCKT without .ENDS")
+    tran = None
+    tstep = 0.0
+    reltol = abstol = None
+    deck = B.deck
+    for ln, toks in body_lines:
+        head = toks[0].upper()
+        if head == ".END":
+            break
+        if head == ".TRAN":
+            pos, kv = _params(toks[1:])
+            nums = [number(p) for p in pos if _is_number(p)]
+            if len(nums) < 2:
+                raise ValueError(".TRAN needs TSTEP and TSTOP")
+            tstep, tstop = nums[0], nums[1]
+            tstart = nums[2] if len(nums) > 2 else 0.0
+            hmax = nums[3] if len(nums) > 3 else 0.0
+            tran = N.Tran(tstop=tstop, tstart=tstart, hmax=hmax)
+        elif head == ".OPTIONS":
+            pos, kv = _params(toks[1:])
+            pkg = pos[0].upper() if pos else ""
+            if pkg == "TIMEINT":
+                for k, v in kv.items():
+                    if k == "RELTOL":
+                        reltol = number(v)
+                    elif k == "ABSTOL":
+                        abstol = number(v)
+                    else:
+                        raise ValueError(f".OPTIONS TIMEINT {k} is not supported")
+            else:
+                raise ValueError(f".OPTIONS {pkg} is not supported")
+        elif head == ".PRINT":
+            if len(toks) < 2 or toks[1].upper() != "TRAN":
+                raise ValueError("only .PRINT TRAN is supported")
+            deck.prints.extend(_print_vars(toks[2:]))
+        elif head in (".MEASURE", ".MEAS"):
+            deck.measures.append(_measure(toks[1:]))
+        elif head.startswith("."):
+            raise ValueError(f"{head} is not supported")
+        else:
+            B.element(toks, "", {})
+    if tran is None:
+        raise ValueError("no .TRAN line")
+    if reltol is not None:
+        tran.reltol = reltol
+    if abstol is not None:
+        tran.abstol = abstol
+    B.finish_sources(tstep, tran.tstop)
+    B.nl.tran = tran
+    B.nl.end_circuit()
+    deck.tstep = tstep
+    return deck
+
+
+def read(path: str) -> Deck:
+    with open(path) as f:
+        return parse(f.read())
+
+
+def _print_vars(toks: list[str]) -> list[str]:
+    """Re-join V(a,b) / I(x) tokens into column names."""
+    out = []
+    i = 0
+    while i < len(toks):
+        t = toks[i]
+        if i + 1 < len(toks) and toks[i + 1] == "(":
+            j = toks.index(")", i)
+            args = [a for a in toks[i + 2:j]]
+            out.append(f"{t.upper()}({','.join(a.upper() for a in args)})")
+            i = j + 1
+        else:
+            out.append(t.upper())
+            i += 1
+    return out
+
+
+def _measure(toks: list[str]) -> Measure:
+    pos, kv = _params(toks)
+    if len(pos) < 3 or pos[0].upper() != "TRAN":
+        raise ValueError(".MEASURE TRAN <name> <func> <var> is the supported form")
+    name, func = pos[1].upper(), pos[2].upper()
+    if func not in ("MAX", "MIN", "PP", "AVG", "RMS", "INTEG"):
+        raise ValueError(f".MEASURE {func} is not supported")
+    var = _print_vars(toks[toks.index(pos[2]) + 1:])
+    if not var:
+        raise ValueError(f".MEASURE {name}: no variable")
+    frm = number(kv["FROM"]) if "FROM" in kv else None
+    to = number(kv["TO"]) if "TO" in kv else None
+    return Measure(name, func, var[0], frm, to)
+
+
+# ---------------------------------------------------------------------------
+# evaluation of print variables on the probe waveforms
+
+def _var_probes(deck: Deck, var: str) -> tuple[list[int], callable]:
+    """Unknowns a variable needs and how to combine them (probe values ->
+    column).  Ground reads as 0."""
+    names = deck.netlist.names
+    m = re.match(r"^V\(([^,()]+)(?:,([^,()]+))?\)$", var)
+    if m:
+        def idx(nm):
+            if nm in ("0", "GND", "GND!"):
+                return None
+            if nm not in names:
+                raise ValueError(f"{var}: unknown node {nm}")
+            return names[nm]
+        a, b = idx(m.group(1)), idx(m.group(2)) if m.group(2) else None
+        us = [u for u in (a, b) if u is not None]
+
+        def f(vals, a=a, b=b):
+            va = vals[a] if a is not None else 0.0
+            vb = vals[b] if b is not None else 0.0
+            return va - vb
+        return us, f
+    m = re.match(r"^I\(([^,()]+)\)$", var)
+    if m:
+        src = m.group(1)
+        if src not in deck.branches:
+            raise ValueError(f"{var}: only voltage-source currents are supported")
+        br = deck.branches[src]
+        return [br], lambda vals, br=br: vals[br]
+    if var == "TEMP":
+        return [], lambda vals: 27.0
+    m = re.match(r"^([RC][^:]*):([RC])$", var)
+    if m and m.group(1) in deck.element_values and m.group(1)[0] == m.group(2):
+        v = deck.element_values[m.group(1)]
+        return [], lambda vals, v=v: v
+    if var == "TIME":
+        return [], None
+    raise ValueError(f"print variable {var} is not supported")
+
+
+@dataclass
+class Result:
+    times: np.ndarray
+    columns: dict[str, np.ndarray]
+    measures: dict[str, float]
+    stats: dict
+
+
+def measure(func: str, t: np.ndarray, v: np.ndarray, frm=None, to=None) -> float:
+    """One .MEASURE over the accepted points inside [frm, to]."""
+    sel = np.ones(len(t), bool)
+    if frm is not None:
+        sel &= t >= frm
+    if to is not None:
+        sel &= t <= to
+    t, v = t[sel], v[sel]
+    if len(t) == 0:
+        return float("nan")
+    if func == "MAX":
+        return float(v.max())
+    if func == "MIN":
+        return float(v.min())
+    if func == "PP":
+        return float(v.max() - v.min())
+    if len(t) < 2:
+        return float("nan")
+    dt = np.diff(t)
+    if func == "INTEG":
+        return float(np.sum(0.5 * dt * (v[1:] + v[:-1])))
+    if func == "AVG":
+        return float(np.sum(0.5 * dt * (v[1:] + v[:-1])) / (t[-1] - t[0]))
+    # RMS: square root of the trapezoid integral of v^2 over the window
+    return float(math.sqrt(np.sum(0.5 * dt * (v[1:] ** 2 + v[:-1] ** 2)) / (t[-1] - t[0])))
+
+
+def run(deck: Deck, device: int = 0, cap: int | None = None) -> Result:
+    """Transient of the deck on the GPU; columns of every .PRINT and
+    .MEASURE variable at the accepted time points."""
+    from . import Circuit
+    nl = deck.netlist
+    wanted = list(dict.fromkeys(deck.prints + [m.var for m in deck.measures]))
+    plan = {}
+    probes: list[int] = []
+    for var in wanted:
+        us, f = _var_probes(deck, var)
+        slots = []
+        for u in us:
+            if u not in probes:
+                probes.append(u)
+            slots.append(probes.index(u))
+        plan[var] = (us, slots, f)
+    if cap is None:
+        tr = nl.tran
+        hmin_guess = tr.hmax if tr.hmax > 0 else tr.tstop / 50.0
+        cap = int(min(2_000_000, max(4096, 20 * tr.tstop / max(hmin_guess, 1e-30))))
+    for _ in range(4):
+        circ = Circuit(nl, device=device)
+        try:
+            counts, times, values, stats = circ.transient(nl.tran, probes=probes or [0], cap=cap)
+        finally:
+            circ.close()
+        n = int(counts[0])
+        if n < cap:
+            break
+        cap *= 4  # the waveform buffer filled up: run again with a larger one
+    else:
+        raise RuntimeError(f"more than {cap} accepted steps")
+    t = times[0, :n].copy()
+    vals = values[0, :n, :]
+    cols = {}
+    for var in wanted:
+        us, slots, f = plan[var]
+        if var == "TIME":
+            cols[var] = t
+            continue
+        sub = {u: vals[:, s] for u, s in zip(us, slots)}
+        col = f(sub)
+        cols[var] = np.broadcast_to(np.asarray(col, dtype=np.float64), t.shape).copy()
+    meas = {m.name: measure(m.func, t, cols[m.var], m.frm, m.to) for m in deck.measures}
+    return Result(t, cols, meas, stats)
+
+
+def write_prn(path: str, deck: Deck, res: Result) -> None:
+    """The reference's .prn table: Index, TIME, then the .PRINT columns."""
+    names = ["TIME"] + [p for p in deck.prints if p != "TIME"]
+    cols = [res.times] + [res.columns[p] for p in names[1:]]
+
+    def head(name, width=17):
+        if width <= len(name):
+            return name
+        left = (width - len(name)) // 2
+        return " " * left + name + " " * (width - left - len(name))
+    with open(path, "w") as f:
+        f.write(" ".join(["Index"] + [head(n) for n in names]) + "\n")
+        for i in range(len(res.times)):
+            row = [f"{i:<5d}"] + [f"{c[i]:>17.9e}" for c in cols]
+            f.write(" ".join(row) + "\n")
+        f.write("End of Xyce(TM) Simulation\n")
+
+
+def read_prn(path: str) -> tuple[list[str], np.ndarray]:
+    """Column names and values of a .prn table (Index column included)."""
+    with open(path) as f:
+        lines = f.read().splitlines()
+    names = lines[0].split()
+    rows = [list(map(float, ln.split())) for ln in lines[1:] if ln and not ln.startswith("End of")]
+    return names, np.array(rows).reshape(-1, len(names))
+
+
+def write_mt0(path: str, deck: Deck, res: Result) -> None:
+    with open(path, "w") as f:
+        for m in deck.measures:
+            v = res.measures[m.name]
+            f.write(f"{m.name} = FAILED\n" if not np.isfinite(v) else f"{m.name} = {v:.6e}\n")
+
+
+def main(argv=None) -> int:
+    """``python -m xyce_gb300.spice netlist.cir`` — run the transient on the
+    GPU and write ``netlist.cir.prn`` (and ``netlist.cir.mt0`` with .MEASURE)."""
+    argv = sys.argv[1:] if argv is None else argv
+    if len(argv) != 1:
+        print("usage: python -m xyce_gb300.spice <netlist>", file=sys.stderr)
+        return 2
+    path = argv[0]
+    deck = read(path)
+    res = run(deck)
+    if deck.prints:
+        write_prn(path + ".prn", deck, res)
+    if deck.measures:
+        write_mt0(path + ".mt0", deck, res)
+        for m in deck.measures:
+            print(f"{m.name} = {res.measures[m.name]:.6e}")
+    print(f"{len(res.times)} accepted time points, {res.stats.get('rejected', 0)} rejected; "
+          f"output {os.path.basename(path)}.prn")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
