@@ -219,6 +219,22 @@ int xg_lu_set_precision(xg_ctx *ctx, int precision, int n_refine);
 int xg_lu_info(xg_ctx *ctx, long long *nnz_lu, int *factor_levels, int *lsolve_levels,
                int *usolve_levels);
 
+/* Schedule the current analysis chose: ordering of the core (XG_ORDER_*),
+ * how the top of the factorization runs and how the tops of the solves run
+ * (XG_TOP_*).  No reference counterpart (KLU's schedule is serial). */
+#define XG_ORDER_ND          0   /* nested dissection                        */
+#define XG_ORDER_MIN_DEGREE  1   /* approximate minimum degree               */
+#define XG_TOP_NONE          0   /* no top: groups cover the matrix          */
+#define XG_TOP_ONE_CTA       1   /* one CTA walks the top                    */
+#define XG_TOP_LEVELS        2   /* a launch (pair) per level on all SMs     */
+int xg_lu_schedule_info(xg_ctx *ctx, int *ordering, int *factor_top, int *solve_top);
+
+/* Override the automatic choices (-1 keeps a choice automatic): the ordering
+ * (XG_ORDER_*) and the factor / solve top schedules (XG_TOP_ONE_CTA or
+ * XG_TOP_LEVELS; a top below 64 columns always runs in one CTA).  Applies
+ * from the next analysis; not allowed while a transient is in progress. */
+int xg_lu_set_schedule(xg_ctx *ctx, int ordering, int factor_top, int solve_top);
+
 /* ---- Newton + time integration driver --------------------------------------
  * Transient::doRun (N_ANP_Transient.C:739-772, 1184-1410, 3262-3325): DC
  * operating point, then OneStep (backward Euler start, trapezoid) with

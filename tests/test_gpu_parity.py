@@ -156,13 +156,21 @@ def test_lu_refactor_same_pattern_new_values(xg, oracle_mod, torch_cuda):
     c.close()
 
 
+_SCHEDULES = [(-1, -1, -1)] + [(o, f, s) for o in (0, 1) for f in (1, 2) for s in (1, 2)]
+
+
+@pytest.mark.parametrize("sched", _SCHEDULES, ids=lambda v: f"order{v[0]}_ftop{v[1]}_stop{v[2]}")
 @pytest.mark.parametrize("maker", [lambda: N.power_grid(40, 50, seed=2),
-                                   lambda: N.bsim4_logic_dag(3000, 16, seed=9, tstop=1e-9)])
-def test_lu_large_top_matches_scipy(xg, oracle_mod, torch_cuda, maker):
-    """Systems whose nested-dissection top is large (a 40 x 40 grid, a BSIM4
-    logic DAG): the top is factored by the pull + right-looking kernels."""
+                                   lambda: N.bsim4_logic_dag(3000, 16, seed=9, tstop=1e-9)],
+                         ids=["grid40", "b4dag3000"])
+def test_lu_large_top_matches_scipy(xg, oracle_mod, torch_cuda, maker, sched):
+    """Systems with a large top (a 40 x 40 grid, a BSIM4 logic DAG), under
+    the automatic schedule and under every forced combination of ordering
+    (nested dissection / minimum degree), factor top (one CTA right-looking /
+    a launch pair per level) and solve tops (one CTA / a launch per level)."""
     nl = maker()
     c = xg.Circuit(nl)
+    c.lu_set_schedule(*sched)
     o = oracle_mod.Oracle(nl)
     rng = np.random.default_rng(5)
     x = rng.uniform(0.0, 1.0, o.n)
@@ -180,6 +188,11 @@ def test_lu_large_top_matches_scipy(xg, oracle_mod, torch_cuda, maker):
         torch_cuda.cuda.synchronize()
         xr = spl.spsolve(A.tocsc(), b)
         np.testing.assert_allclose(xs.cpu().numpy(), xr, rtol=1e-9, atol=1e-12 * np.max(np.abs(xr)))
+    info = c.lu_info()
+    if sched[0] >= 0:
+        assert info["ordering"] == ("min_degree" if sched[0] == 1 else "nested_dissection")
+    if sched[1] >= 0 and info["factor_top"] != "none":
+        assert info["factor_top"] == ("levels" if sched[1] == 2 else "one_cta")
     c.close()
 
 

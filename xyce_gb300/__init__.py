@@ -33,6 +33,8 @@ XG_ERR = {-1: "ARG", -2: "CUDA", -3: "STATE", -4: "UNSUPPORTED", -6: "NAN", -9: 
           -10: "TIMEOUT"}
 LOAD_ALL, LOAD_LINEAR, LOAD_NONLINEAR = 0, 1, 2
 PREC_FP64, PREC_FP32_IR = 0, 1
+ORDER_ND, ORDER_MIN_DEGREE = 0, 1
+TOP_ONE_CTA, TOP_LEVELS = 1, 2
 PRED_POLY, PRED_LEARNED = 0, 1
 MLP_NPARAM, MLP_NNORM = 4609, 12
 FLAG_DCOP, FLAG_INITJCT = 1, 2
@@ -44,7 +46,7 @@ EXPORTED = [
     "xg_add_isources", "xg_add_diodes", "xg_add_mosfet1", "xg_add_bsim4", "xg_finalize", "xg_get_sizes",
     "xg_get_pattern", "xg_update_sources", "xg_update_state", "xg_load_dae_vectors",
     "xg_load_dae_matrices", "xg_lu_analyze", "xg_lu_factor", "xg_lu_solve",
-    "xg_lu_solve_noalloc", "xg_lu_set_precision", "xg_lu_info",
+    "xg_lu_solve_noalloc", "xg_lu_set_precision", "xg_lu_info", "xg_lu_schedule_info", "xg_lu_set_schedule",
     "xg_transient", "xg_tran_start", "xg_tran_advance", "xg_tran_results", "xg_tran_end",
     "xg_tran_predictors", "xg_tran_predictor_stats", "xg_set_predictor", "xg_mlp_set", "xg_mlp_get",
     "xg_mlp_train", "xg_mlp_grad", "xg_mlp_forward",
@@ -123,6 +125,8 @@ def lib() -> C.CDLL:
     L.xg_lu_solve_noalloc.argtypes = [P, P, P]
     L.xg_lu_set_precision.argtypes = [P, I, I]
     L.xg_lu_info.argtypes = [P, C.POINTER(C.c_longlong), C.POINTER(I), C.POINTER(I), C.POINTER(I)]
+    L.xg_lu_schedule_info.argtypes = [P, C.POINTER(I), C.POINTER(I), C.POINTER(I)]
+    L.xg_lu_set_schedule.argtypes = [P, I, I, I]
     L.xg_transient.argtypes = [P, C.POINTER(TranParams), I, ip, I, ip, dp, dp, C.POINTER(TranStats)]
     L.xg_tran_start.argtypes = [P, C.POINTER(TranParams), I, ip, I]
     L.xg_tran_advance.argtypes = [P, I]
@@ -240,12 +244,22 @@ class Circuit:
         """PREC_FP64, or PREC_FP32_IR: FP32 factors + n_refine FP64 refinement steps."""
         self._check(lib().xg_lu_set_precision(self.h, int(precision), int(n_refine)))
 
+    def lu_set_schedule(self, ordering=-1, factor_top=-1, solve_top=-1):
+        """Override the analysis' choices (-1 = automatic): ORDER_ND /
+        ORDER_MIN_DEGREE, and TOP_ONE_CTA / TOP_LEVELS for the factor and
+        solve tops; applies from the next analysis."""
+        self._check(lib().xg_lu_set_schedule(self.h, int(ordering), int(factor_top), int(solve_top)))
+
     def lu_info(self):
         nnz = C.c_longlong()
         f, l, u = C.c_int(), C.c_int(), C.c_int()
         self._check(lib().xg_lu_info(self.h, C.byref(nnz), C.byref(f), C.byref(l), C.byref(u)))
+        o, ft, stp = C.c_int(), C.c_int(), C.c_int()
+        self._check(lib().xg_lu_schedule_info(self.h, C.byref(o), C.byref(ft), C.byref(stp)))
+        tops = {0: "none", 1: "one_cta", 2: "levels"}
         return dict(nnz_lu=nnz.value, factor_levels=f.value, lsolve_levels=l.value,
-                    usolve_levels=u.value)
+                    usolve_levels=u.value, ordering="min_degree" if o.value == 1 else "nested_dissection",
+                    factor_top=tops[ft.value], solve_top=tops[stp.value])
 
     # ---- analyses -------------------------------------------------------
     def dcop(self):

@@ -52,6 +52,7 @@ struct xg_ctx {
   int n_long_row_blocks = 0, n_long_ent_blocks = 0;
   DevArrays d;
   LUDev L;
+  int sched_order = -1, sched_ftop = -1, sched_stop = -1;  // xg_lu_set_schedule (-1: automatic)
   bool lu_ready = false;
   int n_analyze = 0;
   int lu_prec = XG_PREC_FP64, lu_refine = 2;  // xg_lu_set_precision
@@ -788,12 +789,15 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
                     std::make_pair(&L.tgrp_ptr, &H.tgrp_ptr), std::make_pair(&L.tgrp_pos, &H.tgrp_pos),
                     std::make_pair(&L.tgrp_k, &H.tgrp_k)})
       if ((rc = dev_upload(ctx, pr.first, *pr.second, A))) return rc;
-    ctx->h_tlv_item_ptr = H.tlv_item_ptr;
-    ctx->h_tlv_grp_ptr = H.tlv_grp_ptr;
-    L.n_top_lv = (int)H.tlv_item_ptr.size() - 1;
-    L.h_tlv_item_ptr = ctx->h_tlv_item_ptr.data();
-    L.h_tlv_grp_ptr = ctx->h_tlv_grp_ptr.data();
+    if (H.top_multi) {
+      ctx->h_tlv_item_ptr = H.tlv_item_ptr;
+      ctx->h_tlv_grp_ptr = H.tlv_grp_ptr;
+      L.n_top_lv = (int)H.tlv_item_ptr.size() - 1;
+      L.h_tlv_item_ptr = ctx->h_tlv_item_ptr.data();
+      L.h_tlv_grp_ptr = ctx->h_tlv_grp_ptr.data();
+    }
   }
+  L.ordering = H.ordering;
   L.fs_threads = H.fs_threads;
   L.ls_threads = H.ls_threads;
   L.us_threads = H.us_threads;
@@ -809,7 +813,7 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
       if ((rc = dev_upload(ctx, &L.grp_snz, H.grp_snz, A))) return rc;
     }
   }
-  if (H.fsched.n_top_items >= kTopRightLooking) {
+  if (H.solve_top_multi) {
     ctx->h_ls_lvl_ptr = H.lsched.lvl_ptr;
     ctx->h_fs_lvl_ptr = H.fsched.lvl_ptr;
     L.h_ls_lvl_ptr = ctx->h_ls_lvl_ptr.data();
@@ -835,7 +839,11 @@ static int lu_analyze_from_device(xg_ctx *ctx, const double *vals_dev) {
   CK(cudaStreamSynchronize(ctx->stream));
   LUHost H;
   std::string err;
-  int rc = lu_analyze_host(ctx->n, ctx->rp, ctx->ci, v, H, err);
+  int rc = lu_analyze_host(ctx->n, ctx->rp, ctx->ci, v, H, err, ctx->sched_order);
+  if (rc == XG_OK) {
+    if (ctx->sched_ftop >= 0) H.top_multi = (ctx->sched_ftop == XG_TOP_LEVELS);
+    if (ctx->sched_stop >= 0) H.solve_top_multi = (ctx->sched_stop == XG_TOP_LEVELS);
+  }
   if (rc) return fail(ctx, rc, "LU analysis: " + err);
   return lu_upload(ctx, H);
 }
@@ -911,6 +919,20 @@ int xg_lu_set_precision(xg_ctx *ctx, int precision, int n_refine) {
   return XG_OK;
 }
 
+int xg_lu_set_schedule(xg_ctx *ctx, int ordering, int factor_top, int solve_top) {
+  if (!ctx) return XG_ERR_ARG;
+  if (ordering < -1 || ordering > XG_ORDER_MIN_DEGREE) return fail(ctx, XG_ERR_ARG, "unknown ordering");
+  if ((factor_top != -1 && factor_top != XG_TOP_ONE_CTA && factor_top != XG_TOP_LEVELS) ||
+      (solve_top != -1 && solve_top != XG_TOP_ONE_CTA && solve_top != XG_TOP_LEVELS))
+    return fail(ctx, XG_ERR_ARG, "top schedule must be -1, XG_TOP_ONE_CTA or XG_TOP_LEVELS");
+  if (ctx->run) return fail(ctx, XG_ERR_STATE, "the schedule cannot change during a transient");
+  ctx->sched_order = ordering;
+  ctx->sched_ftop = factor_top;
+  ctx->sched_stop = solve_top;
+  ctx->lu_ready = false;  // applies from the next analysis
+  return XG_OK;
+}
+
 int xg_lu_info(xg_ctx *ctx, long long *nnz_lu, int *fl, int *ll, int *ul) {
   if (!ctx) return XG_ERR_ARG;
   if (!ctx->lu_ready) return fail(ctx, XG_ERR_STATE, "no LU analysis");
@@ -918,6 +940,18 @@ int xg_lu_info(xg_ctx *ctx, long long *nnz_lu, int *fl, int *ll, int *ul) {
   if (fl) *fl = ctx->L.f_levels;
   if (ll) *ll = ctx->L.l_levels;
   if (ul) *ul = ctx->L.u_levels;
+  return XG_OK;
+}
+
+int xg_lu_schedule_info(xg_ctx *ctx, int *ordering, int *factor_top, int *solve_top) {
+  if (!ctx) return XG_ERR_ARG;
+  if (!ctx->lu_ready) return fail(ctx, XG_ERR_STATE, "no LU analysis");
+  const LUDev &L = ctx->L;
+  if (ordering) *ordering = L.ordering;
+  if (factor_top)
+    *factor_top = L.fs.n_top_items == 0 ? XG_TOP_NONE : (L.n_top_lv > 0 ? XG_TOP_LEVELS : XG_TOP_ONE_CTA);
+  if (solve_top)
+    *solve_top = L.fs.n_top_items == 0 ? XG_TOP_NONE : (L.h_ls_lvl_ptr ? XG_TOP_LEVELS : XG_TOP_ONE_CTA);
   return XG_OK;
 }
 

@@ -199,6 +199,18 @@ constexpr int kLongColumn = 512;   // factor columns longer than this use the wh
 constexpr int kHubFanout = 64;     // items with more dependents than this run in the prologue
 constexpr int kGroupCap = 512;     // items per dependency-closed group
 constexpr int kTopRightLooking = 64;  // tops at least this large factor right-looking
+// Ordering choice: estimated time = FMAs / kOrderFmaRate + elimination-tree
+// height * kOrderLevelTime (sparse FP64 updates on GB300 run far below the
+// FP64 peak; each dependency level costs a few microseconds of latency).
+constexpr double kOrderFmaRate = 5e9;
+constexpr double kOrderLevelTime = 4e-6;
+// Top schedule choice (one CTA vs a launch per level on all SMs): FP64 FMAs
+// per second of one SM (GB300: ~0.6 TFMA/s over 152 SMs), the gap between
+// back-to-back launches of a graph, a CTA barrier with its dependent loads.
+constexpr double kSmFmaRate = 4e9;
+constexpr double kNumSms = 152;
+constexpr double kLaunchTime = 2.5e-6;
+constexpr double kBarrierTime = 1e-6;
 constexpr int kGroupSmemBytes = 96 * 1024;  // largest group buffer staged in shared memory
 // Short items of the grouped sweeps run on one thread each: a warp-wide FP64
 // instruction takes the same FP64-pipe time with one active lane as with 32,
@@ -248,6 +260,7 @@ struct LUDev {
   int *grp_soff = nullptr, *grp_snz = nullptr;
   int grp_fit[2] = {0, 0};
   int fs_threads = 512, ls_threads = 512, us_threads = 512;  // CTA sizes of the group sweeps
+  int ordering = 0;  // XG_ORDER_* of the analysis
   int ls_top_lo = 0, ls_top_hi = 0, fs_top_lo = 0, fs_top_hi = 0;
   float *lu32 = nullptr;
   double *ir_r = nullptr;
@@ -271,6 +284,13 @@ struct LUHost {
   // grp_soff[j] .. grp_soff[j] + nnz(col j) of its group's buffer (-1: not in a
   // group); grp_snz[g] = entries of group g
   std::vector<int> grp_soff, grp_snz;
+  // ordering of the core: 0 nested dissection, 1 minimum degree; the
+  // estimates it was chosen by (symmetric-factor FMAs, elimination-tree height)
+  int ordering = 0;
+  bool top_multi = false;        // factor top: a launch pair per level (else one CTA)
+  bool solve_top_multi = false;  // solve tops: a launch per level (else one CTA)
+  double order_fma[2] = {0, 0};
+  int order_height[2] = {0, 0};
   // CTA sizes of the group sweeps (factor, L solve, U solve)
   int fs_threads = 512, ls_threads = 512, us_threads = 512;
   std::vector<int> row_of_step, col_of_step, cp, ri, diag, src;
@@ -288,7 +308,7 @@ Schedule build_schedule(int n, const std::function<void(int, std::vector<int> &)
 
 // Analysis entry (xg_symbolic.cpp): CSR pattern + values -> LUHost.
 int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &ci,
-                    const std::vector<double> &vals, LUHost &out, std::string &err);
+                    const std::vector<double> &vals, LUHost &out, std::string &err, int force_ordering = -1);
 
 // Kernel launchers (xg_kernels.cu, xg_lu.cu).
 void launch_sources_k(cudaStream_t st, const DevArrays &d, int n_v, int n_src, int use_explicit, double t);

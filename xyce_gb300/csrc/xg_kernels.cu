@@ -1159,7 +1159,7 @@ void launch_state_commit_k(cudaStream_t st, const DevArrays &d, int nm, int nd, 
 }
 void launch_count_done_k(cudaStream_t st, const DevArrays &d, int ncirc, const int *breakdown,
                          int *status_out) {
-  k_count_done<<<1, 256, 0, st>>>(d, ncirc, breakdown, status_out);
+  k_count_done<<<1, 1024, 0, st>>>(d, ncirc, breakdown, status_out);
 }
 // Next advance: pause again after n_steps more accepted steps (unbounded if <= 0).
 __global__ void k_set_target(DevArrays d, int ncirc, int n_steps) {

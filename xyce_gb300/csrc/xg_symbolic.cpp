@@ -9,8 +9,10 @@
 //   2. peeling of row singletons to the front and column singletons to the
 //      back (the 1x1 blocks a block-triangular form would find: ideal
 //      voltage sources to ground and their branch currents),
-//   3. nested dissection of the remaining core (BFS level-set bisection,
-//      each connected component — e.g. each circuit of a batch — apart),
+//   3. an ordering of the remaining core: nested dissection (BFS level-set
+//      bisection, each connected component — e.g. each circuit of a batch —
+//      apart) or approximate minimum degree, whichever has the smaller
+//      estimated refactorization time (fill work and dependency depth),
 //   4. Gilbert-Peierls symbolic factorization of the permuted matrix, and
 //   5. level schedules for the left-looking factorization and for the
 //      row-oriented L and U solves.
@@ -149,9 +151,9 @@ struct ND {
   const std::vector<std::vector<int>> &adj;
   std::vector<int> part, dist;
   int next_id = 1;
-  std::vector<int> &out;
+  std::vector<int> *out;
   static constexpr int kLeaf = 8;
-  ND(const std::vector<std::vector<int>> &a, std::vector<int> &o) : adj(a), out(o) {
+  ND(const std::vector<std::vector<int>> &a, std::vector<int> &o) : adj(a), out(&o) {
     part.assign(a.size(), 0);
     dist.assign(a.size(), -1);
   }
@@ -176,7 +178,7 @@ struct ND {
 
   void run(std::vector<int> nodes, int id) {
     if ((int)nodes.size() <= kLeaf) {
-      for (int v : nodes) { out.push_back(v); part[v] = -1; }
+      for (int v : nodes) { out->push_back(v); part[v] = -1; }
       return;
     }
     std::vector<int> order, lvl;
@@ -208,7 +210,7 @@ struct ND {
     bfs(start, id, order, lvl);
     int nl = (int)lvl.size() - 1;
     if (nl < 3) {
-      for (int v : nodes) { out.push_back(v); part[v] = -1; }
+      for (int v : nodes) { out->push_back(v); part[v] = -1; }
       return;
     }
     int half = (int)order.size() / 2, m = 1;
@@ -225,14 +227,144 @@ struct ND {
     for (int v : S) part[v] = -1;
     run(A, ida);
     run(B, idb);
-    for (int v : S) out.push_back(v);
+    for (int v : S) out->push_back(v);
   }
 };
+
+// Approximate minimum degree ordering of the graph adj restricted to
+// `nodes` (the published algorithm of Amestoy, Davis & Duff, SIAM J. Matrix
+// Anal. Appl. 17(4), 1996, on the quotient graph; without supervariable
+// detection or aggressive absorption).  Appends the elimination order to out.
+// loc: scratch of adj.size() entries, all -1 on entry and on return.
+void min_degree(const std::vector<std::vector<int>> &adj, const std::vector<int> &nodes, std::vector<int> &out,
+                std::vector<int> &loc) {
+  const int m = (int)nodes.size();
+  if (m == 0) return;
+  for (int i = 0; i < m; ++i) loc[nodes[i]] = i;
+  std::vector<std::vector<int>> A(m), E(m), Le(m);  // variable adjacency, element adjacency, element lists
+  for (int i = 0; i < m; ++i)
+    for (int w : adj[nodes[i]])
+      if (loc[w] >= 0 && loc[w] != i) A[i].push_back(loc[w]);
+  for (int i = 0; i < m; ++i) loc[nodes[i]] = -1;
+  std::vector<char> elim(m, 0), dead(m, 0);
+  std::vector<int> deg(m), head(m + 1, -1), nxt(m, -1), prv(m, -1);
+  auto bucket_add = [&](int i) {
+    const int d = deg[i];
+    nxt[i] = head[d]; prv[i] = -1;
+    if (head[d] >= 0) prv[head[d]] = i;
+    head[d] = i;
+  };
+  auto bucket_del = [&](int i) {
+    if (prv[i] >= 0) nxt[prv[i]] = nxt[i]; else head[deg[i]] = nxt[i];
+    if (nxt[i] >= 0) prv[nxt[i]] = prv[i];
+  };
+  for (int i = 0; i < m; ++i) { deg[i] = (int)A[i].size(); bucket_add(i); }
+  std::vector<int> mark(m, -1), wmark(m, -1), w(m, 0), Lp;
+  int mindeg = 0;
+  for (int k = 0; k < m; ++k) {
+    while (head[mindeg] < 0) ++mindeg;
+    const int p = head[mindeg];
+    bucket_del(p);
+    elim[p] = 1;
+    out.push_back(nodes[p]);
+    // new element Lp = (A_p u union of the elements of p) \ {p}; those
+    // elements are absorbed into it
+    Lp.clear();
+    mark[p] = k;
+    for (int v : A[p])
+      if (!elim[v] && mark[v] != k) { mark[v] = k; Lp.push_back(v); }
+    for (int e : E[p]) {
+      if (dead[e]) continue;
+      for (int v : Le[e])
+        if (!elim[v] && mark[v] != k) { mark[v] = k; Lp.push_back(v); }
+      dead[e] = 1;
+      std::vector<int>().swap(Le[e]);
+    }
+    std::vector<int>().swap(A[p]);
+    std::vector<int>().swap(E[p]);
+    Le[p] = Lp;
+    const int lp = (int)Lp.size();
+    // w(e) = |Le \ Lp| for the live elements next to Lp
+    for (int i : Lp)
+      for (int e : E[i]) {
+        if (dead[e]) continue;
+        if (wmark[e] != k) { wmark[e] = k; w[e] = (int)Le[e].size(); }
+        --w[e];
+      }
+    const int remaining = m - k - 1;
+    for (int i : Lp) {
+      // prune: absorbed elements out of E_i, element p in; variables
+      // covered by Lp (and p) out of A_i
+      int ne = 0;
+      for (int e : E[i])
+        if (!dead[e]) E[i][ne++] = e;
+      E[i].resize(ne);
+      E[i].push_back(p);
+      int na = 0;
+      for (int v : A[i])
+        if (!elim[v] && mark[v] != k) A[i][na++] = v;
+      A[i].resize(na);
+      // approximate external degree
+      long long d = (long long)na + lp - 1;
+      for (int e : E[i])
+        if (e != p) d += w[e] > 0 ? w[e] : 0;
+      d = std::min<long long>(d, (long long)deg[i] + lp - 1);
+      d = std::min<long long>(d, remaining > 0 ? remaining - 1 : 0);
+      if (d < 0) d = 0;
+      bucket_del(i);
+      deg[i] = (int)d;
+      bucket_add(i);
+      if (deg[i] < mindeg) mindeg = deg[i];
+    }
+    // elements whose variables all lie in Lp are absorbed too
+    for (int i : Lp)
+      for (int e : E[i])
+        if (e != p && !dead[e] && w[e] == 0 && wmark[e] == k) {
+          dead[e] = 1;
+          std::vector<int>().swap(Le[e]);
+        }
+  }
+}
+
+// Estimated cost of factoring the symmetrized core graph in `order` (core
+// nodes only): FMA count sum_k (|col k| - 1)^2 of the symmetric factor and
+// the height of its elimination tree (the length of the dependency chain).
+struct OrderCost { double fma = 0; int height = 0; };
+// pos: scratch of adj.size() entries, all -1 on entry and on return.
+OrderCost order_cost(const std::vector<std::vector<int>> &adj, const std::vector<int> &order,
+                     std::vector<int> &pos) {
+  const int m = (int)order.size();
+  for (int k = 0; k < m; ++k) pos[order[k]] = k;
+  std::vector<int> parent(m, -1), anc(m, -1), cnt(m, 1), mark(m, -1), h(m, 0);
+  for (int k = 0; k < m; ++k)
+    for (int u : adj[order[k]]) {
+      int r = pos[u];
+      if (r < 0 || r >= k) continue;
+      while (anc[r] != -1 && anc[r] != k) { const int t = anc[r]; anc[r] = k; r = t; }
+      if (anc[r] == -1) { anc[r] = k; parent[r] = k; }
+    }
+  for (int k = 0; k < m; ++k) {
+    mark[k] = k;
+    for (int u : adj[order[k]]) {
+      int r = pos[u];
+      if (r < 0 || r >= k) continue;
+      while (r != -1 && mark[r] != k) { cnt[r]++; mark[r] = k; r = parent[r]; }
+    }
+  }
+  for (int k = 0; k < m; ++k) pos[order[k]] = -1;
+  OrderCost c;
+  for (int k = 0; k < m; ++k) {
+    c.fma += (double)(cnt[k] - 1) * (double)(cnt[k] - 1);
+    if (parent[k] >= 0) h[parent[k]] = std::max(h[parent[k]], h[k] + 1);
+    c.height = std::max(c.height, h[k] + 1);
+  }
+  return c;
+}
 
 }  // namespace
 
 int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &ci,
-                    const std::vector<double> &vals, LUHost &out, std::string &err) {
+                    const std::vector<double> &vals, LUHost &out, std::string &err, int force_ordering) {
   out = LUHost();
   out.n = n;
   Csc A = to_csc(n, rp, ci);
@@ -291,9 +423,42 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
   order.reserve(n);
   for (int j : front) order.push_back(j);
   if (!core.empty()) {
+    // Per connected component (each circuit of a batch orders exactly as it
+    // would alone): nested dissection keeps the dependency chains short
+    // (levels run in parallel), minimum degree keeps the fill low; take the
+    // one with the smaller estimated refactorization time.
     ND nd(adj, order);
     for (int j = 0; j < n; ++j) nd.part[j] = removed[j] ? -1 : 0;
-    nd.run(core, 0);
+    std::vector<int> comp_of(n, -1), scratch(n, -1), comp, ond, omd;
+    int ncomp = 0, n_md = 0;  // components, unknowns ordered by minimum degree
+    for (int s0 : core) {
+      if (comp_of[s0] >= 0) continue;
+      comp.assign(1, s0);
+      comp_of[s0] = ncomp;
+      for (size_t h = 0; h < comp.size(); ++h)
+        for (int w : adj[comp[h]])
+          if (comp_of[w] < 0) { comp_of[w] = ncomp; comp.push_back(w); }
+      std::sort(comp.begin(), comp.end());
+      const int id = nd.next_id++;
+      for (int v : comp) nd.part[v] = id;
+      ond.clear();
+      nd.out = &ond;
+      nd.run(comp, id);
+      omd.clear();
+      min_degree(adj, comp, omd, scratch);
+      const OrderCost cnd = order_cost(adj, ond, scratch), cmd = order_cost(adj, omd, scratch);
+      const double tnd = cnd.fma / kOrderFmaRate + cnd.height * kOrderLevelTime;
+      const double tmd = cmd.fma / kOrderFmaRate + cmd.height * kOrderLevelTime;
+      const bool use_md = force_ordering >= 0 ? force_ordering == 1 : tmd < tnd;
+      out.order_fma[0] += cnd.fma; out.order_fma[1] += cmd.fma;
+      out.order_height[0] = std::max(out.order_height[0], cnd.height);
+      out.order_height[1] = std::max(out.order_height[1], cmd.height);
+      if (use_md) n_md += (int)comp.size();
+      const std::vector<int> &oc = use_md ? omd : ond;
+      order.insert(order.end(), oc.begin(), oc.end());
+      ++ncomp;
+    }
+    out.ordering = (n_md * 2 > (int)core.size()) ? 1 : 0;  // the ordering of most of the core
   }
   for (auto it = back.rbegin(); it != back.rend(); ++it) order.push_back(*it);
   if ((int)order.size() != n) {
@@ -626,8 +791,43 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
           }
           out.tlv_grp_ptr.push_back((int)out.tgrp_col.size());
         }
+        // One launch pair per level on all SMs, or the whole top in one CTA
+        // (a barrier pair per column)?  Long chains of thin levels (minimum
+        // degree orderings) favour the single CTA.
+        double t_multi = 0, t_single = 0;
+        for (int l = 0; l < nlev; ++l) {
+          double work = 0;
+          for (int t = out.tlv_item_ptr[l]; t < out.tlv_item_ptr[l + 1]; ++t) {
+            const int k = out.tlv_items[t];
+            work += (double)(out.cp[k + 1] - out.diag[k] - 1) * (double)(out.u_ptr[k + 1] - out.u_ptr[k]);
+          }
+          const int items = out.tlv_item_ptr[l + 1] - out.tlv_item_ptr[l];
+          t_multi += 2 * kLaunchTime + work / (kSmFmaRate * kNumSms);
+          t_single += items * 2 * kBarrierTime + work / kSmFmaRate;
+        }
+        out.top_multi = t_multi < t_single;
       }
     }
+  }
+  // The same choice for the tops of the two solves (a launch per level, or
+  // one CTA with a barrier per level).
+  {
+    auto solve_multi = [&](const Schedule &S, const std::vector<int> &ptr) {
+      const int lo = S.grp_lvl[S.n_groups], hi = S.grp_lvl[S.n_groups + 1];
+      double t_multi = 0, t_single = 0;
+      for (int lv = lo; lv < hi; ++lv) {
+        double work = 0;
+        for (int t = S.lvl_ptr[lv]; t < S.lvl_ptr[lv + 1]; ++t) {
+          const int i = S.items[t];
+          work += ptr[i + 1] - ptr[i];
+        }
+        t_multi += kLaunchTime + work / (kSmFmaRate * kNumSms);
+        t_single += kBarrierTime + work / kSmFmaRate;
+      }
+      return t_multi < t_single;
+    };
+    out.solve_top_multi = out.fsched.n_top_items >= kTopRightLooking &&
+                          (solve_multi(out.lsched, out.l_ptr) || solve_multi(out.fsched, out.u_ptr));
   }
   return XG_OK;
 }
