@@ -754,6 +754,11 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
   UP(L.u_ptr, H.u_ptr); UP(L.u_pos, H.u_pos); UP(L.u_col, H.u_col);
   UP(L.exempt, H.exempt);
   UP(L.upd_off, H.upd_off); UP(L.upd_pos, H.upd_pos);
+  {
+    int *um = nullptr;
+    UP(um, H.umeta);
+    L.umeta = reinterpret_cast<const int4 *>(um);
+  }
   for (int w = 0; w < 2; ++w) {
     const Schedule &S = w ? H.lsched : H.fsched;
     SchedDev &D = w ? L.ls : L.fs;

@@ -233,6 +233,7 @@ struct LUDev {
   char *exempt = nullptr;    // per step: skip the threshold test
   int *breakdown = nullptr;  // device flag: first failing step + 1
   int *upd_off = nullptr, *upd_pos = nullptr;  // per U entry: target positions of its update
+  const int4 *umeta = nullptr;                   // per U entry: see LUHost::umeta
   SchedDev fs, ls;           // factor (and, backwards, U solve) / L-solve schedules
   int f_levels = 0, l_levels = 0, u_levels = 0;  // plain level counts (statistics)
   // Mixed precision (FP32 factors, FP64 iterative refinement): lu32 holds the
@@ -300,6 +301,10 @@ struct LUHost {
   std::vector<int> l_long, u_long;  // per solve level: long rows at the end of the level
   Schedule fsched, lsched;
   std::vector<int> upd_off, upd_pos;  // scatter positions of each U entry's update
+  // per U entry p = U(k, j), 4 ints: shared-memory index of L(k+1.., k) in the
+  // group buffer (-1: not staged), |L(:, k)| below the diagonal, upd_off[p],
+  // global position of L(k+1, k) — one load instead of a chain of three
+  std::vector<int> umeta;
 };
 
 Schedule build_schedule(int n, const std::function<void(int, std::vector<int> &)> &deps_of,

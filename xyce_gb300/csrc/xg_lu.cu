@@ -149,15 +149,15 @@ __device__ void factor_column(const LUDev &L, const double *__restrict__ vals, i
   team_sync<BLOCK>();
   bool lost = false;
   for (int p = p0; p < pd; ++p) {
-    const int k = L.ri[p];
+    const int4 um = L.umeta[p];
     const T ukj = lu[p];
     if (nz(ukj)) {
       // positions of L(:,k)'s rows in column j come from the analysis
-      const int q0 = L.diag[k] + 1, q1 = L.cp[k + 1];
-      const int *tgt = L.upd_pos + L.upd_off[p];
-      for (int q = q0 + lane; q < q1; q += nl) {
-        const int pos = tgt[q - q0];
-        if (pos > p && pos < p1) lu[pos] -= lu[q] * ukj;
+      const int *tgt = L.upd_pos + um.z;
+      const T *lk = lu + um.w;
+      for (int q = lane; q < um.y; q += nl) {
+        const int pos = tgt[q];
+        if (pos > p && pos < p1) lu[pos] -= lk[q] * ukj;
         else lost = true;
       }
     }
@@ -187,17 +187,26 @@ __device__ void factor_column_t(const LUDev &L, const double *__restrict__ vals,
     }
   bool lost = false;
   for (int p = p0; p < pd; ++p) {
+    const int4 um = L.umeta[p];
     const T ukj = cj[p - p0];
     if (!nz(ukj)) continue;
-    const int k = L.ri[p];
-    const int q0 = L.diag[k] + 1, q1 = L.cp[k + 1];
-    const int sk = S ? L.grp_soff[k] : -1;
-    const int *tgt = L.upd_pos + L.upd_off[p];
-    for (int q = q0; q < q1; ++q) {
-      const int pos = tgt[q - q0];
-      const T lqk = (sk >= 0) ? S[sk + (q - L.cp[k])] : glu[q];
-      if (pos > p && pos < p1) cj[pos - p0] -= lqk * ukj;
-      else lost = true;
+    const T *lk = (S && um.x >= 0) ? S + um.x : glu + um.w;
+    const int *tgt = L.upd_pos + um.z;
+    // four targets and sources loaded before their updates: one latency per
+    // four products
+    for (int q = 0; q < um.y; q += 4) {
+      int t[4];
+      T l[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (q + u < um.y) { t[u] = tgt[q + u]; l[u] = lk[q + u]; }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (q + u < um.y) {
+          const int pos = t[u];
+          if (pos > p && pos < p1) cj[pos - p0] -= l[u] * ukj;
+          else lost = true;
+        }
     }
   }
   unsigned long long ak = 0;
@@ -460,16 +469,14 @@ __device__ void factor_column_s(const LUDev &L, int j, CircState *cs, int masked
   const T *glu = lu_of<T>(L);
   bool lost = false;
   for (int p = p0; p < pd; ++p) {
-    const int k = L.ri[p];
+    const int4 um = L.umeta[p];
     const T ukj = cj[p - p0];
     if (nz(ukj)) {
-      const int q0 = L.diag[k] + 1, q1 = L.cp[k + 1];
-      const int sk = L.grp_soff[k];
-      const int *tgt = L.upd_pos + L.upd_off[p];
-      for (int q = q0 + lane; q < q1; q += nl) {
-        const int pos = tgt[q - q0];
-        const T lqk = (sk >= 0) ? S[sk + (q - L.cp[k])] : glu[q];
-        if (pos > p && pos < p1) cj[pos - p0] -= lqk * ukj;
+      const T *lk = (um.x >= 0) ? S + um.x : glu + um.w;
+      const int *tgt = L.upd_pos + um.z;
+      for (int q = lane; q < um.y; q += nl) {
+        const int pos = tgt[q];
+        if (pos > p && pos < p1) cj[pos - p0] -= lk[q] * ukj;
         else lost = true;
       }
     }

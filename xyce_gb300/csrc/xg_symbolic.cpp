@@ -672,6 +672,11 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
       [&](int i) { return (out.l_ptr[i + 1] - out.l_ptr[i]) > kLongSolveRow; }, nullptr);
   // Single-thread items: short factor columns (entries and update products),
   // short U rows (backward sweep of the factor schedule), short L rows.
+  // A thread walks its column's updates one after the other (a load latency
+  // each), a warp takes them in one step: single-thread columns pay off when
+  // enough groups run at once to hide that latency (a batch of circuits), not
+  // for a few large groups (one big circuit).
+  const bool thread_columns = out.fsched.n_groups >= 4 * (int)kNumSms;
   out.fsched.is_thread.assign(n, 0);
   out.fsched.is_thread_rev.assign(n, 0);
   out.lsched.is_thread.assign(n, 0);
@@ -682,27 +687,35 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
       const int k = out.ri[t];
       work += out.cp[k + 1] - out.diag[k] - 1;
     }
-    if (!out.fsched.is_long[j] && out.cp[j + 1] - out.cp[j] <= kThreadColumn && work <= kThreadWork)
+    if (thread_columns && !out.fsched.is_long[j] && out.cp[j + 1] - out.cp[j] <= kThreadColumn &&
+        work <= kThreadWork)
       out.fsched.is_thread[j] = 1;
     if (!out.fsched.is_long_rev[j] && out.u_ptr[j + 1] - out.u_ptr[j] <= kThreadRow) out.fsched.is_thread_rev[j] = 1;
     if (!out.lsched.is_long[j] && out.l_ptr[j + 1] - out.l_ptr[j] <= kThreadRow) out.lsched.is_thread[j] = 1;
   }
   // CTA size of each group sweep.  The groups are latency-bound chains of
-  // levels; a smaller CTA lets more groups share an SM.  Level l of group g
-  // needs need(l) threads (a thread per single-thread item, `team` per other
-  // item); a CTA of B threads walks it in ceil(need / B) passes and 2048 / B
-  // CTAs fit on an SM, so B minimizes sum_g sum_l ceil(need / B) * B.
+  // levels.  Level l of group g needs need(l) threads (a thread per
+  // single-thread item, `team` per other item); a CTA of B threads walks it
+  // in ceil(need / B) passes, so group g takes P_g(B) = sum_l ceil(need / B)
+  // passes, and 2048 / B CTAs share an SM.  The sweep takes about
+  // max(max_g P_g(B), sum_g P_g(B) * B / (SMs * 2048)) pass times: few
+  // groups favour wide CTAs, many groups narrow ones.
   auto cta_size = [&](const Schedule &S, const std::vector<char> &thr, int team) {
-    long long best_cost = -1;
+    double best_cost = -1;
     int best = 512;
     for (int B = 64; B <= 512; B *= 2) {
-      long long cost = 0;
-      for (int g = 0; g < S.n_groups; ++g)
+      double total = 0, longest = 0;
+      for (int g = 0; g < S.n_groups; ++g) {
+        double passes = 0;
         for (int lv = S.grp_lvl[g]; lv < S.grp_lvl[g + 1]; ++lv) {
           long long need = 0;
           for (int t = S.lvl_ptr[lv]; t < S.lvl_ptr[lv + 1]; ++t) need += thr[S.items[t]] ? 1 : team;
-          cost += (need + B - 1) / B * B;
+          passes += (double)((need + B - 1) / B);
         }
+        total += passes;
+        longest = std::max(longest, passes);
+      }
+      const double cost = std::max(longest, total * B / (kNumSms * 2048.0));
       if (best_cost < 0 || cost < best_cost) { best_cost = cost; best = B; }
     }
     return best;
@@ -725,6 +738,17 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
       out.grp_snz[g] = off;
     }
   }
+  // Per U entry metadata of the update it drives (after grp_soff).
+  out.umeta.assign((size_t)4 * nnz, 0);
+  for (int j = 0; j < n; ++j)
+    for (int p = out.cp[j]; p < out.diag[j]; ++p) {
+      const int k = out.ri[p];
+      int *u = &out.umeta[(size_t)4 * p];
+      u[0] = (out.grp_soff[j] >= 0 && out.grp_soff[k] >= 0) ? out.grp_soff[k] + (out.diag[k] + 1 - out.cp[k]) : -1;
+      u[1] = out.cp[k + 1] - out.diag[k] - 1;
+      u[2] = out.upd_off[p];
+      u[3] = out.diag[k] + 1;
+    }
   // Can the factor schedule's top run right-looking?  The sub-tree (non-top)
   // rows k of a top column j are pulled first, in step order; that is exact
   // when no top column m < k updates such a row, i.e. when every non-top L
