@@ -246,8 +246,15 @@ typedef struct xg_tran_params {
   double nl_reltol, nl_abstol, nl_deltaxtol, nl_rhstol, nl_smallupdatetol;
   int nl_maxstep;                              /* .OPTIONS NONLIN-TRAN */
   int max_steps;                               /* stop after this many accepted steps (0 = none) */
-  int max_order;                               /* 1 = backward Euler, 2 = trapezoid */
+  int max_order;                               /* 1 = backward Euler, 2 = trapezoid / BDF2 */
+  int method;                                  /* XG_METHOD_*: .OPTIONS TIMEINT METHOD (0 = ONESTEP) */
 } xg_tran_params;
+
+/* Integration methods, numbered as the reference's methodsEnum
+ * (src/TimeIntegrationPKG/N_TIA_fwd.h:56-58): OneStep (trapezoid, the
+ * default) and Gear12 (BDF1/2, N_TIA_Gear12.C). */
+#define XG_METHOD_ONESTEP 7
+#define XG_METHOD_GEAR    8
 
 typedef struct xg_tran_stats {
   long long accepted, rejected, newton_iters, newton_fail, lte_fail, dcop_iters;

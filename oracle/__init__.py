@@ -37,7 +37,7 @@ class TranParams(C.Structure):
                 ("nl_reltol", C.c_double), ("nl_abstol", C.c_double),
                 ("nl_deltaxtol", C.c_double), ("nl_rhstol", C.c_double),
                 ("nl_smallupdatetol", C.c_double), ("nl_maxstep", C.c_int),
-                ("max_steps", C.c_int), ("max_order", C.c_int)]
+                ("max_steps", C.c_int), ("max_order", C.c_int), ("method", C.c_int)]
 
 
 class TranStats(C.Structure):
@@ -166,7 +166,7 @@ class Oracle:
         tp = TranParams(tran.tstart, tran.tstop, tran.hmax, tran.hmin, tran.reltol,
                         tran.abstol, tran.nl_reltol, tran.nl_abstol, tran.nl_deltaxtol,
                         tran.nl_rhstol, tran.nl_smallupdatetol, tran.nl_maxstep,
-                        tran.max_steps, tran.max_order)
+                        tran.max_steps, tran.max_order, tran.method)
         times = np.zeros(cap)
         vals = np.zeros(cap * max(1, len(probes)))
         nout = C.c_int()

@@ -721,6 +721,10 @@ struct Coef {
   const double *qhist0, *qhist2;
   double gshunt;
   int n_nodes_shunt;  // shunts apply to all unknowns < this bound (per circuit none: all)
+  // Gear12::obtainResidual (N_TIA_Gear12.C:208-271): F - B + (a0 Q + a1 qH0 + a2 qH1) / h
+  int gear = 0;
+  double ga[3] = {0, 0, 0}, hinv = 0;
+  const double *gqh1 = nullptr;  // qH1 (second order only)
 };
 
 // origFlag test: did any nonlinear device limit its junction voltages?
@@ -741,9 +745,16 @@ void assemble(orc_ctx *c, Work &w, double time, int iter, int flags, const Coef 
            w.dQv.data(), w.dFdx.data(), w.dQdx.data());
   w.any_limited = device_limited(c, w);
   for (int i = 0; i < w.n; ++i) {
-    double r = cf.fscale * (w.F[i] - w.B[i]);
-    if (cf.qscale != 0.0) r += cf.qscale * (w.Q[i] - cf.qhist0[i]);
-    if (cf.hscale != 0.0) r += cf.hscale * cf.qhist2[i];
+    double r;
+    if (cf.gear) {
+      double q = cf.ga[0] * w.Q[i] + cf.ga[1] * cf.qhist0[i];
+      if (cf.gqh1) q += cf.ga[2] * cf.gqh1[i];
+      r = (w.F[i] - w.B[i]) + cf.hinv * q;  // hinv = 1 / h
+    } else {
+      r = cf.fscale * (w.F[i] - w.B[i]);
+      if (cf.qscale != 0.0) r += cf.qscale * (w.Q[i] - cf.qhist0[i]);
+      if (cf.hscale != 0.0) r += cf.hscale * cf.qhist2[i];
+    }
     if (cf.gshunt != 0.0 && !c->is_branch[i]) r += cf.gshunt * w.x[i];
     w.rhs[i] = -r + cf.qscale * w.dQv[i] + cf.fscale * w.dFv[i];
   }
@@ -920,9 +931,10 @@ extern "C" int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, 
   const double hmax = p->hmax > 0 ? p->hmax : 0.1 * (p->tstop - p->tstart);
   const double hmin = p->hmin;
   const int max_order = p->max_order > 0 ? p->max_order : 2;
+  const bool gear = p->method == 8;  // Gear12 (N_TIA_Gear12.C); else OneStep
   // integrator state (StepErrorControl / OneStep members)
   double t = p->tstart, h = 0.0, lastTimeStep = 0.0, tsum = 0.0, saved = hmax, estOverTol = 0.0;
-  double psi[3] = {0, 0, 0}, beta[3] = {1, 0, 0}, ck = 0.0;
+  double psi[3] = {0, 0, 0}, beta[3] = {1, 0, 0}, alpha[3] = {0, 0, 0}, ck = 0.0;
   int order = 1, numberOfSteps = 0, nef = 0, stepNumber = 0;
   bool beginning = true, lastOk = true;
   double stopTime = next_bp(t);
@@ -943,18 +955,45 @@ extern "C" int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, 
       double time_to_stop = stopTime - t;
       double hn = (t == p->tstart) ? 0.005 * time_to_stop : 0.1 * std::min(saved, time_to_stop);
       if (hn > hmax) hn = hmax;
-      h = (t != p->tstart) ? std::min(h, hn) : hn;
+      // (Gear12::initialize takes the restart step as is, N_TIA_Gear12.C:1225-1245)
+      h = (t != p->tstart && !gear) ? std::min(h, hn) : hn;
       h = std::min(std::max(h, hmin), hmax);
       tsum = 2.0 * h; lastTimeStep = h;
-      xh0 = w.xcurr; std::fill(xh1.begin(), xh1.end(), 0.0);
-      qh0 = Qc;
-      for (int i = 0; i < n; ++i) qh1[i] = -(Fc[i] - Bc[i]) * h;
+      if (gear) {
+        // Gear12::initialize history (N_TIA_Gear12.C:1280-1300)
+        xh0 = w.xcurr; xh1 = w.xcurr;
+        qh0 = Qc; qh1 = Qc;
+      } else {
+        xh0 = w.xcurr; std::fill(xh1.begin(), xh1.end(), 0.0);
+        qh0 = Qc;
+        for (int i = 0; i < n; ++i) qh1[i] = -(Fc[i] - Bc[i]) * h;
+      }
       numberOfSteps = 0; order = 1; psi[0] = h;
     }
-    // OneStep::updateCoeffs (:1584-1640)
     if (order == 2) psi[2] = psi[1];
     psi[1] = psi[0]; psi[0] = h;
-    if (order == 2) {
+    if (gear) {
+      // Gear12::updateCoeffs (N_TIA_Gear12.C:1050-1110)
+      if (order == 2) {
+        beta[2] = h / psi[2] * (h + psi[1]) / (psi[1] + psi[2]);
+        beta[1] = -h / psi[1] - beta[2] * (psi[1] + psi[2]) / psi[1];
+        beta[0] = 1.0 - beta[2] - beta[1];
+        alpha[2] = -h / psi[1] * h / (2 * h + psi[1]);
+        alpha[1] = 1 - alpha[2];
+        alpha[0] = -alpha[1] - alpha[2] * (1 + psi[1] / h);
+        alpha[2] = alpha[2] / alpha[0];
+        alpha[1] = alpha[1] / alpha[0];
+        alpha[0] = -1 / alpha[0];
+        ck = h / (h + psi[1] + psi[2]);
+      } else {
+        beta[0] = 1.0 + h / psi[1];
+        beta[1] = -h / psi[1];
+        alpha[0] = 1.0;
+        alpha[1] = -1.0;
+        ck = h / (h + psi[1]);
+      }
+    } else if (order == 2) {
+      // OneStep::updateCoeffs (:1584-1640)
       beta[1] = h / psi[1] + (h / psi[1]) * (h / psi[1]) / 2;
       beta[2] = -1.0 * h * h / psi[1] / psi[2] / 2;
       ck = (h / tsum) / 3.0;
@@ -966,16 +1005,31 @@ extern "C" int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, 
     double xmax = 0;
     for (int i = 0; i < n; ++i) xmax = std::max(xmax, std::fabs(w.xcurr[i]));
     for (int i = 0; i < n; ++i) errwt[i] = p->reltol * xmax + p->abstol;
-    // OneStep::obtainPredictor (:135-175)
+    // predictor: OneStep::obtainPredictor (:135-175) / Gear12::obtainPredictor (N_TIA_Gear12.C:131-190)
     for (int i = 0; i < n; ++i) {
-      double v = xh0[i] + beta[1] * xh1[i];
-      if (order == 2) v += beta[2] * xh2[i];
+      double v;
+      if (gear) {
+        v = beta[0] * xh0[i];
+        v += beta[1] * xh1[i];
+        if (order == 2) v += beta[2] * xh2[i];
+      } else {
+        v = xh0[i] + beta[1] * xh1[i];
+        if (order == 2) v += beta[2] * xh2[i];
+      }
       xn0[i] = v;
     }
     w.x = xn0;
     double tn = t + h;
     if (std::fabs(tn - stopTime) <= bptol) tn = stopTime;
     Coef cf{1.0 / h, order == 2 ? 0.5 : 1.0, order == 2 ? 0.5 : 0.0, qh0.data(), qh2.data(), 0.0, 0};
+    if (gear) {
+      // Gear12::obtainJacobian (N_TIA_Gear12.C:477-500): (a0 / h) dQdx + dFdx
+      cf.qscale = alpha[0] / h; cf.fscale = 1.0; cf.hscale = 0.0;
+      cf.gear = 1;
+      cf.ga[0] = alpha[0]; cf.ga[1] = alpha[1]; cf.ga[2] = alpha[2];
+      cf.hinv = 1.0 / h;
+      cf.gqh1 = order == 2 ? qh1.data() : nullptr;
+    }
     int iters = 0;
     int ns = newton(c, w, tn, nl, cf, 0, &iters);
     st->newton_iters += iters;
@@ -1010,14 +1064,21 @@ extern "C" int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, 
       double hnew = h;
       if (rr >= 2.0) hnew = 2.0 * h;
       else if (rr <= 1) hnew = std::max(0.25, std::min(0.9, rr)) * h;
-      // OneStep::updateHistory (:1390-1440)
-      if (order == 2) {
-        xh2 = xh1;
-        for (int i = 0; i < n; ++i) qh2[i] = w.F[i] - w.B[i];
-      }
-      for (int i = 0; i < n; ++i) {
-        xh1[i] = w.x[i] - xh0[i];
-        qh1[i] = w.Q[i] - qh0[i];
+      if (gear) {
+        // Gear12::updateHistory (N_TIA_Gear12.C:822-870)
+        if (order == 2) xh2 = xh1;
+        qh1 = qh0;
+        xh1 = xh0;
+      } else {
+        // OneStep::updateHistory (:1390-1440)
+        if (order == 2) {
+          xh2 = xh1;
+          for (int i = 0; i < n; ++i) qh2[i] = w.F[i] - w.B[i];
+        }
+        for (int i = 0; i < n; ++i) {
+          xh1[i] = w.x[i] - xh0[i];
+          qh1[i] = w.Q[i] - qh0[i];
+        }
       }
       xh0 = w.x; qh0 = w.Q;
       hnew = std::min(std::max(hnew, hmin), hmax);
@@ -1051,7 +1112,9 @@ extern "C" int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, 
       double hnew;
       if (ns <= 0) { hnew = h / 8; order = 1; }
       else if (nef == 1) {
-        order = 1;
+        // OneStep drops to first order first; Gear12::rejectStep keeps the
+        // order (N_TIA_Gear12.C:1500-1515)
+        if (!gear) order = 1;
         double rr = std::pow(0.5 / (estOverTol + 0.0001), 1.0 / (order + 1.0));
         rr = std::max(0.25, std::min(0.9, rr));
         hnew = rr * h;

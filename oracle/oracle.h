@@ -78,7 +78,8 @@ typedef struct orc_tran_params {
   double nl_reltol, nl_abstol, nl_deltaxtol, nl_rhstol, nl_smallupdatetol;
   int nl_maxstep;
   int max_steps;                    /* safety cap on accepted steps, 0 = none */
-  int max_order;                    /* 1 = BE only, 2 = trapezoid */
+  int max_order;                    /* 1 = BE only, 2 = trapezoid / BDF2 */
+  int method;                       /* 7 = OneStep (trapezoid), 8 = Gear12 (BDF2); 0 = 7 */
 } orc_tran_params;
 
 typedef struct orc_tran_stats {

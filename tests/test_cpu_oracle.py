@@ -192,3 +192,75 @@ def test_bsim4_chain_switches(oracle_mod):
     assert v[k, 0] > 0.99 and v[k, 1] < 0.05 and v[k, 2] > 0.95 and v[k, 3] < 0.05
     k = np.searchsorted(t, 0.65e-9)  # input low again since ~390 ps
     assert v[k, 0] < 0.01 and v[k, 1] > 0.95 and v[k, 3] > 0.95
+
+
+# ---- Gear12 (BDF1/2), .OPTIONS TIMEINT METHOD=GEAR ---------------------------
+
+def _gear(nl):
+    nl.tran.method = 8
+    return nl
+
+
+def test_gear_testnetlists_exact(oracle_mod):
+    """Source-driven nodes are exact under any integrator."""
+    nl = _gear(N.test_netlist2())
+    t, v, st = oracle_mod.Oracle(nl).transient(probes=[nl.names["1"], nl.names["2"]])
+    assert st["status"] == 0 and st["t_final"] == pytest.approx(1.0)
+    np.testing.assert_allclose(v[:, 0], np.sin(2 * np.pi * t), atol=1e-12)
+    np.testing.assert_allclose(v[:, 1], np.sin(2 * np.pi * t) * 100 / 150, atol=1e-12)
+
+
+def test_gear_rc_step_within_reltol(oracle_mod):
+    nl = _gear(N.rc_step(r=1e3, c=1e-9, v=1.0, tstop=5e-6))
+    t, v, st = oracle_mod.Oracle(nl).transient(probes=[nl.names["out"]])
+    assert st["status"] == 0
+    ref = 1.0 - np.exp(-np.maximum(t - 1e-12, 0.0) / 1e-6)
+    assert np.max(np.abs(v[:, 0] - ref)) < 1e-3
+
+
+def test_gear_rc_converges_at_second_order(oracle_mod):
+    """Steps held at HMAX (tolerances too loose to bind): halving the step
+    divides the error by ~4 for both second-order methods, Gear's error
+    constant being the larger (BDF2 2/9 against the trapezoid's 1/12)."""
+    errs = {}
+    for method in (7, 8):
+        for hm in (20e-9, 10e-9):
+            nl = N.rc_step(r=1e3, c=1e-9, v=1.0, tstop=3e-6)
+            nl.tran.method, nl.tran.reltol, nl.tran.abstol, nl.tran.hmax = method, 1.0, 1.0, hm
+            t, v, st = oracle_mod.Oracle(nl).transient(probes=[nl.names["out"]])
+            assert st["status"] == 0
+            late = t > 1e-6
+            ref = 1.0 - np.exp(-(t[late] - 1e-12) / 1e-6)
+            errs[method, hm] = np.max(np.abs(v[late, 0] - ref))
+    for method in (7, 8):
+        assert 3.0 < errs[method, 20e-9] / errs[method, 10e-9] < 5.0
+    assert 2.0 < errs[8, 10e-9] / errs[7, 10e-9] < 6.0
+
+
+def test_gear_first_order_is_backward_euler(oracle_mod):
+    """MAXORD=1: Gear12 and OneStep both reduce to backward Euler with the
+    same coefficients; their waveforms agree to rounding on a linear circuit
+    (the step-size controllers see different error constants, so compare at
+    a fixed step: HMAX well below every step the error control would take)."""
+    out = []
+    for method in (7, 8):
+        nl = N.rc_step(r=1e3, c=1e-9, v=1.0, tstop=1e-6)
+        nl.tran.method = method
+        nl.tran.max_order = 1
+        nl.tran.hmax = 1e-9
+        nl.tran.reltol = 1.0
+        t, v, st = oracle_mod.Oracle(nl).transient(probes=[nl.names["out"]])
+        out.append((t, v[:, 0]))
+    (t7, v7), (t8, v8) = out
+    n = min(len(t7), len(t8))
+    same = np.flatnonzero(np.abs(t7[:n] - t8[:n]) < 1e-18)
+    assert len(same) > 100
+    np.testing.assert_allclose(v8[same], v7[same], rtol=1e-9, atol=1e-12)
+
+
+def test_gear_ring_oscillates(oracle_mod):
+    nl = _gear(N.ring_oscillator(21, caps=True))
+    t, v, st = oracle_mod.Oracle(nl).transient(probes=[nl.names["n1"]])
+    assert st["status"] == 0
+    late = v[t > 5e-9, 0]
+    assert late.max() > 1.5 and late.min() < 0.3

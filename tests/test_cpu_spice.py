@@ -164,3 +164,11 @@ def test_reference_test_netlists_parse_to_the_known_answer_circuits(fname, maker
             np.testing.assert_array_equal(g, w)
     assert d.netlist.tran.tstop == 1.0
     assert [m.name for m in d.measures][:2] == ["MAXV1", "MINV1"]
+
+
+@pytest.mark.parametrize("opt,method,order", [("METHOD=GEAR", 8, 2), ("METHOD=8 MAXORD=1", 8, 1),
+                                              ("METHOD=TRAP", 7, 2), ("", 7, 2)])
+def test_timeint_method(opt, method, order):
+    d = S.parse(f"t\nR1 a 0 1\nC1 a 0 1n\nI1 0 a PULSE(0 1m 1n)\n.TRAN 1n 1u\n.OPTIONS TIMEINT {opt}\n.END\n"
+                if opt else "t\nR1 a 0 1\n.TRAN 1n 1u\n.END\n")
+    assert d.netlist.tran.method == method and d.netlist.tran.max_order == order

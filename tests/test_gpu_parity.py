@@ -225,6 +225,28 @@ def test_transient_matches_oracle(xg, oracle_mod, torch_cuda, name, maker, probe
     assert err <= tol, (err, tol)
 
 
+@pytest.mark.parametrize("name,maker,probes", [
+    ("rc_step", N.rc_step, ["in", "out"]),
+    ("diode_ladder_50", lambda: N.diode_ladder(50, seed=5), ["n1", "n25", "n50"]),
+    ("ring_21_caps", lambda: N.ring_oscillator(21, caps=True), ["n1", "n11"]),
+    ("b4_chain_3", lambda: N.bsim4_inverter_chain(3), ["in", "n1", "n3"]),
+])
+def test_gear_transient_matches_oracle(xg, oracle_mod, torch_cuda, name, maker, probes):
+    """.OPTIONS TIMEINT METHOD=GEAR (Gear12, BDF1/2) on the GPU against the
+    oracle's restatement: same accepted/rejected steps, waveforms within tolerance."""
+    nl = maker()
+    nl.tran.method = 8
+    pr = [nl.names[p] for p in probes]
+    counts, t, v, st = xg.Circuit(nl).transient(probes=pr, cap=400000)
+    to, vo, so = oracle_mod.Oracle(nl).transient(probes=pr)
+    assert st["status"] == 0 and so["status"] == 0
+    k = int(counts[0])
+    assert st["accepted"] == so["accepted"] and st["rejected"] == so["rejected"]
+    assert k == len(to)
+    err, tol = _compare_waveforms(to, vo, t[0, :k], v[0, :k])
+    assert err <= tol, (err, tol)
+
+
 def test_testnetlists_analytic_on_gpu(xg, torch_cuda):
     nl = N.test_netlist1()
     counts, t, v, st = xg.Circuit(nl).transient(probes=[nl.names["1"]], cap=1000)

@@ -66,7 +66,7 @@ class TranParams(C.Structure):
                 ("nl_reltol", C.c_double), ("nl_abstol", C.c_double),
                 ("nl_deltaxtol", C.c_double), ("nl_rhstol", C.c_double),
                 ("nl_smallupdatetol", C.c_double), ("nl_maxstep", C.c_int),
-                ("max_steps", C.c_int), ("max_order", C.c_int)]
+                ("max_steps", C.c_int), ("max_order", C.c_int), ("method", C.c_int)]
 
 
 class TranStats(C.Structure):
@@ -271,7 +271,8 @@ class Circuit:
     def _tran_params(self, tran):
         return TranParams(tran.tstart, tran.tstop, tran.hmax, tran.hmin, tran.reltol, tran.abstol,
                           tran.nl_reltol, tran.nl_abstol, tran.nl_deltaxtol, tran.nl_rhstol,
-                          tran.nl_smallupdatetol, tran.nl_maxstep, tran.max_steps, tran.max_order)
+                          tran.nl_smallupdatetol, tran.nl_maxstep, tran.max_steps, tran.max_order,
+                          tran.method)
 
     def tran_start(self, tran=None, probes=(), cap=0):
         """Operating point + first analysis; keeps the run resident for tran_advance."""
@@ -359,7 +360,8 @@ class Circuit:
         probes = np.asarray(probes, np.int32)
         tp = TranParams(tran.tstart, tran.tstop, tran.hmax, tran.hmin, tran.reltol, tran.abstol,
                         tran.nl_reltol, tran.nl_abstol, tran.nl_deltaxtol, tran.nl_rhstol,
-                        tran.nl_smallupdatetol, tran.nl_maxstep, tran.max_steps, tran.max_order)
+                        tran.nl_smallupdatetol, tran.nl_maxstep, tran.max_steps, tran.max_order,
+                          tran.method)
         nc = self.n_circuits
         offs = np.asarray(self.netlist.offsets)
         per = np.bincount(np.searchsorted(offs, probes, side="right") - 1, minlength=nc) \

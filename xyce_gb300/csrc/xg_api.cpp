@@ -1093,6 +1093,8 @@ extern "C" int xg_tran_start(xg_ctx *ctx, const xg_tran_params *p, int n_probe, 
   if (!ctx->finalized) return fail(ctx, XG_ERR_STATE, "not finalized");
   if (!(p->tstop > p->tstart)) return fail(ctx, XG_ERR_ARG, "tstop must exceed tstart");
   if (cap < 0 || n_probe < 0) return fail(ctx, XG_ERR_ARG, "negative cap or probe count");
+  if (p->method != 0 && p->method != XG_METHOD_ONESTEP && p->method != XG_METHOD_GEAR)
+    return fail(ctx, XG_ERR_ARG, "method must be XG_METHOD_ONESTEP or XG_METHOD_GEAR");
   CK(cudaSetDevice(ctx->device));
   if (ctx->run) xg_free_run(ctx);
   ctx->run = new TranRun;
@@ -1143,6 +1145,7 @@ extern "C" int xg_tran_start(xg_ctx *ctx, const xg_tran_params *p, int n_probe, 
   tp.nl_reltol = p->nl_reltol; tp.nl_abstol = p->nl_abstol; tp.nl_deltaxtol = p->nl_deltaxtol;
   tp.nl_rhstol = p->nl_rhstol; tp.nl_smallupdatetol = p->nl_smallupdatetol; tp.nl_maxstep = p->nl_maxstep;
   tp.max_steps = p->max_steps; tp.max_order = p->max_order > 0 ? p->max_order : 2;
+  tp.gear = (p->method == XG_METHOD_GEAR) ? 1 : 0;
   tp.bptol = 1e-15 * (p->tstop - p->tstart);
   tp.dc_reltol = 1e-3; tp.dc_abstol = 1e-12; tp.dc_deltaxtol = 1.0; tp.dc_rhstol = 1e-6; tp.dc_maxstep = 200;
   tp.dc_only = (p->max_steps < 0) ? 1 : 0;

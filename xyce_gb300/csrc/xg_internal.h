@@ -34,6 +34,7 @@ struct CircState {
   double stopTime;     // next breakpoint or tstop
   double lastTimeStep, tsum, saved, estOverTol;
   double psi[3], beta[3], ck;
+  double alpha[3];     // Gear12 coefficients of Q, qH0, qH1 (the residual is F - B + (.)/h)
   double qscale, fscale, hscale;   // residual/Jacobian coefficients of this attempt
   double errwt;        // reltol*max|x_curr| + abstol (NEWLTE = 1)
   double xmax_curr;    // max |x_curr|
@@ -62,6 +63,7 @@ struct TranParams {
   double tstart, tstop, hmax, hmin, reltol, abstol;
   double nl_reltol, nl_abstol, nl_deltaxtol, nl_rhstol, nl_smallupdatetol;
   int nl_maxstep, max_steps, max_order;
+  int gear;  // 1 = Gear12 (BDF1/2), 0 = OneStep
   double bptol;
   // operating-point options (N_NLS_Manager.C:1030-1052)
   double dc_reltol, dc_abstol, dc_deltaxtol, dc_rhstol;

@@ -583,9 +583,17 @@ __global__ void __launch_bounds__(kRowBlock) k_assemble_rows(DevArrays d, int n)
         for (int k = d.vB_ptr[r]; k < d.vB_ptr[r + 1]; ++k) B += d.sB[d.vB_idx[k]];
         for (int k = d.vL_ptr[r]; k < d.vL_ptr[r + 1]; ++k) L += d.sL[d.vL_idx[k]];
       }
-      double res = s.fscale * (F - B);
-      if (s.qscale != 0.0) res += s.qscale * (Q - d.qh0[r]);
-      if (s.hscale != 0.0) res += s.hscale * d.qh2[r];
+      double res;
+      if (s.phase == PH_TRAN && d.tp->gear) {
+        // Gear12::obtainResidual (N_TIA_Gear12.C:208-271)
+        double q = s.alpha[0] * Q + s.alpha[1] * d.qh0[r];
+        if (s.order == 2) q += s.alpha[2] * d.qh1[r];
+        res = (F - B) + (1.0 / s.h) * q;
+      } else {
+        res = s.fscale * (F - B);
+        if (s.qscale != 0.0) res += s.qscale * (Q - d.qh0[r]);
+        if (s.hscale != 0.0) res += s.hscale * d.qh2[r];
+      }
       if (s.gshunt != 0.0 && !d.is_branch[r]) res += s.gshunt * d.x[r];
       const double rhs = -res + L;
       d.rhs[r] = rhs;
@@ -787,7 +795,8 @@ __device__ void start_next_step(CircState &s, const TranParams &p, int &init_his
     const double time_to_stop = s.stopTime - s.t;
     double hn = (s.t == p.tstart) ? 0.005 * time_to_stop : 0.1 * fmin(s.saved, time_to_stop);
     if (hn > p.hmax) hn = p.hmax;
-    s.h = (s.t != p.tstart) ? fmin(s.h, hn) : hn;
+    // (Gear12::initialize takes the restart step as is, N_TIA_Gear12.C:1225-1245)
+    s.h = (s.t != p.tstart && !p.gear) ? fmin(s.h, hn) : hn;
     s.h = fmin(fmax(s.h, p.hmin), p.hmax);
     s.tsum = 2.0 * s.h;
     s.lastTimeStep = s.h;
@@ -800,7 +809,29 @@ __device__ void start_next_step(CircState &s, const TranParams &p, int &init_his
   if (s.order == 2) s.psi[2] = s.psi[1];
   s.psi[1] = s.psi[0];
   s.psi[0] = h;
-  if (s.order == 2) {
+  if (p.gear) {
+    // Gear12::updateCoeffs (N_TIA_Gear12.C:1050-1110): variable-step BDF
+    // predictor (beta) and corrector (alpha) coefficients
+    if (s.order == 2) {
+      s.beta[2] = h / s.psi[2] * (h + s.psi[1]) / (s.psi[1] + s.psi[2]);
+      s.beta[1] = -h / s.psi[1] - s.beta[2] * (s.psi[1] + s.psi[2]) / s.psi[1];
+      s.beta[0] = 1.0 - s.beta[2] - s.beta[1];
+      double a2 = -h / s.psi[1] * h / (2 * h + s.psi[1]);
+      double a1 = 1 - a2;
+      const double a0 = -a1 - a2 * (1 + s.psi[1] / h);
+      s.alpha[2] = a2 / a0;
+      s.alpha[1] = a1 / a0;
+      s.alpha[0] = -1 / a0;
+      s.ck = h / (h + s.psi[1] + s.psi[2]);
+    } else {
+      s.beta[0] = 1.0 + h / s.psi[1];
+      s.beta[1] = -h / s.psi[1];
+      s.alpha[0] = 1.0;
+      s.alpha[1] = -1.0;
+      s.alpha[2] = 0.0;
+      s.ck = h / (h + s.psi[1]);
+    }
+  } else if (s.order == 2) {
     s.beta[1] = h / s.psi[1] + (h / s.psi[1]) * (h / s.psi[1]) / 2;
     s.beta[2] = -1.0 * h * h / s.psi[1] / s.psi[2] / 2;
     s.ck = (h / s.tsum) / 3.0;
@@ -812,9 +843,16 @@ __device__ void start_next_step(CircState &s, const TranParams &p, int &init_his
   double tn = s.t + h;
   if (fabs(tn - s.stopTime) <= p.bptol) tn = s.stopTime;
   s.tn = tn;
-  s.qscale = 1.0 / h;
-  s.fscale = (s.order == 2) ? 0.5 : 1.0;
-  s.hscale = (s.order == 2) ? 0.5 : 0.0;
+  if (p.gear) {
+    // Gear12::obtainJacobian (N_TIA_Gear12.C:477-500): (alpha0 / h) dQdx + dFdx
+    s.qscale = s.alpha[0] / h;
+    s.fscale = 1.0;
+    s.hscale = 0.0;
+  } else {
+    s.qscale = 1.0 / h;
+    s.fscale = (s.order == 2) ? 0.5 : 1.0;
+    s.hscale = (s.order == 2) ? 0.5 : 0.0;
+  }
   s.iter = 0;
   s.start_step = 1;
 }
@@ -970,7 +1008,9 @@ __global__ void k_step_ctl(DevArrays d, int ncirc, const double *bps, const int 
       if (status <= 0) {
         hnew = s.h / 8; s.order = 1;
       } else if (s.nef == 1) {
-        s.order = 1;
+        // OneStep drops to first order first; Gear12::rejectStep keeps the
+        // order (N_TIA_Gear12.C:1500-1515)
+        if (!p.gear) s.order = 1;
         double rr = pow(0.5 / (s.estOverTol + 0.0001), 1.0 / (s.order + 1.0));
         rr = fmax(0.25, fmin(0.9, rr));
         hnew = rr * s.h;
@@ -1001,10 +1041,18 @@ __global__ void k_history(DevArrays d, int n, int cap, int pmax) {
   if (!s.step_end && !s.start_step) return;
   const bool accepted_tran = s.accept == 1;
   const bool accepted_dc = s.accept == 2;
+  const bool gear = d.tp->gear;
   if (accepted_tran) {
-    if (s.order == 2) { d.xh2[r] = d.xh1[r]; d.qh2[r] = d.FmB[r]; }
-    d.xh1[r] = d.x[r] - d.xcurr[r];
-    d.qh1[r] = d.Qv[r] - d.qh0[r];
+    if (gear) {
+      // Gear12::updateHistory (N_TIA_Gear12.C:822-870): absolute histories
+      if (s.order == 2) d.xh2[r] = d.xh1[r];
+      d.qh1[r] = d.qh0[r];
+      d.xh1[r] = d.xcurr[r];
+    } else {
+      if (s.order == 2) { d.xh2[r] = d.xh1[r]; d.qh2[r] = d.FmB[r]; }
+      d.xh1[r] = d.x[r] - d.xcurr[r];
+      d.qh1[r] = d.Qv[r] - d.qh0[r];
+    }
     // the learned predictor's history: differences of the last four solutions
     d.mlh3[r] = d.mlh2[r];
     d.mlh2[r] = d.mlh1[r];
@@ -1025,13 +1073,24 @@ __global__ void k_history(DevArrays d, int n, int cap, int pmax) {
   }
   if (s.start_step && (s.phase == PH_TRAN || s.phase == PH_PAUSED)) {
     const TranParams &p = *d.tp;
-    if (s.init_hist) {  // OneStep::initialize history
-      d.xh1[r] = 0.0;
-      d.qh1[r] = -d.FmBc[r] * s.h;
+    if (s.init_hist) {
+      if (gear) {  // Gear12::initialize history (N_TIA_Gear12.C:1280-1300)
+        d.xh1[r] = d.xcurr[r];
+        d.qh1[r] = d.Qc[r];
+      } else {     // OneStep::initialize history
+        d.xh1[r] = 0.0;
+        d.qh1[r] = -d.FmBc[r] * s.h;
+      }
       d.qh0[r] = d.Qc[r];
     }
     const double xc = d.xcurr[r];
-    double xn = xc + s.beta[1] * d.xh1[r];
+    double xn;
+    if (gear) {  // Gear12::obtainPredictor (N_TIA_Gear12.C:131-145)
+      xn = s.beta[0] * xc;
+      xn += s.beta[1] * d.xh1[r];
+    } else {
+      xn = xc + s.beta[1] * d.xh1[r];
+    }
     if (s.order == 2) xn += s.beta[2] * d.xh2[r];
     d.xn0[r] = xn;
     d.x[r] = xn;

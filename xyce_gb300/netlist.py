@@ -103,6 +103,7 @@ class Tran:
     nl_maxstep: int = 20
     max_order: int = 2
     max_steps: int = 0
+    method: int = 7  # 7 = OneStep (trapezoid), 8 = Gear12 (BDF2): TIMEINT METHOD
 
 
 @dataclass

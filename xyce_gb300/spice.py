@@ -9,7 +9,7 @@ output.  The subset is what the path simulates:
   ``D`` (diode level 1), ``M`` (MOSFET level 1; level 54/14 = BSIM4 4.8.2),
   ``X`` (subcircuit instances, flattened);
 * ``.MODEL``, ``.SUBCKT``/``.ENDS``, ``.TRAN``, ``.OPTIONS TIMEINT``
-  (RELTOL, ABSTOL), ``.PRINT TRAN``, ``.MEASURE TRAN`` (MAX, MIN, PP, AVG,
+  (RELTOL, ABSTOL, METHOD=TRAP|GEAR, MAXORD), ``.PRINT TRAN``, ``.MEASURE TRAN`` (MAX, MIN, PP, AVG,
   RMS, INTEG with FROM/TO), ``.END``; ``*`` and ``;`` comments, ``+``
   continuation lines, engineering suffixes (T G MEG K M MIL U N P F);
 * print variables ``V(n)``, ``V(a,b)``, ``I(Vname)``, ``TIME``, ``TEMP``
@@ -394,7 +394,7 @@ def parse(text: str) -> Deck:
         raise ValueError(".SUBCKT without .ENDS")
     tran = None
     tstep = 0.0
-    reltol = abstol = None
+    reltol = abstol = method = maxord = None
     deck = B.deck
     for ln, toks in body_lines:
         head = toks[0].upper()
@@ -418,6 +418,16 @@ def parse(text: str) -> Deck:
                         reltol = number(v)
                     elif k == "ABSTOL":
                         abstol = number(v)
+                    elif k == "METHOD":
+                        mv = v.upper()
+                        methods = {"TRAP": 7, "TRAPEZOID": 7, "7": 7, "1": 7, "GEAR": 8, "8": 8}
+                        if mv not in methods:
+                            raise ValueError(f".OPTIONS TIMEINT METHOD={v} is not supported")
+                        method = methods[mv]
+                    elif k == "MAXORD":
+                        maxord = int(number(v))
+                        if maxord not in (1, 2):
+                            raise ValueError("MAXORD must be 1 or 2")
                     else:
                         raise ValueError(f".OPTIONS TIMEINT {k} is not supported")
             else:
@@ -438,6 +448,10 @@ def parse(text: str) -> Deck:
         tran.reltol = reltol
     if abstol is not None:
         tran.abstol = abstol
+    if method is not None:
+        tran.method = method
+    if maxord is not None:
+        tran.max_order = maxord
     B.finish_sources(tstep, tran.tstop)
     B.nl.tran = tran
     B.nl.end_circuit()
