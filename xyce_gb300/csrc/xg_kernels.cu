@@ -165,7 +165,14 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
   vbd = vbs - vds;
   vgd = vgs - vds;
   const double Vgb = vgs - vbs;
-  const bool origFlag = !(vgs_o != vgs || vds_o != vds || vbs_o != vbs || vbd_o != vbd || vgd_o != vgd);
+  // "no voltage was limited", compared on the bit patterns (integer pipe;
+  // +0 and -0 compare equal as in FP64)
+  auto same = [](double a, double b) {
+    const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    return x == y || ((x | y) << 1) == 0;
+  };
+  const bool origFlag = same(vgs_o, vgs) && same(vds_o, vds) && same(vbs_o, vbs) && same(vbd_o, vbd) &&
+                        same(vgd_o, vgd);
   double gbs, cbs, gbd, cbd;
   if (vbs <= 0) {
     gbs = m.gsatS + kGmin;
@@ -202,7 +209,7 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
     if (vgst <= 0) {
       cdrain = 0; gm = 0; gds = 0; gmbs = 0;
     } else {
-      double vdsm = vds * mode;
+      double vdsm = (mode == 1) ? vds : -vds;
       double betap = Beta * (1 + m.lambda * vdsm);
       if (vgst <= vdsm) {
         cdrain = betap * vgst * vgst * .5;
@@ -262,11 +269,19 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
   }
   const double M = m.M;
   const bool unitM = (M == 1.0);
+  // A model without gate or junction capacitance has no charge: its Q
+  // vector, charge limiter terms and dQdx stamps are zero and are stored
+  // without FP64 arithmetic (as are products with a unit F scale)
+  const bool noq = !m.has_gate_caps && !m.has_junc_caps;
+  const bool fs1 = (fs == 1.0);
   // loadDAEVectors (N_DEV_MOSFET1.C:4343-4576), old Meyer
   const double ceqbs = T(cbs), ceqbd = T(cbd);
-  const double Qbs = T(qbs), Qbd = T(qbd), Qgb = T(qgb), Qgs = T(qgs), Qgd = T(qgd);
   double fv[3] = {-(ceqbd - cdreq), -(ceqbs + cdreq), ceqbs + ceqbd};  // D S B
-  double qv[4] = {Qgs + Qgd + Qgb, Qbs + Qbd - Qgb, -(Qbd + Qgd), -(Qbs + Qgs)};  // G B D S
+  double qv[4] = {0, 0, 0, 0};                                         // G B D S
+  if (!noq) {
+    const double Qbs = T(qbs), Qbd = T(qbd), Qgb = T(qgb), Qgs = T(qgs), Qgd = T(qgd);
+    qv[0] = Qgs + Qgd + Qgb; qv[1] = Qbs + Qbd - Qgb; qv[2] = -(Qbd + Qgd); qv[3] = -(Qbs + Qgs);
+  }
   double lf[4] = {0, 0, 0, 0}, lq[4] = {0, 0, 0, 0};
   if (!origFlag) {
     double dvbd = vbd - vbd_o, dvbs = vbs - vbs_o, dvds = vds - vds_o, dvgs = vgs - vgs_o,
@@ -275,10 +290,12 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
     lf[1] = T((gbd - kGmin) * dvbd + (gbs - kGmin) * dvbs);
     lf[2] = T(-(gbd - kGmin) * dvbd + gds * dvds + sw);
     lf[3] = T(-(gbs - kGmin) * dvbs - gds * dvds - sw);
-    lq[0] = T(Capgd * dvgd + Capgs * dvgs + Capgb * (dvgs - dvbs));
-    lq[1] = T(-Capgb * (dvgs - dvbs) + Capgb * dvbd + capbs * dvbs);
-    lq[2] = T(-Capgd * dvgd - capbd * dvbd);
-    lq[3] = T(-Capgs * dvgs - capbs * dvbs);
+    if (!noq) {
+      lq[0] = T(Capgd * dvgd + Capgs * dvgs + Capgb * (dvgs - dvbs));
+      lq[1] = T(-Capgb * (dvgs - dvbs) + Capgb * dvbd + capbs * dvbs);
+      lq[2] = T(-Capgd * dvgd - capbd * dvbd);
+      lq[3] = T(-Capgs * dvgs - capbs * dvbs);
+    }
   }
   // the multiplier is applied only when it is not 1 (a branch, not a select,
   // so that the FP64 products are skipped)
@@ -286,7 +303,11 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
 #pragma unroll
     for (int k = 0; k < 3; ++k) fv[k] *= M;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) { qv[k] *= M; lf[k] *= M; lq[k] *= M; }
+    for (int k = 0; k < 4; ++k) lf[k] *= M;
+    if (!noq) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) { qv[k] *= M; lq[k] *= M; }
+    }
   }
   double *sF = d.sF + slotF, *sQ = d.sQ + slotQ;
 #pragma unroll
@@ -295,8 +316,13 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
   for (int k = 0; k < 4; ++k) sQ[k * nm + i] = qv[k];
   double *sL = d.sL + slotL;
   if (combined) {
+    if (noq) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) sL[k * nm + i] = fs * lf[k] + qs * lq[k];
+      for (int k = 0; k < 4; ++k) sL[k * nm + i] = fs1 ? lf[k] : fs * lf[k];
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) sL[k * nm + i] = fs * lf[k] + qs * lq[k];
+    }
   } else {
     double *sL2 = d.sL2 + slotL;
 #pragma unroll
@@ -309,10 +335,12 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
   f[15] = gbs + gbd; f[12] = -gbd; f[14] = -gbs;
   f[1] = Gm; f[3] = -gbd + Gmbs; f[0] = gds + gbd + revsum; f[2] = -gds - nrmsum;
   f[9] = -Gm; f[11] = -(gbs + Gmbs); f[8] = -(gds + revsum); f[10] = gds + gbs + nrmsum;
-  q[5] = Capgd + Capgs + Capgb; q[7] = -Capgb; q[4] = -Capgd; q[6] = -Capgs;
-  q[13] = -Capgb; q[15] = capbs + capbd + Capgb; q[12] = -capbd; q[14] = -capbs;
-  q[1] = -Capgd; q[3] = -capbd; q[0] = capbd + Capgd;
-  q[9] = -Capgs; q[11] = -capbs; q[10] = capbs + Capgs;
+  if (!noq) {
+    q[5] = Capgd + Capgs + Capgb; q[7] = -Capgb; q[4] = -Capgd; q[6] = -Capgs;
+    q[13] = -Capgb; q[15] = capbs + capbd + Capgb; q[12] = -capbd; q[14] = -capbs;
+    q[1] = -Capgd; q[3] = -capbd; q[0] = capbd + Capgd;
+    q[9] = -Capgs; q[11] = -capbs; q[10] = capbs + Capgs;
+  }
   // structural zeros of the two 4x4 blocks (the gate conducts no current;
   // no capacitance couples D-S) are stored without FP64 arithmetic
   constexpr bool kFnz[16] = {1, 1, 1, 1, 0, 0, 0, 0, 1, 1, 1, 1, 1, 0, 1, 1};
@@ -321,19 +349,24 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
       if (kFnz[k]) f[k] *= M;
-      if (kQnz[k]) q[k] *= M;
+      if (kQnz[k] && !noq) q[k] *= M;
     }
   }
   double *sM = d.sM + slotM;
   if (combined) {
+    if (noq) {
 #pragma unroll
-    for (int k = 0; k < 16; ++k) {
-      double v;
-      if (kFnz[k] && kQnz[k]) v = fs * f[k] + qs * q[k];
-      else if (kFnz[k]) v = fs * f[k];
-      else if (kQnz[k]) v = qs * q[k];
-      else v = 0.0;
-      sM[k * nm + i] = v;
+      for (int k = 0; k < 16; ++k) sM[k * nm + i] = kFnz[k] ? (fs1 ? f[k] : fs * f[k]) : 0.0;
+    } else {
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        double v;
+        if (kFnz[k] && kQnz[k]) v = fs * f[k] + qs * q[k];
+        else if (kFnz[k]) v = fs * f[k];
+        else if (kQnz[k]) v = qs * q[k];
+        else v = 0.0;
+        sM[k * nm + i] = v;
+      }
     }
   } else {
     double *sM2 = d.sM2 + slotM;
