@@ -303,7 +303,7 @@ def _roofline(xg, circ, nl, dev, flush, stream_of, hbm_peak, peak_kind, args):
             "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
             "algorithmic_bytes_per_launch": bytes_per_inst * nm, "launch_us": us,
-            "fp64_pipe_note": "ncu: FP64 pipe 83.6 % busy in this kernel (profiles/k_mos1_mc1024_full.md); "
+            "fp64_pipe_note": "ncu: FP64 pipe 78.8 % busy in this kernel (profiles/k_mos1_mc1024_full.md); "
                               "the FP64 pipe, not HBM, bounds it on GB300"}
 
 

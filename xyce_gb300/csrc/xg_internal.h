@@ -200,6 +200,8 @@ constexpr int kNoAllocMaxDevices = 64;
 constexpr int kLongColumn = 512;   // factor columns longer than this use the whole CTA
 constexpr int kHubFanout = 64;     // items with more dependents than this run in the prologue
 constexpr int kGroupCap = 512;     // items per dependency-closed group
+constexpr int kPackSmall = 4;      // groups this small are packed together ...
+constexpr int kPackCap = 256;      // ... up to this many items per CTA
 constexpr int kTopRightLooking = 64;  // tops at least this large factor right-looking
 // Ordering choice: estimated time = FMAs / kOrderFmaRate + elimination-tree
 // height * kOrderLevelTime (sparse FP64 updates on GB300 run far below the

@@ -506,8 +506,8 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
   }
   const int it0 = SD.lvl_ptr[SD.grp_lvl[g]], it1 = SD.lvl_ptr[SD.grp_lvl[g + 1]];
   if (it0 >= it1) return;
-  // a group belongs to one circuit: activity is uniform over the CTA
-  if (!item_active(L, cs, masked, SD.items[it0])) return;
+  // a group of one circuit is active or not as a whole; packed tiny groups
+  // may mix circuits, so every item is tested
   // load the group's columns from A (warp per column)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   for (int t = it0 + warp; t < it1; t += nwarps) {
@@ -523,18 +523,19 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
     bool any_long = false;
     for (int t = b + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
       const int j = SD.items[t];
-      if (SD.is_thread[j]) factor_column_t<T>(L, vals, j, cs, masked, pivot_tol, S);
+      if (SD.is_thread[j] && item_active(L, cs, masked, j))
+        factor_column_t<T>(L, vals, j, cs, masked, pivot_tol, S);
     }
     for (int t = b + warp; t < e; t += nwarps) {
       const int j = SD.items[t];
       if (SD.is_long[j]) { any_long = true; continue; }
-      if (SD.is_thread[j]) continue;
+      if (SD.is_thread[j] || !item_active(L, cs, masked, j)) continue;
       factor_column_s<false, T>(L, j, cs, masked, pivot_tol, sm, S);
     }
     if (__syncthreads_or(any_long)) {
       for (int t = b; t < e; ++t) {
         const int j = SD.items[t];
-        if (!SD.is_long[j]) continue;
+        if (!SD.is_long[j] || !item_active(L, cs, masked, j)) continue;
         factor_column_s<true, T>(L, j, cs, masked, pivot_tol, sm, S);
         __syncthreads();
       }

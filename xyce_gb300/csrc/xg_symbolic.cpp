@@ -930,6 +930,32 @@ Schedule build_schedule(int n, const std::function<void(int, std::vector<int> &)
     if (gid[r] < 0) gid[r] = ng++;
     gid[j] = gid[r];
   }
+  // Pack runs of consecutive tiny groups (e.g. the isolated supply-node and
+  // branch columns of every circuit of a batch) into shared CTAs: they are
+  // independent, so their local levels merge.  Packed groups may mix
+  // circuits; the kernels test each item's circuit.
+  {
+    std::vector<int> gsz(ng, 0);
+    for (int j = 0; j < n; ++j)
+      if (gid[j] >= 0) gsz[gid[j]]++;
+    std::vector<int> pack(ng);
+    int np = 0, cur_size = 0;
+    bool cur_small = false;
+    for (int g = 0; g < ng; ++g) {
+      const bool small = gsz[g] <= kPackSmall;
+      if (small && cur_small && cur_size + gsz[g] <= kPackCap) {
+        pack[g] = np - 1;
+        cur_size += gsz[g];
+      } else {
+        pack[g] = np++;
+        cur_size = gsz[g];
+        cur_small = small;
+      }
+    }
+    for (int j = 0; j < n; ++j)
+      if (gid[j] >= 0) gid[j] = pack[gid[j]];
+    ng = np;
+  }
   for (int j = 0; j < n; ++j)
     if (top[j]) gid[j] = ng;
   S.n_groups = ng;
