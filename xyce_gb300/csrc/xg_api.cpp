@@ -803,6 +803,25 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
     }
   }
   L.ordering = H.ordering;
+  for (int w = 0; w < 2; ++w) {
+    const std::vector<int> &gb = w ? H.us_gbytes : H.ls_gbytes;
+    int mx = 0;
+    for (int b : gb) mx = std::max(mx, b);
+    if (mx == 0) continue;
+    if (w == 0) {
+      if ((rc = dev_upload(ctx, &L.ls_eptr, H.ls_eptr, A))) return rc;
+      if ((rc = dev_upload(ctx, &L.ls_epos, H.ls_epos, A))) return rc;
+      if ((rc = dev_upload(ctx, &L.ls_esrc, H.ls_esrc, A))) return rc;
+      if ((rc = dev_upload(ctx, &L.ls_gbytes, H.ls_gbytes, A))) return rc;
+      L.ls_smem = mx;
+    } else {
+      if ((rc = dev_upload(ctx, &L.us_eptr, H.us_eptr, A))) return rc;
+      if ((rc = dev_upload(ctx, &L.us_epos, H.us_epos, A))) return rc;
+      if ((rc = dev_upload(ctx, &L.us_esrc, H.us_esrc, A))) return rc;
+      if ((rc = dev_upload(ctx, &L.us_gbytes, H.us_gbytes, A))) return rc;
+      L.us_smem = mx;
+    }
+  }
   L.fs_threads = H.fs_threads;
   L.ls_threads = H.ls_threads;
   L.us_threads = H.us_threads;
@@ -816,6 +835,28 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
       if ((rc = lu_prepare_k())) return rc;
       if ((rc = dev_upload(ctx, &L.grp_soff, H.grp_soff, A))) return rc;
       if ((rc = dev_upload(ctx, &L.grp_snz, H.grp_snz, A))) return rc;
+      // groups staged with their update metadata: values (16-byte aligned),
+      // then the metadata; the launch buffer covers the largest
+      bool any_meta = false;
+      for (size_t g = 0; g < H.fm_gbytes.size(); ++g) {
+        if (H.fm_gbytes[g] == 0) continue;
+        any_meta = true;
+        for (int w = 0; w < 2; ++w) {
+          const size_t vb = ((size_t)H.grp_snz[g] * (w ? sizeof(float) : sizeof(double)) + 15) / 16 * 16;
+          L.fm_smem[w] = std::max(L.fm_smem[w], (int)(vb + H.fm_gbytes[g]));
+        }
+      }
+      if (any_meta) {
+        int *c = nullptr, *e = nullptr;
+        if ((rc = dev_upload(ctx, &c, H.fm_col, A))) return rc;
+        if ((rc = dev_upload(ctx, &e, H.fm_ent, A))) return rc;
+        L.fm_col = reinterpret_cast<const int4 *>(c);
+        L.fm_ent = reinterpret_cast<const int4 *>(e);
+        if ((rc = dev_upload(ctx, &L.fm_eptr, H.fm_eptr, A))) return rc;
+        if ((rc = dev_upload(ctx, &L.fm_tptr, H.fm_tptr, A))) return rc;
+        if ((rc = dev_upload(ctx, &L.fm_tgt, H.fm_tgt, A))) return rc;
+        if ((rc = dev_upload(ctx, &L.fm_gbytes, H.fm_gbytes, A))) return rc;
+      }
     }
   }
   if (H.solve_top_multi) {

@@ -223,6 +223,8 @@ constexpr int kGroupSmemBytes = 96 * 1024;  // largest group buffer staged in sh
 constexpr int kThreadColumn = 32;  // factor columns with at most this many entries ...
 constexpr int kThreadWork = 96;    // ... and at most this many update products
 constexpr int kThreadRow = 4;      // solve rows with at most this many entries
+constexpr int kSolveSmemBytes = 48 * 1024;  // largest solve group staged in shared memory
+constexpr int kStageRow = 64;               // staged solve groups: rows of at most this many entries
 
 // LU structures (device) produced by the host analysis.  Plain data: it is
 // passed to kernels by value.
@@ -238,6 +240,9 @@ struct LUDev {
   int *breakdown = nullptr;  // device flag: first failing step + 1
   int *upd_off = nullptr, *upd_pos = nullptr;  // per U entry: target positions of its update
   const int4 *umeta = nullptr;                   // per U entry: see LUHost::umeta
+  const int4 *fm_col = nullptr, *fm_ent = nullptr;  // see LUHost::fm_col
+  int *fm_eptr = nullptr, *fm_tptr = nullptr, *fm_tgt = nullptr, *fm_gbytes = nullptr;
+  int fm_smem[2] = {0, 0};  // launch buffer bytes (double | float factors) when metadata is staged
   SchedDev fs, ls;           // factor (and, backwards, U solve) / L-solve schedules
   int f_levels = 0, l_levels = 0, u_levels = 0;  // plain level counts (statistics)
   // Mixed precision (FP32 factors, FP64 iterative refinement): lu32 holds the
@@ -266,6 +271,11 @@ struct LUDev {
   int grp_fit[2] = {0, 0};
   int fs_threads = 512, ls_threads = 512, us_threads = 512;  // CTA sizes of the group sweeps
   int ordering = 0;  // XG_ORDER_* of the analysis
+  // solve groups staged in shared memory (see LUHost::ls_eptr); *_smem =
+  // buffer bytes of the largest staged group (0: none staged)
+  int *ls_eptr = nullptr, *ls_epos = nullptr, *ls_esrc = nullptr, *ls_gbytes = nullptr;
+  int *us_eptr = nullptr, *us_epos = nullptr, *us_esrc = nullptr, *us_gbytes = nullptr;
+  int ls_smem = 0, us_smem = 0;
   int ls_top_lo = 0, ls_top_hi = 0, fs_top_lo = 0, fs_top_hi = 0;
   float *lu32 = nullptr;
   double *ir_r = nullptr;
@@ -298,6 +308,13 @@ struct LUHost {
   int order_height[2] = {0, 0};
   // CTA sizes of the group sweeps (factor, L solve, U solve)
   int fs_threads = 512, ls_threads = 512, us_threads = 512;
+  // Solve groups staged in shared memory: the entries of the rows at
+  // schedule position t are [xs_eptr[t], xs_eptr[t+1]) of xs_epos (LU
+  // position) / xs_esrc (slot of the column's row in its group's buffer, or
+  // -(k+1): row k outside the group); xs_gbytes[g] = buffer bytes of group g
+  // (0: not staged).  ls = L solve (L schedule), us = U solve (factor schedule).
+  std::vector<int> ls_eptr, ls_epos, ls_esrc, ls_gbytes;
+  std::vector<int> us_eptr, us_epos, us_esrc, us_gbytes;
   std::vector<int> row_of_step, col_of_step, cp, ri, diag, src;
   std::vector<int> f_lvl_ptr, f_cols, l_lvl_ptr, l_rows, l_ptr, l_pos, l_col;
   std::vector<int> u_lvl_ptr, u_rows, u_ptr, u_pos, u_col;
@@ -309,6 +326,14 @@ struct LUHost {
   // group buffer (-1: not staged), |L(:, k)| below the diagonal, upd_off[p],
   // global position of L(k+1, k) — one load instead of a chain of three
   std::vector<int> umeta;
+  // Factor groups whose update metadata is staged in shared memory too (after
+  // the values): per schedule position t, 4 ints {value offset in the group
+  // buffer, column entries, diagonal offset, pivot-test flag}; fm_eptr[t] ..
+  // fm_eptr[t+1] its U entries in fm_ent, 4 ints each {L(k+1.., k) source:
+  // buffer index, or -(global position)-1; entry count; offset of its targets
+  // in the group's fm_tgt segment (from fm_tptr[g]); position of U(k, j) in
+  // the column}; fm_gbytes[g] = metadata bytes (0: values only)
+  std::vector<int> fm_col, fm_eptr, fm_ent, fm_tptr, fm_tgt, fm_gbytes;
 };
 
 Schedule build_schedule(int n, const std::function<void(int, std::vector<int> &)> &deps_of,

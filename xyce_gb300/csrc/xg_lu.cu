@@ -21,6 +21,8 @@
 // schedule backwards (its dependency graph is the factor graph reversed).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <mutex>
 #include <string>
 
@@ -121,18 +123,23 @@ template <> __device__ __forceinline__ float *lu_of<float>(const LUDev &L) { ret
 // Pivot test and scaling of column j once its updates are in: d = U(j,j),
 // amax = the largest |L(:,j)| entry (as a key), lost = an update that missed
 // the pattern.  Returns false on breakdown (flag raised by `leader`).
-__device__ __forceinline__ bool pivot_ok(const LUDev &L, int j, CircState *cs, int masked, double pivot_tol,
-                                         double d, double amax, bool lost, bool leader) {
-  // The threshold only matters when row j of U has entries right of the
-  // diagonal: otherwise the multipliers never reach the Schur complement
-  // (e.g. the branch row of a grounded voltage source).
-  const bool urow = L.u_ptr[j + 1] > L.u_ptr[j] && !L.exempt[j];
+__device__ __forceinline__ bool pivot_ok_u(const LUDev &L, int j, CircState *cs, int masked, double pivot_tol,
+                                           double d, double amax, bool lost, bool leader, bool urow) {
   const bool bad = lost || (urow && !(fabs(d) >= pivot_tol * amax)) || !(fabs(d) > 0.0) || isinf(d);
   if (bad && leader) {
     atomicCAS(L.breakdown, 0, j + 1);
     if (masked) cs[L.circ_of_step[j]].singular = 1;
   }
   return !bad;
+}
+
+__device__ __forceinline__ bool pivot_ok(const LUDev &L, int j, CircState *cs, int masked, double pivot_tol,
+                                         double d, double amax, bool lost, bool leader) {
+  // The threshold only matters when row j of U has entries right of the
+  // diagonal: otherwise the multipliers never reach the Schur complement
+  // (e.g. the branch row of a grounded voltage source).
+  const bool urow = L.u_ptr[j + 1] > L.u_ptr[j] && !L.exempt[j];
+  return pivot_ok_u(L, j, cs, masked, pivot_tol, d, amax, lost, leader, urow);
 }
 
 template <bool BLOCK, typename T>
@@ -491,6 +498,47 @@ __device__ void factor_column_s(const LUDev &L, int j, CircState *cs, int masked
   for (int p = pd + 1 + lane; p < p1; p += nl) cj[p - p0] *= inv;
 }
 
+// A column of a group whose update metadata is staged too (mcol: the
+// group's column records, ment: their U entries, mtg: update targets; all
+// in shared memory).  TEAM lanes (1 = a thread per column, 32 = a warp).
+struct FMeta {
+  const int4 *col, *ent;
+  const int *eptr, *tgt;
+};
+template <int TEAM, typename T>
+__device__ void factor_column_m(const LUDev &L, int j, int r, CircState *cs, int masked, double pivot_tol,
+                                double *sm, T *S, const FMeta &M) {
+  const int lane = TEAM == 1 ? 0 : (int)(threadIdx.x & 31);
+  const int4 col = M.col[r];  // value offset, entries, diagonal offset, pivot-test flag
+  T *cj = S + col.x;
+  const T *glu = lu_of<T>(L);
+  bool lost = false;
+  for (int u = M.eptr[r]; u < M.eptr[r + 1]; ++u) {
+    const int4 en = M.ent[u];  // L source, count, target offset, position of U(k, j)
+    const T ukj = cj[en.w];
+    if (nz(ukj)) {
+      const T *lk = en.x >= 0 ? S + en.x : glu + (-en.x - 1);
+      const int *tg = M.tgt + en.z;
+      for (int q = lane; q < en.y; q += TEAM) {
+        const int pos = tg[q];
+        if (pos > en.w && pos < col.y) cj[pos] -= lk[q] * ukj;
+        else lost = true;
+      }
+    }
+    if (TEAM > 1) __syncwarp();
+  }
+  unsigned long long ak = 0;
+  for (int p = col.z + lane; p < col.y; p += TEAM) ak = umax64(ak, mag_key(cj[p]));
+  if (TEAM > 1) {
+    ak = team_max_key<false>(ak, sm);
+    lost = team_any<false>(lost);
+  }
+  if (!pivot_ok_u(L, j, cs, masked, pivot_tol, (double)cj[col.z], key_value<T>(ak), lost, lane == 0, col.w != 0))
+    return;
+  const T inv = (T)1 / cj[col.z];
+  for (int p = col.z + 1 + lane; p < col.y; p += TEAM) cj[p] *= inv;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, const double *__restrict__ vals,
                                                                     CircState *cs, int masked, double pivot_tol,
@@ -517,7 +565,40 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
       S[o + (p - p0)] = (s >= 0) ? (T)vals[s] : (T)0;
     }
   }
-  __syncthreads();
+  const int mbytes = L.fm_gbytes ? L.fm_gbytes[g] : 0;
+  if (mbytes > 0) {
+    // the update metadata of the group, after the values (16-byte aligned)
+    unsigned char *mraw = smraw_lu + ((size_t)L.grp_snz[g] * sizeof(T) + 15) / 16 * 16;
+    const int R = it1 - it0, u0 = L.fm_eptr[it0], U = L.fm_eptr[it1] - u0;
+    const int t0 = L.fm_tptr[g], TG = L.fm_tptr[g + 1] - t0;
+    FMeta M;
+    int4 *mcol = reinterpret_cast<int4 *>(mraw);
+    int4 *ment = mcol + R;
+    int *mep = reinterpret_cast<int *>(ment + U);
+    int *mtg = mep + R + 1;
+    for (int r = threadIdx.x; r <= R; r += blockDim.x) {
+      mep[r] = L.fm_eptr[it0 + r] - u0;
+      if (r < R) mcol[r] = L.fm_col[it0 + r];
+    }
+    for (int u = threadIdx.x; u < U; u += blockDim.x) ment[u] = L.fm_ent[u0 + u];
+    for (int q = threadIdx.x; q < TG; q += blockDim.x) mtg[q] = L.fm_tgt[t0 + q];
+    M.col = mcol; M.ent = ment; M.eptr = mep; M.tgt = mtg;
+    __syncthreads();
+    for (int lv = SD.grp_lvl[g]; lv < SD.grp_lvl[g + 1]; ++lv) {
+      const int b = SD.lvl_ptr[lv], e = SD.lvl_ptr[lv + 1];
+      for (int t = b + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
+        const int j = SD.items[t];
+        if (SD.is_thread[j] && item_active(L, cs, masked, j))
+          factor_column_m<1, T>(L, j, t - it0, cs, masked, pivot_tol, sm, S, M);
+      }
+      for (int t = b + warp; t < e; t += nwarps) {
+        const int j = SD.items[t];
+        if (SD.is_thread[j] || !item_active(L, cs, masked, j)) continue;
+        factor_column_m<32, T>(L, j, t - it0, cs, masked, pivot_tol, sm, S, M);
+      }
+      __syncthreads();
+    }
+  } else {
   for (int lv = SD.grp_lvl[g]; lv < SD.grp_lvl[g + 1]; ++lv) {
     const int b = SD.lvl_ptr[lv], e = SD.lvl_ptr[lv + 1];
     bool any_long = false;
@@ -540,6 +621,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
         __syncthreads();
       }
     }
+  }
   }
   __syncthreads();
   // write the factored columns back (the solves and the top read them)
@@ -581,12 +663,10 @@ __device__ __forceinline__ double row_dot_t(const T *__restrict__ lu, const int 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kGroupThreads) k_lsolve_groups(LUDev L, const double *__restrict__ b,
-                                                        const CircState *cs, int masked, int top) {
-  __shared__ double sm[32];
+__device__ void lsolve_group(const LUDev &L, const double *__restrict__ b, const CircState *cs, int masked, int g,
+                             double *sm) {
   const SchedDev &S = L.ls;
   const T *lu = lu_of<T>(L);
-  const int g = top ? S.n_groups : (int)blockIdx.x;
   const int team = threadIdx.x >> 3, nteams = blockDim.x >> 3, sub = threadIdx.x & 7;
   for (int lv = S.grp_lvl[g]; lv < S.grp_lvl[g + 1]; ++lv) {
     const int bb = S.lvl_ptr[lv], e = S.lvl_ptr[lv + 1];
@@ -630,14 +710,72 @@ __global__ void __launch_bounds__(kGroupThreads) k_lsolve_groups(LUDev L, const 
   }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(kGroupThreads) k_lsolve_groups(LUDev L, const double *__restrict__ b,
+                                                                  const CircState *cs, int masked, int top) {
+  __shared__ double sm[32];
+  lsolve_group<T>(L, b, cs, masked, top ? L.ls.n_groups : (int)blockIdx.x, sm);
+}
+
+// A group's L solve staged in shared memory: its rows' entries (values and
+// buffer slots) and its slice of y are loaded once, coalesced; each level
+// then reads only shared memory (a thread per row), and y is written back
+// at the end.  Groups over the buffer run the global-memory path.
+template <typename T>
+__global__ void __launch_bounds__(kGroupThreads) k_lsolve_groups_s(LUDev L, const double *__restrict__ b,
+                                                                    const CircState *cs, int masked) {
+  extern __shared__ __align__(16) unsigned char smraw_sv[];
+  __shared__ double sm[32];
+  const SchedDev &S = L.ls;
+  const int g = blockIdx.x;
+  if (L.ls_gbytes[g] == 0) {
+    lsolve_group<T>(L, b, cs, masked, g, sm);
+    return;
+  }
+  const T *lu = lu_of<T>(L);
+  const int it0 = S.lvl_ptr[S.grp_lvl[g]], it1 = S.lvl_ptr[S.grp_lvl[g + 1]], R = it1 - it0;
+  const int e0 = L.ls_eptr[it0], E = L.ls_eptr[it1] - e0;
+  double *yv = reinterpret_cast<double *>(smraw_sv);
+  double *ev = yv + R;
+  int *es = reinterpret_cast<int *>(ev + E);
+  int *ep = es + E;
+  int *act = ep + R + 1;
+  for (int r = threadIdx.x; r <= R; r += blockDim.x) {
+    ep[r] = L.ls_eptr[it0 + r] - e0;
+    if (r < R) {
+      const int i = S.items[it0 + r];
+      act[r] = item_active(L, cs, masked, i) ? 1 : 0;
+      yv[r] = b[L.row_of_step[i]];
+    }
+  }
+  for (int e = threadIdx.x; e < E; e += blockDim.x) {
+    ev[e] = (double)lu[L.ls_epos[e0 + e]];
+    es[e] = L.ls_esrc[e0 + e];
+  }
+  __syncthreads();
+  for (int lv = S.grp_lvl[g]; lv < S.grp_lvl[g + 1]; ++lv) {
+    const int r0 = S.lvl_ptr[lv] - it0, r1 = S.lvl_ptr[lv + 1] - it0;
+    for (int r = r0 + (int)threadIdx.x; r < r1; r += (int)blockDim.x) {
+      if (!act[r]) continue;
+      double sum = 0.0;
+      for (int q = ep[r]; q < ep[r + 1]; ++q) {
+        const int src = es[q];
+        sum += ev[q] * (src >= 0 ? yv[src] : L.y[-src - 1]);
+      }
+      yv[r] -= sum;
+    }
+    __syncthreads();
+  }
+  for (int r = threadIdx.x; r < R; r += blockDim.x)
+    if (act[r]) L.y[S.items[it0 + r]] = yv[r];
+}
+
 // ---- U solve (factor schedule, backward) ------------------------------------
 template <typename T, bool ACC>
-__global__ void __launch_bounds__(kGroupThreads) k_usolve_groups(LUDev L, double *__restrict__ x, const CircState *cs,
-                                                        int masked, int top) {
-  __shared__ double sm[32];
+__device__ void usolve_group(const LUDev &L, double *__restrict__ x, const CircState *cs, int masked, int g,
+                             double *sm) {
   const SchedDev &S = L.fs;
   const T *lu = lu_of<T>(L);
-  const int g = top ? S.n_groups : (int)blockIdx.x;
   const int team = threadIdx.x >> 3, nteams = blockDim.x >> 3, sub = threadIdx.x & 7;
   for (int lv = S.grp_lvl[g + 1] - 1; lv >= S.grp_lvl[g]; --lv) {
     const int bb = S.lvl_ptr[lv], e = S.lvl_ptr[lv + 1];
@@ -683,6 +821,72 @@ __global__ void __launch_bounds__(kGroupThreads) k_usolve_groups(LUDev L, double
         __syncthreads();
       }
     }
+  }
+}
+
+template <typename T, bool ACC>
+__global__ void __launch_bounds__(kGroupThreads) k_usolve_groups(LUDev L, double *__restrict__ x,
+                                                                  const CircState *cs, int masked, int top) {
+  __shared__ double sm[32];
+  usolve_group<T, ACC>(L, x, cs, masked, top ? L.fs.n_groups : (int)blockIdx.x, sm);
+}
+
+// The U solve of a group staged in shared memory (the factor schedule run
+// backwards; see k_lsolve_groups_s): y and the diagonal of the group's rows
+// and the entries of their U rows are loaded once.
+template <typename T, bool ACC>
+__global__ void __launch_bounds__(kGroupThreads) k_usolve_groups_s(LUDev L, double *__restrict__ x,
+                                                                    const CircState *cs, int masked) {
+  extern __shared__ __align__(16) unsigned char smraw_sv[];
+  __shared__ double sm[32];
+  const SchedDev &S = L.fs;
+  const int g = blockIdx.x;
+  if (L.us_gbytes[g] == 0) {
+    usolve_group<T, ACC>(L, x, cs, masked, g, sm);
+    return;
+  }
+  const T *lu = lu_of<T>(L);
+  const int it0 = S.lvl_ptr[S.grp_lvl[g]], it1 = S.lvl_ptr[S.grp_lvl[g + 1]], R = it1 - it0;
+  const int e0 = L.us_eptr[it0], E = L.us_eptr[it1] - e0;
+  double *yv = reinterpret_cast<double *>(smraw_sv);
+  double *dv = yv + R;
+  double *ev = dv + R;
+  int *es = reinterpret_cast<int *>(ev + E);
+  int *ep = es + E;
+  int *act = ep + R + 1;
+  for (int r = threadIdx.x; r <= R; r += blockDim.x) {
+    ep[r] = L.us_eptr[it0 + r] - e0;
+    if (r < R) {
+      const int k = S.items[it0 + r];
+      act[r] = item_active(L, cs, masked, k) ? 1 : 0;
+      yv[r] = L.y[k];
+      dv[r] = (double)lu[L.diag[k]];
+    }
+  }
+  for (int e = threadIdx.x; e < E; e += blockDim.x) {
+    ev[e] = (double)lu[L.us_epos[e0 + e]];
+    es[e] = L.us_esrc[e0 + e];
+  }
+  __syncthreads();
+  for (int lv = S.grp_lvl[g + 1] - 1; lv >= S.grp_lvl[g]; --lv) {
+    const int r0 = S.lvl_ptr[lv] - it0, r1 = S.lvl_ptr[lv + 1] - it0;
+    for (int r = r0 + (int)threadIdx.x; r < r1; r += (int)blockDim.x) {
+      if (!act[r]) continue;
+      double sum = 0.0;
+      for (int q = ep[r]; q < ep[r + 1]; ++q) {
+        const int src = es[q];
+        sum += ev[q] * (src >= 0 ? yv[src] : L.y[-src - 1]);
+      }
+      yv[r] = (yv[r] - sum) / dv[r];
+    }
+    __syncthreads();
+  }
+  for (int r = threadIdx.x; r < R; r += blockDim.x) {
+    if (!act[r]) continue;
+    const int k = S.items[it0 + r];
+    L.y[k] = yv[r];
+    if (ACC) x[L.col_of_step[k]] += yv[r];
+    else x[L.col_of_step[k]] = yv[r];
   }
 }
 
@@ -804,10 +1008,11 @@ static void factor_sweeps(cudaStream_t st, const LUDev &L, const double *vals, C
   if (L.fs.n_groups > 0) {
     // groups of up to kGroupSmemBytes factor in shared memory; the buffer is
     // sized for the largest of them, larger groups factor in global memory
-    const int fit = L.grp_fit[sizeof(T) == 4 ? 1 : 0];
+    const int w = sizeof(T) == 4 ? 1 : 0;
+    const int fit = L.grp_fit[w];
+    const size_t smem = std::max((size_t)fit * sizeof(T), (size_t)L.fm_smem[w]);
     if (L.grp_snz && fit > 0)
-      k_factor_groups_s<T><<<L.fs.n_groups, L.fs_threads, (size_t)fit * sizeof(T), st>>>(L, vals, cs, masked,
-                                                                                          pivot_tol, fit);
+      k_factor_groups_s<T><<<L.fs.n_groups, L.fs_threads, smem, st>>>(L, vals, cs, masked, pivot_tol, fit);
     else
       k_factor_groups<T><<<L.fs.n_groups, L.fs_threads, 0, st>>>(L, vals, cs, masked, pivot_tol, 0);
   }
@@ -852,7 +1057,12 @@ template <typename T, bool ACC>
 static void solve_sweeps(cudaStream_t st, const LUDev &L, const double *b, double *x, const CircState *cs,
                          int masked) {
   if (L.ls.n_hub > 0) k_lsolve_hubs<<<(L.ls.n_hub + 255) / 256, 256, 0, st>>>(L, b, cs, masked);
-  if (L.ls.n_groups > 0) k_lsolve_groups<T><<<L.ls.n_groups, L.ls_threads, 0, st>>>(L, b, cs, masked, 0);
+  if (L.ls.n_groups > 0) {
+    if (L.ls_smem > 0)
+      k_lsolve_groups_s<T><<<L.ls.n_groups, L.ls_threads, L.ls_smem, st>>>(L, b, cs, masked);
+    else
+      k_lsolve_groups<T><<<L.ls.n_groups, L.ls_threads, 0, st>>>(L, b, cs, masked, 0);
+  }
   if (L.ls.n_top_items > 0) {
     if (L.h_ls_lvl_ptr) {
       for (int lv = L.ls_top_lo; lv < L.ls_top_hi; ++lv) {
@@ -873,8 +1083,12 @@ static void solve_sweeps(cudaStream_t st, const LUDev &L, const double *b, doubl
       k_usolve_groups<T, ACC><<<1, kGroupThreads, 0, st>>>(L, x, cs, masked, 1);
     }
   }
-  if (L.fs.n_groups > 0)
-    k_usolve_groups<T, ACC><<<L.fs.n_groups, L.us_threads, 0, st>>>(L, x, cs, masked, 0);
+  if (L.fs.n_groups > 0) {
+    if (L.us_smem > 0)
+      k_usolve_groups_s<T, ACC><<<L.fs.n_groups, L.us_threads, L.us_smem, st>>>(L, x, cs, masked);
+    else
+      k_usolve_groups<T, ACC><<<L.fs.n_groups, L.us_threads, 0, st>>>(L, x, cs, masked, 0);
+  }
   if (L.fs.n_hub > 0) k_usolve_hubs<T, ACC><<<L.fs.n_hub, 256, 0, st>>>(L, x, cs, masked);
 }
 

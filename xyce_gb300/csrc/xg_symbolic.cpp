@@ -723,6 +723,47 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
   out.fs_threads = cta_size(out.fsched, out.fsched.is_thread, 32);
   out.ls_threads = cta_size(out.lsched, out.lsched.is_thread, 8);
   out.us_threads = cta_size(out.fsched, out.fsched.is_thread_rev, 8);
+  // Solve groups staged in shared memory: per schedule position the row's
+  // entries with the buffer slot of each entry's column (the L solve reads
+  // L(i, k) y(k) for k in row i's L part, the U solve U(k, j) y(j)).
+  auto stage_solve = [&](const Schedule &S, const std::vector<int> &ptr, const std::vector<int> &epos_src,
+                         const std::vector<int> &ecol_src, int extra_per_row, std::vector<int> &eptr,
+                         std::vector<int> &epos, std::vector<int> &esrc, std::vector<int> &gbytes) {
+    const int ni = (int)S.items.size();
+    std::vector<int> slot(n, -1), owner(n, -1);
+    gbytes.assign(S.n_groups, 0);
+    eptr.assign(ni + 1, 0);
+    epos.clear();
+    esrc.clear();
+    for (int g = 0; g < S.n_groups; ++g) {
+      const int it0 = S.lvl_ptr[S.grp_lvl[g]], it1 = S.lvl_ptr[S.grp_lvl[g + 1]];
+      for (int t = it0; t < it1; ++t) { slot[S.items[t]] = t - it0; owner[S.items[t]] = g; }
+    }
+    for (int t = 0; t < ni; ++t) {
+      const int i = S.items[t];
+      eptr[t] = (int)epos.size();
+      for (int q = ptr[i]; q < ptr[i + 1]; ++q) {
+        const int k = ecol_src[q];
+        epos.push_back(epos_src[q]);
+        esrc.push_back(owner[k] >= 0 && owner[k] == owner[i] ? slot[k] : -(k + 1));
+      }
+    }
+    eptr[ni] = (int)epos.size();
+    for (int g = 0; g < S.n_groups; ++g) {
+      const int it0 = S.lvl_ptr[S.grp_lvl[g]], it1 = S.lvl_ptr[S.grp_lvl[g + 1]];
+      const long long rows = it1 - it0, ents = eptr[it1] - eptr[it0];
+      bool ok = true;
+      for (int t = it0; t < it1 && ok; ++t) ok = eptr[t + 1] - eptr[t] <= kStageRow;
+      // doubles: y (+ the diagonal for the U solve) and entry values; ints:
+      // entry slots, the row entry offsets and the rows' activity flags
+      const long long bytes = 8 * (rows * (1 + extra_per_row) + ents) + 4 * (ents + rows + 1) + 4 * rows;
+      if (ok && bytes <= kSolveSmemBytes) gbytes[g] = (int)((bytes + 15) / 16 * 16);
+    }
+  };
+  stage_solve(out.lsched, out.l_ptr, out.l_pos, out.l_col, 0, out.ls_eptr, out.ls_epos, out.ls_esrc,
+              out.ls_gbytes);
+  stage_solve(out.fsched, out.u_ptr, out.u_pos, out.u_col, 1, out.us_eptr, out.us_epos, out.us_esrc,
+              out.us_gbytes);
   // Shared-memory buffers of the factor groups (not the hubs, not the top).
   {
     const Schedule &S = out.fsched;
@@ -749,6 +790,57 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
       u[2] = out.upd_off[p];
       u[3] = out.diag[k] + 1;
     }
+  // Update metadata of the factor groups staged in shared memory.
+  {
+    const Schedule &S = out.fsched;
+    const int ni = (int)S.items.size();
+    out.fm_col.assign((size_t)4 * ni, 0);
+    out.fm_eptr.assign(ni + 1, 0);
+    out.fm_ent.clear();
+    out.fm_tgt.clear();
+    out.fm_tptr.assign(S.n_groups + 1, 0);
+    out.fm_gbytes.assign(S.n_groups, 0);
+    std::vector<int> owner(n, -1);
+    for (int g = 0; g < S.n_groups; ++g)
+      for (int t = S.lvl_ptr[S.grp_lvl[g]]; t < S.lvl_ptr[S.grp_lvl[g + 1]]; ++t) owner[S.items[t]] = g;
+    int t_group_lo = 0;
+    for (int t = 0; t < ni; ++t) {
+      const int j = S.items[t];
+      const int g = owner[j];
+      out.fm_eptr[t] = (int)out.fm_ent.size() / 4;
+      if (g < 0) continue;
+      if (t == S.lvl_ptr[S.grp_lvl[g]]) {
+        out.fm_tptr[g] = (int)out.fm_tgt.size();
+        t_group_lo = (int)out.fm_tgt.size();
+      }
+      int *c = &out.fm_col[(size_t)4 * t];
+      c[0] = out.grp_soff[j];
+      c[1] = out.cp[j + 1] - out.cp[j];
+      c[2] = out.diag[j] - out.cp[j];
+      c[3] = (out.u_ptr[j + 1] > out.u_ptr[j] && !out.exempt[j]) ? 1 : 0;
+      for (int p = out.cp[j]; p < out.diag[j]; ++p) {
+        const int k = out.ri[p];
+        const int nl = out.cp[k + 1] - out.diag[k] - 1;
+        out.fm_ent.push_back(owner[k] == g ? out.grp_soff[k] + (out.diag[k] + 1 - out.cp[k]) : -(out.diag[k] + 1) - 1);
+        out.fm_ent.push_back(nl);
+        out.fm_ent.push_back((int)out.fm_tgt.size() - t_group_lo);
+        out.fm_ent.push_back(p - out.cp[j]);
+        for (int q = 0; q < nl; ++q) out.fm_tgt.push_back(out.upd_pos[out.upd_off[p] + q] - out.cp[j]);
+      }
+    }
+    out.fm_eptr[ni] = (int)out.fm_ent.size() / 4;
+    out.fm_tptr[S.n_groups] = (int)out.fm_tgt.size();
+    for (int g = 0; g < S.n_groups; ++g) {
+      const int it0 = S.lvl_ptr[S.grp_lvl[g]], it1 = S.lvl_ptr[S.grp_lvl[g + 1]];
+      bool ok = true;
+      for (int t = it0; t < it1 && ok; ++t) ok = !S.is_long[S.items[t]];
+      const long long rows = it1 - it0, ents = out.fm_eptr[it1] - out.fm_eptr[it0];
+      const long long tg = out.fm_tptr[g + 1] - out.fm_tptr[g];
+      const long long meta = 16 * rows + 4 * (rows + 1) + 16 * ents + 4 * tg;
+      const long long vals = ((long long)out.grp_snz[g] * 8 + 15) / 16 * 16;
+      if (ok && vals + meta <= kGroupSmemBytes) out.fm_gbytes[g] = (int)((meta + 15) / 16 * 16);
+    }
+  }
   // Can the factor schedule's top run right-looking?  The sub-tree (non-top)
   // rows k of a top column j are pulled first, in step order; that is exact
   // when no top column m < k updates such a row, i.e. when every non-top L
