@@ -200,8 +200,10 @@ constexpr int kNoAllocMaxDevices = 64;
 constexpr int kLongColumn = 512;   // factor columns longer than this use the whole CTA
 constexpr int kHubFanout = 64;     // items with more dependents than this run in the prologue
 constexpr int kGroupCap = 512;     // items per dependency-closed group
-constexpr int kPackSmall = 4;      // groups this small are packed together ...
-constexpr int kPackCap = 256;      // ... up to this many items per CTA
+constexpr int kPackSmall = 4;        // groups of at most this many items ...
+constexpr int kPackSmallWeight = 16; // ... and entries are packed together ...
+constexpr int kPackCap = 256;        // ... up to this many items ...
+constexpr int kPackCapWeight = 1024; // ... and entries per CTA
 constexpr int kTopRightLooking = 64;  // tops at least this large factor right-looking
 // Ordering choice: estimated time = FMAs / kOrderFmaRate + elimination-tree
 // height * kOrderLevelTime (sparse FP64 updates on GB300 run far below the
@@ -216,6 +218,7 @@ constexpr double kNumSms = 152;
 constexpr double kLaunchTime = 2.5e-6;
 constexpr double kBarrierTime = 1e-6;
 constexpr int kGroupSmemBytes = 96 * 1024;  // largest group buffer staged in shared memory
+constexpr int kSmemPerSm = 227 * 1024;      // shared memory of an SM available to CTAs
 // Short items of the grouped sweeps run on one thread each: a warp-wide FP64
 // instruction takes the same FP64-pipe time with one active lane as with 32,
 // and GB300's FP64 pipe is narrow, so a warp spent on a 3-entry column wastes
@@ -336,9 +339,11 @@ struct LUHost {
   std::vector<int> fm_col, fm_eptr, fm_ent, fm_tptr, fm_tgt, fm_gbytes;
 };
 
+// weight(j): entries item j touches (caps the packing of tiny groups)
 Schedule build_schedule(int n, const std::function<void(int, std::vector<int> &)> &deps_of,
                         const std::function<bool(int)> &is_long,
-                        const std::function<bool(int)> &is_long_rev);
+                        const std::function<bool(int)> &is_long_rev,
+                        const std::function<int(int)> &weight);
 
 // Analysis entry (xg_symbolic.cpp): CSR pattern + values -> LUHost.
 int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &ci,

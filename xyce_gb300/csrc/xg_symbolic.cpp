@@ -666,10 +666,12 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
   out.fsched = build_schedule(
       n, [&](int j, std::vector<int> &d) { for (int t = out.cp[j]; t < out.diag[j]; ++t) d.push_back(out.ri[t]); },
       [&](int j) { return (out.cp[j + 1] - out.diag[j] - 1) > kLongColumn || (out.diag[j] - out.cp[j]) > kLongColumn; },
-      [&](int j) { return (out.u_ptr[j + 1] - out.u_ptr[j]) > kLongSolveRow; });
+      [&](int j) { return (out.u_ptr[j + 1] - out.u_ptr[j]) > kLongSolveRow; },
+      [&](int j) { return out.cp[j + 1] - out.cp[j] + out.u_ptr[j + 1] - out.u_ptr[j]; });
   out.lsched = build_schedule(
       n, [&](int i, std::vector<int> &d) { for (int t = out.l_ptr[i]; t < out.l_ptr[i + 1]; ++t) d.push_back(out.l_col[t]); },
-      [&](int i) { return (out.l_ptr[i + 1] - out.l_ptr[i]) > kLongSolveRow; }, nullptr);
+      [&](int i) { return (out.l_ptr[i + 1] - out.l_ptr[i]) > kLongSolveRow; }, nullptr,
+      [&](int i) { return out.l_ptr[i + 1] - out.l_ptr[i] + 1; });
   // Single-thread items: short factor columns (entries and update products),
   // short U rows (backward sweep of the factor schedule), short L rows.
   // A thread walks its column's updates one after the other (a load latency
@@ -840,6 +842,20 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
       const long long vals = ((long long)out.grp_snz[g] * 8 + 15) / 16 * 16;
       if (ok && vals + meta <= kGroupSmemBytes) out.fm_gbytes[g] = (int)((meta + 15) / 16 * 16);
     }
+    // The metadata shortens each level's latency chain, but a larger buffer
+    // lets fewer CTAs share an SM: keep it only when the launch buffer with
+    // it allows as many resident CTAs as the values alone.
+    long long vmax = 0, mmax = 0;
+    for (int g = 0; g < S.n_groups; ++g) {
+      const long long vb = ((long long)out.grp_snz[g] * 8 + 15) / 16 * 16;
+      if (vb <= kGroupSmemBytes) vmax = std::max(vmax, vb);
+      mmax = std::max(mmax, out.fm_gbytes[g] ? vb + out.fm_gbytes[g] : vb);
+    }
+    auto resident = [&](long long bytes) {
+      const long long by_threads = 2048 / std::max(1, out.fs_threads);
+      return bytes > 0 ? std::min(by_threads, (long long)kSmemPerSm / bytes) : by_threads;
+    };
+    if (resident(mmax) < resident(vmax)) std::fill(out.fm_gbytes.begin(), out.fm_gbytes.end(), 0);
   }
   // Can the factor schedule's top run right-looking?  The sub-tree (non-top)
   // rows k of a top column j are pulled first, in step order; that is exact
@@ -952,7 +968,8 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
 // dependencies, many dependents) and a single-CTA top for the rest.
 Schedule build_schedule(int n, const std::function<void(int, std::vector<int> &)> &deps_of,
                         const std::function<bool(int)> &is_long,
-                        const std::function<bool(int)> &is_long_rev) {
+                        const std::function<bool(int)> &is_long_rev,
+                        const std::function<int(int)> &weight) {
   Schedule S;
   if (n == 0) {
     S.grp_lvl.assign(2, 0);
@@ -1028,19 +1045,23 @@ Schedule build_schedule(int n, const std::function<void(int, std::vector<int> &)
   // circuits; the kernels test each item's circuit.
   {
     std::vector<int> gsz(ng, 0);
+    std::vector<long long> gw(ng, 0);
     for (int j = 0; j < n; ++j)
-      if (gid[j] >= 0) gsz[gid[j]]++;
+      if (gid[j] >= 0) { gsz[gid[j]]++; gw[gid[j]] += weight(j); }
     std::vector<int> pack(ng);
     int np = 0, cur_size = 0;
+    long long cur_w = 0;
     bool cur_small = false;
     for (int g = 0; g < ng; ++g) {
-      const bool small = gsz[g] <= kPackSmall;
-      if (small && cur_small && cur_size + gsz[g] <= kPackCap) {
+      const bool small = gsz[g] <= kPackSmall && gw[g] <= kPackSmallWeight;
+      if (small && cur_small && cur_size + gsz[g] <= kPackCap && cur_w + gw[g] <= kPackCapWeight) {
         pack[g] = np - 1;
         cur_size += gsz[g];
+        cur_w += gw[g];
       } else {
         pack[g] = np++;
         cur_size = gsz[g];
+        cur_w = gw[g];
         cur_small = small;
       }
     }
