@@ -235,6 +235,14 @@ int xg_lu_schedule_info(xg_ctx *ctx, int *ordering, int *factor_top, int *solve_
  * from the next analysis; not allowed while a transient is in progress. */
 int xg_lu_set_schedule(xg_ctx *ctx, int ordering, int factor_top, int solve_top);
 
+/* Host-only analysis of a CSR pattern with values (no context, no device):
+ * the numbers xg_lu_info / xg_lu_schedule_info report after xg_lu_analyze —
+ * nnz(L+U), the ordering chosen (or forced: ordering = XG_ORDER_*, -1 =
+ * automatic), the dependency-closed groups and the top size of the factor
+ * schedule.  The counterpart of klu_analyze's statistics. */
+int xg_lu_analyze_pattern(int n, const int *row_ptr, const int *col_idx, const double *vals, int ordering,
+                          long long *nnz_lu, int *ordering_out, int *n_groups, int *n_top);
+
 /* ---- Newton + time integration driver --------------------------------------
  * Transient::doRun (N_ANP_Transient.C:739-772, 1184-1410, 3262-3325): DC
  * operating point, then OneStep (backward Euler start, trapezoid) with

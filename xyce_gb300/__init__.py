@@ -46,7 +46,7 @@ EXPORTED = [
     "xg_add_isources", "xg_add_diodes", "xg_add_mosfet1", "xg_add_bsim4", "xg_finalize", "xg_get_sizes",
     "xg_get_pattern", "xg_update_sources", "xg_update_state", "xg_load_dae_vectors",
     "xg_load_dae_matrices", "xg_lu_analyze", "xg_lu_factor", "xg_lu_solve",
-    "xg_lu_solve_noalloc", "xg_lu_set_precision", "xg_lu_info", "xg_lu_schedule_info", "xg_lu_set_schedule",
+    "xg_lu_solve_noalloc", "xg_lu_set_precision", "xg_lu_info", "xg_lu_schedule_info", "xg_lu_set_schedule", "xg_lu_analyze_pattern",
     "xg_transient", "xg_tran_start", "xg_tran_advance", "xg_tran_results", "xg_tran_end",
     "xg_tran_predictors", "xg_tran_predictor_stats", "xg_set_predictor", "xg_mlp_set", "xg_mlp_get",
     "xg_mlp_train", "xg_mlp_grad", "xg_mlp_forward",
@@ -127,6 +127,8 @@ def lib() -> C.CDLL:
     L.xg_lu_info.argtypes = [P, C.POINTER(C.c_longlong), C.POINTER(I), C.POINTER(I), C.POINTER(I)]
     L.xg_lu_schedule_info.argtypes = [P, C.POINTER(I), C.POINTER(I), C.POINTER(I)]
     L.xg_lu_set_schedule.argtypes = [P, I, I, I]
+    L.xg_lu_analyze_pattern.argtypes = [I, C.POINTER(I), C.POINTER(I), C.POINTER(C.c_double), I,
+                                        C.POINTER(C.c_longlong), C.POINTER(I), C.POINTER(I), C.POINTER(I)]
     L.xg_transient.argtypes = [P, C.POINTER(TranParams), I, ip, I, ip, dp, dp, C.POINTER(TranStats)]
     L.xg_tran_start.argtypes = [P, C.POINTER(TranParams), I, ip, I]
     L.xg_tran_advance.argtypes = [P, I]
@@ -155,6 +157,24 @@ def _ptr(t):
     if not t.is_cuda or not t.is_contiguous():
         raise ValueError("expected a contiguous CUDA tensor")
     return C.c_void_p(t.data_ptr())
+
+
+def analyze_pattern(row_ptr, col_idx, vals, ordering=-1):
+    """Host-only LU analysis of a CSR matrix (no GPU needed): nnz(L+U), the
+    ordering ('nested_dissection' / 'min_degree'), the factor schedule's
+    dependency-closed groups and top size."""
+    rp = np.ascontiguousarray(row_ptr, np.int32)
+    ci = np.ascontiguousarray(col_idx, np.int32)
+    v = np.ascontiguousarray(vals, np.float64)
+    nnz, o, g, t = C.c_longlong(), C.c_int(), C.c_int(), C.c_int()
+    rc = lib().xg_lu_analyze_pattern(len(rp) - 1, rp.ctypes.data_as(C.POINTER(C.c_int)),
+                                     ci.ctypes.data_as(C.POINTER(C.c_int)),
+                                     v.ctypes.data_as(C.POINTER(C.c_double)), int(ordering),
+                                     C.byref(nnz), C.byref(o), C.byref(g), C.byref(t))
+    if rc != 0:
+        raise XgError(rc, f"xg_lu_analyze_pattern failed ({rc})")
+    return dict(nnz_lu=nnz.value, ordering="min_degree" if o.value == 1 else "nested_dissection",
+                n_groups=g.value, n_top=t.value)
 
 
 class Circuit:

@@ -979,6 +979,29 @@ int xg_lu_set_schedule(xg_ctx *ctx, int ordering, int factor_top, int solve_top)
   return XG_OK;
 }
 
+int xg_lu_analyze_pattern(int n, const int *row_ptr, const int *col_idx, const double *vals, int ordering,
+                          long long *nnz_lu, int *ordering_out, int *n_groups, int *n_top) {
+  if (n <= 0 || !row_ptr || !col_idx || !vals) return XG_ERR_ARG;
+  if (ordering < -1 || ordering > XG_ORDER_MIN_DEGREE) return XG_ERR_ARG;
+  const int nnz = row_ptr[n];
+  if (row_ptr[0] != 0 || nnz < 0) return XG_ERR_ARG;
+  for (int i = 0; i < n; ++i)
+    if (row_ptr[i + 1] < row_ptr[i]) return XG_ERR_ARG;
+  for (int p = 0; p < nnz; ++p)
+    if (col_idx[p] < 0 || col_idx[p] >= n) return XG_ERR_ARG;
+  std::vector<int> rp(row_ptr, row_ptr + n + 1), ci(col_idx, col_idx + nnz);
+  std::vector<double> v(vals, vals + nnz);
+  LUHost H;
+  std::string err;
+  const int rc = lu_analyze_host(n, rp, ci, v, H, err, ordering);
+  if (rc != XG_OK) return rc;
+  if (nnz_lu) *nnz_lu = (long long)H.ri.size();
+  if (ordering_out) *ordering_out = H.ordering;
+  if (n_groups) *n_groups = H.fsched.n_groups;
+  if (n_top) *n_top = H.fsched.n_top_items;
+  return XG_OK;
+}
+
 int xg_lu_info(xg_ctx *ctx, long long *nnz_lu, int *fl, int *ll, int *ul) {
   if (!ctx) return XG_ERR_ARG;
   if (!ctx->lu_ready) return fail(ctx, XG_ERR_STATE, "no LU analysis");
