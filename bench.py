@@ -356,10 +356,11 @@ def run_ours(args):
     else:
         ms_max, steps_all, evals_all = ms_total, float(steps_done), float(evals)
     value = steps_all / (ms_max / 1e3)
-    # kernels per tick: sources, MOSFET, assembly (+2 long-gather pre-passes when
-    # present), Newton control, factor (hub/groups/top), L/U solves, update,
-    # step control, history, state commit, completion count
-    kernels_per_tick = 12 + 3 + 6
+    # kernels per tick: the kernel nodes of the captured tick graph (sources,
+    # device evaluation, assembly and long-gather passes, Newton control, LU
+    # factor and solves, update, step control, history, state commit,
+    # completion count), replayed once per tick
+    kernels_per_tick = int(st1.get("kernels_per_tick", 0))
     gpu_launches = int(ticks * kernels_per_tick)
     circ.tran_end()
 
@@ -419,7 +420,7 @@ def run_ours(args):
                 "config": config,
                 "device_evals_per_s": evals_all / (ms_max / 1e3),
                 "newton_iters_per_step": (st1["newton_iters"] - st0["newton_iters"]) / max(1, steps_done),
-                "ticks": ticks, "gpu_launches": gpu_launches,
+                "ticks": ticks, "kernels_per_tick": kernels_per_tick, "gpu_launches": gpu_launches,
                 "lu": info, "roofline": roof, "forms": forms, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks}
         print(json.dumps(line), flush=True)

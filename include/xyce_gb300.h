@@ -271,6 +271,7 @@ typedef struct xg_tran_stats {
   int n_analyze;                               /* symbolic (re)analyses performed */
   double t_final_min, t_final_max;
   double seconds;                              /* wall time of the run */
+  int kernels_per_tick;                        /* kernel launches of one tick (its CUDA graph) */
 } xg_tran_stats;
 
 /* Runs the transient.  probes: global unknown indices to record; every

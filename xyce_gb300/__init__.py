@@ -75,7 +75,7 @@ class TranStats(C.Structure):
                 ("lte_fail", C.c_longlong), ("dcop_iters", C.c_longlong),
                 ("ticks", C.c_longlong), ("device_evals", C.c_longlong), ("status", C.c_int),
                 ("n_analyze", C.c_int), ("t_final_min", C.c_double),
-                ("t_final_max", C.c_double), ("seconds", C.c_double)]
+                ("t_final_max", C.c_double), ("seconds", C.c_double), ("kernels_per_tick", C.c_int)]
 
 
 _lib = None

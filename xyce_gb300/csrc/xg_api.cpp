@@ -804,6 +804,19 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
   }
   L.ordering = H.ordering;
   for (int w = 0; w < 2; ++w) {
+    const Schedule &S = w ? H.lsched : H.fsched;
+    std::vector<int> gc(std::max(1, S.n_groups), -1);
+    for (int g = 0; g < S.n_groups; ++g) {
+      int c = -2;
+      for (int t = S.lvl_ptr[S.grp_lvl[g]]; t < S.lvl_ptr[S.grp_lvl[g + 1]] && c != -1; ++t) {
+        const int ct = cstep[S.items[t]];
+        c = (c == -2 || c == ct) ? ct : -1;
+      }
+      gc[g] = c < 0 ? -1 : c;
+    }
+    if ((rc = dev_upload(ctx, w ? &L.ls_gcirc : &L.fs_gcirc, gc, A))) return rc;
+  }
+  for (int w = 0; w < 2; ++w) {
     const std::vector<int> &gb = w ? H.us_gbytes : H.ls_gbytes;
     int mx = 0;
     for (int b : gb) mx = std::max(mx, b);
@@ -1038,6 +1051,7 @@ struct TranRun {
   std::vector<void *> allocs;
   std::vector<int> pcount;
   long long ticks = 0;
+  int kernels_per_tick = 0;  // kernel nodes of the captured tick graph
   int batch = 4;
   std::chrono::steady_clock::time_point t0;
   ~TranRun() {
@@ -1087,6 +1101,21 @@ int capture(TranRun &R) {
   launch_back(R);
   launch_count_done_k(ctx->stream, ctx->d, ctx->ncirc, ctx->breakdown_dev, ctx->status_dev);
   CK(cudaStreamEndCapture(ctx->stream, &g));
+  // kernels of one tick (every node of the captured tick is a kernel launch
+  // unless the query says otherwise)
+  {
+    size_t nn = 0;
+    R.kernels_per_tick = 0;
+    if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess && nn > 0) {
+      std::vector<cudaGraphNode_t> nodes(nn);
+      if (cudaGraphGetNodes(g, nodes.data(), &nn) == cudaSuccess)
+        for (size_t k = 0; k < nn; ++k) {
+          cudaGraphNodeType ty;
+          if (cudaGraphNodeGetType(nodes[k], &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel)
+            R.kernels_per_tick++;
+        }
+    }
+  }
   cudaError_t e = cudaGraphInstantiate(&R.exec, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(ctx, XG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
@@ -1297,6 +1326,7 @@ extern "C" int xg_tran_results(xg_ctx *ctx, int *counts, double *times, double *
       evals += (long long)ctx->inst_of_circ[c] * passes;
     }
     stats->ticks = R.ticks;
+    stats->kernels_per_tick = R.kernels_per_tick;
     stats->device_evals = evals;
     stats->n_analyze = ctx->n_analyze;
     stats->status = status;

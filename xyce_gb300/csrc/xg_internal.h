@@ -274,6 +274,9 @@ struct LUDev {
   int grp_fit[2] = {0, 0};
   int fs_threads = 512, ls_threads = 512, us_threads = 512;  // CTA sizes of the group sweeps
   int ordering = 0;  // XG_ORDER_* of the analysis
+  // circuit of every factor / L-solve group (-1: a packed group mixing
+  // circuits): an inactive circuit's group returns before staging anything
+  int *fs_gcirc = nullptr, *ls_gcirc = nullptr;
   // solve groups staged in shared memory (see LUHost::ls_eptr); *_smem =
   // buffer bytes of the largest staged group (0: none staged)
   int *ls_eptr = nullptr, *ls_epos = nullptr, *ls_esrc = nullptr, *ls_gbytes = nullptr;

@@ -41,6 +41,17 @@ __device__ __forceinline__ bool item_active(const LUDev &L, const CircState *cs,
   return s.need_solve && !s.singular && (s.phase == PH_DC || s.phase == PH_TRAN);
 }
 
+// A group of one circuit that has no LU work this tick returns at once
+// (before staging anything); packed groups (gcirc < 0) test their items.
+__device__ __forceinline__ bool group_idle(const LUDev &L, const CircState *cs, int masked, const int *gcirc,
+                                          int g) {
+  if (!masked || !gcirc) return false;
+  const int c = gcirc[g];
+  if (c < 0) return false;
+  const CircState &s = cs[c];
+  return !(s.need_solve && !s.singular && (s.phase == PH_DC || s.phase == PH_TRAN));
+}
+
 template <bool BLOCK>
 __device__ __forceinline__ void team_sync() {
   if (BLOCK) __syncthreads();
@@ -299,6 +310,7 @@ template <typename T>
 __global__ void __launch_bounds__(1024) k_factor_groups(LUDev L, const double *__restrict__ vals, CircState *cs,
                                                         int masked, double pivot_tol, int top) {
   __shared__ double sm[32];
+  if (!top && group_idle(L, cs, masked, L.fs_gcirc, (int)blockIdx.x)) return;
   factor_group<T>(L, vals, cs, masked, pivot_tol, sm, top ? L.fs.n_groups : (int)blockIdx.x);
 }
 
@@ -548,6 +560,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
   __shared__ double sm[32];
   const SchedDev &SD = L.fs;
   const int g = blockIdx.x;
+  if (group_idle(L, cs, masked, L.fs_gcirc, g)) return;
   if (L.grp_snz[g] > cap) {  // too large for the buffer: factor in place in global memory
     factor_group<T>(L, vals, cs, masked, pivot_tol, sm, g);
     return;
@@ -714,6 +727,7 @@ template <typename T>
 __global__ void __launch_bounds__(kGroupThreads) k_lsolve_groups(LUDev L, const double *__restrict__ b,
                                                                   const CircState *cs, int masked, int top) {
   __shared__ double sm[32];
+  if (!top && group_idle(L, cs, masked, L.ls_gcirc, (int)blockIdx.x)) return;
   lsolve_group<T>(L, b, cs, masked, top ? L.ls.n_groups : (int)blockIdx.x, sm);
 }
 
@@ -728,6 +742,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_lsolve_groups_s(LUDev L, cons
   __shared__ double sm[32];
   const SchedDev &S = L.ls;
   const int g = blockIdx.x;
+  if (group_idle(L, cs, masked, L.ls_gcirc, g)) return;
   if (L.ls_gbytes[g] == 0) {
     lsolve_group<T>(L, b, cs, masked, g, sm);
     return;
@@ -828,6 +843,7 @@ template <typename T, bool ACC>
 __global__ void __launch_bounds__(kGroupThreads) k_usolve_groups(LUDev L, double *__restrict__ x,
                                                                   const CircState *cs, int masked, int top) {
   __shared__ double sm[32];
+  if (!top && group_idle(L, cs, masked, L.fs_gcirc, (int)blockIdx.x)) return;
   usolve_group<T, ACC>(L, x, cs, masked, top ? L.fs.n_groups : (int)blockIdx.x, sm);
 }
 
@@ -841,6 +857,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_usolve_groups_s(LUDev L, doub
   __shared__ double sm[32];
   const SchedDev &S = L.fs;
   const int g = blockIdx.x;
+  if (group_idle(L, cs, masked, L.fs_gcirc, g)) return;
   if (L.us_gbytes[g] == 0) {
     usolve_group<T, ACC>(L, x, cs, masked, g, sm);
     return;
