@@ -7,18 +7,26 @@
 // on a grouped schedule:
 //   hubs   — items without dependencies that many others need (e.g. a supply
 //            node's column), one CTA each;
-//   groups — dependency-closed sets of columns/rows, one CTA each, a CTA
-//            barrier between local levels (e.g. one ring of a Monte-Carlo
-//            batch is one group: its whole factorization stays in one CTA);
-//   top    — what remains (the upper separators of the nested dissection),
-//            one 1024-thread CTA.
+//   groups — dependency-closed sets of columns/rows, one CTA each (64-512
+//            threads, chosen by the analysis), a CTA barrier between local
+//            levels (one ring of a Monte-Carlo batch is one group: its whole
+//            factorization stays in one CTA).  A group's values — and, where
+//            that costs no residency, its update metadata — are staged in
+//            shared memory, walked there and written back once; solve groups
+//            stage their rows' entries and their slice of y.  A group whose
+//            circuit has no LU work this tick returns at once;
+//   top    — what remains (the upper separators): pulled in parallel, then
+//            factored right-looking in one CTA or a launch pair per level.
 // Factorization is left-looking per column: load A'(:,j); for each U(k,j), k
 // ascending: col_j -= L(:,k) U(k,j); threshold test of the diagonal against
 // the updated column (kRuntimePivotTol; failures raise a breakdown flag and
-// the host re-pivots); L(:,j) /= U(j,j).  Short columns use a warp, long ones
-// the whole CTA.  The solves are row-oriented gathers (no atomics): 8 lanes
-// per row, the whole CTA for long rows.  The U solve runs the factorization
-// schedule backwards (its dependency graph is the factor graph reversed).
+// the host re-pivots); L(:,j) /= U(j,j).  Short columns run on one thread
+// each when many groups run at once (GB300's FP64 pipe issues a warp-wide
+// instruction at the same cost with 1 or 32 active lanes), else on a warp;
+// long ones use the whole CTA.  Zero tests and pivot maxima run on the
+// integer pipe.  The solves are row-oriented gathers (no atomics): a thread
+// per short row, 8 lanes or the whole CTA for longer ones.  The U solve runs
+// the factorization schedule backwards.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -612,29 +620,29 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
       __syncthreads();
     }
   } else {
-  for (int lv = SD.grp_lvl[g]; lv < SD.grp_lvl[g + 1]; ++lv) {
-    const int b = SD.lvl_ptr[lv], e = SD.lvl_ptr[lv + 1];
-    bool any_long = false;
-    for (int t = b + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
-      const int j = SD.items[t];
-      if (SD.is_thread[j] && item_active(L, cs, masked, j))
-        factor_column_t<T>(L, vals, j, cs, masked, pivot_tol, S);
-    }
-    for (int t = b + warp; t < e; t += nwarps) {
-      const int j = SD.items[t];
-      if (SD.is_long[j]) { any_long = true; continue; }
-      if (SD.is_thread[j] || !item_active(L, cs, masked, j)) continue;
-      factor_column_s<false, T>(L, j, cs, masked, pivot_tol, sm, S);
-    }
-    if (__syncthreads_or(any_long)) {
-      for (int t = b; t < e; ++t) {
+    for (int lv = SD.grp_lvl[g]; lv < SD.grp_lvl[g + 1]; ++lv) {
+      const int b = SD.lvl_ptr[lv], e = SD.lvl_ptr[lv + 1];
+      bool any_long = false;
+      for (int t = b + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
         const int j = SD.items[t];
-        if (!SD.is_long[j] || !item_active(L, cs, masked, j)) continue;
-        factor_column_s<true, T>(L, j, cs, masked, pivot_tol, sm, S);
-        __syncthreads();
+        if (SD.is_thread[j] && item_active(L, cs, masked, j))
+          factor_column_t<T>(L, vals, j, cs, masked, pivot_tol, S);
+      }
+      for (int t = b + warp; t < e; t += nwarps) {
+        const int j = SD.items[t];
+        if (SD.is_long[j]) { any_long = true; continue; }
+        if (SD.is_thread[j] || !item_active(L, cs, masked, j)) continue;
+        factor_column_s<false, T>(L, j, cs, masked, pivot_tol, sm, S);
+      }
+      if (__syncthreads_or(any_long)) {
+        for (int t = b; t < e; ++t) {
+          const int j = SD.items[t];
+          if (!SD.is_long[j] || !item_active(L, cs, masked, j)) continue;
+          factor_column_s<true, T>(L, j, cs, masked, pivot_tol, sm, S);
+          __syncthreads();
+        }
       }
     }
-  }
   }
   __syncthreads();
   // write the factored columns back (the solves and the top read them)
