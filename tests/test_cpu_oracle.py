@@ -264,3 +264,35 @@ def test_gear_ring_oscillates(oracle_mod):
     assert st["status"] == 0
     late = v[t > 5e-9, 0]
     assert late.max() > 1.5 and late.min() < 0.3
+
+
+# ---- failure paths (injected on the host: no GPU fault) ----------------------
+
+def test_nan_parameter_fails_operating_point_with_nan_code(oracle_mod):
+    """A NaN element value makes the residual NaN: DampedNewton's nanFail
+    (-6, N_NLS_DampedNewton.C:1207-1253) ends the operating point, reported
+    as -100 + code."""
+    nl = N.rc_step()
+    a, b, _ = nl.res[0]
+    nl.res[0] = (a, b, float("nan"))
+    t, v, st = oracle_mod.Oracle(nl).transient(probes=[nl.names["out"]])
+    assert st["status"] == -106 and st["accepted"] == 0
+
+
+def test_one_newton_step_limit_fails_the_ring(oracle_mod):
+    """NONLIN-TRAN MAXSTEP=1 on a switching ring: Newton fails on the
+    switching steps, each failure cuts the step by 8 and after 15
+    consecutive failures the transient stops (status -1)."""
+    nl = N.ring_oscillator(21, caps=True)
+    nl.tran.nl_maxstep = 1
+    t, v, st = oracle_mod.Oracle(nl).transient(probes=[nl.names["n1"]])
+    assert st["status"] == -1
+    assert st["newton_fail"] > 0 and st["rejected"] >= st["newton_fail"]
+    assert st["t_final"] < nl.tran.tstop
+
+
+def test_linear_circuit_converges_in_one_newton_step(oracle_mod):
+    nl = N.rc_step()
+    nl.tran.nl_maxstep = 1
+    t, v, st = oracle_mod.Oracle(nl).transient(probes=[nl.names["out"]])
+    assert st["status"] == 0 and st["newton_fail"] == 0
