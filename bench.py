@@ -38,6 +38,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -332,8 +333,8 @@ def run_ours(args):
         print(json.dumps(_roofline(xg, circ, nl, dev, flush, stream_of, hbm_peak, peak_kind, args)), flush=True)
         circ.close()
         return
-    clk_path = os.path.join(HERE, "gpurun_out", f"clocks_rank{rank}.csv") \
-        if os.path.isdir(os.path.join(HERE, "gpurun_out")) else f"/tmp/xg_clocks_{os.getpid()}.csv"
+    clk_path = (f"{args.clocks_csv}.rank{rank}" if world > 1 else args.clocks_csv) if args.clocks_csv \
+        else os.path.join(tempfile.gettempdir(), f"xg_clocks_{os.getpid()}.csv")
     sampler = _clock_sampler(clk_path)
     if world > 1:
         torch.distributed.barrier()
@@ -441,6 +442,8 @@ def main():
     ap.add_argument("--roofline-only", action="store_true",
                     help="only the k_mos1 roofline launches (the profiling case of that kernel)")
     ap.add_argument("--no-forms", dest="forms", action="store_false", help="skip the FP32-IR form")
+    ap.add_argument("--clocks-csv", default=None,
+                    help="keep the nvidia-smi clock samples of the timed region in this file")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

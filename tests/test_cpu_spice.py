@@ -7,7 +7,7 @@ import pytest
 from xyce_gb300 import netlist as N
 from xyce_gb300 import spice as S
 
-REF_TESTS = "/root/reference/test/CircuitPKG"  # read only when present (this container)
+REF_TESTS = "/root/reference/test/CircuitPKG"  # the reference checkout, read only when present
 
 
 @pytest.mark.parametrize("tok,val", [

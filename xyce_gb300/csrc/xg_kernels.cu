@@ -1165,7 +1165,7 @@ __global__ void k_state_commit(DevArrays d, int nm, int nd, int sto_base_m, int 
 }
 
 // Number of finished circuits (done or failed) and the LU breakdown flag,
-// into mapped host memory read by the driver between tick batches.
+// into mapped host memory that the host loop reads between tick batches.
 __global__ void k_count_done(DevArrays d, int ncirc, const int *breakdown, int *status_out) {
   __shared__ int cnt;
   if (threadIdx.x == 0) cnt = 0;
