@@ -172,3 +172,64 @@ def test_timeint_method(opt, method, order):
     d = S.parse(f"t\nR1 a 0 1\nC1 a 0 1n\nI1 0 a PULSE(0 1m 1n)\n.TRAN 1n 1u\n.OPTIONS TIMEINT {opt}\n.END\n"
                 if opt else "t\nR1 a 0 1\n.TRAN 1n 1u\n.END\n")
     assert d.netlist.tran.method == method and d.netlist.tran.max_order == order
+
+
+def test_nested_subcircuits_and_diode_model():
+    d = S.parse("""nested subcircuits
+.SUBCKT LEAF a b
+R1 a m 1k
+D1 m b dmod 2
+.ENDS
+.SUBCKT PAIR x y
+XL1 x mid LEAF
+XL2 mid y LEAF
+.ENDS
+.MODEL dmod D (IS=1e-14 N=1.5 CJ0=1p)
+X1 in 0 PAIR
+V1 in 0 PWL(0 0 1n 1 2n 0)
+.TRAN 10p 2n
+.END
+""")
+    nl = d.netlist
+    assert len(nl.res) == 2 and len(nl.diode) == 2
+    # internal nodes are prefixed by the instance path
+    assert {"X1:MID", "X1:XL1:M", "X1:XL2:M"} <= set(nl.names)
+    row = nl.diode[0][3]
+    f = N.DIODE_FIELDS.index
+    assert row[f("IS")] == 1e-14 and row[f("N")] == 1.5 and row[f("CJO")] == 1e-12 and row[f("AREA")] == 2.0
+    # the diode of XL2 ends on ground (PAIR's y = 0)
+    assert nl.diode[1][1] == -1
+
+
+def test_bsim4_model_card_and_instance():
+    d = S.parse("""bsim4 inverter
+.MODEL n1 NMOS (LEVEL=54 VERSION=4.8.2 TOXE=1.8n VTH0=0.4)
+.MODEL p1 PMOS (LEVEL=54 TOXE=1.8n VTH0=-0.4)
+VDD vdd 0 1.0
+VIN in 0 PULSE(0 1 10p 20p 20p 100p 240p)
+MN out in 0 0 n1 L=45n W=90n
+MP out in vdd vdd p1 L=45n W=180n
+C1 out 0 2f
+.TRAN 1p 500p
+.END
+""")
+    nl = d.netlist
+    assert len(nl.bsim4) == 2 and not nl.mos1
+    f = N.B4_FIELDS.index
+    rn, rp = nl.bsim4[0][4], nl.bsim4[1][4]
+    assert rn[f("TYPE")] == 1 and rp[f("TYPE")] == -1
+    assert rn[f("TOXE")] == 1.8e-9 and rn[f("VTH0")] == 0.4 and rp[f("VTH0")] == -0.4
+    assert rn[f("L")] == 45e-9 and rp[f("W")] == 180e-9
+    assert np.isnan(rn[f("K1")])  # not given: derived by the model as the reference does
+
+
+def test_dollar_comments_and_ac_spec_ignored():
+    d = S.parse("t\nV1 a 0 DC 2 AC 1 0 $ a comment\nR1 a 0 1k ; another\n.TRAN 1n 1u\n.END\n")
+    a = d.netlist.arrays()
+    assert a["vsrc"][3][0] == N.WAVE_DC and a["vsrc"][5][0] == 2.0
+
+
+def test_print_of_unknown_node_raises():
+    d = S.parse("t\nR1 a 0 1k\nI1 0 a 1m\n.TRAN 1n 1u\n.PRINT TRAN V(b)\n.END\n")
+    with pytest.raises(ValueError, match="unknown node"):
+        S._var_probes(d, "V(B)")
