@@ -48,7 +48,7 @@ def build(verbose: bool = False, ptxas_verbose: bool = False) -> str:
     for f in CPP:
         src = os.path.join(CSRC, f)
         obj = os.path.join(OUT, f + ".o")
-        cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function",
+        cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-pthread", "-Wall", "-Wno-unused-function",
                f"-I{CUDA}/include", "-c", src, "-o", obj]
         if _needs(obj, [src, *hdrs]):
             jobs.append(cmd)
@@ -65,7 +65,7 @@ def build(verbose: bool = False, ptxas_verbose: bool = False) -> str:
                 raise RuntimeError("build failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
     objs = [os.path.join(OUT, f + ".o") for f in CU + CPP]
     if _needs(LIB, objs):
-        cmd = [NVCC, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+        cmd = [NVCC, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: " + r.stdout + r.stderr)

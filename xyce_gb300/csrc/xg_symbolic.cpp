@@ -22,8 +22,10 @@
 #include <functional>
 #include <map>
 #include <numeric>
+#include <atomic>
 #include <deque>
 #include <queue>
+#include <thread>
 
 #include "xg_internal.h"
 
@@ -361,6 +363,26 @@ OrderCost order_cost(const std::vector<std::vector<int>> &adj, const std::vector
   return c;
 }
 
+// Runs body(0 .. count-1) on up to hardware_concurrency() threads, items
+// handed out in order; one thread when the work (`weight`) is small.  Each
+// item writes only its own results, so the outcome does not depend on the
+// thread count.
+void parallel_for(size_t count, long long weight, const std::function<void(size_t)> &body) {
+  unsigned nt = std::thread::hardware_concurrency();
+  nt = std::max(1u, std::min({nt, 32u, (unsigned)count}));
+  if (nt == 1 || weight < 20000) {
+    for (size_t i = 0; i < count; ++i) body(i);
+    return;
+  }
+  std::atomic<size_t> next{0};
+  std::vector<std::thread> pool;
+  for (unsigned t = 0; t < nt; ++t)
+    pool.emplace_back([&] {
+      for (size_t i = next++; i < count; i = next++) body(i);
+    });
+  for (auto &th : pool) th.join();
+}
+
 }  // namespace
 
 int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &ci,
@@ -426,37 +448,62 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
     // Per connected component (each circuit of a batch orders exactly as it
     // would alone): nested dissection keeps the dependency chains short
     // (levels run in parallel), minimum degree keeps the fill low; take the
-    // one with the smaller estimated refactorization time.
-    ND nd(adj, order);
-    for (int j = 0; j < n; ++j) nd.part[j] = removed[j] ? -1 : 0;
-    std::vector<int> comp_of(n, -1), scratch(n, -1), comp, ond, omd;
-    int ncomp = 0, n_md = 0;  // components, unknowns ordered by minimum degree
+    // one with the smaller estimated refactorization time.  Components are
+    // ordered on local graphs (node i = the i-th smallest unknown of the
+    // component), in parallel, and concatenated in the order of their
+    // smallest unknown.
+    std::vector<int> comp_of(n, -1), loc_of(n, -1);
+    std::vector<std::vector<int>> comps;
     for (int s0 : core) {
       if (comp_of[s0] >= 0) continue;
-      comp.assign(1, s0);
-      comp_of[s0] = ncomp;
+      const int c = (int)comps.size();
+      comps.emplace_back(1, s0);
+      std::vector<int> &comp = comps.back();
+      comp_of[s0] = c;
       for (size_t h = 0; h < comp.size(); ++h)
         for (int w : adj[comp[h]])
-          if (comp_of[w] < 0) { comp_of[w] = ncomp; comp.push_back(w); }
+          if (comp_of[w] < 0) { comp_of[w] = c; comp.push_back(w); }
       std::sort(comp.begin(), comp.end());
-      const int id = nd.next_id++;
-      for (int v : comp) nd.part[v] = id;
-      ond.clear();
-      nd.out = &ond;
-      nd.run(comp, id);
-      omd.clear();
-      min_degree(adj, comp, omd, scratch);
-      const OrderCost cnd = order_cost(adj, ond, scratch), cmd = order_cost(adj, omd, scratch);
-      const double tnd = cnd.fma / kOrderFmaRate + cnd.height * kOrderLevelTime;
-      const double tmd = cmd.fma / kOrderFmaRate + cmd.height * kOrderLevelTime;
-      const bool use_md = force_ordering >= 0 ? force_ordering == 1 : tmd < tnd;
-      out.order_fma[0] += cnd.fma; out.order_fma[1] += cmd.fma;
-      out.order_height[0] = std::max(out.order_height[0], cnd.height);
-      out.order_height[1] = std::max(out.order_height[1], cmd.height);
-      if (use_md) n_md += (int)comp.size();
-      const std::vector<int> &oc = use_md ? omd : ond;
-      order.insert(order.end(), oc.begin(), oc.end());
-      ++ncomp;
+      for (size_t i = 0; i < comp.size(); ++i) loc_of[comp[i]] = (int)i;
+    }
+    struct CompOrder {
+      std::vector<int> order;  // global unknowns
+      OrderCost cnd, cmd;
+      bool md = false;
+    };
+    std::vector<CompOrder> res(comps.size());
+    auto order_one = [&](size_t c) {
+      const std::vector<int> &comp = comps[c];
+      const int m = (int)comp.size();
+      std::vector<std::vector<int>> ladj(m);
+      for (int i = 0; i < m; ++i) {
+        ladj[i].reserve(adj[comp[i]].size());
+        for (int w : adj[comp[i]]) ladj[i].push_back(loc_of[w]);  // stays sorted
+      }
+      std::vector<int> all(m), ond, omd, scratch(m, -1);
+      std::iota(all.begin(), all.end(), 0);
+      ND nd(ladj, ond);
+      nd.run(all, 0);
+      min_degree(ladj, all, omd, scratch);
+      CompOrder &r = res[c];
+      r.cnd = order_cost(ladj, ond, scratch);
+      r.cmd = order_cost(ladj, omd, scratch);
+      const double tnd = r.cnd.fma / kOrderFmaRate + r.cnd.height * kOrderLevelTime;
+      const double tmd = r.cmd.fma / kOrderFmaRate + r.cmd.height * kOrderLevelTime;
+      r.md = force_ordering >= 0 ? force_ordering == 1 : tmd < tnd;
+      const std::vector<int> &oc = r.md ? omd : ond;
+      r.order.resize(m);
+      for (int i = 0; i < m; ++i) r.order[i] = comp[oc[i]];
+    };
+    parallel_for(comps.size(), (long long)core.size(), order_one);
+    int n_md = 0;  // unknowns ordered by minimum degree
+    for (size_t c = 0; c < comps.size(); ++c) {
+      const CompOrder &r = res[c];
+      out.order_fma[0] += r.cnd.fma; out.order_fma[1] += r.cmd.fma;
+      out.order_height[0] = std::max(out.order_height[0], r.cnd.height);
+      out.order_height[1] = std::max(out.order_height[1], r.cmd.height);
+      if (r.md) n_md += (int)r.order.size();
+      order.insert(order.end(), r.order.begin(), r.order.end());
     }
     out.ordering = (n_md * 2 > (int)core.size()) ? 1 : 0;  // the ordering of most of the core
   }
