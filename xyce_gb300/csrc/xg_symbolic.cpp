@@ -394,18 +394,24 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
   if (!match_rows(n, A, vals, row_of_col, err)) return XG_ERR_SINGULAR;
   std::vector<int> inv(n);  // A row -> M index
   for (int j = 0; j < n; ++j) inv[row_of_col[j]] = j;
-  // M = rows permuted: M row j = A row row_of_col[j].  Build M's row and column lists.
-  std::vector<std::vector<int>> mrow(n), mcol(n);
-  for (int j = 0; j < n; ++j)
-    for (int q = A.cp[j]; q < A.cp[j + 1]; ++q) {
-      int r = inv[A.ri[q]];
-      mrow[r].push_back(j);
-      mcol[j].push_back(r);
-    }
+  // M = rows permuted: M row j = A row row_of_col[j].  M's columns are A's
+  // (A.cp) with rows renumbered; M's rows as CSR, columns ascending.
+  const int annz = (int)A.ri.size();
+  std::vector<int> mcol_idx(annz), mrow_ptr(n + 1, 0), mrow_idx(annz);
+  for (int q = 0; q < annz; ++q) {
+    mcol_idx[q] = inv[A.ri[q]];
+    mrow_ptr[mcol_idx[q] + 1]++;
+  }
+  for (int r = 0; r < n; ++r) mrow_ptr[r + 1] += mrow_ptr[r];
+  {
+    std::vector<int> fill(mrow_ptr.begin(), mrow_ptr.end() - 1);
+    for (int j = 0; j < n; ++j)
+      for (int q = A.cp[j]; q < A.cp[j + 1]; ++q) mrow_idx[fill[mcol_idx[q]]++] = j;
+  }
   // singleton peeling
   std::vector<int> rowcnt(n), colcnt(n);
   std::vector<char> removed(n, 0);
-  for (int j = 0; j < n; ++j) { rowcnt[j] = (int)mrow[j].size(); colcnt[j] = (int)mcol[j].size(); }
+  for (int j = 0; j < n; ++j) { rowcnt[j] = mrow_ptr[j + 1] - mrow_ptr[j]; colcnt[j] = A.cp[j + 1] - A.cp[j]; }
   std::vector<int> front, back;
   std::deque<std::pair<int, int>> q;
   for (int j = 0; j < n; ++j) {
@@ -414,10 +420,14 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
   }
   auto remove = [&](int j) {
     removed[j] = 1;
-    for (int r : mcol[j])
+    for (int t = A.cp[j]; t < A.cp[j + 1]; ++t) {
+      const int r = mcol_idx[t];
       if (r != j && !removed[r] && --rowcnt[r] == 1) q.push_back({r, 0});
-    for (int c : mrow[j])
+    }
+    for (int t = mrow_ptr[j]; t < mrow_ptr[j + 1]; ++t) {
+      const int c = mrow_idx[t];
       if (c != j && !removed[c] && --colcnt[c] == 1) q.push_back({c, 1});
+    }
   };
   while (!q.empty()) {
     auto [j, kind] = q.front();
@@ -430,8 +440,10 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
   std::vector<std::vector<int>> adj(n);
   for (int j = 0; j < n; ++j) {
     if (removed[j]) continue;
-    for (int c : mrow[j])
+    for (int t = mrow_ptr[j]; t < mrow_ptr[j + 1]; ++t) {
+      const int c = mrow_idx[t];
       if (c != j && !removed[c]) { adj[j].push_back(c); adj[c].push_back(j); }
+    }
   }
   std::vector<int> core;
   for (int j = 0; j < n; ++j)
@@ -520,21 +532,19 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
     out.col_of_step[p] = order[p];
     out.row_of_step[p] = row_of_col[order[p]];
   }
-  // A' = Q^T M Q columns in step indices
-  std::vector<std::vector<int>> acol(n);
-  for (int p = 0; p < n; ++p) {
-    int j = order[p];
-    for (int q2 = A.cp[j]; q2 < A.cp[j + 1]; ++q2) acol[p].push_back(qinv[inv[A.ri[q2]]]);
-  }
-  // Gilbert-Peierls symbolic: pattern of column p = reach of A'(:,p) through L.
-  std::vector<std::vector<int>> Lcol(n);  // rows > k of each finished column
+  // Gilbert-Peierls symbolic: pattern of column p = reach of A'(:,p) through
+  // L, A' = Q^T M Q (column p of A' = column order[p] of A, rows in step
+  // indices); the L part of a finished column k is out.ri[diag[k]+1 ..
+  // cp[k+1]).
   out.cp.assign(n + 1, 0);
   out.diag.assign(n, -1);
   std::vector<int> mark(n, -1), stk, pos;
   std::vector<int> colrows;
   for (int p = 0; p < n; ++p) {
     colrows.clear();
-    for (int r0 : acol[p]) {
+    const int j = order[p];
+    for (int q2 = A.cp[j]; q2 < A.cp[j + 1]; ++q2) {
+      const int r0 = qinv[inv[A.ri[q2]]];
       if (mark[r0] == p) continue;
       stk.assign(1, r0);
       mark[r0] = p;
@@ -543,8 +553,10 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
         stk.pop_back();
         colrows.push_back(r);
         if (r < p)
-          for (int i : Lcol[r])
+          for (int t = out.diag[r] + 1; t < out.cp[r + 1]; ++t) {
+            const int i = out.ri[t];
             if (mark[i] != p) { mark[i] = p; stk.push_back(i); }
+          }
       }
     }
     std::sort(colrows.begin(), colrows.end());
@@ -552,8 +564,6 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
       err = "missing structural diagonal after matching";
       return XG_ERR_SINGULAR;
     }
-    for (int r : colrows)
-      if (r > p) Lcol[p].push_back(r);
     out.ri.insert(out.ri.end(), colrows.begin(), colrows.end());
     out.cp[p + 1] = (int)out.ri.size();
     out.diag[p] = out.cp[p] + (int)(std::lower_bound(colrows.begin(), colrows.end(), p) - colrows.begin());
@@ -627,50 +637,6 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
     std::vector<int> f(ptr.begin(), ptr.end() - 1);
     for (int v = 0; v < (int)lev.size(); ++v) items[f[lev[v]]++] = v;
   };
-  // Host trial factorization with the analysis values: a column whose
-  // frozen pivot fails the threshold test even right after re-pivoting is
-  // exempt from that test on the device (re-pivoting cannot improve it; a
-  // typical case is a structurally present but zero U row).
-  out.exempt.assign(n, 0);
-  {
-    std::vector<double> lu(nnz);
-    for (int p = 0; p < n; ++p) {
-      const int p0 = out.cp[p], p1 = out.cp[p + 1], pd = out.diag[p];
-      for (int t = p0; t < p1; ++t) lu[t] = out.src[t] >= 0 ? vals[out.src[t]] : 0.0;
-      for (int t = p0; t < pd; ++t) {
-        const int k = out.ri[t];
-        const double ukj = lu[t];
-        if (ukj == 0.0) continue;
-        for (int q2 = out.diag[k] + 1; q2 < out.cp[k + 1]; ++q2) {
-          auto it = std::lower_bound(out.ri.begin() + t + 1, out.ri.begin() + p1, out.ri[q2]);
-          lu[it - out.ri.begin()] -= lu[q2] * ukj;
-        }
-      }
-      const double d = lu[pd];
-      double amax = 0.0;
-      for (int t = pd; t < p1; ++t) amax = std::max(amax, std::fabs(lu[t]));
-      if (!(std::fabs(d) >= kRuntimePivotTol * amax)) out.exempt[p] = 1;
-      if (d != 0.0)
-        for (int t = pd + 1; t < p1; ++t) lu[t] /= d;
-    }
-  }
-  // within each solve level, long rows go last: they get a whole block each
-  auto split_long = [&](const std::vector<int> &ptr, std::vector<int> &items, const std::vector<int> &rptr,
-                        std::vector<int> &nlong) {
-    nlong.assign(ptr.size() > 0 ? ptr.size() - 1 : 0, 0);
-    for (size_t l = 0; l + 1 < ptr.size(); ++l) {
-      auto b = items.begin() + ptr[l], e = items.begin() + ptr[l + 1];
-      auto mid = std::stable_partition(b, e, [&](int r) { return rptr[r + 1] - rptr[r] <= kLongSolveRow; });
-      nlong[l] = (int)(e - mid);
-    }
-  };
-  if (n > 0) {
-    buckets(flev, fmaxl, out.f_lvl_ptr, out.f_cols);
-    buckets(llev, lmax, out.l_lvl_ptr, out.l_rows);
-    buckets(ulev, umax, out.u_lvl_ptr, out.u_rows);
-    split_long(out.l_lvl_ptr, out.l_rows, out.l_ptr, out.l_long);
-    split_long(out.u_lvl_ptr, out.u_rows, out.u_ptr, out.u_long);
-  }
   // Update maps: for U entry p = (k, j), upd_off[p] .. upd_off[p+1] lists the
   // positions in column j of the rows of L(:,k), so the device factorization
   // scatters without searching.
@@ -708,17 +674,65 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
     }
     out.upd_off[nnz] = (int)w;
   }
+  // Host trial factorization with the analysis values: a column whose
+  // frozen pivot fails the threshold test even right after re-pivoting is
+  // exempt from that test on the device (re-pivoting cannot improve it; a
+  // typical case is a structurally present but zero U row).
+  out.exempt.assign(n, 0);
+  {
+    std::vector<double> lu(nnz);
+    for (int p = 0; p < n; ++p) {
+      const int p0 = out.cp[p], p1 = out.cp[p + 1], pd = out.diag[p];
+      for (int t = p0; t < p1; ++t) lu[t] = out.src[t] >= 0 ? vals[out.src[t]] : 0.0;
+      for (int t = p0; t < pd; ++t) {
+        const int k = out.ri[t];
+        const double ukj = lu[t];
+        if (ukj == 0.0) continue;
+        const int *tgt = out.upd_pos.data() + out.upd_off[t];
+        const int q0 = out.diag[k] + 1;
+        for (int q2 = q0; q2 < out.cp[k + 1]; ++q2) lu[tgt[q2 - q0]] -= lu[q2] * ukj;
+      }
+      const double d = lu[pd];
+      double amax = 0.0;
+      for (int t = pd; t < p1; ++t) amax = std::max(amax, std::fabs(lu[t]));
+      if (!(std::fabs(d) >= kRuntimePivotTol * amax)) out.exempt[p] = 1;
+      if (d != 0.0)
+        for (int t = pd + 1; t < p1; ++t) lu[t] /= d;
+    }
+  }
+  // within each solve level, long rows go last: they get a whole block each
+  auto split_long = [&](const std::vector<int> &ptr, std::vector<int> &items, const std::vector<int> &rptr,
+                        std::vector<int> &nlong) {
+    nlong.assign(ptr.size() > 0 ? ptr.size() - 1 : 0, 0);
+    for (size_t l = 0; l + 1 < ptr.size(); ++l) {
+      auto b = items.begin() + ptr[l], e = items.begin() + ptr[l + 1];
+      auto mid = std::stable_partition(b, e, [&](int r) { return rptr[r + 1] - rptr[r] <= kLongSolveRow; });
+      nlong[l] = (int)(e - mid);
+    }
+  };
+  if (n > 0) {
+    buckets(flev, fmaxl, out.f_lvl_ptr, out.f_cols);
+    buckets(llev, lmax, out.l_lvl_ptr, out.l_rows);
+    buckets(ulev, umax, out.u_lvl_ptr, out.u_rows);
+    split_long(out.l_lvl_ptr, out.l_rows, out.l_ptr, out.l_long);
+    split_long(out.u_lvl_ptr, out.u_rows, out.u_ptr, out.u_long);
+  }
   // Grouped schedules: factorization (deps = U-part rows of each column) and
   // L solve (deps = L-row columns); the U solve runs the factor schedule backwards.
-  out.fsched = build_schedule(
-      n, [&](int j, std::vector<int> &d) { for (int t = out.cp[j]; t < out.diag[j]; ++t) d.push_back(out.ri[t]); },
-      [&](int j) { return (out.cp[j + 1] - out.diag[j] - 1) > kLongColumn || (out.diag[j] - out.cp[j]) > kLongColumn; },
-      [&](int j) { return (out.u_ptr[j + 1] - out.u_ptr[j]) > kLongSolveRow; },
-      [&](int j) { return out.cp[j + 1] - out.cp[j] + out.u_ptr[j + 1] - out.u_ptr[j]; });
-  out.lsched = build_schedule(
-      n, [&](int i, std::vector<int> &d) { for (int t = out.l_ptr[i]; t < out.l_ptr[i + 1]; ++t) d.push_back(out.l_col[t]); },
-      [&](int i) { return (out.l_ptr[i + 1] - out.l_ptr[i]) > kLongSolveRow; }, nullptr,
-      [&](int i) { return out.l_ptr[i + 1] - out.l_ptr[i] + 1; });
+  // (the two are independent: built on two threads)
+  parallel_for(2, (long long)n, [&](size_t w) {
+    if (w == 0)
+      out.fsched = build_schedule(
+          n, [&](int j, std::vector<int> &d) { for (int t = out.cp[j]; t < out.diag[j]; ++t) d.push_back(out.ri[t]); },
+          [&](int j) { return (out.cp[j + 1] - out.diag[j] - 1) > kLongColumn || (out.diag[j] - out.cp[j]) > kLongColumn; },
+          [&](int j) { return (out.u_ptr[j + 1] - out.u_ptr[j]) > kLongSolveRow; },
+          [&](int j) { return out.cp[j + 1] - out.cp[j] + out.u_ptr[j + 1] - out.u_ptr[j]; });
+    else
+      out.lsched = build_schedule(
+          n, [&](int i, std::vector<int> &d) { for (int t = out.l_ptr[i]; t < out.l_ptr[i + 1]; ++t) d.push_back(out.l_col[t]); },
+          [&](int i) { return (out.l_ptr[i + 1] - out.l_ptr[i]) > kLongSolveRow; }, nullptr,
+          [&](int i) { return out.l_ptr[i + 1] - out.l_ptr[i] + 1; });
+  });
   // Single-thread items: short factor columns (entries and update products),
   // short U rows (backward sweep of the factor schedule), short L rows.
   // A thread walks its column's updates one after the other (a load latency
