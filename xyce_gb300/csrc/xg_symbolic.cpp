@@ -853,52 +853,30 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
       u[2] = out.upd_off[p];
       u[3] = out.diag[k] + 1;
     }
-  // Update metadata of the factor groups staged in shared memory.
+  // Update metadata of the factor groups staged in shared memory.  Sizes
+  // first (per group: column records, U entries, update targets); the
+  // arrays are built only when some group stages them.
   {
     const Schedule &S = out.fsched;
     const int ni = (int)S.items.size();
-    out.fm_col.assign((size_t)4 * ni, 0);
-    out.fm_eptr.assign(ni + 1, 0);
-    out.fm_ent.clear();
-    out.fm_tgt.clear();
-    out.fm_tptr.assign(S.n_groups + 1, 0);
     out.fm_gbytes.assign(S.n_groups, 0);
     std::vector<int> owner(n, -1);
     for (int g = 0; g < S.n_groups; ++g)
       for (int t = S.lvl_ptr[S.grp_lvl[g]]; t < S.lvl_ptr[S.grp_lvl[g + 1]]; ++t) owner[S.items[t]] = g;
-    int t_group_lo = 0;
-    for (int t = 0; t < ni; ++t) {
-      const int j = S.items[t];
-      const int g = owner[j];
-      out.fm_eptr[t] = (int)out.fm_ent.size() / 4;
-      if (g < 0) continue;
-      if (t == S.lvl_ptr[S.grp_lvl[g]]) {
-        out.fm_tptr[g] = (int)out.fm_tgt.size();
-        t_group_lo = (int)out.fm_tgt.size();
-      }
-      int *c = &out.fm_col[(size_t)4 * t];
-      c[0] = out.grp_soff[j];
-      c[1] = out.cp[j + 1] - out.cp[j];
-      c[2] = out.diag[j] - out.cp[j];
-      c[3] = (out.u_ptr[j + 1] > out.u_ptr[j] && !out.exempt[j]) ? 1 : 0;
-      for (int p = out.cp[j]; p < out.diag[j]; ++p) {
-        const int k = out.ri[p];
-        const int nl = out.cp[k + 1] - out.diag[k] - 1;
-        out.fm_ent.push_back(owner[k] == g ? out.grp_soff[k] + (out.diag[k] + 1 - out.cp[k]) : -(out.diag[k] + 1) - 1);
-        out.fm_ent.push_back(nl);
-        out.fm_ent.push_back((int)out.fm_tgt.size() - t_group_lo);
-        out.fm_ent.push_back(p - out.cp[j]);
-        for (int q = 0; q < nl; ++q) out.fm_tgt.push_back(out.upd_pos[out.upd_off[p] + q] - out.cp[j]);
-      }
-    }
-    out.fm_eptr[ni] = (int)out.fm_ent.size() / 4;
-    out.fm_tptr[S.n_groups] = (int)out.fm_tgt.size();
     for (int g = 0; g < S.n_groups; ++g) {
       const int it0 = S.lvl_ptr[S.grp_lvl[g]], it1 = S.lvl_ptr[S.grp_lvl[g + 1]];
       bool ok = true;
-      for (int t = it0; t < it1 && ok; ++t) ok = !S.is_long[S.items[t]];
-      const long long rows = it1 - it0, ents = out.fm_eptr[it1] - out.fm_eptr[it0];
-      const long long tg = out.fm_tptr[g + 1] - out.fm_tptr[g];
+      long long ents = 0, tg = 0;
+      for (int t = it0; t < it1 && ok; ++t) {
+        const int j = S.items[t];
+        ok = !S.is_long[j];
+        ents += out.diag[j] - out.cp[j];
+        for (int p = out.cp[j]; p < out.diag[j]; ++p) {
+          const int k = out.ri[p];
+          tg += out.cp[k + 1] - out.diag[k] - 1;
+        }
+      }
+      const long long rows = it1 - it0;
       const long long meta = 16 * rows + 4 * (rows + 1) + 16 * ents + 4 * tg;
       const long long vals = ((long long)out.grp_snz[g] * 8 + 15) / 16 * 16;
       if (ok && vals + meta <= kGroupSmemBytes) out.fm_gbytes[g] = (int)((meta + 15) / 16 * 16);
@@ -917,6 +895,46 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
       return bytes > 0 ? std::min(by_threads, (long long)kSmemPerSm / bytes) : by_threads;
     };
     if (resident(mmax) < resident(vmax)) std::fill(out.fm_gbytes.begin(), out.fm_gbytes.end(), 0);
+    bool any = false;
+    for (int b2 : out.fm_gbytes) any = any || b2 > 0;
+    out.fm_col.clear();
+    out.fm_eptr.clear();
+    out.fm_ent.clear();
+    out.fm_tgt.clear();
+    out.fm_tptr.clear();
+    if (any) {
+      out.fm_col.assign((size_t)4 * ni, 0);
+      out.fm_eptr.assign(ni + 1, 0);
+      out.fm_tptr.assign(S.n_groups + 1, 0);
+      int t_group_lo = 0;
+      for (int t = 0; t < ni; ++t) {
+        const int j = S.items[t];
+        const int g = owner[j];
+        out.fm_eptr[t] = (int)out.fm_ent.size() / 4;
+        if (g < 0) continue;
+        if (t == S.lvl_ptr[S.grp_lvl[g]]) {
+          out.fm_tptr[g] = (int)out.fm_tgt.size();
+          t_group_lo = (int)out.fm_tgt.size();
+        }
+        int *c = &out.fm_col[(size_t)4 * t];
+        c[0] = out.grp_soff[j];
+        c[1] = out.cp[j + 1] - out.cp[j];
+        c[2] = out.diag[j] - out.cp[j];
+        c[3] = (out.u_ptr[j + 1] > out.u_ptr[j] && !out.exempt[j]) ? 1 : 0;
+        for (int p = out.cp[j]; p < out.diag[j]; ++p) {
+          const int k = out.ri[p];
+          const int nl = out.cp[k + 1] - out.diag[k] - 1;
+          out.fm_ent.push_back(owner[k] == g ? out.grp_soff[k] + (out.diag[k] + 1 - out.cp[k])
+                                             : -(out.diag[k] + 1) - 1);
+          out.fm_ent.push_back(nl);
+          out.fm_ent.push_back((int)out.fm_tgt.size() - t_group_lo);
+          out.fm_ent.push_back(p - out.cp[j]);
+          for (int q = 0; q < nl; ++q) out.fm_tgt.push_back(out.upd_pos[out.upd_off[p] + q] - out.cp[j]);
+        }
+      }
+      out.fm_eptr[ni] = (int)out.fm_ent.size() / 4;
+      out.fm_tptr[S.n_groups] = (int)out.fm_tgt.size();
+    }
   }
   // Can the factor schedule's top run right-looking?  The sub-tree (non-top)
   // rows k of a top column j are pulled first, in step order; that is exact
