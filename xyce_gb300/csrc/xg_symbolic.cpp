@@ -1157,10 +1157,20 @@ Schedule build_schedule(int n, const std::function<void(int, std::vector<int> &)
   S.n_hub = (int)S.items.size();
   for (int j = 0; j < n; ++j)
     if (!hub[j]) order.push_back(j);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-    if (gid[a] != gid[b]) return gid[a] < gid[b];
-    return lev[a] < lev[b];
-  });
+  // stable sort by (group, level): counting sort by level, then by group
+  {
+    int maxlev = 0;
+    for (int j : order) maxlev = std::max(maxlev, lev[j]);
+    auto counting = [&](const std::vector<int> &key, int nkeys) {
+      std::vector<int> start(nkeys + 1, 0), sorted(order.size());
+      for (int j : order) start[key[j] + 1]++;
+      for (int k = 0; k < nkeys; ++k) start[k + 1] += start[k];
+      for (int j : order) sorted[start[key[j]]++] = j;
+      order.swap(sorted);
+    };
+    counting(lev, maxlev + 1);
+    counting(gid, ng + 1);  // the top carries gid ng
+  }
   S.lvl_ptr.push_back(S.n_hub);
   S.grp_lvl.assign(ng + 2, 0);
   int cur_g = -1, cur_l = -1;
