@@ -180,14 +180,16 @@ def analyze_pattern(row_ptr, col_idx, vals, ordering=-1):
 class Circuit:
     """A netlist (or batch of circuits) resident on one GB300."""
 
-    def __init__(self, nl, device: int = 0):
+    def __init__(self, nl, device: int = 0, arrays=None):
+        """arrays: nl.arrays() when the caller already holds the flat host
+        arrays of the C-ABI (they are built from the netlist otherwise)."""
         L = lib()
         self.netlist = nl
         self.h = C.c_void_p()
         rc = L.xg_create(C.byref(self.h), device)
         if rc != XG_OK:
             raise XgError(rc, "xg_create: no usable sm_103a (GB300) device")
-        a = nl.arrays()
+        a = arrays if arrays is not None else nl.arrays()
         self._check(L.xg_set_unknowns(self.h, a["n"], len(a["offsets"]) - 1, a["offsets"]))
         p, m, v = a["res"]
         self._check(L.xg_add_resistors(self.h, len(p), p, m, v))
