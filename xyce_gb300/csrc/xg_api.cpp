@@ -336,51 +336,61 @@ int xg_finalize(xg_ctx *ctx) {
     if (!same_circuit({ctx->d_p[k], ctx->d_n[k], ctx->d_r[k]})) return fail(ctx, XG_ERR_ARG, "diode spans two circuits");
   for (int k = 0; k < nb; ++k)
     if (!same_circuit({ctx->b_d[k], ctx->b_g[k], ctx->b_s[k], ctx->b_b[k]})) return fail(ctx, XG_ERR_ARG, "BSIM4 spans two circuits");
-  // matrix stamp positions (row, col) with their slot ids; -1 for ground rows/cols
-  std::vector<std::vector<int>> rows(n);
-  auto addp = [&](int r, int c) { if (r >= 0 && c >= 0) rows[r].push_back(c); };
-  for (size_t k = 0; k < ctx->r_p.size(); ++k) {
-    int p = ctx->r_p[k], m = ctx->r_n[k];
-    addp(p, p); addp(p, m); addp(m, p); addp(m, m);
-  }
-  for (size_t k = 0; k < ctx->c_p.size(); ++k) {
-    int p = ctx->c_p[k], m = ctx->c_n[k];
-    addp(p, p); addp(p, m); addp(m, p); addp(m, m);
-  }
-  for (int k = 0; k < nv; ++k) {
-    int p = ctx->v_p[k], m = ctx->v_n[k], b = ctx->v_b[k];
-    addp(p, b); addp(m, b); addp(b, p); addp(b, m);
-  }
-  const int dpair[7][2] = {{0, 0}, {0, 2}, {1, 1}, {1, 2}, {2, 0}, {2, 1}, {2, 2}};
-  for (int k = 0; k < nd; ++k) {
-    int nn[3] = {ctx->d_p[k], ctx->d_n[k], ctx->d_r[k]};
-    for (auto &pr : dpair) addp(nn[pr[0]], nn[pr[1]]);
-  }
-  for (int k = 0; k < nm; ++k) {
-    int nn[4] = {ctx->m_d[k], ctx->m_g[k], ctx->m_s[k], ctx->m_b[k]};
-    for (int a = 0; a < 4; ++a)
-      for (int b = 0; b < 4; ++b) addp(nn[a], nn[b]);
-  }
-  for (int k = 0; k < nb; ++k) {
-    int nn[4] = {ctx->b_d[k], ctx->b_g[k], ctx->b_s[k], ctx->b_b[k]};
-    for (int a = 0; a < 4; ++a)
-      for (int b = 0; b < 4; ++b) addp(nn[a], nn[b]);
-  }
-  // node unknowns keep a diagonal entry (the operating-point gmin shunt lands
-  // there); voltage-source branch rows have none, as in the device stamps
+  // matrix stamp positions (row, col); -1 for ground rows/cols.  Every
+  // position is enumerated twice (count, then fill) into one flat array, and
+  // each row is sorted and deduplicated in place.  Node unknowns keep a
+  // diagonal entry (the operating-point gmin shunt lands there); voltage-source
+  // branch rows have none, as in the device stamps.
   std::vector<char> is_branch(n, 0);
   for (int k = 0; k < nv; ++k) is_branch[ctx->v_b[k]] = 1;
-  for (int i = 0; i < n; ++i)
-    if (!is_branch[i]) rows[i].push_back(i);
-  ctx->rp.assign(n + 1, 0);
-  ctx->ci.clear();
-  for (int i = 0; i < n; ++i) {
-    auto &r = rows[i];
-    std::sort(r.begin(), r.end());
-    r.erase(std::unique(r.begin(), r.end()), r.end());
-    ctx->ci.insert(ctx->ci.end(), r.begin(), r.end());
-    ctx->rp[i + 1] = (int)ctx->ci.size();
-    std::vector<int>().swap(r);
+  const int dpair[7][2] = {{0, 0}, {0, 2}, {1, 1}, {1, 2}, {2, 0}, {2, 1}, {2, 2}};
+  auto for_positions = [&](auto &&emit) {
+    for (size_t k = 0; k < ctx->r_p.size(); ++k) {
+      int p = ctx->r_p[k], m = ctx->r_n[k];
+      emit(p, p); emit(p, m); emit(m, p); emit(m, m);
+    }
+    for (size_t k = 0; k < ctx->c_p.size(); ++k) {
+      int p = ctx->c_p[k], m = ctx->c_n[k];
+      emit(p, p); emit(p, m); emit(m, p); emit(m, m);
+    }
+    for (int k = 0; k < nv; ++k) {
+      int p = ctx->v_p[k], m = ctx->v_n[k], b = ctx->v_b[k];
+      emit(p, b); emit(m, b); emit(b, p); emit(b, m);
+    }
+    for (int k = 0; k < nd; ++k) {
+      int nn[3] = {ctx->d_p[k], ctx->d_n[k], ctx->d_r[k]};
+      for (auto &pr : dpair) emit(nn[pr[0]], nn[pr[1]]);
+    }
+    for (int k = 0; k < nm; ++k) {
+      int nn[4] = {ctx->m_d[k], ctx->m_g[k], ctx->m_s[k], ctx->m_b[k]};
+      for (int a = 0; a < 4; ++a)
+        for (int b = 0; b < 4; ++b) emit(nn[a], nn[b]);
+    }
+    for (int k = 0; k < nb; ++k) {
+      int nn[4] = {ctx->b_d[k], ctx->b_g[k], ctx->b_s[k], ctx->b_b[k]};
+      for (int a = 0; a < 4; ++a)
+        for (int b = 0; b < 4; ++b) emit(nn[a], nn[b]);
+    }
+    for (int i = 0; i < n; ++i)
+      if (!is_branch[i]) emit(i, i);
+  };
+  {
+    std::vector<long long> cnt(n + 1, 0);
+    for_positions([&](int r, int c) { if (r >= 0 && c >= 0) cnt[r + 1]++; });
+    for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+    std::vector<int> flat(cnt[n]);
+    std::vector<long long> fill(cnt.begin(), cnt.end() - 1);
+    for_positions([&](int r, int c) { if (r >= 0 && c >= 0) flat[fill[r]++] = c; });
+    ctx->rp.assign(n + 1, 0);
+    ctx->ci.clear();
+    ctx->ci.reserve(flat.size());
+    for (int i = 0; i < n; ++i) {
+      auto b = flat.begin() + cnt[i], e = flat.begin() + cnt[i + 1];
+      std::sort(b, e);
+      e = std::unique(b, e);
+      ctx->ci.insert(ctx->ci.end(), b, e);
+      ctx->rp[i + 1] = (int)ctx->ci.size();
+    }
   }
   const int nnz = ctx->nnz = (int)ctx->ci.size();
   auto find = [&](int r, int c) -> int {
@@ -418,9 +428,15 @@ int xg_finalize(xg_ctx *ctx) {
   ctx->sM_m = 0; ctx->sM_b = kMosM * nm; ctx->sM_d = kMosM * nmb;
   const int nF = kMosF * nmb + kDioF * nd, nQ = kMosQ * nmb + kDioQ * nd, nL = kMosL * nmb + kDioL * nd;
   const int nMs = kMosM * nmb + kDioM * nd, nB = nv + 2 * ni;
-  // contribution lists (row -> slots, CSR entry -> slots)
-  std::vector<std::vector<int>> lF(n), lQ(n), lL(n), lB(n), lM(nnz);
-  auto pushv = [&](std::vector<std::vector<int>> &l, int r, int slot) { if (r >= 0) l[r].push_back(slot); };
+  // contribution lists (row -> slots, CSR entry -> slots): every push is
+  // recorded as (key, slot) in order, then a stable counting sort by key
+  // gives each row's / entry's slots in push order (the gathers sum them in
+  // that order)
+  struct Contrib {
+    std::vector<int> key, slot;
+  };
+  Contrib lF, lQ, lL, lB, lM;
+  auto pushv = [&](Contrib &l, int r, int slot) { if (r >= 0) { l.key.push_back(r); l.slot.push_back(slot); } };
   for (int k = 0; k < nm; ++k) {
     int D = ctx->m_d[k], G = ctx->m_g[k], S = ctx->m_s[k], B = ctx->m_b[k];
     pushv(lF, D, ctx->sF_m + 0 * nm + k); pushv(lF, S, ctx->sF_m + 1 * nm + k); pushv(lF, B, ctx->sF_m + 2 * nm + k);
@@ -428,10 +444,7 @@ int xg_finalize(xg_ctx *ctx) {
     for (int j = 0; j < 4; ++j) { pushv(lQ, qn[j], ctx->sQ_m + j * nm + k); pushv(lL, qn[j], ctx->sL_m + j * nm + k); }
     int nn[4] = {D, G, S, B};
     for (int a = 0; a < 4; ++a)
-      for (int b = 0; b < 4; ++b) {
-        int e = find(nn[a], nn[b]);
-        if (e >= 0) lM[e].push_back(ctx->sM_m + (4 * a + b) * nm + k);
-      }
+      for (int b = 0; b < 4; ++b) pushv(lM, find(nn[a], nn[b]), ctx->sM_m + (4 * a + b) * nm + k);
   }
   for (int k = 0; k < nb; ++k) {
     int D = ctx->b_d[k], G = ctx->b_g[k], S = ctx->b_s[k], B = ctx->b_b[k];
@@ -440,10 +453,7 @@ int xg_finalize(xg_ctx *ctx) {
     for (int j = 0; j < 4; ++j) { pushv(lQ, qn[j], ctx->sQ_b + j * nb + k); pushv(lL, qn[j], ctx->sL_b + j * nb + k); }
     int nn[4] = {D, G, S, B};
     for (int a = 0; a < 4; ++a)
-      for (int b = 0; b < 4; ++b) {
-        int e = find(nn[a], nn[b]);
-        if (e >= 0) lM[e].push_back(ctx->sM_b + (4 * a + b) * nb + k);
-      }
+      for (int b = 0; b < 4; ++b) pushv(lM, find(nn[a], nn[b]), ctx->sM_b + (4 * a + b) * nb + k);
   }
   for (int k = 0; k < nd; ++k) {
     int P = ctx->d_p[k], N = ctx->d_n[k], R = ctx->d_r[k];
@@ -452,22 +462,23 @@ int xg_finalize(xg_ctx *ctx) {
     int qn[2] = {N, R};
     for (int j = 0; j < 2; ++j) { pushv(lQ, qn[j], ctx->sQ_d + j * nd + k); pushv(lL, qn[j], ctx->sL_d + j * nd + k); }
     int nn[3] = {P, N, R};
-    for (int s = 0; s < 7; ++s) {
-      int e = find(nn[dpair[s][0]], nn[dpair[s][1]]);
-      if (e >= 0) lM[e].push_back(ctx->sM_d + s * nd + k);
-    }
+    for (int s = 0; s < 7; ++s) pushv(lM, find(nn[dpair[s][0]], nn[dpair[s][1]]), ctx->sM_d + s * nd + k);
   }
   for (int k = 0; k < nv; ++k) pushv(lB, ctx->v_b[k], k);
   for (int k = 0; k < ni; ++k) { pushv(lB, ctx->i_p[k], nv + 2 * k); pushv(lB, ctx->i_n[k], nv + 2 * k + 1); }
-  auto flatten = [&](std::vector<std::vector<int>> &l, std::vector<int> &ptr, std::vector<int> &idx) {
-    ptr.assign(l.size() + 1, 0);
-    for (size_t i = 0; i < l.size(); ++i) ptr[i + 1] = ptr[i] + (int)l[i].size();
-    idx.clear();
-    idx.reserve(ptr.back());
-    for (auto &v : l) { idx.insert(idx.end(), v.begin(), v.end()); std::vector<int>().swap(v); }
+  auto flatten = [&](Contrib &l, int nkeys, std::vector<int> &ptr, std::vector<int> &idx) {
+    ptr.assign(nkeys + 1, 0);
+    for (int k : l.key) ptr[k + 1]++;
+    for (int i = 0; i < nkeys; ++i) ptr[i + 1] += ptr[i];
+    idx.assign(l.key.size(), 0);
+    std::vector<int> f(ptr.begin(), ptr.end() - 1);
+    for (size_t t = 0; t < l.key.size(); ++t) idx[f[l.key[t]]++] = l.slot[t];
+    std::vector<int>().swap(l.key);
+    std::vector<int>().swap(l.slot);
   };
   std::vector<int> pF, iF, pQ, iQ, pL, iL, pB, iB, pM, iM;
-  flatten(lF, pF, iF); flatten(lQ, pQ, iQ); flatten(lL, pL, iL); flatten(lB, pB, iB); flatten(lM, pM, iM);
+  flatten(lF, n, pF, iF); flatten(lQ, n, pQ, iQ); flatten(lL, n, pL, iL); flatten(lB, n, pB, iB);
+  flatten(lM, nnz, pM, iM);
   // Rows and entries with long gathers (a supply node touches every PMOS) are
   // reduced by a whole block in a pre-pass instead of one thread.
   std::vector<int> long_rows, row_long(n, -1), long_ents, ent_long(nnz, -1);
