@@ -233,3 +233,78 @@ def test_print_of_unknown_node_raises():
     d = S.parse("t\nR1 a 0 1k\nI1 0 a 1m\n.TRAN 1n 1u\n.PRINT TRAN V(b)\n.END\n")
     with pytest.raises(ValueError, match="unknown node"):
         S._var_probes(d, "V(B)")
+
+
+SWEEP = """RC sweep
+.PARAM rval=1k
+V1 in 0 PULSE(0 1 1n)
+R1 in out {rval}
+C1 out 0 1n
+.TRAN 10p 2u 0 25n
+.STEP rval LIST 1k 2k 4k
+.PRINT TRAN V(out)
+.MEASURE TRAN vmax MAX V(out)
+.END
+"""
+
+
+def test_param_reference_and_step_list():
+    decks = S.parse_sweep(SWEEP)
+    assert [d.netlist.res[0][2] for d in decks] == [1e3, 2e3, 4e3]
+    assert [d.step_values for d in decks] == [{"RVAL": 1e3}, {"RVAL": 2e3}, {"RVAL": 4e3}]
+    assert decks[0].steps == [("RVAL", [1e3, 2e3, 4e3])]
+
+
+def test_nested_linear_steps_outermost_first():
+    text = SWEEP.replace(".STEP rval LIST 1k 2k 4k", ".STEP rval 1k 2k 1k\n.STEP C1 1n 3n 1n")
+    decks = S.parse_sweep(text)
+    got = [(d.netlist.res[0][2], d.netlist.cap[0][2]) for d in decks]
+    assert got == [(1e3, 1e-9), (1e3, 2e-9), (1e3, 3e-9), (2e3, 1e-9), (2e3, 2e-9), (2e3, 3e-9)]
+
+
+def test_step_of_unknown_name_raises():
+    with pytest.raises(ValueError, match="no parameter or element"):
+        S.parse_sweep(SWEEP.replace(".STEP rval", ".STEP rx"))
+    with pytest.raises(ValueError, match="unknown parameter"):
+        S.parse(SWEEP.replace("{rval}", "{nope}"))
+
+
+def test_run_sweep_splits_the_batch(monkeypatch):
+    """The sweep runs as one batch; each step gets its own circuit's rows
+    (a stand-in for the GPU transient returns per-circuit waveforms)."""
+    import xyce_gb300
+
+    class FakeCircuit:
+        def __init__(self, nl, device=0, arrays=None):
+            self.nl = nl
+
+        def transient(self, tran, probes=(), cap=0):
+            nc = len(self.nl.offsets) - 1
+            counts = np.array([3 + c for c in range(nc)], np.int32)
+            times = np.zeros((nc, cap))
+            values = np.zeros((nc, cap, 1))
+            for c in range(nc):
+                times[c, :counts[c]] = np.arange(counts[c]) * 1e-9
+                values[c, :counts[c], 0] = 10.0 * (c + 1) + np.arange(counts[c])
+            return counts, times, values, {"status": 0, "rejected": 0}
+
+        def close(self):
+            pass
+
+    monkeypatch.setattr(xyce_gb300, "Circuit", FakeCircuit)
+    decks = S.parse_sweep(SWEEP)
+    res = S.run_sweep(decks, cap=64)
+    assert [len(r.times) for r in res] == [3, 4, 5]
+    np.testing.assert_array_equal(res[1].columns["V(OUT)"], [20, 21, 22, 23])
+    assert [r.measures["VMAX"] for r in res] == [12.0, 23.0, 34.0]
+
+
+def test_sweep_prn_layout(tmp_path):
+    d = S.parse(SWEEP)
+    rs = [S.Result(np.array([0.0, 1e-9]), {"V(OUT)": np.array([0.0, 0.5 + k])}, {}, {}) for k in range(2)]
+    p = tmp_path / "s.prn"
+    S.write_prn(str(p), d, rs)
+    lines = p.read_text().splitlines()
+    assert lines[0].split() == ["Index", "TIME", "V(OUT)"]
+    assert [ln.split()[0] for ln in lines[1:-1]] == ["0", "1", "0", "1"]
+    assert lines[-1] == "End of Xyce(TM) Parameter Sweep"

@@ -374,6 +374,31 @@ def monte_carlo_rings(count=4096, min_stages=11, max_stages=301, seed=4) -> Netl
     return nl
 
 
+def batch(nls: list, label: str = "batch") -> Netlist:
+    """Independent netlists as the circuits of one batched netlist (unknowns
+    renumbered into consecutive ranges; node names prefixed "<k>:"); the
+    transient options are the first netlist's."""
+    out = Netlist(label=label)
+    for k, nl in enumerate(nls):
+        nl.end_circuit()
+        base = out.n
+
+        def sh(u, base=base):
+            return -1 if u < 0 else u + base
+        out.n += nl.n
+        out.names.update({f"{k}:{name}": i + base for name, i in nl.names.items()})
+        out.res += [(sh(a), sh(b), r) for (a, b, r) in nl.res]
+        out.cap += [(sh(a), sh(b), c) for (a, b, c) in nl.cap]
+        out.vsrc += [(sh(a), sh(b), sh(br), kd, list(d)) for (a, b, br, kd, d) in nl.vsrc]
+        out.isrc += [(sh(a), sh(b), kd, list(d)) for (a, b, kd, d) in nl.isrc]
+        out.diode += [(sh(a), sh(b), sh(p), row) for (a, b, p, row) in nl.diode]
+        out.mos1 += [(sh(d), sh(g), sh(s_), sh(b), row) for (d, g, s_, b, row) in nl.mos1]
+        out.bsim4 += [(sh(d), sh(g), sh(s_), sh(b), row) for (d, g, s_, b, row) in nl.bsim4]
+        out.offsets += [o + base for o in nl.offsets[1:]]
+    out.tran = nls[0].tran if nls else None
+    return out
+
+
 def extract_circuit(nl: Netlist, ci: int) -> Netlist:
     """Circuit ci of a batch as a netlist of its own (unknowns renumbered from
     0, ground kept at -1), with the batch's transient options."""

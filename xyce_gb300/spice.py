@@ -9,7 +9,9 @@ output.  The subset is what the path simulates:
   ``D`` (diode level 1), ``M`` (MOSFET level 1; level 54/14 = BSIM4 4.8.2),
   ``X`` (subcircuit instances, flattened);
 * ``.MODEL``, ``.SUBCKT``/``.ENDS``, ``.TRAN``, ``.OPTIONS TIMEINT``
-  (RELTOL, ABSTOL, METHOD=TRAP|GEAR, MAXORD), ``.PRINT TRAN``, ``.MEASURE TRAN`` (MAX, MIN, PP, AVG,
+  (RELTOL, ABSTOL, METHOD=TRAP|GEAR, MAXORD), ``.PARAM`` with ``{NAME}``
+  references, ``.STEP`` (linear or LIST; every point of the sweep runs as one
+  circuit of a single GPU batch), ``.PRINT TRAN``, ``.MEASURE TRAN`` (MAX, MIN, PP, AVG,
   RMS, INTEG with FROM/TO), ``.END``; ``*`` and ``;`` comments, ``+``
   continuation lines, engineering suffixes (T G MEG K M MIL U N P F);
 * print variables ``V(n)``, ``V(a,b)``, ``I(Vname)``, ``TIME``, ``TEMP``
@@ -55,16 +57,21 @@ _SUFFIX = {"t": 12, "g": 9, "meg": 6, "k": 3, "m": -3, "u": -6, "n": -9, "p": -1
 _NUM = re.compile(r"^([+-]?(?:\d+\.?\d*|\.\d+)(?:[eE][+-]?\d+)?)(meg|mil|[tgkmunpf])?[a-z]*$", re.I)
 
 
-def number(tok: str) -> float:
-    """SPICE number with an optional engineering suffix and unit letters."""
+def _decimal(tok: str) -> Decimal:
+    """Exact decimal value of a SPICE number (engineering suffix, unit letters)."""
     m = _NUM.match(tok.strip())
     if not m:
         raise ValueError(f"not a number: {tok!r}")
     suf = (m.group(2) or "").lower()
     if suf == "mil":
-        return float(Decimal(m.group(1)) * Decimal("25.4e-6"))
-    # decimal arithmetic: "5u" is the double nearest 5e-6
-    return float(Decimal(m.group(1)).scaleb(_SUFFIX.get(suf, 0)))
+        return Decimal(m.group(1)) * Decimal("25.4e-6")
+    return Decimal(m.group(1)).scaleb(_SUFFIX.get(suf, 0))
+
+
+def number(tok: str) -> float:
+    """SPICE number with an optional engineering suffix and unit letters
+    (decimal arithmetic: "5u" is the double nearest 5e-6)."""
+    return float(_decimal(tok))
 
 
 def _is_number(tok: str) -> bool:
@@ -140,6 +147,9 @@ class Deck:
     tstep: float = 0.0
     element_values: dict[str, float] = field(default_factory=dict)
     branches: dict[str, int] = field(default_factory=dict)
+    steps: list = field(default_factory=list)        # .STEP: (name, [values]), outermost first
+    params: dict[str, float] = field(default_factory=dict)
+    step_values: dict[str, float] = field(default_factory=dict)  # this deck's point of the sweep
 
 
 _DIODE_ALIASES = {"CJ0": "CJO", "CJ": "CJO", "PB": "VJ", "MJ": "M"}
@@ -157,6 +167,21 @@ class _Builder:
         self.models: dict[str, Model] = {}
         self.subckts: dict[str, tuple[list[str], list[str]]] = {}
         self.tran = None
+        self.overrides: dict[str, float] = {}  # element name -> swept value
+
+    def subst(self, toks: list[str]) -> list[str]:
+        """{NAME} tokens -> the .PARAM value (a single parameter; no
+        expressions)."""
+        out = []
+        for t in toks:
+            if t.startswith("{") and t.endswith("}"):
+                key = t[1:-1].strip().upper()
+                if key not in self.deck.params:
+                    raise ValueError(f"unknown parameter {t}")
+                out.append(repr(self.deck.params[key]))
+            else:
+                out.append(t)
+        return out
 
     # ---- nodes ----------------------------------------------------------
     def node(self, name: str) -> int:
@@ -204,6 +229,7 @@ class _Builder:
 
     # ---- elements ---------------------------------------------------------
     def element(self, toks: list[str], prefix: str, nodemap: dict[str, str]):
+        toks = self.subst(toks)
         name = (prefix + toks[0]).upper()
         letter = toks[0][0].upper()
         pos, kv = _params(toks[1:])
@@ -220,6 +246,7 @@ class _Builder:
             if len(pos) < 3:
                 raise ValueError(f"{name}: needs two nodes and a value")
             a, b, v = nd(pos[0]), nd(pos[1]), number(pos[2])
+            v = self.overrides.get(name, v)
             (self.nl.R if letter == "R" else self.nl.C)(a, b, v)
             self.deck.element_values[name] = v
         elif letter in "VI":
@@ -227,6 +254,10 @@ class _Builder:
                 raise ValueError(f"{name}: needs two nodes")
             a, b = nd(pos[0]), nd(pos[1])
             wave = self._wave(name, toks[3:])
+            if name in self.overrides:
+                if wave[0] != "DC":
+                    raise ValueError(f".STEP of {name}: only DC sources can be stepped")
+                wave = ("DC", [self.overrides[name]])
             self._pending_sources.append((letter, name, a, b, wave))
         elif letter == "D":
             if len(pos) < 3:
@@ -290,6 +321,7 @@ class _Builder:
         return m
 
     def model(self, toks: list[str]):
+        toks = self.subst(toks)
         pos, kv = _params(toks[1:])
         if len(pos) < 2:
             raise ValueError(".MODEL needs a name and a type")
@@ -356,11 +388,29 @@ class _Builder:
                 self.nl.I(a, b, k, data)
 
 
-def parse(text: str) -> Deck:
-    """Parse a netlist (the first line is the title, as in SPICE)."""
+def parse(text: str, overrides: dict | None = None) -> Deck:
+    """Parse a netlist (the first line is the title, as in SPICE).
+    overrides: {parameter or element name: value} — one point of a .STEP
+    sweep (parse_sweep builds them)."""
     title, lines = _logical_lines(text)
     B = _Builder(title)
     B._pending_sources = []
+    # .PARAM values first (they may be referenced before their line)
+    for ln in lines:
+        toks = _tokens(ln)
+        if toks[0].upper() == ".PARAM":
+            pos, kv = _params(toks[1:])
+            if pos:
+                raise ValueError(".PARAM takes NAME=value pairs")
+            for k, v in kv.items():
+                B.deck.params[k] = number(v)
+    overrides = {k.upper(): float(v) for k, v in (overrides or {}).items()}
+    for k, v in overrides.items():
+        if k in B.deck.params:
+            B.deck.params[k] = v
+        else:
+            B.overrides[k] = v
+    B.deck.step_values = dict(overrides)
     # pass 1: subcircuit bodies and models
     body_lines = []
     cur = None
@@ -400,6 +450,12 @@ def parse(text: str) -> Deck:
         head = toks[0].upper()
         if head == ".END":
             break
+        if head in (".PARAM",):
+            continue
+        if head == ".STEP":
+            deck.steps.append(_step(toks[1:]))
+            continue
+        toks = B.subst(toks)
         if head == ".TRAN":
             pos, kv = _params(toks[1:])
             nums = [number(p) for p in pos if _is_number(p)]
@@ -444,6 +500,10 @@ def parse(text: str) -> Deck:
             B.element(toks, "", {})
     if tran is None:
         raise ValueError("no .TRAN line")
+    unknown = [k for k in B.overrides if k not in deck.element_values and k not in
+               {src[1] for src in B._pending_sources}]
+    if unknown:
+        raise ValueError(f".STEP names no parameter or element: {unknown}")
     if reltol is not None:
         tran.reltol = reltol
     if abstol is not None:
@@ -462,6 +522,100 @@ def parse(text: str) -> Deck:
 def read(path: str) -> Deck:
     with open(path) as f:
         return parse(f.read())
+
+
+def _step(toks: list[str]) -> tuple[str, list[float]]:
+    """.STEP NAME start stop step | .STEP NAME LIST v1 v2 ... (linear)."""
+    pos, kv = _params(toks)
+    if len(pos) < 2:
+        raise ValueError(".STEP needs a name and values")
+    name = pos[0].upper()
+    if pos[1].upper() == "LIST":
+        vals = [number(v) for v in pos[2:]]
+        if not vals:
+            raise ValueError(".STEP LIST needs values")
+        return name, vals
+    if pos[1].upper() in ("DEC", "OCT", "LIN"):
+        raise ValueError(f".STEP {pos[1]} sweeps are not supported (linear and LIST are)")
+    if len(pos) != 4:
+        raise ValueError(".STEP NAME start stop step")
+    a, b, st = _decimal(pos[1]), _decimal(pos[2]), _decimal(pos[3])
+    if st == 0 or (b - a) / st < 0:
+        raise ValueError(".STEP step must move from start towards stop")
+    k = int((b - a) / st) + 1  # decimal: the end point is not lost to rounding
+    return name, [float(a + i * st) for i in range(k)]
+
+
+def parse_sweep(text: str) -> list[Deck]:
+    """One deck per point of the .STEP sweep (the first .STEP line
+    outermost); a single deck without .STEP."""
+    base = parse(text)
+    if not base.steps:
+        return [base]
+    combos = [{}]
+    for name, vals in base.steps:
+        combos = [dict(c, **{name: v}) for c in combos for v in vals]
+    return [parse(text, c) for c in combos]
+
+
+def run_sweep(decks: list[Deck], device: int = 0, cap: int | None = None) -> list["Result"]:
+    """All points of a sweep as the circuits of one batch on the GPU (each
+    keeps its own step control); one Result per deck."""
+    if len(decks) == 1:
+        return [run(decks[0], device, cap)]
+    from . import Circuit
+    nl = N.batch([d.netlist for d in decks], label=decks[0].title)
+    plans, probes = [], []
+    for k, d in enumerate(decks):
+        base = nl.offsets[k]
+        wanted = list(dict.fromkeys(d.prints + [m.var for m in d.measures]))
+        local: list[int] = []
+        plan = {}
+        for var in wanted:
+            us, f = _var_probes(d, var)
+            slots = []
+            for u in us:
+                if u not in local:
+                    local.append(u)
+                slots.append(local.index(u))
+            plan[var] = (us, slots, f)
+        if not local:
+            local = [0]
+        probes += [base + u for u in local]
+        plans.append((wanted, plan))
+    if cap is None:
+        tr = nl.tran
+        hmin_guess = tr.hmax if tr.hmax > 0 else tr.tstop / 50.0
+        cap = int(min(2_000_000, max(4096, 20 * tr.tstop / max(hmin_guess, 1e-30))))
+    for _ in range(4):
+        circ = Circuit(nl, device=device)
+        try:
+            counts, times, values, stats = circ.transient(nl.tran, probes=probes, cap=cap)
+        finally:
+            circ.close()
+        if int(np.max(counts)) < cap:
+            break
+        cap *= 4
+    else:
+        raise RuntimeError(f"more than {cap} accepted steps")
+    out = []
+    for k, d in enumerate(decks):
+        n = int(counts[k])
+        out.append(_columns(d, plans[k][0], plans[k][1], times[k, :n].copy(), values[k, :n, :], stats))
+    return out
+
+
+def _columns(deck: Deck, wanted, plan, t, vals, stats) -> "Result":
+    cols = {}
+    for var in wanted:
+        us, slots, f = plan[var]
+        if var == "TIME":
+            cols[var] = t
+            continue
+        sub = {u: vals[:, s] for u, s in zip(us, slots)}
+        cols[var] = np.broadcast_to(np.asarray(f(sub), dtype=np.float64), t.shape).copy()
+    meas = {m.name: measure(m.func, t, cols[m.var], m.frm, m.to) for m in deck.measures}
+    return Result(t, cols, meas, stats)
 
 
 def _print_vars(toks: list[str]) -> list[str]:
@@ -604,25 +758,18 @@ def run(deck: Deck, device: int = 0, cap: int | None = None) -> Result:
         cap *= 4  # the waveform buffer filled up: run again with a larger one
     else:
         raise RuntimeError(f"more than {cap} accepted steps")
-    t = times[0, :n].copy()
-    vals = values[0, :n, :]
-    cols = {}
-    for var in wanted:
-        us, slots, f = plan[var]
-        if var == "TIME":
-            cols[var] = t
-            continue
-        sub = {u: vals[:, s] for u, s in zip(us, slots)}
-        col = f(sub)
-        cols[var] = np.broadcast_to(np.asarray(col, dtype=np.float64), t.shape).copy()
-    meas = {m.name: measure(m.func, t, cols[m.var], m.frm, m.to) for m in deck.measures}
-    return Result(t, cols, meas, stats)
+    return _columns(deck, wanted, plan, times[0, :n].copy(), values[0, :n, :], stats)
 
 
-def write_prn(path: str, deck: Deck, res: Result) -> None:
-    """The reference's .prn table: Index, TIME, then the .PRINT columns."""
+def write_prn(path: str, deck: Deck, res) -> None:
+    """The reference's .prn table: Index, TIME, then the .PRINT columns.
+    res: one Result, or a list of them for a .STEP sweep — then the steps
+    follow one another under one header, the Index restarting at 0 for each
+    step, and the footer reads "End of Xyce(TM) Parameter Sweep"
+    (TimePrn::doStartStep / doSteppingComplete,
+    src/IOInterfacePKG/N_IO_OutputterTimePrn.C:165-230)."""
+    results = res if isinstance(res, list) else [res]
     names = ["TIME"] + [p for p in deck.prints if p != "TIME"]
-    cols = [res.times] + [res.columns[p] for p in names[1:]]
 
     def head(name, width=17):
         if width <= len(name):
@@ -631,10 +778,13 @@ def write_prn(path: str, deck: Deck, res: Result) -> None:
         return " " * left + name + " " * (width - left - len(name))
     with open(path, "w") as f:
         f.write(" ".join(["Index"] + [head(n) for n in names]) + "\n")
-        for i in range(len(res.times)):
-            row = [f"{i:<5d}"] + [f"{c[i]:>17.9e}" for c in cols]
-            f.write(" ".join(row) + "\n")
-        f.write("End of Xyce(TM) Simulation\n")
+        for r in results:
+            cols = [r.times] + [r.columns[p] for p in names[1:]]
+            for i in range(len(r.times)):
+                row = [f"{i:<5d}"] + [f"{c[i]:>17.9e}" for c in cols]
+                f.write(" ".join(row) + "\n")
+        f.write("End of Xyce(TM) Parameter Sweep\n" if isinstance(res, list) and len(results) > 1
+                else "End of Xyce(TM) Simulation\n")
 
 
 def read_prn(path: str) -> tuple[list[str], np.ndarray]:
@@ -661,16 +811,28 @@ def main(argv=None) -> int:
         print("usage: python -m xyce_gb300.spice <netlist>", file=sys.stderr)
         return 2
     path = argv[0]
-    deck = read(path)
-    res = run(deck)
+    with open(path) as f:
+        text = f.read()
+    decks = parse_sweep(text)
+    deck = decks[0]
+    if len(decks) == 1:
+        res = run(deck)
+        if deck.prints:
+            write_prn(path + ".prn", deck, res)
+        if deck.measures:
+            write_mt0(path + ".mt0", deck, res)
+            for m in deck.measures:
+                print(f"{m.name} = {res.measures[m.name]:.6e}")
+        print(f"{len(res.times)} accepted time points, {res.stats.get('rejected', 0)} rejected; "
+              f"output {os.path.basename(path)}.prn")
+        return 0
+    results = run_sweep(decks)
     if deck.prints:
-        write_prn(path + ".prn", deck, res)
-    if deck.measures:
-        write_mt0(path + ".mt0", deck, res)
-        for m in deck.measures:
-            print(f"{m.name} = {res.measures[m.name]:.6e}")
-    print(f"{len(res.times)} accepted time points, {res.stats.get('rejected', 0)} rejected; "
-          f"output {os.path.basename(path)}.prn")
+        write_prn(path + ".prn", deck, results)
+    if deck.measures:  # one measure file per step: .mt0, .mt1, ...
+        for k, (d, r) in enumerate(zip(decks, results)):
+            write_mt0(path + f".mt{k}", d, r)
+    print(f"{len(decks)} sweep points run as one batch; output {os.path.basename(path)}.prn")
     return 0
 
 
