@@ -308,3 +308,40 @@ def test_sweep_prn_layout(tmp_path):
     assert lines[0].split() == ["Index", "TIME", "V(OUT)"]
     assert [ln.split()[0] for ln in lines[1:-1]] == ["0", "1", "0", "1"]
     assert lines[-1] == "End of Xyce(TM) Parameter Sweep"
+
+
+SAMPLING = """RC Monte Carlo
+.PARAM rval=1k cval=1n
+V1 in 0 PULSE(0 1 1n)
+R1 in out {rval}
+C1 out 0 {cval}
+.TRAN 10p 2u 0 25n
+.SAMPLING param=rval,cval type=normal,uniform means=1k std_deviations=100
++ lower_bounds=0.5n upper_bounds=1.5n
+.OPTIONS SAMPLES NUMSAMPLES=400 SEED=7
+.MEASURE TRAN vmax MAX V(out)
+.END
+"""
+
+
+def test_sampling_spec_and_lhs_marginals():
+    base = S.parse(SAMPLING)
+    assert base.sampling["PARAM"] == ["RVAL", "CVAL"] and base.sampling["NUMSAMPLES"] == 400
+    pts = S.sample_points(base.sampling)
+    r = np.array([p["RVAL"] for p in pts])
+    c = np.array([p["CVAL"] for p in pts])
+    assert abs(r.mean() - 1e3) < 10 and abs(r.std() - 100) < 10
+    assert c.min() >= 0.5e-9 and c.max() <= 1.5e-9
+    # Latin hypercube: exactly one sample in each of the 400 strata of C
+    strata = np.floor((c - 0.5e-9) / 1e-9 * 400).astype(int)
+    assert sorted(strata) == list(range(400))
+    decks = S.parse_sampling(SAMPLING)
+    assert len(decks) == 400 and decks[3].netlist.res[0][2] == pytest.approx(pts[3]["RVAL"])
+    assert S.sample_points(base.sampling) == pts  # seeded
+
+
+def test_sample_moments():
+    st = S.sample_moments([1.0, 2.0, 3.0, 4.0])
+    assert st["mean"] == 2.5 and st["variance"] == 1.25 and st["min"] == 1.0 and st["max"] == 4.0
+    assert st["skew"] == pytest.approx(0.0) and st["kurtosis"] == pytest.approx(1.64)
+    assert S.sample_moments([2.0, 2.0])["skew"] == 0.0  # 0/0 reads 0

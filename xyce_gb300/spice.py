@@ -11,7 +11,9 @@ output.  The subset is what the path simulates:
 * ``.MODEL``, ``.SUBCKT``/``.ENDS``, ``.TRAN``, ``.OPTIONS TIMEINT``
   (RELTOL, ABSTOL, METHOD=TRAP|GEAR, MAXORD), ``.PARAM`` with ``{NAME}``
   references, ``.STEP`` (linear or LIST; every point of the sweep runs as one
-  circuit of a single GPU batch), ``.PRINT TRAN``, ``.MEASURE TRAN`` (MAX, MIN, PP, AVG,
+  circuit of a single GPU batch), ``.SAMPLING`` with ``.OPTIONS SAMPLES``
+  (Latin hypercube or Monte Carlo samples of NORMAL / UNIFORM parameters,
+  all samples one batch, moments of every .MEASURE), ``.PRINT TRAN``, ``.MEASURE TRAN`` (MAX, MIN, PP, AVG,
   RMS, INTEG with FROM/TO), ``.END``; ``*`` and ``;`` comments, ``+``
   continuation lines, engineering suffixes (T G MEG K M MIL U N P F);
 * print variables ``V(n)``, ``V(a,b)``, ``I(Vname)``, ``TIME``, ``TEMP``
@@ -150,6 +152,7 @@ class Deck:
     steps: list = field(default_factory=list)        # .STEP: (name, [values]), outermost first
     params: dict[str, float] = field(default_factory=dict)
     step_values: dict[str, float] = field(default_factory=dict)  # this deck's point of the sweep
+    sampling: dict = field(default_factory=dict)     # .SAMPLING vectors + .OPTIONS SAMPLES
 
 
 _DIODE_ALIASES = {"CJ0": "CJO", "CJ": "CJO", "PB": "VJ", "MJ": "M"}
@@ -452,6 +455,23 @@ def parse(text: str, overrides: dict | None = None) -> Deck:
             break
         if head in (".PARAM",):
             continue
+        if head == ".SAMPLING":
+            deck.sampling.update(_sampling_spec(ln))
+            continue
+        if head == ".OPTIONS" and len(toks) > 1 and toks[1].upper() == "SAMPLES":
+            pos, kv = _params(toks[2:])
+            for k, v in kv.items():
+                if k == "NUMSAMPLES":
+                    deck.sampling["NUMSAMPLES"] = int(number(v))
+                elif k == "SEED":
+                    deck.sampling["SEED"] = int(number(v))
+                elif k == "SAMPLE_TYPE":
+                    if v.upper() not in ("LHS", "MC"):
+                        raise ValueError("SAMPLE_TYPE must be LHS or MC")
+                    deck.sampling["SAMPLE_TYPE"] = v.upper()
+                else:
+                    raise ValueError(f".OPTIONS SAMPLES {k} is not supported")
+            continue
         if head == ".STEP":
             deck.steps.append(_step(toks[1:]))
             continue
@@ -544,6 +564,88 @@ def _step(toks: list[str]) -> tuple[str, list[float]]:
         raise ValueError(".STEP step must move from start towards stop")
     k = int((b - a) / st) + 1  # decimal: the end point is not lost to rounding
     return name, [float(a + i * st) for i in range(k)]
+
+
+def _sampling_spec(line: str) -> dict:
+    """.SAMPLING PARAM=a,b TYPE=normal,uniform MEANS=.. STD_DEVIATIONS=..
+    LOWER_BOUNDS=.. UPPER_BOUNDS=.. (vectors, one entry per parameter;
+    the keys of Sampling, src/AnalysisPKG/N_ANP_Sampling.C:200-260)."""
+    body = line.split(None, 1)[1] if len(line.split(None, 1)) > 1 else ""
+    out = {}
+    for m in re.finditer(r"(\w+)\s*=\s*(.*?)(?=\s+\w+\s*=|$)", body):
+        key = m.group(1).upper()
+        vals = [v for v in re.split(r"[,\s]+", m.group(2).strip()) if v]
+        if key in ("PARAM", "TYPE"):
+            out[key] = [v.upper() for v in vals]
+        elif key in ("MEANS", "STD_DEVIATIONS", "LOWER_BOUNDS", "UPPER_BOUNDS"):
+            out[key] = [number(v) for v in vals]
+        else:
+            raise ValueError(f".SAMPLING {key} is not supported")
+    return out
+
+
+def sample_points(spec: dict) -> list[dict]:
+    """Parameter values of every sample: Latin hypercube (default) or plain
+    Monte Carlo, NORMAL (MEANS, STD_DEVIATIONS) or UNIFORM (LOWER_BOUNDS,
+    UPPER_BOUNDS) marginals; numpy's generator seeded with SEED (0 by
+    default), so the samples are reproducible but not the reference's
+    (it draws from its own generator)."""
+    import statistics
+    names = spec.get("PARAM", [])
+    types = spec.get("TYPE", [])
+    n = int(spec.get("NUMSAMPLES", 1))
+    if not names or len(types) != len(names):
+        raise ValueError(".SAMPLING needs PARAM and one TYPE per parameter")
+    if n < 1:
+        raise ValueError("NUMSAMPLES must be positive")
+    rng = np.random.default_rng(int(spec.get("SEED", 0)))
+    lhs = spec.get("SAMPLE_TYPE", "LHS") == "LHS"
+    cols = {}
+    iN = iU = 0
+    for name, ty in zip(names, types):
+        u = (rng.permutation(n) + rng.uniform(size=n)) / n if lhs else rng.uniform(size=n)
+        u = np.clip(u, 1e-12, 1 - 1e-12)
+        if ty == "NORMAL":
+            mu, sd = spec["MEANS"][iN], spec["STD_DEVIATIONS"][iN]
+            iN += 1
+            if sd < 0:
+                raise ValueError("STD_DEVIATIONS must be >= 0")
+            nd = statistics.NormalDist(mu, sd) if sd > 0 else None
+            cols[name] = [nd.inv_cdf(float(x)) if nd else mu for x in u]
+        elif ty == "UNIFORM":
+            lo, hi = spec["LOWER_BOUNDS"][iU], spec["UPPER_BOUNDS"][iU]
+            iU += 1
+            cols[name] = [lo + float(x) * (hi - lo) for x in u]
+        else:
+            raise ValueError(f".SAMPLING TYPE {ty} is not supported (NORMAL, UNIFORM)")
+    return [{name: cols[name][k] for name in names} for k in range(n)]
+
+
+def sample_moments(values) -> dict:
+    """Mean, population standard deviation and variance, skew, kurtosis,
+    min and max of one output over the samples; non-finite moments read 0
+    (computeMoments, src/AnalysisPKG/N_ANP_UQSupport.C:80-135)."""
+    v = np.asarray(values, np.float64)
+    if len(v) == 0:
+        return {}
+    mean = v.mean()
+    var = np.mean((v - mean) ** 2)
+    sd = np.sqrt(var)
+    mu3 = np.mean(v ** 3) - 3 * mean * np.mean(v ** 2) + 2 * mean ** 3
+    mu4 = np.mean(v ** 4) - 4 * mean * np.mean(v ** 3) + 6 * mean ** 2 * np.mean(v ** 2) - 3 * mean ** 4
+    with np.errstate(divide="ignore", invalid="ignore"):
+        skew, kurt = mu3 / sd ** 3, mu4 / sd ** 4
+    fix = lambda x: float(x) if np.isfinite(x) else 0.0
+    return dict(mean=fix(mean), stddev=fix(sd), variance=fix(var), skew=fix(skew), kurtosis=fix(kurt),
+                min=float(v.min()), max=float(v.max()))
+
+
+def parse_sampling(text: str) -> list[Deck]:
+    """One deck per sample of the deck's .SAMPLING block."""
+    base = parse(text)
+    if not base.sampling:
+        return [base]
+    return [parse(text, pt) for pt in sample_points(base.sampling)]
 
 
 def parse_sweep(text: str) -> list[Deck]:
@@ -813,6 +915,22 @@ def main(argv=None) -> int:
     path = argv[0]
     with open(path) as f:
         text = f.read()
+    base = parse(text)
+    if base.sampling:
+        if base.steps:
+            raise ValueError(".SAMPLING and .STEP together are not supported")
+        decks = parse_sampling(text)
+        results = run_sweep(decks)
+        if base.prints:
+            write_prn(path + ".prn", base, results)
+        with open(path + ".ms0", "w") as f:
+            for m in base.measures:
+                st = sample_moments([r.measures[m.name] for r in results])
+                line = f"{m.name}: " + ", ".join(f"{k} = {v:.6e}" for k, v in st.items())
+                f.write(line + "\n")
+                print(line)
+        print(f"{len(decks)} samples run as one batch; output {os.path.basename(path)}.prn")
+        return 0
     decks = parse_sweep(text)
     deck = decks[0]
     if len(decks) == 1:
