@@ -374,15 +374,21 @@ def run_ours(args):
     # ---- the FP32-LU + FP64-refinement form, same workload ------------------
     forms = None
     if rank == 0 and args.forms:
-        c2, ms2, s0, s1 = _timed_windows(xg, nl, probes, dev, args, window, xg.PREC_FP32_IR, flush, stream_of)
-        forms = {"fp64": value,
-                 "fp32_lu_fp64_ir": (s1["accepted"] - s0["accepted"]) / (ms2 / 1e3),
-                 "fp32_lu_fp64_ir_newton_iters_per_step":
-                     (s1["newton_iters"] - s0["newton_iters"]) / max(1, s1["accepted"] - s0["accepted"])}
-        c2.tran_end()
-        c2.close()
-        if args.workload == "mc":
-            forms.update(_one_at_a_time(xg, nl, dev, window, stream_of, value))
+        # the comparison forms are reported, not required: a failure there
+        # is recorded in the line instead of losing it
+        try:
+            c2, ms2, s0, s1 = _timed_windows(xg, nl, probes, dev, args, window, xg.PREC_FP32_IR, flush,
+                                             stream_of)
+            forms = {"fp64": value,
+                     "fp32_lu_fp64_ir": (s1["accepted"] - s0["accepted"]) / (ms2 / 1e3),
+                     "fp32_lu_fp64_ir_newton_iters_per_step":
+                         (s1["newton_iters"] - s0["newton_iters"]) / max(1, s1["accepted"] - s0["accepted"])}
+            c2.tran_end()
+            c2.close()
+            if args.workload == "mc":
+                forms.update(_one_at_a_time(xg, nl, dev, window, stream_of, value))
+        except Exception as e:  # noqa: BLE001
+            forms = {"fp64": value, "error": f"{type(e).__name__}: {e}"}
 
     # ---- end to end through the C-ABI with host buffers --------------------
     e2e = None

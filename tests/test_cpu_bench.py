@@ -1,0 +1,48 @@
+"""bench.py helpers that need no GPU: clock-sample parsing, peaks, the
+one-line JSON contract's static parts."""
+import importlib.util
+import json
+import os
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def bench():
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_clock_summary_median_max_and_reasons(bench, tmp_path):
+    p = tmp_path / "clk.csv"
+    p.write_text("0, 2070, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active\n"
+                 "0, 1980, 2070, 1300.0, 0x4, Not Active, Not Active, Not Active, Active\n"
+                 "0, 2070, 2070, 950.0, 0x0, Not Active, Not Active, Not Active, Not Active\n"
+                 "1, 500, 2070, 100.0, 0x0, Active, Not Active, Not Active, Not Active\n"
+                 "0, [N/A], 2070, 0, 0x0, Not Active, Not Active, Not Active, Not Active\n")
+    c = bench._clock_summary(str(p), 0)
+    assert c == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"]}
+    c1 = bench._clock_summary(str(p), 1)
+    assert c1["reasons"] == ["hw_slowdown"]
+
+
+def test_clock_summary_without_samples(bench, tmp_path):
+    assert bench._clock_summary(str(tmp_path / "none.csv"), 0)["reasons"] == ["unsampled"]
+
+
+def test_peaks_read_measured_file_or_fall_back(bench):
+    value, kind = bench._peaks()
+    assert value > 1000.0 and kind in ("measured", "fallback")
+    if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")):
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            assert value == pytest.approx(float(json.load(f)["hbm_gbs"]))
+
+
+def test_workload_descriptions(bench):
+    nl, probes, desc = bench._workload("mc", rings=8)
+    assert desc["circuits"] == 8 and desc["workload"] == "monte_carlo_rings_8"
+    assert len(probes) == 4 and nl.n_circuits == 8
