@@ -345,3 +345,64 @@ def test_sample_moments():
     assert st["mean"] == 2.5 and st["variance"] == 1.25 and st["min"] == 1.0 and st["max"] == 4.0
     assert st["skew"] == pytest.approx(0.0) and st["kurtosis"] == pytest.approx(1.64)
     assert S.sample_moments([2.0, 2.0])["skew"] == 0.0  # 0/0 reads 0
+
+
+class _FakeCircuit:
+    """Stand-in for the GPU transient: circuit c's probe j reads
+    100 (j + 1) + 10 c + sample index at t = 1 ns x sample index."""
+
+    def __init__(self, nl, device=0, arrays=None):
+        self.nl = nl
+
+    def transient(self, tran, probes=(), cap=0):
+        nc = len(self.nl.offsets) - 1
+        per = [0] * nc
+        for u in probes:
+            per[int(np.searchsorted(self.nl.offsets, u, side="right") - 1)] += 1
+        pmax = max(1, max(per))
+        counts = np.full(nc, 4, np.int32)
+        times = np.zeros((nc, cap))
+        values = np.zeros((nc, cap, pmax))
+        for c in range(nc):
+            times[c, :4] = np.arange(4) * 1e-9
+            for j in range(per[c]):
+                values[c, :4, j] = 100.0 * (j + 1) + 10.0 * c + np.arange(4)
+        return counts, times, values, {"status": 0, "rejected": 0}
+
+    def close(self):
+        pass
+
+
+def test_run_and_main_single_deck(monkeypatch, tmp_path):
+    import xyce_gb300
+    monkeypatch.setattr(xyce_gb300, "Circuit", _FakeCircuit)
+    d = S.parse(RC)
+    res = S.run(d, cap=16)
+    # probes in first-use order: V(OUT) -> out; V(IN,OUT) -> in; I(V1) -> branch
+    np.testing.assert_array_equal(res.columns["V(OUT)"], [100, 101, 102, 103])
+    np.testing.assert_array_equal(res.columns["V(IN,OUT)"], [100, 100, 100, 100])  # in - out
+    np.testing.assert_array_equal(res.columns["I(V1)"], [300, 301, 302, 303])
+    assert res.measures["VMAX"] == 103.0
+    path = tmp_path / "rc.cir"
+    path.write_text(RC)
+    assert S.main([str(path)]) == 0
+    names, vals = S.read_prn(str(path) + ".prn")
+    assert names == ["Index", "TIME", "V(OUT)", "V(IN,OUT)", "I(V1)"] and vals.shape == (4, 5)
+    assert (tmp_path / "rc.cir.mt0").read_text().startswith("VMAX = 1.030000e+02")
+
+
+def test_main_sweep_and_sampling_outputs(monkeypatch, tmp_path):
+    import xyce_gb300
+    monkeypatch.setattr(xyce_gb300, "Circuit", _FakeCircuit)
+    p = tmp_path / "sw.cir"
+    p.write_text(SWEEP)
+    assert S.main([str(p)]) == 0
+    lines = (tmp_path / "sw.cir.prn").read_text().splitlines()
+    assert lines[-1] == "End of Xyce(TM) Parameter Sweep" and len(lines) == 1 + 3 * 4 + 1
+    assert [(tmp_path / f"sw.cir.mt{k}").read_text() for k in range(3)] == [
+        "VMAX = 1.030000e+02\n", "VMAX = 1.130000e+02\n", "VMAX = 1.230000e+02\n"]
+    q = tmp_path / "mc.cir"
+    q.write_text(SAMPLING.replace("NUMSAMPLES=400", "NUMSAMPLES=5"))
+    assert S.main([str(q)]) == 0
+    ms = (tmp_path / "mc.cir.ms0").read_text()
+    assert ms.startswith("VMAX: mean = 1.230000e+02")  # circuits 0..4 -> max 103..143
