@@ -75,6 +75,9 @@ def lib():
                                     C.POINTER(C.c_int), C.POINTER(TranStats)]
         L.orc_dcop.argtypes = [P, dp, C.POINTER(C.c_int)]
         L.orc_set_wall_log.argtypes = [P, C.c_void_p, C.c_int]
+        L.orc_set_linear_solver.argtypes = [P, C.c_int, C.c_double, C.c_double]
+        L.orc_set_order.argtypes = [P, C.c_void_p, C.c_int]
+        L.orc_lu_counts.argtypes = [P, np.ctypeslib.ndpointer(np.int64, flags="C"), C.c_int]
         _lib = L
     return _lib
 
@@ -148,6 +151,38 @@ class Oracle:
             raise np.linalg.LinAlgError("oracle LU: singular")
         return x
 
+    def set_order(self, perm=None):
+        """Elimination order of the LU: perm[k] = the unknown eliminated k-th
+        (None: the natural order)."""
+        if perm is None:
+            rc = lib().orc_set_order(self.h, None, 0)
+        else:
+            perm = np.ascontiguousarray(perm, np.int32)
+            rc = lib().orc_set_order(self.h, perm.ctypes.data, len(perm))
+        if rc != 0:
+            raise ValueError("oracle: the elimination order must be a permutation of the unknowns")
+
+    def use_minimum_degree(self):
+        """Order the LU as KLU does before its numeric factorizations: a
+        minimum-degree order of the pattern of A + A^T (min_degree_order)."""
+        self.set_order(min_degree_order(self.row_ptr, self.col_idx))
+
+    LU_COUNTS = ("factor", "reuse", "refined", "refine_steps", "fallback", "repeat")
+
+    def set_linear_solver(self, kind="klu", ir_tol=1e-9, ir_min_tol=1e-2):
+        """.OPTIONS LINSOL TYPE: "klu" refactors on every Newton iteration,
+        "ir" reuses earlier factors with iterative refinement (IRSolver)."""
+        rc = lib().orc_set_linear_solver(self.h, {"klu": 0, "ir": 1}[kind], float(ir_tol),
+                                         float(ir_min_tol))
+        if rc != 0:
+            raise ValueError("oracle: bad linear solver options")
+
+    def lu_counts(self, reset=True):
+        """What the linear solves did since the last reset (LU_COUNTS order)."""
+        out = np.zeros(len(self.LU_COUNTS), np.int64)
+        lib().orc_lu_counts(self.h, out, int(reset))
+        return dict(zip(self.LU_COUNTS, out.tolist()))
+
     def dcop(self):
         x = np.zeros(self.n)
         it = C.c_int()
@@ -176,6 +211,35 @@ class Oracle:
         k = nout.value
         return (times[:k].copy(), vals[: k * len(probes)].reshape(k, len(probes)).copy(),
                 {f: getattr(st, f) for f, _ in TranStats._fields_})
+
+
+def min_degree_order(row_ptr, col_idx):
+    """A minimum-degree elimination order of the pattern of A + A^T.
+
+    KLU (the reference's default solver, SuiteSparse, through Amesos) orders
+    each diagonal block with AMD on A + A^T once, in its symbolic analysis.
+    AMD is not in this image; SuperLU's multiple minimum degree on A + A^T
+    (scipy's splu, permc_spec "MMD_AT_PLUS_A") is the same family of
+    ordering.  Only the pattern matters: it is factored with unit entries and
+    a dominant diagonal so that the factorization that returns the order
+    cannot break down.  Returns perm with perm[k] = the unknown eliminated
+    k-th."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+    row_ptr = np.asarray(row_ptr, np.int64)
+    col_idx = np.asarray(col_idx, np.int64)
+    n = len(row_ptr) - 1
+    if n == 0:
+        return np.zeros(0, np.int32)
+    A = sp.csr_matrix((np.ones(len(col_idx)), col_idx, row_ptr), shape=(n, n))
+    A = (A + A.T).tocsc()
+    A.data[:] = 1.0
+    deg = np.diff(A.indptr).astype(np.float64)
+    A = (A + sp.diags(deg + 1.0)).tocsc()
+    lu = spl.splu(A, permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.0,
+                  options=dict(SymmetricMode=True))
+    # Pr A Pc = L U with column j of A Pc = column i of A where perm_c[i] = j
+    return np.argsort(lu.perm_c).astype(np.int32)
 
 
 def ksparse_solve(row_ptr, col_idx, vals, b):

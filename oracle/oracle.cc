@@ -221,9 +221,12 @@ struct orc_ctx {
   // pattern (CSR) and per-device stamp positions
   std::vector<int> rp, ci;
   std::vector<int> pos_r, pos_c, pos_v, pos_d, pos_m, pos_b;
-  // CSC view for the LU
+  // CSC view for the LU, of P A P^T when an elimination order q is set
+  // (q[k] = the unknown eliminated k-th; empty = the natural order)
   std::vector<int> Ap, Ai, csr2csc;
   std::vector<double> Ax;
+  std::vector<int> q, qinv;
+  std::vector<double> pb, px;  // b and x in the elimination order
   SparseLU lu;
   int nsta = 0, nsto = 0;
   std::vector<char> is_branch;  // unknown is a voltage-source branch current
@@ -231,6 +234,18 @@ struct orc_ctx {
   double *wall_log = nullptr;  // optional: wall-clock seconds at each accepted step
   int wall_cap = 0;
   bool finalized = false;
+  // linear solver: 0 = refactor on every Newton iteration (KLU through
+  // AmesosSolver), 1 = LINSOL TYPE=IR (IRSolver: reuse earlier factors)
+  int lin_type = 0;
+  double ir_tol = 1e-9, ir_min_tol = 1e-2;  // IRSolver defaults, N_LAS_IRSolver.C:74-75
+  bool lu_valid = false;
+  // what the linear solves did: factorizations, reused solves accepted as
+  // they were, reused solves accepted after refinement, refinement steps,
+  // reused solves that fell back to a refactorization, and factorizations
+  // of a matrix equal bit for bit to the one factored before it
+  long long n_factor = 0, n_reuse = 0, n_refined = 0, n_refine_steps = 0, n_fallback = 0;
+  long long n_repeat = 0;
+  std::vector<double> last_factored;  // CSC values of the last factorization
   // state layout: store diode [vd,qd,cd] then mos1 [vbd,vbs,vgs,vds,von,gm]
   // then bsim4 [vbd,vbs,vgs,vds,von]; state mos1 [capgs,capgd,capgb,qgs,qgd,
   // qgb,qbd,qbs] then bsim4 [qg,qd,qb]  (field-major, SoA)
@@ -357,6 +372,35 @@ int orc_add_bsim4(orc_ctx *c, int n, const int *d, const int *g, const int *s, c
 
 // Builder::generateGraphs + setupPointers restated: the CSR pattern is the
 // union of every device's jacobianStamp; each stamp caches its position.
+namespace {
+// CSC structure of the pattern, symmetrically permuted by the elimination
+// order when one is set: column k of P A P^T is column q[k] of A with row i
+// moved to qinv[i].
+void build_csc(orc_ctx *c) {
+  const int nnz = (int)c->ci.size();
+  auto pos = [&](int i) { return c->qinv.empty() ? i : c->qinv[i]; };
+  c->Ap.assign(c->n + 1, 0);
+  for (int p = 0; p < nnz; ++p) c->Ap[pos(c->ci[p]) + 1]++;
+  for (int j = 0; j < c->n; ++j) c->Ap[j + 1] += c->Ap[j];
+  c->Ai.resize(nnz); c->csr2csc.resize(nnz);
+  std::vector<int> next(c->Ap.begin(), c->Ap.end() - 1);
+  for (int i = 0; i < c->n; ++i)
+    for (int p = c->rp[i]; p < c->rp[i + 1]; ++p) {
+      const int k = next[pos(c->ci[p])]++;
+      c->Ai[k] = pos(i); c->csr2csc[p] = k;
+    }
+  c->Ax.resize(nnz);
+}
+
+// x = A^-1 b with the current factors of P A P^T.
+void lu_apply(orc_ctx *c, const double *b, double *x) {
+  if (c->q.empty()) { c->lu.solve(b, x); return; }
+  for (int k = 0; k < c->n; ++k) c->pb[k] = b[c->q[k]];
+  c->lu.solve(c->pb.data(), c->px.data());
+  for (int k = 0; k < c->n; ++k) x[c->q[k]] = c->px[k];
+}
+}  // namespace
+
 int orc_finalize(orc_ctx *c) {
   std::vector<std::pair<int, int>> all;
   stamp_pairs(c, all);
@@ -388,19 +432,7 @@ int orc_finalize(orc_ctx *c) {
   fill(c->pos_d, o, 7 * c->d_p.size()); o += 7 * c->d_p.size();
   fill(c->pos_m, o, 16 * c->m_d.size()); o += 16 * c->m_d.size();
   fill(c->pos_b, o, 16 * c->b_d.size()); o += 16 * c->b_d.size();
-  // CSC structure of the same pattern
-  int nnz = (int)c->ci.size();
-  c->Ap.assign(c->n + 1, 0);
-  for (int p = 0; p < nnz; ++p) c->Ap[c->ci[p] + 1]++;
-  for (int j = 0; j < c->n; ++j) c->Ap[j + 1] += c->Ap[j];
-  c->Ai.resize(nnz); c->csr2csc.resize(nnz);
-  std::vector<int> next(c->Ap.begin(), c->Ap.end() - 1);
-  for (int i = 0; i < c->n; ++i)
-    for (int p = c->rp[i]; p < c->rp[i + 1]; ++p) {
-      int q = next[c->ci[p]]++;
-      c->Ai[q] = i; c->csr2csc[p] = q;
-    }
-  c->Ax.resize(nnz);
+  build_csc(c);
   c->nsto = 3 * (int)c->d_p.size() + 6 * (int)c->m_d.size() + 5 * (int)c->b_d.size();
   c->nsta = 8 * (int)c->m_d.size() + 3 * (int)c->b_d.size();
   c->finalized = true;
@@ -685,7 +717,7 @@ int orc_lu_solve(orc_ctx *c, const double *vals, const double *b, double *x) {
   size_t nnz = c->ci.size();
   for (size_t p = 0; p < nnz; ++p) c->Ax[c->csr2csc[p]] = vals[p];
   if (c->lu.factor(c->n, c->Ap, c->Ai, c->Ax.data()) != 0) return -9;
-  c->lu.solve(b, x);
+  lu_apply(c, b, x);
   return 0;
 }
 
@@ -706,6 +738,7 @@ struct Work {
   int n, nnz, nsta, nsto;
   std::vector<double> x, xcurr, sta_curr, sto_curr, sta_next, sto_next, sto_prev;
   std::vector<double> F, Q, B, dFv, dQv, dFdx, dQdx, J, rhs, dx, solwt;
+  std::vector<double> ir_r, ir_x, ir_d;  // refinement residual, iterate, correction
   bool any_limited = false;
   double t_load = 0, t_solve = 0;
 };
@@ -765,6 +798,71 @@ void assemble(orc_ctx *c, Work &w, double time, int iter, int flags, const Coef 
   w.t_load += now() - t0;
 }
 
+// One linear solve J dx = rhs for Newton iteration nlStep (1-based).
+// Default: factor J, then solve (AmesosSolver::doSolve with KLU).  With
+// lin_type 1, IRSolver::doSolve (N_LAS_IRSolver.C:428-560): the first
+// iteration of every Newton solve factors; later iterations solve with the
+// factors they find and test the relative residual ||rhs - J dx||_2 /
+// ||rhs||_2 (unscaled when ||rhs||_2 is below machine epsilon).  At most
+// ir_tol the solve stands; below ir_min_tol up to 10 refinement steps
+// x += (LU)^-1 (rhs - J x) run while the residual is above ir_tol and does
+// not grow, and stand if they end below ir_tol; anything else refactors.
+// As in the reference, a NaN residual passes the first test (the Newton
+// loop then fails on the non-finite update).
+int linear_solve(orc_ctx *c, Work &w, int nlStep) {
+  auto standard = [&]() {
+    for (int p = 0; p < w.nnz; ++p) c->Ax[c->csr2csc[p]] = w.J[p];
+    c->n_factor++;
+    if (c->lu_valid && c->last_factored == c->Ax) c->n_repeat++;
+    c->last_factored = c->Ax;
+    const int fs = c->lu.factor(w.n, c->Ap, c->Ai, c->Ax.data());
+    c->lu_valid = fs == 0;
+    if (fs != 0) return -9;
+    lu_apply(c, w.rhs.data(), w.dx.data());
+    return 0;
+  };
+  if (c->lin_type != 1 || nlStep == 1 || !c->lu_valid) return standard();
+  const double eps = 2.220446049250313e-16;
+  auto residual = [&](const std::vector<double> &v) {  // ir_r = rhs - J v; returns ||ir_r||_2
+    double s = 0;
+    for (int i = 0; i < w.n; ++i) {
+      double a = 0;
+      for (int p = c->rp[i]; p < c->rp[i + 1]; ++p) a += w.J[p] * v[c->ci[p]];
+      w.ir_r[i] = w.rhs[i] - a;
+      s += w.ir_r[i] * w.ir_r[i];
+    }
+    return std::sqrt(s);
+  };
+  double bn = 0;
+  for (double b : w.rhs) bn += b * b;
+  bn = std::sqrt(bn);
+  auto rel = [&](double rn) { return bn > eps ? rn / bn : rn; };
+  lu_apply(c, w.rhs.data(), w.dx.data());
+  double res = rel(residual(w.dx));
+  if (!(res > c->ir_tol)) { c->n_reuse++; return 0; }
+  if (res < c->ir_min_tol) {
+    w.ir_x = w.dx;
+    int it = 0;
+    bool diverging = false;
+    while (res > c->ir_tol && it < 10 && !diverging) {
+      lu_apply(c, w.ir_r.data(), w.ir_d.data());
+      for (int i = 0; i < w.n; ++i) w.ir_x[i] += w.ir_d[i];
+      const double nr = rel(residual(w.ir_x));
+      if (nr > res) diverging = true;
+      res = nr;
+      ++it;
+    }
+    c->n_refine_steps += it;
+    if (res < c->ir_tol) {
+      w.dx = w.ir_x;
+      c->n_refined++;
+      return 0;
+    }
+  }
+  c->n_fallback++;
+  return standard();
+}
+
 // DampedNewton::solve + converged_ (N_NLS_DampedNewton.C:362-520, 1191-1396),
 // full Newton steps.  Returns the DampedNewton status code; *iters = nlStep_.
 int newton(orc_ctx *c, Work &w, double time, const NLParams &nl, const Coef &cf, int first_flags,
@@ -793,11 +891,9 @@ int newton(orc_ctx *c, Work &w, double time, const NLParams &nl, const Coef &cf,
     if (nan) { status = -6; break; }
     // direction_: solve J dx = rhs
     double t0 = now();
-    for (int p = 0; p < w.nnz; ++p) c->Ax[c->csr2csc[p]] = w.J[p];
-    int fs = c->lu.factor(w.n, c->Ap, c->Ai, c->Ax.data());
-    if (fs != 0) { w.t_solve += now() - t0; status = -9; break; }
-    c->lu.solve(w.rhs.data(), w.dx.data());
+    const int ls = linear_solve(c, w, nlStep);
     w.t_solve += now() - t0;
+    if (ls != 0) { status = -9; break; }
     bool dxnan = false;
     for (int i = 0; i < w.n; ++i) if (!std::isfinite(w.dx[i])) dxnan = true;
     if (dxnan) { status = -6; break; }
@@ -853,7 +949,8 @@ void work_init(orc_ctx *c, Work &w) {
   w.x.assign(w.n, 0.0); w.xcurr.assign(w.n, 0.0);
   w.sta_curr.assign(std::max(1, w.nsta), 0.0); w.sta_next = w.sta_curr;
   w.sto_curr.assign(std::max(1, w.nsto), 0.0); w.sto_next = w.sto_curr; w.sto_prev = w.sto_curr;
-  for (auto *v : {&w.F, &w.Q, &w.B, &w.dFv, &w.dQv, &w.rhs, &w.dx, &w.solwt}) v->assign(w.n, 0.0);
+  for (auto *v : {&w.F, &w.Q, &w.B, &w.dFv, &w.dQv, &w.rhs, &w.dx, &w.solwt, &w.ir_r, &w.ir_x, &w.ir_d})
+    v->assign(w.n, 0.0);
   for (auto *v : {&w.dFdx, &w.dQdx, &w.J}) v->assign(w.nnz, 0.0);
 }
 
@@ -1134,6 +1231,52 @@ extern "C" int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, 
   st->time_total = now() - tstart_wall;
   *n_out = nout;
   return st->status;
+}
+
+// Elimination order of the LU (the ordering KLU's symbolic analysis
+// computes once, AMD on the pattern of A + A^T): perm[k] = the unknown
+// eliminated k-th, a permutation of 0..n-1; n = 0 restores the natural order.
+extern "C" int orc_set_order(orc_ctx *c, const int *perm, int n) {
+  if (!c->finalized) return -1;
+  if (n == 0) {
+    c->q.clear(); c->qinv.clear();
+  } else {
+    if (n != c->n) return -1;
+    std::vector<int> inv(n, -1);
+    for (int k = 0; k < n; ++k) {
+      if (perm[k] < 0 || perm[k] >= n || inv[perm[k]] >= 0) return -1;
+      inv[perm[k]] = k;
+    }
+    c->q.assign(perm, perm + n);
+    c->qinv = std::move(inv);
+    c->pb.assign(n, 0.0); c->px.assign(n, 0.0);
+  }
+  build_csc(c);
+  c->lu_valid = false;
+  c->last_factored.clear();
+  return 0;
+}
+
+// .OPTIONS LINSOL TYPE: 0 refactors every Newton iteration (KLU), 1 is
+// IRSolver with its IR_SOLVER_TOL / IR_MIN_TOL (N_LAS_IRSolver.C:131-145).
+extern "C" int orc_set_linear_solver(orc_ctx *c, int type, double ir_tol, double ir_min_tol) {
+  if (type != 0 && type != 1) return -1;
+  if (!(ir_tol > 0.0) || !(ir_min_tol > 0.0)) return -1;
+  c->lin_type = type;
+  c->ir_tol = ir_tol;
+  c->ir_min_tol = ir_min_tol;
+  return 0;
+}
+
+// Counters of the linear solves since the last reset: factorizations,
+// reused solves, refined solves, refinement steps, fallbacks, repeated
+// factorizations (the matrix equal bit for bit to the last one factored).
+extern "C" int orc_lu_counts(orc_ctx *c, long long *out, int reset) {
+  out[0] = c->n_factor; out[1] = c->n_reuse; out[2] = c->n_refined;
+  out[3] = c->n_refine_steps; out[4] = c->n_fallback; out[5] = c->n_repeat;
+  if (reset)
+    c->n_factor = c->n_reuse = c->n_refined = c->n_refine_steps = c->n_fallback = c->n_repeat = 0;
+  return 0;
 }
 
 // Benchmark support: wall-clock time (seconds since the start of the

@@ -16,6 +16,7 @@
  *   - DataStore error weights/WRMS   src/TimeIntegrationPKG/N_TIA_DataStore.C:1304-1550,1737
  *   - StepErrorControl accept test   src/TimeIntegrationPKG/N_TIA_StepErrorControl.C:458-575
  *   - DampedNewton                   src/NonlinearSolverPKG/N_NLS_DampedNewton.C:297-520,1147-1396
+ *   - IRSolver factor reuse          src/LinearAlgebraServicesPKG/N_LAS_IRSolver.C:428-560
  *   - Sparse LU: Gilbert-Peierls left-looking LU with threshold partial
  *     pivoting (the algorithm of KLU, which Xyce calls through Amesos in
  *     src/LinearAlgebraServicesPKG/N_LAS_AmesosSolver.C:309-396).  It is
@@ -95,6 +96,23 @@ int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, const int *
 
 /* Operating point only (x out, length n_unknowns). */
 int orc_dcop(orc_ctx *c, double *x, int *iters);
+
+/* Elimination order of the sparse LU, as KLU's symbolic analysis fixes one
+ * (AMD on the pattern of A + A^T) before its numeric factorizations:
+ * perm[k] = the unknown eliminated k-th (a permutation of 0..n_unknowns-1),
+ * the LU then factors P A P^T with the same threshold pivoting; n = 0
+ * restores the natural order.  Returns -1 for anything but a permutation. */
+int orc_set_order(orc_ctx *c, const int *perm, int n);
+
+/* Linear solver of the Newton iterations (.OPTIONS LINSOL TYPE): 0 refactors
+ * on every iteration (KLU), 1 is IRSolver (reuse of earlier factors with
+ * iterative refinement, src/LinearAlgebraServicesPKG/N_LAS_IRSolver.C:428-560)
+ * with its IR_SOLVER_TOL (default 1e-9) and IR_MIN_TOL (default 1e-2). */
+int orc_set_linear_solver(orc_ctx *c, int type, double ir_tol, double ir_min_tol);
+/* out[6]: factorizations, reused solves, refined solves, refinement steps,
+ * fallbacks to a refactorization, repeated factorizations (of a matrix equal
+ * bit for bit to the one factored before); reset != 0 zeroes them afterwards. */
+int orc_lu_counts(orc_ctx *c, long long *out, int reset);
 
 /* Benchmark support: record wall-clock seconds at each accepted step. */
 int orc_set_wall_log(orc_ctx *c, double *buf, int cap);
