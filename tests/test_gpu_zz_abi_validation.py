@@ -1,0 +1,49 @@
+"""Topology validation of the C-ABI on a GPU: an xg_add_* call that rejects
+one item appends none of them, and a two-terminal device or source whose
+nodes lie in two circuits of a batch is refused at finalize."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def cuda(xg):
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return xg.lib()
+
+
+def _ctx(xg, L, n, offsets):
+    h = C.c_void_p()
+    assert L.xg_create(C.byref(h), 0) == xg.XG_OK
+    assert L.xg_set_unknowns(h, n, len(offsets) - 1, np.array(offsets, np.int32)) == xg.XG_OK
+    return h
+
+
+def test_rejected_add_appends_nothing(xg, cuda):
+    L = cuda
+    i32 = lambda *v: np.array(v, np.int32)
+    h = _ctx(xg, L, 4, [0, 4])
+    assert L.xg_add_resistors(h, 1, i32(0), i32(1), np.array([1.0])) == xg.XG_OK
+    # the second item is out of range: the first, valid one is not kept either
+    assert L.xg_add_resistors(h, 2, i32(2, 0), i32(3, 9), np.array([1.0, 1.0])) == -1  # XG_ERR_ARG
+    assert L.xg_finalize(h) == xg.XG_OK
+    n, nnz, nsta, nsto = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    assert L.xg_get_sizes(h, C.byref(n), C.byref(nnz), C.byref(nsta), C.byref(nsto)) == xg.XG_OK
+    # the 2x2 block of the kept resistor and the diagonals of nodes 2 and 3
+    assert (n.value, nnz.value) == (4, 6)
+    assert L.xg_destroy(h) == xg.XG_OK
+
+
+def test_device_across_circuits_refused(xg, cuda):
+    L = cuda
+    h = _ctx(xg, L, 4, [0, 2, 4])
+    assert L.xg_add_resistors(h, 1, np.array([1], np.int32), np.array([2], np.int32),
+                              np.array([1.0])) == xg.XG_OK
+    assert L.xg_finalize(h) == -1  # XG_ERR_ARG
+    assert b"spans two circuits" in L.xg_error_string(h)
+    assert L.xg_destroy(h) == xg.XG_OK

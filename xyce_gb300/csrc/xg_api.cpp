@@ -197,34 +197,50 @@ int xg_set_unknowns(xg_ctx *ctx, int n, int ncirc, const int *offsets) {
   return XG_OK;
 }
 
-#define SETUP_CHECK()                                                                  \
+// Common checks of the xg_add_* calls.  Each call validates all n items
+// before it appends any, so a rejected call leaves the topology as it was.
+#define SETUP_CHECK(...)                                                               \
   if (!ctx) return XG_ERR_ARG;                                                         \
   if (!ctx->unknowns_set) return fail(ctx, XG_ERR_STATE, "call xg_set_unknowns first"); \
   if (ctx->finalized) return fail(ctx, XG_ERR_STATE, "topology is already finalized"); \
-  if (n < 0) return fail(ctx, XG_ERR_ARG, "negative count");
+  if (n < 0) return fail(ctx, XG_ERR_ARG, "negative count");                           \
+  if (n > 0 && !all_set({__VA_ARGS__})) return fail(ctx, XG_ERR_ARG, "null array");
+
+static bool all_set(std::initializer_list<const void *> ptrs) {
+  for (const void *p : ptrs)
+    if (!p) return false;
+  return true;
+}
 
 int xg_add_resistors(xg_ctx *ctx, int n, const int *pos, const int *neg, const double *r) {
-  SETUP_CHECK();
+  SETUP_CHECK(pos, neg, r);
   for (int k = 0; k < n; ++k) {
     if (!valid_node(ctx, pos[k]) || !valid_node(ctx, neg[k])) return fail(ctx, XG_ERR_ARG, "resistor node out of range");
     if (!(r[k] != 0.0) || !std::isfinite(r[k])) return fail(ctx, XG_ERR_ARG, "resistor value must be finite and nonzero");
-    ctx->r_p.push_back(pos[k]); ctx->r_n.push_back(neg[k]); ctx->r_v.push_back(r[k]);
   }
+  ctx->r_p.insert(ctx->r_p.end(), pos, pos + n);
+  ctx->r_n.insert(ctx->r_n.end(), neg, neg + n);
+  ctx->r_v.insert(ctx->r_v.end(), r, r + n);
   return XG_OK;
 }
 
 int xg_add_capacitors(xg_ctx *ctx, int n, const int *pos, const int *neg, const double *cv) {
-  SETUP_CHECK();
+  SETUP_CHECK(pos, neg, cv);
   for (int k = 0; k < n; ++k) {
     if (!valid_node(ctx, pos[k]) || !valid_node(ctx, neg[k])) return fail(ctx, XG_ERR_ARG, "capacitor node out of range");
     if (!std::isfinite(cv[k])) return fail(ctx, XG_ERR_ARG, "capacitor value must be finite");
-    ctx->c_p.push_back(pos[k]); ctx->c_n.push_back(neg[k]); ctx->c_v.push_back(cv[k]);
   }
+  ctx->c_p.insert(ctx->c_p.end(), pos, pos + n);
+  ctx->c_n.insert(ctx->c_n.end(), neg, neg + n);
+  ctx->c_v.insert(ctx->c_v.end(), cv, cv + n);
   return XG_OK;
 }
 
-static int check_wave(xg_ctx *ctx, int kind, int len) {
+// Waveform k of a source list: kind, and its values data[off[k] .. off[k+1]).
+static int check_wave(xg_ctx *ctx, int kind, int first, int end) {
   static const int need[4] = {1, 6, 7, 2};
+  const int len = end - first;
+  if (first < 0) return fail(ctx, XG_ERR_ARG, "negative waveform offset");
   if (kind < 0 || kind > 3) return fail(ctx, XG_ERR_ARG, "unknown waveform kind");
   if (len < need[kind]) return fail(ctx, XG_ERR_ARG, "waveform has too few values");
   if (kind == XG_WAVE_PWL && (len % 2) != 0) return fail(ctx, XG_ERR_ARG, "PWL needs time/value pairs");
@@ -233,12 +249,14 @@ static int check_wave(xg_ctx *ctx, int kind, int len) {
 
 int xg_add_vsources(xg_ctx *ctx, int n, const int *pos, const int *neg, const int *branch, const int *kind,
                     const int *off, const double *data) {
-  SETUP_CHECK();
+  SETUP_CHECK(pos, neg, branch, kind, off, data);
   for (int k = 0; k < n; ++k) {
     if (!valid_node(ctx, pos[k]) || !valid_node(ctx, neg[k]) || branch[k] < 0 || branch[k] >= ctx->n)
       return fail(ctx, XG_ERR_ARG, "voltage source node out of range");
-    int rc = check_wave(ctx, kind[k], off[k + 1] - off[k]);
+    int rc = check_wave(ctx, kind[k], off[k], off[k + 1]);
     if (rc) return rc;
+  }
+  for (int k = 0; k < n; ++k) {
     ctx->v_p.push_back(pos[k]); ctx->v_n.push_back(neg[k]); ctx->v_b.push_back(branch[k]);
     ctx->v_w.push_back({kind[k], std::vector<double>(data + off[k], data + off[k + 1])});
   }
@@ -247,11 +265,13 @@ int xg_add_vsources(xg_ctx *ctx, int n, const int *pos, const int *neg, const in
 
 int xg_add_isources(xg_ctx *ctx, int n, const int *pos, const int *neg, const int *kind, const int *off,
                     const double *data) {
-  SETUP_CHECK();
+  SETUP_CHECK(pos, neg, kind, off, data);
   for (int k = 0; k < n; ++k) {
     if (!valid_node(ctx, pos[k]) || !valid_node(ctx, neg[k])) return fail(ctx, XG_ERR_ARG, "current source node out of range");
-    int rc = check_wave(ctx, kind[k], off[k + 1] - off[k]);
+    int rc = check_wave(ctx, kind[k], off[k], off[k + 1]);
     if (rc) return rc;
+  }
+  for (int k = 0; k < n; ++k) {
     ctx->i_p.push_back(pos[k]); ctx->i_n.push_back(neg[k]);
     ctx->i_w.push_back({kind[k], std::vector<double>(data + off[k], data + off[k + 1])});
   }
@@ -259,22 +279,24 @@ int xg_add_isources(xg_ctx *ctx, int n, const int *pos, const int *neg, const in
 }
 
 int xg_add_diodes(xg_ctx *ctx, int n, const int *pos, const int *neg, const int *pri, const double *params) {
-  SETUP_CHECK();
+  SETUP_CHECK(pos, neg, pri, params);
   for (int k = 0; k < n; ++k) {
     if (!valid_node(ctx, pos[k]) || !valid_node(ctx, neg[k]) || !valid_node(ctx, pri[k]))
       return fail(ctx, XG_ERR_ARG, "diode node out of range");
     const double *p = params + (size_t)k * XG_DIODE_NPARAM;
     if ((p[XG_DIODE_RS] == 0.0) != (pri[k] == pos[k]))
       return fail(ctx, XG_ERR_ARG, "diode internal node must equal pos exactly when RS = 0");
-    ctx->d_p.push_back(pos[k]); ctx->d_n.push_back(neg[k]); ctx->d_r.push_back(pri[k]);
-    ctx->d_par.insert(ctx->d_par.end(), p, p + XG_DIODE_NPARAM);
   }
+  ctx->d_p.insert(ctx->d_p.end(), pos, pos + n);
+  ctx->d_n.insert(ctx->d_n.end(), neg, neg + n);
+  ctx->d_r.insert(ctx->d_r.end(), pri, pri + n);
+  ctx->d_par.insert(ctx->d_par.end(), params, params + (size_t)n * XG_DIODE_NPARAM);
   return XG_OK;
 }
 
 int xg_add_mosfet1(xg_ctx *ctx, int n, const int *dd, const int *g, const int *s, const int *b,
                    const double *params) {
-  SETUP_CHECK();
+  SETUP_CHECK(dd, g, s, b, params);
   for (int k = 0; k < n; ++k) {
     if (!valid_node(ctx, dd[k]) || !valid_node(ctx, g[k]) || !valid_node(ctx, s[k]) || !valid_node(ctx, b[k]))
       return fail(ctx, XG_ERR_ARG, "MOSFET node out of range");
@@ -282,15 +304,18 @@ int xg_add_mosfet1(xg_ctx *ctx, int n, const int *dd, const int *g, const int *s
     if (p[XG_MOS1_RD] != 0.0 || p[XG_MOS1_RS] != 0.0)
       return fail(ctx, XG_ERR_UNSUPPORTED, "MOSFET level 1 with series drain/source resistance");
     if (p[XG_MOS1_TYPE] != 1.0 && p[XG_MOS1_TYPE] != -1.0) return fail(ctx, XG_ERR_ARG, "MOSFET TYPE must be +1 or -1");
-    ctx->m_d.push_back(dd[k]); ctx->m_g.push_back(g[k]); ctx->m_s.push_back(s[k]); ctx->m_b.push_back(b[k]);
-    ctx->m_par.insert(ctx->m_par.end(), p, p + XG_MOS1_NPARAM);
   }
+  ctx->m_d.insert(ctx->m_d.end(), dd, dd + n);
+  ctx->m_g.insert(ctx->m_g.end(), g, g + n);
+  ctx->m_s.insert(ctx->m_s.end(), s, s + n);
+  ctx->m_b.insert(ctx->m_b.end(), b, b + n);
+  ctx->m_par.insert(ctx->m_par.end(), params, params + (size_t)n * XG_MOS1_NPARAM);
   return XG_OK;
 }
 
 int xg_add_bsim4(xg_ctx *ctx, int n, const int *dd, const int *g, const int *s, const int *b,
                  const double *params) {
-  SETUP_CHECK();
+  SETUP_CHECK(dd, g, s, b, params);
   for (int k = 0; k < n; ++k) {
     if (!valid_node(ctx, dd[k]) || !valid_node(ctx, g[k]) || !valid_node(ctx, s[k]) || !valid_node(ctx, b[k]))
       return fail(ctx, XG_ERR_ARG, "BSIM4 node out of range");
@@ -299,9 +324,12 @@ int xg_add_bsim4(xg_ctx *ctx, int n, const int *dd, const int *g, const int *s, 
     std::string why;
     int rc = b4::setup(p, probe, &why);
     if (rc) return fail(ctx, rc, "BSIM4: " + why);
-    ctx->b_d.push_back(dd[k]); ctx->b_g.push_back(g[k]); ctx->b_s.push_back(s[k]); ctx->b_b.push_back(b[k]);
-    ctx->b_par.insert(ctx->b_par.end(), p, p + XG_B4_NPARAM);
   }
+  ctx->b_d.insert(ctx->b_d.end(), dd, dd + n);
+  ctx->b_g.insert(ctx->b_g.end(), g, g + n);
+  ctx->b_s.insert(ctx->b_s.end(), s, s + n);
+  ctx->b_b.insert(ctx->b_b.end(), b, b + n);
+  ctx->b_par.insert(ctx->b_par.end(), params, params + (size_t)n * XG_B4_NPARAM);
   return XG_OK;
 }
 
@@ -336,6 +364,23 @@ int xg_finalize(xg_ctx *ctx) {
     if (!same_circuit({ctx->d_p[k], ctx->d_n[k], ctx->d_r[k]})) return fail(ctx, XG_ERR_ARG, "diode spans two circuits");
   for (int k = 0; k < nb; ++k)
     if (!same_circuit({ctx->b_d[k], ctx->b_g[k], ctx->b_s[k], ctx->b_b[k]})) return fail(ctx, XG_ERR_ARG, "BSIM4 spans two circuits");
+  for (size_t k = 0; k < ctx->r_p.size(); ++k)
+    if (!same_circuit({ctx->r_p[k], ctx->r_n[k]})) return fail(ctx, XG_ERR_ARG, "resistor spans two circuits");
+  for (size_t k = 0; k < ctx->c_p.size(); ++k)
+    if (!same_circuit({ctx->c_p[k], ctx->c_n[k]})) return fail(ctx, XG_ERR_ARG, "capacitor spans two circuits");
+  for (int k = 0; k < nv; ++k)
+    if (!same_circuit({ctx->v_p[k], ctx->v_n[k], ctx->v_b[k]}))
+      return fail(ctx, XG_ERR_ARG, "voltage source spans two circuits");
+  for (int k = 0; k < ni; ++k)
+    if (!same_circuit({ctx->i_p[k], ctx->i_n[k]})) return fail(ctx, XG_ERR_ARG, "current source spans two circuits");
+  {
+    // two voltage sources on one branch unknown would share its row
+    std::vector<char> seen(n, 0);
+    for (int k = 0; k < nv; ++k) {
+      if (seen[ctx->v_b[k]]) return fail(ctx, XG_ERR_ARG, "two voltage sources share a branch unknown");
+      seen[ctx->v_b[k]] = 1;
+    }
+  }
   // matrix stamp positions (row, col); -1 for ground rows/cols.  Every
   // position is enumerated twice (count, then fill) into one flat array, and
   // each row is sorted and deduplicated in place.  Node unknowns keep a
