@@ -124,7 +124,10 @@ int xg_synchronize(xg_ctx *ctx);
 /* ---- topology upload (host arrays) ---------------------------------------
  * Replaces Topology::registerLIDswithDevs + Builder::generateGraphs
  * (N_CIR_Xyce.C:657-696, N_LAS_Builder.C:384-418).  n_circuits independent
- * circuits occupy contiguous unknown ranges [offsets[c], offsets[c+1]). */
+ * circuits occupy contiguous unknown ranges [offsets[c], offsets[c+1]).
+ * Node index -1 is ground.  Each xg_add_* call checks all n items (node
+ * ranges, values, cards) before it appends any: a call that fails leaves the
+ * topology as it was. */
 int xg_set_unknowns(xg_ctx *ctx, int n_unknowns, int n_circuits, const int *offsets);
 /* Resistor::Instance (N_DEV_Resistor.C), value in ohms. */
 int xg_add_resistors(xg_ctx *ctx, int n, const int *pos, const int *neg, const double *r);
@@ -151,7 +154,9 @@ int xg_add_bsim4(xg_ctx *ctx, int n, const int *d, const int *g, const int *s,
                  const int *b, const double *params);
 /* Builds the CSR pattern, the stamp map, device-resident SoA instance
  * arrays and the symbolic structures (DeviceMgr::initializeAll + setupPointers,
- * N_CIR_Xyce.C:698-717, N_DEV_Diode.C:778-800). */
+ * N_CIR_Xyce.C:698-717, N_DEV_Diode.C:778-800).  XG_ERR_ARG when a device or
+ * source connects unknowns of two circuits, or two voltage sources share a
+ * branch unknown. */
 int xg_finalize(xg_ctx *ctx);
 
 int xg_get_sizes(xg_ctx *ctx, int *n_unknowns, int *nnz, int *n_state, int *n_store);
