@@ -138,9 +138,7 @@ def _cpu_ring_task(args):
     nl = N.extract_circuit(_BATCH, idx)
     nl.tran.max_steps = n_steps
     t0 = time.perf_counter()
-    o = oracle.Oracle(nl)
-    o.use_minimum_degree()  # KLU's symbolic ordering, once per circuit
-    _, _, st = o.transient(nl.tran, probes=[0], cap=8)
+    _, _, st = oracle.Oracle(nl).transient(nl.tran, probes=[0], cap=8)
     return st["accepted"], time.perf_counter() - t0
 
 
@@ -169,14 +167,15 @@ def cpu_ring(n_steps):
     nl, probes, _ = _workload("ring")
     nl.tran.max_steps = n_steps
     t0 = time.perf_counter()
-    o = oracle.Oracle(nl)
-    o.use_minimum_degree()
-    _, _, st = o.transient(nl.tran, probes=probes, cap=8)
+    _, _, st = oracle.Oracle(nl).transient(nl.tran, probes=probes, cap=8)
     dt = time.perf_counter() - t0
     return st["accepted"] / dt, st["accepted"], dt
 
 
 def cpu_baseline(args):
+    # Rings keep the LU's natural order: it fills little there, while a
+    # minimum-degree order with threshold pivoting fills a long ring's
+    # operating-point factors (5.7 s against 4 ms for 3,001 stages).
     w = WORKLOADS[args.workload]
     if args.workload == "mc":
         cores = os.cpu_count() or 1
@@ -184,13 +183,13 @@ def cpu_baseline(args):
         return {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                 "sample": f"{w['cpu_rings']} rings of the same batch, first {w['cpu_steps']} accepted "
                           f"steps of each from its operating point ({steps} steps, {wall:.1f} s wall), "
-                          f"CPU FP64 restatement (oracle/, minimum-degree LU order), one ring per "
-                          f"process on {cores} processes"}
+                          f"CPU FP64 restatement (oracle/, LU in the ring's natural order), one ring "
+                          f"per process on {cores} processes"}
     v, steps, dt = cpu_ring(w["cpu_steps"])
     return {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": f"first {steps} accepted steps of the same circuit from its operating point "
-                      f"({dt:.1f} s), CPU FP64 restatement (oracle/, minimum-degree LU order), "
-                      f"one thread"}
+                      f"({dt:.1f} s), CPU FP64 restatement (oracle/, LU in the ring's natural "
+                      f"order), one thread"}
 
 
 def run_reference(args):
