@@ -1241,9 +1241,23 @@ extern "C" int xg_tran_start(xg_ctx *ctx, const xg_tran_params *p, int n_probe, 
   if (!ctx || !p) return XG_ERR_ARG;
   if (!ctx->finalized) return fail(ctx, XG_ERR_STATE, "not finalized");
   if (!(p->tstop > p->tstart)) return fail(ctx, XG_ERR_ARG, "tstop must exceed tstart");
+  if (!std::isfinite(p->tstart) || !std::isfinite(p->tstop)) return fail(ctx, XG_ERR_ARG, "tstart and tstop must be finite");
   if (cap < 0 || n_probe < 0) return fail(ctx, XG_ERR_ARG, "negative cap or probe count");
+  if (n_probe > 0 && !probes) return fail(ctx, XG_ERR_ARG, "null probe list");
   if (p->method != 0 && p->method != XG_METHOD_ONESTEP && p->method != XG_METHOD_GEAR)
     return fail(ctx, XG_ERR_ARG, "method must be XG_METHOD_ONESTEP or XG_METHOD_GEAR");
+  {
+    // the error weights and the Newton tests divide by or compare against these
+    auto positive = [](double v) { return v > 0.0 && std::isfinite(v); };
+    auto nonnegative = [](double v) { return v >= 0.0 && std::isfinite(v); };
+    if (!positive(p->reltol) || !positive(p->abstol) || !positive(p->nl_reltol) || !positive(p->nl_abstol) ||
+        !positive(p->nl_deltaxtol) || !positive(p->nl_rhstol))
+      return fail(ctx, XG_ERR_ARG, "tolerances must be positive and finite");
+    if (!nonnegative(p->nl_smallupdatetol) || !nonnegative(p->hmin) || !nonnegative(p->hmax))
+      return fail(ctx, XG_ERR_ARG, "nl_smallupdatetol, hmin and hmax must be non-negative and finite");
+    if (p->nl_maxstep < 1) return fail(ctx, XG_ERR_ARG, "nl_maxstep must be at least 1");
+    if (p->max_order < 0 || p->max_order > 2) return fail(ctx, XG_ERR_ARG, "max_order must be 1 or 2 (0 = 2)");
+  }
   CK(cudaSetDevice(ctx->device));
   if (ctx->run) xg_free_run(ctx);
   ctx->run = new TranRun;
