@@ -47,3 +47,20 @@ def test_device_across_circuits_refused(xg, cuda):
     assert L.xg_finalize(h) == -1  # XG_ERR_ARG
     assert b"spans two circuits" in L.xg_error_string(h)
     assert L.xg_destroy(h) == xg.XG_OK
+
+
+def test_transient_parameters_checked(xg, cuda):
+    """Tolerances the error weights divide by, the Newton step limit and the
+    order are checked before anything is allocated; the context stays usable."""
+    import dataclasses
+    from xyce_gb300 import netlist as N
+    nl = N.rc_step()
+    c = xg.Circuit(nl)
+    for bad in (dict(reltol=0.0), dict(abstol=-1e-9), dict(nl_rhstol=float("nan")), dict(nl_maxstep=0),
+                dict(max_order=3), dict(hmin=-1.0)):
+        with pytest.raises(xg.XgError) as e:
+            c.tran_start(dataclasses.replace(nl.tran, **bad), probes=[nl.names["out"]], cap=16)
+        assert e.value.code == -1
+    counts, t, v, st = c.transient(probes=[nl.names["out"]], cap=20000)
+    assert st["status"] == 0 and counts[0] > 10
+    c.close()

@@ -380,10 +380,7 @@ class Circuit:
         times is [n_circuits, cap] and values [n_circuits, cap, pmax]."""
         tran = tran or self.netlist.tran
         probes = np.asarray(probes, np.int32)
-        tp = TranParams(tran.tstart, tran.tstop, tran.hmax, tran.hmin, tran.reltol, tran.abstol,
-                        tran.nl_reltol, tran.nl_abstol, tran.nl_deltaxtol, tran.nl_rhstol,
-                        tran.nl_smallupdatetol, tran.nl_maxstep, tran.max_steps, tran.max_order,
-                          tran.method)
+        tp = self._tran_params(tran)
         nc = self.n_circuits
         offs = np.asarray(self.netlist.offsets)
         per = np.bincount(np.searchsorted(offs, probes, side="right") - 1, minlength=nc) \
