@@ -174,6 +174,22 @@ def test_timeint_method(opt, method, order):
     assert d.netlist.tran.method == method and d.netlist.tran.max_order == order
 
 
+def test_nonlin_tran_and_linsol_options():
+    """.OPTIONS NONLIN-TRAN sets the transient Newton's tolerances (the keys of
+    N_NLS_NLParams.C:191-220); .OPTIONS LINSOL accepts the direct solvers."""
+    d = S.parse("t\nR1 a 0 1\nC1 a 0 1n\nI1 0 a PULSE(0 1m 1n)\n.TRAN 1n 1u\n"
+                ".OPTIONS NONLIN-TRAN RELTOL=1e-4 ABSTOL=1e-9 DELTAXTOL=0.1 RHSTOL=1e-3\n"
+                "+ SMALLUPDATETOL=1e-8 MAXSTEP=40\n.OPTIONS LINSOL TYPE=KLU\n.END\n")
+    tr = d.netlist.tran
+    assert (tr.nl_reltol, tr.nl_abstol, tr.nl_deltaxtol, tr.nl_rhstol) == (1e-4, 1e-9, 0.1, 1e-3)
+    assert tr.nl_smallupdatetol == 1e-8 and tr.nl_maxstep == 40 and isinstance(tr.nl_maxstep, int)
+    assert tr.reltol == 1e-3  # TIMEINT untouched
+    for bad, msg in (("NONLIN-TRAN NLSTRATEGY=1", "NONLIN-TRAN NLSTRATEGY"),
+                     ("LINSOL TYPE=AZTECOO", "LINSOL TYPE=AZTECOO"), ("LINSOL TYPE=IR", "LINSOL TYPE=IR")):
+        with pytest.raises(ValueError, match=msg):
+            S.parse(f"t\nR1 a 0 1\n.TRAN 1n 1u\n.OPTIONS {bad}\n.END\n")
+
+
 def test_nested_subcircuits_and_diode_model():
     d = S.parse("""nested subcircuits
 .SUBCKT LEAF a b

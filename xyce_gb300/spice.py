@@ -9,7 +9,9 @@ output.  The subset is what the path simulates:
   ``D`` (diode level 1), ``M`` (MOSFET level 1; level 54/14 = BSIM4 4.8.2),
   ``X`` (subcircuit instances, flattened);
 * ``.MODEL``, ``.SUBCKT``/``.ENDS``, ``.TRAN``, ``.OPTIONS TIMEINT``
-  (RELTOL, ABSTOL, METHOD=TRAP|GEAR, MAXORD), ``.PARAM`` with ``{NAME}``
+  (RELTOL, ABSTOL, METHOD=TRAP|GEAR, MAXORD), ``.OPTIONS NONLIN-TRAN``
+  (RELTOL, ABSTOL, DELTAXTOL, RHSTOL, SMALLUPDATETOL, MAXSTEP),
+  ``.OPTIONS LINSOL TYPE=KLU|KSPARSE``, ``.PARAM`` with ``{NAME}``
   references, ``.STEP`` (linear or LIST; every point of the sweep runs as one
   circuit of a single GPU batch), ``.SAMPLING`` with ``.OPTIONS SAMPLES``
   (Latin hypercube or Monte Carlo samples of NORMAL / UNIFORM parameters,
@@ -391,6 +393,12 @@ class _Builder:
                 self.nl.I(a, b, k, data)
 
 
+
+# .OPTIONS NONLIN-TRAN keys and the transient fields they set
+_NONLIN_TRAN = {"RELTOL": "nl_reltol", "ABSTOL": "nl_abstol", "DELTAXTOL": "nl_deltaxtol",
+                "RHSTOL": "nl_rhstol", "SMALLUPDATETOL": "nl_smallupdatetol", "MAXSTEP": "nl_maxstep"}
+
+
 def parse(text: str, overrides: dict | None = None) -> Deck:
     """Parse a netlist (the first line is the title, as in SPICE).
     overrides: {parameter or element name: value} — one point of a .STEP
@@ -448,6 +456,7 @@ def parse(text: str, overrides: dict | None = None) -> Deck:
     tran = None
     tstep = 0.0
     reltol = abstol = method = maxord = None
+    nonlin = {}
     deck = B.deck
     for ln, toks in body_lines:
         head = toks[0].upper()
@@ -506,6 +515,18 @@ def parse(text: str, overrides: dict | None = None) -> Deck:
                             raise ValueError("MAXORD must be 1 or 2")
                     else:
                         raise ValueError(f".OPTIONS TIMEINT {k} is not supported")
+            elif pkg == "NONLIN-TRAN":
+                # the transient Newton's options (N_NLS_NLParams.C:191-220)
+                for k, v in kv.items():
+                    if k not in _NONLIN_TRAN:
+                        raise ValueError(f".OPTIONS NONLIN-TRAN {k} is not supported")
+                    nonlin[_NONLIN_TRAN[k]] = int(number(v)) if k == "MAXSTEP" else number(v)
+            elif pkg == "LINSOL":
+                # every direct solver the reference offers factors and solves the
+                # same system; this path's is the GPU LU
+                for k, v in kv.items():
+                    if k != "TYPE" or v.upper() not in ("DEFAULT", "KLU", "KSPARSE"):
+                        raise ValueError(f".OPTIONS LINSOL {k}={v} is not supported")
             else:
                 raise ValueError(f".OPTIONS {pkg} is not supported")
         elif head == ".PRINT":
@@ -532,6 +553,8 @@ def parse(text: str, overrides: dict | None = None) -> Deck:
         tran.method = method
     if maxord is not None:
         tran.max_order = maxord
+    for k, v in nonlin.items():
+        setattr(tran, k, v)
     B.finish_sources(tstep, tran.tstop)
     B.nl.tran = tran
     B.nl.end_circuit()
