@@ -128,6 +128,31 @@ def test_measures():
     assert S.measure("MAX", t, v, frm=0.5, to=2.5) == 2.0
 
 
+@pytest.mark.parametrize("fmt", ["CSV", "NOINDEX"])
+def test_print_formats(tmp_path, fmt):
+    """.PRINT TRAN FORMAT=CSV writes <deck>.csv (comma-delimited, unpadded,
+    no Index, no footer); FORMAT=NOINDEX the .prn table without Index."""
+    d = S.parse(RC.replace(".PRINT TRAN", f".PRINT TRAN FORMAT={fmt}"))
+    assert d.print_format == fmt and d.prints[:1] == ["V(OUT)"]
+    t = np.array([0.0, 1e-9])
+    cols = {k: np.array([0.5, -1.25e-3]) for k in d.prints}
+    res = S.Result(t, cols, {}, {})
+    out = S.write_print(str(tmp_path / "rc.cir"), d, res)
+    lines = open(out).read().splitlines()
+    if fmt == "CSV":
+        assert out.endswith("rc.cir.csv")
+        assert lines[0] == ",".join(["TIME"] + d.prints)
+        assert lines[1].split(",")[:2] == ["0.000000000e+00", "5.000000000e-01"]
+        assert lines[2].split(",")[1] == "-1.250000000e-03" and len(lines) == 3
+    else:
+        assert out.endswith("rc.cir.prn")
+        assert lines[0].split() == ["TIME"] + d.prints and lines[-1] == "End of Xyce(TM) Simulation"
+        assert lines[1] == "  0.000000000e+00" + " " + "  5.000000000e-01" + " " + \
+            " ".join(["  5.000000000e-01"] * (len(d.prints) - 1))
+    with pytest.raises(ValueError, match="WIDTH"):
+        S.parse(RC.replace(".PRINT TRAN", ".PRINT TRAN WIDTH=12"))
+
+
 def test_prn_layout_and_round_trip(tmp_path):
     d = S.parse(RC)
     t = np.array([0.0, 1e-9, 2.5e-9])

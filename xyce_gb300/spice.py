@@ -15,7 +15,8 @@ output.  The subset is what the path simulates:
   references, ``.STEP`` (linear or LIST; every point of the sweep runs as one
   circuit of a single GPU batch), ``.SAMPLING`` with ``.OPTIONS SAMPLES``
   (Latin hypercube or Monte Carlo samples of NORMAL / UNIFORM parameters,
-  all samples one batch, moments of every .MEASURE), ``.PRINT TRAN``, ``.MEASURE TRAN`` (MAX, MIN, PP, AVG,
+  all samples one batch, moments of every .MEASURE), ``.PRINT TRAN`` (FORMAT=STD,
+  NOINDEX or CSV), ``.MEASURE TRAN`` (MAX, MIN, PP, AVG,
   RMS, INTEG with FROM/TO), ``.END``; ``*`` and ``;`` comments, ``+``
   continuation lines, engineering suffixes (T G MEG K M MIL U N P F);
 * print variables ``V(n)``, ``V(a,b)``, ``I(Vname)``, ``TIME``, ``TEMP``
@@ -147,6 +148,7 @@ class Deck:
     netlist: N.Netlist
     title: str = ""
     prints: list[str] = field(default_factory=list)
+    print_format: str = "STD"                         # .PRINT TRAN FORMAT=STD|NOINDEX|CSV
     measures: list[Measure] = field(default_factory=list)
     tstep: float = 0.0
     element_values: dict[str, float] = field(default_factory=dict)
@@ -532,7 +534,14 @@ def parse(text: str, overrides: dict | None = None) -> Deck:
         elif head == ".PRINT":
             if len(toks) < 2 or toks[1].upper() != "TRAN":
                 raise ValueError("only .PRINT TRAN is supported")
-            deck.prints.extend(_print_vars(toks[2:]))
+            rest = toks[2:]
+            while len(rest) >= 3 and rest[1] == "=":
+                key, val = rest[0].upper(), rest[2].upper()
+                if key != "FORMAT" or val not in ("STD", "NOINDEX", "CSV"):
+                    raise ValueError(f".PRINT TRAN {key}={val} is not supported")
+                deck.print_format = val
+                rest = rest[3:]
+            deck.prints.extend(_print_vars(rest))
         elif head in (".MEASURE", ".MEAS"):
             deck.measures.append(_measure(toks[1:]))
         elif head.startswith("."):
@@ -892,9 +901,11 @@ def write_prn(path: str, deck: Deck, res) -> None:
     follow one another under one header, the Index restarting at 0 for each
     step, and the footer reads "End of Xyce(TM) Parameter Sweep"
     (TimePrn::doStartStep / doSteppingComplete,
-    src/IOInterfacePKG/N_IO_OutputterTimePrn.C:165-230)."""
+    src/IOInterfacePKG/N_IO_OutputterTimePrn.C:165-230).  FORMAT=NOINDEX
+    drops the Index column (printIndexColumn_, N_IO_OutputMgr.C:1655)."""
     results = res if isinstance(res, list) else [res]
     names = ["TIME"] + [p for p in deck.prints if p != "TIME"]
+    index = deck.print_format != "NOINDEX"
 
     def head(name, width=17):
         if width <= len(name):
@@ -902,14 +913,40 @@ def write_prn(path: str, deck: Deck, res) -> None:
         left = (width - len(name)) // 2
         return " " * left + name + " " * (width - left - len(name))
     with open(path, "w") as f:
-        f.write(" ".join(["Index"] + [head(n) for n in names]) + "\n")
+        f.write(" ".join((["Index"] if index else []) + [head(n) for n in names]) + "\n")
         for r in results:
             cols = [r.times] + [r.columns[p] for p in names[1:]]
             for i in range(len(r.times)):
-                row = [f"{i:<5d}"] + [f"{c[i]:>17.9e}" for c in cols]
+                row = ([f"{i:<5d}"] if index else []) + [f"{c[i]:>17.9e}" for c in cols]
                 f.write(" ".join(row) + "\n")
         f.write("End of Xyce(TM) Parameter Sweep\n" if isinstance(res, list) and len(results) > 1
                 else "End of Xyce(TM) Simulation\n")
+
+
+def write_csv(path: str, deck: Deck, res) -> None:
+    """FORMAT=CSV: TIME and the .PRINT columns, comma-delimited, names and
+    values unpadded, 9 digits after the point, no Index column and no footer
+    (TimeCSV, src/IOInterfacePKG/N_IO_OutputterTimeCSV.C:100-170; columns
+    and delimiter N_IO_OutputterLocal.C:201-215, 402-425, 452-470).  A sweep's
+    steps follow one another under the one header."""
+    results = res if isinstance(res, list) else [res]
+    names = ["TIME"] + [p for p in deck.prints if p != "TIME"]
+    with open(path, "w") as f:
+        f.write(",".join(names) + "\n")
+        for r in results:
+            cols = [r.times] + [r.columns[p] for p in names[1:]]
+            for i in range(len(r.times)):
+                f.write(",".join(f"{c[i]:.9e}" for c in cols) + "\n")
+
+
+def write_print(path: str, deck: Deck, res) -> str:
+    """The .PRINT TRAN output in the deck's format; returns the file written
+    (path + ".csv" for FORMAT=CSV, else path + ".prn")."""
+    if deck.print_format == "CSV":
+        write_csv(path + ".csv", deck, res)
+        return path + ".csv"
+    write_prn(path + ".prn", deck, res)
+    return path + ".prn"
 
 
 def read_prn(path: str) -> tuple[list[str], np.ndarray]:
@@ -930,7 +967,8 @@ def write_mt0(path: str, deck: Deck, res: Result) -> None:
 
 def main(argv=None) -> int:
     """``python -m xyce_gb300.spice netlist.cir`` — run the transient on the
-    GPU and write ``netlist.cir.prn`` (and ``netlist.cir.mt0`` with .MEASURE)."""
+    GPU and write ``netlist.cir.prn`` (``.csv`` for FORMAT=CSV; and
+    ``netlist.cir.mt0`` with .MEASURE)."""
     argv = sys.argv[1:] if argv is None else argv
     if len(argv) != 1:
         print("usage: python -m xyce_gb300.spice <netlist>", file=sys.stderr)
@@ -944,36 +982,33 @@ def main(argv=None) -> int:
             raise ValueError(".SAMPLING and .STEP together are not supported")
         decks = parse_sampling(text)
         results = run_sweep(decks)
-        if base.prints:
-            write_prn(path + ".prn", base, results)
+        out = write_print(path, base, results) if base.prints else path + ".ms0"
         with open(path + ".ms0", "w") as f:
             for m in base.measures:
                 st = sample_moments([r.measures[m.name] for r in results])
                 line = f"{m.name}: " + ", ".join(f"{k} = {v:.6e}" for k, v in st.items())
                 f.write(line + "\n")
                 print(line)
-        print(f"{len(decks)} samples run as one batch; output {os.path.basename(path)}.prn")
+        print(f"{len(decks)} samples run as one batch; output {os.path.basename(out)}")
         return 0
     decks = parse_sweep(text)
     deck = decks[0]
     if len(decks) == 1:
         res = run(deck)
-        if deck.prints:
-            write_prn(path + ".prn", deck, res)
+        out = write_print(path, deck, res) if deck.prints else path + ".mt0"
         if deck.measures:
             write_mt0(path + ".mt0", deck, res)
             for m in deck.measures:
                 print(f"{m.name} = {res.measures[m.name]:.6e}")
         print(f"{len(res.times)} accepted time points, {res.stats.get('rejected', 0)} rejected; "
-              f"output {os.path.basename(path)}.prn")
+              f"output {os.path.basename(out)}")
         return 0
     results = run_sweep(decks)
-    if deck.prints:
-        write_prn(path + ".prn", deck, results)
+    out = write_print(path, deck, results) if deck.prints else path + ".mt0"
     if deck.measures:  # one measure file per step: .mt0, .mt1, ...
         for k, (d, r) in enumerate(zip(decks, results)):
             write_mt0(path + f".mt{k}", d, r)
-    print(f"{len(decks)} sweep points run as one batch; output {os.path.basename(path)}.prn")
+    print(f"{len(decks)} sweep points run as one batch; output {os.path.basename(out)}")
     return 0
 
 
