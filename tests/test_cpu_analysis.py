@@ -62,3 +62,13 @@ def test_ring_batch_groups(xg, oracle_mod):
 def test_analyze_pattern_rejects_bad_input(xg):
     with pytest.raises(xg.XgError):
         xg.analyze_pattern(np.array([0, 1, 2]), np.array([0, 5]), np.ones(2))  # column out of range
+
+
+def test_analysis_is_deterministic(xg, oracle_mod):
+    """The host analysis orders components on several threads; its result
+    does not depend on their timing."""
+    m = _matrix(oracle_mod, N.monte_carlo_rings(24))
+    runs = [xg.analyze_pattern(*m) for _ in range(3)]
+    assert runs[0] == runs[1] == runs[2]
+    forced = [xg.analyze_pattern(*m, ordering=o) for o in (xg.ORDER_ND, xg.ORDER_MIN_DEGREE)]
+    assert {f["ordering"] for f in forced} == {"nested_dissection", "min_degree"}
