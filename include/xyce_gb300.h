@@ -202,8 +202,11 @@ int xg_lu_solve(xg_ctx *ctx, const double *rhs, double *x);
  * inputs and outputs as xg_lu_solve (device pointers; the factorization comes
  * from xg_lu_factor on ctx).  Returns XG_ERR_ARG when the system has more than
  * XG_NOALLOC_MAX_N unknowns.  The first call on a device looks the scratch
- * address up; make it before any stream capture.  Every call shares the one
- * scratch array: calls that overlap on the GPU race. */
+ * address up and keeps it for the life of the process; make that call
+ * before any stream capture, and do not reset the device (cudaDeviceReset)
+ * while the library is in use: the kept address belongs to the context it
+ * was looked up in.  Every call shares the one scratch array: calls that
+ * overlap on the GPU race. */
 #define XG_NOALLOC_MAX_N 262144
 int xg_lu_solve_noalloc(xg_ctx *ctx, const double *rhs, double *x);
 

@@ -16,7 +16,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 KSPARSE_PATH = os.path.join(HERE, "_ref", "libksparse.so")
-REFERENCE_KSPARSE = "/root/reference/src/LinearAlgebraServicesPKG/ksparse"
+# Root of the reference checkout (read only, and only where it exists): set
+# XYCE_REFERENCE_ROOT to point the build recipe and the netlist tests at it.
+REFERENCE_ROOT = os.environ.get("XYCE_REFERENCE_ROOT", "/root/reference")
+REFERENCE_KSPARSE = os.path.join(REFERENCE_ROOT, "src", "LinearAlgebraServicesPKG", "ksparse")
 
 _lib = None
 

@@ -4,10 +4,13 @@ import os
 import numpy as np
 import pytest
 
+import oracle
+
 from xyce_gb300 import netlist as N
 from xyce_gb300 import spice as S
 
-REF_TESTS = "/root/reference/test/CircuitPKG"  # the reference checkout, read only when present
+# the reference checkout's test netlists, read only when present
+REF_TESTS = os.path.join(oracle.REFERENCE_ROOT, "test", "CircuitPKG")
 
 
 @pytest.mark.parametrize("tok,val", [

@@ -64,3 +64,29 @@ def test_transient_parameters_checked(xg, cuda):
     counts, t, v, st = c.transient(probes=[nl.names["out"]], cap=20000)
     assert st["status"] == 0 and counts[0] > 10
     c.close()
+
+
+def test_rejected_tran_start_leaves_no_half_built_run(xg, cuda):
+    """A start rejected for a probe out of range or listed twice allocates
+    nothing and builds no run: advancing afterwards is XG_ERR_STATE.  A
+    rejected start after a good one keeps that run and its results."""
+    from xyce_gb300 import netlist as N
+    nl = N.rc_step()
+    c = xg.Circuit(nl)
+    out = nl.names["out"]
+    for probes in ([nl.n + 5], [out, out]):
+        with pytest.raises(xg.XgError) as e:
+            c.tran_start(probes=probes, cap=16)
+        assert e.value.code == -1
+        with pytest.raises(xg.XgError) as e:
+            c.tran_advance(4)
+        assert e.value.code == -3  # XG_ERR_STATE: no run
+    c.tran_start(probes=[out], cap=64)
+    c.tran_advance(5)
+    with pytest.raises(xg.XgError):
+        c.tran_start(probes=[out, out], cap=64)
+    c.tran_advance(5)  # the earlier run is still there
+    counts, t, v, st = c.tran_results()
+    assert st["accepted"] >= 10 and counts[0] >= 11
+    c.tran_end()
+    c.close()

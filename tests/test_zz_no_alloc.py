@@ -35,19 +35,45 @@ def _t(torch, a):
     return torch.as_tensor(np.ascontiguousarray(a, np.float64), device="cuda:0")
 
 
-def test_noalloc_solve_matches_allocated_solve(xg, oracle_mod, torch_cuda):
+_CASES = {
+    # a ring: the whole system factors in dependency-closed groups
+    "ring101": dict(make=lambda: N.ring_oscillator(101), sched=None),
+    # a grid whose upper separators form a large top, with the tops of the
+    # factorization and of both solves forced to one launch per level
+    # (k_toplv_*, k_lsolve_level, k_usolve_level read and write the scratch)
+    "grid40_levels": dict(make=lambda: N.power_grid(40, 50, seed=2), sched=(-1, 2, 2)),
+}
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32_ir"])
+@pytest.mark.parametrize("case", sorted(_CASES))
+def test_noalloc_solve_matches_allocated_solve(xg, oracle_mod, torch_cuda, case, prec):
+    """Two calls in a row, each against xg_lu_solve on the same factors, in
+    FP64 and in the FP32-factor + FP64-refinement form (whose refinement
+    solves also run on the static scratch)."""
     torch = torch_cuda
-    nl = N.ring_oscillator(101)
+    spec = _CASES[case]
+    nl = spec["make"]()
     c = xg.Circuit(nl)
+    if spec["sched"]:
+        c.lu_set_schedule(*spec["sched"])
+    if prec == "fp32_ir":
+        c.lu_set_precision(xg.PREC_FP32_IR, 2)
     o = oracle_mod.Oracle(nl)
-    _, x0, _ = o.dcop()
-    ld = o.load(x0)
+    rng = np.random.default_rng(17)
+    if case == "ring101":
+        _, x0, _ = o.dcop()
+        ld = o.load(x0)
+    else:
+        ld = o.load(rng.uniform(0.0, 1.0, o.n), newton_iter=1)
     vals = ld["dFdx"] + ld["dQdx"] / 1e-12
     v = _t(torch, vals)
     c.lu_analyze(v)
     c.lu_factor(v)
+    if spec["sched"]:
+        info = c.lu_info()
+        assert info["factor_top"] == "levels" and info["solve_top"] == "levels", info
     A = sp.csr_matrix((vals, o.col_idx, o.row_ptr), shape=(o.n, o.n))
-    rng = np.random.default_rng(17)
     for call in range(2):
         b = _t(torch, rng.standard_normal(o.n) * (10.0 ** call))
         x_ref = torch.zeros_like(b)

@@ -300,9 +300,9 @@ class Circuit:
         """Operating point + first analysis; keeps the run resident for tran_advance."""
         tran = tran or self.netlist.tran
         probes = np.asarray(probes, np.int32)
-        self._run = (len(probes), cap, probes)
         self._check(lib().xg_tran_start(self.h, C.byref(self._tran_params(tran)), len(probes),
                                         probes, int(cap)))
+        self._run = (len(probes), cap, probes)  # a rejected start keeps the earlier run's layout
 
     def tran_advance(self, n_steps: int):
         self._check(lib().xg_tran_advance(self.h, int(n_steps)))

@@ -1237,6 +1237,9 @@ int run_until_idle(TranRun &R) {
 
 }  // namespace
 
+static int tran_start_run(xg_ctx *ctx, const xg_tran_params *p, const std::vector<int> &probe_idx,
+                          const std::vector<int> &pcount, int cap);
+
 extern "C" int xg_tran_start(xg_ctx *ctx, const xg_tran_params *p, int n_probe, const int *probes, int cap) {
   if (!ctx || !p) return XG_ERR_ARG;
   if (!ctx->finalized) return fail(ctx, XG_ERR_STATE, "not finalized");
@@ -1258,22 +1261,41 @@ extern "C" int xg_tran_start(xg_ctx *ctx, const xg_tran_params *p, int n_probe, 
     if (p->nl_maxstep < 1) return fail(ctx, XG_ERR_ARG, "nl_maxstep must be at least 1");
     if (p->max_order < 0 || p->max_order > 2) return fail(ctx, XG_ERR_ARG, "max_order must be 1 or 2 (0 = 2)");
   }
+  // Everything a call can be rejected for is checked before the previous
+  // run is released: a rejected call leaves that run (and its results) as
+  // they were.
+  const int n = ctx->n, ncirc = ctx->ncirc;
+  std::vector<int> probe_idx(n, -1), pcount(ncirc, 0);
+  for (int k = 0; k < n_probe; ++k) {
+    if (probes[k] < 0 || probes[k] >= n) return fail(ctx, XG_ERR_ARG, "probe out of range");
+    if (probe_idx[probes[k]] != -1) return fail(ctx, XG_ERR_ARG, "probe listed twice");
+    probe_idx[probes[k]] = pcount[ctx->circ_of_row[probes[k]]]++;
+  }
+  if (ctx->predictor == XG_PRED_LEARNED && !ctx->mlp_ready)
+    return fail(ctx, XG_ERR_STATE, "learned predictor selected but no weights: call xg_mlp_set or xg_mlp_train");
   CK(cudaSetDevice(ctx->device));
   if (ctx->run) xg_free_run(ctx);
   ctx->run = new TranRun;
+  const int rc = tran_start_run(ctx, p, probe_idx, pcount, cap);
+  // a run that failed before its tick graph existed cannot advance: release it
+  if (rc != XG_OK && ctx->run && !ctx->run->exec) {
+    std::string keep = ctx->err;
+    cudaStreamSynchronize(ctx->stream);
+    xg_free_run(ctx);
+    ctx->err = keep;
+  }
+  return rc;
+}
+
+static int tran_start_run(xg_ctx *ctx, const xg_tran_params *p, const std::vector<int> &probe_idx,
+                          const std::vector<int> &pcount, int cap) {
   TranRun &R = *ctx->run;
   R.t0 = std::chrono::steady_clock::now();
   R.ctx = ctx;
   R.cap = cap;
   const int n = ctx->n, ncirc = ctx->ncirc;
   DevArrays &d = ctx->d;
-  std::vector<int> probe_idx(n, -1);
-  R.pcount.assign(ncirc, 0);
-  for (int k = 0; k < n_probe; ++k) {
-    if (probes[k] < 0 || probes[k] >= n) return fail(ctx, XG_ERR_ARG, "probe out of range");
-    int c = ctx->circ_of_row[probes[k]];
-    probe_idx[probes[k]] = R.pcount[c]++;
-  }
+  R.pcount = pcount;
   R.pmax = 1;
   for (int c = 0; c < ncirc; ++c) R.pmax = std::max(R.pmax, R.pcount[c]);
   CK(cudaMemcpyAsync(d.probe_idx, probe_idx.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
@@ -1281,8 +1303,6 @@ extern "C" int xg_tran_start(xg_ctx *ctx, const xg_tran_params *p, int n_probe, 
   if ((rc = dev_alloc(ctx, &d.out_t, (size_t)ncirc * std::max(cap, 1), R.allocs))) return rc;
   if ((rc = dev_alloc(ctx, &d.out_v, (size_t)ncirc * std::max(cap, 1) * R.pmax, R.allocs))) return rc;
   if ((rc = dev_alloc(ctx, &d.out_p, (size_t)ncirc * std::max(cap, 1) * R.pmax, R.allocs))) return rc;
-  if (ctx->predictor == XG_PRED_LEARNED && !ctx->mlp_ready)
-    return fail(ctx, XG_ERR_STATE, "learned predictor selected but no weights: call xg_mlp_set or xg_mlp_train");
   std::vector<std::vector<double>> cb(ncirc);
   for (int k = 0; k < ctx->nv; ++k) breakpoints(ctx->v_w[k], p->tstop, cb[ctx->circ_of_row[ctx->v_b[k]]]);
   for (int k = 0; k < ctx->ni; ++k) {
@@ -1348,7 +1368,7 @@ extern "C" int xg_tran_start(xg_ctx *ctx, const xg_tran_params *p, int n_probe, 
 
 extern "C" int xg_tran_advance(xg_ctx *ctx, int n_steps) {
   if (!ctx) return XG_ERR_ARG;
-  if (!ctx->run) return fail(ctx, XG_ERR_STATE, "call xg_tran_start first");
+  if (!ctx->run || !ctx->run->exec) return fail(ctx, XG_ERR_STATE, "call xg_tran_start first");
   TranRun &R = *ctx->run;
   launch_set_target_k(ctx->stream, ctx->d, ctx->ncirc, n_steps);
   launch_count_done_k(ctx->stream, ctx->d, ctx->ncirc, ctx->breakdown_dev, ctx->status_dev);
@@ -1446,6 +1466,7 @@ extern "C" int xg_transient(xg_ctx *ctx, const xg_tran_params *p, int n_probe, c
                             int *counts, double *times, double *values, xg_tran_stats *stats) {
   if (!ctx || !p) return XG_ERR_ARG;
   if (cap > 0 && (!counts || !times || (n_probe > 0 && !values))) return fail(ctx, XG_ERR_ARG, "output buffers required");
+  if (stats) memset(stats, 0, sizeof *stats);
   int rc = xg_tran_start(ctx, p, n_probe, probes, cap);
   if (rc == XG_OK && p->max_steps >= 0) rc = xg_tran_advance(ctx, p->max_steps > 0 ? p->max_steps : 0);
   int rr = XG_OK;
