@@ -305,6 +305,14 @@ int xg_tran_end(xg_ctx *ctx);
  * step started from — the training target of the learned predictor is the
  * accepted solution minus this guess. */
 int xg_tran_predictors(xg_ctx *ctx, double *pred_values);
+/* Integration order of the recorded points (layout of xg_tran_results'
+ * times, n_circuits x cap): 0 for the operating point, else the order the
+ * accepted step was integrated with (1 backward Euler / BDF1, 2 trapezoid /
+ * BDF2).  Together with the times it is the accepted step sequence, which
+ * another integrator can replay to compare solutions at identical points.
+ * No reference counterpart: Xyce keeps the order in
+ * WorkingIntegrationMethod and does not output it. */
+int xg_tran_orders(xg_ctx *ctx, int *orders);
 /* Steps and Newton iterations taken with the learned and with the
  * polynomial predictor in the current run (learned predictor mode). */
 int xg_tran_predictor_stats(xg_ctx *ctx, long long *learned_steps, long long *learned_iters,

@@ -78,6 +78,8 @@ def lib():
                                     C.POINTER(C.c_int), C.POINTER(TranStats)]
         L.orc_dcop.argtypes = [P, dp, C.POINTER(C.c_int)]
         L.orc_set_wall_log.argtypes = [P, C.c_void_p, C.c_int]
+        L.orc_set_replay.argtypes = [P, C.c_void_p, C.c_void_p, C.c_int]
+        L.orc_recorded_orders.argtypes = [P, ip, C.c_int]
         L.orc_set_linear_solver.argtypes = [P, C.c_int, C.c_double, C.c_double]
         L.orc_set_order.argtypes = [P, C.c_void_p, C.c_int]
         L.orc_lu_counts.argtypes = [P, np.ctypeslib.ndpointer(np.int64, flags="C"), C.c_int]
@@ -192,6 +194,30 @@ class Oracle:
         st = lib().orc_dcop(self.h, x, C.byref(it))
         return st, x, it.value
 
+    def replay(self, times, orders, tran=None, probes=None):
+        """Transient run through a given accepted-step sequence: times[k] and
+        orders[k] of point k (point 0 = the operating point), as recorded by
+        the GPU path (xg_tran_results / xg_tran_orders).  Every step goes to
+        the recorded time with the recorded order; returns what transient()
+        returns, at exactly those points."""
+        t = np.ascontiguousarray(times, np.float64)
+        o = np.ascontiguousarray(orders, np.int32)
+        if len(t) != len(o) or len(t) < 2:
+            raise ValueError("replay needs matching times and orders, at least two points")
+        if lib().orc_set_replay(self.h, t.ctypes.data, o.ctypes.data, len(t)) != 0:
+            raise ValueError("replay: times must increase and orders be 1 or 2")
+        try:
+            return self.transient(tran, probes, cap=len(t) + 1)
+        finally:
+            lib().orc_set_replay(self.h, None, None, 0)
+
+    def recorded_orders(self, count):
+        """Integration order of the points the last transient recorded (0 at
+        the operating point)."""
+        out = np.zeros(max(1, count), np.int32)
+        k = lib().orc_recorded_orders(self.h, out, len(out))
+        return out[:k]
+
     def transient(self, tran=None, probes=None, cap=2_000_000, wall_log=None):
         """Transient run; wall_log (float64 array) receives the wall-clock
         seconds at each accepted step when given."""
@@ -261,3 +287,33 @@ def ksparse_solve(row_ptr, col_idx, vals, b):
     if rc != 0:
         raise np.linalg.LinAlgError(f"ksparse status {rc}")
     return x
+
+
+def _replay_worker(task):
+    """One oracle run in a worker process: task = (netlist, probes, times,
+    orders, min_degree); times None = a free run.  Returns (values, stats)."""
+    nl, probes, times, orders, md = task
+    o = Oracle(nl)
+    if md:
+        o.use_minimum_degree()
+    if times is None:
+        t, v, st = o.transient(probes=probes)
+        return t, v, st
+    t, v, st = o.replay(times, orders, probes=probes)
+    return t, v, st
+
+
+def run_many(tasks, processes=None):
+    """Oracle runs of several circuits in parallel worker processes (spawned,
+    so that a caller holding a CUDA context may use it).  Each task is
+    (netlist, probes, times, orders, min_degree): with times and orders
+    given, a replay of that accepted-step sequence, else a free run.
+    Returns [(times, values, stats)] in task order."""
+    import multiprocessing as mp
+    if not os.path.exists(LIB_PATH):
+        build(with_reference=False)
+    procs = max(1, min(len(tasks), processes or os.cpu_count() or 1))
+    if procs == 1:
+        return [_replay_worker(t) for t in tasks]
+    with mp.get_context("spawn").Pool(procs) as pool:
+        return pool.map(_replay_worker, tasks, chunksize=1)

@@ -246,6 +246,11 @@ struct orc_ctx {
   long long n_factor = 0, n_reuse = 0, n_refined = 0, n_refine_steps = 0, n_fallback = 0;
   long long n_repeat = 0;
   std::vector<double> last_factored;  // CSC values of the last factorization
+  // replay of a given accepted-step sequence (orc_set_replay): times[k] and
+  // integration order[k] of accepted point k (point 0 = the operating point)
+  std::vector<double> replay_t;
+  std::vector<int> replay_o;
+  std::vector<int> rec_o;  // integration order of each point the last transient recorded
   // state layout: store diode [vd,qd,cd] then mos1 [vbd,vbs,vgs,vds,von,gm]
   // then bsim4 [vbd,vbs,vgs,vds,von]; state mos1 [capgs,capgd,capgb,qgs,qgd,
   // qgb,qbd,qbs] then bsim4 [qg,qd,qb]  (field-major, SoA)
@@ -1037,7 +1042,10 @@ extern "C" int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, 
   double stopTime = next_bp(t);
   std::vector<double> xh0(n), xh1(n, 0.0), xh2(n, 0.0), qh0(n), qh1(n, 0.0), qh2(n, 0.0), xn0(n), errwt(n);
   int nout = 0;
+  c->rec_o.clear();
+  int step_order = 0;  // order of the step being recorded (0: the operating point)
   auto record = [&](double tt, const std::vector<double> &xx) {
+    if (nout < cap) c->rec_o.push_back(step_order);
     if (nout < cap) {
       times[nout] = tt;
       for (int k = 0; k < n_probe; ++k) values[(size_t)nout * n_probe + k] = xx[probes[k]];
@@ -1045,8 +1053,16 @@ extern "C" int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, 
     }
   };
   record(t, w.xcurr);
+  // Replay: step k goes exactly to replay_t[k] with order replay_o[k], and
+  // the step stands whenever Newton converges (no error test, no
+  // rejections).  Everything else — histories, coefficients, predictors,
+  // breakpoints — follows the same code as a free run.
+  const int n_replay = (int)c->replay_t.size();
+  const bool replay = n_replay > 0;
   while (t < p->tstop - bptol) {
     if (p->max_steps > 0 && st->accepted >= p->max_steps) break;
+    if (replay && st->accepted + 1 >= n_replay) break;
+    const double h_replay = replay ? c->replay_t[st->accepted + 1] - t : 0.0;
     if (beginning && lastOk) {
       // OneStep::initialize (N_TIA_OneStep.C:1684-1800)
       double time_to_stop = stopTime - t;
@@ -1055,6 +1071,7 @@ extern "C" int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, 
       // (Gear12::initialize takes the restart step as is, N_TIA_Gear12.C:1225-1245)
       h = (t != p->tstart && !gear) ? std::min(h, hn) : hn;
       h = std::min(std::max(h, hmin), hmax);
+      if (replay) h = h_replay;
       tsum = 2.0 * h; lastTimeStep = h;
       if (gear) {
         // Gear12::initialize history (N_TIA_Gear12.C:1280-1300)
@@ -1066,6 +1083,11 @@ extern "C" int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, 
         for (int i = 0; i < n; ++i) qh1[i] = -(Fc[i] - Bc[i]) * h;
       }
       numberOfSteps = 0; order = 1; psi[0] = h;
+    }
+    if (replay) {
+      h = h_replay;
+      order = c->replay_o[st->accepted + 1];
+      if (!(h > 0.0) || (order != 1 && order != 2)) { st->status = -50; break; }
     }
     if (order == 2) psi[2] = psi[1];
     psi[1] = psi[0]; psi[0] = h;
@@ -1118,6 +1140,7 @@ extern "C" int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, 
     w.x = xn0;
     double tn = t + h;
     if (std::fabs(tn - stopTime) <= bptol) tn = stopTime;
+    if (replay) tn = c->replay_t[st->accepted + 1];
     Coef cf{1.0 / h, order == 2 ? 0.5 : 1.0, order == 2 ? 0.5 : 0.0, qh0.data(), qh2.data(), 0.0, 0};
     if (gear) {
       // Gear12::obtainJacobian (N_TIA_Gear12.C:477-500): (a0 / h) dQdx + dFdx
@@ -1132,7 +1155,8 @@ extern "C" int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, 
     st->newton_iters += iters;
     bool ok = ns > 0;
     if (!ok) st->newton_fail++;
-    if (ok) {
+    if (replay && !ok) { st->status = -51; break; }  // the replayed step did not converge
+    if (ok && !replay) {
       // StepErrorControl::evaluateStepError (N_TIA_StepErrorControl.C:458-575)
       bool test = (t == p->tstart) ? (stepNumber >= 1 && !beginning) : (stepNumber >= 1);
       if (test) {
@@ -1147,6 +1171,7 @@ extern "C" int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, 
     }
     if (ok) {
       // OneStep::completeStep (:2124-2240)
+      step_order = order;
       numberOfSteps++; nef = 0;
       double tprev = t;
       t = tn;
@@ -1277,6 +1302,26 @@ extern "C" int orc_lu_counts(orc_ctx *c, long long *out, int reset) {
   if (reset)
     c->n_factor = c->n_reuse = c->n_refined = c->n_refine_steps = c->n_fallback = c->n_repeat = 0;
   return 0;
+}
+
+// Replay of an accepted-step sequence (test support): times[k] and orders[k]
+// of the accepted points, k = 0 the operating point (its order is ignored);
+// n = 0 returns to free runs.
+extern "C" int orc_set_replay(orc_ctx *c, const double *times, const int *orders, int n) {
+  if (n < 0 || (n > 0 && (!times || !orders))) return -1;
+  for (int k = 1; k < n; ++k)
+    if (!(times[k] > times[k - 1]) || (orders[k] != 1 && orders[k] != 2)) return -1;
+  c->replay_t.assign(times, times + n);
+  c->replay_o.assign(orders, orders + n);
+  return 0;
+}
+
+// Integration order of each point the last transient recorded (0 for the
+// operating point); returns the count, at most cap.
+extern "C" int orc_recorded_orders(orc_ctx *c, int *out, int cap) {
+  const int k = std::min(cap, (int)c->rec_o.size());
+  for (int i = 0; i < k; ++i) out[i] = c->rec_o[i];
+  return k;
 }
 
 // Benchmark support: wall-clock time (seconds since the start of the

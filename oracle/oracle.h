@@ -114,6 +114,18 @@ int orc_set_linear_solver(orc_ctx *c, int type, double ir_tol, double ir_min_tol
  * bit for bit to the one factored before); reset != 0 zeroes them afterwards. */
 int orc_lu_counts(orc_ctx *c, long long *out, int reset);
 
+/* Replay of an accepted-step sequence (for comparisons at identical time
+ * points): the next orc_transient steps exactly to times[1], times[2], ...
+ * with integration orders orders[1], orders[2], ... (times[0] / orders[0]:
+ * the operating point), accepts every step whose Newton solve converges
+ * (status -51 otherwise) and stops after the last point.  n = 0 returns to
+ * free runs.  Returns -1 unless the times increase and the orders are 1 or 2. */
+int orc_set_replay(orc_ctx *c, const double *times, const int *orders, int n);
+
+/* Integration order of each point the last orc_transient recorded (0 for
+ * the operating point, else 1 or 2); returns how many were written (<= cap). */
+int orc_recorded_orders(orc_ctx *c, int *out, int cap);
+
 /* Benchmark support: record wall-clock seconds at each accepted step. */
 int orc_set_wall_log(orc_ctx *c, double *buf, int cap);
 

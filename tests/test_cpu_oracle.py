@@ -296,3 +296,38 @@ def test_linear_circuit_converges_in_one_newton_step(oracle_mod):
     nl.tran.nl_maxstep = 1
     t, v, st = oracle_mod.Oracle(nl).transient(probes=[nl.names["out"]])
     assert st["status"] == 0 and st["newton_fail"] == 0
+
+
+@pytest.mark.parametrize("method", [7, 8], ids=["onestep", "gear"])
+@pytest.mark.parametrize("maker,probes", [
+    (lambda: N.ring_oscillator(21, caps=True), ["n1", "n11"]),
+    (lambda: N.diode_ladder(50, seed=5), ["n1", "n25", "n50"]),
+], ids=["ring21", "ladder50"])
+def test_replay_reproduces_a_free_run(oracle_mod, maker, probes, method):
+    """Replaying a run's own accepted times and integration orders gives the
+    same points and values: replay changes which steps are taken, not how a
+    step is computed.  (A replayed step's size is recomputed as the
+    difference of two recorded times, which may differ from the free run's
+    step in the last bit, hence the round-off tolerance.)"""
+    nl = maker()
+    nl.tran.method = method
+    pr = [nl.names[p] for p in probes]
+    o = oracle_mod.Oracle(nl)
+    t, v, st = o.transient(probes=pr)
+    orders = o.recorded_orders(len(t))
+    assert st["status"] == 0 and len(orders) == len(t) and orders[0] == 0
+    assert set(orders[1:].tolist()) <= {1, 2} and 2 in orders[1:]
+    tr, vr, sr = o.replay(t, orders, probes=pr)
+    assert sr["status"] == 0 and sr["rejected"] == 0
+    assert len(tr) == len(t)
+    np.testing.assert_array_equal(tr, t)
+    np.testing.assert_array_equal(o.recorded_orders(len(tr)), orders)
+    np.testing.assert_allclose(vr, v, rtol=0, atol=1e-9 * np.max(np.abs(v)))
+
+
+def test_replay_rejects_bad_sequences(oracle_mod):
+    o = oracle_mod.Oracle(N.rc_step())
+    with pytest.raises(ValueError):
+        o.replay([0.0, 1e-9, 1e-9], [0, 1, 1])   # times must increase
+    with pytest.raises(ValueError):
+        o.replay([0.0, 1e-9, 2e-9], [0, 1, 3])   # orders 1 or 2

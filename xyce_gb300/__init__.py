@@ -48,7 +48,7 @@ EXPORTED = [
     "xg_load_dae_matrices", "xg_lu_analyze", "xg_lu_factor", "xg_lu_solve",
     "xg_lu_solve_noalloc", "xg_lu_set_precision", "xg_lu_info", "xg_lu_schedule_info", "xg_lu_set_schedule", "xg_lu_analyze_pattern",
     "xg_transient", "xg_tran_start", "xg_tran_advance", "xg_tran_results", "xg_tran_end",
-    "xg_tran_predictors", "xg_tran_predictor_stats", "xg_set_predictor", "xg_mlp_set", "xg_mlp_get",
+    "xg_tran_predictors", "xg_tran_orders", "xg_tran_predictor_stats", "xg_set_predictor", "xg_mlp_set", "xg_mlp_get",
     "xg_mlp_train", "xg_mlp_grad", "xg_mlp_forward",
     "xg_dcop", "xg_version",
 ]
@@ -138,6 +138,7 @@ def lib() -> C.CDLL:
     fp = np.ctypeslib.ndpointer(np.float32, flags="C")
     LL = C.POINTER(C.c_longlong)
     L.xg_tran_predictors.argtypes = [P, dp]
+    L.xg_tran_orders.argtypes = [P, ip]
     L.xg_tran_predictor_stats.argtypes = [P, LL, LL, LL, LL]
     L.xg_set_predictor.argtypes = [P, I]
     L.xg_mlp_set.argtypes = [P, fp, fp]
@@ -340,6 +341,14 @@ class Circuit:
         out = np.zeros(max(1, nc * cap * pmax))
         self._check(lib().xg_tran_predictors(self.h, out))
         return out[: nc * cap * pmax].reshape(nc, cap, pmax)
+
+    def tran_orders(self):
+        """Integration order of each recorded point, [n_circuits, cap] (0 at
+        the operating point)."""
+        n_probe, cap, probes = self._run
+        out = np.zeros(max(1, self.n_circuits * cap), np.int32)
+        self._check(lib().xg_tran_orders(self.h, out))
+        return out[: self.n_circuits * cap].reshape(self.n_circuits, cap)
 
     def predictor_stats(self):
         v = [C.c_longlong() for _ in range(4)]

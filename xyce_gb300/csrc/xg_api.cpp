@@ -1113,7 +1113,7 @@ struct TranRun {
   ~TranRun() {
     if (exec) cudaGraphExecDestroy(exec);
     free_list(allocs);
-    if (ctx) { ctx->d.out_t = nullptr; ctx->d.out_v = nullptr; ctx->d.out_p = nullptr; }
+    if (ctx) { ctx->d.out_t = nullptr; ctx->d.out_v = nullptr; ctx->d.out_p = nullptr; ctx->d.out_o = nullptr; }
   }
 };
 
@@ -1301,6 +1301,7 @@ static int tran_start_run(xg_ctx *ctx, const xg_tran_params *p, const std::vecto
   CK(cudaMemcpyAsync(d.probe_idx, probe_idx.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
   int rc = 0;
   if ((rc = dev_alloc(ctx, &d.out_t, (size_t)ncirc * std::max(cap, 1), R.allocs))) return rc;
+  if ((rc = dev_alloc(ctx, &d.out_o, (size_t)ncirc * std::max(cap, 1), R.allocs))) return rc;
   if ((rc = dev_alloc(ctx, &d.out_v, (size_t)ncirc * std::max(cap, 1) * R.pmax, R.allocs))) return rc;
   if ((rc = dev_alloc(ctx, &d.out_p, (size_t)ncirc * std::max(cap, 1) * R.pmax, R.allocs))) return rc;
   std::vector<std::vector<double>> cb(ncirc);
@@ -1434,6 +1435,18 @@ extern "C" int xg_tran_predictors(xg_ctx *ctx, double *pred_values) {
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaMemcpy(pred_values, ctx->d.out_p, sizeof(double) * (size_t)ctx->ncirc * R.cap * R.pmax,
                 cudaMemcpyDeviceToHost));
+  return XG_OK;
+}
+
+extern "C" int xg_tran_orders(xg_ctx *ctx, int *orders) {
+  if (!ctx || !orders) return XG_ERR_ARG;
+  if (!ctx->run) return fail(ctx, XG_ERR_STATE, "call xg_tran_start first");
+  TranRun &R = *ctx->run;
+  if (R.cap <= 0) return fail(ctx, XG_ERR_STATE, "nothing recorded (cap = 0)");
+  CK(cudaStreamSynchronize(ctx->stream));
+  std::vector<signed char> o((size_t)ctx->ncirc * R.cap);
+  CK(cudaMemcpy(o.data(), ctx->d.out_o, o.size(), cudaMemcpyDeviceToHost));
+  for (size_t k = 0; k < o.size(); ++k) orders[k] = o[k];
   return XG_OK;
 }
 

@@ -168,6 +168,7 @@ struct DevArrays {
   // recording
   int *probe_idx = nullptr, *probe_ptr = nullptr;
   double *out_t = nullptr, *out_v = nullptr;
+  signed char *out_o = nullptr;  // integration order of each recorded point (0: operating point)
   int *status = nullptr;      // mapped host memory: [0] finished circuits, [1] LU breakdown
 };
 

@@ -965,7 +965,10 @@ __global__ void k_step_ctl(DevArrays d, int ncirc, const double *bps, const int 
       s.stopTime = next_bp(bps, b0, b1, s.t, p.bptol, s.bp_index);
       s.init_jct = 0;
       s.gshunt = 0.0;
-      if (s.n_out < cap) { d.out_t[(size_t)c * cap + s.n_out] = s.t; }
+      if (s.n_out < cap) {
+        d.out_t[(size_t)c * cap + s.n_out] = s.t;
+        d.out_o[(size_t)c * cap + s.n_out] = 0;
+      }
       s.n_out++;
       if (p.dc_only) return;
     } else {
@@ -995,6 +998,7 @@ __global__ void k_step_ctl(DevArrays d, int ncirc, const double *bps, const int 
       }
     }
     if (ok) {
+      const int step_order = s.order;  // the order this step was integrated with
       s.numberOfSteps++;
       s.nef = 0;
       s.t = s.tn;
@@ -1025,7 +1029,10 @@ __global__ void k_step_ctl(DevArrays d, int ncirc, const double *bps, const int 
       s.lastOk = 1;
       s.accept = 1;
       s.xmax_curr = m;
-      if (s.n_out < cap) { d.out_t[(size_t)c * cap + s.n_out] = s.t; }
+      if (s.n_out < cap) {
+        d.out_t[(size_t)c * cap + s.n_out] = s.t;
+        d.out_o[(size_t)c * cap + s.n_out] = (signed char)step_order;
+      }
       s.n_out++;
       if (s.t >= p.tstop - p.bptol || (p.max_steps > 0 && s.accepted >= p.max_steps)) {
         s.phase = PH_DONE;
