@@ -170,10 +170,14 @@ int xg_update_sources(xg_ctx *ctx, double time);
  * nonlinear device at next_sol, writes next_sta / next_sto, and keeps the
  * per-instance stamp values for the two load calls that follow.
  * History selection follows the reference: newton_iter == 0 reads curr_sto,
- * later iterations read next_sto as left by the previous call. */
+ * later iterations read next_sto as left by the previous call.  flags:
+ * XG_FLAG_*.  load_type (XG_LOAD_*) selects the devices as
+ * DeviceMaster::updateState does (N_DEV_DeviceMaster.h:688-700): ALL and
+ * NONLINEAR evaluate the nonlinear devices; LINEAR has nothing to evaluate
+ * (the linear devices are the constant linear part of the matrix). */
 int xg_update_state(xg_ctx *ctx, const double *next_sol, const double *curr_sta,
                     const double *curr_sto, double *next_sta, double *next_sto,
-                    int newton_iter, int flags);
+                    int newton_iter, int flags, int load_type);
 /* DeviceMgr::loadDAEVectors (N_DEV_DeviceMgr.C:4156-4284): ADDS the device
  * contributions into Q, F, B, dFdxdVp, dQdxdVp (length n).  As in the
  * reference, the caller zeroes them first (N_LOA_NonlinearEquationLoader.C:385-390). */
@@ -352,6 +356,42 @@ int xg_mlp_grad(xg_ctx *ctx, const float *X, const float *Y, int n, float *grad_
                 float *loss_host);
 /* out[r] = MLP(X[r]) in standardized units (DEVICE pointers). */
 int xg_mlp_forward(xg_ctx *ctx, const float *X, int n, float *out);
+
+/* ---- Newton solve ---------------------------------------------------------
+ * Nonlinear::DampedNewton::solve with full Newton steps
+ * (src/NonlinearSolverPKG/N_NLS_DampedNewton.C:362-520; converged_ :1191-1396;
+ * updateWeights_ :297-340), every circuit of the context at once, for a
+ * caller that keeps its own time integrator: it sets the coefficients of
+ * the nonlinear system and calls this once per step attempt.  The residual
+ * and Jacobian are those OneStep::obtainResidual / obtainJacobian form
+ * (N_TIA_OneStep.C:219-290, 469-500):
+ *   RHS = -[qscale (Q(x) - qhist0) + fscale (F(x) - B(time)) + hscale qhist2]
+ *         + qscale dQdxdVp + fscale dFdxdVp
+ *   J   =  qscale dQdx + fscale dFdx
+ * (operating point: qscale = hscale = 0, fscale = 1).  x (DEVICE, length n)
+ * is the initial guess on entry and the last iterate on return; x_curr
+ * (DEVICE, may be NULL = zeros) is the accepted solution of the weights
+ * reltol * max(|x|, |x_curr|) + abstol; qhist0 / qhist2 (DEVICE) may be NULL
+ * when their coefficient is 0.  curr_sta / curr_sto are the accepted device
+ * state and store, next_sta / next_sto receive the iterate's (as for
+ * xg_update_state).  flags: XG_FLAG_DCOP selects the operating-point rules
+ * (weights every iteration, device convergence enforced), XG_FLAG_INITJCT
+ * the junction initialization of the first iteration.
+ * Outputs (HOST, n_circuits each): status[c] = DampedNewton's return code of
+ * circuit c — 2 converged, 1 residual norm below machine epsilon, 4 small
+ * update, -1 too many steps, -2 diverging, -3 stalled, -6 NaN, -9 linear
+ * solve failed; iters[c] (may be NULL) = its Newton iterations.  The return
+ * value is XG_OK when every circuit's solve ran to one of those codes, else
+ * an XG_ERR_* (arguments, CUDA, repeated pivot breakdown).  Not allowed
+ * while a transient is in progress. */
+typedef struct xg_newton_params {
+  double reltol, abstol, deltaxtol, rhstol, smallupdatetol;  /* .OPTIONS NONLIN(-TRAN) */
+  int maxstep;
+} xg_newton_params;
+int xg_newton_solve(xg_ctx *ctx, const xg_newton_params *p, double time, double qscale,
+                    double fscale, double hscale, const double *qhist0, const double *qhist2,
+                    double *x, const double *x_curr, const double *curr_sta, const double *curr_sto,
+                    double *next_sta, double *next_sto, int flags, int *status, int *iters);
 
 /* Operating point only; x_host receives the n solution values. */
 int xg_dcop(xg_ctx *ctx, double *x_host, int *iters);

@@ -77,6 +77,8 @@ def lib():
         L.orc_transient.argtypes = [P, C.POINTER(TranParams), C.c_int, ip, C.c_int, dp, dp,
                                     C.POINTER(C.c_int), C.POINTER(TranStats)]
         L.orc_dcop.argtypes = [P, dp, C.POINTER(C.c_int)]
+        L.orc_newton.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_double, P, P, dp, P, dp, dp,
+                                 dp, dp] + [C.c_double] * 5 + [C.c_int, C.c_int, C.POINTER(C.c_int)]
         L.orc_set_wall_log.argtypes = [P, C.c_void_p, C.c_int]
         L.orc_set_replay.argtypes = [P, C.c_void_p, C.c_void_p, C.c_int]
         L.orc_recorded_orders.argtypes = [P, ip, C.c_int]
@@ -187,6 +189,26 @@ class Oracle:
         out = np.zeros(len(self.LU_COUNTS), np.int64)
         lib().orc_lu_counts(self.h, out, int(reset))
         return dict(zip(self.LU_COUNTS, out.tolist()))
+
+    def newton(self, x, time=0.0, qscale=0.0, fscale=1.0, hscale=0.0, qhist0=None, qhist2=None,
+               x_curr=None, sta_curr=None, sto_curr=None, flags=0, reltol=1e-2, abstol=1e-6,
+               deltaxtol=0.33, rhstol=1e-2, smallupdatetol=1e-6, maxstep=20):
+        """One DampedNewton solve (orc_newton); returns (status, iterations,
+        x, sta_next, sto_next)."""
+        f64 = lambda a: None if a is None else np.ascontiguousarray(a, np.float64)
+        xv = np.array(x, np.float64)
+        z = lambda k: np.zeros(max(1, k))
+        sta_c = z(self.nsta) if sta_curr is None else f64(sta_curr)
+        sto_c = z(self.nsto) if sto_curr is None else f64(sto_curr)
+        sta_n, sto_n = z(self.nsta), z(self.nsto)
+        q0, q2, xc = f64(qhist0), f64(qhist2), f64(x_curr)
+        ptr = lambda a: None if a is None else a.ctypes.data
+        it = C.c_int()
+        st = lib().orc_newton(self.h, float(time), float(qscale), float(fscale), float(hscale), ptr(q0),
+                              ptr(q2), xv, ptr(xc), sta_c, sto_c, sta_n, sto_n, float(reltol), float(abstol),
+                              float(deltaxtol), float(rhstol), float(smallupdatetol), int(maxstep),
+                              int(flags), C.byref(it))
+        return st, it.value, xv, sta_n, sto_n
 
     def dcop(self):
         x = np.zeros(self.n)

@@ -992,6 +992,33 @@ int dcop(orc_ctx *c, Work &w, double t0, int *total_iters) {
 
 }  // namespace
 
+// One DampedNewton solve with caller-given coefficients and histories (the
+// checker of the GPU's xg_newton_solve): RHS = -[qscale (Q - qhist0) +
+// fscale (F - B) + hscale qhist2] + limiter terms, J = qscale dQdx + fscale
+// dFdx; weights reltol * max(|x|, |x_curr|) + abstol.  flags bit0: operating-
+// point rules, bit1: initJct on the first iteration.  x in/out.
+extern "C" int orc_newton(orc_ctx *c, double time, double qscale, double fscale, double hscale,
+                          const double *qhist0, const double *qhist2, double *x, const double *x_curr,
+                          const double *sta_curr, const double *sto_curr, double *sta_next, double *sto_next,
+                          double reltol, double abstol, double deltaxtol, double rhstol, double smallupdatetol,
+                          int maxstep, int flags, int *iters) {
+  Work w;
+  work_init(c, w);
+  const bool dcop = (flags & 1) != 0;
+  std::copy(x, x + w.n, w.x.begin());
+  if (x_curr) std::copy(x_curr, x_curr + w.n, w.xcurr.begin());
+  if (c->nsta) std::copy(sta_curr, sta_curr + c->nsta, w.sta_curr.begin());
+  if (c->nsto) std::copy(sto_curr, sto_curr + c->nsto, w.sto_curr.begin());
+  std::vector<double> zeros(w.n, 0.0);
+  Coef cf{qscale, fscale, hscale, qhist0 ? qhist0 : zeros.data(), qhist2 ? qhist2 : zeros.data(), 0.0, 0};
+  NLParams nl{reltol, abstol, deltaxtol, rhstol, smallupdatetol, maxstep, !dcop, dcop};
+  const int st = newton(c, w, time, nl, cf, flags & 3, iters);
+  std::copy(w.x.begin(), w.x.end(), x);
+  if (c->nsta) std::copy(w.sta_next.begin(), w.sta_next.begin() + c->nsta, sta_next);
+  if (c->nsto) std::copy(w.sto_next.begin(), w.sto_next.begin() + c->nsto, sto_next);
+  return st;
+}
+
 extern "C" int orc_dcop(orc_ctx *c, double *x, int *iters) {
   Work w;
   work_init(c, w);

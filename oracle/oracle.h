@@ -94,6 +94,18 @@ typedef struct orc_tran_stats {
 int orc_transient(orc_ctx *c, const orc_tran_params *p, int n_probe, const int *probes,
                   int cap, double *times, double *values, int *n_out, orc_tran_stats *st);
 
+/* One DampedNewton solve with caller-given coefficients and histories:
+ * RHS = -[qscale (Q - qhist0) + fscale (F - B) + hscale qhist2] + limiter
+ * terms, J = qscale dQdx + fscale dFdx (qhist0 / qhist2 may be NULL = zeros);
+ * weights reltol * max(|x|, |x_curr|) + abstol (x_curr NULL = zeros).
+ * flags: bit0 operating-point rules, bit1 initJct.  x: initial guess in,
+ * last iterate out.  Returns DampedNewton's status; *iters its iterations. */
+int orc_newton(orc_ctx *c, double time, double qscale, double fscale, double hscale,
+               const double *qhist0, const double *qhist2, double *x, const double *x_curr,
+               const double *sta_curr, const double *sto_curr, double *sta_next, double *sto_next,
+               double reltol, double abstol, double deltaxtol, double rhstol, double smallupdatetol,
+               int maxstep, int flags, int *iters);
+
 /* Operating point only (x out, length n_unknowns). */
 int orc_dcop(orc_ctx *c, double *x, int *iters);
 

@@ -331,3 +331,18 @@ def test_replay_rejects_bad_sequences(oracle_mod):
         o.replay([0.0, 1e-9, 1e-9], [0, 1, 1])   # times must increase
     with pytest.raises(ValueError):
         o.replay([0.0, 1e-9, 2e-9], [0, 1, 3])   # orders 1 or 2
+
+
+def test_standalone_newton_matches_operating_point(oracle_mod):
+    """orc_newton with the operating-point rules from x = 0 (initJct on the
+    first iteration) converges where the operating point does, to the same
+    solution; a one-step limit fails with DampedNewton's -1."""
+    nl = N.diode_ladder(30, seed=3)
+    o = oracle_mod.Oracle(nl)
+    st0, x0, _ = o.dcop()
+    st, it, x, _, _ = o.newton(np.zeros(o.n), flags=3, reltol=1e-3, abstol=1e-12, deltaxtol=1.0,
+                               rhstol=1e-6, maxstep=200)
+    assert st0 > 0 and st > 0 and it >= 2
+    np.testing.assert_allclose(x, x0, rtol=1e-9, atol=1e-12)
+    st, it, _, _, _ = o.newton(np.zeros(o.n), flags=3, maxstep=1)
+    assert st == -1 and it == 1

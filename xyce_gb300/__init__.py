@@ -50,7 +50,7 @@ EXPORTED = [
     "xg_transient", "xg_tran_start", "xg_tran_advance", "xg_tran_results", "xg_tran_end",
     "xg_tran_predictors", "xg_tran_orders", "xg_tran_predictor_stats", "xg_set_predictor", "xg_mlp_set", "xg_mlp_get",
     "xg_mlp_train", "xg_mlp_grad", "xg_mlp_forward",
-    "xg_dcop", "xg_version",
+    "xg_dcop", "xg_newton_solve", "xg_version",
 ]
 
 
@@ -67,6 +67,11 @@ class TranParams(C.Structure):
                 ("nl_deltaxtol", C.c_double), ("nl_rhstol", C.c_double),
                 ("nl_smallupdatetol", C.c_double), ("nl_maxstep", C.c_int),
                 ("max_steps", C.c_int), ("max_order", C.c_int), ("method", C.c_int)]
+
+
+class NewtonParams(C.Structure):
+    _fields_ = [("reltol", C.c_double), ("abstol", C.c_double), ("deltaxtol", C.c_double),
+                ("rhstol", C.c_double), ("smallupdatetol", C.c_double), ("maxstep", C.c_int)]
 
 
 class TranStats(C.Structure):
@@ -116,7 +121,7 @@ def lib() -> C.CDLL:
     L.xg_get_sizes.argtypes = [P] + [C.POINTER(I)] * 4
     L.xg_get_pattern.argtypes = [P, ip, ip]
     L.xg_update_sources.argtypes = [P, D]
-    L.xg_update_state.argtypes = [P, P, P, P, P, P, I, I]
+    L.xg_update_state.argtypes = [P, P, P, P, P, P, I, I, I]
     L.xg_load_dae_vectors.argtypes = [P, P, P, P, P, P, P, I]
     L.xg_load_dae_matrices.argtypes = [P, P, P, I]
     L.xg_lu_analyze.argtypes = [P, P]
@@ -135,6 +140,7 @@ def lib() -> C.CDLL:
     L.xg_tran_results.argtypes = [P, ip, dp, dp, C.POINTER(TranStats)]
     L.xg_tran_end.argtypes = [P]
     L.xg_dcop.argtypes = [P, dp, C.POINTER(I)]
+    L.xg_newton_solve.argtypes = [P, C.POINTER(NewtonParams), D, D, D, D, P, P, P, P, P, P, P, P, I, ip, ip]
     fp = np.ctypeslib.ndpointer(np.float32, flags="C")
     LL = C.POINTER(C.c_longlong)
     L.xg_tran_predictors.argtypes = [P, dp]
@@ -235,9 +241,11 @@ class Circuit:
     def update_sources(self, time: float):
         self._check(lib().xg_update_sources(self.h, float(time)))
 
-    def update_state(self, next_sol, curr_sta, curr_sto, next_sta, next_sto, newton_iter=0, flags=0):
+    def update_state(self, next_sol, curr_sta, curr_sto, next_sta, next_sto, newton_iter=0, flags=0,
+                     load_type=LOAD_ALL):
         self._check(lib().xg_update_state(self.h, _ptr(next_sol), _ptr(curr_sta), _ptr(curr_sto),
-                                          _ptr(next_sta), _ptr(next_sto), int(newton_iter), int(flags)))
+                                          _ptr(next_sta), _ptr(next_sto), int(newton_iter), int(flags),
+                                          int(load_type)))
 
     def load_dae_vectors(self, next_sol, Q, F, B, dFdxdVp, dQdxdVp, load_type=LOAD_ALL):
         self._check(lib().xg_load_dae_vectors(self.h, _ptr(next_sol), _ptr(Q), _ptr(F), _ptr(B),
@@ -290,6 +298,22 @@ class Circuit:
         it = C.c_int()
         self._check(lib().xg_dcop(self.h, x, C.byref(it)))
         return x, it.value
+
+    def newton_solve(self, x, curr_sta, curr_sto, next_sta, next_sto, time=0.0, qscale=0.0, fscale=1.0,
+                     hscale=0.0, qhist0=None, qhist2=None, x_curr=None, flags=0, reltol=1e-2,
+                     abstol=1e-6, deltaxtol=0.33, rhstol=1e-2, smallupdatetol=1e-6, maxstep=20):
+        """DampedNewton on the device for every circuit (xg_newton_solve):
+        x (CUDA tensor) holds the initial guess and receives the last iterate;
+        returns (status codes, iterations) per circuit.  Defaults are the
+        NONLIN-TRAN options (N_NLS_Manager.C:1056-1066)."""
+        p = NewtonParams(reltol, abstol, deltaxtol, rhstol, smallupdatetol, maxstep)
+        st = np.zeros(self.n_circuits, np.int32)
+        it = np.zeros(self.n_circuits, np.int32)
+        self._check(lib().xg_newton_solve(self.h, C.byref(p), float(time), float(qscale), float(fscale),
+                                          float(hscale), _ptr(qhist0), _ptr(qhist2), _ptr(x), _ptr(x_curr),
+                                          _ptr(curr_sta), _ptr(curr_sto), _ptr(next_sta), _ptr(next_sto),
+                                          int(flags), st, it))
+        return st, it
 
     def _tran_params(self, tran):
         return TranParams(tran.tstart, tran.tstop, tran.hmax, tran.hmin, tran.reltol, tran.abstol,

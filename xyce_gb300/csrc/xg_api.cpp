@@ -750,9 +750,15 @@ int xg_update_sources(xg_ctx *ctx, double time) {
 }
 
 int xg_update_state(xg_ctx *ctx, const double *next_sol, const double *curr_sta, const double *curr_sto,
-                    double *next_sta, double *next_sto, int newton_iter, int flags) {
+                    double *next_sta, double *next_sto, int newton_iter, int flags, int load_type) {
   if (!ctx || !next_sol) return XG_ERR_ARG;
   if (!ctx->finalized) return fail(ctx, XG_ERR_STATE, "not finalized");
+  if (load_type < 0 || load_type > 2) return fail(ctx, XG_ERR_ARG, "bad load type");
+  if (flags & ~(XG_FLAG_DCOP | XG_FLAG_INITJCT)) return fail(ctx, XG_ERR_ARG, "unknown solver-state flag");
+  // DeviceMaster::updateState (N_DEV_DeviceMaster.h:688-700): a LINEAR load
+  // updates the linear devices only, whose values here are the constant
+  // linear part of the matrix — there is nothing to evaluate
+  if (load_type == XG_LOAD_LINEAR) return XG_OK;
   if ((ctx->nsta > 0 && (!curr_sta || !next_sta)) || (ctx->nsto > 0 && (!curr_sto || !next_sto)))
     return fail(ctx, XG_ERR_ARG, "state/store vectors are required");
   DevArrays d = ctx->d;
@@ -1124,9 +1130,10 @@ void xg_free_run(xg_ctx *ctx) {
 
 namespace {
 
-void launch_front(TranRun &R) {
-  xg_ctx *c = R.ctx;
-  DevArrays &d = c->d;
+// The kernels of one tick before the LU (sources, device evaluation,
+// assembly, Newton decision), on the arrays d (the context's, or a copy
+// pointing at a caller's vectors).
+void front_kernels(xg_ctx *c, const DevArrays &d) {
   launch_sources_k(c->stream, d, c->nv, c->nv + c->ni, 0, 0.0);
   launch_mos1_k(c->stream, d, c->nm, c->sto_base_m, 1, 1, 0, 0, c->sF_m, c->sQ_m, c->sL_m, c->sM_m);
   launch_bsim4_k(c->stream, d, c->nb, c->sto_base_b, c->sta_base_b, 1, 1, 0, 0, c->sF_b, c->sQ_b, c->sL_b,
@@ -1136,13 +1143,21 @@ void launch_front(TranRun &R) {
   launch_newton_ctl_k(c->stream, d, c->ncirc);
 }
 
+// LU factor and solve, Newton update and the per-circuit step decision.
+void back_kernels(xg_ctx *c, const DevArrays &d, double pivot_tol, const double *bps, const int *bp_ptr,
+                  int cap) {
+  launch_lu_factor_k(c->stream, c->L, d.J, d.cs, 1, pivot_tol);
+  launch_lu_solve_k(c->stream, c->L, d.rhs, d.dx, d.cs, 1);
+  launch_update_k(c->stream, d, c->n);
+  launch_step_ctl_k(c->stream, d, c->ncirc, bps, bp_ptr, cap);
+}
+
+void launch_front(TranRun &R) { front_kernels(R.ctx, R.ctx->d); }
+
 void launch_back(TranRun &R) {
   xg_ctx *c = R.ctx;
   DevArrays &d = c->d;
-  launch_lu_factor_k(c->stream, c->L, d.J, d.cs, 1, R.pivot_tol);
-  launch_lu_solve_k(c->stream, c->L, d.rhs, d.dx, d.cs, 1);
-  launch_update_k(c->stream, d, c->n);
-  launch_step_ctl_k(c->stream, d, c->ncirc, R.bps, R.bp_ptr, R.cap);
+  back_kernels(c, d, R.pivot_tol, R.bps, R.bp_ptr, R.cap);
   launch_history_k(c->stream, d, c->n, R.cap, R.pmax);
   if (c->predictor == XG_PRED_LEARNED) launch_ml_predict_k(c->stream, d, c->n, c->ncirc, 1);
   launch_state_commit_k(c->stream, d, c->nm, c->nd, c->sto_base_m, c->nb, c->sto_base_b, c->sta_base_b);
@@ -1502,6 +1517,104 @@ extern "C" int xg_dcop(xg_ctx *ctx, double *x_host, int *iters) {
   if (iters) *iters = (int)st.dcop_iters;
   if (rc) return rc;
   CK(cudaMemcpy(x_host, ctx->d.xcurr, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost));
+  return XG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// One Newton solve per circuit on the device (DampedNewton::solve).
+extern "C" int xg_newton_solve(xg_ctx *ctx, const xg_newton_params *p, double time, double qscale,
+                               double fscale, double hscale, const double *qhist0, const double *qhist2,
+                               double *x, const double *x_curr, const double *curr_sta, const double *curr_sto,
+                               double *next_sta, double *next_sto, int flags, int *status, int *iters) {
+  if (!ctx || !p || !x || !status) return XG_ERR_ARG;
+  if (!ctx->finalized) return fail(ctx, XG_ERR_STATE, "not finalized");
+  if (ctx->run) return fail(ctx, XG_ERR_STATE, "a transient is in progress: end it first");
+  auto positive = [](double v) { return v > 0.0 && std::isfinite(v); };
+  if (!positive(p->reltol) || !positive(p->abstol) || !positive(p->deltaxtol) || !positive(p->rhstol) ||
+      !(p->smallupdatetol >= 0.0 && std::isfinite(p->smallupdatetol)))
+    return fail(ctx, XG_ERR_ARG, "Newton tolerances must be positive and finite");
+  if (p->maxstep < 1) return fail(ctx, XG_ERR_ARG, "maxstep must be at least 1");
+  if (!std::isfinite(time) || !std::isfinite(qscale) || !std::isfinite(fscale) || !std::isfinite(hscale))
+    return fail(ctx, XG_ERR_ARG, "time and coefficients must be finite");
+  if ((qscale != 0.0 && !qhist0) || (hscale != 0.0 && !qhist2))
+    return fail(ctx, XG_ERR_ARG, "a nonzero qscale / hscale needs its history vector");
+  if ((ctx->nsta > 0 && (!curr_sta || !next_sta)) || (ctx->nsto > 0 && (!curr_sto || !next_sto)))
+    return fail(ctx, XG_ERR_ARG, "state/store vectors are required");
+  if (flags & ~(XG_FLAG_DCOP | XG_FLAG_INITJCT)) return fail(ctx, XG_ERR_ARG, "unknown solver-state flag");
+  CK(cudaSetDevice(ctx->device));
+  const int n = ctx->n, ncirc = ctx->ncirc;
+  const bool dcop = (flags & XG_FLAG_DCOP) != 0;
+  TranParams tp{};
+  tp.tstart = time; tp.tstop = time + 1.0; tp.hmax = 1.0;
+  tp.reltol = 1.0; tp.abstol = 1.0;
+  tp.nl_reltol = p->reltol; tp.nl_abstol = p->abstol; tp.nl_deltaxtol = p->deltaxtol;
+  tp.nl_rhstol = p->rhstol; tp.nl_smallupdatetol = p->smallupdatetol; tp.nl_maxstep = p->maxstep;
+  tp.dc_reltol = p->reltol; tp.dc_abstol = p->abstol; tp.dc_deltaxtol = p->deltaxtol;
+  tp.dc_rhstol = p->rhstol; tp.dc_maxstep = p->maxstep;
+  tp.max_order = 1;
+  tp.newton_only = 1;
+  CK(cudaMemcpyAsync(ctx->d.tp, &tp, sizeof tp, cudaMemcpyHostToDevice, ctx->stream));
+  std::vector<CircState> cs(ncirc);
+  for (auto &s : cs) {
+    memset(&s, 0, sizeof s);
+    s.phase = dcop ? PH_DC : PH_TRAN;
+    s.t = s.tn = time;
+    s.qscale = qscale; s.fscale = fscale; s.hscale = hscale;
+    s.init_jct = (flags & XG_FLAG_INITJCT) ? 1 : 0;
+    s.order = 1;
+    s.errwt = 1.0;
+    s.stop_at = 0x7fffffffffffffffLL;
+  }
+  CK(cudaMemcpyAsync(ctx->d.cs, cs.data(), sizeof(CircState) * ncirc, cudaMemcpyHostToDevice, ctx->stream));
+  // the caller's vectors stand in for the context's; absent histories are zeros
+  DevArrays d = ctx->d;
+  d.x = x;
+  if (x_curr) d.xcurr = const_cast<double *>(x_curr);
+  else CK(cudaMemsetAsync(d.xcurr, 0, sizeof(double) * n, ctx->stream));
+  if (qhist0) d.qh0 = const_cast<double *>(qhist0);
+  else CK(cudaMemsetAsync(d.qh0, 0, sizeof(double) * n, ctx->stream));
+  if (qhist2) d.qh2 = const_cast<double *>(qhist2);
+  else CK(cudaMemsetAsync(d.qh2, 0, sizeof(double) * n, ctx->stream));
+  if (ctx->nsta > 0) { d.sta_curr = const_cast<double *>(curr_sta); d.sta_next = next_sta; }
+  if (ctx->nsto > 0) { d.sto_curr = const_cast<double *>(curr_sto); d.sto_next = next_sto; }
+  launch_newton_weights_k(ctx->stream, d, n);
+  CK(cudaMemsetAsync(ctx->breakdown_dev, 0, sizeof(int), ctx->stream));
+  ctx->status_host[0] = ctx->status_host[1] = 0;
+  double pivot_tol = kRuntimePivotTol;
+  int rc = 0;
+  // one Newton iteration of every unfinished circuit per pass; DampedNewton
+  // stops each circuit within maxstep iterations
+  for (int pass = 0; pass <= p->maxstep + 1; ++pass) {
+    front_kernels(ctx, d);
+    CK(cudaGetLastError());
+    if (!ctx->lu_ready && (rc = lu_analyze_from_device(ctx, d.J))) return rc;
+    back_kernels(ctx, d, pivot_tol, nullptr, nullptr, 0);
+    launch_count_done_k(ctx->stream, d, ncirc, ctx->breakdown_dev, ctx->status_dev);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int consecutive = 1; ctx->status_host[1]; ++consecutive) {
+      // a frozen pivot failed: re-pivot from the parked Jacobian and resume
+      if (consecutive > 4) return fail(ctx, XG_ERR_SINGULAR, "LU keeps breaking down after re-pivoting");
+      if ((rc = lu_analyze_from_device(ctx, d.J))) return rc;
+      pivot_tol = (consecutive >= 2) ? 0.0 : kRuntimePivotTol;
+      launch_unstall_k(ctx->stream, d, ncirc);
+      back_kernels(ctx, d, pivot_tol, nullptr, nullptr, 0);
+      launch_count_done_k(ctx->stream, d, ncirc, ctx->breakdown_dev, ctx->status_dev);
+      CK(cudaGetLastError());
+      CK(cudaStreamSynchronize(ctx->stream));
+    }
+    pivot_tol = kRuntimePivotTol;
+    if (ctx->status_host[0] >= ncirc) break;
+  }
+  std::vector<CircState> out(ncirc);
+  CK(cudaMemcpyAsync(out.data(), ctx->d.cs, sizeof(CircState) * ncirc, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (int c = 0; c < ncirc; ++c) {
+    if (out[c].phase != PH_DONE && out[c].phase != PH_FAILED)
+      return fail(ctx, XG_ERR_TIMEOUT, "a Newton solve did not stop within maxstep iterations");
+    status[c] = out[c].newton_status;
+    if (iters) iters[c] = out[c].iter;
+  }
   return XG_OK;
 }
 

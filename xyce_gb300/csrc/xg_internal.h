@@ -69,6 +69,7 @@ struct TranParams {
   double dc_reltol, dc_abstol, dc_deltaxtol, dc_rhstol;
   int dc_maxstep;
   int dc_only;  // stop every circuit once its operating point converges
+  int newton_only;  // one Newton solve per circuit, then stop (xg_newton_solve)
 };
 
 // MOSFET level-1 model-level (effective model) parameters after temperature
@@ -377,6 +378,7 @@ void launch_state_commit_k(cudaStream_t st, const DevArrays &d, int nm, int nd, 
 void launch_count_done_k(cudaStream_t st, const DevArrays &d, int ncirc, const int *breakdown,
                          int *status_out);
 void launch_unstall_k(cudaStream_t st, const DevArrays &d, int ncirc);
+void launch_newton_weights_k(cudaStream_t st, const DevArrays &d, int n);
 void launch_set_target_k(cudaStream_t st, const DevArrays &d, int ncirc, int n_steps);
 int lu_prepare_k();  // shared-memory opt-in of the staged group factorization
 void launch_lu_factor_k(cudaStream_t st, const LUDev &L, const double *vals, CircState *cs, int masked,

@@ -938,6 +938,13 @@ __global__ void k_step_ctl(DevArrays d, int ncirc, const double *bps, const int 
   if (!s.step_end) return;
   const int n_c = d.offsets[c + 1] - d.offsets[c];
   const int status = s.newton_status;
+  if (p.newton_only) {
+    // a Newton solve on its own (xg_newton_solve): the circuit stops with
+    // its DampedNewton status
+    s.newton_iters += s.iter;
+    s.phase = status > 0 ? PH_DONE : PH_FAILED;
+    return;
+  }
   const int b0 = bp_ptr[c], b1 = bp_ptr[c + 1];
   s.accept = 0;
   if (s.phase == PH_DC) {
@@ -1271,6 +1278,19 @@ __global__ void k_set_target(DevArrays d, int ncirc, int n_steps) {
 
 void launch_set_target_k(cudaStream_t st, const DevArrays &d, int ncirc, int n_steps) {
   k_set_target<<<nblk(ncirc, 128), 128, 0, st>>>(d, ncirc, n_steps);
+}
+
+// Solution weights of a Newton solve (DampedNewton::updateWeights_,
+// N_NLS_DampedNewton.C:297-340): reltol * max(|x|, |x_curr|) + abstol.
+__global__ void k_newton_weights(DevArrays d, int n) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const TranParams &p = *d.tp;
+  d.solwt[r] = p.nl_reltol * fmax(fabs(d.x[r]), fabs(d.xcurr[r])) + p.nl_abstol;
+}
+
+void launch_newton_weights_k(cudaStream_t st, const DevArrays &d, int n) {
+  k_newton_weights<<<nblk(n, 256), 256, 0, st>>>(d, n);
 }
 
 void launch_unstall_k(cudaStream_t st, const DevArrays &d, int ncirc) {
