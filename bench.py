@@ -208,11 +208,26 @@ def run_reference(args):
 
 
 # ---- GPU ----------------------------------------------------------------
-def _timed_windows(xg, nl, probes, dev, args, window, prec, flush, stream_of):
+SAMPLE_RINGS = 8          # rings of the mc batch whose waveforms are checked against the oracle
+PROFILE_TICKS = 40        # ticks timed stage by stage for the rooflines
+MOS1_BYTES_SURVEY = 712   # algorithmic bytes per MOSFET-1 evaluation + stamp, per-unit convention
+MOS1_BYTES_CODE = 440     # bytes the transient-mode kernel reads (112) and writes (328) per instance
+LU_BYTES_PER_NNZ = 12     # algorithmic bytes of a refactorization per nnz(L+U): value + index
+
+
+def _sample(nl, workload):
+    """(circuit, probe) pairs whose waveforms the oracle checks."""
+    if workload == "mc":
+        picks = [int(i * nl.n_circuits / SAMPLE_RINGS) for i in range(SAMPLE_RINGS)]
+        return [(ci, nl.names[f"c{ci}.n1"]) for ci in picks]
+    return [(0, nl.names["n1"]), (0, nl.names["n5000"])]
+
+
+def _timed_windows(xg, nl, probes, dev, args, window, prec, flush, stream_of, cap=16):
     import torch
     circ = xg.Circuit(nl, device=dev)
     circ.lu_set_precision(prec, 2)
-    circ.tran_start(probes=probes, cap=16)
+    circ.tran_start(probes=probes, cap=cap)
     stream = stream_of(circ)
     for _ in range(args.warmup):
         circ.tran_advance(window)
@@ -267,51 +282,93 @@ def _one_at_a_time(xg, nl, dev, window, stream_of, batched, sample=8, timed=4):
             "batched_over_one_ring_at_a_time": batched / rate}
 
 
-def _roofline(xg, circ, nl, dev, flush, stream_of, hbm_peak, peak_kind, args):
-    """k_mos1 in loader mode (xg_update_state, separate dF/dQ slots), one
-    launch over every MOSFET of the workload, L2 flushed before each launch."""
-    import torch
-    n = circ.n
-    stream = stream_of(circ)
-    z = lambda k: torch.zeros(max(1, k), dtype=torch.float64, device=f"cuda:{dev}")
-    x = torch.full((n,), 0.9, dtype=torch.float64, device=f"cuda:{dev}")
-    stac, stan, stoc, ston = z(circ.nsta), z(circ.nsta), z(circ.nsto), z(circ.nsto)
-    for _ in range(5):
-        circ.update_state(x, stac, stoc, stan, ston, newton_iter=1)
-    reps = 50
-    us_all = 0.0
-    for _ in range(reps):
-        flush.fill_(1.0)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        circ.update_state(x, stac, stoc, stan, ston, newton_iter=1)
-        e1.record(stream)
-        e1.synchronize()
-        us_all += e0.elapsed_time(e1) * 1e3
-    us = us_all / reps
-    nm = len(nl.mos1)
-    # per instance: reads 4 node indices, model index, circuit index (24 B),
-    # beta + vbi (16 B), 4 node voltages (32 B), 5 history stores (40 B);
-    # writes 6 stores + 8 states (112 B) and 47 stamp slots (376 B): 600 B
-    bytes_per_inst = 24 + 16 + 32 + 40 + 112 + 376
-    achieved = bytes_per_inst * nm / (us * 1e-6) / 1e9
+def _rooflines(circ, nl, window, hbm_peak, peak_kind, info, args):
+    """Rooflines of the two dominant kernels of the tick, timed by the tick
+    profiler (each stage of PROFILE_TICKS ticks of a new window launched on
+    its own, CUDA events on the context's stream, state > L2 between ticks):
+    k_mos1 in its transient form (combined Jacobian slots, the form the tick
+    runs) and the grouped LU refactorization."""
+    s0 = circ.tran_results()[3]
+    stage_ms, ev = circ.tran_profile(PROFILE_TICKS, n_steps=window)
+    s1 = circ.tran_results()[3]
+    total = sum(stage_ms.values())
+    inst = ev["mos1"] / PROFILE_TICKS
+    us = stage_ms["mos1"] * 1e3 / PROFILE_TICKS
+    alg = MOS1_BYTES_SURVEY * inst
+    achieved = alg / (us * 1e-6) / 1e9
     traffic = None
-    prof = os.path.join(HERE, "profiles", f"k_mos1_{args.workload}.traffic.json")
-    if args.workload == "mc" and args.rings != 4096:
-        prof = ""
-    if os.path.exists(prof):
+    prof = os.path.join(HERE, "profiles", "k_mos1_mc4096.traffic.json")
+    if args.workload == "mc" and args.rings == 4096 and os.path.exists(prof):
         try:
-            traffic = json.load(open(prof)).get("dram_bytes_per_launch")
+            t = json.load(open(prof))
+            # the capture's launch evaluated t["instances"]; scale to this launch's active instances
+            traffic = t["dram_bytes_per_launch"] * inst / t["instances"]
         except Exception:
             traffic = None
-    return {"kernel": "k_mos1 (MOSFET-1 evaluation + stamp, separate dF/dQ slots, one launch over "
-                      f"{nm} instances, L2 flushed before each launch)",
-            "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-            "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
-            "algorithmic_bytes_per_launch": bytes_per_inst * nm, "launch_us": us,
-            "fp64_pipe_note": "ncu: FP64 pipe 78.8 % busy in this kernel (profiles/k_mos1_mc1024_full.md); "
-                              "the FP64 pipe, not HBM, bounds it on GB300"}
+    mos = {"kernel": "k_mos1, transient form (MOSFET-1 evaluation + stamp into combined Jacobian slots, "
+                     "masked by circuit activity), as launched by the tick",
+           "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+           "peak_kind": peak_kind, "traffic": traffic,
+           "algorithmic_bytes_per_launch": alg, "bytes_per_instance": MOS1_BYTES_SURVEY,
+           "bytes_moved_by_code_per_instance": MOS1_BYTES_CODE, "instances_per_launch": inst, "launch_us": us,
+           "share_of_tick": stage_ms["mos1"] / total,
+           "note": "FP64-pipe bound on GB300: ncu shows the FP64 pipe ~80 % busy in this kernel"}
+    # the factor launch refactors the circuits whose Newton iteration solves this tick
+    circ_ticks = max(1, ev["circuits"])
+    solving = min(1.0, (s1["newton_iters"] - s0["newton_iters"]) / circ_ticks)
+    lu_us = stage_ms["lu_factor"] * 1e3 / PROFILE_TICKS
+    lu_alg = LU_BYTES_PER_NNZ * info["nnz_lu"] * solving
+    lu_ach = lu_alg / (lu_us * 1e-6) / 1e9
+    lu = {"kernel": "k_factor_groups_s (grouped left-looking refactorization on the frozen pattern)",
+          "bound": "hbm", "achieved": lu_ach, "peak": hbm_peak, "unit": "GB/s", "frac": lu_ach / hbm_peak,
+          "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes_per_launch": lu_alg,
+          "nnz_lu": info["nnz_lu"], "fraction_of_circuits_refactoring": solving, "launch_us": lu_us,
+          "share_of_tick": stage_ms["lu_factor"] / total,
+          "note": "latency-bound: a dependent chain of factor levels per circuit"}
+    stages = {k: v / PROFILE_TICKS * 1e3 for k, v in stage_ms.items()}
+    return mos, lu, stages
+
+
+def _error_vs_fp64(nl, sample, seqs, workload):
+    """Largest |dv| of the sampled circuits' recorded waveforms against the
+    oracle (the CPU FP64 restatement) replaying the same accepted steps, and
+    the oracle's own round-off floor (the same replay in another elimination
+    order); the exact window is where that floor stays below 1e-9 max|v|."""
+    import numpy as np
+    import oracle
+    from xyce_gb300 import netlist as N
+    alt = "md" if workload == "mc" else "reverse"
+    circuits = sorted({ci for ci, _ in sample})
+    tasks, meta = [], []
+    for ci in circuits:
+        sub = N.extract_circuit(nl, ci) if nl.n_circuits > 1 else nl
+        prs = [pr for c, pr in sample if c == ci]
+        t, o, _ = seqs[(ci, prs[0])]
+        v = np.stack([seqs[(ci, pr)][2] for pr in prs], axis=1)
+        lp = [pr - nl.offsets[ci] for pr in prs]
+        tasks += [(sub, lp, t, o, None), (sub, lp, t, o, alt)]
+        meta.append((ci, v))
+    res = oracle.run_many(tasks)
+    worst, worst_exact, floor_max, pts = 0.0, 0.0, 0.0, 0
+    for k, (ci, v) in enumerate(meta):
+        ta, va, sa = res[2 * k]
+        tb, vb, sb = res[2 * k + 1]
+        if sa["status"] != 0 or sb["status"] != 0 or len(va) != len(v) or len(vb) != len(v):
+            return {"error": f"oracle replay of circuit {ci} failed (status {sa['status']}, {sb['status']})"}
+        err = np.max(np.abs(va - v), axis=1)
+        floor = np.max(np.abs(vb - va), axis=1)
+        vmax = float(np.max(np.abs(va)))
+        above = np.nonzero(floor > 1e-9 * vmax)[0]
+        exact = int(above[0]) if len(above) else len(floor)
+        worst = max(worst, float(err.max()))
+        worst_exact = max(worst_exact, float(err[:exact].max()) if exact else 0.0)
+        floor_max = max(floor_max, float(floor.max()))
+        pts += len(v)
+    return {"max_abs_v": worst, "max_abs_v_exact_window": worst_exact, "roundoff_floor_v": floor_max,
+            "circuits": len(meta), "points": pts,
+            "method": "oracle (CPU FP64) replaying the GPU's accepted times and integration orders; "
+                      "floor = the oracle's own replay in another LU elimination order; exact window = points "
+                      "before that floor exceeds 1e-9 max|v|"}
 
 
 def run_ours(args):
@@ -334,17 +391,25 @@ def run_ours(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
     stream_of = lambda c: torch.cuda.ExternalStream(xg.lib().xg_get_stream(c.h))
 
-    if args.roofline_only:
+    if args.ncu_case:
+        # the profiling case: operating point, first analysis and one window
         circ = xg.Circuit(nl, device=dev)
-        print(json.dumps(_roofline(xg, circ, nl, dev, flush, stream_of, hbm_peak, peak_kind, args)), flush=True)
+        circ.tran_start(probes=probes, cap=16)
+        circ.tran_advance(window)
+        torch.cuda.synchronize()
+        print(json.dumps({"ncu_case": desc["workload"], "instances": len(nl.mos1)}), flush=True)
         circ.close()
         return
+    sample = _sample(nl, args.workload)
+    rec_probes = sorted({p for _, p in sample} | set(probes))
+    cap = (args.warmup + args.steps) * window + PROFILE_TICKS + 16
     clk_path = (f"{args.clocks_csv}.rank{rank}" if world > 1 else args.clocks_csv) if args.clocks_csv \
         else os.path.join(tempfile.gettempdir(), f"xg_clocks_{os.getpid()}.csv")
     sampler = _clock_sampler(clk_path)
     if world > 1:
         torch.distributed.barrier()
-    circ, ms_total, st0, st1 = _timed_windows(xg, nl, probes, dev, args, window, xg.PREC_FP64, flush, stream_of)
+    circ, ms_total, st0, st1 = _timed_windows(xg, nl, rec_probes, dev, args, window, xg.PREC_FP64, flush,
+                                              stream_of, cap=cap)
     if sampler:
         sampler.terminate()
         sampler.wait()
@@ -369,11 +434,19 @@ def run_ours(args):
     # completion count), replayed once per tick
     kernels_per_tick = int(st1.get("kernels_per_tick", 0))
     gpu_launches = int(ticks * kernels_per_tick)
-    circ.tran_end()
-
-    # ---- roofline of the device-evaluation kernel (MOSFET eval + stamp) ----
+    # the sampled circuits' accepted-step sequences (for the error against FP64)
+    counts, times, values, _ = circ.tran_results()
+    orders = circ.tran_orders()
+    seqs = {}
+    for ci, pr in sample:
+        m = int(counts[ci])
+        col = [p for p in rec_probes if nl.offsets[ci] <= p < nl.offsets[ci + 1]].index(pr)
+        seqs[(ci, pr)] = (times[ci, :m].copy(), orders[ci, :m].copy(), values[ci, :m, col].copy())
     n_unknowns = circ.n
-    roof = _roofline(xg, circ, nl, dev, flush, stream_of, hbm_peak, peak_kind, args) if rank == 0 else None
+    roof = lu_roof = stages = None
+    if rank == 0:
+        roof, lu_roof, stages = _rooflines(circ, nl, window, hbm_peak, peak_kind, info, args)
+    circ.tran_end()
     circ.close()
 
     # ---- the FP32-LU + FP64-refinement form, same workload ------------------
@@ -404,16 +477,15 @@ def run_ours(args):
         a = nl.arrays()
         h2d = sum(v.nbytes for k, v in a.items() if hasattr(v, "nbytes"))
         h2d += sum(x.nbytes for k in ("res", "cap", "vsrc", "isrc", "diode", "mos1", "bsim4") for x in a[k])
-        cap = per_circuit + 8
+        ecap = per_circuit + 8
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         c3 = xg.Circuit(nl, device=dev, arrays=a)
-        counts, tt, vv, st = c3.transient(tr, probes=probes, cap=cap)
+        counts3, tt, vv, st = c3.transient(tr, probes=probes, cap=ecap)
         dt = time.perf_counter() - t0
         c3.close()
-        cap = per_circuit + 8
         # xg_tran_results copies the time and probe buffers of every circuit
-        d2h = nl.n_circuits * cap * 8 * 2 + nl.n_circuits * 4
+        d2h = nl.n_circuits * ecap * 8 * 2 + nl.n_circuits * 4
         nsteps = args.warmup + args.steps
         e2e = {"value": st["accepted"] / dt, "unit": UNIT,
                "h2d_bytes_per_step": h2d / nsteps, "d2h_bytes_per_step": d2h / nsteps,
@@ -421,7 +493,10 @@ def run_ours(args):
         tr.max_steps = 0
 
     if rank == 0:
-        cpu = cpu_baseline(args) if args.cpu else None
+        cpu = err = None
+        if args.cpu:
+            cpu = cpu_baseline(args)
+            err = _error_vs_fp64(nl, sample, seqs, args.workload)
         clocks = _clock_summary(clk_path, dev)
         config = dict(desc)
         config.update({"unknowns": n_unknowns, "window_steps_per_circuit": window,
@@ -434,7 +509,8 @@ def run_ours(args):
                 "device_evals_per_s": evals_all / (ms_max / 1e3),
                 "newton_iters_per_step": (st1["newton_iters"] - st0["newton_iters"]) / max(1, steps_done),
                 "ticks": ticks, "kernels_per_tick": kernels_per_tick, "gpu_launches": gpu_launches,
-                "lu": info, "roofline": roof, "forms": forms, "cpu_baseline": cpu, "e2e": e2e,
+                "lu": info, "roofline": roof, "roofline_lu": lu_roof, "tick_stages_us": stages,
+                "max_err_vs_fp64": err, "forms": forms, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks}
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -451,8 +527,8 @@ def main():
     ap.add_argument("--rings", type=int, default=4096,
                     help="rings of the mc workload (a smaller batch is the profiling case)")
     ap.add_argument("--no-cpu", dest="cpu", action="store_false", help="skip the CPU baseline")
-    ap.add_argument("--roofline-only", action="store_true",
-                    help="only the k_mos1 roofline launches (the profiling case of that kernel)")
+    ap.add_argument("--ncu-case", action="store_true",
+                    help="only the operating point and one window (the case the ncu captures profile)")
     ap.add_argument("--no-forms", dest="forms", action="store_false", help="skip the FP32-IR form")
     ap.add_argument("--clocks-csv", default=None,
                     help="keep the nvidia-smi clock samples of the timed region in this file")

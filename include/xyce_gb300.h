@@ -309,6 +309,24 @@ int xg_tran_end(xg_ctx *ctx);
  * step started from — the training target of the learned predictor is the
  * accepted solution minus this guess. */
 int xg_tran_predictors(xg_ctx *ctx, double *pred_values);
+/* Per-stage device time of ticks of a transient in progress (a tick is one
+ * Newton iteration of every active circuit).  n_steps > 0 first opens a
+ * window of n_steps more accepted steps per circuit, as xg_tran_advance
+ * does.  Runs n_ticks ticks with the tick's kernels launched one stage at a
+ * time, CUDA events between stages, and ADDS each stage's milliseconds into
+ * stage_ms[XG_STAGE_*]; the run then continues as it would have.  evals
+ * (may be NULL) receives, summed over the ticks, the instances the
+ * MOSFET-1, BSIM4 and diode stages evaluated (evals[0..2]) and the active
+ * circuits (evals[3]).  For
+ * profiling: an advance replays the tick as one CUDA graph.  No reference
+ * counterpart (Xyce prints its load and solve times per run). */
+enum {
+  XG_STAGE_SOURCES, XG_STAGE_MOS1, XG_STAGE_BSIM4, XG_STAGE_DIODE, XG_STAGE_ASSEMBLE,
+  XG_STAGE_NEWTON, XG_STAGE_LU_FACTOR, XG_STAGE_LU_SOLVE, XG_STAGE_UPDATE, XG_STAGE_STEP,
+  XG_STAGE_HISTORY, XG_STAGE_COMMIT, XG_STAGE_COUNT
+};
+int xg_tran_profile(xg_ctx *ctx, int n_steps, int n_ticks, double *stage_ms, long long *evals);
+
 /* Integration order of the recorded points (layout of xg_tran_results'
  * times, n_circuits x cap): 0 for the operating point, else the order the
  * accepted step was integrated with (1 backward Euler / BDF1, 2 trapezoid /

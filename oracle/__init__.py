@@ -313,11 +313,17 @@ def ksparse_solve(row_ptr, col_idx, vals, b):
 
 def _replay_worker(task):
     """One oracle run in a worker process: task = (netlist, probes, times,
-    orders, min_degree); times None = a free run.  Returns (values, stats)."""
-    nl, probes, times, orders, md = task
+    orders, elimination order); times None = a free run.  The elimination
+    order is None (natural), "md" (minimum degree) or "reverse" (the natural
+    order backwards).  Returns (times, values, stats)."""
+    nl, probes, times, orders, order = task
     o = Oracle(nl)
-    if md:
+    if order is True or order == "md":
         o.use_minimum_degree()
+    elif order == "reverse":
+        o.set_order(np.arange(o.n - 1, -1, -1, dtype=np.int32))
+    elif order not in (None, False):
+        raise ValueError(f"unknown elimination order {order!r}")
     if times is None:
         t, v, st = o.transient(probes=probes)
         return t, v, st
@@ -328,8 +334,9 @@ def _replay_worker(task):
 def run_many(tasks, processes=None):
     """Oracle runs of several circuits in parallel worker processes (spawned,
     so that a caller holding a CUDA context may use it).  Each task is
-    (netlist, probes, times, orders, min_degree): with times and orders
-    given, a replay of that accepted-step sequence, else a free run.
+    (netlist, probes, times, orders, elimination order — see _replay_worker):
+    with times and orders given, a replay of that accepted-step sequence,
+    else a free run.
     Returns [(times, values, stats)] in task order."""
     import multiprocessing as mp
     if not os.path.exists(LIB_PATH):

@@ -46,3 +46,29 @@ def test_workload_descriptions(bench):
     nl, probes, desc = bench._workload("mc", rings=8)
     assert desc["circuits"] == 8 and desc["workload"] == "monte_carlo_rings_8"
     assert len(probes) == 4 and nl.n_circuits == 8
+
+
+def test_error_vs_fp64_on_an_oracle_sequence(bench):
+    """The bench's error check, fed sequences the oracle itself produced for
+    a batch of two diode-RC ladders (driven, stable circuits: a replay whose
+    step sizes differ in the last bit stays within round-off): the replay
+    reproduces them, and the summary fields add up."""
+    import oracle
+    from xyce_gb300 import netlist as N
+    nl = N.batch([N.diode_ladder(40, seed=2), N.diode_ladder(30, seed=3)])
+    nl.tran.tstop = 0.5e-6
+    sample = [(0, nl.names["0:n1"]), (0, nl.names["0:n40"]), (1, nl.names["1:n15"])]
+    seqs = {}
+    for ci in (0, 1):
+        sub = N.extract_circuit(nl, ci)
+        prs = [pr for c, pr in sample if c == ci]
+        o = oracle.Oracle(sub)
+        t, v, st = o.transient(probes=[pr - nl.offsets[ci] for pr in prs])
+        od = o.recorded_orders(len(t))
+        for j, pr in enumerate(prs):
+            seqs[(ci, pr)] = (t, od, v[:, j])
+    err = bench._error_vs_fp64(nl, sample, seqs, "mc")
+    assert "error" not in err, err
+    assert err["circuits"] == 2
+    assert err["points"] == len(seqs[sample[0]][0]) + len(seqs[sample[2]][0])
+    assert err["max_abs_v"] < 1e-9 and err["max_abs_v_exact_window"] <= err["max_abs_v"]

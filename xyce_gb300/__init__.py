@@ -48,7 +48,7 @@ EXPORTED = [
     "xg_load_dae_matrices", "xg_lu_analyze", "xg_lu_factor", "xg_lu_solve",
     "xg_lu_solve_noalloc", "xg_lu_set_precision", "xg_lu_info", "xg_lu_schedule_info", "xg_lu_set_schedule", "xg_lu_analyze_pattern",
     "xg_transient", "xg_tran_start", "xg_tran_advance", "xg_tran_results", "xg_tran_end",
-    "xg_tran_predictors", "xg_tran_orders", "xg_tran_predictor_stats", "xg_set_predictor", "xg_mlp_set", "xg_mlp_get",
+    "xg_tran_predictors", "xg_tran_orders", "xg_tran_profile", "xg_tran_predictor_stats", "xg_set_predictor", "xg_mlp_set", "xg_mlp_get",
     "xg_mlp_train", "xg_mlp_grad", "xg_mlp_forward",
     "xg_dcop", "xg_newton_solve", "xg_version",
 ]
@@ -145,6 +145,7 @@ def lib() -> C.CDLL:
     LL = C.POINTER(C.c_longlong)
     L.xg_tran_predictors.argtypes = [P, dp]
     L.xg_tran_orders.argtypes = [P, ip]
+    L.xg_tran_profile.argtypes = [P, I, I, dp, np.ctypeslib.ndpointer(np.int64, flags="C")]
     L.xg_tran_predictor_stats.argtypes = [P, LL, LL, LL, LL]
     L.xg_set_predictor.argtypes = [P, I]
     L.xg_mlp_set.argtypes = [P, fp, fp]
@@ -365,6 +366,19 @@ class Circuit:
         out = np.zeros(max(1, nc * cap * pmax))
         self._check(lib().xg_tran_predictors(self.h, out))
         return out[: nc * cap * pmax].reshape(nc, cap, pmax)
+
+    STAGES = ("sources", "mos1", "bsim4", "diode", "assemble", "newton", "lu_factor", "lu_solve", "update",
+              "step", "history", "commit")
+
+    def tran_profile(self, n_ticks: int, n_steps: int = 0):
+        """Per-stage device milliseconds summed over n_ticks ticks of the
+        run in progress (n_steps > 0: in a new window of that many steps),
+        and, summed over the ticks, the instances each model stage evaluated
+        and the active circuits."""
+        ms = np.zeros(len(self.STAGES))
+        ev = np.zeros(4, np.int64)
+        self._check(lib().xg_tran_profile(self.h, int(n_steps), int(n_ticks), ms, ev))
+        return dict(zip(self.STAGES, ms.tolist())), dict(zip(("mos1", "bsim4", "diode", "circuits"), ev.tolist()))
 
     def tran_orders(self):
         """Integration order of each recorded point, [n_circuits, cap] (0 at

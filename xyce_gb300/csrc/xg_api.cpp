@@ -44,6 +44,7 @@ struct xg_ctx {
   // finalized structure
   std::vector<int> rp, ci, circ_of_row;
   std::vector<long long> inst_of_circ;  // nonlinear device instances per circuit
+  std::vector<long long> circ_m1, circ_b4, circ_d;  // MOSFET-1 / BSIM4 / diode instances per circuit
   int nnz = 0, nm = 0, nd = 0, nv = 0, ni = 0, nb = 0;
   int nsto = 0, nsta = 0, sto_base_m = 0, sto_base_b = 0, sta_base_b = 0;
   int sF_m = 0, sF_d = 0, sQ_m = 0, sQ_d = 0, sL_m = 0, sL_d = 0, sM_m = 0, sM_d = 0;
@@ -645,9 +646,13 @@ int xg_finalize(xg_ctx *ctx) {
     b4circ[k] = c < 0 ? 0 : c;
   }
   ctx->inst_of_circ.assign(ctx->ncirc, 0);
-  for (int k = 0; k < nm; ++k) ctx->inst_of_circ[m1circ[k]]++;
-  for (int k = 0; k < nb; ++k) ctx->inst_of_circ[b4circ[k]]++;
-  for (int k = 0; k < nd; ++k) ctx->inst_of_circ[dcirc[k]]++;
+  ctx->circ_m1.assign(ctx->ncirc, 0);
+  ctx->circ_b4.assign(ctx->ncirc, 0);
+  ctx->circ_d.assign(ctx->ncirc, 0);
+  for (int k = 0; k < nm; ++k) ctx->circ_m1[m1circ[k]]++;
+  for (int k = 0; k < nb; ++k) ctx->circ_b4[b4circ[k]]++;
+  for (int k = 0; k < nd; ++k) ctx->circ_d[dcirc[k]]++;
+  for (int c = 0; c < ctx->ncirc; ++c) ctx->inst_of_circ[c] = ctx->circ_m1[c] + ctx->circ_b4[c] + ctx->circ_d[c];
   // row blocks x circuits partial slots
   const int nblocks = (n + kRowBlock - 1) / kRowBlock;
   std::vector<int> pair_base(nblocks + 1), blk_cfirst(nblocks), pair_cstart(ctx->ncirc + 1, 0);
@@ -1450,6 +1455,87 @@ extern "C" int xg_tran_predictors(xg_ctx *ctx, double *pred_values) {
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaMemcpy(pred_values, ctx->d.out_p, sizeof(double) * (size_t)ctx->ncirc * R.cap * R.pmax,
                 cudaMemcpyDeviceToHost));
+  return XG_OK;
+}
+
+// Ticks of a transient in progress, each kernel stage launched on its own
+// with CUDA events between the stages (the kernels and their order are those
+// of the captured tick graph, so the run continues exactly as it would).
+extern "C" int xg_tran_profile(xg_ctx *ctx, int n_steps, int n_ticks, double *stage_ms, long long *evals) {
+  if (!ctx || !stage_ms || n_ticks < 0) return XG_ERR_ARG;
+  if (!ctx->run || !ctx->run->exec) return fail(ctx, XG_ERR_STATE, "call xg_tran_start first");
+  TranRun &R = *ctx->run;
+  xg_ctx *c = ctx;
+  DevArrays &d = c->d;
+  const cudaStream_t st = c->stream;
+  if (evals) for (int k = 0; k < 4; ++k) evals[k] = 0;
+  if (n_steps > 0) {
+    // a new window, as xg_tran_advance opens one
+    launch_set_target_k(st, d, c->ncirc, n_steps);
+    launch_count_done_k(st, d, c->ncirc, c->breakdown_dev, c->status_dev);
+  }
+  cudaEvent_t ev[XG_STAGE_COUNT + 1];
+  int made = 0;
+  for (auto &e : ev) {
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      for (int k = 0; k < made; ++k) cudaEventDestroy(ev[k]);
+      return fail(ctx, XG_ERR_CUDA, "cudaEventCreate");
+    }
+    made++;
+  }
+  int rc = XG_OK;
+  std::vector<CircState> cs(c->ncirc);
+  for (int t = 0; t < n_ticks && rc == XG_OK; ++t) {
+    if (evals) {
+      // instances each model kernel evaluates this tick: those of active circuits
+      if (cudaMemcpyAsync(cs.data(), d.cs, sizeof(CircState) * c->ncirc, cudaMemcpyDeviceToHost, st) !=
+              cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) { rc = XG_ERR_CUDA; break; }
+      for (int q = 0; q < c->ncirc; ++q)
+        if (cs[q].phase == PH_DC || cs[q].phase == PH_TRAN) {
+          evals[0] += c->circ_m1[q];
+          evals[1] += c->circ_b4[q];
+          evals[2] += c->circ_d[q];
+          evals[3] += 1;
+        }
+    }
+    int s = 0;
+    cudaEventRecord(ev[s++], st);
+    launch_sources_k(st, d, c->nv, c->nv + c->ni, 0, 0.0);
+    cudaEventRecord(ev[s++], st);
+    launch_mos1_k(st, d, c->nm, c->sto_base_m, 1, 1, 0, 0, c->sF_m, c->sQ_m, c->sL_m, c->sM_m);
+    cudaEventRecord(ev[s++], st);
+    launch_bsim4_k(st, d, c->nb, c->sto_base_b, c->sta_base_b, 1, 1, 0, 0, c->sF_b, c->sQ_b, c->sL_b, c->sM_b);
+    cudaEventRecord(ev[s++], st);
+    launch_diode_k(st, d, c->nd, 1, 1, 0, 0, c->sF_d, c->sQ_d, c->sL_d, c->sM_d);
+    cudaEventRecord(ev[s++], st);
+    launch_assemble_k(st, d, c->n, c->nnz, c->n_long_row_blocks, c->n_long_ent_blocks);
+    cudaEventRecord(ev[s++], st);
+    launch_newton_ctl_k(st, d, c->ncirc);
+    cudaEventRecord(ev[s++], st);
+    launch_lu_factor_k(st, c->L, d.J, d.cs, 1, R.pivot_tol);
+    cudaEventRecord(ev[s++], st);
+    launch_lu_solve_k(st, c->L, d.rhs, d.dx, d.cs, 1);
+    cudaEventRecord(ev[s++], st);
+    launch_update_k(st, d, c->n);
+    cudaEventRecord(ev[s++], st);
+    launch_step_ctl_k(st, d, c->ncirc, R.bps, R.bp_ptr, R.cap);
+    cudaEventRecord(ev[s++], st);
+    launch_history_k(st, d, c->n, R.cap, R.pmax);
+    if (c->predictor == XG_PRED_LEARNED) launch_ml_predict_k(st, d, c->n, c->ncirc, 1);
+    cudaEventRecord(ev[s++], st);
+    launch_state_commit_k(st, d, c->nm, c->nd, c->sto_base_m, c->nb, c->sto_base_b, c->sta_base_b);
+    launch_count_done_k(st, d, c->ncirc, c->breakdown_dev, c->status_dev);
+    cudaEventRecord(ev[s++], st);
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) { rc = XG_ERR_CUDA; break; }
+    for (int k = 0; k < XG_STAGE_COUNT; ++k) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+      stage_ms[k] += ms;
+    }
+    R.ticks++;
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  if (rc) return fail(ctx, rc, "tick profile: CUDA failure");
   return XG_OK;
 }
 
