@@ -223,10 +223,11 @@ def _sample(nl, workload):
     return [(0, nl.names["n1"]), (0, nl.names["n5000"])]
 
 
-def _timed_windows(xg, nl, probes, dev, args, window, prec, flush, stream_of, cap=16):
+def _timed_windows(xg, nl, probes, dev, args, window, prec, flush, stream_of, cap=16, tune=None):
     import torch
     circ = xg.Circuit(nl, device=dev)
     circ.lu_set_precision(prec, 2)
+    circ.lu_set_tuning(xg.TUNE_TIMED if tune is None else tune)
     circ.tran_start(probes=probes, cap=cap)
     stream = stream_of(circ)
     for _ in range(args.warmup):
@@ -332,12 +333,13 @@ def _rooflines(circ, nl, window, hbm_peak, peak_kind, info, args):
 def _error_vs_fp64(nl, sample, seqs, workload):
     """Largest |dv| of the sampled circuits' recorded waveforms against the
     oracle (the CPU FP64 restatement) replaying the same accepted steps, and
-    the oracle's own round-off floor (the same replay in another elimination
-    order); the exact window is where that floor stays below 1e-9 max|v|."""
+    the oracle's own round-off floor (the same replay with every time point
+    moved by one ulp); the exact window is where that floor stays below
+    1e-9 max|v|."""
     import numpy as np
     import oracle
     from xyce_gb300 import netlist as N
-    alt = "md" if workload == "mc" else "reverse"
+    alt = "ulp"
     circuits = sorted({ci for ci, _ in sample})
     tasks, meta = [], []
     for ci in circuits:
@@ -367,7 +369,7 @@ def _error_vs_fp64(nl, sample, seqs, workload):
     return {"max_abs_v": worst, "max_abs_v_exact_window": worst_exact, "roundoff_floor_v": floor_max,
             "circuits": len(meta), "points": pts,
             "method": "oracle (CPU FP64) replaying the GPU's accepted times and integration orders; "
-                      "floor = the oracle's own replay in another LU elimination order; exact window = points "
+                      "floor = the oracle's own replay with every time moved by one ulp; exact window = points "
                       "before that floor exceeds 1e-9 max|v|"}
 
 
@@ -417,6 +419,7 @@ def run_ours(args):
     ticks = st1["ticks"] - st0["ticks"]
     evals = st1["device_evals"] - st0["device_evals"]
     info = circ.lu_info()
+    info["tuning"] = circ.lu_tuning()
     local_vals = torch.tensor([ms_total, float(steps_done), float(evals)], dtype=torch.float64,
                               device=f"cuda:{dev}")
     if world > 1:
@@ -463,6 +466,12 @@ def run_ours(args):
                          (s1["newton_iters"] - s0["newton_iters"]) / max(1, s1["accepted"] - s0["accepted"])}
             c2.tran_end()
             c2.close()
+            # the LU sweeps with the analysis' closed-form launch shapes instead of the timed ones
+            c4, ms4, s0, s1 = _timed_windows(xg, nl, probes, dev, args, window, xg.PREC_FP64, flush, stream_of,
+                                             tune=xg.TUNE_MODEL)
+            forms["fp64_lu_model_shapes"] = (s1["accepted"] - s0["accepted"]) / (ms4 / 1e3)
+            c4.tran_end()
+            c4.close()
             if args.workload == "mc":
                 forms.update(_one_at_a_time(xg, nl, dev, window, stream_of, value))
         except Exception as e:  # noqa: BLE001

@@ -247,6 +247,29 @@ int xg_lu_schedule_info(xg_ctx *ctx, int *ordering, int *factor_top, int *solve_
  * from the next analysis; not allowed while a transient is in progress. */
 int xg_lu_set_schedule(xg_ctx *ctx, int ordering, int factor_top, int solve_top);
 
+/* Launch shapes of the LU sweeps.  XG_TUNE_TIMED (default): after each
+ * analysis, candidate shapes — the factorization with and without its
+ * update metadata staged in shared memory, at 64..512 threads per CTA; the
+ * L and U solves at 64..512 threads — are launched on the matrix the
+ * analysis was computed from (L2 flushed before each timed launch) and the
+ * fastest are kept; choices are cached per analysis for the life of the
+ * process.  XG_TUNE_MODEL: the analysis' closed-form estimates.  Every
+ * candidate computes identical results; only the time differs.  Applies
+ * from the next analysis; not allowed while a transient is in progress.
+ * No reference counterpart (KLU's factorization is serial). */
+#define XG_TUNE_MODEL 0
+#define XG_TUNE_TIMED 1
+int xg_lu_set_tuning(xg_ctx *ctx, int mode);
+typedef struct xg_lu_tuning {
+  int mode;                 /* XG_TUNE_* of the current analysis */
+  int from_cache;           /* 1: timed earlier for the same analysis, in this process */
+  int factor_threads, factor_meta, lsolve_threads, usolve_threads;  /* in use */
+  int model_factor_threads, model_factor_meta, model_lsolve_threads, model_usolve_threads;
+  double factor_us, solve_us;              /* timed: the chosen shapes (one factor, one L+U solve) */
+  double model_factor_us, model_solve_us;  /* timed: the closed-form shapes (0 when not timed) */
+} xg_lu_tuning;
+int xg_lu_tuning_info(xg_ctx *ctx, xg_lu_tuning *out);
+
 /* Host-only analysis of a CSR pattern with values (no context, no device):
  * the numbers xg_lu_info / xg_lu_schedule_info report after xg_lu_analyze —
  * nnz(L+U), the ordering chosen (or forced: ordering = XG_ORDER_*, -1 =

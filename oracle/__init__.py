@@ -313,17 +313,24 @@ def ksparse_solve(row_ptr, col_idx, vals, b):
 
 def _replay_worker(task):
     """One oracle run in a worker process: task = (netlist, probes, times,
-    orders, elimination order); times None = a free run.  The elimination
-    order is None (natural), "md" (minimum degree) or "reverse" (the natural
-    order backwards).  Returns (times, values, stats)."""
+    orders, variant); times None = a free run.  The variant is None (the
+    natural elimination order), "md" (minimum-degree order), "reverse" (the
+    natural order backwards) or "ulp" (natural order, every replayed time
+    after the operating point moved up by one unit in the last place — the
+    same steps perturbed at round-off level).  Returns (times, values,
+    stats)."""
     nl, probes, times, orders, order = task
     o = Oracle(nl)
     if order is True or order == "md":
         o.use_minimum_degree()
     elif order == "reverse":
         o.set_order(np.arange(o.n - 1, -1, -1, dtype=np.int32))
+    elif order == "ulp":
+        if times is not None:
+            times = np.array(times, np.float64)
+            times[1:] = np.nextafter(times[1:], np.inf)
     elif order not in (None, False):
-        raise ValueError(f"unknown elimination order {order!r}")
+        raise ValueError(f"unknown variant {order!r}")
     if times is None:
         t, v, st = o.transient(probes=probes)
         return t, v, st

@@ -13,19 +13,21 @@ Pointwise criterion:  |v_gpu - v_oracle| <= WAVE_RTOL * max|v_oracle| + WAVE_ATO
 with WAVE_RTOL = 1e-6 (the reltol of the target forms) and WAVE_ATOL = 1e-9 V.
 
 Round-off floor.  A ring oscillator kicked out of its metastable operating
-point amplifies round-off: every inverter starts at high gain.  Two replays
-by the oracle itself that differ only in the LU elimination order (both
-valid; KLU too picks one order among many) agree pointwise only for the
-first ~100 ps and then differ by up to 0.07 V over 2 ns — a sub-picosecond
-shift of the switching instants.  Where the configuration is such a ring,
-the oracle replays the sequence twice, in two elimination orders, and the
-difference between those two replays is the reference's own round-off
-floor.  The GPU must then meet the pointwise criterion on every point up to
-the first one where the floor exceeds FLOOR_NEGLIGIBLE * max|v| (the floor
-is negligible there, so the comparison is exact), and on the whole run stay
-within max(pointwise tolerance, FLOOR_FACTOR * the largest floor).  Driven,
-stable circuits (the diode ladder, the grid, the logic DAG) do not amplify
-round-off and meet the pointwise criterion everywhere.
+point amplifies round-off: every inverter starts at high gain.  The oracle
+replaying the same accepted steps with every time point moved by one unit
+in the last place — a perturbation of the size of the GPU's own round-off
+(CUDA's exp, another summation order) — agrees with the unperturbed replay
+pointwise only for the first ~100 ps and then differs by up to 0.07 V over
+2 ns: a sub-picosecond shift of the switching instants.  (The LU elimination
+order is not such a perturbation here: on these rings every order gives the
+same bits to 1e-22.)  Where the configuration is such a ring, that
+difference is the reference's own round-off floor.  The GPU must then meet
+the pointwise criterion on every point up to the first one where the floor
+exceeds FLOOR_NEGLIGIBLE * max|v| (the floor is negligible there, so the
+comparison is exact), and on the whole run stay within max(pointwise
+tolerance, FLOOR_FACTOR * the largest floor).  Driven, stable circuits (the
+diode ladder, the grid, the logic DAG) and the first 200 steps of the long
+ring do not amplify round-off and meet the pointwise criterion everywhere.
 
 Newton runs at RELTOL 1e-6 / ABSTOL 1e-9 so that a Newton solve that takes
 one iteration more in one run than in the other still lands within the
@@ -94,9 +96,9 @@ def _replayed(name, t_gpu, res):
 
 
 def _check(name, t_gpu, v_gpu, ref, alt=None):
-    """ref: the oracle's replay; alt: the same replay in another elimination
-    order (None for circuits that do not amplify round-off).  Returns the
-    largest |dv|, the number of exactly compared points and the floor."""
+    """ref: the oracle's replay; alt: the same replay with every time moved
+    by one ulp (None for circuits that do not amplify round-off).  Returns
+    the largest |dv|, the number of exactly compared points and the floor."""
     v_ref = _replayed(name, t_gpu, ref)
     vmax = float(np.max(np.abs(v_ref)))
     tol = WAVE_RTOL * vmax + WAVE_ATOL
@@ -104,7 +106,9 @@ def _check(name, t_gpu, v_gpu, ref, alt=None):
     if alt is None:
         assert float(err.max()) <= tol, (name, float(err.max()), tol)
         return float(err.max()), len(err), 0.0
-    floor = np.max(np.abs(_replayed(name, t_gpu, alt) - v_ref), axis=1)
+    t_alt, v_alt, st_alt = alt
+    assert st_alt["status"] == 0 and len(t_alt) == len(t_gpu), (name, "floor replay", st_alt)
+    floor = np.max(np.abs(v_alt - v_ref), axis=1)
     above = np.nonzero(floor > FLOOR_NEGLIGIBLE * vmax)[0]
     exact = int(above[0]) if len(above) else len(floor)
     assert exact >= min(MIN_EXACT_POINTS, len(floor)), (name, exact)
@@ -118,8 +122,8 @@ def _check(name, t_gpu, v_gpu, ref, alt=None):
 def test_monte_carlo_batch_rings_match_oracle_replay(xg, oracle_mod, torch_cuda):
     """32 rings of the bench's 4,096-ring batch, run as one batch on the GPU
     (each circuit keeps its own step control) at TIMEINT and Newton RELTOL
-    1e-6; every ring is replayed alone by the oracle, in the natural
-    elimination order and (the round-off floor) in minimum-degree order."""
+    1e-6; every ring is replayed alone by the oracle, as recorded and (the
+    round-off floor) with its times moved by one ulp."""
     full = N.monte_carlo_rings(4096)
     picks = [int(i * 4096 / 32) + (i % 7) for i in range(32)]
     rings = [N.extract_circuit(full, ci) for ci in picks]
@@ -137,7 +141,7 @@ def test_monte_carlo_batch_rings_match_oracle_replay(xg, oracle_mod, torch_cuda)
     for k, r in enumerate(rings):
         r.tran = b.tran
         t, o, _ = runs[k]
-        tasks += [(r, local_probes[k], t, o, None), (r, local_probes[k], t, o, "md"),
+        tasks += [(r, local_probes[k], t, o, None), (r, local_probes[k], t, o, "ulp"),
                   (r, local_probes[k], None, None, None)]
     res = oracle_mod.run_many(tasks)
     worst, exact_min = 0.0, None
@@ -155,9 +159,9 @@ def test_monte_carlo_batch_rings_match_oracle_replay(xg, oracle_mod, torch_cuda)
 
 _CONFIGS = {
     # name: (netlist maker, probe names, max accepted steps (0: to tstop), oracle elimination
-    #        order, order of the round-off-floor replay (None: the circuit does not amplify round-off))
+    #        order, round-off-floor replay (None: the circuit does not amplify round-off))
     "c1_diode_ladder_1000": (lambda: N.diode_ladder(1000, seed=1), ["n1", "n500", "n1000"], 0, "md", None),
-    "c2_ring_10001": (lambda: N.ring_oscillator(10001), ["n1", "n5000", "n10001"], 200, None, "reverse"),
+    "c2_ring_10001": (lambda: N.ring_oscillator(10001), ["n1", "n5000", "n10001"], 200, None, "ulp"),
     "c3_power_grid_200": (lambda: N.power_grid(200, 320, seed=3), ["center"], 40, "md", None),
     "c5_bsim4_dag_5000": (lambda: N.bsim4_logic_dag(5000, 16, seed=7, tstop=2e-9), ["g10", "g200", "g600"],
                           100, "md", None),

@@ -36,6 +36,7 @@ PREC_FP64, PREC_FP32_IR = 0, 1
 ORDER_ND, ORDER_MIN_DEGREE = 0, 1
 TOP_ONE_CTA, TOP_LEVELS = 1, 2
 PRED_POLY, PRED_LEARNED = 0, 1
+TUNE_MODEL, TUNE_TIMED = 0, 1
 MLP_NPARAM, MLP_NNORM = 4609, 12
 FLAG_DCOP, FLAG_INITJCT = 1, 2
 
@@ -47,6 +48,7 @@ EXPORTED = [
     "xg_get_pattern", "xg_update_sources", "xg_update_state", "xg_load_dae_vectors",
     "xg_load_dae_matrices", "xg_lu_analyze", "xg_lu_factor", "xg_lu_solve",
     "xg_lu_solve_noalloc", "xg_lu_set_precision", "xg_lu_info", "xg_lu_schedule_info", "xg_lu_set_schedule", "xg_lu_analyze_pattern",
+    "xg_lu_set_tuning", "xg_lu_tuning_info",
     "xg_transient", "xg_tran_start", "xg_tran_advance", "xg_tran_results", "xg_tran_end",
     "xg_tran_predictors", "xg_tran_orders", "xg_tran_profile", "xg_tran_predictor_stats", "xg_set_predictor", "xg_mlp_set", "xg_mlp_get",
     "xg_mlp_train", "xg_mlp_grad", "xg_mlp_forward",
@@ -72,6 +74,15 @@ class TranParams(C.Structure):
 class NewtonParams(C.Structure):
     _fields_ = [("reltol", C.c_double), ("abstol", C.c_double), ("deltaxtol", C.c_double),
                 ("rhstol", C.c_double), ("smallupdatetol", C.c_double), ("maxstep", C.c_int)]
+
+
+class LuTuning(C.Structure):
+    _fields_ = [("mode", C.c_int), ("from_cache", C.c_int), ("factor_threads", C.c_int),
+                ("factor_meta", C.c_int), ("lsolve_threads", C.c_int), ("usolve_threads", C.c_int),
+                ("model_factor_threads", C.c_int), ("model_factor_meta", C.c_int),
+                ("model_lsolve_threads", C.c_int), ("model_usolve_threads", C.c_int),
+                ("factor_us", C.c_double), ("solve_us", C.c_double), ("model_factor_us", C.c_double),
+                ("model_solve_us", C.c_double)]
 
 
 class TranStats(C.Structure):
@@ -132,6 +143,8 @@ def lib() -> C.CDLL:
     L.xg_lu_info.argtypes = [P, C.POINTER(C.c_longlong), C.POINTER(I), C.POINTER(I), C.POINTER(I)]
     L.xg_lu_schedule_info.argtypes = [P, C.POINTER(I), C.POINTER(I), C.POINTER(I)]
     L.xg_lu_set_schedule.argtypes = [P, I, I, I]
+    L.xg_lu_set_tuning.argtypes = [P, I]
+    L.xg_lu_tuning_info.argtypes = [P, C.POINTER(LuTuning)]
     L.xg_lu_analyze_pattern.argtypes = [I, C.POINTER(I), C.POINTER(I), C.POINTER(C.c_double), I,
                                         C.POINTER(C.c_longlong), C.POINTER(I), C.POINTER(I), C.POINTER(I)]
     L.xg_transient.argtypes = [P, C.POINTER(TranParams), I, ip, I, ip, dp, dp, C.POINTER(TranStats)]
@@ -281,6 +294,16 @@ class Circuit:
         ORDER_MIN_DEGREE, and TOP_ONE_CTA / TOP_LEVELS for the factor and
         solve tops; applies from the next analysis."""
         self._check(lib().xg_lu_set_schedule(self.h, int(ordering), int(factor_top), int(solve_top)))
+
+    def lu_set_tuning(self, mode: int):
+        """TUNE_TIMED (default): launch shapes of the LU sweeps chosen by
+        timed trials after each analysis; TUNE_MODEL: closed-form choice."""
+        self._check(lib().xg_lu_set_tuning(self.h, int(mode)))
+
+    def lu_tuning(self):
+        t = LuTuning()
+        self._check(lib().xg_lu_tuning_info(self.h, C.byref(t)))
+        return {f: getattr(t, f) for f, _ in LuTuning._fields_}
 
     def lu_info(self):
         nnz = C.c_longlong()

@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -57,6 +58,8 @@ struct xg_ctx {
   bool lu_ready = false;
   int n_analyze = 0;
   int lu_prec = XG_PREC_FP64, lu_refine = 2;  // xg_lu_set_precision
+  int tune_mode = XG_TUNE_TIMED;               // xg_lu_set_tuning
+  xg_lu_tuning tuning{};                       // what the tuner chose for the current analysis
   int predictor = XG_PRED_POLY;                // xg_set_predictor
   std::vector<int> h_tlv_item_ptr, h_tlv_grp_ptr;  // host copies for the per-level top launches
   std::vector<int> h_ls_lvl_ptr, h_fs_lvl_ptr;
@@ -926,6 +929,7 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
           L.fm_smem[w] = std::max(L.fm_smem[w], (int)(vb + H.fm_gbytes[g]));
         }
       }
+      L.fm_on = any_meta && H.fm_model_on;
       if (any_meta) {
         int *c = nullptr, *e = nullptr;
         if ((rc = dev_upload(ctx, &c, H.fm_col, A))) return rc;
@@ -959,6 +963,175 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
   return XG_OK;
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Launch-shape tuner of the LU sweeps.  Every candidate computes the same
+// bits (the shapes change which threads do the work, not the order of any
+// sum), so the choice is made by timing alone: the factorization with and
+// without the staged update metadata at 64..512 threads per CTA, then the L
+// and the U solve at 64..512 threads, each candidate launched on the
+// matrix the analysis was computed from, L2 flushed before every timed
+// launch (in a tick the device evaluation streams the state through L2
+// between factorizations).  Choices are cached per analysis (a hash of the
+// factor pattern, pivot order and schedules), so a re-analysis of the same
+// pattern or a second context reuses them.
+namespace {
+
+struct TuneChoice {
+  int fm_on, fs, ls, us;
+  double factor_us, solve_us;
+};
+std::mutex g_tune_mu;
+std::map<unsigned long long, TuneChoice> g_tune_cache;
+
+unsigned long long fnv(unsigned long long h, const std::vector<int> &v) {
+  for (int x : v) {
+    h ^= (unsigned)x;
+    h *= 1099511628211ULL;
+  }
+  h ^= v.size();
+  return h * 1099511628211ULL;
+}
+
+unsigned long long analysis_hash(const LUHost &H, int prec, int sms) {
+  unsigned long long h = 1469598103934665603ULL;
+  h = fnv(h, {H.n, prec, sms});
+  for (const std::vector<int> *v : {&H.cp, &H.ri, &H.row_of_step, &H.fsched.items, &H.fsched.grp_lvl,
+                                    &H.lsched.items, &H.lsched.grp_lvl, &H.grp_snz, &H.fm_gbytes})
+    h = fnv(h, *v);
+  return h;
+}
+
+}  // namespace
+
+// Median device time (us) of `timed` launches of fn after one warm-up, L2
+// flushed before each.
+template <class F>
+static int time_launch(xg_ctx *ctx, void *flush, size_t flush_bytes, F &&fn, double *us) {
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return fail(ctx, XG_ERR_CUDA, "cudaEventCreate"); }
+  fn();
+  std::vector<double> t;
+  int rc = XG_OK;
+  for (int k = 0; k < 3 && rc == XG_OK; ++k) {
+    if (cudaMemsetAsync(flush, k + 1, flush_bytes, ctx->stream) != cudaSuccess) { rc = XG_ERR_CUDA; break; }
+    cudaEventRecord(e0, ctx->stream);
+    fn();
+    cudaEventRecord(e1, ctx->stream);
+    float ms = 0.f;
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = XG_ERR_CUDA;
+    t.push_back(ms * 1e3);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc == XG_OK && cudaGetLastError() != cudaSuccess) rc = XG_ERR_CUDA;
+  if (rc) return fail(ctx, rc, "LU tuner: CUDA failure");
+  std::sort(t.begin(), t.end());
+  *us = t[t.size() / 2];
+  return XG_OK;
+}
+
+static int tune_lu(xg_ctx *ctx, const LUHost &H, const double *vals_dev) {
+  LUDev &L = ctx->L;
+  xg_lu_tuning &T = ctx->tuning;
+  T = xg_lu_tuning{};
+  T.mode = ctx->tune_mode;
+  T.model_factor_threads = T.factor_threads = L.fs_threads;
+  T.model_factor_meta = T.factor_meta = L.fm_on;
+  T.model_lsolve_threads = T.lsolve_threads = L.ls_threads;
+  T.model_usolve_threads = T.usolve_threads = L.us_threads;
+  if (ctx->tune_mode != XG_TUNE_TIMED || L.fs.n_groups + L.ls.n_groups == 0) return XG_OK;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  const unsigned long long key = analysis_hash(H, ctx->lu_prec, sms);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      const TuneChoice &c = it->second;
+      L.fm_on = c.fm_on; L.fs_threads = c.fs; L.ls_threads = c.ls; L.us_threads = c.us;
+      T.factor_meta = c.fm_on; T.factor_threads = c.fs; T.lsolve_threads = c.ls; T.usolve_threads = c.us;
+      T.factor_us = c.factor_us; T.solve_us = c.solve_us;
+      T.from_cache = 1;
+      return XG_OK;
+    }
+  }
+  // scratch of the trials: an L2 flush buffer and solve vectors
+  const size_t flush_bytes = 256u << 20;
+  void *flush = nullptr;
+  double *b = nullptr, *x = nullptr;
+  CK(cudaMalloc(&flush, flush_bytes));
+  int rc = XG_OK;
+  if (cudaMalloc((void **)&b, sizeof(double) * L.n) != cudaSuccess ||
+      cudaMalloc((void **)&x, sizeof(double) * L.n) != cudaSuccess) rc = fail(ctx, XG_ERR_CUDA, "cudaMalloc");
+  if (rc == XG_OK) {
+    std::vector<double> ones(L.n, 1.0);
+    if (cudaMemcpyAsync(b, ones.data(), sizeof(double) * L.n, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
+      rc = fail(ctx, XG_ERR_CUDA, "cudaMemcpy");
+    if (L.mixed) L.a_vals = vals_dev;
+  }
+  const int sizes[4] = {64, 128, 256, 512};
+  auto factor = [&]() { launch_lu_factor_k(ctx->stream, L, vals_dev, ctx->d.cs, 0, kRuntimePivotTol); };
+  auto solve = [&]() { launch_lu_solve_k(ctx->stream, L, b, x, ctx->d.cs, 0); };
+  // the model's choice first (its time is reported beside the tuned one)
+  if (rc == XG_OK) rc = time_launch(ctx, flush, flush_bytes, factor, &T.model_factor_us);
+  if (rc == XG_OK) rc = time_launch(ctx, flush, flush_bytes, solve, &T.model_solve_us);
+  double best = T.model_factor_us;
+  const int fm_model = L.fm_on, fs_model = L.fs_threads;
+  int best_fm = fm_model, best_fs = fs_model;
+  const bool can_meta = L.fm_gbytes != nullptr;
+  if (L.fs.n_groups > 0)
+    for (int fm = 0; fm <= (can_meta ? 1 : 0) && rc == XG_OK; ++fm)
+      for (int s : sizes) {
+        if (fm == fm_model && s == fs_model) continue;
+        L.fm_on = fm;
+        L.fs_threads = s;
+        double us = 0;
+        if ((rc = time_launch(ctx, flush, flush_bytes, factor, &us))) break;
+        if (us < best) { best = us; best_fm = fm; best_fs = s; }
+      }
+  L.fm_on = best_fm;
+  L.fs_threads = best_fs;
+  T.factor_us = best;
+  double sbest = T.model_solve_us;
+  for (int w = 0; w < 2 && rc == XG_OK; ++w) {  // L solve, then U solve
+    int &thr = w ? L.us_threads : L.ls_threads;
+    const int keep = thr;
+    int pick = keep;
+    if ((w ? L.fs.n_groups : L.ls.n_groups) == 0) continue;
+    for (int s : sizes) {
+      if (s == keep) continue;
+      thr = s;
+      double us = 0;
+      if ((rc = time_launch(ctx, flush, flush_bytes, solve, &us))) break;
+      if (us < sbest) { sbest = us; pick = s; }
+    }
+    thr = pick;
+  }
+  T.solve_us = sbest;
+  cudaFree(flush);
+  if (b) cudaFree(b);
+  if (x) cudaFree(x);
+  // the trials may have raised the breakdown flag: the analysis' values
+  // are factored for real by the caller
+  if (cudaMemsetAsync(L.breakdown, 0, sizeof(int), ctx->stream) != cudaSuccess && rc == XG_OK)
+    rc = fail(ctx, XG_ERR_CUDA, "cudaMemset");
+  if (rc) {
+    L.fm_on = fm_model; L.fs_threads = fs_model;
+    L.ls_threads = T.model_lsolve_threads; L.us_threads = T.model_usolve_threads;
+    return rc;
+  }
+  T.factor_meta = L.fm_on; T.factor_threads = L.fs_threads;
+  T.lsolve_threads = L.ls_threads; T.usolve_threads = L.us_threads;
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune_cache[key] = TuneChoice{L.fm_on, L.fs_threads, L.ls_threads, L.us_threads, T.factor_us, T.solve_us};
+  return XG_OK;
+}
+
+extern "C" {
+
 static int lu_analyze_from_device(xg_ctx *ctx, const double *vals_dev) {
   std::vector<double> v(ctx->nnz);
   CK(cudaMemcpyAsync(v.data(), vals_dev, sizeof(double) * ctx->nnz, cudaMemcpyDeviceToHost, ctx->stream));
@@ -971,7 +1144,8 @@ static int lu_analyze_from_device(xg_ctx *ctx, const double *vals_dev) {
     if (ctx->sched_stop >= 0) H.solve_top_multi = (ctx->sched_stop == XG_TOP_LEVELS);
   }
   if (rc) return fail(ctx, rc, "LU analysis: " + err);
-  return lu_upload(ctx, H);
+  if ((rc = lu_upload(ctx, H))) return rc;
+  return tune_lu(ctx, H, vals_dev);
 }
 
 int xg_lu_analyze(xg_ctx *ctx, const double *vals) {
@@ -1042,6 +1216,22 @@ int xg_lu_set_precision(xg_ctx *ctx, int precision, int n_refine) {
   ctx->lu_prec = precision;
   ctx->lu_refine = n_refine;
   ctx->lu_ready = false;  // the next xg_lu_analyze (or transient) builds factors of this precision
+  return XG_OK;
+}
+
+int xg_lu_set_tuning(xg_ctx *ctx, int mode) {
+  if (!ctx) return XG_ERR_ARG;
+  if (mode != XG_TUNE_MODEL && mode != XG_TUNE_TIMED) return fail(ctx, XG_ERR_ARG, "mode must be XG_TUNE_MODEL or XG_TUNE_TIMED");
+  if (ctx->run) return fail(ctx, XG_ERR_STATE, "tuning cannot change during a transient");
+  ctx->tune_mode = mode;
+  ctx->lu_ready = false;  // applies from the next analysis
+  return XG_OK;
+}
+
+int xg_lu_tuning_info(xg_ctx *ctx, xg_lu_tuning *out) {
+  if (!ctx || !out) return XG_ERR_ARG;
+  if (!ctx->lu_ready) return fail(ctx, XG_ERR_STATE, "no LU analysis");
+  *out = ctx->tuning;
   return XG_OK;
 }
 

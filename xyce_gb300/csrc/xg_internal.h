@@ -248,6 +248,7 @@ struct LUDev {
   const int4 *fm_col = nullptr, *fm_ent = nullptr;  // see LUHost::fm_col
   int *fm_eptr = nullptr, *fm_tptr = nullptr, *fm_tgt = nullptr, *fm_gbytes = nullptr;
   int fm_smem[2] = {0, 0};  // launch buffer bytes (double | float factors) when metadata is staged
+  int fm_on = 0;            // stage the update metadata of the groups that have it (fm_gbytes > 0)
   SchedDev fs, ls;           // factor (and, backwards, U solve) / L-solve schedules
   int f_levels = 0, l_levels = 0, u_levels = 0;  // plain level counts (statistics)
   // Mixed precision (FP32 factors, FP64 iterative refinement): lu32 holds the
@@ -289,6 +290,34 @@ struct LUDev {
   double *ir_r = nullptr;
   const int *a_rp = nullptr, *a_ci = nullptr, *a_circ = nullptr;
   const double *a_vals = nullptr;
+};
+
+// Circuit-resident form of the tick (batches of small circuits): one CTA
+// runs every stage of a tick for one circuit and loops over ticks until the
+// circuit pauses, finishes, fails or parks on a pivot breakdown; CTAs take
+// circuits from a queue (largest first).  Per circuit c: its MOSFET-1 and
+// diode instances, sources, long rows / long Jacobian entries (CSR lists
+// *_ptr[c] .. *_ptr[c+1]), and its LU levels — lv_ptr[c] .. lv_ptr[c+1] are
+// level indices into f_lptr (factor; the U solve walks them backwards) and
+// l_lptr (L solve), whose items are in f_items / l_items.  Per step: how the
+// grouped kernels compute it (f_kind: 0 one thread, 1 a warp, 2 the whole
+// CTA; l_meth / u_meth: 0 y = b, 1 one thread in entry order, 2 an 8-lane
+// team, 3 the whole CTA in the fixed long-row order), so that both forms
+// compute the same bits.
+constexpr int kFusedMaxRows = 2048;        // largest circuit the resident form takes
+constexpr int kFusedMinCircuits = 64;      // smallest batch the resident form takes
+constexpr int kFusedThreads = 128;         // CTA size of the resident tick
+constexpr int kFusedMaxTicks = 1 << 20;    // ticks of one circuit in one launch, at most
+struct FusedDev {
+  int *order = nullptr, *queue = nullptr;
+  int *m1_ptr = nullptr, *m1_list = nullptr, *d_ptr = nullptr, *d_list = nullptr;
+  int *src_ptr = nullptr, *src_list = nullptr;
+  int *lr_ptr = nullptr, *lr_list = nullptr, *le_ptr = nullptr, *le_list = nullptr;
+  int *f_cl = nullptr, *f_lptr = nullptr, *f_items = nullptr;
+  int *l_cl = nullptr, *l_lptr = nullptr, *l_items = nullptr;
+  signed char *f_kind = nullptr, *l_meth = nullptr, *u_meth = nullptr;
+  unsigned long long *ticks = nullptr;  // [0] largest tick count of a circuit, [1] circuit-ticks (this launch)
+  int max_rows = 0, grid = 0;
 };
 
 // Host-side analysis result.
@@ -342,6 +371,9 @@ struct LUHost {
   // in the group's fm_tgt segment (from fm_tptr[g]); position of U(k, j) in
   // the column}; fm_gbytes[g] = metadata bytes (0: values only)
   std::vector<int> fm_col, fm_eptr, fm_ent, fm_tptr, fm_tgt, fm_gbytes;
+  // the closed-form choice of staging that metadata: on when the launch
+  // buffer with it allows as many resident CTAs as the values alone
+  bool fm_model_on = false;
 };
 
 // weight(j): entries item j touches (caps the packing of tiny groups)

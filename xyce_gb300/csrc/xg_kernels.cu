@@ -68,10 +68,10 @@ __device__ double wave_value_d(int kind, const double *d, int nd, double t) {
   return 0.0;
 }
 
-// One thread per source; V sources own one B slot, I sources two (pos, neg).
-__global__ void k_sources(DevArrays d, int n_v, int n_src, int use_explicit, double t_explicit) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n_src) return;
+// Source k's value into its B slots; V sources own one B slot, I sources
+// two (pos, neg).
+__device__ __forceinline__ void source_value(const DevArrays &d, int k, int n_v, int use_explicit,
+                                             double t_explicit) {
   double t;
   if (use_explicit) {
     t = t_explicit;
@@ -91,15 +91,19 @@ __global__ void k_sources(DevArrays d, int n_v, int n_src, int use_explicit, dou
   }
 }
 
+// One thread per source.
+__global__ void k_sources(DevArrays d, int n_v, int n_src, int use_explicit, double t_explicit) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n_src) source_value(d, k, n_v, use_explicit, t_explicit);
+}
+
 // ---------------------------------------------------------------------------
 // MOSFET level 1, drain/source primes merged (RD = RS = 0).
 // Store planes (x nm): vbd vbs vgs vds von gm; state planes: capgs capgd capgb qgs qgd qgb qbd qbs.
 // Slots: F[D,S,B]  Q[G,B,D,S]  L[G,B,D,S]  M[4x4 over D,G,S,B].
-__global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base, int combined,
-                                              int masked, int it_arg, int flags_arg,
-                                              int slotF, int slotQ, int slotL, int slotM) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nm) return;
+__device__ __forceinline__ void mos1_eval(const DevArrays &d, int i, int nm, int sto_base, int combined,
+                                          int masked, int it_arg, int flags_arg, int slotF, int slotQ, int slotL,
+                                          int slotM) {
   int c = __ldg(d.m1_circ + i);
   int iter = it_arg;
   bool dcop = flags_arg & XG_FLAG_DCOP, initJct = flags_arg & XG_FLAG_INITJCT;
@@ -378,14 +382,19 @@ __global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base,
   }
 }
 
+__global__ void __launch_bounds__(128) k_mos1(DevArrays d, int nm, int sto_base, int combined,
+                                              int masked, int it_arg, int flags_arg,
+                                              int slotF, int slotQ, int slotL, int slotM) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nm) mos1_eval(d, i, nm, sto_base, combined, masked, it_arg, flags_arg, slotF, slotQ, slotL, slotM);
+}
+
 // ---------------------------------------------------------------------------
 // Diode level 1 (no sidewall).  Store planes: vd qd cd.
 // Slots: F[P,N,R]  Q[N,R]  L[N,R]  M[(P,P)(P,R)(N,N)(N,R)(R,P)(R,N)(R,R)].
-__global__ void __launch_bounds__(128) k_diode(DevArrays d, int nd, int combined, int masked,
-                                               int it_arg, int flags_arg, int slotF, int slotQ,
-                                               int slotL, int slotM) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nd) return;
+__device__ __forceinline__ void diode_eval(const DevArrays &d, int i, int nd, int combined, int masked,
+                                           int it_arg, int flags_arg, int slotF, int slotQ, int slotL,
+                                           int slotM) {
   int c = __ldg(d.d_circ + i);
   int iter = it_arg;
   bool dcop = flags_arg & XG_FLAG_DCOP, initJct = flags_arg & XG_FLAG_INITJCT;
@@ -495,6 +504,13 @@ __global__ void __launch_bounds__(128) k_diode(DevArrays d, int nd, int combined
   }
 }
 
+__global__ void __launch_bounds__(128) k_diode(DevArrays d, int nd, int combined, int masked,
+                                               int it_arg, int flags_arg, int slotF, int slotQ,
+                                               int slotL, int slotM) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nd) diode_eval(d, i, nd, combined, masked, it_arg, flags_arg, slotF, slotQ, slotL, slotM);
+}
+
 // ---------------------------------------------------------------------------
 // Deterministic per-(block, circuit) partial reductions.  A row block covers
 // rows [b*kRowBlock, (b+1)*kRowBlock); pair_base[b] is the first partial slot
@@ -529,70 +545,101 @@ __device__ void block_partials(const DevArrays &d, int n, double vmax, double vs
   (void)r;
 }
 
-// Block-wide sum of one double (blockDim.x a multiple of 32, <= 1024).
-__device__ __forceinline__ double block_sum(double v) {
-  __shared__ double wsum[32];
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+// Sums of a long gather in a fixed order, whatever the CTA size: 256
+// virtual lanes (8 virtual warps) each accumulate their strided share, each
+// virtual warp reduces by a butterfly, and one warp reduces the 8 warp sums
+// by a butterfly over 32 lanes (zeros beyond the 8).  W values per lane;
+// the results land in out[0 .. W) of thread 0.  ws: 8 * W doubles of shared
+// memory.
+constexpr int kGatherLanes = 256;
+template <int W, class Lane>
+__device__ __forceinline__ void gather_sums(Lane &&lane_sums, double *ws, double *out) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   __syncthreads();
-  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = v;
-  __syncthreads();
-  double t = 0.0;
-  if (threadIdx.x < 32) {
-    t = (threadIdx.x < (blockDim.x >> 5)) ? wsum[threadIdx.x] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  for (int vw = warp; vw < kGatherLanes / 32; vw += nwarps) {
+    double v[W];
+    lane_sums(vw * 32 + lane, v);
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+      if (lane == 0) ws[k * 8 + vw] = v[k];
+    }
   }
-  return t;  // valid in thread 0
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      double t = lane < kGatherLanes / 32 ? ws[k * 8 + lane] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (lane == 0) out[k] = t;
+    }
+  }
 }
 
-// Long rows (e.g. a supply node touching every PMOS): ceil(items / kLongPart)
-// blocks per row gather F, Q, B, L partial sums, strided over the row's lists.
-__global__ void __launch_bounds__(256) k_long_rows(DevArrays d) {
-  const int lr = d.lrow_blk[blockIdx.x], part = blockIdx.x - d.lrow_ptr[lr];
+// Part `part` of long row lr (e.g. a supply node touching every PMOS): the
+// F, Q, B, L partial sums of its share of the row's lists, into
+// long_rsum[4 * (lrow_ptr[lr] + part) ..].
+__device__ __forceinline__ void long_row_part(const DevArrays &d, int lr, int part, double *ws) {
   const int nparts = d.lrow_ptr[lr + 1] - d.lrow_ptr[lr];
   const int r = d.long_rows[lr];
-  const CircState &s = d.cs[d.circ_of_row[r]];
-  if (!circ_active(s)) return;
-  const int start = part * blockDim.x + threadIdx.x, stride = nparts * blockDim.x;
-  double F = 0.0, Q = 0.0, B = 0.0, L = 0.0;
-  for (int e = d.rp[r] + start; e < d.rp[r + 1]; e += stride) {
-    const double xv = d.x[d.ci[e]];
-    F += d.Glin[e] * xv;
-    Q += d.Clin[e] * xv;
-  }
-  for (int k = d.vF_ptr[r] + start; k < d.vF_ptr[r + 1]; k += stride) F += d.sF[d.vF_idx[k]];
-  for (int k = d.vQ_ptr[r] + start; k < d.vQ_ptr[r + 1]; k += stride) Q += d.sQ[d.vQ_idx[k]];
-  for (int k = d.vB_ptr[r] + start; k < d.vB_ptr[r + 1]; k += stride) B += d.sB[d.vB_idx[k]];
-  for (int k = d.vL_ptr[r] + start; k < d.vL_ptr[r + 1]; k += stride) L += d.sL[d.vL_idx[k]];
-  F = block_sum(F);
-  Q = block_sum(Q);
-  B = block_sum(B);
-  L = block_sum(L);
+  const int stride = nparts * kGatherLanes;
+  double out[4];
+  gather_sums<4>([&](int vl, double *v) {
+    const int start = part * kGatherLanes + vl;
+    double F = 0.0, Q = 0.0, B = 0.0, L = 0.0;
+    for (int e = d.rp[r] + start; e < d.rp[r + 1]; e += stride) {
+      const double xv = d.x[d.ci[e]];
+      F += d.Glin[e] * xv;
+      Q += d.Clin[e] * xv;
+    }
+    for (int k = d.vF_ptr[r] + start; k < d.vF_ptr[r + 1]; k += stride) F += d.sF[d.vF_idx[k]];
+    for (int k = d.vQ_ptr[r] + start; k < d.vQ_ptr[r + 1]; k += stride) Q += d.sQ[d.vQ_idx[k]];
+    for (int k = d.vB_ptr[r] + start; k < d.vB_ptr[r + 1]; k += stride) B += d.sB[d.vB_idx[k]];
+    for (int k = d.vL_ptr[r] + start; k < d.vL_ptr[r + 1]; k += stride) L += d.sL[d.vL_idx[k]];
+    v[0] = F; v[1] = Q; v[2] = B; v[3] = L;
+  }, ws, out);
   if (threadIdx.x == 0) {
-    double *o = d.long_rsum + 4 * (size_t)blockIdx.x;
-    o[0] = F; o[1] = Q; o[2] = B; o[3] = L;
+    double *o = d.long_rsum + 4 * (size_t)(d.lrow_ptr[lr] + part);
+    o[0] = out[0]; o[1] = out[1]; o[2] = out[2]; o[3] = out[3];
   }
 }
 
-// Long Jacobian entries (e.g. a supply node's diagonal): ceil(items / kLongPart) blocks each.
-__global__ void __launch_bounds__(256) k_long_entries(DevArrays d) {
-  const int le = d.lent_blk[blockIdx.x], part = blockIdx.x - d.lent_ptr[le];
+// Part `part` of long Jacobian entry le (e.g. a supply node's diagonal).
+__device__ __forceinline__ void long_entry_part(const DevArrays &d, int le, int part, double *ws) {
   const int nparts = d.lent_ptr[le + 1] - d.lent_ptr[le];
   const int e = d.long_ents[le];
-  const CircState &s = d.cs[d.circ_of_row[d.erow[e]]];
-  if (!circ_active(s)) return;
-  const int start = part * blockDim.x + threadIdx.x, stride = nparts * blockDim.x;
-  double v = 0.0;
-  for (int k = d.m_ptr[e] + start; k < d.m_ptr[e + 1]; k += stride) v += d.sM[d.m_idx[k]];
-  v = block_sum(v);
-  if (threadIdx.x == 0) d.long_esum[blockIdx.x] = v;
+  const int stride = nparts * kGatherLanes;
+  double out[1];
+  gather_sums<1>([&](int vl, double *v) {
+    double s = 0.0;
+    for (int k = d.m_ptr[e] + part * kGatherLanes + vl; k < d.m_ptr[e + 1]; k += stride) s += d.sM[d.m_idx[k]];
+    v[0] = s;
+  }, ws, out);
+  if (threadIdx.x == 0) d.long_esum[d.lent_ptr[le] + part] = out[0];
+}
+
+// Long rows: ceil(items / kLongPart) blocks per row.
+__global__ void __launch_bounds__(256) k_long_rows(DevArrays d) {
+  __shared__ double ws[8 * 4];
+  const int lr = d.lrow_blk[blockIdx.x];
+  if (!circ_active(d.cs[d.circ_of_row[d.long_rows[lr]]])) return;
+  long_row_part(d, lr, blockIdx.x - d.lrow_ptr[lr], ws);
+}
+
+// Long Jacobian entries: ceil(items / kLongPart) blocks each.
+__global__ void __launch_bounds__(256) k_long_entries(DevArrays d) {
+  __shared__ double ws[8];
+  const int le = d.lent_blk[blockIdx.x];
+  if (!circ_active(d.cs[d.circ_of_row[d.erow[d.long_ents[le]]]])) return;
+  long_entry_part(d, le, blockIdx.x - d.lent_ptr[le], ws);
 }
 
 // Residual per row: RHS = -(qscale (Q - Q_hist0) + fscale (F - B) + hscale Q_hist2 + gshunt x)
 //                        + limiter terms     (OneStep::obtainResidual, N_TIA_OneStep.C:219-290)
-__global__ void __launch_bounds__(kRowBlock) k_assemble_rows(DevArrays d, int n) {
-  const int r = blockIdx.x * kRowBlock + threadIdx.x;
-  double vmax = 0.0, vsum = 0.0;
-  if (r < n) {
+__device__ __forceinline__ void assemble_row(const DevArrays &d, int r, double &vmax, double &vsum) {
+  vmax = 0.0;
+  vsum = 0.0;
+  {
     const int c = d.circ_of_row[r];
     const CircState &s = d.cs[c];
     if (circ_active(s)) {
@@ -637,14 +684,18 @@ __global__ void __launch_bounds__(kRowBlock) k_assemble_rows(DevArrays d, int n)
       if (!(vsum == vsum) || isinf(vsum)) vmax = vsum = __longlong_as_double(0x7ff8000000000000ULL);
     }
   }
+}
+
+__global__ void __launch_bounds__(kRowBlock) k_assemble_rows(DevArrays d, int n) {
+  const int r = blockIdx.x * kRowBlock + threadIdx.x;
+  double vmax = 0.0, vsum = 0.0;
+  if (r < n) assemble_row(d, r, vmax, vsum);
   block_partials(d, n, vmax, vsum, r);
 }
 
 // Jacobian per CSR entry: J = qscale dQdx + fscale dFdx (+ gshunt on the diagonal)
 // (OneStep::obtainJacobian, N_TIA_OneStep.C:469-500; EpetraMatrix::linearCombo)
-__global__ void k_assemble_J(DevArrays d, int nnz) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= nnz) return;
+__device__ __forceinline__ void assemble_entry(const DevArrays &d, int e) {
   const int r = d.erow[e];
   const CircState &s = d.cs[d.circ_of_row[r]];
   if (!circ_active(s)) return;
@@ -658,6 +709,11 @@ __global__ void k_assemble_J(DevArrays d, int nnz) {
   }
   if (s.gshunt != 0.0 && d.ci[e] == r) v += s.gshunt;  // branch rows have no diagonal entry
   d.J[e] = v;
+}
+
+__global__ void k_assemble_J(DevArrays d, int nnz) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < nnz) assemble_entry(d, e);
 }
 
 // Loader-API assembly: ADD device contributions into caller vectors (loadDAEVectors).
@@ -699,11 +755,9 @@ __global__ void k_load_matrices(DevArrays d, int nnz, double *dQdx, double *dFdx
 
 // ---------------------------------------------------------------------------
 // Per-circuit Newton decision: DampedNewton::converged_ (N_NLS_DampedNewton.C:1191-1396).
-// One warp per circuit reduces the row partials of its residual.
-__global__ void k_newton_ctl(DevArrays d, int ncirc) {
-  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (c >= ncirc) return;
+// One warp per circuit (all 32 lanes call it) reduces the row partials of
+// its residual.
+__device__ __forceinline__ void newton_ctl_circuit(const DevArrays &d, int c, int lane) {
   CircState &s = d.cs[c];
   if (s.phase == PH_STALL) return;  // parked until the host re-pivots; flags kept
   if (!circ_active(s)) {
@@ -783,13 +837,18 @@ __global__ void k_newton_ctl(DevArrays d, int ncirc) {
   }
 }
 
+__global__ void k_newton_ctl(DevArrays d, int ncirc) {
+  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (c < ncirc) newton_ctl_circuit(d, c, threadIdx.x & 31);
+}
+
 // x += dx with the update norm; at the end of a Newton solve, the LTE sum
 // (DataStore::stepLinearCombo + WRMS_errorNorm, N_TIA_DataStore.C:1495,1737)
 // and max|x| for the next error weights.
-__global__ void __launch_bounds__(kRowBlock) k_update(DevArrays d, int n) {
-  const int r = blockIdx.x * kRowBlock + threadIdx.x;
-  double vmax = 0.0, vsum = 0.0;
-  if (r < n) {
+__device__ __forceinline__ void update_row(const DevArrays &d, int r, double &vmax, double &vsum) {
+  vmax = 0.0;
+  vsum = 0.0;
+  {
     const int c = d.circ_of_row[r];
     const CircState &s = d.cs[c];
     if (circ_active(s)) {
@@ -817,6 +876,12 @@ __global__ void __launch_bounds__(kRowBlock) k_update(DevArrays d, int n) {
       }
     }
   }
+}
+
+__global__ void __launch_bounds__(kRowBlock) k_update(DevArrays d, int n) {
+  const int r = blockIdx.x * kRowBlock + threadIdx.x;
+  double vmax = 0.0, vsum = 0.0;
+  if (r < n) update_row(d, r, vmax, vsum);
   block_partials(d, n, vmax, vsum, r);
 }
 
@@ -900,10 +965,9 @@ __device__ double next_bp(const double *bps, int lo, int hi, double t, double bp
 
 // Per-circuit step decision (StepErrorControl::evaluateStepError, OneStep::completeStep /
 // rejectStep, Transient::processSuccessfulStep) and the operating-point stages.
-__global__ void k_step_ctl(DevArrays d, int ncirc, const double *bps, const int *bp_ptr, int cap) {
-  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (c >= ncirc) return;
+// One warp per circuit (all 32 lanes call it).
+__device__ __forceinline__ void step_ctl_circuit(const DevArrays &d, int c, int lane, const double *bps,
+                                                 const int *bp_ptr, int cap) {
   CircState &s = d.cs[c];
   if (!circ_active(s)) return;
   double m = 0.0, sum = 0.0;
@@ -1077,11 +1141,14 @@ __global__ void k_step_ctl(DevArrays d, int ncirc, const double *bps, const int 
   if (s.accepted >= s.stop_at) s.phase = PH_PAUSED;  // the predictor is applied, then the circuit waits
 }
 
+__global__ void k_step_ctl(DevArrays d, int ncirc, const double *bps, const int *bp_ptr, int cap) {
+  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (c < ncirc) step_ctl_circuit(d, c, threadIdx.x & 31, bps, bp_ptr, cap);
+}
+
 // OneStep::updateHistory (N_TIA_OneStep.C:1390-1440), OneStep::initialize history
 // (:1800-1830) and obtainPredictor (:135-175), per row.
-__global__ void k_history(DevArrays d, int n, int cap, int pmax) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n) return;
+__device__ __forceinline__ void history_row(const DevArrays &d, int r, int cap, int pmax) {
   const int c = d.circ_of_row[r];
   const CircState &s = d.cs[c];
   if (s.accept == 3) { d.x[r] = 0.0; return; }
@@ -1145,10 +1212,15 @@ __global__ void k_history(DevArrays d, int n, int cap, int pmax) {
   }
 }
 
-// Accepted store/state become current (curr <- next) for accepted circuits.
-__global__ void k_state_commit(DevArrays d, int nm, int nd, int sto_base_m, int nb, int sto_base_b,
-                               int sta_base_b) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_history(DevArrays d, int n, int cap, int pmax) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) history_row(d, r, cap, pmax);
+}
+
+// Accepted store/state become current (curr <- next) for accepted circuits;
+// i indexes MOSFET-1 instances, then diodes, then BSIM4 instances.
+__device__ __forceinline__ void commit_instance(const DevArrays &d, int i, int nm, int nd, int sto_base_m, int nb,
+                                                int sto_base_b, int sta_base_b) {
   if (i >= nm + nd && i < nm + nd + nb) {
     const int j = i - nm - nd;
     const CircState &s = d.cs[d.b4_circ[j]];
@@ -1176,6 +1248,12 @@ __global__ void k_state_commit(DevArrays d, int nm, int nd, int sto_base_m, int 
       for (int k = 0; k < 3; ++k) d.sto_curr[k * nd + j] = d.sto_next[k * nd + j];
     }
   }
+}
+
+__global__ void k_state_commit(DevArrays d, int nm, int nd, int sto_base_m, int nb, int sto_base_b,
+                               int sta_base_b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  commit_instance(d, i, nm, nd, sto_base_m, nb, sto_base_b, sta_base_b);
 }
 
 // Number of finished circuits (done or failed) and the LU breakdown flag,

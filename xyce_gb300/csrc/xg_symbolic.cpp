@@ -882,8 +882,9 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
       if (ok && vals + meta <= kGroupSmemBytes) out.fm_gbytes[g] = (int)((meta + 15) / 16 * 16);
     }
     // The metadata shortens each level's latency chain, but a larger buffer
-    // lets fewer CTAs share an SM: keep it only when the launch buffer with
-    // it allows as many resident CTAs as the values alone.
+    // lets fewer CTAs share an SM: the closed-form choice stages it only when
+    // the launch buffer with it allows as many resident CTAs as the values
+    // alone (the launch-shape tuner may choose otherwise by timing).
     long long vmax = 0, mmax = 0;
     for (int g = 0; g < S.n_groups; ++g) {
       const long long vb = ((long long)out.grp_snz[g] * 8 + 15) / 16 * 16;
@@ -894,7 +895,7 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
       const long long by_threads = 2048 / std::max(1, out.fs_threads);
       return bytes > 0 ? std::min(by_threads, (long long)kSmemPerSm / bytes) : by_threads;
     };
-    if (resident(mmax) < resident(vmax)) std::fill(out.fm_gbytes.begin(), out.fm_gbytes.end(), 0);
+    out.fm_model_on = resident(mmax) >= resident(vmax);
     bool any = false;
     for (int b2 : out.fm_gbytes) any = any || b2 > 0;
     out.fm_col.clear();
