@@ -223,11 +223,12 @@ def _sample(nl, workload):
     return [(0, nl.names["n1"]), (0, nl.names["n5000"])]
 
 
-def _timed_windows(xg, nl, probes, dev, args, window, prec, flush, stream_of, cap=16, tune=None):
+def _timed_windows(xg, nl, probes, dev, args, window, prec, flush, stream_of, cap=16, tune=None, form=None):
     import torch
     circ = xg.Circuit(nl, device=dev)
     circ.lu_set_precision(prec, 2)
     circ.lu_set_tuning(xg.TUNE_TIMED if tune is None else tune)
+    circ.tran_set_form(xg.FORM_AUTO if form is None else form)
     circ.tran_start(probes=probes, cap=cap)
     stream = stream_of(circ)
     for _ in range(args.warmup):
@@ -431,12 +432,12 @@ def run_ours(args):
     else:
         ms_max, steps_all, evals_all = ms_total, float(steps_done), float(evals)
     value = steps_all / (ms_max / 1e3)
-    # kernels per tick: the kernel nodes of the captured tick graph (sources,
-    # device evaluation, assembly and long-gather passes, Newton control, LU
-    # factor and solves, update, step control, history, state commit,
-    # completion count), replayed once per tick
+    # kernels launched in the timed windows, counted by the driver: the
+    # kernel nodes of each replayed tick graph, or, in the circuit-resident
+    # form, the resident kernel and the completion count of each launch
     kernels_per_tick = int(st1.get("kernels_per_tick", 0))
-    gpu_launches = int(ticks * kernels_per_tick)
+    gpu_launches = int(st1["kernel_launches"] - st0["kernel_launches"])
+    form = {xg.FORM_TICK_GRAPH: "tick_graph", xg.FORM_RESIDENT: "circuit_resident"}.get(st1["form"], "?")
     # the sampled circuits' accepted-step sequences (for the error against FP64)
     counts, times, values, _ = circ.tran_results()
     orders = circ.tran_orders()
@@ -447,7 +448,19 @@ def run_ours(args):
         seqs[(ci, pr)] = (times[ci, :m].copy(), orders[ci, :m].copy(), values[ci, :m, col].copy())
     n_unknowns = circ.n
     roof = lu_roof = stages = None
+    resident_roof = None
+    if form == "circuit_resident":
+        # the whole tick in one kernel: its algorithmic bytes are the device
+        # evaluations' (the per-instance figure) over the timed windows
+        alg = MOS1_BYTES_SURVEY * evals_all
+        ach = alg / (ms_max / 1e3) / 1e9
+        resident_roof = {"kernel": "k_resident (every stage of every tick of a circuit in one CTA)", "bound": "hbm",
+                         "achieved": ach, "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak,
+                         "peak_kind": peak_kind, "algorithmic_bytes": alg,
+                         "note": "device-evaluation bytes only (MOSFET-1 evaluation + stamp per instance per "
+                                 "Newton iteration) over the timed windows; assembly, LU and control bytes not counted"}
     if rank == 0:
+        # the tick profiler launches the tick-graph kernels one by one, stage by stage
         roof, lu_roof, stages = _rooflines(circ, nl, window, hbm_peak, peak_kind, info, args)
     circ.tran_end()
     circ.close()
@@ -466,10 +479,16 @@ def run_ours(args):
                          (s1["newton_iters"] - s0["newton_iters"]) / max(1, s1["accepted"] - s0["accepted"])}
             c2.tran_end()
             c2.close()
+            # the tick graph (16 kernels per tick over the whole batch) instead of the resident form
+            c5, ms5, s0, s1 = _timed_windows(xg, nl, probes, dev, args, window, xg.PREC_FP64, flush, stream_of,
+                                             form=xg.FORM_TICK_GRAPH)
+            forms["fp64_tick_graph"] = (s1["accepted"] - s0["accepted"]) / (ms5 / 1e3)
+            c5.tran_end()
+            c5.close()
             # the LU sweeps with the analysis' closed-form launch shapes instead of the timed ones
             c4, ms4, s0, s1 = _timed_windows(xg, nl, probes, dev, args, window, xg.PREC_FP64, flush, stream_of,
-                                             tune=xg.TUNE_MODEL)
-            forms["fp64_lu_model_shapes"] = (s1["accepted"] - s0["accepted"]) / (ms4 / 1e3)
+                                             tune=xg.TUNE_MODEL, form=xg.FORM_TICK_GRAPH)
+            forms["fp64_tick_graph_lu_model_shapes"] = (s1["accepted"] - s0["accepted"]) / (ms4 / 1e3)
             c4.tran_end()
             c4.close()
             if args.workload == "mc":
@@ -517,8 +536,9 @@ def run_ours(args):
                 "config": config,
                 "device_evals_per_s": evals_all / (ms_max / 1e3),
                 "newton_iters_per_step": (st1["newton_iters"] - st0["newton_iters"]) / max(1, steps_done),
-                "ticks": ticks, "kernels_per_tick": kernels_per_tick, "gpu_launches": gpu_launches,
-                "lu": info, "roofline": roof, "roofline_lu": lu_roof, "tick_stages_us": stages,
+                "form": form, "ticks": ticks, "kernels_per_tick": kernels_per_tick, "gpu_launches": gpu_launches,
+                "lu": info, "roofline": roof, "roofline_lu": lu_roof, "roofline_resident": resident_roof,
+                "tick_stages_us": stages,
                 "max_err_vs_fp64": err, "forms": forms, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks}
         print(json.dumps(line), flush=True)

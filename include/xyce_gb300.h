@@ -307,7 +307,28 @@ typedef struct xg_tran_stats {
   double t_final_min, t_final_max;
   double seconds;                              /* wall time of the run */
   int kernels_per_tick;                        /* kernel launches of one tick (its CUDA graph) */
+  int form;                                    /* XG_FORM_TICK_GRAPH or XG_FORM_RESIDENT: how it advanced */
+  long long kernel_launches;                   /* kernels launched while advancing */
+  long long circuit_ticks;                     /* resident form: Newton iterations summed over circuits */
 } xg_tran_stats;
+
+/* How a transient advances.  XG_FORM_TICK_GRAPH: a tick (one Newton
+ * iteration of every active circuit, 16 kernels) is a captured CUDA graph,
+ * replayed in batches between host synchronizations.  XG_FORM_RESIDENT:
+ * one kernel runs every stage of every tick for a whole batch — each CTA
+ * takes a circuit and iterates its ticks until the circuit pauses,
+ * finishes, fails or parks on a pivot breakdown, then takes the next —
+ * so a circuit that has finished costs nothing and nothing waits on a
+ * grid-wide barrier.  Both compute the same bits.  The resident form needs
+ * a batch of at least 64 circuits of at most 2,048 unknowns each, MOSFET-1
+ * and diode devices only, FP64 factors, the polynomial predictor and an LU
+ * analysis without a top; XG_FORM_AUTO (default) takes it when the batch
+ * admits it.  No reference counterpart (Xyce runs one circuit per process).
+ * Not allowed while a transient is in progress. */
+#define XG_FORM_AUTO        0
+#define XG_FORM_TICK_GRAPH  1
+#define XG_FORM_RESIDENT    2
+int xg_tran_set_form(xg_ctx *ctx, int form);
 
 /* Runs the transient.  probes: global unknown indices to record; every
  * circuit records, at each accepted point, its time and the values of the

@@ -37,6 +37,7 @@ ORDER_ND, ORDER_MIN_DEGREE = 0, 1
 TOP_ONE_CTA, TOP_LEVELS = 1, 2
 PRED_POLY, PRED_LEARNED = 0, 1
 TUNE_MODEL, TUNE_TIMED = 0, 1
+FORM_AUTO, FORM_TICK_GRAPH, FORM_RESIDENT = 0, 1, 2
 MLP_NPARAM, MLP_NNORM = 4609, 12
 FLAG_DCOP, FLAG_INITJCT = 1, 2
 
@@ -49,7 +50,7 @@ EXPORTED = [
     "xg_load_dae_matrices", "xg_lu_analyze", "xg_lu_factor", "xg_lu_solve",
     "xg_lu_solve_noalloc", "xg_lu_set_precision", "xg_lu_info", "xg_lu_schedule_info", "xg_lu_set_schedule", "xg_lu_analyze_pattern",
     "xg_lu_set_tuning", "xg_lu_tuning_info",
-    "xg_transient", "xg_tran_start", "xg_tran_advance", "xg_tran_results", "xg_tran_end",
+    "xg_transient", "xg_tran_set_form", "xg_tran_start", "xg_tran_advance", "xg_tran_results", "xg_tran_end",
     "xg_tran_predictors", "xg_tran_orders", "xg_tran_profile", "xg_tran_predictor_stats", "xg_set_predictor", "xg_mlp_set", "xg_mlp_get",
     "xg_mlp_train", "xg_mlp_grad", "xg_mlp_forward",
     "xg_dcop", "xg_newton_solve", "xg_version",
@@ -91,7 +92,8 @@ class TranStats(C.Structure):
                 ("lte_fail", C.c_longlong), ("dcop_iters", C.c_longlong),
                 ("ticks", C.c_longlong), ("device_evals", C.c_longlong), ("status", C.c_int),
                 ("n_analyze", C.c_int), ("t_final_min", C.c_double),
-                ("t_final_max", C.c_double), ("seconds", C.c_double), ("kernels_per_tick", C.c_int)]
+                ("t_final_max", C.c_double), ("seconds", C.c_double), ("kernels_per_tick", C.c_int),
+                ("form", C.c_int), ("kernel_launches", C.c_longlong), ("circuit_ticks", C.c_longlong)]
 
 
 _lib = None
@@ -150,6 +152,7 @@ def lib() -> C.CDLL:
     L.xg_transient.argtypes = [P, C.POINTER(TranParams), I, ip, I, ip, dp, dp, C.POINTER(TranStats)]
     L.xg_tran_start.argtypes = [P, C.POINTER(TranParams), I, ip, I]
     L.xg_tran_advance.argtypes = [P, I]
+    L.xg_tran_set_form.argtypes = [P, I]
     L.xg_tran_results.argtypes = [P, ip, dp, dp, C.POINTER(TranStats)]
     L.xg_tran_end.argtypes = [P]
     L.xg_dcop.argtypes = [P, dp, C.POINTER(I)]
@@ -344,6 +347,10 @@ class Circuit:
                           tran.nl_reltol, tran.nl_abstol, tran.nl_deltaxtol, tran.nl_rhstol,
                           tran.nl_smallupdatetol, tran.nl_maxstep, tran.max_steps, tran.max_order,
                           tran.method)
+
+    def tran_set_form(self, form: int):
+        """FORM_AUTO, FORM_TICK_GRAPH or FORM_RESIDENT (see xg_tran_set_form)."""
+        self._check(lib().xg_tran_set_form(self.h, int(form)))
 
     def tran_start(self, tran=None, probes=(), cap=0):
         """Operating point + first analysis; keeps the run resident for tran_advance."""

@@ -52,6 +52,13 @@ struct xg_ctx {
   int sF_b = 0, sQ_b = 0, sL_b = 0, sM_b = 0;
   int n_pairs = 0, n_rowblocks = 0, n_long_rows = 0, n_long_ents = 0;
   int n_long_row_blocks = 0, n_long_ent_blocks = 0;
+  // circuit of every MOSFET-1, diode and source, and the long rows / long
+  // Jacobian entries (kept for the circuit-resident tick's per-circuit lists)
+  std::vector<int> m1_circ_h, d_circ_h, src_circ_h, long_rows_h, long_ents_h;
+  int form = XG_FORM_AUTO;          // xg_tran_set_form
+  bool resident_ok = false;         // the current analysis admits the circuit-resident tick
+  FusedDev F;                       // its device lists (allocated with the analysis)
+  int resident_slots[8] = {0};
   DevArrays d;
   LUDev L;
   int sched_order = -1, sched_ftop = -1, sched_stop = -1;  // xg_lu_set_schedule (-1: automatic)
@@ -648,6 +655,11 @@ int xg_finalize(xg_ctx *ctx) {
     int c = circuit_of_nodes(ctx, {ctx->b_d[k], ctx->b_g[k], ctx->b_s[k], ctx->b_b[k]});
     b4circ[k] = c < 0 ? 0 : c;
   }
+  ctx->m1_circ_h = m1circ;
+  ctx->d_circ_h = dcirc;
+  ctx->src_circ_h = scirc;
+  ctx->long_rows_h = long_rows;
+  ctx->long_ents_h = long_ents;
   ctx->inst_of_circ.assign(ctx->ncirc, 0);
   ctx->circ_m1.assign(ctx->ncirc, 0);
   ctx->circ_b4.assign(ctx->ncirc, 0);
@@ -805,6 +817,123 @@ int xg_load_dae_matrices(xg_ctx *ctx, double *dQdx, double *dFdx, int load_type)
 
 // ---------------------------------------------------------------------------
 // LU entry points.
+// Per-circuit lists of the circuit-resident tick (FusedDev) for the
+// analysis H, when the batch admits that form: many small circuits, MOSFET-1
+// and diode devices only, FP64 factors, the polynomial predictor, and an LU
+// without a top (every column in a hub or a dependency-closed group).
+static int resident_build(xg_ctx *ctx, const LUHost &H) {
+  ctx->resident_ok = false;
+  ctx->F = FusedDev();
+  const int n = H.n, ncirc = ctx->ncirc;
+  int max_rows = 0;
+  for (int c = 0; c < ncirc; ++c) max_rows = std::max(max_rows, ctx->offsets[c + 1] - ctx->offsets[c]);
+  if (ncirc < kFusedMinCircuits || max_rows > kFusedMaxRows || ctx->nb > 0 || ctx->lu_prec != XG_PREC_FP64 ||
+      ctx->predictor != XG_PRED_POLY || H.fsched.n_top_items > 0 || H.lsched.n_top_items > 0)
+    return XG_OK;
+  std::vector<int> circ_of_step(n);
+  for (int j = 0; j < n; ++j) circ_of_step[j] = ctx->circ_of_row[H.col_of_step[j]];
+  // levels per circuit: its hubs, then the local levels of its groups merged
+  // (groups are independent of one another; a group depends only on hubs)
+  auto levels = [&](const Schedule &S, std::vector<int> &cl, std::vector<int> &lptr, std::vector<int> &items) {
+    std::vector<std::vector<std::vector<int>>> per(ncirc);
+    for (int t = 0; t < S.n_hub; ++t) {
+      auto &v = per[circ_of_step[S.items[t]]];
+      if (v.empty()) v.resize(1);
+      v[0].push_back(S.items[t]);
+    }
+    for (int g = 0; g < S.n_groups; ++g)
+      for (int lv = S.grp_lvl[g]; lv < S.grp_lvl[g + 1]; ++lv)
+        for (int t = S.lvl_ptr[lv]; t < S.lvl_ptr[lv + 1]; ++t) {
+          auto &v = per[circ_of_step[S.items[t]]];
+          const size_t li = 1 + (size_t)(lv - S.grp_lvl[g]);
+          if (v.size() <= li) v.resize(li + 1);
+          v[li].push_back(S.items[t]);
+        }
+    cl.assign(1, 0);
+    lptr.assign(1, 0);
+    items.clear();
+    for (int c = 0; c < ncirc; ++c) {
+      for (auto &lv : per[c]) {
+        if (lv.empty()) continue;
+        items.insert(items.end(), lv.begin(), lv.end());
+        lptr.push_back((int)items.size());
+      }
+      cl.push_back((int)lptr.size() - 1);
+    }
+    return (int)items.size() == n;
+  };
+  std::vector<int> f_cl, f_lptr, f_items, l_cl, l_lptr, l_items;
+  if (!levels(H.fsched, f_cl, f_lptr, f_items) || !levels(H.lsched, l_cl, l_lptr, l_items)) return XG_OK;
+  // how the grouped kernels compute each column / row (see FusedDev)
+  std::vector<signed char> f_kind(n, 1), l_meth(n, 2), u_meth(n, 2);
+  for (int g = 0; g < H.fsched.n_groups; ++g)
+    for (int t = H.fsched.lvl_ptr[H.fsched.grp_lvl[g]]; t < H.fsched.lvl_ptr[H.fsched.grp_lvl[g + 1]]; ++t) {
+      const int j = H.fsched.items[t];
+      f_kind[j] = H.fsched.is_thread[j] ? 0 : (H.fsched.is_long[j] ? 2 : 1);
+      u_meth[j] = (H.us_gbytes[g] > 0 || H.fsched.is_thread_rev[j]) ? 1 : (H.fsched.is_long_rev[j] ? 3 : 2);
+    }
+  for (int t = 0; t < H.fsched.n_hub; ++t) {
+    f_kind[H.fsched.items[t]] = 2;
+    u_meth[H.fsched.items[t]] = 3;
+  }
+  for (int g = 0; g < H.lsched.n_groups; ++g)
+    for (int t = H.lsched.lvl_ptr[H.lsched.grp_lvl[g]]; t < H.lsched.lvl_ptr[H.lsched.grp_lvl[g + 1]]; ++t) {
+      const int i = H.lsched.items[t];
+      l_meth[i] = (H.ls_gbytes[g] > 0 || H.lsched.is_thread[i]) ? 1 : (H.lsched.is_long[i] ? 3 : 2);
+    }
+  for (int t = 0; t < H.lsched.n_hub; ++t) l_meth[H.lsched.items[t]] = 0;
+  // instances, sources, long rows and long entries of each circuit
+  auto bucket = [&](const std::vector<int> &circ_of, std::vector<int> &ptr, std::vector<int> &list) {
+    ptr.assign(ncirc + 1, 0);
+    for (int c : circ_of) ptr[c + 1]++;
+    for (int c = 0; c < ncirc; ++c) ptr[c + 1] += ptr[c];
+    list.assign(circ_of.size(), 0);
+    std::vector<int> f(ptr.begin(), ptr.end() - 1);
+    for (size_t k = 0; k < circ_of.size(); ++k) list[f[circ_of[k]]++] = (int)k;
+  };
+  std::vector<int> m1_ptr, m1_list, d_ptr, d_list, src_ptr, src_list, lr_ptr, lr_list, le_ptr, le_list;
+  bucket(ctx->m1_circ_h, m1_ptr, m1_list);
+  bucket(ctx->d_circ_h, d_ptr, d_list);
+  bucket(ctx->src_circ_h, src_ptr, src_list);
+  std::vector<int> lr_circ, le_circ;
+  for (int r : ctx->long_rows_h) lr_circ.push_back(ctx->circ_of_row[r]);
+  for (int e : ctx->long_ents_h) {
+    const int r = (int)(std::upper_bound(ctx->rp.begin(), ctx->rp.end(), e) - ctx->rp.begin()) - 1;
+    le_circ.push_back(ctx->circ_of_row[r]);
+  }
+  bucket(lr_circ, lr_ptr, lr_list);
+  bucket(le_circ, le_ptr, le_list);
+  // largest circuits first: the queue then balances the CTAs
+  std::vector<int> order(ncirc);
+  for (int c = 0; c < ncirc; ++c) order[c] = c;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    const long long wa = ctx->offsets[a + 1] - ctx->offsets[a] + ctx->inst_of_circ[a];
+    const long long wb = ctx->offsets[b + 1] - ctx->offsets[b] + ctx->inst_of_circ[b];
+    return wa > wb;
+  });
+  FusedDev F;
+  auto &A = ctx->lu_allocs;
+  int rc = 0;
+#define UP(ptr, vec) if ((rc = dev_upload(ctx, &ptr, vec, A))) return rc
+  UP(F.order, order);
+  UP(F.m1_ptr, m1_ptr); UP(F.m1_list, m1_list); UP(F.d_ptr, d_ptr); UP(F.d_list, d_list);
+  UP(F.src_ptr, src_ptr); UP(F.src_list, src_list);
+  UP(F.lr_ptr, lr_ptr); UP(F.lr_list, lr_list); UP(F.le_ptr, le_ptr); UP(F.le_list, le_list);
+  UP(F.f_cl, f_cl); UP(F.f_lptr, f_lptr); UP(F.f_items, f_items);
+  UP(F.l_cl, l_cl); UP(F.l_lptr, l_lptr); UP(F.l_items, l_items);
+  UP(F.f_kind, f_kind); UP(F.l_meth, l_meth); UP(F.u_meth, u_meth);
+#undef UP
+  if ((rc = dev_alloc(ctx, &F.queue, 1, A))) return rc;
+  if ((rc = dev_alloc(ctx, &F.ticks, 2, A))) return rc;
+  F.max_rows = max_rows;
+  if (resident_prepare_k(max_rows, ctx->device, &F.grid) != XG_OK) return fail(ctx, XG_ERR_CUDA, "resident tick set-up");
+  ctx->F = F;
+  const int slots[8] = {ctx->sF_m, ctx->sQ_m, ctx->sL_m, ctx->sM_m, ctx->sF_d, ctx->sQ_d, ctx->sL_d, ctx->sM_d};
+  std::copy(slots, slots + 8, ctx->resident_slots);
+  ctx->resident_ok = true;
+  return XG_OK;
+}
+
 static int lu_upload(xg_ctx *ctx, const LUHost &H) {
   CK(cudaStreamSynchronize(ctx->stream));
   free_list(ctx->lu_allocs);
@@ -956,6 +1085,7 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
   L.f_levels = (int)H.f_lvl_ptr.size() - 1;
   L.l_levels = (int)H.l_lvl_ptr.size() - 1;
   L.u_levels = (int)H.u_lvl_ptr.size() - 1;
+  if ((rc = resident_build(ctx, H))) return rc;
   CK(cudaMemsetAsync(ctx->breakdown_dev, 0, sizeof(int), ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->lu_ready = true;
@@ -1310,6 +1440,10 @@ struct TranRun {
   long long ticks = 0;
   int kernels_per_tick = 0;  // kernel nodes of the captured tick graph
   int batch = 4;
+  bool resident = false;          // advance with the circuit-resident tick (else the tick graph)
+  long long circuit_ticks = 0;    // Newton iterations run by the resident tick, summed over circuits
+  long long kernel_launches = 0;  // kernels launched while advancing
+  unsigned long long tick_count[2] = {0, 0};
   std::chrono::steady_clock::time_point t0;
   ~TranRun() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -1430,6 +1564,7 @@ int run_until_idle(TranRun &R) {
       launch_back(R);
       launch_count_done_k(ctx->stream, d, ctx->ncirc, ctx->breakdown_dev, ctx->status_dev);
       CK(cudaGetLastError());
+      R.kernel_launches += R.kernels_per_tick;
       continue;
     }
     if (consecutive && R.pivot_tol == 0.0) {
@@ -1437,10 +1572,28 @@ int run_until_idle(TranRun &R) {
       if ((rc = capture(R))) return rc;
     }
     consecutive = 0;
+    if (R.tick_count[0]) {
+      // the last resident launch: its longest circuit's ticks, and all of them
+      R.ticks += (long long)R.tick_count[0];
+      R.circuit_ticks += (long long)R.tick_count[1];
+      R.tick_count[0] = R.tick_count[1] = 0;
+    }
     if (finished >= ctx->ncirc) return XG_OK;
     if (R.ticks > max_ticks) return fail(ctx, XG_ERR_TIMEOUT, "transient exceeded the tick limit");
+    if (R.resident && ctx->resident_ok) {
+      // every circuit runs its ticks in one CTA until it pauses, finishes,
+      // fails or parks on a pivot breakdown
+      launch_resident_k(ctx->stream, d, ctx->L, ctx->F, ctx->ncirc, ctx->nm, ctx->nd, ctx->nv, ctx->sto_base_m,
+                        ctx->resident_slots, R.bps, R.bp_ptr, R.cap, R.pmax, R.pivot_tol);
+      launch_count_done_k(ctx->stream, d, ctx->ncirc, ctx->breakdown_dev, ctx->status_dev);
+      CK(cudaGetLastError());
+      CK(cudaMemcpyAsync(R.tick_count, ctx->F.ticks, sizeof R.tick_count, cudaMemcpyDeviceToHost, ctx->stream));
+      R.kernel_launches += 2;
+      continue;
+    }
     for (int k = 0; k < R.batch; ++k) CK(cudaGraphLaunch(R.exec, ctx->stream));
     R.ticks += R.batch;
+    R.kernel_launches += (long long)R.batch * R.kernels_per_tick;
     if (R.batch < 64) R.batch *= 2;
   }
 }
@@ -1570,11 +1723,25 @@ static int tran_start_run(xg_ctx *ctx, const xg_tran_params *p, const std::vecto
   launch_front(R);
   CK(cudaGetLastError());
   if ((rc = lu_analyze_from_device(ctx, d.J))) return rc;
+  if (ctx->form == XG_FORM_RESIDENT && !ctx->resident_ok)
+    return fail(ctx, XG_ERR_UNSUPPORTED,
+                "circuit-resident tick: needs >= 64 circuits of <= 2048 unknowns, MOSFET-1 / diode devices, "
+                "FP64 factors, the polynomial predictor and an LU without a top");
+  R.resident = ctx->resident_ok && ctx->form != XG_FORM_TICK_GRAPH;
   if ((rc = capture(R))) return rc;
   launch_back(R);
   launch_count_done_k(ctx->stream, d, ncirc, ctx->breakdown_dev, ctx->status_dev);
   CK(cudaGetLastError());
   return run_until_idle(R);
+}
+
+extern "C" int xg_tran_set_form(xg_ctx *ctx, int form) {
+  if (!ctx) return XG_ERR_ARG;
+  if (form != XG_FORM_AUTO && form != XG_FORM_TICK_GRAPH && form != XG_FORM_RESIDENT)
+    return fail(ctx, XG_ERR_ARG, "form must be XG_FORM_AUTO, XG_FORM_TICK_GRAPH or XG_FORM_RESIDENT");
+  if (ctx->run) return fail(ctx, XG_ERR_STATE, "the form cannot change during a transient");
+  ctx->form = form;
+  return XG_OK;
 }
 
 extern "C" int xg_tran_advance(xg_ctx *ctx, int n_steps) {
@@ -1628,6 +1795,9 @@ extern "C" int xg_tran_results(xg_ctx *ctx, int *counts, double *times, double *
     }
     stats->ticks = R.ticks;
     stats->kernels_per_tick = R.kernels_per_tick;
+    stats->form = R.resident ? XG_FORM_RESIDENT : XG_FORM_TICK_GRAPH;
+    stats->kernel_launches = R.kernel_launches;
+    stats->circuit_ticks = R.circuit_ticks;
     stats->device_evals = evals;
     stats->n_analyze = ctx->n_analyze;
     stats->status = status;

@@ -411,6 +411,10 @@ void launch_count_done_k(cudaStream_t st, const DevArrays &d, int ncirc, const i
                          int *status_out);
 void launch_unstall_k(cudaStream_t st, const DevArrays &d, int ncirc);
 void launch_newton_weights_k(cudaStream_t st, const DevArrays &d, int n);
+int resident_prepare_k(int max_rows, int device, int *grid);
+void launch_resident_k(cudaStream_t st, const DevArrays &d, const LUDev &L, const FusedDev &F, int ncirc, int nm,
+                       int nd, int nv, int sto_base_m, const int *slots, const double *bps, const int *bp_ptr,
+                       int cap, int pmax, double pivot_tol);
 void launch_set_target_k(cudaStream_t st, const DevArrays &d, int ncirc, int n_steps);
 int lu_prepare_k();  // shared-memory opt-in of the staged group factorization
 void launch_lu_factor_k(cudaStream_t st, const LUDev &L, const double *vals, CircState *cs, int masked,

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include "xg_internal.h"
+#include "xg_lu_dev.cuh"
 #include "xg_models.cuh"
 
 namespace xg {
@@ -1291,8 +1292,269 @@ __global__ void k_unstall(DevArrays d, int ncirc) {
 }
 
 // ---------------------------------------------------------------------------
+// Circuit-resident tick (see FusedDev): one CTA per circuit runs every stage
+// of a tick — the same per-item device functions as the kernels above, each
+// item computed the way those kernels compute it — and loops over ticks
+// until its circuit stops being active.  No stage waits on another CTA.
+
+// The per-(row block, circuit) partial max / sum slots of circuit c, as
+// block_partials computes them: a warp per slot, rows strided by 32 from the
+// slot's first row, butterfly.
+__device__ void circuit_partials(const DevArrays &d, int c, int o0, int o1, const double *vm, const double *vs) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  const int b0 = o0 / kRowBlock, b1 = (o1 - 1) / kRowBlock;
+  for (int b = b0 + warp; b <= b1; b += nwarps) {
+    const int lo = max(o0, b * kRowBlock), hi = min(o1, (b + 1) * kRowBlock);
+    double m = 0.0, s = 0.0;
+    for (int r = lo + lane; r < hi; r += 32) {
+      m = fmax(m, vm[r - o0]);
+      s += vs[r - o0];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+      s += __shfl_xor_sync(0xffffffffu, s, o);
+    }
+    if (lane == 0) {
+      const int slot = d.pair_base[b] + (c - d.blk_cfirst[b]);
+      d.pmax[slot] = m;
+      d.psum[slot] = s;
+    }
+  }
+}
+
+// Arguments of the resident tick that the separate launches take one by one.
+struct FusedArgs {
+  int ncirc, nm, nd, nv, sto_base_m;
+  int sF_m, sQ_m, sL_m, sM_m, sF_d, sQ_d, sL_d, sM_d;
+  const double *bps;
+  const int *bp_ptr;
+  int cap, pmax;
+  double pivot_tol;
+};
+
+// The factorization of circuit c, level by level: single-thread columns,
+// warp columns, then the columns that take the whole CTA.
+__device__ void resident_factor(const DevArrays &d, const LUDev &L, const FusedDev &F, int c, double pivot_tol,
+                                double *sm) {
+  const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, nwarps = nth >> 5;
+  for (int lv = F.f_cl[c]; lv < F.f_cl[c + 1]; ++lv) {
+    const int a = F.f_lptr[lv], b = F.f_lptr[lv + 1];
+    for (int t = a + tid; t < b; t += nth) {
+      const int j = F.f_items[t];
+      if (F.f_kind[j] == 0 && item_active(L, d.cs, 1, j)) factor_column_t<double>(L, d.J, j, d.cs, 1, pivot_tol, nullptr);
+    }
+    for (int t = a + warp; t < b; t += nwarps) {
+      const int j = F.f_items[t];
+      if (F.f_kind[j] == 1 && item_active(L, d.cs, 1, j)) factor_column<false, double>(L, d.J, j, d.cs, 1, pivot_tol, sm);
+    }
+    // the thread and warp columns are done, and a breakdown they flagged is
+    // visible to every thread: the tests below read the same values in all
+    __syncthreads();
+    for (int t = a; t < b; ++t) {
+      const int j = F.f_items[t];
+      if (F.f_kind[j] != 2 || !item_active(L, d.cs, 1, j)) continue;
+      factor_column<true, double>(L, d.J, j, d.cs, 1, pivot_tol, sm);
+      __syncthreads();
+    }
+  }
+}
+
+// The L solve (forward) and the U solve (backward) of circuit c; every row
+// is summed the way the grouped kernels sum it (F.l_meth / F.u_meth).
+__device__ void resident_solve(const DevArrays &d, const LUDev &L, const FusedDev &F, int c, double *sm) {
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int team = tid >> 3, nteams = nth >> 3, sub = tid & 7;
+  const double *lu = L.lu;
+  const double *b = d.rhs;
+  double *x = d.dx;
+  for (int lv = F.l_cl[c]; lv < F.l_cl[c + 1]; ++lv) {
+    const int a = F.l_lptr[lv], e = F.l_lptr[lv + 1];
+    for (int t = a + tid; t < e; t += nth) {
+      const int i = F.l_items[t];
+      const int m = F.l_meth[i];
+      if (m == 0) {
+        L.y[i] = b[L.row_of_step[i]];
+      } else if (m == 1) {
+        double sum = 0.0;
+        for (int q = L.l_ptr[i]; q < L.l_ptr[i + 1]; ++q) sum += (double)lu[L.l_pos[q]] * L.y[L.l_col[q]];
+        L.y[i] = b[L.row_of_step[i]] - sum;
+      }
+    }
+    for (int t0 = a; t0 < e; t0 += nteams) {  // warp-uniform bound
+      const int t = t0 + team;
+      const int i = t < e ? F.l_items[t] : 0;
+      const bool act = t < e && F.l_meth[i] == 2;
+      if (__any_sync(0xffffffffu, act)) {
+        double sum = 0.0;
+        if (act)
+          for (int q = L.l_ptr[i] + sub; q < L.l_ptr[i + 1]; q += 8) sum += (double)lu[L.l_pos[q]] * L.y[L.l_col[q]];
+        for (int o = 4; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, 8);
+        if (act && sub == 0) L.y[i] = b[L.row_of_step[i]] - sum;
+      }
+    }
+    for (int t = a; t < e; ++t) {
+      const int i = F.l_items[t];
+      if (F.l_meth[i] != 3) continue;  // uniform
+      const double sum = long_row_dot<double>(lu, L.l_pos, L.l_col, L.y, L.l_ptr[i], L.l_ptr[i + 1], sm);
+      if (tid == 0) L.y[i] = b[L.row_of_step[i]] - sum;
+    }
+    __syncthreads();
+  }
+  for (int lv = F.f_cl[c + 1] - 1; lv >= F.f_cl[c]; --lv) {
+    const int a = F.f_lptr[lv], e = F.f_lptr[lv + 1];
+    for (int t = a + tid; t < e; t += nth) {
+      const int k = F.f_items[t];
+      if (F.u_meth[k] != 1) continue;
+      double sum = 0.0;
+      for (int q = L.u_ptr[k]; q < L.u_ptr[k + 1]; ++q) sum += (double)lu[L.u_pos[q]] * L.y[L.u_col[q]];
+      const double z = (L.y[k] - sum) / (double)lu[L.diag[k]];
+      L.y[k] = z;
+      x[L.col_of_step[k]] = z;
+    }
+    for (int t0 = a; t0 < e; t0 += nteams) {
+      const int t = t0 + team;
+      const int k = t < e ? F.f_items[t] : 0;
+      const bool act = t < e && F.u_meth[k] == 2;
+      if (__any_sync(0xffffffffu, act)) {
+        double sum = 0.0;
+        if (act)
+          for (int q = L.u_ptr[k] + sub; q < L.u_ptr[k + 1]; q += 8) sum += (double)lu[L.u_pos[q]] * L.y[L.u_col[q]];
+        for (int o = 4; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, 8);
+        if (act && sub == 0) {
+          const double z = (L.y[k] - sum) / (double)lu[L.diag[k]];
+          L.y[k] = z;
+          x[L.col_of_step[k]] = z;
+        }
+      }
+    }
+    for (int t = a; t < e; ++t) {
+      const int k = F.f_items[t];
+      if (F.u_meth[k] != 3) continue;  // uniform
+      const double sum = long_row_dot<double>(lu, L.u_pos, L.u_col, L.y, L.u_ptr[k], L.u_ptr[k + 1], sm);
+      if (tid == 0) {
+        const double z = (L.y[k] - sum) / (double)lu[L.diag[k]];
+        L.y[k] = z;
+        x[L.col_of_step[k]] = z;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Ticks of circuit c until it stops being active (paused, done, failed, or
+// parked on a pivot breakdown for the host).
+__device__ void resident_circuit(const DevArrays &d, const LUDev &L, const FusedDev &F, const FusedArgs &A, int c,
+                                 double *vm, double *vs, double *ws, double *sm) {
+  const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
+  const int o0 = d.offsets[c], o1 = d.offsets[c + 1];
+  const int e0 = d.rp[o0], e1 = d.rp[o1];
+  const CircState &s = d.cs[c];
+  int ticks = 0;
+  for (; ticks < kFusedMaxTicks; ++ticks) {
+    __syncthreads();
+    const int ph = s.phase;
+    if (!(ph == PH_DC || ph == PH_TRAN)) break;  // uniform: read after the barrier
+    for (int k = F.src_ptr[c] + tid; k < F.src_ptr[c + 1]; k += nth) source_value(d, F.src_list[k], A.nv, 0, 0.0);
+    __syncthreads();
+    for (int k = F.m1_ptr[c] + tid; k < F.m1_ptr[c + 1]; k += nth)
+      mos1_eval(d, F.m1_list[k], A.nm, A.sto_base_m, 1, 1, 0, 0, A.sF_m, A.sQ_m, A.sL_m, A.sM_m);
+    for (int k = F.d_ptr[c] + tid; k < F.d_ptr[c + 1]; k += nth)
+      diode_eval(d, F.d_list[k], A.nd, 1, 1, 0, 0, A.sF_d, A.sQ_d, A.sL_d, A.sM_d);
+    __syncthreads();
+    for (int q = F.lr_ptr[c]; q < F.lr_ptr[c + 1]; ++q) {
+      const int lr = F.lr_list[q];
+      for (int part = 0; part < d.lrow_ptr[lr + 1] - d.lrow_ptr[lr]; ++part) long_row_part(d, lr, part, ws);
+    }
+    for (int q = F.le_ptr[c]; q < F.le_ptr[c + 1]; ++q) {
+      const int le = F.le_list[q];
+      for (int part = 0; part < d.lent_ptr[le + 1] - d.lent_ptr[le]; ++part) long_entry_part(d, le, part, ws);
+    }
+    __syncthreads();
+    for (int r = o0 + tid; r < o1; r += nth) {
+      double a, b;
+      assemble_row(d, r, a, b);
+      vm[r - o0] = a;
+      vs[r - o0] = b;
+    }
+    for (int e = e0 + tid; e < e1; e += nth) assemble_entry(d, e);
+    __syncthreads();
+    circuit_partials(d, c, o0, o1, vm, vs);
+    __syncthreads();
+    if (warp == 0) newton_ctl_circuit(d, c, lane);
+    __syncthreads();
+    if (s.need_solve && !s.singular) {  // uniform
+      resident_factor(d, L, F, c, A.pivot_tol, sm);
+      if (!s.singular) resident_solve(d, L, F, c, sm);  // uniform: read after the factor's last barrier
+    }
+    __syncthreads();
+    for (int r = o0 + tid; r < o1; r += nth) {
+      double a, b;
+      update_row(d, r, a, b);
+      vm[r - o0] = a;
+      vs[r - o0] = b;
+    }
+    __syncthreads();
+    circuit_partials(d, c, o0, o1, vm, vs);
+    __syncthreads();
+    if (warp == 0) step_ctl_circuit(d, c, lane, A.bps, A.bp_ptr, A.cap);
+    __syncthreads();
+    for (int r = o0 + tid; r < o1; r += nth) history_row(d, r, A.cap, A.pmax);
+    for (int k = F.m1_ptr[c] + tid; k < F.m1_ptr[c + 1]; k += nth)
+      commit_instance(d, F.m1_list[k], A.nm, A.nd, A.sto_base_m, 0, 0, 0);
+    for (int k = F.d_ptr[c] + tid; k < F.d_ptr[c + 1]; k += nth)
+      commit_instance(d, A.nm + F.d_list[k], A.nm, A.nd, A.sto_base_m, 0, 0, 0);
+  }
+  if (tid == 0 && ticks > 0) {
+    atomicMax(F.ticks, (unsigned long long)ticks);
+    atomicAdd(F.ticks + 1, (unsigned long long)ticks);
+  }
+}
+
+// CTAs take circuits from the queue (F.order: largest first) until it is empty.
+__global__ void __launch_bounds__(kFusedThreads, 4) k_resident(DevArrays d, LUDev L, FusedDev F, FusedArgs A) {
+  extern __shared__ __align__(16) double fz_rows[];
+  __shared__ double ws[8 * 4], sm[32];
+  __shared__ int next;
+  double *vm = fz_rows, *vs = fz_rows + F.max_rows;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) next = atomicAdd(F.queue, 1);
+    __syncthreads();
+    const int q = next;
+    if (q >= A.ncirc) return;
+    resident_circuit(d, L, F, A, F.order[q], vm, vs, ws, sm);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Launchers.
 static inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
+
+int resident_prepare_k(int max_rows, int device, int *grid) {
+  const size_t smem = 2 * sizeof(double) * (size_t)max_rows;
+  if (cudaFuncSetAttribute(k_resident, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return XG_ERR_CUDA;
+  int per_sm = 0, sms = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resident, kFusedThreads, smem) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || per_sm < 1)
+    return XG_ERR_CUDA;
+  *grid = per_sm * sms;
+  return XG_OK;
+}
+
+void launch_resident_k(cudaStream_t st, const DevArrays &d, const LUDev &L, const FusedDev &F, int ncirc, int nm,
+                       int nd, int nv, int sto_base_m, const int *slots, const double *bps, const int *bp_ptr,
+                       int cap, int pmax, double pivot_tol) {
+  FusedArgs A;
+  A.ncirc = ncirc; A.nm = nm; A.nd = nd; A.nv = nv; A.sto_base_m = sto_base_m;
+  A.sF_m = slots[0]; A.sQ_m = slots[1]; A.sL_m = slots[2]; A.sM_m = slots[3];
+  A.sF_d = slots[4]; A.sQ_d = slots[5]; A.sL_d = slots[6]; A.sM_d = slots[7];
+  A.bps = bps; A.bp_ptr = bp_ptr; A.cap = cap; A.pmax = pmax; A.pivot_tol = pivot_tol;
+  cudaMemsetAsync(F.queue, 0, sizeof(int), st);
+  cudaMemsetAsync(F.ticks, 0, 2 * sizeof(unsigned long long), st);
+  const size_t smem = 2 * sizeof(double) * (size_t)F.max_rows;
+  k_resident<<<std::min(F.grid, ncirc), kFusedThreads, smem, st>>>(d, L, F, A);
+}
 
 void launch_sources_k(cudaStream_t st, const DevArrays &d, int n_v, int n_src, int use_explicit,
                       double t) {
