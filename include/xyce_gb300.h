@@ -247,6 +247,16 @@ int xg_lu_schedule_info(xg_ctx *ctx, int *ordering, int *factor_top, int *solve_
  * from the next analysis; not allowed while a transient is in progress. */
 int xg_lu_set_schedule(xg_ctx *ctx, int ordering, int factor_top, int solve_top);
 
+/* Factor reuse in the transient.  on = 1 (default): a circuit without
+ * nonlinear devices whose Jacobian coefficients (OneStep's qscale / fscale,
+ * the operating point's gmin shunt) equal those of its last factorization
+ * under the same analysis has the same Jacobian bit for bit; it skips the
+ * refactorization and solves with the factors it has — the results are
+ * identical.  The reference's IRSolver (N_LAS_IRSolver.C:428-560) reuses
+ * stale factors with iterative refinement instead; this reuse is exact.
+ * Not allowed while a transient is in progress. */
+int xg_lu_set_reuse(xg_ctx *ctx, int on);
+
 /* Launch shapes of the LU sweeps.  XG_TUNE_TIMED (default): after each
  * analysis, candidate shapes — the factorization with and without its
  * update metadata staged in shared memory, at 64..512 threads per CTA; the
@@ -310,6 +320,7 @@ typedef struct xg_tran_stats {
   int form;                                    /* XG_FORM_TICK_GRAPH or XG_FORM_RESIDENT: how it advanced */
   long long kernel_launches;                   /* kernels launched while advancing */
   long long circuit_ticks;                     /* resident form: Newton iterations summed over circuits */
+  long long factor_skips;                      /* refactorizations skipped (xg_lu_set_reuse) */
 } xg_tran_stats;
 
 /* How a transient advances.  XG_FORM_TICK_GRAPH: a tick (one Newton

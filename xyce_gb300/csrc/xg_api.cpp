@@ -66,6 +66,8 @@ struct xg_ctx {
   int n_analyze = 0;
   int lu_prec = XG_PREC_FP64, lu_refine = 2;  // xg_lu_set_precision
   int tune_mode = XG_TUNE_TIMED;               // xg_lu_set_tuning
+  int lu_reuse = 1;                            // xg_lu_set_reuse
+  int lu_gen = 0;                              // analyses uploaded so far
   xg_lu_tuning tuning{};                       // what the tuner chose for the current analysis
   int predictor = XG_PRED_POLY;                // xg_set_predictor
   std::vector<int> h_tlv_item_ptr, h_tlv_grp_ptr;  // host copies for the per-level top launches
@@ -732,6 +734,12 @@ int xg_finalize(xg_ctx *ctx) {
   AL(d.pmax, pairs); AL(d.psum, pairs);
   AL(d.probe_idx, n);
   AL(ctx->breakdown_dev, 1);
+  AL(d.lu_gen, 1);
+  {
+    std::vector<char> lin(ctx->ncirc);
+    for (int c = 0; c < ctx->ncirc; ++c) lin[c] = ctx->inst_of_circ[c] == 0 ? 1 : 0;
+    UP(d.circ_linear, lin);
+  }
   d.status = ctx->status_dev;
 #undef UP
 #undef AL
@@ -1086,6 +1094,9 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
   L.l_levels = (int)H.l_lvl_ptr.size() - 1;
   L.u_levels = (int)H.u_lvl_ptr.size() - 1;
   if ((rc = resident_build(ctx, H))) return rc;
+  // a new analysis: every circuit refactors before it may reuse factors again
+  ctx->lu_gen++;
+  CK(cudaMemcpyAsync(ctx->d.lu_gen, &ctx->lu_gen, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemsetAsync(ctx->breakdown_dev, 0, sizeof(int), ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->lu_ready = true;
@@ -1346,6 +1357,14 @@ int xg_lu_set_precision(xg_ctx *ctx, int precision, int n_refine) {
   ctx->lu_prec = precision;
   ctx->lu_refine = n_refine;
   ctx->lu_ready = false;  // the next xg_lu_analyze (or transient) builds factors of this precision
+  return XG_OK;
+}
+
+int xg_lu_set_reuse(xg_ctx *ctx, int on) {
+  if (!ctx) return XG_ERR_ARG;
+  if (on != 0 && on != 1) return fail(ctx, XG_ERR_ARG, "reuse must be 0 or 1");
+  if (ctx->run) return fail(ctx, XG_ERR_STATE, "factor reuse cannot change during a transient");
+  ctx->lu_reuse = on;
   return XG_OK;
 }
 
@@ -1693,6 +1712,7 @@ static int tran_start_run(xg_ctx *ctx, const xg_tran_params *p, const std::vecto
   tp.nl_rhstol = p->nl_rhstol; tp.nl_smallupdatetol = p->nl_smallupdatetol; tp.nl_maxstep = p->nl_maxstep;
   tp.max_steps = p->max_steps; tp.max_order = p->max_order > 0 ? p->max_order : 2;
   tp.gear = (p->method == XG_METHOD_GEAR) ? 1 : 0;
+  tp.reuse_factors = ctx->lu_reuse;
   tp.bptol = 1e-15 * (p->tstop - p->tstart);
   tp.dc_reltol = 1e-3; tp.dc_abstol = 1e-12; tp.dc_deltaxtol = 1.0; tp.dc_rhstol = 1e-6; tp.dc_maxstep = 200;
   tp.dc_only = (p->max_steps < 0) ? 1 : 0;
@@ -1706,6 +1726,8 @@ static int tran_start_run(xg_ctx *ctx, const xg_tran_params *p, const std::vecto
     s.qscale = 0.0; s.fscale = 1.0; s.hscale = 0.0;
     s.init_jct = 1;
     s.order = 1;
+    s.refactor = 1;
+    s.f_gen = -1;
     s.stop_at = 0;  // pause once the operating point is done
   }
   CK(cudaMemcpyAsync(d.cs, cs.data(), sizeof(CircState) * ncirc, cudaMemcpyHostToDevice, ctx->stream));
@@ -1786,6 +1808,7 @@ extern "C" int xg_tran_results(xg_ctx *ctx, int *counts, double *times, double *
       stats->newton_fail += s.newton_fail;
       stats->lte_fail += s.lte_fail;
       stats->dcop_iters += s.dcop_iters;
+      stats->factor_skips += s.factor_skips;
       stats->t_final_min = std::min(stats->t_final_min, s.t);
       stats->t_final_max = std::max(stats->t_final_max, s.t);
       // instance evaluations: one device pass per Newton solve, plus the
@@ -2008,6 +2031,8 @@ extern "C" int xg_newton_solve(xg_ctx *ctx, const xg_newton_params *p, double ti
     s.qscale = qscale; s.fscale = fscale; s.hscale = hscale;
     s.init_jct = (flags & XG_FLAG_INITJCT) ? 1 : 0;
     s.order = 1;
+    s.refactor = 1;
+    s.f_gen = -1;
     s.errwt = 1.0;
     s.stop_at = 0x7fffffffffffffffLL;
   }

@@ -53,6 +53,13 @@ struct CircState {
   int ml_use, ml_pending, ml_backoff, last_iters, ml_steps, plain_steps;
   double plain_ema;
   long long ml_iters, plain_iters;
+  // factor reuse: a circuit without nonlinear devices whose Jacobian
+  // coefficients equal those of its last factorization (same analysis) has
+  // the same Jacobian bit for bit and skips the refactorization
+  int refactor;        // this tick's LU work factors (else only solves)
+  int f_gen;           // analysis generation of the last factorization
+  double f_qscale, f_fscale, f_gshunt;
+  long long factor_skips;
   // counters
   long long accepted, rejected, newton_iters, newton_fail, lte_fail, dcop_iters;
   long long stop_at;   // pause once this many steps are accepted
@@ -70,6 +77,7 @@ struct TranParams {
   int dc_maxstep;
   int dc_only;  // stop every circuit once its operating point converges
   int newton_only;  // one Newton solve per circuit, then stop (xg_newton_solve)
+  int reuse_factors;  // skip bit-identical refactorizations (xg_lu_set_reuse)
 };
 
 // MOSFET level-1 model-level (effective model) parameters after temperature
@@ -171,6 +179,8 @@ struct DevArrays {
   double *out_t = nullptr, *out_v = nullptr;
   signed char *out_o = nullptr;  // integration order of each recorded point (0: operating point)
   int *status = nullptr;      // mapped host memory: [0] finished circuits, [1] LU breakdown
+  int *lu_gen = nullptr;      // generation of the current LU analysis (bumped by every analysis)
+  char *circ_linear = nullptr;  // per circuit: no nonlinear devices (its Jacobian is the linear part)
 };
 
 // Grouped execution schedule of one triangular sweep (factorization, L solve;

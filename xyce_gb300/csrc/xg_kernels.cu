@@ -835,6 +835,21 @@ __device__ __forceinline__ void newton_ctl_circuit(const DevArrays &d, int c, in
   } else {
     s.need_solve = 1;
     s.singular = 0;
+    // the Jacobian of a circuit without nonlinear devices is qscale C +
+    // fscale G (+ gshunt): the same coefficients under the same analysis
+    // give the same matrix bit for bit, and its factors are still in place
+    const int gen = *d.lu_gen;
+    const bool same = p.reuse_factors && d.circ_linear[c] && s.f_gen == gen && s.f_qscale == s.qscale &&
+                      s.f_fscale == s.fscale && s.f_gshunt == s.gshunt;
+    s.refactor = same ? 0 : 1;
+    if (same) {
+      s.factor_skips++;
+    } else {
+      s.f_gen = gen;
+      s.f_qscale = s.qscale;
+      s.f_fscale = s.fscale;
+      s.f_gshunt = s.gshunt;
+    }
   }
 }
 
@@ -1341,18 +1356,18 @@ __device__ void resident_factor(const DevArrays &d, const LUDev &L, const FusedD
     const int a = F.f_lptr[lv], b = F.f_lptr[lv + 1];
     for (int t = a + tid; t < b; t += nth) {
       const int j = F.f_items[t];
-      if (F.f_kind[j] == 0 && item_active(L, d.cs, 1, j)) factor_column_t<double>(L, d.J, j, d.cs, 1, pivot_tol, nullptr);
+      if (F.f_kind[j] == 0 && factor_active(L, d.cs, 1, j)) factor_column_t<double>(L, d.J, j, d.cs, 1, pivot_tol, nullptr);
     }
     for (int t = a + warp; t < b; t += nwarps) {
       const int j = F.f_items[t];
-      if (F.f_kind[j] == 1 && item_active(L, d.cs, 1, j)) factor_column<false, double>(L, d.J, j, d.cs, 1, pivot_tol, sm);
+      if (F.f_kind[j] == 1 && factor_active(L, d.cs, 1, j)) factor_column<false, double>(L, d.J, j, d.cs, 1, pivot_tol, sm);
     }
     // the thread and warp columns are done, and a breakdown they flagged is
     // visible to every thread: the tests below read the same values in all
     __syncthreads();
     for (int t = a; t < b; ++t) {
       const int j = F.f_items[t];
-      if (F.f_kind[j] != 2 || !item_active(L, d.cs, 1, j)) continue;
+      if (F.f_kind[j] != 2 || !factor_active(L, d.cs, 1, j)) continue;
       factor_column<true, double>(L, d.J, j, d.cs, 1, pivot_tol, sm);
       __syncthreads();
     }
@@ -1483,7 +1498,7 @@ __device__ void resident_circuit(const DevArrays &d, const LUDev &L, const Fused
     if (warp == 0) newton_ctl_circuit(d, c, lane);
     __syncthreads();
     if (s.need_solve && !s.singular) {  // uniform
-      resident_factor(d, L, F, c, A.pivot_tol, sm);
+      if (s.refactor) resident_factor(d, L, F, c, A.pivot_tol, sm);
       if (!s.singular) resident_solve(d, L, F, c, sm);  // uniform: read after the factor's last barrier
     }
     __syncthreads();

@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(256) k_factor_hubs(LUDev L, const double *__re
                                                      int masked, double pivot_tol) {
   __shared__ double sm[32];
   const int j = L.fs.items[blockIdx.x];
-  if (!item_active(L, cs, masked, j)) return;
+  if (!factor_active(L, cs, masked, j)) return;
   factor_column<true, T>(L, vals, j, cs, masked, pivot_tol, sm);
 }
 
@@ -64,19 +64,19 @@ __device__ void factor_group(const LUDev &L, const double *__restrict__ vals, Ci
     bool any_long = false;
     for (int t = b + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
       const int j = S.items[t];
-      if (S.is_thread[j] && item_active(L, cs, masked, j))
+      if (S.is_thread[j] && factor_active(L, cs, masked, j))
         factor_column_t<T>(L, vals, j, cs, masked, pivot_tol, nullptr);
     }
     for (int t = b + warp; t < e; t += nwarps) {
       const int j = S.items[t];
       if (S.is_long[j]) { any_long = true; continue; }
       if (S.is_thread[j]) continue;
-      if (item_active(L, cs, masked, j)) factor_column<false, T>(L, vals, j, cs, masked, pivot_tol, sm);
+      if (factor_active(L, cs, masked, j)) factor_column<false, T>(L, vals, j, cs, masked, pivot_tol, sm);
     }
     if (__syncthreads_or(any_long)) {
       for (int t = b; t < e; ++t) {
         const int j = S.items[t];
-        if (!S.is_long[j] || !item_active(L, cs, masked, j)) continue;
+        if (!S.is_long[j] || !factor_active(L, cs, masked, j)) continue;
         factor_column<true, T>(L, vals, j, cs, masked, pivot_tol, sm);
         __syncthreads();
       }
@@ -88,7 +88,7 @@ template <typename T>
 __global__ void __launch_bounds__(1024) k_factor_groups(LUDev L, const double *__restrict__ vals, CircState *cs,
                                                         int masked, double pivot_tol, int top) {
   __shared__ double sm[32];
-  if (!top && group_idle(L, cs, masked, L.fs_gcirc, (int)blockIdx.x)) return;
+  if (!top && factor_group_idle(L, cs, masked, L.fs_gcirc, (int)blockIdx.x)) return;
   factor_group<T>(L, vals, cs, masked, pivot_tol, sm, top ? L.fs.n_groups : (int)blockIdx.x);
 }
 
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(256) k_top_pull(LUDev L, const double *__restr
   const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   if (w >= L.n_top_rl) return;  // warp-uniform
   const int j = L.top_items[w];
-  if (!item_active(L, cs, masked, j)) return;
+  if (!factor_active(L, cs, masked, j)) return;
   T *lu = lu_of<T>(L);
   const int p0 = L.cp[j], p1 = L.cp[j + 1], pd = L.diag[j];
   for (int p = p0 + lane; p < p1; p += 32) {
@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(1024) k_top_rl(LUDev L, CircState *cs, int mas
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   for (int t = 0; t < L.n_top_rl; ++t) {
     const int k = L.top_items[t];
-    if (!item_active(L, cs, masked, k)) continue;  // uniform: every thread reads the same flags
+    if (!factor_active(L, cs, masked, k)) continue;  // uniform: every thread reads the same flags
     const int pd = L.diag[k], p1 = L.cp[k + 1];
     double amax = 0.0;
     for (int p = pd + threadIdx.x; p < p1; p += blockDim.x) amax = fmax(amax, fabs((double)lu[p]));
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(256) k_toplv_pivot(LUDev L, int lv, CircState 
   const int t = L.tlv_item_ptr[lv] + (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   if (t >= L.tlv_item_ptr[lv + 1]) return;  // warp-uniform
   const int k = L.tlv_items[t];
-  if (!item_active(L, cs, masked, k)) return;
+  if (!factor_active(L, cs, masked, k)) return;
   T *lu = lu_of<T>(L);
   const int pd = L.diag[k], p1 = L.cp[k + 1];
   double amax = 0.0;
@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(256) k_toplv_update(LUDev L, int lv, CircState
   bool lost = false;
   for (int e = L.tgrp_ptr[g]; e < L.tgrp_ptr[g + 1]; ++e) {
     const int k = L.tgrp_k[e];
-    if (!item_active(L, cs, masked, k)) continue;  // warp-uniform
+    if (!factor_active(L, cs, masked, k)) continue;  // warp-uniform
     const int p = L.tgrp_pos[e];  // U(k, j)
     const T ukj = lu[p];
     if (ukj != (T)0) {
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
   __shared__ double sm[32];
   const SchedDev &SD = L.fs;
   const int g = blockIdx.x;
-  if (group_idle(L, cs, masked, L.fs_gcirc, g)) return;
+  if (factor_group_idle(L, cs, masked, L.fs_gcirc, g)) return;
   if (L.grp_snz[g] > cap) {  // too large for the buffer: factor in place in global memory
     factor_group<T>(L, vals, cs, masked, pivot_tol, sm, g);
     return;
@@ -379,12 +379,12 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
       const int b = SD.lvl_ptr[lv], e = SD.lvl_ptr[lv + 1];
       for (int t = b + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
         const int j = SD.items[t];
-        if (SD.is_thread[j] && item_active(L, cs, masked, j))
+        if (SD.is_thread[j] && factor_active(L, cs, masked, j))
           factor_column_m<1, T>(L, j, t - it0, cs, masked, pivot_tol, sm, S, M);
       }
       for (int t = b + warp; t < e; t += nwarps) {
         const int j = SD.items[t];
-        if (SD.is_thread[j] || !item_active(L, cs, masked, j)) continue;
+        if (SD.is_thread[j] || !factor_active(L, cs, masked, j)) continue;
         factor_column_m<32, T>(L, j, t - it0, cs, masked, pivot_tol, sm, S, M);
       }
       __syncthreads();
@@ -395,19 +395,19 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
       bool any_long = false;
       for (int t = b + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
         const int j = SD.items[t];
-        if (SD.is_thread[j] && item_active(L, cs, masked, j))
+        if (SD.is_thread[j] && factor_active(L, cs, masked, j))
           factor_column_t<T>(L, vals, j, cs, masked, pivot_tol, S);
       }
       for (int t = b + warp; t < e; t += nwarps) {
         const int j = SD.items[t];
         if (SD.is_long[j]) { any_long = true; continue; }
-        if (SD.is_thread[j] || !item_active(L, cs, masked, j)) continue;
+        if (SD.is_thread[j] || !factor_active(L, cs, masked, j)) continue;
         factor_column_s<false, T>(L, j, cs, masked, pivot_tol, sm, S);
       }
       if (__syncthreads_or(any_long)) {
         for (int t = b; t < e; ++t) {
           const int j = SD.items[t];
-          if (!SD.is_long[j] || !item_active(L, cs, masked, j)) continue;
+          if (!SD.is_long[j] || !factor_active(L, cs, masked, j)) continue;
           factor_column_s<true, T>(L, j, cs, masked, pivot_tol, sm, S);
           __syncthreads();
         }

@@ -16,6 +16,14 @@ __device__ __forceinline__ bool item_active(const LUDev &L, const CircState *cs,
   return s.need_solve && !s.singular && (s.phase == PH_DC || s.phase == PH_TRAN);
 }
 
+// A column is refactored this tick when its circuit has LU work and its
+// Jacobian changed since its last factorization (CircState::refactor).
+__device__ __forceinline__ bool factor_active(const LUDev &L, const CircState *cs, int masked, int j) {
+  if (!masked) return true;
+  const CircState &s = cs[L.circ_of_step[j]];
+  return s.need_solve && s.refactor && !s.singular && (s.phase == PH_DC || s.phase == PH_TRAN);
+}
+
 // A group of one circuit that has no LU work this tick returns at once
 // (before staging anything); packed groups (gcirc < 0) test their items.
 __device__ __forceinline__ bool group_idle(const LUDev &L, const CircState *cs, int masked, const int *gcirc,
@@ -25,6 +33,16 @@ __device__ __forceinline__ bool group_idle(const LUDev &L, const CircState *cs, 
   if (c < 0) return false;
   const CircState &s = cs[c];
   return !(s.need_solve && !s.singular && (s.phase == PH_DC || s.phase == PH_TRAN));
+}
+
+// The same for a factor group: also idle when its circuit reuses its factors.
+__device__ __forceinline__ bool factor_group_idle(const LUDev &L, const CircState *cs, int masked, const int *gcirc,
+                                                 int g) {
+  if (!masked || !gcirc) return false;
+  const int c = gcirc[g];
+  if (c < 0) return false;
+  const CircState &s = cs[c];
+  return !(s.need_solve && s.refactor && !s.singular && (s.phase == PH_DC || s.phase == PH_TRAN));
 }
 
 template <bool BLOCK>
