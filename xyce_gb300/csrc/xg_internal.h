@@ -317,7 +317,7 @@ struct LUDev {
 constexpr int kFusedMaxRows = 2048;        // largest circuit the resident form takes
 constexpr int kFusedMinCircuits = 64;      // smallest batch the resident form takes
 constexpr int kFusedThreads = 128;         // CTA size of the resident tick
-constexpr int kFusedMaxTicks = 1 << 20;    // ticks of one circuit in one launch, at most
+constexpr int kFusedMaxTicks = 4096;       // ticks of one circuit in one launch, at most (then the host relaunches)
 struct FusedDev {
   int *order = nullptr, *queue = nullptr;
   int *m1_ptr = nullptr, *m1_list = nullptr, *d_ptr = nullptr, *d_list = nullptr;
