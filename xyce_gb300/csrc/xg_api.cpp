@@ -890,6 +890,26 @@ static int resident_build(xg_ctx *ctx, const LUHost &H) {
       l_meth[i] = (H.ls_gbytes[g] > 0 || H.lsched.is_thread[i]) ? 1 : (H.lsched.is_long[i] ? 3 : 2);
     }
   for (int t = 0; t < H.lsched.n_hub; ++t) l_meth[H.lsched.items[t]] = 0;
+  // each level's items sorted by kind, with the start of the later kinds
+  auto sort_levels = [](const std::vector<int> &lptr, std::vector<int> &items, std::vector<int2> &split,
+                        auto &&kind) {
+    split.assign(lptr.size() - 1, int2{0, 0});
+    for (size_t lv = 0; lv + 1 < lptr.size(); ++lv) {
+      auto b = items.begin() + lptr[lv], e = items.begin() + lptr[lv + 1];
+      std::stable_sort(b, e, [&](int x, int y) { return kind(x) < kind(y); });
+      int s1 = lptr[lv + 1], s2 = lptr[lv + 1];
+      for (int t = lptr[lv + 1] - 1; t >= lptr[lv]; --t) {
+        if (kind(items[t]) >= 1) s1 = t;
+        if (kind(items[t]) >= 2) s2 = t;
+      }
+      split[lv] = int2{s1, s2};
+    }
+  };
+  std::vector<int> u_items = f_items;
+  std::vector<int2> f_split, u_split, l_split;
+  sort_levels(f_lptr, f_items, f_split, [&](int j) { return (int)f_kind[j]; });
+  sort_levels(f_lptr, u_items, u_split, [&](int k) { return (int)u_meth[k] - 1; });
+  sort_levels(l_lptr, l_items, l_split, [&](int i) { return l_meth[i] <= 1 ? 0 : (int)l_meth[i] - 1; });
   // instances, sources, long rows and long entries of each circuit
   auto bucket = [&](const std::vector<int> &circ_of, std::vector<int> &ptr, std::vector<int> &list) {
     ptr.assign(ncirc + 1, 0);
@@ -927,8 +947,9 @@ static int resident_build(xg_ctx *ctx, const LUHost &H) {
   UP(F.m1_ptr, m1_ptr); UP(F.m1_list, m1_list); UP(F.d_ptr, d_ptr); UP(F.d_list, d_list);
   UP(F.src_ptr, src_ptr); UP(F.src_list, src_list);
   UP(F.lr_ptr, lr_ptr); UP(F.lr_list, lr_list); UP(F.le_ptr, le_ptr); UP(F.le_list, le_list);
-  UP(F.f_cl, f_cl); UP(F.f_lptr, f_lptr); UP(F.f_items, f_items);
+  UP(F.f_cl, f_cl); UP(F.f_lptr, f_lptr); UP(F.f_items, f_items); UP(F.u_items, u_items);
   UP(F.l_cl, l_cl); UP(F.l_lptr, l_lptr); UP(F.l_items, l_items);
+  UP(F.f_split, f_split); UP(F.u_split, u_split); UP(F.l_split, l_split);
   UP(F.f_kind, f_kind); UP(F.l_meth, l_meth); UP(F.u_meth, u_meth);
 #undef UP
   if ((rc = dev_alloc(ctx, &F.queue, 1, A))) return rc;

@@ -318,13 +318,19 @@ constexpr int kFusedMaxRows = 2048;        // largest circuit the resident form 
 constexpr int kFusedMinCircuits = 64;      // smallest batch the resident form takes
 constexpr int kFusedThreads = 128;         // CTA size of the resident tick
 constexpr int kFusedMaxTicks = 4096;       // ticks of one circuit in one launch, at most (then the host relaunches)
+// Within a level the items are sorted by how they are computed, and
+// f_split / l_split / u_split hold, per level, where the later kinds start
+// ({warp, CTA} for the factor, {8-lane team, CTA} for the solves; the L
+// solve's first kind covers y = b and one-thread rows, told apart by
+// l_meth); u_items holds the factor levels' items in U-solve order.
 struct FusedDev {
   int *order = nullptr, *queue = nullptr;
   int *m1_ptr = nullptr, *m1_list = nullptr, *d_ptr = nullptr, *d_list = nullptr;
   int *src_ptr = nullptr, *src_list = nullptr;
   int *lr_ptr = nullptr, *lr_list = nullptr, *le_ptr = nullptr, *le_list = nullptr;
-  int *f_cl = nullptr, *f_lptr = nullptr, *f_items = nullptr;
+  int *f_cl = nullptr, *f_lptr = nullptr, *f_items = nullptr, *u_items = nullptr;
   int *l_cl = nullptr, *l_lptr = nullptr, *l_items = nullptr;
+  int2 *f_split = nullptr, *u_split = nullptr, *l_split = nullptr;
   signed char *f_kind = nullptr, *l_meth = nullptr, *u_meth = nullptr;
   unsigned long long *ticks = nullptr;  // [0] largest tick count of a circuit, [1] circuit-ticks (this launch)
   int max_rows = 0, grid = 0;

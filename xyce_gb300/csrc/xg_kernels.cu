@@ -1348,26 +1348,29 @@ struct FusedArgs {
 };
 
 // The factorization of circuit c, level by level: single-thread columns,
-// warp columns, then the columns that take the whole CTA.
+// warp columns, then the columns that take the whole CTA (each level's
+// items are sorted by kind; F.f_split gives where the warp and CTA kinds
+// start).
 __device__ void resident_factor(const DevArrays &d, const LUDev &L, const FusedDev &F, int c, double pivot_tol,
                                 double *sm) {
   const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, nwarps = nth >> 5;
   for (int lv = F.f_cl[c]; lv < F.f_cl[c + 1]; ++lv) {
     const int a = F.f_lptr[lv], b = F.f_lptr[lv + 1];
-    for (int t = a + tid; t < b; t += nth) {
+    const int2 sp = F.f_split[lv];
+    for (int t = a + tid; t < sp.x; t += nth) {
       const int j = F.f_items[t];
-      if (F.f_kind[j] == 0 && factor_active(L, d.cs, 1, j)) factor_column_t<double>(L, d.J, j, d.cs, 1, pivot_tol, nullptr);
+      if (factor_active(L, d.cs, 1, j)) factor_column_t<double>(L, d.J, j, d.cs, 1, pivot_tol, nullptr);
     }
-    for (int t = a + warp; t < b; t += nwarps) {
+    for (int t = sp.x + warp; t < sp.y; t += nwarps) {
       const int j = F.f_items[t];
-      if (F.f_kind[j] == 1 && factor_active(L, d.cs, 1, j)) factor_column<false, double>(L, d.J, j, d.cs, 1, pivot_tol, sm);
+      if (factor_active(L, d.cs, 1, j)) factor_column<false, double>(L, d.J, j, d.cs, 1, pivot_tol, sm);
     }
     // the thread and warp columns are done, and a breakdown they flagged is
     // visible to every thread: the tests below read the same values in all
     __syncthreads();
-    for (int t = a; t < b; ++t) {
+    for (int t = sp.y; t < b; ++t) {
       const int j = F.f_items[t];
-      if (F.f_kind[j] != 2 || !factor_active(L, d.cs, 1, j)) continue;
+      if (!factor_active(L, d.cs, 1, j)) continue;
       factor_column<true, double>(L, d.J, j, d.cs, 1, pivot_tol, sm);
       __syncthreads();
     }
@@ -1375,7 +1378,8 @@ __device__ void resident_factor(const DevArrays &d, const LUDev &L, const FusedD
 }
 
 // The L solve (forward) and the U solve (backward) of circuit c; every row
-// is summed the way the grouped kernels sum it (F.l_meth / F.u_meth).
+// is summed the way the grouped kernels sum it (F.l_meth / F.u_meth), the
+// level's rows sorted by method (F.l_split / F.u_split).
 __device__ void resident_solve(const DevArrays &d, const LUDev &L, const FusedDev &F, int c, double *sm) {
   const int tid = threadIdx.x, nth = blockDim.x;
   const int team = tid >> 3, nteams = nth >> 3, sub = tid & 7;
@@ -1384,32 +1388,29 @@ __device__ void resident_solve(const DevArrays &d, const LUDev &L, const FusedDe
   double *x = d.dx;
   for (int lv = F.l_cl[c]; lv < F.l_cl[c + 1]; ++lv) {
     const int a = F.l_lptr[lv], e = F.l_lptr[lv + 1];
-    for (int t = a + tid; t < e; t += nth) {
+    const int2 sp = F.l_split[lv];
+    for (int t = a + tid; t < sp.x; t += nth) {
       const int i = F.l_items[t];
-      const int m = F.l_meth[i];
-      if (m == 0) {
+      if (F.l_meth[i] == 0) {
         L.y[i] = b[L.row_of_step[i]];
-      } else if (m == 1) {
+      } else {
         double sum = 0.0;
         for (int q = L.l_ptr[i]; q < L.l_ptr[i + 1]; ++q) sum += (double)lu[L.l_pos[q]] * L.y[L.l_col[q]];
         L.y[i] = b[L.row_of_step[i]] - sum;
       }
     }
-    for (int t0 = a; t0 < e; t0 += nteams) {  // warp-uniform bound
+    for (int t0 = sp.x; t0 < sp.y; t0 += nteams) {  // warp-uniform bound
       const int t = t0 + team;
-      const int i = t < e ? F.l_items[t] : 0;
-      const bool act = t < e && F.l_meth[i] == 2;
-      if (__any_sync(0xffffffffu, act)) {
-        double sum = 0.0;
-        if (act)
-          for (int q = L.l_ptr[i] + sub; q < L.l_ptr[i + 1]; q += 8) sum += (double)lu[L.l_pos[q]] * L.y[L.l_col[q]];
-        for (int o = 4; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, 8);
-        if (act && sub == 0) L.y[i] = b[L.row_of_step[i]] - sum;
-      }
+      const bool act = t < sp.y;
+      const int i = act ? F.l_items[t] : 0;
+      double sum = 0.0;
+      if (act)
+        for (int q = L.l_ptr[i] + sub; q < L.l_ptr[i + 1]; q += 8) sum += (double)lu[L.l_pos[q]] * L.y[L.l_col[q]];
+      for (int o = 4; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, 8);
+      if (act && sub == 0) L.y[i] = b[L.row_of_step[i]] - sum;
     }
-    for (int t = a; t < e; ++t) {
+    for (int t = sp.y; t < e; ++t) {
       const int i = F.l_items[t];
-      if (F.l_meth[i] != 3) continue;  // uniform
       const double sum = long_row_dot<double>(lu, L.l_pos, L.l_col, L.y, L.l_ptr[i], L.l_ptr[i + 1], sm);
       if (tid == 0) L.y[i] = b[L.row_of_step[i]] - sum;
     }
@@ -1417,34 +1418,31 @@ __device__ void resident_solve(const DevArrays &d, const LUDev &L, const FusedDe
   }
   for (int lv = F.f_cl[c + 1] - 1; lv >= F.f_cl[c]; --lv) {
     const int a = F.f_lptr[lv], e = F.f_lptr[lv + 1];
-    for (int t = a + tid; t < e; t += nth) {
-      const int k = F.f_items[t];
-      if (F.u_meth[k] != 1) continue;
+    const int2 sp = F.u_split[lv];
+    for (int t = a + tid; t < sp.x; t += nth) {
+      const int k = F.u_items[t];
       double sum = 0.0;
       for (int q = L.u_ptr[k]; q < L.u_ptr[k + 1]; ++q) sum += (double)lu[L.u_pos[q]] * L.y[L.u_col[q]];
       const double z = (L.y[k] - sum) / (double)lu[L.diag[k]];
       L.y[k] = z;
       x[L.col_of_step[k]] = z;
     }
-    for (int t0 = a; t0 < e; t0 += nteams) {
+    for (int t0 = sp.x; t0 < sp.y; t0 += nteams) {
       const int t = t0 + team;
-      const int k = t < e ? F.f_items[t] : 0;
-      const bool act = t < e && F.u_meth[k] == 2;
-      if (__any_sync(0xffffffffu, act)) {
-        double sum = 0.0;
-        if (act)
-          for (int q = L.u_ptr[k] + sub; q < L.u_ptr[k + 1]; q += 8) sum += (double)lu[L.u_pos[q]] * L.y[L.u_col[q]];
-        for (int o = 4; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, 8);
-        if (act && sub == 0) {
-          const double z = (L.y[k] - sum) / (double)lu[L.diag[k]];
-          L.y[k] = z;
-          x[L.col_of_step[k]] = z;
-        }
+      const bool act = t < sp.y;
+      const int k = act ? F.u_items[t] : 0;
+      double sum = 0.0;
+      if (act)
+        for (int q = L.u_ptr[k] + sub; q < L.u_ptr[k + 1]; q += 8) sum += (double)lu[L.u_pos[q]] * L.y[L.u_col[q]];
+      for (int o = 4; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, 8);
+      if (act && sub == 0) {
+        const double z = (L.y[k] - sum) / (double)lu[L.diag[k]];
+        L.y[k] = z;
+        x[L.col_of_step[k]] = z;
       }
     }
-    for (int t = a; t < e; ++t) {
-      const int k = F.f_items[t];
-      if (F.u_meth[k] != 3) continue;  // uniform
+    for (int t = sp.y; t < e; ++t) {
+      const int k = F.u_items[t];
       const double sum = long_row_dot<double>(lu, L.u_pos, L.u_col, L.y, L.u_ptr[k], L.u_ptr[k + 1], sm);
       if (tid == 0) {
         const double z = (L.y[k] - sum) / (double)lu[L.diag[k]];
