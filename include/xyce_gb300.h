@@ -247,6 +247,17 @@ int xg_lu_schedule_info(xg_ctx *ctx, int *ordering, int *factor_top, int *solve_
  * from the next analysis; not allowed while a transient is in progress. */
 int xg_lu_set_schedule(xg_ctx *ctx, int ordering, int factor_top, int solve_top);
 
+/* Frozen-pivot acceptance of the refactorization (default 1e-2): a pivot
+ * below tol times the largest entry of its updated column is a breakdown
+ * (xg_lu_factor returns XG_ERR_SINGULAR; in a transient the circuit parks
+ * its Newton iteration, the host re-pivots that circuit alone from the
+ * parked Jacobian — every other circuit keeps its pivots, factors and
+ * results — and the iteration resumes).  KLU re-pivots on every
+ * factorization (N_LAS_AmesosSolver.C:315-318); this is the threshold at
+ * which the frozen pivots are given up.  Not allowed while a transient is in
+ * progress. */
+int xg_lu_set_pivot_tolerance(xg_ctx *ctx, double tol);
+
 /* Factor reuse in the transient.  on = 1 (default): a circuit without
  * nonlinear devices whose Jacobian coefficients (OneStep's qscale / fscale,
  * the operating point's gmin shunt) equal those of its last factorization

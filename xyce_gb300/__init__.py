@@ -49,7 +49,7 @@ EXPORTED = [
     "xg_get_pattern", "xg_update_sources", "xg_update_state", "xg_load_dae_vectors",
     "xg_load_dae_matrices", "xg_lu_analyze", "xg_lu_factor", "xg_lu_solve",
     "xg_lu_solve_noalloc", "xg_lu_set_precision", "xg_lu_info", "xg_lu_schedule_info", "xg_lu_set_schedule", "xg_lu_analyze_pattern",
-    "xg_lu_set_tuning", "xg_lu_tuning_info", "xg_lu_set_reuse",
+    "xg_lu_set_tuning", "xg_lu_tuning_info", "xg_lu_set_reuse", "xg_lu_set_pivot_tolerance",
     "xg_transient", "xg_tran_set_form", "xg_tran_start", "xg_tran_advance", "xg_tran_results", "xg_tran_end",
     "xg_tran_predictors", "xg_tran_orders", "xg_tran_profile", "xg_tran_predictor_stats", "xg_set_predictor", "xg_mlp_set", "xg_mlp_get",
     "xg_mlp_train", "xg_mlp_grad", "xg_mlp_forward",
@@ -148,6 +148,7 @@ def lib() -> C.CDLL:
     L.xg_lu_set_schedule.argtypes = [P, I, I, I]
     L.xg_lu_set_tuning.argtypes = [P, I]
     L.xg_lu_set_reuse.argtypes = [P, I]
+    L.xg_lu_set_pivot_tolerance.argtypes = [P, D]
     L.xg_lu_tuning_info.argtypes = [P, C.POINTER(LuTuning)]
     L.xg_lu_analyze_pattern.argtypes = [I, C.POINTER(I), C.POINTER(I), C.POINTER(C.c_double), I,
                                         C.POINTER(C.c_longlong), C.POINTER(I), C.POINTER(I), C.POINTER(I)]
@@ -304,6 +305,10 @@ class Circuit:
         """TUNE_TIMED (default): launch shapes of the LU sweeps chosen by
         timed trials after each analysis; TUNE_MODEL: closed-form choice."""
         self._check(lib().xg_lu_set_tuning(self.h, int(mode)))
+
+    def lu_set_pivot_tolerance(self, tol: float):
+        """Frozen-pivot acceptance threshold (default 1e-2), see xg_lu_set_pivot_tolerance."""
+        self._check(lib().xg_lu_set_pivot_tolerance(self.h, float(tol)))
 
     def lu_set_reuse(self, on: bool):
         """Skip bit-identical refactorizations of linear circuits (default on)."""

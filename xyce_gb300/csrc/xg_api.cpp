@@ -67,6 +67,8 @@ struct xg_ctx {
   int lu_prec = XG_PREC_FP64, lu_refine = 2;  // xg_lu_set_precision
   int tune_mode = XG_TUNE_TIMED;               // xg_lu_set_tuning
   int lu_reuse = 1;                            // xg_lu_set_reuse
+  double pivot_tol = kRuntimePivotTol;         // xg_lu_set_pivot_tolerance
+  std::vector<int> row_of_col_h;               // pivot row of every column in the current analysis
   int lu_gen = 0;                              // analyses uploaded so far
   xg_lu_tuning tuning{};                       // what the tuner chose for the current analysis
   int predictor = XG_PRED_POLY;                // xg_set_predictor
@@ -1115,6 +1117,8 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
   L.l_levels = (int)H.l_lvl_ptr.size() - 1;
   L.u_levels = (int)H.u_lvl_ptr.size() - 1;
   if ((rc = resident_build(ctx, H))) return rc;
+  ctx->row_of_col_h.assign(H.n, -1);
+  for (int p = 0; p < H.n; ++p) ctx->row_of_col_h[H.col_of_step[p]] = H.row_of_step[p];
   // a new analysis: every circuit refactors before it may reuse factors again
   ctx->lu_gen++;
   CK(cudaMemcpyAsync(ctx->d.lu_gen, &ctx->lu_gen, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
@@ -1294,13 +1298,22 @@ static int tune_lu(xg_ctx *ctx, const LUHost &H, const double *vals_dev) {
 
 extern "C" {
 
-static int lu_analyze_from_device(xg_ctx *ctx, const double *vals_dev) {
+// refresh (optional, per circuit): re-pivot only those circuits from the
+// values; every other circuit keeps the pivot rows of the current analysis,
+// so its factors, and its results, stay exactly what they were.
+static int lu_analyze_from_device(xg_ctx *ctx, const double *vals_dev, const std::vector<char> *refresh = nullptr) {
   std::vector<double> v(ctx->nnz);
   CK(cudaMemcpyAsync(v.data(), vals_dev, sizeof(double) * ctx->nnz, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   LUHost H;
   std::string err;
-  int rc = lu_analyze_host(ctx->n, ctx->rp, ctx->ci, v, H, err, ctx->sched_order);
+  std::vector<int> keep;
+  if (refresh && (int)ctx->row_of_col_h.size() == ctx->n) {
+    keep.assign(ctx->n, -1);
+    for (int j = 0; j < ctx->n; ++j)
+      if (!(*refresh)[ctx->circ_of_row[j]]) keep[j] = ctx->row_of_col_h[j];
+  }
+  int rc = lu_analyze_host(ctx->n, ctx->rp, ctx->ci, v, H, err, ctx->sched_order, keep.empty() ? nullptr : &keep);
   if (rc == XG_OK) {
     if (ctx->sched_ftop >= 0) H.top_multi = (ctx->sched_ftop == XG_TOP_LEVELS);
     if (ctx->sched_stop >= 0) H.solve_top_multi = (ctx->sched_stop == XG_TOP_LEVELS);
@@ -1321,7 +1334,7 @@ int xg_lu_factor(xg_ctx *ctx, const double *vals) {
   if (!ctx->lu_ready) return fail(ctx, XG_ERR_STATE, "call xg_lu_analyze first");
   CK(cudaMemsetAsync(ctx->breakdown_dev, 0, sizeof(int), ctx->stream));
   if (ctx->L.mixed) ctx->L.a_vals = vals;
-  launch_lu_factor_k(ctx->stream, ctx->L, vals, ctx->d.cs, 0, kRuntimePivotTol);
+  launch_lu_factor_k(ctx->stream, ctx->L, vals, ctx->d.cs, 0, ctx->pivot_tol);
   CK(cudaGetLastError());
   int bd = 0;
   CK(cudaMemcpyAsync(&bd, ctx->breakdown_dev, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1378,6 +1391,14 @@ int xg_lu_set_precision(xg_ctx *ctx, int precision, int n_refine) {
   ctx->lu_prec = precision;
   ctx->lu_refine = n_refine;
   ctx->lu_ready = false;  // the next xg_lu_analyze (or transient) builds factors of this precision
+  return XG_OK;
+}
+
+int xg_lu_set_pivot_tolerance(xg_ctx *ctx, double tol) {
+  if (!ctx) return XG_ERR_ARG;
+  if (!(tol > 0.0 && tol < 1.0)) return fail(ctx, XG_ERR_ARG, "pivot tolerance must lie in (0, 1)");
+  if (ctx->run) return fail(ctx, XG_ERR_STATE, "the pivot tolerance cannot change during a transient");
+  ctx->pivot_tol = tol;
   return XG_OK;
 }
 
@@ -1581,6 +1602,20 @@ void breakpoints(const Wave &w, double tstop, std::vector<double> &bp) {
   }
 }
 
+// The circuits parked on a pivot breakdown (phase STALL): the ones a
+// re-analysis re-pivots.  Empty vector: none parked (re-pivot all).
+int stalled_circuits(xg_ctx *ctx, std::vector<char> &refresh) {
+  std::vector<CircState> cs(ctx->ncirc);
+  CK(cudaMemcpyAsync(cs.data(), ctx->d.cs, sizeof(CircState) * ctx->ncirc, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  refresh.assign(ctx->ncirc, 0);
+  bool any = false;
+  for (int c = 0; c < ctx->ncirc; ++c)
+    if (cs[c].phase == PH_STALL) { refresh[c] = 1; any = true; }
+  if (!any) refresh.clear();
+  return XG_OK;
+}
+
 // Runs tick batches until every circuit is done, failed or paused; re-pivots
 // on LU breakdown.  One host synchronization per batch of ticks.
 int run_until_idle(TranRun &R) {
@@ -1597,8 +1632,10 @@ int run_until_idle(TranRun &R) {
       // frozen pivots failed: re-pivot from the parked Jacobian and resume it
       consecutive++;
       if (consecutive > 4) return fail(ctx, XG_ERR_SINGULAR, "LU keeps breaking down after re-pivoting");
-      if ((rc = lu_analyze_from_device(ctx, d.J))) return rc;
-      R.pivot_tol = (consecutive >= 2) ? 0.0 : kRuntimePivotTol;
+      std::vector<char> refresh;
+      if ((rc = stalled_circuits(ctx, refresh))) return rc;
+      if ((rc = lu_analyze_from_device(ctx, d.J, refresh.empty() ? nullptr : &refresh))) return rc;
+      R.pivot_tol = (consecutive >= 2) ? 0.0 : ctx->pivot_tol;
       if ((rc = capture(R))) return rc;
       launch_unstall_k(ctx->stream, d, ctx->ncirc);
       launch_back(R);
@@ -1608,7 +1645,7 @@ int run_until_idle(TranRun &R) {
       continue;
     }
     if (consecutive && R.pivot_tol == 0.0) {
-      R.pivot_tol = kRuntimePivotTol;
+      R.pivot_tol = ctx->pivot_tol;
       if ((rc = capture(R))) return rc;
     }
     consecutive = 0;
@@ -1696,6 +1733,7 @@ static int tran_start_run(xg_ctx *ctx, const xg_tran_params *p, const std::vecto
   R.t0 = std::chrono::steady_clock::now();
   R.ctx = ctx;
   R.cap = cap;
+  R.pivot_tol = ctx->pivot_tol;
   const int n = ctx->n, ncirc = ctx->ncirc;
   DevArrays &d = ctx->d;
   R.pcount = pcount;
@@ -2072,7 +2110,7 @@ extern "C" int xg_newton_solve(xg_ctx *ctx, const xg_newton_params *p, double ti
   launch_newton_weights_k(ctx->stream, d, n);
   CK(cudaMemsetAsync(ctx->breakdown_dev, 0, sizeof(int), ctx->stream));
   ctx->status_host[0] = ctx->status_host[1] = 0;
-  double pivot_tol = kRuntimePivotTol;
+  double pivot_tol = ctx->pivot_tol;
   int rc = 0;
   // one Newton iteration of every unfinished circuit per pass; DampedNewton
   // stops each circuit within maxstep iterations
@@ -2087,15 +2125,17 @@ extern "C" int xg_newton_solve(xg_ctx *ctx, const xg_newton_params *p, double ti
     for (int consecutive = 1; ctx->status_host[1]; ++consecutive) {
       // a frozen pivot failed: re-pivot from the parked Jacobian and resume
       if (consecutive > 4) return fail(ctx, XG_ERR_SINGULAR, "LU keeps breaking down after re-pivoting");
-      if ((rc = lu_analyze_from_device(ctx, d.J))) return rc;
-      pivot_tol = (consecutive >= 2) ? 0.0 : kRuntimePivotTol;
+      std::vector<char> refresh;
+      if ((rc = stalled_circuits(ctx, refresh))) return rc;
+      if ((rc = lu_analyze_from_device(ctx, d.J, refresh.empty() ? nullptr : &refresh))) return rc;
+      pivot_tol = (consecutive >= 2) ? 0.0 : ctx->pivot_tol;
       launch_unstall_k(ctx->stream, d, ncirc);
       back_kernels(ctx, d, pivot_tol, nullptr, nullptr, 0);
       launch_count_done_k(ctx->stream, d, ncirc, ctx->breakdown_dev, ctx->status_dev);
       CK(cudaGetLastError());
       CK(cudaStreamSynchronize(ctx->stream));
     }
-    pivot_tol = kRuntimePivotTol;
+    pivot_tol = ctx->pivot_tol;
     if (ctx->status_host[0] >= ncirc) break;
   }
   std::vector<CircState> out(ncirc);

@@ -399,8 +399,11 @@ Schedule build_schedule(int n, const std::function<void(int, std::vector<int> &)
                         const std::function<int(int)> &weight);
 
 // Analysis entry (xg_symbolic.cpp): CSR pattern + values -> LUHost.
+// keep_rows (optional, length n): columns with keep_rows[j] >= 0 keep that
+// pivot row instead of a new match from the values (whole circuits only).
 int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &ci,
-                    const std::vector<double> &vals, LUHost &out, std::string &err, int force_ordering = -1);
+                    const std::vector<double> &vals, LUHost &out, std::string &err, int force_ordering = -1,
+                    const std::vector<int> *keep_rows = nullptr);
 
 // Kernel launchers (xg_kernels.cu, xg_lu.cu).
 void launch_sources_k(cudaStream_t st, const DevArrays &d, int n_v, int n_src, int use_explicit, double t);

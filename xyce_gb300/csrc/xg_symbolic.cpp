@@ -62,18 +62,25 @@ Csc to_csc(int n, const std::vector<int> &rp, const std::vector<int> &ci) {
 // kDiagPref of its column's largest entry, then greedy by magnitude, then augmenting
 // paths (MC21-style depth-first search) for what is left.
 bool match_rows(int n, const Csc &A, const std::vector<double> &vals, std::vector<int> &row_of_col,
-                std::string &err) {
+                std::string &err, const std::vector<int> *keep) {
   std::vector<int> col_of_row(n, -1);
   row_of_col.assign(n, -1);
+  // kept columns (keep[j] >= 0) take their earlier row first; they are
+  // whole independent blocks, so the search below never reaches them
+  if (keep)
+    for (int j = 0; j < n; ++j)
+      if ((*keep)[j] >= 0) { row_of_col[j] = (*keep)[j]; col_of_row[(*keep)[j]] = j; }
   std::vector<double> colmax(n, 0.0);
   for (int j = 0; j < n; ++j)
     for (int q = A.cp[j]; q < A.cp[j + 1]; ++q) colmax[j] = std::max(colmax[j], std::fabs(vals[A.src[q]]));
-  for (int j = 0; j < n; ++j)
+  for (int j = 0; j < n; ++j) {
+    if (row_of_col[j] >= 0) continue;
     for (int q = A.cp[j]; q < A.cp[j + 1]; ++q)
       if (A.ri[q] == j) {
         double a = std::fabs(vals[A.src[q]]);
         if (a > 0 && a >= kDiagPref * colmax[j]) { row_of_col[j] = j; col_of_row[j] = j; }
       }
+  }
   for (int j = 0; j < n; ++j) {
     if (row_of_col[j] >= 0) continue;
     int best = -1;
@@ -386,12 +393,13 @@ void parallel_for(size_t count, long long weight, const std::function<void(size_
 }  // namespace
 
 int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &ci,
-                    const std::vector<double> &vals, LUHost &out, std::string &err, int force_ordering) {
+                    const std::vector<double> &vals, LUHost &out, std::string &err, int force_ordering,
+                    const std::vector<int> *keep_rows) {
   out = LUHost();
   out.n = n;
   Csc A = to_csc(n, rp, ci);
   std::vector<int> row_of_col;
-  if (!match_rows(n, A, vals, row_of_col, err)) return XG_ERR_SINGULAR;
+  if (!match_rows(n, A, vals, row_of_col, err, keep_rows)) return XG_ERR_SINGULAR;
   std::vector<int> inv(n);  // A row -> M index
   for (int j = 0; j < n; ++j) inv[row_of_col[j]] = j;
   // M = rows permuted: M row j = A row row_of_col[j].  M's columns are A's
