@@ -332,6 +332,7 @@ typedef struct xg_tran_stats {
   long long kernel_launches;                   /* kernels launched while advancing */
   long long circuit_ticks;                     /* resident form: Newton iterations summed over circuits */
   long long factor_skips;                      /* refactorizations skipped (xg_lu_set_reuse) */
+  int resident_threads;                        /* resident form: CTA size the timed trials chose (0: not yet) */
 } xg_tran_stats;
 
 /* How a transient advances.  XG_FORM_TICK_GRAPH: a tick (one Newton

@@ -94,7 +94,7 @@ class TranStats(C.Structure):
                 ("n_analyze", C.c_int), ("t_final_min", C.c_double),
                 ("t_final_max", C.c_double), ("seconds", C.c_double), ("kernels_per_tick", C.c_int),
                 ("form", C.c_int), ("kernel_launches", C.c_longlong), ("circuit_ticks", C.c_longlong),
-                ("factor_skips", C.c_longlong)]
+                ("factor_skips", C.c_longlong), ("resident_threads", C.c_int)]
 
 
 _lib = None

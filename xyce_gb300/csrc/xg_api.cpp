@@ -941,10 +941,42 @@ static int resident_build(xg_ctx *ctx, const LUHost &H) {
     const long long wb = ctx->offsets[b + 1] - ctx->offsets[b] + ctx->inst_of_circ[b];
     return wa > wb;
   });
+  // shared-memory buffers of the circuits' factor columns
+  std::vector<int> c_soff(n, 0), c_fcnt(ncirc, 0), c_umeta((size_t)4 * H.ri.size(), 0);
+  int max_fbuf = 0;
+  for (int c = 0; c < ncirc; ++c) {
+    int off = 0;
+    for (int lv = f_cl[c]; lv < f_cl[c + 1]; ++lv)
+      for (int t = f_lptr[lv]; t < f_lptr[lv + 1]; ++t) {
+        const int j = f_items[t];
+        c_soff[j] = off;
+        off += H.cp[j + 1] - H.cp[j];
+      }
+    c_fcnt[c] = off;
+    max_fbuf = std::max(max_fbuf, off);
+  }
+  for (int j = 0; j < n; ++j)
+    for (int p = H.cp[j]; p < H.diag[j]; ++p) {
+      const int k = H.ri[p];
+      int *u = &c_umeta[(size_t)4 * p];
+      u[0] = c_soff[k] + (H.diag[k] + 1 - H.cp[k]);
+      u[1] = H.cp[k + 1] - H.diag[k] - 1;
+      u[2] = H.upd_off[p];
+      u[3] = H.diag[k] + 1;
+    }
+  const bool staged = (2 * (size_t)max_rows + (size_t)max_fbuf) * sizeof(double) <= (size_t)kFusedSmemBytes;
   FusedDev F;
   auto &A = ctx->lu_allocs;
   int rc = 0;
 #define UP(ptr, vec) if ((rc = dev_upload(ctx, &ptr, vec, A))) return rc
+  if (staged) {
+    int *um = nullptr;
+    UP(F.c_soff, c_soff);
+    UP(F.c_fcnt, c_fcnt);
+    UP(um, c_umeta);
+    F.c_umeta = reinterpret_cast<const int4 *>(um);
+    F.max_fbuf = max_fbuf;
+  }
   UP(F.order, order);
   UP(F.m1_ptr, m1_ptr); UP(F.m1_list, m1_list); UP(F.d_ptr, d_ptr); UP(F.d_list, d_list);
   UP(F.src_ptr, src_ptr); UP(F.src_list, src_list);
@@ -957,7 +989,7 @@ static int resident_build(xg_ctx *ctx, const LUHost &H) {
   if ((rc = dev_alloc(ctx, &F.queue, 1, A))) return rc;
   if ((rc = dev_alloc(ctx, &F.ticks, 2, A))) return rc;
   F.max_rows = max_rows;
-  if (resident_prepare_k(max_rows, ctx->device, &F.grid) != XG_OK) return fail(ctx, XG_ERR_CUDA, "resident tick set-up");
+  if (resident_prepare_k(max_rows, F.max_fbuf, ctx->device, F.grid) != XG_OK) return fail(ctx, XG_ERR_CUDA, "resident tick set-up");
   ctx->F = F;
   const int slots[8] = {ctx->sF_m, ctx->sQ_m, ctx->sL_m, ctx->sM_m, ctx->sF_d, ctx->sQ_d, ctx->sL_d, ctx->sM_d};
   std::copy(slots, slots + 8, ctx->resident_slots);
@@ -1505,9 +1537,18 @@ struct TranRun {
   long long circuit_ticks = 0;    // Newton iterations run by the resident tick, summed over circuits
   long long kernel_launches = 0;  // kernels launched while advancing
   unsigned long long tick_count[2] = {0, 0};
+  // CTA size of the resident kernel: the first launches try each of
+  // kResidentThreads (the same bits with every size) and the one with the
+  // shortest device time per circuit-tick is kept
+  int res_threads = 0;
+  double res_trial[3] = {-1.0, -1.0, -1.0};
+  int res_pending = -1;
+  cudaEvent_t res_ev[2] = {nullptr, nullptr};
   std::chrono::steady_clock::time_point t0;
   ~TranRun() {
     if (exec) cudaGraphExecDestroy(exec);
+    for (cudaEvent_t e : res_ev)
+      if (e) cudaEventDestroy(e);
     free_list(allocs);
     if (ctx) { ctx->d.out_t = nullptr; ctx->d.out_v = nullptr; ctx->d.out_p = nullptr; ctx->d.out_o = nullptr; }
   }
@@ -1649,6 +1690,19 @@ int run_until_idle(TranRun &R) {
       if ((rc = capture(R))) return rc;
     }
     consecutive = 0;
+    if (R.res_pending >= 0) {
+      float ms = 0.f;
+      if (R.tick_count[1] > 0 && cudaEventElapsedTime(&ms, R.res_ev[0], R.res_ev[1]) == cudaSuccess) {
+        R.res_trial[R.res_pending] = ms / (double)R.tick_count[1];
+        if (R.res_trial[0] >= 0 && R.res_trial[1] >= 0 && R.res_trial[2] >= 0) {
+          int best = 0;
+          for (int k = 1; k < 3; ++k)
+            if (R.res_trial[k] < R.res_trial[best]) best = k;
+          R.res_threads = kResidentThreads[best];
+        }
+      }
+      R.res_pending = -1;
+    }
     if (R.tick_count[0]) {
       // the last resident launch: its longest circuit's ticks, and all of them
       R.ticks += (long long)R.tick_count[0];
@@ -1660,8 +1714,17 @@ int run_until_idle(TranRun &R) {
     if (R.resident && ctx->resident_ok) {
       // every circuit runs its ticks in one CTA until it pauses, finishes,
       // fails or parks on a pivot breakdown
-      launch_resident_k(ctx->stream, d, ctx->L, ctx->F, ctx->ncirc, ctx->nm, ctx->nd, ctx->nv, ctx->sto_base_m,
-                        ctx->resident_slots, R.bps, R.bp_ptr, R.cap, R.pmax, R.pivot_tol);
+      int threads = R.res_threads;
+      if (!threads) {
+        R.res_pending = R.res_trial[0] < 0 ? 0 : (R.res_trial[1] < 0 ? 1 : 2);
+        threads = kResidentThreads[R.res_pending];
+        for (cudaEvent_t &e : R.res_ev)
+          if (!e) CK(cudaEventCreate(&e));
+        CK(cudaEventRecord(R.res_ev[0], ctx->stream));
+      }
+      launch_resident_k(ctx->stream, d, ctx->L, ctx->F, threads, ctx->ncirc, ctx->nm, ctx->nd, ctx->nv,
+                        ctx->sto_base_m, ctx->resident_slots, R.bps, R.bp_ptr, R.cap, R.pmax, R.pivot_tol);
+      if (R.res_pending >= 0) CK(cudaEventRecord(R.res_ev[1], ctx->stream));
       launch_count_done_k(ctx->stream, d, ctx->ncirc, ctx->breakdown_dev, ctx->status_dev);
       CK(cudaGetLastError());
       CK(cudaMemcpyAsync(R.tick_count, ctx->F.ticks, sizeof R.tick_count, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1880,6 +1943,7 @@ extern "C" int xg_tran_results(xg_ctx *ctx, int *counts, double *times, double *
     stats->form = R.resident ? XG_FORM_RESIDENT : XG_FORM_TICK_GRAPH;
     stats->kernel_launches = R.kernel_launches;
     stats->circuit_ticks = R.circuit_ticks;
+    stats->resident_threads = R.res_threads;
     stats->device_evals = evals;
     stats->n_analyze = ctx->n_analyze;
     stats->status = status;

@@ -316,7 +316,6 @@ struct LUDev {
 // compute the same bits.
 constexpr int kFusedMaxRows = 2048;        // largest circuit the resident form takes
 constexpr int kFusedMinCircuits = 64;      // smallest batch the resident form takes
-constexpr int kFusedThreads = 128;         // CTA size of the resident tick
 constexpr int kFusedMaxTicks = 4096;       // ticks of one circuit in one launch, at most (then the host relaunches)
 // Within a level the items are sorted by how they are computed, and
 // f_split / l_split / u_split hold, per level, where the later kinds start
@@ -333,8 +332,18 @@ struct FusedDev {
   int2 *f_split = nullptr, *u_split = nullptr, *l_split = nullptr;
   signed char *f_kind = nullptr, *l_meth = nullptr, *u_meth = nullptr;
   unsigned long long *ticks = nullptr;  // [0] largest tick count of a circuit, [1] circuit-ticks (this launch)
-  int max_rows = 0, grid = 0;
+  int max_rows = 0;
+  int grid[3] = {0, 0, 0};  // persistent grids of the kResidentThreads CTA sizes
+  // the circuit's factor columns staged in shared memory: column j at
+  // c_soff[j] of its circuit's buffer (c_fcnt[c] entries); c_umeta as
+  // LUDev::umeta with .x the buffer offset of L(k+1.., k); max_fbuf = 0:
+  // columns stay in global memory
+  int *c_soff = nullptr, *c_fcnt = nullptr;
+  const int4 *c_umeta = nullptr;
+  int max_fbuf = 0;
 };
+constexpr int kFusedSmemBytes = 160 * 1024;  // largest resident buffer (row partials + staged columns)
+constexpr int kResidentThreads[3] = {32, 64, 128};  // CTA sizes the driver tries
 
 // Host-side analysis result.
 struct LUHost {
@@ -430,10 +439,10 @@ void launch_count_done_k(cudaStream_t st, const DevArrays &d, int ncirc, const i
                          int *status_out);
 void launch_unstall_k(cudaStream_t st, const DevArrays &d, int ncirc);
 void launch_newton_weights_k(cudaStream_t st, const DevArrays &d, int n);
-int resident_prepare_k(int max_rows, int device, int *grid);
-void launch_resident_k(cudaStream_t st, const DevArrays &d, const LUDev &L, const FusedDev &F, int ncirc, int nm,
-                       int nd, int nv, int sto_base_m, const int *slots, const double *bps, const int *bp_ptr,
-                       int cap, int pmax, double pivot_tol);
+int resident_prepare_k(int max_rows, int max_fbuf, int device, int *grid);
+void launch_resident_k(cudaStream_t st, const DevArrays &d, const LUDev &L, const FusedDev &F, int threads,
+                       int ncirc, int nm, int nd, int nv, int sto_base_m, const int *slots, const double *bps,
+                       const int *bp_ptr, int cap, int pmax, double pivot_tol);
 void launch_set_target_k(cudaStream_t st, const DevArrays &d, int ncirc, int n_steps);
 int lu_prepare_k();  // shared-memory opt-in of the staged group factorization
 void launch_lu_factor_k(cudaStream_t st, const LUDev &L, const double *vals, CircState *cs, int masked,

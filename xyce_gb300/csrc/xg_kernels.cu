@@ -1350,20 +1350,36 @@ struct FusedArgs {
 // The factorization of circuit c, level by level: single-thread columns,
 // warp columns, then the columns that take the whole CTA (each level's
 // items are sorted by kind; F.f_split gives where the warp and CTA kinds
-// start).
+// start).  S (when the circuit's columns fit): the circuit's columns are
+// loaded into shared memory once, factored there and written back once.
 __device__ void resident_factor(const DevArrays &d, const LUDev &L, const FusedDev &F, int c, double pivot_tol,
-                                double *sm) {
-  const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, nwarps = nth >> 5;
-  for (int lv = F.f_cl[c]; lv < F.f_cl[c + 1]; ++lv) {
+                                double *sm, double *S) {
+  const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31, nwarps = nth >> 5;
+  const int lv0 = F.f_cl[c], lv1 = F.f_cl[c + 1];
+  const int *soff = S ? F.c_soff : L.grp_soff;
+  const int4 *umeta = S ? F.c_umeta : L.umeta;
+  if (S) {
+    for (int t = F.f_lptr[lv0] + warp; t < F.f_lptr[lv1]; t += nwarps) {
+      const int j = F.f_items[t], p0 = L.cp[j], p1 = L.cp[j + 1], o = F.c_soff[j];
+      for (int p = p0 + lane; p < p1; p += 32) {
+        const int sp = L.src[p];
+        S[o + (p - p0)] = (sp >= 0) ? d.J[sp] : 0.0;
+      }
+    }
+    __syncthreads();
+  }
+  for (int lv = lv0; lv < lv1; ++lv) {
     const int a = F.f_lptr[lv], b = F.f_lptr[lv + 1];
     const int2 sp = F.f_split[lv];
     for (int t = a + tid; t < sp.x; t += nth) {
       const int j = F.f_items[t];
-      if (factor_active(L, d.cs, 1, j)) factor_column_t<double>(L, d.J, j, d.cs, 1, pivot_tol, nullptr);
+      if (factor_active(L, d.cs, 1, j)) factor_column_t<double>(L, d.J, j, d.cs, 1, pivot_tol, S, soff, umeta);
     }
     for (int t = sp.x + warp; t < sp.y; t += nwarps) {
       const int j = F.f_items[t];
-      if (factor_active(L, d.cs, 1, j)) factor_column<false, double>(L, d.J, j, d.cs, 1, pivot_tol, sm);
+      if (!factor_active(L, d.cs, 1, j)) continue;
+      if (S) factor_column_s<false, double>(L, j, d.cs, 1, pivot_tol, sm, S, soff, umeta);
+      else factor_column<false, double>(L, d.J, j, d.cs, 1, pivot_tol, sm);
     }
     // the thread and warp columns are done, and a breakdown they flagged is
     // visible to every thread: the tests below read the same values in all
@@ -1371,9 +1387,18 @@ __device__ void resident_factor(const DevArrays &d, const LUDev &L, const FusedD
     for (int t = sp.y; t < b; ++t) {
       const int j = F.f_items[t];
       if (!factor_active(L, d.cs, 1, j)) continue;
-      factor_column<true, double>(L, d.J, j, d.cs, 1, pivot_tol, sm);
+      if (S) factor_column_s<true, double>(L, j, d.cs, 1, pivot_tol, sm, S, soff, umeta);
+      else factor_column<true, double>(L, d.J, j, d.cs, 1, pivot_tol, sm);
       __syncthreads();
     }
+  }
+  if (S) {
+    // the factored columns back to global memory (the solves read them there)
+    for (int t = F.f_lptr[lv0] + warp; t < F.f_lptr[lv1]; t += nwarps) {
+      const int j = F.f_items[t], p0 = L.cp[j], p1 = L.cp[j + 1], o = F.c_soff[j];
+      for (int p = p0 + lane; p < p1; p += 32) L.lu[p] = S[o + (p - p0)];
+    }
+    __syncthreads();
   }
 }
 
@@ -1457,7 +1482,7 @@ __device__ void resident_solve(const DevArrays &d, const LUDev &L, const FusedDe
 // Ticks of circuit c until it stops being active (paused, done, failed, or
 // parked on a pivot breakdown for the host).
 __device__ void resident_circuit(const DevArrays &d, const LUDev &L, const FusedDev &F, const FusedArgs &A, int c,
-                                 double *vm, double *vs, double *ws, double *sm) {
+                                 double *vm, double *vs, double *ws, double *sm, double *S) {
   const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
   const int o0 = d.offsets[c], o1 = d.offsets[c + 1];
   const int e0 = d.rp[o0], e1 = d.rp[o1];
@@ -1496,7 +1521,7 @@ __device__ void resident_circuit(const DevArrays &d, const LUDev &L, const Fused
     if (warp == 0) newton_ctl_circuit(d, c, lane);
     __syncthreads();
     if (s.need_solve && !s.singular) {  // uniform
-      if (s.refactor) resident_factor(d, L, F, c, A.pivot_tol, sm);
+      if (s.refactor) resident_factor(d, L, F, c, A.pivot_tol, sm, S);
       if (!s.singular) resident_solve(d, L, F, c, sm);  // uniform: read after the factor's last barrier
     }
     __syncthreads();
@@ -1523,19 +1548,24 @@ __device__ void resident_circuit(const DevArrays &d, const LUDev &L, const Fused
   }
 }
 
-// CTAs take circuits from the queue (F.order: largest first) until it is empty.
-__global__ void __launch_bounds__(kFusedThreads, 4) k_resident(DevArrays d, LUDev L, FusedDev F, FusedArgs A) {
+// CTAs take circuits from the queue (F.order: largest first) until it is
+// empty.  THREADS per CTA, as many CTAs per SM as 128 registers a thread
+// allow; every CTA size computes the same bits.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS, 512 / THREADS > 16 ? 16 : 512 / THREADS) k_resident(DevArrays d, LUDev L,
+                                                                                          FusedDev F, FusedArgs A) {
   extern __shared__ __align__(16) double fz_rows[];
   __shared__ double ws[8 * 4], sm[32];
   __shared__ int next;
   double *vm = fz_rows, *vs = fz_rows + F.max_rows;
+  double *S = F.max_fbuf > 0 ? fz_rows + 2 * F.max_rows : nullptr;
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) next = atomicAdd(F.queue, 1);
     __syncthreads();
     const int q = next;
     if (q >= A.ncirc) return;
-    resident_circuit(d, L, F, A, F.order[q], vm, vs, ws, sm);
+    resident_circuit(d, L, F, A, F.order[q], vm, vs, ws, sm, S);
   }
 }
 
@@ -1543,21 +1573,33 @@ __global__ void __launch_bounds__(kFusedThreads, 4) k_resident(DevArrays d, LUDe
 // Launchers.
 static inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
 
-int resident_prepare_k(int max_rows, int device, int *grid) {
-  const size_t smem = 2 * sizeof(double) * (size_t)max_rows;
-  if (cudaFuncSetAttribute(k_resident, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+template <int THREADS>
+static int resident_grid(size_t smem, int sms, int *grid) {
+  if (cudaFuncSetAttribute(k_resident<THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
     return XG_ERR_CUDA;
-  int per_sm = 0, sms = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resident, kFusedThreads, smem) != cudaSuccess ||
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || per_sm < 1)
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resident<THREADS>, THREADS, smem) != cudaSuccess ||
+      per_sm < 1)
     return XG_ERR_CUDA;
   *grid = per_sm * sms;
   return XG_OK;
 }
 
-void launch_resident_k(cudaStream_t st, const DevArrays &d, const LUDev &L, const FusedDev &F, int ncirc, int nm,
-                       int nd, int nv, int sto_base_m, const int *slots, const double *bps, const int *bp_ptr,
-                       int cap, int pmax, double pivot_tol) {
+// Persistent grids of the CTA sizes kResidentThreads (32, 64, 128).
+int resident_prepare_k(int max_rows, int max_fbuf, int device, int *grid) {
+  const size_t smem = sizeof(double) * (2 * (size_t)max_rows + (size_t)max_fbuf);
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return XG_ERR_CUDA;
+  int rc = resident_grid<32>(smem, sms, &grid[0]);
+  if (rc == XG_OK) rc = resident_grid<64>(smem, sms, &grid[1]);
+  if (rc == XG_OK) rc = resident_grid<128>(smem, sms, &grid[2]);
+  return rc;
+}
+
+void launch_resident_k(cudaStream_t st, const DevArrays &d, const LUDev &L, const FusedDev &F, int threads,
+                       int ncirc, int nm, int nd, int nv, int sto_base_m, const int *slots, const double *bps,
+                       const int *bp_ptr, int cap, int pmax, double pivot_tol) {
   FusedArgs A;
   A.ncirc = ncirc; A.nm = nm; A.nd = nd; A.nv = nv; A.sto_base_m = sto_base_m;
   A.sF_m = slots[0]; A.sQ_m = slots[1]; A.sL_m = slots[2]; A.sM_m = slots[3];
@@ -1565,8 +1607,10 @@ void launch_resident_k(cudaStream_t st, const DevArrays &d, const LUDev &L, cons
   A.bps = bps; A.bp_ptr = bp_ptr; A.cap = cap; A.pmax = pmax; A.pivot_tol = pivot_tol;
   cudaMemsetAsync(F.queue, 0, sizeof(int), st);
   cudaMemsetAsync(F.ticks, 0, 2 * sizeof(unsigned long long), st);
-  const size_t smem = 2 * sizeof(double) * (size_t)F.max_rows;
-  k_resident<<<std::min(F.grid, ncirc), kFusedThreads, smem, st>>>(d, L, F, A);
+  const size_t smem = sizeof(double) * (2 * (size_t)F.max_rows + (size_t)F.max_fbuf);
+  if (threads == 32) k_resident<32><<<std::min(F.grid[0], ncirc), 32, smem, st>>>(d, L, F, A);
+  else if (threads == 64) k_resident<64><<<std::min(F.grid[1], ncirc), 64, smem, st>>>(d, L, F, A);
+  else k_resident<128><<<std::min(F.grid[2], ncirc), 128, smem, st>>>(d, L, F, A);
 }
 
 void launch_sources_k(cudaStream_t st, const DevArrays &d, int n_v, int n_src, int use_explicit,

@@ -65,7 +65,7 @@ __device__ void factor_group(const LUDev &L, const double *__restrict__ vals, Ci
     for (int t = b + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
       const int j = S.items[t];
       if (S.is_thread[j] && factor_active(L, cs, masked, j))
-        factor_column_t<T>(L, vals, j, cs, masked, pivot_tol, nullptr);
+        factor_column_t<T>(L, vals, j, cs, masked, pivot_tol, nullptr, L.grp_soff, L.umeta);
     }
     for (int t = b + warp; t < e; t += nwarps) {
       const int j = S.items[t];
@@ -256,38 +256,6 @@ __global__ void __launch_bounds__(256) k_toplv_update(LUDev L, int lv, CircState
 // memory (the dependent chain of each update step reads U(k, j) and scatters
 // into column j at shared-memory latency), and written back once.  L columns
 // of hubs (outside every group) are read from global memory.
-template <bool BLOCK, typename T>
-__device__ void factor_column_s(const LUDev &L, int j, CircState *cs, int masked, double pivot_tol, double *sm,
-                                T *S) {
-  const int lane = BLOCK ? (int)threadIdx.x : (int)(threadIdx.x & 31);
-  const int nl = BLOCK ? (int)blockDim.x : 32;
-  const int p0 = L.cp[j], p1 = L.cp[j + 1], pd = L.diag[j];
-  T *cj = S + L.grp_soff[j];  // cj[p - p0]
-  const T *glu = lu_of<T>(L);
-  bool lost = false;
-  for (int p = p0; p < pd; ++p) {
-    const int4 um = L.umeta[p];
-    const T ukj = cj[p - p0];
-    if (nz(ukj)) {
-      const T *lk = (um.x >= 0) ? S + um.x : glu + um.w;
-      const int *tgt = L.upd_pos + um.z;
-      for (int q = lane; q < um.y; q += nl) {
-        const int pos = tgt[q];
-        if (pos > p && pos < p1) cj[pos - p0] -= lk[q] * ukj;
-        else lost = true;
-      }
-    }
-    team_sync<BLOCK>();
-  }
-  unsigned long long ak = 0;
-  for (int p = pd + lane; p < p1; p += nl) ak = umax64(ak, mag_key(cj[p - p0]));
-  ak = team_max_key<BLOCK>(ak, sm);
-  lost = team_any<BLOCK>(lost);
-  if (!pivot_ok(L, j, cs, masked, pivot_tol, (double)cj[pd - p0], key_value<T>(ak), lost, lane == 0)) return;
-  const T inv = (T)1 / cj[pd - p0];
-  for (int p = pd + 1 + lane; p < p1; p += nl) cj[p - p0] *= inv;
-}
-
 // A column of a group whose update metadata is staged too (mcol: the
 // group's column records, ment: their U entries, mtg: update targets; all
 // in shared memory).  TEAM lanes (1 = a thread per column, 32 = a warp).
@@ -396,19 +364,19 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
       for (int t = b + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
         const int j = SD.items[t];
         if (SD.is_thread[j] && factor_active(L, cs, masked, j))
-          factor_column_t<T>(L, vals, j, cs, masked, pivot_tol, S);
+          factor_column_t<T>(L, vals, j, cs, masked, pivot_tol, S, L.grp_soff, L.umeta);
       }
       for (int t = b + warp; t < e; t += nwarps) {
         const int j = SD.items[t];
         if (SD.is_long[j]) { any_long = true; continue; }
         if (SD.is_thread[j] || !factor_active(L, cs, masked, j)) continue;
-        factor_column_s<false, T>(L, j, cs, masked, pivot_tol, sm, S);
+        factor_column_s<false, T>(L, j, cs, masked, pivot_tol, sm, S, L.grp_soff, L.umeta);
       }
       if (__syncthreads_or(any_long)) {
         for (int t = b; t < e; ++t) {
           const int j = SD.items[t];
           if (!SD.is_long[j] || !factor_active(L, cs, masked, j)) continue;
-          factor_column_s<true, T>(L, j, cs, masked, pivot_tol, sm, S);
+          factor_column_s<true, T>(L, j, cs, masked, pivot_tol, sm, S, L.grp_soff, L.umeta);
           __syncthreads();
         }
       }

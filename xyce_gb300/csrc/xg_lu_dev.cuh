@@ -172,14 +172,16 @@ __device__ void factor_column(const LUDev &L, const double *__restrict__ vals, i
   for (int p = pd + 1 + lane; p < p1; p += nl) lu[p] *= inv;
 }
 
-// A short column on one thread.  S: the group's shared-memory buffer (column
-// k at S[grp_soff[k]]), or nullptr to factor in place in global memory.
+// A short column on one thread.  S: a shared-memory buffer of staged
+// columns (column k at S[soff[k]]; umeta[p].x the buffer offset of
+// L(k+1.., k), as LUDev::umeta), or nullptr to factor in place in global
+// memory.
 template <typename T>
 __device__ void factor_column_t(const LUDev &L, const double *__restrict__ vals, int j, CircState *cs,
-                                int masked, double pivot_tol, T *S) {
+                                int masked, double pivot_tol, T *S, const int *soff, const int4 *umeta) {
   const int p0 = L.cp[j], p1 = L.cp[j + 1], pd = L.diag[j];
   T *glu = lu_of<T>(L);
-  T *cj = S ? S + L.grp_soff[j] : glu + p0;  // cj[p - p0]
+  T *cj = S ? S + soff[j] : glu + p0;  // cj[p - p0]
   if (!S)
     for (int p = p0; p < p1; ++p) {
       const int s = L.src[p];
@@ -187,7 +189,7 @@ __device__ void factor_column_t(const LUDev &L, const double *__restrict__ vals,
     }
   bool lost = false;
   for (int p = p0; p < pd; ++p) {
-    const int4 um = L.umeta[p];
+    const int4 um = umeta[p];
     const T ukj = cj[p - p0];
     if (!nz(ukj)) continue;
     const T *lk = (S && um.x >= 0) ? S + um.x : glu + um.w;
@@ -214,6 +216,41 @@ __device__ void factor_column_t(const LUDev &L, const double *__restrict__ vals,
   if (!pivot_ok(L, j, cs, masked, pivot_tol, (double)cj[pd - p0], key_value<T>(ak), lost, true)) return;
   const T inv = (T)1 / cj[pd - p0];
   for (int p = pd + 1; p < p1; ++p) cj[p - p0] *= inv;
+}
+
+// A column in a shared-memory buffer of staged columns (see
+// factor_column_t), by a warp (BLOCK false) or the whole CTA.  L columns of
+// columns outside the buffer (umeta[p].x < 0) are read from global memory.
+template <bool BLOCK, typename T>
+__device__ void factor_column_s(const LUDev &L, int j, CircState *cs, int masked, double pivot_tol, double *sm,
+                                T *S, const int *soff, const int4 *umeta) {
+  const int lane = BLOCK ? (int)threadIdx.x : (int)(threadIdx.x & 31);
+  const int nl = BLOCK ? (int)blockDim.x : 32;
+  const int p0 = L.cp[j], p1 = L.cp[j + 1], pd = L.diag[j];
+  T *cj = S + soff[j];  // cj[p - p0]
+  const T *glu = lu_of<T>(L);
+  bool lost = false;
+  for (int p = p0; p < pd; ++p) {
+    const int4 um = umeta[p];
+    const T ukj = cj[p - p0];
+    if (nz(ukj)) {
+      const T *lk = (um.x >= 0) ? S + um.x : glu + um.w;
+      const int *tgt = L.upd_pos + um.z;
+      for (int q = lane; q < um.y; q += nl) {
+        const int pos = tgt[q];
+        if (pos > p && pos < p1) cj[pos - p0] -= lk[q] * ukj;
+        else lost = true;
+      }
+    }
+    team_sync<BLOCK>();
+  }
+  unsigned long long ak = 0;
+  for (int p = pd + lane; p < p1; p += nl) ak = umax64(ak, mag_key(cj[p - p0]));
+  ak = team_max_key<BLOCK>(ak, sm);
+  lost = team_any<BLOCK>(lost);
+  if (!pivot_ok(L, j, cs, masked, pivot_tol, (double)cj[pd - p0], key_value<T>(ak), lost, lane == 0)) return;
+  const T inv = (T)1 / cj[pd - p0];
+  for (int p = pd + 1 + lane; p < p1; p += nl) cj[p - p0] *= inv;
 }
 
 // Dot product of a long row (more than kLongSolveRow entries) by the whole
