@@ -419,10 +419,12 @@ def run_ours(args):
     if args.ncu_case:
         # the profiling case: operating point, first analysis and one window
         circ = xg.Circuit(nl, device=dev)
+        circ.tran_set_form(xg.FORM_RESIDENT if args.ncu_form == "resident" else xg.FORM_TICK_GRAPH)
         circ.tran_start(probes=probes, cap=16)
         circ.tran_advance(window)
         torch.cuda.synchronize()
-        print(json.dumps({"ncu_case": desc["workload"], "instances": len(nl.mos1)}), flush=True)
+        print(json.dumps({"ncu_case": desc["workload"], "form": args.ncu_form, "instances": len(nl.mos1)}),
+              flush=True)
         circ.close()
         return
     sample = _sample(nl, args.workload)
@@ -433,8 +435,9 @@ def run_ours(args):
     sampler = _clock_sampler(clk_path)
     if world > 1:
         torch.distributed.barrier()
+    main_form = {"auto": xg.FORM_AUTO, "tick_graph": xg.FORM_TICK_GRAPH, "resident": xg.FORM_RESIDENT}[args.form]
     circ, ms_total, st0, st1 = _timed_windows(xg, nl, rec_probes, dev, args, window, xg.PREC_FP64, flush,
-                                              stream_of, cap=cap)
+                                              stream_of, cap=cap, form=main_form)
     if sampler:
         sampler.terminate()
         sampler.wait()
@@ -501,12 +504,19 @@ def run_ours(args):
                          (s1["newton_iters"] - s0["newton_iters"]) / max(1, s1["accepted"] - s0["accepted"])}
             c2.tran_end()
             c2.close()
-            # the tick graph (16 kernels per tick over the whole batch) instead of the resident form
+            # the tick graph alone (15 kernels per tick over the whole batch)
             c5, ms5, s0, s1 = _timed_windows(xg, nl, probes, dev, args, window, xg.PREC_FP64, flush, stream_of,
                                              form=xg.FORM_TICK_GRAPH)
             forms["fp64_tick_graph"] = (s1["accepted"] - s0["accepted"]) / (ms5 / 1e3)
             c5.tran_end()
             c5.close()
+            if st1["option"] == 3 and form == "tick_graph" and any(st1["option_us_per_iter"][:3]):
+                # the timed trials chose the tick graph: the resident form alone, for comparison
+                c6, ms6, s0, s1 = _timed_windows(xg, nl, probes, dev, args, window, xg.PREC_FP64, flush,
+                                                 stream_of, form=xg.FORM_RESIDENT)
+                forms["fp64_resident"] = (s1["accepted"] - s0["accepted"]) / (ms6 / 1e3)
+                c6.tran_end()
+                c6.close()
             # the LU sweeps with the analysis' closed-form launch shapes instead of the timed ones
             c4, ms4, s0, s1 = _timed_windows(xg, nl, probes, dev, args, window, xg.PREC_FP64, flush, stream_of,
                                              tune=xg.TUNE_MODEL, form=xg.FORM_TICK_GRAPH)
@@ -560,6 +570,8 @@ def run_ours(args):
                 "device_evals_per_s": evals_all / (ms_max / 1e3),
                 "newton_iters_per_step": (st1["newton_iters"] - st0["newton_iters"]) / max(1, steps_done),
                 "form": form, "ticks": ticks, "kernels_per_tick": kernels_per_tick, "gpu_launches": gpu_launches,
+                "form_trials_us_per_newton_iter": dict(zip(("resident_32", "resident_64", "resident_128",
+                                                            "tick_graph"), st1["option_us_per_iter"])),
                 "lu": info, "roofline": roof, "roofline_lu": lu_roof, "roofline_resident": resident_roof,
                 "tick_stages_us": stages,
                 "max_err_vs_fp64": err, "forms": forms, "cpu_baseline": cpu, "e2e": e2e,
@@ -581,6 +593,10 @@ def main():
     ap.add_argument("--no-cpu", dest="cpu", action="store_false", help="skip the CPU baseline")
     ap.add_argument("--ncu-case", action="store_true",
                     help="only the operating point and one window (the case the ncu captures profile)")
+    ap.add_argument("--form", default="auto", choices=["auto", "tick_graph", "resident"],
+                    help="advancing form of the timed run (auto: timed choice on the run itself)")
+    ap.add_argument("--ncu-form", default="tick_graph", choices=["tick_graph", "resident"],
+                    help="advancing form of the --ncu-case run")
     ap.add_argument("--no-forms", dest="forms", action="store_false", help="skip the FP32-IR form")
     ap.add_argument("--clocks-csv", default=None,
                     help="keep the nvidia-smi clock samples of the timed region in this file")

@@ -332,11 +332,15 @@ typedef struct xg_tran_stats {
   long long kernel_launches;                   /* kernels launched while advancing */
   long long circuit_ticks;                     /* resident form: Newton iterations summed over circuits */
   long long factor_skips;                      /* refactorizations skipped (xg_lu_set_reuse) */
-  int resident_threads;                        /* resident form: CTA size the timed trials chose (0: not yet) */
+  int resident_threads;                        /* resident form: CTA size of its last launch (0: none) */
+  int option;                                  /* advancing option the timed trials chose (-1: not yet):
+                                                  0..2 resident with 32/64/128-thread CTAs, 3 tick graph */
+  double option_us_per_iter[4];                /* device time per circuit Newton iteration of each timed
+                                                  option, microseconds (0: not timed) */
 } xg_tran_stats;
 
 /* How a transient advances.  XG_FORM_TICK_GRAPH: a tick (one Newton
- * iteration of every active circuit, 16 kernels) is a captured CUDA graph,
+ * iteration of every active circuit, 15 kernels) is a captured CUDA graph,
  * replayed in batches between host synchronizations.  XG_FORM_RESIDENT:
  * one kernel runs every stage of every tick for a whole batch — each CTA
  * takes a circuit and iterates its ticks until the circuit pauses,
@@ -345,8 +349,12 @@ typedef struct xg_tran_stats {
  * grid-wide barrier.  Both compute the same bits.  The resident form needs
  * a batch of at least 64 circuits of at most 2,048 unknowns each, MOSFET-1
  * and diode devices only, FP64 factors, the polynomial predictor and an LU
- * analysis without a top; XG_FORM_AUTO (default) takes it when the batch
- * admits it.  No reference counterpart (Xyce runs one circuit per process).
+ * analysis without a top.  XG_FORM_AUTO (default): when the batch admits
+ * the resident form, the first advances after the operating point time
+ * each option (the tick graph over one advance, then the resident kernel
+ * with 64-, 128- and 32-thread CTAs, one launch each) and the rest of the
+ * run keeps the one with the shortest device time per circuit Newton
+ * iteration; XG_FORM_RESIDENT times the three CTA sizes only.  No reference counterpart (Xyce runs one circuit per process).
  * Not allowed while a transient is in progress. */
 #define XG_FORM_AUTO        0
 #define XG_FORM_TICK_GRAPH  1

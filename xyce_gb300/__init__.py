@@ -94,7 +94,15 @@ class TranStats(C.Structure):
                 ("n_analyze", C.c_int), ("t_final_min", C.c_double),
                 ("t_final_max", C.c_double), ("seconds", C.c_double), ("kernels_per_tick", C.c_int),
                 ("form", C.c_int), ("kernel_launches", C.c_longlong), ("circuit_ticks", C.c_longlong),
-                ("factor_skips", C.c_longlong), ("resident_threads", C.c_int)]
+                ("factor_skips", C.c_longlong), ("resident_threads", C.c_int),
+                ("option", C.c_int), ("option_us_per_iter", C.c_double * 4)]
+
+    def as_dict(self):
+        out = {}
+        for f, _ in self._fields_:
+            v = getattr(self, f)
+            out[f] = list(v) if isinstance(v, C.Array) else v
+        return out
 
 
 _lib = None
@@ -387,7 +395,7 @@ class Circuit:
         values = np.zeros(max(1, nc * cap * pmax))
         st = TranStats()
         self._check(lib().xg_tran_results(self.h, counts, times, values, C.byref(st)))
-        stats = {f: getattr(st, f) for f, _ in TranStats._fields_}
+        stats = st.as_dict()
         if cap:
             times = times[: nc * cap].reshape(nc, cap)
             values = values[: nc * cap * pmax].reshape(nc, cap, pmax)
@@ -480,7 +488,7 @@ class Circuit:
         st = TranStats()
         self._check(lib().xg_transient(self.h, C.byref(tp), len(probes), probes, int(cap), counts,
                                        times, values, C.byref(st)))
-        stats = {f: getattr(st, f) for f, _ in TranStats._fields_}
+        stats = st.as_dict()
         if cap:
             times = times[: nc * cap].reshape(nc, cap)
             values = values[: nc * cap * pmax].reshape(nc, cap, pmax)

@@ -79,7 +79,7 @@ struct xg_ctx {
   int mlp_adam_t = 0;
   std::vector<void *> allocs;      // device allocations owned by the context
   std::vector<void *> lu_allocs;   // allocations of the current LU analysis
-  int *status_host = nullptr;      // mapped [finished, breakdown]
+  int *status_host = nullptr;      // mapped [finished, breakdown, Newton iterations (64-bit)]
   int *status_dev = nullptr;
   int *breakdown_dev = nullptr;
 };
@@ -1537,13 +1537,26 @@ struct TranRun {
   long long circuit_ticks = 0;    // Newton iterations run by the resident tick, summed over circuits
   long long kernel_launches = 0;  // kernels launched while advancing
   unsigned long long tick_count[2] = {0, 0};
-  // CTA size of the resident kernel: the first launches try each of
-  // kResidentThreads (the same bits with every size) and the one with the
-  // shortest device time per circuit-tick is kept
-  int res_threads = 0;
-  double res_trial[3] = {-1.0, -1.0, -1.0};
-  int res_pending = -1;
+  // How the run advances.  Options 0..2: the resident kernel with CTAs of
+  // kResidentThreads[k]; option 3: the tick graph.  Every option gives the
+  // same bits, so the first launches of the transient (not of the operating
+  // point) try each admitted option (the resident sizes when the form is
+  // XG_FORM_RESIDENT, all four under XG_FORM_AUTO) and the one with the
+  // shortest device time per circuit Newton iteration is kept.  A resident
+  // trial is one launch; a tick-graph trial runs the graph until the run
+  // goes idle.
+  static constexpr int kOptions = 4, kGraphOption = 3;
+  int option = -1;                        // chosen option (-1: trials not over)
+  double opt_ms[kOptions] = {0, 0, 0, 0};
+  double opt_iters[kOptions] = {0, 0, 0, 0};
+  bool opt_done[kOptions] = {false, false, false, false};
+  int pending = -1;                       // option timed between res_ev[0] and res_ev[1]
+  unsigned long long pending_iters0 = 0;  // Newton iterations before it
   cudaEvent_t res_ev[2] = {nullptr, nullptr};
+  int res_threads = 0;                    // CTA size of the last resident launch
+  long long graph_trial_ticks = 0;        // ticks of the tick-graph trial so far
+  bool try_resident = false, try_graph = true;
+  bool operating_point = false;           // xg_tran_start's run to the operating point: no trials
   std::chrono::steady_clock::time_point t0;
   ~TranRun() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -1601,7 +1614,6 @@ int capture(TranRun &R) {
   CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
   launch_front(R);
   launch_back(R);
-  launch_count_done_k(ctx->stream, ctx->d, ctx->ncirc, ctx->breakdown_dev, ctx->status_dev);
   CK(cudaStreamEndCapture(ctx->stream, &g));
   // kernels of one tick (every node of the captured tick is a kernel launch
   // unless the query says otherwise)
@@ -1677,6 +1689,7 @@ int run_until_idle(TranRun &R) {
       if ((rc = stalled_circuits(ctx, refresh))) return rc;
       if ((rc = lu_analyze_from_device(ctx, d.J, refresh.empty() ? nullptr : &refresh))) return rc;
       R.pivot_tol = (consecutive >= 2) ? 0.0 : ctx->pivot_tol;
+      R.pending = -1;  // a timed launch that parked on a breakdown is not a trial
       if ((rc = capture(R))) return rc;
       launch_unstall_k(ctx->stream, d, ctx->ncirc);
       launch_back(R);
@@ -1690,18 +1703,27 @@ int run_until_idle(TranRun &R) {
       if ((rc = capture(R))) return rc;
     }
     consecutive = 0;
-    if (R.res_pending >= 0) {
+    const unsigned long long iters_now = reinterpret_cast<volatile unsigned long long *>(st)[1];
+    if (R.pending >= 0) {
+      // one timed trial launch (or tick-graph batch) ended
       float ms = 0.f;
-      if (R.tick_count[1] > 0 && cudaEventElapsedTime(&ms, R.res_ev[0], R.res_ev[1]) == cudaSuccess) {
-        R.res_trial[R.res_pending] = ms / (double)R.tick_count[1];
-        if (R.res_trial[0] >= 0 && R.res_trial[1] >= 0 && R.res_trial[2] >= 0) {
-          int best = 0;
-          for (int k = 1; k < 3; ++k)
-            if (R.res_trial[k] < R.res_trial[best]) best = k;
-          R.res_threads = kResidentThreads[best];
-        }
+      if (cudaEventElapsedTime(&ms, R.res_ev[0], R.res_ev[1]) == cudaSuccess) {
+        R.opt_ms[R.pending] += ms;
+        R.opt_iters[R.pending] += (double)(iters_now - R.pending_iters0);
       }
-      R.res_pending = -1;
+      const bool idle = finished >= ctx->ncirc;
+      if ((R.pending != TranRun::kGraphOption || idle || R.graph_trial_ticks >= kFusedMaxTicks) &&
+          R.opt_iters[R.pending] > 0)
+        R.opt_done[R.pending] = true;
+      R.pending = -1;
+      bool all = true;
+      int best = -1;
+      for (int k = 0; k < TranRun::kOptions; ++k) {
+        if (!(k == TranRun::kGraphOption ? R.try_graph : R.try_resident)) continue;
+        if (!R.opt_done[k]) { all = false; break; }
+        if (best < 0 || R.opt_ms[k] / R.opt_iters[k] < R.opt_ms[best] / R.opt_iters[best]) best = k;
+      }
+      if (all && best >= 0) R.option = best;
     }
     if (R.tick_count[0]) {
       // the last resident launch: its longest circuit's ticks, and all of them
@@ -1711,20 +1733,39 @@ int run_until_idle(TranRun &R) {
     }
     if (finished >= ctx->ncirc) return XG_OK;
     if (R.ticks > max_ticks) return fail(ctx, XG_ERR_TIMEOUT, "transient exceeded the tick limit");
-    if (R.resident && ctx->resident_ok) {
+    int opt = R.option;
+    bool trial = false;
+    if (opt < 0 && R.operating_point) {
+      // the operating point's Newton iterations are not the transient's:
+      // the trials wait for the first advance
+      opt = R.try_graph ? TranRun::kGraphOption : 1;
+    } else if (opt < 0) {
+      // the next option not yet timed: the tick graph first, then the
+      // resident CTA sizes from the one that usually wins
+      static constexpr int kTrialOrder[TranRun::kOptions] = {TranRun::kGraphOption, 1, 2, 0};
+      for (int q = 0; q < TranRun::kOptions && opt < 0; ++q) {
+        const int k = kTrialOrder[q];
+        if ((k == TranRun::kGraphOption ? R.try_graph : R.try_resident) && !R.opt_done[k]) opt = k;
+      }
+      trial = opt >= 0;
+      if (opt < 0) opt = TranRun::kGraphOption;
+    }
+    if (opt != TranRun::kGraphOption && !ctx->resident_ok) { opt = TranRun::kGraphOption; trial = false; }
+    if (trial) {
+      for (cudaEvent_t &e : R.res_ev)
+        if (!e) CK(cudaEventCreate(&e));
+      R.pending = opt;
+      R.pending_iters0 = iters_now;
+      CK(cudaEventRecord(R.res_ev[0], ctx->stream));
+    }
+    R.resident = opt != TranRun::kGraphOption;
+    if (R.resident) {
       // every circuit runs its ticks in one CTA until it pauses, finishes,
       // fails or parks on a pivot breakdown
-      int threads = R.res_threads;
-      if (!threads) {
-        R.res_pending = R.res_trial[0] < 0 ? 0 : (R.res_trial[1] < 0 ? 1 : 2);
-        threads = kResidentThreads[R.res_pending];
-        for (cudaEvent_t &e : R.res_ev)
-          if (!e) CK(cudaEventCreate(&e));
-        CK(cudaEventRecord(R.res_ev[0], ctx->stream));
-      }
-      launch_resident_k(ctx->stream, d, ctx->L, ctx->F, threads, ctx->ncirc, ctx->nm, ctx->nd, ctx->nv,
+      R.res_threads = kResidentThreads[opt];
+      launch_resident_k(ctx->stream, d, ctx->L, ctx->F, R.res_threads, ctx->ncirc, ctx->nm, ctx->nd, ctx->nv,
                         ctx->sto_base_m, ctx->resident_slots, R.bps, R.bp_ptr, R.cap, R.pmax, R.pivot_tol);
-      if (R.res_pending >= 0) CK(cudaEventRecord(R.res_ev[1], ctx->stream));
+      if (trial) CK(cudaEventRecord(R.res_ev[1], ctx->stream));
       launch_count_done_k(ctx->stream, d, ctx->ncirc, ctx->breakdown_dev, ctx->status_dev);
       CK(cudaGetLastError());
       CK(cudaMemcpyAsync(R.tick_count, ctx->F.ticks, sizeof R.tick_count, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1732,8 +1773,15 @@ int run_until_idle(TranRun &R) {
       continue;
     }
     for (int k = 0; k < R.batch; ++k) CK(cudaGraphLaunch(R.exec, ctx->stream));
+    // what the host reads between batches (the tick graph itself does not count)
+    launch_count_done_k(ctx->stream, d, ctx->ncirc, ctx->breakdown_dev, ctx->status_dev);
+    CK(cudaGetLastError());
+    if (trial) {
+      CK(cudaEventRecord(R.res_ev[1], ctx->stream));
+      R.graph_trial_ticks += R.batch;
+    }
     R.ticks += R.batch;
-    R.kernel_launches += (long long)R.batch * R.kernels_per_tick;
+    R.kernel_launches += (long long)R.batch * R.kernels_per_tick + 1;
     if (R.batch < 64) R.batch *= 2;
   }
 }
@@ -1871,12 +1919,17 @@ static int tran_start_run(xg_ctx *ctx, const xg_tran_params *p, const std::vecto
     return fail(ctx, XG_ERR_UNSUPPORTED,
                 "circuit-resident tick: needs >= 64 circuits of <= 2048 unknowns, MOSFET-1 / diode devices, "
                 "FP64 factors, the polynomial predictor and an LU without a top");
-  R.resident = ctx->resident_ok && ctx->form != XG_FORM_TICK_GRAPH;
+  R.try_resident = ctx->resident_ok && ctx->form != XG_FORM_TICK_GRAPH;
+  R.try_graph = ctx->form != XG_FORM_RESIDENT;
+  R.resident = R.try_resident;
   if ((rc = capture(R))) return rc;
   launch_back(R);
   launch_count_done_k(ctx->stream, d, ncirc, ctx->breakdown_dev, ctx->status_dev);
   CK(cudaGetLastError());
-  return run_until_idle(R);
+  R.operating_point = true;
+  rc = run_until_idle(R);
+  R.operating_point = false;
+  return rc;
 }
 
 extern "C" int xg_tran_set_form(xg_ctx *ctx, int form) {
@@ -1944,6 +1997,9 @@ extern "C" int xg_tran_results(xg_ctx *ctx, int *counts, double *times, double *
     stats->kernel_launches = R.kernel_launches;
     stats->circuit_ticks = R.circuit_ticks;
     stats->resident_threads = R.res_threads;
+    stats->option = R.option;
+    for (int k = 0; k < TranRun::kOptions; ++k)
+      stats->option_us_per_iter[k] = R.opt_iters[k] > 0 ? 1e3 * R.opt_ms[k] / R.opt_iters[k] : 0.0;
     stats->device_evals = evals;
     stats->n_analyze = ctx->n_analyze;
     stats->status = status;
@@ -2030,8 +2086,9 @@ extern "C" int xg_tran_profile(xg_ctx *ctx, int n_steps, int n_ticks, double *st
     if (c->predictor == XG_PRED_LEARNED) launch_ml_predict_k(st, d, c->n, c->ncirc, 1);
     cudaEventRecord(ev[s++], st);
     launch_state_commit_k(st, d, c->nm, c->nd, c->sto_base_m, c->nb, c->sto_base_b, c->sta_base_b);
-    launch_count_done_k(st, d, c->ncirc, c->breakdown_dev, c->status_dev);
     cudaEventRecord(ev[s++], st);
+    // the completion count runs once per batch of ticks, outside the tick
+    launch_count_done_k(st, d, c->ncirc, c->breakdown_dev, c->status_dev);
     if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) { rc = XG_ERR_CUDA; break; }
     for (int k = 0; k < XG_STAGE_COUNT; ++k) {
       float ms = 0.f;

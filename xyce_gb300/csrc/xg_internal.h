@@ -80,6 +80,8 @@ struct TranParams {
   int reuse_factors;  // skip bit-identical refactorizations (xg_lu_set_reuse)
 };
 
+constexpr double kGmin = 1.0e-12;  // DeviceOptions gmin default
+
 // MOSFET level-1 model-level (effective model) parameters after temperature
 // and geometry processing (N_DEV_MOSFET1.C:383-470, 3487-3730, 3939-4020).
 struct Mos1Model {
@@ -87,6 +89,9 @@ struct Mos1Model {
   double OxideCap, Cgso, Cgdo, Cgbo, Cbd, Cbdsw, Cbs, Cbssw, tDepCap, tBulkPot, MJ, MJSW;
   double f2d, f3d, f4d, f2s, f3s, f4s, M, gammaSqrtPhi;
   double gsatD, gsatS;  // DrainSatCur / vt, SourceSatCur / vt (reverse-bias conductances)
+  double gbdR, gbsR;    // gsatD + gmin, gsatS + gmin
+  double sqrtPhi;       // sqrt(tPhi)
+  double argPhi;        // gamma / (2 sqrt(tPhi)), 0 when sqrt(tPhi) <= 0
   int has_gate_caps, has_junc_caps;
 };
 

@@ -126,7 +126,7 @@ __device__ __forceinline__ void mos1_eval(const DevArrays &d, int i, int nm, int
   const double dt = m.dtype;
   // dt is +1 or -1: products with it are sign flips, done on the integer pipe
   // (exactly the IEEE product) — the FP64 pipe bounds this kernel on GB300
-  const long long tsgn = (dt < 0.0) ? (long long)0x8000000000000000ULL : 0LL;
+  const long long tsgn = f_lt0(dt) ? (long long)0x8000000000000000ULL : 0LL;
   auto T = [tsgn](double v) { return __longlong_as_double(__double_as_longlong(v) ^ tsgn); };
   const double Beta = __ldg(d.m1_beta + i), tVbi = __ldg(d.m1_vbi + i);
   const double tVto = tVbi + T(m.gammaSqrtPhi);
@@ -149,7 +149,7 @@ __device__ __forceinline__ void mos1_eval(const DevArrays &d, int i, int nm, int
   }
   double vgd_old = vgs_old - vds_old;
   int Check = 1;
-  if (vds_old >= 0) {
+  if (f_ge0(vds_old)) {
     vgs = fetlim_d(vgs, vgs_old, Von);
     vds = vgs - vgd;
     vds = limvds_d(vds, vds_old);
@@ -160,7 +160,7 @@ __device__ __forceinline__ void mos1_eval(const DevArrays &d, int i, int nm, int
     vds = -limvds_d(-vds, -vds_old);
     vgs = vgd + vds;
   }
-  if (vds >= 0.0) {
+  if (f_ge0(vds)) {
     vbs = pnjlim_d(vbs, vbs_old, m.vt, m.sourceVcrit, Check);
     vbd = vbs - vds;
   } else {
@@ -179,44 +179,49 @@ __device__ __forceinline__ void mos1_eval(const DevArrays &d, int i, int nm, int
   const bool origFlag = same(vgs_o, vgs) && same(vds_o, vds) && same(vbs_o, vbs) && same(vbd_o, vbd) &&
                         same(vgd_o, vgd);
   double gbs, cbs, gbd, cbd;
-  if (vbs <= 0) {
-    gbs = m.gsatS + kGmin;
+  if (f_le0(vbs)) {
+    gbs = m.gbsR;
     cbs = gbs * vbs;
   } else {
-    double e = exp(fmin(kMaxExpArg, vbs / m.vt));
+    double e = exp(f_min(kMaxExpArg, vbs / m.vt));
     gbs = m.SourceSatCur * e / m.vt + kGmin;
     cbs = m.SourceSatCur * (e - 1) + kGmin * vbs;
   }
-  if (vbd <= 0) {
-    gbd = m.gsatD + kGmin;
+  if (f_le0(vbd)) {
+    gbd = m.gbdR;
     cbd = gbd * vbd;
   } else {
-    double e = exp(fmin(kMaxExpArg, vbd / m.vt));
+    double e = exp(f_min(kMaxExpArg, vbd / m.vt));
     gbd = m.DrainSatCur * e / m.vt + kGmin;
     cbd = m.DrainSatCur * (e - 1) + kGmin * vbd;
   }
-  const int mode = (vds >= 0) ? 1 : -1;
+  const int mode = f_ge0(vds) ? 1 : -1;
   double cdrain, gm, gds, gmbs, Vdsat;
   {
     double vbx = (mode == 1) ? vbs : vbd;
+    // vbx = 0 (bulk tied to the source, the usual case) takes sqrt(phi) and
+    // gamma / (2 sqrt(phi)) from the model: the same correctly rounded values
+    const bool vbx0 = f_is0(vbx);
     double sarg;
-    if (vbx <= 0) {
+    if (vbx0) {
+      sarg = m.sqrtPhi;
+    } else if (f_le0(vbx)) {
       sarg = sqrt(m.tPhi - vbx);
     } else {
-      sarg = sqrt(m.tPhi);
+      sarg = m.sqrtPhi;
       sarg = sarg - vbx / (sarg + sarg);
-      sarg = fmax(0.0, sarg);
+      sarg = f_max(0.0, sarg);
     }
     Von = T(tVbi) + m.gamma * sarg;
     double vgst = ((mode == 1) ? vgs : vgd) - Von;
-    Vdsat = fmax(vgst, 0.0);
-    double arg = (sarg <= 0) ? 0 : m.gamma / (sarg + sarg);
-    if (vgst <= 0) {
+    Vdsat = f_gt0(vgst) ? vgst : 0.0;
+    if (f_le0(vgst)) {
       cdrain = 0; gm = 0; gds = 0; gmbs = 0;
     } else {
+      const double arg = vbx0 ? m.argPhi : (f_le0(sarg) ? 0.0 : m.gamma / (sarg + sarg));
       double vdsm = (mode == 1) ? vds : -vds;
       double betap = Beta * (1 + m.lambda * vdsm);
-      if (vgst <= vdsm) {
+      if (f_le(vgst, vdsm)) {
         cdrain = betap * vgst * vgst * .5;
         gm = betap * vgst;
         gds = m.lambda * Beta * vgst * vgst * .5;
@@ -273,12 +278,12 @@ __device__ __forceinline__ void mos1_eval(const DevArrays &d, int i, int nm, int
     atomicOr(&d.cs[c].limited, 1);
   }
   const double M = m.M;
-  const bool unitM = (M == 1.0);
+  const bool unitM = f_is1(M);
   // A model without gate or junction capacitance has no charge: its Q
   // vector, charge limiter terms and dQdx stamps are zero and are stored
   // without FP64 arithmetic (as are products with a unit F scale)
   const bool noq = !m.has_gate_caps && !m.has_junc_caps;
-  const bool fs1 = (fs == 1.0);
+  const bool fs1 = f_is1(fs);
   // loadDAEVectors (N_DEV_MOSFET1.C:4343-4576), old Meyer
   const double ceqbs = T(cbs), ceqbd = T(cbd);
   double fv[3] = {-(ceqbd - cdreq), -(ceqbs + cdreq), ceqbs + ceqbd};  // D S B
@@ -1274,20 +1279,29 @@ __global__ void k_state_commit(DevArrays d, int nm, int nd, int sto_base_m, int 
 
 // Number of finished circuits (done or failed) and the LU breakdown flag,
 // into mapped host memory that the host loop reads between tick batches.
+// status_out: [0] circuits done, failed or paused, [1] breakdown flag,
+// [2..3] (one 64-bit word) Newton iterations run so far, summed over circuits.
 __global__ void k_count_done(DevArrays d, int ncirc, const int *breakdown, int *status_out) {
   __shared__ int cnt;
-  if (threadIdx.x == 0) cnt = 0;
+  __shared__ unsigned long long iters;
+  if (threadIdx.x == 0) { cnt = 0; iters = 0; }
   __syncthreads();
   int local = 0;
+  unsigned long long it = 0;
+#pragma unroll 4
   for (int c = threadIdx.x; c < ncirc; c += blockDim.x) {
-    int ph = d.cs[c].phase;
+    const CircState &s = d.cs[c];
+    int ph = s.phase;
     local += (ph == PH_DONE || ph == PH_FAILED || ph == PH_PAUSED) ? 1 : 0;
+    it += (unsigned long long)(s.newton_iters + s.dcop_iters);
   }
   atomicAdd(&cnt, local);
+  atomicAdd(&iters, it);
   __syncthreads();
   if (threadIdx.x == 0) {
     status_out[0] = cnt;
     status_out[1] = *breakdown;
+    reinterpret_cast<unsigned long long *>(status_out)[1] = iters;
   }
 }
 

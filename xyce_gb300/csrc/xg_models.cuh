@@ -11,14 +11,37 @@
 
 namespace xg {
 
-constexpr double kGmin = 1.0e-12;      // DeviceOptions gmin default
 constexpr double kMaxExpArg = 100.0;   // CONSTMAX_EXP_ARG
 constexpr double kE = 2.718281828459045235360287471352662498;  // CONSTe
 
+// Comparisons of doubles on the integer pipe.  GB300 issues FP64 at a small
+// fraction of its integer rate and the device evaluations are bound by the
+// FP64 pipe, so their sign tests, comparisons and clamps run on the bit
+// patterns instead.  For operands that are not NaN each helper returns what
+// the FP64 operation returns, with +0 and -0 equal.  fkey maps a double to an
+// integer of the same order: sign-magnitude to two's complement.
+__device__ __forceinline__ long long fkey(double a) {
+  const long long b = __double_as_longlong(a);
+  const long long mag = b & 0x7fffffffffffffffLL;
+  return b < 0 ? -mag : mag;
+}
+__device__ __forceinline__ bool f_lt(double a, double b) { return fkey(a) < fkey(b); }
+__device__ __forceinline__ bool f_le(double a, double b) { return fkey(a) <= fkey(b); }
+__device__ __forceinline__ bool f_le0(double a) { return __double_as_longlong(a) <= 0; }
+__device__ __forceinline__ bool f_gt0(double a) { return __double_as_longlong(a) > 0; }
+__device__ __forceinline__ bool f_lt0(double a) { return fkey(a) < 0; }
+__device__ __forceinline__ bool f_ge0(double a) { return fkey(a) >= 0; }
+__device__ __forceinline__ bool f_is0(double a) { return (__double_as_longlong(a) << 1) == 0; }
+__device__ __forceinline__ bool f_is1(double a) { return __double_as_longlong(a) == 0x3ff0000000000000LL; }
+__device__ __forceinline__ double f_min(double a, double b) { return f_le(a, b) ? a : b; }
+__device__ __forceinline__ double f_max(double a, double b) { return f_le(b, a) ? a : b; }
+
 __device__ __forceinline__ double pnjlim_d(double vnew, double vold, double vt, double vcrit,
                                            int &icheck) {
-  if (vnew > vcrit && fabs(vnew - vold) > (vt + vt)) {
-    if (vold > 0) {
+  // |vnew - vold| > 2 vt, with the magnitude taken from the bit pattern
+  if (f_lt(vcrit, vnew) &&
+      fkey(vt + vt) < (__double_as_longlong(vnew - vold) & 0x7fffffffffffffffLL)) {
+    if (f_gt0(vold)) {
       double arg = 1 + (vnew - vold) / vt;
       vnew = (arg > 0) ? vold + vt * log(arg) : vcrit;
     } else {
@@ -32,41 +55,46 @@ __device__ __forceinline__ double pnjlim_d(double vnew, double vold, double vt, 
 }
 
 __device__ __forceinline__ double limvds_d(double vnew, double vold) {
-  if (vold >= 3.5) {
-    if (vnew > vold) vnew = fmin(vnew, 3.0 * vold + 2.0);
-    else if (vnew < 3.5) vnew = fmax(vnew, 2.0);
+  if (f_le(3.5, vold)) {
+    if (f_lt(vold, vnew)) vnew = f_min(vnew, 3.0 * vold + 2.0);
+    else if (f_lt(vnew, 3.5)) vnew = f_max(vnew, 2.0);
   } else {
-    vnew = (vnew > vold) ? fmin(vnew, 4.0) : fmax(vnew, -0.5);
+    vnew = f_lt(vold, vnew) ? f_min(vnew, 4.0) : f_max(vnew, -0.5);
   }
   return vnew;
 }
 
+// The limits are formed only on the paths that read them.  -delv > x is
+// tested as fkey(x) < -fkey(delv) (negation is exact).
 __device__ __forceinline__ double fetlim_d(double vnew, double vold, double vto) {
-  double vtsthi = fabs(2 * (vold - vto)) + 2;
-  double vtstlo = vtsthi / 2 + 2;
-  double vtox = vto + 3.5;
-  double delv = vnew - vold;
-  if (vold >= vto) {
-    if (vold >= vtox) {
-      if (delv <= 0) {
-        if (vnew >= vtox) {
-          if (-delv > vtstlo) vnew = vold - vtstlo;
+  auto hi = [&] { return fabs(2 * (vold - vto)) + 2; };  // vtsthi
+  const double delv = vnew - vold;
+  if (f_le(vto, vold)) {
+    const double vtox = vto + 3.5;
+    if (f_le(vtox, vold)) {
+      if (f_le0(delv)) {
+        if (f_le(vtox, vnew)) {
+          const double vtstlo = hi() / 2 + 2;
+          if (fkey(vtstlo) < -fkey(delv)) vnew = vold - vtstlo;
         } else {
-          vnew = fmax(vnew, vto + 2.0);
+          vnew = f_max(vnew, vto + 2.0);
         }
-      } else if (delv >= vtsthi) {
-        vnew = vold + vtsthi;
+      } else {
+        const double vtsthi = hi();
+        if (f_le(vtsthi, delv)) vnew = vold + vtsthi;
       }
     } else {
-      vnew = (delv <= 0) ? fmax(vnew, vto - 0.5) : fmin(vnew, vto + 4.0);
+      vnew = f_le0(delv) ? f_max(vnew, vto - 0.5) : f_min(vnew, vto + 4.0);
     }
   } else {
-    if (delv <= 0) {
-      if (-delv > vtsthi) vnew = vold - vtsthi;
+    if (f_le0(delv)) {
+      const double vtsthi = hi();
+      if (fkey(vtsthi) < -fkey(delv)) vnew = vold - vtsthi;
     } else {
       double vtemp = vto + 0.5;
-      if (vnew <= vtemp) {
-        if (delv > vtstlo) vnew = vold + vtstlo;
+      if (f_le(vnew, vtemp)) {
+        const double vtstlo = hi() / 2 + 2;
+        if (f_lt(vtstlo, delv)) vnew = vold + vtstlo;
       } else {
         vnew = vtemp;
       }

@@ -155,6 +155,12 @@ Mos1Instance mos1_instance(const double *p) {
   m.vt = vt;
   m.gsatD = m.DrainSatCur / vt;
   m.gsatS = m.SourceSatCur / vt;
+  // per-evaluation terms that depend on the model only (the device computes
+  // the same IEEE operations on the same operands when it needs them)
+  m.gbdR = m.gsatD + kGmin;
+  m.gbsR = m.gsatS + kGmin;
+  m.sqrtPhi = std::sqrt(tPhi);
+  m.argPhi = (m.sqrtPhi <= 0) ? 0.0 : gamma / (m.sqrtPhi + m.sqrtPhi);
   m.OxideCap = oxideCapFactor * Leff * W;
   m.Cgso = p[XG_MOS1_CGSO] * W;
   m.Cgdo = p[XG_MOS1_CGDO] * W;
