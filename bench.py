@@ -484,9 +484,18 @@ def run_ours(args):
                          "peak_kind": peak_kind, "algorithmic_bytes": alg,
                          "note": "device-evaluation bytes only (MOSFET-1 evaluation + stamp per instance per "
                                  "Newton iteration) over the timed windows; assembly, LU and control bytes not counted"}
+    resident_stages = None
     if rank == 0:
         # the tick profiler launches the tick-graph kernels one by one, stage by stage
         roof, lu_roof, stages = _rooflines(circ, nl, window, hbm_peak, peak_kind, info, args)
+        try:
+            # where the circuit-resident tick's CTAs spend their cycles (one window, 64-thread CTAs)
+            cyc, cticks = circ.tran_profile_resident(window, threads=64)
+            tot = sum(cyc.values())
+            resident_stages = {"cta_kcycles_per_circuit_iter": tot / max(1, cticks) / 1e3,
+                               "share": {k: v / tot for k, v in cyc.items()}, "circuit_iters": cticks}
+        except xg.XgError as e:
+            resident_stages = {"unavailable": str(e)}
     circ.tran_end()
     circ.close()
 
@@ -510,7 +519,7 @@ def run_ours(args):
             forms["fp64_tick_graph"] = (s1["accepted"] - s0["accepted"]) / (ms5 / 1e3)
             c5.tran_end()
             c5.close()
-            if st1["option"] == 3 and form == "tick_graph" and any(st1["option_us_per_iter"][:3]):
+            if st1["option"] == 5 and form == "tick_graph" and any(st1["option_us_per_iter"][:5]):
                 # the timed trials chose the tick graph: the resident form alone, for comparison
                 c6, ms6, s0, s1 = _timed_windows(xg, nl, probes, dev, args, window, xg.PREC_FP64, flush,
                                                  stream_of, form=xg.FORM_RESIDENT)
@@ -571,9 +580,10 @@ def run_ours(args):
                 "newton_iters_per_step": (st1["newton_iters"] - st0["newton_iters"]) / max(1, steps_done),
                 "form": form, "ticks": ticks, "kernels_per_tick": kernels_per_tick, "gpu_launches": gpu_launches,
                 "form_trials_us_per_newton_iter": dict(zip(("resident_32", "resident_64", "resident_128",
-                                                            "tick_graph"), st1["option_us_per_iter"])),
+                                                            "resident_256", "resident_512", "tick_graph"),
+                                                           st1["option_us_per_iter"])),
                 "lu": info, "roofline": roof, "roofline_lu": lu_roof, "roofline_resident": resident_roof,
-                "tick_stages_us": stages,
+                "tick_stages_us": stages, "resident_stages": resident_stages,
                 "max_err_vs_fp64": err, "forms": forms, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks}
         print(json.dumps(line), flush=True)

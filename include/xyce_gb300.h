@@ -334,8 +334,9 @@ typedef struct xg_tran_stats {
   long long factor_skips;                      /* refactorizations skipped (xg_lu_set_reuse) */
   int resident_threads;                        /* resident form: CTA size of its last launch (0: none) */
   int option;                                  /* advancing option the timed trials chose (-1: not yet):
-                                                  0..2 resident with 32/64/128-thread CTAs, 3 tick graph */
-  double option_us_per_iter[4];                /* device time per circuit Newton iteration of each timed
+                                                  0..4 resident with 32/64/128/256/512-thread CTAs,
+                                                  5 tick graph */
+  double option_us_per_iter[6];                /* device time per circuit Newton iteration of each timed
                                                   option, microseconds (0: not timed) */
 } xg_tran_stats;
 
@@ -351,10 +352,11 @@ typedef struct xg_tran_stats {
  * and diode devices only, FP64 factors, the polynomial predictor and an LU
  * analysis without a top.  XG_FORM_AUTO (default): when the batch admits
  * the resident form, the first advances after the operating point time
- * each option (the tick graph over one advance, then the resident kernel
- * with 64-, 128- and 32-thread CTAs, one launch each) and the rest of the
- * run keeps the one with the shortest device time per circuit Newton
- * iteration; XG_FORM_RESIDENT times the three CTA sizes only.  No reference counterpart (Xyce runs one circuit per process).
+ * the options (the tick graph over one advance, then the resident kernel,
+ * one launch per CTA size: 128 and 256 threads, then on towards 512 or
+ * down to 64 and 32 while the size keeps getting faster) and the rest of
+ * the run keeps the one with the shortest device time per circuit Newton
+ * iteration; XG_FORM_RESIDENT times the CTA sizes only.  No reference counterpart (Xyce runs one circuit per process).
  * Not allowed while a transient is in progress. */
 #define XG_FORM_AUTO        0
 #define XG_FORM_TICK_GRAPH  1
@@ -401,6 +403,22 @@ enum {
   XG_STAGE_HISTORY, XG_STAGE_COMMIT, XG_STAGE_COUNT
 };
 int xg_tran_profile(xg_ctx *ctx, int n_steps, int n_ticks, double *stage_ms, long long *evals);
+/* Where the circuit-resident tick (XG_FORM_RESIDENT) spends its time, for a
+ * transient in progress whose analysis admits that form.  n_steps > 0 first
+ * opens a window as xg_tran_advance does; one launch of the resident kernel
+ * with CTAs of `threads` (32, 64 or 128) threads then runs every active
+ * circuit with a clock in each CTA, and stage_cycles[XG_RSTAGE_*] receives
+ * the SM cycles the CTAs spent in each stage of their ticks (barrier waits
+ * included), summed over CTAs and ticks.  circuit_ticks (may be NULL)
+ * receives the Newton iterations that launch ran, summed over circuits.
+ * The window then finishes as xg_tran_advance would finish it.  No
+ * reference counterpart. */
+enum {
+  XG_RSTAGE_SOURCES, XG_RSTAGE_DEVICES, XG_RSTAGE_LONG_GATHERS, XG_RSTAGE_ASSEMBLE, XG_RSTAGE_NEWTON,
+  XG_RSTAGE_FACTOR, XG_RSTAGE_SOLVE, XG_RSTAGE_UPDATE, XG_RSTAGE_STEP, XG_RSTAGE_COMMIT, XG_RSTAGE_COUNT
+};
+int xg_tran_profile_resident(xg_ctx *ctx, int n_steps, int threads, double *stage_cycles,
+                             long long *circuit_ticks);
 
 /* Integration order of the recorded points (layout of xg_tran_results'
  * times, n_circuits x cap): 0 for the operating point, else the order the

@@ -85,23 +85,26 @@ def test_resident_form_refused_where_it_does_not_apply(xg, torch_cuda):
     c.close()
 
 
-def test_auto_times_every_option_and_keeps_the_bits(xg, torch_cuda):
+def test_auto_times_the_options_and_keeps_the_bits(xg, torch_cuda):
     """XG_FORM_AUTO on a batch that admits the resident form: the first
-    launches time the resident kernel at each CTA size and the tick graph,
-    switching between them mid-run, and the run still equals the tick graph's
-    bit for bit; the stats name the option kept and each option's time."""
+    advances time the tick graph and resident CTA sizes (128 and 256
+    threads, then on in the direction that got faster), switching between
+    them mid-run, and the run still equals the tick graph's bit for bit; the
+    stats name the option kept and each timed option's time."""
     nl = N.monte_carlo_rings(96, 11, 301, seed=13)
     probes = [nl.names[f"c{i}.n1"] for i in range(0, 96, 5)]
-    g = _windows(xg, nl, probes, xg.FORM_TICK_GRAPH, 6, 20)
-    a = _windows(xg, nl, probes, xg.FORM_AUTO, 6, 20)
+    g = _windows(xg, nl, probes, xg.FORM_TICK_GRAPH, 7, 20)
+    a = _windows(xg, nl, probes, xg.FORM_AUTO, 7, 20)
     _same(g, a)
     st = a[3]
-    assert st["option"] in (0, 1, 2, 3), st["option"]
-    assert all(u > 0 for u in st["option_us_per_iter"]), st["option_us_per_iter"]
-    best = min(range(4), key=lambda k: st["option_us_per_iter"][k])
+    us = st["option_us_per_iter"]
+    timed = [k for k in range(6) if us[k] > 0]
+    assert 5 in timed and 2 in timed and 3 in timed, us
+    assert len(timed) in (4, 5, 6), us
+    best = min(timed, key=lambda k: us[k])
     assert st["option"] == best
-    assert st["form"] == (xg.FORM_TICK_GRAPH if best == 3 else xg.FORM_RESIDENT)
-    # the forced resident form times its three CTA sizes only
+    assert st["form"] == (xg.FORM_TICK_GRAPH if best == 5 else xg.FORM_RESIDENT)
+    # the forced resident form times CTA sizes only
     r = _windows(xg, nl, probes, xg.FORM_RESIDENT, 6, 20)
-    assert r[3]["option"] in (0, 1, 2) and r[3]["option_us_per_iter"][3] == 0
-    print("us per circuit Newton iteration:", st["option_us_per_iter"], "kept", st["option"])
+    assert 0 <= r[3]["option"] <= 4 and r[3]["option_us_per_iter"][5] == 0
+    print("us per circuit Newton iteration:", us, "kept", st["option"])

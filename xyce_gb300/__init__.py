@@ -51,7 +51,7 @@ EXPORTED = [
     "xg_lu_solve_noalloc", "xg_lu_set_precision", "xg_lu_info", "xg_lu_schedule_info", "xg_lu_set_schedule", "xg_lu_analyze_pattern",
     "xg_lu_set_tuning", "xg_lu_tuning_info", "xg_lu_set_reuse", "xg_lu_set_pivot_tolerance",
     "xg_transient", "xg_tran_set_form", "xg_tran_start", "xg_tran_advance", "xg_tran_results", "xg_tran_end",
-    "xg_tran_predictors", "xg_tran_orders", "xg_tran_profile", "xg_tran_predictor_stats", "xg_set_predictor", "xg_mlp_set", "xg_mlp_get",
+    "xg_tran_predictors", "xg_tran_orders", "xg_tran_profile", "xg_tran_profile_resident", "xg_tran_predictor_stats", "xg_set_predictor", "xg_mlp_set", "xg_mlp_get",
     "xg_mlp_train", "xg_mlp_grad", "xg_mlp_forward",
     "xg_dcop", "xg_newton_solve", "xg_version",
 ]
@@ -95,7 +95,7 @@ class TranStats(C.Structure):
                 ("t_final_max", C.c_double), ("seconds", C.c_double), ("kernels_per_tick", C.c_int),
                 ("form", C.c_int), ("kernel_launches", C.c_longlong), ("circuit_ticks", C.c_longlong),
                 ("factor_skips", C.c_longlong), ("resident_threads", C.c_int),
-                ("option", C.c_int), ("option_us_per_iter", C.c_double * 4)]
+                ("option", C.c_int), ("option_us_per_iter", C.c_double * 6)]
 
     def as_dict(self):
         out = {}
@@ -173,6 +173,7 @@ def lib() -> C.CDLL:
     L.xg_tran_predictors.argtypes = [P, dp]
     L.xg_tran_orders.argtypes = [P, ip]
     L.xg_tran_profile.argtypes = [P, I, I, dp, np.ctypeslib.ndpointer(np.int64, flags="C")]
+    L.xg_tran_profile_resident.argtypes = [P, I, I, dp, C.POINTER(C.c_longlong)]
     L.xg_tran_predictor_stats.argtypes = [P, LL, LL, LL, LL]
     L.xg_set_predictor.argtypes = [P, I]
     L.xg_mlp_set.argtypes = [P, fp, fp]
@@ -428,6 +429,19 @@ class Circuit:
         ev = np.zeros(4, np.int64)
         self._check(lib().xg_tran_profile(self.h, int(n_steps), int(n_ticks), ms, ev))
         return dict(zip(self.STAGES, ms.tolist())), dict(zip(("mos1", "bsim4", "diode", "circuits"), ev.tolist()))
+
+    RSTAGES = ("sources", "devices", "long_gathers", "assemble", "newton", "factor", "solve", "update", "step",
+               "commit")
+
+    def tran_profile_resident(self, n_steps: int = 0, threads: int = 64):
+        """SM cycles the circuit-resident tick's CTAs spend in each stage
+        (summed over CTAs and ticks) over one resident launch of the run in
+        progress (n_steps > 0: a new window of that many steps), and the
+        circuit Newton iterations that launch ran."""
+        cyc = np.zeros(len(self.RSTAGES))
+        ticks = C.c_longlong()
+        self._check(lib().xg_tran_profile_resident(self.h, int(n_steps), int(threads), cyc, C.byref(ticks)))
+        return dict(zip(self.RSTAGES, cyc.tolist())), ticks.value
 
     def tran_orders(self):
         """Integration order of each recorded point, [n_circuits, cap] (0 at

@@ -1537,19 +1537,18 @@ struct TranRun {
   long long circuit_ticks = 0;    // Newton iterations run by the resident tick, summed over circuits
   long long kernel_launches = 0;  // kernels launched while advancing
   unsigned long long tick_count[2] = {0, 0};
-  // How the run advances.  Options 0..2: the resident kernel with CTAs of
-  // kResidentThreads[k]; option 3: the tick graph.  Every option gives the
-  // same bits, so the first launches of the transient (not of the operating
-  // point) try each admitted option (the resident sizes when the form is
-  // XG_FORM_RESIDENT, all four under XG_FORM_AUTO) and the one with the
-  // shortest device time per circuit Newton iteration is kept.  A resident
-  // trial is one launch; a tick-graph trial runs the graph until the run
-  // goes idle.
-  static constexpr int kOptions = 4, kGraphOption = 3;
+  // How the run advances.  Options 0..4: the resident kernel with CTAs of
+  // kResidentThreads[k]; option 5: the tick graph.  Every option gives the
+  // same bits, so the first advances of the transient (not the operating
+  // point) time the admitted options and keep the one with the shortest
+  // device time per circuit Newton iteration: the tick graph (under
+  // XG_FORM_AUTO) over one advance, then resident CTA sizes one launch each,
+  // from 128 threads up while larger sizes get faster, else down.
+  static constexpr int kOptions = kResidentSizes + 1, kGraphOption = kResidentSizes;
   int option = -1;                        // chosen option (-1: trials not over)
-  double opt_ms[kOptions] = {0, 0, 0, 0};
-  double opt_iters[kOptions] = {0, 0, 0, 0};
-  bool opt_done[kOptions] = {false, false, false, false};
+  double opt_ms[kOptions] = {};
+  double opt_iters[kOptions] = {};
+  bool opt_done[kOptions] = {};
   int pending = -1;                       // option timed between res_ev[0] and res_ev[1]
   unsigned long long pending_iters0 = 0;  // Newton iterations before it
   cudaEvent_t res_ev[2] = {nullptr, nullptr};
@@ -1669,6 +1668,26 @@ int stalled_circuits(xg_ctx *ctx, std::vector<char> &refresh) {
   return XG_OK;
 }
 
+// The next option to time (-1: none left).  The tick graph first; then the
+// resident CTA sizes: 128 and 256 threads, then on in the direction that got
+// faster (512, or 64 and then 32) until a size is slower than the last.
+int next_trial(const TranRun &R) {
+  if (R.try_graph && !R.opt_done[TranRun::kGraphOption]) return TranRun::kGraphOption;
+  if (!R.try_resident) return -1;
+  auto per = [&](int k) { return R.opt_ms[k] / R.opt_iters[k]; };
+  int k = 2;
+  if (!R.opt_done[k]) return k;
+  if (!R.opt_done[k + 1]) return k + 1;
+  const int dir = per(k + 1) < per(k) ? 1 : -1;
+  if (dir > 0) k = k + 1;
+  while (k + dir >= 0 && k + dir < kResidentSizes) {
+    if (!R.opt_done[k + dir]) return k + dir;
+    if (!(per(k + dir) < per(k))) break;
+    k += dir;
+  }
+  return -1;
+}
+
 // Runs tick batches until every circuit is done, failed or paused; re-pivots
 // on LU breakdown.  One host synchronization per batch of ticks.
 int run_until_idle(TranRun &R) {
@@ -1716,14 +1735,13 @@ int run_until_idle(TranRun &R) {
           R.opt_iters[R.pending] > 0)
         R.opt_done[R.pending] = true;
       R.pending = -1;
-      bool all = true;
-      int best = -1;
-      for (int k = 0; k < TranRun::kOptions; ++k) {
-        if (!(k == TranRun::kGraphOption ? R.try_graph : R.try_resident)) continue;
-        if (!R.opt_done[k]) { all = false; break; }
-        if (best < 0 || R.opt_ms[k] / R.opt_iters[k] < R.opt_ms[best] / R.opt_iters[best]) best = k;
+      if (next_trial(R) < 0) {
+        int best = -1;
+        for (int k = 0; k < TranRun::kOptions; ++k)
+          if (R.opt_done[k] && (best < 0 || R.opt_ms[k] / R.opt_iters[k] < R.opt_ms[best] / R.opt_iters[best]))
+            best = k;
+        if (best >= 0) R.option = best;
       }
-      if (all && best >= 0) R.option = best;
     }
     if (R.tick_count[0]) {
       // the last resident launch: its longest circuit's ticks, and all of them
@@ -1738,15 +1756,9 @@ int run_until_idle(TranRun &R) {
     if (opt < 0 && R.operating_point) {
       // the operating point's Newton iterations are not the transient's:
       // the trials wait for the first advance
-      opt = R.try_graph ? TranRun::kGraphOption : 1;
+      opt = R.try_graph ? TranRun::kGraphOption : 2;
     } else if (opt < 0) {
-      // the next option not yet timed: the tick graph first, then the
-      // resident CTA sizes from the one that usually wins
-      static constexpr int kTrialOrder[TranRun::kOptions] = {TranRun::kGraphOption, 1, 2, 0};
-      for (int q = 0; q < TranRun::kOptions && opt < 0; ++q) {
-        const int k = kTrialOrder[q];
-        if ((k == TranRun::kGraphOption ? R.try_graph : R.try_resident) && !R.opt_done[k]) opt = k;
-      }
+      opt = next_trial(R);
       trial = opt >= 0;
       if (opt < 0) opt = TranRun::kGraphOption;
     }
@@ -2100,6 +2112,42 @@ extern "C" int xg_tran_profile(xg_ctx *ctx, int n_steps, int n_ticks, double *st
   for (auto &e : ev) cudaEventDestroy(e);
   if (rc) return fail(ctx, rc, "tick profile: CUDA failure");
   return XG_OK;
+}
+
+extern "C" int xg_tran_profile_resident(xg_ctx *ctx, int n_steps, int threads, double *stage_cycles,
+                                        long long *circuit_ticks) {
+  if (!ctx || !stage_cycles) return XG_ERR_ARG;
+  if (threads != 32 && threads != 64 && threads != 128)
+    return fail(ctx, XG_ERR_ARG, "threads must be 32, 64 or 128");
+  if (!ctx->run || !ctx->run->exec) return fail(ctx, XG_ERR_STATE, "call xg_tran_start first");
+  if (!ctx->resident_ok) return fail(ctx, XG_ERR_UNSUPPORTED, "the run's analysis does not admit the resident tick");
+  TranRun &R = *ctx->run;
+  DevArrays &d = ctx->d;
+  CK(cudaSetDevice(ctx->device));
+  unsigned long long *clk = nullptr;
+  CK(cudaMalloc(&clk, sizeof(unsigned long long) * XG_RSTAGE_COUNT));
+  std::vector<unsigned long long> h(XG_RSTAGE_COUNT, 0);
+  int rc = XG_OK;
+  auto step = [&](cudaError_t e) {
+    if (rc == XG_OK && e != cudaSuccess) rc = fail(ctx, XG_ERR_CUDA, std::string("resident profile: ") + cudaGetErrorString(e));
+  };
+  step(cudaMemsetAsync(clk, 0, sizeof(unsigned long long) * XG_RSTAGE_COUNT, ctx->stream));
+  if (n_steps > 0) launch_set_target_k(ctx->stream, d, ctx->ncirc, n_steps);
+  launch_resident_k(ctx->stream, d, ctx->L, ctx->F, threads, ctx->ncirc, ctx->nm, ctx->nd, ctx->nv, ctx->sto_base_m,
+                    ctx->resident_slots, R.bps, R.bp_ptr, R.cap, R.pmax, R.pivot_tol, clk);
+  launch_count_done_k(ctx->stream, d, ctx->ncirc, ctx->breakdown_dev, ctx->status_dev);
+  step(cudaGetLastError());
+  step(cudaMemcpyAsync(h.data(), clk, sizeof(unsigned long long) * XG_RSTAGE_COUNT, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+  step(cudaMemcpyAsync(R.tick_count, ctx->F.ticks, sizeof R.tick_count, cudaMemcpyDeviceToHost, ctx->stream));
+  step(cudaStreamSynchronize(ctx->stream));
+  cudaFree(clk);
+  if (rc) return rc;
+  for (int k = 0; k < XG_RSTAGE_COUNT; ++k) stage_cycles[k] = (double)h[k];
+  if (circuit_ticks) *circuit_ticks = (long long)R.tick_count[1];
+  R.kernel_launches += 2;
+  // circuits parked on a breakdown or stopped by the tick bound finish the window as an advance would
+  return run_until_idle(R);
 }
 
 extern "C" int xg_tran_orders(xg_ctx *ctx, int *orders) {

@@ -338,7 +338,7 @@ struct FusedDev {
   signed char *f_kind = nullptr, *l_meth = nullptr, *u_meth = nullptr;
   unsigned long long *ticks = nullptr;  // [0] largest tick count of a circuit, [1] circuit-ticks (this launch)
   int max_rows = 0;
-  int grid[3] = {0, 0, 0};  // persistent grids of the kResidentThreads CTA sizes
+  int grid[5] = {0, 0, 0, 0, 0};  // persistent grids of the kResidentThreads CTA sizes
   // the circuit's factor columns staged in shared memory: column j at
   // c_soff[j] of its circuit's buffer (c_fcnt[c] entries); c_umeta as
   // LUDev::umeta with .x the buffer offset of L(k+1.., k); max_fbuf = 0:
@@ -348,7 +348,8 @@ struct FusedDev {
   int max_fbuf = 0;
 };
 constexpr int kFusedSmemBytes = 160 * 1024;  // largest resident buffer (row partials + staged columns)
-constexpr int kResidentThreads[3] = {32, 64, 128};  // CTA sizes the driver tries
+constexpr int kResidentSizes = 5;
+constexpr int kResidentThreads[kResidentSizes] = {32, 64, 128, 256, 512};  // CTA sizes the driver tries
 
 // Host-side analysis result.
 struct LUHost {
@@ -447,7 +448,8 @@ void launch_newton_weights_k(cudaStream_t st, const DevArrays &d, int n);
 int resident_prepare_k(int max_rows, int max_fbuf, int device, int *grid);
 void launch_resident_k(cudaStream_t st, const DevArrays &d, const LUDev &L, const FusedDev &F, int threads,
                        int ncirc, int nm, int nd, int nv, int sto_base_m, const int *slots, const double *bps,
-                       const int *bp_ptr, int cap, int pmax, double pivot_tol);
+                       const int *bp_ptr, int cap, int pmax, double pivot_tol,
+                       unsigned long long *clk = nullptr);
 void launch_set_target_k(cudaStream_t st, const DevArrays &d, int ncirc, int n_steps);
 int lu_prepare_k();  // shared-memory opt-in of the staged group factorization
 void launch_lu_factor_k(cudaStream_t st, const LUDev &L, const double *vals, CircState *cs, int masked,

@@ -1359,6 +1359,27 @@ struct FusedArgs {
   const int *bp_ptr;
   int cap, pmax;
   double pivot_tol;
+  // per-stage clock: when not null, thread 0 of each CTA adds the cycles its
+  // CTA spends in each stage of a tick (XG_RSTAGE_*) into clk[stage]
+  unsigned long long *clk;
+};
+
+// Stage clock of the resident tick: cycles since the last mark, into stage k.
+struct StageClock {
+  unsigned long long *clk;
+  long long t;
+  __device__ explicit StageClock(unsigned long long *c) {
+    clk = c;
+    t = 0;
+    if (c && threadIdx.x == 0) t = clock64();
+  }
+  __device__ void mark(int k) {
+    if (clk && threadIdx.x == 0) {
+      const long long now = clock64();
+      atomicAdd(clk + k, (unsigned long long)(now - t));
+      t = now;
+    }
+  }
 };
 
 // The factorization of circuit c, level by level: single-thread columns,
@@ -1501,6 +1522,7 @@ __device__ void resident_circuit(const DevArrays &d, const LUDev &L, const Fused
   const int o0 = d.offsets[c], o1 = d.offsets[c + 1];
   const int e0 = d.rp[o0], e1 = d.rp[o1];
   const CircState &s = d.cs[c];
+  StageClock clk(A.clk);
   int ticks = 0;
   for (; ticks < kFusedMaxTicks; ++ticks) {
     __syncthreads();
@@ -1508,11 +1530,13 @@ __device__ void resident_circuit(const DevArrays &d, const LUDev &L, const Fused
     if (!(ph == PH_DC || ph == PH_TRAN)) break;  // uniform: read after the barrier
     for (int k = F.src_ptr[c] + tid; k < F.src_ptr[c + 1]; k += nth) source_value(d, F.src_list[k], A.nv, 0, 0.0);
     __syncthreads();
+    clk.mark(XG_RSTAGE_SOURCES);
     for (int k = F.m1_ptr[c] + tid; k < F.m1_ptr[c + 1]; k += nth)
       mos1_eval(d, F.m1_list[k], A.nm, A.sto_base_m, 1, 1, 0, 0, A.sF_m, A.sQ_m, A.sL_m, A.sM_m);
     for (int k = F.d_ptr[c] + tid; k < F.d_ptr[c + 1]; k += nth)
       diode_eval(d, F.d_list[k], A.nd, 1, 1, 0, 0, A.sF_d, A.sQ_d, A.sL_d, A.sM_d);
     __syncthreads();
+    clk.mark(XG_RSTAGE_DEVICES);
     for (int q = F.lr_ptr[c]; q < F.lr_ptr[c + 1]; ++q) {
       const int lr = F.lr_list[q];
       for (int part = 0; part < d.lrow_ptr[lr + 1] - d.lrow_ptr[lr]; ++part) long_row_part(d, lr, part, ws);
@@ -1522,6 +1546,7 @@ __device__ void resident_circuit(const DevArrays &d, const LUDev &L, const Fused
       for (int part = 0; part < d.lent_ptr[le + 1] - d.lent_ptr[le]; ++part) long_entry_part(d, le, part, ws);
     }
     __syncthreads();
+    clk.mark(XG_RSTAGE_LONG_GATHERS);
     for (int r = o0 + tid; r < o1; r += nth) {
       double a, b;
       assemble_row(d, r, a, b);
@@ -1530,15 +1555,19 @@ __device__ void resident_circuit(const DevArrays &d, const LUDev &L, const Fused
     }
     for (int e = e0 + tid; e < e1; e += nth) assemble_entry(d, e);
     __syncthreads();
+    clk.mark(XG_RSTAGE_ASSEMBLE);
     circuit_partials(d, c, o0, o1, vm, vs);
     __syncthreads();
     if (warp == 0) newton_ctl_circuit(d, c, lane);
     __syncthreads();
+    clk.mark(XG_RSTAGE_NEWTON);
     if (s.need_solve && !s.singular) {  // uniform
       if (s.refactor) resident_factor(d, L, F, c, A.pivot_tol, sm, S);
+      clk.mark(XG_RSTAGE_FACTOR);
       if (!s.singular) resident_solve(d, L, F, c, sm);  // uniform: read after the factor's last barrier
     }
     __syncthreads();
+    clk.mark(XG_RSTAGE_SOLVE);
     for (int r = o0 + tid; r < o1; r += nth) {
       double a, b;
       update_row(d, r, a, b);
@@ -1548,13 +1577,16 @@ __device__ void resident_circuit(const DevArrays &d, const LUDev &L, const Fused
     __syncthreads();
     circuit_partials(d, c, o0, o1, vm, vs);
     __syncthreads();
+    clk.mark(XG_RSTAGE_UPDATE);
     if (warp == 0) step_ctl_circuit(d, c, lane, A.bps, A.bp_ptr, A.cap);
     __syncthreads();
+    clk.mark(XG_RSTAGE_STEP);
     for (int r = o0 + tid; r < o1; r += nth) history_row(d, r, A.cap, A.pmax);
     for (int k = F.m1_ptr[c] + tid; k < F.m1_ptr[c + 1]; k += nth)
       commit_instance(d, F.m1_list[k], A.nm, A.nd, A.sto_base_m, 0, 0, 0);
     for (int k = F.d_ptr[c] + tid; k < F.d_ptr[c + 1]; k += nth)
       commit_instance(d, A.nm + F.d_list[k], A.nm, A.nd, A.sto_base_m, 0, 0, 0);
+    clk.mark(XG_RSTAGE_COMMIT);
   }
   if (tid == 0 && ticks > 0) {
     atomicMax(F.ticks, (unsigned long long)ticks);
@@ -1600,7 +1632,7 @@ static int resident_grid(size_t smem, int sms, int *grid) {
   return XG_OK;
 }
 
-// Persistent grids of the CTA sizes kResidentThreads (32, 64, 128).
+// Persistent grids of the CTA sizes kResidentThreads (32 ... 512).
 int resident_prepare_k(int max_rows, int max_fbuf, int device, int *grid) {
   const size_t smem = sizeof(double) * (2 * (size_t)max_rows + (size_t)max_fbuf);
   int sms = 0;
@@ -1608,13 +1640,16 @@ int resident_prepare_k(int max_rows, int max_fbuf, int device, int *grid) {
   int rc = resident_grid<32>(smem, sms, &grid[0]);
   if (rc == XG_OK) rc = resident_grid<64>(smem, sms, &grid[1]);
   if (rc == XG_OK) rc = resident_grid<128>(smem, sms, &grid[2]);
+  if (rc == XG_OK) rc = resident_grid<256>(smem, sms, &grid[3]);
+  if (rc == XG_OK) rc = resident_grid<512>(smem, sms, &grid[4]);
   return rc;
 }
 
 void launch_resident_k(cudaStream_t st, const DevArrays &d, const LUDev &L, const FusedDev &F, int threads,
                        int ncirc, int nm, int nd, int nv, int sto_base_m, const int *slots, const double *bps,
-                       const int *bp_ptr, int cap, int pmax, double pivot_tol) {
+                       const int *bp_ptr, int cap, int pmax, double pivot_tol, unsigned long long *clk) {
   FusedArgs A;
+  A.clk = clk;
   A.ncirc = ncirc; A.nm = nm; A.nd = nd; A.nv = nv; A.sto_base_m = sto_base_m;
   A.sF_m = slots[0]; A.sQ_m = slots[1]; A.sL_m = slots[2]; A.sM_m = slots[3];
   A.sF_d = slots[4]; A.sQ_d = slots[5]; A.sL_d = slots[6]; A.sM_d = slots[7];
@@ -1622,9 +1657,13 @@ void launch_resident_k(cudaStream_t st, const DevArrays &d, const LUDev &L, cons
   cudaMemsetAsync(F.queue, 0, sizeof(int), st);
   cudaMemsetAsync(F.ticks, 0, 2 * sizeof(unsigned long long), st);
   const size_t smem = sizeof(double) * (2 * (size_t)F.max_rows + (size_t)F.max_fbuf);
-  if (threads == 32) k_resident<32><<<std::min(F.grid[0], ncirc), 32, smem, st>>>(d, L, F, A);
-  else if (threads == 64) k_resident<64><<<std::min(F.grid[1], ncirc), 64, smem, st>>>(d, L, F, A);
-  else k_resident<128><<<std::min(F.grid[2], ncirc), 128, smem, st>>>(d, L, F, A);
+  switch (threads) {
+    case 32: k_resident<32><<<std::min(F.grid[0], ncirc), 32, smem, st>>>(d, L, F, A); break;
+    case 64: k_resident<64><<<std::min(F.grid[1], ncirc), 64, smem, st>>>(d, L, F, A); break;
+    case 128: k_resident<128><<<std::min(F.grid[2], ncirc), 128, smem, st>>>(d, L, F, A); break;
+    case 256: k_resident<256><<<std::min(F.grid[3], ncirc), 256, smem, st>>>(d, L, F, A); break;
+    default: k_resident<512><<<std::min(F.grid[4], ncirc), 512, smem, st>>>(d, L, F, A); break;
+  }
 }
 
 void launch_sources_k(cudaStream_t st, const DevArrays &d, int n_v, int n_src, int use_explicit,
