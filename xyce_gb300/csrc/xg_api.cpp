@@ -1670,7 +1670,8 @@ int stalled_circuits(xg_ctx *ctx, std::vector<char> &refresh) {
 
 // The next option to time (-1: none left).  The tick graph first; then the
 // resident CTA sizes: 128 and 256 threads, then on in the direction that got
-// faster (512, or 64 and then 32) until a size is slower than the last.
+// faster (512, or 64 and then 32) until a size is slower than the last —
+// unless both sizes took more than 1.15 times the tick graph's time.
 int next_trial(const TranRun &R) {
   if (R.try_graph && !R.opt_done[TranRun::kGraphOption]) return TranRun::kGraphOption;
   if (!R.try_resident) return -1;
@@ -1678,6 +1679,8 @@ int next_trial(const TranRun &R) {
   int k = 2;
   if (!R.opt_done[k]) return k;
   if (!R.opt_done[k + 1]) return k + 1;
+  // both resident sizes well behind the tick graph: the others will not catch up
+  if (R.try_graph && std::min(per(k), per(k + 1)) > 1.15 * per(TranRun::kGraphOption)) return -1;
   const int dir = per(k + 1) < per(k) ? 1 : -1;
   if (dir > 0) k = k + 1;
   while (k + dir >= 0 && k + dir < kResidentSizes) {

@@ -217,8 +217,7 @@ constexpr int kNoAllocMaxDevices = 64;
 constexpr int kLongColumn = 512;   // factor columns longer than this use the whole CTA
 constexpr int kHubFanout = 64;     // items with more dependents than this run in the prologue
 constexpr int kGroupCap = 512;     // items per dependency-closed group
-constexpr int kPackSmall = 4;        // groups of at most this many items ...
-constexpr int kPackSmallWeight = 16; // ... and entries are packed together ...
+constexpr int kPackSmall = 4;        // groups of at most this many items are packed together ...
 constexpr int kPackCap = 256;        // ... up to this many items ...
 constexpr int kPackCapWeight = 1024; // ... and entries per CTA
 constexpr int kTopRightLooking = 64;  // tops at least this large factor right-looking

@@ -558,86 +558,115 @@ __device__ void block_partials(const DevArrays &d, int n, double vmax, double vs
 // the results land in out[0 .. W) of thread 0.  ws: 8 * W doubles of shared
 // memory.
 constexpr int kGatherLanes = 256;
-template <int W, class Lane>
-__device__ __forceinline__ void gather_sums(Lane &&lane_sums, double *ws, double *out) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-  __syncthreads();
-  for (int vw = warp; vw < kGatherLanes / 32; vw += nwarps) {
-    double v[W];
-    lane_sums(vw * 32 + lane, v);
+
+// One part of a long gather, summed in a fixed order by one warp: 256
+// virtual lanes (virtual lane vl = 32 vw + lane of virtual warp vw sums the
+// part's items vl, vl + stride, ... in order), a butterfly within each
+// virtual warp, then the eight virtual-warp totals by a butterfly over
+// lanes 0..7 (lanes 8..31 add zeros).  Each lane runs its eight virtual
+// lanes round by round, so their loads are independent.  All lanes return
+// the totals.
+template <int W>
+__device__ __forceinline__ void warp_totals(double (&v)[8][W], double *out) {
+  const int lane = threadIdx.x & 31;
 #pragma unroll
-    for (int k = 0; k < W; ++k) {
-      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-      if (lane == 0) ws[k * 8 + vw] = v[k];
+  for (int k = 0; k < W; ++k) {
+    double t = 0.0;
+#pragma unroll
+    for (int vw = 0; vw < 8; ++vw) {
+      double s = v[vw][k];
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == vw) t = s;  // every lane holds the same total (the butterfly's sums commute)
     }
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    out[k] = t;
   }
-  __syncthreads();
-  if (warp == 0) {
+}
+
+// Adds sv[idx[k]] for the part's items of list [k0, k1) into v[vw][f]:
+// item k0 + off + 32 vw for off = start, start + stride, ...
+template <int W>
+__device__ __forceinline__ void warp_gather(double (&v)[8][W], int f, const int *idx, const double *sv, int k0,
+                                            int k1, int start, int stride) {
+  for (int off = start; k0 + off < k1; off += stride) {
+    int ix[8];
 #pragma unroll
-    for (int k = 0; k < W; ++k) {
-      double t = lane < kGatherLanes / 32 ? ws[k * 8 + lane] : 0.0;
-      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-      if (lane == 0) out[k] = t;
-    }
+    for (int vw = 0; vw < 8; ++vw) ix[vw] = (k0 + off + 32 * vw < k1) ? idx[k0 + off + 32 * vw] : -1;
+#pragma unroll
+    for (int vw = 0; vw < 8; ++vw)
+      if (ix[vw] >= 0) v[vw][f] += sv[ix[vw]];
   }
 }
 
 // Part `part` of long row lr (e.g. a supply node touching every PMOS): the
 // F, Q, B, L partial sums of its share of the row's lists, into
-// long_rsum[4 * (lrow_ptr[lr] + part) ..].
-__device__ __forceinline__ void long_row_part(const DevArrays &d, int lr, int part, double *ws) {
+// long_rsum[4 * (lrow_ptr[lr] + part) ..].  One warp.
+__device__ __forceinline__ void long_row_part(const DevArrays &d, int lr, int part) {
+  const int lane = threadIdx.x & 31;
   const int nparts = d.lrow_ptr[lr + 1] - d.lrow_ptr[lr];
   const int r = d.long_rows[lr];
-  const int stride = nparts * kGatherLanes;
-  double out[4];
-  gather_sums<4>([&](int vl, double *v) {
-    const int start = part * kGatherLanes + vl;
-    double F = 0.0, Q = 0.0, B = 0.0, L = 0.0;
-    for (int e = d.rp[r] + start; e < d.rp[r + 1]; e += stride) {
-      const double xv = d.x[d.ci[e]];
-      F += d.Glin[e] * xv;
-      Q += d.Clin[e] * xv;
+  const int stride = nparts * kGatherLanes, start = part * kGatherLanes + lane;
+  double v[8][4];
+#pragma unroll
+  for (int vw = 0; vw < 8; ++vw) v[vw][0] = v[vw][1] = v[vw][2] = v[vw][3] = 0.0;
+  {
+    const int e0 = d.rp[r], e1 = d.rp[r + 1];
+    for (int off = start; e0 + off < e1; off += stride) {
+      double xv[8];
+#pragma unroll
+      for (int vw = 0; vw < 8; ++vw) xv[vw] = (e0 + off + 32 * vw < e1) ? d.x[d.ci[e0 + off + 32 * vw]] : 0.0;
+#pragma unroll
+      for (int vw = 0; vw < 8; ++vw) {
+        const int e = e0 + off + 32 * vw;
+        if (e < e1) {
+          v[vw][0] += d.Glin[e] * xv[vw];
+          v[vw][1] += d.Clin[e] * xv[vw];
+        }
+      }
     }
-    for (int k = d.vF_ptr[r] + start; k < d.vF_ptr[r + 1]; k += stride) F += d.sF[d.vF_idx[k]];
-    for (int k = d.vQ_ptr[r] + start; k < d.vQ_ptr[r + 1]; k += stride) Q += d.sQ[d.vQ_idx[k]];
-    for (int k = d.vB_ptr[r] + start; k < d.vB_ptr[r + 1]; k += stride) B += d.sB[d.vB_idx[k]];
-    for (int k = d.vL_ptr[r] + start; k < d.vL_ptr[r + 1]; k += stride) L += d.sL[d.vL_idx[k]];
-    v[0] = F; v[1] = Q; v[2] = B; v[3] = L;
-  }, ws, out);
-  if (threadIdx.x == 0) {
+  }
+  warp_gather(v, 0, d.vF_idx, d.sF, d.vF_ptr[r], d.vF_ptr[r + 1], start, stride);
+  warp_gather(v, 1, d.vQ_idx, d.sQ, d.vQ_ptr[r], d.vQ_ptr[r + 1], start, stride);
+  warp_gather(v, 2, d.vB_idx, d.sB, d.vB_ptr[r], d.vB_ptr[r + 1], start, stride);
+  warp_gather(v, 3, d.vL_idx, d.sL, d.vL_ptr[r], d.vL_ptr[r + 1], start, stride);
+  double out[4];
+  warp_totals(v, out);
+  if (lane == 0) {
     double *o = d.long_rsum + 4 * (size_t)(d.lrow_ptr[lr] + part);
     o[0] = out[0]; o[1] = out[1]; o[2] = out[2]; o[3] = out[3];
   }
 }
 
-// Part `part` of long Jacobian entry le (e.g. a supply node's diagonal).
-__device__ __forceinline__ void long_entry_part(const DevArrays &d, int le, int part, double *ws) {
+// Part `part` of long Jacobian entry le (e.g. a supply node's diagonal).  One warp.
+__device__ __forceinline__ void long_entry_part(const DevArrays &d, int le, int part) {
+  const int lane = threadIdx.x & 31;
   const int nparts = d.lent_ptr[le + 1] - d.lent_ptr[le];
   const int e = d.long_ents[le];
-  const int stride = nparts * kGatherLanes;
+  double v[8][1];
+#pragma unroll
+  for (int vw = 0; vw < 8; ++vw) v[vw][0] = 0.0;
+  warp_gather(v, 0, d.m_idx, d.sM, d.m_ptr[e], d.m_ptr[e + 1], part * kGatherLanes + lane, nparts * kGatherLanes);
   double out[1];
-  gather_sums<1>([&](int vl, double *v) {
-    double s = 0.0;
-    for (int k = d.m_ptr[e] + part * kGatherLanes + vl; k < d.m_ptr[e + 1]; k += stride) s += d.sM[d.m_idx[k]];
-    v[0] = s;
-  }, ws, out);
-  if (threadIdx.x == 0) d.long_esum[d.lent_ptr[le] + part] = out[0];
+  warp_totals(v, out);
+  if (lane == 0) d.long_esum[d.lent_ptr[le] + part] = out[0];
 }
 
-// Long rows: ceil(items / kLongPart) blocks per row.
-__global__ void __launch_bounds__(256) k_long_rows(DevArrays d) {
-  __shared__ double ws[8 * 4];
-  const int lr = d.lrow_blk[blockIdx.x];
+// Long rows: a warp per part (ceil(items / 256) parts per row).
+__global__ void __launch_bounds__(256) k_long_rows(DevArrays d, int n_parts) {
+  const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (i >= n_parts) return;
+  const int lr = d.lrow_blk[i];
   if (!circ_active(d.cs[d.circ_of_row[d.long_rows[lr]]])) return;
-  long_row_part(d, lr, blockIdx.x - d.lrow_ptr[lr], ws);
+  long_row_part(d, lr, i - d.lrow_ptr[lr]);
 }
 
-// Long Jacobian entries: ceil(items / kLongPart) blocks each.
-__global__ void __launch_bounds__(256) k_long_entries(DevArrays d) {
-  __shared__ double ws[8];
-  const int le = d.lent_blk[blockIdx.x];
+// Long Jacobian entries: a warp per part.
+__global__ void __launch_bounds__(256) k_long_entries(DevArrays d, int n_parts) {
+  const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (i >= n_parts) return;
+  const int le = d.lent_blk[i];
   if (!circ_active(d.cs[d.circ_of_row[d.erow[d.long_ents[le]]]])) return;
-  long_entry_part(d, le, blockIdx.x - d.lent_ptr[le], ws);
+  long_entry_part(d, le, i - d.lent_ptr[le]);
 }
 
 // Residual per row: RHS = -(qscale (Q - Q_hist0) + fscale (F - B) + hscale Q_hist2 + gshunt x)
@@ -1537,13 +1566,14 @@ __device__ void resident_circuit(const DevArrays &d, const LUDev &L, const Fused
       diode_eval(d, F.d_list[k], A.nd, 1, 1, 0, 0, A.sF_d, A.sQ_d, A.sL_d, A.sM_d);
     __syncthreads();
     clk.mark(XG_RSTAGE_DEVICES);
+    // a warp per part of the circuit's long rows, then of its long entries
     for (int q = F.lr_ptr[c]; q < F.lr_ptr[c + 1]; ++q) {
       const int lr = F.lr_list[q];
-      for (int part = 0; part < d.lrow_ptr[lr + 1] - d.lrow_ptr[lr]; ++part) long_row_part(d, lr, part, ws);
+      for (int part = warp; part < d.lrow_ptr[lr + 1] - d.lrow_ptr[lr]; part += nth >> 5) long_row_part(d, lr, part);
     }
     for (int q = F.le_ptr[c]; q < F.le_ptr[c + 1]; ++q) {
       const int le = F.le_list[q];
-      for (int part = 0; part < d.lent_ptr[le + 1] - d.lent_ptr[le]; ++part) long_entry_part(d, le, part, ws);
+      for (int part = warp; part < d.lent_ptr[le + 1] - d.lent_ptr[le]; part += nth >> 5) long_entry_part(d, le, part);
     }
     __syncthreads();
     clk.mark(XG_RSTAGE_LONG_GATHERS);
@@ -1682,8 +1712,8 @@ void launch_diode_k(cudaStream_t st, const DevArrays &d, int nd, int combined, i
 }
 void launch_assemble_k(cudaStream_t st, const DevArrays &d, int n, int nnz, int n_long_row_blocks,
                        int n_long_ent_blocks) {
-  if (n_long_row_blocks > 0) k_long_rows<<<n_long_row_blocks, 256, 0, st>>>(d);
-  if (n_long_ent_blocks > 0) k_long_entries<<<n_long_ent_blocks, 256, 0, st>>>(d);
+  if (n_long_row_blocks > 0) k_long_rows<<<nblk(n_long_row_blocks, 8), 256, 0, st>>>(d, n_long_row_blocks);
+  if (n_long_ent_blocks > 0) k_long_entries<<<nblk(n_long_ent_blocks, 8), 256, 0, st>>>(d, n_long_ent_blocks);
   k_assemble_rows<<<nblk(n, kRowBlock), kRowBlock, 0, st>>>(d, n);
   k_assemble_J<<<nblk(nnz, 256), 256, 0, st>>>(d, nnz);
 }

@@ -1127,21 +1127,30 @@ Schedule build_schedule(int n, const std::function<void(int, std::vector<int> &)
     if (gid[r] < 0) gid[r] = ng++;
     gid[j] = gid[r];
   }
-  // Pack runs of consecutive tiny groups (e.g. the isolated supply-node and
-  // branch columns of every circuit of a batch) into shared CTAs: they are
-  // independent, so their local levels merge.  Packed groups may mix
-  // circuits; the kernels test each item's circuit.
+  // Groups are independent of one another, so their order is free: the
+  // larger groups first, by decreasing work (the longest CTAs start first,
+  // the launch's tail is short), then the tiny groups (e.g. the isolated
+  // supply-node and branch columns of every circuit of a batch), packed
+  // into shared CTAs up to a size and work cap — their local levels merge.
+  // Packed groups may mix circuits; the kernels test each item's circuit.
   {
     std::vector<int> gsz(ng, 0);
     std::vector<long long> gw(ng, 0);
     for (int j = 0; j < n; ++j)
       if (gid[j] >= 0) { gsz[gid[j]]++; gw[gid[j]] += weight(j); }
+    std::vector<int> gorder(ng);
+    std::iota(gorder.begin(), gorder.end(), 0);
+    std::stable_sort(gorder.begin(), gorder.end(), [&](int a, int b) {
+      const bool sa = gsz[a] <= kPackSmall, sb = gsz[b] <= kPackSmall;
+      if (sa != sb) return sb;  // tiny groups last
+      return !sa && gw[a] > gw[b];
+    });
     std::vector<int> pack(ng);
     int np = 0, cur_size = 0;
     long long cur_w = 0;
     bool cur_small = false;
-    for (int g = 0; g < ng; ++g) {
-      const bool small = gsz[g] <= kPackSmall && gw[g] <= kPackSmallWeight;
+    for (int g : gorder) {
+      const bool small = gsz[g] <= kPackSmall && gw[g] <= kPackCapWeight;
       if (small && cur_small && cur_size + gsz[g] <= kPackCap && cur_w + gw[g] <= kPackCapWeight) {
         pack[g] = np - 1;
         cur_size += gsz[g];
