@@ -306,6 +306,57 @@ def _one_at_a_time(xg, nl, dev, window, stream_of, batched, sample=8, timed=4):
             "batched_over_one_ring_at_a_time": batched / rate}
 
 
+OTHER_CONFIGS = (
+    # name, netlist builder, window (accepted steps per advance), timed windows
+    ("c1_diode_ladder_1000", lambda N: N.diode_ladder(1000, seed=1), 200, 3),
+    ("c2_ring_10001", lambda N: N.ring_oscillator(10001), 200, 3),
+    ("c3_power_grid_200x200", lambda N: N.power_grid(200), 10, 3),
+    ("c3_power_grid_500x500", lambda N: N.power_grid(500), 5, 2),
+    ("c5_bsim4_logic_dag_50000", lambda N: N.bsim4_logic_dag(50000), 10, 3),
+)
+
+
+def _other_configs(xg, dev, flush, stream_of):
+    """Steps/s of the plain FP64 path on the other single-circuit configs,
+    timed like the headline (CUDA events on the context's stream around each
+    advance, L2 flushed between advances, after one warm-up advance past the
+    operating point): the full-size diode ladder, the 10,001-stage ring, the
+    200x200 and 500x500 power grids and the 50k-transistor BSIM4 logic DAG."""
+    import torch
+    from xyce_gb300 import netlist as N
+    out = {}
+    for name, build, window, timed in OTHER_CONFIGS:
+        try:
+            nl = build(N)
+            t0 = time.perf_counter()
+            c = xg.Circuit(nl, device=dev)
+            c.tran_start(probes=[0], cap=16)
+            c.tran_advance(window)
+            setup_s = time.perf_counter() - t0
+            stream = stream_of(c)
+            a0 = c.tran_results()[3]
+            ms = 0.0
+            for _ in range(timed):
+                flush.fill_(1.0)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                c.tran_advance(window)
+                e1.record(stream)
+                e1.synchronize()
+                ms += e0.elapsed_time(e1)
+            a1 = c.tran_results()[3]
+            steps = a1["accepted"] - a0["accepted"]
+            out[name] = {"steps_per_s": steps / (ms / 1e3), "steps": steps, "unknowns": c.n,
+                         "newton_iters_per_step": (a1["newton_iters"] - a0["newton_iters"]) / max(1, steps),
+                         "setup_and_first_window_s": setup_s}
+            c.tran_end()
+            c.close()
+        except Exception as e:  # noqa: BLE001 - reported, not required
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+    return out
+
+
 def _rooflines(circ, nl, window, hbm_peak, peak_kind, info, args):
     """Rooflines of the two dominant kernels of the tick, timed by the tick
     profiler (each stage of PROFILE_TICKS ticks of a new window launched on
@@ -507,10 +558,15 @@ def run_ours(args):
         try:
             c2, ms2, s0, s1 = _timed_windows(xg, nl, probes, dev, args, window, xg.PREC_FP32_IR, flush,
                                              stream_of)
+            t32 = c2.lu_tuning()
             forms = {"fp64": value,
                      "fp32_lu_fp64_ir": (s1["accepted"] - s0["accepted"]) / (ms2 / 1e3),
                      "fp32_lu_fp64_ir_newton_iters_per_step":
-                         (s1["newton_iters"] - s0["newton_iters"]) / max(1, s1["accepted"] - s0["accepted"])}
+                         (s1["newton_iters"] - s0["newton_iters"]) / max(1, s1["accepted"] - s0["accepted"]),
+                     # one factorization and one solve as the tuner timed them on this pattern
+                     # (all circuits refactoring; the FP32 solve includes its refinement steps)
+                     "fp32_factor_us": t32["factor_us"], "fp32_solve_us": t32["solve_us"],
+                     "fp64_factor_us": info["tuning"]["factor_us"], "fp64_solve_us": info["tuning"]["solve_us"]}
             c2.tran_end()
             c2.close()
             # the tick graph alone (15 kernels per tick over the whole batch)
@@ -536,6 +592,11 @@ def run_ours(args):
                 forms.update(_one_at_a_time(xg, nl, dev, window, stream_of, value))
         except Exception as e:  # noqa: BLE001
             forms = {"fp64": value, "error": f"{type(e).__name__}: {e}"}
+
+    # ---- the other configs, plain FP64 path ---------------------------------
+    others = None
+    if rank == 0 and args.others and args.workload == "mc":
+        others = _other_configs(xg, dev, flush, stream_of)
 
     # ---- end to end through the C-ABI with host buffers --------------------
     e2e = None
@@ -584,7 +645,7 @@ def run_ours(args):
                                                            st1["option_us_per_iter"])),
                 "lu": info, "roofline": roof, "roofline_lu": lu_roof, "roofline_resident": resident_roof,
                 "tick_stages_us": stages, "resident_stages": resident_stages,
-                "max_err_vs_fp64": err, "forms": forms, "cpu_baseline": cpu, "e2e": e2e,
+                "max_err_vs_fp64": err, "forms": forms, "other_configs": others, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks}
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -608,6 +669,8 @@ def main():
     ap.add_argument("--ncu-form", default="tick_graph", choices=["tick_graph", "resident"],
                     help="advancing form of the --ncu-case run")
     ap.add_argument("--no-forms", dest="forms", action="store_false", help="skip the FP32-IR form")
+    ap.add_argument("--no-others", dest="others", action="store_false",
+                    help="skip the other configs (diode ladder, 10,001-stage ring, grid, BSIM4 DAG)")
     ap.add_argument("--clocks-csv", default=None,
                     help="keep the nvidia-smi clock samples of the timed region in this file")
     args = ap.parse_args()

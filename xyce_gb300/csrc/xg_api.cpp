@@ -716,6 +716,7 @@ int xg_finalize(xg_ctx *ctx) {
   UP(d.long_rows, long_rows); UP(d.row_long, row_long); UP(d.long_ents, long_ents); UP(d.ent_long, ent_long);
   UP(d.lrow_ptr, lrow_ptr); UP(d.lrow_blk, lrow_blk); UP(d.lent_ptr, lent_ptr); UP(d.lent_blk, lent_blk);
   AL(d.long_rsum, 4 * (size_t)ctx->n_long_row_blocks); AL(d.long_esum, (size_t)ctx->n_long_ent_blocks);
+  AL(d.done_acc, 3);
   AL(d.sF, nF); AL(d.sQ, nQ); AL(d.sL, nL); AL(d.sL2, nL); AL(d.sB, nB); AL(d.sM, nMs); AL(d.sM2, nMs);
   UP(d.src_kind, skind); UP(d.src_off, soff); UP(d.src_circ, scirc); UP(d.src_data, sdata);
   UP(d.m1_node, m1node); UP(d.m1_model, m1model); UP(d.m1_circ, m1circ);

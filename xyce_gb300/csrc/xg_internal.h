@@ -14,8 +14,8 @@ namespace xg {
 
 constexpr int kRowBlock = 256;       // rows per block of the row kernels (fixed: partial slots)
 constexpr int kMaxPwlScan = 1 << 20; // bound on PWL point scans
-constexpr int kLongGather = 96;      // gathers longer than this are split across blocks
-constexpr int kLongPart = 2048;      // gathered items per block of a long gather
+constexpr int kLongGather = 96;      // gathers longer than this are split into parts, a warp each
+constexpr int kLongPart = 256;       // gathered items per part of a long gather
 constexpr int kLongSolveRow = 256;   // triangular-solve rows longer than this get a whole block
 // Frozen-pivot acceptance on the device: a pivot below this fraction of its
 // updated column triggers re-pivoting by the host.
@@ -138,13 +138,15 @@ struct DevArrays {
   int *vB_ptr = nullptr, *vB_idx = nullptr;
   int *m_ptr = nullptr, *m_idx = nullptr;
   char *is_branch = nullptr;                 // per row: voltage-source branch unknown
-  // long gathers, reduced by a block in a pre-pass: rows (F, Q, B, L sums) and J entries
-  // (a long gather of w items is split over ceil(w / kLongPart) blocks; block b
-  // handles part b - ptr[l] of gather l = *_blk[b]; the parts of gather l are
-  // blocks ptr[l] .. ptr[l+1])
+  // long gathers, reduced by warps in a pre-pass: rows (F, Q, B, L sums) and J entries
+  // (a long gather of w items is split into P = ceil(w / kLongPart) parts;
+  // part b handles part b - ptr[l] of gather l = *_blk[b]; the parts of
+  // gather l are ptr[l] .. ptr[l+1]; part p of P takes the items p*32 + lane
+  // + m*32*P of each list)
   int *long_rows = nullptr, *row_long = nullptr, *long_ents = nullptr, *ent_long = nullptr;
   int *lrow_ptr = nullptr, *lrow_blk = nullptr, *lent_ptr = nullptr, *lent_blk = nullptr;
   double *long_rsum = nullptr, *long_esum = nullptr;
+  unsigned long long *done_acc = nullptr;  // completion count scratch: [done, Newton iterations, blocks]
   // slot value buffers
   double *sF = nullptr, *sQ = nullptr, *sL = nullptr, *sL2 = nullptr, *sB = nullptr;
   double *sM = nullptr, *sM2 = nullptr;   // combined J slots / (dF, dQ) in separate mode

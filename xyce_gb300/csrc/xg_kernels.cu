@@ -551,51 +551,25 @@ __device__ void block_partials(const DevArrays &d, int n, double vmax, double vs
   (void)r;
 }
 
-// Sums of a long gather in a fixed order, whatever the CTA size: 256
-// virtual lanes (8 virtual warps) each accumulate their strided share, each
-// virtual warp reduces by a butterfly, and one warp reduces the 8 warp sums
-// by a butterfly over 32 lanes (zeros beyond the 8).  W values per lane;
-// the results land in out[0 .. W) of thread 0.  ws: 8 * W doubles of shared
-// memory.
-constexpr int kGatherLanes = 256;
-
-// One part of a long gather, summed in a fixed order by one warp: 256
-// virtual lanes (virtual lane vl = 32 vw + lane of virtual warp vw sums the
-// part's items vl, vl + stride, ... in order), a butterfly within each
-// virtual warp, then the eight virtual-warp totals by a butterfly over
-// lanes 0..7 (lanes 8..31 add zeros).  Each lane runs its eight virtual
-// lanes round by round, so their loads are independent.  All lanes return
-// the totals.
-template <int W>
-__device__ __forceinline__ void warp_totals(double (&v)[8][W], double *out) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int k = 0; k < W; ++k) {
-    double t = 0.0;
-#pragma unroll
-    for (int vw = 0; vw < 8; ++vw) {
-      double s = v[vw][k];
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == vw) t = s;  // every lane holds the same total (the butterfly's sums commute)
-    }
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    out[k] = t;
+// Long gathers: part p of a gather in P parts is summed by one warp — lane
+// l adds the items p*32 + l + m*32*P of each list in order (four loads in
+// flight), then a butterfly over the 32 lanes.  Every lane ends with the
+// same total (the butterfly's additions commute); the parts of a gather are
+// added in order by the row / entry that owns it.
+__device__ __forceinline__ double gather_seq(double acc, const int *idx, const double *sv, int k, int k1,
+                                             int stride) {
+  for (; k + 3 * stride < k1; k += 4 * stride) {
+    const int i0 = idx[k], i1 = idx[k + stride], i2 = idx[k + 2 * stride], i3 = idx[k + 3 * stride];
+    const double a0 = sv[i0], a1 = sv[i1], a2 = sv[i2], a3 = sv[i3];
+    acc += a0; acc += a1; acc += a2; acc += a3;
   }
+  for (; k < k1; k += stride) acc += sv[idx[k]];
+  return acc;
 }
 
-// Adds sv[idx[k]] for the part's items of list [k0, k1) into v[vw][f]:
-// item k0 + off + 32 vw for off = start, start + stride, ...
-template <int W>
-__device__ __forceinline__ void warp_gather(double (&v)[8][W], int f, const int *idx, const double *sv, int k0,
-                                            int k1, int start, int stride) {
-  for (int off = start; k0 + off < k1; off += stride) {
-    int ix[8];
-#pragma unroll
-    for (int vw = 0; vw < 8; ++vw) ix[vw] = (k0 + off + 32 * vw < k1) ? idx[k0 + off + 32 * vw] : -1;
-#pragma unroll
-    for (int vw = 0; vw < 8; ++vw)
-      if (ix[vw] >= 0) v[vw][f] += sv[ix[vw]];
-  }
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
 }
 
 // Part `part` of long row lr (e.g. a supply node touching every PMOS): the
@@ -605,35 +579,29 @@ __device__ __forceinline__ void long_row_part(const DevArrays &d, int lr, int pa
   const int lane = threadIdx.x & 31;
   const int nparts = d.lrow_ptr[lr + 1] - d.lrow_ptr[lr];
   const int r = d.long_rows[lr];
-  const int stride = nparts * kGatherLanes, start = part * kGatherLanes + lane;
-  double v[8][4];
-#pragma unroll
-  for (int vw = 0; vw < 8; ++vw) v[vw][0] = v[vw][1] = v[vw][2] = v[vw][3] = 0.0;
+  const int stride = 32 * nparts, start = 32 * part + lane;
+  double F = 0.0, Q = 0.0;
   {
-    const int e0 = d.rp[r], e1 = d.rp[r + 1];
-    for (int off = start; e0 + off < e1; off += stride) {
-      double xv[8];
-#pragma unroll
-      for (int vw = 0; vw < 8; ++vw) xv[vw] = (e0 + off + 32 * vw < e1) ? d.x[d.ci[e0 + off + 32 * vw]] : 0.0;
-#pragma unroll
-      for (int vw = 0; vw < 8; ++vw) {
-        const int e = e0 + off + 32 * vw;
-        if (e < e1) {
-          v[vw][0] += d.Glin[e] * xv[vw];
-          v[vw][1] += d.Clin[e] * xv[vw];
-        }
-      }
+    int e = d.rp[r] + start;
+    const int e1 = d.rp[r + 1];
+    for (; e + stride < e1; e += 2 * stride) {
+      const double x0 = d.x[d.ci[e]], x1 = d.x[d.ci[e + stride]];
+      F += d.Glin[e] * x0; Q += d.Clin[e] * x0;
+      F += d.Glin[e + stride] * x1; Q += d.Clin[e + stride] * x1;
+    }
+    if (e < e1) {
+      const double x0 = d.x[d.ci[e]];
+      F += d.Glin[e] * x0; Q += d.Clin[e] * x0;
     }
   }
-  warp_gather(v, 0, d.vF_idx, d.sF, d.vF_ptr[r], d.vF_ptr[r + 1], start, stride);
-  warp_gather(v, 1, d.vQ_idx, d.sQ, d.vQ_ptr[r], d.vQ_ptr[r + 1], start, stride);
-  warp_gather(v, 2, d.vB_idx, d.sB, d.vB_ptr[r], d.vB_ptr[r + 1], start, stride);
-  warp_gather(v, 3, d.vL_idx, d.sL, d.vL_ptr[r], d.vL_ptr[r + 1], start, stride);
-  double out[4];
-  warp_totals(v, out);
+  F = gather_seq(F, d.vF_idx, d.sF, d.vF_ptr[r] + start, d.vF_ptr[r + 1], stride);
+  Q = gather_seq(Q, d.vQ_idx, d.sQ, d.vQ_ptr[r] + start, d.vQ_ptr[r + 1], stride);
+  const double B = gather_seq(0.0, d.vB_idx, d.sB, d.vB_ptr[r] + start, d.vB_ptr[r + 1], stride);
+  const double L = gather_seq(0.0, d.vL_idx, d.sL, d.vL_ptr[r] + start, d.vL_ptr[r + 1], stride);
+  const double tF = warp_sum(F), tQ = warp_sum(Q), tB = warp_sum(B), tL = warp_sum(L);
   if (lane == 0) {
     double *o = d.long_rsum + 4 * (size_t)(d.lrow_ptr[lr] + part);
-    o[0] = out[0]; o[1] = out[1]; o[2] = out[2]; o[3] = out[3];
+    o[0] = tF; o[1] = tQ; o[2] = tB; o[3] = tL;
   }
 }
 
@@ -642,13 +610,9 @@ __device__ __forceinline__ void long_entry_part(const DevArrays &d, int le, int 
   const int lane = threadIdx.x & 31;
   const int nparts = d.lent_ptr[le + 1] - d.lent_ptr[le];
   const int e = d.long_ents[le];
-  double v[8][1];
-#pragma unroll
-  for (int vw = 0; vw < 8; ++vw) v[vw][0] = 0.0;
-  warp_gather(v, 0, d.m_idx, d.sM, d.m_ptr[e], d.m_ptr[e + 1], part * kGatherLanes + lane, nparts * kGatherLanes);
-  double out[1];
-  warp_totals(v, out);
-  if (lane == 0) d.long_esum[d.lent_ptr[le] + part] = out[0];
+  const double s = gather_seq(0.0, d.m_idx, d.sM, d.m_ptr[e] + 32 * part + lane, d.m_ptr[e + 1], 32 * nparts);
+  const double t = warp_sum(s);
+  if (lane == 0) d.long_esum[d.lent_ptr[le] + part] = t;
 }
 
 // Long rows: a warp per part (ceil(items / 256) parts per row).
@@ -1310,27 +1274,44 @@ __global__ void k_state_commit(DevArrays d, int nm, int nd, int sto_base_m, int 
 // into mapped host memory that the host loop reads between tick batches.
 // status_out: [0] circuits done, failed or paused, [1] breakdown flag,
 // [2..3] (one 64-bit word) Newton iterations run so far, summed over circuits.
-__global__ void k_count_done(DevArrays d, int ncirc, const int *breakdown, int *status_out) {
-  __shared__ int cnt;
-  __shared__ unsigned long long iters;
-  if (threadIdx.x == 0) { cnt = 0; iters = 0; }
+// A thread per circuit; the blocks add into d.done_acc and the last block to
+// finish writes the status and clears the accumulators for the next launch.
+__global__ void __launch_bounds__(256) k_count_done(DevArrays d, int ncirc, const int *breakdown, int *status_out) {
+  __shared__ unsigned long long s_cnt, s_it;
+  __shared__ bool last;
+  if (threadIdx.x == 0) { s_cnt = 0; s_it = 0; }
   __syncthreads();
-  int local = 0;
-  unsigned long long it = 0;
-#pragma unroll 4
-  for (int c = threadIdx.x; c < ncirc; c += blockDim.x) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long cnt = 0, it = 0;
+  if (c < ncirc) {
     const CircState &s = d.cs[c];
-    int ph = s.phase;
-    local += (ph == PH_DONE || ph == PH_FAILED || ph == PH_PAUSED) ? 1 : 0;
-    it += (unsigned long long)(s.newton_iters + s.dcop_iters);
+    const int ph = s.phase;
+    cnt = (ph == PH_DONE || ph == PH_FAILED || ph == PH_PAUSED) ? 1 : 0;
+    it = (unsigned long long)(s.newton_iters + s.dcop_iters);
   }
-  atomicAdd(&cnt, local);
-  atomicAdd(&iters, it);
+  for (int o = 16; o > 0; o >>= 1) {
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    it += __shfl_xor_sync(0xffffffffu, it, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&s_cnt, cnt);
+    atomicAdd(&s_it, it);
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
-    status_out[0] = cnt;
+    atomicAdd(d.done_acc, s_cnt);
+    atomicAdd(d.done_acc + 1, s_it);
+    __threadfence();
+    last = atomicAdd(d.done_acc + 2, 1ULL) == (unsigned long long)gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    const unsigned long long total = atomicAdd(d.done_acc, 0ULL), iters = atomicAdd(d.done_acc + 1, 0ULL);
+    status_out[0] = (int)total;
     status_out[1] = *breakdown;
     reinterpret_cast<unsigned long long *>(status_out)[1] = iters;
+    d.done_acc[0] = 0; d.done_acc[1] = 0; d.done_acc[2] = 0;
   }
 }
 
@@ -1745,7 +1726,7 @@ void launch_state_commit_k(cudaStream_t st, const DevArrays &d, int nm, int nd, 
 }
 void launch_count_done_k(cudaStream_t st, const DevArrays &d, int ncirc, const int *breakdown,
                          int *status_out) {
-  k_count_done<<<1, 1024, 0, st>>>(d, ncirc, breakdown, status_out);
+  k_count_done<<<nblk(ncirc, 256), 256, 0, st>>>(d, ncirc, breakdown, status_out);
 }
 // Next advance: pause again after n_steps more accepted steps (unbounded if <= 0).
 __global__ void k_set_target(DevArrays d, int ncirc, int n_steps) {
