@@ -553,45 +553,46 @@ def run_ours(args):
     # ---- the FP32-LU + FP64-refinement form, same workload ------------------
     forms = None
     if rank == 0 and args.forms:
-        # the comparison forms are reported, not required: a failure there
-        # is recorded in the line instead of losing it
-        try:
-            c2, ms2, s0, s1 = _timed_windows(xg, nl, probes, dev, args, window, xg.PREC_FP32_IR, flush,
-                                             stream_of)
-            t32 = c2.lu_tuning()
-            forms = {"fp64": value,
-                     "fp32_lu_fp64_ir": (s1["accepted"] - s0["accepted"]) / (ms2 / 1e3),
-                     "fp32_lu_fp64_ir_newton_iters_per_step":
-                         (s1["newton_iters"] - s0["newton_iters"]) / max(1, s1["accepted"] - s0["accepted"]),
-                     # one factorization and one solve as the tuner timed them on this pattern
-                     # (all circuits refactoring; the FP32 solve includes its refinement steps)
-                     "fp32_factor_us": t32["factor_us"], "fp32_solve_us": t32["solve_us"],
-                     "fp64_factor_us": info["tuning"]["factor_us"], "fp64_solve_us": info["tuning"]["solve_us"]}
-            c2.tran_end()
-            c2.close()
-            # the tick graph alone (15 kernels per tick over the whole batch)
-            c5, ms5, s0, s1 = _timed_windows(xg, nl, probes, dev, args, window, xg.PREC_FP64, flush, stream_of,
-                                             form=xg.FORM_TICK_GRAPH)
-            forms["fp64_tick_graph"] = (s1["accepted"] - s0["accepted"]) / (ms5 / 1e3)
-            c5.tran_end()
-            c5.close()
-            if st1["option"] == 5 and form == "tick_graph" and any(st1["option_us_per_iter"][:5]):
-                # the timed trials chose the tick graph: the resident form alone, for comparison
-                c6, ms6, s0, s1 = _timed_windows(xg, nl, probes, dev, args, window, xg.PREC_FP64, flush,
-                                                 stream_of, form=xg.FORM_RESIDENT)
-                forms["fp64_resident"] = (s1["accepted"] - s0["accepted"]) / (ms6 / 1e3)
-                c6.tran_end()
-                c6.close()
-            # the LU sweeps with the analysis' closed-form launch shapes instead of the timed ones
-            c4, ms4, s0, s1 = _timed_windows(xg, nl, probes, dev, args, window, xg.PREC_FP64, flush, stream_of,
-                                             tune=xg.TUNE_MODEL, form=xg.FORM_TICK_GRAPH)
-            forms["fp64_tick_graph_lu_model_shapes"] = (s1["accepted"] - s0["accepted"]) / (ms4 / 1e3)
-            c4.tran_end()
-            c4.close()
-            if args.workload == "mc":
-                forms.update(_one_at_a_time(xg, nl, dev, window, stream_of, value))
-        except Exception as e:  # noqa: BLE001
-            forms = {"fp64": value, "error": f"{type(e).__name__}: {e}"}
+        # the comparison forms are reported, not required: a failure of one
+        # is recorded under its name instead of losing the others
+        forms = {"fp64": value}
+
+        def rate(prec, **kw):
+            c, ms_, s0_, s1_ = _timed_windows(xg, nl, probes, dev, args, window, prec, flush, stream_of, **kw)
+            tun = c.lu_tuning()
+            c.tran_end()
+            c.close()
+            steps = s1_["accepted"] - s0_["accepted"]
+            return steps / (ms_ / 1e3), (s1_["newton_iters"] - s0_["newton_iters"]) / max(1, steps), tun
+
+        def attempt(name, fn):
+            try:
+                fn()
+            except Exception as e:  # noqa: BLE001
+                forms[name + "_error"] = f"{type(e).__name__}: {e}"
+
+        def fp32():
+            r, it, t32 = rate(xg.PREC_FP32_IR)
+            forms.update({"fp32_lu_fp64_ir": r, "fp32_lu_fp64_ir_newton_iters_per_step": it,
+                          # one factorization and one solve as the tuner timed them on this pattern
+                          # (all circuits refactoring; the FP32 solve includes its refinement steps)
+                          "fp32_factor_us": t32["factor_us"], "fp32_solve_us": t32["solve_us"],
+                          "fp64_factor_us": info["tuning"]["factor_us"], "fp64_solve_us": info["tuning"]["solve_us"]})
+
+        attempt("fp32_lu_fp64_ir", fp32)
+        # the tick graph alone (15 kernels per tick over the whole batch)
+        attempt("fp64_tick_graph",
+                lambda: forms.__setitem__("fp64_tick_graph", rate(xg.PREC_FP64, form=xg.FORM_TICK_GRAPH)[0]))
+        if st1["option"] == 5 and form == "tick_graph" and any(st1["option_us_per_iter"][:5]):
+            # the timed trials chose the tick graph: the resident form alone, for comparison
+            attempt("fp64_resident",
+                    lambda: forms.__setitem__("fp64_resident", rate(xg.PREC_FP64, form=xg.FORM_RESIDENT)[0]))
+        # the LU sweeps with the analysis' closed-form launch shapes instead of the timed ones
+        attempt("fp64_tick_graph_lu_model_shapes",
+                lambda: forms.__setitem__("fp64_tick_graph_lu_model_shapes",
+                                          rate(xg.PREC_FP64, tune=xg.TUNE_MODEL, form=xg.FORM_TICK_GRAPH)[0]))
+        if args.workload == "mc":
+            attempt("one_ring_at_a_time", lambda: forms.update(_one_at_a_time(xg, nl, dev, window, stream_of, value)))
 
     # ---- the other configs, plain FP64 path ---------------------------------
     others = None

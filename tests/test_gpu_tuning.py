@@ -22,6 +22,10 @@ def torch_cuda():
 _CASES = {
     "mc64": (lambda: N.monte_carlo_rings(64, seed=11), lambda nl: [nl.names[f"c{i}.n1"] for i in (0, 31, 63)],
              0.5e-9),
+    # enough groups for single-thread factor columns, and packs of supply
+    # columns that mix circuits
+    "mc1024": (lambda: N.monte_carlo_rings(1024, seed=11),
+               lambda nl: [nl.names[f"c{i}.n1"] for i in range(0, 1024, 97)], 0.3e-9),
     "ring101": (lambda: N.ring_oscillator(101), lambda nl: [nl.names["n1"], nl.names["n50"]], 2e-9),
     "grid40": (lambda: N.power_grid(40, 50, seed=2), lambda nl: [nl.names["center"]], 0.2e-9),
     "b4dag3000": (lambda: N.bsim4_logic_dag(3000, 16, seed=9, tstop=1e-9), lambda nl: [nl.names["g40"]], 0.3e-9),

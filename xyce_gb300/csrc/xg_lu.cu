@@ -358,6 +358,9 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
       __syncthreads();
     }
   } else {
+    // every column staged before any is read (a column's thread or warp
+    // need not be the warp that staged it)
+    __syncthreads();
     for (int lv = SD.grp_lvl[g]; lv < SD.grp_lvl[g + 1]; ++lv) {
       const int b = SD.lvl_ptr[lv], e = SD.lvl_ptr[lv + 1];
       bool any_long = false;
@@ -383,10 +386,14 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
     }
   }
   __syncthreads();
-  // write the factored columns back (the solves and the top read them)
+  // write the factored columns back (the solves and the top read them); a
+  // group that mixes circuits writes only the columns it factored, so the
+  // factors of a circuit that is not refactoring stay as they are
   T *lu = lu_of<T>(L);
+  const bool mixed = masked && L.fs_gcirc && L.fs_gcirc[g] < 0;
   for (int t = it0 + warp; t < it1; t += nwarps) {
     const int j = SD.items[t], p0 = L.cp[j], p1 = L.cp[j + 1], o = L.grp_soff[j];
+    if (mixed && !factor_active(L, cs, masked, j)) continue;
     for (int p = p0 + lane; p < p1; p += 32) lu[p] = S[o + (p - p0)];
   }
 }
