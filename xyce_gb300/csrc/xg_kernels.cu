@@ -1392,7 +1392,8 @@ struct StageClock {
   }
 };
 
-// The factorization of circuit c, level by level: single-thread columns,
+// The factorization of circuit c (refactoring this tick: every column is
+// factored), level by level: single-thread columns,
 // warp columns, then the columns that take the whole CTA (each level's
 // items are sorted by kind; F.f_split gives where the warp and CTA kinds
 // start).  S (when the circuit's columns fit): the circuit's columns are
@@ -1418,11 +1419,10 @@ __device__ void resident_factor(const DevArrays &d, const LUDev &L, const FusedD
     const int2 sp = F.f_split[lv];
     for (int t = a + tid; t < sp.x; t += nth) {
       const int j = F.f_items[t];
-      if (factor_active(L, d.cs, 1, j)) factor_column_t<double>(L, d.J, j, d.cs, 1, pivot_tol, S, soff, umeta);
+      factor_column_t<double>(L, d.J, j, d.cs, 1, pivot_tol, S, soff, umeta);
     }
     for (int t = sp.x + warp; t < sp.y; t += nwarps) {
       const int j = F.f_items[t];
-      if (!factor_active(L, d.cs, 1, j)) continue;
       if (S) factor_column_s<false, double>(L, j, d.cs, 1, pivot_tol, sm, S, soff, umeta);
       else factor_column<false, double>(L, d.J, j, d.cs, 1, pivot_tol, sm);
     }
@@ -1431,7 +1431,6 @@ __device__ void resident_factor(const DevArrays &d, const LUDev &L, const FusedD
     __syncthreads();
     for (int t = sp.y; t < b; ++t) {
       const int j = F.f_items[t];
-      if (!factor_active(L, d.cs, 1, j)) continue;
       if (S) factor_column_s<true, double>(L, j, d.cs, 1, pivot_tol, sm, S, soff, umeta);
       else factor_column<true, double>(L, d.J, j, d.cs, 1, pivot_tol, sm);
       __syncthreads();

@@ -59,24 +59,27 @@ __device__ void factor_group(const LUDev &L, const double *__restrict__ vals, Ci
                              double pivot_tol, double *sm, int g) {
   const SchedDev &S = L.fs;
   const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  // one circuit's group (not idle: tested by the caller) or the top: test
+  // the columns of the top and of groups that mix circuits only
+  const bool multi = masked && (g >= S.n_groups || !L.fs_gcirc || L.fs_gcirc[g] < 0);
   for (int lv = S.grp_lvl[g]; lv < S.grp_lvl[g + 1]; ++lv) {
     const int b = S.lvl_ptr[lv], e = S.lvl_ptr[lv + 1];
     bool any_long = false;
     for (int t = b + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
       const int j = S.items[t];
-      if (S.is_thread[j] && factor_active(L, cs, masked, j))
+      if (S.is_thread[j] && (!multi || factor_active(L, cs, masked, j)))
         factor_column_t<T>(L, vals, j, cs, masked, pivot_tol, nullptr, L.grp_soff, L.umeta);
     }
     for (int t = b + warp; t < e; t += nwarps) {
       const int j = S.items[t];
       if (S.is_long[j]) { any_long = true; continue; }
       if (S.is_thread[j]) continue;
-      if (factor_active(L, cs, masked, j)) factor_column<false, T>(L, vals, j, cs, masked, pivot_tol, sm);
+      if (!multi || factor_active(L, cs, masked, j)) factor_column<false, T>(L, vals, j, cs, masked, pivot_tol, sm);
     }
     if (__syncthreads_or(any_long)) {
       for (int t = b; t < e; ++t) {
         const int j = S.items[t];
-        if (!S.is_long[j] || !factor_active(L, cs, masked, j)) continue;
+        if (!S.is_long[j] || !(!multi || factor_active(L, cs, masked, j))) continue;
         factor_column<true, T>(L, vals, j, cs, masked, pivot_tol, sm);
         __syncthreads();
       }
@@ -307,6 +310,10 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
   const SchedDev &SD = L.fs;
   const int g = blockIdx.x;
   if (factor_group_idle(L, cs, masked, L.fs_gcirc, g)) return;
+  // a group of one circuit that is not idle refactors every column (its
+  // circuit's state is tested once, above); a group that mixes circuits
+  // tests each column's
+  const bool multi = masked && (!L.fs_gcirc || L.fs_gcirc[g] < 0);
   if (L.grp_snz[g] > cap) {  // too large for the buffer: factor in place in global memory
     factor_group<T>(L, vals, cs, masked, pivot_tol, sm, g);
     return;
@@ -347,12 +354,12 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
       const int b = SD.lvl_ptr[lv], e = SD.lvl_ptr[lv + 1];
       for (int t = b + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
         const int j = SD.items[t];
-        if (SD.is_thread[j] && factor_active(L, cs, masked, j))
+        if (SD.is_thread[j] && (!multi || factor_active(L, cs, masked, j)))
           factor_column_m<1, T>(L, j, t - it0, cs, masked, pivot_tol, sm, S, M);
       }
       for (int t = b + warp; t < e; t += nwarps) {
         const int j = SD.items[t];
-        if (SD.is_thread[j] || !factor_active(L, cs, masked, j)) continue;
+        if (SD.is_thread[j] || !(!multi || factor_active(L, cs, masked, j))) continue;
         factor_column_m<32, T>(L, j, t - it0, cs, masked, pivot_tol, sm, S, M);
       }
       __syncthreads();
@@ -366,19 +373,19 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
       bool any_long = false;
       for (int t = b + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
         const int j = SD.items[t];
-        if (SD.is_thread[j] && factor_active(L, cs, masked, j))
+        if (SD.is_thread[j] && (!multi || factor_active(L, cs, masked, j)))
           factor_column_t<T>(L, vals, j, cs, masked, pivot_tol, S, L.grp_soff, L.umeta);
       }
       for (int t = b + warp; t < e; t += nwarps) {
         const int j = SD.items[t];
         if (SD.is_long[j]) { any_long = true; continue; }
-        if (SD.is_thread[j] || !factor_active(L, cs, masked, j)) continue;
+        if (SD.is_thread[j] || !(!multi || factor_active(L, cs, masked, j))) continue;
         factor_column_s<false, T>(L, j, cs, masked, pivot_tol, sm, S, L.grp_soff, L.umeta);
       }
       if (__syncthreads_or(any_long)) {
         for (int t = b; t < e; ++t) {
           const int j = SD.items[t];
-          if (!SD.is_long[j] || !factor_active(L, cs, masked, j)) continue;
+          if (!SD.is_long[j] || !(!multi || factor_active(L, cs, masked, j))) continue;
           factor_column_s<true, T>(L, j, cs, masked, pivot_tol, sm, S, L.grp_soff, L.umeta);
           __syncthreads();
         }
@@ -390,10 +397,9 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
   // group that mixes circuits writes only the columns it factored, so the
   // factors of a circuit that is not refactoring stay as they are
   T *lu = lu_of<T>(L);
-  const bool mixed = masked && L.fs_gcirc && L.fs_gcirc[g] < 0;
   for (int t = it0 + warp; t < it1; t += nwarps) {
     const int j = SD.items[t], p0 = L.cp[j], p1 = L.cp[j + 1], o = L.grp_soff[j];
-    if (mixed && !factor_active(L, cs, masked, j)) continue;
+    if (multi && !factor_active(L, cs, masked, j)) continue;
     for (int p = p0 + lane; p < p1; p += 32) lu[p] = S[o + (p - p0)];
   }
 }
