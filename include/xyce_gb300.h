@@ -338,6 +338,8 @@ typedef struct xg_tran_stats {
                                                   5 tick graph */
   double option_us_per_iter[6];                /* device time per circuit Newton iteration of each timed
                                                   option, microseconds (0: not timed) */
+  long long tail_launches;                     /* resident launches that finished tick-graph advances
+                                                  (xg_tran_set_tail) */
 } xg_tran_stats;
 
 /* How a transient advances.  XG_FORM_TICK_GRAPH: a tick (one Newton
@@ -362,6 +364,14 @@ typedef struct xg_tran_stats {
 #define XG_FORM_TICK_GRAPH  1
 #define XG_FORM_RESIDENT    2
 int xg_tran_set_form(xg_ctx *ctx, int form);
+
+/* The tail of an advance under the tick graph: once at most active_fraction
+ * of the batch's circuits are still running (checked between batches of 64
+ * ticks), one resident-kernel launch (256-thread CTAs) finishes them, each
+ * circuit at its own pace, instead of more full-batch tick graphs.  The
+ * same bits either way.  Applies where the resident form does; 0 turns it
+ * off.  No reference counterpart. */
+int xg_tran_set_tail(xg_ctx *ctx, double active_fraction);
 
 /* Runs the transient.  probes: global unknown indices to record; every
  * circuit records, at each accepted point, its time and the values of the

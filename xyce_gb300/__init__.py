@@ -50,7 +50,7 @@ EXPORTED = [
     "xg_load_dae_matrices", "xg_lu_analyze", "xg_lu_factor", "xg_lu_solve",
     "xg_lu_solve_noalloc", "xg_lu_set_precision", "xg_lu_info", "xg_lu_schedule_info", "xg_lu_set_schedule", "xg_lu_analyze_pattern",
     "xg_lu_set_tuning", "xg_lu_tuning_info", "xg_lu_set_reuse", "xg_lu_set_pivot_tolerance",
-    "xg_transient", "xg_tran_set_form", "xg_tran_start", "xg_tran_advance", "xg_tran_results", "xg_tran_end",
+    "xg_transient", "xg_tran_set_form", "xg_tran_set_tail", "xg_tran_start", "xg_tran_advance", "xg_tran_results", "xg_tran_end",
     "xg_tran_predictors", "xg_tran_orders", "xg_tran_profile", "xg_tran_profile_resident", "xg_tran_predictor_stats", "xg_set_predictor", "xg_mlp_set", "xg_mlp_get",
     "xg_mlp_train", "xg_mlp_grad", "xg_mlp_forward",
     "xg_dcop", "xg_newton_solve", "xg_version",
@@ -95,7 +95,8 @@ class TranStats(C.Structure):
                 ("t_final_max", C.c_double), ("seconds", C.c_double), ("kernels_per_tick", C.c_int),
                 ("form", C.c_int), ("kernel_launches", C.c_longlong), ("circuit_ticks", C.c_longlong),
                 ("factor_skips", C.c_longlong), ("resident_threads", C.c_int),
-                ("option", C.c_int), ("option_us_per_iter", C.c_double * 6)]
+                ("option", C.c_int), ("option_us_per_iter", C.c_double * 6),
+                ("tail_launches", C.c_longlong)]
 
     def as_dict(self):
         out = {}
@@ -164,6 +165,7 @@ def lib() -> C.CDLL:
     L.xg_tran_start.argtypes = [P, C.POINTER(TranParams), I, ip, I]
     L.xg_tran_advance.argtypes = [P, I]
     L.xg_tran_set_form.argtypes = [P, I]
+    L.xg_tran_set_tail.argtypes = [P, C.c_double]
     L.xg_tran_results.argtypes = [P, ip, dp, dp, C.POINTER(TranStats)]
     L.xg_tran_end.argtypes = [P]
     L.xg_dcop.argtypes = [P, dp, C.POINTER(I)]
@@ -371,6 +373,12 @@ class Circuit:
     def tran_set_form(self, form: int):
         """FORM_AUTO, FORM_TICK_GRAPH or FORM_RESIDENT (see xg_tran_set_form)."""
         self._check(lib().xg_tran_set_form(self.h, int(form)))
+
+    def tran_set_tail(self, active_fraction: float):
+        """Finish a tick-graph advance with the resident kernel once at most
+        this fraction of the circuits is still running (0: off; see
+        xg_tran_set_tail)."""
+        self._check(lib().xg_tran_set_tail(self.h, float(active_fraction)))
 
     def tran_start(self, tran=None, probes=(), cap=0):
         """Operating point + first analysis; keeps the run resident for tran_advance."""

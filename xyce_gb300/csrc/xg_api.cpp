@@ -56,6 +56,7 @@ struct xg_ctx {
   // Jacobian entries (kept for the circuit-resident tick's per-circuit lists)
   std::vector<int> m1_circ_h, d_circ_h, src_circ_h, long_rows_h, long_ents_h;
   int form = XG_FORM_AUTO;          // xg_tran_set_form
+  double tail_fraction = 0.0;       // xg_tran_set_tail
   bool resident_ok = false;         // the current analysis admits the circuit-resident tick
   FusedDev F;                       // its device lists (allocated with the analysis)
   int resident_slots[8] = {0};
@@ -1555,6 +1556,7 @@ struct TranRun {
   cudaEvent_t res_ev[2] = {nullptr, nullptr};
   int res_threads = 0;                    // CTA size of the last resident launch
   long long graph_trial_ticks = 0;        // ticks of the tick-graph trial so far
+  long long tail_launches = 0;            // resident launches that finished a tick-graph advance
   bool try_resident = false, try_graph = true;
   bool operating_point = false;           // xg_tran_start's run to the operating point: no trials
   std::chrono::steady_clock::time_point t0;
@@ -1774,11 +1776,18 @@ int run_until_idle(TranRun &R) {
       R.pending_iters0 = iters_now;
       CK(cudaEventRecord(R.res_ev[0], ctx->stream));
     }
-    R.resident = opt != TranRun::kGraphOption;
+    // the tail of an advance under the tick graph: once few circuits are
+    // still active, the resident kernel finishes them (the same bits; a
+    // handful of circuits no longer pays full-batch launches per tick)
+    const int active = ctx->ncirc - finished;
+    const bool tail = opt == TranRun::kGraphOption && ctx->resident_ok && ctx->tail_fraction > 0.0 &&
+                      active <= ctx->tail_fraction * ctx->ncirc;
+    R.resident = opt != TranRun::kGraphOption || tail;
     if (R.resident) {
       // every circuit runs its ticks in one CTA until it pauses, finishes,
       // fails or parks on a pivot breakdown
-      R.res_threads = kResidentThreads[opt];
+      R.res_threads = tail ? kResidentThreads[3] : kResidentThreads[opt];
+      if (tail) R.tail_launches++;
       launch_resident_k(ctx->stream, d, ctx->L, ctx->F, R.res_threads, ctx->ncirc, ctx->nm, ctx->nd, ctx->nv,
                         ctx->sto_base_m, ctx->resident_slots, R.bps, R.bp_ptr, R.cap, R.pmax, R.pivot_tol);
       if (trial) CK(cudaEventRecord(R.res_ev[1], ctx->stream));
@@ -1957,6 +1966,14 @@ extern "C" int xg_tran_set_form(xg_ctx *ctx, int form) {
   return XG_OK;
 }
 
+extern "C" int xg_tran_set_tail(xg_ctx *ctx, double active_fraction) {
+  if (!ctx) return XG_ERR_ARG;
+  if (!(active_fraction >= 0.0 && active_fraction <= 1.0))
+    return fail(ctx, XG_ERR_ARG, "active_fraction must be in [0, 1]");
+  ctx->tail_fraction = active_fraction;
+  return XG_OK;
+}
+
 extern "C" int xg_tran_advance(xg_ctx *ctx, int n_steps) {
   if (!ctx) return XG_ERR_ARG;
   if (!ctx->run || !ctx->run->exec) return fail(ctx, XG_ERR_STATE, "call xg_tran_start first");
@@ -2014,6 +2031,7 @@ extern "C" int xg_tran_results(xg_ctx *ctx, int *counts, double *times, double *
     stats->circuit_ticks = R.circuit_ticks;
     stats->resident_threads = R.res_threads;
     stats->option = R.option;
+    stats->tail_launches = R.tail_launches;
     for (int k = 0; k < TranRun::kOptions; ++k)
       stats->option_us_per_iter[k] = R.opt_iters[k] > 0 ? 1e3 * R.opt_ms[k] / R.opt_iters[k] : 0.0;
     stats->device_evals = evals;

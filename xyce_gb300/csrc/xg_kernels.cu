@@ -754,8 +754,34 @@ __global__ void k_load_matrices(DevArrays d, int nnz, double *dQdx, double *dFdx
 
 // ---------------------------------------------------------------------------
 // Per-circuit Newton decision: DampedNewton::converged_ (N_NLS_DampedNewton.C:1191-1396).
-// One warp per circuit (all 32 lanes call it) reduces the row partials of
-// its residual.
+// A warp reduces the row partials of a circuit's residual; one thread then
+// takes the decision.
+//
+// The max and the sum of circuit c's per-(row block, circuit) partials, by
+// one warp (lane-strided, then a butterfly: every lane gets the totals), and
+// whether any partial is NaN.
+__device__ __forceinline__ void circuit_norms(const DevArrays &d, int c, int lane, double &m, double &sum,
+                                              bool *bad) {
+  m = 0.0;
+  sum = 0.0;
+  bool b = false;
+  for (int k = d.pair_cstart[c] + lane; k < d.pair_cstart[c + 1]; k += 32) {
+    const double a = d.pmax[k], v = d.psum[k];
+    if (!(a == a) || !(v == v)) b = true;
+    m = fmax(m, a);
+    sum += v;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  }
+  if (bad) *bad = __any_sync(0xffffffffu, b);
+}
+
+// The Newton decision of an active circuit from its residual norms (one thread).
+__device__ void newton_ctl_scalar(const DevArrays &d, int c, double m, double sum, bool bad);
+
+// One warp per circuit (all 32 lanes call it).
 __device__ __forceinline__ void newton_ctl_circuit(const DevArrays &d, int c, int lane) {
   CircState &s = d.cs[c];
   if (s.phase == PH_STALL) return;  // parked until the host re-pivots; flags kept
@@ -763,20 +789,14 @@ __device__ __forceinline__ void newton_ctl_circuit(const DevArrays &d, int c, in
     if (lane == 0) { s.need_solve = 0; s.step_end = 0; s.accept = 0; s.start_step = 0; }
     return;
   }
-  double m = 0.0, sum = 0.0;
-  bool bad = false;
-  for (int k = d.pair_cstart[c] + lane; k < d.pair_cstart[c + 1]; k += 32) {
-    double a = d.pmax[k], b = d.psum[k];
-    if (!(a == a) || !(b == b)) bad = true;
-    m = fmax(m, a);
-    sum += b;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    sum += __shfl_xor_sync(0xffffffffu, sum, o);
-  }
-  bad = __any_sync(0xffffffffu, bad);
-  if (lane != 0) return;
+  double m, sum;
+  bool bad;
+  circuit_norms(d, c, lane, m, sum, &bad);
+  if (lane == 0) newton_ctl_scalar(d, c, m, sum, bad);
+}
+
+__device__ void newton_ctl_scalar(const DevArrays &d, int c, double m, double sum, bool bad) {
+  CircState &s = d.cs[c];
   const TranParams &p = *d.tp;
   const bool tran = s.phase == PH_TRAN;
   const double normRHS = bad ? __longlong_as_double(0x7ff8000000000000ULL) : sqrt(sum);
@@ -851,9 +871,31 @@ __device__ __forceinline__ void newton_ctl_circuit(const DevArrays &d, int c, in
   }
 }
 
-__global__ void k_newton_ctl(DevArrays d, int ncirc) {
-  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (c < ncirc) newton_ctl_circuit(d, c, threadIdx.x & 31);
+// A warp per 32 circuits: the warp reduces each circuit's partials in turn,
+// then each lane takes one circuit's decision, so the FP64 work of 32
+// decisions shares warp instructions.
+__global__ void __launch_bounds__(128) k_newton_ctl(DevArrays d, int ncirc) {
+  const int lane = threadIdx.x & 31;
+  const int base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32;
+  double my_m = 0.0, my_sum = 0.0;
+  bool my_bad = false;
+  for (int i = 0; i < 32 && base + i < ncirc; ++i) {
+    const CircState &s = d.cs[base + i];
+    if (s.phase == PH_STALL || !circ_active(s)) continue;  // uniform over the warp
+    double m, sum;
+    bool bad;
+    circuit_norms(d, base + i, lane, m, sum, &bad);
+    if (lane == i) { my_m = m; my_sum = sum; my_bad = bad; }
+  }
+  const int c = base + lane;
+  if (c >= ncirc) return;
+  CircState &s = d.cs[c];
+  if (s.phase == PH_STALL) return;
+  if (!circ_active(s)) {
+    s.need_solve = 0; s.step_end = 0; s.accept = 0; s.start_step = 0;
+    return;
+  }
+  newton_ctl_scalar(d, c, my_m, my_sum, my_bad);
 }
 
 // x += dx with the update norm; at the end of a Newton solve, the LTE sum
@@ -978,22 +1020,23 @@ __device__ double next_bp(const double *bps, int lo, int hi, double t, double bp
 }
 
 // Per-circuit step decision (StepErrorControl::evaluateStepError, OneStep::completeStep /
-// rejectStep, Transient::processSuccessfulStep) and the operating-point stages.
-// One warp per circuit (all 32 lanes call it).
+// rejectStep, Transient::processSuccessfulStep) and the operating-point stages:
+// a warp reduces the norms of the circuit's update, one thread decides.
+__device__ void step_ctl_scalar(const DevArrays &d, int c, double m, double sum, const double *bps,
+                                const int *bp_ptr, int cap);
+
 __device__ __forceinline__ void step_ctl_circuit(const DevArrays &d, int c, int lane, const double *bps,
                                                  const int *bp_ptr, int cap) {
+  if (!circ_active(d.cs[c])) return;
+  double m, sum;
+  circuit_norms(d, c, lane, m, sum, nullptr);
+  if (lane == 0) step_ctl_scalar(d, c, m, sum, bps, bp_ptr, cap);
+}
+
+// The step decision of an active circuit from the norms of its update (one thread).
+__device__ void step_ctl_scalar(const DevArrays &d, int c, double m, double sum, const double *bps,
+                                const int *bp_ptr, int cap) {
   CircState &s = d.cs[c];
-  if (!circ_active(s)) return;
-  double m = 0.0, sum = 0.0;
-  for (int k = d.pair_cstart[c] + lane; k < d.pair_cstart[c + 1]; k += 32) {
-    m = fmax(m, d.pmax[k]);
-    sum += d.psum[k];
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    sum += __shfl_xor_sync(0xffffffffu, sum, o);
-  }
-  if (lane != 0) return;
   const TranParams &p = *d.tp;
   if (s.need_solve) {
     if (s.singular) {
@@ -1155,9 +1198,20 @@ __device__ __forceinline__ void step_ctl_circuit(const DevArrays &d, int c, int 
   if (s.accepted >= s.stop_at) s.phase = PH_PAUSED;  // the predictor is applied, then the circuit waits
 }
 
-__global__ void k_step_ctl(DevArrays d, int ncirc, const double *bps, const int *bp_ptr, int cap) {
-  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (c < ncirc) step_ctl_circuit(d, c, threadIdx.x & 31, bps, bp_ptr, cap);
+// A warp per 32 circuits, as k_newton_ctl.
+__global__ void __launch_bounds__(128) k_step_ctl(DevArrays d, int ncirc, const double *bps, const int *bp_ptr,
+                                                  int cap) {
+  const int lane = threadIdx.x & 31;
+  const int base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32;
+  double my_m = 0.0, my_sum = 0.0;
+  for (int i = 0; i < 32 && base + i < ncirc; ++i) {
+    if (!circ_active(d.cs[base + i])) continue;  // uniform over the warp
+    double m, sum;
+    circuit_norms(d, base + i, lane, m, sum, nullptr);
+    if (lane == i) { my_m = m; my_sum = sum; }
+  }
+  const int c = base + lane;
+  if (c < ncirc && circ_active(d.cs[c])) step_ctl_scalar(d, c, my_m, my_sum, bps, bp_ptr, cap);
 }
 
 // OneStep::updateHistory (N_TIA_OneStep.C:1390-1440), OneStep::initialize history
@@ -1706,14 +1760,14 @@ void launch_load_matrices_k(cudaStream_t st, const DevArrays &d, int nnz, double
   k_load_matrices<<<nblk(nnz, 256), 256, 0, st>>>(d, nnz, dQdx, dFdx, lt);
 }
 void launch_newton_ctl_k(cudaStream_t st, const DevArrays &d, int ncirc) {
-  k_newton_ctl<<<nblk(ncirc, 4), 128, 0, st>>>(d, ncirc);
+  k_newton_ctl<<<nblk(ncirc, 128), 128, 0, st>>>(d, ncirc);
 }
 void launch_update_k(cudaStream_t st, const DevArrays &d, int n) {
   k_update<<<nblk(n, kRowBlock), kRowBlock, 0, st>>>(d, n);
 }
 void launch_step_ctl_k(cudaStream_t st, const DevArrays &d, int ncirc, const double *bps,
                        const int *bp_ptr, int cap) {
-  k_step_ctl<<<nblk(ncirc, 4), 128, 0, st>>>(d, ncirc, bps, bp_ptr, cap);
+  k_step_ctl<<<nblk(ncirc, 128), 128, 0, st>>>(d, ncirc, bps, bp_ptr, cap);
 }
 void launch_history_k(cudaStream_t st, const DevArrays &d, int n, int cap, int pmax) {
   k_history<<<nblk(n, 256), 256, 0, st>>>(d, n, cap, pmax);
