@@ -251,6 +251,8 @@ def _timed_windows(xg, nl, probes, dev, args, window, prec, flush, stream_of, ca
     circ.lu_set_precision(prec, 2)
     circ.lu_set_tuning(xg.TUNE_TIMED if tune is None else tune)
     circ.tran_set_form(xg.FORM_AUTO if form is None else form)
+    if args.tail is not None:
+        circ.tran_set_tail(args.tail)
     circ.tran_start(probes=probes, cap=cap)
     stream = stream_of(circ)
     for _ in range(args.warmup):
@@ -665,6 +667,9 @@ def main():
     ap.add_argument("--no-cpu", dest="cpu", action="store_false", help="skip the CPU baseline")
     ap.add_argument("--ncu-case", action="store_true",
                     help="only the operating point and one window (the case the ncu captures profile)")
+    ap.add_argument("--tail", type=float, default=None,
+                    help="active fraction below which the resident kernel finishes a tick-graph advance "
+                         "(default: the library's)")
     ap.add_argument("--form", default="auto", choices=["auto", "tick_graph", "resident"],
                     help="advancing form of the timed run (auto: timed choice on the run itself)")
     ap.add_argument("--ncu-form", default="tick_graph", choices=["tick_graph", "resident"],

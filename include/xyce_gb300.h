@@ -365,12 +365,13 @@ typedef struct xg_tran_stats {
 #define XG_FORM_RESIDENT    2
 int xg_tran_set_form(xg_ctx *ctx, int form);
 
-/* The tail of an advance under the tick graph: once at most active_fraction
- * of the batch's circuits are still running (checked between batches of 64
- * ticks), one resident-kernel launch (256-thread CTAs) finishes them, each
- * circuit at its own pace, instead of more full-batch tick graphs.  The
- * same bits either way.  Applies where the resident form does; 0 turns it
- * off.  No reference counterpart. */
+/* The tail of an advance under XG_FORM_AUTO when the trials kept the tick
+ * graph: once at most active_fraction of the batch's circuits are still
+ * running (checked between batches of ticks), one resident-kernel launch
+ * (256-thread CTAs) finishes them, each circuit at its own pace, instead of
+ * more full-batch tick graphs.  The same bits either way.  Applies where
+ * the resident form does; 0 turns it off; the default is 0.25.  No
+ * reference counterpart. */
 int xg_tran_set_tail(xg_ctx *ctx, double active_fraction);
 
 /* Runs the transient.  probes: global unknown indices to record; every

@@ -56,7 +56,7 @@ struct xg_ctx {
   // Jacobian entries (kept for the circuit-resident tick's per-circuit lists)
   std::vector<int> m1_circ_h, d_circ_h, src_circ_h, long_rows_h, long_ents_h;
   int form = XG_FORM_AUTO;          // xg_tran_set_form
-  double tail_fraction = 0.0;       // xg_tran_set_tail
+  double tail_fraction = 0.25;      // xg_tran_set_tail
   bool resident_ok = false;         // the current analysis admits the circuit-resident tick
   FusedDev F;                       // its device lists (allocated with the analysis)
   int resident_slots[8] = {0};
@@ -1780,8 +1780,8 @@ int run_until_idle(TranRun &R) {
     // still active, the resident kernel finishes them (the same bits; a
     // handful of circuits no longer pays full-batch launches per tick)
     const int active = ctx->ncirc - finished;
-    const bool tail = opt == TranRun::kGraphOption && ctx->resident_ok && ctx->tail_fraction > 0.0 &&
-                      active <= ctx->tail_fraction * ctx->ncirc;
+    const bool tail = opt == TranRun::kGraphOption && ctx->form == XG_FORM_AUTO && ctx->resident_ok &&
+                      ctx->tail_fraction > 0.0 && active <= ctx->tail_fraction * ctx->ncirc;
     R.resident = opt != TranRun::kGraphOption || tail;
     if (R.resident) {
       // every circuit runs its ticks in one CTA until it pauses, finishes,
@@ -2026,7 +2026,10 @@ extern "C" int xg_tran_results(xg_ctx *ctx, int *counts, double *times, double *
     }
     stats->ticks = R.ticks;
     stats->kernels_per_tick = R.kernels_per_tick;
-    stats->form = R.resident ? XG_FORM_RESIDENT : XG_FORM_TICK_GRAPH;
+    // the form the run advances with (the option the trials kept, else the
+    // last launch's; a resident tail does not change a tick-graph run's form)
+    const bool res = R.option >= 0 ? R.option != TranRun::kGraphOption : (R.resident && R.tail_launches == 0);
+    stats->form = res ? XG_FORM_RESIDENT : XG_FORM_TICK_GRAPH;
     stats->kernel_launches = R.kernel_launches;
     stats->circuit_ticks = R.circuit_ticks;
     stats->resident_threads = R.res_threads;
