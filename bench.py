@@ -359,6 +359,48 @@ def _other_configs(xg, dev, flush, stream_of):
     return out
 
 
+def _learned_form(xg):
+    """The learned-predictor form on the BSIM4 logic family: train on the
+    plain runs of two 800-transistor DAGs (the network's own forward and
+    backward kernels on the GPU), then run an unseen third DAG with the
+    polynomial and with the learned predictor (TIMEINT reltol 1e-4, abstol
+    1e-7); Newton iterations per step and accepted steps per second of
+    each (wall time of the whole transient, operating point included)."""
+    from xyce_gb300 import netlist as N
+    from xyce_gb300 import predictor as P
+    import numpy as np
+
+    def fam(seed):
+        nl = N.bsim4_logic_dag(800, 12, seed=seed, tstop=3e-9)
+        nl.tran.reltol, nl.tran.abstol = 1e-4, 1e-7
+        return nl
+
+    Xs, Ys = [], []
+    t0 = time.perf_counter()
+    for seed in (21, 22):
+        counts, t, v, p, probes, st = P.record(fam(seed), cap=4000)
+        X, Y = P.dataset(counts, t, v, p, [len(probes)])
+        Xs.append(X)
+        Ys.append(Y)
+    c = xg.Circuit(N.bsim4_inverter_chain(2))
+    theta, norm, hist = P.train(c, np.concatenate(Xs), np.concatenate(Ys), iters=600, lr=3e-3, batch=200000)
+    c.close()
+    train_s = time.perf_counter() - t0
+    test = fam(23)
+    out = {"family": "bsim4_logic_dag_800, trained on seeds 21 and 22, run on seed 23",
+           "train_loss_first_last": [float(hist[0]), float(hist[-1])], "record_and_train_s": train_s}
+    for name, args in (("polynomial", ()), ("learned", (theta, norm))):
+        a = time.perf_counter()
+        _, _, _, st, ps = P.run(test, *args)
+        dt = time.perf_counter() - a
+        out[name] = {"newton_iters_per_step": st["newton_iters"] / max(1, st["accepted"]),
+                     "steps_per_s_wall": st["accepted"] / dt, "accepted": st["accepted"]}
+        if args:
+            out[name]["learned_steps"] = ps["learned_steps"]
+            out[name]["fallback_steps"] = ps["poly_steps"]
+    return out
+
+
 def _rooflines(circ, nl, window, hbm_peak, peak_kind, info, args):
     """Rooflines of the two dominant kernels of the tick, timed by the tick
     profiler (each stage of PROFILE_TICKS ticks of a new window launched on
@@ -595,6 +637,7 @@ def run_ours(args):
                                           rate(xg.PREC_FP64, tune=xg.TUNE_MODEL, form=xg.FORM_TICK_GRAPH)[0]))
         if args.workload == "mc":
             attempt("one_ring_at_a_time", lambda: forms.update(_one_at_a_time(xg, nl, dev, window, stream_of, value)))
+            attempt("learned_predictor", lambda: forms.__setitem__("learned_predictor", _learned_form(xg)))
 
     # ---- the other configs, plain FP64 path ---------------------------------
     others = None

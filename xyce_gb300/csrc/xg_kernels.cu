@@ -871,31 +871,10 @@ __device__ void newton_ctl_scalar(const DevArrays &d, int c, double m, double su
   }
 }
 
-// A warp per 32 circuits: the warp reduces each circuit's partials in turn,
-// then each lane takes one circuit's decision, so the FP64 work of 32
-// decisions shares warp instructions.
+// A warp per circuit.
 __global__ void __launch_bounds__(128) k_newton_ctl(DevArrays d, int ncirc) {
-  const int lane = threadIdx.x & 31;
-  const int base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32;
-  double my_m = 0.0, my_sum = 0.0;
-  bool my_bad = false;
-  for (int i = 0; i < 32 && base + i < ncirc; ++i) {
-    const CircState &s = d.cs[base + i];
-    if (s.phase == PH_STALL || !circ_active(s)) continue;  // uniform over the warp
-    double m, sum;
-    bool bad;
-    circuit_norms(d, base + i, lane, m, sum, &bad);
-    if (lane == i) { my_m = m; my_sum = sum; my_bad = bad; }
-  }
-  const int c = base + lane;
-  if (c >= ncirc) return;
-  CircState &s = d.cs[c];
-  if (s.phase == PH_STALL) return;
-  if (!circ_active(s)) {
-    s.need_solve = 0; s.step_end = 0; s.accept = 0; s.start_step = 0;
-    return;
-  }
-  newton_ctl_scalar(d, c, my_m, my_sum, my_bad);
+  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (c < ncirc) newton_ctl_circuit(d, c, threadIdx.x & 31);
 }
 
 // x += dx with the update norm; at the end of a Newton solve, the LTE sum
@@ -1198,20 +1177,11 @@ __device__ void step_ctl_scalar(const DevArrays &d, int c, double m, double sum,
   if (s.accepted >= s.stop_at) s.phase = PH_PAUSED;  // the predictor is applied, then the circuit waits
 }
 
-// A warp per 32 circuits, as k_newton_ctl.
+// A warp per circuit.
 __global__ void __launch_bounds__(128) k_step_ctl(DevArrays d, int ncirc, const double *bps, const int *bp_ptr,
                                                   int cap) {
-  const int lane = threadIdx.x & 31;
-  const int base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32;
-  double my_m = 0.0, my_sum = 0.0;
-  for (int i = 0; i < 32 && base + i < ncirc; ++i) {
-    if (!circ_active(d.cs[base + i])) continue;  // uniform over the warp
-    double m, sum;
-    circuit_norms(d, base + i, lane, m, sum, nullptr);
-    if (lane == i) { my_m = m; my_sum = sum; }
-  }
-  const int c = base + lane;
-  if (c < ncirc && circ_active(d.cs[c])) step_ctl_scalar(d, c, my_m, my_sum, bps, bp_ptr, cap);
+  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (c < ncirc) step_ctl_circuit(d, c, threadIdx.x & 31, bps, bp_ptr, cap);
 }
 
 // OneStep::updateHistory (N_TIA_OneStep.C:1390-1440), OneStep::initialize history
@@ -1760,14 +1730,14 @@ void launch_load_matrices_k(cudaStream_t st, const DevArrays &d, int nnz, double
   k_load_matrices<<<nblk(nnz, 256), 256, 0, st>>>(d, nnz, dQdx, dFdx, lt);
 }
 void launch_newton_ctl_k(cudaStream_t st, const DevArrays &d, int ncirc) {
-  k_newton_ctl<<<nblk(ncirc, 128), 128, 0, st>>>(d, ncirc);
+  k_newton_ctl<<<nblk(ncirc, 4), 128, 0, st>>>(d, ncirc);
 }
 void launch_update_k(cudaStream_t st, const DevArrays &d, int n) {
   k_update<<<nblk(n, kRowBlock), kRowBlock, 0, st>>>(d, n);
 }
 void launch_step_ctl_k(cudaStream_t st, const DevArrays &d, int ncirc, const double *bps,
                        const int *bp_ptr, int cap) {
-  k_step_ctl<<<nblk(ncirc, 128), 128, 0, st>>>(d, ncirc, bps, bp_ptr, cap);
+  k_step_ctl<<<nblk(ncirc, 4), 128, 0, st>>>(d, ncirc, bps, bp_ptr, cap);
 }
 void launch_history_k(cudaStream_t st, const DevArrays &d, int n, int cap, int pmax) {
   k_history<<<nblk(n, 256), 256, 0, st>>>(d, n, cap, pmax);

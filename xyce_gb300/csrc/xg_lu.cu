@@ -365,6 +365,14 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
       __syncthreads();
     }
   } else {
+    // the update records of the group's columns (read level by level below,
+    // in a chain of dependent loads) are pulled into L1 first; a prefetch
+    // holds no register and no shared memory
+    for (int t = it0 + (int)threadIdx.x; t < it1; t += (int)blockDim.x) {
+      const int j = SD.items[t];
+      const int4 *u0 = L.umeta + L.cp[j], *u1 = L.umeta + L.diag[j];
+      for (const int4 *u = u0; u < u1; u += 8) asm volatile("prefetch.global.L1 [%0];" ::"l"(u));
+    }
     // every column staged before any is read (a column's thread or warp
     // need not be the warp that staged it)
     __syncthreads();
