@@ -277,10 +277,18 @@ int xg_lu_set_reuse(xg_ctx *ctx, int on);
  * process.  XG_TUNE_MODEL: the analysis' closed-form estimates.  Every
  * candidate computes identical results; only the time differs.  Applies
  * from the next analysis; not allowed while a transient is in progress.
- * No reference counterpart (KLU's factorization is serial). */
+ * XG_TUNE_FIXED is set by xg_lu_set_shapes.  No reference counterpart
+ * (KLU's factorization is serial). */
 #define XG_TUNE_MODEL 0
 #define XG_TUNE_TIMED 1
+#define XG_TUNE_FIXED 2
 int xg_lu_set_tuning(xg_ctx *ctx, int mode);
+/* Fixed launch shapes (XG_TUNE_FIXED) from the next analysis: threads per
+ * CTA of the factorization, the L solve and the U solve (64, 128, 256 or
+ * 512; 0 keeps the analysis' choice) and the factorization's update
+ * metadata staged (1), not staged (0) or as the analysis chose (-1;
+ * staging needs metadata the analysis laid out, else it stays off). */
+int xg_lu_set_shapes(xg_ctx *ctx, int factor_threads, int factor_meta, int lsolve_threads, int usolve_threads);
 typedef struct xg_lu_tuning {
   int mode;                 /* XG_TUNE_* of the current analysis */
   int from_cache;           /* 1: timed earlier for the same analysis, in this process */

@@ -85,3 +85,42 @@ def test_tuning_is_cached_per_analysis(xg, torch_cuda):
     assert picks[0]["from_cache"] == 0 and picks[1]["from_cache"] == 1
     for k in ("factor_threads", "factor_meta", "lsolve_threads", "usolve_threads"):
         assert picks[0][k] == picks[1][k]
+
+
+_SHAPE_CASES = {
+    "mc1024": (lambda: N.monte_carlo_rings(1024, seed=11), lambda nl: [nl.names[f"c{i}.n1"] for i in range(0, 1024, 97)],
+               0.2e-9),
+    "b4dag3000": (lambda: N.bsim4_logic_dag(3000, 16, seed=9, tstop=1e-9), lambda nl: [nl.names["g40"]], 0.2e-9),
+    "grid40": (lambda: N.power_grid(40, 50, seed=2), lambda nl: [nl.names["center"]], 0.1e-9),
+}
+
+
+@pytest.mark.parametrize("name", sorted(_SHAPE_CASES))
+def test_every_launch_shape_gives_identical_runs(xg, torch_cuda, name):
+    """Each candidate shape the tuner may pick, pinned with xg_lu_set_shapes
+    (the factorization at every CTA size with and without its metadata
+    staged, then each solve at every CTA size), runs the transient to the
+    same bits as the closed-form shapes."""
+    make, probes_of, tstop = _SHAPE_CASES[name]
+    nl = make()
+    nl.tran.tstop = tstop
+    probes = probes_of(nl)
+    ref = _run(xg, nl, probes, xg.TUNE_MODEL)
+    shapes = [(s, m, 0, 0) for s in (64, 128, 256, 512) for m in (0, 1)]
+    shapes += [(0, -1, s, 0) for s in (64, 128, 256, 512)] + [(0, -1, 0, s) for s in (64, 128, 256, 512)]
+    for sh in shapes:
+        c = xg.Circuit(nl)
+        c.lu_set_shapes(*sh)
+        c.tran_start(probes=probes, cap=200000)
+        c.tran_advance(0)
+        counts, t, v, st = c.tran_results()
+        tun = c.lu_tuning()
+        c.tran_end()
+        c.close()
+        assert tun["mode"] == xg.TUNE_FIXED
+        assert st["status"] == 0, (sh, st["status"])
+        for k in ("accepted", "rejected", "newton_iters", "n_analyze"):
+            assert st[k] == ref[3][k], (sh, k, st[k], ref[3][k])
+        np.testing.assert_array_equal(counts, ref[0], err_msg=str(sh))
+        np.testing.assert_array_equal(t, ref[1], err_msg=str(sh))
+        np.testing.assert_array_equal(v, ref[2], err_msg=str(sh))

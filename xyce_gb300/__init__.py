@@ -36,7 +36,7 @@ PREC_FP64, PREC_FP32_IR = 0, 1
 ORDER_ND, ORDER_MIN_DEGREE = 0, 1
 TOP_ONE_CTA, TOP_LEVELS = 1, 2
 PRED_POLY, PRED_LEARNED = 0, 1
-TUNE_MODEL, TUNE_TIMED = 0, 1
+TUNE_MODEL, TUNE_TIMED, TUNE_FIXED = 0, 1, 2
 FORM_AUTO, FORM_TICK_GRAPH, FORM_RESIDENT = 0, 1, 2
 MLP_NPARAM, MLP_NNORM = 4609, 12
 FLAG_DCOP, FLAG_INITJCT = 1, 2
@@ -49,7 +49,7 @@ EXPORTED = [
     "xg_get_pattern", "xg_update_sources", "xg_update_state", "xg_load_dae_vectors",
     "xg_load_dae_matrices", "xg_lu_analyze", "xg_lu_factor", "xg_lu_solve",
     "xg_lu_solve_noalloc", "xg_lu_set_precision", "xg_lu_info", "xg_lu_schedule_info", "xg_lu_set_schedule", "xg_lu_analyze_pattern",
-    "xg_lu_set_tuning", "xg_lu_tuning_info", "xg_lu_set_reuse", "xg_lu_set_pivot_tolerance",
+    "xg_lu_set_tuning", "xg_lu_set_shapes", "xg_lu_tuning_info", "xg_lu_set_reuse", "xg_lu_set_pivot_tolerance",
     "xg_transient", "xg_tran_set_form", "xg_tran_set_tail", "xg_tran_start", "xg_tran_advance", "xg_tran_results", "xg_tran_end",
     "xg_tran_predictors", "xg_tran_orders", "xg_tran_profile", "xg_tran_profile_resident", "xg_tran_predictor_stats", "xg_set_predictor", "xg_mlp_set", "xg_mlp_get",
     "xg_mlp_train", "xg_mlp_grad", "xg_mlp_forward",
@@ -156,6 +156,7 @@ def lib() -> C.CDLL:
     L.xg_lu_schedule_info.argtypes = [P, C.POINTER(I), C.POINTER(I), C.POINTER(I)]
     L.xg_lu_set_schedule.argtypes = [P, I, I, I]
     L.xg_lu_set_tuning.argtypes = [P, I]
+    L.xg_lu_set_shapes.argtypes = [P, I, I, I, I]
     L.xg_lu_set_reuse.argtypes = [P, I]
     L.xg_lu_set_pivot_tolerance.argtypes = [P, D]
     L.xg_lu_tuning_info.argtypes = [P, C.POINTER(LuTuning)]
@@ -316,6 +317,12 @@ class Circuit:
         """TUNE_TIMED (default): launch shapes of the LU sweeps chosen by
         timed trials after each analysis; TUNE_MODEL: closed-form choice."""
         self._check(lib().xg_lu_set_tuning(self.h, int(mode)))
+
+    def lu_set_shapes(self, factor_threads=0, factor_meta=-1, lsolve_threads=0, usolve_threads=0):
+        """Fixed launch shapes of the LU sweeps (TUNE_FIXED; 0 / -1 keep the
+        analysis' choice of that part)."""
+        self._check(lib().xg_lu_set_shapes(self.h, int(factor_threads), int(factor_meta), int(lsolve_threads),
+                                           int(usolve_threads)))
 
     def lu_set_pivot_tolerance(self, tol: float):
         """Frozen-pivot acceptance threshold (default 1e-2), see xg_lu_set_pivot_tolerance."""

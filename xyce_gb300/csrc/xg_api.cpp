@@ -67,6 +67,7 @@ struct xg_ctx {
   int n_analyze = 0;
   int lu_prec = XG_PREC_FP64, lu_refine = 2;  // xg_lu_set_precision
   int tune_mode = XG_TUNE_TIMED;               // xg_lu_set_tuning
+  int fixed_shapes[4] = {0, -1, 0, 0};         // xg_lu_set_shapes: factor threads, meta, L / U solve threads
   int lu_reuse = 1;                            // xg_lu_set_reuse
   double pivot_tol = kRuntimePivotTol;         // xg_lu_set_pivot_tolerance
   std::vector<int> row_of_col_h;               // pivot row of every column in the current analysis
@@ -1242,6 +1243,16 @@ static int tune_lu(xg_ctx *ctx, const LUHost &H, const double *vals_dev) {
   T.model_factor_meta = T.factor_meta = L.fm_on;
   T.model_lsolve_threads = T.lsolve_threads = L.ls_threads;
   T.model_usolve_threads = T.usolve_threads = L.us_threads;
+  if (ctx->tune_mode == XG_TUNE_FIXED) {
+    const int *f = ctx->fixed_shapes;
+    if (f[0]) L.fs_threads = f[0];
+    if (f[1] >= 0) L.fm_on = (f[1] && L.fm_gbytes) ? 1 : 0;
+    if (f[2]) L.ls_threads = f[2];
+    if (f[3]) L.us_threads = f[3];
+    T.factor_threads = L.fs_threads; T.factor_meta = L.fm_on;
+    T.lsolve_threads = L.ls_threads; T.usolve_threads = L.us_threads;
+    return XG_OK;
+  }
   if (ctx->tune_mode != XG_TUNE_TIMED || L.fs.n_groups + L.ls.n_groups == 0) return XG_OK;
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
@@ -1441,6 +1452,22 @@ int xg_lu_set_reuse(xg_ctx *ctx, int on) {
   if (on != 0 && on != 1) return fail(ctx, XG_ERR_ARG, "reuse must be 0 or 1");
   if (ctx->run) return fail(ctx, XG_ERR_STATE, "factor reuse cannot change during a transient");
   ctx->lu_reuse = on;
+  return XG_OK;
+}
+
+int xg_lu_set_shapes(xg_ctx *ctx, int factor_threads, int factor_meta, int lsolve_threads, int usolve_threads) {
+  if (!ctx) return XG_ERR_ARG;
+  auto ok = [](int t) { return t == 0 || t == 64 || t == 128 || t == 256 || t == 512; };
+  if (!ok(factor_threads) || !ok(lsolve_threads) || !ok(usolve_threads))
+    return fail(ctx, XG_ERR_ARG, "threads must be 0, 64, 128, 256 or 512");
+  if (factor_meta < -1 || factor_meta > 1) return fail(ctx, XG_ERR_ARG, "factor_meta must be -1, 0 or 1");
+  if (ctx->run) return fail(ctx, XG_ERR_STATE, "launch shapes cannot change during a transient");
+  ctx->fixed_shapes[0] = factor_threads;
+  ctx->fixed_shapes[1] = factor_meta;
+  ctx->fixed_shapes[2] = lsolve_threads;
+  ctx->fixed_shapes[3] = usolve_threads;
+  ctx->tune_mode = XG_TUNE_FIXED;
+  ctx->lu_ready = false;  // applies from the next analysis
   return XG_OK;
 }
 
@@ -1808,6 +1835,10 @@ int run_until_idle(TranRun &R) {
     R.ticks += R.batch;
     R.kernel_launches += (long long)R.batch * R.kernels_per_tick + 1;
     if (R.batch < 64) R.batch *= 2;
+    // near the tail threshold, short batches let the host see it promptly
+    if (ctx->form == XG_FORM_AUTO && ctx->resident_ok && ctx->tail_fraction > 0.0 &&
+        active <= 2.0 * ctx->tail_fraction * ctx->ncirc)
+      R.batch = std::min(R.batch, 8);
   }
 }
 
