@@ -499,7 +499,8 @@ __global__ void __launch_bounds__(kGroupThreads) k_lsolve_groups_s(LUDev L, cons
   const int e0 = L.ls_eptr[it0], E = L.ls_eptr[it1] - e0;
   double *yv = reinterpret_cast<double *>(smraw_sv);
   double *ev = yv + R;
-  int *es = reinterpret_cast<int *>(ev + E);
+  double *xv = ev + E;  // y of an entry's column outside the group (final before this launch)
+  int *es = reinterpret_cast<int *>(xv + E);
   int *ep = es + E;
   int *act = ep + R + 1;
   for (int r = threadIdx.x; r <= R; r += blockDim.x) {
@@ -512,7 +513,9 @@ __global__ void __launch_bounds__(kGroupThreads) k_lsolve_groups_s(LUDev L, cons
   }
   for (int e = threadIdx.x; e < E; e += blockDim.x) {
     ev[e] = (double)lu[L.ls_epos[e0 + e]];
-    es[e] = L.ls_esrc[e0 + e];
+    const int src = L.ls_esrc[e0 + e];
+    es[e] = src;
+    if (src < 0) xv[e] = L.y[-src - 1];
   }
   __syncthreads();
   for (int lv = S.grp_lvl[g]; lv < S.grp_lvl[g + 1]; ++lv) {
@@ -522,7 +525,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_lsolve_groups_s(LUDev L, cons
       double sum = 0.0;
       for (int q = ep[r]; q < ep[r + 1]; ++q) {
         const int src = es[q];
-        sum += ev[q] * (src >= 0 ? yv[src] : L.y[-src - 1]);
+        sum += ev[q] * (src >= 0 ? yv[src] : xv[q]);
       }
       yv[r] -= sum;
     }
@@ -615,7 +618,8 @@ __global__ void __launch_bounds__(kGroupThreads) k_usolve_groups_s(LUDev L, doub
   double *yv = reinterpret_cast<double *>(smraw_sv);
   double *dv = yv + R;
   double *ev = dv + R;
-  int *es = reinterpret_cast<int *>(ev + E);
+  double *xv = ev + E;  // y of an entry's column outside the group (final before this launch)
+  int *es = reinterpret_cast<int *>(xv + E);
   int *ep = es + E;
   int *act = ep + R + 1;
   for (int r = threadIdx.x; r <= R; r += blockDim.x) {
@@ -629,7 +633,9 @@ __global__ void __launch_bounds__(kGroupThreads) k_usolve_groups_s(LUDev L, doub
   }
   for (int e = threadIdx.x; e < E; e += blockDim.x) {
     ev[e] = (double)lu[L.us_epos[e0 + e]];
-    es[e] = L.us_esrc[e0 + e];
+    const int src = L.us_esrc[e0 + e];
+    es[e] = src;
+    if (src < 0) xv[e] = L.y[-src - 1];
   }
   __syncthreads();
   for (int lv = S.grp_lvl[g + 1] - 1; lv >= S.grp_lvl[g]; --lv) {
@@ -639,7 +645,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_usolve_groups_s(LUDev L, doub
       double sum = 0.0;
       for (int q = ep[r]; q < ep[r + 1]; ++q) {
         const int src = es[q];
-        sum += ev[q] * (src >= 0 ? yv[src] : L.y[-src - 1]);
+        sum += ev[q] * (src >= 0 ? yv[src] : xv[q]);
       }
       yv[r] = (yv[r] - sum) / dv[r];
     }

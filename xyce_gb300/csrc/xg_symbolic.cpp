@@ -825,9 +825,10 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
       const long long rows = it1 - it0, ents = eptr[it1] - eptr[it0];
       bool ok = true;
       for (int t = it0; t < it1 && ok; ++t) ok = eptr[t + 1] - eptr[t] <= kStageRow;
-      // doubles: y (+ the diagonal for the U solve) and entry values; ints:
-      // entry slots, the row entry offsets and the rows' activity flags
-      const long long bytes = 8 * (rows * (1 + extra_per_row) + ents) + 4 * (ents + rows + 1) + 4 * rows;
+      // doubles: y (+ the diagonal for the U solve), entry values and the
+      // y of each entry's column outside the group; ints: entry slots, the
+      // row entry offsets and the rows' activity flags
+      const long long bytes = 8 * (rows * (1 + extra_per_row) + 2 * ents) + 4 * (ents + rows + 1) + 4 * rows;
       if (ok && bytes <= kSolveSmemBytes) gbytes[g] = (int)((bytes + 15) / 16 * 16);
     }
   };
