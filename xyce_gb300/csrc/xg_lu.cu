@@ -41,6 +41,18 @@ namespace xg {
 
 constexpr int kGroupThreads = 512;  // largest group CTA (the analysis picks 64..512)
 
+// The level pointers of a group's levels lv0 .. lv1 (at most kStagedLevels
+// levels) copied into shared memory lvp[0 .. lv1 - lv0], so that the level
+// loop does not wait on a global load per level; more levels are read in
+// place.  Returns the array to index by lv - lv0; the caller's barrier
+// after its staging makes the copy visible.
+constexpr int kStagedLevels = 128;
+__device__ __forceinline__ const int *stage_levels(const SchedDev &S, int lv0, int lv1, int *lvp) {
+  if (lv1 - lv0 > kStagedLevels) return S.lvl_ptr + lv0;
+  for (int k = threadIdx.x; k <= lv1 - lv0; k += blockDim.x) lvp[k] = S.lvl_ptr[lv0 + k];
+  return lvp;
+}
+
 void launch_lu_solve_k(cudaStream_t st, const LUDev &L, const double *b, double *x, const CircState *cs,
                        int masked);
 
@@ -307,6 +319,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
   extern __shared__ __align__(16) unsigned char smraw_lu[];
   T *S = reinterpret_cast<T *>(smraw_lu);
   __shared__ double sm[32];
+  __shared__ int lvp[kStagedLevels + 1];
   const SchedDev &SD = L.fs;
   const int g = blockIdx.x;
   if (factor_group_idle(L, cs, masked, L.fs_gcirc, g)) return;
@@ -320,6 +333,8 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
   }
   const int it0 = SD.lvl_ptr[SD.grp_lvl[g]], it1 = SD.lvl_ptr[SD.grp_lvl[g + 1]];
   if (it0 >= it1) return;
+  const int lv0 = SD.grp_lvl[g];
+  const int *lp = stage_levels(SD, lv0, SD.grp_lvl[g + 1], lvp);
   // a group of one circuit is active or not as a whole; packed tiny groups
   // may mix circuits, so every item is tested
   // load the group's columns from A (warp per column)
@@ -351,7 +366,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
     M.col = mcol; M.ent = ment; M.eptr = mep; M.tgt = mtg;
     __syncthreads();
     for (int lv = SD.grp_lvl[g]; lv < SD.grp_lvl[g + 1]; ++lv) {
-      const int b = SD.lvl_ptr[lv], e = SD.lvl_ptr[lv + 1];
+      const int b = lp[lv - lv0], e = lp[lv - lv0 + 1];
       for (int t = b + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
         const int j = SD.items[t];
         if (SD.is_thread[j] && (!multi || factor_active(L, cs, masked, j)))
@@ -377,7 +392,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
     // need not be the warp that staged it)
     __syncthreads();
     for (int lv = SD.grp_lvl[g]; lv < SD.grp_lvl[g + 1]; ++lv) {
-      const int b = SD.lvl_ptr[lv], e = SD.lvl_ptr[lv + 1];
+      const int b = lp[lv - lv0], e = lp[lv - lv0 + 1];
       bool any_long = false;
       for (int t = b + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
         const int j = SD.items[t];
@@ -487,6 +502,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_lsolve_groups_s(LUDev L, cons
                                                                     const CircState *cs, int masked) {
   extern __shared__ __align__(16) unsigned char smraw_sv[];
   __shared__ double sm[32];
+  __shared__ int lvp[kStagedLevels + 1];
   const SchedDev &S = L.ls;
   const int g = blockIdx.x;
   if (group_idle(L, cs, masked, L.ls_gcirc, g)) return;
@@ -503,6 +519,8 @@ __global__ void __launch_bounds__(kGroupThreads) k_lsolve_groups_s(LUDev L, cons
   int *es = reinterpret_cast<int *>(xv + E);
   int *ep = es + E;
   int *act = ep + R + 1;
+  const int lv0 = S.grp_lvl[g];
+  const int *lp = stage_levels(S, lv0, S.grp_lvl[g + 1], lvp);
   for (int r = threadIdx.x; r <= R; r += blockDim.x) {
     ep[r] = L.ls_eptr[it0 + r] - e0;
     if (r < R) {
@@ -519,7 +537,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_lsolve_groups_s(LUDev L, cons
   }
   __syncthreads();
   for (int lv = S.grp_lvl[g]; lv < S.grp_lvl[g + 1]; ++lv) {
-    const int r0 = S.lvl_ptr[lv] - it0, r1 = S.lvl_ptr[lv + 1] - it0;
+    const int r0 = lp[lv - lv0] - it0, r1 = lp[lv - lv0 + 1] - it0;
     for (int r = r0 + (int)threadIdx.x; r < r1; r += (int)blockDim.x) {
       if (!act[r]) continue;
       double sum = 0.0;
@@ -605,6 +623,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_usolve_groups_s(LUDev L, doub
                                                                     const CircState *cs, int masked) {
   extern __shared__ __align__(16) unsigned char smraw_sv[];
   __shared__ double sm[32];
+  __shared__ int lvp[kStagedLevels + 1];
   const SchedDev &S = L.fs;
   const int g = blockIdx.x;
   if (group_idle(L, cs, masked, L.fs_gcirc, g)) return;
@@ -622,6 +641,8 @@ __global__ void __launch_bounds__(kGroupThreads) k_usolve_groups_s(LUDev L, doub
   int *es = reinterpret_cast<int *>(xv + E);
   int *ep = es + E;
   int *act = ep + R + 1;
+  const int lv0 = S.grp_lvl[g];
+  const int *lp = stage_levels(S, lv0, S.grp_lvl[g + 1], lvp);
   for (int r = threadIdx.x; r <= R; r += blockDim.x) {
     ep[r] = L.us_eptr[it0 + r] - e0;
     if (r < R) {
@@ -639,7 +660,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_usolve_groups_s(LUDev L, doub
   }
   __syncthreads();
   for (int lv = S.grp_lvl[g + 1] - 1; lv >= S.grp_lvl[g]; --lv) {
-    const int r0 = S.lvl_ptr[lv] - it0, r1 = S.lvl_ptr[lv + 1] - it0;
+    const int r0 = lp[lv - lv0] - it0, r1 = lp[lv - lv0 + 1] - it0;
     for (int r = r0 + (int)threadIdx.x; r < r1; r += (int)blockDim.x) {
       if (!act[r]) continue;
       double sum = 0.0;
