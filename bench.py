@@ -217,10 +217,13 @@ def run_reference(args):
     world, rank, _ = _dist()
     if rank != 0:
         return
-    _, _, desc = _workload(args.workload, args.rings)
+    nl, _, desc = _workload(args.workload, args.rings)
     cb = cpu_baseline(args)
+    # a step of the GPU arm is one window: `window` accepted steps of every circuit
+    step_units = WORKLOADS[args.workload]["window"] * nl.n_circuits
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * step_units / cb["value"],
+            "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": desc,
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
