@@ -47,6 +47,40 @@ constexpr int kGroupThreads = 512;  // largest group CTA (the analysis picks 64.
 // place.  Returns the array to index by lv - lv0; the caller's barrier
 // after its staging makes the copy visible.
 constexpr int kStagedLevels = 128;
+
+// 1-D bulk copies (the TMA's cp.async.bulk) of contiguous global ranges into
+// this CTA's shared memory, completing on one mbarrier.  Addresses and sizes
+// are multiples of 16 bytes (the callers copy int4 arrays).
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long *mbar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect(unsigned long long *mbar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_to_smem(void *dst, const void *src, unsigned bytes,
+                                             unsigned long long *mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(mbar))
+               : "memory");
+}
+// Waits (at most max_polls polls) for the mbarrier's phase 0 to complete.
+__device__ __forceinline__ bool mbar_wait0(unsigned long long *mbar, int max_polls) {
+  for (int i = 0; i < max_polls; ++i) {
+    unsigned done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(smem_addr(mbar))
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+constexpr int kBulkWaitPolls = 1 << 22;  // far beyond any copy's time; a timeout is reported as a breakdown
 __device__ __forceinline__ const int *stage_levels(const SchedDev &S, int lv0, int lv1, int *lvp) {
   if (lv1 - lv0 > kStagedLevels) return S.lvl_ptr + lv0;
   for (int k = threadIdx.x; k <= lv1 - lv0; k += blockDim.x) lvp[k] = S.lvl_ptr[lv0 + k];
@@ -320,6 +354,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
   T *S = reinterpret_cast<T *>(smraw_lu);
   __shared__ double sm[32];
   __shared__ int lvp[kStagedLevels + 1];
+  __shared__ __align__(8) unsigned long long mbar;
   const SchedDev &SD = L.fs;
   const int g = blockIdx.x;
   if (factor_group_idle(L, cs, masked, L.fs_gcirc, g)) return;
@@ -357,14 +392,26 @@ __global__ void __launch_bounds__(kGroupThreads) k_factor_groups_s(LUDev L, cons
     int4 *ment = mcol + R;
     int *mep = reinterpret_cast<int *>(ment + U);
     int *mtg = mep + R + 1;
-    for (int r = threadIdx.x; r <= R; r += blockDim.x) {
-      mep[r] = L.fm_eptr[it0 + r] - u0;
-      if (r < R) mcol[r] = L.fm_col[it0 + r];
+    // the column records and their update entries (contiguous int4 ranges)
+    // by two bulk copies; the offsets and the targets by plain loads meanwhile
+    if (threadIdx.x == 0) mbar_init(&mbar);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      mbar_expect(&mbar, 16u * (unsigned)(R + U));
+      bulk_to_smem(mcol, L.fm_col + it0, 16u * (unsigned)R, &mbar);
+      if (U > 0) bulk_to_smem(ment, L.fm_ent + u0, 16u * (unsigned)U, &mbar);
     }
-    for (int u = threadIdx.x; u < U; u += blockDim.x) ment[u] = L.fm_ent[u0 + u];
+    for (int r = threadIdx.x; r <= R; r += blockDim.x) mep[r] = L.fm_eptr[it0 + r] - u0;
     for (int q = threadIdx.x; q < TG; q += blockDim.x) mtg[q] = L.fm_tgt[t0 + q];
     M.col = mcol; M.ent = ment; M.eptr = mep; M.tgt = mtg;
-    __syncthreads();
+    const bool landed = mbar_wait0(&mbar, kBulkWaitPolls);
+    if (!__syncthreads_and(landed)) {
+      // the copies did not land in time: report a breakdown (the host
+      // re-analyses and refactors) rather than factor from unfilled memory
+      if (threadIdx.x == 0) atomicCAS(L.breakdown, 0, it0 + 1);
+      mbar_wait0(&mbar, kBulkWaitPolls);
+      return;
+    }
     for (int lv = SD.grp_lvl[g]; lv < SD.grp_lvl[g + 1]; ++lv) {
       const int b = lp[lv - lv0], e = lp[lv - lv0 + 1];
       for (int t = b + (int)threadIdx.x; t < e; t += (int)blockDim.x) {
