@@ -1103,6 +1103,7 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
   L.fs_threads = H.fs_threads;
   L.ls_threads = H.ls_threads;
   L.us_threads = H.us_threads;
+  if ((rc = lu_prepare_k())) return rc;  // shared-memory opt-ins of the staged kernels
   if (!H.grp_snz.empty()) {
     for (int w = 0; w < 2; ++w) {
       const int cap = kGroupSmemBytes / (w ? (int)sizeof(float) : (int)sizeof(double));
@@ -1110,7 +1111,6 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
         if (z <= cap) L.grp_fit[w] = std::max(L.grp_fit[w], z);
     }
     if (L.grp_fit[0] > 0 || L.grp_fit[1] > 0) {
-      if ((rc = lu_prepare_k())) return rc;
       if ((rc = dev_upload(ctx, &L.grp_soff, H.grp_soff, A))) return rc;
       if ((rc = dev_upload(ctx, &L.grp_snz, H.grp_snz, A))) return rc;
       // groups staged with their update metadata: values (16-byte aligned),

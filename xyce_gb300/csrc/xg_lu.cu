@@ -874,12 +874,22 @@ static void factor_sweeps(cudaStream_t st, const LUDev &L, const double *vals, C
   }
 }
 
-// FP64 factors, or FP32 factors when the analysis selected the refined solve.
+// Opt-in of the staged kernels to their largest buffers: beyond 48 KB of
+// dynamic plus static shared memory a launch needs it, and the staged solve
+// kernels' own static arrays sit on top of buffers of up to kSolveSmemBytes.
 int lu_prepare_k() {
-  if (cudaFuncSetAttribute(k_factor_groups_s<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           kGroupSmemBytes) != cudaSuccess ||
-      cudaFuncSetAttribute(k_factor_groups_s<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           kGroupSmemBytes) != cudaSuccess)
+  const int solve_bytes = kSolveSmemBytes + 4096;
+  auto set = [](const void *f, int bytes) {
+    return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess;
+  };
+  if (!set((const void *)k_factor_groups_s<double>, kGroupSmemBytes) ||
+      !set((const void *)k_factor_groups_s<float>, kGroupSmemBytes) ||
+      !set((const void *)k_lsolve_groups_s<double>, solve_bytes) ||
+      !set((const void *)k_lsolve_groups_s<float>, solve_bytes) ||
+      !set((const void *)k_usolve_groups_s<double, false>, solve_bytes) ||
+      !set((const void *)k_usolve_groups_s<double, true>, solve_bytes) ||
+      !set((const void *)k_usolve_groups_s<float, false>, solve_bytes) ||
+      !set((const void *)k_usolve_groups_s<float, true>, solve_bytes))
     return XG_ERR_CUDA;
   return XG_OK;
 }
