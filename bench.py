@@ -48,7 +48,9 @@ sys.path.insert(0, HERE)
 METRIC = "transient steps/s (device evals/s alongside), FP64"
 UNIT = "steps/s"
 WORKLOADS = {
-    "mc": dict(window=50, cpu_steps=300, cpu_rings=64),
+    # mc: the CPU arm times each sampled ring's accepted steps 151..650, the
+    # region the GPU arm times (3 warm-up windows of 50 steps, then 10 timed)
+    "mc": dict(window=50, cpu_steps=500, cpu_warm=150, cpu_rings=64),
     "ring": dict(window=200, cpu_steps=1500, cpu_rings=0),
     "grid": dict(window=10, cpu_steps=6, cpu_rings=0),
     "dag": dict(window=10, cpu_steps=20, cpu_rings=0),
@@ -142,25 +144,33 @@ def _cpu_init():
 
 
 def _cpu_ring_task(args):
-    """One Monte-Carlo ring, run alone by the oracle for its first n accepted steps."""
-    idx, n_steps = args
+    """One Monte-Carlo ring run alone by the oracle: its accepted steps
+    n_warm+1 .. n_warm+n_steps, timed from the per-step wall-clock log
+    (the operating point and the first n_warm steps are not timed)."""
+    idx, n_warm, n_steps = args
+    import numpy as np
     import oracle
     from xyce_gb300 import netlist as N
     nl = N.extract_circuit(_BATCH, idx)
-    nl.tran.max_steps = n_steps
-    t0 = time.perf_counter()
-    _, _, st = oracle.Oracle(nl).transient(nl.tran, probes=[0], cap=8)
-    return st["accepted"], time.perf_counter() - t0
+    nl.tran.max_steps = n_warm + n_steps
+    wall = np.zeros(n_warm + n_steps + 1)
+    _, _, st = oracle.Oracle(nl).transient(nl.tran, probes=[0], cap=8, wall_log=wall)
+    k = int(st["accepted"])
+    if k <= n_warm:
+        return 0, 0.0
+    return k - n_warm, float(wall[k - 1] - wall[n_warm - 1])
 
 
-def cpu_mc(n_rings, n_steps, cores):
+def cpu_mc(n_rings, n_warm, n_steps, cores):
     """Aggregate steps/s of the oracle on a sample of the batch's rings, one
     ring per process on `cores` processes (spawned: no state shared with a
-    CUDA context)."""
+    CUDA context): the per-core rate over the timed steps of every sampled
+    ring (sum of steps / sum of their seconds) times the cores, the rings
+    being independent."""
     import oracle
     if not os.path.exists(oracle.LIB_PATH):
         oracle.build(with_reference=False)
-    tasks = [(int(i), n_steps) for i in range(0, 4096, max(1, 4096 // n_rings))][:n_rings]
+    tasks = [(int(i), n_warm, n_steps) for i in range(0, 4096, max(1, 4096 // n_rings))][:n_rings]
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores, initializer=_cpu_init) as pool:
         pool.map(abs, range(cores))  # workers up and the batch built before the clock starts
@@ -168,7 +178,8 @@ def cpu_mc(n_rings, n_steps, cores):
         res = pool.map(_cpu_ring_task, tasks, chunksize=1)
         wall = time.perf_counter() - t0
     steps = sum(r[0] for r in res)
-    return steps / wall, steps, wall
+    secs = sum(r[1] for r in res)
+    return cores * steps / secs, steps, secs, wall
 
 
 def cpu_single(workload, n_steps):
@@ -199,12 +210,14 @@ def cpu_baseline(args):
     w = WORKLOADS[args.workload]
     if args.workload == "mc":
         cores = os.cpu_count() or 1
-        v, steps, wall = cpu_mc(w["cpu_rings"], w["cpu_steps"], cores)
+        v, steps, secs, wall = cpu_mc(w["cpu_rings"], w["cpu_warm"], w["cpu_steps"], cores)
+        a, b = w["cpu_warm"] + 1, w["cpu_warm"] + w["cpu_steps"]
         return {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                "sample": f"{w['cpu_rings']} rings of the same batch, first {w['cpu_steps']} accepted "
-                          f"steps of each from its operating point ({steps} steps, {wall:.1f} s wall), "
-                          f"CPU FP64 restatement (oracle/, LU in the ring's natural order), one ring "
-                          f"per process on {cores} processes"}
+                "sample": f"{w['cpu_rings']} rings of the same batch, accepted steps {a}..{b} of each (the "
+                          f"steps the GPU arm times; {steps} timed steps, {secs:.1f} core-seconds, "
+                          f"{wall:.1f} s wall with the untimed operating points and first {w['cpu_warm']} "
+                          f"steps), CPU FP64 restatement (oracle/, LU in the ring's natural order), one ring "
+                          f"per process on {cores} processes; rate = cores x timed steps / core-seconds"}
     v, steps, dt = cpu_single(args.workload, w["cpu_steps"])
     order = "the natural order" if args.workload == "ring" else "minimum-degree order"
     return {"value": v, "unit": UNIT, "cores": 1, "kind": "port",

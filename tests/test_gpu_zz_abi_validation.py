@@ -90,3 +90,29 @@ def test_rejected_tran_start_leaves_no_half_built_run(xg, cuda):
     assert st["accepted"] >= 10 and counts[0] >= 11
     c.tran_end()
     c.close()
+
+
+def test_tuning_form_and_tail_setters_checked(xg, cuda):
+    """The launch-shape, form and tail setters reject values outside their
+    ranges, and refuse to change while a transient is in progress."""
+    from xyce_gb300 import netlist as N
+    L = cuda
+    nl = N.monte_carlo_rings(64, 11, 21, seed=3)
+    nl.tran.tstop = 0.05e-9
+    c = xg.Circuit(nl)
+    h = c.h
+    assert L.xg_lu_set_shapes(h, 96, 0, 0, 0) == -1          # not a CTA size
+    assert L.xg_lu_set_shapes(h, 128, 2, 0, 0) == -1         # meta must be -1, 0 or 1
+    assert L.xg_lu_set_shapes(h, 0, -1, 64, 1024) == -1      # too large
+    assert L.xg_tran_set_tail(h, C.c_double(-0.1)) == -1
+    assert L.xg_tran_set_tail(h, C.c_double(1.5)) == -1
+    assert L.xg_tran_set_form(h, 7) == -1
+    assert L.xg_lu_set_shapes(h, 128, 1, 64, 64) == xg.XG_OK
+    c.tran_start(probes=[0], cap=16)
+    assert c.lu_tuning()["mode"] == xg.TUNE_FIXED and c.lu_tuning()["factor_threads"] == 128
+    assert L.xg_lu_set_shapes(h, 256, 0, 0, 0) == -3         # XG_ERR_STATE during a transient
+    assert L.xg_tran_set_form(h, xg.FORM_TICK_GRAPH) == -3
+    c.tran_advance(0)
+    c.tran_end()
+    assert L.xg_tran_set_tail(h, C.c_double(0.5)) == xg.XG_OK
+    c.close()
