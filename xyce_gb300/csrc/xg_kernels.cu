@@ -222,9 +222,11 @@ __device__ __forceinline__ void mos1_eval(const DevArrays &d, int i, int nm, int
       double vdsm = (mode == 1) ? vds : -vds;
       double betap = Beta * (1 + m.lambda * vdsm);
       if (f_le(vgst, vdsm)) {
-        cdrain = betap * vgst * vgst * .5;
+        // saturation: half vgst^2 once for the current and its output conductance
+        const double h = vgst * vgst * .5;
+        cdrain = betap * h;
         gm = betap * vgst;
-        gds = m.lambda * Beta * vgst * vgst * .5;
+        gds = m.lambda * Beta * h;
       } else {
         cdrain = betap * vdsm * (vgst - .5 * vdsm);
         gm = betap * vdsm;
@@ -343,8 +345,13 @@ __device__ __forceinline__ void mos1_eval(const DevArrays &d, int i, int nm, int
 #pragma unroll
   for (int k = 0; k < 16; ++k) { f[k] = 0.0; q[k] = 0.0; }
   f[15] = gbs + gbd; f[12] = -gbd; f[14] = -gbs;
-  f[1] = Gm; f[3] = -gbd + Gmbs; f[0] = gds + gbd + revsum; f[2] = -gds - nrmsum;
-  f[9] = -Gm; f[11] = -(gbs + Gmbs); f[8] = -(gds + revsum); f[10] = gds + gbs + nrmsum;
+  f[1] = Gm; f[3] = -gbd + Gmbs; f[9] = -Gm; f[11] = -(gbs + Gmbs);
+  // one of revsum / nrmsum is zero (by the mode): its additions are skipped
+  if (mode >= 0) {
+    f[0] = gds + gbd; f[2] = -gds - nrmsum; f[8] = -gds; f[10] = gds + gbs + nrmsum;
+  } else {
+    f[0] = gds + gbd + revsum; f[2] = -gds; f[8] = -(gds + revsum); f[10] = gds + gbs;
+  }
   if (!noq) {
     q[5] = Capgd + Capgs + Capgb; q[7] = -Capgb; q[4] = -Capgd; q[6] = -Capgs;
     q[13] = -Capgb; q[15] = capbs + capbd + Capgb; q[12] = -capbd; q[14] = -capbs;
