@@ -222,11 +222,9 @@ __device__ __forceinline__ void mos1_eval(const DevArrays &d, int i, int nm, int
       double vdsm = (mode == 1) ? vds : -vds;
       double betap = Beta * (1 + m.lambda * vdsm);
       if (f_le(vgst, vdsm)) {
-        // saturation: half vgst^2 once for the current and its output conductance
-        const double h = vgst * vgst * .5;
-        cdrain = betap * h;
+        cdrain = betap * vgst * vgst * .5;
         gm = betap * vgst;
-        gds = m.lambda * Beta * h;
+        gds = m.lambda * Beta * vgst * vgst * .5;
       } else {
         cdrain = betap * vdsm * (vgst - .5 * vdsm);
         gm = betap * vdsm;
