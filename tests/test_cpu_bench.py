@@ -72,3 +72,18 @@ def test_error_vs_fp64_on_an_oracle_sequence(bench):
     assert err["circuits"] == 2
     assert err["points"] == len(seqs[sample[0]][0]) + len(seqs[sample[2]][0])
     assert err["max_abs_v"] < 1e-9 and err["max_abs_v_exact_window"] <= err["max_abs_v"]
+
+
+def test_cpu_ring_sample_times_only_the_later_steps(bench):
+    """The CPU arm's ring task runs a ring from its operating point and times
+    only the accepted steps after the first n_warm (the steps the GPU arm
+    times): it returns that many steps and a positive time."""
+    from xyce_gb300 import netlist as N
+    bench._BATCH = N.monte_carlo_rings(4, 11, 21, seed=7)
+    steps, secs = bench._cpu_ring_task((1, 20, 30))
+    assert steps == 30 and secs > 0.0
+    # no timed steps when the ring stops within the warm-up
+    nl = bench._BATCH
+    nl.tran.tstop = 1e-12
+    steps0, secs0 = bench._cpu_ring_task((1, 20, 30))
+    assert steps0 == 0 and secs0 == 0.0
