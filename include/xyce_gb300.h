@@ -64,7 +64,13 @@ enum {
   XG_DIODE_IS, XG_DIODE_N, XG_DIODE_RS, XG_DIODE_CJO, XG_DIODE_VJ, XG_DIODE_M,
   XG_DIODE_FC, XG_DIODE_TT, XG_DIODE_BV, XG_DIODE_IBV, XG_DIODE_NBV, XG_DIODE_IKF,
   XG_DIODE_ISR, XG_DIODE_NR, XG_DIODE_EG, XG_DIODE_XTI, XG_DIODE_AREA,
-  XG_DIODE_BVGIVEN, XG_DIODE_NPARAM
+  XG_DIODE_BVGIVEN,
+  /* sidewall junction: JSW (0 = none), NS and whether it was given (not
+   * given: the sidewall current joins the bottom one), CJSW, VJSW (PHP),
+   * MJSW, FCS; the instance perimeter PJ */
+  XG_DIODE_JSW, XG_DIODE_NS, XG_DIODE_NSGIVEN, XG_DIODE_CJSW, XG_DIODE_VJSW, XG_DIODE_MJSW,
+  XG_DIODE_FCS, XG_DIODE_PJ,
+  XG_DIODE_NPARAM
 };
 
 /* ---- MOSFET level-1 parameter row (N_DEV_MOSFET1.C:61-331) -------------- */

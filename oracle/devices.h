@@ -21,7 +21,8 @@ static const double kGmin = 1.0e-12;  // N_DEV_DeviceOptions.C default gmin
 // Parameter row layouts (identical numbering in include/xyce_gb300.h).
 enum DiodeParam {
   DP_IS, DP_N, DP_RS, DP_CJO, DP_VJ, DP_M, DP_FC, DP_TT, DP_BV, DP_IBV, DP_NBV,
-  DP_IKF, DP_ISR, DP_NR, DP_EG, DP_XTI, DP_AREA, DP_BVGIVEN, DP_COUNT
+  DP_IKF, DP_ISR, DP_NR, DP_EG, DP_XTI, DP_AREA, DP_BVGIVEN,
+  DP_JSW, DP_NS, DP_NSGIVEN, DP_CJSW, DP_VJSW, DP_MJSW, DP_FCS, DP_PJ, DP_COUNT
 };
 enum Mos1Param {
   MP_TYPE, MP_VTO, MP_KP, MP_GAMMA, MP_PHI, MP_LAMBDA, MP_RD, MP_RS, MP_CBD, MP_CBS,
@@ -126,6 +127,10 @@ struct DiodeT {
   double Isat, IsatR, Vte, VteR, VteBRK, Gspr, tVcrit, tIKF, tJctPot, tJctCap, tDepCap,
       tF1, F2, F3, M, TT, tBrkdwnV, area;
   bool bvGiven;
+  // sidewall junction: sw 0 none, 1 own characteristic (NS given), 2 its
+  // saturation current joined to the bottom one (JSW given, NS not)
+  int sw;
+  double IsatSW, VteSW, CzeroSW, tJctSWPot, tDepSWCap, F2SW, F3SW, MJSW;
 };
 
 inline DiodeT diode_temperature(const double *p) {
@@ -180,8 +185,32 @@ inline DiodeT diode_temperature(const double *p) {
     }
     t.tBrkdwnV = xbv;
   }
+  // sidewall (updateTemperature N_DEV_Diode.C:1473-1494, Model::processParams
+  // :1632-1636; PJ scales the sidewall as AREA scales the bottom)
+  {
+    const double VJSW = p[DP_VJSW], MJSW = p[DP_MJSW], FCS = p[DP_FCS], PJ = p[DP_PJ], NS = p[DP_NS];
+    const double pboSW = (VJSW - pbfact1) / fact1;
+    const double gmaSWold = (VJSW - pboSW) / pboSW;
+    double tJctSWCap = p[DP_CJSW] / (1.0 + MJSW * (4.0e-4 * (TNOM - kRefTemp) - gmaSWold));
+    const double tJctSWPot = pbfact + fact2 * pboSW;
+    const double gmaSWnew = (tJctSWPot - pboSW) / pboSW;
+    tJctSWCap *= 1.0 + MJSW * (4.0e-4 * (Temp - kRefTemp) - gmaSWnew);
+    const double tSatSWCur =
+        p[DP_JSW] * std::exp(((Temp / TNOM) - 1.0) * EG / (NS * vt) + XTI / NS * std::log(Temp / TNOM));
+    const double xfcs = std::log(1.0 - FCS);
+    t.tJctSWPot = tJctSWPot;
+    t.tDepSWCap = FCS * tJctSWPot;
+    t.F2SW = std::exp((1.0 + MJSW) * xfcs);
+    t.F3SW = 1.0 - FCS * (1.0 + MJSW);
+    t.MJSW = MJSW;
+    t.IsatSW = tSatSWCur * PJ;
+    t.VteSW = NS * vt;
+    t.CzeroSW = tJctSWCap * PJ;
+    t.sw = (p[DP_JSW] != 0.0) ? (p[DP_NSGIVEN] != 0.0 ? 1 : 2) : 0;
+  }
   t.area = p[DP_AREA];
   t.Isat = tSatCur * t.area;
+  if (t.sw == 2) t.Isat = t.Isat + t.IsatSW;  // the bottom characteristic carries both
   t.IsatR = tSatCurR * t.area;
   t.Vte = N * vt;
   t.VteR = NR * vt;
@@ -200,8 +229,8 @@ struct DiodeOut {
   double Vd, Vd_orig, Id, Gd, Qd, Cd;
 };
 
-// Diode::Instance::updateIntermediateVars, N_DEV_Diode.C:1072-1420
-// (no sidewall: JSW = 0, PJ = 0).
+// Diode::Instance::updateIntermediateVars, N_DEV_Diode.C:1072-1420, with the
+// sidewall current (:1226-1260) and charge (:1380-1400).
 // vd_hist is the stored junction voltage: currSto at newton_iter 0, nextSto after.
 inline DiodeOut diode_eval(const DiodeT &t, double Vpp, double Vn, double vd_hist, int newton_iter,
                            bool dcop, bool initJct) {
@@ -223,6 +252,23 @@ inline DiodeOut diode_eval(const DiodeT &t, double Vpp, double Vn, double vd_his
   } else {
     Vd = pnjlim(Vd, Vd_old, t.Vte, t.tVcrit, &ichk);
   }
+  double IdSW = 0.0, GdSW = 0.0;
+  if (t.sw == 1) {
+    if (Vd >= -3.0 * t.VteSW) {  // sidewall forward
+      double evd = std::exp(std::min(kMaxExpArg, Vd / t.VteSW));
+      IdSW = t.IsatSW * (evd - 1.0);
+      GdSW = t.IsatSW * evd / t.VteSW;
+    } else if (!t.tBrkdwnV || Vd >= -t.tBrkdwnV) {  // sidewall reverse
+      double argsw = 3.0 * t.VteSW / (Vd * std::exp(1.0));
+      argsw = argsw * argsw * argsw;
+      IdSW = -t.IsatSW * (1.0 + argsw);
+      GdSW = t.IsatSW * 3.0 * argsw / Vd;
+    } else {  // sidewall breakdown
+      double evrev = std::exp(std::min(kMaxExpArg, -(t.tBrkdwnV + Vd) / t.VteBRK));
+      IdSW = -t.IsatSW * evrev;
+      GdSW = t.IsatSW * evrev / t.VteBRK;
+    }
+  }
   double Id, Gd;
   if (Vd >= -3.0 * t.Vte) {
     double evd = std::exp(std::min(kMaxExpArg, Vd / t.Vte));
@@ -242,17 +288,17 @@ inline DiodeOut diode_eval(const DiodeT &t, double Vpp, double Vn, double vd_his
       Kgen = std::sqrt(std::pow(a * a + 0.005, t.M));
       DKgen = -t.M * a * Kgen / (t.tJctPot * (a * a + 0.005));
     }
-    Id = Inorm * Khi + Irec * Kgen;
-    Gd = Gd1 * Khi + Inorm * DKhi + Gd2 * Kgen + Irec * DKgen;
+    Id = Inorm * Khi + Irec * Kgen + IdSW;
+    Gd = Gd1 * Khi + Inorm * DKhi + Gd2 * Kgen + Irec * DKgen + GdSW;
   } else if (!t.tBrkdwnV || Vd >= -t.tBrkdwnV) {
     double arg = 3.0 * t.Vte / (Vd * std::exp(1.0));
     arg = arg * arg * arg;
-    Id = -t.Isat * (1.0 + arg) + kGmin * Vd;
-    Gd = t.Isat * 3.0 * arg / Vd + kGmin;
+    Id = -t.Isat * (1.0 + arg) + IdSW + kGmin * Vd;
+    Gd = t.Isat * 3.0 * arg / Vd + GdSW + kGmin;
   } else {
     double evrev = std::exp(std::min(kMaxExpArg, -(t.tBrkdwnV + Vd) / t.VteBRK));
-    Id = -t.Isat * evrev + kGmin * Vd;
-    Gd = t.Isat * evrev / t.VteBRK + kGmin;
+    Id = -t.Isat * evrev + IdSW + kGmin * Vd;
+    Gd = t.Isat * evrev / t.VteBRK + GdSW + kGmin;
   }
   double Qd = 0, Cd = 0;
   if (t.tJctCap != 0.0) {
@@ -269,6 +315,21 @@ inline DiodeOut diode_eval(const DiodeT &t, double Vpp, double Vn, double vd_his
       Qd = t.TT * Id + Czero * t.tF1 +
            Czof2 * (t.F3 * (Vc - t.tDepCap) + 0.5 * MotJctPot * (Vc * Vc - t.tDepCap * t.tDepCap));
       Cd = t.TT * Gd + Czof2 * (t.F3 + MotJctPot * Vc);
+    }
+    // sidewall depletion charge (computed where the bottom one is, as the
+    // reference does)
+    const double CzeroSW = t.CzeroSW;
+    if (Vc < t.tDepSWCap) {
+      double argSW = 1.0 - Vc / t.tJctSWPot;
+      double sargSW = std::exp(std::min(kMaxExpArg, -t.MJSW * std::log(argSW)));
+      Qd += t.tJctSWPot * CzeroSW * (1.0 - argSW * sargSW) / (1.0 - t.MJSW);
+      Cd += CzeroSW * sargSW;
+    } else {
+      double Czof2SW = CzeroSW / t.F2SW;
+      double MotJctSWPot = t.MJSW / t.tJctSWPot;
+      Qd += CzeroSW * t.tF1 +
+            Czof2SW * (t.F3SW * (Vc - t.tDepSWCap) + (0.5 * MotJctSWPot) * (Vc * Vc - t.tDepSWCap * t.tDepSWCap));
+      Cd += Czof2SW * (t.F3SW + MotJctSWPot * Vc);
     }
   }
   o.Vd = Vd; o.Id = Id; o.Gd = Gd; o.Qd = Qd; o.Cd = Cd;

@@ -47,15 +47,24 @@ def test_rc_step_within_reltol(oracle_mod):
     assert np.max(np.abs(v[:, 0] - ref)) < 1e-3
 
 
-def _fd_check(oracle_mod, nl, rng, dcop):
+def _fd_check(oracle_mod, nl, rng, dcop, shift=0.0):
     o = oracle_mod.Oracle(nl)
     _, x0, _ = o.dcop()
-    x = x0 + 0.05 * rng.standard_normal(o.n)
+    x = x0 + shift + 0.05 * rng.standard_normal(o.n)
     z = np.zeros(max(1, o.nsta))
     base = o.load(x, dcop=dcop, sta_curr=z, sto_curr=np.zeros(max(1, o.nsto)), newton_iter=0)
     # history equal to the point itself: no limiting, and the back-averaged
     # Meyer charge has its capacitance as exact derivative
     sta_c, sto_c = base["sta_next"], base["sto_next"]
+    # from a zero history the junction limiting may have moved the stored
+    # voltages (a diode in breakdown); reload until the history is the point
+    for _ in range(200):
+        nxt = o.load(x, dcop=dcop, sta_curr=sta_c, sto_curr=sto_c, sto_prev=sto_c, newton_iter=1)
+        if np.array_equal(nxt["sto_next"], sto_c):
+            break
+        sta_c, sto_c = nxt["sta_next"], nxt["sto_next"]
+    else:
+        raise AssertionError("junction history did not settle")
     ref = o.load(x, dcop=dcop, sta_curr=sta_c, sto_curr=sto_c, sto_prev=sto_c, newton_iter=1)
     J = {k: sp.csr_matrix((ref[k], o.col_idx, o.row_ptr), shape=(o.n, o.n)).toarray()
          for k in ("dFdx", "dQdx")}
@@ -75,6 +84,7 @@ def _fd_check(oracle_mod, nl, rng, dcop):
 
 
 @pytest.mark.parametrize("maker", [lambda: N.diode_ladder(8, seed=3),
+                                   lambda: N.diode_ladder(9, seed=3, sidewall=True),
                                    lambda: N.ring_oscillator(5),
                                    lambda: N.ring_oscillator(5, caps=True),
                                    lambda: N.bsim4_inverter_chain(2),
@@ -82,6 +92,15 @@ def _fd_check(oracle_mod, nl, rng, dcop):
 def test_finite_difference_jacobian(oracle_mod, maker):
     rng = np.random.default_rng(7)
     _fd_check(oracle_mod, maker(), rng, dcop=False)
+
+
+@pytest.mark.parametrize("shift", [1.6, -4.2])
+def test_finite_difference_jacobian_sidewall_regimes(oracle_mod, shift):
+    """The sidewall ladder's operating point is reverse-biased (-1 V); shifted
+    points put the junctions forward, above the sidewall depletion threshold
+    (+0.6 V), and in breakdown for the BV = 4 V card (-5.2 V)."""
+    rng = np.random.default_rng(11)
+    _fd_check(oracle_mod, N.diode_ladder(9, seed=3, sidewall=True), rng, dcop=False, shift=shift)
 
 
 def test_lu_matches_ksparse_golden(oracle_mod):
@@ -155,6 +174,31 @@ def test_diode_iv_point(oracle_mod):
     # the operating-point Newton stops at RHSTOL = 1e-6 A (N_NLS_Manager.C:1033)
     assert abs(i_r - i_d) < 1e-6
     assert 0.55 < vd < 0.75
+
+
+@pytest.mark.parametrize("ns", [1.3, None])
+def test_diode_sidewall_iv_point(oracle_mod, ns):
+    """Sidewall current at DC (N_DEV_Diode.C:1226-1260): with NS given it adds
+    JSW*PJ*(exp(Vd/(NS Vt)) - 1); without NS, JSW*PJ joins IS*AREA in the
+    bottom characteristic."""
+    nl = N.Netlist(label="diode_sw_iv")
+    a, k = nl.node("a"), nl.node("k")
+    nl.V(a, -1, N.WAVE_DC, [1.0])
+    nl.R(a, k, 1e3)
+    card = dict(IS=1e-14, N=1.0, JSW=4e-14, PJ=2.5, CJSW=1e-13)
+    if ns is not None:
+        card["NS"] = ns
+    nl.D(k, -1, **card)
+    st, x, it = oracle_mod.Oracle(nl).dcop()
+    vd = x[k]
+    vt = 1.3806226e-23 * 300.15 / 1.6021918e-19
+    isw = 4e-14 * 2.5
+    if ns is None:
+        i_d = (1e-14 + isw) * np.expm1(vd / vt)
+    else:
+        i_d = 1e-14 * np.expm1(vd / vt) + isw * np.expm1(vd / (ns * vt))
+    assert abs((1.0 - vd) / 1e3 - (i_d + 1e-12 * vd)) < 1e-6
+    assert 0.45 < vd < 0.75
 
 
 def test_bsim4_iv_known_behaviour(oracle_mod):

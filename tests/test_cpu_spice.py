@@ -245,6 +245,27 @@ V1 in 0 PWL(0 0 1n 1 2n 0)
     assert nl.diode[1][1] == -1
 
 
+def test_diode_sidewall_card():
+    d = S.parse("""sidewall
+.MODEL dsw D (IS=1e-14 JSW=2e-15 NS=1.2 CJP=0.1p PHP=0.7 MJSW=0.3 FCS=0.4)
+.MODEL dmerged D (IS=1e-14 JSW=2e-15)
+V1 a 0 SIN(0 1 1MEG)
+D1 a 0 dsw PJ=3
+D2 a 0 dmerged
+.TRAN 1n 1u
+.END
+""")
+    f = N.DIODE_FIELDS.index
+    r1, r2 = d.netlist.diode[0][3], d.netlist.diode[1][3]
+    assert r1[f("JSW")] == 2e-15 and r1[f("NS")] == 1.2 and r1[f("NSGIVEN")] == 1.0
+    assert r1[f("CJSW")] == 1e-13 and r1[f("VJSW")] == 0.7 and r1[f("MJSW")] == 0.3
+    assert r1[f("FCS")] == 0.4 and r1[f("PJ")] == 3.0
+    # NS not given: the sidewall current merges into the bottom characteristic
+    assert r2[f("NSGIVEN")] == 0.0 and r2[f("NS")] == 1.0 and r2[f("PJ")] == 0.0
+    with pytest.raises(ValueError):
+        S.parse("bad\n.MODEL d1 D (NSGIVEN=1)\nD1 a 0 d1\nV1 a 0 1\n.TRAN 1n 1u\n.END\n")
+
+
 def test_bsim4_model_card_and_instance():
     d = S.parse("""bsim4 inverter
 .MODEL n1 NMOS (LEVEL=54 VERSION=4.8.2 TOXE=1.8n VTH0=0.4)

@@ -47,14 +47,15 @@ def _assert_stamps(name, g, r, floor=STAMP_FLOOR):
     assert not bad.any(), f"{name}: {np.count_nonzero(bad)} entries, worst {np.max(np.abs(g - r)[bad])}"
 
 
-def _loader_case(xg, oracle_mod, torch, nl, seed, newton_iter, dcop, init_jct, consistent_caps):
+def _loader_case(xg, oracle_mod, torch, nl, seed, newton_iter, dcop, init_jct, consistent_caps,
+                 xlo=-0.4):
     c = xg.Circuit(nl)
     o = oracle_mod.Oracle(nl)
     assert (c.n, c.nnz, c.nsta, c.nsto) == (o.n, o.nnz, o.nsta, o.nsto)
     np.testing.assert_array_equal(c.row_ptr, o.row_ptr)
     np.testing.assert_array_equal(c.col_idx, o.col_idx)
     rng = np.random.default_rng(seed)
-    x = rng.uniform(-0.4, 2.0, o.n)
+    x = rng.uniform(xlo, 2.0, o.n)
     sta_c = rng.standard_normal(max(1, o.nsta)) * 1e-15
     if not consistent_caps:
         sta_c[:] = 0.0  # models without gate capacitance only ever hold zero gate states
@@ -108,6 +109,16 @@ def test_device_stamps_match_oracle(xg, oracle_mod, torch_cuda, maker, caps, mod
     it, dcop, init = {"tran0": (0, False, False), "tran2": (2, False, False),
                       "dcop_init": (0, True, True)}[mode]
     _loader_case(xg, oracle_mod, torch_cuda, maker(), 11, it, dcop, init, caps)
+
+
+@pytest.mark.parametrize("mode", ["tran0", "tran2", "dcop_init"])
+def test_diode_sidewall_stamps_match_oracle(xg, oracle_mod, torch_cuda, mode):
+    """Sidewall currents (own NS, merged) and charges; junction voltages down
+    to -5.5 V reach the breakdown of the BV = 4 V card."""
+    it, dcop, init = {"tran0": (0, False, False), "tran2": (2, False, False),
+                      "dcop_init": (0, True, True)}[mode]
+    _loader_case(xg, oracle_mod, torch_cuda, N.diode_ladder(30, seed=3, sidewall=True), 13, it, dcop,
+                 init, False, xlo=-5.5)
 
 
 def test_lu_matches_ksparse_golden(xg, torch_cuda):
@@ -207,6 +218,7 @@ def _compare_waveforms(t_ref, v_ref, t_gpu, v_gpu):
     ("testnetlist2", N.test_netlist2, ["1", "2"]),
     ("rc_step", N.rc_step, ["in", "out"]),
     ("diode_ladder_50", lambda: N.diode_ladder(50, seed=5), ["n1", "n25", "n50"]),
+    ("diode_ladder_sw_30", lambda: N.diode_ladder(30, seed=5, sidewall=True), ["n1", "n2", "n15"]),
     ("ring_101", lambda: N.ring_oscillator(101), ["n1", "n50", "n101"]),
     ("ring_21_caps", lambda: N.ring_oscillator(21, caps=True), ["n1", "n11"]),
     ("b4_chain_3", lambda: N.bsim4_inverter_chain(3), ["in", "n1", "n3"]),

@@ -95,11 +95,14 @@ struct Mos1Model {
   int has_gate_caps, has_junc_caps;
 };
 
-// Diode model-level parameters after temperature processing (N_DEV_Diode.C:2040-2237).
+// Diode model-level parameters after temperature processing (N_DEV_Diode.C:2040-2237),
+// with the instance's AREA and PJ folded in.  Sidewall: sw 0 none, 1 its own
+// characteristic (NS given), 2 merged into Isat (JSW given, NS not).
 struct DiodeModel {
   double Isat, IsatR, Vte, VteR, VteBRK, Gspr, tVcrit, tIKF, tJctPot, tJctCap, tDepCap;
   double tF1, F2, F3, M, TT, tBrkdwnV;
-  int bvGiven;
+  double IsatSW, VteSW, CzeroSW, tJctSWPot, tDepSWCap, F2SW, F3SW, MJSW;
+  int bvGiven, sw;
 };
 
 // Learned predictor MLP 5 -> 64 -> 64 -> 1 (xg_mlp.cu).  Master parameter

@@ -439,6 +439,24 @@ __device__ __forceinline__ void diode_eval(const DevArrays &d, int i, int nd, in
   } else {
     Vd = pnjlim_d(Vd, Vd_old, t.Vte, t.tVcrit, ichk);
   }
+  // sidewall current with its own characteristic (N_DEV_Diode.C:1226-1256)
+  double IdSW = 0.0, GdSW = 0.0;
+  if (t.sw == 1) {
+    if (Vd >= -3.0 * t.VteSW) {
+      const double evd = exp(fmin(kMaxExpArg, Vd / t.VteSW));
+      IdSW = t.IsatSW * (evd - 1.0);
+      GdSW = t.IsatSW * evd / t.VteSW;
+    } else if (!t.tBrkdwnV || Vd >= -t.tBrkdwnV) {
+      double argsw = 3.0 * t.VteSW / (Vd * kE);
+      argsw = argsw * argsw * argsw;
+      IdSW = -t.IsatSW * (1.0 + argsw);
+      GdSW = t.IsatSW * 3.0 * argsw / Vd;
+    } else {
+      const double evrev = exp(fmin(kMaxExpArg, -(t.tBrkdwnV + Vd) / t.VteBRK));
+      IdSW = -t.IsatSW * evrev;
+      GdSW = t.IsatSW * evrev / t.VteBRK;
+    }
+  }
   double Id, Gd;
   if (Vd >= -3.0 * t.Vte) {
     double evd = exp(fmin(kMaxExpArg, Vd / t.Vte));
@@ -458,17 +476,17 @@ __device__ __forceinline__ void diode_eval(const DevArrays &d, int i, int nd, in
       Kgen = sqrt(pow(a * a + 0.005, t.M));
       DKgen = -t.M * a * Kgen / (t.tJctPot * (a * a + 0.005));
     }
-    Id = Inorm * Khi + Irec * Kgen;
-    Gd = Gd1 * Khi + Inorm * DKhi + Gd2 * Kgen + Irec * DKgen;
+    Id = Inorm * Khi + Irec * Kgen + IdSW;
+    Gd = Gd1 * Khi + Inorm * DKhi + Gd2 * Kgen + Irec * DKgen + GdSW;
   } else if (!t.tBrkdwnV || Vd >= -t.tBrkdwnV) {
     double arg = 3.0 * t.Vte / (Vd * kE);
     arg = arg * arg * arg;
-    Id = -t.Isat * (1.0 + arg) + kGmin * Vd;
-    Gd = t.Isat * 3.0 * arg / Vd + kGmin;
+    Id = -t.Isat * (1.0 + arg) + IdSW + kGmin * Vd;
+    Gd = t.Isat * 3.0 * arg / Vd + GdSW + kGmin;
   } else {
     double evrev = exp(fmin(kMaxExpArg, -(t.tBrkdwnV + Vd) / t.VteBRK));
-    Id = -t.Isat * evrev + kGmin * Vd;
-    Gd = t.Isat * evrev / t.VteBRK + kGmin;
+    Id = -t.Isat * evrev + IdSW + kGmin * Vd;
+    Gd = t.Isat * evrev / t.VteBRK + GdSW + kGmin;
   }
   double Qd = 0, Cd = 0;
   if (t.tJctCap != 0.0) {
@@ -484,6 +502,23 @@ __device__ __forceinline__ void diode_eval(const DevArrays &d, int i, int nd, in
       Qd = t.TT * Id + Czero * t.tF1 +
            Czof2 * (t.F3 * (Vd - t.tDepCap) + 0.5 * MotJctPot * (Vd * Vd - t.tDepCap * t.tDepCap));
       Cd = t.TT * Gd + Czof2 * (t.F3 + MotJctPot * Vd);
+    }
+    // sidewall depletion charge (N_DEV_Diode.C:1380-1400); it adds zeros when
+    // the perimeter capacitance is zero, so that case skips it
+    const double CzeroSW = t.CzeroSW;
+    if (CzeroSW != 0.0) {
+      if (Vd < t.tDepSWCap) {
+        const double argSW = 1.0 - Vd / t.tJctSWPot;
+        const double sargSW = exp(fmin(kMaxExpArg, -t.MJSW * log(argSW)));
+        Qd += t.tJctSWPot * CzeroSW * (1.0 - argSW * sargSW) / (1.0 - t.MJSW);
+        Cd += CzeroSW * sargSW;
+      } else {
+        const double Czof2SW = CzeroSW / t.F2SW;
+        const double MotJctSWPot = t.MJSW / t.tJctSWPot;
+        Qd += CzeroSW * t.tF1 + Czof2SW * (t.F3SW * (Vd - t.tDepSWCap) +
+                                           0.5 * MotJctSWPot * (Vd * Vd - t.tDepSWCap * t.tDepSWCap));
+        Cd += Czof2SW * (t.F3SW + MotJctSWPot * Vd);
+      }
     }
   }
   d.sto_next[i] = Vd; d.sto_next[nd + i] = Qd; d.sto_next[2 * nd + i] = Cd;

@@ -2,7 +2,8 @@
 // model tables (temperature = TNOM = 27 C, the reference's default).
 //
 //   Diode: Model::processParams + updateTemperature
-//          src/DeviceModelPKG/OpenModels/N_DEV_Diode.C:1612-1639, 2040-2237
+//          src/DeviceModelPKG/OpenModels/N_DEV_Diode.C:1612-1639, 2040-2237;
+//          the sidewall junction :1473-1494, :1632-1636
 //   MOSFET level 1: Model::processParams, Instance::processParams, updateTemperature
 //          src/DeviceModelPKG/OpenModels/N_DEV_MOSFET1.C:3939-4020, 383-470, 3487-3730
 #include <algorithm>
@@ -66,7 +67,29 @@ DiodeModel diode_model(const double *p) {
     }
     m.tBrkdwnV = xbv;
   }
+  // sidewall junction, scaled by the perimeter PJ as the bottom is by AREA
+  const double VJSW = p[XG_DIODE_VJSW], MJSW = p[XG_DIODE_MJSW], FCS = p[XG_DIODE_FCS];
+  const double NS = p[XG_DIODE_NS], PJ = p[XG_DIODE_PJ];
+  const double pboSW = (VJSW - pbfact1) / fact1;
+  const double gmaSWold = (VJSW - pboSW) / pboSW;
+  double tJctSWCap = p[XG_DIODE_CJSW] / (1.0 + MJSW * (4.0e-4 * (TN - REFTEMP) - gmaSWold));
+  const double tJctSWPot = pbfact + fact2 * pboSW;
+  const double gmaSWnew = (tJctSWPot - pboSW) / pboSW;
+  tJctSWCap *= 1.0 + MJSW * (4.0e-4 * (T - REFTEMP) - gmaSWnew);
+  const double tSatSWCur =
+      p[XG_DIODE_JSW] * std::exp(((T / TN) - 1.0) * EG / (NS * vt) + XTI / NS * std::log(T / TN));
+  const double xfcs = std::log(1.0 - FCS);
+  m.sw = p[XG_DIODE_JSW] != 0.0 ? (p[XG_DIODE_NSGIVEN] != 0.0 ? 1 : 2) : 0;
+  m.IsatSW = tSatSWCur * PJ;
+  m.VteSW = NS * vt;
+  m.CzeroSW = tJctSWCap * PJ;
+  m.tJctSWPot = tJctSWPot;
+  m.tDepSWCap = FCS * tJctSWPot;
+  m.F2SW = std::exp((1.0 + MJSW) * xfcs);
+  m.F3SW = 1.0 - FCS * (1.0 + MJSW);
+  m.MJSW = MJSW;
   m.Isat = tSatCur * area;
+  if (m.sw == 2) m.Isat = m.Isat + m.IsatSW;  // one characteristic carries both
   m.IsatR = tSatCurR * area;
   m.Vte = vte;
   m.VteR = NR * vt;

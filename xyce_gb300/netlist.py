@@ -26,10 +26,12 @@ WAVE_DC, WAVE_SIN, WAVE_PULSE, WAVE_PWL = 0, 1, 2, 3
 
 # Diode parameter row (N_DEV_Diode.C addPar defaults).
 DIODE_FIELDS = ["IS", "N", "RS", "CJO", "VJ", "M", "FC", "TT", "BV", "IBV", "NBV",
-                "IKF", "ISR", "NR", "EG", "XTI", "AREA", "BVGIVEN"]
+                "IKF", "ISR", "NR", "EG", "XTI", "AREA", "BVGIVEN",
+                "JSW", "NS", "NSGIVEN", "CJSW", "VJSW", "MJSW", "FCS", "PJ"]
 DIODE_DEFAULTS = dict(IS=1e-14, N=1.0, RS=0.0, CJO=0.0, VJ=1.0, M=0.5, FC=0.5, TT=0.0,
                       BV=1e99, IBV=1e-3, NBV=None, IKF=0.0, ISR=0.0, NR=2.0, EG=1.11,
-                      XTI=3.0, AREA=1.0, BVGIVEN=0.0)
+                      XTI=3.0, AREA=1.0, BVGIVEN=0.0,
+                      JSW=0.0, NS=1.0, NSGIVEN=0.0, CJSW=0.0, VJSW=1.0, MJSW=0.33, FCS=0.5, PJ=0.0)
 
 # MOSFET level-1 parameter row (model + instance; N_DEV_MOSFET1.C addPar defaults).
 MOS1_FIELDS = ["TYPE", "VTO", "KP", "GAMMA", "PHI", "LAMBDA", "RD", "RS", "CBD", "CBS",
@@ -73,6 +75,8 @@ def diode_row(**kw) -> np.ndarray:
         p["NBV"] = p["N"]
     if "BV" in kw:
         p["BVGIVEN"] = 1.0
+    if "NS" in kw:
+        p["NSGIVEN"] = 1.0
     return np.array([p[f] for f in DIODE_FIELDS], dtype=np.float64)
 
 
@@ -255,21 +259,39 @@ def rc_step(r=1e3, c=1e-9, v=1.0, tstop=5e-6) -> Netlist:
 # ---------------------------------------------------------------------------
 # Synthetic workloads.
 
-def diode_ladder(n_nodes=1000, seed=1) -> Netlist:
+# Diode cards with sidewall junctions (JSW / NS / CJSW / VJSW / MJSW / FCS,
+# perimeter PJ): own sidewall characteristic, sidewall current merged into
+# the bottom one (NS not given), and sidewall charge beside a bottom one.
+SIDEWALL_DIODES = (
+    dict(IS=1e-14, N=1.0, RS=10.0, CJO=0.2e-12, JSW=2e-15, NS=1.3, CJSW=0.05e-12, VJSW=0.8, MJSW=0.4,
+         FCS=0.6, PJ=3.0, BV=4.0),
+    dict(IS=1e-14, N=1.0, RS=10.0, CJO=0.1e-12, JSW=5e-15, CJSW=0.03e-12, PJ=2.0),
+    dict(IS=2e-14, N=1.1, RS=0.0, CJO=0.3e-12, TT=1e-10, CJSW=0.1e-12, MJSW=0.25, PJ=1.5),
+)
+
+
+def diode_ladder(n_nodes=1000, seed=1, sidewall=False) -> Netlist:
     """Diode-RC ladder: chain of n_nodes, R_i ~ U[500,2000] ohm, C_i ~ U[0.1,1] pF,
     a level-1 diode (IS=1e-14, N=1, RS=10) from every node to ground, node 1
-    driven by SIN(1 1 1MEG); .TRAN 0 5u, max step 10 n, RELTOL 1e-3 ABSTOL 1e-12."""
+    driven by SIN(1 1 1MEG); .TRAN 0 5u, max step 10 n, RELTOL 1e-3 ABSTOL 1e-12.
+    sidewall: the diodes cycle through SIDEWALL_DIODES instead, and the
+    source swings between -5.5 V and 3.5 V so the reverse and breakdown
+    (BV = 4 V) regimes are reached."""
     rng = np.random.default_rng(seed)
     nl = Netlist(label=f"diode_ladder_{n_nodes}")
     nodes = [nl.node(f"n{i + 1}") for i in range(n_nodes)]
     rv = rng.uniform(500.0, 2000.0, n_nodes - 1)
     cv = rng.uniform(0.1e-12, 1e-12, n_nodes)
-    nl.V(nodes[0], -1, WAVE_SIN, [1.0, 1.0, 1e6, 0.0, 0.0, 0.0], name="V1#branch")
+    amp = [-1.0, 4.5] if sidewall else [1.0, 1.0]
+    nl.V(nodes[0], -1, WAVE_SIN, [amp[0], amp[1], 1e6, 0.0, 0.0, 0.0], name="V1#branch")
     for i in range(n_nodes - 1):
         nl.R(nodes[i], nodes[i + 1], rv[i])
     for i in range(n_nodes):
         nl.C(nodes[i], -1, cv[i])
-        nl.D(nodes[i], -1, IS=1e-14, N=1.0, RS=10.0)
+        if sidewall:
+            nl.D(nodes[i], -1, **SIDEWALL_DIODES[i % len(SIDEWALL_DIODES)])
+        else:
+            nl.D(nodes[i], -1, IS=1e-14, N=1.0, RS=10.0)
     nl.tran = Tran(tstop=5e-6, hmax=10e-9, reltol=1e-3, abstol=1e-12)
     return nl
 

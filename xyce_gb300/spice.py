@@ -159,7 +159,7 @@ class Deck:
     sampling: dict = field(default_factory=dict)     # .SAMPLING vectors + .OPTIONS SAMPLES
 
 
-_DIODE_ALIASES = {"CJ0": "CJO", "CJ": "CJO", "PB": "VJ", "MJ": "M"}
+_DIODE_ALIASES = {"CJ0": "CJO", "CJ": "CJO", "PB": "VJ", "MJ": "M", "CJP": "CJSW", "PHP": "VJSW"}
 _MOS1_MODEL = {"VTO", "KP", "GAMMA", "PHI", "LAMBDA", "RD", "RS", "CBD", "CBS", "IS", "PB", "CGSO",
                "CGDO", "CGBO", "CJ", "MJ", "CJSW", "MJSW", "JS", "TOX", "LD", "FC"}
 _MOS1_INST = {"W", "L", "AD", "AS", "PD", "PS", "M"}
@@ -274,6 +274,8 @@ class _Builder:
             area = kv.get("AREA") or (pos[3] if len(pos) > 3 else None)
             if area is not None:
                 p["AREA"] = number(area)
+            if "PJ" in kv:
+                p["PJ"] = number(kv["PJ"])
             self.nl.D(nd(pos[0]), nd(pos[1]), **p)
         elif letter == "M":
             if len(pos) < 5:
@@ -345,7 +347,7 @@ class _Builder:
             out = {}
             for k, v in params.items():
                 k = _DIODE_ALIASES.get(k, k)
-                if k not in N.DIODE_FIELDS or k == "BVGIVEN":
+                if k not in N.DIODE_FIELDS or k in ("BVGIVEN", "NSGIVEN", "PJ"):
                     raise ValueError(f"model {name}: unsupported diode parameter {k}")
                 out[k] = v
             params = out
