@@ -246,7 +246,7 @@ def run_reference(args):
 # ---- GPU ----------------------------------------------------------------
 SAMPLE_RINGS = 8          # rings of the mc batch whose waveforms are checked against the oracle
 PROFILE_TICKS = 40        # ticks timed stage by stage for the rooflines
-MOS1_BYTES_SURVEY = 712   # algorithmic bytes per MOSFET-1 evaluation + stamp, per-unit convention
+MOS1_ALG_BYTES = 712      # algorithmic bytes per MOSFET-1 evaluation + stamp, per-unit convention
 MOS1_BYTES_CODE = 440     # bytes the transient-mode kernel reads (112) and writes (328) per instance
 LU_BYTES_PER_NNZ = 12     # algorithmic bytes of a refactorization per nnz(L+U): value + index
 
@@ -429,7 +429,7 @@ def _rooflines(circ, nl, window, hbm_peak, peak_kind, info, args):
     total = sum(stage_ms.values())
     inst = ev["mos1"] / PROFILE_TICKS
     us = stage_ms["mos1"] * 1e3 / PROFILE_TICKS
-    alg = MOS1_BYTES_SURVEY * inst
+    alg = MOS1_ALG_BYTES * inst
     achieved = alg / (us * 1e-6) / 1e9
     traffic = None
     prof = os.path.join(HERE, "profiles", "k_mos1_mc4096.traffic.json")
@@ -444,7 +444,7 @@ def _rooflines(circ, nl, window, hbm_peak, peak_kind, info, args):
                      "masked by circuit activity), as launched by the tick",
            "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
            "peak_kind": peak_kind, "traffic": traffic,
-           "algorithmic_bytes_per_launch": alg, "bytes_per_instance": MOS1_BYTES_SURVEY,
+           "algorithmic_bytes_per_launch": alg, "bytes_per_instance": MOS1_ALG_BYTES,
            "bytes_moved_by_code_per_instance": MOS1_BYTES_CODE, "instances_per_launch": inst, "launch_us": us,
            "share_of_tick": stage_ms["mos1"] / total,
            "note": "FP64-pipe bound on GB300: ncu shows the FP64 pipe ~80 % busy in this kernel"}
@@ -588,7 +588,7 @@ def run_ours(args):
     if form == "circuit_resident":
         # the whole tick in one kernel: its algorithmic bytes are the device
         # evaluations' (the per-instance figure) over the timed windows
-        alg = MOS1_BYTES_SURVEY * evals_all
+        alg = MOS1_ALG_BYTES * evals_all
         ach = alg / (ms_max / 1e3) / 1e9
         resident_roof = {"kernel": "k_resident (every stage of every tick of a circuit in one CTA)", "bound": "hbm",
                          "achieved": ach, "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak,
