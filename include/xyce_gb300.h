@@ -73,13 +73,17 @@ enum {
   XG_DIODE_NPARAM
 };
 
-/* ---- MOSFET level-1 parameter row (N_DEV_MOSFET1.C:61-331) -------------- */
+/* ---- MOSFET level-1 parameter row (N_DEV_MOSFET1.C:61-331) --------------
+ * RD / RS: series drain / source resistance; RSH sheet resistance with the
+ * instance's NRD / NRS squares, used where RD / RS is zero
+ * (Instance::processParams, N_DEV_MOSFET1.C:410-450). */
 enum {
   XG_MOS1_TYPE, XG_MOS1_VTO, XG_MOS1_KP, XG_MOS1_GAMMA, XG_MOS1_PHI, XG_MOS1_LAMBDA,
   XG_MOS1_RD, XG_MOS1_RS, XG_MOS1_CBD, XG_MOS1_CBS, XG_MOS1_IS, XG_MOS1_PB,
   XG_MOS1_CGSO, XG_MOS1_CGDO, XG_MOS1_CGBO, XG_MOS1_CJ, XG_MOS1_MJ, XG_MOS1_CJSW,
   XG_MOS1_MJSW, XG_MOS1_JS, XG_MOS1_TOX, XG_MOS1_LD, XG_MOS1_FC, XG_MOS1_W, XG_MOS1_L,
-  XG_MOS1_AD, XG_MOS1_AS, XG_MOS1_PD, XG_MOS1_PS, XG_MOS1_M, XG_MOS1_NPARAM
+  XG_MOS1_AD, XG_MOS1_AS, XG_MOS1_PD, XG_MOS1_PS, XG_MOS1_M, XG_MOS1_RSH, XG_MOS1_NRD,
+  XG_MOS1_NRS, XG_MOS1_NPARAM
 };
 
 /* ---- BSIM4 (Xyce level 54, BSIM 4.8.2) parameter row --------------------
@@ -151,9 +155,20 @@ int xg_add_isources(xg_ctx *ctx, int n, const int *pos, const int *neg,
 int xg_add_diodes(xg_ctx *ctx, int n, const int *pos, const int *neg, const int *pri,
                   const double *params);
 /* MOSFET1::Instance (N_DEV_MOSFET1.C); params n x XG_MOS1_NPARAM row-major.
- * Series drain/source resistance (RD, RS, RSH) is XG_ERR_UNSUPPORTED. */
+ * Rows with a series drain/source resistance need the internal nodes:
+ * XG_ERR_ARG here, use xg_add_mosfet1_rs. */
 int xg_add_mosfet1(xg_ctx *ctx, int n, const int *d, const int *g, const int *s,
                    const int *b, const double *params);
+/* The same with the drain' / source' internal nodes (li_DrainPrime /
+ * li_SourcePrime, N_DEV_MOSFET1.C:1437-1445): dp[k] must differ from d[k]
+ * exactly when the drain conductance (RD, or RSH * NRD) is nonzero, sp[k]
+ * likewise.  The device equations act on (dp, g, sp, b); drainConductance *
+ * M joins d to dp and sourceConductance * M s to sp.  These constant
+ * conductances load with the linear part (loadType XG_LOAD_LINEAR), where
+ * the reference loads them with the device: the sum of the two parts is the
+ * same. */
+int xg_add_mosfet1_rs(xg_ctx *ctx, int n, const int *d, const int *g, const int *s,
+                      const int *b, const int *dp, const int *sp, const double *params);
 /* MOSFET_B4::Instance (N_DEV_MOSFET_B4.C); params n x XG_B4_NPARAM row-major.
  * A card outside the restated scope is XG_ERR_UNSUPPORTED. */
 int xg_add_bsim4(xg_ctx *ctx, int n, const int *d, const int *g, const int *s,

@@ -67,7 +67,7 @@ def lib():
         L.orc_add_vsources.argtypes = [P, C.c_int, ip, ip, ip, ip, ip, dp]
         L.orc_add_isources.argtypes = [P, C.c_int, ip, ip, ip, ip, dp]
         L.orc_add_diodes.argtypes = [P, C.c_int, ip, ip, ip, dp]
-        L.orc_add_mosfet1.argtypes = [P, C.c_int, ip, ip, ip, ip, dp]
+        L.orc_add_mosfet1.argtypes = [P, C.c_int, ip, ip, ip, ip, ip, ip, dp]
         L.orc_add_bsim4.argtypes = [P, C.c_int, ip, ip, ip, ip, dp]
         L.orc_finalize.argtypes = [P]
         L.orc_sizes.argtypes = [P] + [C.POINTER(C.c_int)] * 4
@@ -107,10 +107,11 @@ class Oracle:
         L.orc_add_isources(self.h, len(p), p, m, k, o, d)
         p, m, r, prm = a["diode"]
         L.orc_add_diodes(self.h, len(p), p, m, r, prm)
-        dd, g, s, b, prm = a["mos1"]
-        rc = L.orc_add_mosfet1(self.h, len(dd), dd, g, s, b, prm)
+        dd, g, s, b, dpr, spr, prm = a["mos1"]
+        rc = L.orc_add_mosfet1(self.h, len(dd), dd, g, s, b, dpr, spr, prm)
         if rc != 0:
-            raise ValueError("oracle: MOSFET series resistance is not restated")
+            raise ValueError("oracle: MOSFET drain'/source' nodes must differ from drain/source "
+                             "exactly when the series resistance is nonzero")
         dd, g, s, b, prm = a["bsim4"]
         if len(dd):
             rc = L.orc_add_bsim4(self.h, len(dd), dd, g, s, b, np.ascontiguousarray(prm))

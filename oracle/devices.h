@@ -27,7 +27,8 @@ enum DiodeParam {
 enum Mos1Param {
   MP_TYPE, MP_VTO, MP_KP, MP_GAMMA, MP_PHI, MP_LAMBDA, MP_RD, MP_RS, MP_CBD, MP_CBS,
   MP_IS, MP_PB, MP_CGSO, MP_CGDO, MP_CGBO, MP_CJ, MP_MJ, MP_CJSW, MP_MJSW, MP_JS,
-  MP_TOX, MP_LD, MP_FC, MP_W, MP_L, MP_AD, MP_AS, MP_PD, MP_PS, MP_M, MP_COUNT
+  MP_TOX, MP_LD, MP_FC, MP_W, MP_L, MP_AD, MP_AS, MP_PD, MP_PS, MP_M, MP_RSH, MP_NRD, MP_NRS,
+  MP_COUNT
 };
 
 // DeviceSupport::pnjlim, N_DEV_DeviceSupport.C:188-235.
@@ -343,7 +344,16 @@ struct Mos1T {
   double dtype, Beta, tVbi, tVto, gamma, tPhi, lambda, vt, DrainSatCur, SourceSatCur,
       sourceVcrit, drainVcrit, OxideCap, Cgso, Cgdo, Cgbo, Cbd, Cbdsw, Cbs, Cbssw, tDepCap,
       tBulkPot, MJ, MJSW, f2d, f3d, f4d, f2s, f3s, f4s, M;
+  double drainConductance, sourceConductance;  // series RD / RS (0 = none)
 };
+
+// Series drain/source conductance, Instance::processParams N_DEV_MOSFET1.C:410-450:
+// RD (RS) when nonzero, else 1/(RSH * NRD (NRS)) when RSH is nonzero, else 0.
+inline double mos1_series_conductance(double r, double rsh, double squares) {
+  if (r != 0.0) return 1.0 / r;
+  if (rsh != 0.0) return 1.0 / (rsh * squares);
+  return 0.0;
+}
 
 inline Mos1T mos1_temperature(const double *p) {
   Mos1T t{};
@@ -425,11 +435,13 @@ inline Mos1T mos1_temperature(const double *p) {
   t.Cgso = p[MP_CGSO] * W; t.Cgdo = p[MP_CGDO] * W; t.Cgbo = p[MP_CGBO] * Leff;
   t.tDepCap = tDepCap; t.tBulkPot = tBulkPot; t.MJ = mj; t.MJSW = mjsw;
   t.M = p[MP_M];
+  t.drainConductance = mos1_series_conductance(p[MP_RD], p[MP_RSH], p[MP_NRD]);
+  t.sourceConductance = mos1_series_conductance(p[MP_RS], p[MP_RSH], p[MP_NRS]);
   return t;
 }
 
-// Results of one MOSFET-1 evaluation (drain/source primes coincide with
-// drain/source: RD = RS = 0).
+// Results of one MOSFET-1 evaluation, at the drain' and source' nodes (the
+// drain and source themselves when there is no series resistance).
 struct Mos1Out {
   double vbs, vbd, vgs, vds, vgd, Vgb, von, vdsat;
   double vbs_orig, vbd_orig, vgs_orig, vds_orig, vgd_orig;

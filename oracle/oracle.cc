@@ -215,7 +215,7 @@ struct orc_ctx {
   std::vector<int> v_p, v_n, v_b; std::vector<Wave> v_w;
   std::vector<int> i_p, i_n; std::vector<Wave> i_w;
   std::vector<int> d_p, d_n, d_pri; std::vector<DiodeT> d_t;
-  std::vector<int> m_d, m_g, m_s, m_b; std::vector<Mos1T> m_t;
+  std::vector<int> m_d, m_g, m_s, m_b, m_dp, m_sp; std::vector<Mos1T> m_t;
   std::vector<int> b_d, b_g, b_s, b_b; std::vector<b4::Inst> b_t;
   std::vector<double> b_von;  // BSIM4 instance member von (last evaluation's Vth)
   // pattern (CSR) and per-device stamp positions
@@ -269,7 +269,9 @@ int csr_find(const orc_ctx *c, int r, int col) {
 // Resistor (N_DEV_Resistor.C): (p,p)(p,n)(n,p)(n,n).  Capacitor likewise.
 // Vsrc (N_DEV_Vsrc.C:1430-1460): (p,b)(n,b)(b,p)(b,n).
 // Diode (N_DEV_Diode.C:741-768): (P,P)(P,Pri)(N,N)(N,Pri)(Pri,P)(Pri,N)(Pri,Pri).
-// MOSFET1 without series resistance: full 4x4 over (D,G,S,B).
+// MOSFET1 (N_DEV_MOSFET1.C:1640-1700): full 4x4 over (D',G,S',B), then
+// (D,D)(D,D')(D',D) and (S,S)(S,S')(S',S) for the series resistances (these
+// land on the core's (D',D') / (S',S') when there is none).
 void stamp_pairs(orc_ctx *c, std::vector<std::pair<int, int>> &all) {
   for (size_t k = 0; k < c->r_p.size(); ++k) {
     int p = c->r_p[k], n = c->r_n[k];
@@ -289,9 +291,12 @@ void stamp_pairs(orc_ctx *c, std::vector<std::pair<int, int>> &all) {
     all.push_back({R, P}); all.push_back({R, N}); all.push_back({R, R});
   }
   for (size_t k = 0; k < c->m_d.size(); ++k) {
-    int nd[4] = {c->m_d[k], c->m_g[k], c->m_s[k], c->m_b[k]};
+    int nd[4] = {c->m_dp[k], c->m_g[k], c->m_sp[k], c->m_b[k]};
     for (int a = 0; a < 4; ++a)
       for (int b = 0; b < 4; ++b) all.push_back({nd[a], nd[b]});
+    const int D = c->m_d[k], Dp = c->m_dp[k], S = c->m_s[k], Sp = c->m_sp[k];
+    all.push_back({D, D}); all.push_back({D, Dp}); all.push_back({Dp, D});
+    all.push_back({S, S}); all.push_back({S, Sp}); all.push_back({Sp, S});
   }
   // BSIM4 without internal nodes: full 4x4 over (D,G,S,B)
   for (size_t k = 0; k < c->b_d.size(); ++k) {
@@ -352,12 +357,17 @@ int orc_add_diodes(orc_ctx *c, int n, const int *p, const int *m, const int *pri
   return 0;
 }
 int orc_add_mosfet1(orc_ctx *c, int n, const int *d, const int *g, const int *s, const int *b,
-                    const double *params) {
+                    const int *dp, const int *sp, const double *params) {
   for (int k = 0; k < n; ++k) {
     const double *pp = params + (size_t)k * MP_COUNT;
-    if (pp[MP_RD] != 0.0 || pp[MP_RS] != 0.0) return -2;  // series R not restated
+    const Mos1T t = mos1_temperature(pp);
+    // the internal nodes exist exactly when the conductances are nonzero
+    // (N_DEV_MOSFET1.C:1437-1445)
+    if ((t.drainConductance != 0.0) == (dp[k] == d[k])) return -2;
+    if ((t.sourceConductance != 0.0) == (sp[k] == s[k])) return -2;
     c->m_d.push_back(d[k]); c->m_g.push_back(g[k]); c->m_s.push_back(s[k]); c->m_b.push_back(b[k]);
-    c->m_t.push_back(mos1_temperature(pp));
+    c->m_dp.push_back(dp[k]); c->m_sp.push_back(sp[k]);
+    c->m_t.push_back(t);
   }
   return 0;
 }
@@ -435,7 +445,7 @@ int orc_finalize(orc_ctx *c) {
   fill(c->pos_c, o, 4 * c->c_p.size()); o += 4 * c->c_p.size();
   fill(c->pos_v, o, 4 * c->v_p.size()); o += 4 * c->v_p.size();
   fill(c->pos_d, o, 7 * c->d_p.size()); o += 7 * c->d_p.size();
-  fill(c->pos_m, o, 16 * c->m_d.size()); o += 16 * c->m_d.size();
+  fill(c->pos_m, o, 22 * c->m_d.size()); o += 22 * c->m_d.size();
   fill(c->pos_b, o, 16 * c->b_d.size()); o += 16 * c->b_d.size();
   build_csc(c);
   c->nsto = 3 * (int)c->d_p.size() + 6 * (int)c->m_d.size() + 5 * (int)c->b_d.size();
@@ -532,7 +542,10 @@ int orc_load(orc_ctx *c, double time, const double *x, const double *sta_curr, c
   const int so = 3 * nd;  // store offset of the MOSFET block
   for (int k = 0; k < nm; ++k) {
     const Mos1T &t = c->m_t[k];
-    int D = c->m_d[k], G = c->m_g[k], S = c->m_s[k], Bn = c->m_b[k];
+    // D and S are the drain' and source' nodes the device equations act on;
+    // Dx and Sx the external ones, joined to them by the series conductances
+    int D = c->m_dp[k], G = c->m_g[k], S = c->m_sp[k], Bn = c->m_b[k];
+    const int Dx = c->m_d[k], Sx = c->m_s[k];
     const double *hs = (newton_iter == 0) ? sto_curr : sto_next_in;
     double hist[5] = {hs[so + 0 * nm + k], hs[so + 1 * nm + k], hs[so + 2 * nm + k], hs[so + 3 * nm + k],
                       hs[so + 4 * nm + k]};
@@ -549,9 +562,15 @@ int orc_load(orc_ctx *c, double time, const double *x, const double *sta_curr, c
     sta_next[6 * nm + k] = o.qbd; sta_next[7 * nm + k] = o.qbs;
     const double dt = t.dtype, M = t.M;
     double ceqbs = dt * o.cbs, ceqbd = dt * o.cbd;
+    // series resistances: Idrain = drainConductance * Vddp (N_DEV_MOSFET1.C:3386),
+    // loadDAEFVector :2212-2240
+    const double gdpr = t.drainConductance, gspr = t.sourceConductance;
+    const double Idrain = gdpr * (X(Dx) - X(D)), Isource = gspr * (X(Sx) - X(S));
+    if (gdpr != 0.0) addv(F, Dx, Idrain * M);
+    if (gspr != 0.0) addv(F, Sx, Isource * M);
     addv(F, Bn, (ceqbs + ceqbd) * M);
-    addv(F, D, (-(ceqbd - o.cdreq)) * M);
-    addv(F, S, (-(ceqbs + o.cdreq)) * M);
+    addv(F, D, (-Idrain - (ceqbd - o.cdreq)) * M);
+    addv(F, S, (-Isource - (ceqbs + o.cdreq)) * M);
     double Qeqbs = dt * o.qbs, Qeqbd = dt * o.qbd, Qeqgb = dt * o.qgb, Qeqgs = dt * o.qgs, Qeqgd = dt * o.qgd;
     addv(Q, G, (Qeqgs + Qeqgd + Qeqgb) * M);
     addv(Q, Bn, (Qeqbs + Qeqbd - Qeqgb) * M);
@@ -574,21 +593,28 @@ int orc_load(orc_ctx *c, double time, const double *x, const double *sta_curr, c
       double q6 = dt * (-gcgs * dvgs - gcbs * dvbs);
       addv(dQdxdVp, G, q2 * M); addv(dQdxdVp, Bn, q4 * M); addv(dQdxdVp, D, q5 * M); addv(dQdxdVp, S, q6 * M);
     }
-    // Jacobian: positions pos_m[16k + 4a + b] for nodes (D,G,S,B) = (0,1,2,3)
-    const int *ps = &c->pos_m[16 * k];
+    // Jacobian: positions pos_m[22k + 4a + b] for nodes (D',G,S',B) = (0,1,2,3),
+    // then pos_m[22k + 16..21] for (D,D)(D,D')(D',D)(S,S)(S,S')(S',S)
+    const int *ps = &c->pos_m[22 * k];
     auto J = [&](int a, int b) { return ps[4 * a + b]; };
-    // dFdx (drain/source conductances are zero: RD = RS = 0)
+    // dFdx (loadDAEdFdx, N_DEV_MOSFET1.C:2484-2660)
+    if (gdpr != 0.0) {
+      addm(dFdx, ps[16], gdpr * M); addm(dFdx, ps[17], -(gdpr * M)); addm(dFdx, ps[18], -(gdpr * M));
+    }
+    if (gspr != 0.0) {
+      addm(dFdx, ps[19], gspr * M); addm(dFdx, ps[20], -(gspr * M)); addm(dFdx, ps[21], -(gspr * M));
+    }
     addm(dFdx, J(3, 3), (o.gbs + o.gbd) * M);
     addm(dFdx, J(3, 0), -o.gbd * M);
     addm(dFdx, J(3, 2), -o.gbs * M);
     addm(dFdx, J(0, 1), o.Gm * M);
     addm(dFdx, J(0, 3), (-o.gbd + o.Gmbs) * M);
-    addm(dFdx, J(0, 0), (o.gds + o.gbd + o.revsum) * M);
+    addm(dFdx, J(0, 0), (gdpr + o.gds + o.gbd + o.revsum) * M);
     addm(dFdx, J(0, 2), (-o.gds - o.nrmsum) * M);
     addm(dFdx, J(2, 1), -o.Gm * M);
     addm(dFdx, J(2, 3), -(o.gbs + o.Gmbs) * M);
     addm(dFdx, J(2, 0), -(o.gds + o.revsum) * M);
-    addm(dFdx, J(2, 2), (o.gds + o.gbs + o.nrmsum) * M);
+    addm(dFdx, J(2, 2), (gspr + o.gds + o.gbs + o.nrmsum) * M);
     // dQdx (old Meyer; TRANOP and transient load the capacitances)
     double gcgd = o.Capgd, gcgs = o.Capgs, gcgb = o.Capgb, gcbs = o.capbs, gcbd = o.capbd;
     addm(dQdx, J(1, 1), (gcgd + gcgs + gcgb) * M);

@@ -51,8 +51,9 @@ int orc_add_isources(orc_ctx *c, int n, const int *pos, const int *neg,
                      const int *kind, const int *off, const double *data);
 int orc_add_diodes(orc_ctx *c, int n, const int *pos, const int *neg, const int *pri,
                    const double *params);
+/* dp / sp: the drain' / source' nodes (== d / s without series resistance). */
 int orc_add_mosfet1(orc_ctx *c, int n, const int *d, const int *g, const int *s, const int *b,
-                    const double *params);
+                    const int *dp, const int *sp, const double *params);
 /* BSIM 4.8.2 (level 54), restated scope in bsim4.h; params n x b4::P_COUNT
  * (NaN = not given).  Returns -4 for a card outside that scope. */
 int orc_add_bsim4(orc_ctx *c, int n, const int *d, const int *g, const int *s, const int *b,

@@ -87,6 +87,8 @@ def _fd_check(oracle_mod, nl, rng, dcop, shift=0.0):
                                    lambda: N.diode_ladder(9, seed=3, sidewall=True),
                                    lambda: N.ring_oscillator(5),
                                    lambda: N.ring_oscillator(5, caps=True),
+                                   lambda: N.ring_oscillator(5, series=True),
+                                   lambda: N.ring_oscillator(5, caps=True, series=True),
                                    lambda: N.bsim4_inverter_chain(2),
                                    lambda: N.bsim4_logic_dag(60, 4, seed=2, tstop=0.3e-9)])
 def test_finite_difference_jacobian(oracle_mod, maker):
@@ -199,6 +201,45 @@ def test_diode_sidewall_iv_point(oracle_mod, ns):
         i_d = 1e-14 * np.expm1(vd / vt) + isw * np.expm1(vd / (ns * vt))
     assert abs((1.0 - vd) / 1e3 - (i_d + 1e-12 * vd)) < 1e-6
     assert 0.45 < vd < 0.75
+
+
+def test_mosfet1_series_resistance_dc_point(oracle_mod):
+    """NMOS in saturation with RS in the source and RD in the drain
+    (N_DEV_MOSFET1.C:410-450, 2212-2240): Id = beta/2 (Vg - Id RS - VTO)^2,
+    the drain' sits Id * RD below the supply, the source' Id * RS above ground."""
+    nl = N.Netlist(label="nmos_rs")
+    vdd, gate = nl.node("vdd"), nl.node("g")
+    nl.V(vdd, -1, N.WAVE_DC, [1.8])
+    nl.V(gate, -1, N.WAVE_DC, [1.2])
+    nl.M1(vdd, gate, -1, -1, TYPE=1.0, VTO=0.5, KP=120e-6, W=2e-6, L=0.18e-6, RD=2000.0, RS=500.0)
+    d, g, s, b, row, dp, sp = nl.mos1[0]
+    assert dp != d and sp != s and sp >= 0
+    st, x, it = oracle_mod.Oracle(nl).dcop()
+    beta = 120e-6 * 2e-6 / 0.18e-6
+    # beta/2 (v - RS Id)^2 = Id with v = Vg - VTO: the smaller root
+    v, rs = 1.2 - 0.5, 500.0
+    a = beta / 2 * rs * rs
+    bq = -(beta * rs * v + 1.0)
+    cq = beta / 2 * v * v
+    i_d = (-bq - np.sqrt(bq * bq - 4 * a * cq)) / (2 * a)
+    assert abs(x[sp] - i_d * rs) < 1e-6 and abs(1.8 - x[dp] - i_d * 2000.0) < 1e-6
+    # RSH with squares gives the same point as the equal RD / RS
+    nl2 = N.Netlist(label="nmos_rsh")
+    vdd, gate = nl2.node("vdd"), nl2.node("g")
+    nl2.V(vdd, -1, N.WAVE_DC, [1.8])
+    nl2.V(gate, -1, N.WAVE_DC, [1.2])
+    nl2.M1(vdd, gate, -1, -1, TYPE=1.0, VTO=0.5, KP=120e-6, W=2e-6, L=0.18e-6, RSH=100.0, NRD=20.0,
+           NRS=5.0)
+    st2, x2, _ = oracle_mod.Oracle(nl2).dcop()
+    assert abs(x2[nl2.mos1[0][6]] - x[sp]) < 1e-9 and abs(x2[nl2.mos1[0][5]] - x[dp]) < 1e-9
+
+
+def test_mosfet1_series_nodes_are_checked(oracle_mod):
+    nl = N.ring_oscillator(3, series=True)
+    d, g, s, b, row, dp, sp = nl.mos1[0]
+    nl.mos1[0] = (d, g, s, b, row, d, sp)  # RD given but no drain' node
+    with pytest.raises(ValueError):
+        oracle_mod.Oracle(nl)
 
 
 def test_bsim4_iv_known_behaviour(oracle_mod):

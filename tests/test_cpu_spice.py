@@ -266,6 +266,26 @@ D2 a 0 dmerged
         S.parse("bad\n.MODEL d1 D (NSGIVEN=1)\nD1 a 0 d1\nV1 a 0 1\n.TRAN 1n 1u\n.END\n")
 
 
+def test_mosfet1_series_resistance_card():
+    d = S.parse("""series
+.MODEL nrs NMOS (LEVEL=1 VTO=0.5 KP=120u RD=40 RS=25)
+.MODEL psh PMOS (LEVEL=1 VTO=-0.5 KP=40u RSH=50)
+VDD vdd 0 1.8
+M1 out in 0 0 nrs W=2u L=0.18u
+M2 out in vdd vdd psh W=4u L=0.18u NRD=2 NRS=1.5
+V1 in 0 PULSE(0 1.8 0 10p 10p 100p 200p)
+.TRAN 1p 100p
+.END
+""")
+    nl = d.netlist
+    f = N.MOS1_FIELDS.index
+    (d1, g1, s1, b1, r1, dp1, sp1), (d2, g2, s2, b2, r2, dp2, sp2) = nl.mos1
+    assert r1[f("RD")] == 40.0 and r1[f("RS")] == 25.0 and dp1 != d1 and sp1 != s1
+    assert r2[f("RSH")] == 50.0 and r2[f("NRD")] == 2.0 and r2[f("NRS")] == 1.5
+    assert dp2 != d2 and sp2 != s2
+    assert N.mos1_series(r2) == (1.0 / 100.0, 1.0 / 75.0)
+
+
 def test_bsim4_model_card_and_instance():
     d = S.parse("""bsim4 inverter
 .MODEL n1 NMOS (LEVEL=54 VERSION=4.8.2 TOXE=1.8n VTH0=0.4)

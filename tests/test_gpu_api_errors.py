@@ -49,13 +49,25 @@ def test_bad_arguments_and_order(xg, torch_cuda):
     assert L.xg_destroy(h) == xg.XG_OK
 
 
+def test_mosfet1_series_resistance_nodes_checked(xg, torch_cuda):
+    """A row with RD (or RSH) needs the drain' node: xg_add_mosfet1 refuses
+    it, and xg_add_mosfet1_rs wants d' != d exactly when the conductance is
+    nonzero."""
+    L, h = _ctx(xg, n=4)
+    i32 = lambda *v: np.array(v, np.int32)
+    row = N.mos1_row(TYPE=1.0, VTO=0.5, KP=1e-4, RD=10.0)
+    assert L.xg_add_mosfet1(h, 1, i32(0), i32(1), i32(-1), i32(-1), row) == -1
+    assert b"xg_add_mosfet1_rs" in L.xg_error_string(h)
+    assert L.xg_add_mosfet1_rs(h, 1, i32(0), i32(1), i32(-1), i32(-1), i32(0), i32(-1), row) == -1
+    assert L.xg_add_mosfet1_rs(h, 1, i32(0), i32(1), i32(-1), i32(-1), i32(2), i32(3), row) == -1
+    ok = N.mos1_row(TYPE=1.0, VTO=0.5, KP=1e-4, RSH=5.0, NRD=2.0)  # RS = 0, RSH * NRS = 5 ohm
+    assert L.xg_add_mosfet1_rs(h, 1, i32(0), i32(1), i32(-1), i32(-1), i32(2), i32(3), ok) == xg.XG_OK
+    bad = N.mos1_row(TYPE=1.0, VTO=0.5, KP=1e-4, RSH=5.0, NRD=0.0)  # 1/(RSH * 0)
+    assert L.xg_add_mosfet1_rs(h, 1, i32(0), i32(1), i32(-1), i32(-1), i32(2), i32(3), bad) == -1
+    assert L.xg_destroy(h) == xg.XG_OK
+
+
 def test_unsupported_device_cards(xg, torch_cuda):
-    nl = N.Netlist(label="unsupported")
-    a, b = nl.node("a"), nl.node("b")
-    nl.M1(a, b, -1, -1, TYPE=1.0, VTO=0.5, KP=1e-4, RD=10.0)  # MOSFET-1 series resistance
-    with pytest.raises(xg.XgError) as e:
-        xg.Circuit(nl)
-    assert e.value.code == -4
     nl = N.Netlist(label="b4_bad_type")
     a, b = nl.node("a"), nl.node("b")
     nl.M4(a, b, -1, -1, TYPE=0.5, L=45e-9, W=90e-9)  # TYPE must be +-1

@@ -37,6 +37,11 @@ def torch_cuda():
     return torch
 
 
+def _short(nl, tstop):
+    nl.tran.tstop = tstop
+    return nl
+
+
 def _t(torch, a):
     return torch.as_tensor(np.ascontiguousarray(a, np.float64), device="cuda:0")
 
@@ -99,6 +104,8 @@ def _loader_case(xg, oracle_mod, torch, nl, seed, newton_iter, dcop, init_jct, c
     (lambda: N.diode_ladder(30, seed=3), False),
     (lambda: N.ring_oscillator(11), False),
     (lambda: N.ring_oscillator(11, caps=True), True),
+    (lambda: N.ring_oscillator(11, series=True), False),
+    (lambda: N.ring_oscillator(11, caps=True, series=True), True),
     (lambda: N.monte_carlo_rings(3, 11, 21, seed=2), False),
     (lambda: N.power_grid(6, 5, seed=1), False),
     (lambda: N.bsim4_inverter_chain(3), True),
@@ -220,6 +227,8 @@ def _compare_waveforms(t_ref, v_ref, t_gpu, v_gpu):
     ("diode_ladder_50", lambda: N.diode_ladder(50, seed=5), ["n1", "n25", "n50"]),
     ("ring_101", lambda: N.ring_oscillator(101), ["n1", "n50", "n101"]),
     ("ring_21_caps", lambda: N.ring_oscillator(21, caps=True), ["n1", "n11"]),
+    ("ring_11_caps_rs", lambda: _short(N.ring_oscillator(11, caps=True, series=True), 6e-9),
+     ["n1", "n6", "n11"]),
     ("b4_chain_3", lambda: N.bsim4_inverter_chain(3), ["in", "n1", "n3"]),
     ("b4_dag_300", lambda: N.bsim4_logic_dag(300, 8, seed=4, tstop=1e-9), ["g10", "g40", "g70"]),
 ])
@@ -346,9 +355,9 @@ def test_batched_circuits_match_independent_runs(xg, oracle_mod, torch_cuda):
         for (a, b, kind, data) in batch.isrc:
             if off0 <= max(a, b) < off1:
                 single.isrc.append((remap(a), remap(b), kind, data))
-        for (d, g, s, bb, row) in batch.mos1:
+        for (d, g, s, bb, row, dp, sp) in batch.mos1:
             if off0 <= d < off1:
-                single.mos1.append((remap(d), remap(g), remap(s), remap(bb), row))
+                single.mos1.append((remap(d), remap(g), remap(s), remap(bb), row, remap(dp), remap(sp)))
         single.tran = batch.tran
         k = int(counts[i])
         # the same circuit alone on the GPU

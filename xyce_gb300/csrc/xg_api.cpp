@@ -34,6 +34,10 @@ struct xg_ctx {
   bool unknowns_set = false, finalized = false;
   // host copies of the devices
   std::vector<int> r_p, r_n, c_p, c_n, v_p, v_n, v_b, i_p, i_n;
+  // MOSFET-1 series conductances (drainConductance * M between d and d',
+  // sourceConductance * M between s and s'): constant, in the linear part
+  std::vector<int> sg_p, sg_n;
+  std::vector<double> sg_v;
   std::vector<double> r_v, c_v;
   std::vector<Wave> v_w, i_w;
   std::vector<int> d_p, d_n, d_r;
@@ -311,23 +315,65 @@ int xg_add_diodes(xg_ctx *ctx, int n, const int *pos, const int *neg, const int 
   return XG_OK;
 }
 
-int xg_add_mosfet1(xg_ctx *ctx, int n, const int *dd, const int *g, const int *s, const int *b,
-                   const double *params) {
-  SETUP_CHECK(dd, g, s, b, params);
+// Series drain or source conductance (Instance::processParams,
+// N_DEV_MOSFET1.C:410-450): 1/R when R is nonzero, else 1/(RSH * squares)
+// when RSH is nonzero, else 0.
+static double mos1_series_conductance(double r, double rsh, double squares) {
+  if (r != 0.0) return 1.0 / r;
+  if (rsh != 0.0) return 1.0 / (rsh * squares);
+  return 0.0;
+}
+
+// dp / sp null: the row must have no series resistance (xg_add_mosfet1).
+static int add_mosfet1(xg_ctx *ctx, int n, const int *dd, const int *g, const int *s, const int *b,
+                       const int *dp, const int *sp, const double *params) {
+  std::vector<double> gd(n), gs(n);
   for (int k = 0; k < n; ++k) {
     if (!valid_node(ctx, dd[k]) || !valid_node(ctx, g[k]) || !valid_node(ctx, s[k]) || !valid_node(ctx, b[k]))
       return fail(ctx, XG_ERR_ARG, "MOSFET node out of range");
     const double *p = params + (size_t)k * XG_MOS1_NPARAM;
-    if (p[XG_MOS1_RD] != 0.0 || p[XG_MOS1_RS] != 0.0)
-      return fail(ctx, XG_ERR_UNSUPPORTED, "MOSFET level 1 with series drain/source resistance");
     if (p[XG_MOS1_TYPE] != 1.0 && p[XG_MOS1_TYPE] != -1.0) return fail(ctx, XG_ERR_ARG, "MOSFET TYPE must be +1 or -1");
+    gd[k] = mos1_series_conductance(p[XG_MOS1_RD], p[XG_MOS1_RSH], p[XG_MOS1_NRD]);
+    gs[k] = mos1_series_conductance(p[XG_MOS1_RS], p[XG_MOS1_RSH], p[XG_MOS1_NRS]);
+    if (!std::isfinite(gd[k]) || !std::isfinite(gs[k]) || !std::isfinite(gd[k] * p[XG_MOS1_M]) ||
+        !std::isfinite(gs[k] * p[XG_MOS1_M]))
+      return fail(ctx, XG_ERR_ARG, "MOSFET series conductance (RD, RS, RSH * NRD / NRS) must be finite");
+    if (!dp) {
+      if (gd[k] != 0.0 || gs[k] != 0.0)
+        return fail(ctx, XG_ERR_ARG, "MOSFET series resistance needs the internal nodes: use xg_add_mosfet1_rs");
+      continue;
+    }
+    if (!valid_node(ctx, dp[k]) || !valid_node(ctx, sp[k])) return fail(ctx, XG_ERR_ARG, "MOSFET node out of range");
+    if ((gd[k] != 0.0) == (dp[k] == dd[k]))
+      return fail(ctx, XG_ERR_ARG, "MOSFET drain' must differ from drain exactly when the drain conductance is nonzero");
+    if ((gs[k] != 0.0) == (sp[k] == s[k]))
+      return fail(ctx, XG_ERR_ARG, "MOSFET source' must differ from source exactly when the source conductance is nonzero");
+    if ((gd[k] != 0.0 && dp[k] < 0) || (gs[k] != 0.0 && sp[k] < 0))
+      return fail(ctx, XG_ERR_ARG, "MOSFET drain'/source' internal node cannot be ground");
   }
-  ctx->m_d.insert(ctx->m_d.end(), dd, dd + n);
+  ctx->m_d.insert(ctx->m_d.end(), dp ? dp : dd, (dp ? dp : dd) + n);
   ctx->m_g.insert(ctx->m_g.end(), g, g + n);
-  ctx->m_s.insert(ctx->m_s.end(), s, s + n);
+  ctx->m_s.insert(ctx->m_s.end(), sp ? sp : s, (sp ? sp : s) + n);
   ctx->m_b.insert(ctx->m_b.end(), b, b + n);
   ctx->m_par.insert(ctx->m_par.end(), params, params + (size_t)n * XG_MOS1_NPARAM);
+  for (int k = 0; dp && k < n; ++k) {
+    const double M = params[(size_t)k * XG_MOS1_NPARAM + XG_MOS1_M];
+    if (gd[k] != 0.0) { ctx->sg_p.push_back(dd[k]); ctx->sg_n.push_back(dp[k]); ctx->sg_v.push_back(gd[k] * M); }
+    if (gs[k] != 0.0) { ctx->sg_p.push_back(s[k]); ctx->sg_n.push_back(sp[k]); ctx->sg_v.push_back(gs[k] * M); }
+  }
   return XG_OK;
+}
+
+int xg_add_mosfet1(xg_ctx *ctx, int n, const int *dd, const int *g, const int *s, const int *b,
+                   const double *params) {
+  SETUP_CHECK(dd, g, s, b, params);
+  return add_mosfet1(ctx, n, dd, g, s, b, nullptr, nullptr, params);
+}
+
+int xg_add_mosfet1_rs(xg_ctx *ctx, int n, const int *dd, const int *g, const int *s, const int *b,
+                      const int *dp, const int *sp, const double *params) {
+  SETUP_CHECK(dd, g, s, b, dp, sp, params);
+  return add_mosfet1(ctx, n, dd, g, s, b, dp, sp, params);
 }
 
 int xg_add_bsim4(xg_ctx *ctx, int n, const int *dd, const int *g, const int *s, const int *b,
@@ -383,6 +429,8 @@ int xg_finalize(xg_ctx *ctx) {
     if (!same_circuit({ctx->b_d[k], ctx->b_g[k], ctx->b_s[k], ctx->b_b[k]})) return fail(ctx, XG_ERR_ARG, "BSIM4 spans two circuits");
   for (size_t k = 0; k < ctx->r_p.size(); ++k)
     if (!same_circuit({ctx->r_p[k], ctx->r_n[k]})) return fail(ctx, XG_ERR_ARG, "resistor spans two circuits");
+  for (size_t k = 0; k < ctx->sg_p.size(); ++k)
+    if (!same_circuit({ctx->sg_p[k], ctx->sg_n[k]})) return fail(ctx, XG_ERR_ARG, "MOSFET spans two circuits");
   for (size_t k = 0; k < ctx->c_p.size(); ++k)
     if (!same_circuit({ctx->c_p[k], ctx->c_n[k]})) return fail(ctx, XG_ERR_ARG, "capacitor spans two circuits");
   for (int k = 0; k < nv; ++k)
@@ -409,6 +457,10 @@ int xg_finalize(xg_ctx *ctx) {
   auto for_positions = [&](auto &&emit) {
     for (size_t k = 0; k < ctx->r_p.size(); ++k) {
       int p = ctx->r_p[k], m = ctx->r_n[k];
+      emit(p, p); emit(p, m); emit(m, p); emit(m, m);
+    }
+    for (size_t k = 0; k < ctx->sg_p.size(); ++k) {
+      int p = ctx->sg_p[k], m = ctx->sg_n[k];
       emit(p, p); emit(p, m); emit(m, p); emit(m, m);
     }
     for (size_t k = 0; k < ctx->c_p.size(); ++k) {
@@ -470,6 +522,11 @@ int xg_finalize(xg_ctx *ctx) {
   for (size_t k = 0; k < ctx->r_p.size(); ++k) {
     int p = ctx->r_p[k], m = ctx->r_n[k];
     double G = 1.0 / ctx->r_v[k];
+    addv(Glin, p, p, G); addv(Glin, p, m, -G); addv(Glin, m, p, -G); addv(Glin, m, m, G);
+  }
+  for (size_t k = 0; k < ctx->sg_p.size(); ++k) {
+    int p = ctx->sg_p[k], m = ctx->sg_n[k];
+    double G = ctx->sg_v[k];
     addv(Glin, p, p, G); addv(Glin, p, m, -G); addv(Glin, m, p, -G); addv(Glin, m, m, G);
   }
   for (size_t k = 0; k < ctx->c_p.size(); ++k) {

@@ -36,11 +36,25 @@ DIODE_DEFAULTS = dict(IS=1e-14, N=1.0, RS=0.0, CJO=0.0, VJ=1.0, M=0.5, FC=0.5, T
 # MOSFET level-1 parameter row (model + instance; N_DEV_MOSFET1.C addPar defaults).
 MOS1_FIELDS = ["TYPE", "VTO", "KP", "GAMMA", "PHI", "LAMBDA", "RD", "RS", "CBD", "CBS",
                "IS", "PB", "CGSO", "CGDO", "CGBO", "CJ", "MJ", "CJSW", "MJSW", "JS",
-               "TOX", "LD", "FC", "W", "L", "AD", "AS", "PD", "PS", "M"]
+               "TOX", "LD", "FC", "W", "L", "AD", "AS", "PD", "PS", "M", "RSH", "NRD", "NRS"]
 MOS1_DEFAULTS = dict(TYPE=1.0, VTO=0.0, KP=2e-5, GAMMA=0.0, PHI=0.6, LAMBDA=0.0, RD=0.0,
                      RS=0.0, CBD=0.0, CBS=0.0, IS=1e-14, PB=0.8, CGSO=0.0, CGDO=0.0,
                      CGBO=0.0, CJ=0.0, MJ=0.5, CJSW=0.0, MJSW=0.5, JS=0.0, TOX=0.0, LD=0.0,
-                     FC=0.5, W=1e-4, L=1e-4, AD=0.0, AS=0.0, PD=0.0, PS=0.0, M=1.0)
+                     FC=0.5, W=1e-4, L=1e-4, AD=0.0, AS=0.0, PD=0.0, PS=0.0, M=1.0, RSH=0.0,
+                     NRD=1.0, NRS=1.0)
+
+
+def mos1_series(row) -> tuple:
+    """(drain, source) series conductances of a MOSFET-1 row
+    (Instance::processParams, N_DEV_MOSFET1.C:410-450): 1/RD when RD is
+    nonzero, else 1/(RSH*NRD) when RSH is nonzero, else 0 (no internal node)."""
+    f = MOS1_FIELDS.index
+
+    def g(r, sq):
+        if row[f(r)] != 0.0:
+            return 1.0 / row[f(r)]
+        return 1.0 / (row[f("RSH")] * row[f(sq)]) if row[f("RSH")] != 0.0 else 0.0
+    return g("RD", "NRD"), g("RS", "NRS")
 
 
 # BSIM4 (level 54) parameter row: instance + model parameters in the order of
@@ -160,7 +174,14 @@ class Netlist:
         self.diode.append((a, b, pri, row))
 
     def M1(self, d, g, s, b, **params):
-        self.mos1.append((d, g, s, b, mos1_row(**params)))
+        """MOSFET level 1; drain' / source' internal nodes are made when the
+        series resistance (RD / RS, or RSH with NRD / NRS) is nonzero.
+        Stored as (d, g, s, b, row, d', s')."""
+        row = mos1_row(**params)
+        gd, gs = mos1_series(row)
+        dp = self.node() if gd != 0.0 else d
+        sp = self.node() if gs != 0.0 else s
+        self.mos1.append((d, g, s, b, row, dp, sp))
 
     def M4(self, d, g, s, b, **params):
         """BSIM4 (level 54) instance; parameters not named are not given."""
@@ -196,6 +217,7 @@ class Netlist:
                         f64(np.array([d[3] for d in self.diode]).reshape(-1, len(DIODE_FIELDS))))
         out["mos1"] = (i32([m[0] for m in self.mos1]), i32([m[1] for m in self.mos1]),
                        i32([m[2] for m in self.mos1]), i32([m[3] for m in self.mos1]),
+                       i32([m[5] for m in self.mos1]), i32([m[6] for m in self.mos1]),
                        f64(np.array([m[4] for m in self.mos1]).reshape(-1, len(MOS1_FIELDS))))
         out["bsim4"] = (i32([m[0] for m in self.bsim4]), i32([m[1] for m in self.bsim4]),
                         i32([m[2] for m in self.bsim4]), i32([m[3] for m in self.bsim4]),
@@ -320,20 +342,31 @@ def _ring(nl: Netlist, stages: int, vdd=1.8, cload=5e-15, nmos=None, pmos=None,
     nl.I(-1, outs[0], WAVE_PWL, [0.0, 0.0, 10e-12, kick, 990e-12, kick, 1e-9, 0.0])
 
 
-def ring_oscillator(stages=101, caps=False) -> Netlist:
+def ring_oscillator(stages=101, caps=False, series=False) -> Netlist:
     """CMOS ring oscillator of MOSFET level-1 inverters: VDD=1.8 V, NMOS VTO=0.5
     KP=120u, PMOS VTO=-0.5 KP=40u, W/L=2u/0.18u (PMOS W=4u), 5 fF per stage, a
     1 ns PWL kick on node 1; .TRAN 0 20n, max step 5 p.
 
     caps=True adds gate oxide (TOX), overlap and bulk-junction capacitances so
-    that the Meyer and junction-charge paths of the model are exercised."""
+    that the Meyer and junction-charge paths of the model are exercised.
+
+    series=True adds series resistances: RD = 400, RS = 250 ohm on the NMOS;
+    RSH = 50 ohm with NRD = 2, NRS = 1.5 squares on the PMOS, which are also
+    two in parallel (M = 2)."""
     assert stages % 2 == 1
-    nl = Netlist(label=f"ring_{stages}" + ("_caps" if caps else ""))
+    nl = Netlist(label=f"ring_{stages}" + ("_caps" if caps else "") + ("_rs" if series else ""))
+    nmos, pmos = dict(NMOS_CARD), dict(PMOS_CARD)
     if caps:
         extra = dict(TOX=4e-9, CGSO=2e-10, CGDO=2e-10, CGBO=1e-10, CJ=1e-3, CJSW=2e-10,
                      MJ=0.45, MJSW=0.33, AD=1e-12, AS=1e-12, PD=4e-6, PS=4e-6, GAMMA=0.4,
                      LAMBDA=0.05, PHI=0.7)
-        _ring(nl, stages, nmos=dict(NMOS_CARD, **extra), pmos=dict(PMOS_CARD, **extra))
+        nmos.update(extra)
+        pmos.update(extra)
+    if series:
+        nmos.update(RD=400.0, RS=250.0)
+        pmos.update(RSH=50.0, NRD=2.0, NRS=1.5, M=2.0)
+    if caps or series:
+        _ring(nl, stages, nmos=nmos, pmos=pmos)
     else:
         _ring(nl, stages)
     nl.tran = Tran(tstop=20e-9, hmax=5e-12)
@@ -414,7 +447,8 @@ def batch(nls: list, label: str = "batch") -> Netlist:
         out.vsrc += [(sh(a), sh(b), sh(br), kd, list(d)) for (a, b, br, kd, d) in nl.vsrc]
         out.isrc += [(sh(a), sh(b), kd, list(d)) for (a, b, kd, d) in nl.isrc]
         out.diode += [(sh(a), sh(b), sh(p), row) for (a, b, p, row) in nl.diode]
-        out.mos1 += [(sh(d), sh(g), sh(s_), sh(b), row) for (d, g, s_, b, row) in nl.mos1]
+        out.mos1 += [(sh(d), sh(g), sh(s_), sh(b), row, sh(dp), sh(sp))
+                     for (d, g, s_, b, row, dp, sp) in nl.mos1]
         out.bsim4 += [(sh(d), sh(g), sh(s_), sh(b), row) for (d, g, s_, b, row) in nl.bsim4]
         out.offsets += [o + base for o in nl.offsets[1:]]
     out.tran = nls[0].tran if nls else None
@@ -436,7 +470,8 @@ def extract_circuit(nl: Netlist, ci: int) -> Netlist:
     out.vsrc = [(rm(a), rm(b), rm(br), k, d) for (a, b, br, k, d) in nl.vsrc if inside(br)]
     out.isrc = [(rm(a), rm(b), k, d) for (a, b, k, d) in nl.isrc if inside(a, b)]
     out.diode = [(rm(a), rm(b), rm(r), row) for (a, b, r, row) in nl.diode if inside(a, b, r)]
-    out.mos1 = [(rm(d), rm(g), rm(s), rm(b), row) for (d, g, s, b, row) in nl.mos1 if inside(d, g, s, b)]
+    out.mos1 = [(rm(d), rm(g), rm(s), rm(b), row, rm(dp), rm(sp))
+                for (d, g, s, b, row, dp, sp) in nl.mos1 if inside(d, g, s, b)]
     out.bsim4 = [(rm(d), rm(g), rm(s), rm(b), row) for (d, g, s, b, row) in nl.bsim4 if inside(d, g, s, b)]
     out.tran = nl.tran
     return out

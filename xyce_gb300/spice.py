@@ -161,8 +161,8 @@ class Deck:
 
 _DIODE_ALIASES = {"CJ0": "CJO", "CJ": "CJO", "PB": "VJ", "MJ": "M", "CJP": "CJSW", "PHP": "VJSW"}
 _MOS1_MODEL = {"VTO", "KP", "GAMMA", "PHI", "LAMBDA", "RD", "RS", "CBD", "CBS", "IS", "PB", "CGSO",
-               "CGDO", "CGBO", "CJ", "MJ", "CJSW", "MJSW", "JS", "TOX", "LD", "FC"}
-_MOS1_INST = {"W", "L", "AD", "AS", "PD", "PS", "M"}
+               "CGDO", "CGBO", "CJ", "MJ", "CJSW", "MJSW", "JS", "TOX", "LD", "FC", "RSH"}
+_MOS1_INST = {"W", "L", "AD", "AS", "PD", "PS", "M", "NRD", "NRS"}
 _B4_INST = {"L", "W", "AS", "AD", "PS", "PD", "M"}
 _IGNORED_MODEL = {"LEVEL", "VERSION", "TNOM"}
 
