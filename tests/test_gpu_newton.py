@@ -65,6 +65,31 @@ def test_operating_point_solve_matches_oracle(xg, oracle_mod, torch_cuda):
     _assert_same(gpu, ref)
 
 
+def test_operating_point_through_a_near_singular_start(xg, oracle_mod, torch_cuda):
+    """A ring with series drain/source resistances at junction initialisation:
+    every MOSFET is cut off, so each output node and its two drain' nodes
+    reach ground only through gmin-sized conductances (the first Jacobian
+    has condition number ~1e12).  The analysis of that matrix exempts those
+    columns from the full pivot threshold; on the second iteration the
+    devices conduct and the frozen order's pivot there collapses, which must
+    still re-pivot (the bounded exemption) rather than be accepted.  Status
+    and iteration count equal the oracle's; the converged iterate agrees
+    within the conditioning of the first solve (1e-6)."""
+    nl = N.ring_oscillator(11, series=True)
+    x0 = np.zeros(nl.n)
+    gpu, ref = _solve_both(xg, oracle_mod, torch_cuda, nl, x0, flags=xg.FLAG_DCOP | xg.FLAG_INITJCT, **DC)
+    assert ref[0] > 0
+    st, it, x = gpu
+    assert (int(st[0]), int(it[0])) == (ref[0], ref[1])
+    np.testing.assert_allclose(x, ref[2], rtol=0, atol=1e-6 * np.max(np.abs(ref[2])))
+    c = xg.Circuit(nl)
+    xd, itd = c.dcop()
+    c.close()
+    ost, ox, oit = oracle_mod.Oracle(nl).dcop()
+    assert ost > 0 and itd == oit
+    np.testing.assert_allclose(xd, ox, rtol=0, atol=1e-6 * np.max(np.abs(ox)))
+
+
 @pytest.mark.parametrize("maker,caps", [(lambda: N.ring_oscillator(101), False),
                                         (lambda: N.ring_oscillator(21, caps=True), True),
                                         (lambda: N.bsim4_inverter_chain(3), True)],

@@ -1074,7 +1074,7 @@ static int lu_upload(xg_ctx *ctx, const LUHost &H) {
   UP(L.cp, H.cp); UP(L.ri, H.ri); UP(L.diag, H.diag); UP(L.src, H.src);
   UP(L.l_ptr, H.l_ptr); UP(L.l_pos, H.l_pos); UP(L.l_col, H.l_col);
   UP(L.u_ptr, H.u_ptr); UP(L.u_pos, H.u_pos); UP(L.u_col, H.u_col);
-  UP(L.exempt, H.exempt);
+  UP(L.exempt, H.exempt); UP(L.pscale, H.pscale);
   UP(L.upd_off, H.upd_off); UP(L.upd_pos, H.upd_pos);
   {
     int *um = nullptr;

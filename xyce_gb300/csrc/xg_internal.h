@@ -20,6 +20,11 @@ constexpr int kLongSolveRow = 256;   // triangular-solve rows longer than this g
 // Frozen-pivot acceptance on the device: a pivot below this fraction of its
 // updated column triggers re-pivoting by the host.
 constexpr double kRuntimePivotTol = 1e-2;
+// A column whose pivot already failed that test in the analysis' own trial
+// factorization (a near-singular matrix: re-pivoting cannot help it) is held
+// to this fraction of the pivot ratio it had there instead, so that a frozen
+// order that goes bad on later values still re-pivots.
+constexpr double kExemptSlack = 1e-4;
 
 // Circuit phases of the device-resident state machine.
 enum Phase : int { PH_DC = 0, PH_TRAN = 1, PH_DONE = 2, PH_FAILED = 3, PH_STALL = 4, PH_PAUSED = 5 };
@@ -260,7 +265,8 @@ struct LUDev {
   double *lu = nullptr, *y = nullptr;
   int *l_ptr = nullptr, *l_pos = nullptr, *l_col = nullptr;   // L by rows (solves)
   int *u_ptr = nullptr, *u_pos = nullptr, *u_col = nullptr;   // U by rows (solves)
-  char *exempt = nullptr;    // per step: skip the threshold test
+  char *exempt = nullptr;    // per step: threshold test scaled by pscale (kExemptSlack)
+  double *pscale = nullptr;  // per exempt step: its threshold as a fraction of pivot_tol
   int *breakdown = nullptr;  // device flag: first failing step + 1
   int *upd_off = nullptr, *upd_pos = nullptr;  // per U entry: target positions of its update
   const int4 *umeta = nullptr;                   // per U entry: see LUHost::umeta
@@ -390,7 +396,8 @@ struct LUHost {
   std::vector<int> row_of_step, col_of_step, cp, ri, diag, src;
   std::vector<int> f_lvl_ptr, f_cols, l_lvl_ptr, l_rows, l_ptr, l_pos, l_col;
   std::vector<int> u_lvl_ptr, u_rows, u_ptr, u_pos, u_col;
-  std::vector<char> exempt;  // columns exempt from the pivot threshold test
+  std::vector<char> exempt;    // columns held to a scaled pivot threshold (kExemptSlack)
+  std::vector<double> pscale;  // that scale: kExemptSlack * analysis pivot ratio / kRuntimePivotTol
   std::vector<int> l_long, u_long;  // per solve level: long rows at the end of the level
   Schedule fsched, lsched;
   std::vector<int> upd_off, upd_pos;  // scatter positions of each U entry's update
@@ -400,7 +407,9 @@ struct LUHost {
   std::vector<int> umeta;
   // Factor groups whose update metadata is staged in shared memory too (after
   // the values): per schedule position t, 4 ints {value offset in the group
-  // buffer, column entries, diagonal offset, pivot-test flag}; fm_eptr[t] ..
+  // buffer, column entries, diagonal offset, pivot test (0 none: no U row
+  // right of the diagonal, 1 the threshold, 2 the exempt column's scaled
+  // threshold)}; fm_eptr[t] ..
   // fm_eptr[t+1] its U entries in fm_ent, 4 ints each {L(k+1.., k) source:
   // buffer index, or -(global position)-1; entry count; offset of its targets
   // in the group's fm_tgt segment (from fm_tptr[g]); position of U(k, j) in

@@ -200,8 +200,9 @@ __global__ void __launch_bounds__(1024) k_top_rl(LUDev L, CircState *cs, int mas
     for (int p = pd + threadIdx.x; p < p1; p += blockDim.x) amax = fmax(amax, fabs((double)lu[p]));
     amax = team_max<true>(amax, sm);
     const double d = (double)lu[pd];
-    const bool urow = L.u_ptr[k + 1] > L.u_ptr[k] && !L.exempt[k];
-    const bool bad = (urow && !(fabs(d) >= pivot_tol * amax)) || !(fabs(d) > 0.0) || isinf(d);
+    const bool urow = L.u_ptr[k + 1] > L.u_ptr[k];
+    const double tol = L.exempt[k] ? pivot_tol * L.pscale[k] : pivot_tol;
+    const bool bad = (urow && !(fabs(d) >= tol * amax)) || !(fabs(d) > 0.0) || isinf(d);
     if (bad) {
       if (threadIdx.x == 0) {
         atomicCAS(L.breakdown, 0, k + 1);
@@ -257,8 +258,9 @@ __global__ void __launch_bounds__(256) k_toplv_pivot(LUDev L, int lv, CircState 
   for (int p = pd + lane; p < p1; p += 32) amax = fmax(amax, fabs((double)lu[p]));
   for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
   const double d = (double)lu[pd];
-  const bool urow = L.u_ptr[k + 1] > L.u_ptr[k] && !L.exempt[k];
-  const bool bad = (urow && !(fabs(d) >= pivot_tol * amax)) || !(fabs(d) > 0.0) || isinf(d);
+  const bool urow = L.u_ptr[k + 1] > L.u_ptr[k];
+  const double tol = L.exempt[k] ? pivot_tol * L.pscale[k] : pivot_tol;
+  const bool bad = (urow && !(fabs(d) >= tol * amax)) || !(fabs(d) > 0.0) || isinf(d);
   if (bad) {
     if (lane == 0) {
       atomicCAS(L.breakdown, 0, k + 1);
@@ -340,7 +342,8 @@ __device__ void factor_column_m(const LUDev &L, int j, int r, CircState *cs, int
     ak = team_max_key<false>(ak, sm);
     lost = team_any<false>(lost);
   }
-  if (!pivot_ok_u(L, j, cs, masked, pivot_tol, (double)cj[col.z], key_value<T>(ak), lost, lane == 0, col.w != 0))
+  const double tol = col.w == 2 ? pivot_tol * L.pscale[j] : pivot_tol;
+  if (!pivot_ok_u(L, j, cs, masked, tol, (double)cj[col.z], key_value<T>(ak), lost, lane == 0, col.w != 0))
     return;
   const T inv = (T)1 / cj[col.z];
   for (int p = col.z + 1 + lane; p < col.y; p += TEAM) cj[p] *= inv;

@@ -130,9 +130,11 @@ __device__ __forceinline__ bool pivot_ok(const LUDev &L, int j, CircState *cs, i
                                          double d, double amax, bool lost, bool leader) {
   // The threshold only matters when row j of U has entries right of the
   // diagonal: otherwise the multipliers never reach the Schur complement
-  // (e.g. the branch row of a grounded voltage source).
-  const bool urow = L.u_ptr[j + 1] > L.u_ptr[j] && !L.exempt[j];
-  return pivot_ok_u(L, j, cs, masked, pivot_tol, d, amax, lost, leader, urow);
+  // (e.g. the branch row of a grounded voltage source).  An exempt column's
+  // threshold is scaled down (kExemptSlack).
+  const bool urow = L.u_ptr[j + 1] > L.u_ptr[j];
+  const double tol = L.exempt[j] ? pivot_tol * L.pscale[j] : pivot_tol;
+  return pivot_ok_u(L, j, cs, masked, tol, d, amax, lost, leader, urow);
 }
 
 template <bool BLOCK, typename T>

@@ -685,8 +685,13 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
   // Host trial factorization with the analysis values: a column whose
   // frozen pivot fails the threshold test even right after re-pivoting is
   // exempt from that test on the device (re-pivoting cannot improve it; a
-  // typical case is a structurally present but zero U row).
+  // typical case is a structurally present but zero U row, or a block tied
+  // to ground only by gmin-sized conductances).  The exemption is bounded:
+  // the column is still held to kExemptSlack times the pivot ratio it has
+  // here, so that a pivot that collapses on later values (the frozen order
+  // gone bad) still triggers re-pivoting.
   out.exempt.assign(n, 0);
+  out.pscale.assign(n, 1.0);
   {
     std::vector<double> lu(nnz);
     for (int p = 0; p < n; ++p) {
@@ -703,7 +708,10 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
       const double d = lu[pd];
       double amax = 0.0;
       for (int t = pd; t < p1; ++t) amax = std::max(amax, std::fabs(lu[t]));
-      if (!(std::fabs(d) >= kRuntimePivotTol * amax)) out.exempt[p] = 1;
+      if (!(std::fabs(d) >= kRuntimePivotTol * amax)) {
+        out.exempt[p] = 1;
+        out.pscale[p] = amax > 0.0 ? kExemptSlack * (std::fabs(d) / amax) / kRuntimePivotTol : 0.0;
+      }
       if (d != 0.0)
         for (int t = pd + 1; t < p1; ++t) lu[t] /= d;
     }
@@ -930,7 +938,7 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
         c[0] = out.grp_soff[j];
         c[1] = out.cp[j + 1] - out.cp[j];
         c[2] = out.diag[j] - out.cp[j];
-        c[3] = (out.u_ptr[j + 1] > out.u_ptr[j] && !out.exempt[j]) ? 1 : 0;
+        c[3] = (out.u_ptr[j + 1] > out.u_ptr[j]) ? (out.exempt[j] ? 2 : 1) : 0;
         for (int p = out.cp[j]; p < out.diag[j]; ++p) {
           const int k = out.ri[p];
           const int nl = out.cp[k + 1] - out.diag[k] - 1;
