@@ -390,10 +390,148 @@ void parallel_for(size_t count, long long weight, const std::function<void(size_
   for (auto &th : pool) th.join();
 }
 
+// Pivot rows of a left-looking LU with threshold partial pivoting
+// (Gilbert-Peierls: the numeric factorization KLU runs, with its diagonal
+// preference) in the column order col_order, for the columns in scope (whole
+// connected components).  preferred[j] is kept while it is within kDiagPref
+// of column j's largest candidate.  False when a column has no candidate row.
+bool partial_pivot_rows(int n, const Csc &A, const std::vector<double> &vals, const std::vector<int> &col_order,
+                        const std::vector<char> &scope, const std::vector<int> &preferred, std::vector<int> &rows) {
+  std::vector<int> pinv(n, -1), prow, lp(1, 0), li;
+  std::vector<double> lx, x(n, 0.0);
+  std::vector<int> rmark(n, -1), smark, touched, topo, stk, spos;
+  rows.assign(n, -1);
+  int s = 0;
+  for (int j : col_order) {
+    if (!scope[j]) continue;
+    touched.clear();
+    topo.clear();
+    smark.resize(s + 1, -1);
+    auto touch = [&](int r) { if (rmark[r] != s) { rmark[r] = s; touched.push_back(r); } };
+    // reach of A(:, j) through the columns of L, in topological order
+    for (int q = A.cp[j]; q < A.cp[j + 1]; ++q) {
+      const int i = A.ri[q];
+      touch(i);
+      x[i] = vals[A.src[q]];
+      const int k0 = pinv[i];
+      if (k0 < 0 || smark[k0] == s) continue;
+      smark[k0] = s;
+      stk.assign(1, k0);
+      spos.assign(1, lp[k0]);
+      while (!stk.empty()) {
+        const int k = stk.back();
+        int &t = spos.back();
+        bool pushed = false;
+        for (; t < lp[k + 1]; ++t) {
+          const int k2 = pinv[li[t]];
+          if (k2 >= 0 && smark[k2] != s) {
+            smark[k2] = s;
+            ++t;
+            stk.push_back(k2);
+            spos.push_back(lp[k2]);
+            pushed = true;
+            break;
+          }
+        }
+        if (!pushed) { topo.push_back(k); stk.pop_back(); spos.pop_back(); }
+      }
+    }
+    for (auto it = topo.rbegin(); it != topo.rend(); ++it) {
+      const int k = *it;
+      const double xk = x[prow[k]];
+      if (xk == 0.0) continue;
+      for (int t = lp[k]; t < lp[k + 1]; ++t) {
+        touch(li[t]);
+        x[li[t]] -= lx[t] * xk;
+      }
+    }
+    int best = -1;
+    double amax = -1.0;
+    for (int r : touched)
+      if (pinv[r] < 0 && std::fabs(x[r]) > amax) { amax = std::fabs(x[r]); best = r; }
+    if (best < 0) return false;
+    const int pr = preferred[j];
+    if (pr >= 0 && pinv[pr] < 0 && rmark[pr] == s && std::fabs(x[pr]) >= kDiagPref * amax) best = pr;
+    const double piv = x[best];
+    for (int r : touched)
+      if (pinv[r] < 0 && r != best && x[r] != 0.0) { li.push_back(r); lx.push_back(piv != 0.0 ? x[r] / piv : 0.0); }
+    lp.push_back((int)li.size());
+    pinv[best] = s;
+    prow.push_back(best);
+    rows[j] = best;
+    for (int r : touched) x[r] = 0.0;
+    ++s;
+  }
+  return true;
+}
+
+// The smallest pivot ratio among the columns the trial factorization exempted
+// (1 when none): the exemption scale stores it.
+double worst_exempt_ratio(const LUHost &H) {
+  double w = 1.0;
+  for (int p = 0; p < H.n; ++p)
+    if (H.exempt[p]) w = std::min(w, H.pscale[p] * kRuntimePivotTol / kExemptSlack);
+  return w;
+}
+
 }  // namespace
 
+static int analyze_once(int n, const std::vector<int> &rp, const std::vector<int> &ci,
+                        const std::vector<double> &vals, LUHost &out, std::string &err, int force_ordering,
+                        const std::vector<int> *keep_rows);
+
+// The analysis, repaired where its static pivots fail.  The row matching
+// and the symmetric ordering pivot on the (matched) diagonal; elimination
+// can cancel such a diagonal (a MOSFET's drain' node: the series conductance
+// on the diagonal, gds ~ 0 left after the drain' is eliminated, while the
+// next stage's gm sits below it).  The reference's KLU pivots during the
+// numeric factorization instead.  So when the trial factorization of the
+// analysis finds columns below the pivot threshold, the connected
+// components holding them are pivoted once by threshold partial pivoting in
+// the analysed order, and analysed again with those rows kept; the repair
+// is taken when its worst pivot is better.
 int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &ci,
                     const std::vector<double> &vals, LUHost &out, std::string &err, int force_ordering,
+                    const std::vector<int> *keep_rows) {
+  int rc = analyze_once(n, rp, ci, vals, out, err, force_ordering, keep_rows);
+  if (rc != XG_OK) return rc;
+  for (int round = 0; round < 2; ++round) {
+    const double worst = worst_exempt_ratio(out);
+    if (worst >= 1.0) return XG_OK;
+    // connected components of the pattern
+    std::vector<int> comp(n);
+    std::iota(comp.begin(), comp.end(), 0);
+    std::function<int(int)> root = [&](int v) {
+      while (comp[v] != v) { comp[v] = comp[comp[v]]; v = comp[v]; }
+      return v;
+    };
+    for (int i = 0; i < n; ++i)
+      for (int e = rp[i]; e < rp[i + 1]; ++e) {
+        const int a = root(i), b = root(ci[e]);
+        if (a != b) comp[a] = b;
+      }
+    std::vector<char> bad_comp(n, 0), scope(n, 0);
+    for (int p = 0; p < n; ++p)
+      if (out.exempt[p]) bad_comp[root(out.col_of_step[p])] = 1;
+    std::vector<int> cur_row(n), keep2(n);
+    for (int p = 0; p < n; ++p) cur_row[out.col_of_step[p]] = out.row_of_step[p];
+    for (int j = 0; j < n; ++j)
+      scope[j] = bad_comp[root(j)] && !(keep_rows && (*keep_rows)[j] >= 0);
+    Csc A = to_csc(n, rp, ci);
+    std::vector<int> gp_rows;
+    if (!partial_pivot_rows(n, A, vals, out.col_of_step, scope, cur_row, gp_rows)) return XG_OK;
+    for (int j = 0; j < n; ++j) keep2[j] = scope[j] ? gp_rows[j] : cur_row[j];
+    LUHost rep;
+    std::string err2;
+    if (analyze_once(n, rp, ci, vals, rep, err2, force_ordering, &keep2) != XG_OK) return XG_OK;
+    if (!(worst_exempt_ratio(rep) > worst)) return XG_OK;
+    out = std::move(rep);
+  }
+  return XG_OK;
+}
+
+static int analyze_once(int n, const std::vector<int> &rp, const std::vector<int> &ci,
+                        const std::vector<double> &vals, LUHost &out, std::string &err, int force_ordering,
                     const std::vector<int> *keep_rows) {
   out = LUHost();
   out.n = n;
