@@ -70,6 +70,11 @@ enum {
    * MJSW, FCS; the instance perimeter PJ */
   XG_DIODE_JSW, XG_DIODE_NS, XG_DIODE_NSGIVEN, XG_DIODE_CJSW, XG_DIODE_VJSW, XG_DIODE_MJSW,
   XG_DIODE_FCS, XG_DIODE_PJ,
+  /* temperature: TNOM (model) and TEMP (the device's own: instance TEMP, else
+   * the circuit temperature plus DTEMP), both in kelvin; the coefficients
+   * TIKF, TBV1/TBV2, TRS1/TRS2 of IKF, BV and RS (N_DEV_Diode.C:1430-1545) */
+  XG_DIODE_TNOM, XG_DIODE_TEMP, XG_DIODE_TIKF, XG_DIODE_TBV1, XG_DIODE_TBV2, XG_DIODE_TRS1,
+  XG_DIODE_TRS2,
   XG_DIODE_NPARAM
 };
 
@@ -83,7 +88,11 @@ enum {
   XG_MOS1_CGSO, XG_MOS1_CGDO, XG_MOS1_CGBO, XG_MOS1_CJ, XG_MOS1_MJ, XG_MOS1_CJSW,
   XG_MOS1_MJSW, XG_MOS1_JS, XG_MOS1_TOX, XG_MOS1_LD, XG_MOS1_FC, XG_MOS1_W, XG_MOS1_L,
   XG_MOS1_AD, XG_MOS1_AS, XG_MOS1_PD, XG_MOS1_PS, XG_MOS1_M, XG_MOS1_RSH, XG_MOS1_NRD,
-  XG_MOS1_NRS, XG_MOS1_NPARAM
+  XG_MOS1_NRS,
+  /* TNOM (model) and TEMP (the device's own: instance TEMP, else the circuit
+   * temperature plus DTEMP), kelvin (Instance::updateTemperature,
+   * N_DEV_MOSFET1.C:3487-3640) */
+  XG_MOS1_TNOM, XG_MOS1_TEMP, XG_MOS1_NPARAM
 };
 
 /* ---- BSIM4 (Xyce level 54, BSIM 4.8.2) parameter row --------------------

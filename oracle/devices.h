@@ -22,13 +22,14 @@ static const double kGmin = 1.0e-12;  // N_DEV_DeviceOptions.C default gmin
 enum DiodeParam {
   DP_IS, DP_N, DP_RS, DP_CJO, DP_VJ, DP_M, DP_FC, DP_TT, DP_BV, DP_IBV, DP_NBV,
   DP_IKF, DP_ISR, DP_NR, DP_EG, DP_XTI, DP_AREA, DP_BVGIVEN,
-  DP_JSW, DP_NS, DP_NSGIVEN, DP_CJSW, DP_VJSW, DP_MJSW, DP_FCS, DP_PJ, DP_COUNT
+  DP_JSW, DP_NS, DP_NSGIVEN, DP_CJSW, DP_VJSW, DP_MJSW, DP_FCS, DP_PJ,
+  DP_TNOM, DP_TEMP, DP_TIKF, DP_TBV1, DP_TBV2, DP_TRS1, DP_TRS2, DP_COUNT
 };
 enum Mos1Param {
   MP_TYPE, MP_VTO, MP_KP, MP_GAMMA, MP_PHI, MP_LAMBDA, MP_RD, MP_RS, MP_CBD, MP_CBS,
   MP_IS, MP_PB, MP_CGSO, MP_CGDO, MP_CGBO, MP_CJ, MP_MJ, MP_CJSW, MP_MJSW, MP_JS,
   MP_TOX, MP_LD, MP_FC, MP_W, MP_L, MP_AD, MP_AS, MP_PD, MP_PS, MP_M, MP_RSH, MP_NRD, MP_NRS,
-  MP_COUNT
+  MP_TNOM, MP_TEMP, MP_COUNT
 };
 
 // DeviceSupport::pnjlim, N_DEV_DeviceSupport.C:188-235.
@@ -136,7 +137,7 @@ struct DiodeT {
 
 inline DiodeT diode_temperature(const double *p) {
   DiodeT t{};
-  double Temp = kRefTemp, TNOM = kRefTemp;
+  double Temp = p[DP_TEMP], TNOM = p[DP_TNOM];
   double M = std::min(p[DP_M], 0.9);
   double FC = std::min(p[DP_FC], 0.95);
   double EG = std::max(p[DP_EG], 0.1);
@@ -164,14 +165,15 @@ inline DiodeT diode_temperature(const double *p) {
   t.tVcrit = vte * std::log(vte / (std::sqrt(2.0) * (tSatCur == 0.0 ? 1e-14 : tSatCur)));
   double NR = p[DP_NR];
   double tSatCurR = p[DP_ISR] * std::exp((Temp / TNOM - 1.0) * EG / (NR * vt) + XTI / NR * std::log(Temp / TNOM));
-  t.tIKF = p[DP_IKF];
-  double tRS = p[DP_RS];
+  // N_DEV_Diode.C:1520-1529
+  t.tIKF = p[DP_IKF] * (1 + p[DP_TIKF] * (Temp - TNOM));
+  double tRS = p[DP_RS] * (1 + (Temp - TNOM) * (p[DP_TRS1] + p[DP_TRS2] * (Temp - TNOM)));
   double tCOND = (tRS != 0.0) ? 1.0 / tRS : 0.0;
   double NBV = p[DP_NBV];
   t.bvGiven = p[DP_BVGIVEN] != 0.0;
   t.tBrkdwnV = 0.0;
   if (t.bvGiven) {
-    double tempBV = p[DP_BV];
+    double tempBV = p[DP_BV] * (1 + (Temp - TNOM) * (p[DP_TBV1] + p[DP_TBV2] * (Temp - TNOM)));
     double cbv = p[DP_IBV], xbv;
     if (cbv < tSatCur * tempBV / vt) {
       xbv = tempBV;
@@ -357,7 +359,7 @@ inline double mos1_series_conductance(double r, double rsh, double squares) {
 
 inline Mos1T mos1_temperature(const double *p) {
   Mos1T t{};
-  double temp = kRefTemp, tnom = kRefTemp;
+  double temp = p[MP_TEMP], tnom = p[MP_TNOM];
   t.dtype = p[MP_TYPE];
   double fact1 = tnom / kRefTemp;
   double vtnom = tnom * kKoverQ;

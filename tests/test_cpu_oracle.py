@@ -90,7 +90,11 @@ def _fd_check(oracle_mod, nl, rng, dcop, shift=0.0):
                                    lambda: N.ring_oscillator(5, series=True),
                                    lambda: N.ring_oscillator(5, caps=True, series=True),
                                    lambda: N.bsim4_inverter_chain(2),
-                                   lambda: N.bsim4_logic_dag(60, 4, seed=2, tstop=0.3e-9)])
+                                   lambda: N.bsim4_logic_dag(60, 4, seed=2, tstop=0.3e-9),
+                                   lambda: N.at_temperature(N.ring_oscillator(5, caps=True), 100.0, 40.0),
+                                   lambda: N.at_temperature(N.diode_ladder(9, seed=3, sidewall=True), -20.0, 50.0,
+                                                            IKF=5e-3, TIKF=0.01, TBV1=1e-3, TBV2=1e-6,
+                                                            TRS1=2e-3, TRS2=1e-5)])
 def test_finite_difference_jacobian(oracle_mod, maker):
     rng = np.random.default_rng(7)
     _fd_check(oracle_mod, maker(), rng, dcop=False)
@@ -201,6 +205,63 @@ def test_diode_sidewall_iv_point(oracle_mod, ns):
         i_d = 1e-14 * np.expm1(vd / vt) + isw * np.expm1(vd / (ns * vt))
     assert abs((1.0 - vd) / 1e3 - (i_d + 1e-12 * vd)) < 1e-6
     assert 0.45 < vd < 0.75
+
+
+KB, QE, TREF = 1.3806226e-23, 1.6021918e-19, 300.15
+
+
+def test_diode_temperature_dc_point(oracle_mod):
+    """Diode at 75 C with TNOM 27 C (updateTemperature, N_DEV_Diode.C:1430-1470):
+    IS(T) = IS exp((T/TNOM - 1) EG/(N vt) + XTI/N ln(T/TNOM)), vt = kT/q;
+    RS(T) = RS (1 + dT (TRS1 + TRS2 dT))."""
+    nl = N.Netlist(label="diode_75C")
+    a, k = nl.node("a"), nl.node("k")
+    nl.V(a, -1, N.WAVE_DC, [1.0])
+    nl.R(a, k, 1e3)
+    nl.D(k, -1, IS=1e-14, N=1.2, EG=1.11, XTI=3.0, RS=20.0, TRS1=5e-3, TRS2=1e-5,
+         TEMP=75.0 + N.CTOK, TNOM=27.0 + N.CTOK)
+    st, x, it = oracle_mod.Oracle(nl).dcop()
+    T, TN = 75.0 + N.CTOK, 27.0 + N.CTOK
+    vt = KB * T / QE
+    is_t = 1e-14 * np.exp((T / TN - 1.0) * 1.11 / (1.2 * vt) + 3.0 / 1.2 * np.log(T / TN))
+    rs_t = 20.0 * (1 + (T - TN) * (5e-3 + 1e-5 * (T - TN)))
+    pri = nl.diode[0][2]
+    vd = x[pri]
+    i_r = (1.0 - x[k]) / 1e3
+    assert abs(i_r - (x[k] - vd) / rs_t) < 1e-9
+    assert abs(i_r - (is_t * np.expm1(vd / (1.2 * vt)) + 1e-12 * vd)) < 1e-6
+    assert 0.3 < vd < 0.7
+
+
+def test_mosfet1_temperature_saturation_current(oracle_mod):
+    """NMOS (GAMMA = 0, LAMBDA = 0) in saturation at 100 C with TNOM 27 C
+    (Instance::updateTemperature, N_DEV_MOSFET1.C:3525-3560): beta scales by
+    (T/TNOM)^-1.5 and VTO moves by (egfet(TNOM) - egfet(T))/2 + (tPhi - PHI)/2.
+    The reverse-biased drain junction adds (IS(T)/vt + gmin) * Vdb, with
+    IS(T) = IS exp(-egfet(T)/vt + egfet(TNOM)/vtnom) (the linear reverse
+    junction of the reference's MOSFET-1)."""
+    T, TN, vto, phi, kp = 100.0 + N.CTOK, 27.0 + N.CTOK, 0.5, 0.6, 120e-6
+    nl = N.Netlist(label="nmos_100C")
+    vdd, gate = nl.node("vdd"), nl.node("g")
+    br = nl.V(vdd, -1, N.WAVE_DC, [1.8])
+    nl.V(gate, -1, N.WAVE_DC, [1.2])
+    nl.M1(vdd, gate, -1, -1, TYPE=1.0, VTO=vto, KP=kp, PHI=phi, W=2e-6, L=0.18e-6, TEMP=T, TNOM=TN)
+    st, x, it = oracle_mod.Oracle(nl).dcop()
+    egfet = lambda t: 1.16 - 7.02e-4 * t * t / (t + 1108)
+
+    def pbfact(t):
+        vt = KB * t / QE
+        arg = -egfet(t) / (2 * KB * t) + 1.1150877 / (KB * (TREF + TREF))
+        return -2 * vt * (1.5 * np.log(t / TREF) + QE * arg)
+    phio = (phi - pbfact(TN)) / (TN / TREF)
+    tphi = T / TREF * phio + pbfact(T)
+    tvto = vto + 0.5 * (egfet(TN) - egfet(T)) + 0.5 * (tphi - phi)
+    beta = kp / (T / TN) ** 1.5 * 2e-6 / 0.18e-6
+    vt, vtnom = KB * T / QE, KB * TN / QE
+    is_t = 1e-14 * np.exp(-egfet(T) / vt + egfet(TN) / vtnom)
+    i_d = beta / 2 * (1.2 - tvto) ** 2 + (is_t / vt + 1e-12) * 1.8
+    assert abs(abs(x[br]) - i_d) < 1e-9 * i_d
+    assert abs(tvto - vto) > 0.05  # the shift is not negligible at 100 C
 
 
 def test_mosfet1_series_resistance_dc_point(oracle_mod):

@@ -286,6 +286,37 @@ V1 in 0 PULSE(0 1.8 0 10p 10p 100p 200p)
     assert N.mos1_series(r2) == (1.0 / 100.0, 1.0 / 75.0)
 
 
+def test_temperature_statements():
+    d = S.parse("""temperatures
+.TEMP 85
+.OPTIONS DEVICE TNOM=25
+.MODEL d1 D (IS=1e-14)
+.MODEL d2 D (IS=1e-14 TNOM=50 TRS1=1m)
+.MODEL n1 NMOS (LEVEL=1 VTO=0.5 KP=100u)
+V1 a 0 1
+D1 a 0 d1
+D2 a 0 d2 DTEMP=10
+D3 a 0 d1 TEMP=-40
+M1 a a 0 0 n1 W=1u L=1u
+.PRINT TRAN V(a) TEMP
+.TRAN 1n 10n
+.END
+""")
+    nl = d.netlist
+    fd, fm = N.DIODE_FIELDS.index, N.MOS1_FIELDS.index
+    k = lambda c: c + N.CTOK
+    (r1, r2, r3) = (nl.diode[i][3] for i in range(3))
+    assert r1[fd("TEMP")] == k(85.0) and r1[fd("TNOM")] == k(25.0)
+    assert r2[fd("TEMP")] == k(95.0) and r2[fd("TNOM")] == k(50.0) and r2[fd("TRS1")] == 1e-3
+    assert r3[fd("TEMP")] == k(-40.0)
+    m = nl.mos1[0][4]
+    assert m[fm("TEMP")] == k(85.0) and m[fm("TNOM")] == k(25.0)
+    assert d.temp_c == 85.0
+    with pytest.raises(ValueError):  # the BSIM4 restatement runs at 27 C only
+        S.parse(".title\n.TEMP 50\n.MODEL n4 NMOS (LEVEL=54)\nV1 a 0 1\nM1 a a 0 0 n4 L=45n W=90n\n"
+                ".TRAN 1p 10p\n.END\n")
+
+
 def test_bsim4_model_card_and_instance():
     d = S.parse("""bsim4 inverter
 .MODEL n1 NMOS (LEVEL=54 VERSION=4.8.2 TOXE=1.8n VTH0=0.4)

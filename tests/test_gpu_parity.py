@@ -106,6 +106,7 @@ def _loader_case(xg, oracle_mod, torch, nl, seed, newton_iter, dcop, init_jct, c
     (lambda: N.ring_oscillator(11, caps=True), True),
     (lambda: N.ring_oscillator(11, series=True), False),
     (lambda: N.ring_oscillator(11, caps=True, series=True), True),
+    (lambda: N.at_temperature(N.ring_oscillator(11, caps=True, series=True), 100.0, 40.0), True),
     (lambda: N.monte_carlo_rings(3, 11, 21, seed=2), False),
     (lambda: N.power_grid(6, 5, seed=1), False),
     (lambda: N.bsim4_inverter_chain(3), True),
@@ -118,14 +119,19 @@ def test_device_stamps_match_oracle(xg, oracle_mod, torch_cuda, maker, caps, mod
     _loader_case(xg, oracle_mod, torch_cuda, maker(), 11, it, dcop, init, caps)
 
 
+@pytest.mark.parametrize("maker", [
+    lambda: N.diode_ladder(30, seed=3, sidewall=True),
+    lambda: N.at_temperature(N.diode_ladder(30, seed=3, sidewall=True), -20.0, 50.0, IKF=5e-3, TIKF=0.01,
+                             TBV1=1e-3, TBV2=1e-6, TRS1=2e-3, TRS2=1e-5)], ids=["27C", "-20C_tnom50C"])
 @pytest.mark.parametrize("mode", ["tran0", "tran2", "dcop_init"])
-def test_diode_sidewall_stamps_match_oracle(xg, oracle_mod, torch_cuda, mode):
+def test_diode_sidewall_stamps_match_oracle(xg, oracle_mod, torch_cuda, maker, mode):
     """Sidewall currents (own NS, merged) and charges; junction voltages down
-    to -5.5 V reach the breakdown of the BV = 4 V card."""
+    to -5.5 V reach the breakdown of the BV = 4 V card; at 27 C, and at
+    -20 C against TNOM 50 C with every temperature coefficient of IKF, BV
+    and RS set."""
     it, dcop, init = {"tran0": (0, False, False), "tran2": (2, False, False),
                       "dcop_init": (0, True, True)}[mode]
-    _loader_case(xg, oracle_mod, torch_cuda, N.diode_ladder(30, seed=3, sidewall=True), 13, it, dcop,
-                 init, False, xlo=-5.5)
+    _loader_case(xg, oracle_mod, torch_cuda, maker(), 13, it, dcop, init, False, xlo=-5.5)
 
 
 def test_lu_matches_ksparse_golden(xg, torch_cuda):

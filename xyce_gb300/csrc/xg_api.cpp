@@ -307,6 +307,9 @@ int xg_add_diodes(xg_ctx *ctx, int n, const int *pos, const int *neg, const int 
     const double *p = params + (size_t)k * XG_DIODE_NPARAM;
     if ((p[XG_DIODE_RS] == 0.0) != (pri[k] == pos[k]))
       return fail(ctx, XG_ERR_ARG, "diode internal node must equal pos exactly when RS = 0");
+    if (!(p[XG_DIODE_TEMP] > 0.0) || !(p[XG_DIODE_TNOM] > 0.0) || !std::isfinite(p[XG_DIODE_TEMP]) ||
+        !std::isfinite(p[XG_DIODE_TNOM]))
+      return fail(ctx, XG_ERR_ARG, "diode TEMP and TNOM are kelvin: positive and finite");
   }
   ctx->d_p.insert(ctx->d_p.end(), pos, pos + n);
   ctx->d_n.insert(ctx->d_n.end(), neg, neg + n);
@@ -333,6 +336,9 @@ static int add_mosfet1(xg_ctx *ctx, int n, const int *dd, const int *g, const in
       return fail(ctx, XG_ERR_ARG, "MOSFET node out of range");
     const double *p = params + (size_t)k * XG_MOS1_NPARAM;
     if (p[XG_MOS1_TYPE] != 1.0 && p[XG_MOS1_TYPE] != -1.0) return fail(ctx, XG_ERR_ARG, "MOSFET TYPE must be +1 or -1");
+    if (!(p[XG_MOS1_TEMP] > 0.0) || !(p[XG_MOS1_TNOM] > 0.0) || !std::isfinite(p[XG_MOS1_TEMP]) ||
+        !std::isfinite(p[XG_MOS1_TNOM]))
+      return fail(ctx, XG_ERR_ARG, "MOSFET TEMP and TNOM are kelvin: positive and finite");
     gd[k] = mos1_series_conductance(p[XG_MOS1_RD], p[XG_MOS1_RSH], p[XG_MOS1_NRD]);
     gs[k] = mos1_series_conductance(p[XG_MOS1_RS], p[XG_MOS1_RSH], p[XG_MOS1_NRS]);
     if (!std::isfinite(gd[k]) || !std::isfinite(gs[k]) || !std::isfinite(gd[k] * p[XG_MOS1_M]) ||

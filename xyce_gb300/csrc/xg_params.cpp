@@ -1,5 +1,6 @@
 // xg_params.cpp — host processing of device parameters into the device-side
-// model tables (temperature = TNOM = 27 C, the reference's default).
+// model tables, at each device's temperature TEMP with its model's TNOM
+// (kelvin, from the parameter row).
 //
 //   Diode: Model::processParams + updateTemperature
 //          src/DeviceModelPKG/OpenModels/N_DEV_Diode.C:1612-1639, 2040-2237;
@@ -27,7 +28,7 @@ double pb_factor(double T) {
 
 DiodeModel diode_model(const double *p) {
   DiodeModel m{};
-  const double T = REFTEMP, TN = REFTEMP;
+  const double T = p[XG_DIODE_TEMP], TN = p[XG_DIODE_TNOM];
   const double M = std::min(p[XG_DIODE_M], 0.9);
   const double FC = std::min(p[XG_DIODE_FC], 0.95);
   const double EG = std::max(p[XG_DIODE_EG], 0.1);
@@ -47,12 +48,14 @@ DiodeModel diode_model(const double *p) {
   const double NR = p[XG_DIODE_NR], NBV = p[XG_DIODE_NBV];
   const double tSatCurR = p[XG_DIODE_ISR] * std::exp((T / TN - 1.0) * EG / (NR * vt) + XTI / NR * std::log(T / TN));
   const double area = p[XG_DIODE_AREA];
-  const double RS = p[XG_DIODE_RS];
+  // N_DEV_Diode.C:1520-1529: IKF, RS and BV at the device temperature
+  const double RS = p[XG_DIODE_RS] * (1 + (T - TN) * (p[XG_DIODE_TRS1] + p[XG_DIODE_TRS2] * (T - TN)));
   m.tVcrit = vte * std::log(vte / (std::sqrt(2.0) * (tSatCur == 0.0 ? 1e-14 : tSatCur)));
   m.bvGiven = p[XG_DIODE_BVGIVEN] != 0.0;
   m.tBrkdwnV = 0.0;
   if (m.bvGiven) {
-    const double BV = p[XG_DIODE_BV], cbv = p[XG_DIODE_IBV];
+    const double BV = p[XG_DIODE_BV] * (1 + (T - TN) * (p[XG_DIODE_TBV1] + p[XG_DIODE_TBV2] * (T - TN)));
+    const double cbv = p[XG_DIODE_IBV];
     double xbv;
     if (cbv < tSatCur * BV / vt) {
       xbv = BV;
@@ -95,7 +98,7 @@ DiodeModel diode_model(const double *p) {
   m.VteR = NR * vt;
   m.VteBRK = NBV * vt;
   m.Gspr = (RS != 0.0 ? 1.0 / RS : 0.0) * area;
-  m.tIKF = p[XG_DIODE_IKF];
+  m.tIKF = p[XG_DIODE_IKF] * (1 + p[XG_DIODE_TIKF] * (T - TN));
   m.tJctPot = tJctPot;
   m.tJctCap = tJctCap * area;  // Czero = tJctCap * Area
   m.tDepCap = FC * tJctPot;
@@ -110,7 +113,7 @@ DiodeModel diode_model(const double *p) {
 Mos1Instance mos1_instance(const double *p) {
   Mos1Instance r{};
   Mos1Model &m = r.model;
-  const double temp = REFTEMP, tnom = REFTEMP;
+  const double temp = p[XG_MOS1_TEMP], tnom = p[XG_MOS1_TNOM];
   const double dtype = p[XG_MOS1_TYPE];
   const double fact1 = tnom / REFTEMP, fact2 = temp / REFTEMP;
   const double vtnom = tnom * KOVERQ, vt = temp * KOVERQ;

@@ -27,21 +27,46 @@ WAVE_DC, WAVE_SIN, WAVE_PULSE, WAVE_PWL = 0, 1, 2, 3
 # Diode parameter row (N_DEV_Diode.C addPar defaults).
 DIODE_FIELDS = ["IS", "N", "RS", "CJO", "VJ", "M", "FC", "TT", "BV", "IBV", "NBV",
                 "IKF", "ISR", "NR", "EG", "XTI", "AREA", "BVGIVEN",
-                "JSW", "NS", "NSGIVEN", "CJSW", "VJSW", "MJSW", "FCS", "PJ"]
+                "JSW", "NS", "NSGIVEN", "CJSW", "VJSW", "MJSW", "FCS", "PJ",
+                "TNOM", "TEMP", "TIKF", "TBV1", "TBV2", "TRS1", "TRS2"]
 DIODE_DEFAULTS = dict(IS=1e-14, N=1.0, RS=0.0, CJO=0.0, VJ=1.0, M=0.5, FC=0.5, TT=0.0,
                       BV=1e99, IBV=1e-3, NBV=None, IKF=0.0, ISR=0.0, NR=2.0, EG=1.11,
                       XTI=3.0, AREA=1.0, BVGIVEN=0.0,
-                      JSW=0.0, NS=1.0, NSGIVEN=0.0, CJSW=0.0, VJSW=1.0, MJSW=0.33, FCS=0.5, PJ=0.0)
+                      JSW=0.0, NS=1.0, NSGIVEN=0.0, CJSW=0.0, VJSW=1.0, MJSW=0.33, FCS=0.5, PJ=0.0,
+                      TNOM=300.15, TEMP=300.15, TIKF=0.0, TBV1=0.0, TBV2=0.0, TRS1=0.0, TRS2=0.0)
+# TNOM and TEMP in the rows are kelvin (the netlist's degrees Celsius + 273.15,
+# as the reference's parameter layer converts them); 300.15 K = 27 C, the
+# reference's default for both.
+CTOK = 273.15
 
 # MOSFET level-1 parameter row (model + instance; N_DEV_MOSFET1.C addPar defaults).
 MOS1_FIELDS = ["TYPE", "VTO", "KP", "GAMMA", "PHI", "LAMBDA", "RD", "RS", "CBD", "CBS",
                "IS", "PB", "CGSO", "CGDO", "CGBO", "CJ", "MJ", "CJSW", "MJSW", "JS",
-               "TOX", "LD", "FC", "W", "L", "AD", "AS", "PD", "PS", "M", "RSH", "NRD", "NRS"]
+               "TOX", "LD", "FC", "W", "L", "AD", "AS", "PD", "PS", "M", "RSH", "NRD", "NRS",
+               "TNOM", "TEMP"]
 MOS1_DEFAULTS = dict(TYPE=1.0, VTO=0.0, KP=2e-5, GAMMA=0.0, PHI=0.6, LAMBDA=0.0, RD=0.0,
                      RS=0.0, CBD=0.0, CBS=0.0, IS=1e-14, PB=0.8, CGSO=0.0, CGDO=0.0,
                      CGBO=0.0, CJ=0.0, MJ=0.5, CJSW=0.0, MJSW=0.5, JS=0.0, TOX=0.0, LD=0.0,
                      FC=0.5, W=1e-4, L=1e-4, AD=0.0, AS=0.0, PD=0.0, PS=0.0, M=1.0, RSH=0.0,
-                     NRD=1.0, NRS=1.0)
+                     NRD=1.0, NRS=1.0, TNOM=300.15, TEMP=300.15)
+
+
+def at_temperature(nl: "Netlist", temp_c: float, tnom_c: float = 27.0, **diode_coeffs) -> "Netlist":
+    """Every diode and level-1 MOSFET of nl at temp_c with model TNOM tnom_c
+    (degrees C; the rows hold kelvin); diode_coeffs (TIKF, TBV1, TBV2, TRS1,
+    TRS2) are set on every diode."""
+    fd, fm = DIODE_FIELDS.index, MOS1_FIELDS.index
+    for k, (a, b, p, row) in enumerate(nl.diode):
+        row = np.array(row, dtype=np.float64)
+        row[fd("TEMP")], row[fd("TNOM")] = temp_c + CTOK, tnom_c + CTOK
+        for name, v in diode_coeffs.items():
+            row[fd(name)] = v
+        nl.diode[k] = (a, b, p, row)
+    for k, m in enumerate(nl.mos1):
+        row = np.array(m[4], dtype=np.float64)
+        row[fm("TEMP")], row[fm("TNOM")] = temp_c + CTOK, tnom_c + CTOK
+        nl.mos1[k] = m[:4] + (row,) + m[5:]
+    return nl
 
 
 def mos1_series(row) -> tuple:

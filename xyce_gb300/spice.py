@@ -11,7 +11,9 @@ output.  The subset is what the path simulates:
 * ``.MODEL``, ``.SUBCKT``/``.ENDS``, ``.TRAN``, ``.OPTIONS TIMEINT``
   (RELTOL, ABSTOL, METHOD=TRAP|GEAR, MAXORD), ``.OPTIONS NONLIN-TRAN``
   (RELTOL, ABSTOL, DELTAXTOL, RHSTOL, SMALLUPDATETOL, MAXSTEP),
-  ``.OPTIONS LINSOL TYPE=KLU|KSPARSE``, ``.PARAM`` with ``{NAME}``
+  ``.OPTIONS LINSOL TYPE=KLU|KSPARSE``, ``.TEMP`` and ``.OPTIONS DEVICE
+  TEMP= TNOM=`` (diodes and level-1 MOSFETs; the instance TEMP / DTEMP and
+  the model TNOM too), ``.PARAM`` with ``{NAME}``
   references, ``.STEP`` (linear or LIST; every point of the sweep runs as one
   circuit of a single GPU batch), ``.SAMPLING`` with ``.OPTIONS SAMPLES``
   (Latin hypercube or Monte Carlo samples of NORMAL / UNIFORM parameters,
@@ -157,14 +159,15 @@ class Deck:
     params: dict[str, float] = field(default_factory=dict)
     step_values: dict[str, float] = field(default_factory=dict)  # this deck's point of the sweep
     sampling: dict = field(default_factory=dict)     # .SAMPLING vectors + .OPTIONS SAMPLES
+    temp_c: float = 27.0                              # .TEMP / .OPTIONS DEVICE TEMP (degrees C)
 
 
 _DIODE_ALIASES = {"CJ0": "CJO", "CJ": "CJO", "PB": "VJ", "MJ": "M", "CJP": "CJSW", "PHP": "VJSW"}
 _MOS1_MODEL = {"VTO", "KP", "GAMMA", "PHI", "LAMBDA", "RD", "RS", "CBD", "CBS", "IS", "PB", "CGSO",
-               "CGDO", "CGBO", "CJ", "MJ", "CJSW", "MJSW", "JS", "TOX", "LD", "FC", "RSH"}
-_MOS1_INST = {"W", "L", "AD", "AS", "PD", "PS", "M", "NRD", "NRS"}
+               "CGDO", "CGBO", "CJ", "MJ", "CJSW", "MJSW", "JS", "TOX", "LD", "FC", "RSH", "TNOM"}
+_MOS1_INST = {"W", "L", "AD", "AS", "PD", "PS", "M", "NRD", "NRS", "TEMP", "DTEMP"}
 _B4_INST = {"L", "W", "AS", "AD", "PS", "PD", "M"}
-_IGNORED_MODEL = {"LEVEL", "VERSION", "TNOM"}
+_IGNORED_MODEL = {"LEVEL", "VERSION"}
 
 
 class _Builder:
@@ -175,6 +178,10 @@ class _Builder:
         self.subckts: dict[str, tuple[list[str], list[str]]] = {}
         self.tran = None
         self.overrides: dict[str, float] = {}  # element name -> swept value
+        # .TEMP / .OPTIONS DEVICE TEMP and TNOM (degrees C; the reference's
+        # defaults are 27)
+        self.temp_c = 27.0
+        self.tnom_c = 27.0
 
     def subst(self, toks: list[str]) -> list[str]:
         """{NAME} tokens -> the .PARAM value (a single parameter; no
@@ -276,6 +283,10 @@ class _Builder:
                 p["AREA"] = number(area)
             if "PJ" in kv:
                 p["PJ"] = number(kv["PJ"])
+            bad = set(kv) - {"AREA", "PJ", "TEMP", "DTEMP"}
+            if bad:
+                raise ValueError(f"{name}: unsupported diode instance parameter(s) {sorted(bad)}")
+            p.update(self._device_temps({k: number(v) for k, v in kv.items()}, p))
             self.nl.D(nd(pos[0]), nd(pos[1]), **p)
         elif letter == "M":
             if len(pos) < 5:
@@ -289,12 +300,16 @@ class _Builder:
                     raise ValueError(f"{name}: unsupported MOSFET instance parameter(s) {sorted(bad)}")
                 p = dict(m.params)
                 p.update(inst)
+                p.pop("DTEMP", None)
+                p.update(self._device_temps(inst, m.params))
                 p["TYPE"] = 1.0 if m.kind == "NMOS" else -1.0
                 self.nl.M1(d, g, s, b, **p)
             else:
                 bad = set(inst) - _B4_INST
                 if bad:
                     raise ValueError(f"{name}: unsupported BSIM4 instance parameter(s) {sorted(bad)}")
+                if abs(self.temp_c - 27.0) > 1e-12 or abs(self.tnom_c - 27.0) > 1e-12:
+                    raise ValueError(f"{name}: BSIM4 at a temperature other than 27 C is not supported")
                 p = dict(m.params)
                 p.update(inst)
                 p["TYPE"] = 1.0 if m.kind == "NMOS" else -1.0
@@ -329,6 +344,14 @@ class _Builder:
             raise ValueError(f"model {mname} is not a MOSFET model")
         return m
 
+    def _device_temps(self, inst: dict, model_params: dict) -> dict:
+        """TEMP and TNOM of a diode or level-1 MOSFET row, kelvin: the
+        instance TEMP, else the circuit temperature plus DTEMP
+        (Instance::processParams, N_DEV_Diode.C:392-410, N_DEV_MOSFET1.C:383-400);
+        the model's TNOM, else .OPTIONS DEVICE TNOM."""
+        temp_c = inst["TEMP"] if "TEMP" in inst else self.temp_c + inst.get("DTEMP", 0.0)
+        return {"TEMP": temp_c + N.CTOK, "TNOM": model_params.get("TNOM", self.tnom_c + N.CTOK)}
+
     def model(self, toks: list[str]):
         toks = self.subst(toks)
         pos, kv = _params(toks[1:])
@@ -339,15 +362,18 @@ class _Builder:
         params = {}
         for k, v in kv.items():
             if k in _IGNORED_MODEL:
-                if k == "TNOM" and abs(number(v) - 27.0) > 1e-12:
+                continue
+            if k == "TNOM" and not (kind == "D" or level == 1):
+                # the BSIM4 restatement runs at TNOM = 27 C only
+                if abs(number(v) - 27.0) > 1e-12:
                     raise ValueError(f"model {name}: TNOM other than 27 is not supported")
                 continue
-            params[k] = number(v)
+            params[k] = number(v) + N.CTOK if k == "TNOM" else number(v)
         if kind == "D":
             out = {}
             for k, v in params.items():
                 k = _DIODE_ALIASES.get(k, k)
-                if k not in N.DIODE_FIELDS or k in ("BVGIVEN", "NSGIVEN", "PJ"):
+                if k not in N.DIODE_FIELDS or k in ("BVGIVEN", "NSGIVEN", "PJ", "TEMP"):
                     raise ValueError(f"model {name}: unsupported diode parameter {k}")
                 out[k] = v
             params = out
@@ -462,11 +488,28 @@ def parse(text: str, overrides: dict | None = None) -> Deck:
     reltol = abstol = method = maxord = None
     nonlin = {}
     deck = B.deck
+    # the circuit temperature applies to every device, wherever the line is
+    for ln, toks in body_lines:
+        head = toks[0].upper()
+        if head == ".TEMP":
+            vals = [number(t) for t in B.subst(toks[1:])]
+            if len(vals) != 1:
+                raise ValueError(".TEMP takes one temperature (no sweeps)")
+            B.temp_c = deck.temp_c = vals[0]
+        elif head == ".OPTIONS" and len(toks) > 1 and toks[1].upper() == "DEVICE":
+            pos, kv = _params(B.subst(toks)[2:])
+            for k, v in kv.items():
+                if k == "TEMP":
+                    B.temp_c = deck.temp_c = number(v)
+                elif k == "TNOM":
+                    B.tnom_c = number(v)
+                else:
+                    raise ValueError(f".OPTIONS DEVICE {k} is not supported")
     for ln, toks in body_lines:
         head = toks[0].upper()
         if head == ".END":
             break
-        if head in (".PARAM",):
+        if head in (".PARAM", ".TEMP") or (head == ".OPTIONS" and len(toks) > 1 and toks[1].upper() == "DEVICE"):
             continue
         if head == ".SAMPLING":
             deck.sampling.update(_sampling_spec(ln))
@@ -817,7 +860,7 @@ def _var_probes(deck: Deck, var: str) -> tuple[list[int], callable]:
         br = deck.branches[src]
         return [br], lambda vals, br=br: vals[br]
     if var == "TEMP":
-        return [], lambda vals: 27.0
+        return [], lambda vals, tc=deck.temp_c: tc
     m = re.match(r"^([RC][^:]*):([RC])$", var)
     if m and m.group(1) in deck.element_values and m.group(1)[0] == m.group(2):
         v = deck.element_values[m.group(1)]
