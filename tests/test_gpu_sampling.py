@@ -82,3 +82,42 @@ def test_sampling_deck_matches_oracle_per_sample(xg, oracle_mod, torch_cuda):
         assert abs(results[k].measures["VMAX"] - vmax_oracle) <= tol, (k, results[k].measures["VMAX"], vmax_oracle)
     mom = S.sample_moments([r.measures["VMAX"] for r in results])
     assert 0.5 < mom["mean"] < 2.0 and mom["variance"] > 0
+
+
+ES_DECK = f"""Clamped RC embedded sampling
+.PARAM rval=1k cval=1n
+V1 in 0 SIN(0 2 1MEG)
+R1 in out {{rval}}
+C1 out 0 {{cval}}
+D1 out 0 dclamp
+.MODEL dclamp D(IS=1e-14 N=1 RS=10 CJO=1p)
+.TRAN 1n 3u 0 10n
+.OPTIONS NONLIN-TRAN RELTOL=1e-6 ABSTOL=1e-9
+.EMBEDDEDSAMPLING param=rval,cval type=normal,uniform means=1k std_deviations=100
++ lower_bounds=0.5n upper_bounds=1.5n
+.OPTIONS EMBEDDEDSAMPLES NUMSAMPLES=32 SEED=11 OUTPUTS={{V(OUT)}},{{V(IN,OUT)}}
+.END
+"""
+
+
+def test_embedded_sampling_block_system_matches_oracle(xg, oracle_mod, torch_cuda):
+    """.EMBEDDEDSAMPLING: the 32 samples as ONE circuit (one block system,
+    one step control) on the GPU, against the oracle running the same
+    union netlist: the same accepted and rejected steps, and every sample's
+    outputs within WAVE_RTOL * max|v| + WAVE_ATOL at the oracle's time points."""
+    decks = S.parse_embedded(ES_DECK)
+    ens = S.run_embedded(decks)
+
+    def oracle_run(nl, probes, cap):
+        return oracle_mod.Oracle(nl).transient(probes=probes)
+    ref = S.run_embedded(decks, transient=oracle_run)
+    assert ens.stats["status"] == 0 and ref.stats["status"] == 0
+    assert (ens.stats["accepted"], ens.stats["rejected"]) == (ref.stats["accepted"], ref.stats["rejected"])
+    assert len(ens.times) == len(ref.times)
+    for var in ("V(OUT)", "V(IN,OUT)"):
+        g, r = ens.samples[var], ref.samples[var]
+        tol = WAVE_RTOL * np.max(np.abs(r)) + WAVE_ATOL
+        gi = np.stack([np.interp(ref.times, ens.times, g[k]) for k in range(g.shape[0])])
+        assert np.max(np.abs(gi - r)) <= tol, (var, float(np.max(np.abs(gi - r))), tol)
+        np.testing.assert_allclose(ens.moments(var)["stddev"], ref.moments(var)["stddev"], rtol=0,
+                                   atol=2 * tol)

@@ -17,7 +17,10 @@ output.  The subset is what the path simulates:
   references, ``.STEP`` (linear or LIST; every point of the sweep runs as one
   circuit of a single GPU batch), ``.SAMPLING`` with ``.OPTIONS SAMPLES``
   (Latin hypercube or Monte Carlo samples of NORMAL / UNIFORM parameters,
-  all samples one batch, moments of every .MEASURE), ``.PRINT TRAN`` (FORMAT=STD,
+  all samples one batch, moments of every .MEASURE), ``.EMBEDDEDSAMPLING``
+  with ``.OPTIONS EMBEDDEDSAMPLES`` (the samples as one block system with one
+  step control; per-point moments of each output in ``<netlist>_ensemble.prn``),
+  ``.PRINT TRAN`` (FORMAT=STD,
   NOINDEX or CSV), ``.MEASURE TRAN`` (MAX, MIN, PP, AVG,
   RMS, INTEG with FROM/TO), ``.END``; ``*`` and ``;`` comments, ``+``
   continuation lines, engineering suffixes (T G MEG K M MIL U N P F);
@@ -160,6 +163,7 @@ class Deck:
     step_values: dict[str, float] = field(default_factory=dict)  # this deck's point of the sweep
     sampling: dict = field(default_factory=dict)     # .SAMPLING vectors + .OPTIONS SAMPLES
     temp_c: float = 27.0                              # .TEMP / .OPTIONS DEVICE TEMP (degrees C)
+    embedded: dict = field(default_factory=dict)     # .EMBEDDEDSAMPLING + .OPTIONS EMBEDDEDSAMPLES
 
 
 _DIODE_ALIASES = {"CJ0": "CJO", "CJ": "CJO", "PB": "VJ", "MJ": "M", "CJP": "CJSW", "PHP": "VJSW"}
@@ -514,6 +518,12 @@ def parse(text: str, overrides: dict | None = None) -> Deck:
         if head == ".SAMPLING":
             deck.sampling.update(_sampling_spec(ln))
             continue
+        if head == ".EMBEDDEDSAMPLING":
+            deck.embedded.update(_sampling_spec(ln, ".EMBEDDEDSAMPLING"))
+            continue
+        if head == ".OPTIONS" and len(toks) > 1 and toks[1].upper() == "EMBEDDEDSAMPLES":
+            deck.embedded.update(_embedded_options(ln))
+            continue
         if head == ".OPTIONS" and len(toks) > 1 and toks[1].upper() == "SAMPLES":
             pos, kv = _params(toks[2:])
             for k, v in kv.items():
@@ -643,10 +653,11 @@ def _step(toks: list[str]) -> tuple[str, list[float]]:
     return name, [float(a + i * st) for i in range(k)]
 
 
-def _sampling_spec(line: str) -> dict:
+def _sampling_spec(line: str, what: str = ".SAMPLING") -> dict:
     """.SAMPLING PARAM=a,b TYPE=normal,uniform MEANS=.. STD_DEVIATIONS=..
     LOWER_BOUNDS=.. UPPER_BOUNDS=.. (vectors, one entry per parameter;
-    the keys of Sampling, src/AnalysisPKG/N_ANP_Sampling.C:200-260)."""
+    the keys of Sampling, src/AnalysisPKG/N_ANP_Sampling.C:200-260, and of
+    EmbeddedSampling::setAnalysisParams, N_ANP_EmbeddedSampling.C:291-380)."""
     body = line.split(None, 1)[1] if len(line.split(None, 1)) > 1 else ""
     out = {}
     for m in re.finditer(r"(\w+)\s*=\s*(.*?)(?=\s+\w+\s*=|$)", body):
@@ -657,7 +668,41 @@ def _sampling_spec(line: str) -> dict:
         elif key in ("MEANS", "STD_DEVIATIONS", "LOWER_BOUNDS", "UPPER_BOUNDS"):
             out[key] = [number(v) for v in vals]
         else:
-            raise ValueError(f".SAMPLING {key} is not supported")
+            raise ValueError(f"{what} {key} is not supported")
+    return out
+
+
+def _embedded_options(line: str) -> dict:
+    """.OPTIONS EMBEDDEDSAMPLES NUMSAMPLES= SAMPLE_TYPE=LHS|MC SEED=
+    OUTPUTS={expr},{expr} OUTPUT_SAMPLE_STATS= OUTPUT_ALL_SAMPLES=
+    OUTPUTFORMAT=STD|TECPLOT (EmbeddedSampling::setEmbeddedSamplingOptions,
+    N_ANP_EmbeddedSampling.C:513-640; defaults :2044-2065).  The polynomial
+    chaos options are not supported."""
+    parts = line.split(None, 2)
+    body = parts[2] if len(parts) > 2 else ""
+    out = {}
+    flag = lambda v: v.strip().upper() in ("1", "TRUE", "YES") or (_is_number(v) and number(v) != 0)
+    for m in re.finditer(r"(\w+)\s*=\s*(.*?)(?=\s+\w+\s*=|$)", body):
+        key, val = m.group(1).upper(), m.group(2).strip()
+        if key == "OUTPUTS":
+            outs = re.findall(r"\{([^}]*)\}", val) or [v for v in re.split(r"[,\s]+", val) if v]
+            out["OUTPUTS"] = [o.strip().upper() for o in outs]
+        elif key in ("NUMSAMPLES", "SEED"):
+            out[key] = int(number(val))
+        elif key == "SAMPLE_TYPE":
+            if val.upper() not in ("LHS", "MC"):
+                raise ValueError("SAMPLE_TYPE must be LHS or MC")
+            out[key] = val.upper()
+        elif key in ("OUTPUT_SAMPLE_STATS", "OUTPUT_ALL_SAMPLES"):
+            out[key] = flag(val)
+        elif key == "OUTPUTFORMAT":
+            if val.upper() not in ("STD", "TECPLOT"):
+                raise ValueError("OUTPUTFORMAT must be STD or TECPLOT")
+            out[key] = val.upper()
+        else:
+            raise ValueError(f".OPTIONS EMBEDDEDSAMPLES {key} is not supported")
+    if out.get("NUMSAMPLES", 1) < 1:
+        raise ValueError("NUMSAMPLES on .OPTIONS EMBEDDEDSAMPLES must be > 0")
     return out
 
 
@@ -723,6 +768,142 @@ def parse_sampling(text: str) -> list[Deck]:
     if not base.sampling:
         return [base]
     return [parse(text, pt) for pt in sample_points(base.sampling)]
+
+
+def parse_embedded(text: str) -> list[Deck]:
+    """One deck per sample of the deck's .EMBEDDEDSAMPLING block (the same
+    parameter vectors and sample generator as .SAMPLING)."""
+    base = parse(text)
+    if not base.embedded:
+        raise ValueError("the deck has no .EMBEDDEDSAMPLING")
+    if base.sampling or base.steps:
+        raise ValueError(".EMBEDDEDSAMPLING with .SAMPLING or .STEP is not supported")
+    return [parse(text, pt) for pt in sample_points(base.embedded)]
+
+
+def ensemble_netlist(decks: list[Deck]) -> tuple[N.Netlist, list[int]]:
+    """Every sample as a block of ONE circuit, and each block's first
+    unknown.  As in the reference's embedded sampling (ESLoader and the
+    block vectors of N_ANP_EmbeddedSampling.C) the blocks share one
+    transient: one step sequence, one Newton solve per step over the whole
+    block system, error norms over every block, every sample's breakpoints.
+    (.SAMPLING instead runs each sample as its own circuit of a batch, with
+    its own step control.)"""
+    nl = N.batch([d.netlist for d in decks], label=decks[0].title)
+    bases = list(nl.offsets[:-1])
+    nl.offsets = [0, nl.n]
+    return nl, bases
+
+
+@dataclass
+class Ensemble:
+    """An embedded-sampling run: the shared time points and, per output,
+    every sample's values [n_samples, n_points]."""
+    times: np.ndarray
+    samples: dict[str, np.ndarray]
+    stats: dict
+
+    def moments(self, var: str) -> dict:
+        """Mean, population standard deviation and variance over the samples
+        at every time point (computeMoments, N_ANP_UQSupport.C:80-135)."""
+        v = self.samples[var]
+        mean = v.mean(axis=0)
+        var_ = np.mean((v - mean) ** 2, axis=0)
+        return dict(mean=mean, stddev=np.sqrt(var_), variance=var_)
+
+
+def _gpu_transient(nl: N.Netlist, probes: list[int], cap: int, device: int = 0):
+    from . import Circuit
+    circ = Circuit(nl, device=device)
+    try:
+        counts, times, values, stats = circ.transient(nl.tran, probes=probes, cap=cap)
+    finally:
+        circ.close()
+    n = int(counts[0])
+    return times[0, :n].copy(), values[0, :n, :].copy(), stats
+
+
+def run_embedded(decks: list[Deck], device: int = 0, cap: int | None = None, transient=None) -> Ensemble:
+    """The samples as one block system on the GPU (ensemble_netlist).
+    Outputs: OUTPUTS of .OPTIONS EMBEDDEDSAMPLES, else the .PRINT variables.
+    transient(nl, probes, cap) -> (times, values[points, probes], stats)
+    replaces the GPU run (a checker drives the same netlist through it)."""
+    spec = decks[0].embedded
+    outs = spec.get("OUTPUTS") or [v for v in decks[0].prints if v != "TIME"]
+    if not outs:
+        raise ValueError("embedded sampling needs OUTPUTS or .PRINT variables")
+    nl, bases = ensemble_netlist(decks)
+    probes, plan = [], []
+    for d, base in zip(decks, bases):
+        row = []
+        for var in outs:
+            us, f = _var_probes(d, var)
+            slots = []
+            for u in us:
+                probes.append(base + u)
+                slots.append(len(probes) - 1)
+            row.append((us, slots, f))
+        plan.append(row)
+    if not probes:
+        probes = [0]
+    if cap is None:
+        tr = nl.tran
+        hmin_guess = tr.hmax if tr.hmax > 0 else tr.tstop / 50.0
+        cap = int(min(2_000_000, max(4096, 20 * tr.tstop / max(hmin_guess, 1e-30))))
+    run_t = transient or (lambda n_, p_, c_: _gpu_transient(n_, p_, c_, device))
+    for _ in range(4):
+        t, vals, stats = run_t(nl, probes, cap)
+        if len(t) < cap:
+            break
+        cap *= 4
+    else:
+        raise RuntimeError(f"more than {cap} accepted steps")
+    samples = {}
+    for j, var in enumerate(outs):
+        cols = []
+        for row in plan:
+            us, slots, f = row[j]
+            sub_ = {u: vals[:, s] for u, s in zip(us, slots)}
+            cols.append(np.broadcast_to(np.asarray(f(sub_), np.float64), t.shape))
+        samples[var] = np.stack(cols)
+    return Ensemble(t, samples, stats)
+
+
+def write_ensemble(path: str, deck: Deck, ens: Ensemble) -> str:
+    """<netlist>_ensemble.prn (OUTPUTFORMAT=STD, the default) or .dat
+    (TECPLOT) in the reference's layout (EmbeddedSampling::hackEnsembleOutput,
+    N_ANP_EmbeddedSampling.C:1377-1560): a TECPLOT-style header naming TIME
+    and, per output, its mean, mean -/+ one and two standard deviations,
+    standard deviation and variance (OUTPUT_SAMPLE_STATS) and every sample
+    (OUTPUT_ALL_SAMPLES), then one row per accepted time point."""
+    spec = deck.embedded
+    stats_on = spec.get("OUTPUT_SAMPLE_STATS", True)
+    all_on = spec.get("OUTPUT_ALL_SAMPLES", False)
+    out = path + ("_ensemble.dat" if spec.get("OUTPUTFORMAT", "STD") == "TECPLOT" else "_ensemble.prn")
+    names = list(ens.samples)
+    with open(out, "w") as f:
+        f.write('TITLE = "embedded sampling output"\tVARIABLES= \n')
+        f.write('\t" TIME "\n')
+        for var in names:
+            if stats_on:
+                for suffix in ("_mean", "_meanPlus", "_meanMinus", "_meanPlusTwoSigma", "_meanMinusTwoSigma",
+                               "_stddev", "_variance"):
+                    f.write(f'\t" {var}{suffix}"\n')
+            if all_on:
+                for i in range(ens.samples[var].shape[0]):
+                    f.write(f'\t" {var}_{i}"\n')
+        f.write('ZONE F=POINT  T="Xyce data"\n')
+        mom = {var: ens.moments(var) for var in names}
+        for k, t in enumerate(ens.times):
+            cells = [f"{t:.6e}"]
+            for var in names:
+                if stats_on:
+                    m, s, v = mom[var]["mean"][k], mom[var]["stddev"][k], mom[var]["variance"][k]
+                    cells += [f"{x:.6e}" for x in (m, m + s, m - s, m + 2 * s, m - 2 * s, s, v)]
+                if all_on:
+                    cells += [f"{x:.6e}" for x in ens.samples[var][:, k]]
+            f.write("\t".join(cells) + "\n")
+    return out
 
 
 def parse_sweep(text: str) -> list[Deck]:
@@ -1022,6 +1203,13 @@ def main(argv=None) -> int:
     with open(path) as f:
         text = f.read()
     base = parse(text)
+    if base.embedded:
+        decks = parse_embedded(text)
+        ens = run_embedded(decks)
+        out = write_ensemble(path, decks[0], ens)
+        print(f"{len(decks)} samples as one block system, {len(ens.times)} shared time points; "
+              f"output {os.path.basename(out)}")
+        return 0
     if base.sampling:
         if base.steps:
             raise ValueError(".SAMPLING and .STEP together are not supported")
