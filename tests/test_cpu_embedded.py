@@ -27,6 +27,7 @@ D1 out 0 dclamp
 
 def _oracle_runner(oracle_mod):
     def run(nl, probes, cap):
+        assert len(set(probes)) == len(probes)  # the C-ABI takes each unknown once
         t, v, st = oracle_mod.Oracle(nl).transient(probes=probes)
         return t, v, st
     return run

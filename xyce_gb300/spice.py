@@ -833,15 +833,17 @@ def run_embedded(decks: list[Deck], device: int = 0, cap: int | None = None, tra
     if not outs:
         raise ValueError("embedded sampling needs OUTPUTS or .PRINT variables")
     nl, bases = ensemble_netlist(decks)
-    probes, plan = [], []
+    probes, plan, slot_of = [], [], {}
     for d, base in zip(decks, bases):
         row = []
         for var in outs:
             us, f = _var_probes(d, var)
             slots = []
             for u in us:
-                probes.append(base + u)
-                slots.append(len(probes) - 1)
+                if base + u not in slot_of:  # each unknown is probed once
+                    slot_of[base + u] = len(probes)
+                    probes.append(base + u)
+                slots.append(slot_of[base + u])
             row.append((us, slots, f))
         plan.append(row)
     if not probes:
