@@ -119,7 +119,7 @@ def test_min_degree_order_same_transient(oracle_mod):
 
 
 def test_min_degree_order_solves(oracle_mod):
-    """The ordered LU solves the same systems (scipy as the judge of the
+    """The ordered LU solves the same systems (scipy's solve checks the
     answer), and the order is a permutation of the unknowns."""
     nl = N.power_grid(20, 10, seed=1)
     o = oracle_mod.Oracle(nl)
