@@ -6,11 +6,16 @@
 // The analysis runs on vals_a; both value sets are then factored in the
 // analysed (frozen) order exactly as the device factorization does
 // (left-looking, the analysis' update maps), and the probe prints one line:
-//   rc exempt min_ratio_a min_ratio_b recon_err_a
+//   rc exempt min_ratio_a min_ratio_b recon_err_a factor_sched_ok lsolve_sched_ok
+//   factor_hubs factor_top_items
 // min_ratio_x: the smallest |pivot| / max|updated column| over the columns
 // whose U row has entries right of the diagonal (the device's threshold
 // test); recon_err_a: max |(L U)(i,j) - A'(i,j)| / max|A| over the
-// permuted matrix A'(i, j) = A(row_of_step[i], col_of_step[j]).
+// permuted matrix A'(i, j) = A(row_of_step[i], col_of_step[j]);
+// *_sched_ok: every step appears once in the schedule, hubs have no
+// dependencies, an item of a group depends only on hubs and on earlier
+// levels of its own group, and an item of the top only on hubs, groups and
+// earlier levels of the top (factor: U(:, p); L solve: L(p, :)).
 #include <cmath>
 #include <cstdio>
 #include <string>
@@ -19,6 +24,36 @@
 #include "../xyce_gb300/csrc/xg_internal.h"
 
 using namespace xg;
+
+static bool schedule_ok(const Schedule &S, int n, const std::vector<std::vector<int>> &deps) {
+  std::vector<int> grp(n, -2), lvl(n, -1);
+  for (int t = 0; t < S.n_hub; ++t) {
+    const int j = S.items[t];
+    if (j < 0 || j >= n || grp[j] != -2) return false;
+    grp[j] = -1;
+  }
+  for (int g = 0; g <= S.n_groups; ++g)  // g == n_groups: the top
+    for (int lv = S.grp_lvl[g]; lv < S.grp_lvl[g + 1]; ++lv)
+      for (int t = S.lvl_ptr[lv]; t < S.lvl_ptr[lv + 1]; ++t) {
+        const int j = S.items[t];
+        if (j < 0 || j >= n || grp[j] != -2) return false;
+        grp[j] = g;
+        lvl[j] = lv;
+      }
+  for (int j = 0; j < n; ++j) {
+    if (grp[j] == -2) return false;
+    if (grp[j] == -1 && !deps[j].empty()) return false;
+    for (int k : deps[j]) {
+      if (grp[k] == -1) continue;
+      if (grp[j] == S.n_groups) {
+        if (grp[k] == S.n_groups && lvl[k] >= lvl[j]) return false;
+      } else if (grp[k] != grp[j] || lvl[k] >= lvl[j]) {
+        return false;
+      }
+    }
+  }
+  return true;
+}
 
 static void factor(const LUHost &H, const std::vector<double> &vals, std::vector<double> &lu, double &min_ratio) {
   const int n = H.n;
@@ -60,7 +95,7 @@ int main(int argc, char **argv) {
   std::string err;
   const int rc = lu_analyze_host(n, rp, ci, va, H, err);
   if (rc != XG_OK) {
-    std::printf("%d 0 0 0 0\n", rc);
+    std::printf("%d 0 0 0 0 0 0 0 0\n", rc);
     return 0;
   }
   int exempt = 0;
@@ -94,6 +129,15 @@ int main(int argc, char **argv) {
       for (int k = 0; k <= std::min(i, j); ++k) s += Ld[size_t(i) * n + k] * Ud[size_t(k) * n + j];
       rerr = std::max(rerr, std::fabs(s - A[size_t(i) * n + j]));
     }
-  std::printf("%d %d %.17g %.17g %.17g\n", rc, exempt, ra, rb, amax > 0.0 ? rerr / amax : 0.0);
+  std::vector<std::vector<int>> fdeps(n), ldeps(n);
+  for (int p = 0; p < n; ++p) {
+    for (int t = H.cp[p]; t < H.diag[p]; ++t) fdeps[p].push_back(H.ri[t]);
+    for (int t = H.l_ptr[p]; t < H.l_ptr[p + 1]; ++t) ldeps[p].push_back(H.l_col[t]);
+  }
+  const bool fok = schedule_ok(H.fsched, n, fdeps), lok = schedule_ok(H.lsched, n, ldeps);
+  const Schedule &F = H.fsched;
+  const int top_items = F.lvl_ptr[F.grp_lvl[F.n_groups + 1]] - F.lvl_ptr[F.grp_lvl[F.n_groups]];
+  std::printf("%d %d %.17g %.17g %.17g %d %d %d %d\n", rc, exempt, ra, rb, amax > 0.0 ? rerr / amax : 0.0,
+              fok ? 1 : 0, lok ? 1 : 0, F.n_hub, top_items);
   return 0;
 }

@@ -4,7 +4,9 @@ the permuted matrix; the analysis of a matrix whose static pivots are
 cancelled by elimination (a ring with series drain/source resistance at its
 operating point) falls back to threshold partial pivoting and leaves no
 column below the device's pivot threshold; an order frozen on one matrix is
-tested, as the device does, on the next one."""
+tested, as the device does, on the next one; the factor and L-solve
+schedules (hubs, dependency-closed groups, the top) respect every
+dependency."""
 import os
 import shutil
 import subprocess
@@ -51,6 +53,9 @@ def _run(probe, tmp_path, rp, ci, va, vb=None):
         np.asarray(vb, np.float64).tofile(f)
     out = subprocess.run([probe, path], check=True, capture_output=True, text=True).stdout.split()
     rc, exempt = int(out[0]), int(out[1])
+    # every analysis' factor and L-solve schedules respect the dependencies
+    assert rc != 0 or (out[5], out[6]) == ("1", "1"), out
+    _run.layout = (int(out[7]), int(out[8]))  # factor hubs, factor top items
     return rc, exempt, float(out[2]), float(out[3]), float(out[4])
 
 
@@ -87,6 +92,19 @@ def test_analysed_factors_reconstruct_the_matrix(probe, oracle_mod, tmp_path, ma
     for vals in (init, conv, tran):
         rc, ex, ra, rb, err = _run(probe, tmp_path, o.row_ptr, o.col_idx, vals)
         assert rc == 0 and ex == 0 and ra >= RUNTIME_PIVOT_TOL and err < 1e-12
+
+
+@pytest.mark.parametrize("maker", [lambda: N.power_grid(30, 30, seed=4), lambda: N.diode_ladder(300, seed=1)],
+                         ids=["grid30", "diode300"])
+def test_schedules_with_a_top(probe, oracle_mod, tmp_path, maker):
+    """Circuits larger than one dependency-closed group (512 items): the
+    columns that depend on several groups form the top (30 items on a
+    30 x 30 grid, 2 on a 300-node diode ladder).  The schedules still
+    respect every dependency (checked inside _run)."""
+    o, init, conv, tran = _jacobians(oracle_mod, maker())
+    rc, ex, ra, rb, err = _run(probe, tmp_path, o.row_ptr, o.col_idx, tran)
+    hubs, top = _run.layout
+    assert rc == 0 and err < 1e-12 and top > 0, _run.layout
 
 
 @pytest.mark.parametrize("seed", range(6))
