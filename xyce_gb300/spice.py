@@ -22,7 +22,8 @@ output.  The subset is what the path simulates:
   step control; per-point moments of each output in ``<netlist>_ensemble.prn``),
   ``.PRINT TRAN`` (FORMAT=STD,
   NOINDEX or CSV), ``.MEASURE TRAN`` (MAX, MIN, PP, AVG,
-  RMS, INTEG with FROM/TO), ``.END``; ``*`` and ``;`` comments, ``+``
+  RMS, INTEG with FROM/TO; TRIG/TARG with VAL, TD and RISE/FALL/CROSS=n|LAST;
+  WHEN; FIND ... WHEN / AT), ``.END``; ``*`` and ``;`` comments, ``+``
   continuation lines, engineering suffixes (T G MEG K M MIL U N P F);
 * print variables ``V(n)``, ``V(a,b)``, ``I(Vname)``, ``TIME``, ``TEMP``
   and ``<R|C name>:R|C`` (the element value).
@@ -140,11 +141,19 @@ class Model:
 
 @dataclass
 class Measure:
+    """func: MAX, MIN, PP, AVG, RMS, INTEG over var; or TRIGTARG, WHEN, FIND
+    (spec holds their clauses).  vars: every variable the measure reads."""
     name: str
     func: str
     var: str
     frm: float | None = None
     to: float | None = None
+    spec: dict = field(default_factory=dict)
+    vars: list = field(default_factory=list)
+
+    def __post_init__(self):
+        if not self.vars:
+            self.vars = [self.var]
 
 
 @dataclass
@@ -930,7 +939,7 @@ def run_sweep(decks: list[Deck], device: int = 0, cap: int | None = None) -> lis
     plans, probes = [], []
     for k, d in enumerate(decks):
         base = nl.offsets[k]
-        wanted = list(dict.fromkeys(d.prints + [m.var for m in d.measures]))
+        wanted = list(dict.fromkeys(d.prints + [v for m in d.measures for v in m.vars]))
         local: list[int] = []
         plan = {}
         for var in wanted:
@@ -976,7 +985,7 @@ def _columns(deck: Deck, wanted, plan, t, vals, stats) -> "Result":
             continue
         sub = {u: vals[:, s] for u, s in zip(us, slots)}
         cols[var] = np.broadcast_to(np.asarray(f(sub), dtype=np.float64), t.shape).copy()
-    meas = {m.name: measure(m.func, t, cols[m.var], m.frm, m.to) for m in deck.measures}
+    meas = {m.name: evaluate_measure(m, t, cols) for m in deck.measures}
     return Result(t, cols, meas, stats)
 
 
@@ -997,7 +1006,95 @@ def _print_vars(toks: list[str]) -> list[str]:
     return out
 
 
+_RFC = ("RISE", "FALL", "CROSS")
+MINVAL = 1e-12  # the measures' MINVAL default, N_IO_MeasureBase.C:69
+
+
+def _one_var(toks: list[str], i: int) -> tuple[str, int]:
+    if i + 1 < len(toks) and toks[i + 1] == "(" and ")" in toks[i:]:
+        j = toks.index(")", i)
+        return f"{toks[i].upper()}({','.join(a.upper() for a in toks[i + 2:j])})", j + 1
+    raise ValueError(f".MEASURE: expected V(...) or I(...) at {' '.join(toks[i:i + 3])}")
+
+
+def _kv_run(toks: list[str], i: int) -> tuple[dict, int]:
+    """KEY = VALUE pairs from toks[i] on."""
+    out = {}
+    while i + 2 < len(toks) + 1 and i + 1 < len(toks) and toks[i + 1] == "=" and toks[i] != "=":
+        out[toks[i].upper()] = toks[i + 2]
+        i += 3
+    return out, i
+
+
+def _rfc(kv: dict) -> tuple:
+    """(RISE|FALL|CROSS or None, count); count -1 = LAST; none given: the
+    first crossing."""
+    given = [k for k in _RFC if k in kv]
+    if len(given) > 1:
+        raise ValueError(".MEASURE: give one of RISE, FALL, CROSS")
+    if not given:
+        return None, 0
+    v = kv[given[0]].upper()
+    return given[0], (-1 if v == "LAST" else int(number(v)))
+
+
+def _timing_measure(name: str, toks: list[str]) -> Measure:
+    """TRIG/TARG (RiseFallDelay), WHEN and FIND ... WHEN / AT (FindWhen,
+    WhenAT), src/IOInterfacePKG/Output/N_IO_MeasureRiseFallDelay.C,
+    N_IO_MeasureFindWhen.C, N_IO_MeasureWhenAT.C."""
+    head = toks[0].upper()
+    allowed = set(_RFC) | {"TD", "FROM", "TO", "VAL"}
+
+    def clause(i):
+        var, i = _one_var(toks, i)
+        kv, i = _kv_run(toks, i)
+        bad = set(kv) - allowed
+        if bad or "VAL" not in kv:
+            raise ValueError(f".MEASURE {name}: TRIG/TARG need VAL= (and only {sorted(allowed)})")
+        return dict(var=var, val=number(kv["VAL"]), td=number(kv.get("TD", "0")), rfc=_rfc(kv)), i
+
+    def when(i):
+        var, i = _one_var(toks, i)
+        if i + 1 >= len(toks) or toks[i] != "=":
+            raise ValueError(f".MEASURE {name}: WHEN <var>=<value>")
+        val = number(toks[i + 1])
+        kv, i = _kv_run(toks, i + 2)
+        bad = set(kv) - (allowed - {"VAL"})
+        if bad:
+            raise ValueError(f".MEASURE {name}: unsupported {sorted(bad)}")
+        spec = dict(var=var, val=val, rfc=_rfc(kv), td=number(kv.get("TD", "0")),
+                    frm=number(kv["FROM"]) if "FROM" in kv else None, to=number(kv["TO"]) if "TO" in kv else None)
+        return spec, i
+
+    if head == "TRIG":
+        trig, i = clause(1)
+        if i >= len(toks) or toks[i].upper() != "TARG":
+            raise ValueError(f".MEASURE {name}: TRIG ... TARG ...")
+        targ, i = clause(i + 1)
+        if i != len(toks):
+            raise ValueError(f".MEASURE {name}: unexpected {' '.join(toks[i:])}")
+        return Measure(name, "TRIGTARG", trig["var"], spec=dict(trig=trig, targ=targ), vars=[trig["var"], targ["var"]])
+    if head == "WHEN":
+        w, i = when(1)
+        if i != len(toks):
+            raise ValueError(f".MEASURE {name}: unexpected {' '.join(toks[i:])}")
+        return Measure(name, "WHEN", w["var"], spec=dict(when=w), vars=[w["var"]])
+    # FIND <var> WHEN ... | FIND <var> AT=<t>
+    fvar, i = _one_var(toks, 1)
+    if i < len(toks) and toks[i].upper() == "WHEN":
+        w, i = when(i + 1)
+        if i != len(toks):
+            raise ValueError(f".MEASURE {name}: unexpected {' '.join(toks[i:])}")
+        return Measure(name, "FIND", fvar, spec=dict(when=w), vars=[fvar, w["var"]])
+    kv, i = _kv_run(toks, i)
+    if set(kv) != {"AT"} or i != len(toks):
+        raise ValueError(f".MEASURE {name}: FIND <var> WHEN ... or FIND <var> AT=<time>")
+    return Measure(name, "FIND", fvar, spec=dict(at=number(kv["AT"])), vars=[fvar])
+
+
 def _measure(toks: list[str]) -> Measure:
+    if len(toks) >= 3 and toks[0].upper() == "TRAN" and toks[2].upper() in ("TRIG", "WHEN", "FIND"):
+        return _timing_measure(toks[1].upper(), toks[2:])
     pos, kv = _params(toks)
     if len(pos) < 3 or pos[0].upper() != "TRAN":
         raise ValueError(".MEASURE TRAN <name> <func> <var> is the supported form")
@@ -1061,6 +1158,96 @@ class Result:
     stats: dict
 
 
+def _rfc_event_time(t, v, val, rfc, td):
+    """TRIG or TARG: the time of the counted crossing of val (RISE: v - val
+    from < 0 to >= 0; FALL: from > 0 to <= 0; CROSS: either; none given:
+    the first crossing), over the points at or after TD, interpolated
+    linearly between the two points around it; LAST: the last such
+    crossing (Base::withinRiseFallCrossWindow, N_IO_MeasureBase.C:781-880;
+    RiseFallDelay::updateTran, N_IO_MeasureRiseFallDelay.C:220-470)."""
+    kind, count = rfc
+    sel = t >= td * (1 - MINVAL)
+    t, v = t[sel], v[sel]
+    nr = nf = nc = 0
+    found = float("nan")
+    for k in range(1, len(t)):
+        a, b = v[k - 1] - val, v[k] - val
+        rise, fall = (b >= 0.0 and a < 0.0), (b <= 0.0 and a > 0.0)
+        if not (rise or fall):
+            continue
+        nr += rise
+        nf += fall
+        nc += 1
+        hit = ((kind is None and nc == 1) or (kind == "RISE" and rise and (nr == count or count < 0)) or
+               (kind == "FALL" and fall and (nf == count or count < 0)) or
+               (kind == "CROSS" and (nc == count or count < 0)))
+        if hit:
+            dv = v[k] - v[k - 1]
+            found = t[k - 1] if abs(dv) < MINVAL else t[k - 1] + (t[k] - t[k - 1]) * (val - v[k - 1]) / dv
+            if count >= 0:
+                break
+    return found
+
+
+def _when(t, v, f, w):
+    """WHEN (and FIND ... WHEN): the interpolated time at which v reaches
+    w["val"], counted as RISE/FALL/CROSS among the crossings inside
+    TD/FROM/TO, with f (the FIND variable) interpolated at that time
+    (FindWhenBase::updateTran, WhenAT::isWHENcondition /
+    interpolateCalculationInstant / withinRFCWindowForWhen,
+    N_IO_MeasureFindWhen.C:108-175,420-480, N_IO_MeasureWhenAT.C:107-250)."""
+    val, (kind, count) = w["val"], w["rfc"]
+    td, frm, to = w["td"], w["frm"], w["to"]
+    nr = nf = nc = 0
+    res_t = res_f = float("nan")
+    for k in range(1, len(t)):
+        lv, cv = v[k - 1], v[k]
+        if cv == lv:
+            continue
+        if not (abs(cv - val) < MINVAL or (lv - val < 0.0 < cv - val) or (lv - val > 0.0 > cv - val)):
+            continue
+        a = (cv - lv) / (t[k] - t[k - 1])
+        tw = (val - (cv - a * t[k])) / a
+        if (tw < td * (1 - MINVAL) or (frm is not None and tw < frm * (1 - MINVAL)) or
+                (to is not None and tw > to * (1 + MINVAL))):
+            continue
+        nc += 1
+        rising = cv > lv
+        nr += rising
+        nf += not rising
+        ok = ((kind == "RISE" and rising and nr >= count) or (kind == "FALL" and not rising and nf >= count) or
+              (kind not in ("RISE", "FALL") and nc >= count))
+        if not ok:
+            continue
+        res_t = tw
+        if f is not None:
+            res_f = f[k] if abs(cv - val) < MINVAL else f[k] - (t[k] - tw) * (f[k] - f[k - 1]) / (t[k] - t[k - 1])
+        if count >= 0:
+            break
+    return res_t, res_f
+
+
+def evaluate_measure(m: Measure, t: np.ndarray, cols: dict) -> float:
+    """One .MEASURE from the columns of its variables at the accepted points;
+    NaN when it fails (written FAILED)."""
+    if m.func == "TRIGTARG":
+        tr, tg = m.spec["trig"], m.spec["targ"]
+        t1 = _rfc_event_time(t, cols[tr["var"]], tr["val"], tr["rfc"], tr["td"])
+        t2 = _rfc_event_time(t, cols[tg["var"]], tg["val"], tg["rfc"], tg["td"])
+        return float(t2 - t1)
+    if m.func == "WHEN":
+        return float(_when(t, cols[m.var], None, m.spec["when"])[0])
+    if m.func == "FIND":
+        if "at" in m.spec:
+            at = m.spec["at"]
+            if len(t) == 0 or at < t[0] or at > t[-1]:
+                return float("nan")
+            return float(np.interp(at, t, cols[m.var]))
+        w = m.spec["when"]
+        return float(_when(t, cols[w["var"]], cols[m.var], w)[1])
+    return measure(m.func, t, cols[m.var], m.frm, m.to)
+
+
 def measure(func: str, t: np.ndarray, v: np.ndarray, frm=None, to=None) -> float:
     """One .MEASURE over the accepted points inside [frm, to]."""
     sel = np.ones(len(t), bool)
@@ -1093,7 +1280,7 @@ def run(deck: Deck, device: int = 0, cap: int | None = None) -> Result:
     .MEASURE variable at the accepted time points."""
     from . import Circuit
     nl = deck.netlist
-    wanted = list(dict.fromkeys(deck.prints + [m.var for m in deck.measures]))
+    wanted = list(dict.fromkeys(deck.prints + [v for m in deck.measures for v in m.vars]))
     plan = {}
     probes: list[int] = []
     for var in wanted:
