@@ -1,0 +1,81 @@
+"""Physical invariants of every nonlinear device's load, checked on the
+oracle with the device alone in a netlist (so F, Q and the Jacobians hold
+its stamps only).  They hold for the reference's models by construction and
+do not depend on how this build restates them:
+  * Kirchhoff: the terminal currents (F) and terminal charges (Q) sum to
+    zero (BSIM4's charge model is charge-conserving: the source charge is
+    minus the sum of the others, N_DEV_MOSFET_B4p82.C);
+  * conservation under perturbation: every column of dFdx and dQdx sums to
+    zero;
+  * only voltage differences matter: every row of dFdx and dQdx sums to
+    zero.
+The GPU stamps equal the oracle's to 1e-12 (tests/test_gpu_parity.py), so
+the invariants carry over to the kernels."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from xyce_gb300 import netlist as N
+
+REL = 1e-9
+
+
+def _settled_load(o, x):
+    """A load at x whose junction history is x itself (no limiting)."""
+    z = np.zeros(max(1, o.nsta))
+    base = o.load(x, sta_curr=z, sto_curr=np.zeros(max(1, o.nsto)), newton_iter=0)
+    sta, sto = base["sta_next"], base["sto_next"]
+    for _ in range(200):
+        nxt = o.load(x, sta_curr=sta, sto_curr=sto, sto_prev=sto, newton_iter=1)
+        if np.array_equal(nxt["sto_next"], sto):
+            return nxt
+        sta, sto = nxt["sta_next"], nxt["sto_next"]
+    raise AssertionError("history did not settle")
+
+
+def _check(oracle_mod, nl, seed, lo, hi):
+    o = oracle_mod.Oracle(nl)
+    rng = np.random.default_rng(seed)
+    for _ in range(4):
+        x = rng.uniform(lo, hi, o.n)
+        ld = _settled_load(o, x)
+        for vec in ("F", "Q"):
+            v = ld[vec]
+            assert abs(v.sum()) <= REL * np.abs(v).max() + 1e-30, (nl.label, vec, v.sum(), np.abs(v).max())
+        for mat in ("dFdx", "dQdx"):
+            J = sp.csr_matrix((ld[mat], o.col_idx, o.row_ptr), shape=(o.n, o.n)).toarray()
+            scale = np.abs(J).max() + 1e-300
+            assert np.abs(J.sum(axis=0)).max() <= REL * scale, (nl.label, mat, "columns")
+            assert np.abs(J.sum(axis=1)).max() <= REL * scale, (nl.label, mat, "rows")
+
+
+def _alone(label, add):
+    nl = N.Netlist(label=label)
+    nodes = [nl.node(f"t{k}") for k in range(4)]
+    add(nl, nodes)
+    nl.tran = N.Tran(tstop=1e-9)
+    return nl
+
+
+@pytest.mark.parametrize("card", ["nmos", "pmos"])
+def test_bsim4_conserves(oracle_mod, card):
+    c = N.B4_NMOS if card == "nmos" else N.B4_PMOS
+    nl = _alone(f"b4_{card}", lambda nl, t: nl.M4(t[0], t[1], t[2], t[3], **c))
+    _check(oracle_mod, nl, 1, -0.3, 1.2)
+
+
+@pytest.mark.parametrize("series", [False, True])
+def test_mosfet1_conserves(oracle_mod, series):
+    card = dict(N.NMOS_CARD, TOX=4e-9, CGSO=2e-10, CGDO=2e-10, CGBO=1e-10, CJ=1e-3, CJSW=2e-10, AD=1e-12,
+                AS=1e-12, PD=4e-6, PS=4e-6, GAMMA=0.4, LAMBDA=0.05, PHI=0.7)
+    if series:
+        card.update(RD=300.0, RSH=20.0, NRS=2.0, M=2.0)
+    nl = _alone("mos1", lambda nl, t: nl.M1(t[0], t[1], t[2], t[3], **card))
+    _check(oracle_mod, nl, 2, -0.5, 2.0)
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_diode_conserves(oracle_mod, k):
+    card = N.SIDEWALL_DIODES[k]
+    nl = _alone(f"diode{k}", lambda nl, t: nl.D(t[0], t[1], **card))
+    _check(oracle_mod, nl, 3, -5.0, 1.0)
