@@ -79,3 +79,36 @@ def test_diode_conserves(oracle_mod, k):
     card = N.SIDEWALL_DIODES[k]
     nl = _alone(f"diode{k}", lambda nl, t: nl.D(t[0], t[1], **card))
     _check(oracle_mod, nl, 3, -5.0, 1.0)
+
+
+@pytest.mark.parametrize("model", ["b4_nmos", "b4_pmos", "mos1"])
+def test_source_drain_symmetry(oracle_mod, model):
+    """A MOSFET with symmetric geometry is symmetric in drain and source:
+    swapping the two terminal voltages swaps their currents and charges and
+    leaves the gate's and the bulk's unchanged (the reverse mode of the
+    reference's models, e.g. N_DEV_MOSFET_B4p82.C's mode = -1 branch).
+    MOSFET-1's Meyer charges are incremental (the stored charge plus
+    C * the change of voltage since the stored state), so they depend on
+    the history and only its currents are compared."""
+    if model == "mos1":
+        card = dict(N.NMOS_CARD, TOX=4e-9, CGSO=2e-10, CGDO=2e-10, CJ=1e-3, CJSW=2e-10, AD=1e-12, AS=1e-12,
+                    PD=4e-6, PS=4e-6, GAMMA=0.4, LAMBDA=0.05, PHI=0.7)
+        nl = _alone("mos1", lambda nl, t: nl.M1(t[0], t[1], t[2], t[3], **card))
+    else:
+        c = dict(N.B4_NMOS if model == "b4_nmos" else N.B4_PMOS)
+        c.update(AS=2e-14, AD=2e-14, PS=6e-7, PD=6e-7)
+        nl = _alone(model, lambda nl, t: nl.M4(t[0], t[1], t[2], t[3], **c))
+    o = oracle_mod.Oracle(nl)
+    d, g, s, b = (nl.names[f"t{k}"] for k in range(4))
+    rng = np.random.default_rng(5)
+    sign = -1.0 if model == "b4_pmos" else 1.0
+    for _ in range(4):
+        x = sign * rng.uniform(-0.2, 1.2, o.n)
+        y = x.copy()
+        y[d], y[s] = x[s], x[d]
+        a, r = _settled_load(o, x), _settled_load(o, y)
+        for vec in (("F",) if model == "mos1" else ("F", "Q")):
+            va, vr = a[vec], r[vec]
+            tol = REL * np.abs(va).max() + 1e-30
+            assert abs(vr[d] - va[s]) <= tol and abs(vr[s] - va[d]) <= tol, (model, vec)
+            assert abs(vr[g] - va[g]) <= tol and abs(vr[b] - va[b]) <= tol, (model, vec)
