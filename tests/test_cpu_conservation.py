@@ -112,3 +112,42 @@ def test_source_drain_symmetry(oracle_mod, model):
             tol = REL * np.abs(va).max() + 1e-30
             assert abs(vr[d] - va[s]) <= tol and abs(vr[s] - va[d]) <= tol, (model, vec)
             assert abs(vr[g] - va[g]) <= tol and abs(vr[b] - va[b]) <= tol, (model, vec)
+
+
+def test_bsim4_textbook_behaviour(oracle_mod):
+    """The 45 nm-like NMOS card shows the behaviours every MOSFET model has:
+    an exponential subthreshold region no steeper than the thermal limit
+    (kT/q ln 10 = 59.6 mV/decade at 300 K), drain-induced barrier lowering
+    (more subthreshold current at high Vds), the body effect (less current
+    with reverse body bias) and saturation (output conductance far below
+    the linear region's).  The body effect is checked on a 1 um channel:
+    with the card's default short-channel parameters the 45 nm device's
+    current rises with reverse body bias (the depletion width, and with it
+    the short-channel threshold roll-off and ETAB's DIBL, grow with it)."""
+    nl = _alone("b4_textbook", lambda nl, t: nl.M4(t[0], t[1], t[2], t[3], **N.B4_NMOS))
+    o = oracle_mod.Oracle(nl)
+    d, g, s, b = (nl.names[f"t{k}"] for k in range(4))
+
+    def ids(vg, vd, vb=0.0):
+        x = np.zeros(o.n)
+        x[d], x[g], x[b] = vd, vg, vb
+        return _settled_load(o, x)["F"][d]
+
+    sub = np.array([ids(vg, 1.0) for vg in (0.0, 0.05, 0.10, 0.15)])
+    assert np.all(sub > 0)
+    swing = 0.05 / np.diff(np.log10(sub))  # volts per decade
+    vt = 1.3806226e-23 * 300.15 / 1.6021918e-19
+    assert np.all(swing > vt * np.log(10) * 0.999) and np.all(swing < 0.15), swing
+    assert np.max(swing) / np.min(swing) < 1.2, swing  # exponential: a steady slope
+    assert ids(0.1, 1.0) > 2.0 * ids(0.1, 0.05)  # DIBL
+    long_ch = _alone("b4_long", lambda nl, t: nl.M4(t[0], t[1], t[2], t[3], **dict(N.B4_NMOS, L=1e-6, W=2e-6)))
+    ol = oracle_mod.Oracle(long_ch)
+
+    def ids_long(vb):
+        x = np.zeros(ol.n)
+        x[d], x[g], x[b] = 1.0, 0.6, vb
+        return _settled_load(ol, x)["F"][d]
+    assert ids_long(-0.5) < ids_long(-0.2) < ids_long(0.0)  # body effect
+    g_lin = (ids(1.0, 0.06) - ids(1.0, 0.04)) / 0.02
+    g_sat = (ids(1.0, 1.0) - ids(1.0, 0.9)) / 0.1
+    assert 0 < g_sat < 0.2 * g_lin, (g_sat, g_lin)
