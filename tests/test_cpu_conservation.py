@@ -143,11 +143,15 @@ def test_bsim4_textbook_behaviour(oracle_mod):
     long_ch = _alone("b4_long", lambda nl, t: nl.M4(t[0], t[1], t[2], t[3], **dict(N.B4_NMOS, L=1e-6, W=2e-6)))
     ol = oracle_mod.Oracle(long_ch)
 
-    def ids_long(vb):
+    def ids_long(vg, vd, vb=0.0):
         x = np.zeros(ol.n)
-        x[d], x[g], x[b] = 1.0, 0.6, vb
+        x[d], x[g], x[b] = vd, vg, vb
         return _settled_load(ol, x)["F"][d]
-    assert ids_long(-0.5) < ids_long(-0.2) < ids_long(0.0)  # body effect
-    g_lin = (ids(1.0, 0.06) - ids(1.0, 0.04)) / 0.02
-    g_sat = (ids(1.0, 1.0) - ids(1.0, 0.9)) / 0.1
-    assert 0 < g_sat < 0.2 * g_lin, (g_sat, g_lin)
+    assert ids_long(0.6, 1.0, -0.5) < ids_long(0.6, 1.0, -0.2) < ids_long(0.6, 1.0)  # body effect
+    # saturation: the output conductance is well below the linear region's,
+    # by a large factor on the long channel (short channels keep a sizeable
+    # one from channel-length modulation and DIBL)
+    for f, bound in ((ids_long, 0.2), (ids, 0.5)):
+        g_lin = (f(1.0, 0.06) - f(1.0, 0.04)) / 0.02
+        g_sat = (f(1.0, 1.0) - f(1.0, 0.9)) / 0.1
+        assert 0 < g_sat < bound * g_lin, (g_sat, g_lin)
