@@ -156,6 +156,11 @@ int xg_add_capacitors(xg_ctx *ctx, int n, const int *pos, const int *neg, const 
  * Waveform k is kind[k] with data[off[k] .. off[k+1]). */
 int xg_add_vsources(xg_ctx *ctx, int n, const int *pos, const int *neg, const int *branch,
                     const int *kind, const int *off, const double *data);
+/* Inductor::Instance (N_DEV_Inductor.C:540-650), without IC: branch is the
+ * unknown carrying its current (as a voltage source's); l in henry.  The
+ * stamps are constant and load with the linear part. */
+int xg_add_inductors(xg_ctx *ctx, int n, const int *pos, const int *neg, const int *branch,
+                     const double *l);
 /* ISRC::Instance (N_DEV_ISRC.C). */
 int xg_add_isources(xg_ctx *ctx, int n, const int *pos, const int *neg,
                     const int *kind, const int *off, const double *data);

@@ -66,6 +66,7 @@ def lib():
         L.orc_add_capacitors.argtypes = [P, C.c_int, ip, ip, dp]
         L.orc_add_vsources.argtypes = [P, C.c_int, ip, ip, ip, ip, ip, dp]
         L.orc_add_isources.argtypes = [P, C.c_int, ip, ip, ip, ip, dp]
+        L.orc_add_inductors.argtypes = [P, C.c_int, ip, ip, ip, dp]
         L.orc_add_diodes.argtypes = [P, C.c_int, ip, ip, ip, dp]
         L.orc_add_mosfet1.argtypes = [P, C.c_int, ip, ip, ip, ip, ip, ip, dp]
         L.orc_add_bsim4.argtypes = [P, C.c_int, ip, ip, ip, ip, dp]
@@ -105,6 +106,9 @@ class Oracle:
         L.orc_add_vsources(self.h, len(p), p, m, b, k, o, d)
         p, m, k, o, d = a["isrc"]
         L.orc_add_isources(self.h, len(p), p, m, k, o, d)
+        p, m, b, lv = a["ind"]
+        if len(p):
+            L.orc_add_inductors(self.h, len(p), p, m, b, lv)
         p, m, r, prm = a["diode"]
         L.orc_add_diodes(self.h, len(p), p, m, r, prm)
         dd, g, s, b, dpr, spr, prm = a["mos1"]

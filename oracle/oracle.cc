@@ -213,6 +213,7 @@ struct orc_ctx {
   std::vector<int> r_p, r_n; std::vector<double> r_g;
   std::vector<int> c_p, c_n; std::vector<double> c_c;
   std::vector<int> v_p, v_n, v_b; std::vector<Wave> v_w;
+  std::vector<int> l_p, l_n, l_b; std::vector<double> l_l;  // inductors
   std::vector<int> i_p, i_n; std::vector<Wave> i_w;
   std::vector<int> d_p, d_n, d_pri; std::vector<DiodeT> d_t;
   std::vector<int> m_d, m_g, m_s, m_b, m_dp, m_sp; std::vector<Mos1T> m_t;
@@ -220,7 +221,7 @@ struct orc_ctx {
   std::vector<double> b_von;  // BSIM4 instance member von (last evaluation's Vth)
   // pattern (CSR) and per-device stamp positions
   std::vector<int> rp, ci;
-  std::vector<int> pos_r, pos_c, pos_v, pos_d, pos_m, pos_b;
+  std::vector<int> pos_r, pos_c, pos_v, pos_l, pos_d, pos_m, pos_b;
   // CSC view for the LU, of P A P^T when an elimination order q is set
   // (q[k] = the unknown eliminated k-th; empty = the natural order)
   std::vector<int> Ap, Ai, csr2csc;
@@ -285,6 +286,12 @@ void stamp_pairs(orc_ctx *c, std::vector<std::pair<int, int>> &all) {
     int p = c->v_p[k], n = c->v_n[k], b = c->v_b[k];
     all.push_back({p, b}); all.push_back({n, b}); all.push_back({b, p}); all.push_back({b, n});
   }
+  // Inductor (N_DEV_Inductor.C:606-650): (p,b)(n,b)(b,p)(b,n)(b,b)
+  for (size_t k = 0; k < c->l_p.size(); ++k) {
+    int p = c->l_p[k], n = c->l_n[k], b = c->l_b[k];
+    all.push_back({p, b}); all.push_back({n, b}); all.push_back({b, p}); all.push_back({b, n});
+    all.push_back({b, b});
+  }
   for (size_t k = 0; k < c->d_p.size(); ++k) {
     int P = c->d_p[k], N = c->d_n[k], R = c->d_pri[k];
     all.push_back({P, P}); all.push_back({P, R}); all.push_back({N, N}); all.push_back({N, R});
@@ -337,6 +344,12 @@ int orc_add_vsources(orc_ctx *c, int n, const int *p, const int *m, const int *b
     c->v_p.push_back(p[k]); c->v_n.push_back(m[k]); c->v_b.push_back(b[k]);
     Wave w; w.kind = kind[k]; w.d.assign(data + off[k], data + off[k + 1]);
     c->v_w.push_back(w);
+  }
+  return 0;
+}
+int orc_add_inductors(orc_ctx *c, int n, const int *p, const int *m, const int *b, const double *l) {
+  for (int k = 0; k < n; ++k) {
+    c->l_p.push_back(p[k]); c->l_n.push_back(m[k]); c->l_b.push_back(b[k]); c->l_l.push_back(l[k]);
   }
   return 0;
 }
@@ -426,6 +439,7 @@ int orc_finalize(orc_ctx *c) {
   // branch unknowns of voltage sources have none, as in the device stamps
   c->is_branch.assign(c->n, 0);
   for (int b : c->v_b) c->is_branch[b] = 1;
+  for (int b : c->l_b) c->is_branch[b] = 1;
   for (int i = 0; i < c->n; ++i)
     if (!c->is_branch[i]) rows[i].push_back(i);
   c->rp.assign(c->n + 1, 0);
@@ -444,6 +458,7 @@ int orc_finalize(orc_ctx *c) {
   fill(c->pos_r, o, 4 * c->r_p.size()); o += 4 * c->r_p.size();
   fill(c->pos_c, o, 4 * c->c_p.size()); o += 4 * c->c_p.size();
   fill(c->pos_v, o, 4 * c->v_p.size()); o += 4 * c->v_p.size();
+  fill(c->pos_l, o, 5 * c->l_p.size()); o += 5 * c->l_p.size();
   fill(c->pos_d, o, 7 * c->d_p.size()); o += 7 * c->d_p.size();
   fill(c->pos_m, o, 22 * c->m_d.size()); o += 22 * c->m_d.size();
   fill(c->pos_b, o, 16 * c->b_d.size()); o += 16 * c->b_d.size();
@@ -506,6 +521,17 @@ int orc_load(orc_ctx *c, double time, const double *x, const double *sta_curr, c
     addv(B, b, wave_value(c->v_w[k], time));
     const int *ps = &c->pos_v[4 * k];
     addm(dFdx, ps[0], 1.0); addm(dFdx, ps[1], -1.0); addm(dFdx, ps[2], 1.0); addm(dFdx, ps[3], -1.0);
+  }
+  // Inductor, N_DEV_Inductor.C:540-650 (no IC): F[p] += i, F[n] -= i,
+  // F[b] -= v(p) - v(n), Q[b] = L i
+  for (size_t k = 0; k < c->l_p.size(); ++k) {
+    int p = c->l_p[k], m = c->l_n[k], b = c->l_b[k];
+    double ib = x[b];
+    addv(F, p, ib); addv(F, m, -ib); addv(F, b, -(X(p) - X(m)));
+    addv(Q, b, c->l_l[k] * ib);
+    const int *ps = &c->pos_l[5 * k];
+    addm(dFdx, ps[0], 1.0); addm(dFdx, ps[1], -1.0); addm(dFdx, ps[2], -1.0); addm(dFdx, ps[3], 1.0);
+    addm(dQdx, ps[4], c->l_l[k]);
   }
   // ISRC, N_DEV_ISRC.C:1108-1172
   for (size_t k = 0; k < c->i_p.size(); ++k) {

@@ -47,6 +47,8 @@ int orc_add_resistors(orc_ctx *c, int n, const int *pos, const int *neg, const d
 int orc_add_capacitors(orc_ctx *c, int n, const int *pos, const int *neg, const double *cap);
 int orc_add_vsources(orc_ctx *c, int n, const int *pos, const int *neg, const int *branch,
                      const int *kind, const int *off, const double *data);
+/* Inductor (N_DEV_Inductor.C): branch b carries the current; l in henry. */
+int orc_add_inductors(orc_ctx *c, int n, const int *p, const int *m, const int *b, const double *l);
 int orc_add_isources(orc_ctx *c, int n, const int *pos, const int *neg,
                      const int *kind, const int *off, const double *data);
 int orc_add_diodes(orc_ctx *c, int n, const int *pos, const int *neg, const int *pri,

@@ -88,6 +88,7 @@ def _fd_check(oracle_mod, nl, rng, dcop, shift=0.0):
                                    lambda: N.ring_oscillator(5),
                                    lambda: N.ring_oscillator(5, caps=True),
                                    lambda: N.ring_oscillator(5, series=True),
+                                   lambda: N.rlc_ladder(6, seed=2),
                                    lambda: N.ring_oscillator(5, caps=True, series=True),
                                    lambda: N.bsim4_inverter_chain(2),
                                    lambda: N.bsim4_logic_dag(60, 4, seed=2, tstop=0.3e-9),
@@ -208,6 +209,25 @@ def test_diode_sidewall_iv_point(oracle_mod, ns):
 
 
 KB, QE, TREF = 1.3806226e-23, 1.6021918e-19, 300.15
+
+
+def test_rl_step_response(oracle_mod):
+    """Inductor (N_DEV_Inductor.C): a 1 V step through R into L gives
+    i(t) = (V/R)(1 - exp(-t R/L)); at DC the inductor is a short."""
+    nl = N.Netlist(label="rl")
+    a, k = nl.node("a"), nl.node("k")
+    nl.V(a, -1, N.WAVE_PULSE, [0.0, 1.0, 0.0, 1e-12, 1e-12, 1.0, 2.0])
+    nl.R(a, k, 100.0)
+    br = nl.L(k, -1, 1e-6)
+    nl.tran = N.Tran(tstop=50e-9, hmax=0.2e-9, reltol=1e-4)
+    t, v, st = oracle_mod.Oracle(nl).transient(probes=[br, k])
+    assert st["status"] == 0
+    tau = 1e-6 / 100.0
+    ref = 0.01 * (1.0 - np.exp(-np.maximum(t - 1e-12, 0.0) / tau))
+    assert np.max(np.abs(v[:, 0] - ref)) < 2e-3 * 0.01
+    # the inductor's voltage is L di/dt = V exp(-t/tau)
+    late = t > 5e-9
+    np.testing.assert_allclose(v[late, 1], np.exp(-(t[late] - 1e-12) / tau), rtol=0, atol=5e-3)
 
 
 def test_diode_temperature_dc_point(oracle_mod):

@@ -317,6 +317,16 @@ M1 a a 0 0 n1 W=1u L=1u
                 ".TRAN 1p 10p\n.END\n")
 
 
+def test_inductor_element():
+    d = S.parse("rl\nV1 a 0 PULSE(0 1 0 1p 1p 1 2)\nR1 a b 100\nL1 b 0 1u\n.PRINT TRAN I(L1) V(b)\n"
+                ".TRAN 1n 50n\n.END\n")
+    nl = d.netlist
+    assert len(nl.ind) == 1 and nl.ind[0][3] == 1e-6 and d.branches["L1"] == nl.ind[0][2]
+    assert d.element_values["L1"] == 1e-6
+    with pytest.raises(ValueError):
+        S.parse("rl\nV1 a 0 1\nL1 a 0 1u IC=1m\n.TRAN 1n 50n\n.END\n")
+
+
 def test_bsim4_model_card_and_instance():
     d = S.parse("""bsim4 inverter
 .MODEL n1 NMOS (LEVEL=54 VERSION=4.8.2 TOXE=1.8n VTH0=0.4)

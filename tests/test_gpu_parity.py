@@ -109,6 +109,7 @@ def _loader_case(xg, oracle_mod, torch, nl, seed, newton_iter, dcop, init_jct, c
     (lambda: N.at_temperature(N.ring_oscillator(11, caps=True, series=True), 100.0, 40.0), True),
     (lambda: N.monte_carlo_rings(3, 11, 21, seed=2), False),
     (lambda: N.power_grid(6, 5, seed=1), False),
+    (lambda: N.rlc_ladder(12, seed=3), False),
     (lambda: N.bsim4_inverter_chain(3), True),
     (lambda: N.bsim4_logic_dag(120, 6, seed=3, tstop=0.5e-9), True),
 ])
@@ -235,6 +236,7 @@ def _compare_waveforms(t_ref, v_ref, t_gpu, v_gpu):
     ("ring_21_caps", lambda: N.ring_oscillator(21, caps=True), ["n1", "n11"]),
     ("ring_11_caps_rs", lambda: _short(N.ring_oscillator(11, caps=True, series=True), 6e-9),
      ["n1", "n6", "n11"]),
+    ("rlc_ladder_20", lambda: N.rlc_ladder(20, seed=1), ["n1", "n10", "n20", "L5#branch"]),
     ("b4_chain_3", lambda: N.bsim4_inverter_chain(3), ["in", "n1", "n3"]),
     ("b4_dag_300", lambda: N.bsim4_logic_dag(300, 8, seed=4, tstop=1e-9), ["g10", "g40", "g70"]),
 ])

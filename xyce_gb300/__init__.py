@@ -45,7 +45,7 @@ FLAG_DCOP, FLAG_INITJCT = 1, 2
 EXPORTED = [
     "xg_create", "xg_destroy", "xg_error_string", "xg_get_stream", "xg_synchronize",
     "xg_set_unknowns", "xg_add_resistors", "xg_add_capacitors", "xg_add_vsources",
-    "xg_add_isources", "xg_add_diodes", "xg_add_mosfet1", "xg_add_mosfet1_rs", "xg_add_bsim4", "xg_finalize", "xg_get_sizes",
+    "xg_add_isources", "xg_add_diodes", "xg_add_mosfet1", "xg_add_mosfet1_rs", "xg_add_inductors", "xg_add_bsim4", "xg_finalize", "xg_get_sizes",
     "xg_get_pattern", "xg_update_sources", "xg_update_state", "xg_load_dae_vectors",
     "xg_load_dae_matrices", "xg_lu_analyze", "xg_lu_factor", "xg_lu_solve",
     "xg_lu_solve_noalloc", "xg_lu_set_precision", "xg_lu_info", "xg_lu_schedule_info", "xg_lu_set_schedule", "xg_lu_analyze_pattern",
@@ -137,6 +137,7 @@ def lib() -> C.CDLL:
     L.xg_add_capacitors.argtypes = [P, I, ip, ip, dp]
     L.xg_add_vsources.argtypes = [P, I, ip, ip, ip, ip, ip, dp]
     L.xg_add_isources.argtypes = [P, I, ip, ip, ip, ip, dp]
+    L.xg_add_inductors.argtypes = [P, I, ip, ip, ip, dp]
     L.xg_add_diodes.argtypes = [P, I, ip, ip, ip, dp]
     L.xg_add_mosfet1.argtypes = [P, I, ip, ip, ip, ip, dp]
     L.xg_add_mosfet1_rs.argtypes = [P, I, ip, ip, ip, ip, ip, ip, dp]
@@ -239,6 +240,9 @@ class Circuit:
         self._check(L.xg_add_vsources(self.h, len(p), p, m, b, k, o, d))
         p, m, k, o, d = a["isrc"]
         self._check(L.xg_add_isources(self.h, len(p), p, m, k, o, d))
+        p, m, b, lv = a["ind"]
+        if len(p):
+            self._check(L.xg_add_inductors(self.h, len(p), p, m, b, lv))
         p, m, r, prm = a["diode"]
         self._check(L.xg_add_diodes(self.h, len(p), p, m, r, prm))
         dd, g, s, b, dpr, spr, prm = a["mos1"]

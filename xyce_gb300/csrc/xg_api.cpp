@@ -38,6 +38,9 @@ struct xg_ctx {
   // sourceConductance * M between s and s'): constant, in the linear part
   std::vector<int> sg_p, sg_n;
   std::vector<double> sg_v;
+  // inductors: pos, neg, branch current unknown, inductance (all constant)
+  std::vector<int> ind_p, ind_n, ind_b;
+  std::vector<double> ind_l;
   std::vector<double> r_v, c_v;
   std::vector<Wave> v_w, i_w;
   std::vector<int> d_p, d_n, d_r;
@@ -245,6 +248,20 @@ int xg_add_resistors(xg_ctx *ctx, int n, const int *pos, const int *neg, const d
   return XG_OK;
 }
 
+int xg_add_inductors(xg_ctx *ctx, int n, const int *pos, const int *neg, const int *branch, const double *l) {
+  SETUP_CHECK(pos, neg, branch, l);
+  for (int k = 0; k < n; ++k) {
+    if (!valid_node(ctx, pos[k]) || !valid_node(ctx, neg[k]) || branch[k] < 0 || branch[k] >= ctx->n)
+      return fail(ctx, XG_ERR_ARG, "inductor node or branch out of range");
+    if (!std::isfinite(l[k])) return fail(ctx, XG_ERR_ARG, "inductance must be finite");
+  }
+  ctx->ind_p.insert(ctx->ind_p.end(), pos, pos + n);
+  ctx->ind_n.insert(ctx->ind_n.end(), neg, neg + n);
+  ctx->ind_b.insert(ctx->ind_b.end(), branch, branch + n);
+  ctx->ind_l.insert(ctx->ind_l.end(), l, l + n);
+  return XG_OK;
+}
+
 int xg_add_capacitors(xg_ctx *ctx, int n, const int *pos, const int *neg, const double *cv) {
   SETUP_CHECK(pos, neg, cv);
   for (int k = 0; k < n; ++k) {
@@ -437,6 +454,8 @@ int xg_finalize(xg_ctx *ctx) {
     if (!same_circuit({ctx->r_p[k], ctx->r_n[k]})) return fail(ctx, XG_ERR_ARG, "resistor spans two circuits");
   for (size_t k = 0; k < ctx->sg_p.size(); ++k)
     if (!same_circuit({ctx->sg_p[k], ctx->sg_n[k]})) return fail(ctx, XG_ERR_ARG, "MOSFET spans two circuits");
+  for (size_t k = 0; k < ctx->ind_p.size(); ++k)
+    if (!same_circuit({ctx->ind_p[k], ctx->ind_n[k], ctx->ind_b[k]})) return fail(ctx, XG_ERR_ARG, "inductor spans two circuits");
   for (size_t k = 0; k < ctx->c_p.size(); ++k)
     if (!same_circuit({ctx->c_p[k], ctx->c_n[k]})) return fail(ctx, XG_ERR_ARG, "capacitor spans two circuits");
   for (int k = 0; k < nv; ++k)
@@ -451,6 +470,10 @@ int xg_finalize(xg_ctx *ctx) {
       if (seen[ctx->v_b[k]]) return fail(ctx, XG_ERR_ARG, "two voltage sources share a branch unknown");
       seen[ctx->v_b[k]] = 1;
     }
+    for (size_t k = 0; k < ctx->ind_b.size(); ++k) {
+      if (seen[ctx->ind_b[k]]) return fail(ctx, XG_ERR_ARG, "an inductor's branch unknown is shared");
+      seen[ctx->ind_b[k]] = 1;
+    }
   }
   // matrix stamp positions (row, col); -1 for ground rows/cols.  Every
   // position is enumerated twice (count, then fill) into one flat array, and
@@ -459,6 +482,7 @@ int xg_finalize(xg_ctx *ctx) {
   // branch rows have none, as in the device stamps.
   std::vector<char> is_branch(n, 0);
   for (int k = 0; k < nv; ++k) is_branch[ctx->v_b[k]] = 1;
+  for (int b : ctx->ind_b) is_branch[b] = 1;
   const int dpair[7][2] = {{0, 0}, {0, 2}, {1, 1}, {1, 2}, {2, 0}, {2, 1}, {2, 2}};
   auto for_positions = [&](auto &&emit) {
     for (size_t k = 0; k < ctx->r_p.size(); ++k) {
@@ -476,6 +500,10 @@ int xg_finalize(xg_ctx *ctx) {
     for (int k = 0; k < nv; ++k) {
       int p = ctx->v_p[k], m = ctx->v_n[k], b = ctx->v_b[k];
       emit(p, b); emit(m, b); emit(b, p); emit(b, m);
+    }
+    for (size_t k = 0; k < ctx->ind_p.size(); ++k) {
+      int p = ctx->ind_p[k], m = ctx->ind_n[k], b = ctx->ind_b[k];
+      emit(p, b); emit(m, b); emit(b, p); emit(b, m); emit(b, b);
     }
     for (int k = 0; k < nd; ++k) {
       int nn[3] = {ctx->d_p[k], ctx->d_n[k], ctx->d_r[k]};
@@ -543,6 +571,13 @@ int xg_finalize(xg_ctx *ctx) {
   for (int k = 0; k < nv; ++k) {
     int p = ctx->v_p[k], m = ctx->v_n[k], b = ctx->v_b[k];
     addv(Glin, p, b, 1.0); addv(Glin, m, b, -1.0); addv(Glin, b, p, 1.0); addv(Glin, b, m, -1.0);
+  }
+  // inductors (N_DEV_Inductor.C:540-650): F[p] += i, F[n] -= i,
+  // F[b] -= v(p) - v(n), Q[b] = L i
+  for (size_t k = 0; k < ctx->ind_p.size(); ++k) {
+    int p = ctx->ind_p[k], m = ctx->ind_n[k], b = ctx->ind_b[k];
+    addv(Glin, p, b, 1.0); addv(Glin, m, b, -1.0); addv(Glin, b, p, -1.0); addv(Glin, b, m, 1.0);
+    addv(Clin, b, b, ctx->ind_l[k]);
   }
   // slot layout: MOSFET level 1, then BSIM4 (same slot counts), then
   // diodes, plane-major within a type

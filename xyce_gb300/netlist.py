@@ -157,8 +157,9 @@ class Netlist:
     cap: list = field(default_factory=list)      # (p, n, C)
     vsrc: list = field(default_factory=list)     # (p, n, branch, kind, data)
     isrc: list = field(default_factory=list)     # (p, n, kind, data)
+    ind: list = field(default_factory=list)      # (p, n, branch, L)
     diode: list = field(default_factory=list)    # (p, n, pri, row)
-    mos1: list = field(default_factory=list)     # (d, g, s, b, row)
+    mos1: list = field(default_factory=list)     # (d, g, s, b, row, d', s')
     bsim4: list = field(default_factory=list)    # (d, g, s, b, row)
     names: dict = field(default_factory=dict)
     tran: Tran | None = None
@@ -186,6 +187,12 @@ class Netlist:
     def V(self, a, b, kind, data, name=None):
         br = self.node(name)
         self.vsrc.append((a, b, br, kind, [float(x) for x in data]))
+        return br
+
+    def L(self, a, b, value, name=None):
+        """Inductor (henry); its branch current is a new unknown, returned."""
+        br = self.node(name)
+        self.ind.append((a, b, br, float(value)))
         return br
 
     def I(self, a, b, kind, data):
@@ -237,6 +244,8 @@ class Netlist:
                        i32([v[2] for v in self.vsrc]), vk, vo, vd)
         ik, io, idat = waves(self.isrc, 2, 3)
         out["isrc"] = (i32([v[0] for v in self.isrc]), i32([v[1] for v in self.isrc]), ik, io, idat)
+        out["ind"] = (i32([v[0] for v in self.ind]), i32([v[1] for v in self.ind]), i32([v[2] for v in self.ind]),
+                      f64([v[3] for v in self.ind]))
         out["diode"] = (i32([d[0] for d in self.diode]), i32([d[1] for d in self.diode]),
                         i32([d[2] for d in self.diode]),
                         f64(np.array([d[3] for d in self.diode]).reshape(-1, len(DIODE_FIELDS))))
@@ -260,7 +269,7 @@ class Netlist:
         return int(np.searchsorted(self.offsets, u, side="right") - 1)
 
     def device_count(self) -> int:
-        return len(self.res) + len(self.cap) + len(self.vsrc) + len(self.isrc) + \
+        return len(self.res) + len(self.cap) + len(self.vsrc) + len(self.isrc) + len(self.ind) + \
             len(self.diode) + len(self.mos1) + len(self.bsim4)
 
 
@@ -398,6 +407,27 @@ def ring_oscillator(stages=101, caps=False, series=False) -> Netlist:
     return nl
 
 
+def rlc_ladder(n=20, seed=1) -> Netlist:
+    """A driven RLC ladder: node 1 driven by PULSE(0 1 0.1n 0.1n 0.1n 5n 10n)
+    through 50 ohm, then n sections of a series inductor L ~ U[1,3] nH into
+    a shunt capacitor C ~ U[0.5,2] pF with a 1 kohm shunt; .TRAN 0 20n,
+    max step 20 ps."""
+    rng = np.random.default_rng(seed)
+    nl = Netlist(label=f"rlc_ladder_{n}")
+    src, first = nl.node("src"), nl.node("n0")
+    nl.V(src, -1, WAVE_PULSE, [0.0, 1.0, 0.1e-9, 0.1e-9, 0.1e-9, 5e-9, 10e-9], name="V1#branch")
+    nl.R(src, first, 50.0)
+    prev = first
+    for i in range(n):
+        node = nl.node(f"n{i + 1}")
+        nl.L(prev, node, rng.uniform(1e-9, 3e-9), name=f"L{i + 1}#branch")
+        nl.C(node, -1, rng.uniform(0.5e-12, 2e-12))
+        nl.R(node, -1, 1e3)
+        prev = node
+    nl.tran = Tran(tstop=20e-9, hmax=20e-12)
+    return nl
+
+
 def power_grid(k=500, n_sinks=2000, seed=3) -> Netlist:
     """k x k resistive mesh, R ~ U[0.05,0.2] ohm, decaps ~ U[1,10] fF, n_sinks
     seed-placed PWL current sinks ramping to U[0,5] mA over 100 ps windows,
@@ -471,6 +501,7 @@ def batch(nls: list, label: str = "batch") -> Netlist:
         out.cap += [(sh(a), sh(b), c) for (a, b, c) in nl.cap]
         out.vsrc += [(sh(a), sh(b), sh(br), kd, list(d)) for (a, b, br, kd, d) in nl.vsrc]
         out.isrc += [(sh(a), sh(b), kd, list(d)) for (a, b, kd, d) in nl.isrc]
+        out.ind += [(sh(a), sh(b), sh(br), lv) for (a, b, br, lv) in nl.ind]
         out.diode += [(sh(a), sh(b), sh(p), row) for (a, b, p, row) in nl.diode]
         out.mos1 += [(sh(d), sh(g), sh(s_), sh(b), row, sh(dp), sh(sp))
                      for (d, g, s_, b, row, dp, sp) in nl.mos1]
@@ -494,6 +525,7 @@ def extract_circuit(nl: Netlist, ci: int) -> Netlist:
     out.cap = [(rm(a), rm(b), c) for (a, b, c) in nl.cap if inside(a, b)]
     out.vsrc = [(rm(a), rm(b), rm(br), k, d) for (a, b, br, k, d) in nl.vsrc if inside(br)]
     out.isrc = [(rm(a), rm(b), k, d) for (a, b, k, d) in nl.isrc if inside(a, b)]
+    out.ind = [(rm(a), rm(b), rm(br), lv) for (a, b, br, lv) in nl.ind if inside(br)]
     out.diode = [(rm(a), rm(b), rm(r), row) for (a, b, r, row) in nl.diode if inside(a, b, r)]
     out.mos1 = [(rm(d), rm(g), rm(s), rm(b), row, rm(dp), rm(sp))
                 for (d, g, s, b, row, dp, sp) in nl.mos1 if inside(d, g, s, b)]

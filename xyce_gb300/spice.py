@@ -5,7 +5,7 @@ Lets a netlist written for the reference drive the device-resident
 transient (``Circuit.transient``) and produce the reference's tabular
 output.  The subset is what the path simulates:
 
-* elements ``R``, ``C``, ``V`` and ``I`` (DC, ``SIN``, ``PULSE``, ``PWL``),
+* elements ``R``, ``C``, ``L`` (no IC), ``V`` and ``I`` (DC, ``SIN``, ``PULSE``, ``PWL``),
   ``D`` (diode level 1), ``M`` (MOSFET level 1; level 54/14 = BSIM4 4.8.2),
   ``X`` (subcircuit instances, flattened);
 * ``.MODEL``, ``.SUBCKT``/``.ENDS``, ``.TRAN``, ``.OPTIONS TIMEINT``
@@ -275,6 +275,14 @@ class _Builder:
             a, b, v = nd(pos[0]), nd(pos[1]), number(pos[2])
             v = self.overrides.get(name, v)
             (self.nl.R if letter == "R" else self.nl.C)(a, b, v)
+            self.deck.element_values[name] = v
+        elif letter == "L":
+            if len(pos) < 3:
+                raise ValueError(f"{name}: needs two nodes and a value")
+            if kv:
+                raise ValueError(f"{name}: inductor parameters {sorted(kv)} are not supported (no IC)")
+            v = self.overrides.get(name, number(pos[2]))
+            self.deck.branches[name] = self.nl.L(nd(pos[0]), nd(pos[1]), v, name=f"{name}#branch")
             self.deck.element_values[name] = v
         elif letter in "VI":
             if len(pos) < 2:
@@ -1136,7 +1144,7 @@ def _var_probes(deck: Deck, var: str) -> tuple[list[int], callable]:
     if m:
         src = m.group(1)
         if src not in deck.branches:
-            raise ValueError(f"{var}: only voltage-source currents are supported")
+            raise ValueError(f"{var}: only voltage-source and inductor currents are supported")
         br = deck.branches[src]
         return [br], lambda vals, br=br: vals[br]
     if var == "TEMP":
