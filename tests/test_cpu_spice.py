@@ -106,7 +106,7 @@ def test_subcircuit_flattening():
 
 
 @pytest.mark.parametrize("bad,msg", [
-    ("t\nL1 a 0 1n\n.TRAN 1n 1u\n.END\n", "not supported"),
+    ("t\nL1 a 0 1n\nL2 b 0 1n\nK1 L1 L2 0.5\n.TRAN 1n 1u\n.END\n", "not supported"),
     ("t\nM1 d g 0 0 m1\n.MODEL m1 NMOS (LEVEL=3)\n.TRAN 1n 1u\n.END\n", "level 3"),
     ("t\nM1 d g 0 0 m1\n.MODEL m1 NMOS (UO=600)\n.TRAN 1n 1u\n.END\n", "UO"),
     ("t\nR1 a 0 1\n.END\n", ".TRAN"),
