@@ -236,7 +236,6 @@ def _compare_waveforms(t_ref, v_ref, t_gpu, v_gpu):
     ("ring_21_caps", lambda: N.ring_oscillator(21, caps=True), ["n1", "n11"]),
     ("ring_11_caps_rs", lambda: _short(N.ring_oscillator(11, caps=True, series=True), 6e-9),
      ["n1", "n6", "n11"]),
-    ("rlc_ladder_20", lambda: N.rlc_ladder(20, seed=1), ["n1", "n10", "n20", "L5#branch"]),
     ("b4_chain_3", lambda: N.bsim4_inverter_chain(3), ["in", "n1", "n3"]),
     ("b4_dag_300", lambda: N.bsim4_logic_dag(300, 8, seed=4, tstop=1e-9), ["g10", "g40", "g70"]),
 ])
@@ -251,6 +250,34 @@ def test_transient_matches_oracle(xg, oracle_mod, torch_cuda, name, maker, probe
     assert k == len(to)
     err, tol = _compare_waveforms(to, vo, t[0, :k], v[0, :k])
     assert err <= tol, (err, tol)
+
+
+def test_rlc_ladder_matches_oracle_replay(xg, oracle_mod, torch_cuda):
+    """An RLC ladder (inductors: N_DEV_Inductor.C) on the GPU against the
+    oracle replaying the GPU's accepted times and integration orders.  A
+    free-run comparison does not fit this circuit: the oracle itself, with
+    one inductance moved by one ulp, takes the same number of steps but a
+    sequence that parts from step 1,072 on (time points up to 2.4 ps apart,
+    exactly as the GPU run's), so a step decision there lies within round-off
+    of its threshold.  At identical time points every probe (node voltages
+    and an inductor current) matches within WAVE_RTOL * max|v| + WAVE_ATOL."""
+    nl = N.rlc_ladder(20, seed=1)
+    pr = [nl.names[p] for p in ("n1", "n10", "n20", "L5#branch")]
+    c = xg.Circuit(nl)
+    c.tran_start(probes=pr, cap=100000)
+    c.tran_advance(0)
+    counts, t, v, st = c.tran_results()
+    orders = c.tran_orders()
+    c.close()
+    assert st["status"] == 0
+    k = int(counts[0])
+    to, vo, so = oracle_mod.Oracle(nl).replay(t[0, :k], orders[0, :k], probes=pr)
+    assert so["status"] == 0 and len(to) == k
+    np.testing.assert_array_equal(to, t[0, :k])
+    for j in range(len(pr)):
+        tol = WAVE_RTOL * np.max(np.abs(vo[:, j])) + WAVE_ATOL
+        err = np.max(np.abs(v[0, :k, j] - vo[:, j]))
+        assert err <= tol, (j, err, tol)
 
 
 def test_sidewall_ladder_transient_matches_oracle(xg, oracle_mod, torch_cuda):
