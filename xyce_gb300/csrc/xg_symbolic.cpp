@@ -478,7 +478,7 @@ double worst_exempt_ratio(const LUHost &H) {
 
 static int analyze_once(int n, const std::vector<int> &rp, const std::vector<int> &ci,
                         const std::vector<double> &vals, LUHost &out, std::string &err, int force_ordering,
-                        const std::vector<int> *keep_rows);
+                        const std::vector<int> *keep_rows, const std::vector<int> *force_order = nullptr);
 
 // The analysis, repaired where its static pivots fail.  The row matching
 // and the symmetric ordering pivot on the (matched) diagonal; elimination
@@ -488,8 +488,9 @@ static int analyze_once(int n, const std::vector<int> &rp, const std::vector<int
 // numeric factorization instead.  So when the trial factorization of the
 // analysis finds columns below the pivot threshold, the connected
 // components holding them are pivoted once by threshold partial pivoting in
-// the analysed order, and analysed again with those rows kept; the repair
-// is taken when its worst pivot is better.
+// the analysed order, and analysed again with those rows and that order
+// kept (the same elimination, so the same pivots); the repair is taken when
+// its worst pivot is better.
 int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &ci,
                     const std::vector<double> &vals, LUHost &out, std::string &err, int force_ordering,
                     const std::vector<int> *keep_rows) {
@@ -523,7 +524,7 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
     for (int j = 0; j < n; ++j) keep2[j] = scope[j] ? gp_rows[j] : cur_row[j];
     LUHost rep;
     std::string err2;
-    if (analyze_once(n, rp, ci, vals, rep, err2, force_ordering, &keep2) != XG_OK) return XG_OK;
+    if (analyze_once(n, rp, ci, vals, rep, err2, force_ordering, &keep2, &out.col_of_step) != XG_OK) return XG_OK;
     if (!(worst_exempt_ratio(rep) > worst)) return XG_OK;
     out = std::move(rep);
   }
@@ -532,7 +533,7 @@ int lu_analyze_host(int n, const std::vector<int> &rp, const std::vector<int> &c
 
 static int analyze_once(int n, const std::vector<int> &rp, const std::vector<int> &ci,
                         const std::vector<double> &vals, LUHost &out, std::string &err, int force_ordering,
-                    const std::vector<int> *keep_rows) {
+                        const std::vector<int> *keep_rows, const std::vector<int> *force_order) {
   out = LUHost();
   out.n = n;
   Csc A = to_csc(n, rp, ci);
@@ -666,6 +667,7 @@ static int analyze_once(int n, const std::vector<int> &rp, const std::vector<int
     out.ordering = (n_md * 2 > (int)core.size()) ? 1 : 0;  // the ordering of most of the core
   }
   for (auto it = back.rbegin(); it != back.rend(); ++it) order.push_back(*it);
+  if (force_order) order = *force_order;  // a repair keeps the order its pivots were chosen in
   if ((int)order.size() != n) {
     err = "ordering lost unknowns";
     return XG_ERR_STATE;
