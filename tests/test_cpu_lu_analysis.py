@@ -82,6 +82,16 @@ def test_cancelled_static_pivots_fall_back_to_partial_pivoting(probe, oracle_mod
     assert rc == 0 and ex == 0 and ra >= RUNTIME_PIVOT_TOL and err < 1e-12
 
 
+def test_fallback_keeps_the_order_it_pivoted_in(probe, oracle_mod, tmp_path):
+    """An RLC ladder's operating point (inductors are shorts: a branch row
+    with no diagonal): the static pivots leave columns below the threshold;
+    the fallback's rows, kept together with the order they were chosen in,
+    reproduce threshold partial pivoting, so no column stays exempt."""
+    o, init, conv, tran = _jacobians(oracle_mod, N.rlc_ladder(20, seed=1))
+    rc, ex, ra, rb, err = _run(probe, tmp_path, o.row_ptr, o.col_idx, conv)
+    assert rc == 0 and ex == 0 and ra >= 0.1 and err < 1e-12
+
+
 @pytest.mark.parametrize("maker", [lambda: N.ring_oscillator(31), lambda: N.ring_oscillator(21, caps=True),
                                    lambda: N.diode_ladder(40, seed=2), lambda: N.power_grid(8, 12, seed=3),
                                    lambda: N.bsim4_logic_dag(120, 6, seed=3, tstop=0.5e-9),
