@@ -532,3 +532,58 @@ def test_main_sweep_and_sampling_outputs(monkeypatch, tmp_path):
     assert S.main([str(q)]) == 0
     ms = (tmp_path / "mc.cir.ms0").read_text()
     assert ms.startswith("VMAX: mean = 1.230000e+02")  # circuits 0..4 -> max 103..143
+
+
+@pytest.mark.parametrize("expr,val", [("2*1k", 2000.0), ("sqrt(4)+1", 3.0), ("2^3", 8.0), ("2**3", 8.0),
+                                      ("-(1.5MEG/3)", -5e5), ("max(1,2.5)+min(3,-1)", 1.5), ("10n*1e9", 10.0),
+                                      ("exp(0)*log(1)+abs(-2)", 2.0)])
+def test_expression_values(expr, val):
+    assert S.eval_expr(expr, {}) == pytest.approx(val, rel=1e-14)
+
+
+def test_expression_errors():
+    for bad in ("1/0", "__import__('os')", "x.y", "a if 1 else 2"):
+        with pytest.raises(ValueError):
+            S.eval_expr(bad, {"A": 1.0})
+    with pytest.raises(ValueError):
+        S.parse("t\n.PARAM a={b+1} b={a*2}\nR1 x 0 {a}\n.TRAN 1n 1u\n.END\n")  # a cycle
+    with pytest.raises(ValueError):
+        S.parse("t\nR1 x 0 {nosuch*2}\n.TRAN 1n 1u\n.END\n")
+
+
+DECK_EXPR = """expressions
+.PARAM r2={2*r1} r1=1k amp='r1/1k*0.5' cv={ 1p * (1 + 1) }
+V1 in 0 SIN(0 {amp} 1MEG)
+R1 in out {r2 + 500}
+C1 out 0 {cv}
+D1 out 0 dm
+.MODEL dm D (IS={1e-15*10} N={sqrt(1.21)})
+.TRAN 1n 1u
+.END
+"""
+
+
+def test_param_expressions_in_elements_and_models():
+    d = S.parse(DECK_EXPR)
+    nl = d.netlist
+    assert d.params["R1"] == 1000.0 and d.params["R2"] == 2000.0 and d.params["AMP"] == 0.5
+    assert nl.res[0][2] == 2500.0 and nl.cap[0][2] == pytest.approx(2e-12, rel=1e-15)
+    assert nl.vsrc[0][4][1] == 0.5
+    f = N.DIODE_FIELDS.index
+    assert nl.diode[0][3][f("IS")] == pytest.approx(1e-14) and nl.diode[0][3][f("N")] == pytest.approx(1.1)
+    # a sweep point fixes r1, and r2 follows it
+    d2 = S.parse(DECK_EXPR, {"r1": 5e3})
+    assert d2.params["R2"] == 1e4 and d2.netlist.res[0][2] == 1.05e4
+
+
+def test_include(tmp_path):
+    sub = tmp_path / "lib"
+    sub.mkdir()
+    (sub / "models.inc").write_text(".MODEL dm D (IS=2e-14)\n.INC 'more.inc'\n")
+    (sub / "more.inc").write_text("R9 out 0 3k\n")
+    text = "inc\n.INCLUDE \"lib/models.inc\"\nV1 in 0 1\nR1 in out 1k\nD1 out 0 dm\n.TRAN 1n 1u\n.END\n"
+    d = S.parse(text, base_dir=str(tmp_path))
+    f = N.DIODE_FIELDS.index
+    assert d.netlist.diode[0][3][f("IS")] == 2e-14 and sorted(r[2] for r in d.netlist.res) == [1000.0, 3000.0]
+    with pytest.raises(ValueError):
+        S.parse("inc\n.INCLUDE nosuch.inc\n.TRAN 1n 1u\n.END\n", base_dir=str(tmp_path))

@@ -11,7 +11,9 @@ output.  The subset is what the path simulates:
 * ``.MODEL``, ``.SUBCKT``/``.ENDS``, ``.TRAN``, ``.OPTIONS TIMEINT``
   (RELTOL, ABSTOL, METHOD=TRAP|GEAR, MAXORD), ``.OPTIONS NONLIN-TRAN``
   (RELTOL, ABSTOL, DELTAXTOL, RHSTOL, SMALLUPDATETOL, MAXSTEP),
-  ``.OPTIONS LINSOL TYPE=KLU|KSPARSE``, ``.TEMP`` and ``.OPTIONS DEVICE
+  ``.OPTIONS LINSOL TYPE=KLU|KSPARSE``, ``.INCLUDE``, ``{expression}`` values
+  (arithmetic, parameters, SPICE numbers, SQRT EXP LOG ... functions) in
+  elements, sources, models and ``.PARAM``, ``.TEMP`` and ``.OPTIONS DEVICE
   TEMP= TNOM=`` (diodes and level-1 MOSFETs; the instance TEMP / DTEMP and
   the model TNOM too), ``.PARAM`` with ``{NAME}``
   references, ``.STEP`` (linear or LIST; every point of the sweep runs as one
@@ -52,6 +54,7 @@ Reference behaviour restated:
 """
 from __future__ import annotations
 
+import ast
 import math
 import os
 from decimal import Decimal
@@ -90,15 +93,128 @@ def _is_number(tok: str) -> bool:
 
 
 def _tokens(line: str) -> list[str]:
-    line = re.sub(r"([(),=])", r" \1 ", line)
-    return [t for t in line.split() if t != ","]
+    """Tokens of a logical line; a {...} expression stays one token (its
+    spaces dropped; its parentheses and commas are its own)."""
+    out: list[str] = []
+    for part in re.split(r"(\{[^{}]*\})", line):
+        if part.startswith("{") and part.endswith("}"):
+            out.append("{" + re.sub(r"\s+", "", part[1:-1]) + "}")
+        else:
+            part = re.sub(r"([(),=])", r" \1 ", part)
+            out += [t for t in part.split() if t != ","]
+    return out
 
 
-def _logical_lines(text: str) -> tuple[str, list[str]]:
+# ---------------------------------------------------------------------------
+# expressions: {...} in element, source and model values and in .PARAM
+# (arithmetic, parameters, SPICE numbers, a few functions; the reference's
+# expression language, src/UtilityPKG/N_UTL_Expression*, is far larger)
+
+class _Unresolved(Exception):
+    """An expression names a parameter that has no value yet."""
+
+
+_FUNCS = {"SQRT": math.sqrt, "EXP": math.exp, "LOG": math.log, "LN": math.log, "LOG10": math.log10,
+          "ABS": abs, "MIN": min, "MAX": max, "POW": math.pow, "PWR": math.pow, "SIN": math.sin,
+          "COS": math.cos, "TAN": math.tan, "ATAN": math.atan, "SINH": math.sinh, "COSH": math.cosh,
+          "TANH": math.tanh, "FLOOR": math.floor, "CEIL": math.ceil}
+_BINOPS = {ast.Add: lambda a, b: a + b, ast.Sub: lambda a, b: a - b, ast.Mult: lambda a, b: a * b,
+           ast.Div: lambda a, b: a / b, ast.Pow: lambda a, b: a ** b}
+_SPICE_NUM = re.compile(r"(?<![A-Za-z_0-9.])(?:\d+\.?\d*|\.\d+)(?:[eE][+-]?\d+)?([A-Za-z]+)?")
+
+
+def eval_expr(expr: str, params: dict) -> float:
+    """Value of an expression (without its braces) given the parameters
+    (upper-case names).  Numbers may carry SPICE suffixes (1k, 2.5MEG, 10n);
+    ** and ^ are powers."""
+    src = _SPICE_NUM.sub(lambda m: repr(number(m.group(0))) if m.group(1) else m.group(0), expr)
+    try:
+        tree = ast.parse(src.replace("^", "**"), mode="eval")
+    except SyntaxError as e:
+        raise ValueError(f"expression {{{expr}}}: {e.msg}") from None
+
+    def ev(n):
+        if isinstance(n, ast.Constant) and isinstance(n.value, (int, float)) and not isinstance(n.value, bool):
+            return float(n.value)
+        if isinstance(n, ast.Name):
+            k = n.id.upper()
+            if k in params:
+                return float(params[k])
+            if k == "PI":
+                return math.pi
+            raise _Unresolved(n.id)
+        if isinstance(n, ast.UnaryOp) and isinstance(n.op, (ast.USub, ast.UAdd)):
+            v = ev(n.operand)
+            return -v if isinstance(n.op, ast.USub) else v
+        if isinstance(n, ast.BinOp) and type(n.op) in _BINOPS:
+            return _BINOPS[type(n.op)](ev(n.left), ev(n.right))
+        if (isinstance(n, ast.Call) and isinstance(n.func, ast.Name) and n.func.id.upper() in _FUNCS
+                and not n.keywords):
+            return float(_FUNCS[n.func.id.upper()](*[ev(a) for a in n.args]))
+        raise ValueError(f"expression {{{expr}}}: unsupported element {ast.dump(n)[:40]}")
+    try:
+        return ev(tree.body)
+    except (ZeroDivisionError, OverflowError, TypeError) as e:
+        raise ValueError(f"expression {{{expr}}}: {e}") from None
+
+
+def _param_value(raw: str, params: dict) -> float:
+    v = raw.strip()
+    if len(v) >= 2 and v[0] in "{'\"" and v[-1] in "}'\"":
+        v = v[1:-1]
+    return number(v) if _is_number(v) else eval_expr(v, params)
+
+
+def resolve_params(raw: dict, fixed: dict | None = None) -> dict:
+    """.PARAM definitions (NAME -> text) to values, in whatever order they
+    refer to each other; fixed values (a sweep point) replace definitions."""
+    vals = dict(fixed or {})
+    pending = {k: v for k, v in raw.items() if k not in vals}
+    while pending:
+        progress = False
+        for k, v in list(pending.items()):
+            try:
+                vals[k] = _param_value(v, vals)
+            except _Unresolved:
+                continue
+            del pending[k]
+            progress = True
+        if not progress:
+            raise ValueError(f".PARAM: cannot resolve {sorted(pending)} (an unknown name or a cycle)")
+    return vals
+
+
+_INCLUDE = re.compile(r"^\s*\.INC(?:LUDE)?\s+(['\"]?)(.+?)\1\s*$", re.IGNORECASE)
+
+
+def _with_includes(lines: list[str], base_dir: str | None, depth: int = 0) -> list[str]:
+    """.INCLUDE / .INC lines replaced by the named file's lines (relative to
+    the including file's directory; the whole file, no title line)."""
+    if depth > 16:
+        raise ValueError(".INCLUDE nested more than 16 deep (a cycle?)")
+    out: list[str] = []
+    for ln in lines:
+        m = _INCLUDE.match(ln)
+        if not m:
+            out.append(ln)
+            continue
+        path = m.group(2)
+        if not os.path.isabs(path):
+            path = os.path.join(base_dir or os.getcwd(), path)
+        try:
+            with open(path) as f:
+                body = f.read().splitlines()
+        except OSError as e:
+            raise ValueError(f".INCLUDE {m.group(2)}: {e.strerror}") from None
+        out += _with_includes(body, os.path.dirname(path), depth + 1)
+    return out
+
+
+def _logical_lines(text: str, base_dir: str | None = None) -> tuple[str, list[str]]:
     raw = text.splitlines()
     title = raw[0].strip() if raw else ""
     out: list[str] = []
-    for ln in raw[1:]:
+    for ln in _with_includes(raw[1:], base_dir):
         s = ln.split(";", 1)[0]
         s = re.split(r"\s\$\s", s, maxsplit=1)[0].rstrip()
         st = s.strip()
@@ -197,15 +313,14 @@ class _Builder:
         self.tnom_c = 27.0
 
     def subst(self, toks: list[str]) -> list[str]:
-        """{NAME} tokens -> the .PARAM value (a single parameter; no
-        expressions)."""
+        """{expression} tokens -> their value from the .PARAM values."""
         out = []
         for t in toks:
             if t.startswith("{") and t.endswith("}"):
-                key = t[1:-1].strip().upper()
-                if key not in self.deck.params:
-                    raise ValueError(f"unknown parameter {t}")
-                out.append(repr(self.deck.params[key]))
+                try:
+                    out.append(repr(eval_expr(t[1:-1], self.deck.params)))
+                except _Unresolved as e:
+                    raise ValueError(f"unknown parameter {e} in {t}") from None
             else:
                 out.append(t)
         return out
@@ -450,27 +565,28 @@ _NONLIN_TRAN = {"RELTOL": "nl_reltol", "ABSTOL": "nl_abstol", "DELTAXTOL": "nl_d
                 "RHSTOL": "nl_rhstol", "SMALLUPDATETOL": "nl_smallupdatetol", "MAXSTEP": "nl_maxstep"}
 
 
-def parse(text: str, overrides: dict | None = None) -> Deck:
+def parse(text: str, overrides: dict | None = None, base_dir: str | None = None) -> Deck:
     """Parse a netlist (the first line is the title, as in SPICE).
     overrides: {parameter or element name: value} — one point of a .STEP
     sweep (parse_sweep builds them)."""
-    title, lines = _logical_lines(text)
+    title, lines = _logical_lines(text, base_dir)
     B = _Builder(title)
     B._pending_sources = []
-    # .PARAM values first (they may be referenced before their line)
+    # .PARAM values first (they may be referenced before their line, and
+    # refer to each other); a sweep point fixes its parameters, and every
+    # parameter defined from them follows
+    raw_params = {}
     for ln in lines:
         toks = _tokens(ln)
         if toks[0].upper() == ".PARAM":
             pos, kv = _params(toks[1:])
             if pos:
                 raise ValueError(".PARAM takes NAME=value pairs")
-            for k, v in kv.items():
-                B.deck.params[k] = number(v)
+            raw_params.update(kv)
     overrides = {k.upper(): float(v) for k, v in (overrides or {}).items()}
+    B.deck.params = resolve_params(raw_params, {k: v for k, v in overrides.items() if k in raw_params})
     for k, v in overrides.items():
-        if k in B.deck.params:
-            B.deck.params[k] = v
-        else:
+        if k not in raw_params:
             B.overrides[k] = v
     B.deck.step_values = dict(overrides)
     # pass 1: subcircuit bodies and models
@@ -779,23 +895,23 @@ def sample_moments(values) -> dict:
                 min=float(v.min()), max=float(v.max()))
 
 
-def parse_sampling(text: str) -> list[Deck]:
+def parse_sampling(text: str, base_dir: str | None = None) -> list[Deck]:
     """One deck per sample of the deck's .SAMPLING block."""
-    base = parse(text)
+    base = parse(text, base_dir=base_dir)
     if not base.sampling:
         return [base]
-    return [parse(text, pt) for pt in sample_points(base.sampling)]
+    return [parse(text, pt, base_dir) for pt in sample_points(base.sampling)]
 
 
-def parse_embedded(text: str) -> list[Deck]:
+def parse_embedded(text: str, base_dir: str | None = None) -> list[Deck]:
     """One deck per sample of the deck's .EMBEDDEDSAMPLING block (the same
     parameter vectors and sample generator as .SAMPLING)."""
-    base = parse(text)
+    base = parse(text, base_dir=base_dir)
     if not base.embedded:
         raise ValueError("the deck has no .EMBEDDEDSAMPLING")
     if base.sampling or base.steps:
         raise ValueError(".EMBEDDEDSAMPLING with .SAMPLING or .STEP is not supported")
-    return [parse(text, pt) for pt in sample_points(base.embedded)]
+    return [parse(text, pt, base_dir) for pt in sample_points(base.embedded)]
 
 
 def ensemble_netlist(decks: list[Deck]) -> tuple[N.Netlist, list[int]]:
@@ -925,16 +1041,16 @@ def write_ensemble(path: str, deck: Deck, ens: Ensemble) -> str:
     return out
 
 
-def parse_sweep(text: str) -> list[Deck]:
+def parse_sweep(text: str, base_dir: str | None = None) -> list[Deck]:
     """One deck per point of the .STEP sweep (the first .STEP line
     outermost); a single deck without .STEP."""
-    base = parse(text)
+    base = parse(text, base_dir=base_dir)
     if not base.steps:
         return [base]
     combos = [{}]
     for name, vals in base.steps:
         combos = [dict(c, **{name: v}) for c in combos for v in vals]
-    return [parse(text, c) for c in combos]
+    return [parse(text, c, base_dir) for c in combos]
 
 
 def run_sweep(decks: list[Deck], device: int = 0, cap: int | None = None) -> list["Result"]:
@@ -1399,9 +1515,10 @@ def main(argv=None) -> int:
     path = argv[0]
     with open(path) as f:
         text = f.read()
-    base = parse(text)
+    where = os.path.dirname(os.path.abspath(path))
+    base = parse(text, base_dir=where)
     if base.embedded:
-        decks = parse_embedded(text)
+        decks = parse_embedded(text, where)
         ens = run_embedded(decks)
         out = write_ensemble(path, decks[0], ens)
         print(f"{len(decks)} samples as one block system, {len(ens.times)} shared time points; "
@@ -1410,7 +1527,7 @@ def main(argv=None) -> int:
     if base.sampling:
         if base.steps:
             raise ValueError(".SAMPLING and .STEP together are not supported")
-        decks = parse_sampling(text)
+        decks = parse_sampling(text, where)
         results = run_sweep(decks)
         out = write_print(path, base, results) if base.prints else path + ".ms0"
         with open(path + ".ms0", "w") as f:
@@ -1421,7 +1538,7 @@ def main(argv=None) -> int:
                 print(line)
         print(f"{len(decks)} samples run as one batch; output {os.path.basename(out)}")
         return 0
-    decks = parse_sweep(text)
+    decks = parse_sweep(text, where)
     deck = decks[0]
     if len(decks) == 1:
         res = run(deck)
