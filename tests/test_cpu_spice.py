@@ -587,3 +587,18 @@ def test_include(tmp_path):
     assert d.netlist.diode[0][3][f("IS")] == 2e-14 and sorted(r[2] for r in d.netlist.res) == [1000.0, 3000.0]
     with pytest.raises(ValueError):
         S.parse("inc\n.INCLUDE nosuch.inc\n.TRAN 1n 1u\n.END\n", base_dir=str(tmp_path))
+
+
+def test_expression_print_variables():
+    d = S.parse("t\nV1 a 0 1\nR1 a b 1k\nR2 b 0 1k\n.PRINT TRAN {V(a)-V(b)} {sqrt(abs(V(b)))*2}\n"
+                ".MEASURE TRAN m MAX {V(a,b)*1k}\n.TRAN 1n 1u\n.END\n")
+    assert d.prints == ["{V(A)-V(B)}", "{SQRT(ABS(V(B)))*2}"] and d.measures[0].var == "{V(A,B)*1K}"
+    names = d.netlist.names
+    va, vb = np.array([1.0, 2.0]), np.array([0.25, 1.0])
+    vals = {names["A"]: va, names["B"]: vb}
+    for var, want in ((d.prints[0], va - vb), (d.prints[1], np.sqrt(vb) * 2), (d.measures[0].var, (va - vb) * 1e3)):
+        us, f = S._var_probes(d, var)
+        assert set(us) == {names[k] for k in ("A", "B") if names[k] in us}
+        np.testing.assert_allclose(f(vals), want, rtol=1e-15)
+    with pytest.raises(ValueError):
+        S._var_probes(d, "{V(A)+NOSUCH}")

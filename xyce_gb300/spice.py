@@ -110,23 +110,28 @@ def _tokens(line: str) -> list[str]:
 # (arithmetic, parameters, SPICE numbers, a few functions; the reference's
 # expression language, src/UtilityPKG/N_UTL_Expression*, is far larger)
 
-class _Unresolved(Exception):
-    """An expression names a parameter that has no value yet."""
+class _Unresolved(ValueError):
+    """An expression names a parameter that has no value (yet)."""
 
 
 _FUNCS = {"SQRT": math.sqrt, "EXP": math.exp, "LOG": math.log, "LN": math.log, "LOG10": math.log10,
           "ABS": abs, "MIN": min, "MAX": max, "POW": math.pow, "PWR": math.pow, "SIN": math.sin,
           "COS": math.cos, "TAN": math.tan, "ATAN": math.atan, "SINH": math.sinh, "COSH": math.cosh,
           "TANH": math.tanh, "FLOOR": math.floor, "CEIL": math.ceil}
+_VFUNCS = {"SQRT": np.sqrt, "EXP": np.exp, "LOG": np.log, "LN": np.log, "LOG10": np.log10, "ABS": np.abs,
+           "MIN": np.minimum, "MAX": np.maximum, "POW": np.power, "PWR": np.power, "SIN": np.sin,
+           "COS": np.cos, "TAN": np.tan, "ATAN": np.arctan, "SINH": np.sinh, "COSH": np.cosh, "TANH": np.tanh,
+           "FLOOR": np.floor, "CEIL": np.ceil}
 _BINOPS = {ast.Add: lambda a, b: a + b, ast.Sub: lambda a, b: a - b, ast.Mult: lambda a, b: a * b,
            ast.Div: lambda a, b: a / b, ast.Pow: lambda a, b: a ** b}
 _SPICE_NUM = re.compile(r"(?<![A-Za-z_0-9.])(?:\d+\.?\d*|\.\d+)(?:[eE][+-]?\d+)?([A-Za-z]+)?")
 
 
-def eval_expr(expr: str, params: dict) -> float:
+def eval_expr(expr: str, params: dict, vector: bool = False):
     """Value of an expression (without its braces) given the parameters
     (upper-case names).  Numbers may carry SPICE suffixes (1k, 2.5MEG, 10n);
-    ** and ^ are powers."""
+    ** and ^ are powers.  vector: the parameters may be arrays (waveforms)
+    and the result is an array."""
     src = _SPICE_NUM.sub(lambda m: repr(number(m.group(0))) if m.group(1) else m.group(0), expr)
     try:
         tree = ast.parse(src.replace("^", "**"), mode="eval")
@@ -139,7 +144,7 @@ def eval_expr(expr: str, params: dict) -> float:
         if isinstance(n, ast.Name):
             k = n.id.upper()
             if k in params:
-                return float(params[k])
+                return params[k] if vector else float(params[k])
             if k == "PI":
                 return math.pi
             raise _Unresolved(n.id)
@@ -150,6 +155,8 @@ def eval_expr(expr: str, params: dict) -> float:
             return _BINOPS[type(n.op)](ev(n.left), ev(n.right))
         if (isinstance(n, ast.Call) and isinstance(n.func, ast.Name) and n.func.id.upper() in _FUNCS
                 and not n.keywords):
+            if vector:
+                return _VFUNCS[n.func.id.upper()](*[ev(a) for a in n.args])
             return float(_FUNCS[n.func.id.upper()](*[ev(a) for a in n.args]))
         raise ValueError(f"expression {{{expr}}}: unsupported element {ast.dump(n)[:40]}")
     try:
@@ -313,10 +320,12 @@ class _Builder:
         self.tnom_c = 27.0
 
     def subst(self, toks: list[str]) -> list[str]:
-        """{expression} tokens -> their value from the .PARAM values."""
+        """{expression} tokens -> their value from the .PARAM values
+        (expressions of waveforms, V(...) / I(...), are left for .PRINT and
+        .MEASURE)."""
         out = []
         for t in toks:
-            if t.startswith("{") and t.endswith("}"):
+            if t.startswith("{") and t.endswith("}") and not re.search(r"(?i)(?<![A-Za-z_0-9])[VI]\(", t):
                 try:
                     out.append(repr(eval_expr(t[1:-1], self.deck.params)))
                 except _Unresolved as e:
@@ -1271,6 +1280,21 @@ def _var_probes(deck: Deck, var: str) -> tuple[list[int], callable]:
         return [], lambda vals, v=v: v
     if var == "TIME":
         return [], None
+    if var.startswith("{") and var.endswith("}"):
+        # an expression of V(...) / I(...) columns, e.g. {V(A)-V(B)} or {I(V1)*V(IN)}
+        body = var[1:-1]
+        refs = list(dict.fromkeys(re.findall(r"[VI]\([^()]*\)", body)))
+        parts = [_var_probes(deck, r) for r in refs]
+        expr = body
+        for k, r in enumerate(refs):
+            expr = expr.replace(r, f"__R{k}")
+        eval_expr(expr, {f"__R{k}": 0.0 for k in range(len(refs))})  # syntax and names, early
+        us = list(dict.fromkeys(u for ps, _ in parts for u in ps))
+
+        def f(vals, parts=parts, expr=expr):
+            env = {f"__R{k}": np.asarray(g(vals), np.float64) for k, (ps, g) in enumerate(parts)}
+            return eval_expr(expr, env, vector=True)
+        return us, f
     raise ValueError(f"print variable {var} is not supported")
 
 
