@@ -27,8 +27,9 @@ output.  The subset is what the path simulates:
   RMS, INTEG with FROM/TO; TRIG/TARG with VAL, TD and RISE/FALL/CROSS=n|LAST;
   WHEN; FIND ... WHEN / AT), ``.END``; ``*`` and ``;`` comments, ``+``
   continuation lines, engineering suffixes (T G MEG K M MIL U N P F);
-* print variables ``V(n)``, ``V(a,b)``, ``I(Vname)``, ``TIME``, ``TEMP``
-  and ``<R|C name>:R|C`` (the element value).
+* print variables ``V(n)``, ``V(a,b)``, ``I(Vname)`` / ``I(Lname)``, ``TIME``,
+  ``TEMP``, ``<R|C name>:R|C`` (the element value) and ``{expressions}`` of
+  V(...) / I(...), e.g. ``{V(a)-V(b)}``.
 
 Anything outside the subset (another element letter, a model level, an
 unknown model parameter, an expression) raises ``ValueError`` rather than
