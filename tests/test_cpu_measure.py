@@ -68,3 +68,11 @@ def test_measure_variables_are_probed():
     d = S.parse("m\nV1 a 0 1\nR1 a b 1k\nR2 b 0 1k\n.TRAN 1n 10n\n"
                 ".MEASURE TRAN f FIND V(b) WHEN V(a)=0.5\n.END\n")
     assert d.measures[0].vars == ["V(B)", "V(A)"]
+
+
+def test_deriv():
+    # the triangle's slope: +1 on (0,1) and (3,5), -1 on (1,3)
+    assert meas(".MEASURE TRAN d1 DERIV V(a) AT=0.6") == pytest.approx(1.0, abs=1e-12)
+    assert meas(".MEASURE TRAN d2 DERIVATIVE V(a) AT=2.0") == pytest.approx(-1.0, abs=1e-12)
+    assert meas(".MEASURE TRAN d3 DERIV V(b) WHEN V(a)=0.5 FALL=1") == pytest.approx(-1.0, abs=1e-12)
+    assert np.isnan(meas(".MEASURE TRAN d4 DERIV V(a) AT=20"))

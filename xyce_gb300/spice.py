@@ -25,7 +25,7 @@ output.  The subset is what the path simulates:
   ``.PRINT TRAN`` (FORMAT=STD,
   NOINDEX or CSV), ``.MEASURE TRAN`` (MAX, MIN, PP, AVG,
   RMS, INTEG with FROM/TO; TRIG/TARG with VAL, TD and RISE/FALL/CROSS=n|LAST;
-  WHEN; FIND ... WHEN / AT), ``.END``; ``*`` and ``;`` comments, ``+``
+  WHEN; FIND and DERIV ... WHEN / AT), ``.END``; ``*`` and ``;`` comments, ``+``
   continuation lines, engineering suffixes (T G MEG K M MIL U N P F);
 * print variables ``V(n)``, ``V(a,b)``, ``I(Vname)`` / ``I(Lname)``, ``TIME``,
   ``TEMP``, ``<R|C name>:R|C`` (the element value) and ``{expressions}`` of
@@ -1213,21 +1213,23 @@ def _timing_measure(name: str, toks: list[str]) -> Measure:
         if i != len(toks):
             raise ValueError(f".MEASURE {name}: unexpected {' '.join(toks[i:])}")
         return Measure(name, "WHEN", w["var"], spec=dict(when=w), vars=[w["var"]])
-    # FIND <var> WHEN ... | FIND <var> AT=<t>
+    # FIND|DERIV <var> WHEN ... | FIND|DERIV <var> AT=<t>
+    func = "FIND" if head == "FIND" else "DERIV"
     fvar, i = _one_var(toks, 1)
     if i < len(toks) and toks[i].upper() == "WHEN":
         w, i = when(i + 1)
         if i != len(toks):
             raise ValueError(f".MEASURE {name}: unexpected {' '.join(toks[i:])}")
-        return Measure(name, "FIND", fvar, spec=dict(when=w), vars=[fvar, w["var"]])
+        return Measure(name, func, fvar, spec=dict(when=w), vars=[fvar, w["var"]])
     kv, i = _kv_run(toks, i)
     if set(kv) != {"AT"} or i != len(toks):
-        raise ValueError(f".MEASURE {name}: FIND <var> WHEN ... or FIND <var> AT=<time>")
-    return Measure(name, "FIND", fvar, spec=dict(at=number(kv["AT"])), vars=[fvar])
+        raise ValueError(f".MEASURE {name}: {head} <var> WHEN ... or {head} <var> AT=<time>")
+    return Measure(name, func, fvar, spec=dict(at=number(kv["AT"])), vars=[fvar])
 
 
 def _measure(toks: list[str]) -> Measure:
-    if len(toks) >= 3 and toks[0].upper() == "TRAN" and toks[2].upper() in ("TRIG", "WHEN", "FIND"):
+    if len(toks) >= 3 and toks[0].upper() == "TRAN" and toks[2].upper() in ("TRIG", "WHEN", "FIND", "DERIV",
+                                                                             "DERIVATIVE"):
         return _timing_measure(toks[1].upper(), toks[2:])
     pos, kv = _params(toks)
     if len(pos) < 3 or pos[0].upper() != "TRAN":
@@ -1348,7 +1350,7 @@ def _when(t, v, f, w):
     val, (kind, count) = w["val"], w["rfc"]
     td, frm, to = w["td"], w["frm"], w["to"]
     nr = nf = nc = 0
-    res_t = res_f = float("nan")
+    res_t = res_f = res_d = float("nan")
     for k in range(1, len(t)):
         lv, cv = v[k - 1], v[k]
         if cv == lv:
@@ -1371,9 +1373,13 @@ def _when(t, v, f, w):
         res_t = tw
         if f is not None:
             res_f = f[k] if abs(cv - val) < MINVAL else f[k] - (t[k] - tw) * (f[k] - f[k - 1]) / (t[k] - t[k - 1])
+            # DERIV: the backward difference over the step that met the
+            # condition (DerivativeEvaluationBase::getDerivativeValue,
+            # N_IO_MeasureDerivativeEvaluation.C)
+            res_d = (f[k] - f[k - 1]) / (t[k] - t[k - 1])
         if count >= 0:
             break
-    return res_t, res_f
+    return res_t, res_f, res_d
 
 
 def evaluate_measure(m: Measure, t: np.ndarray, cols: dict) -> float:
@@ -1386,6 +1392,17 @@ def evaluate_measure(m: Measure, t: np.ndarray, cols: dict) -> float:
         return float(t2 - t1)
     if m.func == "WHEN":
         return float(_when(t, cols[m.var], None, m.spec["when"])[0])
+    if m.func == "DERIV":
+        f = cols[m.var]
+        if "at" in m.spec:
+            at = m.spec["at"]
+            for k in range(1, len(t)):
+                b, c = t[k - 1] - at, t[k] - at
+                if (b < 0.0 < c) or abs(b) < MINVAL or abs(c) < MINVAL:
+                    return float((f[k] - f[k - 1]) / (t[k] - t[k - 1]))
+            return float("nan")
+        w = m.spec["when"]
+        return float(_when(t, cols[w["var"]], f, w)[2])
     if m.func == "FIND":
         if "at" in m.spec:
             at = m.spec["at"]
