@@ -602,3 +602,15 @@ def test_expression_print_variables():
         np.testing.assert_allclose(f(vals), want, rtol=1e-15)
     with pytest.raises(ValueError):
         S._var_probes(d, "{V(A)+NOSUCH}")
+
+
+@pytest.mark.parametrize("line,name,vals", [
+    (".STEP DEC RV 1k 100k 2", "RV", [1e3, 1e3 * 10 ** 0.5, 1e4, 1e4 * 10 ** 0.5, 1e5]),
+    (".STEP OCT RV 1 8 1", "RV", [1.0, 2.0, 4.0, 8.0]),
+    (".STEP LIN RV 1 3 1", "RV", [1.0, 2.0, 3.0]),
+    (".STEP DEC RV 100 1 3", "RV", [100.0]),
+])
+def test_step_sweep_kinds(line, name, vals):
+    n, v = S._step(S._tokens(line)[1:])
+    assert n == name
+    np.testing.assert_allclose(v, vals, rtol=1e-12)

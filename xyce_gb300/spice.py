@@ -775,18 +775,35 @@ def read(path: str) -> Deck:
 
 
 def _step(toks: list[str]) -> tuple[str, list[float]]:
-    """.STEP NAME start stop step | .STEP NAME LIST v1 v2 ... (linear)."""
+    """.STEP [LIN] NAME start stop step | .STEP DEC|OCT NAME start stop
+    points | .STEP NAME LIST v1 v2 ... (SweepParam, src/AnalysisPKG/
+    N_ANP_SweepParam.C:95-135, 385-440: DEC and OCT multiply by
+    exp(ln 10 / points) or exp(ln 2 / points), floor(decades * points + 1)
+    values; a start above the stop gives the start alone)."""
     pos, kv = _params(toks)
     if len(pos) < 2:
         raise ValueError(".STEP needs a name and values")
+    kind = pos[0].upper()
+    if kind in ("DEC", "OCT"):
+        if len(pos) != 5:
+            raise ValueError(f".STEP {kind} NAME start stop points")
+        name, a, b, pts = pos[1].upper(), number(pos[2]), number(pos[3]), number(pos[4])
+        if not (a > 0 and b > 0 and pts >= 1):
+            raise ValueError(f".STEP {kind}: start and stop must be positive, points at least 1")
+        base = 10.0 if kind == "DEC" else 2.0
+        mult = math.exp(math.log(base) / pts)
+        if a > b + 2.0 * 2.220446049250313e-16:
+            return name, [a]
+        count = int(math.floor(abs(math.log(a) - math.log(b)) / math.log(base) * pts + 1))
+        return name, [a * mult ** k for k in range(count)]
+    if kind == "LIN":
+        pos = pos[1:]
     name = pos[0].upper()
     if pos[1].upper() == "LIST":
         vals = [number(v) for v in pos[2:]]
         if not vals:
             raise ValueError(".STEP LIST needs values")
         return name, vals
-    if pos[1].upper() in ("DEC", "OCT", "LIN"):
-        raise ValueError(f".STEP {pos[1]} sweeps are not supported (linear and LIST are)")
     if len(pos) != 4:
         raise ValueError(".STEP NAME start stop step")
     a, b, st = _decimal(pos[1]), _decimal(pos[2]), _decimal(pos[3])
