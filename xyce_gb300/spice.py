@@ -16,7 +16,7 @@ output.  The subset is what the path simulates:
   elements, sources, models and ``.PARAM``, ``.TEMP`` and ``.OPTIONS DEVICE
   TEMP= TNOM=`` (diodes and level-1 MOSFETs; the instance TEMP / DTEMP and
   the model TNOM too), ``.PARAM`` with ``{NAME}``
-  references, ``.STEP`` (linear or LIST; every point of the sweep runs as one
+  references, ``.STEP`` (LIN, DEC, OCT or LIST; every point of the sweep runs as one
   circuit of a single GPU batch), ``.SAMPLING`` with ``.OPTIONS SAMPLES``
   (Latin hypercube or Monte Carlo samples of NORMAL / UNIFORM parameters,
   all samples one batch, moments of every .MEASURE), ``.EMBEDDEDSAMPLING``
