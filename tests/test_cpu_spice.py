@@ -614,3 +614,9 @@ def test_step_sweep_kinds(line, name, vals):
     n, v = S._step(S._tokens(line)[1:])
     assert n == name
     np.testing.assert_allclose(v, vals, rtol=1e-12)
+
+
+@pytest.mark.parametrize("tran,expect", [(".TRAN 1n 1u", 5e-9), (".TRAN 1n 1u 0 2n", 2e-9), (".TRAN 1n 1u 0 9n", 5e-9)])
+def test_timeint_delmax(tran, expect):
+    d = S.parse(f"t\nV1 a 0 1\nR1 a 0 1k\n{tran}\n.OPTIONS TIMEINT DELMAX=5n\n.END\n")
+    assert d.netlist.tran.hmax == pytest.approx(expect)

@@ -632,7 +632,7 @@ def parse(text: str, overrides: dict | None = None, base_dir: str | None = None)
         raise ValueError(".SUBCKT without .ENDS")
     tran = None
     tstep = 0.0
-    reltol = abstol = method = maxord = None
+    reltol = abstol = method = maxord = delmax = None
     nonlin = {}
     deck = B.deck
     # the circuit temperature applies to every device, wherever the line is
@@ -709,6 +709,12 @@ def parse(text: str, overrides: dict | None = None, base_dir: str | None = None)
                         if mv not in methods:
                             raise ValueError(f".OPTIONS TIMEINT METHOD={v} is not supported")
                         method = methods[mv]
+                    elif k == "DELMAX":
+                        # the largest step, with .TRAN's TMAX the smaller of the
+                        # two (StepErrorControl, N_TIA_StepErrorControl.C:899-901)
+                        delmax = number(v)
+                        if not delmax > 0:
+                            raise ValueError("DELMAX must be positive")
                     elif k == "MAXORD":
                         maxord = int(number(v))
                         if maxord not in (1, 2):
@@ -760,6 +766,8 @@ def parse(text: str, overrides: dict | None = None, base_dir: str | None = None)
         tran.method = method
     if maxord is not None:
         tran.max_order = maxord
+    if delmax is not None:
+        tran.hmax = min(tran.hmax, delmax) if tran.hmax > 0 else delmax
     for k, v in nonlin.items():
         setattr(tran, k, v)
     B.finish_sources(tstep, tran.tstop)
