@@ -76,3 +76,18 @@ def test_deriv():
     assert meas(".MEASURE TRAN d2 DERIVATIVE V(a) AT=2.0") == pytest.approx(-1.0, abs=1e-12)
     assert meas(".MEASURE TRAN d3 DERIV V(b) WHEN V(a)=0.5 FALL=1") == pytest.approx(-1.0, abs=1e-12)
     assert np.isnan(meas(".MEASURE TRAN d4 DERIV V(a) AT=20"))
+
+
+def test_freq_and_duty():
+    """A square wave of period 1 (on for the first half of each period)
+    sampled every 0.01: inside FROM=0.25 TO=9.75 it falls 10 times and rises
+    9 times in 9.5 time units, so FREQ = 0.5 * 19 / 9.5 = 1; it is on half
+    the time."""
+    t = np.round(np.arange(0.0, 10.0 + 1e-9, 0.01), 10)
+    sq = np.where(np.mod(t, 1.0) < 0.5, 1.0, 0.0)
+    d = S.parse("m\nV1 a 0 1\nR1 a 0 1k\n.TRAN 1n 10n\n"
+                ".MEASURE TRAN f FREQ V(a) ON=0.8 OFF=0.2 FROM=0.25 TO=9.75\n"
+                ".MEASURE TRAN dc DUTY V(a) ON=0.8 OFF=0.2 FROM=0.25 TO=9.75\n.END\n")
+    cols = {"V(A)": sq}
+    assert S.evaluate_measure(d.measures[0], t, cols) == pytest.approx(1.0, rel=1e-12)
+    assert S.evaluate_measure(d.measures[1], t, cols) == pytest.approx(0.5, abs=0.02)

@@ -25,7 +25,7 @@ output.  The subset is what the path simulates:
   ``.PRINT TRAN`` (FORMAT=STD,
   NOINDEX or CSV), ``.MEASURE TRAN`` (MAX, MIN, PP, AVG,
   RMS, INTEG with FROM/TO; TRIG/TARG with VAL, TD and RISE/FALL/CROSS=n|LAST;
-  WHEN; FIND and DERIV ... WHEN / AT), ``.END``; ``*`` and ``;`` comments, ``+``
+  WHEN; FIND and DERIV ... WHEN / AT; FREQ and DUTY with ON/OFF), ``.END``; ``*`` and ``;`` comments, ``+``
   continuation lines, engineering suffixes (T G MEG K M MIL U N P F);
 * print variables ``V(n)``, ``V(a,b)``, ``I(Vname)`` / ``I(Lname)``, ``TIME``,
   ``TEMP``, ``<R|C name>:R|C`` (the element value) and ``{expressions}`` of
@@ -1260,6 +1260,14 @@ def _measure(toks: list[str]) -> Measure:
     if len(pos) < 3 or pos[0].upper() != "TRAN":
         raise ValueError(".MEASURE TRAN <name> <func> <var> is the supported form")
     name, func = pos[1].upper(), pos[2].upper()
+    if func in ("FREQ", "DUTY"):
+        var = _print_vars(toks[toks.index(pos[2]) + 1:])
+        bad = set(kv) - {"ON", "OFF", "FROM", "TO"}
+        if not var or bad:
+            raise ValueError(f".MEASURE {name}: {func} <var> ON= OFF= [FROM= TO=]")
+        return Measure(name, func, var[0], number(kv["FROM"]) if "FROM" in kv else None,
+                       number(kv["TO"]) if "TO" in kv else None,
+                       spec=dict(on=number(kv.get("ON", "0")), off=number(kv.get("OFF", "0"))))
     if func not in ("MAX", "MIN", "PP", "AVG", "RMS", "INTEG"):
         raise ValueError(f".MEASURE {func} is not supported")
     var = _print_vars(toks[toks.index(pos[2]) + 1:])
@@ -1407,6 +1415,38 @@ def _when(t, v, f, w):
     return res_t, res_f, res_d
 
 
+def _tran_stats(func, t, v, on, off, frm, to) -> float:
+    """FREQ: half the number of OFF->ON and ON->OFF transitions per unit of
+    time; DUTY: the fraction of the time spent ON (above ON, or above OFF
+    once on), over the points inside FROM/TO, the first of which only sets
+    the state (TranStats::updateTran, Frequency / Duty::updateMeasureVars,
+    src/IOInterfacePKG/Output/N_IO_MeasureTranStats.C:90-117,
+    N_IO_MeasureFrequency.C:80-127, N_IO_MeasureDuty.C:80-118)."""
+    sel = np.ones(len(t), bool)
+    if frm is not None:
+        sel &= t >= frm * (1 - MINVAL)
+    if to is not None:
+        sel &= t <= to * (1 + MINVAL)
+    t, v = t[sel], v[sel]
+    window = on_time = 0.0
+    ups = downs = 0
+    in_on = False
+    for k in range(1, len(t)):
+        dt, x, last = t[k] - t[k - 1], v[k], v[k - 1]
+        window += dt
+        if func == "FREQ":
+            ups += (x + MINVAL > on) and (last < on)
+            downs += (x - MINVAL < off) and (last > off)
+        elif (x + MINVAL > on) or (in_on and x + MINVAL > off):
+            on_time += dt
+            in_on = True
+        else:
+            in_on = False
+    if not window > 0:
+        return float("nan")
+    return float(0.5 * (ups + downs) / window if func == "FREQ" else on_time / window)
+
+
 def evaluate_measure(m: Measure, t: np.ndarray, cols: dict) -> float:
     """One .MEASURE from the columns of its variables at the accepted points;
     NaN when it fails (written FAILED)."""
@@ -1415,6 +1455,8 @@ def evaluate_measure(m: Measure, t: np.ndarray, cols: dict) -> float:
         t1 = _rfc_event_time(t, cols[tr["var"]], tr["val"], tr["rfc"], tr["td"])
         t2 = _rfc_event_time(t, cols[tg["var"]], tg["val"], tg["rfc"], tg["td"])
         return float(t2 - t1)
+    if m.func in ("FREQ", "DUTY"):
+        return _tran_stats(m.func, t, cols[m.var], m.spec["on"], m.spec["off"], m.frm, m.to)
     if m.func == "WHEN":
         return float(_when(t, cols[m.var], None, m.spec["when"])[0])
     if m.func == "DERIV":
