@@ -91,3 +91,18 @@ def test_freq_and_duty():
     cols = {"V(A)": sq}
     assert S.evaluate_measure(d.measures[0], t, cols) == pytest.approx(1.0, rel=1e-12)
     assert S.evaluate_measure(d.measures[1], t, cols) == pytest.approx(0.5, abs=0.02)
+
+
+def test_on_and_off_time():
+    """The same square wave: each on phase lasts 0.5 (ten intervals of 0.01
+    ending at an on sample... 50 of them), entered 9 times inside the
+    window after the first sample; the off phases likewise."""
+    t = np.round(np.arange(0.0, 10.0 + 1e-9, 0.01), 10)
+    sq = np.where(np.mod(t, 1.0) < 0.5, 1.0, 0.0)
+    d = S.parse("m\nV1 a 0 1\nR1 a 0 1k\n.TRAN 1n 10n\n"
+                ".MEASURE TRAN ton ON_TIME V(a) ON=0.8 OFF=0.2 FROM=0.25 TO=9.75\n"
+                ".MEASURE TRAN toff OFF_TIME V(a) ON=0.8 OFF=0.2 FROM=0.25 TO=9.75\n.END\n")
+    cols = {"V(A)": sq}
+    ton = S.evaluate_measure(d.measures[0], t, cols)
+    toff = S.evaluate_measure(d.measures[1], t, cols)
+    assert ton == pytest.approx(0.5, abs=0.03) and toff == pytest.approx(0.5, abs=0.03)

@@ -25,7 +25,8 @@ output.  The subset is what the path simulates:
   ``.PRINT TRAN`` (FORMAT=STD,
   NOINDEX or CSV), ``.MEASURE TRAN`` (MAX, MIN, PP, AVG,
   RMS, INTEG with FROM/TO; TRIG/TARG with VAL, TD and RISE/FALL/CROSS=n|LAST;
-  WHEN; FIND and DERIV ... WHEN / AT; FREQ and DUTY with ON/OFF), ``.END``; ``*`` and ``;`` comments, ``+``
+  WHEN; FIND and DERIV ... WHEN / AT; FREQ, DUTY, ON_TIME and OFF_TIME with
+  ON/OFF), ``.END``; ``*`` and ``;`` comments, ``+``
   continuation lines, engineering suffixes (T G MEG K M MIL U N P F);
 * print variables ``V(n)``, ``V(a,b)``, ``I(Vname)`` / ``I(Lname)``, ``TIME``,
   ``TEMP``, ``<R|C name>:R|C`` (the element value) and ``{expressions}`` of
@@ -1260,7 +1261,7 @@ def _measure(toks: list[str]) -> Measure:
     if len(pos) < 3 or pos[0].upper() != "TRAN":
         raise ValueError(".MEASURE TRAN <name> <func> <var> is the supported form")
     name, func = pos[1].upper(), pos[2].upper()
-    if func in ("FREQ", "DUTY"):
+    if func in ("FREQ", "DUTY", "ON_TIME", "OFF_TIME"):
         var = _print_vars(toks[toks.index(pos[2]) + 1:])
         bad = set(kv) - {"ON", "OFF", "FROM", "TO"}
         if not var or bad:
@@ -1418,10 +1419,13 @@ def _when(t, v, f, w):
 def _tran_stats(func, t, v, on, off, frm, to) -> float:
     """FREQ: half the number of OFF->ON and ON->OFF transitions per unit of
     time; DUTY: the fraction of the time spent ON (above ON, or above OFF
-    once on), over the points inside FROM/TO, the first of which only sets
-    the state (TranStats::updateTran, Frequency / Duty::updateMeasureVars,
+    once on); ON_TIME / OFF_TIME: the time at or above ON (at or below OFF)
+    per entry into that state; over the points inside FROM/TO, the first of
+    which only sets the state (TranStats::updateTran, Frequency / Duty /
+    OnTime / OffTime::updateMeasureVars,
     src/IOInterfacePKG/Output/N_IO_MeasureTranStats.C:90-117,
-    N_IO_MeasureFrequency.C:80-127, N_IO_MeasureDuty.C:80-118)."""
+    N_IO_MeasureFrequency.C:80-127, N_IO_MeasureDuty.C:80-118,
+    N_IO_MeasureOnTime.C:80-105, N_IO_MeasureOffTime.C:80-105)."""
     sel = np.ones(len(t), bool)
     if frm is not None:
         sel &= t >= frm * (1 - MINVAL)
@@ -1429,7 +1433,7 @@ def _tran_stats(func, t, v, on, off, frm, to) -> float:
         sel &= t <= to * (1 + MINVAL)
     t, v = t[sel], v[sel]
     window = on_time = 0.0
-    ups = downs = 0
+    ups = downs = cycles = 0
     in_on = False
     for k in range(1, len(t)):
         dt, x, last = t[k] - t[k - 1], v[k], v[k - 1]
@@ -1437,6 +1441,14 @@ def _tran_stats(func, t, v, on, off, frm, to) -> float:
         if func == "FREQ":
             ups += (x + MINVAL > on) and (last < on)
             downs += (x - MINVAL < off) and (last > off)
+        elif func == "ON_TIME":
+            if x + MINVAL >= on:
+                on_time += dt
+                cycles += last < on
+        elif func == "OFF_TIME":
+            if x - MINVAL <= off:
+                on_time += dt
+                cycles += last > off
         elif (x + MINVAL > on) or (in_on and x + MINVAL > off):
             on_time += dt
             in_on = True
@@ -1444,6 +1456,8 @@ def _tran_stats(func, t, v, on, off, frm, to) -> float:
             in_on = False
     if not window > 0:
         return float("nan")
+    if func in ("ON_TIME", "OFF_TIME"):
+        return float(on_time / cycles if cycles > 0 else on_time)
     return float(0.5 * (ups + downs) / window if func == "FREQ" else on_time / window)
 
 
@@ -1455,7 +1469,7 @@ def evaluate_measure(m: Measure, t: np.ndarray, cols: dict) -> float:
         t1 = _rfc_event_time(t, cols[tr["var"]], tr["val"], tr["rfc"], tr["td"])
         t2 = _rfc_event_time(t, cols[tg["var"]], tg["val"], tg["rfc"], tg["td"])
         return float(t2 - t1)
-    if m.func in ("FREQ", "DUTY"):
+    if m.func in ("FREQ", "DUTY", "ON_TIME", "OFF_TIME"):
         return _tran_stats(m.func, t, cols[m.var], m.spec["on"], m.spec["off"], m.frm, m.to)
     if m.func == "WHEN":
         return float(_when(t, cols[m.var], None, m.spec["when"])[0])
