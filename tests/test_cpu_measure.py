@@ -94,9 +94,9 @@ def test_freq_and_duty():
 
 
 def test_on_and_off_time():
-    """The same square wave: each on phase lasts 0.5 (ten intervals of 0.01
-    ending at an on sample... 50 of them), entered 9 times inside the
-    window after the first sample; the off phases likewise."""
+    """The same square wave: each on phase lasts 0.5 (the intervals of 0.01
+    that end at an on sample), and the wave enters it once per period inside
+    the window; the off phases likewise."""
     t = np.round(np.arange(0.0, 10.0 + 1e-9, 0.01), 10)
     sq = np.where(np.mod(t, 1.0) < 0.5, 1.0, 0.0)
     d = S.parse("m\nV1 a 0 1\nR1 a 0 1k\n.TRAN 1n 10n\n"
